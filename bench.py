@@ -1,0 +1,307 @@
+"""Benchmark of the engine's substep: particle-steps/s on one GB300 (or N replicas).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl engine|reference] [--workload NAME]
+
+A step is one substep of the whole tank (sort, P2G, grid passes, pressure solve, projection,
+G2P/advection) on a seeded synthetic tank (sprout_gb300.workloads). `value` is
+live particles x substeps / device seconds with the tank resident on the device
+(CUDA events on the engine's stream, tank working set far larger than L2, so no flush is
+needed between steps); `e2e` is the same metric through the public API with a host
+round trip every step (the step call's host -> device copies and the stats read-back).
+Under torchrun (N > 1) every rank advances its own tank (replicas: one tank does not
+shard), the timed region is bracketed by barriers and the slowest rank's time counts.
+
+`--impl reference` times the reference's algorithm on the host cores instead: the CPU
+oracle (a C restatement of the reference's shaders, all host threads), on the same tank.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "particle-steps/s at 1024x576, mixed vs plain, equal residual; p50/p99 step latency"
+UNIT = "particle-steps/s"
+
+
+def workload(name: str, rank: int):
+    from sprout_gb300 import workloads as WL
+    if name == "dam_break_1024":
+        # 1024 x 576 MAC grid, 1 mm cells, water over the left 40 % and bottom 60 %, 4 particles
+        # per cell, closed box, fixed 1/240 s substeps, pressure to relative residual 1e-5.
+        t = WL.dam_break(1024, 576, cell=0.001, width=0.4, height=0.6, tol=1e-5)
+        desc = {"workload": "dam_break_1024x576", "grid": [1024, 576], "cell_size_m": 0.001,
+                "fill": "water, left 40% x bottom 60%", "ppc": 4, "substep_s": 1 / 240, "pressure_tol": 1e-5,
+                "solver": "plain fp32 MGPCG", "surface_tension": 0, "viscosity": "explicit (water)"}
+    elif name == "dam_break_384":
+        t = WL.dam_break(384, 216, cell=0.002, width=0.4, height=0.6, tol=1e-5)
+        desc = {"workload": "dam_break_384x216", "grid": [384, 216], "cell_size_m": 0.002,
+                "fill": "water, left 40% x bottom 60%", "ppc": 4, "substep_s": 1 / 240, "pressure_tol": 1e-5,
+                "solver": "plain fp32 MGPCG"}
+    else:
+        raise SystemExit(f"unknown workload {name}")
+    return t, desc
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, index: int):
+        self.index = index
+        self.rows = []
+        self.proc = None
+        self.thread = None
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                          "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=2)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm = [float(r[1]) for r in self.rows if len(r) > 2 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) > 2 and r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            for k, n in enumerate(names):
+                if len(r) > 5 + k and r[5 + k].lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.rows)}
+
+
+def dist_setup(n_gpus: int):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo", init_method="env://")
+        pg = dist
+    return rank, world, local, pg
+
+
+def barrier(pg):
+    if pg is not None:
+        pg.barrier()
+
+
+def allreduce_max(pg, x: float) -> float:
+    if pg is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def allreduce_sum(pg, x: float) -> float:
+    if pg is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    pg.all_reduce(t, op=pg.ReduceOp.SUM)
+    return float(t.item())
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def cpu_oracle_rate(tank, seconds_budget: float = 15.0):
+    """The oracle (the reference's algorithm restated in C) on all host threads, a bounded sample."""
+    from oracle import oracle as O
+    threads = O.threads_available()
+    sim, parts, _ = O.build_tank(tank, threads=threads)
+    dt = 1.0 / 240.0
+    sim.step(1, dt)   # first substep: scatter only
+    t0 = time.perf_counter()
+    sim.step(1, dt)
+    one = time.perf_counter() - t0
+    n = int(max(1, min(20, seconds_budget / max(one, 1e-3))))
+    t0 = time.perf_counter()
+    sim.step(n, n * dt)
+    el = time.perf_counter() - t0
+    live = int(np.count_nonzero(sim.particles()["kind"]))
+    return {"value": live * n / el, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{n} substeps of the same tank after 2 warm-up substeps, {el:.1f} s"}, live, el / n
+
+
+def run_reference(args, rank, world, pg):
+    tank, desc = workload(args.workload, rank)
+    if rank != 0:
+        return
+    from oracle import oracle as O
+    threads = O.threads_available()
+    sim, parts, _ = O.build_tank(tank, threads=threads)
+    dt = 1.0 / 240.0
+    for _ in range(args.warmup):
+        sim.step(1, dt)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        sim.step(1, dt)
+    el = time.perf_counter() - t0
+    live = int(np.count_nonzero(sim.particles()["kind"]))
+    value = live * args.steps / el
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded tank, no dataset)", "config": desc,
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"{args.steps} substeps after {args.warmup} warm-up substeps"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def kernels_per_substep(stats) -> int:
+    n = 2 + 5 + 1                 # step + advance; scan x3 + place + cell gather; p2g
+    n += 4 + 1                    # grid_prep, coef/smooth, curvature, jumps; rhs
+    n += 1 if stats.thermal else 0
+    n += 2 if stats.viscosity_mode == 1 else 0
+    n += 1 + 1                    # pressure (persistent), project
+    return n
+
+
+def run_engine(args, rank, world, local, pg):
+    import sprout_gb300 as S
+    from sprout_gb300 import bytes_model as BM
+    try:
+        import torch
+        torch.cuda.set_device(local)
+    except Exception:
+        pass
+    tank, desc = workload(args.workload, rank)
+    sim, parts, _ = tank.engine()
+    dt = 1.0 / 240.0
+    for _ in range(max(args.warmup, 3)):
+        sim.step(1, dt)
+    sim.sync()
+    st0 = sim.stats()
+    live = st0.n_live
+    # ---- device-resident throughput ------------------------------------------------------
+    barrier(pg)
+    sim.sync()
+    with Clocks(local) as clk:
+        ms = sim.profile(args.steps)
+    sim.sync()
+    barrier(pg)
+    ms = allreduce_max(pg, ms)
+    live_all = allreduce_sum(pg, float(live))
+    st1 = sim.stats()
+    value = live_all * args.steps / (ms / 1e3)
+    # ---- per-stage times (CUDA events) and the roofline of the dominant stage ---------------
+    stages = sim.profile_passes()
+    st2 = sim.stats()
+    hbm, src = peaks()
+    unknowns = int(np.count_nonzero(sim.field("mgd")[: tank.w * tank.h] > 0))
+    iters = max(st2.pressure_iters[0], st2.pressure_iters[1])
+    top = max(stages, key=stages.get)
+    algo = BM.stage_bytes(top, st2.n_live, tank.w * tank.h, unknowns, iters, st2.acc_stride, bool(st2.thermal),
+                          st2.viscosity_mode)
+    achieved = algo / (stages[top] * 1e-3) / 1e9
+    roof = {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": hbm, "unit": "GB/s",
+            "frac": achieved / hbm, "peak_source": src, "traffic": None,
+            "algorithmic_bytes": algo, "stage_ms": stages[top]}
+    traffic_file = ROOT / "profiles" / "traffic.json"
+    if traffic_file.exists():
+        tr = json.loads(traffic_file.read_text()).get(args.workload, {}).get(top)
+        if tr:
+            roof["traffic"] = tr
+    # ---- end to end through the public API: a host round trip every step -------------------
+    h0 = sim.stats()
+    lat = []
+    barrier(pg)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        a = time.perf_counter()
+        sim.step(1, dt)
+        s = sim.stats()           # the step's result read back to the host (blocking)
+        lat.append(time.perf_counter() - a)
+    el = time.perf_counter() - t0
+    el = allreduce_max(pg, el)
+    h1 = sim.stats()
+    e2e_value = live_all * args.steps / el
+    e2e = {"value": e2e_value, "unit": UNIT,
+           "h2d_bytes_per_step": (h1.h2d_bytes - h0.h2d_bytes) / args.steps,
+           # h1's own read is counted in h1 - h0 with the K reads of the loop, all the same size
+           "d2h_bytes_per_step": (h1.d2h_bytes - h0.d2h_bytes) / (args.steps + 1),
+           "p50_ms": float(np.percentile(lat, 50) * 1e3), "p99_ms": float(np.percentile(lat, 99) * 1e3)}
+    if rank != 0:
+        return
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic (seeded tank, no dataset)",
+            "config": dict(desc, particles=int(live), parallelism=f"replicas x{world}",
+                           l2="working set > L2 (126 MB of particles alone): no flush",
+                           pressure_iters_last=list(st2.pressure_iters), pressure_residual=st2.pressure_residual,
+                           pressure_unconverged=st2.pressure_unconverged),
+            "clocks": clk.summary(), "e2e": e2e, "gpu_launches": kernels_per_substep(st2) * args.steps,
+            "roofline": roof, "stages_ms": stages, "latency_ms": {"p50": e2e["p50_ms"], "p99": e2e["p99_ms"]}}
+    if not args.no_cpu_baseline:
+        cb, _, _ = cpu_oracle_rate(tank)
+        line["cpu_baseline"] = cb
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
+    ap.add_argument("--workload", default="dam_break_1024")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    rank, world, local, pg = dist_setup(args.gpus)
+    try:
+        if args.impl == "reference":
+            run_reference(args, rank, world, pg)
+        else:
+            from sprout_gb300 import build
+            build.build()
+            run_engine(args, rank, world, local, pg)
+    finally:
+        if pg is not None:
+            pg.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

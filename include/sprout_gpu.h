@@ -1,0 +1,166 @@
+/*
+ * sprout_gpu.h -- C ABI of the GB300 engine for Sprout's per-substep fluid solver.
+ *
+ * The entry points replace the Rust `FluidSim` interface of the reference
+ * (src/sim/mod.rs:862-3474) and its `SimParams` parameter table (src/sim/params.rs:668-996),
+ * plus the two CPU helpers the headless tools use to build a tank
+ * (Scene::rasterize, src/scene.rs:215-310; maps::fill_rect, src/maps.rs:466-492).
+ * Plain pointers and sizes only. Every call returns an int status (SPROUT_OK or a negative
+ * SPROUT_E_* code); sprout_last_error() gives the message of the last failure on the
+ * calling thread. Nothing aborts the process.
+ *
+ * Ownership: the library owns all device memory; host arrays passed in are copied and
+ * never retained. Threading: one SproutSim = one CUDA stream; calls on one handle must be
+ * serialised by the caller; distinct handles may be used from different threads.
+ */
+#ifndef SPROUT_GPU_H
+#define SPROUT_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SPROUT_OK 0
+#define SPROUT_E_ARG (-1)          /* a bad argument (null handle, size, unknown key) */
+#define SPROUT_E_NOMEM (-2)        /* a device or host allocation failed */
+#define SPROUT_E_CAPACITY (-3)     /* more particles or materials than the tank holds */
+#define SPROUT_E_DIVERGED (-4)     /* a solve produced a non-finite residual */
+#define SPROUT_E_TIMEOUT (-5)      /* a bounded device-side wait ran out */
+#define SPROUT_E_CUDA (-6)         /* a CUDA runtime error */
+#define SPROUT_E_UNSUPPORTED (-7)  /* the tank needs a capability this engine does not carry */
+
+/* One particle, 48 bytes: Particle of src/sim/params.rs:35-54 (shaders/common.glsl:11-19). */
+typedef struct SproutParticle {
+    float pos[2];   /* cells */
+    float vel[2];   /* cells / s */
+    float c[4];     /* APIC affine matrix (du/dx, du/dy, dv/dx, dv/dy), 1 / s */
+    float s;        /* concentration */
+    uint32_t kind;  /* 0 dead, else material row + 1 in the low byte */
+    uint32_t id;    /* permanent identity */
+    float t;        /* enthalpy temperature, deg C */
+} SproutParticle;
+
+/* ToolState (src/sim/params.rs:1141-1150): the mouse tool for one step call. */
+typedef struct SproutTool {
+    float pos[2], vel[2], radius;
+    int32_t mode;   /* 0 none, 1 grab, 2 erase, 3 push, 4 nozzle, 5 heat, 6 cool, 7 whirl, 8 hold */
+    float strength;
+} SproutTool;
+
+/* SolverStats (src/sim/mod.rs:334-363) plus the step scalars of StepBuf (common.glsl:122-135). */
+typedef struct SproutSolverStats {
+    uint64_t substeps;                 /* substeps run since the last reset */
+    double sim_time;                   /* simulated seconds since the last reset */
+    float dt, dt_prev;                 /* the last substep and the one before, s */
+    uint32_t pressure_iters[2];        /* iterations of the last pressure solve (P, psi) */
+    uint32_t pressure_iters_max;       /* most iterations any pressure solve needed */
+    uint32_t pressure_unconverged;     /* pressure solves that hit pressure_max_iters */
+    uint32_t pressure2_iters_max, pressure2_unconverged;
+    uint32_t viscosity_iters_max, viscosity_unconverged;
+    uint32_t solves;
+    float pressure_residual;           /* |r| / |b| of the last pressure solve */
+    float pressure_residual_max;
+    float viscosity_residual_max;
+    float umax_grid, umax_part;        /* cells / s */
+    uint32_t n_slots, n_live;
+    uint32_t caps, acc_stride, thermal, viscosity_mode, levels, tail;
+    uint32_t device_error;             /* non-zero: a bounded device wait ran out */
+    uint64_t h2d_bytes, d2h_bytes;     /* host <-> device bytes this sim has moved (cumulative) */
+} SproutSolverStats;
+
+typedef struct SproutParams SproutParams;   /* SimParams */
+typedef struct SproutScene SproutScene;     /* Scene */
+typedef struct SproutSim SproutSim;         /* FluidSim */
+
+const char* sprout_last_error(void);
+const char* sprout_version(void);
+
+/* ---- parameters: SimParams (src/sim/params.rs:149-451) ------------------------------- */
+/* SimParams::default() (params.rs:386-451) with the built-in material table. */
+int sprout_params_new(SproutParams** out);
+int sprout_params_free(SproutParams* p);
+int sprout_params_copy(const SproutParams* src, SproutParams** out);
+/* SimParams::set (params.rs:986-996): by name (PARAMS, ALIASES, MAT_PARAMS as
+ * `<prop>_<material>` or `<material>.<prop>`, custom rows `mat<row>`), clamped to the
+ * parameter's range. *ok = 1 if the name resolved and v is not NaN, else 0 and nothing
+ * changes (the reference's `false`). */
+int sprout_params_set(SproutParams* p, const char* key, float v, int* ok);
+/* Reads a parameter by the same names; *ok = 0 for an unknown name. */
+int sprout_params_get(const SproutParams* p, const char* key, float* v, int* ok);
+
+/* ---- scene: Scene (src/scene.rs) ---------------------------------------------------- */
+int sprout_scene_new(uint32_t w, uint32_t h, SproutScene** out);
+int sprout_scene_free(SproutScene* s);
+/* Shape::Box (scene.rs:16): centre, half-extents, angle (radians); temp: the temperature
+ * it is held at (deg C), or NaN for an insulating solid (Scene::temps). */
+int sprout_scene_add_box(SproutScene* s, float cx, float cy, float hx, float hy, float angle, float temp);
+/* Shape::Circle (scene.rs:12). */
+int sprout_scene_add_circle(SproutScene* s, float cx, float cy, float r, float temp);
+/* Scene::sdf (scene.rs:195-198). */
+int sprout_scene_sdf(const SproutScene* s, float x, float y, float* d);
+/* Scene::rasterize (scene.rs:215-310): sdf[(w+1)(h+1)], solid[4 w h] (open fraction of
+ * the left face, of the bottom face, smoothed solid occupancy, open volume), region[w h],
+ * temp[w h] (may be NULL; *heated = 1 if any shape is held at a temperature). */
+int sprout_scene_rasterize(const SproutScene* s, float* sdf, float* solid4, uint32_t* region,
+                           float* temp, int* heated);
+/* maps::fill_rect (maps.rs:466-492): rest-density particles of `material` in rect
+ * (x0, y0, x1, y1, cells), skipping solids. `n_before` is the number of particles already
+ * placed (it seeds the jitter, as out.len() does in the reference). Writes at most `cap`
+ * particles to out and sets *n to the number the rectangle holds. */
+int sprout_fill_rect(const SproutScene* s, const float rect[4], uint32_t material,
+                     uint32_t n_before, SproutParticle* out, uint32_t cap, uint32_t* n);
+
+/* ---- the simulation: FluidSim (src/sim/mod.rs:862-3474) ----------------------------- */
+/* FluidSim::new (mod.rs:1034): a w x h grid for at most `capacity` particles, on the
+ * current CUDA device. */
+int sprout_sim_create(uint32_t w, uint32_t h, uint32_t capacity, const SproutParams* p,
+                      SproutSim** out);
+int sprout_sim_destroy(SproutSim* sim);
+/* Replaces `params` (the pub field of FluidSim); takes effect at the next step. */
+int sprout_sim_set_params(SproutSim* sim, const SproutParams* p);
+/* FluidSim::set_solids (mod.rs:1976): arrays as sprout_scene_rasterize fills them. */
+int sprout_sim_set_solids(SproutSim* sim, const float* sdf, const float* solid4,
+                          const uint32_t* region, const float* temp);
+/* FluidSim::reset (mod.rs:1981-2002): replaces every particle (ids = index, spawn fields
+ * settled). SPROUT_E_UNSUPPORTED if the tank needs a capability the engine lacks. */
+int sprout_sim_reset(SproutSim* sim, const SproutParticle* p, uint32_t n);
+/* FluidSim::record + submit (mod.rs:2400-2562): `substeps` substeps meant to cover
+ * `target` seconds (ignored with a fixed step rate). Asynchronous on the sim's stream.
+ * tool may be NULL. */
+int sprout_sim_step(SproutSim* sim, uint32_t substeps, float target, const SproutTool* tool);
+/* FluidSim::step_blocking (mod.rs:3315-3338): `substeps` ticks of 1/240 s, blocking. */
+int sprout_sim_step_blocking(SproutSim* sim, uint32_t substeps, const SproutTool* tool);
+/* FluidSim::advance_blocking (mod.rs:3284-3312): exactly `seconds`, blocking. */
+int sprout_sim_advance_blocking(SproutSim* sim, double seconds, const SproutTool* tool);
+/* Waits for the sim's stream. */
+int sprout_sim_sync(SproutSim* sim);
+/* FluidSim::download_particles: the particle slots in the engine's order (it keeps them
+ * sorted by cell, live ones first); *n = slots in use. Blocking. */
+int sprout_sim_download_particles(SproutSim* sim, SproutParticle* out, uint32_t cap, uint32_t* n);
+/* FluidSim::download_pressure: the two potentials per cell (p dt, psi), 2 w h floats. */
+int sprout_sim_download_pressure(SproutSim* sim, float* out);
+/* A named grid field (vel, cell, comp, coef, acc, pres, prhs, mga, mgd, pjump, surf, sprop,
+ * therm, dheat, hcell, vw, vs, ptile, step, region_air, ledger) into `out` (at most cap
+ * bytes); *bytes = its size. Blocking. For tests and tools. */
+int sprout_sim_download_field(SproutSim* sim, const char* name, void* out, size_t cap, size_t* bytes);
+/* SolverStats and the step scalars. Blocking. */
+int sprout_sim_stats(SproutSim* sim, SproutSolverStats* out);
+/* Device memory the sim holds, bytes. */
+int sprout_sim_device_bytes(SproutSim* sim, size_t* bytes);
+/* FluidSim::substep_cost (mod.rs:2537-2558): runs `substeps` substeps of the last step
+ * call's batch and returns their device time in ms, from CUDA events on the sim's stream.
+ * Blocking. */
+int sprout_sim_profile(SproutSim* sim, uint32_t substeps, float* ms);
+/* FluidSim::profile_passes (mod.rs:3120-3160): one substep, stage by stage, each timed by
+ * CUDA events: ms[0] advance (G2P, advection, collision), ms[1] sort, ms[2] P2G,
+ * ms[3] grid passes (prep, coefficients, surface tension, heat, viscosity, rhs),
+ * ms[4] pressure solve, ms[5] projection. n >= 6. Blocking. */
+int sprout_sim_profile_passes(SproutSim* sim, float* ms, uint32_t n);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

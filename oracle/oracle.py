@@ -1,0 +1,312 @@
+"""ctypes binding of the CPU oracle (liboracle.so).
+
+TEST INFRASTRUCTURE ONLY: the checker the parity tests compare the CUDA engine with. Only
+tests/, __graft_entry__.smoke() and bench.py's cpu_baseline leg may import this module.
+The oracle restates the reference's substep (shaders/*.comp and src/sim/mod.rs); see
+oracle/sprout_oracle.c for the file:line of each part.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB = HERE / "_build" / "liboracle.so"
+
+PARTICLE_DTYPE = np.dtype(
+    [("pos", "<f4", 2), ("vel", "<f4", 2), ("c", "<f4", 4), ("s", "<f4"), ("kind", "<u4"),
+     ("id", "<u4"), ("t", "<f4")]
+)
+assert PARTICLE_DTYPE.itemsize == 48
+
+
+class OMat(C.Structure):
+    _fields_ = [
+        ("group", C.c_uint32), ("diluent", C.c_int32),
+        ("density", C.c_float), ("density_solid", C.c_float), ("viscosity", C.c_float),
+        ("rheology", C.c_uint32), ("temp_model", C.c_uint32),
+        ("temp_b", C.c_float), ("temp_c", C.c_float), ("temp_ref", C.c_float),
+        ("tension", C.c_float), ("contact_angle", C.c_float), ("mix_rate", C.c_float),
+        ("grain", C.c_float), ("load", C.c_float),
+        ("heat_capacity", C.c_float), ("conductivity", C.c_float), ("expansion", C.c_float),
+        ("melt_lo", C.c_float), ("melt_hi", C.c_float), ("latent", C.c_float),
+        ("emissivity", C.c_float), ("boil", C.c_float), ("latent_vap", C.c_float),
+        ("freeze_shift", C.c_float), ("spawn_temp", C.c_float),
+        ("shear_modulus", C.c_float), ("susceptibility", C.c_float), ("skin", C.c_float),
+        ("friction", C.c_float), ("self_heat", C.c_float), ("volatility", C.c_float),
+        ("react_with", C.c_int32), ("react_rate", C.c_float), ("fume", C.c_float),
+    ]
+
+
+class OSimParams(C.Structure):
+    _fields_ = [
+        ("cell_size", C.c_float), ("gravity", C.c_float),
+        ("pair_tension", (C.c_float * 4) * 4),
+        ("ambient_temp", C.c_float), ("heat_rate", C.c_float), ("air_cooling", C.c_float),
+        ("contact_heat", C.c_float), ("eddy_heat", C.c_float), ("evaporation", C.c_uint32),
+        ("rigid_viscosity", C.c_float), ("heat_power", C.c_float), ("steam", C.c_uint32),
+        ("droplet_cells", C.c_float), ("cfl", C.c_float), ("advection_order", C.c_uint32),
+        ("dt_max", C.c_float), ("fixed_hz", C.c_float), ("pressure_tol", C.c_float),
+        ("pressure_max_iters", C.c_uint32), ("correction_tol", C.c_float),
+        ("viscosity_tol", C.c_float), ("viscosity_max_iters", C.c_uint32),
+        ("implicit_viscosity_min", C.c_float),
+        ("viscous_projection", C.c_uint32), ("viscous_warm", C.c_uint32),
+        ("viscosity_warm", C.c_uint32), ("viscosity_precond", C.c_uint32),
+        ("viscosity_mg_levels", C.c_uint32), ("viscosity_mg_sweeps", C.c_uint32),
+        ("spray_cfl", C.c_float), ("speed_cap", C.c_float), ("correction_time", C.c_float),
+        ("correction_max", C.c_float), ("correction_deadband", C.c_float),
+        ("correction_step_max", C.c_float), ("crowd_jitter", C.c_float),
+        ("tool_crowd_max", C.c_float), ("apic_clamp", C.c_float), ("curvature_max", C.c_float),
+        ("slip_cap", C.c_uint32), ("sealed_vent", C.c_uint32),
+        ("mat", OMat * 96),
+    ]
+
+
+class OTool(C.Structure):
+    _fields_ = [("pos", C.c_float * 2), ("vel", C.c_float * 2), ("radius", C.c_float),
+                ("mode", C.c_int32), ("strength", C.c_float)]
+
+
+class OShape(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("c", C.c_float * 2), ("half", C.c_float * 2),
+                ("r", C.c_float), ("angle", C.c_float), ("temp", C.c_float)]
+
+
+class OStats(C.Structure):
+    _fields_ = [
+        ("substeps", C.c_uint64), ("sim_time", C.c_float), ("dt", C.c_float), ("dt_prev", C.c_float),
+        ("p_iters", C.c_uint32 * 2), ("p_done", C.c_uint32 * 2), ("p2_iters", C.c_uint32),
+        ("v_iters", C.c_uint32), ("v_done", C.c_uint32),
+        ("p_it_max", C.c_uint32), ("p_unconv", C.c_uint32), ("v_it_max", C.c_uint32),
+        ("v_unconv", C.c_uint32), ("p2_it_max", C.c_uint32), ("p2_unconv", C.c_uint32),
+        ("solves", C.c_uint32), ("p_res_max", C.c_float), ("v_res_max", C.c_float),
+        ("p_rr", C.c_float * 2), ("p_bb", C.c_float * 2), ("v_rr", C.c_float), ("v_r0", C.c_float),
+        ("umax_grid", C.c_float), ("umax_part", C.c_float),
+        ("n_slots", C.c_uint32), ("caps", C.c_uint32), ("acc_stride", C.c_uint32),
+        ("thermal", C.c_uint32), ("viscosity_mode", C.c_uint32), ("levels", C.c_uint32),
+        ("tail", C.c_uint32),
+    ]
+
+
+def build(force: bool = False) -> Path:
+    """Compiles the oracle (gcc, no fused multiply-add) into oracle/_build/liboracle.so."""
+    src = HERE / "sprout_oracle.c"
+    if LIB.exists() and not force and LIB.stat().st_mtime >= src.stat().st_mtime:
+        return LIB
+    LIB.parent.mkdir(exist_ok=True)
+    cmd = ["gcc", "-O2", "-std=c11", "-D_GNU_SOURCE", "-ffp-contract=off", "-fopenmp", "-fPIC",
+           "-shared", "-o", str(LIB), str(src), "-lm"]
+    subprocess.run(cmd, check=True)
+    return LIB
+
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(str(LIB))
+        P = C.POINTER
+        L.oparams_default.argtypes = [P(OSimParams)]
+        L.oscene_rasterize.argtypes = [C.c_int, C.c_int, C.c_int, P(OShape), P(C.c_float),
+                                       P(C.c_float), P(C.c_uint32), P(C.c_float)]
+        L.oscene_rasterize.restype = C.c_int
+        L.oscene_sdf.argtypes = [C.c_int, C.c_int, C.c_int, P(OShape), C.c_float, C.c_float]
+        L.oscene_sdf.restype = C.c_float
+        L.ofill_rect.argtypes = [C.c_int, C.c_int, C.c_int, P(OShape), P(C.c_float), C.c_uint32,
+                                 C.c_void_p, C.c_uint32, C.c_uint32]
+        L.ofill_rect.restype = C.c_uint32
+        L.osim_create.argtypes = [C.c_int, C.c_int, C.c_uint32, P(OSimParams)]
+        L.osim_create.restype = C.c_void_p
+        L.osim_destroy.argtypes = [C.c_void_p]
+        L.osim_set_params.argtypes = [C.c_void_p, P(OSimParams)]
+        L.osim_set_solids.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        L.osim_reset.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32]
+        L.osim_reset.restype = C.c_int
+        L.osim_step.argtypes = [C.c_void_p, C.c_uint32, C.c_float, P(OTool)]
+        L.osim_step.restype = C.c_int
+        L.osim_sort.argtypes = [C.c_void_p]
+        L.osim_particles.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32]
+        L.osim_particles.restype = C.c_uint32
+        L.osim_field.argtypes = [C.c_void_p, C.c_char_p, C.c_void_p, C.c_size_t]
+        L.osim_field.restype = C.c_long
+        L.osim_stats.argtypes = [C.c_void_p, P(OStats)]
+        L.osim_set_threads.argtypes = [C.c_int]
+        L.o_expf.argtypes = [C.c_float]
+        L.o_expf.restype = C.c_float
+        _lib = L
+    return _lib
+
+
+def default_params() -> OSimParams:
+    p = OSimParams()
+    lib().oparams_default(C.byref(p))
+    return p
+
+
+def shapes_array(shapes) -> tuple:
+    arr = (OShape * max(len(shapes), 1))()
+    for k, s in enumerate(shapes):
+        arr[k].kind = 0 if s["kind"] == "circle" else 1
+        arr[k].c[0], arr[k].c[1] = s["c"]
+        if s["kind"] == "circle":
+            arr[k].r = s["r"]
+        else:
+            arr[k].half[0], arr[k].half[1] = s["half"]
+            arr[k].angle = s.get("angle", 0.0)
+        t = s.get("temp")
+        arr[k].temp = -2e9 if t is None else t
+    return arr, len(shapes)
+
+
+def rasterize(w: int, h: int, shapes=()):
+    arr, n = shapes_array(shapes)
+    sdf = np.zeros((h + 1) * (w + 1), np.float32)
+    solid = np.zeros((h * w, 4), np.float32)
+    region = np.zeros(h * w, np.uint32)
+    temp = np.zeros(h * w, np.float32)
+    f = lambda a: a.ctypes.data_as(C.POINTER(C.c_float))
+    heated = lib().oscene_rasterize(w, h, n, arr, f(sdf), f(solid), region.ctypes.data_as(C.POINTER(C.c_uint32)), f(temp))
+    return sdf, solid, region, (temp if heated else None)
+
+
+def fill_rect(w: int, h: int, rect, material: int, shapes=(), existing: np.ndarray | None = None):
+    arr, n = shapes_array(shapes)
+    n0 = 0 if existing is None else len(existing)
+    r = (C.c_float * 4)(*rect)
+    count = lib().ofill_rect(w, h, n, arr, r, material, None, n0, n0)
+    out = np.zeros(count, PARTICLE_DTYPE)
+    if existing is not None:
+        out[:n0] = existing
+    lib().ofill_rect(w, h, n, arr, r, material, out.ctypes.data, n0, count)
+    return out
+
+
+class OracleSim:
+    """The oracle behind the same calls as FluidSim (src/sim/mod.rs:862-)."""
+
+    def __init__(self, w: int, h: int, capacity: int, params: OSimParams):
+        self.w, self.h = w, h
+        self.params = params
+        self.h_ = lib().osim_create(w, h, capacity, C.byref(params))
+        if not self.h_:
+            raise ValueError("oracle: bad grid")
+
+    def close(self):
+        if self.h_:
+            lib().osim_destroy(self.h_)
+            self.h_ = None
+
+    __del__ = close
+
+    def set_solids(self, sdf, solid, region, temp=None):
+        self._keep = (np.ascontiguousarray(sdf, np.float32), np.ascontiguousarray(solid, np.float32),
+                      np.ascontiguousarray(region, np.uint32),
+                      None if temp is None else np.ascontiguousarray(temp, np.float32))
+        a, b, c, d = self._keep
+        lib().osim_set_solids(self.h_, a.ctypes.data, b.ctypes.data, c.ctypes.data, None if d is None else d.ctypes.data)
+
+    def reset(self, particles: np.ndarray) -> int:
+        p = np.ascontiguousarray(particles, PARTICLE_DTYPE)
+        return lib().osim_reset(self.h_, p.ctypes.data, len(p))
+
+    def step(self, substeps: int, target: float = 0.0, tool: OTool | None = None):
+        return lib().osim_step(self.h_, substeps, target, None if tool is None else C.byref(tool))
+
+    def sort(self):
+        lib().osim_sort(self.h_)
+
+    def particles(self) -> np.ndarray:
+        n = lib().osim_particles(self.h_, None, 0)
+        out = np.zeros(n, PARTICLE_DTYPE)
+        lib().osim_particles(self.h_, out.ctypes.data, n)
+        return out
+
+    def field(self, name: str, dtype=np.float32) -> np.ndarray:
+        n = lib().osim_field(self.h_, name.encode(), None, 0)
+        if n < 0:
+            raise KeyError(name)
+        buf = np.zeros(n // np.dtype(dtype).itemsize, dtype)
+        lib().osim_field(self.h_, name.encode(), buf.ctypes.data, n)
+        return buf
+
+    def stats(self) -> OStats:
+        s = OStats()
+        lib().osim_stats(self.h_, C.byref(s))
+        return s
+
+
+def set_threads(n: int):
+    lib().osim_set_threads(n)
+
+
+def threads_available() -> int:
+    return len(os.sched_getaffinity(0))
+
+
+# ---- building the oracle's tank from a workload description -----------------------------
+
+BUILTIN_ROWS = {"water": 0, "honey": 1, "oil": 2}
+MAT_FIELDS = {f for f, _ in OMat._fields_} - {"group", "diluent", "rheology", "react_with"}
+
+
+def _row(name: str) -> int:
+    if name in BUILTIN_ROWS:
+        return BUILTIN_ROWS[name]
+    if name.startswith("mat"):
+        return int(name[3:])
+    raise KeyError(name)
+
+
+def apply_setting(p: OSimParams, key: str, v: float):
+    """The oracle-side counterpart of SimParams::set for the names the workloads use."""
+    prop = row = None
+    if "." in key:
+        mat, prop = key.split(".", 1)
+        row = _row(mat)
+    else:
+        for f in sorted(MAT_FIELDS, key=len, reverse=True):
+            if key.startswith(f + "_"):
+                try:
+                    row, prop = _row(key[len(f) + 1:]), f
+                    break
+                except (KeyError, ValueError):
+                    pass
+    if prop is not None:
+        m = p.mat[row]
+        typ = dict(m._fields_)[prop]
+        setattr(m, prop, int(v) if typ in (C.c_uint32, C.c_int32) else float(v))
+        return
+    names = dict(p._fields_)
+    if key not in names:
+        raise KeyError(key)
+    setattr(p, key, int(round(v)) if names[key] is C.c_uint32 else float(v))
+
+
+def build_tank(tank, threads: int | None = None):
+    """(OracleSim, particles, solids) for a workload description (sprout_gb300.workloads.Tank)."""
+    p = default_params()
+    for k, v in tank.settings.items():
+        apply_setting(p, k, v)
+    sdf, solid, region, temp = rasterize(tank.w, tank.h, tank.shapes)
+    parts = None
+    for rect, mat, t in tank.fills:
+        before = 0 if parts is None else len(parts)
+        parts = fill_rect(tank.w, tank.h, rect, mat, tank.shapes, parts)
+        if t is not None:
+            parts["t"][before:] = t
+            parts["kind"][before:] |= 0x20000
+    sim = OracleSim(tank.w, tank.h, len(parts) + tank.capacity_extra, p)
+    sim.set_solids(sdf, solid, region, temp)
+    rc = sim.reset(parts)
+    if rc != 0:
+        raise RuntimeError(f"the oracle does not carry this tank ({rc})")
+    if threads is not None:
+        set_threads(threads)
+    return sim, parts, (sdf, solid, region, temp)

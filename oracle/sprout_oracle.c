@@ -1,0 +1,3159 @@
+/*
+ * sprout_oracle.c -- CPU oracle of the Sprout fluid substep.
+ *
+ * TEST INFRASTRUCTURE ONLY (see sprout_oracle.h). A plain-C restatement, one function per
+ * reference shader, of the per-substep 2D APIC/PIC solver of Testro-lol/Sprout:
+ *   step.comp, sort.comp, particles.comp (core branches), grid_prep.comp, grid_coef.comp,
+ *   surf_smooth.comp, surf_curv.comp, surf_apply.comp, heat.comp, visc_setup.comp +
+ *   visc_apply.comp (explicit viscosity), rhs.comp, mg_build.comp, mg_tail.comp,
+ *   mg_down.comp, mg_up.comp, cg_scale.comp, cg_init.comp, cg_apply.comp, cg_update.comp,
+ *   reduce.glsl + reduce_tail.glsl, project.comp,
+ * plus the Rust host code that sets them up: Scene::rasterize (src/scene.rs:215-470),
+ * maps::fill_rect (src/maps.rs:455-492), Tank::layout (src/sim/mod.rs:271-329),
+ * Levels::new (src/sim/mod.rs:714-753), gpu_materials / gpu_params
+ * (src/sim/mod.rs:2179-2339), record / record_substep / record_pressure
+ * (src/sim/mod.rs:2400-2708, 2929-3010).
+ *
+ * Build: -O2 -ffp-contract=off (no fused multiply-add: every float operation rounds the
+ * way the shader source writes it). GLSL built-ins are spelled out per the GLSL spec:
+ * mix(x, y, a) = x * (1 - a) + y * a, length(v) = sqrt(dot(v, v)), normalize(v) =
+ * v / length(v), smoothstep per its definition. Work-group reductions keep the shaders'
+ * order (256-invocation trees per 16 x 16 tile, then the strided totals of
+ * reduce_tail.glsl:268-281).
+ */
+#include "sprout_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+/* ------------------------------------------------------------------------------------ */
+/* Small vector algebra (GLSL semantics)                                                 */
+/* ------------------------------------------------------------------------------------ */
+
+typedef struct { float x, y; } V2;
+typedef struct { float x, y, z, w; } V4;
+typedef struct { int x, y; } I2;
+
+static inline V2 v2(float x, float y) { V2 r = {x, y}; return r; }
+static inline V4 v4(float x, float y, float z, float w) { V4 r = {x, y, z, w}; return r; }
+/* GLSL min / max (GLSL spec 8.3): min(x, y) = y < x ? y : x, max(x, y) = x < y ? y : x */
+static inline float minf(float x, float y) { return y < x ? y : x; }
+static inline float maxf(float x, float y) { return x < y ? y : x; }
+static inline float clampf(float x, float lo, float hi) { return minf(maxf(x, lo), hi); }
+static inline int mini(int a, int b) { return a < b ? a : b; }
+static inline int maxi(int a, int b) { return a > b ? a : b; }
+static inline int clampi(int x, int lo, int hi) { return mini(maxi(x, lo), hi); }
+static inline float mixf(float x, float y, float a) { return x * (1.0f - a) + y * a; }
+static inline float signf(float x) { return x > 0.0f ? 1.0f : (x < 0.0f ? -1.0f : 0.0f); }
+static inline float len2(V2 v) { return sqrtf(v.x * v.x + v.y * v.y); }
+static inline float smoothstepf(float e0, float e1, float x) {
+    float t = clampf((x - e0) / (e1 - e0), 0.0f, 1.0f);
+    return t * t * (3.0f - 2.0f * t);
+}
+static inline uint32_t fbits(float f) { uint32_t u; memcpy(&u, &f, 4); return u; }
+static inline float bitsf(uint32_t u) { float f; memcpy(&f, &u, 4); return f; }
+
+/* air.glsl:4-11 */
+static inline uint32_t hash32(uint32_t x) {
+    x ^= x >> 16;
+    x *= 0x7feb352du;
+    x ^= x >> 15;
+    x *= 0x846ca68bu;
+    x ^= x >> 16;
+    return x;
+}
+
+/* exp(x): Cody & Waite argument reduction x = n ln2 + r with ln2 split in two parts,
+ * |r| <= ln2 / 2, e^r by its Taylor series to degree 7 (Horner), times 2^n assembled from
+ * the exponent bits (two factors, so subnormal results stay exact). */
+float o_expf(float x) {
+    if (x != x) return x;
+    if (x > 88.72283f) return bitsf(0x7f800000u);
+    if (x < -103.972f) return 0.0f;
+    const float LOG2E = 1.44269504f;
+    const float LN2_HI = 0.693145752f;   /* 0x3f317200: 16 significant bits */
+    const float LN2_LO = 1.42860677e-06f;
+    float n = floorf(x * LOG2E + 0.5f);
+    float r = (x - n * LN2_HI) - n * LN2_LO;
+    float p = 1.98412698e-04f;           /* 1/5040 */
+    p = p * r + 1.38888889e-03f;         /* 1/720 */
+    p = p * r + 8.33333333e-03f;         /* 1/120 */
+    p = p * r + 4.16666667e-02f;         /* 1/24 */
+    p = p * r + 1.66666667e-01f;         /* 1/6 */
+    p = p * r + 0.5f;
+    p = p * r + 1.0f;
+    p = p * r + 1.0f;
+    int k = (int)n;
+    int k1 = k / 2, k2 = k - k1;
+    float s1 = bitsf((uint32_t)(k1 + 127) << 23);
+    float s2 = bitsf((uint32_t)(k2 + 127) << 23);
+    return (p * s1) * s2;
+}
+
+/* ------------------------------------------------------------------------------------ */
+/* Constants (shaders/common.glsl, src/sim/ sources)                                       */
+/* ------------------------------------------------------------------------------------ */
+
+#define KIND_DEAD 0u
+#define KIND_FRESH 0x10000u
+#define KIND_REAL_T 0x20000u
+#define SPAWN_TEMP (-1.0e4f)
+#define SPAWN_S (-1.0f)
+#define MAX_PRESENT 12
+#define GROUPS 4
+#define MASS_SCALE 1048576.0f
+#define MOM_SCALE 4194304.0f
+#define MIN_FACE_MASS 64
+#define THETA_MIN 0.1f
+#define REST_PHI 1.0f
+#define LIQUID_THR 0.5f
+#define FACE_EMPTY 1e30f
+#define FACE_CLOSED (-1e30f)
+#define NO_TEMP (-1e9f)
+#define LEDGER_SCALE 65536.0f
+#define T_SCALE 4096.0f
+#define REGION_MASK 31u
+#define REGION_VENT 256u
+#define CAP_FAMILIES 1u
+#define CAP_THERMAL 2u
+#define CAP_RIGID 4u
+#define CAP_RHEO 8u
+#define CAP_MAGNET 16u
+#define CAP_ELASTIC 32u
+#define CAP_SETTLE 64u
+#define CAP_STEAM 128u
+#define CAP_REACT 256u
+#define WATER_DENSITY 998.0f
+#define WATER_HEAT (998.0f * 4182.0f)
+#define STEFAN_BOLTZMANN 5.670374e-8f
+#define T_REF 20.0f
+#define NO_MELT (-1.0e9f)
+#define ACC_MIN 8
+#define ACC_MAX 32
+#define ACC_FIRST 5
+#define COARSEST_CELLS 4
+#define TAIL_CELLS 1500
+#define MG_OMEGA 1.8f
+#define GRID_GROUP 16
+#define SORT_INTERVAL 128u
+#define SORT_MIN_PARTICLES 16384u
+#define WALL 3.0f
+#define PPC 4
+
+static int is_inside_f(float d) { return d < 0.0f; }
+
+/* ------------------------------------------------------------------------------------ */
+/* Parameters: SimParams::default and the built-ins the configs use                      */
+/* ------------------------------------------------------------------------------------ */
+
+static void mat_default(OMat* m) {
+    memset(m, 0, sizeof *m);
+    m->group = 0;
+    m->diluent = -1;
+    m->density = 998.0f;
+    m->density_solid = 0.0f;
+    m->viscosity = 1.0e-6f;
+    m->rheology = 0;
+    m->temp_model = 0;
+    m->temp_b = 0.0f;
+    m->temp_c = 0.0f;
+    m->temp_ref = T_REF;
+    m->tension = 0.072f;
+    m->contact_angle = 90.0f;
+    m->mix_rate = 0.0f;
+    m->grain = 0.0f;
+    m->load = 1.0f;
+    m->heat_capacity = 4182.0f;
+    m->conductivity = 0.6f;
+    m->expansion = 4.0e-4f;
+    m->melt_lo = -1.0e9f;
+    m->melt_hi = -1.0e9f;
+    m->latent = 0.0f;
+    m->emissivity = 0.9f;
+    m->boil = 1.0e9f;
+    m->latent_vap = 0.0f;
+    m->freeze_shift = 0.0f;
+    m->spawn_temp = T_REF;
+    m->react_with = -1;
+}
+
+void oparams_default(OSimParams* p) {
+    memset(p, 0, sizeof *p);
+    p->cell_size = 0.01f;
+    p->gravity = 9.81f;
+    /* material.rs:489-507 */
+    float t[GROUPS][GROUPS] = {{0}};
+#define SETPT(a, b, v) (t[a][b] = (v), t[b][a] = (v))
+    SETPT(0, 1, 0.025f);
+    SETPT(0, 2, 0.375f);
+    SETPT(1, 2, 0.36f);
+    SETPT(0, 3, 0.2f);
+    SETPT(1, 3, 0.2f);
+    SETPT(2, 3, 0.4f);
+#undef SETPT
+    memcpy(p->pair_tension, t, sizeof t);
+    p->ambient_temp = T_REF;
+    p->heat_rate = 1.0f;
+    p->air_cooling = 10.0f;
+    p->contact_heat = 3000.0f;
+    p->eddy_heat = 0.17f;
+    p->evaporation = 1;
+    p->rigid_viscosity = 1.0f;
+    p->heat_power = 300.0f;
+    p->steam = 1;
+    p->droplet_cells = 1.0f;
+    p->cfl = 4.0f;
+    p->advection_order = 2;
+    p->dt_max = 1.0f / 80.0f;
+    p->fixed_hz = 0.0f;
+    p->pressure_tol = 1e-4f;
+    p->pressure_max_iters = 60;
+    p->correction_tol = 1e-2f;
+    p->viscosity_tol = 1e-3f;
+    p->viscosity_max_iters = 200;
+    p->implicit_viscosity_min = 1e-3f;
+    p->viscous_projection = 1;
+    p->viscous_warm = 1;
+    p->viscosity_warm = 1;
+    p->viscosity_precond = 1;
+    p->viscosity_mg_levels = 1;
+    p->viscosity_mg_sweeps = 2;
+    p->spray_cfl = 4.0f;
+    p->speed_cap = 1.0f;
+    p->correction_time = (1.0f / 240.0f) / 0.693147182f;
+    p->correction_max = 0.5f;
+    p->correction_deadband = 0.25f;
+    p->correction_step_max = 0.5f;
+    p->crowd_jitter = 0.5f;
+    p->tool_crowd_max = 2.0f;
+    p->apic_clamp = 1.0f;
+    p->curvature_max = 0.5f;
+    p->slip_cap = 1;
+    p->sealed_vent = 1;
+    for (int r = 0; r < O_MAX_MATERIALS; r++) mat_default(&p->mat[r]);
+    /* water (presets.rs:37-60) */
+    OMat* w = &p->mat[0];
+    w->temp_model = 2; w->temp_b = 578.9f; w->temp_c = 137.5f;
+    w->melt_lo = -0.5f; w->melt_hi = 0.0f; w->latent = 334.0e3f; w->density_solid = 917.0f;
+    w->boil = 100.0f; w->latent_vap = 2257.0e3f; w->emissivity = 0.96f;
+    /* honey (presets.rs:61-90) */
+    OMat* h = &p->mat[1];
+    h->diluent = 0; h->density = 1.4f * 998.0f; h->viscosity = 0.06f; h->temp_model = 1;
+    h->temp_b = 10500.0f; h->tension = 0.076f; h->mix_rate = 1.5f; h->heat_capacity = 2300.0f;
+    h->conductivity = 0.35f; h->expansion = 5.0e-4f; h->boil = 110.0f; h->latent_vap = 2257.0e3f;
+    /* olive oil (presets.rs:92-117) */
+    OMat* o = &p->mat[2];
+    o->group = 1; o->density = 0.9f * 998.0f; o->viscosity = 6.0e-5f; o->temp_model = 1;
+    o->temp_b = 3900.0f; o->tension = 0.032f; o->heat_capacity = 1970.0f; o->conductivity = 0.17f;
+    o->expansion = 7.0e-4f; o->melt_lo = -8.0f; o->melt_hi = -4.0f; o->latent = 150.0e3f;
+    o->density_solid = 925.0f;
+}
+
+/* ------------------------------------------------------------------------------------ */
+/* Scene (src/scene.rs)                                                                  */
+/* ------------------------------------------------------------------------------------ */
+
+static void rotate2(float px, float py, float angle, float* ox, float* oy) {
+    float s = sinf(angle), c = cosf(angle);
+    *ox = c * px + s * py;
+    *oy = -s * px + c * py;
+}
+
+/* Shape::sdf (scene.rs:68-93): circle and box. */
+static float shape_sdf(const OShape* s, float px, float py) {
+    if (s->kind == 0) return hypotf(px - s->c[0], py - s->c[1]) - s->r;
+    float qx, qy;
+    rotate2(px - s->c[0], py - s->c[1], s->angle, &qx, &qy);
+    float dx = fabsf(qx) - s->half[0], dy = fabsf(qy) - s->half[1];
+    return hypotf(maxf(dx, 0.0f), maxf(dy, 0.0f)) + minf(maxf(dx, dy), 0.0f);
+}
+
+static void shape_bound(const OShape* s, float* c, float* r) {
+    c[0] = s->c[0];
+    c[1] = s->c[1];
+    *r = s->kind == 0 ? s->r : hypotf(s->half[0], s->half[1]);
+}
+
+static float wall_sdf(int w, int h, float x, float y) {
+    float W = (float)w, H = (float)h;
+    return fminf(fminf(fminf(x - WALL, W - WALL - x), y - WALL), H - WALL - y);
+}
+
+float oscene_sdf(int w, int h, int nshapes, const OShape* shapes, float x, float y) {
+    float d = wall_sdf(w, h, x, y);
+    for (int k = 0; k < nshapes; k++) d = fminf(d, shape_sdf(&shapes[k], x, y));
+    return d;
+}
+
+/* open_fraction (scene.rs:177-189) */
+static float open_fraction(float d0, float d1) {
+    float f;
+    if (d0 > 0.0f && d1 > 0.0f) f = 1.0f;
+    else if (d0 <= 0.0f && d1 <= 0.0f) f = 0.0f;
+    else f = fmaxf(d0, d1) / (fmaxf(d0, d1) - fminf(d0, d1));
+    return f < 0.05f ? 0.0f : f;
+}
+
+/* Scene::union_depth (scene.rs:318-381) */
+static void union_depth(float* sdf, int nw, int nh) {
+    const float FAR = 1e9f;
+    float* depth = (float*)calloc((size_t)nw * nh, sizeof(float));
+    static const int NB8[8][2] = {{-1, 0}, {1, 0}, {0, -1}, {0, 1}, {-1, -1}, {1, -1}, {-1, 1}, {1, 1}};
+    for (int j = 0; j < nh; j++)
+        for (int i = 0; i < nw; i++) {
+            int k = j * nw + i;
+            if (!is_inside_f(sdf[k])) continue;
+            int edge = 0;
+            for (int q = 0; q < 8; q++) {
+                int a = i + NB8[q][0], b = j + NB8[q][1];
+                if (a >= 0 && b >= 0 && a < nw && b < nh && !is_inside_f(sdf[b * nw + a])) { edge = 1; break; }
+            }
+            depth[k] = edge ? -sdf[k] : FAR;
+        }
+    const float D = 1.41421354f;
+#define RELAX(k, n, st) do { if (depth[n] + (st) < depth[k]) depth[k] = depth[n] + (st); } while (0)
+    for (int j = 0; j < nh; j++)
+        for (int i = 0; i < nw; i++) {
+            int k = j * nw + i;
+            if (depth[k] == 0.0f) continue;
+            if (i > 0) RELAX(k, k - 1, 1.0f);
+            if (j > 0) {
+                RELAX(k, k - nw, 1.0f);
+                if (i > 0) RELAX(k, k - nw - 1, D);
+                if (i + 1 < nw) RELAX(k, k - nw + 1, D);
+            }
+        }
+    for (int j = nh - 1; j >= 0; j--)
+        for (int i = nw - 1; i >= 0; i--) {
+            int k = j * nw + i;
+            if (depth[k] == 0.0f) continue;
+            if (i + 1 < nw) RELAX(k, k + 1, 1.0f);
+            if (j + 1 < nh) {
+                RELAX(k, k + nw, 1.0f);
+                if (i + 1 < nw) RELAX(k, k + nw + 1, D);
+                if (i > 0) RELAX(k, k + nw - 1, D);
+            }
+        }
+#undef RELAX
+    for (int k = 0; k < nw * nh; k++)
+        if (is_inside_f(sdf[k]) && depth[k] < FAR) sdf[k] = fminf(sdf[k], -depth[k]);
+    free(depth);
+}
+
+static void faces_of(const float* open, const float* sdf, int w, int i, int j, float out[2]) {
+    int nw = w + 1;
+    int here = open[j * w + i] > 0.0f;
+    int left = here && i > 0 && open[j * w + i - 1] > 0.0f;
+    int below = here && j > 0 && open[(j - 1) * w + i] > 0.0f;
+    out[0] = left ? open_fraction(sdf[j * nw + i], sdf[(j + 1) * nw + i]) : 0.0f;
+    out[1] = below ? open_fraction(sdf[j * nw + i], sdf[j * nw + i + 1]) : 0.0f;
+}
+
+/* Scene::seal_pockets (scene.rs:431-470) */
+static void seal_pockets(float* open, float* sdf, int w, int h) {
+    int nw = w + 1;
+    size_t n = (size_t)w * h;
+    uint32_t* label = (uint32_t*)malloc(n * sizeof(uint32_t));
+    int* stack = (int*)malloc(n * sizeof(int));
+    int* members = (int*)malloc(n * sizeof(int));
+    for (size_t k = 0; k < n; k++) label[k] = 0xffffffffu;
+    for (int start = 0; start < (int)n; start++) {
+        if (open[start] == 0.0f || label[start] != 0xffffffffu) continue;
+        int nm = 0, sp = 0;
+        label[start] = (uint32_t)start;
+        stack[sp++] = start;
+        while (sp > 0) {
+            int k = stack[--sp];
+            members[nm++] = k;
+            int i = k % w, j = k / w;
+            float lb[2], rr[2], ab[2];
+            faces_of(open, sdf, w, i, j, lb);
+            float right = 0.0f, above = 0.0f;
+            if (i + 1 < w) { faces_of(open, sdf, w, i + 1, j, rr); right = rr[0]; }
+            if (j + 1 < h) { faces_of(open, sdf, w, i, j + 1, ab); above = ab[1]; }
+            int nb[4] = {k - 1, k + 1, k - w, k + w};
+            float a[4] = {lb[0], right, lb[1], above};
+            for (int q = 0; q < 4; q++)
+                if (a[q] > 0.0f && label[nb[q]] == 0xffffffffu) {
+                    label[nb[q]] = (uint32_t)start;
+                    stack[sp++] = nb[q];
+                }
+        }
+        if (nm < 16) {
+            for (int m = 0; m < nm; m++) {
+                int k = members[m];
+                open[k] = 0.0f;
+                int i = k % w, j = k / w;
+                int nodes[4] = {j * nw + i, j * nw + i + 1, (j + 1) * nw + i, (j + 1) * nw + i + 1};
+                for (int q = 0; q < 4; q++) sdf[nodes[q]] = fminf(sdf[nodes[q]], -0.5f);
+            }
+        }
+    }
+    free(label);
+    free(stack);
+    free(members);
+}
+
+/* Scene::regions (scene.rs:385-425) */
+static void regions_of(const float* solid4, int w, int h, uint32_t* region) {
+    size_t n = (size_t)w * h;
+    int* stack = (int*)malloc(n * sizeof(int));
+    for (size_t k = 0; k < n; k++) region[k] = 0xffffffffu;
+    uint32_t count = 0;
+    for (int start = 0; start < (int)n; start++) {
+        if (solid4[4 * start + 3] == 0.0f || region[start] != 0xffffffffu) continue;
+        uint32_t id = count < 31u ? count : 31u;
+        count++;
+        int vent = start, sp = 0;
+        region[start] = id;
+        stack[sp++] = start;
+        while (sp > 0) {
+            int k = stack[--sp];
+            if (k / w > vent / w || (k / w == vent / w && k < vent)) vent = k;
+            int i = k % w, j = k / w;
+            int okl = i > 0, okr = i + 1 < w, okb = j > 0, okt = j + 1 < h;
+            float al = solid4[4 * k + 0];
+            float ar = okr ? solid4[4 * (k + 1) + 0] : 0.0f;
+            float ab = solid4[4 * k + 1];
+            float at = okt ? solid4[4 * (k + w) + 1] : 0.0f;
+            int nb[4] = {k - 1, k + 1, k - w, k + w};
+            int ok[4] = {okl, okr, okb, okt};
+            float a[4] = {al, ar, ab, at};
+            for (int q = 0; q < 4; q++)
+                if (ok[q] && a[q] > 0.0f && region[nb[q]] == 0xffffffffu) {
+                    region[nb[q]] = id;
+                    stack[sp++] = nb[q];
+                }
+        }
+        region[vent] |= REGION_VENT;
+    }
+    for (size_t k = 0; k < n; k++)
+        if (region[k] == 0xffffffffu) region[k] = 0;
+    free(stack);
+}
+
+int oscene_rasterize(int w, int h, int nshapes, const OShape* shapes, float* sdf,
+                     float* solid4, uint32_t* region, float* temp) {
+    int nw = w + 1, nh = h + 1;
+    for (int j = 0; j < nh; j++)
+        for (int i = 0; i < nw; i++) sdf[j * nw + i] = wall_sdf(w, h, (float)i, (float)j);
+    const float REACH = 6.0f;
+    for (int s = 0; s < nshapes; s++) {
+        float c[2], r;
+        shape_bound(&shapes[s], c, &r);
+        r = r + REACH;
+        int i0 = (int)fmaxf(floorf(c[0] - r), 0.0f);
+        int i1 = clampi((int)ceilf(c[0] + r), 0, nw - 1);
+        int j0 = (int)fmaxf(floorf(c[1] - r), 0.0f);
+        int j1 = clampi((int)ceilf(c[1] + r), 0, nh - 1);
+        int jend = mini(maxi(j1, j0), nh - 1), iend = mini(maxi(i1, i0), nw - 1);
+        for (int j = j0; j <= jend; j++)
+            for (int i = i0; i <= iend; i++) {
+                float* d = &sdf[j * nw + i];
+                *d = fminf(*d, shape_sdf(&shapes[s], (float)i, (float)j));
+            }
+    }
+    union_depth(sdf, nw, nh);
+    float* open = (float*)malloc((size_t)w * h * sizeof(float));
+    static const float FX[4][2] = {{0.25f, 0.25f}, {0.75f, 0.25f}, {0.25f, 0.75f}, {0.75f, 0.75f}};
+    for (int j = 0; j < h; j++)
+        for (int i = 0; i < w; i++) {
+            float d[4] = {sdf[j * nw + i], sdf[j * nw + i + 1], sdf[(j + 1) * nw + i], sdf[(j + 1) * nw + i + 1]};
+            float acc = 0.0f;
+            for (int q = 0; q < 4; q++) {
+                float fx = FX[q][0], fy = FX[q][1];
+                float v = (d[0] * (1.0f - fx) + d[1] * fx) * (1.0f - fy) + (d[2] * (1.0f - fx) + d[3] * fx) * fy;
+                acc += clampf(v / 0.5f + 0.5f, 0.0f, 1.0f);
+            }
+            open[j * w + i] = acc * 0.25f < 0.1f ? 0.0f : acc * 0.25f;
+        }
+    seal_pockets(open, sdf, w, h);
+    static const float K[3] = {1.0f / 6.0f, 2.0f / 3.0f, 1.0f / 6.0f};
+    for (int j = 0; j < h; j++)
+        for (int i = 0; i < w; i++) {
+            float occ = 0.0f;
+            for (int b = 0; b < 3; b++)
+                for (int a = 0; a < 3; a++) {
+                    int ii = i + a - 1, jj = j + b - 1;
+                    float sv = (ii < 0 || jj < 0 || ii >= w || jj >= h) ? 1.0f : 1.0f - open[jj * w + ii];
+                    occ += K[a] * K[b] * sv;
+                }
+            float f[2];
+            faces_of(open, sdf, w, i, j, f);
+            float* o = &solid4[4 * (j * w + i)];
+            o[0] = f[0];
+            o[1] = f[1];
+            o[2] = occ;
+            o[3] = open[j * w + i];
+        }
+    regions_of(solid4, w, h, region);
+    int any = 0;
+    for (int s = 0; s < nshapes; s++) any |= shapes[s].temp > -1e8f;
+    if (any && temp) {
+        for (int k = 0; k < w * h; k++) temp[k] = NO_TEMP;
+        for (int s = 0; s < nshapes; s++) {
+            if (!(shapes[s].temp > -1e8f)) continue;
+            float c[2], r;
+            shape_bound(&shapes[s], c, &r);
+            r = r + 2.0f;
+            int i0 = (int)fmaxf(floorf(c[0] - r), 0.0f);
+            int i1 = mini((int)fmaxf(ceilf(c[0] + r), 0.0f), w);
+            int j0 = (int)fmaxf(floorf(c[1] - r), 0.0f);
+            int j1 = mini((int)fmaxf(ceilf(c[1] + r), 0.0f), h);
+            for (int j = j0; j < j1; j++)
+                for (int i = i0; i < i1; i++)
+                    if (shape_sdf(&shapes[s], (float)i + 0.5f, (float)j + 0.5f) < 0.75f) temp[j * w + i] = shapes[s].temp;
+        }
+    }
+    free(open);
+    return any;
+}
+
+/* maps.rs:455-492. Rust's f32::round rounds half away from zero, as C's roundf. */
+static float rng_next(uint32_t* s) {
+    *s ^= *s << 13;
+    *s ^= *s >> 17;
+    *s ^= *s << 5;
+    return (float)(*s >> 8) / (float)(1u << 24);
+}
+
+uint32_t ofill_rect(int w, int h, int nshapes, const OShape* shapes, const float rect[4],
+                    uint32_t material, OParticle* out, uint32_t n0, uint32_t cap) {
+    const int sub = 2;
+    const float step = 1.0f / (float)sub;
+    float W = (float)w, H = (float)h;
+    int x0 = (int)roundf(fmaxf(rect[0], WALL) / step);
+    int x1 = (int)roundf(fminf(rect[2], W - WALL) / step);
+    int y0 = (int)roundf(fmaxf(rect[1], WALL) / step);
+    int y1 = (int)roundf(fminf(rect[3], H - WALL) / step);
+    uint32_t rng = 0x9E3779B9u ^ (n0 * 747796405u + 1u);
+    uint32_t n = n0;
+    for (int j = y0; j < y1; j++)
+        for (int i = x0; i < x1; i++) {
+            float px = ((float)i + 0.5f + (rng_next(&rng) - 0.5f) * 0.5f) * step;
+            float py = ((float)j + 0.5f + (rng_next(&rng) - 0.5f) * 0.5f) * step;
+            if (oscene_sdf(w, h, nshapes, shapes, px, py) > 0.1f) {
+                if (n < cap) {
+                    OParticle* p = &out[n];
+                    memset(p, 0, sizeof *p);
+                    p->pos[0] = px;
+                    p->pos[1] = py;
+                    p->s = SPAWN_S;
+                    p->kind = material + 1u;
+                    p->t = SPAWN_TEMP;
+                }
+                n++;
+            }
+        }
+    return n;
+}
+
+/* ------------------------------------------------------------------------------------ */
+/* GPU-side tables: materials and parameters in grid units                                */
+/* ------------------------------------------------------------------------------------ */
+
+typedef struct GMat {   /* common.glsl:224-238 (the fields the restated passes read) */
+    int ia[4], ib[4];
+    float a[4], b[4], temp[4], th[4], th2[4], el[4], misc[4], rx[4];
+} GMat;
+
+typedef struct GParams {   /* common.glsl:37-86 (subset) */
+    int grid[2];
+    uint32_t n_slots;
+    float dt_fixed, gravity, inv_ppc, apic_clamp;
+    float pair[GROUPS][GROUPS];
+    float misc[4];
+    int n_present, acc_stride, n_fam;
+    uint32_t group_mask, caps;
+    int primary;
+    uint32_t group_heat;
+    int present[MAX_PRESENT];
+    float heat[4], heat2[4];
+    float sep_tau, cfl, tool_crowd_max, density_k, dt_max, crowd_jitter, ext_speed, wall_margin;
+    float tool_pos[2], tool_vel[2], tool_radius;
+    int tool_mode;
+    float tool_strength;
+    float tol[4], ext[4], corr[4], heat3[4];
+    float corr_gain;   /* min(1 - exp(-dt / tol.w), density_k) is per substep: see rhs */
+} GParams;
+
+typedef struct Tank {   /* mod.rs:222-245 */
+    int nrows;
+    int rows[MAX_PRESENT];
+    int chan[MAX_PRESENT][3];
+    int stride, families, primary, chan_t;
+    uint32_t group_mask;
+    int chan_g[GROUPS];
+} Tank;
+
+typedef struct StepBuf {   /* common.glsl:122-135 */
+    float frame_left, advanced;
+    uint32_t batch_steps, batch_done;
+    float dt, dt_prev;
+    uint32_t umax_grid, umax_part;
+    float dt_cfl;
+    uint32_t substeps;
+    float umax_seen;
+    uint32_t pad0;
+} StepBuf;
+
+typedef struct SolveBuf {   /* common.glsl:138-149 */
+    float p_rz[2], p_alpha[2], p_beta[2], p_bb[2], p_rr[2];
+    uint32_t p_done[2], p_iters[2];
+    uint32_t p_it_max, p_unconv, p2_it_max, p2_unconv, solves;
+    float p_res_max;
+} SolveBuf;
+
+typedef struct Levels {   /* mod.rs:714-753 */
+    int n;
+    int dims[24][2];
+    int offs[24];
+    int total, tail;
+    int tile_offs[24];
+    int tiles;
+} Levels;
+
+struct OSim {
+    int W, H;
+    uint32_t capacity, n_slots;
+    OSimParams prm;
+    Tank tank;
+    int thermal, solids_heated, cleared, grid_valid;
+    uint32_t caps;
+    int visc_mode;   /* 0 none, 1 explicit, 2 implicit */
+    uint32_t since_sort;
+    uint64_t substeps_done;
+    GMat mats[O_MAX_MATERIALS];
+    GParams P;
+    StepBuf S;
+    SolveBuf K;
+    Levels lv;
+    int nwg;
+    double sim_time;
+    /* particles */
+    OParticle* particles;
+    OParticle* sorted;
+    /* grid */
+    int32_t* acc;
+    V4 *vel, *cell, *comp, *coef, *sprop, *surf, *surf2, *aux, *grho, *therm, *dheat, *vw, *vs, *prhs;
+    V2 *vel0, *pjump, *pres;
+    float* p2keep;
+    I2* hcell;
+    V4* solid;
+    float* sdf;
+    uint32_t* region;
+    uint32_t region_air;
+    float* solid_t;
+    uint64_t ledger[8];
+    /* multigrid / Krylov */
+    V4* mga;
+    float* mgd;
+    V2 *mgx, *mgz, *mgr, *cgp, *cgp2, *cgq;
+    uint32_t* ptile;
+    V4* part;
+    /* scratch for the particle pass */
+    struct Scat* scat;
+};
+
+static int g_threads = 1;
+void osim_set_threads(int n) { g_threads = n > 0 ? n : 1; }
+
+static float tension_cells(const OSimParams* p, float sigma) {
+    float dx = p->cell_size;
+    return sigma / (WATER_DENSITY * dx * dx * dx);
+}
+
+static int freezes(const OMat* m) { return m->melt_hi > -273.0f; }
+
+static float temp_factor_ln(const OMat* m, float t) {   /* material.rs:429-440 */
+    float tk = maxf(t + 273.15f, 1.0f);
+    float tref = m->temp_ref + 273.15f;
+    float x = 0.0f;
+    if (m->temp_model == 1) x = m->temp_b * (1.0f / tk - 1.0f / tref);
+    else if (m->temp_model == 2) x = m->temp_b / maxf(tk - m->temp_c, 5.0f) - m->temp_b / maxf(tref - m->temp_c, 5.0f);
+    return clampf(x, -30.0f, 30.0f);
+}
+
+static float viscosity_at(const OMat* m, float t) { return m->viscosity * expf(temp_factor_ln(m, t)); }
+
+/* Tank::layout (mod.rs:271-329). rows ascending. Returns 0 if they do not fit. */
+static int tank_layout(Tank* t, const int* rows, int nrows, const OSimParams* p, int thermal) {
+    memset(t, 0, sizeof *t);
+    if (nrows > MAX_PRESENT) return 0;
+    int next = ACC_FIRST;
+    uint32_t gm = 0;
+    int primary = -1;
+    for (int k = 0; k < nrows; k++)
+        if (p->mat[rows[k]].diluent == rows[0]) { primary = k; break; }
+    int families = primary >= 0 ? 1 : 0;
+    for (int k = 0; k < nrows; k++) {
+        const OMat* m = &p->mat[rows[k]];
+        gm |= 1u << (m->group < GROUPS - 1 ? m->group : GROUPS - 1);
+        int c[3] = {-1, -1, -1};
+        if (k > 0 && k != primary) c[0] = next++;
+        if (m->diluent >= 0) {
+            c[1] = next++;
+            if (k == primary) c[2] = 0;
+            else c[2] = families++;
+        }
+        memcpy(t->chan[k], c, sizeof c);
+        t->rows[k] = rows[k];
+    }
+    t->nrows = nrows;
+    t->chan_t = thermal ? next : -1;
+    next += thermal ? 1 : 0;
+    for (int g = 0; g < GROUPS; g++) t->chan_g[g] = -1;
+    if (thermal) {
+        int first = 1;
+        for (int g = 0; g < GROUPS; g++)
+            if (gm & (1u << g)) {
+                if (!first) t->chan_g[g] = next++;
+                first = 0;
+            }
+    }
+    if (next > ACC_MAX) return 0;
+    int stride = next > ACC_MIN ? next : ACC_MIN;
+    stride = (stride + 3) / 4 * 4;
+    t->stride = stride;
+    t->families = families;
+    t->group_mask = gm;
+    t->primary = primary >= 0 ? rows[primary] : -1;
+    return 1;
+}
+
+static float dt_capillary(const OSimParams* p, const Tank* t) {   /* params.rs:962-982 */
+    float worst = 0.0f;
+    for (int a = 0; a < t->nrows; a++) {
+        if (t->rows[a] == 57) continue;
+        const OMat* m = &p->mat[t->rows[a]];
+        worst = maxf(worst, tension_cells(p, m->tension) / (m->density / WATER_DENSITY));
+        for (int b = 0; b < t->nrows; b++) {
+            if (t->rows[b] == 57) continue;
+            const OMat* n = &p->mat[t->rows[b]];
+            if (n->group != m->group) {
+                float sigma = tension_cells(p, p->pair_tension[m->group][n->group]);
+                worst = maxf(worst, sigma / (minf(m->density, n->density) / WATER_DENSITY));
+            }
+        }
+    }
+    if (worst <= 0.0f) return INFINITY;
+    return 0.5f * sqrtf(1.0f / (2.0f * 3.14159274f * worst));
+}
+
+static float particle_heat_vol(const OSimParams* p, int row) {
+    int r = row == 57 ? 0 : row;
+    return p->mat[r].density * p->mat[r].heat_capacity;
+}
+
+static float dt_thermal(const OSimParams* p, const Tank* t) {   /* params.rs:907-914 */
+    if (p->heat_rate <= 0.0f) return INFINITY;
+    float dx2 = p->cell_size * p->cell_size;
+    float m = INFINITY;
+    for (int k = 0; k < t->nrows; k++) {
+        int i = t->rows[k];
+        float v = 0.2f * dx2 * particle_heat_vol(p, i) / maxf(p->mat[i].conductivity, 1e-6f) / p->heat_rate;
+        m = minf(m, v);
+    }
+    return m;
+}
+
+static float dt_limit(const OSim* s) {   /* mod.rs:2332-2339 */
+    const OSimParams* p = &s->prm;
+    float dt = minf(p->dt_max, dt_capillary(p, &s->tank));
+    if (s->thermal) dt = minf(dt, dt_thermal(p, &s->tank));
+    return dt;
+}
+
+static int viscosity_mode(const OSim* s) {   /* mod.rs:2768-2792 */
+    float dt = dt_limit(s);
+    const OSimParams* p = &s->prm;
+    float d = 0.0f;
+    for (int k = 0; k < s->tank.nrows; k++) {
+        const OMat* m = &p->mat[s->tank.rows[k]];
+        float cells = 1.0f / (p->cell_size * p->cell_size);
+        float nu;
+        if (!s->thermal) nu = viscosity_at(m, p->ambient_temp) * cells;
+        else if (freezes(m) || m->temp_model != 0) nu = INFINITY;
+        else nu = m->viscosity * cells;
+        d = maxf(d, nu * dt);
+    }
+    if (d <= 0.0f) return 0;
+    if (d <= 0.05f) return 1;
+    return 2;
+}
+
+static uint32_t compute_caps(const OSim* s) {   /* mod.rs:2717-2761 (the bits that apply) */
+    const OSimParams* p = &s->prm;
+    uint32_t caps = 0;
+    if (s->tank.families > 0) caps |= CAP_FAMILIES;
+    if (s->thermal) caps |= CAP_THERMAL;
+    int rigid = 0;
+    for (int k = 0; k < s->tank.nrows; k++) {
+        const OMat* m = &p->mat[s->tank.rows[k]];
+        const OMat* dil = m->diluent >= 0 ? &p->mat[m->diluent] : NULL;
+        if (m->rheology != 0 || m->skin > 0.0f || m->friction > 0.0f) {
+            caps |= CAP_RHEO;
+            rigid |= m->rheology == 2 || m->rheology == 3 || m->skin > 0.0f || m->friction > 0.0f;
+        }
+        if (s->thermal)
+            rigid |= freezes(m) || (dil && freezes(dil)) || m->temp_model != 0 || (dil && dil->temp_model != 0);
+        rigid |= viscosity_at(m, p->ambient_temp) >= p->rigid_viscosity || (!s->thermal && freezes(m) && p->ambient_temp < m->melt_hi);
+    }
+    if (rigid) caps |= CAP_RIGID;
+    for (int k = 0; k < s->tank.nrows; k++)
+        if (s->tank.rows[k] == 57 && s->thermal) caps |= CAP_STEAM;
+    return caps;
+}
+
+/* gpu_materials (mod.rs:2179-2236) */
+static void build_mats(OSim* s) {
+    const OSimParams* p = &s->prm;
+    float dx = p->cell_size;
+    for (int r = 0; r < O_MAX_MATERIALS; r++) {
+        const OMat* m = &p->mat[r];
+        GMat* g = &s->mats[r];
+        memset(g, 0, sizeof *g);
+        int chan[3] = {-1, -1, -1};
+        for (int k = 0; k < s->tank.nrows; k++)
+            if (s->tank.rows[k] == r) memcpy(chan, s->tank.chan[k], sizeof chan);
+        float ang = m->contact_angle * (3.14159274f / 180.0f);
+        float sn = sinf(ang), cs = cosf(ang);
+        float solid = m->density_solid > 0.0f ? m->density_solid : m->density;
+        float cvol = particle_heat_vol(p, r);
+        float ln_nu = logf(maxf(m->viscosity / (dx * dx), 1e-8f));
+        float rho = m->density;
+        if (!s->thermal) {
+            ln_nu += temp_factor_ln(m, p->ambient_temp);
+            rho *= clampf(1.0f - m->expansion * (p->ambient_temp - m->temp_ref), 0.7f, 1.3f);
+            if (freezes(m) && m->diluent < 0 && p->ambient_temp < m->melt_hi) {
+                float fs = clampf((m->melt_hi - p->ambient_temp) / maxf(m->melt_hi - m->melt_lo, 1e-3f), 0.0f, 1.0f);
+                float frozen = maxf(logf(p->rigid_viscosity / (dx * dx)), ln_nu);
+                ln_nu += (frozen - ln_nu) * fs;
+                rho += (solid - rho) * fs;
+            }
+        }
+        g->ia[0] = (int)(m->group < GROUPS - 1 ? m->group : GROUPS - 1);
+        g->ia[1] = m->diluent;
+        g->ia[2] = chan[0];
+        g->ia[3] = chan[1];
+        g->ib[0] = chan[2];
+        g->ib[1] = (int)m->rheology;
+        g->ib[2] = (int)m->temp_model;
+        g->ib[3] = -1;
+        g->a[0] = rho / WATER_DENSITY;
+        g->a[1] = ln_nu;
+        g->a[2] = tension_cells(p, m->tension);
+        g->a[3] = m->mix_rate;
+        g->b[0] = cs;
+        g->b[1] = sn;
+        g->b[2] = m->grain / dx;
+        g->b[3] = solid / WATER_DENSITY;
+        g->temp[0] = m->temp_b;
+        g->temp[1] = m->temp_c;
+        g->temp[2] = m->temp_ref + 273.15f;
+        g->temp[3] = tension_cells(p, m->skin);
+        g->th[0] = cvol / WATER_HEAT;
+        g->th[1] = m->conductivity / (WATER_HEAT * dx * dx);
+        g->th[2] = maxf(m->melt_lo, NO_MELT);
+        g->th[3] = maxf(maxf(m->melt_hi, m->melt_lo + 0.25f), NO_MELT);
+        g->th2[0] = (freezes(m) || m->diluent >= 0) ? m->latent / m->heat_capacity : 0.0f;
+        g->th2[1] = m->emissivity;
+        g->th2[2] = m->boil;
+        g->th2[3] = m->latent_vap / m->heat_capacity;
+        g->el[2] = m->susceptibility;
+        g->misc[0] = m->freeze_shift;
+        g->misc[1] = m->load;
+        g->misc[2] = 1.0f;
+        g->misc[3] = m->expansion;
+        g->rx[2] = m->self_heat / m->heat_capacity;
+        g->rx[3] = m->volatility;
+    }
+}
+
+static float speed_cap_cells(const OSimParams* p, int height) {
+    float g = p->gravity / p->cell_size;
+    if (p->speed_cap > 0.0f && g > 0.0f) return p->speed_cap * sqrtf(2.0f * g * (float)height);
+    return 1e30f;
+}
+
+static float tool_speed(const OTool* t) {   /* params.rs:1201-1208 */
+    switch (t->mode) {
+    case 1: return hypotf(t->vel[0], t->vel[1]) + 4.0f * t->radius;
+    case 3:
+    case 4: return hypotf(t->vel[0], t->vel[1]);
+    case 7: return fabsf(t->vel[0]) + 2.0f * t->radius;
+    default: return 0.0f;
+    }
+}
+
+/* gpu_params (mod.rs:2238-2328) */
+static void build_params(OSim* s, const OTool* tool) {
+    const OSimParams* p = &s->prm;
+    GParams* P = &s->P;
+    memset(P, 0, sizeof *P);
+    float dx = p->cell_size;
+    P->grid[0] = s->W;
+    P->grid[1] = s->H;
+    P->n_slots = s->n_slots;
+    P->dt_fixed = p->fixed_hz > 0.0f ? 1.0f / p->fixed_hz : 0.0f;
+    P->gravity = p->gravity / p->cell_size;
+    P->inv_ppc = 1.0f / (float)PPC;
+    P->apic_clamp = p->apic_clamp;
+    for (int a = 0; a < GROUPS; a++)
+        for (int b = 0; b < GROUPS; b++) P->pair[a][b] = tension_cells(p, p->pair_tension[a][b]);
+    P->misc[0] = p->curvature_max;
+    P->misc[1] = (float)p->sealed_vent;
+    P->misc[2] = p->cell_size;
+    P->misc[3] = -1.0f;
+    P->n_present = s->tank.nrows;
+    P->acc_stride = s->tank.stride > ACC_MIN ? s->tank.stride : ACC_MIN;
+    P->n_fam = s->tank.families;
+    P->group_mask = s->tank.group_mask;
+    P->caps = s->caps;
+    P->primary = s->tank.nrows == 0 ? -1 : s->tank.primary;
+    uint32_t gh = 0;
+    for (int g = 0; g < GROUPS; g++) gh += ((uint32_t)(s->tank.chan_g[g] + 1) & 255u) << (8 * g);
+    P->group_heat = gh;
+    for (int k = 0; k < s->tank.nrows; k++) P->present[k] = s->tank.rows[k];
+    P->heat[0] = p->ambient_temp;
+    P->heat[1] = p->heat_rate;
+    P->heat[2] = p->air_cooling / (WATER_HEAT * dx);
+    P->heat[3] = STEFAN_BOLTZMANN / (WATER_HEAT * dx);
+    P->heat2[0] = logf(p->rigid_viscosity / (dx * dx));
+    P->heat2[1] = p->heat_power;
+    P->heat2[2] = (float)s->tank.chan_t;
+    P->heat2[3] = p->contact_heat / (WATER_HEAT * dx);
+    P->sep_tau = p->droplet_cells;
+    P->cfl = p->cfl;
+    P->tool_crowd_max = p->tool_crowd_max;
+    P->density_k = p->correction_max;
+    P->dt_max = dt_limit(s);
+    P->crowd_jitter = p->crowd_jitter;
+    P->ext_speed = tool ? tool_speed(tool) : 0.0f;
+    P->wall_margin = 0.1f;
+    if (tool) {
+        P->tool_pos[0] = tool->pos[0];
+        P->tool_pos[1] = tool->pos[1];
+        P->tool_vel[0] = tool->vel[0];
+        P->tool_vel[1] = tool->vel[1];
+        P->tool_radius = maxf(tool->radius, 0.01f);
+        P->tool_mode = tool->mode;
+        P->tool_strength = tool->strength;
+    } else {
+        P->tool_radius = 0.01f;
+    }
+    P->tol[0] = p->pressure_tol;
+    P->tol[1] = p->correction_tol;
+    P->tol[2] = p->viscosity_tol;
+    P->tol[3] = p->correction_time;
+    P->ext[0] = speed_cap_cells(p, s->H);
+    P->ext[1] = (float)p->advection_order;
+    P->ext[2] = p->spray_cfl;
+    P->ext[3] = 0.0f;
+    P->corr[0] = p->correction_step_max;
+    P->corr[1] = p->correction_deadband;
+    P->corr[2] = (float)p->slip_cap;
+    P->corr[3] = p->implicit_viscosity_min;
+    P->heat3[0] = maxf(p->eddy_heat, 0.0f);
+    P->heat3[1] = p->evaporation ? 2.257e6f / 1005.0f : 0.0f;
+    P->heat3[2] = 0.0f;
+}
+
+/* Levels::new (mod.rs:734-753) */
+static void levels_new(Levels* L, int w, int h) {
+    memset(L, 0, sizeof *L);
+    L->dims[0][0] = w;
+    L->dims[0][1] = h;
+    L->n = 1;
+    while (L->dims[L->n - 1][0] * L->dims[L->n - 1][1] > COARSEST_CELLS) {
+        int pw = L->dims[L->n - 1][0], ph = L->dims[L->n - 1][1];
+        L->dims[L->n][0] = (pw + 1) / 2;
+        L->dims[L->n][1] = (ph + 1) / 2;
+        L->n++;
+    }
+    int total = 0;
+    for (int l = 0; l < L->n; l++) {
+        L->offs[l] = total;
+        total += L->dims[l][0] * L->dims[l][1];
+    }
+    L->total = total;
+    int tail = L->n - 1;
+    for (int l = 1; l < L->n; l++)
+        if (L->dims[l][0] * L->dims[l][1] <= TAIL_CELLS) { tail = l; break; }
+    if (tail < 1) tail = 1;
+    if (tail > L->n - 1) tail = L->n - 1;
+    L->tail = tail;
+    int tiles = 0;
+    for (int l = 0; l <= tail; l++) {
+        L->tile_offs[l] = tiles;
+        tiles += ((L->dims[l][0] + 15) / 16) * ((L->dims[l][1] + 15) / 16);
+    }
+    L->tiles = tiles;
+}
+
+/* ------------------------------------------------------------------------------------ */
+/* Helpers over the tables (common.glsl)                                                 */
+/* ------------------------------------------------------------------------------------ */
+
+#define P_ (s->P)
+static inline int cidx(const OSim* s, int x, int y) { return y * s->W + x; }
+static inline int face_live(float st) { return fabsf(st) < 1e29f; }
+static inline int face_closed(float st) { return st < -1e29f; }
+static inline int has_cap(const OSim* s, uint32_t c) { return (s->caps & c) != 0u; }
+
+static float row_density(const OSim* s, uint32_t row, float sc) {   /* common.glsl:475-479 */
+    int d = s->mats[row].ia[1];
+    float rho = s->mats[row].a[0];
+    return d >= 0 ? mixf(s->mats[d].a[0], rho, sc) : rho;
+}
+
+static float expansion_of(const OSim* s, uint32_t row, float sc, float T) {   /* common.glsl:485-494 */
+    const GMat* m = &s->mats[row];
+    int d = m->ia[1];
+    float b = m->misc[3], tr = m->temp[2] - 273.15f, tb = m->th2[2];
+    if (d >= 0) {
+        b = mixf(s->mats[d].misc[3], b, sc);
+        tr = mixf(s->mats[d].temp[2] - 273.15f, tr, sc);
+        tb = mixf(s->mats[d].th2[2], tb, sc);
+    }
+    return clampf(1.0f - b * (minf(T, tb) - tr), 0.7f, 1.3f);
+}
+
+static V4 thermal_of(const OSim* s, uint32_t row, float sc) {   /* common.glsl:500-509 */
+    const GMat* m = &s->mats[row];
+    float ld = m->th2[0];
+    int d = m->ia[1];
+    if (d < 0) return v4(m->th[2], m->th[3], ld, m->th[0]);
+    const float* dth = s->mats[d].th;
+    float shift = m->misc[0] * sc;
+    float C = mixf(dth[0], m->th[0], sc);
+    return v4(dth[2] + shift, dth[3] + shift, mixf(dth[0] * s->mats[d].th2[0], m->th[0] * ld, sc) / C, C);
+}
+
+static V2 phase_of(float te, V4 m) {   /* common.glsl:515-521 */
+    if (te >= m.y) return v2(te, 0.0f);
+    float lo = m.x - m.z;
+    if (te <= lo) return v2(te + m.z, 1.0f);
+    float fr = (te - lo) / (m.y - lo);
+    return v2(m.x + fr * (m.y - m.x), 1.0f - fr);
+}
+
+static float temp_law(const OSim* s, int r, float T) {   /* common.glsl:410-417 */
+    int model = s->mats[r].ib[2];
+    if (model == 0) return 0.0f;
+    const float* tp = s->mats[r].temp;
+    float Tk = maxf(T + 273.15f, 1.0f);
+    float x = model == 1 ? tp[0] * (1.0f / Tk - 1.0f / tp[2])
+                         : tp[0] / maxf(Tk - tp[1], 5.0f) - tp[0] / maxf(tp[2] - tp[1], 5.0f);
+    return clampf(x, -30.0f, 30.0f);
+}
+
+static int group_heat_chan(const OSim* s, int g) { return (int)((P_.group_heat >> (8u * (uint32_t)g)) & 255u) - 1; }
+
+static void bspline(float fx, float fy, V2 w[3]) {   /* common.glsl:639-643 */
+    w[0] = v2(0.5f * (1.5f - fx) * (1.5f - fx), 0.5f * (1.5f - fy) * (1.5f - fy));
+    w[1] = v2(0.75f - (fx - 1.0f) * (fx - 1.0f), 0.75f - (fy - 1.0f) * (fy - 1.0f));
+    w[2] = v2(0.5f * (fx - 0.5f) * (fx - 0.5f), 0.5f * (fy - 0.5f) * (fy - 0.5f));
+}
+
+static void ledger_add(OSim* s, int entry, float v) {   /* common.glsl:448-453 */
+    uint32_t x = (uint32_t)(v * LEDGER_SCALE + 0.5f);
+    if (x == 0u) return;
+#pragma omp atomic
+    s->ledger[entry] += x;
+}
+
+/* air.glsl:13-22 */
+static float sample_sdf(const OSim* s, V2 x, V2* grad) {
+    float gx = clampf(x.x, 0.0f, (float)s->W - 0.001f), gy = clampf(x.y, 0.0f, (float)s->H - 0.001f);
+    int ix = (int)gx, iy = (int)gy;
+    float fx = gx - (float)ix, fy = gy - (float)iy;
+    int w1 = s->W + 1;
+    int k = iy * w1 + ix;
+    float d00 = s->sdf[k], d10 = s->sdf[k + 1], d01 = s->sdf[k + w1], d11 = s->sdf[k + w1 + 1];
+    grad->x = mixf(d10 - d00, d11 - d01, fy);
+    grad->y = mixf(d01 - d00, d11 - d10, fx);
+    return mixf(mixf(d00, d10, fx), mixf(d01, d11, fx), fy);
+}
+
+/* air.glsl:31-37 */
+static V2 tool_target(const OSim* s, V2 d) {
+    float l = len2(d);
+    if (P_.tool_mode == 3) { float q = maxf(l, 0.15f * P_.tool_radius); return v2(-d.x / q * P_.tool_vel[0], -d.y / q * P_.tool_vel[0]); }
+    if (P_.tool_mode == 4) return v2(P_.tool_vel[0], P_.tool_vel[1]);
+    if (P_.tool_mode == 7) {
+        float q = maxf(l, 0.4f * P_.tool_radius);
+        return v2(d.y / q * P_.tool_vel[0] + d.x * 2.0f, -d.x / q * P_.tool_vel[0] + d.y * 2.0f);
+    }
+    if (P_.tool_mode == 8) return v2(0.0f, 0.0f);
+    return v2(P_.tool_vel[0] + d.x * 4.0f, P_.tool_vel[1] + d.y * 4.0f);
+}
+
+/* air.glsl:41-78 */
+static V2 sample_vel(const OSim* s, V2 x, V2 fallback) {
+    V2 o = fallback;
+    {
+        float gx = x.x, gy = x.y - 0.5f;
+        int bx = (int)floorf(gx), by = (int)floorf(gy);
+        float fx = gx - (float)bx, fy = gy - (float)by;
+        float sw = 0.0f, su = 0.0f;
+        for (int b = 0; b < 2; b++)
+            for (int a = 0; a < 2; a++) {
+                V4 q = s->vel[cidx(s, bx + a, by + b)];
+                if (face_live(q.z)) {
+                    float wt = (a == 0 ? 1.0f - fx : fx) * (b == 0 ? 1.0f - fy : fy);
+                    sw += wt;
+                    su += wt * q.x;
+                }
+            }
+        if (sw > 1e-3f) o.x = su / sw;
+    }
+    {
+        float gx = x.x - 0.5f, gy = x.y;
+        int bx = (int)floorf(gx), by = (int)floorf(gy);
+        float fx = gx - (float)bx, fy = gy - (float)by;
+        float sw = 0.0f, su = 0.0f;
+        for (int b = 0; b < 2; b++)
+            for (int a = 0; a < 2; a++) {
+                V4 q = s->vel[cidx(s, bx + a, by + b)];
+                if (face_live(q.w)) {
+                    float wt = (a == 0 ? 1.0f - fx : fx) * (b == 0 ? 1.0f - fy : fy);
+                    sw += wt;
+                    su += wt * q.y;
+                }
+            }
+        if (sw > 1e-3f) o.y = su / sw;
+    }
+    return o;
+}
+
+/* particles.comp:51-65 */
+static int collide(const OSim* s, V2* x, V2* v, int beyond) {
+    V2 n;
+    float d = sample_sdf(s, *x, &n);
+    if (d < P_.wall_margin) {
+        float l = len2(n);
+        if (l > 1e-5f) {
+            n.x /= l;
+            n.y /= l;
+            float push = P_.wall_margin - d + (beyond ? maxf(-d, 0.0f) : 0.0f);
+            x->x += n.x * push;
+            x->y += n.y * push;
+            float vn = v->x * n.x + v->y * n.y;
+            if (vn < 0.0f) {
+                v->x -= vn * n.x;
+                v->y -= vn * n.y;
+            }
+            return 1;
+        }
+    }
+    return 0;
+}
+
+/* particles.comp:70-73 */
+static I2 heat_quanta(float C, float T) {
+    int ci = (int)floorf(C * MASS_SCALE + 0.5f);
+    I2 r = {ci, (int)floorf((float)ci * (T + 273.15f) / T_SCALE + 0.5f)};
+    return r;
+}
+
+/* ------------------------------------------------------------------------------------ */
+/* step.comp                                                                             */
+/* ------------------------------------------------------------------------------------ */
+
+static void k_step(OSim* s) {
+    StepBuf* S = &s->S;
+    float u = maxf(minf(bitsf(S->umax_grid), P_.ext[0]), bitsf(S->umax_part));
+    u = maxf(u, P_.ext_speed);
+    float dt_cfl = P_.cfl / (u + sqrtf(5.0f * maxf(P_.gravity, 0.0f)) + 1e-6f);
+    float dt;
+    if (P_.dt_fixed > 0.0f) {
+        dt = P_.dt_fixed;
+    } else {
+        uint32_t left = S->batch_steps > S->batch_done ? S->batch_steps - S->batch_done : 1u;
+        dt = minf(minf(dt_cfl, P_.dt_max), maxf(S->frame_left, 0.0f) / (float)left);
+    }
+    dt = maxf(dt, 1e-6f);
+    S->dt_prev = S->dt > 0.0f ? S->dt : dt;
+    S->dt = dt;
+    S->dt_cfl = minf(dt_cfl, P_.dt_max);
+    S->umax_seen = u;
+    S->frame_left -= dt;
+    float lo = bitsf(S->pad0);
+    float y = dt - lo;
+    float t = S->advanced + y;
+    S->pad0 = fbits((t - S->advanced) - y);
+    S->advanced = t;
+    S->batch_done += 1u;
+    S->substeps += 1u;
+    S->umax_grid = 0u;
+    S->umax_part = 0u;
+    s->region_air = 0u;
+}
+
+/* ------------------------------------------------------------------------------------ */
+/* particles.comp                                                                        */
+/* ------------------------------------------------------------------------------------ */
+
+typedef struct Scat {
+    int live;
+    V2 pos, vs;
+    V4 Cs;
+    float rho, sc, CT;
+    int cw, cs, ct, cg;
+} Scat;
+
+static void report_umax(uint32_t* slot, float m) {
+    uint32_t b = fbits(m);
+#pragma omp critical(umax)
+    {
+        if (m > bitsf(*slot)) *slot = b;
+    }
+}
+
+/* advance() (particles.comp:98-985) restricted to the capabilities the oracle carries:
+ * single phase group or several without drift, no families, no rigid bodies, elasticity,
+ * settling, steam, reactions or evaporation; thermal conduction and exchange supported. */
+static void advance(OSim* s, uint32_t id, int gather, Scat* g) {
+    g->live = 0;
+    if (id >= P_.n_slots) return;
+    OParticle p = s->particles[id];
+    if (p.kind == KIND_DEAD) return;
+    if ((p.kind & 255u) == 0u) return;   /* puffs are not made by the supported tanks */
+    float dt = s->S.dt;
+    uint32_t row = (p.kind & 255u) - 1u;
+    const int* Mia = s->mats[row].ia;
+    int thermal = has_cap(s, CAP_THERMAL);
+    V2 pos = v2(p.pos[0], p.pos[1]);
+    if (gather) {
+        V2 v = v2(p.vel[0], p.vel[1]);
+        V4 C = v4(p.c[0], p.c[1], p.c[2], p.c[3]);
+        V2 corr = v2(0.0f, 0.0f);
+        float slip = 0.0f, crowd = 0.0f;
+        V2 w[3];
+        /* u faces */
+        {
+            V2 gp = v2(pos.x - 0.0f, pos.y - 0.5f);
+            int bx = (int)floorf(gp.x - 0.5f), by = (int)floorf(gp.y - 0.5f);
+            float fx = gp.x - (float)bx, fy = gp.y - (float)by;
+            bspline(fx, fy, w);
+            float sw = 0.0f, su = 0.0f, sc = 0.0f;
+            V2 sd = v2(0, 0), sud = v2(0, 0);
+            for (int b = 0; b < 3; b++)
+                for (int a = 0; a < 3; a++) {
+                    V4 q = s->vel[cidx(s, bx + a, by + b)];
+                    if (face_live(q.z)) {
+                        float wt = w[a].x * w[b].y;
+                        V2 d = v2((float)a - fx, (float)b - fy);
+                        sw += wt;
+                        su += wt * q.x;
+                        sc += wt * q.z;
+                        sd.x += wt * d.x;
+                        sd.y += wt * d.y;
+                        sud.x += wt * q.x * d.x;
+                        sud.y += wt * q.x * d.y;
+                    }
+                }
+            if (sw > 1e-4f) {
+                float u = su / sw;
+                v.x = u;
+                corr.x = sc / sw;
+                C.x = 4.0f * (sud.x - u * sd.x) / sw;
+                C.y = 4.0f * (sud.y - u * sd.y) / sw;
+            }
+        }
+        /* v faces */
+        {
+            V2 gp = v2(pos.x - 0.5f, pos.y - 0.0f);
+            int bx = (int)floorf(gp.x - 0.5f), by = (int)floorf(gp.y - 0.5f);
+            float fx = gp.x - (float)bx, fy = gp.y - (float)by;
+            bspline(fx, fy, w);
+            float sw = 0.0f, su = 0.0f, sc = 0.0f;
+            V2 sd = v2(0, 0), sud = v2(0, 0);
+            for (int b = 0; b < 3; b++)
+                for (int a = 0; a < 3; a++) {
+                    V4 q = s->vel[cidx(s, bx + a, by + b)];
+                    if (face_live(q.w)) {
+                        float wt = w[a].x * w[b].y;
+                        V2 d = v2((float)a - fx, (float)b - fy);
+                        sw += wt;
+                        su += wt * q.y;
+                        sc += wt * q.w;
+                        sd.x += wt * d.x;
+                        sd.y += wt * d.y;
+                        sud.x += wt * q.y * d.x;
+                        sud.y += wt * q.y * d.y;
+                    }
+                }
+            if (sw > 1e-4f) {
+                float u = su / sw;
+                v.y = u;
+                corr.y = sc / sw;
+                C.z = 4.0f * (sud.x - u * sd.x) / sw;
+                C.w = 4.0f * (sud.y - u * sd.y) / sw;
+            }
+        }
+        if (P_.apic_clamp > 0.0f) {
+            float lim = P_.apic_clamp / dt;
+            C.x = clampf(C.x, -lim, lim);
+            C.y = clampf(C.y, -lim, lim);
+            C.z = clampf(C.z, -lim, lim);
+            C.w = clampf(C.w, -lim, lim);
+        }
+        if (P_.corr[0] > 0.0f) {
+            float cl = len2(corr), cmax = P_.corr[0] / dt;
+            if (cl > cmax) {
+                corr.x *= cmax / cl;
+                corr.y *= cmax / cl;
+            }
+        }
+        /* composition (particles.comp:288-571) */
+        {
+            V2 gp = v2(pos.x - 0.5f, pos.y - 0.5f);
+            int bx = (int)floorf(gp.x - 0.5f), by = (int)floorf(gp.y - 0.5f);
+            float fx = gp.x - (float)bx, fy = gp.y - (float)by;
+            bspline(fx, fy, w);
+            float sw = 0.0f;
+            for (int b = 0; b < 3; b++)
+                for (int a = 0; a < 3; a++) {
+                    int ci = cidx(s, bx + a, by + b);
+                    V4 q = s->comp[ci];
+                    float wt = w[a].x * w[b].y;
+                    crowd += wt * q.w;
+                    if (q.x > 0.0f) sw += wt;
+                }
+            if (thermal && (p.kind & KIND_FRESH) == 0u) {
+                float dT = 0.0f;
+                for (int b = 0; b < 3; b++)
+                    for (int a = 0; a < 3; a++) dT += w[a].x * w[b].y * s->dheat[cidx(s, bx + a, by + b)].x;
+                int ox = clampi((int)floorf(pos.x), 0, s->W - 1), oy = clampi((int)floorf(pos.y), 0, s->H - 1);
+                V4 own = s->dheat[cidx(s, ox, oy)];
+                if (own.y > 0.0f) {
+                    V4 th = thermal_of(s, row, p.s);
+                    float tb = Mia[1] >= 0 ? mixf(s->mats[Mia[1]].th2[2], s->mats[row].th2[2], p.s) : s->mats[row].th2[2];
+                    I2 q = heat_quanta(th.w, minf(phase_of(p.t, th).x, tb));
+                    dT += own.y * (own.z - (float)q.y / (float)q.x) * T_SCALE;
+                }
+                p.t += dT;
+            }
+            (void)sw;
+        }
+        /* mouse tool (particles.comp:596-631) */
+        int pushed = 0;
+        if (P_.tool_mode != 0) {
+            V2 d = v2(P_.tool_pos[0] - pos.x, P_.tool_pos[1] - pos.y);
+            float r2 = (d.x * d.x + d.y * d.y) / (P_.tool_radius * P_.tool_radius);
+            if (r2 < 1.0f) {
+                if (P_.tool_mode == 2) {
+                    s->particles[id].kind = KIND_DEAD;
+                    return;
+                }
+                float fall = 1.0f - r2;
+                if (P_.tool_mode == 5 || P_.tool_mode == 6) {
+                    if (thermal) {
+                        float e = P_.heat2[1] * fall * dt;
+                        float Cc = thermal_of(s, row, p.s).w;
+                        if (P_.tool_mode == 6) e = minf(e, maxf(phase_of(p.t, thermal_of(s, row, p.s)).x + 150.0f, 0.0f) * Cc);
+                        p.t += (P_.tool_mode == 5 ? e : -e) / Cc;
+                        ledger_add(s, P_.tool_mode == 5 ? 4 : 5, e * P_.inv_ppc);
+                    }
+                } else {
+                    float k = clampf(P_.tool_strength * fall * dt, 0.0f, 1.0f);
+                    if (P_.tool_crowd_max > 0.0f && P_.tool_mode != 4)
+                        k *= clampf((P_.tool_crowd_max - crowd) / (0.25f * P_.tool_crowd_max), 0.0f, 1.0f);
+                    V2 tt = tool_target(s, d);
+                    v = v2(mixf(v.x, tt.x, k), mixf(v.y, tt.y, k));
+                    pushed = 1;
+                }
+            }
+        }
+        /* self-heating (particles.comp:735-739) */
+        if (thermal && s->mats[row].rx[2] > 0.0f) {
+            float e = s->mats[row].rx[2] * s->mats[row].th[0] * (Mia[1] >= 0 ? p.s : 1.0f) * dt * P_.heat[1];
+            p.t += e / thermal_of(s, row, p.s).w;
+            ledger_add(s, 7, e * P_.inv_ppc);
+        }
+        /* speed cap */
+        float vcap = P_.ext[0];
+        {
+            float sp = len2(v);
+            if (sp > vcap) {
+                v.x *= vcap / sp;
+                v.y *= vcap / sp;
+            }
+        }
+        /* advect (particles.comp:847-865) */
+        V2 va = v;
+        if (P_.ext[1] >= 2.0f && !pushed) {
+            V2 xm = v2(clampf(pos.x + 0.5f * dt * (v.x + corr.x + 0.0f), 2.01f, (float)s->W - 2.01f),
+                       clampf(pos.y + 0.5f * dt * (v.y + corr.y + slip), 2.01f, (float)s->H - 2.01f));
+            V2 here = sample_vel(s, pos, v);
+            V2 there = sample_vel(s, xm, here);
+            va = v2(v.x + there.x - here.x, v.y + there.y - here.y);
+            float sp = len2(va);
+            if (sp > vcap) {
+                va.x *= vcap / sp;
+                va.y *= vcap / sp;
+            }
+            if (crowd < LIQUID_THR && (va.x * va.x + va.y * va.y) < 0.01f * (v.x * v.x + v.y * v.y)) v = va;
+        }
+        V2 disp = v2(va.x + corr.x + 0.0f, va.y + corr.y + slip);
+        {
+            float mine = len2(disp);
+            if (crowd < LIQUID_THR) mine /= P_.ext[2];
+            report_umax(&s->S.umax_part, mine);
+        }
+        V2 step_d = v2(dt * disp.x, dt * disp.y);
+        int pieces = clampi((int)ceilf(len2(step_d)), 1, 32);
+        step_d.x /= (float)pieces;
+        step_d.y /= (float)pieces;
+        V2 x = pos;
+        for (int k = 1; k < pieces; k++) {
+            x.x += step_d.x;
+            x.y += step_d.y;
+            collide(s, &x, &v, 1);
+        }
+        x.x += step_d.x;
+        x.y += step_d.y;
+        float excess = clampf(crowd - 1.5f, 0.0f, 1.0f);
+        if (excess > 0.0f && P_.crowd_jitter > 0.0f) {
+            uint32_t hh = hash32(p.id ^ hash32(fbits(pos.x) ^ s->S.substeps));
+            x.x += ((float)(hh & 0xffffu) / 65535.0f - 0.5f) * P_.crowd_jitter * excess;
+            x.y += ((float)(hh >> 16) / 65535.0f - 0.5f) * P_.crowd_jitter * excess;
+        }
+        collide(s, &x, &v, 1);
+        int again = collide(s, &x, &v, 1);
+        if (again) {
+            V2 gg;
+            if (sample_sdf(s, x, &gg) < -1.0f) collide(s, &x, &v, 0);
+        }
+        x.x = clampf(x.x, 2.01f, (float)s->W - 2.01f);
+        x.y = clampf(x.y, 2.01f, (float)s->H - 2.01f);
+        p.pos[0] = x.x;
+        p.pos[1] = x.y;
+        p.vel[0] = v.x;
+        p.vel[1] = v.y;
+        p.c[0] = C.x;
+        p.c[1] = C.y;
+        p.c[2] = C.z;
+        p.c[3] = C.w;
+        p.kind &= ~KIND_FRESH;
+        s->particles[id] = p;
+    }
+    float rho_p = row_density(s, row, p.s);
+    float CT = 0.0f;
+    if (thermal) {
+        V4 th = thermal_of(s, row, p.s);
+        V2 ph = phase_of(p.t, th);
+        float tb = Mia[1] >= 0 ? mixf(s->mats[Mia[1]].th2[2], s->mats[row].th2[2], p.s) : s->mats[row].th2[2];
+        rho_p *= expansion_of(s, row, p.s, ph.x);
+        if (ph.y > 0.0f) {
+            float rs = Mia[1] >= 0 ? mixf(s->mats[Mia[1]].b[3], s->mats[row].b[3], p.s) : s->mats[row].b[3];
+            rho_p = mixf(rho_p, rs, ph.y);
+        }
+        CT = th.w * (minf(ph.x, tb) + 273.15f) / T_SCALE;
+        int hx = clampi((int)floorf(p.pos[0]), 0, s->W - 1), hy = clampi((int)floorf(p.pos[1]), 0, s->H - 1);
+        int hc = cidx(s, hx, hy);
+        I2 q = heat_quanta(th.w, minf(ph.x, tb));
+#pragma omp atomic
+        s->hcell[hc].x += q.x;
+#pragma omp atomic
+        s->hcell[hc].y += q.y;
+    }
+    g->live = 1;
+    g->pos = v2(p.pos[0], p.pos[1]);
+    g->vs = v2(p.vel[0] * s->S.dt, p.vel[1] * s->S.dt);
+    g->Cs = v4(p.c[0] * s->S.dt, p.c[1] * s->S.dt, p.c[2] * s->S.dt, p.c[3] * s->S.dt);
+    g->rho = rho_p;
+    g->sc = p.s;
+    g->CT = CT;
+    g->cw = Mia[2];
+    g->cs = Mia[3];
+    g->ct = thermal ? (int)P_.heat2[2] : -1;
+    g->cg = thermal ? group_heat_chan(s, Mia[0]) : -1;
+}
+
+static inline void acc_add(OSim* s, int x, int y, int ch, int v) {
+#pragma omp atomic
+    s->acc[cidx(s, x, y) * P_.acc_stride + ch] += v;
+}
+
+/* deposit() (particles.comp:1006-1062) */
+static void deposit(OSim* s, const Scat* g) {
+    V2 w[3];
+    {
+        V2 gp = v2(g->pos.x - 0.0f, g->pos.y - 0.5f);
+        int bx = (int)floorf(gp.x - 0.5f), by = (int)floorf(gp.y - 0.5f);
+        float fx = gp.x - (float)bx, fy = gp.y - (float)by;
+        bspline(fx, fy, w);
+        for (int b = 0; b < 3; b++)
+            for (int a = 0; a < 3; a++) {
+                float m = w[a].x * w[b].y * g->rho;
+                V2 d = v2((float)a - fx, (float)b - fy);
+                acc_add(s, bx + a, by + b, 0, (int)floorf(m * MASS_SCALE + 0.5f));
+                acc_add(s, bx + a, by + b, 1, (int)floorf(m * (g->vs.x + (g->Cs.x * d.x + g->Cs.y * d.y)) * MOM_SCALE + 0.5f));
+            }
+    }
+    {
+        V2 gp = v2(g->pos.x - 0.5f, g->pos.y - 0.0f);
+        int bx = (int)floorf(gp.x - 0.5f), by = (int)floorf(gp.y - 0.5f);
+        float fx = gp.x - (float)bx, fy = gp.y - (float)by;
+        bspline(fx, fy, w);
+        for (int b = 0; b < 3; b++)
+            for (int a = 0; a < 3; a++) {
+                float m = w[a].x * w[b].y * g->rho;
+                V2 d = v2((float)a - fx, (float)b - fy);
+                acc_add(s, bx + a, by + b, 2, (int)floorf(m * MASS_SCALE + 0.5f));
+                acc_add(s, bx + a, by + b, 3, (int)floorf(m * (g->vs.y + (g->Cs.z * d.x + g->Cs.w * d.y)) * MOM_SCALE + 0.5f));
+            }
+    }
+    {
+        V2 gp = v2(g->pos.x - 0.5f, g->pos.y - 0.5f);
+        int bx = (int)floorf(gp.x - 0.5f), by = (int)floorf(gp.y - 0.5f);
+        float fx = gp.x - (float)bx, fy = gp.y - (float)by;
+        bspline(fx, fy, w);
+        for (int b = 0; b < 3; b++)
+            for (int a = 0; a < 3; a++) {
+                int nx = bx + a, ny = by + b;
+                int wi = (int)floorf(w[a].x * w[b].y * MASS_SCALE + 0.5f);
+                acc_add(s, nx, ny, 4, wi);
+                if (g->cw >= 0) acc_add(s, nx, ny, g->cw, wi);
+                if (g->cs >= 0 && g->sc > 0.0f) acc_add(s, nx, ny, g->cs, (int)floorf(w[a].x * w[b].y * g->sc * MASS_SCALE + 0.5f));
+                if (g->ct >= 0) {
+                    int hq = (int)floorf(w[a].x * w[b].y * g->CT * MASS_SCALE + 0.5f);
+                    acc_add(s, nx, ny, g->ct, hq);
+                    if (g->cg >= 0) acc_add(s, nx, ny, g->cg, hq);
+                }
+            }
+    }
+}
+
+static void k_particles(OSim* s, int gather) {
+    int n = (int)P_.n_slots;
+#pragma omp parallel for schedule(static) num_threads(g_threads)
+    for (int i = 0; i < n; i++) {
+        Scat g;
+        advance(s, (uint32_t)i, gather, &g);
+        if (g.live) deposit(s, &g);
+    }
+}
+
+/* ------------------------------------------------------------------------------------ */
+/* sort.comp: stable counting sort by cell, dead slots last                              */
+/* ------------------------------------------------------------------------------------ */
+
+void osim_sort(OSim* s) {
+    int ncell = s->W * s->H;
+    uint32_t* count = (uint32_t*)calloc((size_t)ncell + 1, sizeof(uint32_t));
+    uint32_t n = s->n_slots;
+    for (uint32_t i = 0; i < n; i++) {
+        const OParticle* p = &s->particles[i];
+        if (p->kind == KIND_DEAD) continue;
+        int cx = clampi((int)p->pos[0], 0, s->W - 1), cy = clampi((int)p->pos[1], 0, s->H - 1);
+        count[cidx(s, cx, cy)]++;
+    }
+    uint32_t run = 0;
+    for (int c = 0; c < ncell; c++) {
+        uint32_t k = count[c];
+        count[c] = run;
+        run += k;
+    }
+    memset(s->sorted, 0, (size_t)n * sizeof(OParticle));
+    for (uint32_t i = 0; i < n; i++) {
+        const OParticle* p = &s->particles[i];
+        if (p->kind == KIND_DEAD) continue;
+        int cx = clampi((int)p->pos[0], 0, s->W - 1), cy = clampi((int)p->pos[1], 0, s->H - 1);
+        s->sorted[count[cidx(s, cx, cy)]++] = *p;
+    }
+    memcpy(s->particles, s->sorted, (size_t)n * sizeof(OParticle));
+    free(count);
+}
+
+/* ------------------------------------------------------------------------------------ */
+/* grid_prep.comp                                                                        */
+/* ------------------------------------------------------------------------------------ */
+
+static int packed(const OSim* s, int i) {
+    V4 sol = s->solid[i];
+    float phi_f = (float)s->acc[i * P_.acc_stride + 4] / MASS_SCALE * P_.inv_ppc;
+    return sol.w > 0.02f && phi_f > 0.04f && phi_f + sol.z > LIQUID_THR;
+}
+
+static void group_temperatures(const OSim* s, int k, int cw, float Csh, const float Cg[GROUPS], float* T, float Tg[GROUPS]) {
+    for (int g = 0; g < GROUPS; g++) Tg[g] = *T;
+    if (Csh <= 0.0f) return;
+    int Htot = s->acc[k + (int)P_.heat2[2]];
+    *T = (float)Htot * T_SCALE / (Csh * (float)cw) - 273.15f;
+    for (int g = 0; g < GROUPS; g++) Tg[g] = *T;
+    int rest = Htot;
+    int first = -1;
+    for (int g = 0; g < GROUPS; g++) {
+        int ch = group_heat_chan(s, g);
+        if (ch >= 0) {
+            int hh = s->acc[k + ch];
+            rest -= hh;
+            if (Cg[g] > 0.0f) Tg[g] = (float)hh * T_SCALE / (Cg[g] * (float)cw) - 273.15f;
+        } else if (first < 0 && (P_.group_mask & (1u << (uint32_t)g)) != 0u) {
+            first = g;
+        }
+    }
+    if (first >= 0 && Cg[first] > 0.0f) Tg[first] = (float)rest * T_SCALE / (Cg[first] * (float)cw) - 273.15f;
+}
+
+static void k_grid_prep(OSim* s) {
+    int W = s->W, H = s->H;
+    uint32_t region_air = 0;
+#pragma omp parallel for schedule(static) num_threads(g_threads) reduction(| : region_air)
+    for (int cy = 0; cy < H; cy++)
+        for (int cx = 0; cx < W; cx++) {
+            int i = cidx(s, cx, cy);
+            int k = i * P_.acc_stride;
+            int um = s->acc[k], umom = s->acc[k + 1], vm = s->acc[k + 2], vmom = s->acc[k + 3];
+            int cw = s->acc[k + 4];
+            V4 sol = s->solid[i];
+            float dt = s->S.dt;
+            V4 o = v4(0.0f, 0.0f, FACE_EMPTY, FACE_EMPTY);
+            if (sol.x <= 0.0f) o.z = FACE_CLOSED;
+            else if (um >= MIN_FACE_MASS) {
+                o.x = ((float)umom / MOM_SCALE) / ((float)um / MASS_SCALE) / dt;
+                o.z = 0.0f;
+            }
+            if (sol.y <= 0.0f) o.w = FACE_CLOSED;
+            else if (vm >= MIN_FACE_MASS) {
+                o.y = ((float)vmom / MOM_SCALE) / ((float)vm / MASS_SCALE) / dt - P_.gravity * dt;
+                o.w = 0.0f;
+            }
+            s->vel[i] = o;
+            s->vel0[i] = v2(o.x, o.y);
+            float phi_f = (float)cw / MASS_SCALE * P_.inv_ppc;
+            float f[GROUPS] = {0}, rg[GROUPS] = {0}, lg[GROUPS] = {0};
+            float sigma = 0.0f;
+            V2 contact = v2(0.0f, 0.0f);
+            float fam0 = -1.0f;
+            float rho = 0.0f, mu = 0.0f, rho_c = 0.0f, nu_c = 0.0f;
+            int thermal = has_cap(s, CAP_THERMAL);
+            float T = P_.heat[0], kappa = 0.0f, emis = 0.0f, frozen = 0.0f, Craw = 0.0f;
+            int major = 0, top_row = -1;
+            float top_share = 0.0f;
+            if (cw > 0) {
+                int others = 0;
+                for (int j = 0; j < P_.n_present; j++) {
+                    int ch = s->mats[P_.present[j]].ia[2];
+                    if (ch >= 0) others += s->acc[k + ch];
+                }
+                float sh[MAX_PRESENT], scn[MAX_PRESENT];
+                float Csh = 0.0f;
+                float Cg[GROUPS] = {0};
+                for (int j = 0; j < P_.n_present; j++) {
+                    sh[j] = 0.0f;
+                    scn[j] = 1.0f;
+                    int r = P_.present[j];
+                    const int* ia = s->mats[r].ia;
+                    if (ia[2] < 0 && P_.primary >= 0 && r != P_.primary) continue;
+                    int wgt = ia[2] >= 0 ? s->acc[k + ia[2]] : maxi(cw - others, 0);
+                    if (wgt <= 0) continue;
+                    sh[j] = wgt >= cw ? 1.0f : clampf((float)wgt / (float)cw, 0.0f, 1.0f);
+                    if (ia[1] >= 0 && ia[3] >= 0) scn[j] = clampf((float)s->acc[k + ia[3]] / (float)wgt, 0.0f, 1.0f);
+                    if (thermal) {
+                        float cr = sh[j] * thermal_of(s, (uint32_t)r, scn[j]).w;
+                        Csh += cr;
+                        Cg[ia[0]] += cr;
+                        float kp = s->mats[r].th[1];
+                        kappa += sh[j] * (ia[1] >= 0 ? mixf(s->mats[ia[1]].th[1], kp, scn[j]) : kp);
+                        float em = s->mats[r].th2[1];
+                        emis += sh[j] * (ia[1] >= 0 ? mixf(s->mats[ia[1]].th2[1], em, scn[j]) : em);
+                    }
+                }
+                float Tg[GROUPS];
+                group_temperatures(s, k, cw, thermal ? Csh : 0.0f, Cg, &T, Tg);
+                for (int j = 0; j < P_.n_present; j++) {
+                    float share = sh[j];
+                    if (share <= 0.0f) continue;
+                    int r = P_.present[j];
+                    const int* ia = s->mats[r].ia;
+                    float sc = scn[j];
+                    const float* ma = s->mats[r].a;
+                    float rho_m = ma[0], lnu = ma[1], sig = ma[2];
+                    float Tm = Tg[ia[0]];
+                    if (thermal) lnu += temp_law(s, r, Tm);
+                    float xp = thermal ? expansion_of(s, (uint32_t)r, sc, Tm) : 1.0f;
+                    V2 csv = v2(s->mats[r].b[0], s->mats[r].b[1]);
+                    if (ia[1] >= 0) {
+                        const float* da = s->mats[ia[1]].a;
+                        rho_m = mixf(da[0], rho_m, sc);
+                        lnu = mixf(thermal ? da[1] + temp_law(s, ia[1], Tm) : da[1], lnu, sc);
+                        sig = mixf(da[2], sig, sc);
+                        csv = v2(mixf(s->mats[ia[1]].b[0], csv.x, sc), mixf(s->mats[ia[1]].b[1], csv.y, sc));
+                        if (s->mats[r].ib[0] == 0) fam0 = sc;
+                    }
+                    rho_m *= xp;
+                    if (thermal) {
+                        V4 th = thermal_of(s, (uint32_t)r, sc);
+                        float fs = th.y > -1e8f ? clampf((th.y - Tm) / maxf(th.y - th.x, 1e-3f), 0.0f, 1.0f) : 0.0f;
+                        if (fs > 0.0f) {
+                            lnu = mixf(lnu, maxf(lnu, P_.heat2[0]), fs);
+                            float rs = s->mats[r].b[3];
+                            rho_m = mixf(rho_m, ia[1] >= 0 ? mixf(s->mats[ia[1]].b[3], rs, sc) : rs, fs);
+                            frozen += share * fs;
+                        }
+                    }
+                    if (r != 57 && share > top_share) {
+                        top_share = share;
+                        top_row = r;
+                    }
+                    int g = ia[0];
+                    f[g] += share;
+                    rg[g] += share * rho_m;
+                    lg[g] += share * lnu;
+                    sigma += share * sig;
+                    contact.x += share * csv.x;
+                    contact.y += share * csv.y;
+                }
+                for (int g = 0; g < GROUPS; g++) {
+                    if (f[g] <= 0.0f) continue;
+                    rho += rg[g];
+                    mu += rg[g] * o_expf(lg[g] / f[g]);
+                    if (f[g] > f[major]) major = g;
+                }
+                if (f[major] > 0.0f) {
+                    rho_c = rg[major] / f[major];
+                    nu_c = o_expf(lg[major] / f[major]);
+                }
+                Craw = Csh * (float)cw / MASS_SCALE;
+            }
+            float phi_t = phi_f + sol.z;
+            int has = phi_f > 0.04f && sol.w > 0.02f;
+            float level = has ? phi_t - LIQUID_THR : -LIQUID_THR;
+            if (has && level <= 0.0f && cx > 0 && cy > 0 && cx < W - 1 && cy < H - 1) {
+                if ((packed(s, i - 1) && packed(s, i + 1)) || (packed(s, i - W) && packed(s, i + W))) level = 0.05f;
+                else if (P_.gravity > 0.0f && phi_t > 0.25f && packed(s, i - W)) level = 0.05f;
+            }
+            if (sol.w > 0.0f && level <= 0.0f) region_air |= 1u << (s->region[i] & REGION_MASK);
+            s->cell[i] = v4(phi_f, rho, mu, level);
+            s->comp[i] = v4(rho, f[1], fam0, phi_t);
+            if ((P_.group_mask & (P_.group_mask - 1u)) != 0u) {
+                s->aux[i] = v4(nu_c, rho_c, f[2], f[3]);
+                s->grho[i] = v4(rg[0], rg[1], rg[2], rg[3]);
+            }
+            s->sprop[i] = v4(sigma, contact.x, contact.y, (float)major + (float)(top_row + 1) / 128.0f);
+            if (thermal) {
+                s->therm[i] = v4(T, Craw, kappa, frozen);
+                s->dheat[i] = v4(P_.heat[1] > 0.0f ? emis : 0.0f, 0.0f, 0.0f, 0.0f);
+            }
+            if (level <= 0.0f) s->pres[i] = v2(0.0f, 0.0f);
+        }
+    s->region_air |= region_air;
+}
+
+/* ------------------------------------------------------------------------------------ */
+/* grid_coef.comp, surf_smooth.comp, surf_curv.comp, surf_apply.comp                      */
+/* ------------------------------------------------------------------------------------ */
+
+static void coef_face(V4 a, V4 b, float open, float* g, float* rho) {
+    float wsum = a.x + b.x;
+    *rho = wsum > 1e-6f ? (a.x * a.y + b.x * b.y) / wsum : 1.0f;
+    *g = 0.0f;
+    int fa = a.w > 0.0f, fb = b.w > 0.0f;
+    if (open <= 0.0f || !(fa || fb)) return;
+    float theta = 1.0f;
+    if (fa != fb) {
+        float lf = fa ? a.w : b.w;
+        float la = fa ? b.w : a.w;
+        theta = clampf(lf / (lf - la), THETA_MIN, 1.0f);
+    }
+    *g = 1.0f / (maxf(*rho, 0.05f) * theta);
+}
+
+static void k_grid_coef(OSim* s) {
+#pragma omp parallel for schedule(static) num_threads(g_threads)
+    for (int cy = 0; cy < s->H; cy++)
+        for (int cx = 0; cx < s->W; cx++) {
+            int i = cidx(s, cx, cy);
+            V4 o = v4(0.0f, 0.0f, 1.0f, 1.0f);
+            if (cx > 0 && cy > 0) {
+                V4 me = s->cell[i];
+                V4 sol = s->solid[i];
+                coef_face(me, s->cell[i - 1], sol.x, &o.x, &o.z);
+                coef_face(me, s->cell[i - s->W], sol.y, &o.y, &o.w);
+            }
+            s->coef[i] = o;
+        }
+}
+
+static void k_surf_smooth(OSim* s) {
+    static const float B5[5] = {1.0f, 4.0f, 6.0f, 4.0f, 1.0f};
+    int more = (P_.group_mask & 12u) != 0u;
+#pragma omp parallel for schedule(static) num_threads(g_threads)
+    for (int cy = 0; cy < s->H; cy++)
+        for (int cx = 0; cx < s->W; cx++) {
+            V2 sum = v2(0, 0), sum2 = v2(0, 0);
+            float wsum = 0.0f;
+            for (int b = -2; b <= 2; b++)
+                for (int a = -2; a <= 2; a++) {
+                    int nx = cx + a, ny = cy + b;
+                    if (nx < 0 || ny < 0 || nx >= s->W || ny >= s->H) continue;
+                    int j = cidx(s, nx, ny);
+                    float open = s->solid[j].w;
+                    if (open <= 0.02f) continue;
+                    float phi = clampf(s->cell[j].x / (REST_PHI * open), 0.0f, 1.0f);
+                    float w = B5[a + 2] * B5[b + 2];
+                    sum.x += w * phi;
+                    sum.y += w * (phi * s->comp[j].y);
+                    if (more) {
+                        sum2.x += w * phi * s->aux[j].z;
+                        sum2.y += w * phi * s->aux[j].w;
+                    }
+                    wsum += w;
+                }
+            int i = cidx(s, cx, cy);
+            s->surf[i].x = wsum > 0.0f ? sum.x / wsum : 0.0f;
+            s->surf[i].y = wsum > 0.0f ? sum.y / wsum : 0.0f;
+            if (more) {
+                s->surf2[i].x = wsum > 0.0f ? sum2.x / wsum : 0.0f;
+                s->surf2[i].y = wsum > 0.0f ? sum2.y / wsum : 0.0f;
+            }
+        }
+}
+
+static float surf_field(const OSim* s, int x, int y, int k) {
+    x = clampi(x, 0, s->W - 1);
+    y = clampi(y, 0, s->H - 1);
+    int i = cidx(s, x, y);
+    if (k < 2) return k == 0 ? s->surf[i].x : s->surf[i].y;
+    return k == 2 ? s->surf2[i].x : s->surf2[i].y;
+}
+
+static V2 grad_node(const OSim* s, int nx, int ny, int k) {
+    float a = surf_field(s, nx, ny, k), b = surf_field(s, nx - 1, ny, k), d = surf_field(s, nx, ny - 1, k), e = surf_field(s, nx - 1, ny - 1, k);
+    return v2(0.5f * (a + d - b - e), 0.5f * (a + b - d - e));
+}
+
+static float node_sdf(const OSim* s, int x, int y) {
+    x = clampi(x, 0, s->W);
+    y = clampi(y, 0, s->H);
+    return s->sdf[y * (s->W + 1) + x];
+}
+
+static V2 contact_at(const OSim* s, int nx, int ny) {
+    int i0 = cidx(s, clampi(nx, 0, s->W - 1), clampi(ny, 0, s->H - 1));
+    V2 cs = v2(s->sprop[i0].y, s->sprop[i0].z);
+    if (cs.x * cs.x + cs.y * cs.y > 1e-12f) {
+        float l = len2(cs);
+        return v2(cs.x / l, cs.y / l);
+    }
+    for (int b = -3; b <= 2; b++)
+        for (int a = -3; a <= 2; a++) {
+            int j = cidx(s, clampi(nx + a, 0, s->W - 1), clampi(ny + b, 0, s->H - 1));
+            cs.x += s->sprop[j].y * s->cell[j].x;
+            cs.y += s->sprop[j].z * s->cell[j].x;
+        }
+    if (cs.x * cs.x + cs.y * cs.y > 1e-12f) {
+        float l = len2(cs);
+        return v2(cs.x / l, cs.y / l);
+    }
+    return v2(0.0f, 1.0f);
+}
+
+static V2 normal_node(const OSim* s, int nx, int ny, int k, float* mag) {
+    const float G_MIN = 0.05f, WALL_BAND = 0.5f;
+    V2 g = grad_node(s, nx, ny, k);
+    *mag = len2(g);
+    if (*mag < G_MIN) return v2(0.0f, 0.0f);
+    V2 nn = v2(-g.x / *mag, -g.y / *mag);
+    if (k == 0) {
+        float d = node_sdf(s, nx, ny);
+        if (d < WALL_BAND) {
+            V2 gw = v2(node_sdf(s, nx + 1, ny) - node_sdf(s, nx - 1, ny), node_sdf(s, nx, ny + 1) - node_sdf(s, nx, ny - 1));
+            if (len2(gw) > 1e-4f) {
+                float lw = len2(gw);
+                V2 nw = v2(gw.x / lw, gw.y / lw);
+                float gd = g.x * nw.x + g.y * nw.y;
+                V2 gt = v2(g.x - gd * nw.x, g.y - gd * nw.y);
+                float along = len2(gt);
+                if (along > 0.5f * G_MIN) {
+                    V2 t = v2(-gt.x / along, -gt.y / along);
+                    V2 cs = contact_at(s, nx, ny);
+                    V2 nc = v2(cs.x * nw.x + cs.y * t.x, cs.x * nw.y + cs.y * t.y);
+                    float sm = smoothstepf(0.5f * G_MIN, G_MIN, along);
+                    V2 m = v2(mixf(nn.x, nc.x, sm), mixf(nn.y, nc.y, sm));
+                    float lm = len2(m);
+                    nn = lm > 1e-4f ? v2(m.x / lm, m.y / lm) : nc;
+                }
+            }
+        }
+    }
+    return nn;
+}
+
+static float curvature_at(const OSim* s, int cx, int cy, int k, float kmax) {
+    float m00, m10, m01, m11;
+    V2 n00 = normal_node(s, cx, cy, k, &m00);
+    V2 n10 = normal_node(s, cx + 1, cy, k, &m10);
+    V2 n01 = normal_node(s, cx, cy + 1, k, &m01);
+    V2 n11 = normal_node(s, cx + 1, cy + 1, k, &m11);
+    if (0.25f * (m00 + m10 + m01 + m11) < 0.05f) return 0.0f;
+    float kap = 0.5f * (n10.x + n11.x - n00.x - n01.x) + 0.5f * (n01.y + n11.y - n00.y - n10.y);
+    return kmax > 0.0f ? clampf(kap, -kmax, kmax) : kap;
+}
+
+static void k_surf_curv(OSim* s) {
+    float kmax = P_.misc[0];
+#pragma omp parallel for schedule(static) num_threads(g_threads)
+    for (int cy = 0; cy < s->H; cy++)
+        for (int cx = 0; cx < s->W; cx++) {
+            int i = cidx(s, cx, cy);
+            float k0 = curvature_at(s, cx, cy, 0, kmax);
+            float k1 = curvature_at(s, cx, cy, 1, kmax);
+            s->surf[i].z = k0;
+            s->surf[i].w = k1;
+            if ((P_.group_mask & 12u) != 0u) {
+                s->surf2[i].z = (P_.group_mask & 4u) != 0u ? curvature_at(s, cx, cy, 2, kmax) : 0.0f;
+                s->surf2[i].w = (P_.group_mask & 8u) != 0u ? curvature_at(s, cx, cy, 3, kmax) : 0.0f;
+            }
+        }
+}
+
+static float air_jump(const OSim* s, int a, int b) {
+    int la = s->cell[a].w > 0.0f;
+    int liq = la ? a : b, air = la ? b : a;
+    float lf = s->cell[liq].w, lgv = s->cell[air].w;
+    float theta = clampf(lf / (lf - lgv), THETA_MIN, 1.0f);
+    float kl = s->surf[liq].z, kg = s->surf[air].z;
+    float kap = kg != 0.0f ? mixf(kl, kg, theta) : kl;
+    return s->S.dt * s->sprop[liq].x * kap;
+}
+
+static float share_of(const OSim* s, int i, int g) {
+    if (g == 1) return s->comp[i].y;
+    if (g == 2) return s->aux[i].z;
+    if (g == 3) return s->aux[i].w;
+    return 1.0f - s->comp[i].y - s->aux[i].z - s->aux[i].w;
+}
+
+static float curv_of(const OSim* s, int i, int g) { return g == 1 ? s->surf[i].w : g == 2 ? s->surf2[i].z : s->surf2[i].w; }
+
+static float pair_jump(const OSim* s, int c, int n) {
+    int gc = (int)s->sprop[c].w, gn = (int)s->sprop[n].w;
+    if (gc == gn) return 0.0f;
+    int hi = maxi(gc, gn), lo = mini(gc, gn);
+    float dc = share_of(s, c, hi) - share_of(s, c, lo), dn = share_of(s, n, hi) - share_of(s, n, lo);
+    if (dc * dn >= 0.0f) return 0.0f;
+    float theta = -dn / (dc - dn);
+    float kc = curv_of(s, c, hi), kn = curv_of(s, n, hi);
+    float kap = kc == 0.0f ? kn : kn == 0.0f ? kc : mixf(kn, kc, theta);
+    float j = s->S.dt * P_.pair[hi][lo] * kap;
+    return gc == hi ? j : -j;
+}
+
+static float face_jump(const OSim* s, int c, int n, float open) {
+    if (open <= 0.0f) return 0.0f;
+    int lc = s->cell[c].w > 0.0f, ln = s->cell[n].w > 0.0f;
+    if (lc != ln) return air_jump(s, c, n);
+    if (lc && ln) return pair_jump(s, c, n);
+    return 0.0f;
+}
+
+static void k_surf_apply(OSim* s) {
+#pragma omp parallel for schedule(static) num_threads(g_threads)
+    for (int cy = 0; cy < s->H; cy++)
+        for (int cx = 0; cx < s->W; cx++) {
+            int i = cidx(s, cx, cy);
+            V2 pj = v2(0.0f, 0.0f);
+            if (cx > 0 && cy > 0) {
+                V4 sol = s->solid[i];
+                pj.x = face_jump(s, i, i - 1, sol.x);
+                pj.y = face_jump(s, i, i - s->W, sol.y);
+            }
+            s->pjump[i] = pj;
+        }
+}
+
+/* ------------------------------------------------------------------------------------ */
+/* heat.comp                                                                             */
+/* ------------------------------------------------------------------------------------ */
+
+static float y_sat(float T) {
+    T = clampf(T, -40.0f, 99.0f);
+    float p = 0.61078f * o_expf(17.27f * T / (T + 237.3f));
+    return 0.622f * p / (101.325f - 0.378f * p);
+}
+
+static V2 centre_vel(const OSim* s, int i) {
+    int last = s->W * s->H - 1;
+    V4 v = s->vel[i], vr = s->vel[mini(i + 1, last)], vt = s->vel[mini(i + s->W, last)];
+    V2 a = v2(face_live(v.z) ? v.x : 0.0f, face_live(v.w) ? v.y : 0.0f);
+    V2 b = v2(face_live(vr.z) ? vr.x : 0.0f, face_live(vt.w) ? vt.y : 0.0f);
+    return v2(0.5f * (a.x + b.x), 0.5f * (a.y + b.y));
+}
+
+static int lead_of(float w) { float f = w - floorf(w); return (int)(f * 128.0f + 0.5f); }
+
+static void k_heat(OSim* s) {
+    /* dheat is rewritten in place (dheat.x holds the emissivity on entry), so read it first */
+    int W = s->W, H = s->H;
+    V4* out = (V4*)malloc((size_t)W * H * sizeof(V4));
+    float air_tot_pos = 0, air_tot_neg = 0;
+    (void)air_tot_pos; (void)air_tot_neg;
+#pragma omp parallel for schedule(static) num_threads(g_threads)
+    for (int cy = 0; cy < H; cy++)
+        for (int cx = 0; cx < W; cx++) {
+            int i = cidx(s, cx, cy);
+            V4 me = s->therm[i];
+            float emis = s->dheat[i].x;
+            float phi = s->cell[i].x;
+            float k = s->S.dt * P_.heat[1];
+            I2 hsum = s->hcell[i];
+            V2 own = v2(0.0f, 0.0f);
+            if (hsum.x > 0 && me.y > 0.0f && phi > 0.0f) {
+                float rate = 5.78f * me.z * 3.14159265f / (P_.inv_ppc * me.y * P_.inv_ppc / phi);
+                own = v2(1.0f - o_expf(-k * rate), (float)hsum.y / (float)hsum.x);
+            }
+            if (phi <= 0.04f || me.y <= 0.0f || cx < 1 || cy < 1 || cx >= W - 1 || cy >= H - 1) {
+                out[i] = v4(0.0f, own.x, own.y, 0.0f);
+                continue;
+            }
+            phi = minf(phi, 1.0f);
+            int nb[4] = {i - 1, i + 1, i - W, i + W};
+            float open[4] = {s->solid[i].x, s->solid[i + 1].x, s->solid[i].y, s->solid[i + W].y};
+            float Tk = me.x + 273.15f, Ta = P_.heat[0] + 273.15f;
+            float cond = 0.0f, air = 0.0f, wall = 0.0f, contact = 0.0f;
+            float cpc = me.y * P_.inv_ppc;
+            float hc = P_.heat2[3];
+            int lead = lead_of(s->sprop[i].w);
+            float eddy_l2 = P_.heat3[0] * P_.heat3[0] / 0.85f;
+            int eddy = eddy_l2 > 0.0f && me.w < 0.5f;
+            V2 u_me = eddy ? centre_vel(s, i) : v2(0.0f, 0.0f);
+            float eddy_max = 0.2f / maxf(k, 1e-9f);
+            float per_rate = 1.0f / maxf(P_.heat[1], 1e-6f);
+            float evap = 0.0f;
+            for (int q = 0; q < 4; q++) {
+                int n = nb[q];
+                float a = open[q];
+                float pn = s->cell[n].x;
+                V4 o = s->therm[n];
+                if (a > 0.0f) {
+                    float pl = (pn > 0.04f && o.y > 0.0f) ? minf(pn, 1.0f) : 0.0f;
+                    if (pl > 0.0f) {
+                        float gc = 2.0f * me.z * o.z / maxf(me.z + o.z, 1e-12f);
+                        if (eddy && o.w < 0.5f && lead_of(s->sprop[n].w) == lead) {
+                            V2 cn = centre_vel(s, n);
+                            float strain = 1.4142f * len2(v2(cn.x - u_me.x, cn.y - u_me.y));
+                            float alpha = minf(eddy_l2 * strain * per_rate, eddy_max);
+                            float c1 = cpc / phi, c2 = o.y * P_.inv_ppc / pl;
+                            gc += alpha * 2.0f * c1 * c2 / maxf(c1 + c2, 1e-12f);
+                        }
+                        cond += a * minf(phi, pl) * gc * (o.x - me.x);
+                        if (hc > 0.0f && lead_of(s->sprop[n].w) != lead) {
+                            float g1 = maxf(2.0f * me.z, hc), g2 = maxf(2.0f * o.z, hc);
+                            float gx = maxf(g1 * g2 / (g1 + g2) - gc, 0.0f) * a * minf(phi, pl);
+                            float cn = o.y * P_.inv_ppc;
+                            float x = gx * k * (1.0f / cpc + 1.0f / cn);
+                            contact += 0.25f * (1.0f - o_expf(-4.0f * x)) * cpc * cn / (cpc + cn) * (o.x - me.x);
+                        }
+                    }
+                    float exposed = maxf(phi - pl, 0.0f);
+                    if (exposed > 0.0f && s->solid[n].w > 0.02f) {
+                        float hh = P_.heat[2] + emis * P_.heat[3] * (Ta * Ta + Tk * Tk) * (Ta + Tk);
+                        air += a * exposed * hh * (P_.heat[0] - me.x);
+                        if (P_.heat3[1] > 0.0f && lead > 0 && s->mats[lead - 1].ia[0] == 0 && s->mats[lead - 1].th2[2] < 150.0f && me.w < 0.5f)
+                            evap += a * exposed * P_.heat[2] * P_.heat3[1] * maxf(y_sat(me.x) - y_sat(P_.heat[0]), 0.0f);
+                    }
+                }
+                if (a < 1.0f) {
+                    float ts = maxf(s->solid_t[n], s->solid_t[i]);
+                    if (ts > 0.5f * NO_TEMP) wall += (1.0f - a) * phi * 2.0f * me.z * (ts - me.x);
+                }
+            }
+            if (evap > 0.0f) air -= evap;
+            air *= k;
+            wall *= k;
+            float lim = cpc * fabsf(P_.heat[0] - me.x);
+            air = clampf(air, -lim, lim);
+            float e = k * cond + contact + air + wall;
+            out[i] = v4(e / cpc, own.x, own.y, 0.0f);
+            if (air > 0.0f) ledger_add(s, 0, air); else ledger_add(s, 1, -air);
+            if (wall > 0.0f) ledger_add(s, 2, wall); else ledger_add(s, 3, -wall);
+        }
+    memcpy(s->dheat, out, (size_t)W * H * sizeof(V4));
+    free(out);
+}
+
+/* ------------------------------------------------------------------------------------ */
+/* Explicit viscosity: visc.glsl, visc_setup.comp, visc_apply.comp mode 2                 */
+/* ------------------------------------------------------------------------------------ */
+
+static inline int live_u(const OSim* s, int i) { return face_live(s->vel[i].z); }
+static inline int live_v(const OSim* s, int i) { return face_live(s->vel[i].w); }
+static inline int closed_u(const OSim* s, int i) { return face_closed(s->vel[i].z); }
+static inline int closed_v(const OSim* s, int i) { return face_closed(s->vel[i].w); }
+static inline float vel_u(const OSim* s, int i) { return live_u(s, i) ? s->vel[i].x : 0.0f; }
+static inline float vel_v(const OSim* s, int i) { return live_v(s, i) ? s->vel[i].y : 0.0f; }
+
+static V4 strain_of_vel(const OSim* s, int i, V2 w) {
+    int W = s->W;
+    V4 o = v4(0, 0, 0, 0);
+    if (w.x > 0.0f) {
+        o.x = w.x * (vel_u(s, i + 1) - vel_u(s, i));
+        o.y = w.x * (vel_v(s, i + W) - vel_v(s, i));
+    }
+    if (w.y > 0.0f) {
+        float ua = vel_u(s, i), ub = vel_u(s, i - W), va = vel_v(s, i), vb = vel_v(s, i - 1);
+        if (closed_u(s, i) && live_u(s, i - W)) ua = -ub;
+        if (closed_u(s, i - W) && live_u(s, i)) ub = -ua;
+        if (closed_v(s, i) && live_v(s, i - 1)) va = -vb;
+        if (closed_v(s, i - 1) && live_v(s, i)) vb = -va;
+        o.z = w.y * 0.5f * ((ua - ub) + (va - vb));
+    }
+    return o;
+}
+
+static inline int ok_u(const OSim* s, int i) { return live_u(s, i) || closed_u(s, i); }
+static inline int ok_v(const OSim* s, int i) { return live_v(s, i) || closed_v(s, i); }
+
+static void k_visc_setup(OSim* s) {
+    int W = s->W, H = s->H;
+    float dt = s->S.dt;
+#pragma omp parallel for schedule(static) num_threads(g_threads)
+    for (int cy = 0; cy < H; cy++)
+        for (int cx = 0; cx < W; cx++) {
+            int i = cidx(s, cx, cy);
+            float wc = 0.0f, wn = 0.0f;
+            if (cx >= 1 && cy >= 1 && cx < W - 1 && cy < H - 1) {
+                V4 me = s->cell[i];
+                if (me.w > 0.0f && ok_u(s, i) && ok_u(s, i + 1) && ok_v(s, i) && ok_v(s, i + W)) wc = 2.0f * dt * me.z;
+                int cs[4] = {i - W - 1, i - W, i - 1, i};
+                int nliq = 0, any_air = 0;
+                float mu = 0.0f;
+                for (int k = 0; k < 4; k++) {
+                    V4 q = s->cell[cs[k]];
+                    if (q.w > 0.0f) {
+                        nliq++;
+                        mu += q.z;
+                    } else if (s->solid[cs[k]].w > 0.02f) {
+                        any_air = 1;
+                    }
+                }
+                if (nliq > 0 && !any_air && ok_u(s, i) && ok_u(s, i - W) && ok_v(s, i) && ok_v(s, i - 1))
+                    wn = 4.0f * dt * (mu / (float)nliq) * ((float)nliq / 4.0f);
+            }
+            s->vw[i].x = wc;
+            s->vw[i].y = wn;
+        }
+#pragma omp parallel for schedule(static) num_threads(g_threads)
+    for (int i = 0; i < W * H; i++) s->vs[i] = strain_of_vel(s, i, v2(s->vw[i].x, s->vw[i].y));
+}
+
+static V2 gts(const OSim* s, int i) {
+    int W = s->W;
+    V2 g = v2(0.0f, 0.0f);
+    if (live_u(s, i)) {
+        float c1 = closed_u(s, i - W) ? 1.0f : 0.5f, c2 = closed_u(s, i + W) ? -1.0f : -0.5f;
+        g.x = s->vs[i - 1].x - s->vs[i].x + s->vs[i].z * c1 + s->vs[i + W].z * c2;
+    }
+    if (live_v(s, i)) {
+        float d1 = closed_v(s, i - 1) ? 1.0f : 0.5f, d2 = closed_v(s, i + 1) ? -1.0f : -0.5f;
+        g.y = s->vs[i - W].y - s->vs[i].y + s->vs[i].z * d1 + s->vs[i + 1].z * d2;
+    }
+    return g;
+}
+
+static void k_visc_apply_explicit(OSim* s) {
+    int W = s->W, H = s->H;
+#pragma omp parallel for schedule(static) num_threads(g_threads)
+    for (int cy = 1; cy < H - 1; cy++)
+        for (int cx = 1; cx < W - 1; cx++) {
+            int i = cidx(s, cx, cy);
+            V2 g = gts(s, i);
+            int lu = live_u(s, i), lv = live_v(s, i);
+            V4 cf = s->coef[i];
+            V4 v = s->vel[i];
+            if (lu) v.x -= g.x / cf.z;
+            if (lv) v.y -= g.y / cf.w;
+            s->vel[i].x = v.x;
+            s->vel[i].y = v.y;
+        }
+}
+
+/* ------------------------------------------------------------------------------------ */
+/* rhs.comp                                                                              */
+/* ------------------------------------------------------------------------------------ */
+
+static void k_rhs(OSim* s) {
+    int W = s->W, H = s->H;
+    int tw = (W + 15) / 16;
+    float dt = s->S.dt;
+    float gain = P_.corr_gain;
+#pragma omp parallel for schedule(static) num_threads(g_threads)
+    for (int cy = 0; cy < H; cy++)
+        for (int cx = 0; cx < W; cx++) {
+            int i = cidx(s, cx, cy);
+            V4 me = s->cell[i];
+            if (me.w <= 0.0f || cx == 0 || cy == 0 || cx == W - 1 || cy == H - 1) {
+                s->mga[i] = v4(0, 0, 0, 0);
+                s->mgd[i] = 0.0f;
+                s->prhs[i] = v4(0, 0, 0, 0);
+                continue;
+            }
+            V4 sol = s->solid[i];
+            V4 cf = s->coef[i];
+            float aL = sol.x, aB = sol.y, aR = s->solid[i + 1].x, aT = s->solid[i + W].y;
+            V4 w = v4(aL * cf.x, aR * s->coef[i + 1].x, aB * cf.y, aT * s->coef[i + W].y);
+            float diag = w.x + w.y + w.z + w.w;
+            {
+                uint32_t rg = s->region[i];
+                if ((rg & REGION_VENT) != 0u && (s->region_air & (1u << (rg & REGION_MASK))) == 0u && P_.misc[1] > 0.0f)
+                    diag += 1.0f / maxf(me.y, 0.05f);
+            }
+            V4 vme = s->vel[i];
+            float div = aR * s->vel[i + 1].x - aL * vme.x + aT * s->vel[i + W].y - aB * vme.y;
+            int lL = s->cell[i - 1].w > 0.0f, lR = s->cell[i + 1].w > 0.0f, lB = s->cell[i - W].w > 0.0f, lT = s->cell[i + W].w > 0.0f;
+            (void)lL; (void)lB;
+            float jump = w.x * s->pjump[i].x + w.y * (lR ? -s->pjump[i + 1].x : s->pjump[i + 1].x)
+                       + w.z * s->pjump[i].y + w.w * (lT ? -s->pjump[i + W].y : s->pjump[i + W].y);
+            float err = clampf(s->comp[i].w - REST_PHI, -0.5f, 0.5f);
+            {
+                int interior = (aL <= 0.0f || s->cell[i - 1].w > 0.0f) && (aR <= 0.0f || s->cell[i + 1].w > 0.0f)
+                            && (aB <= 0.0f || s->cell[i - W].w > 0.0f) && (aT <= 0.0f || s->cell[i + W].w > 0.0f);
+                int pressed = s->pres[i].x * (dt / s->S.dt_prev) > 0.5f * me.y * P_.gravity * dt;
+                if (interior && !pressed) err = maxf(err - P_.corr[1], 0.0f);
+                else if (!interior && err < 0.0f) err = 0.0f;
+            }
+            float sv = gain * err;
+            if ((s->region_air & (1u << (s->region[i] & REGION_MASK))) == 0u && P_.misc[1] > 0.0f) sv = 0.0f;
+            if (diag > 1e-9f) {
+                int t = (cy >> 4) * tw + (cx >> 4);
+                s->ptile[t] = 1u;
+            }
+            s->mga[i] = diag > 1e-9f ? w : v4(0, 0, 0, 0);
+            s->mgd[i] = diag > 1e-9f ? diag : 0.0f;
+            s->prhs[i] = v4(-div + jump, sv / dt, 0.0f, 0.0f);
+        }
+}
+
+/* ------------------------------------------------------------------------------------ */
+/* Pressure MGPCG: mg_build, mg_tail, mg_down, mg_up, cg_*, reduce_tail                   */
+/* ------------------------------------------------------------------------------------ */
+
+static inline float wcomp(V4 w, int k) { return k == 0 ? w.x : k == 1 ? w.y : k == 2 ? w.z : w.w; }
+static const int NBX[4] = {-1, 1, 0, 0}, NBY[4] = {0, 0, -1, 1};
+
+typedef struct Lv { int off, w, h, toff; } Lv;
+static Lv lev(const OSim* s, int l) { Lv r = {s->lv.offs[l], s->lv.dims[l][0], s->lv.dims[l][1], s->lv.tile_offs[l]}; return r; }
+static inline int l_inside(Lv L, int x, int y) { return x >= 0 && y >= 0 && x < L.w && y < L.h; }
+static inline int l_at(Lv L, int x, int y) { return L.off + y * L.w + x; }
+static inline int l_unknown(const OSim* s, Lv L, int x, int y) { return l_inside(L, x, y) && s->mgd[l_at(L, x, y)] > 0.0f; }
+
+/* mg_build.comp: level l+1 from level l, tile by tile of level l+1 */
+static void k_mg_build(OSim* s, int l) {
+    Lv F = lev(s, l), C = lev(s, l + 1);
+    int tfx = (F.w + 15) >> 4, tfy = (F.h + 15) >> 4;
+    int tcx = (C.w + 15) >> 4, tcy = (C.h + 15) >> 4;
+    for (int ty = 0; ty < tcy; ty++)
+        for (int tx = 0; tx < tcx; tx++) {
+            uint32_t on = 0;
+            for (int k = 0; k < 4; k++) {
+                int fx = 2 * tx + (k & 1), fy = 2 * ty + (k >> 1);
+                if (fx < tfx && fy < tfy) on |= s->ptile[F.toff + fy * tfx + fx];
+            }
+            uint32_t slot = (uint32_t)C.toff + (uint32_t)(ty * tcx + tx);
+            uint32_t was = s->ptile[slot];
+            s->ptile[slot] = on != 0u ? 1u : 0u;
+            uint32_t state = (on != 0u ? 1u : 0u) | (was != 0u ? 2u : 0u);
+            if (state == 0u) continue;
+            for (int ly = 0; ly < 16; ly++)
+                for (int lx = 0; lx < 16; lx++) {
+                    int Cx = tx * 16 + lx, Cy = ty * 16 + ly;
+                    if (Cx >= C.w || Cy >= C.h) continue;
+                    int o = l_at(C, Cx, Cy);
+                    if ((state & 1u) == 0u) {
+                        s->mgd[o] = 0.0f;
+                        s->mga[o] = v4(0, 0, 0, 0);
+                        continue;
+                    }
+                    float D = 0.0f;
+                    V4 A = v4(0, 0, 0, 0);
+                    for (int k = 0; k < 4; k++) {
+                        int cx = 2 * Cx + (k & 1), cy = 2 * Cy + (k >> 1);
+                        if (!l_unknown(s, F, cx, cy)) continue;
+                        int i = l_at(F, cx, cy);
+                        D += s->mgd[i];
+                        V4 w = s->mga[i];
+                        for (int d = 0; d < 4; d++) {
+                            int nx = cx + NBX[d], ny = cy + NBY[d];
+                            if (!l_unknown(s, F, nx, ny)) continue;
+                            float wd = wcomp(w, d);
+                            if ((nx >> 1) == Cx && (ny >> 1) == Cy) D -= wd;
+                            else if (d == 0) A.x += wd;
+                            else if (d == 1) A.y += wd;
+                            else if (d == 2) A.z += wd;
+                            else A.w += wd;
+                        }
+                    }
+                    s->mgd[o] = D > 1e-7f ? D : 0.0f;
+                    s->mga[o] = D > 1e-7f ? A : v4(0, 0, 0, 0);
+                }
+        }
+}
+
+/* mg_tail.comp mode 1: Galerkin matrices of the tail levels */
+static void k_tail_build(OSim* s) {
+    for (int l = s->lv.tail; l < s->lv.n - 1; l++) {
+        Lv F = lev(s, l), C = lev(s, l + 1);
+        for (int t = 0; t < C.w * C.h; t++) {
+            int ccx = t % C.w, ccy = t / C.w;
+            float D = 0.0f;
+            V4 A = v4(0, 0, 0, 0);
+            for (int k = 0; k < 4; k++) {
+                int cx = 2 * ccx + (k & 1), cy = 2 * ccy + (k >> 1);
+                if (!l_unknown(s, F, cx, cy)) continue;
+                int i = l_at(F, cx, cy);
+                D += s->mgd[i];
+                V4 w = s->mga[i];
+                for (int d = 0; d < 4; d++) {
+                    int nx = cx + NBX[d], ny = cy + NBY[d];
+                    if (!l_unknown(s, F, nx, ny)) continue;
+                    float wd = wcomp(w, d);
+                    if ((nx >> 1) == ccx && (ny >> 1) == ccy) D -= wd;
+                    else if (d == 0) A.x += wd;
+                    else if (d == 1) A.y += wd;
+                    else if (d == 2) A.z += wd;
+                    else A.w += wd;
+                }
+            }
+            int o = C.off + t;
+            s->mgd[o] = D > 1e-7f ? D : 0.0f;
+            s->mga[o] = D > 1e-7f ? A : v4(0, 0, 0, 0);
+        }
+    }
+}
+
+static inline int tile_on(const OSim* s, Lv L, int tx, int ty) {
+    int tw = (L.w + 15) >> 4;
+    return s->ptile[L.toff + ty * tw + tx] != 0u;
+}
+
+/* mg_down.comp black(): value of black cell n after the half-sweep from zero */
+static V2 down_black(const OSim* s, Lv L, int nx, int ny) {
+    int i = l_at(L, nx, ny);
+    V4 w = s->mga[i];
+    V2 sum = s->mgr[i];
+    for (int d = 0; d < 4; d++) {
+        int mx = nx + NBX[d], my = ny + NBY[d];
+        if (!l_unknown(s, L, mx, my)) continue;
+        int j = l_at(L, mx, my);
+        float wd = wcomp(w, d);
+        sum.x += wd * s->mgr[j].x / s->mgd[j];
+        sum.y += wd * s->mgr[j].y / s->mgd[j];
+    }
+    return v2(sum.x / s->mgd[i], sum.y / s->mgd[i]);
+}
+
+static void k_mg_down(OSim* s, int l) {
+    Lv F = lev(s, l), C = lev(s, l + 1);
+    int tw = (F.w + 15) >> 4, th = (F.h + 15) >> 4;
+    for (int ty = 0; ty < th; ty++)
+        for (int tx = 0; tx < tw; tx++) {
+            if (!tile_on(s, F, tx, ty)) continue;
+            V2 sz[256];
+            for (int ly = 0; ly < 16; ly++)
+                for (int lx = 0; lx < 16; lx++) {
+                    int cx = tx * 16 + lx, cy = ty * 16 + ly;
+                    int red = ((cx + cy) & 1) == 0;
+                    int unk = l_unknown(s, F, cx, cy);
+                    V2 z = v2(0, 0);
+                    if (l_inside(F, cx, cy)) {
+                        int i = l_at(F, cx, cy);
+                        if (unk) z = red ? v2(s->mgr[i].x / s->mgd[i], s->mgr[i].y / s->mgd[i]) : down_black(s, F, cx, cy);
+                        s->mgx[i] = z;
+                    }
+                    sz[ly * 16 + lx] = z;
+                }
+            for (int ly = 0; ly < 16; ly += 2)
+                for (int lx = 0; lx < 16; lx += 2) {
+                    int cx = tx * 16 + lx, cy = ty * 16 + ly;
+                    int Cx = cx >> 1, Cy = cy >> 1;
+                    if (Cx >= C.w || Cy >= C.h) continue;
+                    V2 sum = v2(0, 0);
+                    for (int k = 0; k < 2; k++) {
+                        int qx = cx + k, qy = cy + k;
+                        if (!l_unknown(s, F, qx, qy)) continue;
+                        V4 w = s->mga[l_at(F, qx, qy)];
+                        int lqx = lx + k, lqy = ly + k;
+                        for (int d = 0; d < 4; d++) {
+                            int nx = qx + NBX[d], ny = qy + NBY[d];
+                            if (!l_unknown(s, F, nx, ny)) continue;
+                            int lnx = lqx + NBX[d], lny = lqy + NBY[d];
+                            int here = lnx >= 0 && lny >= 0 && lnx < 16 && lny < 16;
+                            V2 zb = here ? sz[lny * 16 + lnx] : down_black(s, F, nx, ny);
+                            float wd = wcomp(w, d);
+                            sum.x += wd * zb.x;
+                            sum.y += wd * zb.y;
+                        }
+                    }
+                    s->mgr[l_at(C, Cx, Cy)] = sum;
+                }
+        }
+}
+
+/* mg_up.comp black(): new value of black cell n after the coarse correction */
+static V2 up_black(const OSim* s, Lv L, Lv C, int nx, int ny) {
+    int i = l_at(L, nx, ny);
+    V4 w = s->mga[i];
+    V2 sum = s->mgr[i];
+    for (int d = 0; d < 4; d++) {
+        int mx = nx + NBX[d], my = ny + NBY[d];
+        if (!l_unknown(s, L, mx, my)) continue;
+        V2 xm = s->mgx[l_at(L, mx, my)];
+        V2 zc = s->mgz[l_at(C, mx >> 1, my >> 1)];
+        float wd = wcomp(w, d);
+        sum.x += wd * (xm.x + MG_OMEGA * zc.x);
+        sum.y += wd * (xm.y + MG_OMEGA * zc.y);
+    }
+    return v2(sum.x / s->mgd[i], sum.y / s->mgd[i]);
+}
+
+/* work-group sum of reduce.glsl:230-239: the tree over 256 invocations */
+static V4 group_tree(V4 buf[256]) {
+    for (int st = 128; st > 0; st >>= 1)
+        for (int t = 0; t < st; t++) {
+            buf[t].x += buf[t + st].x;
+            buf[t].y += buf[t + st].y;
+            buf[t].z += buf[t + st].z;
+            buf[t].w += buf[t + st].w;
+        }
+    return buf[0];
+}
+
+/* mg_up on level l; on level 0 (flag) writes part[slot] = (r.z, r.r) sums */
+static void k_mg_up(OSim* s, int l, int flag) {
+    Lv F = lev(s, l), C = lev(s, l + 1);
+    int tw = (F.w + 15) >> 4, th = (F.h + 15) >> 4;
+    for (int ty = 0; ty < th; ty++)
+        for (int tx = 0; tx < tw; tx++) {
+            int slot = ty * tw + tx;
+            if (!tile_on(s, F, tx, ty)) {
+                if (flag) s->part[slot] = v4(0, 0, 0, 0);
+                continue;
+            }
+            V2 sz[256];
+            V4 accb[256];
+            for (int ly = 0; ly < 16; ly++)
+                for (int lx = 0; lx < 16; lx++) {
+                    int cx = tx * 16 + lx, cy = ty * 16 + ly;
+                    int red = ((cx + cy) & 1) == 0;
+                    V2 z = v2(0, 0);
+                    if (l_unknown(s, F, cx, cy) && !red) z = up_black(s, F, C, cx, cy);
+                    sz[ly * 16 + lx] = z;
+                }
+            for (int ly = 0; ly < 16; ly++)
+                for (int lx = 0; lx < 16; lx++) {
+                    int cx = tx * 16 + lx, cy = ty * 16 + ly;
+                    int red = ((cx + cy) & 1) == 0;
+                    V2 z = sz[ly * 16 + lx];
+                    V4 a4 = v4(0, 0, 0, 0);
+                    if (l_inside(F, cx, cy)) {
+                        int i = l_at(F, cx, cy);
+                        if (l_unknown(s, F, cx, cy)) {
+                            V2 r = s->mgr[i];
+                            if (red) {
+                                V4 w = s->mga[i];
+                                V2 sum = r;
+                                for (int d = 0; d < 4; d++) {
+                                    int nx = cx + NBX[d], ny = cy + NBY[d];
+                                    if (!l_unknown(s, F, nx, ny)) continue;
+                                    int lnx = lx + NBX[d], lny = ly + NBY[d];
+                                    int here = lnx >= 0 && lny >= 0 && lnx < 16 && lny < 16;
+                                    V2 zb = here ? sz[lny * 16 + lnx] : up_black(s, F, C, nx, ny);
+                                    float wd = wcomp(w, d);
+                                    sum.x += wd * zb.x;
+                                    sum.y += wd * zb.y;
+                                }
+                                z = v2(sum.x / s->mgd[i], sum.y / s->mgd[i]);
+                            }
+                            a4 = v4(r.x * z.x, r.y * z.y, r.x * r.x, r.y * r.y);
+                        }
+                        s->mgz[i] = z;
+                    }
+                    accb[ly * 16 + lx] = a4;
+                }
+            if (flag) s->part[slot] = group_tree(accb);
+        }
+}
+
+/* mg_tail.comp mode 0: the V-cycle on the tail levels, rhs in mgr[first], result in mgz[first] */
+static void k_tail_vcycle(OSim* s) {
+    int first = s->lv.tail, last = s->lv.n - 1;
+    Lv Fst = lev(s, first);
+    int base = Fst.off;
+    Lv E = lev(s, last);
+    int total = E.off + E.w * E.h - base;
+    int nf = Fst.w * Fst.h;
+    V2* sx = (V2*)calloc((size_t)total, sizeof(V2));
+    float* sd = (float*)malloc((size_t)total * sizeof(float));
+    V2* sr = (V2*)calloc((size_t)(total > nf ? total - nf : 1), sizeof(V2));
+    for (int t = 0; t < total; t++) sd[t] = s->mgd[base + t];
+#define RHS_AT(sl) ((sl) < nf ? s->mgr[base + (sl)] : sr[(sl) - nf])
+#define SAT(L, x, y) ((L).off - base + (y) * (L).w + (x))
+#define SUNK(L, x, y) (l_inside((L), (x), (y)) && sd[SAT((L), (x), (y))] > 0.0f)
+    /* A half-sweep reads only cells of the other colour (5-point stencil), so the loop
+     * order within it does not change the result. */
+#define SWEEP(L, colour, zero)                                                                 \
+    do {                                                                                      \
+        for (int t = 0; t < (L).w * (L).h; t++) {                                             \
+            int x = t % (L).w, y = t / (L).w;                                                 \
+            int sl = (L).off - base + t;                                                      \
+            float D = sd[sl];                                                                 \
+            if (D <= 0.0f) { if (zero) sx[sl] = v2(0, 0); continue; }                         \
+            if (((x + y) & 1) != (colour)) { if (zero) sx[sl] = v2(0, 0); continue; }         \
+            V2 sum = RHS_AT(sl);                                                              \
+            if (!(zero)) {                                                                    \
+                V4 w = s->mga[base + sl];                                                     \
+                for (int d = 0; d < 4; d++) {                                                 \
+                    int nx = x + NBX[d], ny = y + NBY[d];                                     \
+                    if (SUNK(L, nx, ny)) {                                                    \
+                        float wd = wcomp(w, d);                                               \
+                        V2 xn = sx[SAT(L, nx, ny)];                                           \
+                        sum.x += wd * xn.x;                                                   \
+                        sum.y += wd * xn.y;                                                   \
+                    }                                                                         \
+                }                                                                             \
+            }                                                                                 \
+            sx[sl] = v2(sum.x / D, sum.y / D);                                                \
+        }                                                                                     \
+    } while (0)
+    for (int l = first; l < last; l++) {
+        Lv L = lev(s, l), C = lev(s, l + 1);
+        SWEEP(L, 0, 1);
+        SWEEP(L, 1, 0);
+        for (int t = 0; t < C.w * C.h; t++) {
+            int ccx = t % C.w, ccy = t / C.w;
+            V2 sum = v2(0, 0);
+            for (int k = 0; k < 4; k++) {
+                int cx = 2 * ccx + (k & 1), cy = 2 * ccy + (k >> 1);
+                if (!SUNK(L, cx, cy)) continue;
+                int sl = SAT(L, cx, cy);
+                V4 w = s->mga[base + sl];
+                V2 az = v2(sd[sl] * sx[sl].x, sd[sl] * sx[sl].y);
+                for (int d = 0; d < 4; d++) {
+                    int nx = cx + NBX[d], ny = cy + NBY[d];
+                    if (SUNK(L, nx, ny)) {
+                        float wd = wcomp(w, d);
+                        V2 xn = sx[SAT(L, nx, ny)];
+                        az.x -= wd * xn.x;
+                        az.y -= wd * xn.y;
+                    }
+                }
+                V2 rh = RHS_AT(sl);
+                sum.x += rh.x - az.x;
+                sum.y += rh.y - az.y;
+            }
+            sr[C.off - base + t - nf] = sum;
+        }
+    }
+    {
+        Lv L = lev(s, last);
+        SWEEP(L, 0, 1);
+        for (int st = 1; st < 9; st++) SWEEP(L, st & 1, 0);
+    }
+    for (int l = last - 1; l >= first; l--) {
+        Lv F = lev(s, l), C = lev(s, l + 1);
+        for (int t = 0; t < F.w * F.h; t++) {
+            int x = t % F.w, y = t / F.w;
+            if (((x + y) & 1) == 0) continue;
+            int sl = F.off - base + t;
+            float D = sd[sl];
+            if (D <= 0.0f) continue;
+            V4 w = s->mga[base + sl];
+            V2 sum = RHS_AT(sl);
+            for (int d = 0; d < 4; d++) {
+                int nx = x + NBX[d], ny = y + NBY[d];
+                if (!SUNK(F, nx, ny)) continue;
+                float wd = wcomp(w, d);
+                V2 xn = sx[SAT(F, nx, ny)];
+                V2 xc = sx[SAT(C, nx >> 1, ny >> 1)];
+                sum.x += wd * (xn.x + MG_OMEGA * xc.x);
+                sum.y += wd * (xn.y + MG_OMEGA * xc.y);
+            }
+            sx[sl] = v2(sum.x / D, sum.y / D);
+        }
+        SWEEP(F, 0, 0);
+    }
+    for (int t = 0; t < nf; t++) s->mgz[base + t] = sx[t];
+#undef SWEEP
+#undef SUNK
+#undef SAT
+#undef RHS_AT
+    free(sx);
+    free(sd);
+    free(sr);
+}
+
+static void vcycle(OSim* s) {
+    for (int l = 0; l < s->lv.tail; l++) k_mg_down(s, l);
+    k_tail_vcycle(s);
+    for (int l = s->lv.tail - 1; l >= 0; l--) k_mg_up(s, l, l == 0);
+}
+
+/* reduce_tail.glsl:268-281: sum of n partials starting at base, in the shader's order */
+static V4 total(const OSim* s, int base, int n) {
+    V4 buf[256];
+    for (int t = 0; t < 256; t++) {
+        V4 a = v4(0, 0, 0, 0);
+        for (int k = t; k < n; k += 256) {
+            a.x += s->part[base + k].x;
+            a.y += s->part[base + k].y;
+            a.z += s->part[base + k].z;
+            a.w += s->part[base + k].w;
+        }
+        buf[t] = a;
+    }
+    return group_tree(buf);
+}
+
+static void k_cg_scale(OSim* s, int mode) {
+    Lv F = lev(s, 0);
+    float ratio = s->S.dt / s->S.dt_prev;
+    for (int cy = 0; cy < F.h; cy++)
+        for (int cx = 0; cx < F.w; cx++) {
+            if (!tile_on(s, F, cx >> 4, cy >> 4)) continue;
+            int i = l_at(F, cx, cy);
+            if (s->mgd[i] > 0.0f) {
+                float p = s->pres[i].x;
+                if (mode == 1) p -= s->p2keep[i];
+                else s->p2keep[i] = 0.0f;
+                s->pres[i].x = p * ratio;
+            } else {
+                s->pres[i] = v2(0, 0);
+            }
+        }
+}
+
+static void k_cg_init(OSim* s) {
+    Lv F = lev(s, 0);
+    int tw = (F.w + 15) >> 4, th = (F.h + 15) >> 4;
+    int n = s->nwg;
+    for (int ty = 0; ty < th; ty++)
+        for (int tx = 0; tx < tw; tx++) {
+            int slot = ty * tw + tx;
+            if (!tile_on(s, F, tx, ty)) {
+                s->part[n + slot] = v4(0, 0, 0, 0);
+                continue;
+            }
+            V4 accb[256];
+            for (int ly = 0; ly < 16; ly++)
+                for (int lx = 0; lx < 16; lx++) {
+                    int cx = tx * 16 + lx, cy = ty * 16 + ly;
+                    V4 a4 = v4(0, 0, 0, 0);
+                    if (l_inside(F, cx, cy)) {
+                        int i = l_at(F, cx, cy);
+                        float D = s->mgd[i];
+                        if (D > 0.0f) {
+                            V2 x = s->pres[i];
+                            V4 w = s->mga[i];
+                            V2 ax = v2(D * x.x, D * x.y);
+                            for (int d = 0; d < 4; d++) {
+                                int nx = cx + NBX[d], ny = cy + NBY[d];
+                                if (l_unknown(s, F, nx, ny)) {
+                                    float wd = wcomp(w, d);
+                                    V2 pn = s->pres[l_at(F, nx, ny)];
+                                    ax.x -= wd * pn.x;
+                                    ax.y -= wd * pn.y;
+                                }
+                            }
+                            V2 b = v2(s->prhs[i].x, s->prhs[i].y);
+                            s->mgr[i] = v2(b.x - ax.x, b.y - ax.y);
+                            a4 = v4(b.x * b.x, b.y * b.y, 0.0f, 0.0f);
+                        } else {
+                            s->mgr[i] = v2(0, 0);
+                        }
+                    }
+                    accb[ly * 16 + lx] = a4;
+                }
+            s->part[n + slot] = group_tree(accb);
+        }
+}
+
+static V2 cg_direction(const OSim* s, const V2* cgp, int i) {
+    V2 z = s->mgz[i];
+    const float* b = s->K.p_beta;
+    if (b[0] == 0.0f && b[1] == 0.0f) return z;
+    V2 po = cgp[i];
+    return v2(b[0] != 0.0f ? z.x + b[0] * po.x : z.x, b[1] != 0.0f ? z.y + b[1] * po.y : z.y);
+}
+
+static void k_cg_apply(OSim* s, const V2* cgp, V2* cgp2) {
+    Lv F = lev(s, 0);
+    int tw = (F.w + 15) >> 4, th = (F.h + 15) >> 4;
+    int n = s->nwg;
+    for (int ty = 0; ty < th; ty++)
+        for (int tx = 0; tx < tw; tx++) {
+            int slot = ty * tw + tx;
+            if (!tile_on(s, F, tx, ty)) {
+                s->part[n + slot] = v4(0, 0, 0, 0);
+                continue;
+            }
+            V4 accb[256];
+            for (int ly = 0; ly < 16; ly++)
+                for (int lx = 0; lx < 16; lx++) {
+                    int cx = tx * 16 + lx, cy = ty * 16 + ly;
+                    V4 a4 = v4(0, 0, 0, 0);
+                    if (l_inside(F, cx, cy)) {
+                        int i = l_at(F, cx, cy);
+                        float D = s->mgd[i];
+                        if (D > 0.0f) {
+                            V2 p = cg_direction(s, cgp, i);
+                            V4 w = s->mga[i];
+                            V2 q = v2(D * p.x, D * p.y);
+                            for (int d = 0; d < 4; d++) {
+                                int nx = cx + NBX[d], ny = cy + NBY[d];
+                                if (l_unknown(s, F, nx, ny)) {
+                                    V2 pn = cg_direction(s, cgp, l_at(F, nx, ny));
+                                    float wd = wcomp(w, d);
+                                    q.x -= wd * pn.x;
+                                    q.y -= wd * pn.y;
+                                }
+                            }
+                            cgp2[i] = p;
+                            s->cgq[i] = q;
+                            a4 = v4(0.0f, 0.0f, p.x * q.x, p.y * q.y);
+                        } else {
+                            cgp2[i] = v2(0, 0);
+                        }
+                    }
+                    accb[ly * 16 + lx] = a4;
+                }
+            s->part[n + slot] = group_tree(accb);
+        }
+}
+
+static void k_cg_update(OSim* s, const V2* cgp2) {
+    Lv F = lev(s, 0);
+    const float* a = s->K.p_alpha;
+    for (int cy = 0; cy < F.h; cy++)
+        for (int cx = 0; cx < F.w; cx++) {
+            if (!tile_on(s, F, cx >> 4, cy >> 4)) continue;
+            int i = l_at(F, cx, cy);
+            if (s->mgd[i] <= 0.0f) continue;
+            s->pres[i].x += a[0] * cgp2[i].x;
+            s->pres[i].y += a[1] * cgp2[i].y;
+            s->mgr[i].x -= a[0] * s->cgq[i].x;
+            s->mgr[i].y -= a[1] * s->cgq[i].y;
+        }
+}
+
+/* reduce_tail.glsl:299-355, the pressure modes */
+static void reduce_start(OSim* s, int mode) {
+    int n = s->nwg;
+    V4 a = total(s, 0, n), b = total(s, n, n);
+    SolveBuf* K = &s->K;
+    K->p_bb[0] = b.x;
+    K->p_bb[1] = b.y;
+    K->p_rz[0] = a.x;
+    K->p_rz[1] = a.y;
+    K->p_rr[0] = a.z;
+    K->p_rr[1] = a.w;
+    K->p_beta[0] = K->p_beta[1] = 0.0f;
+    K->p_alpha[0] = K->p_alpha[1] = 0.0f;
+    K->p_iters[0] = K->p_iters[1] = 0u;
+    float tx = P_.tol[0], ty = P_.tol[1];
+    K->p_done[0] = a.z <= tx * tx * b.x;
+    K->p_done[1] = a.w <= ty * ty * b.y;
+    if (mode == 8) K->p_done[1] = 1u;
+    K->solves += 1u;
+}
+
+static void reduce_alpha(OSim* s) {
+    int n = s->nwg;
+    V4 b = total(s, n, n);
+    SolveBuf* K = &s->K;
+    float ax = 0.0f, ay = 0.0f;
+    if (K->p_done[0] == 0u && b.z > 0.0f) ax = K->p_rz[0] / b.z;
+    if (K->p_done[1] == 0u && b.w > 0.0f) ay = K->p_rz[1] / b.w;
+    K->p_alpha[0] = ax;
+    K->p_alpha[1] = ay;
+}
+
+static void reduce_beta(OSim* s) {
+    int n = s->nwg;
+    V4 a = total(s, 0, n);
+    SolveBuf* K = &s->K;
+    uint32_t was0 = K->p_done[0], was1 = K->p_done[1];
+    K->p_iters[0] += 1u - was0;
+    K->p_iters[1] += 1u - was1;
+    float tx = P_.tol[0], ty = P_.tol[1];
+    uint32_t now0 = a.z <= tx * tx * K->p_bb[0], now1 = a.w <= ty * ty * K->p_bb[1];
+    uint32_t d0 = was0 > now0 ? was0 : now0, d1 = was1 > now1 ? was1 : now1;
+    float bx = 0.0f, by = 0.0f;
+    if (d0 == 0u && K->p_rz[0] > 0.0f) bx = a.x / K->p_rz[0];
+    if (d1 == 0u && K->p_rz[1] > 0.0f) by = a.y / K->p_rz[1];
+    K->p_beta[0] = bx;
+    K->p_beta[1] = by;
+    K->p_rz[0] = a.x;
+    K->p_rz[1] = a.y;
+    K->p_rr[0] = mixf(a.z, K->p_rr[0], (float)was0);
+    K->p_rr[1] = mixf(a.w, K->p_rr[1], (float)was1);
+    K->p_done[0] = d0;
+    K->p_done[1] = d1;
+}
+
+static void reduce_end(OSim* s, int mode) {
+    SolveBuf* K = &s->K;
+    if (mode == 3) {
+        uint32_t m = K->p_iters[0] > K->p_iters[1] ? K->p_iters[0] : K->p_iters[1];
+        if (m > K->p_it_max) K->p_it_max = m;
+        if (K->p_done[0] == 0u) K->p_unconv += 1u;
+    } else {
+        if (K->p_iters[0] > K->p2_it_max) K->p2_it_max = K->p_iters[0];
+        if (K->p_done[0] == 0u) K->p2_unconv += 1u;
+    }
+    float rel = K->p_bb[0] > 0.0f ? sqrtf(K->p_rr[0] / K->p_bb[0]) : 0.0f;
+    K->p_res_max = maxf(K->p_res_max, rel);
+}
+
+/* record_pressure + record_cg (mod.rs:2956-3010) with the device-decided loop: the
+ * iterations run until both potentials are done or pressure_max_iters have run. */
+static void pressure_solve(OSim* s, int second) {
+    if (!second) {
+        for (int l = 1; l <= s->lv.tail; l++) k_mg_build(s, l - 1);
+        if (s->lv.tail < s->lv.n - 1) k_tail_build(s);
+        int warm = s->visc_mode == 2 && s->prm.viscous_projection != 0 && s->prm.viscous_warm != 0;
+        k_cg_scale(s, warm ? 1 : 0);
+    }
+    k_cg_init(s);
+    vcycle(s);
+    reduce_start(s, second ? 8 : 0);
+    V2* pa = s->cgp;
+    V2* pb = s->cgp2;
+    for (uint32_t k = 0; k < s->prm.pressure_max_iters; k++) {
+        if (s->K.p_done[0] && s->K.p_done[1]) break;
+        k_cg_apply(s, pa, pb);
+        reduce_alpha(s);
+        k_cg_update(s, pb);
+        vcycle(s);
+        reduce_beta(s);
+        V2* t = pa;
+        pa = pb;
+        pb = t;
+    }
+    reduce_end(s, second ? 9 : 3);
+}
+
+/* ------------------------------------------------------------------------------------ */
+/* project.comp                                                                          */
+/* ------------------------------------------------------------------------------------ */
+
+static float p_difference(int lc, int ln, float pc, float pn, float j) {
+    if (lc && ln) return pc - pn - j;
+    return (lc ? pc : j) - (ln ? pn : j);
+}
+
+static void k_project(OSim* s) {
+    int W = s->W;
+    float m_all = 0.0f;
+    for (int cy = 1; cy < s->H; cy++)
+        for (int cx = 1; cx < W; cx++) {
+            int i = cidx(s, cx, cy);
+            V4 cf = s->coef[i];
+            V4 me = s->vel[i];
+            if (s->mgd[i] > 0.0f) s->prhs[i].z = s->pres[i].x;
+            if (cf.x != 0.0f || cf.y != 0.0f) {
+                V2 p = s->pres[i];
+                int liq = s->cell[i].w > 0.0f;
+                if (face_live(me.z) && cf.x != 0.0f) {
+                    int n = i - 1;
+                    me.x -= cf.x * p_difference(liq, s->cell[n].w > 0.0f, p.x, s->pres[n].x, s->pjump[i].x);
+                    me.z = -cf.x * (p.y - s->pres[n].y);
+                }
+                if (face_live(me.w) && cf.y != 0.0f) {
+                    int n = i - W;
+                    me.y -= cf.y * p_difference(liq, s->cell[n].w > 0.0f, p.x, s->pres[n].x, s->pjump[i].y);
+                    me.w = -cf.y * (p.y - s->pres[n].y);
+                }
+                s->vel[i] = me;
+            }
+            float m = 0.0f;
+            if (face_live(me.z) && cf.x != 0.0f) m = fabsf(me.x);
+            if (face_live(me.w) && cf.y != 0.0f) m = maxf(m, fabsf(me.y));
+            if (m > m_all) m_all = m;
+        }
+    if (m_all > bitsf(s->S.umax_grid)) s->S.umax_grid = fbits(m_all);
+}
+
+/* ------------------------------------------------------------------------------------ */
+/* The substep (record_substep, mod.rs:2615-2708)                                         */
+/* ------------------------------------------------------------------------------------ */
+
+static void substep(OSim* s, int gather) {
+    k_step(s);
+    /* The per-substep gain of the density correction (rhs.comp:79) depends only on dt. */
+    P_.corr_gain = minf(1.0f - o_expf(-s->S.dt / P_.tol[3]), P_.density_k);
+    memset(s->acc, 0, (size_t)s->W * s->H * P_.acc_stride * sizeof(int32_t));
+    if (s->thermal) memset(s->hcell, 0, (size_t)s->W * s->H * sizeof(I2));
+    k_particles(s, gather);
+    k_grid_prep(s);
+    k_grid_coef(s);
+    k_surf_smooth(s);
+    k_surf_curv(s);
+    k_surf_apply(s);
+    if (s->thermal && s->prm.heat_rate > 0.0f) k_heat(s);
+    if (s->visc_mode == 1) {
+        k_visc_setup(s);
+        k_visc_apply_explicit(s);
+    }
+    memset(s->ptile, 0, (size_t)s->nwg * sizeof(uint32_t));
+    k_rhs(s);
+    pressure_solve(s, 0);
+    k_project(s);
+}
+
+/* ------------------------------------------------------------------------------------ */
+/* API                                                                                   */
+/* ------------------------------------------------------------------------------------ */
+
+#define ALLOC(ptr, n) do { (ptr) = calloc((size_t)(n), sizeof(*(ptr))); } while (0)
+
+OSim* osim_create(int w, int h, uint32_t capacity, const OSimParams* p) {
+    if (w < 16 || h < 16) return NULL;
+    OSim* s = (OSim*)calloc(1, sizeof(OSim));
+    s->W = w;
+    s->H = h;
+    s->capacity = capacity;
+    s->prm = *p;
+    levels_new(&s->lv, w, h);
+    s->nwg = ((w + 15) / 16) * ((h + 15) / 16);
+    size_t nc = (size_t)w * h;
+    ALLOC(s->particles, capacity);
+    ALLOC(s->sorted, capacity);
+    ALLOC(s->acc, nc * ACC_MAX);
+    ALLOC(s->vel, nc); ALLOC(s->cell, nc); ALLOC(s->comp, nc); ALLOC(s->coef, nc);
+    ALLOC(s->sprop, nc); ALLOC(s->surf, nc); ALLOC(s->surf2, nc); ALLOC(s->aux, nc);
+    ALLOC(s->grho, nc); ALLOC(s->therm, nc); ALLOC(s->dheat, nc); ALLOC(s->vw, nc);
+    ALLOC(s->vs, nc); ALLOC(s->prhs, nc); ALLOC(s->vel0, nc); ALLOC(s->pjump, nc);
+    ALLOC(s->pres, nc); ALLOC(s->p2keep, nc); ALLOC(s->hcell, nc); ALLOC(s->solid, nc);
+    ALLOC(s->sdf, (size_t)(w + 1) * (h + 1)); ALLOC(s->region, nc); ALLOC(s->solid_t, nc);
+    ALLOC(s->mga, s->lv.total); ALLOC(s->mgd, s->lv.total); ALLOC(s->mgx, s->lv.total);
+    ALLOC(s->mgz, s->lv.total); ALLOC(s->mgr, s->lv.total);
+    ALLOC(s->cgp, nc); ALLOC(s->cgp2, nc); ALLOC(s->cgq, nc);
+    ALLOC(s->ptile, s->lv.tiles);
+    ALLOC(s->part, 2 * s->nwg);
+    for (size_t k = 0; k < nc; k++) s->solid_t[k] = NO_TEMP;
+    return s;
+}
+
+void osim_destroy(OSim* s) {
+    if (!s) return;
+    void* ptrs[] = {s->particles, s->sorted, s->acc, s->vel, s->cell, s->comp, s->coef, s->sprop,
+                    s->surf, s->surf2, s->aux, s->grho, s->therm, s->dheat, s->vw, s->vs, s->prhs,
+                    s->vel0, s->pjump, s->pres, s->p2keep, s->hcell, s->solid, s->sdf, s->region,
+                    s->solid_t, s->mga, s->mgd, s->mgx, s->mgz, s->mgr, s->cgp, s->cgp2, s->cgq,
+                    s->ptile, s->part};
+    for (size_t k = 0; k < sizeof ptrs / sizeof ptrs[0]; k++) free(ptrs[k]);
+    free(s);
+}
+
+int osim_set_params(OSim* s, const OSimParams* p) {
+    s->prm = *p;
+    return 0;
+}
+
+int osim_set_solids(OSim* s, const float* sdf, const float* solid4, const uint32_t* region, const float* temp) {
+    size_t nc = (size_t)s->W * s->H;
+    memcpy(s->sdf, sdf, (size_t)(s->W + 1) * (s->H + 1) * sizeof(float));
+    memcpy(s->solid, solid4, nc * sizeof(V4));
+    memcpy(s->region, region, nc * sizeof(uint32_t));
+    s->solids_heated = temp != NULL;
+    for (size_t k = 0; k < nc; k++) s->solid_t[k] = temp ? temp[k] : NO_TEMP;
+    return 0;
+}
+
+static float melting_lat(const OMat* d) { return freezes(d) ? d->latent / d->heat_capacity : 0.0f; }
+
+/* SimParams::enthalpy_temp (params.rs:848-860) with melting (params.rs:830-845) */
+static float enthalpy_temp(const OSimParams* p, int row, float sc, float t) {
+    const OMat* own = &p->mat[row];
+    float lo, hi, l;
+    if (own->diluent < 0) {
+        lo = own->melt_lo;
+        hi = maxf(own->melt_hi, own->melt_lo + 0.25f);
+        l = melting_lat(own);
+    } else {
+        const OMat* d = &p->mat[own->diluent];
+        float shift = own->freeze_shift * sc;
+        float cd = d->density * d->heat_capacity, co = own->density * own->heat_capacity;
+        float c = cd + (co - cd) * sc;
+        l = (cd * melting_lat(d) + (co * own->latent / own->heat_capacity - cd * melting_lat(d)) * sc) / c;
+        lo = d->melt_lo + shift;
+        hi = maxf(d->melt_hi, d->melt_lo + 0.25f) + shift;
+    }
+    if (lo < -273.0f || t >= hi) return t;
+    if (t <= lo) return t - l;
+    float fr = (t - lo) / maxf(hi - lo, 1e-3f);
+    return (lo - l) + fr * (hi - lo + l);
+}
+
+int osim_reset(OSim* s, const OParticle* in, uint32_t n) {
+    if (n > s->capacity) n = s->capacity;
+    const OSimParams* p = &s->prm;
+    /* reset: ids, settle_spawn (params.rs:71-88) */
+    for (uint32_t k = 0; k < n; k++) {
+        OParticle q = in[k];
+        q.id = k;
+        if (!isfinite(q.pos[0]) || !isfinite(q.pos[1])) return -1;
+        q.pos[0] = minf(maxf(q.pos[0], 2.01f), (float)s->W - 2.01f);
+        q.pos[1] = minf(maxf(q.pos[1], 2.01f), (float)s->H - 2.01f);
+        uint32_t mat = (q.kind & 255u);
+        if (mat != 0u && q.kind != KIND_DEAD) {
+            const OMat* def = &p->mat[mat - 1u];
+            if (q.t == SPAWN_TEMP) {
+                q.t = def->spawn_temp;
+                q.kind |= KIND_REAL_T;
+            }
+            if (q.s == SPAWN_S) q.s = def->diluent >= 0 ? clampf(def->load, 0.0f, 1.0f) : 1.0f;
+            if (q.kind & KIND_REAL_T) {
+                q.kind &= ~KIND_REAL_T;
+                q.t = enthalpy_temp(p, (int)mat - 1, q.s, q.t);
+            }
+        }
+        s->particles[k] = q;
+    }
+    s->n_slots = n;
+    /* the tank: rows present (note_materials), thermal from heated solids or temperatures */
+    int present[O_MAX_MATERIALS] = {0};
+    int thermal = s->solids_heated;
+    for (uint32_t k = 0; k < n; k++) {
+        uint32_t m = s->particles[k].kind & 255u;
+        if (m == 0u || s->particles[k].kind == KIND_DEAD) continue;
+        present[m - 1u] = 1;
+        thermal |= fabsf(s->particles[k].t - p->ambient_temp) > 0.05f || p->mat[m - 1u].self_heat > 0.0f;
+    }
+    if (fabsf(p->ambient_temp - T_REF) > 0.05f) thermal = 1;
+    int rows[MAX_PRESENT], nrows = 0;
+    for (int r = 0; r < O_MAX_MATERIALS; r++)
+        if (present[r]) {
+            if (nrows == MAX_PRESENT) return -2;
+            rows[nrows++] = r;
+            if (p->mat[r].diluent >= 0 && !present[p->mat[r].diluent]) return -3;
+        }
+    if (!tank_layout(&s->tank, rows, nrows, p, thermal)) return -2;
+    s->thermal = thermal;
+    s->caps = compute_caps(s);
+    /* capabilities the oracle does not carry */
+    if (s->tank.families > 0) return -4;
+    if (s->caps & (CAP_RIGID | CAP_RHEO | CAP_MAGNET | CAP_ELASTIC | CAP_SETTLE | CAP_STEAM | CAP_REACT)) return -4;
+    if (__builtin_popcount(s->tank.group_mask) > 1) return -4;
+    for (int k = 0; k < nrows; k++) {
+        const OMat* m = &p->mat[rows[k]];
+        if (m->volatility > 0.0f || (thermal && m->boil < 1e8f)) return -4;
+    }
+    s->visc_mode = viscosity_mode(s);
+    if (s->visc_mode == 2) return -5;
+    build_mats(s);
+    /* buffers a reset clears (mod.rs:2451-2460) */
+    size_t nc = (size_t)s->W * s->H;
+    memset(s->pres, 0, nc * sizeof(V2));
+    memset(s->p2keep, 0, nc * sizeof(float));
+    memset(&s->S, 0, sizeof s->S);
+    memset(s->dheat, 0, nc * sizeof(V4));
+    memset(s->ledger, 0, sizeof s->ledger);
+    s->grid_valid = 0;
+    s->since_sort = 0;
+    s->sim_time = 0.0;
+    return 0;
+}
+
+int osim_step(OSim* s, uint32_t substeps, float target, const OTool* tool) {
+    build_params(s, tool);
+    if (substeps > 0) {
+        s->S.frame_left = maxf(target, 0.0f);
+        s->S.batch_steps = substeps;
+        s->S.batch_done = 0;
+    }
+    for (uint32_t k = 0; k < substeps; k++) {
+        s->since_sort++;
+        if (s->since_sort >= SORT_INTERVAL && s->n_slots >= SORT_MIN_PARTICLES) {
+            s->since_sort = 0;
+            osim_sort(s);
+        }
+        substep(s, s->grid_valid);
+        s->grid_valid = 1;
+        s->substeps_done++;
+    }
+    s->sim_time = s->S.advanced;
+    return 0;
+}
+
+uint32_t osim_particles(const OSim* s, OParticle* out, uint32_t cap) {
+    uint32_t n = s->n_slots < cap ? s->n_slots : cap;
+    memcpy(out, s->particles, (size_t)n * sizeof(OParticle));
+    return s->n_slots;
+}
+
+long osim_field(const OSim* s, const char* name, void* out, size_t cap) {
+    size_t nc = (size_t)s->W * s->H;
+    const void* src = NULL;
+    size_t bytes = 0;
+#define F(nm, ptr, sz) else if (strcmp(name, nm) == 0) { src = (ptr); bytes = (sz); }
+    if (0) {}
+    F("acc", s->acc, nc * (size_t)s->P.acc_stride * 4)
+    F("vel", s->vel, nc * 16)
+    F("vel0", s->vel0, nc * 8)
+    F("cell", s->cell, nc * 16)
+    F("comp", s->comp, nc * 16)
+    F("coef", s->coef, nc * 16)
+    F("sprop", s->sprop, nc * 16)
+    F("surf", s->surf, nc * 16)
+    F("pjump", s->pjump, nc * 8)
+    F("therm", s->therm, nc * 16)
+    F("dheat", s->dheat, nc * 16)
+    F("hcell", s->hcell, nc * 8)
+    F("vw", s->vw, nc * 16)
+    F("vs", s->vs, nc * 16)
+    F("pres", s->pres, nc * 8)
+    F("prhs", s->prhs, nc * 16)
+    F("mga", s->mga, (size_t)s->lv.total * 16)
+    F("mgd", s->mgd, (size_t)s->lv.total * 4)
+    F("mgz", s->mgz, (size_t)s->lv.total * 8)
+    F("ptile", s->ptile, (size_t)s->lv.tiles * 4)
+    F("ledger", s->ledger, sizeof s->ledger)
+    F("region_air", &s->region_air, 4)
+    F("step", &s->S, sizeof s->S)
+#undef F
+    if (!src) return -1;
+    if (out && cap >= bytes) memcpy(out, src, bytes);
+    return (long)bytes;
+}
+
+void osim_stats(const OSim* s, OStats* o) {
+    memset(o, 0, sizeof *o);
+    o->substeps = s->substeps_done;
+    o->sim_time = s->S.advanced;
+    o->dt = s->S.dt;
+    o->dt_prev = s->S.dt_prev;
+    o->p_iters[0] = s->K.p_iters[0];
+    o->p_iters[1] = s->K.p_iters[1];
+    o->p_done[0] = s->K.p_done[0];
+    o->p_done[1] = s->K.p_done[1];
+    o->p_it_max = s->K.p_it_max;
+    o->p_unconv = s->K.p_unconv;
+    o->p2_it_max = s->K.p2_it_max;
+    o->p2_unconv = s->K.p2_unconv;
+    o->solves = s->K.solves;
+    o->p_res_max = s->K.p_res_max;
+    o->p_rr[0] = s->K.p_rr[0];
+    o->p_rr[1] = s->K.p_rr[1];
+    o->p_bb[0] = s->K.p_bb[0];
+    o->p_bb[1] = s->K.p_bb[1];
+    o->umax_grid = bitsf(s->S.umax_grid);
+    o->umax_part = bitsf(s->S.umax_part);
+    o->n_slots = s->n_slots;
+    o->caps = s->caps;
+    o->acc_stride = (uint32_t)(s->tank.stride > ACC_MIN ? s->tank.stride : ACC_MIN);
+    o->thermal = (uint32_t)s->thermal;
+    o->viscosity_mode = (uint32_t)s->visc_mode;
+    o->levels = (uint32_t)s->lv.n;
+    o->tail = (uint32_t)s->lv.tail;
+}

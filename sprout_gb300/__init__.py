@@ -1,0 +1,296 @@
+"""sprout_gb300: a GB300 (sm_103a) engine for Sprout's per-substep 2D APIC/PIC fluid solver.
+
+The engine is the C-ABI library libsprout_gpu.so (include/sprout_gpu.h); this module is a
+thin ctypes layer over it with the reference's names: SimParams (with `set` by name, as
+`--set k=v` / SimParams::set), Scene (Scene::rasterize, maps::fill_rect) and FluidSim
+(reset, step, step_blocking, advance_blocking, download_particles, download_pressure,
+stats). The library must have been built (sprout_gb300/build.py); nothing here falls back
+to a CPU path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB_PATH = HERE / "libsprout_gpu.so"
+
+PARTICLE_DTYPE = np.dtype(
+    [("pos", "<f4", 2), ("vel", "<f4", 2), ("c", "<f4", 4), ("s", "<f4"), ("kind", "<u4"),
+     ("id", "<u4"), ("t", "<f4")]
+)
+assert PARTICLE_DTYPE.itemsize == 48
+
+SPROUT_OK = 0
+ERRORS = {
+    -1: "SPROUT_E_ARG", -2: "SPROUT_E_NOMEM", -3: "SPROUT_E_CAPACITY", -4: "SPROUT_E_DIVERGED",
+    -5: "SPROUT_E_TIMEOUT", -6: "SPROUT_E_CUDA", -7: "SPROUT_E_UNSUPPORTED",
+}
+
+# Every entry point include/sprout_gpu.h declares.
+EXPORTS = [
+    "sprout_last_error", "sprout_version", "sprout_params_new", "sprout_params_free", "sprout_params_copy",
+    "sprout_params_set", "sprout_params_get", "sprout_scene_new", "sprout_scene_free", "sprout_scene_add_box",
+    "sprout_scene_add_circle", "sprout_scene_sdf", "sprout_scene_rasterize", "sprout_fill_rect",
+    "sprout_sim_create", "sprout_sim_destroy", "sprout_sim_set_params", "sprout_sim_set_solids",
+    "sprout_sim_reset", "sprout_sim_step", "sprout_sim_step_blocking", "sprout_sim_advance_blocking",
+    "sprout_sim_sync", "sprout_sim_download_particles", "sprout_sim_download_pressure",
+    "sprout_sim_download_field", "sprout_sim_stats", "sprout_sim_device_bytes", "sprout_sim_profile",
+    "sprout_sim_profile_passes",
+]
+
+STAGES = ["advance", "sort", "p2g", "grid", "pressure", "project"]
+
+
+class SproutError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class Tool(C.Structure):
+    """ToolState (src/sim/params.rs:1141-1150)."""
+    _fields_ = [("pos", C.c_float * 2), ("vel", C.c_float * 2), ("radius", C.c_float), ("mode", C.c_int32),
+                ("strength", C.c_float)]
+
+    @staticmethod
+    def whirl(pos, radius: float, speed: float, clockwise: bool = False) -> "Tool":
+        """ToolState::whirl (params.rs:1175-1181) with the rim speed in cells/s."""
+        t = Tool()
+        t.pos[0], t.pos[1] = pos
+        t.vel[0] = -speed if clockwise else speed
+        t.radius, t.mode, t.strength = radius, 7, 30.0
+        return t
+
+
+class SolverStats(C.Structure):
+    _fields_ = [
+        ("substeps", C.c_uint64), ("sim_time", C.c_double), ("dt", C.c_float), ("dt_prev", C.c_float),
+        ("pressure_iters", C.c_uint32 * 2), ("pressure_iters_max", C.c_uint32),
+        ("pressure_unconverged", C.c_uint32), ("pressure2_iters_max", C.c_uint32),
+        ("pressure2_unconverged", C.c_uint32), ("viscosity_iters_max", C.c_uint32),
+        ("viscosity_unconverged", C.c_uint32), ("solves", C.c_uint32),
+        ("pressure_residual", C.c_float), ("pressure_residual_max", C.c_float),
+        ("viscosity_residual_max", C.c_float), ("umax_grid", C.c_float), ("umax_part", C.c_float),
+        ("n_slots", C.c_uint32), ("n_live", C.c_uint32), ("caps", C.c_uint32), ("acc_stride", C.c_uint32),
+        ("thermal", C.c_uint32), ("viscosity_mode", C.c_uint32), ("levels", C.c_uint32), ("tail", C.c_uint32),
+        ("device_error", C.c_uint32), ("h2d_bytes", C.c_uint64), ("d2h_bytes", C.c_uint64),
+    ]
+
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    """The engine library. Raises if it has not been built: there is no fallback."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB_PATH.exists():
+        raise RuntimeError(f"{LIB_PATH} is missing: build it with `python -m sprout_gb300.build` (CUDA toolkit required)")
+    L = C.CDLL(str(LIB_PATH))
+    P, V = C.POINTER, C.c_void_p
+    sig = {
+        "sprout_last_error": ([], C.c_char_p), "sprout_version": ([], C.c_char_p),
+        "sprout_params_new": ([P(V)], C.c_int), "sprout_params_free": ([V], C.c_int),
+        "sprout_params_copy": ([V, P(V)], C.c_int),
+        "sprout_params_set": ([V, C.c_char_p, C.c_float, P(C.c_int)], C.c_int),
+        "sprout_params_get": ([V, C.c_char_p, P(C.c_float), P(C.c_int)], C.c_int),
+        "sprout_scene_new": ([C.c_uint32, C.c_uint32, P(V)], C.c_int), "sprout_scene_free": ([V], C.c_int),
+        "sprout_scene_add_box": ([V] + [C.c_float] * 6, C.c_int),
+        "sprout_scene_add_circle": ([V] + [C.c_float] * 4, C.c_int),
+        "sprout_scene_sdf": ([V, C.c_float, C.c_float, P(C.c_float)], C.c_int),
+        "sprout_scene_rasterize": ([V, V, V, V, V, P(C.c_int)], C.c_int),
+        "sprout_fill_rect": ([V, P(C.c_float), C.c_uint32, C.c_uint32, V, C.c_uint32, P(C.c_uint32)], C.c_int),
+        "sprout_sim_create": ([C.c_uint32, C.c_uint32, C.c_uint32, V, P(V)], C.c_int),
+        "sprout_sim_destroy": ([V], C.c_int), "sprout_sim_set_params": ([V, V], C.c_int),
+        "sprout_sim_set_solids": ([V, V, V, V, V], C.c_int),
+        "sprout_sim_reset": ([V, V, C.c_uint32], C.c_int),
+        "sprout_sim_step": ([V, C.c_uint32, C.c_float, P(Tool)], C.c_int),
+        "sprout_sim_step_blocking": ([V, C.c_uint32, P(Tool)], C.c_int),
+        "sprout_sim_advance_blocking": ([V, C.c_double, P(Tool)], C.c_int),
+        "sprout_sim_sync": ([V], C.c_int),
+        "sprout_sim_download_particles": ([V, V, C.c_uint32, P(C.c_uint32)], C.c_int),
+        "sprout_sim_download_pressure": ([V, V], C.c_int),
+        "sprout_sim_download_field": ([V, C.c_char_p, V, C.c_size_t, P(C.c_size_t)], C.c_int),
+        "sprout_sim_stats": ([V, P(SolverStats)], C.c_int),
+        "sprout_sim_device_bytes": ([V, P(C.c_size_t)], C.c_int),
+        "sprout_sim_profile": ([V, C.c_uint32, P(C.c_float)], C.c_int),
+        "sprout_sim_profile_passes": ([V, P(C.c_float), C.c_uint32], C.c_int),
+    }
+    for name, (args, res) in sig.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = res
+    _lib = L
+    return L
+
+
+def _check(rc: int):
+    if rc != SPROUT_OK:
+        raise SproutError(rc, lib().sprout_last_error().decode())
+
+
+class SimParams:
+    """SimParams (src/sim/params.rs:149-451) behind the engine's table of names."""
+
+    def __init__(self, settings: dict | None = None):
+        self._h = C.c_void_p()
+        _check(lib().sprout_params_new(C.byref(self._h)))
+        for k, v in (settings or {}).items():
+            if not self.set(k, v):
+                raise KeyError(f"unknown parameter {k!r}")
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().sprout_params_free(self._h)
+            self._h = None
+
+    def set(self, key: str, value: float) -> bool:
+        """SimParams::set: False for an unknown name or NaN; clamps to the range."""
+        ok = C.c_int()
+        _check(lib().sprout_params_set(self._h, key.encode(), float(value), C.byref(ok)))
+        return bool(ok.value)
+
+    def get(self, key: str) -> float:
+        v, ok = C.c_float(), C.c_int()
+        _check(lib().sprout_params_get(self._h, key.encode(), C.byref(v), C.byref(ok)))
+        if not ok.value:
+            raise KeyError(key)
+        return v.value
+
+
+class Scene:
+    """Scene (src/scene.rs): box walls plus boxes and circles, optionally held at a temperature."""
+
+    def __init__(self, w: int, h: int):
+        self.w, self.h = w, h
+        self._h = C.c_void_p()
+        _check(lib().sprout_scene_new(w, h, C.byref(self._h)))
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().sprout_scene_free(self._h)
+            self._h = None
+
+    def add_box(self, c, half, angle: float = 0.0, temp: float | None = None):
+        _check(lib().sprout_scene_add_box(self._h, c[0], c[1], half[0], half[1], angle, math.nan if temp is None else temp))
+
+    def add_circle(self, c, r: float, temp: float | None = None):
+        _check(lib().sprout_scene_add_circle(self._h, c[0], c[1], r, math.nan if temp is None else temp))
+
+    def sdf(self, x: float, y: float) -> float:
+        d = C.c_float()
+        _check(lib().sprout_scene_sdf(self._h, x, y, C.byref(d)))
+        return d.value
+
+    def rasterize(self):
+        """(sdf, solid[n,4], region, temp or None), as Scene::rasterize fills SolidField."""
+        w, h = self.w, self.h
+        sdf = np.zeros((h + 1) * (w + 1), np.float32)
+        solid = np.zeros((h * w, 4), np.float32)
+        region = np.zeros(h * w, np.uint32)
+        temp = np.zeros(h * w, np.float32)
+        heated = C.c_int()
+        _check(lib().sprout_scene_rasterize(self._h, sdf.ctypes.data, solid.ctypes.data, region.ctypes.data,
+                                            temp.ctypes.data, C.byref(heated)))
+        return sdf, solid, region, (temp if heated.value else None)
+
+    def fill_rect(self, rect, material: int, existing: np.ndarray | None = None) -> np.ndarray:
+        """maps::fill_rect: appends rest-density particles of `material` in rect to `existing`."""
+        n0 = 0 if existing is None else len(existing)
+        r = (C.c_float * 4)(*rect)
+        n = C.c_uint32()
+        _check(lib().sprout_fill_rect(self._h, r, material, n0, None, 0, C.byref(n)))
+        out = np.zeros(n0 + n.value, PARTICLE_DTYPE)
+        if existing is not None:
+            out[:n0] = existing
+        _check(lib().sprout_fill_rect(self._h, r, material, n0, out[n0:].ctypes.data, n.value, C.byref(n)))
+        return out
+
+
+class FluidSim:
+    """FluidSim (src/sim/mod.rs:862-) on the current CUDA device."""
+
+    def __init__(self, w: int, h: int, capacity: int, params: SimParams):
+        self.w, self.h = w, h
+        self._h = C.c_void_p()
+        _check(lib().sprout_sim_create(w, h, capacity, params._h, C.byref(self._h)))
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().sprout_sim_destroy(self._h)
+            self._h = None
+
+    __del__ = close
+
+    def set_params(self, params: SimParams):
+        _check(lib().sprout_sim_set_params(self._h, params._h))
+
+    def set_solids(self, sdf, solid, region, temp=None):
+        a = np.ascontiguousarray(sdf, np.float32)
+        b = np.ascontiguousarray(solid, np.float32)
+        c = np.ascontiguousarray(region, np.uint32)
+        d = None if temp is None else np.ascontiguousarray(temp, np.float32)
+        _check(lib().sprout_sim_set_solids(self._h, a.ctypes.data, b.ctypes.data, c.ctypes.data,
+                                           None if d is None else d.ctypes.data))
+
+    def reset(self, particles: np.ndarray):
+        p = np.ascontiguousarray(particles, PARTICLE_DTYPE)
+        _check(lib().sprout_sim_reset(self._h, p.ctypes.data, len(p)))
+
+    def step(self, substeps: int, target: float = 0.0, tool: Tool | None = None):
+        _check(lib().sprout_sim_step(self._h, substeps, target, None if tool is None else C.byref(tool)))
+
+    def step_blocking(self, substeps: int, tool: Tool | None = None):
+        _check(lib().sprout_sim_step_blocking(self._h, substeps, None if tool is None else C.byref(tool)))
+
+    def advance_blocking(self, seconds: float, tool: Tool | None = None):
+        _check(lib().sprout_sim_advance_blocking(self._h, seconds, None if tool is None else C.byref(tool)))
+
+    def sync(self):
+        _check(lib().sprout_sim_sync(self._h))
+
+    def download_particles(self) -> np.ndarray:
+        n = C.c_uint32()
+        _check(lib().sprout_sim_download_particles(self._h, None, 0, C.byref(n)))
+        out = np.zeros(n.value, PARTICLE_DTYPE)
+        _check(lib().sprout_sim_download_particles(self._h, out.ctypes.data, n.value, C.byref(n)))
+        return out
+
+    def download_pressure(self) -> np.ndarray:
+        out = np.zeros((self.h * self.w, 2), np.float32)
+        _check(lib().sprout_sim_download_pressure(self._h, out.ctypes.data))
+        return out
+
+    def field(self, name: str, dtype=np.float32) -> np.ndarray:
+        b = C.c_size_t()
+        _check(lib().sprout_sim_download_field(self._h, name.encode(), None, 0, C.byref(b)))
+        out = np.zeros(b.value // np.dtype(dtype).itemsize, dtype)
+        _check(lib().sprout_sim_download_field(self._h, name.encode(), out.ctypes.data, b.value, C.byref(b)))
+        return out
+
+    def stats(self) -> SolverStats:
+        s = SolverStats()
+        _check(lib().sprout_sim_stats(self._h, C.byref(s)))
+        return s
+
+    def profile(self, substeps: int) -> float:
+        """Device ms of `substeps` more substeps (CUDA events on the sim's stream)."""
+        ms = C.c_float()
+        _check(lib().sprout_sim_profile(self._h, substeps, C.byref(ms)))
+        return ms.value
+
+    def profile_passes(self) -> dict:
+        """One substep stage by stage: device ms per stage (STAGES)."""
+        ms = (C.c_float * 6)()
+        _check(lib().sprout_sim_profile_passes(self._h, ms, 6))
+        return dict(zip(STAGES, list(ms)))
+
+    def device_bytes(self) -> int:
+        b = C.c_size_t()
+        _check(lib().sprout_sim_device_bytes(self._h, C.byref(b)))
+        return b.value

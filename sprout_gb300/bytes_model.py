@@ -1,0 +1,57 @@
+"""Algorithmic bytes of each stage of a substep: the unique bytes a stage must move (every
+field it needs read once, every field it produces written once), in the FP32 engine's own
+layouts. These are the numerators of the roofline figures the benchmark reports; traffic
+measured by ncu above them means re-reads.
+
+Per live particle (48-byte records): advance reads and writes the particle (96) and writes
+its new cell and rank (8); the sort moves it once more (96) with its permutation entry
+(4 written, 4 read, 4 read by the placement); P2G reads it once (48).
+Per cell: see the per-stage tables below (float4 records = 16 bytes).
+"""
+from __future__ import annotations
+
+PARTICLE = {"advance": 48 + 48 + 8, "sort": 8 + 4 + 4 + 4 + 48 + 48, "p2g": 48}
+
+
+def cell_bytes(stage: str, stride: int, thermal: bool, visc_mode: int) -> int:
+    """Bytes per grid cell of one launch of `stage`."""
+    if stage == "advance":
+        return 16 + 16 + 4 + (32 if thermal else 0)          # vel, comp, sdf (+ dheat, hcell)
+    if stage == "sort":
+        return 4 + 4 + 4 + 4 + 4 + 4                          # count clear + read, start write + read + add
+    if stage == "p2g":
+        return 4 + 4 * stride                                  # start (row ranges), accumulators written once
+    if stage == "grid":
+        prep = 4 * stride + 16 + 16 + 8 + 16 + 16 + 16 + (32 if thermal else 0) + 8
+        coef_smooth = 16 + 16 + 16 + 8 + 16
+        curv = 8 + 16 + 4 + 8 + 16
+        apply = 16 + 16 + 16 + 16 + 8
+        heat = (16 * 5 + 8 + 4) if thermal else 0
+        visc = (16 + 16 + 16 + 16 + 16 + 16 + 8) if visc_mode == 1 else 0
+        rhs = 16 + 16 + 16 + 16 + 8 + 16 + 4 + 8 + 16 + 4 + 16
+        return prep + coef_smooth + curv + apply + heat + visc + rhs
+    if stage == "project":
+        return 16 + 16 + 8 + 16 + 8 + 4 + 4 + 16
+    raise KeyError(stage)
+
+
+# The pressure solve, per level-0 unknown: the set-up (warm-start scaling 16, the residual
+# r = b - A x with its matrix row 20 + x 8 + b 8 + r 8, the coarse-matrix build 0.33 of a
+# row 20 + 20), then per iteration: apply (z 8, p_old 8, matrix 20, p 8, q 8 = 52), update
+# fused with the way down (x 8 + 8, p 8, r 8 + 8, q 8, z_pre 8, coarse rhs 2 = 58), the way up
+# (rhs 8, z_pre 8, coarse z 2, matrix 20, z 8 = 46): 156 on level 0, and a third more on the
+# coarser levels (the hierarchy holds 1/3 of the cells again).
+PRESSURE_SETUP = 16 + 44 + 14
+PRESSURE_ITER_L0 = 52 + 58 + 46
+PRESSURE_ITER = PRESSURE_ITER_L0 + (38 + 46) / 3.0
+
+
+def pressure_bytes(unknowns: int, iterations: int) -> float:
+    return unknowns * (PRESSURE_SETUP + (iterations + 1) * PRESSURE_ITER)
+
+
+def stage_bytes(stage: str, particles: int, cells: int, unknowns: int, iterations: int, stride: int,
+                thermal: bool, visc_mode: int) -> float:
+    if stage == "pressure":
+        return pressure_bytes(unknowns, iterations)
+    return particles * PARTICLE.get(stage, 0) + cells * cell_bytes(stage, stride, thermal, visc_mode)

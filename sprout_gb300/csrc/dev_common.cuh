@@ -1,0 +1,203 @@
+// Device-side helpers shared by the engine's kernels.
+//
+// All kernels are compiled with -fmad=false: every float operation rounds the way it is
+// written (as the reference's shaders spell it), which makes the FP32 path reproducible
+// to the bit against a CPU evaluation of the same expressions. GLSL built-ins follow the
+// GLSL spec definitions: mix(x, y, a) = x (1 - a) + y a, length = sqrt(dot),
+// normalize = v / length(v).
+#pragma once
+
+#include <cstdint>
+
+#include "device_types.h"
+
+namespace sprout {
+
+#define DEV __device__ __forceinline__
+
+constexpr float MASS_SCALE = 1048576.0f;   // 2^20
+constexpr float MOM_SCALE = 4194304.0f;    // 2^22
+constexpr int MIN_FACE_MASS = 64;
+constexpr float THETA_MIN = 0.1f;
+constexpr float REST_PHI = 1.0f;
+constexpr float LIQUID_THR = 0.5f;
+constexpr float FACE_EMPTY = 1e30f;
+constexpr float FACE_CLOSED = -1e30f;
+constexpr float NO_TEMP = -1e9f;
+constexpr float LEDGER_SCALE = 65536.0f;
+constexpr float T_SCALE = 4096.0f;
+constexpr uint32_t REGION_MASK = 31u;
+constexpr uint32_t REGION_VENT = 256u;
+constexpr uint32_t KIND_DEAD = 0u;
+constexpr uint32_t KIND_FRESH = 0x10000u;
+constexpr float MG_OMEGA = 1.8f;
+
+// Device buffers of one tank. Grid fields are W x H cells, row-major; the multigrid
+// fields hold every level back to back (Levels offsets).
+struct DevScene {
+    int W, H, ncell, stride;
+    uint32_t capacity;
+    const DevParams* P;
+    const DevMat* mats;
+    StepState* S;
+    SolveState* K;
+    // particles: 3 float4 per particle (pos.xy vel.xy | c | s kind id t)
+    float4* part;     // sorted by cell after every substep, live ones first
+    float4* part2;    // the advanced particles in the previous order
+    uint32_t* pkey;   // new cell of each advanced particle (0xffffffff: dead)
+    uint32_t* prank;  // its arrival rank in that cell
+    uint32_t* perm;   // sorted slot -> slot in part2
+    uint32_t* count;  // particles per cell (ncell + 1)
+    uint32_t* start;  // first sorted slot of each cell (ncell + 1)
+    uint32_t* scan_tmp;
+    // grid
+    int32_t* acc;
+    float4 *vel, *cell, *comp, *coef, *sprop, *surf, *surf2, *aux, *grho, *therm, *dheat, *vw, *vs, *prhs;
+    float2 *vel0, *pjump, *pres;
+    float* p2keep;
+    int2* hcell;
+    const float4* solid;
+    const float* sdf;
+    const uint32_t* region;
+    const float* solid_t;
+    unsigned long long* ledger;
+    // multigrid / Krylov
+    float4* mga;
+    float* mgd;
+    float2 *mgx, *mgz, *mgr, *mgr2, *cgp, *cgp2, *cgq;
+    uint32_t* ptile;
+    float4* partials;   // 2 x nwg
+    int nwg;
+    Levels lv;
+};
+
+// GLSL min / max (GLSL spec 8.3): min(x, y) = y < x ? y : x, max(x, y) = x < y ? y : x.
+DEV float minf(float x, float y) { return y < x ? y : x; }
+DEV float maxf(float x, float y) { return x < y ? y : x; }
+DEV float clampf(float x, float lo, float hi) { return minf(maxf(x, lo), hi); }
+DEV int clampi(int x, int lo, int hi) { return min(max(x, lo), hi); }
+DEV float mixf(float x, float y, float a) { return x * (1.0f - a) + y * a; }
+DEV float len2(float x, float y) { return sqrtf(x * x + y * y); }
+DEV float smoothstepf(float e0, float e1, float x) {
+    float t = clampf((x - e0) / (e1 - e0), 0.0f, 1.0f);
+    return t * t * (3.0f - 2.0f * t);
+}
+DEV bool face_live(float st) { return fabsf(st) < 1e29f; }
+DEV bool face_closed(float st) { return st < -1e29f; }
+
+DEV uint32_t hash32(uint32_t x) {
+    x ^= x >> 16;
+    x *= 0x7feb352du;
+    x ^= x >> 15;
+    x *= 0x846ca68bu;
+    x ^= x >> 16;
+    return x;
+}
+
+// exp(x) by Cody-Waite reduction x = n ln2 + r (ln2 in two parts), e^r by its Taylor
+// series to degree 7 in Horner form, times 2^n assembled from exponent bits in two factors.
+// The same operations in the same order as the CPU evaluation used by the tests, so both
+// round identically (relative error within 2 ulp of the true value over the range used).
+DEV float sp_expf(float x) {
+    if (x != x) return x;
+    if (x > 88.72283f) return __int_as_float(0x7f800000);
+    if (x < -103.972f) return 0.0f;
+    const float LOG2E = 1.44269504f;
+    const float LN2_HI = 0.693145752f;
+    const float LN2_LO = 1.42860677e-06f;
+    float n = floorf(x * LOG2E + 0.5f);
+    float r = (x - n * LN2_HI) - n * LN2_LO;
+    float p = 1.98412698e-04f;
+    p = p * r + 1.38888889e-03f;
+    p = p * r + 8.33333333e-03f;
+    p = p * r + 4.16666667e-02f;
+    p = p * r + 1.66666667e-01f;
+    p = p * r + 0.5f;
+    p = p * r + 1.0f;
+    p = p * r + 1.0f;
+    int k = (int)n;
+    int k1 = k / 2, k2 = k - k1;
+    float s1 = __int_as_float((k1 + 127) << 23);
+    float s2 = __int_as_float((k2 + 127) << 23);
+    return (p * s1) * s2;
+}
+
+// Quadratic B-spline weights (common.glsl:639-643) of a point at offset f from its base node.
+DEV void bspline(float fx, float fy, float wx[3], float wy[3]) {
+    wx[0] = 0.5f * (1.5f - fx) * (1.5f - fx);
+    wy[0] = 0.5f * (1.5f - fy) * (1.5f - fy);
+    wx[1] = 0.75f - (fx - 1.0f) * (fx - 1.0f);
+    wy[1] = 0.75f - (fy - 1.0f) * (fy - 1.0f);
+    wx[2] = 0.5f * (fx - 0.5f) * (fx - 0.5f);
+    wy[2] = 0.5f * (fy - 0.5f) * (fy - 0.5f);
+}
+
+DEV float row_density(const DevMat* mats, uint32_t row, float s) {
+    int d = mats[row].ia[1];
+    float rho = mats[row].a[0];
+    return d >= 0 ? mixf(mats[d].a[0], rho, s) : rho;
+}
+
+DEV float expansion_of(const DevMat* mats, uint32_t row, float s, float T) {
+    const DevMat& m = mats[row];
+    int d = m.ia[1];
+    float b = m.misc[3], tr = m.temp[2] - 273.15f, tb = m.th2[2];
+    if (d >= 0) {
+        b = mixf(mats[d].misc[3], b, s);
+        tr = mixf(mats[d].temp[2] - 273.15f, tr, s);
+        tb = mixf(mats[d].th2[2], tb, s);
+    }
+    return clampf(1.0f - b * (minf(T, tb) - tr), 0.7f, 1.3f);
+}
+
+// Solidus, liquidus, latent heat (degrees), heat capacity of `row` at concentration s.
+DEV float4 thermal_of(const DevMat* mats, uint32_t row, float s) {
+    const DevMat& m = mats[row];
+    float ld = m.th2[0];
+    int d = m.ia[1];
+    if (d < 0) return make_float4(m.th[2], m.th[3], ld, m.th[0]);
+    const DevMat& dm = mats[d];
+    float shift = m.misc[0] * s;
+    float C = mixf(dm.th[0], m.th[0], s);
+    return make_float4(dm.th[2] + shift, dm.th[3] + shift, mixf(dm.th[0] * dm.th2[0], m.th[0] * ld, s) / C, C);
+}
+
+// Temperature and frozen share from the enthalpy temperature.
+DEV float2 phase_of(float te, float4 m) {
+    if (te >= m.y) return make_float2(te, 0.0f);
+    float lo = m.x - m.z;
+    if (te <= lo) return make_float2(te + m.z, 1.0f);
+    float fr = (te - lo) / (m.y - lo);
+    return make_float2(m.x + fr * (m.y - m.x), 1.0f - fr);
+}
+
+DEV float temp_law(const DevMat* mats, int r, float T) {
+    int model = mats[r].ib[2];
+    if (model == 0) return 0.0f;
+    const float* tp = mats[r].temp;
+    float Tk = maxf(T + 273.15f, 1.0f);
+    float x = model == 1 ? tp[0] * (1.0f / Tk - 1.0f / tp[2]) : tp[0] / maxf(Tk - tp[1], 5.0f) - tp[0] / maxf(tp[2] - tp[1], 5.0f);
+    return clampf(x, -30.0f, 30.0f);
+}
+
+DEV int group_heat_chan(const DevParams* P, int g) { return (int)((P->group_heat >> (8u * (uint32_t)g)) & 255u) - 1; }
+
+DEV int2 heat_quanta(float C, float T) {
+    int ci = (int)floorf(C * MASS_SCALE + 0.5f);
+    return make_int2(ci, (int)floorf((float)ci * (T + 273.15f) / T_SCALE + 0.5f));
+}
+
+DEV void ledger_add(unsigned long long* ledger, int entry, float v) {
+    uint32_t x = (uint32_t)(v * LEDGER_SCALE + 0.5f);
+    if (x == 0u) return;
+    atomicAdd(&ledger[entry], (unsigned long long)x);
+}
+
+// Warp max of a non-negative float, then one atomicMax of its bits per warp.
+DEV void report_max(uint32_t* slot, float m) {
+    uint32_t b = __float_as_uint(m);
+    b = __reduce_max_sync(0xffffffffu, b);
+    if ((threadIdx.x & 31) == 0) atomicMax(slot, b);
+}
+
+}  // namespace sprout

@@ -1,0 +1,104 @@
+// Plain structs shared by the host orchestration and the device kernels of the engine.
+// DevParams / DevMat carry the per-substep constants and the material table in grid units
+// (the Params uniform and Mat table of shaders/common.glsl:37-86, 224-238); StepState and
+// SolveState are the device-resident step and Krylov scalars (StepBuf, SolveBuf,
+// common.glsl:122-149).
+#pragma once
+
+#include <array>
+#include <cstdint>
+
+namespace std {
+using array3i = std::array<int, 3>;
+}
+
+namespace sprout {
+
+constexpr int kMaxPresent = 12;
+constexpr int kGroups = 4;
+constexpr int kMaxLevels = 24;
+
+constexpr uint32_t CAP_FAMILIES = 1u, CAP_THERMAL = 2u, CAP_RIGID = 4u, CAP_RHEO = 8u, CAP_MAGNET = 16u,
+                   CAP_ELASTIC = 32u, CAP_SETTLE = 64u, CAP_STEAM = 128u, CAP_REACT = 256u;
+
+struct ToolState {
+    float pos[2], vel[2], radius;
+    int32_t mode;
+    float strength;
+};
+
+// One material row in grid units (the fields the engine's passes read).
+struct DevMat {
+    int ia[4];      // phase group; diluent row; channel of its weight; channel of weight x concentration
+    int ib[4];      // family; rheology; temperature model; residue
+    float a[4];     // relative density; ln kinematic viscosity (cells^2/s); tension vs air (cells^3/s^2); mix rate
+    float b[4];     // cos, sin of the contact angle; grain (cells); relative density when frozen
+    float temp[4];  // temperature law B, C (K), reference temperature (K); skin
+    float th[4];    // heat capacity / water's; conductivity (grid units); solidus, liquidus (deg C)
+    float th2[4];   // latent heat (degrees); emissivity; boiling point; latent heat of vaporisation
+    float misc[4];  // freeze shift; load; viscosity blend exponent; thermal expansion (1/K)
+    float rx[4];    // reaction rate; reaction heat; self-heating (K/s); volatility
+};
+
+struct DevParams {
+    int grid[2];
+    uint32_t n_slots;
+    float dt_fixed, gravity, inv_ppc, apic_clamp;
+    float pair[kGroups][kGroups];
+    float misc[4];   // curvature limit; sealed vent; cell size (m); unused
+    int n_present, acc_stride, n_fam;
+    uint32_t group_mask, caps;
+    int primary;
+    uint32_t group_heat;
+    int present[kMaxPresent];
+    float heat[4], heat2[4], heat3[4];
+    float sep_tau, cfl, tool_crowd_max, density_k, dt_max, crowd_jitter, ext_speed, wall_margin;
+    float tool_pos[2], tool_vel[2], tool_radius;
+    int tool_mode;
+    float tool_strength;
+    float tol[4], ext[4], corr[4];
+    uint32_t pressure_max_iters;
+    int visc_mode;    // 0 none, 1 explicit, 2 implicit
+    int thermal;
+    int pad;
+};
+
+// StepBuf (common.glsl:122-135) plus the engine's own step flags.
+struct StepState {
+    float frame_left, advanced;
+    uint32_t batch_steps, batch_done;
+    float dt, dt_prev;
+    uint32_t umax_grid, umax_part;
+    float dt_cfl;
+    uint32_t substeps;
+    float umax_seen;
+    uint32_t pad0;
+    uint32_t gather;      // 0 on the first substep after a reset
+    uint32_t region_air;  // bit per region holding a cell without liquid (grid_prep.comp)
+    uint32_t n_live;      // live particles after the last sort
+    float corr_gain;      // min(1 - exp(-dt / tau), density_k): rhs.comp:79
+};
+
+// SolveBuf (common.glsl:138-149): pressure scalars and statistics.
+struct SolveState {
+    float p_rz[2], p_alpha[2], p_beta[2], p_bb[2], p_rr[2];
+    uint32_t p_done[2], p_iters[2];
+    uint32_t p_it_max, p_unconv, p2_it_max, p2_unconv, solves;
+    float p_res_max;
+    uint32_t v_it_max, v_unconv;
+    float v_res_max;
+    uint32_t error;       // non-zero: a bounded wait in a persistent kernel ran out
+    uint32_t bar_count, bar_gen;   // the persistent kernels' grid barrier
+    uint32_t pad[2];
+};
+
+// The multigrid hierarchy (Levels, src/sim/mod.rs:714-753).
+struct Levels {
+    int n = 0;
+    int w[kMaxLevels] = {}, h[kMaxLevels] = {};
+    int off[kMaxLevels] = {};
+    int toff[kMaxLevels] = {};
+    int total = 0, tail = 0, tiles = 0;
+};
+
+}  // namespace sprout

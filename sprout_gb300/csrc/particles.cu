@@ -1,0 +1,704 @@
+// Particle side of the substep on sm_103a:
+//   k_step      the substep length on the device (step.comp:22-51)
+//   k_advance   G2P gather, tool, speed cap, midpoint advection, path walk with SDF
+//               collisions, crowd jitter (particles.comp:98-949); float4 particle loads;
+//               emits the particle's new cell and its arrival rank there
+//   scan        exclusive scan of the per-cell counts
+//   k_place / k_cell_gather
+//               a stable counting sort by cell (ties by slot), the permutation the
+//               reference's sort.comp:83-119 defines up to its within-cell atomic order;
+//               dead slots go to the end and are cleared
+//   k_p2g       P2G as a per-tile gather over the sorted particles: each 16 x 16 tile of
+//               nodes accumulates the fixed-point mass / momentum / channel sums of the
+//               particles of its 19 x 19 cell neighbourhood in shared memory (integer
+//               atomics only, so the sums are exact and order-free) and writes its nodes
+//               once; no zero fill and no global atomics (deposit, particles.comp:997-1062)
+#include <cuda_runtime.h>
+
+#include "dev_common.cuh"
+#include "kernels.h"
+
+namespace sprout {
+
+constexpr uint32_t DEAD_KEY = 0xffffffffu;
+
+__global__ void k_step(DevScene d) {
+    const DevParams* P = d.P;
+    StepState* S = d.S;
+    float u = maxf(minf(__uint_as_float(S->umax_grid), P->ext[0]), __uint_as_float(S->umax_part));
+    u = maxf(u, P->ext_speed);
+    float dt_cfl = P->cfl / (u + sqrtf(5.0f * maxf(P->gravity, 0.0f)) + 1e-6f);
+    float dt;
+    if (P->dt_fixed > 0.0f) {
+        dt = P->dt_fixed;
+    } else {
+        uint32_t left = S->batch_steps > S->batch_done ? S->batch_steps - S->batch_done : 1u;
+        dt = minf(minf(dt_cfl, P->dt_max), maxf(S->frame_left, 0.0f) / (float)left);
+    }
+    dt = maxf(dt, 1e-6f);
+    S->dt_prev = S->dt > 0.0f ? S->dt : dt;
+    S->dt = dt;
+    S->dt_cfl = minf(dt_cfl, P->dt_max);
+    S->umax_seen = u;
+    S->frame_left -= dt;
+    float lo = __uint_as_float(S->pad0);
+    float y = dt - lo;
+    float t = S->advanced + y;
+    S->pad0 = __float_as_uint((t - S->advanced) - y);
+    S->advanced = t;
+    S->batch_done += 1u;
+    S->substeps += 1u;
+    S->umax_grid = 0u;
+    S->umax_part = 0u;
+    S->region_air = 0u;
+    S->corr_gain = minf(1.0f - sp_expf(-dt / P->tol[3]), P->density_k);
+}
+
+// ---- G2P and advection ------------------------------------------------------------------
+
+struct Grid {
+    const float4* vel;
+    const float* sdf;
+    int W, H;
+    DEV float4 v(int x, int y) const { return __ldg(&vel[y * W + x]); }
+};
+
+DEV float sample_sdf(const Grid& g, float x, float y, float* gx_out, float* gy_out) {
+    float gx = clampf(x, 0.0f, (float)g.W - 0.001f), gy = clampf(y, 0.0f, (float)g.H - 0.001f);
+    int ix = (int)gx, iy = (int)gy;
+    float fx = gx - (float)ix, fy = gy - (float)iy;
+    int w1 = g.W + 1;
+    int k = iy * w1 + ix;
+    float d00 = __ldg(&g.sdf[k]), d10 = __ldg(&g.sdf[k + 1]), d01 = __ldg(&g.sdf[k + w1]), d11 = __ldg(&g.sdf[k + w1 + 1]);
+    *gx_out = mixf(d10 - d00, d11 - d01, fy);
+    *gy_out = mixf(d01 - d00, d11 - d10, fx);
+    return mixf(mixf(d00, d10, fx), mixf(d01, d11, fx), fy);
+}
+
+DEV bool collide(const Grid& g, float wall_margin, float& x, float& y, float& vx, float& vy, bool beyond) {
+    float nx, ny;
+    float d = sample_sdf(g, x, y, &nx, &ny);
+    if (d < wall_margin) {
+        float l = len2(nx, ny);
+        if (l > 1e-5f) {
+            nx = nx / l;
+            ny = ny / l;
+            float push = wall_margin - d + (beyond ? maxf(-d, 0.0f) : 0.0f);
+            x += nx * push;
+            y += ny * push;
+            float vn = vx * nx + vy * ny;
+            if (vn < 0.0f) {
+                vx -= vn * nx;
+                vy -= vn * ny;
+            }
+            return true;
+        }
+    }
+    return false;
+}
+
+// Bilinear grid velocity over live faces; components without a live face keep the fallback.
+DEV float2 sample_vel(const Grid& g, float x, float y, float2 fb) {
+    float2 o = fb;
+    {
+        float gx = x, gy = y - 0.5f;
+        int bx = (int)floorf(gx), by = (int)floorf(gy);
+        float fx = gx - (float)bx, fy = gy - (float)by;
+        float sw = 0.0f, su = 0.0f;
+#pragma unroll
+        for (int b = 0; b < 2; b++)
+#pragma unroll
+            for (int a = 0; a < 2; a++) {
+                float4 q = g.v(bx + a, by + b);
+                if (face_live(q.z)) {
+                    float wt = (a == 0 ? 1.0f - fx : fx) * (b == 0 ? 1.0f - fy : fy);
+                    sw += wt;
+                    su += wt * q.x;
+                }
+            }
+        if (sw > 1e-3f) o.x = su / sw;
+    }
+    {
+        float gx = x - 0.5f, gy = y;
+        int bx = (int)floorf(gx), by = (int)floorf(gy);
+        float fx = gx - (float)bx, fy = gy - (float)by;
+        float sw = 0.0f, su = 0.0f;
+#pragma unroll
+        for (int b = 0; b < 2; b++)
+#pragma unroll
+            for (int a = 0; a < 2; a++) {
+                float4 q = g.v(bx + a, by + b);
+                if (face_live(q.w)) {
+                    float wt = (a == 0 ? 1.0f - fx : fx) * (b == 0 ? 1.0f - fy : fy);
+                    sw += wt;
+                    su += wt * q.y;
+                }
+            }
+        if (sw > 1e-3f) o.y = su / sw;
+    }
+    return o;
+}
+
+DEV float2 tool_target(const DevParams* P, float dx, float dy) {
+    float l = len2(dx, dy);
+    if (P->tool_mode == 3) {
+        float q = maxf(l, 0.15f * P->tool_radius);
+        return make_float2(-dx / q * P->tool_vel[0], -dy / q * P->tool_vel[0]);
+    }
+    if (P->tool_mode == 4) return make_float2(P->tool_vel[0], P->tool_vel[1]);
+    if (P->tool_mode == 7) {
+        float q = maxf(l, 0.4f * P->tool_radius);
+        return make_float2(dy / q * P->tool_vel[0] + dx * 2.0f, -dx / q * P->tool_vel[0] + dy * 2.0f);
+    }
+    if (P->tool_mode == 8) return make_float2(0.0f, 0.0f);
+    return make_float2(P->tool_vel[0] + dx * 4.0f, P->tool_vel[1] + dy * 4.0f);
+}
+
+// APIC gather on one face grid: u faces (axis 0) at (i, j + 0.5), v faces (axis 1) at
+// (i + 0.5, j). Returns whether any live face was near; writes velocity, correction
+// velocity and the two affine entries.
+template <int AXIS>
+DEV bool gather_face(const Grid& g, float px, float py, float& vel_out, float& corr_out, float& c0, float& c1) {
+    float gx = AXIS == 0 ? px - 0.0f : px - 0.5f;
+    float gy = AXIS == 0 ? py - 0.5f : py - 0.0f;
+    int bx = (int)floorf(gx - 0.5f), by = (int)floorf(gy - 0.5f);
+    float fx = gx - (float)bx, fy = gy - (float)by;
+    float wx[3], wy[3];
+    bspline(fx, fy, wx, wy);
+    float sw = 0.0f, su = 0.0f, sc = 0.0f, sdx = 0.0f, sdy = 0.0f, sudx = 0.0f, sudy = 0.0f;
+#pragma unroll
+    for (int b = 0; b < 3; b++)
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+            float4 q = g.v(bx + a, by + b);
+            float st = AXIS == 0 ? q.z : q.w;
+            float val = AXIS == 0 ? q.x : q.y;
+            if (face_live(st)) {
+                float wt = wx[a] * wy[b];
+                float ddx = (float)a - fx, ddy = (float)b - fy;
+                sw += wt;
+                su += wt * val;
+                sc += wt * st;
+                sdx += wt * ddx;
+                sdy += wt * ddy;
+                sudx += wt * val * ddx;
+                sudy += wt * val * ddy;
+            }
+        }
+    if (sw > 1e-4f) {
+        float u = su / sw;
+        vel_out = u;
+        corr_out = sc / sw;
+        c0 = 4.0f * (sudx - u * sdx) / sw;
+        c1 = 4.0f * (sudy - u * sdy) / sw;
+        return true;
+    }
+    return false;
+}
+
+__global__ void __launch_bounds__(256) k_advance(DevScene d) {
+    const DevParams* P = d.P;
+    const StepState* S = d.S;
+    uint32_t id = blockIdx.x * blockDim.x + threadIdx.x;
+    float report = 0.0f;
+    uint32_t key = DEAD_KEY;
+    if (id < P->n_slots) {
+        float4 q0 = d.part[3 * id + 0], q1 = d.part[3 * id + 1], q2 = d.part[3 * id + 2];
+        uint32_t kind = __float_as_uint(q2.y);
+        if (kind != KIND_DEAD && (kind & 255u) != 0u) {
+            const DevMat* mats = d.mats;
+            float dt = S->dt;
+            uint32_t row = (kind & 255u) - 1u;
+            int ia1 = mats[row].ia[1];
+            bool thermal = P->thermal != 0;
+            float px = q0.x, py = q0.y;
+            float pvx = q0.z, pvy = q0.w;
+            float4 C = q1;
+            float ps = q2.x, pt = q2.w;
+            uint32_t pid = __float_as_uint(q2.z);
+            bool alive = true;
+            if (S->gather) {
+                Grid g{d.vel, d.sdf, d.W, d.H};
+                float vx = pvx, vy = pvy, corrx = 0.0f, corry = 0.0f;
+                const float slip = 0.0f;
+                float crowd = 0.0f;
+                gather_face<0>(g, px, py, vx, corrx, C.x, C.y);
+                gather_face<1>(g, px, py, vy, corry, C.z, C.w);
+                if (P->apic_clamp > 0.0f) {
+                    float lim = P->apic_clamp / dt;
+                    C.x = clampf(C.x, -lim, lim);
+                    C.y = clampf(C.y, -lim, lim);
+                    C.z = clampf(C.z, -lim, lim);
+                    C.w = clampf(C.w, -lim, lim);
+                }
+                if (P->corr[0] > 0.0f) {
+                    float cl = len2(corrx, corry), cmax = P->corr[0] / dt;
+                    if (cl > cmax) {
+                        corrx *= cmax / cl;
+                        corry *= cmax / cl;
+                    }
+                }
+                // composition: occupancy around the particle and the heat it takes
+                {
+                    float gx = px - 0.5f, gy = py - 0.5f;
+                    int bx = (int)floorf(gx - 0.5f), by = (int)floorf(gy - 0.5f);
+                    float fx = gx - (float)bx, fy = gy - (float)by;
+                    float wx[3], wy[3];
+                    bspline(fx, fy, wx, wy);
+#pragma unroll
+                    for (int b = 0; b < 3; b++)
+#pragma unroll
+                        for (int a = 0; a < 3; a++) crowd += wx[a] * wy[b] * __ldg(&d.comp[(by + b) * d.W + bx + a]).w;
+                    if (thermal && (kind & KIND_FRESH) == 0u) {
+                        float dT = 0.0f;
+#pragma unroll
+                        for (int b = 0; b < 3; b++)
+#pragma unroll
+                            for (int a = 0; a < 3; a++) dT += wx[a] * wy[b] * d.dheat[(by + b) * d.W + bx + a].x;
+                        int ox = clampi((int)floorf(px), 0, d.W - 1), oy = clampi((int)floorf(py), 0, d.H - 1);
+                        float4 own = d.dheat[oy * d.W + ox];
+                        if (own.y > 0.0f) {
+                            float4 th = thermal_of(mats, row, ps);
+                            float tb = ia1 >= 0 ? mixf(mats[ia1].th2[2], mats[row].th2[2], ps) : mats[row].th2[2];
+                            int2 hq = heat_quanta(th.w, minf(phase_of(pt, th).x, tb));
+                            dT += own.y * (own.z - (float)hq.y / (float)hq.x) * T_SCALE;
+                        }
+                        pt += dT;
+                    }
+                }
+                bool pushed = false;
+                if (P->tool_mode != 0) {
+                    float dx = P->tool_pos[0] - px, dy = P->tool_pos[1] - py;
+                    float r2 = (dx * dx + dy * dy) / (P->tool_radius * P->tool_radius);
+                    if (r2 < 1.0f) {
+                        float fall = 1.0f - r2;
+                        if (P->tool_mode == 2) {
+                            alive = false;
+                        } else if (P->tool_mode == 5 || P->tool_mode == 6) {
+                            if (thermal) {
+                                float e = P->heat2[1] * fall * dt;
+                                float Cc = thermal_of(mats, row, ps).w;
+                                if (P->tool_mode == 6) e = minf(e, maxf(phase_of(pt, thermal_of(mats, row, ps)).x + 150.0f, 0.0f) * Cc);
+                                pt += (P->tool_mode == 5 ? e : -e) / Cc;
+                                ledger_add(d.ledger, P->tool_mode == 5 ? 4 : 5, e * P->inv_ppc);
+                            }
+                        } else {
+                            float k = clampf(P->tool_strength * fall * dt, 0.0f, 1.0f);
+                            if (P->tool_crowd_max > 0.0f && P->tool_mode != 4)
+                                k *= clampf((P->tool_crowd_max - crowd) / (0.25f * P->tool_crowd_max), 0.0f, 1.0f);
+                            float2 tt = tool_target(P, dx, dy);
+                            vx = mixf(vx, tt.x, k);
+                            vy = mixf(vy, tt.y, k);
+                            pushed = true;
+                        }
+                    }
+                }
+                if (alive) {
+                    if (thermal && mats[row].rx[2] > 0.0f) {
+                        float e = mats[row].rx[2] * mats[row].th[0] * (ia1 >= 0 ? ps : 1.0f) * dt * P->heat[1];
+                        pt += e / thermal_of(mats, row, ps).w;
+                        ledger_add(d.ledger, 7, e * P->inv_ppc);
+                    }
+                    float vcap = P->ext[0];
+                    {
+                        float sp = len2(vx, vy);
+                        if (sp > vcap) {
+                            vx *= vcap / sp;
+                            vy *= vcap / sp;
+                        }
+                    }
+                    float vax = vx, vay = vy;
+                    if (P->ext[1] >= 2.0f && !pushed) {
+                        float xmx = clampf(px + 0.5f * dt * (vx + corrx + 0.0f), 2.01f, (float)d.W - 2.01f);
+                        float xmy = clampf(py + 0.5f * dt * (vy + corry + slip), 2.01f, (float)d.H - 2.01f);
+                        float2 here = sample_vel(g, px, py, make_float2(vx, vy));
+                        float2 there = sample_vel(g, xmx, xmy, here);
+                        vax = vx + there.x - here.x;
+                        vay = vy + there.y - here.y;
+                        float sp = len2(vax, vay);
+                        if (sp > vcap) {
+                            vax *= vcap / sp;
+                            vay *= vcap / sp;
+                        }
+                        if (crowd < LIQUID_THR && (vax * vax + vay * vay) < 0.01f * (vx * vx + vy * vy)) {
+                            vx = vax;
+                            vy = vay;
+                        }
+                    }
+                    float dispx = vax + corrx + 0.0f, dispy = vay + corry + slip;
+                    {
+                        float mine = len2(dispx, dispy);
+                        if (crowd < LIQUID_THR) mine /= P->ext[2];
+                        report = mine;
+                    }
+                    float sx = dt * dispx, sy = dt * dispy;
+                    int pieces = clampi((int)ceilf(len2(sx, sy)), 1, 32);
+                    sx /= (float)pieces;
+                    sy /= (float)pieces;
+                    float x = px, y = py;
+                    float wm = P->wall_margin;
+                    for (int k = 1; k < pieces; k++) {
+                        x += sx;
+                        y += sy;
+                        collide(g, wm, x, y, vx, vy, true);
+                    }
+                    x += sx;
+                    y += sy;
+                    float excess = clampf(crowd - 1.5f, 0.0f, 1.0f);
+                    if (excess > 0.0f && P->crowd_jitter > 0.0f) {
+                        uint32_t hh = hash32(pid ^ hash32(__float_as_uint(px) ^ S->substeps));
+                        x += ((float)(hh & 0xffffu) / 65535.0f - 0.5f) * P->crowd_jitter * excess;
+                        y += ((float)(hh >> 16) / 65535.0f - 0.5f) * P->crowd_jitter * excess;
+                    }
+                    collide(g, wm, x, y, vx, vy, true);
+                    bool again = collide(g, wm, x, y, vx, vy, true);
+                    if (again) {
+                        float ggx, ggy;
+                        if (sample_sdf(g, x, y, &ggx, &ggy) < -1.0f) collide(g, wm, x, y, vx, vy, false);
+                    }
+                    x = clampf(x, 2.01f, (float)d.W - 2.01f);
+                    y = clampf(y, 2.01f, (float)d.H - 2.01f);
+                    px = x;
+                    py = y;
+                    pvx = vx;
+                    pvy = vy;
+                    kind &= ~KIND_FRESH;
+                }
+            }
+            if (alive) {
+                if (thermal) {
+                    float4 th = thermal_of(mats, row, ps);
+                    float2 ph = phase_of(pt, th);
+                    float tb = ia1 >= 0 ? mixf(mats[ia1].th2[2], mats[row].th2[2], ps) : mats[row].th2[2];
+                    int hx = clampi((int)floorf(px), 0, d.W - 1), hy = clampi((int)floorf(py), 0, d.H - 1);
+                    int2 hq = heat_quanta(th.w, minf(ph.x, tb));
+                    atomicAdd(&d.hcell[hy * d.W + hx].x, hq.x);
+                    atomicAdd(&d.hcell[hy * d.W + hx].y, hq.y);
+                }
+                int cx = clampi((int)px, 0, d.W - 1), cy = clampi((int)py, 0, d.H - 1);
+                key = (uint32_t)(cy * d.W + cx);
+                d.part2[3 * id + 0] = make_float4(px, py, pvx, pvy);
+                d.part2[3 * id + 1] = C;
+                d.part2[3 * id + 2] = make_float4(ps, __uint_as_float(kind), __uint_as_float(pid), pt);
+            }
+        }
+    }
+    report_max(&d.S->umax_part, report);
+    if (id < P->n_slots) {
+        d.pkey[id] = key;
+        d.prank[id] = key != DEAD_KEY ? atomicAdd(&d.count[key], 1u) : 0u;
+    }
+}
+
+// ---- the sort ---------------------------------------------------------------------------
+
+constexpr int SCAN_BLOCK = 1024;
+
+// Block-wise exclusive scan of count[0..n) into start, block totals into tmp.
+__global__ void __launch_bounds__(SCAN_BLOCK) k_scan_blocks(const uint32_t* count, uint32_t* start, uint32_t* tmp, int n) {
+    __shared__ uint32_t warp_sums[SCAN_BLOCK / 32];
+    int i = blockIdx.x * SCAN_BLOCK + threadIdx.x;
+    uint32_t v = i < n ? count[i] : 0u;
+    uint32_t x = v;
+    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_sums[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+        uint32_t s = warp_sums[lane];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t y = __shfl_up_sync(0xffffffffu, s, o);
+            if (lane >= o) s += y;
+        }
+        warp_sums[lane] = s;
+    }
+    __syncthreads();
+    uint32_t base = wid > 0 ? warp_sums[wid - 1] : 0u;
+    if (i < n) start[i] = base + x - v;
+    if (threadIdx.x == SCAN_BLOCK - 1) tmp[blockIdx.x] = base + x;
+}
+
+// Exclusive scan of the block totals (one block, any count); the grand total is the
+// number of live particles.
+__global__ void __launch_bounds__(SCAN_BLOCK) k_scan_top(uint32_t* tmp, int nb, StepState* S) {
+    __shared__ uint32_t warp_sums[SCAN_BLOCK / 32];
+    __shared__ uint32_t carry;
+    if (threadIdx.x == 0) carry = 0u;
+    __syncthreads();
+    for (int b0 = 0; b0 < nb; b0 += SCAN_BLOCK) {
+        int i = b0 + threadIdx.x;
+        uint32_t v = i < nb ? tmp[i] : 0u;
+        uint32_t x = v;
+        int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) warp_sums[wid] = x;
+        __syncthreads();
+        if (wid == 0) {
+            uint32_t s = warp_sums[lane];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                uint32_t y = __shfl_up_sync(0xffffffffu, s, o);
+                if (lane >= o) s += y;
+            }
+            warp_sums[lane] = s;
+        }
+        __syncthreads();
+        uint32_t base = (wid > 0 ? warp_sums[wid - 1] : 0u) + carry;
+        if (i < nb) tmp[i] = base + x - v;
+        __syncthreads();
+        if (threadIdx.x == SCAN_BLOCK - 1) carry = base + x;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) S->n_live = carry;
+}
+
+__global__ void k_scan_add(uint32_t* start, const uint32_t* tmp, int n) {
+    int i = blockIdx.x * SCAN_BLOCK + threadIdx.x;
+    if (i < n) start[i] += tmp[blockIdx.x];
+}
+
+__global__ void k_place(DevScene d) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.P->n_slots) return;
+    uint32_t key = d.pkey[i];
+    if (key == DEAD_KEY) return;
+    d.perm[d.start[key] + d.prank[i]] = i;
+}
+
+// One thread per cell: orders the cell's arrivals by slot (insertion sort in registers for
+// up to 16, in place otherwise), then copies the particles into their sorted slots.
+// Threads past the last cell clear the slots after the live particles.
+__global__ void __launch_bounds__(256) k_cell_gather(DevScene d) {
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c < d.ncell) {
+        uint32_t n = d.count[c];
+        if (n == 0u) return;
+        uint32_t s0 = d.start[c];
+        uint32_t* seg = d.perm + s0;
+        if (n <= 16u) {
+            uint32_t v[16];
+#pragma unroll
+            for (int k = 0; k < 16; k++)
+                if ((uint32_t)k < n) v[k] = seg[k];
+            for (uint32_t k = 1; k < n; k++) {
+                uint32_t x = v[k];
+                int j = (int)k - 1;
+                while (j >= 0 && v[j] > x) {
+                    v[j + 1] = v[j];
+                    j--;
+                }
+                v[j + 1] = x;
+            }
+#pragma unroll
+            for (int k = 0; k < 16; k++)
+                if ((uint32_t)k < n) {
+                    uint32_t src = v[k];
+                    seg[k] = src;
+                    d.part[3 * (s0 + k) + 0] = d.part2[3 * src + 0];
+                    d.part[3 * (s0 + k) + 1] = d.part2[3 * src + 1];
+                    d.part[3 * (s0 + k) + 2] = d.part2[3 * src + 2];
+                }
+        } else {
+            for (uint32_t k = 1; k < n; k++) {
+                uint32_t x = seg[k];
+                int j = (int)k - 1;
+                while (j >= 0 && seg[j] > x) {
+                    seg[j + 1] = seg[j];
+                    j--;
+                }
+                seg[j + 1] = x;
+            }
+            for (uint32_t k = 0; k < n; k++) {
+                uint32_t src = seg[k];
+                d.part[3 * (s0 + k) + 0] = d.part2[3 * src + 0];
+                d.part[3 * (s0 + k) + 1] = d.part2[3 * src + 1];
+                d.part[3 * (s0 + k) + 2] = d.part2[3 * src + 2];
+            }
+        }
+    } else {
+        // slots [n_live, n_slots) become dead (zero) slots
+        uint32_t k0 = d.S->n_live + (uint32_t)(c - d.ncell);
+        uint32_t stride = gridDim.x * blockDim.x - (uint32_t)d.ncell;
+        for (uint32_t k = k0; k < d.P->n_slots; k += stride) {
+            float4 z = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            d.part[3 * k + 0] = z;
+            d.part[3 * k + 1] = z;
+            d.part[3 * k + 2] = z;
+        }
+    }
+}
+
+// ---- P2G gather ------------------------------------------------------------------------
+
+constexpr int P2G_T = 16;                 // nodes per tile edge
+constexpr int P2G_HALO_ROWS = P2G_T + 3;  // particle cells [n0 - 2, n0 + 16]
+
+DEV void sadd(int* sacc, int stride, int lx, int ly, int ch, int v) {
+    if (lx >= 0 && ly >= 0 && lx < P2G_T && ly < P2G_T) atomicAdd(&sacc[(ly * P2G_T + lx) * stride + ch], v);
+}
+
+__global__ void __launch_bounds__(256) k_p2g(DevScene d) {
+    extern __shared__ int sacc[];
+    __shared__ uint32_t row_beg[P2G_HALO_ROWS], row_pre[P2G_HALO_ROWS + 1];
+    const DevParams* P = d.P;
+    const DevMat* mats = d.mats;
+    const int stride = d.stride;
+    const int n0x = blockIdx.x * P2G_T, n0y = blockIdx.y * P2G_T;
+    for (int k = threadIdx.x; k < P2G_T * P2G_T * stride; k += blockDim.x) sacc[k] = 0;
+    if (threadIdx.x < P2G_HALO_ROWS) {
+        int cy = n0y - 2 + threadIdx.x;
+        uint32_t b = 0, e = 0;
+        if (cy >= 0 && cy < d.H) {
+            int x0 = max(n0x - 2, 0), x1 = min(n0x + P2G_T, d.W - 1);
+            b = d.start[cy * d.W + x0];
+            e = d.start[cy * d.W + x1 + 1];
+        }
+        row_beg[threadIdx.x] = b;
+        row_pre[threadIdx.x + 1] = e - b;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        row_pre[0] = 0;
+        for (int r = 0; r < P2G_HALO_ROWS; r++) row_pre[r + 1] += row_pre[r];
+    }
+    __syncthreads();
+    const uint32_t total = row_pre[P2G_HALO_ROWS];
+    const float dt = d.S->dt;
+    const bool thermal = P->thermal != 0;
+    const int ct = thermal ? (int)P->heat2[2] : -1;
+    for (uint32_t f = threadIdx.x; f < total; f += blockDim.x) {
+        int r = 0;
+        while (row_pre[r + 1] <= f) r++;
+        uint32_t pi = row_beg[r] + (f - row_pre[r]);
+        float4 q0 = d.part[3 * pi + 0], q1 = d.part[3 * pi + 1], q2 = d.part[3 * pi + 2];
+        uint32_t kind = __float_as_uint(q2.y);
+        uint32_t row = (kind & 255u) - 1u;
+        const int* ia = mats[row].ia;
+        float ps = q2.x;
+        float rho = row_density(mats, row, ps);
+        float CT = 0.0f;
+        int cg = -1;
+        if (thermal) {
+            float4 th = thermal_of(mats, row, ps);
+            float2 ph = phase_of(q2.w, th);
+            float tb = ia[1] >= 0 ? mixf(mats[ia[1]].th2[2], mats[row].th2[2], ps) : mats[row].th2[2];
+            rho *= expansion_of(mats, row, ps, ph.x);
+            if (ph.y > 0.0f) {
+                float rs = ia[1] >= 0 ? mixf(mats[ia[1]].b[3], mats[row].b[3], ps) : mats[row].b[3];
+                rho = mixf(rho, rs, ph.y);
+            }
+            CT = th.w * (minf(ph.x, tb) + 273.15f) / T_SCALE;
+            cg = group_heat_chan(P, ia[0]);
+        }
+        const float px = q0.x, py = q0.y;
+        const float vsx = q0.z * dt, vsy = q0.w * dt;
+        const float csx = q1.x * dt, csy = q1.y * dt, csz = q1.z * dt, csw = q1.w * dt;
+        const int cw = ia[2], cs = ia[3];
+        float wx[3], wy[3];
+        {   // u faces at (i, j + 0.5)
+            float gx = px - 0.0f, gy = py - 0.5f;
+            int bx = (int)floorf(gx - 0.5f), by = (int)floorf(gy - 0.5f);
+            float fx = gx - (float)bx, fy = gy - (float)by;
+            bspline(fx, fy, wx, wy);
+#pragma unroll
+            for (int b = 0; b < 3; b++)
+#pragma unroll
+                for (int a = 0; a < 3; a++) {
+                    int lx = bx + a - n0x, ly = by + b - n0y;
+                    if (lx < 0 || ly < 0 || lx >= P2G_T || ly >= P2G_T) continue;
+                    float m = wx[a] * wy[b] * rho;
+                    float ddx = (float)a - fx, ddy = (float)b - fy;
+                    sadd(sacc, stride, lx, ly, 0, (int)floorf(m * MASS_SCALE + 0.5f));
+                    sadd(sacc, stride, lx, ly, 1, (int)floorf(m * (vsx + (csx * ddx + csy * ddy)) * MOM_SCALE + 0.5f));
+                }
+        }
+        {   // v faces at (i + 0.5, j)
+            float gx = px - 0.5f, gy = py - 0.0f;
+            int bx = (int)floorf(gx - 0.5f), by = (int)floorf(gy - 0.5f);
+            float fx = gx - (float)bx, fy = gy - (float)by;
+            bspline(fx, fy, wx, wy);
+#pragma unroll
+            for (int b = 0; b < 3; b++)
+#pragma unroll
+                for (int a = 0; a < 3; a++) {
+                    int lx = bx + a - n0x, ly = by + b - n0y;
+                    if (lx < 0 || ly < 0 || lx >= P2G_T || ly >= P2G_T) continue;
+                    float m = wx[a] * wy[b] * rho;
+                    float ddx = (float)a - fx, ddy = (float)b - fy;
+                    sadd(sacc, stride, lx, ly, 2, (int)floorf(m * MASS_SCALE + 0.5f));
+                    sadd(sacc, stride, lx, ly, 3, (int)floorf(m * (vsy + (csz * ddx + csw * ddy)) * MOM_SCALE + 0.5f));
+                }
+        }
+        {   // cell centres
+            float gx = px - 0.5f, gy = py - 0.5f;
+            int bx = (int)floorf(gx - 0.5f), by = (int)floorf(gy - 0.5f);
+            float fx = gx - (float)bx, fy = gy - (float)by;
+            bspline(fx, fy, wx, wy);
+#pragma unroll
+            for (int b = 0; b < 3; b++)
+#pragma unroll
+                for (int a = 0; a < 3; a++) {
+                    int lx = bx + a - n0x, ly = by + b - n0y;
+                    if (lx < 0 || ly < 0 || lx >= P2G_T || ly >= P2G_T) continue;
+                    int wi = (int)floorf(wx[a] * wy[b] * MASS_SCALE + 0.5f);
+                    sadd(sacc, stride, lx, ly, 4, wi);
+                    if (cw >= 0) sadd(sacc, stride, lx, ly, cw, wi);
+                    if (cs >= 0 && ps > 0.0f) sadd(sacc, stride, lx, ly, cs, (int)floorf(wx[a] * wy[b] * ps * MASS_SCALE + 0.5f));
+                    if (ct >= 0) {
+                        int hq = (int)floorf(wx[a] * wy[b] * CT * MASS_SCALE + 0.5f);
+                        sadd(sacc, stride, lx, ly, ct, hq);
+                        if (cg >= 0) sadd(sacc, stride, lx, ly, cg, hq);
+                    }
+                }
+        }
+    }
+    __syncthreads();
+    // write the tile's nodes: one row of the tile is 16 x stride contiguous ints
+    for (int k = threadIdx.x; k < P2G_T * P2G_T * stride; k += blockDim.x) {
+        int node = k / stride, ch = k - node * stride;
+        int nx = n0x + (node % P2G_T), ny = n0y + node / P2G_T;
+        if (nx < d.W && ny < d.H) d.acc[(ny * d.W + nx) * stride + ch] = sacc[k];
+    }
+}
+
+// ---- launchers ------------------------------------------------------------------------
+
+void launch_advance(const DevScene& d, const LaunchCfg& cfg, cudaStream_t st) {
+    k_step<<<1, 1, 0, st>>>(d);
+    cudaMemsetAsync(d.count, 0, (size_t)(d.ncell + 1) * sizeof(uint32_t), st);
+    if (cfg.thermal) cudaMemsetAsync(d.hcell, 0, (size_t)d.ncell * sizeof(int2), st);
+    uint32_t nb = (cfg.n_slots + 255) / 256;
+    if (nb == 0) nb = 1;
+    k_advance<<<nb, 256, 0, st>>>(d);
+}
+
+void launch_sort(const DevScene& d, const LaunchCfg& cfg, cudaStream_t st) {
+    uint32_t nb = (cfg.n_slots + 255) / 256;
+    if (nb == 0) nb = 1;
+    int n = d.ncell + 1;
+    int sb = (n + SCAN_BLOCK - 1) / SCAN_BLOCK;
+    k_scan_blocks<<<sb, SCAN_BLOCK, 0, st>>>(d.count, d.start, d.scan_tmp, n);
+    k_scan_top<<<1, SCAN_BLOCK, 0, st>>>(d.scan_tmp, sb, d.S);
+    k_scan_add<<<sb, SCAN_BLOCK, 0, st>>>(d.start, d.scan_tmp, n);
+    k_place<<<nb, 256, 0, st>>>(d);
+    int cg = (d.ncell + 255) / 256 + 64;
+    k_cell_gather<<<cg, 256, 0, st>>>(d);
+}
+
+void launch_p2g(const DevScene& d, const LaunchCfg& cfg, cudaStream_t st) {
+    (void)cfg;
+    dim3 tiles((d.W + P2G_T - 1) / P2G_T, (d.H + P2G_T - 1) / P2G_T);
+    size_t smem = (size_t)P2G_T * P2G_T * d.stride * sizeof(int);
+    k_p2g<<<tiles, 256, smem, st>>>(d);
+}
+
+}  // namespace sprout

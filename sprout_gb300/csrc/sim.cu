@@ -1,0 +1,805 @@
+// The engine's host side: FluidSim's lifecycle (src/sim/mod.rs:862-3474) on one CUDA
+// stream, and the C ABI of include/sprout_gpu.h.
+//
+// A substep is recorded once into a CUDA graph (sort + P2G, grid passes, the persistent
+// pressure kernel, projection) and replayed; the per-call data (parameters, tool, the
+// batch's target time) live in device memory the graph reads, so one graph serves every
+// call until the tank's configuration (particle slots, capabilities, viscosity mode)
+// changes. The step scalars stay on the device: the substep length is picked there
+// (step.comp), and solve iterations end on the device (no host-recorded counts).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/sprout_gpu.h"
+#include "dev_common.cuh"
+#include "kernels.h"
+#include "params.h"
+#include "scene.h"
+
+using namespace sprout;
+
+namespace {
+
+thread_local std::string g_error;
+
+int fail(int code, const std::string& msg) {
+    g_error = msg;
+    return code;
+}
+
+#define CUDA_TRY(expr)                                                                          \
+    do {                                                                                         \
+        cudaError_t e_ = (expr);                                                                 \
+        if (e_ != cudaSuccess) return fail(SPROUT_E_CUDA, std::string(#expr) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+constexpr float kNominalDt = 1.0f / 240.0f;
+
+Levels make_levels(int w, int h) {
+    Levels L;
+    L.w[0] = w;
+    L.h[0] = h;
+    L.n = 1;
+    while (L.w[L.n - 1] * L.h[L.n - 1] > 4) {
+        L.w[L.n] = (L.w[L.n - 1] + 1) / 2;
+        L.h[L.n] = (L.h[L.n - 1] + 1) / 2;
+        L.n++;
+    }
+    int total = 0;
+    for (int l = 0; l < L.n; l++) {
+        L.off[l] = total;
+        total += L.w[l] * L.h[l];
+    }
+    L.total = total;
+    int tail = L.n - 1;
+    for (int l = 1; l < L.n; l++)
+        if (L.w[l] * L.h[l] <= 1500) { tail = l; break; }
+    L.tail = std::min(std::max(tail, 1), L.n - 1);
+    int tiles = 0;
+    for (int l = 0; l <= L.tail; l++) {
+        L.toff[l] = tiles;
+        tiles += ((L.w[l] + 15) / 16) * ((L.h[l] + 15) / 16);
+    }
+    L.tiles = tiles;
+    return L;
+}
+
+}  // namespace
+
+struct SproutParams {
+    SimParams p;
+};
+
+struct SproutScene {
+    Scene s;
+};
+
+struct SproutSim {
+    int W = 0, H = 0;
+    uint32_t capacity = 0, n_slots = 0;
+    SimParams params;
+    Tank tank;
+    bool thermal = false, solids_heated = false;
+    uint32_t caps = 0;
+    int visc_mode = 0;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    DevScene d{};
+    std::vector<void*> allocs;
+    size_t bytes = 0;
+    LaunchCfg cfg;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    bool graph_ok = false, use_graph = true;
+    double sim_time = 0.0;
+    float dt_est = kNominalDt;
+    std::vector<float> solid_host;   // kept for nothing but the device copy's lifetime
+
+    ~SproutSim() {
+        if (stage_params) cudaFreeHost(stage_params);
+        if (stage_mats) cudaFreeHost(stage_mats);
+        if (stage_done) cudaEventDestroy(stage_done);
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        for (void* p : allocs) cudaFree(p);
+        if (stream) cudaStreamDestroy(stream);
+    }
+
+    template <class T>
+    int alloc(T** out, size_t n) {
+        void* p = nullptr;
+        size_t b = std::max<size_t>(n, 1) * sizeof(T);
+        if (cudaMalloc(&p, b) != cudaSuccess) return fail(SPROUT_E_NOMEM, "device allocation of " + std::to_string(b) + " bytes failed");
+        cudaMemset(p, 0, b);
+        allocs.push_back(p);
+        bytes += b;
+        *out = static_cast<T*>(p);
+        return SPROUT_OK;
+    }
+
+    int init(uint32_t w, uint32_t h, uint32_t cap, const SimParams& prm) {
+        W = (int)w;
+        H = (int)h;
+        capacity = cap;
+        params = prm;
+        CUDA_TRY(cudaGetDevice(&device));
+        CUDA_TRY(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+        d.W = W;
+        d.H = H;
+        d.ncell = W * H;
+        d.stride = 8;
+        d.capacity = cap;
+        d.lv = make_levels(W, H);
+        d.nwg = ((W + 15) / 16) * ((H + 15) / 16);
+        size_t nc = (size_t)W * H;
+        int rc = SPROUT_OK;
+#define A(ptr, n) do { if ((rc = alloc(&(ptr), (n))) != SPROUT_OK) return rc; } while (0)
+        DevParams* P;
+        DevMat* M;
+        StepState* S;
+        SolveState* K;
+        A(P, 1);
+        A(M, kMaxMaterials);
+        A(S, 1);
+        A(K, 1);
+        d.P = P;
+        d.mats = M;
+        d.S = S;
+        d.K = K;
+        A(d.part, 3 * (size_t)cap);
+        A(d.part2, 3 * (size_t)cap);
+        A(d.pkey, cap);
+        A(d.prank, cap);
+        A(d.perm, cap);
+        A(d.count, nc + 1);
+        A(d.start, nc + 1);
+        A(d.scan_tmp, (nc + 1 + 1023) / 1024 + 1);
+        A(d.acc, nc * 32);
+        A(d.vel, nc); A(d.cell, nc); A(d.comp, nc); A(d.coef, nc); A(d.sprop, nc); A(d.surf, nc);
+        A(d.surf2, nc); A(d.aux, nc); A(d.grho, nc); A(d.therm, nc); A(d.dheat, nc); A(d.vw, nc);
+        A(d.vs, nc); A(d.prhs, nc); A(d.vel0, nc); A(d.pjump, nc); A(d.pres, nc); A(d.p2keep, nc);
+        A(d.hcell, nc);
+        float4* solid;
+        float* sdf;
+        uint32_t* region;
+        float* solid_t;
+        A(solid, nc);
+        A(sdf, (size_t)(W + 1) * (H + 1));
+        A(region, nc);
+        A(solid_t, nc);
+        d.solid = solid;
+        d.sdf = sdf;
+        d.region = region;
+        d.solid_t = solid_t;
+        A(d.ledger, 8);
+        A(d.mga, (size_t)d.lv.total);
+        A(d.mgd, (size_t)d.lv.total);
+        A(d.mgx, (size_t)d.lv.total);
+        A(d.mgz, (size_t)d.lv.total);
+        A(d.mgr, (size_t)d.lv.total);
+        A(d.mgr2, nc);
+        A(d.cgp, nc);
+        A(d.cgp2, nc);
+        A(d.cgq, nc);
+        A(d.ptile, (size_t)d.lv.tiles);
+        A(d.partials, 2 * (size_t)d.nwg);
+#undef A
+        std::vector<float> nt(nc, NO_TEMP);
+        CUDA_TRY(cudaMemcpy(solid_t, nt.data(), nc * sizeof(float), cudaMemcpyHostToDevice));
+        int mx = pressure_blocks_max(device);
+        cfg.mg_blocks = std::max(1, std::min(d.nwg, mx));
+        CUDA_TRY(cudaDeviceSynchronize());
+        return SPROUT_OK;
+    }
+
+    float dt_limit() const {
+        float dt = std::min(params.dt_max, params.dt_capillary(tank.rows));
+        if (thermal) dt = std::min(dt, params.dt_thermal(tank.rows));
+        return dt;
+    }
+
+    int viscosity_mode() const {
+        float dt = dt_limit();
+        float dmax = 0.0f;
+        for (int r : tank.rows) {
+            const MatProps& m = params.mat[r];
+            float cells = 1.0f / (params.cell_size * params.cell_size);
+            float nu;
+            if (!thermal) nu = m.viscosity_at(params.ambient_temp) * cells;
+            else if (m.freezes() || m.temp_model != 0) nu = INFINITY;
+            else nu = m.viscosity * cells;
+            dmax = std::max(dmax, nu * dt);
+        }
+        if (dmax <= 0.0f) return 0;
+        if (dmax <= 0.05f) return 1;
+        return 2;
+    }
+
+    uint32_t compute_caps() const {
+        uint32_t c = 0;
+        if (tank.families > 0) c |= CAP_FAMILIES;
+        if (thermal) c |= CAP_THERMAL;
+        bool rigid = false;
+        for (int r : tank.rows) {
+            const MatProps& m = params.mat[r];
+            const MatProps* dil = m.diluent >= 0 ? &params.mat[m.diluent] : nullptr;
+            if (m.rheology != 0 || m.skin > 0.0f || m.friction > 0.0f) {
+                c |= CAP_RHEO;
+                rigid |= m.rheology == 2 || m.rheology == 3 || m.skin > 0.0f || m.friction > 0.0f;
+            }
+            if (thermal) rigid |= m.freezes() || (dil && dil->freezes()) || m.temp_model != 0 || (dil && dil->temp_model != 0);
+            rigid |= m.viscosity_at(params.ambient_temp) >= params.rigid_viscosity || (!thermal && m.freezes() && params.ambient_temp < m.melt_hi);
+            if (m.shear_modulus > 0.0f) c |= CAP_ELASTIC;
+            if (m.react_with >= 0 && m.react_rate > 0.0f && std::find(tank.rows.begin(), tank.rows.end(), m.react_with) != tank.rows.end()) c |= CAP_REACT;
+            if (r == 57 && thermal) c |= CAP_STEAM;
+        }
+        if (rigid) c |= CAP_RIGID;
+        return c;
+    }
+
+    // The parameters and material table in grid units, uploaded when they change (the
+    // reference re-uploads its uniform every record and the table when it changed,
+    // mod.rs:2512-2520). Pinned staging, so the copies stay asynchronous; a copy waits for
+    // the previous one before its staging is rewritten.
+    DevParams* stage_params = nullptr;
+    DevMat* stage_mats = nullptr;
+    cudaEvent_t stage_done = nullptr;
+    DevParams last_params{};
+    std::vector<DevMat> last_mats;
+    size_t h2d_bytes = 0, d2h_bytes = 0;
+
+    int upload_tables(const ToolState* tool) {
+        if (!stage_params) {
+            CUDA_TRY(cudaMallocHost(&stage_params, sizeof(DevParams)));
+            CUDA_TRY(cudaMallocHost(&stage_mats, sizeof(DevMat) * kMaxMaterials));
+            CUDA_TRY(cudaEventCreateWithFlags(&stage_done, cudaEventDisableTiming));
+        }
+        DevParams P;
+        build_params(params, tank, thermal, caps, W, H, n_slots, dt_limit(), tool, &P);
+        P.visc_mode = visc_mode;
+        std::vector<DevMat> mats(kMaxMaterials);
+        build_materials(params, tank, thermal, mats.data());
+        bool pchg = std::memcmp(&P, &last_params, sizeof P) != 0 || last_mats.empty();
+        bool mchg = last_mats.empty() || std::memcmp(mats.data(), last_mats.data(), sizeof(DevMat) * kMaxMaterials) != 0;
+        if (!pchg && !mchg) return SPROUT_OK;
+        CUDA_TRY(cudaEventSynchronize(stage_done));
+        if (pchg) {
+            *stage_params = P;
+            CUDA_TRY(cudaMemcpyAsync(const_cast<DevParams*>(d.P), stage_params, sizeof P, cudaMemcpyHostToDevice, stream));
+            h2d_bytes += sizeof P;
+            last_params = P;
+        }
+        if (mchg) {
+            std::memcpy(stage_mats, mats.data(), sizeof(DevMat) * kMaxMaterials);
+            CUDA_TRY(cudaMemcpyAsync(const_cast<DevMat*>(d.mats), stage_mats, sizeof(DevMat) * kMaxMaterials, cudaMemcpyHostToDevice, stream));
+            h2d_bytes += sizeof(DevMat) * kMaxMaterials;
+            last_mats = mats;
+        }
+        CUDA_TRY(cudaEventRecord(stage_done, stream));
+        return SPROUT_OK;
+    }
+
+    // Times `substeps` substeps with CUDA events on the sim's stream (blocking).
+    int profile(uint32_t substeps, float* ms) {
+        cudaEvent_t a, b;
+        CUDA_TRY(cudaEventCreate(&a));
+        CUDA_TRY(cudaEventCreate(&b));
+        int rc = ensure_graph();
+        if (rc != SPROUT_OK) return rc;
+        CUDA_TRY(cudaEventRecord(a, stream));
+        for (uint32_t k = 0; k < substeps; k++) {
+            if (use_graph && graph_ok) CUDA_TRY(cudaGraphLaunch(exec, stream));
+            else record_substep(stream);
+        }
+        CUDA_TRY(cudaEventRecord(b, stream));
+        CUDA_TRY(cudaEventSynchronize(b));
+        CUDA_TRY(cudaEventElapsedTime(ms, a, b));
+        cudaEventDestroy(a);
+        cudaEventDestroy(b);
+        return check_device_error();
+    }
+
+    // One substep stage by stage, each bracketed by CUDA events (profile_passes, mod.rs:3120).
+    int profile_passes(float* ms) {
+        int rc = ensure_graph();
+        if (rc != SPROUT_OK) return rc;
+        cudaEvent_t ev[kStages + 1];
+        for (auto& e : ev) CUDA_TRY(cudaEventCreate(&e));
+        CUDA_TRY(cudaEventRecord(ev[0], stream));
+        for (int k = 0; k < kStages; k++) {
+            record_stage(k, stream);
+            CUDA_TRY(cudaEventRecord(ev[k + 1], stream));
+        }
+        CUDA_TRY(cudaEventSynchronize(ev[kStages]));
+        for (int k = 0; k < kStages; k++) CUDA_TRY(cudaEventElapsedTime(&ms[k], ev[k], ev[k + 1]));
+        for (auto& e : ev) cudaEventDestroy(e);
+        return check_device_error();
+    }
+
+    // The stages of a substep, in order (profile_passes times each one).
+    static constexpr int kStages = 6;
+    void record_stage(int k, cudaStream_t st) {
+        switch (k) {
+        case 0: launch_advance(d, cfg, st); break;
+        case 1: launch_sort(d, cfg, st); break;
+        case 2: launch_p2g(d, cfg, st); break;
+        case 3: launch_grid(d, cfg, st); break;
+        case 4: launch_pressure(d, cfg, st); break;
+        default: launch_project(d, cfg, st); break;
+        }
+    }
+
+    void record_substep(cudaStream_t st) {
+        for (int k = 0; k < kStages; k++) record_stage(k, st);
+    }
+
+    int ensure_graph() {
+        LaunchCfg want = cfg;
+        want.n_slots = n_slots;
+        want.thermal = thermal;
+        want.heat = thermal && params.heat_rate > 0.0f;
+        want.visc_mode = visc_mode;
+        bool same = graph_ok && want.n_slots == cfg.n_slots && want.thermal == cfg.thermal && want.heat == cfg.heat &&
+                    want.visc_mode == cfg.visc_mode && d.stride == tank.stride;
+        cfg = want;
+        d.stride = std::max(tank.stride, 8);
+        if (same || !use_graph) return SPROUT_OK;
+        if (exec) { cudaGraphExecDestroy(exec); exec = nullptr; }
+        if (graph) { cudaGraphDestroy(graph); graph = nullptr; }
+        graph_ok = false;
+        if (cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+            cudaGetLastError();
+            use_graph = false;
+            return SPROUT_OK;
+        }
+        record_substep(stream);
+        cudaError_t e = cudaStreamEndCapture(stream, &graph);
+        if (e != cudaSuccess || graph == nullptr) {
+            cudaGetLastError();
+            use_graph = false;
+            graph = nullptr;
+            return SPROUT_OK;
+        }
+        if (cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess) {
+            cudaGetLastError();
+            cudaGraphDestroy(graph);
+            graph = nullptr;
+            use_graph = false;
+            return SPROUT_OK;
+        }
+        graph_ok = true;
+        return SPROUT_OK;
+    }
+
+    int reset(const SproutParticle* in, uint32_t n) {
+        if (n > capacity) n = capacity;
+        std::vector<SproutParticle> ps(in, in + n);
+        for (uint32_t k = 0; k < n; k++) {
+            SproutParticle& q = ps[k];
+            q.id = k;
+            // Positions stay inside [2.01, size - 2.01], the range every substep leaves them in
+            // (particles.comp:912), so that the first gather's 3 x 3 stencils stay on the grid.
+            if (!std::isfinite(q.pos[0]) || !std::isfinite(q.pos[1]))
+                return fail(SPROUT_E_ARG, "particle " + std::to_string(k) + " has a non-finite position");
+            q.pos[0] = std::min(std::max(q.pos[0], 2.01f), (float)W - 2.01f);
+            q.pos[1] = std::min(std::max(q.pos[1], 2.01f), (float)H - 2.01f);
+            uint32_t mat = q.kind & 255u;
+            if (q.kind != 0u && mat != 0u) {
+                const MatProps& def = params.mat[mat - 1u];
+                if (q.t == -1.0e4f) {
+                    q.t = def.spawn_temp;
+                    q.kind |= 0x20000u;
+                }
+                if (q.s == -1.0f) q.s = def.diluent >= 0 ? std::min(std::max(def.load, 0.0f), 1.0f) : 1.0f;
+                if (q.kind & 0x20000u) {
+                    q.kind &= ~0x20000u;
+                    q.t = params.enthalpy_temp((int)mat - 1, q.s, q.t);
+                }
+            }
+        }
+        bool present[kMaxMaterials] = {};
+        bool th = solids_heated;
+        for (uint32_t k = 0; k < n; k++) {
+            uint32_t m = ps[k].kind & 255u;
+            if (m == 0u || ps[k].kind == 0u) continue;
+            present[m - 1u] = true;
+            th |= std::fabs(ps[k].t - params.ambient_temp) > 0.05f || params.mat[m - 1u].self_heat > 0.0f;
+        }
+        if (std::fabs(params.ambient_temp - kTRef) > 0.05f) th = true;
+        std::vector<int> rows;
+        for (int r = 0; r < kMaxMaterials; r++)
+            if (present[r]) {
+                if (params.mat[r].diluent >= 0 && !present[params.mat[r].diluent]) rows.push_back(params.mat[r].diluent);
+                rows.push_back(r);
+            }
+        std::sort(rows.begin(), rows.end());
+        rows.erase(std::unique(rows.begin(), rows.end()), rows.end());
+        Tank t;
+        if (!t.layout(rows, params, th)) return fail(SPROUT_E_CAPACITY, "the tank's materials do not fit the accumulator channels");
+        tank = t;
+        thermal = th;
+        caps = compute_caps();
+        if (tank.families > 0) return fail(SPROUT_E_UNSUPPORTED, "concentration families (a material with a diluent) are not carried by this engine yet");
+        if (caps & (CAP_RIGID | CAP_RHEO | CAP_MAGNET | CAP_ELASTIC | CAP_SETTLE | CAP_STEAM | CAP_REACT))
+            return fail(SPROUT_E_UNSUPPORTED, "the tank needs rigid / rheology / magnet / elastic / settling / steam / reaction passes, which this engine does not carry");
+        if (__builtin_popcount(tank.group_mask) > 1) return fail(SPROUT_E_UNSUPPORTED, "several phase groups in one tank (drift, pair tension) are not carried by this engine yet");
+        for (int r : tank.rows) {
+            const MatProps& m = params.mat[r];
+            if (m.volatility > 0.0f || (thermal && m.boil < 1e8f))
+                return fail(SPROUT_E_UNSUPPORTED, "evaporation and boiling are not carried by this engine");
+        }
+        visc_mode = viscosity_mode();
+        if (visc_mode == 2) return fail(SPROUT_E_UNSUPPORTED, "implicit viscosity is not carried by this engine yet");
+        n_slots = n;
+        d.stride = std::max(tank.stride, 8);
+        CUDA_TRY(cudaStreamSynchronize(stream));
+        size_t nc = (size_t)W * H;
+        if (n > 0) CUDA_TRY(cudaMemcpy(d.part, ps.data(), (size_t)n * sizeof(SproutParticle), cudaMemcpyHostToDevice));
+        CUDA_TRY(cudaMemset(d.pres, 0, nc * sizeof(float2)));
+        CUDA_TRY(cudaMemset(d.p2keep, 0, nc * sizeof(float)));
+        CUDA_TRY(cudaMemset(d.S, 0, sizeof(StepState)));
+        CUDA_TRY(cudaMemset(d.K, 0, sizeof(SolveState)));
+        CUDA_TRY(cudaMemset(d.dheat, 0, nc * sizeof(float4)));
+        CUDA_TRY(cudaMemset(d.ledger, 0, 8 * sizeof(unsigned long long)));
+        sim_time = 0.0;
+        dt_est = kNominalDt;
+        return upload_tables(nullptr);
+    }
+
+    int step(uint32_t substeps, float target, const ToolState* tool) {
+        if (n_slots == 0 || tank.rows.empty()) return fail(SPROUT_E_ARG, "step before reset (no particles)");
+        int rc = upload_tables(tool);
+        if (rc != SPROUT_OK) return rc;
+        if (substeps == 0) return SPROUT_OK;
+        float fl = std::max(target, 0.0f);
+        uint32_t batch[2] = {substeps, 0u};
+        CUDA_TRY(cudaMemcpyAsync(&d.S->frame_left, &fl, 4, cudaMemcpyHostToDevice, stream));
+        CUDA_TRY(cudaMemcpyAsync(&d.S->batch_steps, batch, 8, cudaMemcpyHostToDevice, stream));
+        h2d_bytes += 12;
+        if ((rc = ensure_graph()) != SPROUT_OK) return rc;
+        for (uint32_t k = 0; k < substeps; k++) {
+            if (use_graph && graph_ok) CUDA_TRY(cudaGraphLaunch(exec, stream));
+            else record_substep(stream);
+        }
+        CUDA_TRY(cudaGetLastError());
+        return SPROUT_OK;
+    }
+
+    int poll() {
+        StepState S;
+        CUDA_TRY(cudaMemcpyAsync(&S, d.S, sizeof S, cudaMemcpyDeviceToHost, stream));
+        CUDA_TRY(cudaStreamSynchronize(stream));
+        d2h_bytes += sizeof S;
+        double t = (double)S.advanced - (double)__builtin_bit_cast(float, S.pad0);
+        if (t > sim_time) sim_time = t;
+        if (S.dt_cfl > 0.0f) dt_est = S.dt_cfl;
+        return SPROUT_OK;
+    }
+
+    float dt_estimate() const { return params.fixed_hz > 0.0f ? 1.0f / params.fixed_hz : dt_est; }
+
+    int check_device_error() {
+        uint32_t err = 0;
+        CUDA_TRY(cudaMemcpy(&err, &d.K->error, 4, cudaMemcpyDeviceToHost));
+        if (err) return fail(SPROUT_E_TIMEOUT, "a bounded device-side wait ran out (grid barrier of the pressure solve)");
+        return SPROUT_OK;
+    }
+
+    // FluidSim::step_blocking (mod.rs:3315-3338).
+    int step_blocking(uint32_t substeps, const ToolState* tool) {
+        if (substeps == 0) {
+            int rc = upload_tables(tool);
+            if (rc != SPROUT_OK) return rc;
+            CUDA_TRY(cudaStreamSynchronize(stream));
+            return SPROUT_OK;
+        }
+        double seconds = (double)substeps * (double)kNominalDt;
+        double start = sim_time;
+        float sliver = std::max(params.min_substep_share, 1e-6f);
+        for (int guard = 0; guard < 1000000; guard++) {
+            double left = seconds - (sim_time - start);
+            double dt = dt_estimate();
+            if (left <= sliver * dt) break;
+            uint32_t n = (uint32_t)std::min(std::max(std::ceil(left / dt), 1.0), 16.0);
+            double target = params.fixed_hz > 0.0f ? n * dt : left;
+            int rc = step(n, (float)target, tool);
+            if (rc != SPROUT_OK) return rc;
+            if ((rc = poll()) != SPROUT_OK) return rc;
+        }
+        return check_device_error();
+    }
+
+    // FluidSim::advance_blocking (mod.rs:3284-3312).
+    int advance_blocking(double seconds, const ToolState* tool) {
+        double goal = sim_time + seconds;
+        bool first = true;
+        float sliver = std::max(params.min_substep_share, 1e-6f);
+        for (int guard = 0; guard < 1000000; guard++) {
+            double left = goal - sim_time;
+            double dt = dt_estimate();
+            if (left <= sliver * dt) break;
+            double nn = params.fixed_hz > 0.0f ? std::max(std::round(left / dt), 1.0) : std::ceil(left / dt);
+            uint32_t n = (uint32_t)std::min(std::max(nn, 1.0), 16.0);
+            double target = params.fixed_hz > 0.0f ? n * dt : left;
+            ToolState t0{};
+            const ToolState* use = tool;
+            if (!first && tool) {
+                t0 = *tool;
+                t0.mode = 0;
+                use = &t0;
+            }
+            int rc = step(n, (float)target, use);
+            if (rc != SPROUT_OK) return rc;
+            if ((rc = poll()) != SPROUT_OK) return rc;
+            first = false;
+            if (params.fixed_hz > 0.0f && (goal - sim_time) < 0.5 * dt) break;
+        }
+        return check_device_error();
+    }
+};
+
+// ---- C ABI --------------------------------------------------------------------------------
+
+extern "C" {
+
+const char* sprout_last_error(void) { return g_error.c_str(); }
+const char* sprout_version(void) { return "sprout_gb300 0.1 (sm_103a)"; }
+
+int sprout_params_new(SproutParams** out) {
+    if (!out) return fail(SPROUT_E_ARG, "null out");
+    *out = new (std::nothrow) SproutParams();
+    return *out ? SPROUT_OK : fail(SPROUT_E_NOMEM, "host allocation failed");
+}
+int sprout_params_free(SproutParams* p) {
+    delete p;
+    return SPROUT_OK;
+}
+int sprout_params_copy(const SproutParams* src, SproutParams** out) {
+    if (!src || !out) return fail(SPROUT_E_ARG, "null argument");
+    *out = new (std::nothrow) SproutParams(*src);
+    return *out ? SPROUT_OK : fail(SPROUT_E_NOMEM, "host allocation failed");
+}
+int sprout_params_set(SproutParams* p, const char* key, float v, int* ok) {
+    if (!p || !key || !ok) return fail(SPROUT_E_ARG, "null argument");
+    *ok = p->p.set(key, v) ? 1 : 0;
+    return SPROUT_OK;
+}
+int sprout_params_get(const SproutParams* p, const char* key, float* v, int* ok) {
+    if (!p || !key || !v || !ok) return fail(SPROUT_E_ARG, "null argument");
+    *ok = p->p.get(key, v) ? 1 : 0;
+    return SPROUT_OK;
+}
+
+int sprout_scene_new(uint32_t w, uint32_t h, SproutScene** out) {
+    if (!out || w < 8 || h < 8) return fail(SPROUT_E_ARG, "bad scene size");
+    *out = new (std::nothrow) SproutScene();
+    if (!*out) return fail(SPROUT_E_NOMEM, "host allocation failed");
+    (*out)->s.w = (int)w;
+    (*out)->s.h = (int)h;
+    return SPROUT_OK;
+}
+int sprout_scene_free(SproutScene* s) {
+    delete s;
+    return SPROUT_OK;
+}
+int sprout_scene_add_box(SproutScene* s, float cx, float cy, float hx, float hy, float angle, float temp) {
+    if (!s) return fail(SPROUT_E_ARG, "null scene");
+    Shape sh;
+    sh.kind = Shape::Box;
+    sh.cx = cx; sh.cy = cy; sh.hx = hx; sh.hy = hy; sh.angle = angle;
+    sh.held = !std::isnan(temp);
+    sh.temp = sh.held ? temp : 0.0f;
+    s->s.shapes.push_back(sh);
+    return SPROUT_OK;
+}
+int sprout_scene_add_circle(SproutScene* s, float cx, float cy, float r, float temp) {
+    if (!s) return fail(SPROUT_E_ARG, "null scene");
+    Shape sh;
+    sh.kind = Shape::Circle;
+    sh.cx = cx; sh.cy = cy; sh.r = r;
+    sh.held = !std::isnan(temp);
+    sh.temp = sh.held ? temp : 0.0f;
+    s->s.shapes.push_back(sh);
+    return SPROUT_OK;
+}
+int sprout_scene_sdf(const SproutScene* s, float x, float y, float* d) {
+    if (!s || !d) return fail(SPROUT_E_ARG, "null argument");
+    *d = s->s.sdf(x, y);
+    return SPROUT_OK;
+}
+int sprout_scene_rasterize(const SproutScene* s, float* sdf, float* solid4, uint32_t* region, float* temp, int* heated) {
+    if (!s || !sdf || !solid4 || !region) return fail(SPROUT_E_ARG, "null argument");
+    bool h = s->s.rasterize(sdf, solid4, region, temp);
+    if (heated) *heated = h ? 1 : 0;
+    return SPROUT_OK;
+}
+int sprout_fill_rect(const SproutScene* s, const float rect[4], uint32_t material, uint32_t n_before,
+                     SproutParticle* out, uint32_t cap, uint32_t* n) {
+    if (!s || !rect || !n) return fail(SPROUT_E_ARG, "null argument");
+    if (material >= (uint32_t)kMaxMaterials) return fail(SPROUT_E_ARG, "material row out of range");
+    *n = s->s.fill_rect(rect, material, n_before, reinterpret_cast<SproutParticleHost*>(out), out ? cap : 0);
+    return SPROUT_OK;
+}
+
+int sprout_sim_create(uint32_t w, uint32_t h, uint32_t capacity, const SproutParams* p, SproutSim** out) {
+    if (!out || !p) return fail(SPROUT_E_ARG, "null argument");
+    if (w < 16 || h < 16 || w > 16384 || h > 16384) return fail(SPROUT_E_ARG, "grid must be between 16 and 16384 cells a side");
+    if (capacity == 0) return fail(SPROUT_E_ARG, "capacity must be positive");
+    SproutSim* s = new (std::nothrow) SproutSim();
+    if (!s) return fail(SPROUT_E_NOMEM, "host allocation failed");
+    int rc = s->init(w, h, capacity, p->p);
+    if (rc != SPROUT_OK) {
+        delete s;
+        return rc;
+    }
+    *out = s;
+    return SPROUT_OK;
+}
+int sprout_sim_destroy(SproutSim* sim) {
+    if (sim) cudaStreamSynchronize(sim->stream);
+    delete sim;
+    return SPROUT_OK;
+}
+int sprout_sim_set_params(SproutSim* sim, const SproutParams* p) {
+    if (!sim || !p) return fail(SPROUT_E_ARG, "null argument");
+    sim->params = p->p;
+    return SPROUT_OK;
+}
+int sprout_sim_set_solids(SproutSim* sim, const float* sdf, const float* solid4, const uint32_t* region, const float* temp) {
+    if (!sim || !sdf || !solid4 || !region) return fail(SPROUT_E_ARG, "null argument");
+    size_t nc = (size_t)sim->W * sim->H;
+    CUDA_TRY(cudaStreamSynchronize(sim->stream));
+    CUDA_TRY(cudaMemcpy((void*)sim->d.sdf, sdf, (size_t)(sim->W + 1) * (sim->H + 1) * sizeof(float), cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemcpy((void*)sim->d.solid, solid4, nc * sizeof(float4), cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemcpy((void*)sim->d.region, region, nc * sizeof(uint32_t), cudaMemcpyHostToDevice));
+    if (temp) {
+        CUDA_TRY(cudaMemcpy((void*)sim->d.solid_t, temp, nc * sizeof(float), cudaMemcpyHostToDevice));
+    } else {
+        std::vector<float> nt(nc, NO_TEMP);
+        CUDA_TRY(cudaMemcpy((void*)sim->d.solid_t, nt.data(), nc * sizeof(float), cudaMemcpyHostToDevice));
+    }
+    sim->solids_heated = temp != nullptr;
+    return SPROUT_OK;
+}
+int sprout_sim_reset(SproutSim* sim, const SproutParticle* p, uint32_t n) {
+    if (!sim || (!p && n > 0)) return fail(SPROUT_E_ARG, "null argument");
+    return sim->reset(p, n);
+}
+int sprout_sim_step(SproutSim* sim, uint32_t substeps, float target, const SproutTool* tool) {
+    if (!sim) return fail(SPROUT_E_ARG, "null sim");
+    return sim->step(substeps, target, reinterpret_cast<const ToolState*>(tool));
+}
+int sprout_sim_step_blocking(SproutSim* sim, uint32_t substeps, const SproutTool* tool) {
+    if (!sim) return fail(SPROUT_E_ARG, "null sim");
+    return sim->step_blocking(substeps, reinterpret_cast<const ToolState*>(tool));
+}
+int sprout_sim_advance_blocking(SproutSim* sim, double seconds, const SproutTool* tool) {
+    if (!sim) return fail(SPROUT_E_ARG, "null sim");
+    return sim->advance_blocking(seconds, reinterpret_cast<const ToolState*>(tool));
+}
+int sprout_sim_sync(SproutSim* sim) {
+    if (!sim) return fail(SPROUT_E_ARG, "null sim");
+    CUDA_TRY(cudaStreamSynchronize(sim->stream));
+    return sim->check_device_error();
+}
+int sprout_sim_download_particles(SproutSim* sim, SproutParticle* out, uint32_t cap, uint32_t* n) {
+    if (!sim || !n) return fail(SPROUT_E_ARG, "null argument");
+    CUDA_TRY(cudaStreamSynchronize(sim->stream));
+    *n = sim->n_slots;
+    uint32_t m = std::min(cap, sim->n_slots);
+    if (out && m > 0) CUDA_TRY(cudaMemcpy(out, sim->d.part, (size_t)m * sizeof(SproutParticle), cudaMemcpyDeviceToHost));
+    if (out) sim->d2h_bytes += (size_t)m * sizeof(SproutParticle);
+    return SPROUT_OK;
+}
+int sprout_sim_download_pressure(SproutSim* sim, float* out) {
+    if (!sim || !out) return fail(SPROUT_E_ARG, "null argument");
+    CUDA_TRY(cudaStreamSynchronize(sim->stream));
+    CUDA_TRY(cudaMemcpy(out, sim->d.pres, (size_t)sim->W * sim->H * sizeof(float2), cudaMemcpyDeviceToHost));
+    return SPROUT_OK;
+}
+int sprout_sim_download_field(SproutSim* sim, const char* name, void* out, size_t cap, size_t* bytes) {
+    if (!sim || !name || !bytes) return fail(SPROUT_E_ARG, "null argument");
+    const DevScene& d = sim->d;
+    size_t nc = (size_t)sim->W * sim->H;
+    const void* src = nullptr;
+    size_t b = 0;
+    std::string n(name);
+    if (n == "acc") { src = d.acc; b = nc * d.stride * 4; }
+    else if (n == "vel") { src = d.vel; b = nc * 16; }
+    else if (n == "vel0") { src = d.vel0; b = nc * 8; }
+    else if (n == "cell") { src = d.cell; b = nc * 16; }
+    else if (n == "comp") { src = d.comp; b = nc * 16; }
+    else if (n == "coef") { src = d.coef; b = nc * 16; }
+    else if (n == "sprop") { src = d.sprop; b = nc * 16; }
+    else if (n == "surf") { src = d.surf; b = nc * 16; }
+    else if (n == "pjump") { src = d.pjump; b = nc * 8; }
+    else if (n == "therm") { src = d.therm; b = nc * 16; }
+    else if (n == "dheat") { src = d.dheat; b = nc * 16; }
+    else if (n == "hcell") { src = d.hcell; b = nc * 8; }
+    else if (n == "vw") { src = d.vw; b = nc * 16; }
+    else if (n == "vs") { src = d.vs; b = nc * 16; }
+    else if (n == "pres") { src = d.pres; b = nc * 8; }
+    else if (n == "prhs") { src = d.prhs; b = nc * 16; }
+    else if (n == "mga") { src = d.mga; b = (size_t)d.lv.total * 16; }
+    else if (n == "mgd") { src = d.mgd; b = (size_t)d.lv.total * 4; }
+    else if (n == "mgz") { src = d.mgz; b = (size_t)d.lv.total * 8; }
+    else if (n == "ptile") { src = d.ptile; b = (size_t)d.lv.tiles * 4; }
+    else if (n == "ledger") { src = d.ledger; b = 8 * 8; }
+    else if (n == "count") { src = d.count; b = nc * 4; }
+    else if (n == "start") { src = d.start; b = (nc + 1) * 4; }
+    else if (n == "step") { src = d.S; b = sizeof(StepState); }
+    else if (n == "region_air") { src = &d.S->region_air; b = 4; }
+    else return fail(SPROUT_E_ARG, "unknown field " + n);
+    *bytes = b;
+    if (!out) return SPROUT_OK;
+    if (cap < b) return fail(SPROUT_E_ARG, "buffer too small for field " + n);
+    CUDA_TRY(cudaStreamSynchronize(sim->stream));
+    CUDA_TRY(cudaMemcpy(out, src, b, cudaMemcpyDeviceToHost));
+    return SPROUT_OK;
+}
+int sprout_sim_stats(SproutSim* sim, SproutSolverStats* o) {
+    if (!sim || !o) return fail(SPROUT_E_ARG, "null argument");
+    StepState S;
+    SolveState K;
+    CUDA_TRY(cudaStreamSynchronize(sim->stream));
+    CUDA_TRY(cudaMemcpy(&S, sim->d.S, sizeof S, cudaMemcpyDeviceToHost));
+    CUDA_TRY(cudaMemcpy(&K, sim->d.K, sizeof K, cudaMemcpyDeviceToHost));
+    sim->d2h_bytes += sizeof S + sizeof K;
+    std::memset(o, 0, sizeof *o);
+    o->substeps = S.substeps;
+    o->sim_time = (double)S.advanced - (double)__builtin_bit_cast(float, S.pad0);
+    o->dt = S.dt;
+    o->dt_prev = S.dt_prev;
+    o->pressure_iters[0] = K.p_iters[0];
+    o->pressure_iters[1] = K.p_iters[1];
+    o->pressure_iters_max = std::max(K.p_it_max, K.p2_it_max);
+    o->pressure_unconverged = K.p_unconv;
+    o->pressure2_iters_max = K.p2_it_max;
+    o->pressure2_unconverged = K.p2_unconv;
+    o->viscosity_iters_max = K.v_it_max;
+    o->viscosity_unconverged = K.v_unconv;
+    o->solves = K.solves;
+    o->pressure_residual = K.p_bb[0] > 0.0f ? std::sqrt(K.p_rr[0] / K.p_bb[0]) : 0.0f;
+    o->pressure_residual_max = K.p_res_max;
+    o->viscosity_residual_max = K.v_res_max;
+    o->umax_grid = __builtin_bit_cast(float, S.umax_grid);
+    o->umax_part = __builtin_bit_cast(float, S.umax_part);
+    o->n_slots = sim->n_slots;
+    o->n_live = S.n_live;
+    o->caps = sim->caps;
+    o->acc_stride = (uint32_t)std::max(sim->tank.stride, 8);
+    o->thermal = sim->thermal ? 1u : 0u;
+    o->viscosity_mode = (uint32_t)sim->visc_mode;
+    o->levels = (uint32_t)sim->d.lv.n;
+    o->tail = (uint32_t)sim->d.lv.tail;
+    o->device_error = K.error;
+    o->h2d_bytes = sim->h2d_bytes;
+    o->d2h_bytes = sim->d2h_bytes;
+    return SPROUT_OK;
+}
+int sprout_sim_profile(SproutSim* sim, uint32_t substeps, float* ms) {
+    if (!sim || !ms) return fail(SPROUT_E_ARG, "null argument");
+    if (sim->n_slots == 0) return fail(SPROUT_E_ARG, "profile before reset");
+    return sim->profile(substeps, ms);
+}
+int sprout_sim_profile_passes(SproutSim* sim, float* ms, uint32_t n) {
+    if (!sim || !ms) return fail(SPROUT_E_ARG, "null argument");
+    if (n < (uint32_t)SproutSim::kStages) return fail(SPROUT_E_ARG, "need room for 6 stage times");
+    if (sim->n_slots == 0) return fail(SPROUT_E_ARG, "profile before reset");
+    return sim->profile_passes(ms);
+}
+int sprout_sim_device_bytes(SproutSim* sim, size_t* bytes) {
+    if (!sim || !bytes) return fail(SPROUT_E_ARG, "null argument");
+    *bytes = sim->bytes;
+    return SPROUT_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,86 @@
+"""Tank descriptions: the synthetic workloads of the engine's tests and benchmark.
+
+A tank is a grid, named parameter settings (as `--set k=v`, src/sim/params.rs:986), scene
+shapes (src/scene.rs) and rectangles filled with rest-density particles (maps::fill_rect,
+src/maps.rs:466). Rows of custom liquids are `mat<row>`. The description is plain data, so
+other implementations (the tests' CPU oracle) can be built from the same one.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+
+import numpy as np
+
+@dataclass
+class Tank:
+    w: int
+    h: int
+    settings: dict = field(default_factory=dict)
+    shapes: list = field(default_factory=list)      # dicts: kind box/circle, c, half/r, angle, temp
+    fills: list = field(default_factory=list)       # (rect, material row, temperature or None)
+    capacity_extra: int = 64
+
+    # ---- the engine -----------------------------------------------------------------------
+    def engine(self):
+        import sprout_gb300 as S
+        p = S.SimParams(self.settings)
+        sc = S.Scene(self.w, self.h)
+        for s in self.shapes:
+            if s["kind"] == "box":
+                sc.add_box(s["c"], s["half"], s.get("angle", 0.0), s.get("temp"))
+            else:
+                sc.add_circle(s["c"], s["r"], s.get("temp"))
+        sdf, solid, region, temp = sc.rasterize()
+        parts = None
+        for rect, mat, t in self.fills:
+            before = 0 if parts is None else len(parts)
+            parts = sc.fill_rect(rect, mat, parts)
+            if t is not None:
+                parts["t"][before:] = t
+                parts["kind"][before:] |= 0x20000   # KIND_REAL_T: a temperature to settle
+        sim = S.FluidSim(self.w, self.h, len(parts) + self.capacity_extra, p)
+        sim.set_solids(sdf, solid, region, temp)
+        sim.reset(parts)
+        return sim, parts, (sdf, solid, region, temp)
+
+
+
+# ---- the configurations the benchmark names, at their sizes or scaled down ------------------
+
+def dam_break(w: int = 384, h: int = 216, cell: float = 0.002, width: float = 0.4, height: float = 0.6,
+              tol: float = 1e-5, extra: dict | None = None) -> Tank:
+    """A plain water dam break: water over the left `width` and bottom `height` of a closed box,
+    fixed 1/240 s substeps, no surface tension (the 384 x 216 form is the first configuration)."""
+    s = {"cell_size": cell, "fixed_hz": 240.0, "pressure_tol": tol, "tension_water": 0.0}
+    s.update(extra or {})
+    return Tank(w, h, s, [], [([0.0, 0.0, width * w, height * h], 0, None)])
+
+
+def layered_custom(w: int, h: int, rows: list[dict], cell: float = 0.001, heater_rows: int = 0,
+                   heater_temp: float = 326.85, ambient: float = 19.85, tol: float = 1e-5,
+                   columns: bool = True, seed: int = 0, extra: dict | None = None) -> Tank:
+    """Several custom liquids (rows 59.. of the material table) filling the tank in vertical
+    columns (or horizontal layers), optionally over a heater strip held at `heater_temp`."""
+    s = {"cell_size": cell, "fixed_hz": 240.0, "pressure_tol": tol, "ambient_temp": ambient}
+    for k, props in enumerate(rows):
+        r = 59 + k
+        for name, val in props.items():
+            s[f"mat{r}.{name}"] = val
+    s.update(extra or {})
+    shapes = []
+    if heater_rows > 0:
+        # a box over the bottom rows, held at the heater temperature (solid floor strip)
+        shapes.append({"kind": "box", "c": [w / 2.0, 3.0 + heater_rows / 2.0], "half": [w / 2.0, heater_rows / 2.0],
+                       "angle": 0.0, "temp": heater_temp})
+    rng = np.random.default_rng(seed)
+    fills = []
+    n = len(rows)
+    if columns:
+        edges = np.sort(rng.uniform(0.0, 1.0, n - 1)) if n > 1 else np.array([])
+        edges = np.concatenate([[0.0], edges, [1.0]])
+        for k in range(n):
+            fills.append(([edges[k] * w, 0.0, edges[k + 1] * w, float(h)], 59 + k, ambient))
+    else:
+        for k in range(n):
+            fills.append(([0.0, k * h / n, float(w), (k + 1) * h / n], 59 + k, ambient))
+    return Tank(w, h, s, shapes, fills)
