@@ -25,6 +25,8 @@ void launch_grid(const DevScene& d, const LaunchCfg& cfg, cudaStream_t st);
 cudaError_t launch_pressure(const DevScene& d, const LaunchCfg& cfg, cudaStream_t st);
 void launch_project(const DevScene& d, const LaunchCfg& cfg, cudaStream_t st);
 // Blocks of the persistent pressure kernel that fit on the device at once.
-int pressure_blocks_max(int device);
+int pressure_blocks_max(int device, size_t smem);
+// Dynamic shared memory of the persistent pressure kernel: the tail levels of each block.
+size_t pressure_smem(const Levels& lv);
 
 }  // namespace sprout

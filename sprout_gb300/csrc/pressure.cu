@@ -101,7 +101,7 @@ DEV float4 total(const float4* part, int n, float4* buf) {
     const int t = threadIdx.x;
     float4 s = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     for (int k = t; k < n; k += NT) {
-        float4 v = __ldcg(&part[k]);
+        float4 v = part[k];
         s = make_float4(s.x + v.x, s.y + v.y, s.z + v.z, s.w + v.w);
     }
     buf[t] = s;
@@ -144,7 +144,7 @@ DEV void phase_cg_scale(const DevScene& d, int mode) {
     }
 }
 
-DEV bool unknown(const DevScene& d, const Lv& L, int x, int y) { return l_inside(L, x, y) && __ldcg(&d.mgd[l_at(L, x, y)]) > 0.0f; }
+DEV bool unknown(const DevScene& d, const Lv& L, int x, int y) { return l_inside(L, x, y) && d.mgd[l_at(L, x, y)] > 0.0f; }
 
 // mg_build.comp: coarse level l + 1 from level l over the tiles of the coarse level.
 DEV void phase_mg_build(const DevScene& d, int l) {
@@ -159,7 +159,7 @@ DEV void phase_mg_build(const DevScene& d, int l) {
             uint32_t on = 0u;
             for (int k = 0; k < 4; k++) {
                 int fx = 2 * tx + (k & 1), fy = 2 * ty + (k >> 1);
-                if (fx < tfx && fy < tfy) on |= __ldcg(&d.ptile[F.toff + fy * tfx + fx]);
+                if (fx < tfx && fy < tfy) on |= d.ptile[F.toff + fy * tfx + fx];
             }
             uint32_t slot = (uint32_t)C.toff + (uint32_t)t;
             uint32_t was = d.ptile[slot];
@@ -183,8 +183,8 @@ DEV void phase_mg_build(const DevScene& d, int l) {
             int cx = 2 * Cx + (k & 1), cy = 2 * Cy + (k >> 1);
             if (!unknown(d, F, cx, cy)) continue;
             int i = l_at(F, cx, cy);
-            D += __ldcg(&d.mgd[i]);
-            float4 w = __ldcg(&d.mga[i]);
+            D += d.mgd[i];
+            float4 w = d.mga[i];
             for (int q = 0; q < 4; q++) {
                 int nx = cx + NBX[q], ny = cy + NBY[q];
                 if (!unknown(d, F, nx, ny)) continue;
@@ -198,39 +198,6 @@ DEV void phase_mg_build(const DevScene& d, int l) {
         }
         d.mgd[o] = D > 1e-7f ? D : 0.0f;
         d.mga[o] = D > 1e-7f ? A : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    }
-}
-
-// mg_tail.comp mode 1, by block 0 alone: the Galerkin matrices of the tail levels.
-DEV void phase_tail_build(const DevScene& d) {
-    for (int l = d.lv.tail; l < d.lv.n - 1; l++) {
-        Lv F = lev(d.lv, l), C = lev(d.lv, l + 1);
-        for (int t = threadIdx.x; t < C.w * C.h; t += NT) {
-            int ccx = t % C.w, ccy = t / C.w;
-            float D = 0.0f;
-            float4 A = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-            for (int k = 0; k < 4; k++) {
-                int cx = 2 * ccx + (k & 1), cy = 2 * ccy + (k >> 1);
-                if (!unknown(d, F, cx, cy)) continue;
-                int i = l_at(F, cx, cy);
-                D += __ldcg(&d.mgd[i]);
-                float4 w = __ldcg(&d.mga[i]);
-                for (int q = 0; q < 4; q++) {
-                    int nx = cx + NBX[q], ny = cy + NBY[q];
-                    if (!unknown(d, F, nx, ny)) continue;
-                    float wd = wcomp(w, q);
-                    if ((nx >> 1) == ccx && (ny >> 1) == ccy) D -= wd;
-                    else if (q == 0) A.x += wd;
-                    else if (q == 1) A.y += wd;
-                    else if (q == 2) A.z += wd;
-                    else A.w += wd;
-                }
-            }
-            int o = C.off + t;
-            d.mgd[o] = D > 1e-7f ? D : 0.0f;
-            d.mga[o] = D > 1e-7f ? A : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-        }
-        __syncthreads();
     }
 }
 
@@ -250,14 +217,14 @@ DEV void phase_cg_init(const DevScene& d, float2* r0, float4* buf) {
             const int i = l_at(F, cx, cy);
             const float D = d.mgd[i];
             if (D > 0.0f) {
-                float2 x = __ldcg(&d.pres[i]);
+                float2 x = d.pres[i];
                 float4 w = d.mga[i];
                 float axx = D * x.x, axy = D * x.y;
                 for (int q = 0; q < 4; q++) {
                     int nx = cx + NBX[q], ny = cy + NBY[q];
                     if (unknown(d, F, nx, ny)) {
                         float wd = wcomp(w, q);
-                        float2 pn = __ldcg(&d.pres[l_at(F, nx, ny)]);
+                        float2 pn = d.pres[l_at(F, nx, ny)];
                         axx -= wd * pn.x;
                         axy -= wd * pn.y;
                     }
@@ -285,9 +252,9 @@ struct Rsrc {
     const float2* q;      // A p, for the fused update (null: no update)
     float ax, ay;
     DEV float2 at(int i) const {
-        float2 v = __ldcg(&r[i]);
+        float2 v = r[i];
         if (q) {
-            float2 qq = __ldcg(&q[i]);
+            float2 qq = q[i];
             v.x = v.x - ax * qq.x;
             v.y = v.y - ay * qq.y;
         }
@@ -298,7 +265,7 @@ struct Rsrc {
 // mg_down black(): value of black cell n after the half-sweep from zero.
 DEV float2 down_black(const DevScene& d, const Lv& L, const Rsrc& R, int nx, int ny) {
     int i = l_at(L, nx, ny);
-    float4 w = __ldcg(&d.mga[i]);
+    float4 w = d.mga[i];
     float2 sum = R.at(i);
     for (int q = 0; q < 4; q++) {
         int mx = nx + NBX[q], my = ny + NBY[q];
@@ -306,11 +273,11 @@ DEV float2 down_black(const DevScene& d, const Lv& L, const Rsrc& R, int nx, int
         int j = l_at(L, mx, my);
         float wd = wcomp(w, q);
         float2 rj = R.at(j);
-        float dj = __ldcg(&d.mgd[j]);
+        float dj = d.mgd[j];
         sum.x += wd * rj.x / dj;
         sum.y += wd * rj.y / dj;
     }
-    float di = __ldcg(&d.mgd[i]);
+    float di = d.mgd[i];
     return make_float2(sum.x / di, sum.y / di);
 }
 
@@ -323,13 +290,13 @@ DEV void phase_down(const DevScene& d, int l, const Rsrc& R, float2* r_out, cons
     const int lx = threadIdx.x & 15, ly = threadIdx.x >> 4;
     float2* mgr_c = d.mgr;   // coarse right-hand sides live at the coarse level's offset
     for (int t = blockIdx.x; t < T; t += gridDim.x) {
-        if (__ldcg(&d.ptile[F.toff + t]) == 0u) continue;
+        if (d.ptile[F.toff + t] == 0u) continue;
         const int cx = (t % tx_n) * 16 + lx, cy = (t / tx_n) * 16 + ly;
         const bool red = ((cx + cy) & 1) == 0;
         float2 z = make_float2(0.0f, 0.0f);
         if (l_inside(F, cx, cy)) {
             const int i = l_at(F, cx, cy);
-            const float D = __ldcg(&d.mgd[i]);
+            const float D = d.mgd[i];
             if (D > 0.0f) {
                 if (red) {
                     float2 r = R.at(i);
@@ -339,8 +306,8 @@ DEV void phase_down(const DevScene& d, int l, const Rsrc& R, float2* r_out, cons
                 }
                 if (r_out) {
                     // cg_update.comp: x += alpha p, r -= alpha q (unknowns of active tiles)
-                    float2 pp = __ldcg(&p[i]);
-                    float2 x = __ldcg(&d.pres[i]);
+                    float2 pp = p[i];
+                    float2 x = d.pres[i];
                     x.x += R.ax * pp.x;
                     x.y += R.ay * pp.y;
                     d.pres[i] = x;
@@ -358,7 +325,7 @@ DEV void phase_down(const DevScene& d, int l, const Rsrc& R, float2* r_out, cons
                 for (int k = 0; k < 2; k++) {
                     int qx = cx + k, qy = cy + k;
                     if (!unknown(d, F, qx, qy)) continue;
-                    float4 w = __ldcg(&d.mga[l_at(F, qx, qy)]);
+                    float4 w = d.mga[l_at(F, qx, qy)];
                     int lqx = lx + k, lqy = ly + k;
                     for (int q = 0; q < 4; q++) {
                         int nx = qx + NBX[q], ny = qy + NBY[q];
@@ -378,32 +345,91 @@ DEV void phase_down(const DevScene& d, int l, const Rsrc& R, float2* r_out, cons
     }
 }
 
-// mg_up black(): new value of black cell n after the coarse correction.
-DEV float2 up_black(const DevScene& d, const Lv& L, const Lv& C, const float2* rhs, int nx, int ny) {
+// The tail levels' state in each block's shared memory (dynamic): per tail cell the matrix
+// row (couplings, diagonal), the iterate and the right-hand side, at its offset from the
+// first tail level (the slots of mg_tail.comp).
+struct Tail {
+    float4* a;
+    float* dg;
+    float2* x;
+    float2* r;
+    int base, T, nf;
+};
+
+DEV bool t_unknown(const Tail& tl, const Lv& L, int x, int y) { return l_inside(L, x, y) && tl.dg[L.off - tl.base + y * L.w + x] > 0.0f; }
+
+// mg_tail.comp mode 1 in every block's shared memory, once per solve: the first tail
+// level's matrix from global memory, then the Galerkin matrices of the coarser tail levels
+// (the arithmetic of mg_build.comp). Block 0 also stores them for inspection.
+DEV void tail_setup(const DevScene& d, const Tail& tl) {
+    for (int s = threadIdx.x; s < tl.nf; s += NT) {
+        tl.a[s] = d.mga[tl.base + s];
+        tl.dg[s] = d.mgd[tl.base + s];
+    }
+    __syncthreads();
+    for (int l = d.lv.tail; l < d.lv.n - 1; l++) {
+        Lv F = lev(d.lv, l), C = lev(d.lv, l + 1);
+        const int o = F.off - tl.base, oc = C.off - tl.base;
+        for (int t = threadIdx.x; t < C.w * C.h; t += NT) {
+            int ccx = t % C.w, ccy = t / C.w;
+            float D = 0.0f;
+            float4 A = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            for (int k = 0; k < 4; k++) {
+                int cx = 2 * ccx + (k & 1), cy = 2 * ccy + (k >> 1);
+                if (!t_unknown(tl, F, cx, cy)) continue;
+                int i = o + cy * F.w + cx;
+                D += tl.dg[i];
+                float4 w = tl.a[i];
+                for (int q = 0; q < 4; q++) {
+                    int nx = cx + NBX[q], ny = cy + NBY[q];
+                    if (!t_unknown(tl, F, nx, ny)) continue;
+                    float wd = wcomp(w, q);
+                    if ((nx >> 1) == ccx && (ny >> 1) == ccy) D -= wd;
+                    else if (q == 0) A.x += wd;
+                    else if (q == 1) A.y += wd;
+                    else if (q == 2) A.z += wd;
+                    else A.w += wd;
+                }
+            }
+            tl.dg[oc + t] = D > 1e-7f ? D : 0.0f;
+            tl.a[oc + t] = D > 1e-7f ? A : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            if (blockIdx.x == 0) {
+                d.mgd[C.off + t] = tl.dg[oc + t];
+                d.mga[C.off + t] = tl.a[oc + t];
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// mg_up black(): new value of black cell n after the coarse correction. The coarse level's
+// finished values come from zc (row width zw): global memory, or this block's shared copy
+// of the first tail level.
+DEV float2 up_black(const DevScene& d, const Lv& L, const float2* zc, int zw, const float2* rhs, int nx, int ny) {
     int i = l_at(L, nx, ny);
-    float4 w = __ldcg(&d.mga[i]);
-    float2 sum = __ldcg(&rhs[i]);
+    float4 w = d.mga[i];
+    float2 sum = rhs[i];
     for (int q = 0; q < 4; q++) {
         int mx = nx + NBX[q], my = ny + NBY[q];
         if (!unknown(d, L, mx, my)) continue;
-        float2 xm = __ldcg(&d.mgx[l_at(L, mx, my)]);
-        float2 zc = __ldcg(&d.mgz[l_at(C, mx >> 1, my >> 1)]);
+        float2 xm = d.mgx[l_at(L, mx, my)];
+        float2 zcv = zc[(my >> 1) * zw + (mx >> 1)];
         float wd = wcomp(w, q);
-        sum.x += wd * (xm.x + MG_OMEGA * zc.x);
-        sum.y += wd * (xm.y + MG_OMEGA * zc.y);
+        sum.x += wd * (xm.x + MG_OMEGA * zcv.x);
+        sum.y += wd * (xm.y + MG_OMEGA * zcv.y);
     }
-    float di = __ldcg(&d.mgd[i]);
+    float di = d.mgd[i];
     return make_float2(sum.x / di, sum.y / di);
 }
 
 // mg_up.comp on level l; on level 0 (flag) the partial sums r.z, r.r into part[tile].
-DEV void phase_up(const DevScene& d, int l, bool flag, const float2* rhs, float2* sz, float4* buf) {
+DEV void phase_up(const DevScene& d, int l, bool flag, const float2* rhs, const float2* zc, float2* sz, float4* buf) {
     Lv F = lev(d.lv, l), C = lev(d.lv, l + 1);
     const int tx_n = tiles_x(F);
     const int T = tx_n * tiles_y(F);
     const int lx = threadIdx.x & 15, ly = threadIdx.x >> 4;
     for (int t = blockIdx.x; t < T; t += gridDim.x) {
-        if (__ldcg(&d.ptile[F.toff + t]) == 0u) {
+        if (d.ptile[F.toff + t] == 0u) {
             if (flag && threadIdx.x == 0) d.partials[t] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
             continue;
         }
@@ -411,28 +437,28 @@ DEV void phase_up(const DevScene& d, int l, bool flag, const float2* rhs, float2
         const bool red = ((cx + cy) & 1) == 0;
         const bool unk = unknown(d, F, cx, cy);
         float2 z = make_float2(0.0f, 0.0f);
-        if (unk && !red) z = up_black(d, F, C, rhs, cx, cy);
+        if (unk && !red) z = up_black(d, F, zc, C.w, rhs, cx, cy);
         sz[threadIdx.x] = z;
         __syncthreads();
         float4 a4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         if (l_inside(F, cx, cy)) {
             const int i = l_at(F, cx, cy);
             if (unk) {
-                float2 r = __ldcg(&rhs[i]);
+                float2 r = rhs[i];
                 if (red) {
-                    float4 w = __ldcg(&d.mga[i]);
+                    float4 w = d.mga[i];
                     float sx = r.x, sy = r.y;
                     for (int q = 0; q < 4; q++) {
                         int nx = cx + NBX[q], ny = cy + NBY[q];
                         if (!unknown(d, F, nx, ny)) continue;
                         int lnx = lx + NBX[q], lny = ly + NBY[q];
                         bool here = lnx >= 0 && lny >= 0 && lnx < 16 && lny < 16;
-                        float2 zb = here ? sz[lny * 16 + lnx] : up_black(d, F, C, rhs, nx, ny);
+                        float2 zb = here ? sz[lny * 16 + lnx] : up_black(d, F, zc, C.w, rhs, nx, ny);
                         float wd = wcomp(w, q);
                         sx += wd * zb.x;
                         sy += wd * zb.y;
                     }
-                    float di = __ldcg(&d.mgd[i]);
+                    float di = d.mgd[i];
                     z = make_float2(sx / di, sy / di);
                 }
                 a4 = make_float4(r.x * z.x, r.y * z.y, r.x * r.x, r.y * r.y);
@@ -448,41 +474,44 @@ DEV void phase_up(const DevScene& d, int l, bool flag, const float2* rhs, float2
     }
 }
 
-// mg_tail.comp mode 0 by block 0 alone, in global memory (L2): the V-cycle on the tail
-// levels, right-hand side in mgr[first], result in mgz[first]. The iterate of each tail
-// level lives in mgx, the restricted right-hand sides of the levels below the first in mgr.
-DEV void phase_tail(const DevScene& d) {
+// mg_tail.comp mode 0, computed by EVERY block in its own shared memory: the V-cycle on the
+// tail levels, right-hand side the first tail level's mgr, result left in tl.x (the first
+// tail level's slots). Every block gets the same values; the way up of the level above
+// reads them from its own copy, so no grid barrier follows the tail.
+DEV void phase_tail(const DevScene& d, const Tail& tl) {
     const int first = d.lv.tail, last = d.lv.n - 1;
-    float2* sx = d.mgx;
-    float2* rhs = d.mgr;
+    for (int s = threadIdx.x; s < tl.nf; s += NT) tl.r[s] = d.mgr[tl.base + s];
+    __syncthreads();
     auto sweep = [&](const Lv& L, int colour, bool zero) {
+        const int o = L.off - tl.base;
         for (int t = threadIdx.x; t < L.w * L.h; t += NT) {
             int x = t % L.w, y = t / L.w;
-            int s = L.off + t;
-            float D = __ldcg(&d.mgd[s]);
+            int s = o + t;
+            float D = tl.dg[s];
             if (D <= 0.0f || ((x + y) & 1) != colour) {
-                if (zero) sx[s] = make_float2(0.0f, 0.0f);
+                if (zero) tl.x[s] = make_float2(0.0f, 0.0f);
                 continue;
             }
-            float2 sum = __ldcg(&rhs[s]);
+            float2 sum = tl.r[s];
             if (!zero) {
-                float4 w = __ldcg(&d.mga[s]);
+                float4 w = tl.a[s];
                 for (int q = 0; q < 4; q++) {
                     int nx = x + NBX[q], ny = y + NBY[q];
-                    if (unknown(d, L, nx, ny)) {
+                    if (t_unknown(tl, L, nx, ny)) {
                         float wd = wcomp(w, q);
-                        float2 xn = __ldcg(&sx[l_at(L, nx, ny)]);
+                        float2 xn = tl.x[o + ny * L.w + nx];
                         sum.x += wd * xn.x;
                         sum.y += wd * xn.y;
                     }
                 }
             }
-            sx[s] = make_float2(sum.x / D, sum.y / D);
+            tl.x[s] = make_float2(sum.x / D, sum.y / D);
         }
         __syncthreads();
     };
     for (int l = first; l < last; l++) {
         Lv L = lev(d.lv, l), C = lev(d.lv, l + 1);
+        const int o = L.off - tl.base, oc = C.off - tl.base;
         sweep(L, 0, true);
         sweep(L, 1, false);
         for (int t = threadIdx.x; t < C.w * C.h; t += NT) {
@@ -490,26 +519,26 @@ DEV void phase_tail(const DevScene& d) {
             float sumx = 0.0f, sumy = 0.0f;
             for (int k = 0; k < 4; k++) {
                 int cx = 2 * ccx + (k & 1), cy = 2 * ccy + (k >> 1);
-                if (!unknown(d, L, cx, cy)) continue;
-                int s = l_at(L, cx, cy);
-                float4 w = __ldcg(&d.mga[s]);
-                float Ds = __ldcg(&d.mgd[s]);
-                float2 xs = __ldcg(&sx[s]);
+                if (!t_unknown(tl, L, cx, cy)) continue;
+                int s = o + cy * L.w + cx;
+                float4 w = tl.a[s];
+                float Ds = tl.dg[s];
+                float2 xs = tl.x[s];
                 float azx = Ds * xs.x, azy = Ds * xs.y;
                 for (int q = 0; q < 4; q++) {
                     int nx = cx + NBX[q], ny = cy + NBY[q];
-                    if (unknown(d, L, nx, ny)) {
+                    if (t_unknown(tl, L, nx, ny)) {
                         float wd = wcomp(w, q);
-                        float2 xn = __ldcg(&sx[l_at(L, nx, ny)]);
+                        float2 xn = tl.x[o + ny * L.w + nx];
                         azx -= wd * xn.x;
                         azy -= wd * xn.y;
                     }
                 }
-                float2 rh = __ldcg(&rhs[s]);
+                float2 rh = tl.r[s];
                 sumx += rh.x - azx;
                 sumy += rh.y - azy;
             }
-            rhs[C.off + t] = make_float2(sumx, sumy);
+            tl.r[oc + t] = make_float2(sumx, sumy);
         }
         __syncthreads();
     }
@@ -520,35 +549,36 @@ DEV void phase_tail(const DevScene& d) {
     }
     for (int l = last - 1; l >= first; l--) {
         Lv F = lev(d.lv, l), C = lev(d.lv, l + 1);
+        const int o = F.off - tl.base, oc = C.off - tl.base;
         for (int t = threadIdx.x; t < F.w * F.h; t += NT) {
             int x = t % F.w, y = t / F.w;
             if (((x + y) & 1) == 0) continue;
-            int s = F.off + t;
-            float D = __ldcg(&d.mgd[s]);
+            int s = o + t;
+            float D = tl.dg[s];
             if (D <= 0.0f) continue;
-            float4 w = __ldcg(&d.mga[s]);
-            float2 sum = __ldcg(&rhs[s]);
+            float4 w = tl.a[s];
+            float2 sum = tl.r[s];
             for (int q = 0; q < 4; q++) {
                 int nx = x + NBX[q], ny = y + NBY[q];
-                if (!unknown(d, F, nx, ny)) continue;
+                if (!t_unknown(tl, F, nx, ny)) continue;
                 float wd = wcomp(w, q);
-                float2 xn = __ldcg(&sx[l_at(F, nx, ny)]);
-                float2 xc = __ldcg(&sx[l_at(C, nx >> 1, ny >> 1)]);
+                float2 xn = tl.x[o + ny * F.w + nx];
+                float2 xc = tl.x[oc + (ny >> 1) * C.w + (nx >> 1)];
                 sum.x += wd * (xn.x + MG_OMEGA * xc.x);
                 sum.y += wd * (xn.y + MG_OMEGA * xc.y);
             }
-            sx[s] = make_float2(sum.x / D, sum.y / D);
+            tl.x[s] = make_float2(sum.x / D, sum.y / D);
         }
         __syncthreads();
         sweep(F, 0, false);
     }
-    Lv Fst = lev(d.lv, first);
-    for (int t = threadIdx.x; t < Fst.w * Fst.h; t += NT) d.mgz[Fst.off + t] = __ldcg(&sx[Fst.off + t]);
+    if (blockIdx.x == 0)   // the first tail level's result, for inspection
+        for (int s = threadIdx.x; s < tl.nf; s += NT) d.mgz[tl.base + s] = tl.x[s];
 }
 
 // One V-cycle: level 0's right-hand side through R (fused with the CG update when R.q is
 // set), result in mgz of level 0, partials of r.z and r.r. Returns false on a barrier timeout.
-DEV bool vcycle(const DevScene& d, const Rsrc& R, float2* r_out, const float2* p, const float2* r_new, float2* sz, float4* buf) {
+DEV bool vcycle(const DevScene& d, const Tail& tl, const Rsrc& R, float2* r_out, const float2* p, const float2* r_new, float2* sz, float4* buf) {
     const int tail = d.lv.tail;
     for (int l = 0; l < tail; l++) {
         Rsrc Rl = R;
@@ -556,10 +586,10 @@ DEV bool vcycle(const DevScene& d, const Rsrc& R, float2* r_out, const float2* p
         phase_down(d, l, Rl, l == 0 ? r_out : nullptr, p, sz);
         if (!grid_sync(d.K)) return false;
     }
-    if (blockIdx.x == 0) phase_tail(d);
-    if (!grid_sync(d.K)) return false;
+    phase_tail(d, tl);
     for (int l = tail - 1; l >= 0; l--) {
-        phase_up(d, l, l == 0, l == 0 ? r_new : d.mgr, sz, buf);
+        const float2* zc = (l == tail - 1) ? tl.x : d.mgz + lev(d.lv, l + 1).off;
+        phase_up(d, l, l == 0, l == 0 ? r_new : d.mgr, zc, sz, buf);
         if (!grid_sync(d.K)) return false;
     }
     return true;
@@ -573,13 +603,13 @@ DEV void phase_apply(const DevScene& d, const Solve& K, const float2* p_old, flo
     const int n = d.nwg;
     const bool nob = K.beta[0] == 0.0f && K.beta[1] == 0.0f;
     auto direction = [&](int i) {
-        float2 z = __ldcg(&d.mgz[i]);
+        float2 z = d.mgz[i];
         if (nob) return z;
-        float2 po = __ldcg(&p_old[i]);
+        float2 po = p_old[i];
         return make_float2(K.beta[0] != 0.0f ? z.x + K.beta[0] * po.x : z.x, K.beta[1] != 0.0f ? z.y + K.beta[1] * po.y : z.y);
     };
     for (int t = blockIdx.x; t < T; t += gridDim.x) {
-        if (__ldcg(&d.ptile[F.toff + t]) == 0u) {
+        if (d.ptile[F.toff + t] == 0u) {
             if (threadIdx.x == 0) d.partials[n + t] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
             continue;
         }
@@ -587,10 +617,10 @@ DEV void phase_apply(const DevScene& d, const Solve& K, const float2* p_old, flo
         float4 a4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         if (l_inside(F, cx, cy)) {
             const int i = l_at(F, cx, cy);
-            const float D = __ldcg(&d.mgd[i]);
+            const float D = d.mgd[i];
             if (D > 0.0f) {
                 float2 pp = direction(i);
-                float4 w = __ldcg(&d.mga[i]);
+                float4 w = d.mga[i];
                 float qx = D * pp.x, qy = D * pp.y;
                 for (int q = 0; q < 4; q++) {
                     int nx = cx + NBX[q], ny = cy + NBY[q];
@@ -623,25 +653,34 @@ __global__ void __launch_bounds__(NT) k_mgpcg(DevScene d, int second, int scale_
     __shared__ float2 sz[NT];
     __shared__ float4 buf[NT];
     __shared__ Solve K;
+    extern __shared__ __align__(16) unsigned char tail_smem[];
     const DevParams* P = d.P;
     const int n = d.nwg;
+    Tail tl;
+    {
+        const Lv F = lev(d.lv, d.lv.tail), E = lev(d.lv, d.lv.n - 1);
+        tl.base = F.off;
+        tl.T = E.off + E.w * E.h - F.off;
+        tl.nf = F.w * F.h;
+        tl.a = reinterpret_cast<float4*>(tail_smem);
+        tl.x = reinterpret_cast<float2*>(tl.a + tl.T);
+        tl.r = tl.x + tl.T;
+        tl.dg = reinterpret_cast<float*>(tl.r + tl.T);
+    }
     if (!second) {
         phase_cg_scale(d, scale_mode);
         for (int l = 1; l <= d.lv.tail; l++) {
             if (!grid_sync(d.K)) return;
             phase_mg_build(d, l - 1);
         }
-        if (blockIdx.x == 0 && d.lv.tail < d.lv.n - 1) {
-            __syncthreads();
-            phase_tail_build(d);
-        }
         if (!grid_sync(d.K)) return;
     }
+    tail_setup(d, tl);
     float2* r_cur = d.mgr;    // level 0 of mgr: the residual, double-buffered with mgr2
     float2* r_nxt = d.mgr2;
     phase_cg_init(d, r_cur, buf);
     if (!grid_sync(d.K)) return;
-    if (!vcycle(d, Rsrc{r_cur, nullptr, 0.0f, 0.0f}, nullptr, nullptr, r_cur, sz, buf)) return;
+    if (!vcycle(d, tl, Rsrc{r_cur, nullptr, 0.0f, 0.0f}, nullptr, nullptr, r_cur, sz, buf)) return;
     {
         float4 a = total(d.partials, n, buf), b = total(d.partials + n, n, buf);
         if (threadIdx.x == 0) {
@@ -679,7 +718,7 @@ __global__ void __launch_bounds__(NT) k_mgpcg(DevScene d, int second, int scale_
             __syncthreads();
         }
         Rsrc R{r_cur, d.cgq, K.alpha[0], K.alpha[1]};
-        if (!vcycle(d, R, r_nxt, p_new, r_nxt, sz, buf)) return;
+        if (!vcycle(d, tl, R, r_nxt, p_new, r_nxt, sz, buf)) return;
         {
             float4 a = total(d.partials, n, buf);
             if (threadIdx.x == 0) {
@@ -735,10 +774,22 @@ __global__ void __launch_bounds__(NT) k_mgpcg(DevScene d, int second, int scale_
     }
 }
 
-int pressure_blocks_max(int device) {
+size_t pressure_smem(const Levels& lv) {
+    int T = lv.off[lv.n - 1] + lv.w[lv.n - 1] * lv.h[lv.n - 1] - lv.off[lv.tail];
+    return (size_t)T * (sizeof(float4) + 2 * sizeof(float2) + sizeof(float));
+}
+
+int pressure_blocks_max(int device, size_t smem) {
     int sms = 0, per = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_mgpcg, NT, 0);
+    // Opt in to the dynamic shared memory the largest tank so far needs (static + dynamic
+    // above 48 KB needs it; the attribute belongs to the kernel, shared by every sim).
+    static size_t opted = 0;
+    if (smem > opted) {
+        cudaFuncSetAttribute(k_mgpcg, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        opted = smem;
+    }
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_mgpcg, NT, smem);
     return sms * per;
 }
 
@@ -747,7 +798,7 @@ cudaError_t launch_pressure(const DevScene& d, const LaunchCfg& cfg, cudaStream_
     cudaMemsetAsync(&d.K->bar_count, 0, sizeof(uint32_t), st);
     int second = 0, scale_mode = 0;
     void* args[] = {(void*)&d, &second, &scale_mode};
-    return cudaLaunchCooperativeKernel((const void*)k_mgpcg, dim3(cfg.mg_blocks), dim3(NT), args, 0, st);
+    return cudaLaunchCooperativeKernel((const void*)k_mgpcg, dim3(cfg.mg_blocks), dim3(NT), args, pressure_smem(d.lv), st);
 }
 
 }  // namespace sprout

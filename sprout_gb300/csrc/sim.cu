@@ -12,6 +12,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <new>
@@ -194,8 +195,14 @@ struct SproutSim {
 #undef A
         std::vector<float> nt(nc, NO_TEMP);
         CUDA_TRY(cudaMemcpy(solid_t, nt.data(), nc * sizeof(float), cudaMemcpyHostToDevice));
-        int mx = pressure_blocks_max(device);
+        int mx = pressure_blocks_max(device, pressure_smem(d.lv));
         cfg.mg_blocks = std::max(1, std::min(d.nwg, mx));
+        // SPROUT_MG_BLOCKS: a tuning override of the persistent kernel's block count
+        // (at most what fits on the device at once).
+        if (const char* e = std::getenv("SPROUT_MG_BLOCKS")) {
+            int want = std::atoi(e);
+            if (want > 0) cfg.mg_blocks = std::max(1, std::min(want, mx));
+        }
         CUDA_TRY(cudaDeviceSynchronize());
         return SPROUT_OK;
     }
