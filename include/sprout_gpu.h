@@ -160,6 +160,31 @@ int sprout_sim_profile(SproutSim* sim, uint32_t substeps, float* ms);
  * ms[4] pressure solve, ms[5] projection. n >= 6. Blocking. */
 int sprout_sim_profile_passes(SproutSim* sim, float* ms, uint32_t n);
 
+/* ---- a pressure solve that allocates nothing ------------------------------------------
+ * No counterpart in the reference: an addition for callers that cannot allocate device
+ * memory (a host whose allocator owns the whole device, a path that must not allocate
+ * while it runs, an FFI host with a fixed memory budget). It runs the engine's pressure
+ * solve (the same kernel as a substep's) on a system the caller holds on the device:
+ * mga, mgd, rhs and x are device pointers, w x h cells, laid out as the engine's fields of
+ * those names (mga 4 floats per cell: couplings to the left, right, bottom, top neighbour;
+ * mgd the diagonal, 0 where the cell is no unknown; rhs 2 floats per cell: pressure and
+ * density-correction right-hand sides; x 2 floats per cell, the starting guess on entry
+ * and the solution on return, zeroed where the cell is no unknown).
+ * All scratch (multigrid hierarchy, Krylov vectors, the solve's scalars) lives in one
+ * fixed device array of about 16 MB inside the library, which every GPU that loads it
+ * holds until the process exits; grids above 147,456 cells (512 x 288) are refused with
+ * SPROUT_E_CAPACITY. No cudaMalloc, cudaFree or allocating routine is called.
+ * The first call on each device looks up the array's device address (with that device
+ * current); make that first call before any stream capture. Every call shares the array
+ * and starts from cleared scratch, so calls whose work overlaps on the GPU (different
+ * streams, several host threads) race: serialise them. `stream` is a cudaStream_t (NULL:
+ * the default stream). iters_out (2 values) and residual_out may be NULL; if either is
+ * given the call waits for the solve and reports its iterations and |r|/|b|. */
+int sprout_pressure_solve_static(uint32_t w, uint32_t h, const float* mga, const float* mgd,
+                                 const float* rhs, float* x, float tol_p, float tol_psi,
+                                 uint32_t max_iters, void* stream, uint32_t* iters_out,
+                                 float* residual_out);
+
 #ifdef __cplusplus
 }
 #endif

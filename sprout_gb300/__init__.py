@@ -39,7 +39,7 @@ EXPORTS = [
     "sprout_sim_reset", "sprout_sim_step", "sprout_sim_step_blocking", "sprout_sim_advance_blocking",
     "sprout_sim_sync", "sprout_sim_download_particles", "sprout_sim_download_pressure",
     "sprout_sim_download_field", "sprout_sim_stats", "sprout_sim_device_bytes", "sprout_sim_profile",
-    "sprout_sim_profile_passes",
+    "sprout_sim_profile_passes", "sprout_pressure_solve_static",
 ]
 
 STAGES = ["advance", "sort", "p2g", "grid", "pressure", "project"]
@@ -120,6 +120,8 @@ def lib() -> C.CDLL:
         "sprout_sim_device_bytes": ([V, P(C.c_size_t)], C.c_int),
         "sprout_sim_profile": ([V, C.c_uint32, P(C.c_float)], C.c_int),
         "sprout_sim_profile_passes": ([V, P(C.c_float), C.c_uint32], C.c_int),
+        "sprout_pressure_solve_static": ([C.c_uint32, C.c_uint32, V, V, V, V, C.c_float, C.c_float, C.c_uint32, V,
+                                          P(C.c_uint32), P(C.c_float)], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -294,3 +296,14 @@ class FluidSim:
         b = C.c_size_t()
         _check(lib().sprout_sim_device_bytes(self._h, C.byref(b)))
         return b.value
+
+
+def pressure_solve_static(w: int, h: int, mga_ptr: int, mgd_ptr: int, rhs_ptr: int, x_ptr: int, tol_p: float,
+                          tol_psi: float, max_iters: int = 60, stream: int | None = None):
+    """The pressure solve on a system held on the device, using no allocation (device pointers
+    in; see sprout_pressure_solve_static in include/sprout_gpu.h). Returns (iterations, |r|/|b|)."""
+    iters = (C.c_uint32 * 2)()
+    res = C.c_float()
+    _check(lib().sprout_pressure_solve_static(w, h, mga_ptr, mgd_ptr, rhs_ptr, x_ptr, tol_p, tol_psi, max_iters, stream,
+                                              iters, C.byref(res)))
+    return list(iters), res.value

@@ -802,3 +802,216 @@ cudaError_t launch_pressure(const DevScene& d, const LaunchCfg& cfg, cudaStream_
 }
 
 }  // namespace sprout
+
+namespace sprout {
+
+// ---- the pressure solve on caller buffers, with no allocation ----------------------------
+//
+// For callers that cannot allocate device memory themselves or through this library: code
+// running where cudaMalloc is unavailable or forbidden (a host whose allocator owns the whole
+// device, a capture-time or real-time path that must not allocate, an FFI host with a fixed
+// memory budget). The multigrid hierarchy, the Krylov vectors and the solve's scalars live
+// in one file-scope device array of fixed size, which every GPU that loads this library
+// holds until the process exits.
+
+constexpr int kStaticMaxCells = 512 * 288;   // the largest grid the array holds (147,456 cells)
+constexpr int kStaticMaxLevels = kMaxLevels;
+
+// Byte layout of the array for kStaticMaxCells (every level of the hierarchy adds at most a
+// third again: 4/3 n + one cell per level).
+constexpr size_t kStaticTotal = (size_t)kStaticMaxCells * 4 / 3 + 64;
+constexpr size_t kStaticTiles = (size_t)kStaticMaxCells / 256 * 2 + 256;
+constexpr size_t align256(size_t b) { return (b + 255) / 256 * 256; }
+constexpr size_t kStaticBytes =
+    align256(sizeof(DevParams)) + align256(sizeof(StepState)) + align256(sizeof(SolveState)) +
+    align256((size_t)kStaticMaxCells * sizeof(float4)) +          // rhs as the engine lays it out
+    align256((size_t)kStaticMaxCells * sizeof(float)) +           // viscous part of the warm start
+    align256(kStaticTiles * sizeof(uint32_t)) +                   // tile flags of every level
+    align256(2 * ((size_t)kStaticMaxCells / 256 + 64) * sizeof(float4)) +   // per-tile partial sums
+    align256(kStaticTotal * sizeof(float4)) + align256(kStaticTotal * sizeof(float)) +
+    3 * align256(kStaticTotal * sizeof(float2)) + 4 * align256((size_t)kStaticMaxCells * sizeof(float2));
+
+static __device__ __align__(256) unsigned char g_solve_scratch[kStaticBytes];
+
+namespace {
+
+Levels static_levels(int w, int h) {
+    Levels L;
+    L.w[0] = w;
+    L.h[0] = h;
+    L.n = 1;
+    while (L.w[L.n - 1] * L.h[L.n - 1] > 4 && L.n < kStaticMaxLevels) {
+        L.w[L.n] = (L.w[L.n - 1] + 1) / 2;
+        L.h[L.n] = (L.h[L.n - 1] + 1) / 2;
+        L.n++;
+    }
+    int total = 0;
+    for (int l = 0; l < L.n; l++) {
+        L.off[l] = total;
+        total += L.w[l] * L.h[l];
+    }
+    L.total = total;
+    int tail = L.n - 1;
+    for (int l = 1; l < L.n; l++)
+        if (L.w[l] * L.h[l] <= 1500) { tail = l; break; }
+    L.tail = tail < 1 ? 1 : (tail > L.n - 1 ? L.n - 1 : tail);
+    int tiles = 0;
+    for (int l = 0; l <= L.tail; l++) {
+        L.toff[l] = tiles;
+        tiles += ((L.w[l] + 15) / 16) * ((L.h[l] + 15) / 16);
+    }
+    L.tiles = tiles;
+    return L;
+}
+
+// Prepares a solve in the array: the level-0 matrix and right-hand side copied in, every
+// coarse matrix and tile flag cleared (a call starts as the first solve of a fresh tank),
+// the level-0 tile flags from the diagonal, the scalars reset.
+__global__ void k_static_prep(DevScene d, const float4* mga, const float* mgd, const float2* rhs, float tol_p,
+                              float tol_psi, uint32_t max_iters) {
+    const int n0 = d.W * d.H;
+    const int stride = gridDim.x * blockDim.x;
+    const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
+    for (int i = t0; i < d.lv.total; i += stride) {
+        if (i < n0) {
+            d.mga[i] = mga[i];
+            d.mgd[i] = mgd[i];
+            float2 b = rhs[i];
+            d.prhs[i] = make_float4(b.x, b.y, 0.0f, 0.0f);
+            d.p2keep[i] = 0.0f;
+        } else {
+            d.mga[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            d.mgd[i] = 0.0f;
+        }
+    }
+    const int tw = (d.W + 15) / 16, th = (d.H + 15) / 16;
+    for (int t = t0; t < d.lv.tiles; t += stride) {
+        uint32_t on = 0u;
+        if (t < tw * th) {
+            const int x0 = (t % tw) * 16, y0 = (t / tw) * 16;
+            for (int y = y0; y < y0 + 16 && y < d.H && !on; y++)
+                for (int x = x0; x < x0 + 16 && x < d.W; x++)
+                    if (mgd[y * d.W + x] > 0.0f) { on = 1u; break; }
+        }
+        d.ptile[t] = on;
+    }
+    if (t0 == 0) {
+        DevParams* P = const_cast<DevParams*>(d.P);
+        P->tol[0] = tol_p;
+        P->tol[1] = tol_psi;
+        P->pressure_max_iters = max_iters;
+        d.S->dt = 1.0f;
+        d.S->dt_prev = 1.0f;
+        SolveState* K = d.K;
+        unsigned char* k = reinterpret_cast<unsigned char*>(K);
+        for (size_t b = 0; b < sizeof(SolveState); b++) k[b] = 0;
+    }
+}
+
+struct StaticSlot {
+    int ready;
+    unsigned char* base;
+};
+StaticSlot g_slots[64];
+
+}  // namespace
+
+void sprout_internal_set_error(const char* msg);
+
+}  // namespace sprout
+
+extern "C" int sprout_pressure_solve_static(uint32_t w, uint32_t h, const float* mga, const float* mgd, const float* rhs,
+                                            float* x, float tol_p, float tol_psi, uint32_t max_iters, void* stream,
+                                            uint32_t* iters_out, float* residual_out) {
+    using namespace sprout;
+    if (!mga || !mgd || !rhs || !x) {
+        sprout_internal_set_error("null argument");
+        return -1;
+    }
+    if (w < 16 || h < 16 || (size_t)w * h > (size_t)kStaticMaxCells) {
+        sprout_internal_set_error("grid outside 16 x 16 .. 147,456 cells, the most the fixed solve array holds");
+        return -3;
+    }
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+        sprout_internal_set_error("no current CUDA device");
+        return -6;
+    }
+    StaticSlot& slot = g_slots[dev];
+    if (!slot.ready) {
+        // With this device current: the array's device address (its host-side name is only
+        // a stand-in). Done on the first call on each device.
+        void* ptr = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&ptr, g_solve_scratch);
+        if (e != cudaSuccess || ptr == nullptr) {
+            sprout_internal_set_error(cudaGetErrorString(e));
+            return -6;
+        }
+        slot.base = static_cast<unsigned char*>(ptr);
+        slot.ready = 1;
+    }
+    const Levels L = static_levels((int)w, (int)h);
+    DevScene d{};
+    d.W = (int)w;
+    d.H = (int)h;
+    d.ncell = (int)(w * h);
+    d.lv = L;
+    d.nwg = (int)(((w + 15) / 16) * ((h + 15) / 16));
+    unsigned char* p = slot.base;
+    auto take = [&](size_t bytes) { unsigned char* q = p; p += align256(bytes); return q; };
+    DevParams* P = reinterpret_cast<DevParams*>(take(sizeof(DevParams)));
+    d.P = P;
+    d.S = reinterpret_cast<StepState*>(take(sizeof(StepState)));
+    d.K = reinterpret_cast<SolveState*>(take(sizeof(SolveState)));
+    d.prhs = reinterpret_cast<float4*>(take((size_t)kStaticMaxCells * sizeof(float4)));
+    d.p2keep = reinterpret_cast<float*>(take((size_t)kStaticMaxCells * sizeof(float)));
+    d.ptile = reinterpret_cast<uint32_t*>(take(kStaticTiles * sizeof(uint32_t)));
+    d.partials = reinterpret_cast<float4*>(take(2 * ((size_t)kStaticMaxCells / 256 + 64) * sizeof(float4)));
+    d.mga = reinterpret_cast<float4*>(take(kStaticTotal * sizeof(float4)));
+    d.mgd = reinterpret_cast<float*>(take(kStaticTotal * sizeof(float)));
+    d.mgx = reinterpret_cast<float2*>(take(kStaticTotal * sizeof(float2)));
+    d.mgz = reinterpret_cast<float2*>(take(kStaticTotal * sizeof(float2)));
+    d.mgr = reinterpret_cast<float2*>(take(kStaticTotal * sizeof(float2)));
+    d.mgr2 = reinterpret_cast<float2*>(take((size_t)kStaticMaxCells * sizeof(float2)));
+    d.cgp = reinterpret_cast<float2*>(take((size_t)kStaticMaxCells * sizeof(float2)));
+    d.cgp2 = reinterpret_cast<float2*>(take((size_t)kStaticMaxCells * sizeof(float2)));
+    d.cgq = reinterpret_cast<float2*>(take((size_t)kStaticMaxCells * sizeof(float2)));
+    d.pres = reinterpret_cast<float2*>(x);
+    if ((size_t)(p - slot.base) > kStaticBytes || (size_t)L.total > kStaticTotal || (size_t)L.tiles > kStaticTiles) {
+        sprout_internal_set_error("fixed solve array layout overflow");
+        return -3;
+    }
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    k_static_prep<<<128, 256, 0, st>>>(d, reinterpret_cast<const float4*>(mga), mgd, reinterpret_cast<const float2*>(rhs),
+                                       tol_p, tol_psi, max_iters);
+    const size_t smem = pressure_smem(L);
+    int blocks = pressure_blocks_max(dev, smem);
+    if (blocks > d.nwg) blocks = d.nwg;
+    if (blocks < 1) blocks = 1;
+    int second = 0, scale_mode = 0;
+    void* args[] = {(void*)&d, &second, &scale_mode};
+    cudaError_t e = cudaLaunchCooperativeKernel((const void*)k_mgpcg, dim3(blocks), dim3(NT), args, smem, st);
+    if (e != cudaSuccess) {
+        sprout_internal_set_error(cudaGetErrorString(e));
+        return -6;
+    }
+    if (iters_out || residual_out) {
+        SolveState K;
+        e = cudaMemcpyAsync(&K, d.K, sizeof K, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) {
+            sprout_internal_set_error(cudaGetErrorString(e));
+            return -6;
+        }
+        if (K.error) {
+            sprout_internal_set_error("a bounded device-side wait ran out (grid barrier of the pressure solve)");
+            return -5;
+        }
+        if (iters_out) {
+            iters_out[0] = K.p_iters[0];
+            iters_out[1] = K.p_iters[1];
+        }
+        if (residual_out) *residual_out = K.p_bb[0] > 0.0f ? sqrtf(K.p_rr[0] / K.p_bb[0]) : 0.0f;
+    }
+    return 0;
+}

@@ -75,6 +75,11 @@ Levels make_levels(int w, int h) {
 
 }  // namespace
 
+namespace sprout {
+// Lets other translation units of the library report through sprout_last_error().
+void sprout_internal_set_error(const char* msg) { g_error = msg ? msg : ""; }
+}  // namespace sprout
+
 struct SproutParams {
     SimParams p;
 };
