@@ -137,6 +137,10 @@ def lib() -> C.CDLL:
         L.osim_field.argtypes = [C.c_void_p, C.c_char_p, C.c_void_p, C.c_size_t]
         L.osim_field.restype = C.c_long
         L.osim_stats.argtypes = [C.c_void_p, P(OStats)]
+        L.osim_visc_operator.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        L.osim_visc_operator.restype = C.c_long
+        L.osim_vmg_apply.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
+        L.osim_vmg_apply.restype = C.c_long
         L.osim_set_threads.argtypes = [C.c_int]
         L.o_expf.argtypes = [C.c_float]
         L.o_expf.restype = C.c_float
@@ -235,6 +239,23 @@ class OracleSim:
         buf = np.zeros(n // np.dtype(dtype).itemsize, dtype)
         lib().osim_field(self.h_, name.encode(), buf.ctypes.data, n)
         return buf
+
+    def visc_operator(self, x: np.ndarray):
+        """The implicit viscosity's level-0 matrix and its matrix-free form applied to x
+        (float32, 2 per cell): (unknown count, A_assembled x, A_matrix_free x)."""
+        x = np.ascontiguousarray(x, np.float32)
+        y0 = np.zeros_like(x)
+        y1 = np.zeros_like(x)
+        n = lib().osim_visc_operator(self.h_, x.ctypes.data, y0.ctypes.data, y1.ctypes.data)
+        return n, y0, y1
+
+    def vmg_apply(self, level: int, x: np.ndarray) -> np.ndarray:
+        """The assembled viscosity matrix of multigrid `level` applied to x (2 per cell)."""
+        x = np.ascontiguousarray(x, np.float32)
+        y = np.zeros_like(x)
+        if lib().osim_vmg_apply(self.h_, level, x.ctypes.data, y.ctypes.data) < 0:
+            raise ValueError(level)
+        return y
 
     def stats(self) -> OStats:
         s = OStats()

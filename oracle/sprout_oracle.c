@@ -606,6 +606,9 @@ typedef struct SolveBuf {   /* common.glsl:138-149 */
     uint32_t p_done[2], p_iters[2];
     uint32_t p_it_max, p_unconv, p2_it_max, p2_unconv, solves;
     float p_res_max;
+    float v_rz, v_alpha, v_beta, v_r0, v_rr, v_pq;
+    uint32_t v_done, v_iters, v_it_max, v_unconv;
+    float v_res_max;
 } SolveBuf;
 
 typedef struct Levels {   /* mod.rs:714-753 */
@@ -655,6 +658,11 @@ struct OSim {
     V2 *mgx, *mgz, *mgr, *cgp, *cgp2, *cgq;
     uint32_t* ptile;
     V4* part;
+    /* implicit viscosity (visc*.comp, vmg*.comp) */
+    V2 *vr, *vr2, *vp, *vq, *vq2, *vd, *vaz;
+    V4 *vma, *vmb;
+    V2 *vmd, *vmr, *vmx, *vmz;
+    uint32_t *tiles, *vtile;
     /* scratch for the particle pass */
     struct Scat* scat;
 };
@@ -2142,6 +2150,16 @@ static void k_visc_setup(OSim* s) {
             }
             s->vw[i].x = wc;
             s->vw[i].y = wn;
+            /* the tiles that need the implicit solve (visc_setup.comp:111-120) */
+            V4 me = s->cell[i];
+            if (s->visc_mode == 2 && me.w > 0.0f && dt * me.z / maxf(me.y, 0.05f) >= P_.corr[3]) {
+                int tw = (W + 15) >> 4;
+                for (int b = -1; b <= 1; b++)
+                    for (int a = -1; a <= 1; a++) {
+                        int nx = clampi(cx + a, 0, W - 1), ny = clampi(cy + b, 0, H - 1);
+                        s->tiles[(ny >> 4) * tw + (nx >> 4)] = 1u;
+                    }
+            }
         }
 #pragma omp parallel for schedule(static) num_threads(g_threads)
     for (int i = 0; i < W * H; i++) s->vs[i] = strain_of_vel(s, i, v2(s->vw[i].x, s->vw[i].y));
@@ -2416,7 +2434,7 @@ static V2 up_black(const OSim* s, Lv L, Lv C, int nx, int ny) {
     return v2(sum.x / s->mgd[i], sum.y / s->mgd[i]);
 }
 
-/* work-group sum of reduce.glsl:230-239: the tree over 256 invocations */
+/* work-group sum of reduce.glsl:5-14: the tree over 256 invocations */
 static V4 group_tree(V4 buf[256]) {
     for (int st = 128; st > 0; st >>= 1)
         for (int t = 0; t < st; t++) {
@@ -2884,6 +2902,629 @@ static void k_project(OSim* s) {
 }
 
 /* ------------------------------------------------------------------------------------ */
+/* Implicit viscosity: visc_split, visc_diag, vmg_build, visc_strain, visc_apply mode 0,  */
+/* visc_iter WARM, vmg_down / vmg_up / visc_mgu / visc_mgz, reduce_tail modes 4-13        */
+/* ------------------------------------------------------------------------------------ */
+/* The reference works in 16 x 16 tiles with a shrinking halo recomputed in shared memory
+ * (vmg.glsl:142-147): after h half-sweeps the values in ring >= h of a tile's region are
+ * exactly those of red-black half-sweeps over the whole level. The restatement below
+ * therefore sweeps whole levels; cells of inactive tiles carry zero matrices (visc_diag,
+ * vmg_build clear them) and so stay zero, as they do in the reference. */
+
+static inline int in_grid_c(const OSim* s, int x, int y) { return x >= 0 && y >= 0 && x < s->W && y < s->H; }
+static inline int interior_c(const OSim* s, int x, int y) { return x >= 1 && y >= 1 && x < s->W - 1 && y < s->H - 1; }
+static inline uint32_t tile_of_c(const OSim* s, int x, int y) { return (uint32_t)((y >> 4) * ((s->W + 15) >> 4) + (x >> 4)); }
+static inline int tile_active_c(const OSim* s, int x, int y) { return s->tiles[tile_of_c(s, x, y)] != 0u; }
+
+/* visc_split.comp: explicit step in the inactive tiles */
+static void k_visc_split(OSim* s) {
+    int W = s->W, H = s->H;
+    for (int cy = 1; cy < H - 1; cy++)
+        for (int cx = 1; cx < W - 1; cx++) {
+            if (tile_active_c(s, cx, cy)) continue;
+            int i = cidx(s, cx, cy);
+            V2 g = gts(s, i);
+            V4 cf = s->coef[i];
+            if (live_u(s, i)) s->vel[i].x -= g.x / cf.z;
+            if (live_v(s, i)) s->vel[i].y -= g.y / cf.w;
+        }
+}
+
+static inline V2 wts(const OSim* s, int x, int y, int i) {
+    return s->tiles[tile_of_c(s, x, y)] != 0u ? v2(s->vw[i].x, s->vw[i].y) : v2(0.0f, 0.0f);
+}
+static inline int unk_u(const OSim* s, int x, int y) { return interior_c(s, x, y) && s->tiles[tile_of_c(s, x, y)] != 0u && live_u(s, cidx(s, x, y)); }
+static inline int unk_v(const OSim* s, int x, int y) { return interior_c(s, x, y) && s->tiles[tile_of_c(s, x, y)] != 0u && live_v(s, cidx(s, x, y)); }
+
+/* visc_diag.comp:23-52 */
+static void couplings(const OSim* s, int cx, int cy, int i, V4* a, V4* b) {
+    int W = s->W;
+    int u = unk_u(s, cx, cy), v = unk_v(s, cx, cy);
+    *a = v4(0, 0, 0, 0);
+    *b = v4(0, 0, 0, 0);
+    if (u && unk_u(s, cx - 1, cy)) a->x = -wts(s, cx - 1, cy, i - 1).x;
+    if (v && unk_v(s, cx, cy - 1)) a->w = -wts(s, cx, cy - 1, i - W).x;
+    float wn = wts(s, cx, cy, i).y;
+    if (wn > 0.0f) {
+        float ua = u ? (closed_u(s, i - W) ? 1.0f : 0.5f) : 0.0f;
+        float ub = unk_u(s, cx, cy - 1) ? -(closed_u(s, i) ? 1.0f : 0.5f) : 0.0f;
+        float va = v ? (closed_v(s, i - 1) ? 1.0f : 0.5f) : 0.0f;
+        float vb = unk_v(s, cx - 1, cy) ? -(closed_v(s, i) ? 1.0f : 0.5f) : 0.0f;
+        a->y = wn * ua * ub;
+        a->z = wn * va * vb;
+        b->x = wn * ua * va;
+        b->y = wn * ua * vb;
+    }
+    float wu = wts(s, cx, cy + 1, i + W).y;
+    if (wu > 0.0f && u) {
+        float ub = -(closed_u(s, i + W) ? 1.0f : 0.5f);
+        float va = unk_v(s, cx, cy + 1) ? (closed_v(s, i + W - 1) ? 1.0f : 0.5f) : 0.0f;
+        float vb = unk_v(s, cx - 1, cy + 1) ? -(closed_v(s, i + W) ? 1.0f : 0.5f) : 0.0f;
+        b->z = wu * ub * va;
+        b->w = wu * ub * vb;
+    }
+}
+
+/* visc_diag.comp:56-119 */
+static void k_visc_diag(OSim* s, int warm, int mg) {
+    int W = s->W, H = s->H;
+    int tw = (W + 15) >> 4, th = (H + 15) >> 4;
+    float ratio = s->S.dt / s->S.dt_prev;
+    /* vw.zw and the warm start first: the couplings read vw.xy only */
+    uint32_t* was = (uint32_t*)malloc((size_t)tw * th * sizeof(uint32_t));
+    for (int t = 0; t < tw * th; t++) {
+        was[t] = s->vtile[t];
+        if (mg) s->vtile[t] = s->tiles[t];
+    }
+    V4* outw = (V4*)malloc((size_t)W * H * sizeof(V4));
+    for (int cy = 0; cy < H; cy++)
+        for (int cx = 0; cx < W; cx++) {
+            int i = cidx(s, cx, cy);
+            int on = tile_active_c(s, cx, cy);
+            V2 d = v2(1.0f, 1.0f);
+            if (interior_c(s, cx, cy)) {
+                V4 cf = s->coef[i];
+                V2 me = wts(s, cx, cy, i);
+                if (live_u(s, i)) {
+                    float c1 = closed_u(s, i - W) ? 1.0f : 0.5f, c2 = closed_u(s, i + W) ? 1.0f : 0.5f;
+                    d.x = cf.z + wts(s, cx - 1, cy, i - 1).x + me.x + me.y * c1 * c1 + wts(s, cx, cy + 1, i + W).y * c2 * c2;
+                }
+                if (live_v(s, i)) {
+                    float d1 = closed_v(s, i - 1) ? 1.0f : 0.5f, d2 = closed_v(s, i + 1) ? 1.0f : 0.5f;
+                    d.y = cf.w + wts(s, cx, cy - 1, i - W).x + me.x + me.y * d1 * d1 + wts(s, cx + 1, cy, i + 1).y * d2 * d2;
+                }
+            }
+            V4 o = s->vw[i];
+            o.z = d.x;
+            o.w = d.y;
+            V2 dv = v2(0.0f, 0.0f);
+            if (warm && on && interior_c(s, cx, cy)) {
+                dv = v2(s->vd[i].x * ratio * (live_u(s, i) ? 1.0f : 0.0f), s->vd[i].y * ratio * (live_v(s, i) ? 1.0f : 0.0f));
+            }
+            s->vd[i] = dv;
+            if (!on) {
+                o.x = 0.0f;
+                o.y = 0.0f;
+            }
+            outw[i] = o;
+        }
+    /* the level-0 matrix (reads vw.xy through wts, which is zero in inactive tiles already) */
+    if (mg) {
+        for (int cy = 0; cy < H; cy++)
+            for (int cx = 0; cx < W; cx++) {
+                int i = cidx(s, cx, cy);
+                int on = tile_active_c(s, cx, cy);
+                if (!(on || was[tile_of_c(s, cx, cy)] != 0u)) continue;
+                V4 a = v4(0, 0, 0, 0), b = v4(0, 0, 0, 0);
+                V2 dm = v2(0.0f, 0.0f);
+                if (on && interior_c(s, cx, cy)) {
+                    couplings(s, cx, cy, i, &a, &b);
+                    dm = v2(outw[i].z * (live_u(s, i) ? 1.0f : 0.0f), outw[i].w * (live_v(s, i) ? 1.0f : 0.0f));
+                }
+                if (!on) {
+                    s->vmz[i] = v2(0, 0);
+                    s->vaz[i] = v2(0, 0);
+                    s->vr2[i] = v2(0, 0);
+                    s->vq2[i] = v2(0, 0);
+                }
+                s->vma[i] = a;
+                s->vmb[i] = b;
+                s->vmd[i] = dm;
+            }
+    }
+    for (int i = 0; i < W * H; i++) {
+        int cx = i % W, cy = i / W;
+        s->vw[i] = outw[i];
+        if (!tile_active_c(s, cx, cy)) {
+            s->vs[i] = v4(0, 0, 0, 0);
+            s->vr[i] = v2(0, 0);
+            s->vp[i] = v2(0, 0);
+            s->vq[i] = v2(0, 0);
+        }
+    }
+    free(outw);
+    free(was);
+}
+
+/* vmg_build.comp: viscosity level l from level l - 1 */
+static void k_vmg_build(OSim* s, int l) {
+    Lv F = lev(s, l - 1), C = lev(s, l);
+    int tfx = (F.w + 15) >> 4, tfy = (F.h + 15) >> 4;
+    int tcx = (C.w + 15) >> 4, tcy = (C.h + 15) >> 4;
+    static const int UVX[4] = {0, -1, 0, -1}, UVY[4] = {0, 0, 1, 1};
+    for (int ty = 0; ty < tcy; ty++)
+        for (int tx = 0; tx < tcx; tx++) {
+            uint32_t on = 0u;
+            for (int k = 0; k < 4; k++) {
+                int fx = 2 * tx + (k & 1), fy = 2 * ty + (k >> 1);
+                if (fx < tfx && fy < tfy) on |= (l - 1 == 0) ? s->tiles[fy * tfx + fx] : s->vtile[F.toff + fy * tfx + fx];
+            }
+            uint32_t slot = (uint32_t)C.toff + (uint32_t)(ty * tcx + tx);
+            uint32_t was = s->vtile[slot];
+            s->vtile[slot] = on != 0u ? 1u : 0u;
+            uint32_t state = (on != 0u ? 1u : 0u) | (was != 0u ? 2u : 0u);
+            if (state == 0u) continue;
+            for (int ly = 0; ly < 16; ly++)
+                for (int lx = 0; lx < 16; lx++) {
+                    int ccx = tx * 16 + lx, ccy = ty * 16 + ly;
+                    if (!l_inside(C, ccx, ccy)) continue;
+                    int o = l_at(C, ccx, ccy);
+                    if ((state & 1u) == 0u) {
+                        s->vma[o] = v4(0, 0, 0, 0);
+                        s->vmb[o] = v4(0, 0, 0, 0);
+                        s->vmd[o] = v2(0, 0);
+                        continue;
+                    }
+                    V2 D = v2(0, 0);
+                    V4 A = v4(0, 0, 0, 0), B = v4(0, 0, 0, 0);
+                    for (int k = 0; k < 4; k++) {
+                        int abx = k & 1, aby = k >> 1;
+                        int fx = 2 * ccx + abx, fy = 2 * ccy + aby;
+                        if (!l_inside(F, fx, fy)) continue;
+                        int i = l_at(F, fx, fy);
+                        V4 a = s->vma[i], b = s->vmb[i];
+                        D.x += s->vmd[i].x;
+                        D.y += s->vmd[i].y;
+                        if (abx == 1) { D.x += 2.0f * a.x; D.y += 2.0f * a.z; }
+                        else { A.x += a.x; A.z += a.z; }
+                        if (aby == 1) { D.x += 2.0f * a.y; D.y += 2.0f * a.w; }
+                        else { A.y += a.y; A.w += a.w; }
+                        for (int m = 0; m < 4; m++) {
+                            int rx = ((fx + UVX[m]) >> 1) - ccx, ry = ((fy + UVY[m]) >> 1) - ccy;
+                            int sl = (rx == 0 ? 0 : 1) + (ry == 0 ? 0 : 2);
+                            float bm = m == 0 ? b.x : m == 1 ? b.y : m == 2 ? b.z : b.w;
+                            if (sl == 0) B.x += bm; else if (sl == 1) B.y += bm; else if (sl == 2) B.z += bm; else B.w += bm;
+                        }
+                    }
+                    s->vma[o] = A;
+                    s->vmb[o] = B;
+                    s->vmd[o] = v2(maxf(D.x, 0.0f), maxf(D.y, 0.0f));
+                }
+        }
+}
+
+/* visc_strain.comp: strain of the current velocity in the active tiles */
+static void k_visc_strain(OSim* s) {
+    for (int cy = 0; cy < s->H; cy++)
+        for (int cx = 0; cx < s->W; cx++) {
+            if (!tile_active_c(s, cx, cy)) continue;
+            int i = cidx(s, cx, cy);
+            s->vs[i] = strain_of_vel(s, i, v2(s->vw[i].x, s->vw[i].y));
+        }
+}
+
+/* per-tile partial sums over level-0 tiles (group_sum, reduce.glsl), inactive tiles zero */
+typedef V4 (*CellDot)(OSim* s, int cx, int cy, void* ctx);
+static void tile_partials(OSim* s, V4* part, CellDot f, void* ctx) {
+    int tw = (s->W + 15) >> 4, th = (s->H + 15) >> 4;
+    for (int ty = 0; ty < th; ty++)
+        for (int tx = 0; tx < tw; tx++) {
+            int slot = ty * tw + tx;
+            if (s->tiles[slot] == 0u) {
+                part[slot] = v4(0, 0, 0, 0);
+                continue;
+            }
+            V4 buf[256];
+            for (int ly = 0; ly < 16; ly++)
+                for (int lx = 0; lx < 16; lx++) buf[ly * 16 + lx] = f(s, tx * 16 + lx, ty * 16 + ly, ctx);
+            part[slot] = group_tree(buf);
+        }
+}
+
+static inline float dot2(V2 a, V2 b) { return a.x * b.x + a.y * b.y; }
+
+/* visc_apply.comp mode 0 at one cell: r = -G^T W G u*, z = r / diag */
+static V4 cell_visc_start(OSim* s, int cx, int cy, void* ctx) {
+    (void)ctx;
+    if (!in_grid_c(s, cx, cy)) return v4(0, 0, 0, 0);
+    int i = cidx(s, cx, cy);
+    if (interior_c(s, cx, cy)) {
+        V2 g = gts(s, i);
+        V2 live = v2(live_u(s, i) ? 1.0f : 0.0f, live_v(s, i) ? 1.0f : 0.0f);
+        V2 diag = v2(s->vw[i].z, s->vw[i].w);
+        V2 r = v2(-g.x * live.x, -g.y * live.y);
+        V2 z = v2(r.x / diag.x, r.y / diag.y);
+        s->vr[i] = r;
+        s->vp[i] = z;
+        return v4(dot2(r, z), dot2(r, r), 0.0f, 0.0f);
+    }
+    s->vr[i] = v2(0, 0);
+    s->vp[i] = v2(0, 0);
+    return v4(0, 0, 0, 0);
+}
+
+/* visc_iter.comp WARM: step to u* + d and r -= A d; p and its strain from vd */
+static inline V2 warm_dir(const OSim* s, int x, int y) {
+    if (!in_grid_c(s, x, y) || !interior_c(s, x, y)) return v2(0, 0);
+    return s->vd[cidx(s, x, y)];
+}
+static inline float pU(const OSim* s, int x, int y, int i) { return live_u(s, i) ? warm_dir(s, x, y).x : 0.0f; }
+static inline float pV(const OSim* s, int x, int y, int i) { return live_v(s, i) ? warm_dir(s, x, y).y : 0.0f; }
+static V4 strain_of_dir(const OSim* s, int cx, int cy) {
+    if (!in_grid_c(s, cx, cy)) return v4(0, 0, 0, 0);
+    int i = cidx(s, cx, cy), W = s->W;
+    V4 o = v4(0, 0, 0, 0);
+    V4 w = s->vw[i];
+    if (w.x > 0.0f) {
+        o.x = w.x * (pU(s, cx + 1, cy, i + 1) - pU(s, cx, cy, i));
+        o.y = w.x * (pV(s, cx, cy + 1, i + W) - pV(s, cx, cy, i));
+    }
+    if (w.y > 0.0f) {
+        float ua = pU(s, cx, cy, i), ub = pU(s, cx, cy - 1, i - W), va = pV(s, cx, cy, i), vb = pV(s, cx - 1, cy, i - 1);
+        if (closed_u(s, i) && live_u(s, i - W)) ua = -ub;
+        if (closed_u(s, i - W) && live_u(s, i)) ub = -ua;
+        if (closed_v(s, i) && live_v(s, i - 1)) va = -vb;
+        if (closed_v(s, i - 1) && live_v(s, i)) vb = -va;
+        o.z = w.y * 0.5f * ((ua - ub) + (va - vb));
+    }
+    return o;
+}
+static V4 cell_visc_warm(OSim* s, int cx, int cy, void* ctx) {
+    (void)ctx;
+    if (!in_grid_c(s, cx, cy) || !interior_c(s, cx, cy)) return v4(0, 0, 0, 0);
+    int i = cidx(s, cx, cy), W = s->W;
+    V2 g = v2(0, 0);
+    if (live_u(s, i)) {
+        float c1 = closed_u(s, i - W) ? 1.0f : 0.5f, c2 = closed_u(s, i + W) ? -1.0f : -0.5f;
+        V4 sl = strain_of_dir(s, cx - 1, cy), sc = strain_of_dir(s, cx, cy), su = strain_of_dir(s, cx, cy + 1);
+        g.x = sl.x - sc.x + sc.z * c1 + su.z * c2;
+    }
+    if (live_v(s, i)) {
+        float d1 = closed_v(s, i - 1) ? 1.0f : 0.5f, d2 = closed_v(s, i + 1) ? -1.0f : -0.5f;
+        V4 sd = strain_of_dir(s, cx, cy - 1), sc = strain_of_dir(s, cx, cy), sr = strain_of_dir(s, cx + 1, cy);
+        g.y = sd.y - sc.y + sc.z * d1 + sr.z * d2;
+    }
+    V2 live = v2(live_u(s, i) ? 1.0f : 0.0f, live_v(s, i) ? 1.0f : 0.0f);
+    V4 cf = s->coef[i];
+    V2 dd = warm_dir(s, cx, cy);
+    V2 d = v2(dd.x * live.x, dd.y * live.y);
+    V2 q = v2((cf.z * d.x + g.x) * live.x, (cf.w * d.y + g.y) * live.y);
+    /* results are written after every cell's inputs were read (the kernel reads vd, vw and
+     * the velocity flags, which the update does not change) */
+    V2* outr = (V2*)ctx;
+    s->vel[i].x += d.x;
+    s->vel[i].y += d.y;
+    V2 r = v2(s->vr[i].x - q.x, s->vr[i].y - q.y);
+    outr[i] = r;
+    V2 z = v2(r.x / s->vw[i].z, r.y / s->vw[i].w);
+    return v4(dot2(r, z), dot2(r, r), 0.0f, 0.0f);
+}
+
+/* vmg.glsl: the viscosity multigrid on one level, as whole-level sweeps */
+static inline V4 vma_at(const OSim* s, Lv L, int x, int y) { return l_inside(L, x, y) ? s->vma[l_at(L, x, y)] : v4(0, 0, 0, 0); }
+static inline V4 vmb_at(const OSim* s, Lv L, int x, int y) { return l_inside(L, x, y) ? s->vmb[l_at(L, x, y)] : v4(0, 0, 0, 0); }
+static inline V2 vx_at(const V2* X, Lv L, int x, int y) { return l_inside(L, x, y) ? X[y * L.w + x] : v2(0, 0); }
+
+/* offd (vmg.glsl:189-197) of X (level-local array) at (x, y) */
+static V2 voffd(const OSim* s, Lv L, const V2* X, int x, int y) {
+    V4 a = vma_at(s, L, x, y), b = vmb_at(s, L, x, y);
+    V2 xl = vx_at(X, L, x - 1, y), xr = vx_at(X, L, x + 1, y), xd = vx_at(X, L, x, y - 1), xu = vx_at(X, L, x, y + 1);
+    V2 xc = vx_at(X, L, x, y);
+    float u = a.x * xl.x + vma_at(s, L, x + 1, y).x * xr.x + a.y * xd.x + vma_at(s, L, x, y + 1).y * xu.x
+            + b.x * xc.y + b.y * xl.y + b.z * xu.y + b.w * vx_at(X, L, x - 1, y + 1).y;
+    float v = a.z * xl.y + vma_at(s, L, x + 1, y).z * xr.y + a.w * xd.y + vma_at(s, L, x, y + 1).w * xu.y
+            + b.x * xc.x + vmb_at(s, L, x + 1, y).y * xr.x + vmb_at(s, L, x, y - 1).z * xd.x
+            + vmb_at(s, L, x + 1, y - 1).w * vx_at(X, L, x + 1, y - 1).x;
+    return v2(u, v);
+}
+
+/* one half-sweep of one colour over the level: every update reads the values before it */
+static void vhalf_sweep(const OSim* s, Lv L, V2* X, const V2* R, int red) {
+    int n = L.w * L.h;
+    V2* nv = (V2*)malloc((size_t)n * sizeof(V2));
+    for (int t = 0; t < n; t++) {
+        int x = t % L.w, y = t / L.w;
+        if ((((x + y) & 1) == 0) != red) continue;
+        V2 d = s->vmd[L.off + t];
+        V2 o = voffd(s, L, X, x, y);
+        V2 sv = v2(R[t].x - o.x, R[t].y - o.y);
+        nv[t] = v2(d.x > 0.0f ? sv.x / d.x : 0.0f, d.y > 0.0f ? sv.y / d.y : 0.0f);
+    }
+    for (int t = 0; t < n; t++) {
+        int x = t % L.w, y = t / L.w;
+        if ((((x + y) & 1) == 0) == red) X[t] = nv[t];
+    }
+    free(nv);
+}
+
+/* way_down (vmg.glsl:264-287) on level l with right-hand side R: pre-smoothing from zero,
+ * the result to vmx, the residual summed over 2 x 2 aggregates into vmr of level l + 1 */
+static void vmg_down(OSim* s, int l, const V2* R, int coarsest, int halo) {
+    Lv L = lev(s, l);
+    int n = L.w * L.h;
+    V2* X = (V2*)calloc((size_t)n, sizeof(V2));
+    for (int t = 0; t < n; t++) {
+        int x = t % L.w, y = t / L.w;
+        V2 d = s->vmd[L.off + t];
+        V2 xr = v2(d.x > 0.0f ? R[t].x / d.x : 0.0f, d.y > 0.0f ? R[t].y / d.y : 0.0f);
+        X[t] = ((x + y) & 1) == 0 ? xr : v2(0, 0);
+    }
+    for (int h = 1; h < halo; h++) vhalf_sweep(s, L, X, R, (h & 1) == 0);
+    for (int t = 0; t < n; t++) s->vmx[L.off + t] = X[t];
+    if (!coarsest) {
+        Lv C = lev(s, l + 1);
+        V2* res = (V2*)calloc((size_t)n, sizeof(V2));
+        for (int t = 0; t < n; t++) {
+            int x = t % L.w, y = t / L.w;
+            V2 d = s->vmd[L.off + t];
+            V2 o = voffd(s, L, X, x, y);
+            V2 rr = v2(R[t].x - d.x * X[t].x - o.x, R[t].y - d.y * X[t].y - o.y);
+            res[t] = v2(rr.x * (d.x > 0.0f ? 1.0f : 0.0f), rr.y * (d.y > 0.0f ? 1.0f : 0.0f));
+        }
+        for (int cy = 0; cy < C.h; cy++)
+            for (int cx = 0; cx < C.w; cx++) {
+                V2 a = vx_at(res, L, 2 * cx, 2 * cy), b = vx_at(res, L, 2 * cx + 1, 2 * cy);
+                V2 c = vx_at(res, L, 2 * cx, 2 * cy + 1), e = vx_at(res, L, 2 * cx + 1, 2 * cy + 1);
+                s->vmr[l_at(C, cx, cy)] = v2(a.x + b.x + c.x + e.x, a.y + b.y + c.y + e.y);
+            }
+        free(res);
+    }
+    free(X);
+}
+
+/* the way up (vmg_up.comp / visc_mgz.comp): x = vmx + the coarse values, post-smoothing
+ * black then red; result in X (level-local) */
+static void vmg_up_into(OSim* s, int l, const V2* R, int coarse_corr, int halo, V2* X) {
+    Lv L = lev(s, l);
+    int n = L.w * L.h;
+    for (int t = 0; t < n; t++) {
+        int x = t % L.w, y = t / L.w;
+        V2 xv = s->vmx[L.off + t];
+        if (coarse_corr) {
+            Lv C = lev(s, l + 1);
+            V2 zc = s->vmz[l_at(C, x >> 1, y >> 1)];
+            xv = v2(xv.x + zc.x, xv.y + zc.y);
+        }
+        V2 d = s->vmd[L.off + t];
+        X[t] = v2(xv.x * (d.x > 0.0f ? 1.0f : 0.0f), xv.y * (d.y > 0.0f ? 1.0f : 0.0f));
+    }
+    for (int h = 1; h <= halo; h++) vhalf_sweep(s, L, X, R, (h & 1) == 0);
+}
+
+/* the coarse levels of one viscosity V-cycle (record_visc_coarse, mod.rs:2835-2853) */
+static void vmg_coarse(OSim* s, int nlev, int halo) {
+    for (int l = 1; l <= nlev; l++) {
+        Lv L = lev(s, l);
+        vmg_down(s, l, s->vmr + L.off, l == nlev, halo);
+    }
+    for (int l = nlev; l >= 1; l--) {
+        Lv L = lev(s, l);
+        int n = L.w * L.h;
+        V2* X = (V2*)malloc((size_t)n * sizeof(V2));
+        vmg_up_into(s, l, s->vmr + L.off, l != nlev, halo, X);
+        memcpy(s->vmz + L.off, X, (size_t)n * sizeof(V2));
+        free(X);
+    }
+}
+
+/* visc_mgz.comp: the way up on level 0 with A z and the dot products of the solve */
+typedef struct MgzCtx { V2* Z; V2* AZ; const V2* R; const V2* Q; } MgzCtx;
+static V4 cell_mgz(OSim* s, int cx, int cy, void* ctx) {
+    MgzCtx* c = (MgzCtx*)ctx;
+    if (!in_grid_c(s, cx, cy)) return v4(0, 0, 0, 0);
+    int i = cidx(s, cx, cy);
+    V2 z = c->Z[i], az = c->AZ[i];
+    s->vmz[i] = z;
+    s->vaz[i] = az;
+    return v4(dot2(c->R[i], z), dot2(z, az), dot2(z, c->Q[i]), 0.0f);
+}
+static void visc_mgz(OSim* s, const V2* R, const V2* Q, int halo) {
+    int n = s->W * s->H;
+    Lv L0 = lev(s, 0);
+    V2* Z = (V2*)malloc((size_t)n * sizeof(V2));
+    V2* AZ = (V2*)malloc((size_t)n * sizeof(V2));
+    vmg_up_into(s, 0, R, 1, halo, Z);
+    for (int t = 0; t < n; t++) {
+        int x = t % s->W, y = t / s->W;
+        V2 d = s->vmd[t];
+        V2 o = voffd(s, L0, Z, x, y);
+        AZ[t] = v2(d.x * Z[t].x + o.x, d.y * Z[t].y + o.y);
+    }
+    MgzCtx c = {Z, AZ, R, Q};
+    tile_partials(s, s->part, cell_mgz, &c);
+    free(Z);
+    free(AZ);
+}
+
+/* visc_mgu.comp at one cell: p, q, x, r of the iteration, before the way down */
+typedef struct MguCtx { const V2* Rold; const V2* Qold; V2* Rnew; V2* Qnew; } MguCtx;
+static V4 cell_mgu(OSim* s, int cx, int cy, void* ctx) {
+    MguCtx* c = (MguCtx*)ctx;
+    if (!in_grid_c(s, cx, cy)) return v4(0, 0, 0, 0);
+    int i = cidx(s, cx, cy);
+    float a = s->K.v_alpha, b = s->K.v_beta;
+    V2 z = s->vmz[i];
+    V2 p = b == 0.0f ? z : v2(z.x + b * s->vp[i].x, z.y + b * s->vp[i].y);
+    V2 sq = s->vaz[i];
+    V2 q = b == 0.0f ? sq : v2(sq.x + b * c->Qold[i].x, sq.y + b * c->Qold[i].y);
+    V2 r = v2(c->Rold[i].x - a * q.x, c->Rold[i].y - a * q.y);
+    if (interior_c(s, cx, cy)) {
+        if (face_live(s->vel[i].z)) s->vel[i].x += a * p.x;
+        if (face_live(s->vel[i].w)) s->vel[i].y += a * p.y;
+        s->vd[i].x += a * p.x;
+        s->vd[i].y += a * p.y;
+    }
+    s->vp[i] = p;
+    c->Qnew[i] = q;
+    c->Rnew[i] = r;
+    return v4(0.0f, dot2(r, r), dot2(p, q), 0.0f);
+}
+
+/* new_r of visc_mgu.comp at every cell of the level: the residual the way down reads */
+static void mgu_new_r(OSim* s, const V2* Rold, const V2* Qold, V2* out) {
+    float a = s->K.v_alpha, b = s->K.v_beta;
+    for (int i = 0; i < s->W * s->H; i++) {
+        V2 sq = s->vaz[i];
+        V2 q = b == 0.0f ? sq : v2(sq.x + b * Qold[i].x, sq.y + b * Qold[i].y);
+        out[i] = v2(Rold[i].x - a * q.x, Rold[i].y - a * q.y);
+    }
+}
+
+/* record_viscosity_solve (mod.rs:2867-2923) with the device-decided loop */
+static void viscosity_solve(OSim* s, int restrain) {
+    const int nlev = (int)mini(maxi((int)s->prm.viscosity_mg_levels, 1), s->lv.tail);
+    const int halo = 2 * (int)mini(maxi((int)s->prm.viscosity_mg_sweeps, 1), 2);
+    const float tz = P_.tol[2];
+    SolveBuf* K = &s->K;
+    int n = s->W * s->H;
+    if (restrain) k_visc_strain(s);
+    /* visc_apply mode 0 + cg_reduce mode 4 */
+    tile_partials(s, s->part, cell_visc_start, NULL);
+    {
+        V4 a = total(s, 0, s->nwg);
+        K->v_rz = a.x;
+        K->v_r0 = a.y;
+        K->v_rr = a.y;
+        K->v_beta = 0.0f;
+        K->v_alpha = 0.0f;
+        K->v_iters = 0u;
+        K->v_done = (a.y <= 1e-30f || a.x <= 0.0f) ? 1u : 0u;
+    }
+    if (s->prm.viscosity_warm != 0 && !K->v_done) {
+        V2* outr = (V2*)malloc((size_t)n * sizeof(V2));
+        memcpy(outr, s->vr, (size_t)n * sizeof(V2));
+        tile_partials(s, s->part, cell_visc_warm, outr);
+        memcpy(s->vr, outr, (size_t)n * sizeof(V2));
+        free(outr);
+        V4 a = total(s, 0, s->nwg);
+        K->v_rz = a.x;
+        K->v_rr = a.y;
+        K->v_beta = 0.0f;
+        K->v_done = (a.y <= tz * tz * K->v_r0 || a.x <= 0.0f) ? 1u : 0u;
+    }
+    /* the buffers of the two parities: the current residual alternates between vr and vr2 */
+    V2 *RA = s->vr, *RB = s->vr2, *QA = s->vq, *QB = s->vq2;
+    if (!K->v_done) {
+        vmg_down(s, 0, RA, 0, halo);
+        vmg_coarse(s, nlev, halo);
+        visc_mgz(s, RA, QA, halo);
+        V4 a = total(s, 0, s->nwg);
+        K->v_rz = a.x;
+        K->v_beta = 0.0f;
+        K->v_pq = a.y;
+        K->v_alpha = a.y > 0.0f ? a.x / a.y : 0.0f;
+        if (a.x <= 0.0f || a.y <= 0.0f) K->v_done = 1u;
+    }
+    V2* newr = (V2*)malloc((size_t)n * sizeof(V2));
+    for (uint32_t k = 0; k < s->prm.viscosity_max_iters && !K->v_done; k++) {
+        V2 *Rold = (k % 2 == 0) ? RA : RB, *Qold = (k % 2 == 0) ? QA : QB;
+        V2 *Rnew = (k % 2 == 0) ? RB : RA, *Qnew = (k % 2 == 0) ? QB : QA;
+        mgu_new_r(s, Rold, Qold, newr);
+        MguCtx c = {Rold, Qold, Rnew, Qnew};
+        tile_partials(s, s->part, cell_mgu, &c);
+        vmg_down(s, 0, newr, 0, halo);
+        {
+            V4 a = total(s, 0, s->nwg);
+            uint32_t was = K->v_done;
+            K->v_iters += 1u - was;
+            uint32_t now = a.y <= tz * tz * K->v_r0;
+            if (was == 0u) K->v_rr = a.y;
+            K->v_pq = a.z;
+            K->v_done = was > now ? was : now;
+        }
+        if (K->v_done) break;
+        vmg_coarse(s, nlev, halo);
+        visc_mgz(s, Rnew, Qnew, halo);
+        {
+            V4 a = total(s, 0, s->nwg);
+            float beta = (K->v_done == 0u && K->v_rz > 0.0f) ? a.x / K->v_rz : 0.0f;
+            float pq = a.y + 2.0f * beta * a.z + beta * beta * K->v_pq;
+            K->v_beta = beta;
+            K->v_alpha = (K->v_done == 0u && pq > 0.0f) ? a.x / pq : 0.0f;
+            K->v_rz = a.x;
+        }
+    }
+    free(newr);
+    /* mode 7 */
+    if (K->v_iters > K->v_it_max) K->v_it_max = K->v_iters;
+    if (K->v_done == 0u) K->v_unconv += 1u;
+    float rel = K->v_r0 > 0.0f ? sqrtf(K->v_rr / K->v_r0) : 0.0f;
+    K->v_res_max = maxf(K->v_res_max, rel);
+}
+
+/* rhs_visc.comp */
+static void k_rhs_visc(OSim* s, int warm) {
+    int W = s->W, H = s->H;
+    float ratio = s->S.dt / s->S.dt_prev;
+    V4* out = (V4*)malloc((size_t)W * H * sizeof(V4));
+    memcpy(out, s->prhs, (size_t)W * H * sizeof(V4));
+    for (int cy = 0; cy < H; cy++)
+        for (int cx = 0; cx < W; cx++) {
+            int i = cidx(s, cx, cy);
+            float D = s->mgd[i];
+            if (D <= 0.0f) {
+                out[i].z = 0.0f;
+                continue;
+            }
+            V4 w = s->mga[i];
+            float p1 = s->prhs[i].z;
+            float ap = D * p1;
+            if (s->mgd[i - 1] > 0.0f) ap -= w.x * s->prhs[i - 1].z;
+            if (s->mgd[i + 1] > 0.0f) ap -= w.y * s->prhs[i + 1].z;
+            if (s->mgd[i - W] > 0.0f) ap -= w.z * s->prhs[i - W].z;
+            if (s->mgd[i + W] > 0.0f) ap -= w.w * s->prhs[i + W].z;
+            float aL = s->solid[i].x, aB = s->solid[i].y, aR = s->solid[i + 1].x, aT = s->solid[i + W].y;
+            V4 vme = s->vel[i];
+            float div = aR * s->vel[i + 1].x - aL * vme.x + aT * s->vel[i + W].y - aB * vme.y;
+            V4 r = s->prhs[i];
+            out[i] = v4(ap - div, r.y, p1, 0.0f);
+            if (warm) s->pres[i].x = p1 + s->p2keep[i] * ratio;
+        }
+    memcpy(s->prhs, out, (size_t)W * H * sizeof(V4));
+    free(out);
+}
+
+/* project_visc.comp */
+static float p2_of(const OSim* s, int i) { return s->mgd[i] > 0.0f ? s->pres[i].x - s->prhs[i].z : 0.0f; }
+static void k_project_visc(OSim* s) {
+    int W = s->W;
+    float m_all = 0.0f;
+    float* keep = (float*)malloc((size_t)W * s->H * sizeof(float));
+    memcpy(keep, s->p2keep, (size_t)W * s->H * sizeof(float));
+    for (int cy = 1; cy < s->H; cy++)
+        for (int cx = 1; cx < W; cx++) {
+            int i = cidx(s, cx, cy);
+            keep[i] = p2_of(s, i);
+            V4 cf = s->coef[i];
+            V4 me = s->vel[i];
+            int lu = face_live(me.z) && cf.x != 0.0f, lv = face_live(me.w) && cf.y != 0.0f;
+            if (lu || lv) {
+                float pc = p2_of(s, i);
+                if (lu) me.x -= cf.x * (pc - p2_of(s, i - 1));
+                if (lv) me.y -= cf.y * (pc - p2_of(s, i - W));
+                s->vel[i] = me;
+            }
+            float m = 0.0f;
+            if (lu) m = fabsf(me.x);
+            if (lv) m = maxf(m, fabsf(me.y));
+            if (m > m_all) m_all = m;
+        }
+    memcpy(s->p2keep, keep, (size_t)W * s->H * sizeof(float));
+    free(keep);
+    if (m_all > bitsf(s->S.umax_grid)) s->S.umax_grid = fbits(m_all);
+}
+
+/* ------------------------------------------------------------------------------------ */
 /* The substep (record_substep, mod.rs:2615-2708)                                         */
 /* ------------------------------------------------------------------------------------ */
 
@@ -2904,10 +3545,28 @@ static void substep(OSim* s, int gather) {
         k_visc_setup(s);
         k_visc_apply_explicit(s);
     }
+    /* implicit viscosity between two pressure solves (viscous_projection) or before one */
+    const int twice = s->visc_mode == 2 && s->prm.viscous_projection != 0;
+    if (s->visc_mode == 2) {
+        /* record_viscosity_split (mod.rs:2812-2836) */
+        memset(s->tiles, 0, (size_t)s->nwg * sizeof(uint32_t));
+        k_visc_setup(s);
+        k_visc_split(s);
+        k_visc_diag(s, s->prm.viscosity_warm != 0, 1);
+        const int nlev = mini(maxi((int)s->prm.viscosity_mg_levels, 1), s->lv.tail);
+        for (int l = 1; l <= nlev; l++) k_vmg_build(s, l);
+        if (!twice) viscosity_solve(s, 0);
+    }
     memset(s->ptile, 0, (size_t)s->nwg * sizeof(uint32_t));
     k_rhs(s);
     pressure_solve(s, 0);
     k_project(s);
+    if (twice) {
+        viscosity_solve(s, 1);
+        k_rhs_visc(s, s->prm.viscous_warm != 0);
+        pressure_solve(s, 1);
+        k_project_visc(s);
+    }
 }
 
 /* ------------------------------------------------------------------------------------ */
@@ -2938,6 +3597,11 @@ OSim* osim_create(int w, int h, uint32_t capacity, const OSimParams* p) {
     ALLOC(s->mga, s->lv.total); ALLOC(s->mgd, s->lv.total); ALLOC(s->mgx, s->lv.total);
     ALLOC(s->mgz, s->lv.total); ALLOC(s->mgr, s->lv.total);
     ALLOC(s->cgp, nc); ALLOC(s->cgp2, nc); ALLOC(s->cgq, nc);
+    ALLOC(s->vr, nc); ALLOC(s->vr2, nc); ALLOC(s->vp, nc); ALLOC(s->vq, nc); ALLOC(s->vq2, nc);
+    ALLOC(s->vd, nc); ALLOC(s->vaz, nc);
+    ALLOC(s->vma, s->lv.total); ALLOC(s->vmb, s->lv.total); ALLOC(s->vmd, s->lv.total);
+    ALLOC(s->vmr, s->lv.total); ALLOC(s->vmx, s->lv.total); ALLOC(s->vmz, s->lv.total);
+    ALLOC(s->tiles, s->nwg); ALLOC(s->vtile, s->lv.tiles);
     ALLOC(s->ptile, s->lv.tiles);
     ALLOC(s->part, 2 * s->nwg);
     for (size_t k = 0; k < nc; k++) s->solid_t[k] = NO_TEMP;
@@ -2950,7 +3614,8 @@ void osim_destroy(OSim* s) {
                     s->surf, s->surf2, s->aux, s->grho, s->therm, s->dheat, s->vw, s->vs, s->prhs,
                     s->vel0, s->pjump, s->pres, s->p2keep, s->hcell, s->solid, s->sdf, s->region,
                     s->solid_t, s->mga, s->mgd, s->mgx, s->mgz, s->mgr, s->cgp, s->cgp2, s->cgq,
-                    s->ptile, s->part};
+                    s->ptile, s->part, s->vr, s->vr2, s->vp, s->vq, s->vq2, s->vd, s->vaz, s->vma,
+                    s->vmb, s->vmd, s->vmr, s->vmx, s->vmz, s->tiles, s->vtile};
     for (size_t k = 0; k < sizeof ptrs / sizeof ptrs[0]; k++) free(ptrs[k]);
     free(s);
 }
@@ -3050,7 +3715,8 @@ int osim_reset(OSim* s, const OParticle* in, uint32_t n) {
         if (m->volatility > 0.0f || (thermal && m->boil < 1e8f)) return -4;
     }
     s->visc_mode = viscosity_mode(s);
-    if (s->visc_mode == 2) return -5;
+    /* the implicit solve with its multigrid preconditioner on at least one coarse level */
+    if (s->visc_mode == 2 && (s->prm.viscosity_precond == 0 || s->lv.tail < 1)) return -4;
     build_mats(s);
     /* buffers a reset clears (mod.rs:2451-2460) */
     size_t nc = (size_t)s->W * s->H;
@@ -3118,6 +3784,13 @@ long osim_field(const OSim* s, const char* name, void* out, size_t cap) {
     F("mgd", s->mgd, (size_t)s->lv.total * 4)
     F("mgz", s->mgz, (size_t)s->lv.total * 8)
     F("ptile", s->ptile, (size_t)s->lv.tiles * 4)
+    F("p2keep", s->p2keep, nc * 4)
+    F("tiles", s->tiles, (size_t)s->nwg * 4)
+    F("vtile", s->vtile, (size_t)s->lv.tiles * 4)
+    F("vd", s->vd, nc * 8)
+    F("vma", s->vma, (size_t)s->lv.total * 16)
+    F("vmb", s->vmb, (size_t)s->lv.total * 16)
+    F("vmd", s->vmd, (size_t)s->lv.total * 8)
     F("ledger", s->ledger, sizeof s->ledger)
     F("region_air", &s->region_air, 4)
     F("step", &s->S, sizeof s->S)
@@ -3125,6 +3798,76 @@ long osim_field(const OSim* s, const char* name, void* out, size_t cap) {
     if (!src) return -1;
     if (out && cap >= bytes) memcpy(out, src, bytes);
     return (long)bytes;
+}
+
+/* Self-check of the implicit viscosity restatement: the level-0 matrix that visc_diag writes
+ * out (vma, vmb, vmd, applied as vmg.glsl's offd) against the matrix-free operator of
+ * visc_iter.comp (M d + G^T W G d through the weighted strain), for x on the unknown faces.
+ * Writes both products to y_mg and y_free (2 floats per cell); returns the unknown count. */
+long osim_visc_operator(OSim* s, const float* x, float* y_mg, float* y_free) {
+    int n = s->W * s->H;
+    Lv L0 = lev(s, 0);
+    V2* X = (V2*)calloc((size_t)n, sizeof(V2));
+    long unknowns = 0;
+    for (int i = 0; i < n; i++) {
+        V2 d = s->vmd[i];
+        X[i] = v2(d.x > 0.0f ? x[2 * i] : 0.0f, d.y > 0.0f ? x[2 * i + 1] : 0.0f);
+        unknowns += (d.x > 0.0f) + (d.y > 0.0f);
+    }
+    V2* keep = (V2*)malloc((size_t)n * sizeof(V2));
+    memcpy(keep, s->vd, (size_t)n * sizeof(V2));
+    memcpy(s->vd, X, (size_t)n * sizeof(V2));
+    for (int cy = 0; cy < s->H; cy++)
+        for (int cx = 0; cx < s->W; cx++) {
+            int i = cidx(s, cx, cy);
+            V2 d = s->vmd[i];
+            V2 o = voffd(s, L0, X, cx, cy);
+            y_mg[2 * i] = d.x * X[i].x + o.x;
+            y_mg[2 * i + 1] = d.y * X[i].y + o.y;
+            y_free[2 * i] = y_free[2 * i + 1] = 0.0f;
+            if (!interior_c(s, cx, cy) || !tile_active_c(s, cx, cy)) continue;
+            V2 g = v2(0, 0);
+            int W = s->W;
+            if (live_u(s, i)) {
+                float c1 = closed_u(s, i - W) ? 1.0f : 0.5f, c2 = closed_u(s, i + W) ? -1.0f : -0.5f;
+                V4 sl = strain_of_dir(s, cx - 1, cy), sc = strain_of_dir(s, cx, cy), su = strain_of_dir(s, cx, cy + 1);
+                g.x = sl.x - sc.x + sc.z * c1 + su.z * c2;
+            }
+            if (live_v(s, i)) {
+                float d1 = closed_v(s, i - 1) ? 1.0f : 0.5f, d2 = closed_v(s, i + 1) ? -1.0f : -0.5f;
+                V4 sd = strain_of_dir(s, cx, cy - 1), sc = strain_of_dir(s, cx, cy), sr = strain_of_dir(s, cx + 1, cy);
+                g.y = sd.y - sc.y + sc.z * d1 + sr.z * d2;
+            }
+            V4 cf = s->coef[i];
+            y_free[2 * i] = live_u(s, i) ? cf.z * X[i].x + g.x : 0.0f;
+            y_free[2 * i + 1] = live_v(s, i) ? cf.w * X[i].y + g.y : 0.0f;
+        }
+    memcpy(s->vd, keep, (size_t)n * sizeof(V2));
+    free(keep);
+    free(X);
+    return unknowns;
+}
+
+/* Test hook: the assembled viscosity matrix of multigrid level l (vmg.glsl's diagonal and
+ * offd) applied to x (2 floats per cell of that level, zeroed where no unknown); returns the
+ * level's cell count. */
+long osim_vmg_apply(OSim* s, int l, const float* x, float* y) {
+    if (l < 0 || l >= s->lv.n) return -1;
+    Lv L = lev(s, l);
+    int n = L.w * L.h;
+    V2* X = (V2*)calloc((size_t)n, sizeof(V2));
+    for (int t = 0; t < n; t++) {
+        V2 d = s->vmd[L.off + t];
+        X[t] = v2(d.x > 0.0f ? x[2 * t] : 0.0f, d.y > 0.0f ? x[2 * t + 1] : 0.0f);
+    }
+    for (int t = 0; t < n; t++) {
+        V2 d = s->vmd[L.off + t];
+        V2 o = voffd(s, L, X, t % L.w, t / L.w);
+        y[2 * t] = d.x * X[t].x + o.x;
+        y[2 * t + 1] = d.y * X[t].y + o.y;
+    }
+    free(X);
+    return n;
 }
 
 void osim_stats(const OSim* s, OStats* o) {
@@ -3147,6 +3890,13 @@ void osim_stats(const OSim* s, OStats* o) {
     o->p_rr[1] = s->K.p_rr[1];
     o->p_bb[0] = s->K.p_bb[0];
     o->p_bb[1] = s->K.p_bb[1];
+    o->v_iters = s->K.v_iters;
+    o->v_done = s->K.v_done;
+    o->v_it_max = s->K.v_it_max;
+    o->v_unconv = s->K.v_unconv;
+    o->v_res_max = s->K.v_res_max;
+    o->v_rr = s->K.v_rr;
+    o->v_r0 = s->K.v_r0;
     o->umax_grid = bitsf(s->S.umax_grid);
     o->umax_part = bitsf(s->S.umax_part);
     o->n_slots = s->n_slots;

@@ -139,6 +139,11 @@ uint32_t osim_particles(const OSim* s, OParticle* out, uint32_t cap);
 /* Copies a named field (see sprout_oracle.c: field table). Returns bytes, or -1. */
 long osim_field(const OSim* s, const char* name, void* out, size_t cap);
 void osim_stats(const OSim* s, OStats* out);
+/* Test hook: the implicit viscosity's assembled level-0 matrix and its matrix-free operator
+ * applied to x (2 floats per cell) on the unknown faces; returns the number of unknowns. */
+long osim_visc_operator(OSim* s, const float* x, float* y_mg, float* y_free);
+/* Test hook: the assembled viscosity matrix of multigrid level l applied to x. */
+long osim_vmg_apply(OSim* s, int l, const float* x, float* y);
 /* Threads the oracle uses (OpenMP); 1 = sequential. */
 void osim_set_threads(int n);
 

@@ -48,12 +48,17 @@ class Tank:
 # ---- the configurations the benchmark names, at their sizes or scaled down ------------------
 
 def dam_break(w: int = 384, h: int = 216, cell: float = 0.002, width: float = 0.4, height: float = 0.6,
-              tol: float = 1e-5, extra: dict | None = None) -> Tank:
-    """A plain water dam break: water over the left `width` and bottom `height` of a closed box,
-    fixed 1/240 s substeps, no surface tension (the 384 x 216 form is the first configuration)."""
+              tol: float = 1e-5, extra: dict | None = None, mat: int = 0) -> Tank:
+    """A plain dam break: liquid row `mat` (0 water, 1 honey, 2 oil) over the left `width` and
+    bottom `height` of a closed box, fixed 1/240 s substeps, no surface tension (the 384 x 216
+    water form is the first configuration). Honey takes the implicit viscosity solve."""
     s = {"cell_size": cell, "fixed_hz": 240.0, "pressure_tol": tol, "tension_water": 0.0}
+    if mat == 1:
+        s["tension_honey"] = 0.0
+    elif mat == 2:
+        s["tension_oil"] = 0.0
     s.update(extra or {})
-    return Tank(w, h, s, [], [([0.0, 0.0, width * w, height * h], 0, None)])
+    return Tank(w, h, s, [], [([0.0, 0.0, width * w, height * h], mat, None)])
 
 
 def layered_custom(w: int, h: int, rows: list[dict], cell: float = 0.001, heater_rows: int = 0,
@@ -84,3 +89,25 @@ def layered_custom(w: int, h: int, rows: list[dict], cell: float = 0.001, heater
         for k in range(n):
             fills.append(([0.0, k * h / n, float(w), (k + 1) * h / n], 59 + k, ambient))
     return Tank(w, h, s, shapes, fills)
+
+
+# The three layers of the stratified tank: honey, water, olive oil (rho in kg/m^3, kinematic
+# viscosity mu / rho in m^2/s), each a fifth of the height.
+STRATIFIED_LAYERS = [
+    {"density": 1420.0, "viscosity": 10.0 / 1420.0, "tension": 0.0},
+    {"density": 1000.0, "viscosity": 1e-3 / 1000.0, "tension": 0.0},
+    {"density": 910.0, "viscosity": 0.08 / 910.0, "tension": 0.0},
+]
+
+
+def stratified(w: int = 512, h: int = 288, cell: float = 0.002, tol: float = 1e-5,
+               extra: dict | None = None) -> Tank:
+    """Honey, water and olive oil stacked bottom to top, each 20% of the height (the second
+    configuration at 512 x 288); the honey layer takes the implicit viscosity solve."""
+    s = {"cell_size": cell, "fixed_hz": 240.0, "pressure_tol": tol, "viscosity_tol": tol}
+    for k, props in enumerate(STRATIFIED_LAYERS):
+        for name, val in props.items():
+            s[f"mat{59 + k}.{name}"] = val
+    s.update(extra or {})
+    fills = [([0.0, k * 0.2 * h, float(w), (k + 1) * 0.2 * h], 59 + k, None) for k in range(3)]
+    return Tank(w, h, s, [], fills)
