@@ -69,6 +69,8 @@ typedef struct SproutSolverStats {
     uint32_t caps, acc_stride, thermal, viscosity_mode, levels, tail;
     uint32_t device_error;             /* non-zero: a bounded device wait ran out */
     uint64_t h2d_bytes, d2h_bytes;     /* host <-> device bytes this sim has moved (cumulative) */
+    uint32_t viscosity_iters;          /* iterations of the last implicit viscosity solve */
+    float viscosity_residual;          /* |r| / |r0| of the last implicit viscosity solve */
 } SproutSolverStats;
 
 typedef struct SproutParams SproutParams;   /* SimParams */
@@ -156,8 +158,11 @@ int sprout_sim_device_bytes(SproutSim* sim, size_t* bytes);
 int sprout_sim_profile(SproutSim* sim, uint32_t substeps, float* ms);
 /* FluidSim::profile_passes (mod.rs:3120-3160): one substep, stage by stage, each timed by
  * CUDA events: ms[0] advance (G2P, advection, collision), ms[1] sort, ms[2] P2G,
- * ms[3] grid passes (prep, coefficients, surface tension, heat, viscosity, rhs),
- * ms[4] pressure solve, ms[5] projection. n >= 6. Blocking. */
+ * ms[3] grid passes (prep, coefficients, surface tension, heat, viscosity setup, rhs),
+ * ms[4] pressure solve, ms[5] projection, ms[6] implicit viscosity solve, ms[7] second
+ * projection (rhs_visc, second pressure solve, project_visc); the last two are zero-cost
+ * unless the tank takes the implicit viscosity between two pressure solves. n >= 6; with
+ * n < 8 the stages past n - 1 are added to ms[5]. Blocking. */
 int sprout_sim_profile_passes(SproutSim* sim, float* ms, uint32_t n);
 
 /* ---- a pressure solve that allocates nothing ------------------------------------------

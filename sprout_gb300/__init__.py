@@ -42,7 +42,7 @@ EXPORTS = [
     "sprout_sim_profile_passes", "sprout_pressure_solve_static",
 ]
 
-STAGES = ["advance", "sort", "p2g", "grid", "pressure", "project"]
+STAGES = ["advance", "sort", "p2g", "grid", "pressure", "project", "viscosity", "project2"]
 
 
 class SproutError(RuntimeError):
@@ -78,6 +78,7 @@ class SolverStats(C.Structure):
         ("n_slots", C.c_uint32), ("n_live", C.c_uint32), ("caps", C.c_uint32), ("acc_stride", C.c_uint32),
         ("thermal", C.c_uint32), ("viscosity_mode", C.c_uint32), ("levels", C.c_uint32), ("tail", C.c_uint32),
         ("device_error", C.c_uint32), ("h2d_bytes", C.c_uint64), ("d2h_bytes", C.c_uint64),
+        ("viscosity_iters", C.c_uint32), ("viscosity_residual", C.c_float),
     ]
 
 
@@ -288,8 +289,8 @@ class FluidSim:
 
     def profile_passes(self) -> dict:
         """One substep stage by stage: device ms per stage (STAGES)."""
-        ms = (C.c_float * 6)()
-        _check(lib().sprout_sim_profile_passes(self._h, ms, 6))
+        ms = (C.c_float * len(STAGES))()
+        _check(lib().sprout_sim_profile_passes(self._h, ms, len(STAGES)))
         return dict(zip(STAGES, list(ms)))
 
     def device_bytes(self) -> int:

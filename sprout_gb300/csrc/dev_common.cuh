@@ -69,6 +69,15 @@ struct DevScene {
     float4* partials;   // 2 x nwg
     int nwg;
     Levels lv;
+    // implicit viscosity (visc*.comp, vmg*.comp): Krylov vectors on the grid, the multigrid
+    // hierarchy over the levels of lv, tile flags and the compact lists of active tiles
+    float2 *vr, *vr2, *vp, *vq, *vq2, *vd, *vaz;
+    float4 *vma, *vmb;
+    float2 *vmd, *vmr, *vmx, *vmz;
+    uint32_t* tiles;    // level-0 tiles that take the implicit solve (nwg)
+    uint32_t* vtile;    // per level, tiles active in the last build (lv.tiles)
+    uint32_t* vlist;    // per level, the active tiles in order (lv.tiles)
+    uint32_t* vcount;   // per level, how many (kMaxLevels)
 };
 
 // GLSL min / max (GLSL spec 8.3): min(x, y) = y < x ? y : x, max(x, y) = x < y ? y : x.

@@ -60,7 +60,11 @@ struct DevParams {
     uint32_t pressure_max_iters;
     int visc_mode;    // 0 none, 1 explicit, 2 implicit
     int thermal;
-    int pad;
+    // the implicit viscosity solve (params.rs:289-320)
+    uint32_t viscosity_max_iters;
+    int visc_levels;   // levels below the grid in its V-cycle: min(viscosity_mg_levels, tail)
+    int visc_sweeps;   // Gauss-Seidel sweeps per visit of a level (1 or 2)
+    int viscosity_warm, viscous_warm, viscous_projection;
 };
 
 // StepBuf (common.glsl:122-135) plus the engine's own step flags.
@@ -89,7 +93,8 @@ struct SolveState {
     float v_res_max;
     uint32_t error;       // non-zero: a bounded wait in a persistent kernel ran out
     uint32_t bar_count, bar_gen;   // the persistent kernels' grid barrier
-    uint32_t pad[2];
+    uint32_t v_iters, v_done;      // the last viscosity solve
+    float v_rr, v_r0;
 };
 
 // The multigrid hierarchy (Levels, src/sim/mod.rs:714-753).

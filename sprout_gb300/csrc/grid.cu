@@ -569,6 +569,20 @@ __global__ void __launch_bounds__(256) k_visc_setup(DevScene d) {
         o.z = wn * 0.5f * ((ua - ub) + (va - vb));
     }
     d.vs[i] = o;
+    // the tiles that need the implicit solve: within one cell of a cell whose diffusion
+    // number reaches implicit_viscosity_min (visc_setup.comp:49-56)
+    if (d.P->visc_mode == 2) {
+        const float4 me = d.cell[i];
+        if (me.w > 0.0f && dt * me.z / maxf(me.y, 0.05f) >= d.P->corr[3]) {
+            const int tw = (W + 15) >> 4;
+            for (int b = -1; b <= 1; b++)
+                for (int a = -1; a <= 1; a++) {
+                    const int nx = clampi(cx + a, 0, W - 1), ny = clampi(cy + b, 0, H - 1);
+                    const int t = (ny >> 4) * tw + (nx >> 4);
+                    if (d.tiles[t] == 0u) atomicOr(&d.tiles[t], 1u);
+                }
+        }
+    }
 }
 
 __global__ void __launch_bounds__(256) k_visc_explicit(DevScene d) {
@@ -691,6 +705,13 @@ void launch_grid(const DevScene& d, const LaunchCfg& cfg, cudaStream_t st) {
     if (cfg.visc_mode == 1) {
         k_visc_setup<<<grd, blk, 0, st>>>(d);
         k_visc_explicit<<<grd, blk, 0, st>>>(d);
+    } else if (cfg.visc_mode == 2) {
+        // record_viscosity_split (mod.rs:2812-2836), and the solve itself here unless it
+        // runs between two pressure solves (record_viscosity, mod.rs:2805-2808)
+        cudaMemsetAsync(d.tiles, 0, (size_t)d.nwg * sizeof(uint32_t), st);
+        k_visc_setup<<<grd, blk, 0, st>>>(d);
+        launch_viscosity_setup(d, cfg, st);
+        if (!cfg.twice) launch_viscosity(d, cfg, st, 0);
     }
     k_rhs<<<grd, blk, 0, st>>>(d);
 }

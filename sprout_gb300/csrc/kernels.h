@@ -14,6 +14,11 @@ struct LaunchCfg {
     bool thermal = false;
     bool heat = false;        // thermal and heat_rate > 0: heat.comp runs
     int visc_mode = 0;        // 0 none, 1 explicit, 2 implicit
+    bool twice = false;       // implicit viscosity between two pressure solves
+    bool viscous_warm = false;   // the first solve starts from last substep's P1 (cg_scale mode 1)
+    int visc_levels = 0;      // levels below the grid in the viscosity V-cycle
+    int visc_sweeps = 2;      // Gauss-Seidel sweeps per visit of a level (1 or 2)
+    int visc_blocks = 0;      // blocks of the persistent viscosity kernel
     int mg_blocks = 0;        // blocks of the persistent pressure kernel
     int mg_threads = 256;
 };
@@ -22,8 +27,18 @@ void launch_advance(const DevScene& d, const LaunchCfg& cfg, cudaStream_t st);
 void launch_sort(const DevScene& d, const LaunchCfg& cfg, cudaStream_t st);
 void launch_p2g(const DevScene& d, const LaunchCfg& cfg, cudaStream_t st);
 void launch_grid(const DevScene& d, const LaunchCfg& cfg, cudaStream_t st);
-cudaError_t launch_pressure(const DevScene& d, const LaunchCfg& cfg, cudaStream_t st);
+// `second`: the pressure solve after the implicit viscosity (same matrix and hierarchy).
+cudaError_t launch_pressure(const DevScene& d, const LaunchCfg& cfg, cudaStream_t st, int second);
 void launch_project(const DevScene& d, const LaunchCfg& cfg, cudaStream_t st);
+// The implicit viscosity: the passes before the solve (split, diagonal, multigrid levels),
+// the solve itself (`restrain`: take the strain of u* again first), and the right-hand side
+// and projection of the second pressure solve.
+void launch_viscosity_setup(const DevScene& d, const LaunchCfg& cfg, cudaStream_t st);
+cudaError_t launch_viscosity(const DevScene& d, const LaunchCfg& cfg, cudaStream_t st, int restrain);
+void launch_second_projection_rhs(const DevScene& d, cudaStream_t st);
+void launch_second_projection(const DevScene& d, cudaStream_t st);
+// Blocks of the persistent viscosity kernel that fit on the device at once.
+int viscosity_blocks_max(int device, int sweeps);
 // Blocks of the persistent pressure kernel that fit on the device at once.
 int pressure_blocks_max(int device, size_t smem);
 // Dynamic shared memory of the persistent pressure kernel: the tail levels of each block.

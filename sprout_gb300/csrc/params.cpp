@@ -606,6 +606,12 @@ void build_params(const SimParams& p, const Tank& t, bool thermal, uint32_t caps
     P->corr[3] = p.implicit_viscosity_min;
     P->pressure_max_iters = p.pressure_max_iters;
     P->thermal = thermal ? 1 : 0;
+    P->viscosity_max_iters = p.viscosity_max_iters;
+    P->visc_sweeps = (int)std::min<uint32_t>(std::max<uint32_t>(p.viscosity_mg_sweeps, 1u), 2u);
+    P->visc_levels = (int)std::max<uint32_t>(p.viscosity_mg_levels, 1u);   // the host clamps to the tail
+    P->viscosity_warm = p.viscosity_warm != 0 ? 1 : 0;
+    P->viscous_warm = p.viscous_warm != 0 ? 1 : 0;
+    P->viscous_projection = p.viscous_projection != 0 ? 1 : 0;
 }
 
 }  // namespace sprout

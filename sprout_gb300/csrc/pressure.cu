@@ -20,96 +20,16 @@
 
 #include "dev_common.cuh"
 #include "kernels.h"
+#include "solve_common.cuh"
 
 namespace sprout {
 
 namespace {
 
-constexpr int NT = 256;                // threads per block: one 16 x 16 tile at a time
-constexpr uint32_t SPIN_LIMIT = 1u << 24;
+using namespace solve;
 
-struct Lv {
-    int off, w, h, toff;
-};
-
-DEV Lv lev(const Levels& L, int l) { return Lv{L.off[l], L.w[l], L.h[l], L.toff[l]}; }
-DEV bool l_inside(const Lv& L, int x, int y) { return x >= 0 && y >= 0 && x < L.w && y < L.h; }
-DEV int l_at(const Lv& L, int x, int y) { return L.off + y * L.w + x; }
-DEV int tiles_x(const Lv& L) { return (L.w + 15) >> 4; }
-DEV int tiles_y(const Lv& L) { return (L.h + 15) >> 4; }
-DEV float wcomp(float4 w, int k) { return k == 0 ? w.x : k == 1 ? w.y : k == 2 ? w.z : w.w; }
 __constant__ int NBX[4] = {-1, 1, 0, 0};
 __constant__ int NBY[4] = {0, 0, -1, 1};
-
-// Grid-wide barrier over the co-resident blocks of a cooperative launch. Thread 0 of each
-// block arrives on a counter and waits on a generation word with a bounded spin; the last
-// to arrive resets the counter and advances the generation. Returns false (and every block
-// leaves) once any wait has run out.
-DEV bool grid_sync(SolveState* K) {
-    __shared__ int s_ok;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        int ok = 1;
-        volatile uint32_t* vgen = &K->bar_gen;
-        volatile uint32_t* verr = &K->error;
-        if (*verr != 0u) {
-            ok = 0;
-        } else {
-            uint32_t g = *vgen;
-            __threadfence();
-            uint32_t arrived = atomicAdd(&K->bar_count, 1u) + 1u;
-            if (arrived == gridDim.x) {
-                atomicExch(&K->bar_count, 0u);
-                __threadfence();
-                atomicAdd(&K->bar_gen, 1u);
-            } else {
-                uint32_t spins = 0;
-                while (*vgen == g) {
-                    if (*verr != 0u) { ok = 0; break; }
-                    __nanosleep(32);
-                    if (++spins > SPIN_LIMIT) {
-                        atomicExch(&K->error, 1u);
-                        ok = 0;
-                        break;
-                    }
-                }
-            }
-            __threadfence();
-        }
-        s_ok = ok;
-    }
-    __syncthreads();
-    return s_ok != 0;
-}
-
-// Work-group tree of reduce.glsl:230-239 over the 256 values in buf; result in buf[0].
-DEV void block_tree(float4* buf) {
-    const int t = threadIdx.x;
-    __syncthreads();
-    for (int s = 128; s > 0; s >>= 1) {
-        if (t < s) {
-            float4 a = buf[t], b = buf[t + s];
-            buf[t] = make_float4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w);
-        }
-        __syncthreads();
-    }
-}
-
-// total() of reduce_tail.glsl:268-281: thread t sums partials t, t + 256, ... in order,
-// then the tree. Every block calls it and gets the same value.
-DEV float4 total(const float4* part, int n, float4* buf) {
-    const int t = threadIdx.x;
-    float4 s = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    for (int k = t; k < n; k += NT) {
-        float4 v = part[k];
-        s = make_float4(s.x + v.x, s.y + v.y, s.z + v.z, s.w + v.w);
-    }
-    buf[t] = s;
-    block_tree(buf);
-    float4 r = buf[0];
-    __syncthreads();
-    return r;
-}
 
 struct Solve {
     float rz[2], alpha[2], beta[2], bb[2], rr[2];
@@ -793,10 +713,12 @@ int pressure_blocks_max(int device, size_t smem) {
     return sms * per;
 }
 
-cudaError_t launch_pressure(const DevScene& d, const LaunchCfg& cfg, cudaStream_t st) {
+cudaError_t launch_pressure(const DevScene& d, const LaunchCfg& cfg, cudaStream_t st, int second) {
     // barrier counter back to zero (a solve left by a timeout may have stopped mid-barrier)
     cudaMemsetAsync(&d.K->bar_count, 0, sizeof(uint32_t), st);
-    int second = 0, scale_mode = 0;
+    // cg_scale mode 1: with the viscosity between two solves, the first starts from last
+    // substep's P1 alone (viscous_warm, mod.rs:2979-2983)
+    int scale_mode = (!second && cfg.visc_mode == 2 && cfg.twice && cfg.viscous_warm) ? 1 : 0;
     void* args[] = {(void*)&d, &second, &scale_mode};
     return cudaLaunchCooperativeKernel((const void*)k_mgpcg, dim3(cfg.mg_blocks), dim3(NT), args, pressure_smem(d.lv), st);
 }

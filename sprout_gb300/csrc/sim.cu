@@ -131,6 +131,42 @@ struct SproutSim {
         return SPROUT_OK;
     }
 
+    // The implicit viscosity's buffers, allocated the first time a tank needs the solve.
+    bool visc_alloc = false;
+    int visc_max[2] = {0, 0};   // co-resident blocks of the viscosity kernel, 1 and 2 sweeps
+
+    int ensure_visc_buffers() {
+        if (visc_alloc) return SPROUT_OK;
+        size_t nc = (size_t)W * H, tot = (size_t)d.lv.total;
+        int rc = SPROUT_OK;
+#define A(ptr, n) do { if ((rc = alloc(&(ptr), (n))) != SPROUT_OK) return rc; } while (0)
+        A(d.vr, nc); A(d.vr2, nc); A(d.vp, nc); A(d.vq, nc); A(d.vq2, nc); A(d.vd, nc); A(d.vaz, nc);
+        A(d.vma, tot); A(d.vmb, tot); A(d.vmd, tot); A(d.vmr, tot); A(d.vmx, tot); A(d.vmz, tot);
+        A(d.tiles, (size_t)d.nwg);
+        A(d.vtile, (size_t)d.lv.tiles);
+        A(d.vlist, (size_t)d.lv.tiles);
+        A(d.vcount, (size_t)kMaxLevels);
+#undef A
+        visc_max[0] = viscosity_blocks_max(device, 1);
+        visc_max[1] = viscosity_blocks_max(device, 2);
+        CUDA_TRY(cudaDeviceSynchronize());
+        visc_alloc = true;
+        // a new set of device pointers: the captured substep is stale
+        graph_ok = false;
+        return SPROUT_OK;
+    }
+
+    // The viscosity treatment of the tank (FluidSim::viscosity_mode, mod.rs:2768-2792),
+    // re-derived before every record as the reference does, and what this engine carries.
+    int derive_viscosity() {
+        visc_mode = viscosity_mode();
+        if (visc_mode != 2) return SPROUT_OK;
+        if (params.viscosity_precond == 0)
+            return fail(SPROUT_E_UNSUPPORTED, "the Jacobi-preconditioned viscosity solve (viscosity_precond 0) is not carried by this engine; use the multigrid one (1, the default)");
+        if (d.lv.tail < 1) return fail(SPROUT_E_UNSUPPORTED, "the implicit viscosity solve needs a grid with at least one multigrid level below it");
+        return ensure_visc_buffers();
+    }
+
     int init(uint32_t w, uint32_t h, uint32_t cap, const SimParams& prm) {
         W = (int)w;
         H = (int)h;
@@ -277,6 +313,7 @@ struct SproutSim {
         DevParams P;
         build_params(params, tank, thermal, caps, W, H, n_slots, dt_limit(), tool, &P);
         P.visc_mode = visc_mode;
+        P.visc_levels = std::min(P.visc_levels, d.lv.tail);
         std::vector<DevMat> mats(kMaxMaterials);
         build_materials(params, tank, thermal, mats.data());
         bool pchg = std::memcmp(&P, &last_params, sizeof P) != 0 || last_mats.empty();
@@ -336,16 +373,27 @@ struct SproutSim {
         return check_device_error();
     }
 
-    // The stages of a substep, in order (profile_passes times each one).
-    static constexpr int kStages = 6;
+    // The stages of a substep, in order (profile_passes times each one). The last two run
+    // only with the implicit viscosity between two pressure solves (viscous_projection).
+    static constexpr int kStages = 8;
     void record_stage(int k, cudaStream_t st) {
         switch (k) {
         case 0: launch_advance(d, cfg, st); break;
         case 1: launch_sort(d, cfg, st); break;
         case 2: launch_p2g(d, cfg, st); break;
         case 3: launch_grid(d, cfg, st); break;
-        case 4: launch_pressure(d, cfg, st); break;
-        default: launch_project(d, cfg, st); break;
+        case 4: launch_pressure(d, cfg, st, 0); break;
+        case 5: launch_project(d, cfg, st); break;
+        case 6:
+            if (cfg.visc_mode == 2 && cfg.twice) launch_viscosity(d, cfg, st, 1);
+            break;
+        default:
+            if (cfg.visc_mode == 2 && cfg.twice) {
+                launch_second_projection_rhs(d, st);
+                launch_pressure(d, cfg, st, 1);
+                launch_second_projection(d, st);
+            }
+            break;
         }
     }
 
@@ -359,8 +407,15 @@ struct SproutSim {
         want.thermal = thermal;
         want.heat = thermal && params.heat_rate > 0.0f;
         want.visc_mode = visc_mode;
+        want.twice = visc_mode == 2 && params.viscous_projection != 0;
+        want.viscous_warm = params.viscous_warm != 0;
+        want.visc_levels = std::min((int)std::max(params.viscosity_mg_levels, 1u), d.lv.tail);
+        want.visc_sweeps = (int)std::min(std::max(params.viscosity_mg_sweeps, 1u), 2u);
+        want.visc_blocks = std::max(1, std::min(d.nwg, visc_max[want.visc_sweeps - 1]));
         bool same = graph_ok && want.n_slots == cfg.n_slots && want.thermal == cfg.thermal && want.heat == cfg.heat &&
-                    want.visc_mode == cfg.visc_mode && d.stride == tank.stride;
+                    want.visc_mode == cfg.visc_mode && want.twice == cfg.twice && want.viscous_warm == cfg.viscous_warm &&
+                    want.visc_levels == cfg.visc_levels && want.visc_sweeps == cfg.visc_sweeps &&
+                    want.visc_blocks == cfg.visc_blocks && d.stride == tank.stride;
         cfg = want;
         d.stride = std::max(tank.stride, 8);
         if (same || !use_graph) return SPROUT_OK;
@@ -448,8 +503,8 @@ struct SproutSim {
             if (m.volatility > 0.0f || (thermal && m.boil < 1e8f))
                 return fail(SPROUT_E_UNSUPPORTED, "evaporation and boiling are not carried by this engine");
         }
-        visc_mode = viscosity_mode();
-        if (visc_mode == 2) return fail(SPROUT_E_UNSUPPORTED, "implicit viscosity is not carried by this engine yet");
+        int rc = derive_viscosity();
+        if (rc != SPROUT_OK) return rc;
         n_slots = n;
         d.stride = std::max(tank.stride, 8);
         CUDA_TRY(cudaStreamSynchronize(stream));
@@ -468,7 +523,9 @@ struct SproutSim {
 
     int step(uint32_t substeps, float target, const ToolState* tool) {
         if (n_slots == 0 || tank.rows.empty()) return fail(SPROUT_E_ARG, "step before reset (no particles)");
-        int rc = upload_tables(tool);
+        int rc = derive_viscosity();
+        if (rc != SPROUT_OK) return rc;
+        rc = upload_tables(tool);
         if (rc != SPROUT_OK) return rc;
         if (substeps == 0) return SPROUT_OK;
         float fl = std::max(target, 0.0f);
@@ -744,6 +801,13 @@ int sprout_sim_download_field(SproutSim* sim, const char* name, void* out, size_
     else if (n == "mgd") { src = d.mgd; b = (size_t)d.lv.total * 4; }
     else if (n == "mgz") { src = d.mgz; b = (size_t)d.lv.total * 8; }
     else if (n == "ptile") { src = d.ptile; b = (size_t)d.lv.tiles * 4; }
+    else if (n == "p2keep") { src = d.p2keep; b = nc * 4; }
+    else if (sim->visc_alloc && n == "tiles") { src = d.tiles; b = (size_t)d.nwg * 4; }
+    else if (sim->visc_alloc && n == "vtile") { src = d.vtile; b = (size_t)d.lv.tiles * 4; }
+    else if (sim->visc_alloc && n == "vd") { src = d.vd; b = nc * 8; }
+    else if (sim->visc_alloc && n == "vma") { src = d.vma; b = (size_t)d.lv.total * 16; }
+    else if (sim->visc_alloc && n == "vmb") { src = d.vmb; b = (size_t)d.lv.total * 16; }
+    else if (sim->visc_alloc && n == "vmd") { src = d.vmd; b = (size_t)d.lv.total * 8; }
     else if (n == "ledger") { src = d.ledger; b = 8 * 8; }
     else if (n == "count") { src = d.count; b = nc * 4; }
     else if (n == "start") { src = d.start; b = (nc + 1) * 4; }
@@ -793,6 +857,8 @@ int sprout_sim_stats(SproutSim* sim, SproutSolverStats* o) {
     o->levels = (uint32_t)sim->d.lv.n;
     o->tail = (uint32_t)sim->d.lv.tail;
     o->device_error = K.error;
+    o->viscosity_iters = K.v_iters;
+    o->viscosity_residual = K.v_r0 > 0.0f ? std::sqrt(K.v_rr / K.v_r0) : 0.0f;
     o->h2d_bytes = sim->h2d_bytes;
     o->d2h_bytes = sim->d2h_bytes;
     return SPROUT_OK;
@@ -804,9 +870,16 @@ int sprout_sim_profile(SproutSim* sim, uint32_t substeps, float* ms) {
 }
 int sprout_sim_profile_passes(SproutSim* sim, float* ms, uint32_t n) {
     if (!sim || !ms) return fail(SPROUT_E_ARG, "null argument");
-    if (n < (uint32_t)SproutSim::kStages) return fail(SPROUT_E_ARG, "need room for 6 stage times");
+    if (n < 6) return fail(SPROUT_E_ARG, "need room for 6 stage times");
     if (sim->n_slots == 0) return fail(SPROUT_E_ARG, "profile before reset");
-    return sim->profile_passes(ms);
+    float all[SproutSim::kStages];
+    int rc = sim->profile_passes(all);
+    if (rc != SPROUT_OK) return rc;
+    uint32_t m = std::min(n, (uint32_t)SproutSim::kStages);
+    for (uint32_t k = 0; k < m; k++) ms[k] = all[k];
+    // with room for 6 only, the stages after the projection count with it
+    for (uint32_t k = m; k < (uint32_t)SproutSim::kStages; k++) ms[5] += all[k];
+    return SPROUT_OK;
 }
 int sprout_sim_device_bytes(SproutSim* sim, size_t* bytes) {
     if (!sim || !bytes) return fail(SPROUT_E_ARG, "null argument");

@@ -1,0 +1,100 @@
+// Device helpers shared by the persistent solver kernels (pressure.cu, viscosity.cu): the
+// multigrid level geometry, the grid-wide barrier of a cooperative launch with its bounded
+// wait, and the work-group trees and strided totals of reduce.glsl / reduce_tail.glsl that
+// every block evaluates in the same order (so every block gets the same scalars).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "dev_common.cuh"
+
+namespace sprout {
+namespace solve {
+
+constexpr int NT = 256;                // threads per block: one 16 x 16 tile at a time
+constexpr uint32_t SPIN_LIMIT = 1u << 24;
+
+struct Lv {
+    int off, w, h, toff;
+};
+
+DEV Lv lev(const Levels& L, int l) { return Lv{L.off[l], L.w[l], L.h[l], L.toff[l]}; }
+DEV bool l_inside(const Lv& L, int x, int y) { return x >= 0 && y >= 0 && x < L.w && y < L.h; }
+DEV int l_at(const Lv& L, int x, int y) { return L.off + y * L.w + x; }
+DEV int tiles_x(const Lv& L) { return (L.w + 15) >> 4; }
+DEV int tiles_y(const Lv& L) { return (L.h + 15) >> 4; }
+DEV float wcomp(float4 w, int k) { return k == 0 ? w.x : k == 1 ? w.y : k == 2 ? w.z : w.w; }
+
+// Grid-wide barrier over the co-resident blocks of a cooperative launch. Thread 0 of each
+// block arrives on a counter and waits on a generation word with a bounded spin; the last
+// to arrive resets the counter and advances the generation. Returns false (and every block
+// leaves) once any wait has run out.
+DEV bool grid_sync(SolveState* K) {
+    __shared__ int s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int ok = 1;
+        volatile uint32_t* vgen = &K->bar_gen;
+        volatile uint32_t* verr = &K->error;
+        if (*verr != 0u) {
+            ok = 0;
+        } else {
+            uint32_t g = *vgen;
+            __threadfence();
+            uint32_t arrived = atomicAdd(&K->bar_count, 1u) + 1u;
+            if (arrived == gridDim.x) {
+                atomicExch(&K->bar_count, 0u);
+                __threadfence();
+                atomicAdd(&K->bar_gen, 1u);
+            } else {
+                uint32_t spins = 0;
+                while (*vgen == g) {
+                    if (*verr != 0u) { ok = 0; break; }
+                    __nanosleep(32);
+                    if (++spins > SPIN_LIMIT) {
+                        atomicExch(&K->error, 1u);
+                        ok = 0;
+                        break;
+                    }
+                }
+            }
+            __threadfence();
+        }
+        s_ok = ok;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+// Work-group tree of reduce.glsl:5-14 over the 256 values in buf; result in buf[0].
+DEV void block_tree(float4* buf) {
+    const int t = threadIdx.x;
+    __syncthreads();
+    for (int s = 128; s > 0; s >>= 1) {
+        if (t < s) {
+            float4 a = buf[t], b = buf[t + s];
+            buf[t] = make_float4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w);
+        }
+        __syncthreads();
+    }
+}
+
+// total() of reduce_tail.glsl:268-281: thread t sums partials t, t + 256, ... in order,
+// then the tree. Every block calls it and gets the same value.
+DEV float4 total(const float4* part, int n, float4* buf) {
+    const int t = threadIdx.x;
+    float4 s = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    for (int k = t; k < n; k += NT) {
+        float4 v = part[k];
+        s = make_float4(s.x + v.x, s.y + v.y, s.z + v.z, s.w + v.w);
+    }
+    buf[t] = s;
+    block_tree(buf);
+    float4 r = buf[0];
+    __syncthreads();
+    return r;
+}
+
+
+}  // namespace solve
+}  // namespace sprout

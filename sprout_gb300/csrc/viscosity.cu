@@ -1,0 +1,941 @@
+// The implicit viscosity solve on sm_103a, and the second pressure projection after it.
+//
+// Backward-Euler viscosity in the variational form (visc.glsl:39-56): A u = M u*, with
+// A = M + G^T W G over the u and v faces of the active 16 x 16 tiles (cells within one cell
+// of a diffusion number >= implicit_viscosity_min), solved by conjugate gradients
+// preconditioned with an aggregation V-cycle whose smoother is red-black Gauss-Seidel over
+// cells, u and v together (vmg.glsl). The weakly viscous tiles take the explicit step
+// (visc_split.comp) and leave the system.
+//
+// Kernels:
+//   k_visc_split        visc_split.comp: explicit step in the inactive tiles
+//   k_visc_diag         visc_diag.comp: diagonal, warm start, level-0 matrix, clears
+//   k_vmg_build         vmg_build.comp: Galerkin coarse level l from l - 1
+//   k_visc_solve<NU>    the whole solve, ONE persistent cooperative kernel: strain of u*,
+//                       start (visc_apply mode 0), warm start (visc_iter WARM), the first
+//                       V-cycle, then per iteration the update fused with the way down on
+//                       level 0 (visc_mgu.comp), the coarse levels down and up (vmg_down,
+//                       vmg_up) and the way up on level 0 with A z and both step lengths
+//                       (visc_mgz.comp). Phases are separated by the grid barrier of
+//                       solve_common.cuh; every block evaluates the solve's scalars itself
+//                       from the per-tile partial sums (reduce_tail.glsl modes 4, 10-13, 7),
+//                       so the loop exits on the device as soon as the solve has converged.
+//   k_rhs_visc          rhs_visc.comp: right-hand side of the second pressure solve
+//   k_project_visc      project_visc.comp: subtracts the gradient of P2, keeps it
+//
+// Each smoothing pass holds a tile and 2 NU (+1 for A z) cells around it in shared memory and
+// recomputes the ring around the tile that its neighbours also compute (vmg.glsl:142-147): a
+// half-sweep over ring >= h leaves exactly the values that global half-sweeps would, so the
+// result does not depend on the tiling.
+#include <cuda_runtime.h>
+
+#include "dev_common.cuh"
+#include "kernels.h"
+#include "solve_common.cuh"
+
+namespace sprout {
+
+namespace {
+
+using namespace solve;
+
+DEV bool v_live_u(const DevScene& d, int i) { return face_live(d.vel[i].z); }
+DEV bool v_live_v(const DevScene& d, int i) { return face_live(d.vel[i].w); }
+DEV bool v_closed_u(const DevScene& d, int i) { return face_closed(d.vel[i].z); }
+DEV bool v_closed_v(const DevScene& d, int i) { return face_closed(d.vel[i].w); }
+DEV bool in_grid(const DevScene& d, int x, int y) { return x >= 0 && y >= 0 && x < d.W && y < d.H; }
+DEV bool interior(const DevScene& d, int x, int y) { return x >= 1 && y >= 1 && x < d.W - 1 && y < d.H - 1; }
+DEV uint32_t tile_of(const DevScene& d, int x, int y) { return (uint32_t)((y >> 4) * ((d.W + 15) >> 4) + (x >> 4)); }
+DEV float2 f2(float x, float y) { return make_float2(x, y); }
+DEV float dot2(float2 a, float2 b) { return a.x * b.x + a.y * b.y; }
+DEV float2 mask_of(float2 d) { return f2(d.x > 0.0f ? 1.0f : 0.0f, d.y > 0.0f ? 1.0f : 0.0f); }
+
+// G^T of the weighted strain in vs at the faces of cell i (visc_split.comp:12-24).
+DEV float2 gts_vs(const DevScene& d, int i) {
+    const int W = d.W;
+    float2 g = f2(0.0f, 0.0f);
+    if (v_live_u(d, i)) {
+        float c1 = v_closed_u(d, i - W) ? 1.0f : 0.5f, c2 = v_closed_u(d, i + W) ? -1.0f : -0.5f;
+        g.x = d.vs[i - 1].x - d.vs[i].x + d.vs[i].z * c1 + d.vs[i + W].z * c2;
+    }
+    if (v_live_v(d, i)) {
+        float d1 = v_closed_v(d, i - 1) ? 1.0f : 0.5f, d2 = v_closed_v(d, i + 1) ? -1.0f : -0.5f;
+        g.y = d.vs[i - W].y - d.vs[i].y + d.vs[i].z * d1 + d.vs[i + 1].z * d2;
+    }
+    return g;
+}
+
+DEV void store_vel_xy(const DevScene& d, int i, float x, float y) {
+    reinterpret_cast<float2*>(d.vel)[2 * i] = f2(x, y);
+}
+
+// ---- the passes before the solve -------------------------------------------------------
+
+__global__ void __launch_bounds__(256) k_visc_split(DevScene d) {
+    const int cx = blockIdx.x * 16 + threadIdx.x, cy = blockIdx.y * 16 + threadIdx.y;
+    if (!in_grid(d, cx, cy) || d.tiles[blockIdx.y * gridDim.x + blockIdx.x] != 0u) return;
+    if (!interior(d, cx, cy)) return;
+    const int i = cy * d.W + cx;
+    float2 g = gts_vs(d, i);
+    float4 cf = d.coef[i];
+    float4 v = d.vel[i];
+    if (face_live(v.z)) v.x -= g.x / cf.z;
+    if (face_live(v.w)) v.y -= g.y / cf.w;
+    store_vel_xy(d, i, v.x, v.y);
+}
+
+// Strain weights as the implicit system sees them (visc_diag.comp:12-16).
+DEV float2 wts(const DevScene& d, int x, int y, int i) {
+    if (d.tiles[tile_of(d, x, y)] == 0u) return f2(0.0f, 0.0f);
+    float4 w = d.vw[i];
+    return f2(w.x, w.y);
+}
+DEV bool unk_u(const DevScene& d, int x, int y) { return interior(d, x, y) && d.tiles[tile_of(d, x, y)] != 0u && v_live_u(d, y * d.W + x); }
+DEV bool unk_v(const DevScene& d, int x, int y) { return interior(d, x, y) && d.tiles[tile_of(d, x, y)] != 0u && v_live_v(d, y * d.W + x); }
+
+// visc_diag.comp:23-52: the couplings of A at cell (cx, cy) as the multigrid stores them.
+DEV void couplings(const DevScene& d, int cx, int cy, int i, float4& a, float4& b) {
+    const int W = d.W;
+    const bool u = unk_u(d, cx, cy), v = unk_v(d, cx, cy);
+    a = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    b = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (u && unk_u(d, cx - 1, cy)) a.x = -wts(d, cx - 1, cy, i - 1).x;
+    if (v && unk_v(d, cx, cy - 1)) a.w = -wts(d, cx, cy - 1, i - W).x;
+    const float wn = wts(d, cx, cy, i).y;
+    if (wn > 0.0f) {
+        float ua = u ? (v_closed_u(d, i - W) ? 1.0f : 0.5f) : 0.0f;
+        float ub = unk_u(d, cx, cy - 1) ? -(v_closed_u(d, i) ? 1.0f : 0.5f) : 0.0f;
+        float va = v ? (v_closed_v(d, i - 1) ? 1.0f : 0.5f) : 0.0f;
+        float vb = unk_v(d, cx - 1, cy) ? -(v_closed_v(d, i) ? 1.0f : 0.5f) : 0.0f;
+        a.y = wn * ua * ub;
+        a.z = wn * va * vb;
+        b.x = wn * ua * va;
+        b.y = wn * ua * vb;
+    }
+    const float wu = wts(d, cx, cy + 1, i + W).y;
+    if (wu > 0.0f && u) {
+        float ub = -(v_closed_u(d, i + W) ? 1.0f : 0.5f);
+        float va = unk_v(d, cx, cy + 1) ? (v_closed_v(d, i + W - 1) ? 1.0f : 0.5f) : 0.0f;
+        float vb = unk_v(d, cx - 1, cy + 1) ? -(v_closed_v(d, i + W) ? 1.0f : 0.5f) : 0.0f;
+        b.z = wu * ub * va;
+        b.w = wu * ub * vb;
+    }
+}
+
+// visc_diag.comp:56-119, with the multigrid's level 0 (viscosity_precond 1).
+__global__ void __launch_bounds__(256) k_visc_diag(DevScene d) {
+    __shared__ uint32_t s_was;
+    const uint32_t slot = blockIdx.y * gridDim.x + blockIdx.x;
+    const int t = threadIdx.y * 16 + threadIdx.x;
+    if (t == 0) s_was = d.vtile[slot];
+    __syncthreads();
+    if (t == 0) d.vtile[slot] = d.tiles[slot];
+    const int cx = blockIdx.x * 16 + threadIdx.x, cy = blockIdx.y * 16 + threadIdx.y;
+    if (!in_grid(d, cx, cy)) return;
+    const int W = d.W;
+    const int i = cy * W + cx;
+    const bool on = d.tiles[slot] != 0u;
+    float2 dg = f2(1.0f, 1.0f);
+    const bool inner = interior(d, cx, cy);
+    if (inner) {
+        float4 cf = d.coef[i];
+        float2 me = wts(d, cx, cy, i);
+        if (v_live_u(d, i)) {
+            float c1 = v_closed_u(d, i - W) ? 1.0f : 0.5f, c2 = v_closed_u(d, i + W) ? 1.0f : 0.5f;
+            dg.x = cf.z + wts(d, cx - 1, cy, i - 1).x + me.x + me.y * c1 * c1 + wts(d, cx, cy + 1, i + W).y * c2 * c2;
+        }
+        if (v_live_v(d, i)) {
+            float d1 = v_closed_v(d, i - 1) ? 1.0f : 0.5f, d2 = v_closed_v(d, i + 1) ? 1.0f : 0.5f;
+            dg.y = cf.w + wts(d, cx, cy - 1, i - W).x + me.x + me.y * d1 * d1 + wts(d, cx + 1, cy, i + 1).y * d2 * d2;
+        }
+    }
+    float4 o = d.vw[i];
+    o.z = dg.x;
+    o.w = dg.y;
+    float2 dv = f2(0.0f, 0.0f);
+    if (d.P->viscosity_warm != 0 && on && inner) {
+        const float ratio = d.S->dt / d.S->dt_prev;
+        float2 old = d.vd[i];
+        dv = f2(old.x * ratio * (v_live_u(d, i) ? 1.0f : 0.0f), old.y * ratio * (v_live_v(d, i) ? 1.0f : 0.0f));
+    }
+    d.vd[i] = dv;
+    const float2 zero = f2(0.0f, 0.0f);
+    if (!on) {
+        o.x = 0.0f;
+        o.y = 0.0f;
+        d.vs[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        d.vr[i] = zero;
+        d.vp[i] = zero;
+        d.vq[i] = zero;
+    }
+    if (on || s_was != 0u) {
+        float4 a = make_float4(0.0f, 0.0f, 0.0f, 0.0f), b = a;
+        float2 dm = zero;
+        if (on && inner) {
+            couplings(d, cx, cy, i, a, b);
+            dm = f2(dg.x * (v_live_u(d, i) ? 1.0f : 0.0f), dg.y * (v_live_v(d, i) ? 1.0f : 0.0f));
+        }
+        if (!on) {
+            d.vmz[i] = zero;
+            d.vaz[i] = zero;
+            d.vr2[i] = zero;
+            d.vq2[i] = zero;
+        }
+        d.vma[i] = a;
+        d.vmb[i] = b;
+        d.vmd[i] = dm;
+    }
+    // vw last: the couplings above read vw.xy of the neighbours, which this pass leaves as
+    // they were wherever a tile is active (and wts() reads none in an inactive one)
+    d.vw[i] = o;
+}
+
+// vmg_build.comp: level l of the viscosity multigrid from level l - 1. One block per coarse
+// tile of level l.
+__global__ void __launch_bounds__(256) k_vmg_build(DevScene d, int l) {
+    __shared__ uint32_t s_state;
+    const Lv F = lev(d.lv, l - 1), C = lev(d.lv, l);
+    const int t = threadIdx.y * 16 + threadIdx.x;
+    if (t == 0) {
+        const int tfx = tiles_x(F), tfy = tiles_y(F);
+        uint32_t on = 0u;
+        for (int k = 0; k < 4; k++) {
+            int fx = 2 * (int)blockIdx.x + (k & 1), fy = 2 * (int)blockIdx.y + (k >> 1);
+            if (fx < tfx && fy < tfy) {
+                uint32_t s = (uint32_t)(fy * tfx + fx);
+                on |= (l - 1 == 0) ? d.tiles[s] : d.vtile[F.toff + s];
+            }
+        }
+        uint32_t slot = (uint32_t)C.toff + blockIdx.y * gridDim.x + blockIdx.x;
+        uint32_t was = d.vtile[slot];
+        d.vtile[slot] = on != 0u ? 1u : 0u;
+        s_state = (on != 0u ? 1u : 0u) | (was != 0u ? 2u : 0u);
+    }
+    __syncthreads();
+    const uint32_t state = s_state;
+    if (state == 0u) return;
+    const int ccx = blockIdx.x * 16 + threadIdx.x, ccy = blockIdx.y * 16 + threadIdx.y;
+    if (!l_inside(C, ccx, ccy)) return;
+    const int o = l_at(C, ccx, ccy);
+    if ((state & 1u) == 0u) {
+        d.vma[o] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        d.vmb[o] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        d.vmd[o] = f2(0.0f, 0.0f);
+        return;
+    }
+    const int UVX[4] = {0, -1, 0, -1}, UVY[4] = {0, 0, 1, 1};
+    float2 D = f2(0.0f, 0.0f);
+    float4 A = make_float4(0.0f, 0.0f, 0.0f, 0.0f), B = A;
+    for (int k = 0; k < 4; k++) {
+        const int abx = k & 1, aby = k >> 1;
+        const int fx = 2 * ccx + abx, fy = 2 * ccy + aby;
+        if (!l_inside(F, fx, fy)) continue;
+        const int i = l_at(F, fx, fy);
+        const float4 a = d.vma[i], b = d.vmb[i];
+        const float2 dd = d.vmd[i];
+        D.x += dd.x;
+        D.y += dd.y;
+        if (abx == 1) { D.x += 2.0f * a.x; D.y += 2.0f * a.z; }
+        else { A.x += a.x; A.z += a.z; }
+        if (aby == 1) { D.x += 2.0f * a.y; D.y += 2.0f * a.w; }
+        else { A.y += a.y; A.w += a.w; }
+        for (int m = 0; m < 4; m++) {
+            const int rx = ((fx + UVX[m]) >> 1) - ccx, ry = ((fy + UVY[m]) >> 1) - ccy;
+            const int s = (rx == 0 ? 0 : 1) + (ry == 0 ? 0 : 2);
+            const float bm = m == 0 ? b.x : m == 1 ? b.y : m == 2 ? b.z : b.w;
+            if (s == 0) B.x += bm; else if (s == 1) B.y += bm; else if (s == 2) B.z += bm; else B.w += bm;
+        }
+    }
+    d.vma[o] = A;
+    d.vmb[o] = B;
+    d.vmd[o] = f2(maxf(D.x, 0.0f), maxf(D.y, 0.0f));
+}
+
+// ---- the persistent solve ----------------------------------------------------------------
+
+template <int NU>
+struct VCfg {
+    static constexpr int HALO = 2 * NU;
+    static constexpr int RHMAX = HALO + 1;            // the way up on level 0 forms A z too
+    static constexpr int RWMAX = 16 + 2 * RHMAX;
+    static constexpr int NMAX = RWMAX * RWMAX;
+};
+
+template <int NU>
+struct VSmem {
+    float4 sa[VCfg<NU>::NMAX];
+    float4 sb[VCfg<NU>::NMAX];
+    float2 sd[VCfg<NU>::NMAX];
+    float2 sx[VCfg<NU>::NMAX];
+    float2 sr[VCfg<NU>::NMAX];
+    float2 sres[NT];
+    float4 buf[NT];
+};
+
+// The solve's scalars (SolveBuf v_*, common.glsl:138-149), one copy per block.
+struct VScal {
+    float rz, alpha, beta, r0, rr, pq;
+    uint32_t done, iters;
+};
+
+// One region of RH cells around a 16 x 16 tile: the matrix, right-hand side and iterate.
+template <int NU, int RH>
+struct Region {
+    static constexpr int RW = 16 + 2 * RH;
+    static constexpr int N = RW * RW;
+    static constexpr int PER = (N + NT - 1) / NT;
+    VSmem<NU>& s;
+    int ox, oy;   // first cell of the tile
+
+    DEV int cell_x(int k) const { return ox - RH + k % RW; }
+    DEV int cell_y(int k) const { return oy - RH + k / RW; }
+    DEV static bool red(int k) { return (((k % RW) + (k / RW)) & 1) == 0; }   // ox, oy, 2 RH even
+    DEV static bool in_ring(int k, int lo) {
+        int lx = k % RW, ly = k / RW;
+        return lx >= lo && ly >= lo && lx < RW - lo && ly < RW - lo;
+    }
+    DEV static int tile_slot(int t) { return ((t >> 4) + RH) * RW + (t & 15) + RH; }
+
+    // offd of vmg.glsl:70-78 at slot k (x in sx)
+    DEV float2 offd(int k) const {
+        const float4 a = s.sa[k], b = s.sb[k];
+        const float2 xl = s.sx[k - 1], xr = s.sx[k + 1], xd = s.sx[k - RW], xu = s.sx[k + RW];
+        float u = a.x * xl.x + s.sa[k + 1].x * xr.x + a.y * xd.x + s.sa[k + RW].y * xu.x
+                + b.x * s.sx[k].y + b.y * xl.y + b.z * xu.y + b.w * s.sx[k + RW - 1].y;
+        float v = a.z * xl.y + s.sa[k + 1].z * xr.y + a.w * xd.y + s.sa[k + RW].w * xu.y
+                + b.x * s.sx[k].x + s.sb[k + 1].y * xr.x + s.sb[k - RW].z * xd.x + s.sb[k + 1 - RW].w * s.sx[k + 1 - RW].x;
+        return f2(u, v);
+    }
+    DEV float2 relax(int k) const {
+        const float2 dd = s.sd[k];
+        const float2 o = offd(k);
+        const float2 rr = s.sr[k];
+        const float sx_ = rr.x - o.x, sy_ = rr.y - o.y;
+        return f2(dd.x > 0.0f ? sx_ / dd.x : 0.0f, dd.y > 0.0f ? sy_ / dd.y : 0.0f);
+    }
+
+    // load_region (vmg.glsl:90-111) with the right-hand side from rhs(i)
+    template <class F>
+    DEV void load(const DevScene& d, const Lv& L, F rhs) const {
+        for (int k = threadIdx.x; k < N; k += NT) {
+            const int x = cell_x(k), y = cell_y(k);
+            float4 a = make_float4(0.0f, 0.0f, 0.0f, 0.0f), b = a;
+            float2 dd = f2(0.0f, 0.0f), r = dd;
+            if (l_inside(L, x, y)) {
+                const int i = l_at(L, x, y);
+                a = d.vma[i];
+                b = d.vmb[i];
+                dd = d.vmd[i];
+                r = rhs(i);
+            }
+            s.sa[k] = a;
+            s.sb[k] = b;
+            s.sd[k] = dd;
+            s.sr[k] = r;
+        }
+    }
+
+    // half_sweep (vmg.glsl:121-134)
+    DEV void half_sweep(bool is_red, int lo) const {
+        float2 nv[PER];
+#pragma unroll
+        for (int j = 0; j < PER; j++) {
+            const int k = threadIdx.x + NT * j;
+            nv[j] = f2(0.0f, 0.0f);
+            if (k < N && in_ring(k, lo) && red(k) == is_red) nv[j] = relax(k);
+        }
+        __syncthreads();
+#pragma unroll
+        for (int j = 0; j < PER; j++) {
+            const int k = threadIdx.x + NT * j;
+            if (k < N && in_ring(k, lo) && red(k) == is_red) s.sx[k] = nv[j];
+        }
+        __syncthreads();
+    }
+
+    // way_down (vmg.glsl:145-168) on the loaded region: pre-smoothing from zero, the tile's
+    // values to vmx and, unless coarsest, its residual summed over 2 x 2 aggregates into
+    // vmr of the next level.
+    DEV void way_down(const DevScene& d, const Lv& L, const Lv* LC) const {
+        for (int k = threadIdx.x; k < N; k += NT) {
+            const float2 dd = s.sd[k], r = s.sr[k];
+            const float2 x = f2(dd.x > 0.0f ? r.x / dd.x : 0.0f, dd.y > 0.0f ? r.y / dd.y : 0.0f);
+            s.sx[k] = red(k) ? x : f2(0.0f, 0.0f);
+        }
+        __syncthreads();
+        for (int h = 1; h < VCfg<NU>::HALO; h++) half_sweep((h & 1) == 0, h);
+        const int t = threadIdx.x;
+        const int k = tile_slot(t);
+        const int cx = ox + (t & 15), cy = oy + (t >> 4);
+        const float2 x = s.sx[k], dd = s.sd[k], r = s.sr[k];
+        const float2 o = offd(k);
+        const float2 m = mask_of(dd);
+        const float2 res = f2((r.x - dd.x * x.x - o.x) * m.x, (r.y - dd.y * x.y - o.y) * m.y);
+        if (l_inside(L, cx, cy)) d.vmx[l_at(L, cx, cy)] = x;
+        if (LC) {
+            s.sres[t] = res;
+            __syncthreads();
+            const int ccx = cx >> 1, ccy = cy >> 1;
+            if (((t & 1) | ((t >> 4) & 1)) == 0 && l_inside(*LC, ccx, ccy)) {
+                const float2 a0 = s.sres[t], a1 = s.sres[t + 1], a2 = s.sres[t + 16], a3 = s.sres[t + 17];
+                d.vmr[l_at(*LC, ccx, ccy)] = f2(a0.x + a1.x + a2.x + a3.x, a0.y + a1.y + a2.y + a3.y);
+            }
+        }
+        __syncthreads();
+    }
+
+    // the start of a way up (vmg_up.comp:37-46, visc_mgz.comp:33-38): x = vmx plus the
+    // coarse values (LC, if any), zero where a face is no unknown; then HALO half-sweeps,
+    // black first.
+    DEV void way_up(const DevScene& d, const Lv& L, const Lv* LC) const {
+        for (int k = threadIdx.x; k < N; k += NT) {
+            const int x = cell_x(k), y = cell_y(k);
+            float2 v = f2(0.0f, 0.0f);
+            if (l_inside(L, x, y)) {
+                v = d.vmx[l_at(L, x, y)];
+                if (LC) {
+                    const float2 zc = d.vmz[l_at(*LC, x >> 1, y >> 1)];
+                    v = f2(v.x + zc.x, v.y + zc.y);
+                }
+            }
+            const float2 m = mask_of(s.sd[k]);
+            s.sx[k] = f2(v.x * m.x, v.y * m.y);
+        }
+        __syncthreads();
+        for (int h = 1; h <= VCfg<NU>::HALO; h++) half_sweep((h & 1) == 0, h);
+    }
+};
+
+template <int NU>
+struct VSolve {
+    const DevScene& d;
+    VSmem<NU>& s;
+    VScal& K;
+    int n;   // level-0 tiles (partial slots per half)
+
+    DEV const uint32_t* list(int l) const { return d.vlist + d.lv.toff[l]; }
+
+    // Every block sums one half of the partials in the shader's order (reduce_tail.glsl).
+    DEV float4 sum(int half) const { return total(d.partials + half * n, n, s.buf); }
+
+    // group_sum (reduce.glsl:5-14) of this thread's acc into the tile's slot of one half
+    DEV void tile_sum(float4 acc, int half, uint32_t slot) const {
+        s.buf[threadIdx.x] = acc;
+        block_tree(s.buf);
+        if (threadIdx.x == 0) d.partials[half * n + slot] = s.buf[0];
+        __syncthreads();
+    }
+
+    // the compact lists of active tiles per level (block 0)
+    DEV void build_lists(int nlev) const {
+        __shared__ uint32_t wsum[NT / 32];
+        __shared__ uint32_t s_base;
+        for (int l = 0; l <= nlev; l++) {
+            const Lv L = lev(d.lv, l);
+            const int T = tiles_x(L) * tiles_y(L);
+            const uint32_t* flags = l == 0 ? d.tiles : d.vtile + L.toff;
+            uint32_t* out = d.vlist + L.toff;
+            if (threadIdx.x == 0) s_base = 0u;
+            __syncthreads();
+            for (int b0 = 0; b0 < T; b0 += NT) {
+                const int k = b0 + threadIdx.x;
+                const bool on = k < T && flags[k] != 0u;
+                const uint32_t bal = __ballot_sync(0xffffffffu, on);
+                const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+                if (lane == 0) wsum[w] = __popc(bal);
+                __syncthreads();
+                uint32_t before = s_base;
+                for (int j = 0; j < w; j++) before += wsum[j];
+                before += __popc(bal & ((1u << lane) - 1u));
+                if (on) out[before] = (uint32_t)k;
+                __syncthreads();
+                if (threadIdx.x == 0) {
+                    uint32_t tot = 0;
+                    for (int j = 0; j < NT / 32; j++) tot += wsum[j];
+                    s_base += tot;
+                }
+                __syncthreads();
+            }
+            if (threadIdx.x == 0) d.vcount[l] = s_base;
+            __syncthreads();
+        }
+    }
+
+    // visc_strain.comp: the weighted strain of the current velocities in the active tiles
+    DEV void strain() const {
+        const Lv L0 = lev(d.lv, 0);
+        const int tw = tiles_x(L0), T = n;
+        const int W = d.W;
+        for (int tt = blockIdx.x; tt < T; tt += gridDim.x) {
+            if (d.tiles[tt] == 0u) continue;
+            const int cx = (tt % tw) * 16 + (threadIdx.x & 15), cy = (tt / tw) * 16 + (threadIdx.x >> 4);
+            if (!in_grid(d, cx, cy)) continue;
+            const int i = cy * W + cx;
+            const float4 w4 = d.vw[i];
+            float4 o = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            auto vu = [&](int j) { float4 v = d.vel[j]; return face_live(v.z) ? v.x : 0.0f; };
+            auto vv = [&](int j) { float4 v = d.vel[j]; return face_live(v.w) ? v.y : 0.0f; };
+            if (w4.x > 0.0f) {
+                o.x = w4.x * (vu(i + 1) - vu(i));
+                o.y = w4.x * (vv(i + W) - vv(i));
+            }
+            if (w4.y > 0.0f) {
+                float ua = vu(i), ub = vu(i - W), va = vv(i), vb = vv(i - 1);
+                if (v_closed_u(d, i) && v_live_u(d, i - W)) ua = -ub;
+                if (v_closed_u(d, i - W) && v_live_u(d, i)) ub = -ua;
+                if (v_closed_v(d, i) && v_live_v(d, i - 1)) va = -vb;
+                if (v_closed_v(d, i - 1) && v_live_v(d, i)) vb = -va;
+                o.z = w4.y * 0.5f * ((ua - ub) + (va - vb));
+            }
+            d.vs[i] = o;
+        }
+    }
+
+    // visc_apply.comp mode 0 over every level-0 tile: r = -G^T W G u*, z = r / diag in the
+    // active ones, zero partials (both halves) in the others.
+    DEV void start() const {
+        const Lv L0 = lev(d.lv, 0);
+        const int tw = tiles_x(L0);
+        for (int tt = blockIdx.x; tt < n; tt += gridDim.x) {
+            if (d.tiles[tt] == 0u) {
+                if (threadIdx.x == 0) {
+                    d.partials[tt] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                    d.partials[n + tt] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                }
+                continue;
+            }
+            const int cx = (tt % tw) * 16 + (threadIdx.x & 15), cy = (tt / tw) * 16 + (threadIdx.x >> 4);
+            float4 acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            if (in_grid(d, cx, cy)) {
+                const int i = cy * d.W + cx;
+                if (interior(d, cx, cy)) {
+                    const float2 g = gts_vs(d, i);
+                    const float lu = v_live_u(d, i) ? 1.0f : 0.0f, lv = v_live_v(d, i) ? 1.0f : 0.0f;
+                    const float4 w4 = d.vw[i];
+                    const float2 r = f2(-g.x * lu, -g.y * lv);
+                    const float2 z = f2(r.x / w4.z, r.y / w4.w);
+                    d.vr[i] = r;
+                    d.vp[i] = z;
+                    acc = make_float4(dot2(r, z), dot2(r, r), 0.0f, 0.0f);
+                } else {
+                    d.vr[i] = f2(0.0f, 0.0f);
+                    d.vp[i] = f2(0.0f, 0.0f);
+                }
+            }
+            tile_sum(acc, 0, (uint32_t)tt);
+        }
+    }
+
+    // visc_iter.comp WARM at one interior cell: the step d of the warm start
+    DEV float2 warm_dir(int x, int y) const {
+        if (!in_grid(d, x, y) || !interior(d, x, y)) return f2(0.0f, 0.0f);
+        return d.vd[y * d.W + x];
+    }
+    DEV float4 strain_dir(int cx, int cy) const {
+        if (!in_grid(d, cx, cy)) return make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        const int W = d.W, i = cy * W + cx;
+        float4 o = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        const float4 w = d.vw[i];
+        auto U = [&](int x, int y, int j) { return v_live_u(d, j) ? warm_dir(x, y).x : 0.0f; };
+        auto V = [&](int x, int y, int j) { return v_live_v(d, j) ? warm_dir(x, y).y : 0.0f; };
+        if (w.x > 0.0f) {
+            o.x = w.x * (U(cx + 1, cy, i + 1) - U(cx, cy, i));
+            o.y = w.x * (V(cx, cy + 1, i + W) - V(cx, cy, i));
+        }
+        if (w.y > 0.0f) {
+            float ua = U(cx, cy, i), ub = U(cx, cy - 1, i - W), va = V(cx, cy, i), vb = V(cx - 1, cy, i - 1);
+            if (v_closed_u(d, i) && v_live_u(d, i - W)) ua = -ub;
+            if (v_closed_u(d, i - W) && v_live_u(d, i)) ub = -ua;
+            if (v_closed_v(d, i) && v_live_v(d, i - 1)) va = -vb;
+            if (v_closed_v(d, i - 1) && v_live_v(d, i)) vb = -va;
+            o.z = w.y * 0.5f * ((ua - ub) + (va - vb));
+        }
+        return o;
+    }
+    DEV void warm(int half) const {
+        const Lv L0 = lev(d.lv, 0);
+        const int tw = tiles_x(L0);
+        const uint32_t cnt = d.vcount[0];
+        const int W = d.W;
+        for (uint32_t j = blockIdx.x; j < cnt; j += gridDim.x) {
+            const uint32_t tt = list(0)[j];
+            const int cx = (int)(tt % tw) * 16 + (threadIdx.x & 15), cy = (int)(tt / tw) * 16 + (threadIdx.x >> 4);
+            float4 acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            if (in_grid(d, cx, cy) && interior(d, cx, cy)) {
+                const int i = cy * W + cx;
+                float2 g = f2(0.0f, 0.0f);
+                if (v_live_u(d, i)) {
+                    float c1 = v_closed_u(d, i - W) ? 1.0f : 0.5f, c2 = v_closed_u(d, i + W) ? -1.0f : -0.5f;
+                    const float4 sl = strain_dir(cx - 1, cy), sc = strain_dir(cx, cy), su = strain_dir(cx, cy + 1);
+                    g.x = sl.x - sc.x + sc.z * c1 + su.z * c2;
+                }
+                if (v_live_v(d, i)) {
+                    float d1 = v_closed_v(d, i - 1) ? 1.0f : 0.5f, d2 = v_closed_v(d, i + 1) ? -1.0f : -0.5f;
+                    const float4 sd_ = strain_dir(cx, cy - 1), sc = strain_dir(cx, cy), sr_ = strain_dir(cx + 1, cy);
+                    g.y = sd_.y - sc.y + sc.z * d1 + sr_.z * d2;
+                }
+                const float lu = v_live_u(d, i) ? 1.0f : 0.0f, lv = v_live_v(d, i) ? 1.0f : 0.0f;
+                const float4 cf = d.coef[i];
+                const float2 p = warm_dir(cx, cy);
+                const float2 dd = f2(p.x * lu, p.y * lv);
+                const float2 q = f2((cf.z * dd.x + g.x) * lu, (cf.w * dd.y + g.y) * lv);
+                const float4 v = d.vel[i];
+                store_vel_xy(d, i, v.x + dd.x, v.y + dd.y);
+                const float2 r0 = d.vr[i];
+                const float2 r = f2(r0.x - q.x, r0.y - q.y);
+                d.vr[i] = r;
+                const float4 w4 = d.vw[i];
+                const float2 z = f2(r.x / w4.z, r.y / w4.w);
+                acc = make_float4(dot2(r, z), dot2(r, r), 0.0f, 0.0f);
+            }
+            tile_sum(acc, half, tt);
+        }
+    }
+
+    // vmg_down.comp on level l (l = 0 at the start of a solve, right-hand side vr)
+    DEV void down(int l, int nlev, const float2* rhs0) const {
+        const Lv L = lev(d.lv, l);
+        const Lv LC = lev(d.lv, l + 1);
+        const int tw = tiles_x(L);
+        const uint32_t cnt = d.vcount[l];
+        for (uint32_t j = blockIdx.x; j < cnt; j += gridDim.x) {
+            const uint32_t tt = list(l)[j];
+            Region<NU, VCfg<NU>::HALO> R{s, (int)(tt % tw) * 16, (int)(tt / tw) * 16};
+            if (l == 0) R.load(d, L, [&](int i) { return rhs0[i]; });
+            else R.load(d, L, [&](int i) { return d.vmr[i]; });
+            __syncthreads();
+            R.way_down(d, L, l == nlev ? nullptr : &LC);
+        }
+    }
+
+    // vmg_up.comp on a coarse level l: the finished values to vmz
+    DEV void up(int l, int nlev) const {
+        const Lv L = lev(d.lv, l);
+        const Lv LC = lev(d.lv, l + 1);
+        const int tw = tiles_x(L);
+        const uint32_t cnt = d.vcount[l];
+        for (uint32_t j = blockIdx.x; j < cnt; j += gridDim.x) {
+            const uint32_t tt = list(l)[j];
+            Region<NU, VCfg<NU>::HALO> R{s, (int)(tt % tw) * 16, (int)(tt / tw) * 16};
+            R.load(d, L, [&](int i) { return d.vmr[i]; });
+            __syncthreads();
+            R.way_up(d, L, l == nlev ? nullptr : &LC);
+            const int t = threadIdx.x;
+            const int cx = R.ox + (t & 15), cy = R.oy + (t >> 4);
+            if (l_inside(L, cx, cy)) d.vmz[l_at(L, cx, cy)] = s.sx[R.tile_slot(t)];
+            __syncthreads();
+        }
+    }
+
+    // visc_mgz.comp: the way up on level 0 with A z and the partial sums of r.z, z.A z, z.q
+    DEV void mgz(const float2* rn, const float2* qn, int half) const {
+        const Lv L = lev(d.lv, 0);
+        const Lv LC = lev(d.lv, 1);
+        const int tw = tiles_x(L);
+        const uint32_t cnt = d.vcount[0];
+        for (uint32_t j = blockIdx.x; j < cnt; j += gridDim.x) {
+            const uint32_t tt = list(0)[j];
+            Region<NU, VCfg<NU>::HALO + 1> R{s, (int)(tt % tw) * 16, (int)(tt / tw) * 16};
+            R.load(d, L, [&](int i) { return rn[i]; });
+            __syncthreads();
+            R.way_up(d, L, &LC);
+            const int t = threadIdx.x;
+            const int cx = R.ox + (t & 15), cy = R.oy + (t >> 4);
+            const int k = R.tile_slot(t);
+            float4 acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            if (l_inside(L, cx, cy)) {
+                const int i = l_at(L, cx, cy);
+                const float2 z = s.sx[k], dd = s.sd[k];
+                const float2 o = R.offd(k);
+                const float2 az = f2(dd.x * z.x + o.x, dd.y * z.y + o.y);
+                d.vmz[i] = z;
+                d.vaz[i] = az;
+                acc = make_float4(dot2(s.sr[k], z), dot2(z, az), dot2(z, qn[i]), 0.0f);
+            }
+            tile_sum(acc, half, tt);
+        }
+    }
+
+    // visc_mgu.comp: p, q, x, r of the iteration and the way down on level 0 from the new r
+    DEV void mgu(const float2* ro, const float2* qo, float2* rn, float2* qn, int half) const {
+        const Lv L = lev(d.lv, 0);
+        const Lv LC = lev(d.lv, 1);
+        const int tw = tiles_x(L);
+        const uint32_t cnt = d.vcount[0];
+        const float a = K.alpha, b = K.beta;
+        auto new_q = [&](int i) {
+            const float2 sq = d.vaz[i];
+            if (b == 0.0f) return sq;
+            const float2 q = qo[i];
+            return f2(sq.x + b * q.x, sq.y + b * q.y);
+        };
+        for (uint32_t j = blockIdx.x; j < cnt; j += gridDim.x) {
+            const uint32_t tt = list(0)[j];
+            Region<NU, VCfg<NU>::HALO> R{s, (int)(tt % tw) * 16, (int)(tt / tw) * 16};
+            const int t = threadIdx.x;
+            const int cx = R.ox + (t & 15), cy = R.oy + (t >> 4);
+            float4 acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            if (cx < d.W && cy < d.H) {
+                const int i = cy * d.W + cx;
+                const float2 z = d.vmz[i];
+                float2 p = z;
+                if (b != 0.0f) {
+                    const float2 po = d.vp[i];
+                    p = f2(z.x + b * po.x, z.y + b * po.y);
+                }
+                const float2 q = new_q(i);
+                const float2 r0 = ro[i];
+                const float2 r = f2(r0.x - a * q.x, r0.y - a * q.y);
+                if (interior(d, cx, cy)) {
+                    float4 v = d.vel[i];
+                    if (face_live(v.z)) v.x += a * p.x;
+                    if (face_live(v.w)) v.y += a * p.y;
+                    store_vel_xy(d, i, v.x, v.y);
+                    const float2 dv = d.vd[i];
+                    d.vd[i] = f2(dv.x + a * p.x, dv.y + a * p.y);
+                }
+                d.vp[i] = p;
+                qn[i] = q;
+                rn[i] = r;
+                acc = make_float4(0.0f, dot2(r, r), dot2(p, q), 0.0f);
+            }
+            R.load(d, L, [&](int i) {
+                const float2 q = new_q(i);
+                const float2 r0 = ro[i];
+                return f2(r0.x - a * q.x, r0.y - a * q.y);
+            });
+            __syncthreads();
+            R.way_down(d, L, &LC);
+            tile_sum(acc, half, tt);
+        }
+    }
+
+    // record_visc_coarse (mod.rs:2838-2853): the coarse levels down, then up
+    DEV bool coarse(int nlev) const {
+        for (int l = 1; l <= nlev; l++) {
+            down(l, nlev, nullptr);
+            if (!grid_sync(d.K)) return false;
+        }
+        for (int l = nlev; l >= 1; l--) {
+            up(l, nlev);
+            if (!grid_sync(d.K)) return false;
+        }
+        return true;
+    }
+};
+
+}  // namespace
+
+// The whole viscosity solve (record_viscosity_solve, mod.rs:2867-2908, with the
+// multigrid preconditioner). `restrain`: take the strain of u* again first (the first
+// pressure solve changed the velocity since visc_setup).
+template <int NU>
+__global__ void __launch_bounds__(NT) k_visc_solve(DevScene d, int restrain) {
+    __shared__ VSmem<NU> sm;
+    __shared__ VScal K;
+    const DevParams* P = d.P;
+    const int nlev = P->visc_levels;
+    VSolve<NU> V{d, sm, K, d.nwg};
+    const float tz = P->tol[2];
+    if (blockIdx.x == 0) V.build_lists(nlev);
+    if (restrain) V.strain();
+    if (!grid_sync(d.K)) return;
+    V.start();
+    if (!grid_sync(d.K)) return;
+    {   // cg_reduce mode 4
+        const float4 a = V.sum(0);
+        if (threadIdx.x == 0) {
+            K.rz = a.x;
+            K.r0 = a.y;
+            K.rr = a.y;
+            K.beta = 0.0f;
+            K.alpha = 0.0f;
+            K.pq = 0.0f;
+            K.iters = 0u;
+            K.done = (a.y <= 1e-30f || a.x <= 0.0f) ? 1u : 0u;
+        }
+        __syncthreads();
+    }
+    int half = 1;
+    if (P->viscosity_warm != 0 && K.done == 0u) {
+        V.warm(half);
+        if (!grid_sync(d.K)) return;
+        const float4 a = V.sum(half);   // mode 10
+        if (threadIdx.x == 0) {
+            K.rz = a.x;
+            K.rr = a.y;
+            K.beta = 0.0f;
+            K.done = (a.y <= tz * tz * K.r0 || a.x <= 0.0f) ? 1u : 0u;
+        }
+        __syncthreads();
+        half ^= 1;
+    }
+    // the two parities of the residual and of q: the current residual alternates between
+    // vr and vr2 (visc_mgu.comp writes the other one)
+    float2 *ra = d.vr, *rb = d.vr2, *qa = d.vq, *qb = d.vq2;
+    if (K.done == 0u) {
+        V.down(0, nlev, ra);
+        if (!grid_sync(d.K)) return;
+        if (!V.coarse(nlev)) return;
+        V.mgz(ra, qa, half);
+        if (!grid_sync(d.K)) return;
+        const float4 a = V.sum(half);   // mode 11
+        if (threadIdx.x == 0) {
+            K.rz = a.x;
+            K.beta = 0.0f;
+            K.pq = a.y;
+            K.alpha = a.y > 0.0f ? a.x / a.y : 0.0f;
+            if (a.x <= 0.0f || a.y <= 0.0f) K.done = 1u;
+        }
+        __syncthreads();
+        half ^= 1;
+    }
+    for (uint32_t k = 0; k < P->viscosity_max_iters && K.done == 0u; k++) {
+        V.mgu(ra, qa, rb, qb, half);
+        if (!grid_sync(d.K)) return;
+        {
+            const float4 a = V.sum(half);   // mode 12
+            if (threadIdx.x == 0) {
+                const uint32_t was = K.done;
+                K.iters += 1u - was;
+                const uint32_t now = a.y <= tz * tz * K.r0 ? 1u : 0u;
+                if (was == 0u) K.rr = a.y;
+                K.pq = a.z;
+                K.done = was > now ? was : now;
+            }
+            __syncthreads();
+            half ^= 1;
+        }
+        if (K.done != 0u) break;
+        if (!V.coarse(nlev)) return;
+        V.mgz(rb, qb, half);
+        if (!grid_sync(d.K)) return;
+        {
+            const float4 a = V.sum(half);   // mode 13
+            if (threadIdx.x == 0) {
+                const float beta = (K.done == 0u && K.rz > 0.0f) ? a.x / K.rz : 0.0f;
+                const float pq = a.y + 2.0f * beta * a.z + beta * beta * K.pq;
+                K.beta = beta;
+                K.alpha = (K.done == 0u && pq > 0.0f) ? a.x / pq : 0.0f;
+                K.rz = a.x;
+            }
+            __syncthreads();
+            half ^= 1;
+        }
+        float2* t = ra;
+        ra = rb;
+        rb = t;
+        t = qa;
+        qa = qb;
+        qb = t;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {   // mode 7
+        SolveState* G = d.K;
+        if (K.iters > G->v_it_max) G->v_it_max = K.iters;
+        if (K.done == 0u) G->v_unconv += 1u;
+        const float rel = K.r0 > 0.0f ? sqrtf(K.rr / K.r0) : 0.0f;
+        G->v_res_max = maxf(G->v_res_max, rel);
+        G->v_iters = K.iters;
+        G->v_done = K.done;
+        G->v_rr = K.rr;
+        G->v_r0 = K.r0;
+    }
+}
+
+namespace {
+
+// rhs_visc.comp
+__global__ void __launch_bounds__(256) k_rhs_visc(DevScene d) {
+    const int cx = blockIdx.x * 16 + threadIdx.x, cy = blockIdx.y * 16 + threadIdx.y;
+    if (cx >= d.W || cy >= d.H) return;
+    const int W = d.W;
+    const int i = cy * W + cx;
+    const float D = d.mgd[i];
+    if (D <= 0.0f) {
+        d.prhs[i].z = 0.0f;
+        return;
+    }
+    const float4 w = d.mga[i];
+    const float p1 = d.prhs[i].z;
+    float ap = D * p1;
+    if (d.mgd[i - 1] > 0.0f) ap -= w.x * d.prhs[i - 1].z;
+    if (d.mgd[i + 1] > 0.0f) ap -= w.y * d.prhs[i + 1].z;
+    if (d.mgd[i - W] > 0.0f) ap -= w.z * d.prhs[i - W].z;
+    if (d.mgd[i + W] > 0.0f) ap -= w.w * d.prhs[i + W].z;
+    const float aL = __ldg(&d.solid[i]).x, aB = __ldg(&d.solid[i]).y, aR = __ldg(&d.solid[i + 1]).x, aT = __ldg(&d.solid[i + W]).y;
+    const float4 vme = d.vel[i];
+    const float div = aR * d.vel[i + 1].x - aL * vme.x + aT * d.vel[i + W].y - aB * vme.y;
+    const float4 r = d.prhs[i];
+    d.prhs[i] = make_float4(ap - div, r.y, p1, 0.0f);
+    if (d.P->viscous_warm != 0) d.pres[i].x = p1 + d.p2keep[i] * (d.S->dt / d.S->dt_prev);
+}
+
+// project_visc.comp
+DEV float p2_of(const DevScene& d, int i) { return d.mgd[i] > 0.0f ? d.pres[i].x - d.prhs[i].z : 0.0f; }
+
+__global__ void __launch_bounds__(256) k_project_visc(DevScene d) {
+    const int cx = blockIdx.x * 16 + threadIdx.x, cy = blockIdx.y * 16 + threadIdx.y;
+    float m = 0.0f;
+    if (cx >= 1 && cy >= 1 && cx < d.W && cy < d.H) {
+        const int i = cy * d.W + cx;
+        const float pc = p2_of(d, i);
+        d.p2keep[i] = pc;
+        const float4 cf = d.coef[i];
+        float4 me = d.vel[i];
+        const bool lu = face_live(me.z) && cf.x != 0.0f, lv = face_live(me.w) && cf.y != 0.0f;
+        if (lu || lv) {
+            if (lu) me.x -= cf.x * (pc - p2_of(d, i - 1));
+            if (lv) me.y -= cf.y * (pc - p2_of(d, i - d.W));
+            store_vel_xy(d, i, me.x, me.y);
+        }
+        if (lu) m = fabsf(me.x);
+        if (lv) m = maxf(m, fabsf(me.y));
+    }
+    report_max(&d.S->umax_grid, m);
+}
+
+template <int NU>
+int visc_blocks_max_nu(int device) {
+    int sms = 0, per = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_visc_solve<NU>, NT, 0);
+    return sms * per;
+}
+
+}  // namespace
+
+int viscosity_blocks_max(int device, int sweeps) {
+    return sweeps >= 2 ? visc_blocks_max_nu<2>(device) : visc_blocks_max_nu<1>(device);
+}
+
+void launch_viscosity_setup(const DevScene& d, const LaunchCfg& cfg, cudaStream_t st) {
+    dim3 blk(16, 16);
+    dim3 grd((d.W + 15) / 16, (d.H + 15) / 16);
+    k_visc_split<<<grd, blk, 0, st>>>(d);
+    k_visc_diag<<<grd, blk, 0, st>>>(d);
+    for (int l = 1; l <= cfg.visc_levels; l++) {
+        dim3 g((d.lv.w[l] + 15) / 16, (d.lv.h[l] + 15) / 16);
+        k_vmg_build<<<g, blk, 0, st>>>(d, l);
+    }
+}
+
+cudaError_t launch_viscosity(const DevScene& d, const LaunchCfg& cfg, cudaStream_t st, int restrain) {
+    cudaMemsetAsync(&d.K->bar_count, 0, sizeof(uint32_t), st);
+    void* args[] = {(void*)&d, &restrain};
+    const void* fn = cfg.visc_sweeps >= 2 ? (const void*)k_visc_solve<2> : (const void*)k_visc_solve<1>;
+    return cudaLaunchCooperativeKernel(fn, dim3(cfg.visc_blocks), dim3(NT), args, 0, st);
+}
+
+void launch_second_projection_rhs(const DevScene& d, cudaStream_t st) {
+    dim3 blk(16, 16);
+    dim3 grd((d.W + 15) / 16, (d.H + 15) / 16);
+    k_rhs_visc<<<grd, blk, 0, st>>>(d);
+}
+
+void launch_second_projection(const DevScene& d, cudaStream_t st) {
+    dim3 blk(16, 16);
+    dim3 grd((d.W + 15) / 16, (d.H + 15) / 16);
+    k_project_visc<<<grd, blk, 0, st>>>(d);
+}
+
+}  // namespace sprout

@@ -118,3 +118,50 @@ def test_surface_tension_and_heat_bit_exact():
         n, k = first_diff(sim.field(name), ora.field(name))
         assert n == 0, f"{name} differs"
     assert np.array_equal(sim.field("ledger", np.uint64), ora.field("ledger", np.uint64))
+
+
+VISC_FIELDS = ["vw", "vs", "vd", "p2keep", "vma", "vmb", "vmd"]
+
+
+def compare_viscosity(sim, ora):
+    msgs = []
+    for name in VISC_FIELDS:
+        n, k = first_diff(sim.field(name), ora.field(name))
+        if n:
+            msgs.append(f"viscosity field {name} differs in {n} values (first {k})")
+    for name in ["tiles", "vtile"]:
+        if not np.array_equal(sim.field(name, np.uint32), ora.field(name, np.uint32)):
+            msgs.append(f"tile flags {name} differ")
+    a, b = sim.stats(), ora.stats()
+    if (a.viscosity_iters, a.viscosity_iters_max, a.viscosity_unconverged) != (b.v_iters, b.v_it_max, b.v_unconv):
+        msgs.append(f"viscosity iterations differ: {a.viscosity_iters}/{a.viscosity_iters_max} vs {b.v_iters}/{b.v_it_max}")
+    if a.viscosity_residual_max != b.v_res_max:
+        msgs.append(f"viscosity residual differs: {a.viscosity_residual_max} vs {b.v_res_max}")
+    if (a.pressure2_iters_max, a.pressure2_unconverged) != (b.p2_it_max, b.p2_unconv):
+        msgs.append("second pressure solve differs")
+    return msgs
+
+
+def test_implicit_viscosity_bit_exact():
+    """Honey, water and oil: the honey layer takes the implicit MG-PCG viscosity solve between
+    two pressure solves (visc*.comp, vmg*.comp, rhs_visc.comp, project_visc.comp)."""
+    t = tanks.stratified(128, 72)
+    sim, ora, problems = run_pair(t, 8, check_every=4)
+    assert not problems, "\n".join(problems)
+    st = sim.stats()
+    assert st.viscosity_mode == 2 and st.viscosity_iters_max > 0 and st.pressure2_iters_max > 0
+    problems = compare_viscosity(sim, ora)
+    assert not problems, "\n".join(problems)
+
+
+def test_implicit_viscosity_variants_bit_exact():
+    """One pressure solve after the viscosity, one sweep per level, two coarse levels, no
+    warm starts: the other recordings of record_viscosity_solve."""
+    t = tanks.stratified(160, 96, extra={"viscous_projection": 0, "viscosity_mg_sweeps": 1,
+                                         "viscosity_mg_levels": 2, "viscosity_warm": 0})
+    sim, ora, problems = run_pair(t, 6, check_every=3)
+    assert not problems, "\n".join(problems)
+    st = sim.stats()
+    assert st.viscosity_mode == 2 and st.viscosity_iters_max > 0 and st.pressure2_iters_max == 0
+    problems = compare_viscosity(sim, ora)
+    assert not problems, "\n".join(problems)
