@@ -3,7 +3,9 @@
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl engine|reference] [--workload NAME]
 
 A step is one substep of the whole tank (sort, P2G, grid passes, pressure solve, projection,
-G2P/advection) on a seeded synthetic tank (sprout_gb300.workloads). `value` is
+the implicit viscosity and the second projection where the tank needs them, G2P/advection) on
+a seeded synthetic tank (sprout_gb300.workloads); by default the full-physics pour at
+1024 x 576 (8 liquids, heater, surface tension, implicit viscosity). `value` is
 live particles x substeps / device seconds with the tank resident on the device
 (CUDA events on the engine's stream, tank working set far larger than L2, so no flush is
 needed between steps); `e2e` is the same metric through the public API with a host
@@ -37,7 +39,22 @@ UNIT = "particle-steps/s"
 
 def workload(name: str, rank: int):
     from sprout_gb300 import workloads as WL
-    if name == "dam_break_1024":
+    if name == "full_physics_1024":
+        # The full-physics pour: 1024 x 576, 1 mm cells, 8 seeded liquids in random vertical
+        # columns over the whole tank (rho 800-13500, mu 1e-3-50 Pa s log-uniform, tension
+        # 0.02-0.5 N/m), 293 K over a 600 K heater strip on the bottom 8 rows, heat diffusion,
+        # surface tension and implicit viscosity on, pressure and viscosity to 1e-5.
+        t = WL.full_physics(1024, 576, cell=0.001, n_liquids=8, seed=0, heater_rows=8, tol=1e-5)
+        desc = {"workload": "full_physics_pour_1024x576", "grid": [1024, 576], "cell_size_m": 0.001,
+                "fill": "8 liquids, seeded vertical columns, whole tank", "ppc": 4, "substep_s": 1 / 240,
+                "pressure_tol": 1e-5, "viscosity_tol": 1e-5, "solver": "plain fp32 MGPCG + implicit viscosity MG-PCG",
+                "heater": "600 K, bottom 8 rows", "surface_tension": "0.02-0.5 N/m", "seed": 0}
+    elif name == "stratified_512":
+        t = WL.stratified(512, 288, cell=0.002, tol=1e-5)
+        desc = {"workload": "stratified_honey_water_oil_512x288", "grid": [512, 288], "cell_size_m": 0.002,
+                "fill": "honey / water / olive oil layers, 20% of the height each", "ppc": 4, "substep_s": 1 / 240,
+                "pressure_tol": 1e-5, "viscosity_tol": 1e-5, "solver": "plain fp32 MGPCG + implicit viscosity MG-PCG"}
+    elif name == "dam_break_1024":
         # 1024 x 576 MAC grid, 1 mm cells, water over the left 40 % and bottom 60 %, 4 particles
         # per cell, closed box, fixed 1/240 s substeps, pressure to relative residual 1e-5.
         t = WL.dam_break(1024, 576, cell=0.001, width=0.4, height=0.6, tol=1e-5)
@@ -165,7 +182,10 @@ def cpu_oracle_rate(tank, seconds_budget: float = 15.0):
             "sample": f"{n} substeps of the same tank after 2 warm-up substeps, {el:.1f} s"}, live, el / n
 
 
-def run_reference(args, rank, world, pg):
+def run_reference(args, rank, world, pg, budget_s: float = 90.0):
+    """The reference's algorithm on the host cores (the oracle, all threads): up to `steps`
+    substeps of the same tank after `warmup` (at most 3) warm-up substeps, stopping early once
+    `budget_s` seconds of timed work have run, so the whole run ends within a few minutes."""
     tank, desc = workload(args.workload, rank)
     if rank != 0:
         return
@@ -173,30 +193,51 @@ def run_reference(args, rank, world, pg):
     threads = O.threads_available()
     sim, parts, _ = O.build_tank(tank, threads=threads)
     dt = 1.0 / 240.0
-    for _ in range(args.warmup):
+    warm = min(args.warmup, 3)
+    for _ in range(warm):
         sim.step(1, dt)
+    done = 0
     t0 = time.perf_counter()
-    for _ in range(args.steps):
+    while done < args.steps:
         sim.step(1, dt)
+        done += 1
+        if time.perf_counter() - t0 > budget_s:
+            break
     el = time.perf_counter() - t0
     live = int(np.count_nonzero(sim.particles()["kind"]))
-    value = live * args.steps / el
+    value = live * done / el
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+            "warmup": args.warmup, "ms_per_step": el / done * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded tank, no dataset)", "config": desc,
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": f"{args.steps} substeps after {args.warmup} warm-up substeps"},
+                             "sample": f"{done} of {args.steps} substeps timed after {warm} warm-up substeps, {el:.1f} s"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
-def kernels_per_substep(stats) -> int:
+def kernels_per_substep(stats, settings: dict) -> int:
     n = 2 + 5 + 1                 # step + advance; scan x3 + place + cell gather; p2g
     n += 4 + 1                    # grid_prep, coef/smooth, curvature, jumps; rhs
     n += 1 if stats.thermal else 0
     n += 2 if stats.viscosity_mode == 1 else 0
     n += 1 + 1                    # pressure (persistent), project
+    if stats.viscosity_mode == 2:
+        levels = min(max(int(settings.get("viscosity_mg_levels", 1)), 1), stats.tail)
+        n += 3 + levels + 1       # visc_setup, split, diag, coarse builds, the solve (persistent)
+        if int(settings.get("viscous_projection", 1)) != 0:
+            n += 3                # rhs_visc, second pressure solve, project_visc
     return n
+
+
+def active_viscosity_cells(sim, w: int, h: int) -> int:
+    """Cells of the tiles that take the implicit viscosity solve."""
+    tiles = sim.field("tiles", np.uint32)
+    tw = (w + 15) // 16
+    n = 0
+    for t in np.nonzero(tiles)[0]:
+        x0, y0 = (t % tw) * 16, (t // tw) * 16
+        n += (min(x0 + 16, w) - x0) * (min(y0 + 16, h) - y0)
+    return int(n)
 
 
 def run_engine(args, rank, world, local, pg):
@@ -233,8 +274,10 @@ def run_engine(args, rank, world, local, pg):
     unknowns = int(np.count_nonzero(sim.field("mgd")[: tank.w * tank.h] > 0))
     iters = max(st2.pressure_iters[0], st2.pressure_iters[1])
     top = max(stages, key=stages.get)
+    active = active_viscosity_cells(sim, tank.w, tank.h) if st2.viscosity_mode == 2 else 0
     algo = BM.stage_bytes(top, st2.n_live, tank.w * tank.h, unknowns, iters, st2.acc_stride, bool(st2.thermal),
-                          st2.viscosity_mode)
+                          st2.viscosity_mode, active_cells=active, visc_iterations=st2.viscosity_iters,
+                          iterations2=st2.pressure2_iters)
     achieved = algo / (stages[top] * 1e-3) / 1e9
     roof = {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": hbm, "unit": "GB/s",
             "frac": achieved / hbm, "peak_source": src, "traffic": None,
@@ -269,10 +312,13 @@ def run_engine(args, rank, world, local, pg):
             "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic (seeded tank, no dataset)",
             "config": dict(desc, particles=int(live), parallelism=f"replicas x{world}",
-                           l2="working set > L2 (126 MB of particles alone): no flush",
+                           l2="working set > L2 (particles alone 48 B x live > 129 MB): no flush",
                            pressure_iters_last=list(st2.pressure_iters), pressure_residual=st2.pressure_residual,
-                           pressure_unconverged=st2.pressure_unconverged),
-            "clocks": clk.summary(), "e2e": e2e, "gpu_launches": kernels_per_substep(st2) * args.steps,
+                           pressure_unconverged=st2.pressure_unconverged,
+                           viscosity_iters_last=st2.viscosity_iters, viscosity_residual=st2.viscosity_residual,
+                           viscosity_unconverged=st2.viscosity_unconverged, pressure2_iters_last=st2.pressure2_iters,
+                           viscosity_active_cells=active),
+            "clocks": clk.summary(), "e2e": e2e, "gpu_launches": kernels_per_substep(st2, tank.settings) * args.steps,
             "roofline": roof, "stages_ms": stages, "latency_ms": {"p50": e2e["p50_ms"], "p99": e2e["p99_ms"]}}
     if not args.no_cpu_baseline:
         cb, _, _ = cpu_oracle_rate(tank)
@@ -286,7 +332,8 @@ def main():
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
-    ap.add_argument("--workload", default="dam_break_1024")
+    ap.add_argument("--workload", default="full_physics_1024",
+                    choices=["full_physics_1024", "stratified_512", "dam_break_1024", "dam_break_384"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)

@@ -55,7 +55,7 @@ typedef struct SproutSolverStats {
     uint64_t substeps;                 /* substeps run since the last reset */
     double sim_time;                   /* simulated seconds since the last reset */
     float dt, dt_prev;                 /* the last substep and the one before, s */
-    uint32_t pressure_iters[2];        /* iterations of the last pressure solve (P, psi) */
+    uint32_t pressure_iters[2];        /* iterations of the last (first) pressure solve (P, psi) */
     uint32_t pressure_iters_max;       /* most iterations any pressure solve needed */
     uint32_t pressure_unconverged;     /* pressure solves that hit pressure_max_iters */
     uint32_t pressure2_iters_max, pressure2_unconverged;
@@ -71,6 +71,7 @@ typedef struct SproutSolverStats {
     uint64_t h2d_bytes, d2h_bytes;     /* host <-> device bytes this sim has moved (cumulative) */
     uint32_t viscosity_iters;          /* iterations of the last implicit viscosity solve */
     float viscosity_residual;          /* |r| / |r0| of the last implicit viscosity solve */
+    uint32_t pressure2_iters;          /* iterations of the last second pressure solve */
 } SproutSolverStats;
 
 typedef struct SproutParams SproutParams;   /* SimParams */

@@ -19,7 +19,7 @@
  * mix(x, y, a) = x * (1 - a) + y * a, length(v) = sqrt(dot(v, v)), normalize(v) =
  * v / length(v), smoothstep per its definition. Work-group reductions keep the shaders'
  * order (256-invocation trees per 16 x 16 tile, then the strided totals of
- * reduce_tail.glsl:268-281).
+ * reduce_tail.glsl:28-41).
  */
 #include "sprout_oracle.h"
 
@@ -609,6 +609,7 @@ typedef struct SolveBuf {   /* common.glsl:138-149 */
     float v_rz, v_alpha, v_beta, v_r0, v_rr, v_pq;
     uint32_t v_done, v_iters, v_it_max, v_unconv;
     float v_res_max;
+    uint32_t p1_iters[2], p2_last;   /* bookkeeping: the last first and second solves' iterations */
 } SolveBuf;
 
 typedef struct Levels {   /* mod.rs:714-753 */
@@ -2616,7 +2617,7 @@ static void vcycle(OSim* s) {
     for (int l = s->lv.tail - 1; l >= 0; l--) k_mg_up(s, l, l == 0);
 }
 
-/* reduce_tail.glsl:268-281: sum of n partials starting at base, in the shader's order */
+/* reduce_tail.glsl:28-41: sum of n partials starting at base, in the shader's order */
 static V4 total(const OSim* s, int base, int n) {
     V4 buf[256];
     for (int t = 0; t < 256; t++) {
@@ -2763,7 +2764,7 @@ static void k_cg_update(OSim* s, const V2* cgp2) {
         }
 }
 
-/* reduce_tail.glsl:299-355, the pressure modes */
+/* reduce_tail.glsl:61-116, the pressure modes */
 static void reduce_start(OSim* s, int mode) {
     int n = s->nwg;
     V4 a = total(s, 0, n), b = total(s, n, n);
@@ -2858,6 +2859,12 @@ static void pressure_solve(OSim* s, int second) {
         pb = t;
     }
     reduce_end(s, second ? 9 : 3);
+    if (!second) {
+        s->K.p1_iters[0] = s->K.p_iters[0];
+        s->K.p1_iters[1] = s->K.p_iters[1];
+    } else {
+        s->K.p2_last = s->K.p_iters[0];
+    }
 }
 
 /* ------------------------------------------------------------------------------------ */
@@ -2919,6 +2926,7 @@ static inline int tile_active_c(const OSim* s, int x, int y) { return s->tiles[t
 /* visc_split.comp: explicit step in the inactive tiles */
 static void k_visc_split(OSim* s) {
     int W = s->W, H = s->H;
+#pragma omp parallel for schedule(static) num_threads(g_threads)
     for (int cy = 1; cy < H - 1; cy++)
         for (int cx = 1; cx < W - 1; cx++) {
             if (tile_active_c(s, cx, cy)) continue;
@@ -2977,6 +2985,7 @@ static void k_visc_diag(OSim* s, int warm, int mg) {
         if (mg) s->vtile[t] = s->tiles[t];
     }
     V4* outw = (V4*)malloc((size_t)W * H * sizeof(V4));
+#pragma omp parallel for schedule(static) num_threads(g_threads)
     for (int cy = 0; cy < H; cy++)
         for (int cx = 0; cx < W; cx++) {
             int i = cidx(s, cx, cy);
@@ -3010,6 +3019,7 @@ static void k_visc_diag(OSim* s, int warm, int mg) {
         }
     /* the level-0 matrix (reads vw.xy through wts, which is zero in inactive tiles already) */
     if (mg) {
+#pragma omp parallel for schedule(static) num_threads(g_threads)
         for (int cy = 0; cy < H; cy++)
             for (int cx = 0; cx < W; cx++) {
                 int i = cidx(s, cx, cy);
@@ -3032,6 +3042,7 @@ static void k_visc_diag(OSim* s, int warm, int mg) {
                 s->vmd[i] = dm;
             }
     }
+#pragma omp parallel for schedule(static) num_threads(g_threads)
     for (int i = 0; i < W * H; i++) {
         int cx = i % W, cy = i / W;
         s->vw[i] = outw[i];
@@ -3052,6 +3063,7 @@ static void k_vmg_build(OSim* s, int l) {
     int tfx = (F.w + 15) >> 4, tfy = (F.h + 15) >> 4;
     int tcx = (C.w + 15) >> 4, tcy = (C.h + 15) >> 4;
     static const int UVX[4] = {0, -1, 0, -1}, UVY[4] = {0, 0, 1, 1};
+#pragma omp parallel for schedule(static) num_threads(g_threads)
     for (int ty = 0; ty < tcy; ty++)
         for (int tx = 0; tx < tcx; tx++) {
             uint32_t on = 0u;
@@ -3105,6 +3117,7 @@ static void k_vmg_build(OSim* s, int l) {
 
 /* visc_strain.comp: strain of the current velocity in the active tiles */
 static void k_visc_strain(OSim* s) {
+#pragma omp parallel for schedule(static) num_threads(g_threads)
     for (int cy = 0; cy < s->H; cy++)
         for (int cx = 0; cx < s->W; cx++) {
             if (!tile_active_c(s, cx, cy)) continue;
@@ -3117,6 +3130,7 @@ static void k_visc_strain(OSim* s) {
 typedef V4 (*CellDot)(OSim* s, int cx, int cy, void* ctx);
 static void tile_partials(OSim* s, V4* part, CellDot f, void* ctx) {
     int tw = (s->W + 15) >> 4, th = (s->H + 15) >> 4;
+#pragma omp parallel for schedule(static) num_threads(g_threads)
     for (int ty = 0; ty < th; ty++)
         for (int tx = 0; tx < tw; tx++) {
             int slot = ty * tw + tx;
@@ -3232,6 +3246,7 @@ static V2 voffd(const OSim* s, Lv L, const V2* X, int x, int y) {
 static void vhalf_sweep(const OSim* s, Lv L, V2* X, const V2* R, int red) {
     int n = L.w * L.h;
     V2* nv = (V2*)malloc((size_t)n * sizeof(V2));
+#pragma omp parallel for schedule(static) num_threads(g_threads)
     for (int t = 0; t < n; t++) {
         int x = t % L.w, y = t / L.w;
         if ((((x + y) & 1) == 0) != red) continue;
@@ -3240,6 +3255,7 @@ static void vhalf_sweep(const OSim* s, Lv L, V2* X, const V2* R, int red) {
         V2 sv = v2(R[t].x - o.x, R[t].y - o.y);
         nv[t] = v2(d.x > 0.0f ? sv.x / d.x : 0.0f, d.y > 0.0f ? sv.y / d.y : 0.0f);
     }
+#pragma omp parallel for schedule(static) num_threads(g_threads)
     for (int t = 0; t < n; t++) {
         int x = t % L.w, y = t / L.w;
         if ((((x + y) & 1) == 0) == red) X[t] = nv[t];
@@ -3253,6 +3269,7 @@ static void vmg_down(OSim* s, int l, const V2* R, int coarsest, int halo) {
     Lv L = lev(s, l);
     int n = L.w * L.h;
     V2* X = (V2*)calloc((size_t)n, sizeof(V2));
+#pragma omp parallel for schedule(static) num_threads(g_threads)
     for (int t = 0; t < n; t++) {
         int x = t % L.w, y = t / L.w;
         V2 d = s->vmd[L.off + t];
@@ -3264,6 +3281,7 @@ static void vmg_down(OSim* s, int l, const V2* R, int coarsest, int halo) {
     if (!coarsest) {
         Lv C = lev(s, l + 1);
         V2* res = (V2*)calloc((size_t)n, sizeof(V2));
+#pragma omp parallel for schedule(static) num_threads(g_threads)
         for (int t = 0; t < n; t++) {
             int x = t % L.w, y = t / L.w;
             V2 d = s->vmd[L.off + t];
@@ -3271,6 +3289,7 @@ static void vmg_down(OSim* s, int l, const V2* R, int coarsest, int halo) {
             V2 rr = v2(R[t].x - d.x * X[t].x - o.x, R[t].y - d.y * X[t].y - o.y);
             res[t] = v2(rr.x * (d.x > 0.0f ? 1.0f : 0.0f), rr.y * (d.y > 0.0f ? 1.0f : 0.0f));
         }
+#pragma omp parallel for schedule(static) num_threads(g_threads)
         for (int cy = 0; cy < C.h; cy++)
             for (int cx = 0; cx < C.w; cx++) {
                 V2 a = vx_at(res, L, 2 * cx, 2 * cy), b = vx_at(res, L, 2 * cx + 1, 2 * cy);
@@ -3287,6 +3306,7 @@ static void vmg_down(OSim* s, int l, const V2* R, int coarsest, int halo) {
 static void vmg_up_into(OSim* s, int l, const V2* R, int coarse_corr, int halo, V2* X) {
     Lv L = lev(s, l);
     int n = L.w * L.h;
+#pragma omp parallel for schedule(static) num_threads(g_threads)
     for (int t = 0; t < n; t++) {
         int x = t % L.w, y = t / L.w;
         V2 xv = s->vmx[L.off + t];
@@ -3334,6 +3354,7 @@ static void visc_mgz(OSim* s, const V2* R, const V2* Q, int halo) {
     V2* Z = (V2*)malloc((size_t)n * sizeof(V2));
     V2* AZ = (V2*)malloc((size_t)n * sizeof(V2));
     vmg_up_into(s, 0, R, 1, halo, Z);
+#pragma omp parallel for schedule(static) num_threads(g_threads)
     for (int t = 0; t < n; t++) {
         int x = t % s->W, y = t / s->W;
         V2 d = s->vmd[t];
@@ -3373,6 +3394,7 @@ static V4 cell_mgu(OSim* s, int cx, int cy, void* ctx) {
 /* new_r of visc_mgu.comp at every cell of the level: the residual the way down reads */
 static void mgu_new_r(OSim* s, const V2* Rold, const V2* Qold, V2* out) {
     float a = s->K.v_alpha, b = s->K.v_beta;
+#pragma omp parallel for schedule(static) num_threads(g_threads)
     for (int i = 0; i < s->W * s->H; i++) {
         V2 sq = s->vaz[i];
         V2 q = b == 0.0f ? sq : v2(sq.x + b * Qold[i].x, sq.y + b * Qold[i].y);
@@ -3468,6 +3490,7 @@ static void k_rhs_visc(OSim* s, int warm) {
     float ratio = s->S.dt / s->S.dt_prev;
     V4* out = (V4*)malloc((size_t)W * H * sizeof(V4));
     memcpy(out, s->prhs, (size_t)W * H * sizeof(V4));
+#pragma omp parallel for schedule(static) num_threads(g_threads)
     for (int cy = 0; cy < H; cy++)
         for (int cx = 0; cx < W; cx++) {
             int i = cidx(s, cx, cy);
@@ -3501,6 +3524,7 @@ static void k_project_visc(OSim* s) {
     float m_all = 0.0f;
     float* keep = (float*)malloc((size_t)W * s->H * sizeof(float));
     memcpy(keep, s->p2keep, (size_t)W * s->H * sizeof(float));
+#pragma omp parallel for schedule(static) num_threads(g_threads) reduction(max : m_all)
     for (int cy = 1; cy < s->H; cy++)
         for (int cx = 1; cx < W; cx++) {
             int i = cidx(s, cx, cy);
@@ -3876,8 +3900,9 @@ void osim_stats(const OSim* s, OStats* o) {
     o->sim_time = s->S.advanced;
     o->dt = s->S.dt;
     o->dt_prev = s->S.dt_prev;
-    o->p_iters[0] = s->K.p_iters[0];
-    o->p_iters[1] = s->K.p_iters[1];
+    o->p_iters[0] = s->K.p1_iters[0];
+    o->p_iters[1] = s->K.p1_iters[1];
+    o->p2_iters = s->K.p2_last;
     o->p_done[0] = s->K.p_done[0];
     o->p_done[1] = s->K.p_done[1];
     o->p_it_max = s->K.p_it_max;

@@ -78,7 +78,7 @@ class SolverStats(C.Structure):
         ("n_slots", C.c_uint32), ("n_live", C.c_uint32), ("caps", C.c_uint32), ("acc_stride", C.c_uint32),
         ("thermal", C.c_uint32), ("viscosity_mode", C.c_uint32), ("levels", C.c_uint32), ("tail", C.c_uint32),
         ("device_error", C.c_uint32), ("h2d_bytes", C.c_uint64), ("d2h_bytes", C.c_uint64),
-        ("viscosity_iters", C.c_uint32), ("viscosity_residual", C.c_float),
+        ("viscosity_iters", C.c_uint32), ("viscosity_residual", C.c_float), ("pressure2_iters", C.c_uint32),
     ]
 
 

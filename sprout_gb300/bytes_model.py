@@ -28,6 +28,8 @@ def cell_bytes(stage: str, stride: int, thermal: bool, visc_mode: int) -> int:
         apply = 16 + 16 + 16 + 16 + 8
         heat = (16 * 5 + 8 + 4) if thermal else 0
         visc = (16 + 16 + 16 + 16 + 16 + 16 + 8) if visc_mode == 1 else 0
+        if visc_mode == 2:   # visc_setup, split, diag with the level-0 matrix, coarse builds
+            visc = (16 + 16 + 16 + 16 + 16) + (16 + 16 + 16 + 8) + (16 + 16 + 8 + 8 + 16 + 16 + 8 + 16) + 20
         rhs = 16 + 16 + 16 + 16 + 8 + 16 + 4 + 8 + 16 + 4 + 16
         return prep + coef_smooth + curv + apply + heat + visc + rhs
     if stage == "project":
@@ -50,8 +52,35 @@ def pressure_bytes(unknowns: int, iterations: int) -> float:
     return unknowns * (PRESSURE_SETUP + (iterations + 1) * PRESSURE_ITER)
 
 
+# The implicit viscosity solve, per cell of an active tile (both faces, float2 vectors of 8
+# bytes, the level-0 matrix 16 + 16 + 8 = 40): set-up (strain: vw 16, vel 16, vs 16; start:
+# vs 16, coef 16, vw 16, r 8, z 8; warm start: vd 8, vw 16, coef 16, vel 16 + 8, r 8 + 8; the
+# first way down and up as one iteration's) and per iteration: the update fused with the way
+# down (z 8, p 8 + 8, A z 8, q 8 + 8, r 8 + 8, vel 16 + 8, vd 8 + 8, matrix 40, vmx 8, coarse
+# rhs 2 = 162), the way up with A z (r 8, matrix 40, vmx 8, coarse z 2, q 8, z 8, A z 8 = 82)
+# and the coarse levels a quarter of the cells each way (down 58 + up 66) / 4.
+VISC_SETUP = 48 + 64 + 104
+VISC_ITER = 162 + 82 + (58 + 66) / 4.0
+
+
+def viscosity_bytes(active_cells: int, iterations: int) -> float:
+    return active_cells * (VISC_SETUP + (iterations + 1) * VISC_ITER)
+
+
+# The second projection: rhs_visc per cell (mgd 4 + 4 x 4, mga 16, prhs 16 + 16 + neighbours'
+# P1 16, solid 16 x 3, vel 16 x 3 = 180 read, prhs 16 + pres 8 + p2keep 4 written), the
+# second pressure solve on the same hierarchy (no build, no scaling), project_visc per cell
+# (mgd 4 x 3, pres 8 x 3, prhs 16 x 3, coef 16, vel 16 + 8, p2keep 4 = 128).
+PROJECT2_CELL = 180 + 28 + 128
+
+
 def stage_bytes(stage: str, particles: int, cells: int, unknowns: int, iterations: int, stride: int,
-                thermal: bool, visc_mode: int) -> float:
+                thermal: bool, visc_mode: int, active_cells: int = 0, visc_iterations: int = 0,
+                iterations2: int = 0) -> float:
     if stage == "pressure":
         return pressure_bytes(unknowns, iterations)
+    if stage == "viscosity":
+        return viscosity_bytes(active_cells, visc_iterations)
+    if stage == "project2":
+        return cells * PROJECT2_CELL + unknowns * (44 + (iterations2 + 1) * PRESSURE_ITER)
     return particles * PARTICLE.get(stage, 0) + cells * cell_bytes(stage, stride, thermal, visc_mode)

@@ -95,6 +95,8 @@ struct SolveState {
     uint32_t bar_count, bar_gen;   // the persistent kernels' grid barrier
     uint32_t v_iters, v_done;      // the last viscosity solve
     float v_rr, v_r0;
+    uint32_t p2_iters;             // iterations of the last second pressure solve
+    uint32_t pad;
 };
 
 // The multigrid hierarchy (Levels, src/sim/mod.rs:714-753).

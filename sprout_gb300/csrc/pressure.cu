@@ -2,7 +2,7 @@
 //
 // Multigrid-preconditioned conjugate gradients on the two potentials (pressure * dt and
 // the density-correction potential) side by side, each with its own step lengths and
-// convergence flag (reduce_tail.glsl:299-355), preconditioned by an aggregation V-cycle:
+// convergence flag (reduce_tail.glsl:61-116), preconditioned by an aggregation V-cycle:
 // Galerkin 2 x 2 coarse matrices (mg_build.comp:147-197, mg_tail.comp:44-70), red-black
 // Gauss-Seidel from zero on the way down with restriction of the residual (mg_down.comp),
 // coarse correction with omega = 1.8 and the mirrored sweep on the way up (mg_up.comp),
@@ -678,8 +678,9 @@ __global__ void __launch_bounds__(NT) k_mgpcg(DevScene d, int second, int scale_
             G->p_bb[c] = K.bb[c];
             G->p_rr[c] = K.rr[c];
             G->p_done[c] = K.done[c];
-            G->p_iters[c] = K.iters[c];
+            if (!second) G->p_iters[c] = K.iters[c];
         }
+        if (second) G->p2_iters = K.iters[0];
         G->solves += 1u;
         if (!second) {
             uint32_t m = K.iters[0] > K.iters[1] ? K.iters[0] : K.iters[1];

@@ -858,6 +858,7 @@ int sprout_sim_stats(SproutSim* sim, SproutSolverStats* o) {
     o->tail = (uint32_t)sim->d.lv.tail;
     o->device_error = K.error;
     o->viscosity_iters = K.v_iters;
+    o->pressure2_iters = K.p2_iters;
     o->viscosity_residual = K.v_r0 > 0.0f ? std::sqrt(K.v_rr / K.v_r0) : 0.0f;
     o->h2d_bytes = sim->h2d_bytes;
     o->d2h_bytes = sim->d2h_bytes;

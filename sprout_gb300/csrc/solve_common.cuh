@@ -79,7 +79,7 @@ DEV void block_tree(float4* buf) {
     }
 }
 
-// total() of reduce_tail.glsl:268-281: thread t sums partials t, t + 256, ... in order,
+// total() of reduce_tail.glsl:28-41: thread t sums partials t, t + 256, ... in order,
 // then the tree. Every block calls it and gets the same value.
 DEV float4 total(const float4* part, int n, float4* buf) {
     const int t = threadIdx.x;

@@ -111,3 +111,22 @@ def stratified(w: int = 512, h: int = 288, cell: float = 0.002, tol: float = 1e-
     s.update(extra or {})
     fills = [([0.0, k * 0.2 * h, float(w), (k + 1) * 0.2 * h], 59 + k, None) for k in range(3)]
     return Tank(w, h, s, [], fills)
+
+
+def full_physics(w: int = 1024, h: int = 576, cell: float = 0.001, n_liquids: int = 8, seed: int = 0,
+                 heater_rows: int = 8, tol: float = 1e-5, extra: dict | None = None) -> Tank:
+    """The full-physics pour (the 1024 x 576 configuration): `n_liquids` custom liquids in
+    seeded random vertical columns over the whole tank, rho uniform in 800-13500 kg/m^3,
+    dynamic viscosity log-uniform in 1e-3-50 Pa s, surface tension uniform in 0.02-0.5 N/m;
+    293 K everywhere over a 600 K heater strip along the bottom `heater_rows` rows; heat
+    diffusion, surface tension and implicit viscosity all on."""
+    rng = np.random.default_rng(seed)
+    rows = []
+    for _ in range(n_liquids):
+        rho = float(rng.uniform(800.0, 13500.0))
+        mu = float(np.exp(rng.uniform(np.log(1e-3), np.log(50.0))))
+        rows.append({"density": rho, "viscosity": min(mu / rho, 0.5), "tension": float(rng.uniform(0.02, 0.5))})
+    ex = {"viscosity_tol": tol}
+    ex.update(extra or {})
+    return layered_custom(w, h, rows, cell=cell, heater_rows=heater_rows, heater_temp=326.85,
+                          ambient=19.85, tol=tol, columns=True, seed=seed + 1, extra=ex)

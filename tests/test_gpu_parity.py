@@ -165,3 +165,25 @@ def test_implicit_viscosity_variants_bit_exact():
     assert st.viscosity_mode == 2 and st.viscosity_iters_max > 0 and st.pressure2_iters_max == 0
     problems = compare_viscosity(sim, ora)
     assert not problems, "\n".join(problems)
+
+
+def test_full_physics_pour_bit_exact():
+    """The full-physics pour at 160 x 96 (same physical tank, 6.4 mm cells): eight liquids,
+    heater strip, surface tension, heat and the implicit viscosity together."""
+    t = tanks.full_physics(160, 96, cell=0.0064)
+    sim, ora, problems = run_pair(t, 8, check_every=4)
+    assert not problems, "\n".join(problems)
+    st = sim.stats()
+    assert st.thermal == 1 and st.viscosity_mode == 2
+    problems = compare_viscosity(sim, ora)
+    for name in ["therm", "dheat"]:
+        n, k = first_diff(sim.field(name), ora.field(name))
+        if n:
+            problems.append(f"{name} differs in {n} values")
+    if not np.array_equal(sim.field("ledger", np.uint64), ora.field("ledger", np.uint64)):
+        problems.append("heat ledger differs")
+    a, b = sim.stats(), ora.stats()
+    if (list(a.pressure_iters), a.pressure2_iters) != (list(b.p_iters), b.p2_iters):
+        problems.append(f"pressure iterations differ: {list(a.pressure_iters)}/{a.pressure2_iters} vs "
+                        f"{list(b.p_iters)}/{b.p2_iters}")
+    assert not problems, "\n".join(problems)
