@@ -287,6 +287,26 @@ def run_engine(args, rank, world, local, pg):
         tr = json.loads(traffic_file.read_text()).get(args.workload, {}).get(top)
         if tr:
             roof["traffic"] = tr
+    # ---- the mixed-precision solve on the same tank (BF16 matrices, FP64 dot products) ------
+    mixed = None
+    if args.precision in ("both", "mixed"):
+        msim, _, _ = tank.engine()
+        msim.set_precision("mixed")
+        for _ in range(max(args.warmup, 3)):
+            msim.step(1, dt)
+        msim.sync()
+        mlive = msim.stats().n_live
+        barrier(pg)
+        mms = allreduce_max(pg, msim.profile(args.steps))
+        mst = msim.stats()
+        mstages = msim.profile_passes()
+        mixed = {"value": allreduce_sum(pg, float(mlive)) * args.steps / (mms / 1e3), "unit": UNIT,
+                 "ms_per_step": mms / args.steps, "stages_ms": mstages,
+                 "pressure_iters_last": list(mst.pressure_iters), "pressure2_iters_last": mst.pressure2_iters,
+                 "pressure_residual_max": mst.pressure_residual_max, "pressure_unconverged": mst.pressure_unconverged,
+                 "pressure_true_residual_max_fp64": mst.pressure_true_residual_max,
+                 "storage": "BF16 couplings + FP32 row-sum-keeping diagonal on every level; FP32 vectors",
+                 "dots": "FP64", "speedup_vs_plain": (ms / args.steps) / (mms / args.steps)}
     # ---- end to end through the public API: a host round trip every step -------------------
     h0 = sim.stats()
     lat = []
@@ -320,9 +340,20 @@ def run_engine(args, rank, world, local, pg):
                            viscosity_active_cells=active),
             "clocks": clk.summary(), "e2e": e2e, "gpu_launches": kernels_per_substep(st2, tank.settings) * args.steps,
             "roofline": roof, "stages_ms": stages, "latency_ms": {"p50": e2e["p50_ms"], "p99": e2e["p99_ms"]}}
+    if mixed is not None:
+        line["mixed"] = mixed
     if not args.no_cpu_baseline:
+        # the checkers, on the host: the oracle's rate, and the FP64 reference solution of each
+        # arm's last pressure system
         cb, _, _ = cpu_oracle_rate(tank)
         line["cpu_baseline"] = cb
+        from oracle.fp64_mgpcg import accuracy
+        acc = {}
+        for name, s_ in [("plain", sim)] + ([("mixed", msim)] if mixed is not None else []):
+            a = accuracy(s_.field("mga"), s_.field("mgd"), s_.field("prhs"), s_.field("pres"), tank.w, tank.h, columns=(0,))
+            acc[name] = {"pressure_error_vs_fp64": a[0]["error_vs_fp64"], "pressure_residual_fp64": a[0]["residual_fp64"]}
+        acc["system"] = "the last pressure solve of each arm's tank, solved again by an FP64 MGPCG to 1e-12"
+        line["accuracy"] = acc
     print(json.dumps(line), flush=True)
 
 
@@ -335,6 +366,9 @@ def main():
     ap.add_argument("--workload", default="full_physics_1024",
                     choices=["full_physics_1024", "stratified_512", "dam_break_1024", "dam_break_384"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--precision", default="both", choices=["plain", "mixed", "both"],
+                    help="plain: the reference's FP32 arithmetic (the headline value); mixed: also time "
+                         "the mixed-precision pressure solve on the same tank (reported under 'mixed')")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, world, local, pg = dist_setup(args.gpus)

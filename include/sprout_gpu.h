@@ -72,6 +72,9 @@ typedef struct SproutSolverStats {
     uint32_t viscosity_iters;          /* iterations of the last implicit viscosity solve */
     float viscosity_residual;          /* |r| / |r0| of the last implicit viscosity solve */
     uint32_t pressure2_iters;          /* iterations of the last second pressure solve */
+    float pressure_true_residual;      /* mixed precision: |b - A x| / |b| of the last solve's
+                                          pressure evaluated in FP64 (0 in plain mode) */
+    float pressure_true_residual_max;
 } SproutSolverStats;
 
 typedef struct SproutParams SproutParams;   /* SimParams */
@@ -165,6 +168,18 @@ int sprout_sim_profile(SproutSim* sim, uint32_t substeps, float* ms);
  * unless the tank takes the implicit viscosity between two pressure solves. n >= 6; with
  * n < 8 the stages past n - 1 are added to ms[5]. Blocking. */
 int sprout_sim_profile_passes(SproutSim* sim, float* ms, uint32_t n);
+
+/* ---- precision of the pressure solve -------------------------------------------------
+ * No counterpart in the reference (it solves in FP32 only). mode 0: the reference's
+ * arithmetic, FP32 throughout (the default). mode 1: mixed precision: the multigrid
+ * hierarchy's matrices stored in BF16 (with an FP32 diagonal that keeps every row sum) and
+ * computed in FP32; every vector, the CG iterate, residual and operator in FP32; the dot
+ * products, step lengths and convergence test in FP64; at the end of each solve the true
+ * residual b - A x evaluated in FP64 (stats: pressure_true_residual). Both stop at the same
+ * relative residual (pressure_tol) of the residual the iteration carries, as the reference
+ * does. Takes effect from the next step; the first switch to mode 1 allocates the BF16
+ * matrices. */
+int sprout_sim_set_precision(SproutSim* sim, int mode);
 
 /* ---- a pressure solve that allocates nothing ------------------------------------------
  * No counterpart in the reference: an addition for callers that cannot allocate device

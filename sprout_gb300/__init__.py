@@ -39,7 +39,7 @@ EXPORTS = [
     "sprout_sim_reset", "sprout_sim_step", "sprout_sim_step_blocking", "sprout_sim_advance_blocking",
     "sprout_sim_sync", "sprout_sim_download_particles", "sprout_sim_download_pressure",
     "sprout_sim_download_field", "sprout_sim_stats", "sprout_sim_device_bytes", "sprout_sim_profile",
-    "sprout_sim_profile_passes", "sprout_pressure_solve_static",
+    "sprout_sim_profile_passes", "sprout_pressure_solve_static", "sprout_sim_set_precision",
 ]
 
 STAGES = ["advance", "sort", "p2g", "grid", "pressure", "project", "viscosity", "project2"]
@@ -79,6 +79,7 @@ class SolverStats(C.Structure):
         ("thermal", C.c_uint32), ("viscosity_mode", C.c_uint32), ("levels", C.c_uint32), ("tail", C.c_uint32),
         ("device_error", C.c_uint32), ("h2d_bytes", C.c_uint64), ("d2h_bytes", C.c_uint64),
         ("viscosity_iters", C.c_uint32), ("viscosity_residual", C.c_float), ("pressure2_iters", C.c_uint32),
+        ("pressure_true_residual", C.c_float), ("pressure_true_residual_max", C.c_float),
     ]
 
 
@@ -121,6 +122,7 @@ def lib() -> C.CDLL:
         "sprout_sim_device_bytes": ([V, P(C.c_size_t)], C.c_int),
         "sprout_sim_profile": ([V, C.c_uint32, P(C.c_float)], C.c_int),
         "sprout_sim_profile_passes": ([V, P(C.c_float), C.c_uint32], C.c_int),
+        "sprout_sim_set_precision": ([V, C.c_int], C.c_int),
         "sprout_pressure_solve_static": ([C.c_uint32, C.c_uint32, V, V, V, V, C.c_float, C.c_float, C.c_uint32, V,
                                           P(C.c_uint32), P(C.c_float)], C.c_int),
     }
@@ -286,6 +288,12 @@ class FluidSim:
         ms = C.c_float()
         _check(lib().sprout_sim_profile(self._h, substeps, C.byref(ms)))
         return ms.value
+
+    def set_precision(self, mode: str | int):
+        """The pressure solve's precision: "plain" (0, FP32 as the reference) or "mixed" (1:
+        BF16 matrices, FP64 dot products and convergence test, FP64 true residual at the end)."""
+        m = {"plain": 0, "mixed": 1}.get(mode, mode)
+        _check(lib().sprout_sim_set_precision(self._h, int(m)))
 
     def profile_passes(self) -> dict:
         """One substep stage by stage: device ms per stage (STAGES)."""

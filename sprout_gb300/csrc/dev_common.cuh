@@ -34,6 +34,11 @@ constexpr float MG_OMEGA = 1.8f;
 
 // Device buffers of one tank. Grid fields are W x H cells, row-major; the multigrid
 // fields hold every level back to back (Levels offsets).
+// Four FP64 partial sums (the mixed-precision solve's dot products).
+struct alignas(16) Dbl4 {
+    double x, y, z, w;
+};
+
 struct DevScene {
     int W, H, ncell, stride;
     uint32_t capacity;
@@ -69,6 +74,12 @@ struct DevScene {
     float4* partials;   // 2 x nwg
     int nwg;
     Levels lv;
+    // the mixed-precision solve's copy of the hierarchy's matrices (indexed like mga / mgd)
+    // and its FP64 per-tile partial sums (2 x nwg)
+    uint2* hga;         // four BF16 couplings per cell
+    float* hgd;         // FP32 diagonal, rebuilt so that each row keeps its exact excess over
+                        // the BF16 couplings (the part of D that is no coupling: air, vent)
+    Dbl4* partials64;
     // implicit viscosity (visc*.comp, vmg*.comp): Krylov vectors on the grid, the multigrid
     // hierarchy over the levels of lv, tile flags and the compact lists of active tiles
     float2 *vr, *vr2, *vp, *vq, *vq2, *vd, *vaz;

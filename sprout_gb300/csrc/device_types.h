@@ -96,7 +96,9 @@ struct SolveState {
     uint32_t v_iters, v_done;      // the last viscosity solve
     float v_rr, v_r0;
     uint32_t p2_iters;             // iterations of the last second pressure solve
-    uint32_t pad;
+    uint32_t err_arrived;          // on a barrier timeout: blocks that had arrived, of
+    uint32_t err_blocks;           // the grid's blocks (diagnostics)
+    float p_true_res, p_true_res_max;   // mixed precision: |b - A x| / |b| in FP64, last / max
 };
 
 // The multigrid hierarchy (Levels, src/sim/mod.rs:714-753).

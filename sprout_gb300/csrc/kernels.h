@@ -21,6 +21,8 @@ struct LaunchCfg {
     int visc_blocks = 0;      // blocks of the persistent viscosity kernel
     int mg_blocks = 0;        // blocks of the persistent pressure kernel
     int mg_threads = 256;
+    bool mixed = false;       // the mixed-precision pressure solve
+    int mg_blocks_mixed = 0;  // blocks of its persistent kernel
 };
 
 void launch_advance(const DevScene& d, const LaunchCfg& cfg, cudaStream_t st);
@@ -39,8 +41,9 @@ void launch_second_projection_rhs(const DevScene& d, cudaStream_t st);
 void launch_second_projection(const DevScene& d, cudaStream_t st);
 // Blocks of the persistent viscosity kernel that fit on the device at once.
 int viscosity_blocks_max(int device, int sweeps);
-// Blocks of the persistent pressure kernel that fit on the device at once.
-int pressure_blocks_max(int device, size_t smem);
+// Blocks of the persistent pressure kernel (plain or mixed precision) that fit on the
+// device at once.
+int pressure_blocks_max(int device, size_t smem, bool mixed);
 // Dynamic shared memory of the persistent pressure kernel: the tail levels of each block.
 size_t pressure_smem(const Levels& lv);
 

@@ -16,6 +16,21 @@
 // reduce.glsl / reduce_tail.glsl, so every block gets identical values), and the residual
 // update of conjugate gradients is fused into the first restriction of the next V-cycle by
 // double-buffering the level-0 residual.
+//
+// Two precisions, one kernel template:
+//   Plain  the reference's arithmetic: every value FP32, the dot products summed in FP32 in
+//          the reference's order (bit-exact with the oracle).
+//   Mixed  the V-cycle's matrices (every level's couplings) stored in BF16 and computed in
+//          FP32; the CG operator (level 0's matrix), every vector, iterate, residual and
+//          direction stay FP32; the dot products, step
+//          lengths and convergence test in FP64; and at the end of each solve the true
+//          residual b - A x of the pressure evaluated in FP64 arithmetic and reported (it is
+//          not fed back: for these near-singular systems the FP32-evaluated true residual is
+//          rounding noise at 1e-3 |b| and the best FP32 iterate's FP64 one sits near
+//          5e-5 |b|, so replacing the carried residual with either stalls the iteration
+//          above the reference's 1e-5 tolerance). The BF16 couplings come with an FP32
+//          diagonal that keeps each row's exact excess over them (see Mixed::setA).
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include "dev_common.cuh"
@@ -31,28 +46,106 @@ using namespace solve;
 __constant__ int NBX[4] = {-1, 1, 0, 0};
 __constant__ int NBY[4] = {0, 0, -1, 1};
 
-struct Solve {
-    float rz[2], alpha[2], beta[2], bb[2], rr[2];
-    uint32_t done[2], iters[2];
+
+// ---- the two precisions ---------------------------------------------------------------
+
+struct Plain {
+    static constexpr bool kMixed = false;
+    using acc = float;
+    using acc4 = float4;
+    DEV static float4 A(const DevScene& d, int i) { return d.mga[i]; }
+    DEV static float Dg(const DevScene& d, int i) { return d.mgd[i]; }
+    DEV static void setA(const DevScene& d, int i, float4 a, float dg) { d.mga[i] = a; d.mgd[i] = dg; }
+    DEV static float2 X(const DevScene& d, int i) { return d.mgx[i]; }
+    DEV static void setX(const DevScene& d, int i, float2 v) { d.mgx[i] = v; }
+    DEV static float2 Z(const DevScene& d, int i) { return d.mgz[i]; }
+    DEV static void setZ(const DevScene& d, int i, float2 v) { d.mgz[i] = v; }
+    DEV static float2 R(const DevScene& d, int i) { return d.mgr[i]; }   // a coarse level's rhs
+    DEV static void setR(const DevScene& d, int i, float2 v) { d.mgr[i] = v; }
+    DEV static acc4* part(const DevScene& d) { return d.partials; }
+    DEV static acc4 a4(float x, float y, float z, float w) { return make_float4(x, y, z, w); }
 };
 
-struct Ctx {
-    DevScene d;
-    Lv L0;
+// a pair of BF16 values in 32 bits (x in the low half), rounded to nearest even
+DEV uint32_t pack(float2 v) {
+    __nv_bfloat162 h = __floats2bfloat162_rn(v.x, v.y);
+    return *reinterpret_cast<const uint32_t*>(&h);
+}
+DEV float2 unpack(uint32_t u) { return __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&u)); }
+
+struct Mixed {
+    static constexpr bool kMixed = true;
+    using acc = double;
+    using acc4 = Dbl4;
+    // the hierarchy in BF16: a row's four couplings as two bfloat162 in a uint2
+    DEV static float4 A(const DevScene& d, int i) {
+        const uint2 u = d.hga[i];
+        const float2 a = unpack(u.x), b = unpack(u.y);
+        return make_float4(a.x, a.y, b.x, b.y);
+    }
+    DEV static float Dg(const DevScene& d, int i) { return d.hgd[i]; }
+    // A row whose couplings m (a mask of the unknown neighbours) link it to other unknowns:
+    // the couplings rounded to BF16, the diagonal rebuilt as its excess over the FP32
+    // couplings plus the rounded ones, so that every row sum (the air, solid and vent terms
+    // that keep a sealed region's matrix definite) is kept exactly and the stored matrix
+    // stays a weighted graph Laplacian plus the same non-negative diagonal.
+    DEV static void setA(const DevScene& d, int i, float4 a, float dg, int m = 15) {
+        const uint2 u = make_uint2(pack(make_float2(a.x, a.y)), pack(make_float2(a.z, a.w)));
+        d.hga[i] = u;
+        if (dg <= 0.0f) {
+            d.hgd[i] = 0.0f;
+            return;
+        }
+        const float2 lo = unpack(u.x), hi = unpack(u.y);
+        const float c32 = ((m & 1) ? a.x : 0.0f) + ((m & 2) ? a.y : 0.0f) + ((m & 4) ? a.z : 0.0f) + ((m & 8) ? a.w : 0.0f);
+        const float c16 = ((m & 1) ? lo.x : 0.0f) + ((m & 2) ? lo.y : 0.0f) + ((m & 4) ? hi.x : 0.0f) + ((m & 8) ? hi.y : 0.0f);
+        d.hgd[i] = (dg - c32) + c16;
+    }
+    // the vectors stay FP32 on every level: rounding them would make the V-cycle a
+    // nonlinear operator, which conjugate gradients does not tolerate (it stagnates near the
+    // rounding level); the matrices are fixed during a solve, so the V-cycle built on their
+    // BF16 copies stays a linear, symmetric positive definite preconditioner
+    DEV static float2 X(const DevScene& d, int i) { return d.mgx[i]; }
+    DEV static void setX(const DevScene& d, int i, float2 v) { d.mgx[i] = v; }
+    DEV static float2 Z(const DevScene& d, int i) { return d.mgz[i]; }
+    DEV static void setZ(const DevScene& d, int i, float2 v) { d.mgz[i] = v; }
+    DEV static float2 R(const DevScene& d, int i) { return d.mgr[i]; }
+    DEV static void setR(const DevScene& d, int i, float2 v) { d.mgr[i] = v; }
+    DEV static acc4* part(const DevScene& d) { return d.partials64; }
+    DEV static acc4 a4(double x, double y, double z, double w) { return Dbl4{x, y, z, w}; }
+};
+
+template <class T>
+struct Solve {
+    T rz[2], alpha[2], beta[2], bb[2], rr[2];
+    uint32_t done[2], iters[2];
 };
 
 // ---- setup phases ---------------------------------------------------------------------
 
-// cg_scale.comp: warm start from last substep's potential rescaled to this substep.
+// Unknowns of the V-cycle's level (M's copy of the diagonal) and of the CG operator.
+template <class M>
+DEV bool unknown(const DevScene& d, const Lv& L, int x, int y) { return l_inside(L, x, y) && M::Dg(d, l_at(L, x, y)) > 0.0f; }
+DEV bool unknown_op(const DevScene& d, const Lv& L, int x, int y) { return l_inside(L, x, y) && d.mgd[l_at(L, x, y)] > 0.0f; }
+
+
+// cg_scale.comp: warm start from last substep's potential rescaled to this substep. Mixed:
+// also level 0's matrix in BF16 for the V-cycle (every cell: rhs.comp rewrote them all).
+template <class M>
 DEV void phase_cg_scale(const DevScene& d, int mode) {
     Lv F = lev(d.lv, 0);
     const float ratio = d.S->dt / d.S->dt_prev;
     const int T = tiles_x(F) * tiles_y(F);
     for (int t = blockIdx.x; t < T; t += gridDim.x) {
-        if (d.ptile[F.toff + t] == 0u) continue;
         int cx = (t % tiles_x(F)) * 16 + (threadIdx.x & 15), cy = (t / tiles_x(F)) * 16 + (threadIdx.x >> 4);
         if (!l_inside(F, cx, cy)) continue;
         int i = l_at(F, cx, cy);
+        if (M::kMixed) {
+            int m = 0;
+            for (int q = 0; q < 4; q++) m |= unknown_op(d, F, cx + NBX[q], cy + NBY[q]) ? (1 << q) : 0;
+            Mixed::setA(d, i, d.mga[i], d.mgd[i], m);
+        }
+        if (d.ptile[F.toff + t] == 0u) continue;
         if (d.mgd[i] > 0.0f) {
             float p = d.pres[i].x;
             if (mode == 1) p -= d.p2keep[i];
@@ -64,9 +157,8 @@ DEV void phase_cg_scale(const DevScene& d, int mode) {
     }
 }
 
-DEV bool unknown(const DevScene& d, const Lv& L, int x, int y) { return l_inside(L, x, y) && d.mgd[l_at(L, x, y)] > 0.0f; }
-
 // mg_build.comp: coarse level l + 1 from level l over the tiles of the coarse level.
+template <class M>
 DEV void phase_mg_build(const DevScene& d, int l) {
     Lv F = lev(d.lv, l), C = lev(d.lv, l + 1);
     const int tfx = tiles_x(F), tfy = tiles_y(F), tcx = tiles_x(C);
@@ -93,21 +185,20 @@ DEV void phase_mg_build(const DevScene& d, int l) {
         if (Cx >= C.w || Cy >= C.h) continue;
         const int o = l_at(C, Cx, Cy);
         if ((state & 1u) == 0u) {
-            d.mgd[o] = 0.0f;
-            d.mga[o] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            M::setA(d, o, make_float4(0.0f, 0.0f, 0.0f, 0.0f), 0.0f);
             continue;
         }
         float D = 0.0f;
         float4 A = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         for (int k = 0; k < 4; k++) {
             int cx = 2 * Cx + (k & 1), cy = 2 * Cy + (k >> 1);
-            if (!unknown(d, F, cx, cy)) continue;
+            if (!unknown<M>(d, F, cx, cy)) continue;
             int i = l_at(F, cx, cy);
-            D += d.mgd[i];
-            float4 w = d.mga[i];
+            D += M::Dg(d, i);
+            float4 w = M::A(d, i);
             for (int q = 0; q < 4; q++) {
                 int nx = cx + NBX[q], ny = cy + NBY[q];
-                if (!unknown(d, F, nx, ny)) continue;
+                if (!unknown<M>(d, F, nx, ny)) continue;
                 float wd = wcomp(w, q);
                 if ((nx >> 1) == Cx && (ny >> 1) == Cy) D -= wd;
                 else if (q == 0) A.x += wd;
@@ -116,23 +207,26 @@ DEV void phase_mg_build(const DevScene& d, int l) {
                 else A.w += wd;
             }
         }
-        d.mgd[o] = D > 1e-7f ? D : 0.0f;
-        d.mga[o] = D > 1e-7f ? A : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        M::setA(d, o, D > 1e-7f ? A : make_float4(0.0f, 0.0f, 0.0f, 0.0f), D > 1e-7f ? D : 0.0f);
     }
 }
 
-// cg_init.comp: r = b - A x, partial sums of b.b into part[n + tile].
-DEV void phase_cg_init(const DevScene& d, float2* r0, float4* buf) {
+// cg_init.comp: r = b - A x (the FP32 operator), partial sums of b.b into part[n + tile].
+// With `rr`: the true residual of the refinement instead, partial sums of r.r into part[tile].
+template <class M>
+DEV void phase_residual(const DevScene& d, float2* r0, typename M::acc4* buf, bool rr) {
+    using acc = typename M::acc;
     Lv F = lev(d.lv, 0);
     const int T = tiles_x(F) * tiles_y(F);
     const int n = d.nwg;
+    typename M::acc4* part = M::part(d) + (rr ? 0 : n);
     for (int t = blockIdx.x; t < T; t += gridDim.x) {
         if (d.ptile[F.toff + t] == 0u) {
-            if (threadIdx.x == 0) d.partials[n + t] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            if (threadIdx.x == 0) part[t] = M::a4(0, 0, 0, 0);
             continue;
         }
         const int cx = (t % tiles_x(F)) * 16 + (threadIdx.x & 15), cy = (t / tiles_x(F)) * 16 + (threadIdx.x >> 4);
-        float4 a4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        typename M::acc4 a4 = M::a4(0, 0, 0, 0);
         if (l_inside(F, cx, cy)) {
             const int i = l_at(F, cx, cy);
             const float D = d.mgd[i];
@@ -142,7 +236,7 @@ DEV void phase_cg_init(const DevScene& d, float2* r0, float4* buf) {
                 float axx = D * x.x, axy = D * x.y;
                 for (int q = 0; q < 4; q++) {
                     int nx = cx + NBX[q], ny = cy + NBY[q];
-                    if (unknown(d, F, nx, ny)) {
+                    if (unknown_op(d, F, nx, ny)) {
                         float wd = wcomp(w, q);
                         float2 pn = d.pres[l_at(F, nx, ny)];
                         axx -= wd * pn.x;
@@ -150,28 +244,32 @@ DEV void phase_cg_init(const DevScene& d, float2* r0, float4* buf) {
                     }
                 }
                 float4 b = d.prhs[i];
-                r0[i] = make_float2(b.x - axx, b.y - axy);
-                a4 = make_float4(b.x * b.x, b.y * b.y, 0.0f, 0.0f);
+                const float2 r = make_float2(b.x - axx, b.y - axy);
+                r0[i] = r;
+                if (rr) a4 = M::a4(0, 0, (acc)r.x * (acc)r.x, (acc)r.y * (acc)r.y);
+                else a4 = M::a4((acc)b.x * (acc)b.x, (acc)b.y * (acc)b.y, 0, 0);
             } else {
                 r0[i] = make_float2(0.0f, 0.0f);
             }
         }
         buf[threadIdx.x] = a4;
         block_tree(buf);
-        if (threadIdx.x == 0) d.partials[n + t] = buf[0];
+        if (threadIdx.x == 0) part[t] = buf[0];
         __syncthreads();
     }
 }
 
 // ---- the V-cycle --------------------------------------------------------------------------
 
-// The residual of level-0 cell j as the next iterate sees it: fused with the update
-// r -= alpha q of cg_update.comp, or as stored.
+// The right-hand side a way down reads: level 0's residual (FP32), fused with the update
+// r -= alpha q of cg_update.comp when q is set; or a coarse level's, through M.
+template <class M>
 struct Rsrc {
-    const float2* r;      // level-0 residual before the update (or the level's rhs)
+    const float2* r;      // level-0 residual before the update (null: a coarse level)
     const float2* q;      // A p, for the fused update (null: no update)
     float ax, ay;
-    DEV float2 at(int i) const {
+    DEV float2 at(const DevScene& d, int i) const {
+        if (!r) return M::R(d, i);
         float2 v = r[i];
         if (q) {
             float2 qq = q[i];
@@ -183,32 +281,33 @@ struct Rsrc {
 };
 
 // mg_down black(): value of black cell n after the half-sweep from zero.
-DEV float2 down_black(const DevScene& d, const Lv& L, const Rsrc& R, int nx, int ny) {
+template <class M>
+DEV float2 down_black(const DevScene& d, const Lv& L, const Rsrc<M>& R, int nx, int ny) {
     int i = l_at(L, nx, ny);
-    float4 w = d.mga[i];
-    float2 sum = R.at(i);
+    float4 w = M::A(d, i);
+    float2 sum = R.at(d, i);
     for (int q = 0; q < 4; q++) {
         int mx = nx + NBX[q], my = ny + NBY[q];
-        if (!unknown(d, L, mx, my)) continue;
+        if (!unknown<M>(d, L, mx, my)) continue;
         int j = l_at(L, mx, my);
         float wd = wcomp(w, q);
-        float2 rj = R.at(j);
-        float dj = d.mgd[j];
+        float2 rj = R.at(d, j);
+        float dj = M::Dg(d, j);
         sum.x += wd * rj.x / dj;
         sum.y += wd * rj.y / dj;
     }
-    float di = d.mgd[i];
+    float di = M::Dg(d, i);
     return make_float2(sum.x / di, sum.y / di);
 }
 
-// mg_down.comp on level l. On level 0 with `upd` it also applies cg_update.comp:
+// mg_down.comp on level l. On level 0 with `r_out` it also applies cg_update.comp:
 // x += alpha p and the residual update into r_out.
-DEV void phase_down(const DevScene& d, int l, const Rsrc& R, float2* r_out, const float2* p, float2* sz) {
+template <class M>
+DEV void phase_down(const DevScene& d, int l, const Rsrc<M>& R, float2* r_out, const float2* p, float2* sz) {
     Lv F = lev(d.lv, l), C = lev(d.lv, l + 1);
     const int tx_n = tiles_x(F);
     const int T = tx_n * tiles_y(F);
     const int lx = threadIdx.x & 15, ly = threadIdx.x >> 4;
-    float2* mgr_c = d.mgr;   // coarse right-hand sides live at the coarse level's offset
     for (int t = blockIdx.x; t < T; t += gridDim.x) {
         if (d.ptile[F.toff + t] == 0u) continue;
         const int cx = (t % tx_n) * 16 + lx, cy = (t / tx_n) * 16 + ly;
@@ -216,25 +315,25 @@ DEV void phase_down(const DevScene& d, int l, const Rsrc& R, float2* r_out, cons
         float2 z = make_float2(0.0f, 0.0f);
         if (l_inside(F, cx, cy)) {
             const int i = l_at(F, cx, cy);
-            const float D = d.mgd[i];
+            const float D = M::Dg(d, i);
             if (D > 0.0f) {
                 if (red) {
-                    float2 r = R.at(i);
+                    float2 r = R.at(d, i);
                     z = make_float2(r.x / D, r.y / D);
                 } else {
-                    z = down_black(d, F, R, cx, cy);
-                }
-                if (r_out) {
-                    // cg_update.comp: x += alpha p, r -= alpha q (unknowns of active tiles)
-                    float2 pp = p[i];
-                    float2 x = d.pres[i];
-                    x.x += R.ax * pp.x;
-                    x.y += R.ay * pp.y;
-                    d.pres[i] = x;
-                    r_out[i] = R.at(i);
+                    z = down_black<M>(d, F, R, cx, cy);
                 }
             }
-            d.mgx[i] = z;
+            if (r_out && d.mgd[i] > 0.0f) {
+                // cg_update.comp: x += alpha p, r -= alpha q (unknowns of active tiles)
+                float2 pp = p[i];
+                float2 x = d.pres[i];
+                x.x += R.ax * pp.x;
+                x.y += R.ay * pp.y;
+                d.pres[i] = x;
+                r_out[i] = R.at(d, i);
+            }
+            M::setX(d, i, z);
         }
         sz[threadIdx.x] = z;
         __syncthreads();
@@ -244,30 +343,30 @@ DEV void phase_down(const DevScene& d, int l, const Rsrc& R, float2* r_out, cons
                 float sx = 0.0f, sy = 0.0f;
                 for (int k = 0; k < 2; k++) {
                     int qx = cx + k, qy = cy + k;
-                    if (!unknown(d, F, qx, qy)) continue;
-                    float4 w = d.mga[l_at(F, qx, qy)];
+                    if (!unknown<M>(d, F, qx, qy)) continue;
+                    float4 w = M::A(d, l_at(F, qx, qy));
                     int lqx = lx + k, lqy = ly + k;
                     for (int q = 0; q < 4; q++) {
                         int nx = qx + NBX[q], ny = qy + NBY[q];
-                        if (!unknown(d, F, nx, ny)) continue;
+                        if (!unknown<M>(d, F, nx, ny)) continue;
                         int lnx = lqx + NBX[q], lny = lqy + NBY[q];
                         bool here = lnx >= 0 && lny >= 0 && lnx < 16 && lny < 16;
-                        float2 zb = here ? sz[lny * 16 + lnx] : down_black(d, F, R, nx, ny);
+                        float2 zb = here ? sz[lny * 16 + lnx] : down_black<M>(d, F, R, nx, ny);
                         float wd = wcomp(w, q);
                         sx += wd * zb.x;
                         sy += wd * zb.y;
                     }
                 }
-                mgr_c[l_at(C, Cx, Cy)] = make_float2(sx, sy);
+                M::setR(d, l_at(C, Cx, Cy), make_float2(sx, sy));
             }
         }
         __syncthreads();
     }
 }
 
-// The tail levels' state in each block's shared memory (dynamic): per tail cell the matrix
-// row (couplings, diagonal), the iterate and the right-hand side, at its offset from the
-// first tail level (the slots of mg_tail.comp).
+// The tail levels' state in each block's shared memory (dynamic, FP32 in both precisions):
+// per tail cell the matrix row (couplings, diagonal), the iterate and the right-hand side,
+// at its offset from the first tail level (the slots of mg_tail.comp).
 struct Tail {
     float4* a;
     float* dg;
@@ -281,10 +380,11 @@ DEV bool t_unknown(const Tail& tl, const Lv& L, int x, int y) { return l_inside(
 // mg_tail.comp mode 1 in every block's shared memory, once per solve: the first tail
 // level's matrix from global memory, then the Galerkin matrices of the coarser tail levels
 // (the arithmetic of mg_build.comp). Block 0 also stores them for inspection.
+template <class M>
 DEV void tail_setup(const DevScene& d, const Tail& tl) {
     for (int s = threadIdx.x; s < tl.nf; s += NT) {
-        tl.a[s] = d.mga[tl.base + s];
-        tl.dg[s] = d.mgd[tl.base + s];
+        tl.a[s] = M::A(d, tl.base + s);
+        tl.dg[s] = M::Dg(d, tl.base + s);
     }
     __syncthreads();
     for (int l = d.lv.tail; l < d.lv.n - 1; l++) {
@@ -313,82 +413,94 @@ DEV void tail_setup(const DevScene& d, const Tail& tl) {
             }
             tl.dg[oc + t] = D > 1e-7f ? D : 0.0f;
             tl.a[oc + t] = D > 1e-7f ? A : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-            if (blockIdx.x == 0) {
-                d.mgd[C.off + t] = tl.dg[oc + t];
-                d.mga[C.off + t] = tl.a[oc + t];
-            }
+            if (blockIdx.x == 0) M::setA(d, C.off + t, tl.a[oc + t], tl.dg[oc + t]);
         }
         __syncthreads();
     }
 }
 
-// mg_up black(): new value of black cell n after the coarse correction. The coarse level's
-// finished values come from zc (row width zw): global memory, or this block's shared copy
-// of the first tail level.
-DEV float2 up_black(const DevScene& d, const Lv& L, const float2* zc, int zw, const float2* rhs, int nx, int ny) {
+// Where a way up reads the coarse level's finished values: this block's shared copy of the
+// first tail level (s), or the level in global memory through M (at offset off).
+struct Zc {
+    const float2* s;
+    int off, w;
+};
+
+// mg_up black(): new value of black cell n after the coarse correction.
+template <class M>
+DEV float2 coarse_z(const DevScene& d, const Zc& zc, int mx, int my) {
+    const int k = (my >> 1) * zc.w + (mx >> 1);
+    return zc.s ? zc.s[k] : M::Z(d, zc.off + k);
+}
+
+template <class M>
+DEV float2 up_black(const DevScene& d, const Lv& L, const Zc& zc, const Rsrc<M>& rhs, int nx, int ny) {
     int i = l_at(L, nx, ny);
-    float4 w = d.mga[i];
-    float2 sum = rhs[i];
+    float4 w = M::A(d, i);
+    float2 sum = rhs.at(d, i);
     for (int q = 0; q < 4; q++) {
         int mx = nx + NBX[q], my = ny + NBY[q];
-        if (!unknown(d, L, mx, my)) continue;
-        float2 xm = d.mgx[l_at(L, mx, my)];
-        float2 zcv = zc[(my >> 1) * zw + (mx >> 1)];
+        if (!unknown<M>(d, L, mx, my)) continue;
+        float2 xm = M::X(d, l_at(L, mx, my));
+        float2 zcv = coarse_z<M>(d, zc, mx, my);
         float wd = wcomp(w, q);
         sum.x += wd * (xm.x + MG_OMEGA * zcv.x);
         sum.y += wd * (xm.y + MG_OMEGA * zcv.y);
     }
-    float di = d.mgd[i];
+    float di = M::Dg(d, i);
     return make_float2(sum.x / di, sum.y / di);
 }
 
 // mg_up.comp on level l; on level 0 (flag) the partial sums r.z, r.r into part[tile].
-DEV void phase_up(const DevScene& d, int l, bool flag, const float2* rhs, const float2* zc, float2* sz, float4* buf) {
-    Lv F = lev(d.lv, l), C = lev(d.lv, l + 1);
+template <class M>
+DEV void phase_up(const DevScene& d, int l, bool flag, const Rsrc<M>& rhs, const Zc& zc, float2* sz, typename M::acc4* buf) {
+    using acc = typename M::acc;
+    Lv F = lev(d.lv, l);
     const int tx_n = tiles_x(F);
     const int T = tx_n * tiles_y(F);
     const int lx = threadIdx.x & 15, ly = threadIdx.x >> 4;
+    typename M::acc4* part = M::part(d);
     for (int t = blockIdx.x; t < T; t += gridDim.x) {
         if (d.ptile[F.toff + t] == 0u) {
-            if (flag && threadIdx.x == 0) d.partials[t] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            if (flag && threadIdx.x == 0) part[t] = M::a4(0, 0, 0, 0);
             continue;
         }
         const int cx = (t % tx_n) * 16 + lx, cy = (t / tx_n) * 16 + ly;
         const bool red = ((cx + cy) & 1) == 0;
-        const bool unk = unknown(d, F, cx, cy);
+        const bool unk = unknown<M>(d, F, cx, cy);
         float2 z = make_float2(0.0f, 0.0f);
-        if (unk && !red) z = up_black(d, F, zc, C.w, rhs, cx, cy);
+        if (unk && !red) z = up_black<M>(d, F, zc, rhs, cx, cy);
         sz[threadIdx.x] = z;
         __syncthreads();
-        float4 a4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        typename M::acc4 a4 = M::a4(0, 0, 0, 0);
         if (l_inside(F, cx, cy)) {
             const int i = l_at(F, cx, cy);
             if (unk) {
-                float2 r = rhs[i];
+                float2 r = rhs.at(d, i);
                 if (red) {
-                    float4 w = d.mga[i];
+                    float4 w = M::A(d, i);
                     float sx = r.x, sy = r.y;
                     for (int q = 0; q < 4; q++) {
                         int nx = cx + NBX[q], ny = cy + NBY[q];
-                        if (!unknown(d, F, nx, ny)) continue;
+                        if (!unknown<M>(d, F, nx, ny)) continue;
                         int lnx = lx + NBX[q], lny = ly + NBY[q];
                         bool here = lnx >= 0 && lny >= 0 && lnx < 16 && lny < 16;
-                        float2 zb = here ? sz[lny * 16 + lnx] : up_black(d, F, zc, C.w, rhs, nx, ny);
+                        float2 zb = here ? sz[lny * 16 + lnx] : up_black<M>(d, F, zc, rhs, nx, ny);
                         float wd = wcomp(w, q);
                         sx += wd * zb.x;
                         sy += wd * zb.y;
                     }
-                    float di = d.mgd[i];
+                    float di = M::Dg(d, i);
                     z = make_float2(sx / di, sy / di);
                 }
-                a4 = make_float4(r.x * z.x, r.y * z.y, r.x * r.x, r.y * r.y);
+                a4 = M::a4((acc)r.x * (acc)z.x, (acc)r.y * (acc)z.y, (acc)r.x * (acc)r.x, (acc)r.y * (acc)r.y);
             }
-            d.mgz[i] = z;
+            M::setZ(d, i, z);
         }
         if (flag) {
             buf[threadIdx.x] = a4;
             block_tree(buf);
-            if (threadIdx.x == 0) d.partials[t] = buf[0];
+            if (threadIdx.x == 0) part[t] = buf[0];
         }
         __syncthreads();
     }
@@ -398,9 +510,10 @@ DEV void phase_up(const DevScene& d, int l, bool flag, const float2* rhs, const 
 // tail levels, right-hand side the first tail level's mgr, result left in tl.x (the first
 // tail level's slots). Every block gets the same values; the way up of the level above
 // reads them from its own copy, so no grid barrier follows the tail.
+template <class M>
 DEV void phase_tail(const DevScene& d, const Tail& tl) {
     const int first = d.lv.tail, last = d.lv.n - 1;
-    for (int s = threadIdx.x; s < tl.nf; s += NT) tl.r[s] = d.mgr[tl.base + s];
+    for (int s = threadIdx.x; s < tl.nf; s += NT) tl.r[s] = M::R(d, tl.base + s);
     __syncthreads();
     auto sweep = [&](const Lv& L, int colour, bool zero) {
         const int o = L.off - tl.base;
@@ -493,48 +606,91 @@ DEV void phase_tail(const DevScene& d, const Tail& tl) {
         sweep(F, 0, false);
     }
     if (blockIdx.x == 0)   // the first tail level's result, for inspection
-        for (int s = threadIdx.x; s < tl.nf; s += NT) d.mgz[tl.base + s] = tl.x[s];
+        for (int s = threadIdx.x; s < tl.nf; s += NT) M::setZ(d, tl.base + s, tl.x[s]);
 }
 
 // One V-cycle: level 0's right-hand side through R (fused with the CG update when R.q is
 // set), result in mgz of level 0, partials of r.z and r.r. Returns false on a barrier timeout.
-DEV bool vcycle(const DevScene& d, const Tail& tl, const Rsrc& R, float2* r_out, const float2* p, const float2* r_new, float2* sz, float4* buf) {
+template <class M>
+DEV bool vcycle(const DevScene& d, const Tail& tl, const Rsrc<M>& R, float2* r_out, const float2* p, const float2* r_new,
+                float2* sz, typename M::acc4* buf) {
     const int tail = d.lv.tail;
     for (int l = 0; l < tail; l++) {
-        Rsrc Rl = R;
-        if (l > 0) Rl = Rsrc{d.mgr, nullptr, 0.0f, 0.0f};
-        phase_down(d, l, Rl, l == 0 ? r_out : nullptr, p, sz);
+        Rsrc<M> Rl = R;
+        if (l > 0) Rl = Rsrc<M>{nullptr, nullptr, 0.0f, 0.0f};
+        phase_down<M>(d, l, Rl, l == 0 ? r_out : nullptr, p, sz);
         if (!grid_sync(d.K)) return false;
     }
-    phase_tail(d, tl);
+    phase_tail<M>(d, tl);
     for (int l = tail - 1; l >= 0; l--) {
-        const float2* zc = (l == tail - 1) ? tl.x : d.mgz + lev(d.lv, l + 1).off;
-        phase_up(d, l, l == 0, l == 0 ? r_new : d.mgr, zc, sz, buf);
+        const Lv C = lev(d.lv, l + 1);
+        const Zc zc{(l == tail - 1) ? tl.x : nullptr, C.off, C.w};
+        const Rsrc<M> rhs = l == 0 ? Rsrc<M>{r_new, nullptr, 0.0f, 0.0f} : Rsrc<M>{nullptr, nullptr, 0.0f, 0.0f};
+        phase_up<M>(d, l, l == 0, rhs, zc, sz, buf);
         if (!grid_sync(d.K)) return false;
     }
     return true;
 }
 
-// cg_apply.comp: p = z + beta p_old, q = A p, partial sums of p.q into part[n + tile].
-DEV void phase_apply(const DevScene& d, const Solve& K, const float2* p_old, float2* p_new, float4* buf) {
+// The mixed solve's closing check: the true residual b - A x of the final iterate with FP64
+// arithmetic (the products and sums of the FP32 values in double), per tile the sums of
+// |b - A x|^2 and |b|^2 of the pressure potential into part[tile].
+DEV void phase_true_residual(const DevScene& d, Dbl4* part, Dbl4* buf) {
+    Lv F = lev(d.lv, 0);
+    const int tx_n = tiles_x(F);
+    const int T = tx_n * tiles_y(F);
+    for (int t = blockIdx.x; t < T; t += gridDim.x) {
+        if (d.ptile[F.toff + t] == 0u) {
+            if (threadIdx.x == 0) part[t] = Dbl4{0.0, 0.0, 0.0, 0.0};
+            continue;
+        }
+        const int cx = (t % tx_n) * 16 + (threadIdx.x & 15), cy = (t / tx_n) * 16 + (threadIdx.x >> 4);
+        Dbl4 a4{0.0, 0.0, 0.0, 0.0};
+        if (l_inside(F, cx, cy)) {
+            const int i = l_at(F, cx, cy);
+            const float D = d.mgd[i];
+            if (D > 0.0f) {
+                const float4 w = d.mga[i];
+                double r = (double)d.prhs[i].x - (double)D * (double)d.pres[i].x;
+                for (int q = 0; q < 4; q++) {
+                    int nx = cx + NBX[q], ny = cy + NBY[q];
+                    if (unknown_op(d, F, nx, ny)) r += (double)wcomp(w, q) * (double)d.pres[l_at(F, nx, ny)].x;
+                }
+                const double b = (double)d.prhs[i].x;
+                a4 = Dbl4{r * r, b * b, 0.0, 0.0};
+            }
+        }
+        buf[threadIdx.x] = a4;
+        block_tree(buf);
+        if (threadIdx.x == 0) part[t] = buf[0];
+        __syncthreads();
+    }
+}
+
+// cg_apply.comp: p = z + beta p_old, q = A p (the FP32 operator), partial sums of p.q into
+// part[n + tile].
+template <class M>
+DEV void phase_apply(const DevScene& d, float b0, float b1, const float2* p_old, float2* p_new, typename M::acc4* buf) {
+    using acc = typename M::acc;
     Lv F = lev(d.lv, 0);
     const int tx_n = tiles_x(F);
     const int T = tx_n * tiles_y(F);
     const int n = d.nwg;
-    const bool nob = K.beta[0] == 0.0f && K.beta[1] == 0.0f;
+    typename M::acc4* part = M::part(d) + n;
+    const bool nob = b0 == 0.0f && b1 == 0.0f;
     auto direction = [&](int i) {
         float2 z = d.mgz[i];
         if (nob) return z;
         float2 po = p_old[i];
-        return make_float2(K.beta[0] != 0.0f ? z.x + K.beta[0] * po.x : z.x, K.beta[1] != 0.0f ? z.y + K.beta[1] * po.y : z.y);
+        return make_float2(b0 != 0.0f ? z.x + b0 * po.x : z.x, b1 != 0.0f ? z.y + b1 * po.y : z.y);
     };
     for (int t = blockIdx.x; t < T; t += gridDim.x) {
         if (d.ptile[F.toff + t] == 0u) {
-            if (threadIdx.x == 0) d.partials[n + t] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            if (threadIdx.x == 0) part[t] = M::a4(0, 0, 0, 0);
             continue;
         }
         const int cx = (t % tx_n) * 16 + (threadIdx.x & 15), cy = (t / tx_n) * 16 + (threadIdx.x >> 4);
-        float4 a4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        typename M::acc4 a4 = M::a4(0, 0, 0, 0);
         if (l_inside(F, cx, cy)) {
             const int i = l_at(F, cx, cy);
             const float D = d.mgd[i];
@@ -544,7 +700,7 @@ DEV void phase_apply(const DevScene& d, const Solve& K, const float2* p_old, flo
                 float qx = D * pp.x, qy = D * pp.y;
                 for (int q = 0; q < 4; q++) {
                     int nx = cx + NBX[q], ny = cy + NBY[q];
-                    if (unknown(d, F, nx, ny)) {
+                    if (unknown_op(d, F, nx, ny)) {
                         float2 pn = direction(l_at(F, nx, ny));
                         float wd = wcomp(w, q);
                         qx -= wd * pn.x;
@@ -553,29 +709,38 @@ DEV void phase_apply(const DevScene& d, const Solve& K, const float2* p_old, flo
                 }
                 p_new[i] = pp;
                 d.cgq[i] = make_float2(qx, qy);
-                a4 = make_float4(0.0f, 0.0f, pp.x * qx, pp.y * qy);
+                a4 = M::a4(0, 0, (acc)pp.x * (acc)qx, (acc)pp.y * (acc)qy);
             } else {
                 p_new[i] = make_float2(0.0f, 0.0f);
             }
         }
         buf[threadIdx.x] = a4;
         block_tree(buf);
-        if (threadIdx.x == 0) d.partials[n + t] = buf[0];
+        if (threadIdx.x == 0) part[t] = buf[0];
         __syncthreads();
     }
 }
+
+template <class T>
+DEV T mix_was(T a, T keep, uint32_t was) { return mixf(a, keep, (float)was); }
+template <>
+DEV double mix_was<double>(double a, double keep, uint32_t was) { return was ? keep : a; }
 
 }  // namespace
 
 // The whole pressure solve. `second`: the solve after the implicit viscosity (cg_reduce
 // mode 8/9: same matrix and hierarchy, density correction counted as solved).
+template <class M>
 __global__ void __launch_bounds__(NT) k_mgpcg(DevScene d, int second, int scale_mode) {
+    using acc = typename M::acc;
+    using acc4 = typename M::acc4;
     __shared__ float2 sz[NT];
-    __shared__ float4 buf[NT];
-    __shared__ Solve K;
+    __shared__ acc4 buf[NT];
+    __shared__ Solve<acc> K;
     extern __shared__ __align__(16) unsigned char tail_smem[];
     const DevParams* P = d.P;
     const int n = d.nwg;
+    acc4* part = M::part(d);
     Tail tl;
     {
         const Lv F = lev(d.lv, d.lv.tail), E = lev(d.lv, d.lv.n - 1);
@@ -588,21 +753,25 @@ __global__ void __launch_bounds__(NT) k_mgpcg(DevScene d, int second, int scale_
         tl.dg = reinterpret_cast<float*>(tl.r + tl.T);
     }
     if (!second) {
-        phase_cg_scale(d, scale_mode);
+        phase_cg_scale<M>(d, scale_mode);
         for (int l = 1; l <= d.lv.tail; l++) {
             if (!grid_sync(d.K)) return;
-            phase_mg_build(d, l - 1);
+            phase_mg_build<M>(d, l - 1);
         }
         if (!grid_sync(d.K)) return;
     }
-    tail_setup(d, tl);
+    tail_setup<M>(d, tl);
     float2* r_cur = d.mgr;    // level 0 of mgr: the residual, double-buffered with mgr2
     float2* r_nxt = d.mgr2;
-    phase_cg_init(d, r_cur, buf);
+    phase_residual<M>(d, r_cur, buf, false);
     if (!grid_sync(d.K)) return;
-    if (!vcycle(d, tl, Rsrc{r_cur, nullptr, 0.0f, 0.0f}, nullptr, nullptr, r_cur, sz, buf)) return;
+    // b.b now, while nothing writes the second half of the partials: the first apply phase
+    // after the V-cycle does, and a block can reach it before a slower one has summed them
+    const acc4 b = total(part + n, n, buf);
+    if (!vcycle<M>(d, tl, Rsrc<M>{r_cur, nullptr, 0.0f, 0.0f}, nullptr, nullptr, r_cur, sz, buf)) return;
+    const acc tx = (acc)P->tol[0], ty = (acc)P->tol[1];
     {
-        float4 a = total(d.partials, n, buf), b = total(d.partials + n, n, buf);
+        acc4 a = total(part, n, buf);
         if (threadIdx.x == 0) {
             K.bb[0] = b.x;
             K.bb[1] = b.y;
@@ -610,10 +779,9 @@ __global__ void __launch_bounds__(NT) k_mgpcg(DevScene d, int second, int scale_
             K.rz[1] = a.y;
             K.rr[0] = a.z;
             K.rr[1] = a.w;
-            K.beta[0] = K.beta[1] = 0.0f;
-            K.alpha[0] = K.alpha[1] = 0.0f;
+            K.beta[0] = K.beta[1] = 0;
+            K.alpha[0] = K.alpha[1] = 0;
             K.iters[0] = K.iters[1] = 0u;
-            float tx = P->tol[0], ty = P->tol[1];
             K.done[0] = a.z <= tx * tx * b.x ? 1u : 0u;
             K.done[1] = a.w <= ty * ty * b.y ? 1u : 0u;
             if (second) K.done[1] = 1u;
@@ -624,39 +792,38 @@ __global__ void __launch_bounds__(NT) k_mgpcg(DevScene d, int second, int scale_
     float2* p_new = d.cgp2;
     for (uint32_t it = 0; it < P->pressure_max_iters; it++) {
         if (K.done[0] && K.done[1]) break;
-        phase_apply(d, K, p_old, p_new, buf);
+        phase_apply<M>(d, (float)K.beta[0], (float)K.beta[1], p_old, p_new, buf);
         if (!grid_sync(d.K)) return;
         {
-            float4 b = total(d.partials + n, n, buf);
+            acc4 b = total(part + n, n, buf);
             if (threadIdx.x == 0) {
-                float ax = 0.0f, ay = 0.0f;
-                if (K.done[0] == 0u && b.z > 0.0f) ax = K.rz[0] / b.z;
-                if (K.done[1] == 0u && b.w > 0.0f) ay = K.rz[1] / b.w;
+                acc ax = 0, ay = 0;
+                if (K.done[0] == 0u && b.z > 0) ax = K.rz[0] / b.z;
+                if (K.done[1] == 0u && b.w > 0) ay = K.rz[1] / b.w;
                 K.alpha[0] = ax;
                 K.alpha[1] = ay;
             }
             __syncthreads();
         }
-        Rsrc R{r_cur, d.cgq, K.alpha[0], K.alpha[1]};
-        if (!vcycle(d, tl, R, r_nxt, p_new, r_nxt, sz, buf)) return;
+        Rsrc<M> R{r_cur, d.cgq, (float)K.alpha[0], (float)K.alpha[1]};
+        if (!vcycle<M>(d, tl, R, r_nxt, p_new, r_nxt, sz, buf)) return;
         {
-            float4 a = total(d.partials, n, buf);
+            acc4 a = total(part, n, buf);
             if (threadIdx.x == 0) {
                 uint32_t was0 = K.done[0], was1 = K.done[1];
                 K.iters[0] += 1u - was0;
                 K.iters[1] += 1u - was1;
-                float tx = P->tol[0], ty = P->tol[1];
                 uint32_t now0 = a.z <= tx * tx * K.bb[0] ? 1u : 0u, now1 = a.w <= ty * ty * K.bb[1] ? 1u : 0u;
                 uint32_t d0 = was0 > now0 ? was0 : now0, d1 = was1 > now1 ? was1 : now1;
-                float bx = 0.0f, by = 0.0f;
-                if (d0 == 0u && K.rz[0] > 0.0f) bx = a.x / K.rz[0];
-                if (d1 == 0u && K.rz[1] > 0.0f) by = a.y / K.rz[1];
+                acc bx = 0, by = 0;
+                if (d0 == 0u && K.rz[0] > 0) bx = a.x / K.rz[0];
+                if (d1 == 0u && K.rz[1] > 0) by = a.y / K.rz[1];
                 K.beta[0] = bx;
                 K.beta[1] = by;
                 K.rz[0] = a.x;
                 K.rz[1] = a.y;
-                K.rr[0] = mixf(a.z, K.rr[0], (float)was0);
-                K.rr[1] = mixf(a.w, K.rr[1], (float)was1);
+                K.rr[0] = mix_was<acc>(a.z, K.rr[0], was0);
+                K.rr[1] = mix_was<acc>(a.w, K.rr[1], was1);
                 K.done[0] = d0;
                 K.done[1] = d1;
             }
@@ -669,14 +836,25 @@ __global__ void __launch_bounds__(NT) k_mgpcg(DevScene d, int second, int scale_
         r_cur = r_nxt;
         r_nxt = t;
     }
+    double true_rel = -1.0;
+    if constexpr (M::kMixed) {
+        phase_true_residual(d, d.partials64, reinterpret_cast<Dbl4*>(buf));
+        if (!grid_sync(d.K)) return;
+        const Dbl4 t4 = total(d.partials64, n, reinterpret_cast<Dbl4*>(buf));
+        true_rel = t4.y > 0.0 ? sqrt(t4.x / t4.y) : 0.0;
+    }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         SolveState* G = d.K;
+        if (true_rel >= 0.0) {
+            G->p_true_res = (float)true_rel;
+            G->p_true_res_max = maxf(G->p_true_res_max, (float)true_rel);
+        }
         for (int c = 0; c < 2; c++) {
-            G->p_rz[c] = K.rz[c];
-            G->p_alpha[c] = K.alpha[c];
-            G->p_beta[c] = K.beta[c];
-            G->p_bb[c] = K.bb[c];
-            G->p_rr[c] = K.rr[c];
+            G->p_rz[c] = (float)K.rz[c];
+            G->p_alpha[c] = (float)K.alpha[c];
+            G->p_beta[c] = (float)K.beta[c];
+            G->p_bb[c] = (float)K.bb[c];
+            G->p_rr[c] = (float)K.rr[c];
             G->p_done[c] = K.done[c];
             if (!second) G->p_iters[c] = K.iters[c];
         }
@@ -690,8 +868,8 @@ __global__ void __launch_bounds__(NT) k_mgpcg(DevScene d, int second, int scale_
             if (K.iters[0] > G->p2_it_max) G->p2_it_max = K.iters[0];
             if (K.done[0] == 0u) G->p2_unconv += 1u;
         }
-        float rel = K.bb[0] > 0.0f ? sqrtf(K.rr[0] / K.bb[0]) : 0.0f;
-        G->p_res_max = maxf(G->p_res_max, rel);
+        const float rel = K.bb[0] > 0 ? (float)sqrt((double)K.rr[0] / (double)K.bb[0]) : 0.0f;
+        G->p_res_max = maxf(G->p_res_max, M::kMixed ? rel : (K.bb[0] > 0 ? sqrtf((float)K.rr[0] / (float)K.bb[0]) : 0.0f));
     }
 }
 
@@ -700,18 +878,25 @@ size_t pressure_smem(const Levels& lv) {
     return (size_t)T * (sizeof(float4) + 2 * sizeof(float2) + sizeof(float));
 }
 
-int pressure_blocks_max(int device, size_t smem) {
+namespace {
+template <class M>
+int blocks_max(int device, size_t smem) {
     int sms = 0, per = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     // Opt in to the dynamic shared memory the largest tank so far needs (static + dynamic
     // above 48 KB needs it; the attribute belongs to the kernel, shared by every sim).
     static size_t opted = 0;
     if (smem > opted) {
-        cudaFuncSetAttribute(k_mgpcg, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaFuncSetAttribute(k_mgpcg<M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         opted = smem;
     }
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_mgpcg, NT, smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_mgpcg<M>, NT, smem);
     return sms * per;
+}
+}  // namespace
+
+int pressure_blocks_max(int device, size_t smem, bool mixed) {
+    return mixed ? blocks_max<Mixed>(device, smem) : blocks_max<Plain>(device, smem);
 }
 
 cudaError_t launch_pressure(const DevScene& d, const LaunchCfg& cfg, cudaStream_t st, int second) {
@@ -721,7 +906,9 @@ cudaError_t launch_pressure(const DevScene& d, const LaunchCfg& cfg, cudaStream_
     // substep's P1 alone (viscous_warm, mod.rs:2979-2983)
     int scale_mode = (!second && cfg.visc_mode == 2 && cfg.twice && cfg.viscous_warm) ? 1 : 0;
     void* args[] = {(void*)&d, &second, &scale_mode};
-    return cudaLaunchCooperativeKernel((const void*)k_mgpcg, dim3(cfg.mg_blocks), dim3(NT), args, pressure_smem(d.lv), st);
+    const void* fn = cfg.mixed ? (const void*)k_mgpcg<Mixed> : (const void*)k_mgpcg<Plain>;
+    const int blocks = cfg.mixed ? cfg.mg_blocks_mixed : cfg.mg_blocks;
+    return cudaLaunchCooperativeKernel(fn, dim3(blocks), dim3(NT), args, pressure_smem(d.lv), st);
 }
 
 }  // namespace sprout
@@ -908,12 +1095,12 @@ extern "C" int sprout_pressure_solve_static(uint32_t w, uint32_t h, const float*
     k_static_prep<<<128, 256, 0, st>>>(d, reinterpret_cast<const float4*>(mga), mgd, reinterpret_cast<const float2*>(rhs),
                                        tol_p, tol_psi, max_iters);
     const size_t smem = pressure_smem(L);
-    int blocks = pressure_blocks_max(dev, smem);
+    int blocks = pressure_blocks_max(dev, smem, false);
     if (blocks > d.nwg) blocks = d.nwg;
     if (blocks < 1) blocks = 1;
     int second = 0, scale_mode = 0;
     void* args[] = {(void*)&d, &second, &scale_mode};
-    cudaError_t e = cudaLaunchCooperativeKernel((const void*)k_mgpcg, dim3(blocks), dim3(NT), args, smem, st);
+    cudaError_t e = cudaLaunchCooperativeKernel((const void*)k_mgpcg<Plain>, dim3(blocks), dim3(NT), args, smem, st);
     if (e != cudaSuccess) {
         sprout_internal_set_error(cudaGetErrorString(e));
         return -6;

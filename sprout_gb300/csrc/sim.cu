@@ -156,6 +156,34 @@ struct SproutSim {
         return SPROUT_OK;
     }
 
+    // The mixed-precision pressure solve: its BF16 matrices and FP64 partial sums,
+    // allocated the first time it is asked for.
+    bool mixed = false, mixed_alloc = false;
+
+    int set_precision(int mode) {
+        if (mode != 0 && mode != 1) return fail(SPROUT_E_ARG, "precision mode is 0 (plain FP32) or 1 (mixed)");
+        if (mode == 1 && !mixed_alloc) {
+            CUDA_TRY(cudaStreamSynchronize(stream));
+            size_t tot = (size_t)d.lv.total;
+            int rc = SPROUT_OK;
+#define A(ptr, n) do { if ((rc = alloc(&(ptr), (n))) != SPROUT_OK) return rc; } while (0)
+            A(d.hga, tot); A(d.hgd, tot);
+            A(d.partials64, 2 * (size_t)d.nwg);
+#undef A
+            int mx = pressure_blocks_max(device, pressure_smem(d.lv), true);
+            cfg.mg_blocks_mixed = std::max(1, std::min(d.nwg, mx));
+            if (const char* e = std::getenv("SPROUT_MG_BLOCKS")) {
+                int want = std::atoi(e);
+                if (want > 0) cfg.mg_blocks_mixed = std::max(1, std::min(want, mx));
+            }
+            CUDA_TRY(cudaDeviceSynchronize());
+            mixed_alloc = true;
+            graph_ok = false;   // new device pointers: the captured substep is stale
+        }
+        mixed = mode == 1;
+        return SPROUT_OK;
+    }
+
     // The viscosity treatment of the tank (FluidSim::viscosity_mode, mod.rs:2768-2792),
     // re-derived before every record as the reference does, and what this engine carries.
     int derive_viscosity() {
@@ -236,7 +264,7 @@ struct SproutSim {
 #undef A
         std::vector<float> nt(nc, NO_TEMP);
         CUDA_TRY(cudaMemcpy(solid_t, nt.data(), nc * sizeof(float), cudaMemcpyHostToDevice));
-        int mx = pressure_blocks_max(device, pressure_smem(d.lv));
+        int mx = pressure_blocks_max(device, pressure_smem(d.lv), false);
         cfg.mg_blocks = std::max(1, std::min(d.nwg, mx));
         // SPROUT_MG_BLOCKS: a tuning override of the persistent kernel's block count
         // (at most what fits on the device at once).
@@ -412,10 +440,11 @@ struct SproutSim {
         want.visc_levels = std::min((int)std::max(params.viscosity_mg_levels, 1u), d.lv.tail);
         want.visc_sweeps = (int)std::min(std::max(params.viscosity_mg_sweeps, 1u), 2u);
         want.visc_blocks = std::max(1, std::min(d.nwg, visc_max[want.visc_sweeps - 1]));
+        want.mixed = mixed;
         bool same = graph_ok && want.n_slots == cfg.n_slots && want.thermal == cfg.thermal && want.heat == cfg.heat &&
                     want.visc_mode == cfg.visc_mode && want.twice == cfg.twice && want.viscous_warm == cfg.viscous_warm &&
                     want.visc_levels == cfg.visc_levels && want.visc_sweeps == cfg.visc_sweeps &&
-                    want.visc_blocks == cfg.visc_blocks && d.stride == tank.stride;
+                    want.visc_blocks == cfg.visc_blocks && want.mixed == cfg.mixed && d.stride == tank.stride;
         cfg = want;
         d.stride = std::max(tank.stride, 8);
         if (same || !use_graph) return SPROUT_OK;
@@ -717,6 +746,10 @@ int sprout_sim_destroy(SproutSim* sim) {
     delete sim;
     return SPROUT_OK;
 }
+int sprout_sim_set_precision(SproutSim* sim, int mode) {
+    if (!sim) return fail(SPROUT_E_ARG, "null argument");
+    return sim->set_precision(mode);
+}
 int sprout_sim_set_params(SproutSim* sim, const SproutParams* p) {
     if (!sim || !p) return fail(SPROUT_E_ARG, "null argument");
     sim->params = p->p;
@@ -812,6 +845,7 @@ int sprout_sim_download_field(SproutSim* sim, const char* name, void* out, size_
     else if (n == "count") { src = d.count; b = nc * 4; }
     else if (n == "start") { src = d.start; b = (nc + 1) * 4; }
     else if (n == "step") { src = d.S; b = sizeof(StepState); }
+    else if (n == "solve") { src = d.K; b = sizeof(SolveState); }
     else if (n == "region_air") { src = &d.S->region_air; b = 4; }
     else return fail(SPROUT_E_ARG, "unknown field " + n);
     *bytes = b;
@@ -859,6 +893,8 @@ int sprout_sim_stats(SproutSim* sim, SproutSolverStats* o) {
     o->device_error = K.error;
     o->viscosity_iters = K.v_iters;
     o->pressure2_iters = K.p2_iters;
+    o->pressure_true_residual = K.p_true_res;
+    o->pressure_true_residual_max = K.p_true_res_max;
     o->viscosity_residual = K.v_r0 > 0.0f ? std::sqrt(K.v_rr / K.v_r0) : 0.0f;
     o->h2d_bytes = sim->h2d_bytes;
     o->d2h_bytes = sim->d2h_bytes;

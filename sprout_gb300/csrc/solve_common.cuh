@@ -52,7 +52,10 @@ DEV bool grid_sync(SolveState* K) {
                     if (*verr != 0u) { ok = 0; break; }
                     __nanosleep(32);
                     if (++spins > SPIN_LIMIT) {
-                        atomicExch(&K->error, 1u);
+                        if (atomicExch(&K->error, 1u) == 0u) {
+                            K->err_arrived = *(volatile uint32_t*)&K->bar_count;
+                            K->err_blocks = gridDim.x;
+                        }
                         ok = 0;
                         break;
                     }
@@ -66,35 +69,33 @@ DEV bool grid_sync(SolveState* K) {
     return s_ok != 0;
 }
 
+DEV float4 add4(float4 a, float4 b) { return make_float4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w); }
+DEV Dbl4 add4(Dbl4 a, Dbl4 b) { return Dbl4{a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w}; }
+
 // Work-group tree of reduce.glsl:5-14 over the 256 values in buf; result in buf[0].
-DEV void block_tree(float4* buf) {
+template <class T>
+DEV void block_tree(T* buf) {
     const int t = threadIdx.x;
     __syncthreads();
     for (int s = 128; s > 0; s >>= 1) {
-        if (t < s) {
-            float4 a = buf[t], b = buf[t + s];
-            buf[t] = make_float4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w);
-        }
+        if (t < s) buf[t] = add4(buf[t], buf[t + s]);
         __syncthreads();
     }
 }
 
 // total() of reduce_tail.glsl:28-41: thread t sums partials t, t + 256, ... in order,
 // then the tree. Every block calls it and gets the same value.
-DEV float4 total(const float4* part, int n, float4* buf) {
+template <class T>
+DEV T total(const T* part, int n, T* buf) {
     const int t = threadIdx.x;
-    float4 s = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    for (int k = t; k < n; k += NT) {
-        float4 v = part[k];
-        s = make_float4(s.x + v.x, s.y + v.y, s.z + v.z, s.w + v.w);
-    }
+    T s{};
+    for (int k = t; k < n; k += NT) s = add4(s, part[k]);
     buf[t] = s;
     block_tree(buf);
-    float4 r = buf[0];
+    T r = buf[0];
     __syncthreads();
     return r;
 }
-
 
 }  // namespace solve
 }  // namespace sprout

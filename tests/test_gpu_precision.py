@@ -1,0 +1,86 @@
+"""The mixed-precision pressure solve (BF16 hierarchy, FP32 iterate and residual, FP64 dot
+products and convergence test, true-residual refinement) against the plain FP32 solve and the
+FP64 reference solution, on the same tanks.
+
+Mixed precision changes the preconditioner's rounding, so its results are not bit-exact with
+the reference's arithmetic; what must hold is the reference's own stopping rule — the same
+relative residual (pressure_tol = 1e-5) — and an error against the FP64 solution of the same
+order as the plain solve's (both stated here with the tolerance the test uses).
+"""
+import numpy as np
+import pytest
+
+import tanks
+from oracle.fp64_mgpcg import accuracy
+
+pytestmark = pytest.mark.gpu
+
+
+def pair(tank):
+    a, _, _ = tank.engine()
+    b, _, _ = tank.engine()
+    b.set_precision("mixed")
+    return a, b
+
+
+def last_system_accuracy(sim, tank, columns):
+    return accuracy(sim.field("mga"), sim.field("mgd"), sim.field("prhs"), sim.field("pres"), tank.w, tank.h,
+                    columns=columns)
+
+
+def test_mixed_first_solve_matches_plain():
+    """The first substep from the same state: both solve the same system (everything before
+    the solve is the same FP32 arithmetic), to the same tolerance, and agree with each other
+    and with the FP64 solution to the order of that tolerance."""
+    t = tanks.dam_break(128, 72)
+    plain, mixed = pair(t)
+    plain.step(1, 1 / 240.0)
+    mixed.step(1, 1 / 240.0)
+    for s in (plain, mixed):
+        st = s.stats()
+        assert st.device_error == 0 and st.pressure_unconverged == 0
+    # the same system (prhs.xy; prhs.z keeps each one's own solution for the projection)
+    assert np.array_equal(plain.field("prhs").reshape(-1, 4)[:, :2], mixed.field("prhs").reshape(-1, 4)[:, :2])
+    pp = plain.field("pres").reshape(-1, 2)[:, 0].astype(np.float64)
+    pm = mixed.field("pres").reshape(-1, 2)[:, 0].astype(np.float64)
+    assert np.linalg.norm(pm - pp) <= 1e-4 * np.linalg.norm(pp)
+    ap = last_system_accuracy(plain, t, (0,))
+    am = last_system_accuracy(mixed, t, (0,))
+    # stopping rule 1e-5 on the residual; against the FP64 solution both stay below 1e-4
+    assert ap[0]["error_vs_fp64"] < 1e-4 and am[0]["error_vs_fp64"] < 1e-4, (ap, am)
+    assert am[0]["residual_fp64"] < 1e-4, am
+    assert mixed.stats().pressure_residual <= 1e-5 * 1.0001
+    # the FP64 true residual the mixed solve reports agrees with the one computed here
+    assert abs(mixed.stats().pressure_true_residual - am[0]["residual_fp64"]) <= 1e-3 * am[0]["residual_fp64"] + 1e-9
+
+
+def test_mixed_keeps_converging_over_a_run():
+    t = tanks.dam_break(128, 72)
+    plain, mixed = pair(t)
+    for s in (plain, mixed):
+        s.step(24, 24 / 240.0)
+    sp, sm = plain.stats(), mixed.stats()
+    assert sm.device_error == 0 and sm.pressure_unconverged == 0
+    assert sm.pressure_residual_max <= 1e-5 * 1.0001
+    # the BF16 preconditioner is a little weaker: at most half as many iterations again
+    assert max(sm.pressure_iters) <= 1.5 * max(sp.pressure_iters) + 2
+
+
+def test_mixed_runs_the_full_physics_pour():
+    t = tanks.full_physics(160, 96, cell=0.0064)
+    plain, mixed = pair(t)
+    for s in (plain, mixed):
+        s.step(12, 12 / 240.0)
+    sp, sm = plain.stats(), mixed.stats()
+    assert sm.device_error == 0
+    assert sm.pressure_unconverged == 0 and sm.pressure2_unconverged == 0
+    assert sm.pressure_residual_max <= 1e-5 * 1.0001
+    assert 0.0 < sm.pressure_true_residual_max < 1e-3
+    # the tanks evolve alike: particle positions within a small fraction of a cell
+    g = np.sort(plain.download_particles(), order="id")
+    m = np.sort(mixed.download_particles(), order="id")
+    assert np.array_equal(g["id"], m["id"])
+    d = np.abs(g["pos"] - m["pos"]).max()
+    assert d < 0.05, d
+    am = last_system_accuracy(mixed, t, (0,))
+    assert am[0]["error_vs_fp64"] < 1e-2, am
