@@ -181,6 +181,29 @@ int sprout_sim_profile_passes(SproutSim* sim, float* ms, uint32_t n);
  * matrices. */
 int sprout_sim_set_precision(SproutSim* sim, int mode);
 
+/* ---- batches: many tanks, one captured graph per substep -------------------------------
+ * The batched and serving layer the reference does not have (it steps one FluidSim). A
+ * batch advances its tanks (sims created, filled and reset as usual) together: their
+ * particle and grid stages as concurrent branches of one CUDA graph per substep, their
+ * pressure solves as one persistent kernel over all their tiles. Each tank's results are
+ * the same as when it steps alone (same arithmetic, same reduction order). A sim belongs to
+ * at most one batch; while it does, sprout_sim_step refuses it (step the batch); its stats,
+ * downloads and parameters work as usual. The implicit viscosity is carried with
+ * viscous_projection 1 (the default). Blocking: sync, profile. */
+typedef struct SproutBatch SproutBatch;
+int sprout_batch_create(SproutBatch** out);
+int sprout_batch_destroy(SproutBatch* b);
+int sprout_batch_add(SproutBatch* b, SproutSim* sim);
+int sprout_batch_remove(SproutBatch* b, SproutSim* sim);
+int sprout_batch_size(SproutBatch* b, uint32_t* n);
+/* 0 plain, 1 mixed (see sprout_sim_set_precision), for every tank of the batch. */
+int sprout_batch_set_precision(SproutBatch* b, int mode);
+/* `substeps` substeps of every tank (each at its own dt), asynchronous. */
+int sprout_batch_step(SproutBatch* b, uint32_t substeps);
+int sprout_batch_sync(SproutBatch* b);
+/* Device ms of `substeps` more substeps of the batch, from CUDA events (blocking). */
+int sprout_batch_profile(SproutBatch* b, uint32_t substeps, float* ms);
+
 /* ---- a pressure solve that allocates nothing ------------------------------------------
  * No counterpart in the reference: an addition for callers that cannot allocate device
  * memory (a host whose allocator owns the whole device, a path that must not allocate

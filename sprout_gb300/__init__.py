@@ -40,6 +40,8 @@ EXPORTS = [
     "sprout_sim_sync", "sprout_sim_download_particles", "sprout_sim_download_pressure",
     "sprout_sim_download_field", "sprout_sim_stats", "sprout_sim_device_bytes", "sprout_sim_profile",
     "sprout_sim_profile_passes", "sprout_pressure_solve_static", "sprout_sim_set_precision",
+    "sprout_batch_create", "sprout_batch_destroy", "sprout_batch_add", "sprout_batch_remove", "sprout_batch_size",
+    "sprout_batch_set_precision", "sprout_batch_step", "sprout_batch_sync", "sprout_batch_profile",
 ]
 
 STAGES = ["advance", "sort", "p2g", "grid", "pressure", "project", "viscosity", "project2"]
@@ -123,6 +125,15 @@ def lib() -> C.CDLL:
         "sprout_sim_profile": ([V, C.c_uint32, P(C.c_float)], C.c_int),
         "sprout_sim_profile_passes": ([V, P(C.c_float), C.c_uint32], C.c_int),
         "sprout_sim_set_precision": ([V, C.c_int], C.c_int),
+        "sprout_batch_create": ([P(V)], C.c_int),
+        "sprout_batch_destroy": ([V], C.c_int),
+        "sprout_batch_add": ([V, V], C.c_int),
+        "sprout_batch_remove": ([V, V], C.c_int),
+        "sprout_batch_size": ([V, P(C.c_uint32)], C.c_int),
+        "sprout_batch_set_precision": ([V, C.c_int], C.c_int),
+        "sprout_batch_step": ([V, C.c_uint32], C.c_int),
+        "sprout_batch_sync": ([V], C.c_int),
+        "sprout_batch_profile": ([V, C.c_uint32, P(C.c_float)], C.c_int),
         "sprout_pressure_solve_static": ([C.c_uint32, C.c_uint32, V, V, V, V, C.c_float, C.c_float, C.c_uint32, V,
                                           P(C.c_uint32), P(C.c_float)], C.c_int),
     }
@@ -316,3 +327,46 @@ def pressure_solve_static(w: int, h: int, mga_ptr: int, mgd_ptr: int, rhs_ptr: i
     _check(lib().sprout_pressure_solve_static(w, h, mga_ptr, mgd_ptr, rhs_ptr, x_ptr, tol_p, tol_psi, max_iters, stream,
                                               iters, C.byref(res)))
     return list(iters), res.value
+
+
+class Batch:
+    """Many FluidSims advanced together: one CUDA graph per substep, their pressure solves
+    in one persistent kernel (sprout_batch_*). Each tank's results equal stepping it alone."""
+
+    def __init__(self, sims=(), precision: str | int = "plain"):
+        self._h = C.c_void_p()
+        _check(lib().sprout_batch_create(C.byref(self._h)))
+        self.sims = []
+        self.set_precision(precision)
+        for s in sims:
+            self.add(s)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().sprout_batch_destroy(self._h)
+            self._h = None
+
+    __del__ = close
+
+    def add(self, sim: FluidSim):
+        _check(lib().sprout_batch_add(self._h, sim._h))
+        self.sims.append(sim)
+
+    def remove(self, sim: FluidSim):
+        _check(lib().sprout_batch_remove(self._h, sim._h))
+        self.sims.remove(sim)
+
+    def set_precision(self, mode: str | int):
+        m = {"plain": 0, "mixed": 1}.get(mode, mode)
+        _check(lib().sprout_batch_set_precision(self._h, int(m)))
+
+    def step(self, substeps: int = 1):
+        _check(lib().sprout_batch_step(self._h, substeps))
+
+    def sync(self):
+        _check(lib().sprout_batch_sync(self._h))
+
+    def profile(self, substeps: int) -> float:
+        ms = C.c_float()
+        _check(lib().sprout_batch_profile(self._h, substeps, C.byref(ms)))
+        return ms.value

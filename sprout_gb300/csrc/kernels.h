@@ -41,6 +41,22 @@ void launch_second_projection_rhs(const DevScene& d, cudaStream_t st);
 void launch_second_projection(const DevScene& d, cudaStream_t st);
 // Blocks of the persistent viscosity kernel that fit on the device at once.
 int viscosity_blocks_max(int device, int sweeps);
+
+// A batch of scenes for one persistent pressure solve over all of them (device arrays).
+struct BatchView {
+    const DevScene* scenes;   // ns scenes
+    int ns;
+    const int* off;           // level l: the ns + 1 prefix sums of the scenes' level-l tiles at l * (ns + 1)
+                              // (a scene counts its levels 0 .. tail)
+    void* scal;               // per scene, the solve's scalars (pressure_batch_scalar_bytes each)
+    const int* scale;         // per scene, the warm-start mode of cg_scale (0 or 1)
+    SolveState* K;            // the batch's grid barrier and error word
+    int max_tail;             // the deepest tail level over the scenes
+};
+// The batched pressure solve: `second` for the solve after the implicit viscosity.
+cudaError_t launch_pressure_batch(const BatchView& B, bool mixed, int blocks, size_t smem, cudaStream_t st, int second);
+int pressure_batch_blocks_max(int device, size_t smem, bool mixed);
+size_t pressure_batch_scalar_bytes();
 // Blocks of the persistent pressure kernel (plain or mixed precision) that fit on the
 // device at once.
 int pressure_blocks_max(int device, size_t smem, bool mixed);

@@ -129,134 +129,132 @@ DEV bool unknown(const DevScene& d, const Lv& L, int x, int y) { return l_inside
 DEV bool unknown_op(const DevScene& d, const Lv& L, int x, int y) { return l_inside(L, x, y) && d.mgd[l_at(L, x, y)] > 0.0f; }
 
 
-// cg_scale.comp: warm start from last substep's potential rescaled to this substep. Mixed:
-// also level 0's matrix in BF16 for the V-cycle (every cell: rhs.comp rewrote them all).
+// cg_scale.comp on level-0 tile t: warm start from last substep's potential rescaled to
+// this substep. Mixed: also level 0's matrix in BF16 for the V-cycle (every cell: rhs.comp
+// rewrote them all).
 template <class M>
-DEV void phase_cg_scale(const DevScene& d, int mode) {
-    Lv F = lev(d.lv, 0);
+DEV void cg_scale_tile(const DevScene& d, int t, int mode) {
+    const Lv F = lev(d.lv, 0);
     const float ratio = d.S->dt / d.S->dt_prev;
-    const int T = tiles_x(F) * tiles_y(F);
-    for (int t = blockIdx.x; t < T; t += gridDim.x) {
-        int cx = (t % tiles_x(F)) * 16 + (threadIdx.x & 15), cy = (t / tiles_x(F)) * 16 + (threadIdx.x >> 4);
-        if (!l_inside(F, cx, cy)) continue;
-        int i = l_at(F, cx, cy);
-        if (M::kMixed) {
-            int m = 0;
-            for (int q = 0; q < 4; q++) m |= unknown_op(d, F, cx + NBX[q], cy + NBY[q]) ? (1 << q) : 0;
-            Mixed::setA(d, i, d.mga[i], d.mgd[i], m);
-        }
-        if (d.ptile[F.toff + t] == 0u) continue;
-        if (d.mgd[i] > 0.0f) {
-            float p = d.pres[i].x;
-            if (mode == 1) p -= d.p2keep[i];
-            else d.p2keep[i] = 0.0f;
-            d.pres[i].x = p * ratio;
-        } else {
-            d.pres[i] = make_float2(0.0f, 0.0f);
-        }
+    const int cx = (t % tiles_x(F)) * 16 + (threadIdx.x & 15), cy = (t / tiles_x(F)) * 16 + (threadIdx.x >> 4);
+    if (!l_inside(F, cx, cy)) return;
+    const int i = l_at(F, cx, cy);
+    if (M::kMixed) {
+        int m = 0;
+        for (int q = 0; q < 4; q++) m |= unknown_op(d, F, cx + NBX[q], cy + NBY[q]) ? (1 << q) : 0;
+        Mixed::setA(d, i, d.mga[i], d.mgd[i], m);
+    }
+    if (d.ptile[F.toff + t] == 0u) return;
+    if (d.mgd[i] > 0.0f) {
+        float p = d.pres[i].x;
+        if (mode == 1) p -= d.p2keep[i];
+        else d.p2keep[i] = 0.0f;
+        d.pres[i].x = p * ratio;
+    } else {
+        d.pres[i] = make_float2(0.0f, 0.0f);
     }
 }
 
-// mg_build.comp: coarse level l + 1 from level l over the tiles of the coarse level.
+// mg_build.comp on tile t of coarse level l + 1, from level l.
 template <class M>
-DEV void phase_mg_build(const DevScene& d, int l) {
-    Lv F = lev(d.lv, l), C = lev(d.lv, l + 1);
+DEV void mg_build_tile(const DevScene& d, int l, int t) {
+    const Lv F = lev(d.lv, l), C = lev(d.lv, l + 1);
     const int tfx = tiles_x(F), tfy = tiles_y(F), tcx = tiles_x(C);
-    const int T = tcx * tiles_y(C);
     __shared__ uint32_t s_state;
-    for (int t = blockIdx.x; t < T; t += gridDim.x) {
-        const int tx = t % tcx, ty = t / tcx;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            uint32_t on = 0u;
-            for (int k = 0; k < 4; k++) {
-                int fx = 2 * tx + (k & 1), fy = 2 * ty + (k >> 1);
-                if (fx < tfx && fy < tfy) on |= d.ptile[F.toff + fy * tfx + fx];
-            }
-            uint32_t slot = (uint32_t)C.toff + (uint32_t)t;
-            uint32_t was = d.ptile[slot];
-            d.ptile[slot] = on != 0u ? 1u : 0u;
-            s_state = (on != 0u ? 1u : 0u) | (was != 0u ? 2u : 0u);
-        }
-        __syncthreads();
-        const uint32_t state = s_state;
-        if (state == 0u) continue;
-        const int Cx = tx * 16 + (threadIdx.x & 15), Cy = ty * 16 + (threadIdx.x >> 4);
-        if (Cx >= C.w || Cy >= C.h) continue;
-        const int o = l_at(C, Cx, Cy);
-        if ((state & 1u) == 0u) {
-            M::setA(d, o, make_float4(0.0f, 0.0f, 0.0f, 0.0f), 0.0f);
-            continue;
-        }
-        float D = 0.0f;
-        float4 A = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    const int tx = t % tcx, ty = t / tcx;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t on = 0u;
         for (int k = 0; k < 4; k++) {
-            int cx = 2 * Cx + (k & 1), cy = 2 * Cy + (k >> 1);
-            if (!unknown<M>(d, F, cx, cy)) continue;
-            int i = l_at(F, cx, cy);
-            D += M::Dg(d, i);
-            float4 w = M::A(d, i);
-            for (int q = 0; q < 4; q++) {
-                int nx = cx + NBX[q], ny = cy + NBY[q];
-                if (!unknown<M>(d, F, nx, ny)) continue;
-                float wd = wcomp(w, q);
-                if ((nx >> 1) == Cx && (ny >> 1) == Cy) D -= wd;
-                else if (q == 0) A.x += wd;
-                else if (q == 1) A.y += wd;
-                else if (q == 2) A.z += wd;
-                else A.w += wd;
-            }
+            int fx = 2 * tx + (k & 1), fy = 2 * ty + (k >> 1);
+            if (fx < tfx && fy < tfy) on |= d.ptile[F.toff + fy * tfx + fx];
         }
-        M::setA(d, o, D > 1e-7f ? A : make_float4(0.0f, 0.0f, 0.0f, 0.0f), D > 1e-7f ? D : 0.0f);
+        uint32_t slot = (uint32_t)C.toff + (uint32_t)t;
+        uint32_t was = d.ptile[slot];
+        d.ptile[slot] = on != 0u ? 1u : 0u;
+        s_state = (on != 0u ? 1u : 0u) | (was != 0u ? 2u : 0u);
     }
+    __syncthreads();
+    const uint32_t state = s_state;
+    if (state == 0u) return;
+    const int Cx = tx * 16 + (threadIdx.x & 15), Cy = ty * 16 + (threadIdx.x >> 4);
+    if (Cx >= C.w || Cy >= C.h) return;
+    const int o = l_at(C, Cx, Cy);
+    if ((state & 1u) == 0u) {
+        M::setA(d, o, make_float4(0.0f, 0.0f, 0.0f, 0.0f), 0.0f);
+        return;
+    }
+    float D = 0.0f;
+    float4 A = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    for (int k = 0; k < 4; k++) {
+        int cx = 2 * Cx + (k & 1), cy = 2 * Cy + (k >> 1);
+        if (!unknown<M>(d, F, cx, cy)) continue;
+        int i = l_at(F, cx, cy);
+        D += M::Dg(d, i);
+        float4 w = M::A(d, i);
+        for (int q = 0; q < 4; q++) {
+            int nx = cx + NBX[q], ny = cy + NBY[q];
+            if (!unknown<M>(d, F, nx, ny)) continue;
+            float wd = wcomp(w, q);
+            if ((nx >> 1) == Cx && (ny >> 1) == Cy) D -= wd;
+            else if (q == 0) A.x += wd;
+            else if (q == 1) A.y += wd;
+            else if (q == 2) A.z += wd;
+            else A.w += wd;
+        }
+    }
+    M::setA(d, o, D > 1e-7f ? A : make_float4(0.0f, 0.0f, 0.0f, 0.0f), D > 1e-7f ? D : 0.0f);
 }
 
-// cg_init.comp: r = b - A x (the FP32 operator), partial sums of b.b into part[n + tile].
-// With `rr`: the true residual of the refinement instead, partial sums of r.r into part[tile].
+// cg_init.comp on level-0 tile t: r = b - A x (the FP32 operator), the tile's sum of b.b
+// into part[n + t] (or, with `rr`, of r.r into part[t]).
 template <class M>
-DEV void phase_residual(const DevScene& d, float2* r0, typename M::acc4* buf, bool rr) {
+DEV void residual_tile(const DevScene& d, int t, float2* r0, typename M::acc4* buf, bool rr) {
     using acc = typename M::acc;
-    Lv F = lev(d.lv, 0);
-    const int T = tiles_x(F) * tiles_y(F);
+    const Lv F = lev(d.lv, 0);
     const int n = d.nwg;
     typename M::acc4* part = M::part(d) + (rr ? 0 : n);
-    for (int t = blockIdx.x; t < T; t += gridDim.x) {
-        if (d.ptile[F.toff + t] == 0u) {
-            if (threadIdx.x == 0) part[t] = M::a4(0, 0, 0, 0);
-            continue;
-        }
-        const int cx = (t % tiles_x(F)) * 16 + (threadIdx.x & 15), cy = (t / tiles_x(F)) * 16 + (threadIdx.x >> 4);
-        typename M::acc4 a4 = M::a4(0, 0, 0, 0);
-        if (l_inside(F, cx, cy)) {
-            const int i = l_at(F, cx, cy);
-            const float D = d.mgd[i];
-            if (D > 0.0f) {
-                float2 x = d.pres[i];
-                float4 w = d.mga[i];
-                float axx = D * x.x, axy = D * x.y;
-                for (int q = 0; q < 4; q++) {
-                    int nx = cx + NBX[q], ny = cy + NBY[q];
-                    if (unknown_op(d, F, nx, ny)) {
-                        float wd = wcomp(w, q);
-                        float2 pn = d.pres[l_at(F, nx, ny)];
-                        axx -= wd * pn.x;
-                        axy -= wd * pn.y;
-                    }
-                }
-                float4 b = d.prhs[i];
-                const float2 r = make_float2(b.x - axx, b.y - axy);
-                r0[i] = r;
-                if (rr) a4 = M::a4(0, 0, (acc)r.x * (acc)r.x, (acc)r.y * (acc)r.y);
-                else a4 = M::a4((acc)b.x * (acc)b.x, (acc)b.y * (acc)b.y, 0, 0);
-            } else {
-                r0[i] = make_float2(0.0f, 0.0f);
-            }
-        }
-        buf[threadIdx.x] = a4;
-        block_tree(buf);
-        if (threadIdx.x == 0) part[t] = buf[0];
-        __syncthreads();
+    if (d.ptile[F.toff + t] == 0u) {
+        if (threadIdx.x == 0) part[t] = M::a4(0, 0, 0, 0);
+        return;
     }
+    const int cx = (t % tiles_x(F)) * 16 + (threadIdx.x & 15), cy = (t / tiles_x(F)) * 16 + (threadIdx.x >> 4);
+    typename M::acc4 a4 = M::a4(0, 0, 0, 0);
+    if (l_inside(F, cx, cy)) {
+        const int i = l_at(F, cx, cy);
+        const float D = d.mgd[i];
+        if (D > 0.0f) {
+            float2 x = d.pres[i];
+            float4 w = d.mga[i];
+            float axx = D * x.x, axy = D * x.y;
+            for (int q = 0; q < 4; q++) {
+                int nx = cx + NBX[q], ny = cy + NBY[q];
+                if (unknown_op(d, F, nx, ny)) {
+                    float wd = wcomp(w, q);
+                    float2 pn = d.pres[l_at(F, nx, ny)];
+                    axx -= wd * pn.x;
+                    axy -= wd * pn.y;
+                }
+            }
+            float4 b = d.prhs[i];
+            const float2 r = make_float2(b.x - axx, b.y - axy);
+            r0[i] = r;
+            if (rr) a4 = M::a4(0, 0, (acc)r.x * (acc)r.x, (acc)r.y * (acc)r.y);
+            else a4 = M::a4((acc)b.x * (acc)b.x, (acc)b.y * (acc)b.y, 0, 0);
+        } else {
+            r0[i] = make_float2(0.0f, 0.0f);
+        }
+    }
+    buf[threadIdx.x] = a4;
+    block_tree(buf);
+    if (threadIdx.x == 0) part[t] = buf[0];
+    __syncthreads();
+}
+
+// Tiles of level l of one scene.
+DEV int level_tiles(const DevScene& d, int l) {
+    const Lv L = lev(d.lv, l);
+    return tiles_x(L) * tiles_y(L);
 }
 
 // ---- the V-cycle --------------------------------------------------------------------------
@@ -300,68 +298,65 @@ DEV float2 down_black(const DevScene& d, const Lv& L, const Rsrc<M>& R, int nx, 
     return make_float2(sum.x / di, sum.y / di);
 }
 
-// mg_down.comp on level l. On level 0 with `r_out` it also applies cg_update.comp:
-// x += alpha p and the residual update into r_out.
+// mg_down.comp on tile t of level l. On level 0 with `r_out` it also applies
+// cg_update.comp: x += alpha p and the residual update into r_out.
 template <class M>
-DEV void phase_down(const DevScene& d, int l, const Rsrc<M>& R, float2* r_out, const float2* p, float2* sz) {
-    Lv F = lev(d.lv, l), C = lev(d.lv, l + 1);
+DEV void down_tile(const DevScene& d, int l, int t, const Rsrc<M>& R, float2* r_out, const float2* p, float2* sz) {
+    const Lv F = lev(d.lv, l), C = lev(d.lv, l + 1);
     const int tx_n = tiles_x(F);
-    const int T = tx_n * tiles_y(F);
     const int lx = threadIdx.x & 15, ly = threadIdx.x >> 4;
-    for (int t = blockIdx.x; t < T; t += gridDim.x) {
-        if (d.ptile[F.toff + t] == 0u) continue;
-        const int cx = (t % tx_n) * 16 + lx, cy = (t / tx_n) * 16 + ly;
-        const bool red = ((cx + cy) & 1) == 0;
-        float2 z = make_float2(0.0f, 0.0f);
-        if (l_inside(F, cx, cy)) {
-            const int i = l_at(F, cx, cy);
-            const float D = M::Dg(d, i);
-            if (D > 0.0f) {
-                if (red) {
-                    float2 r = R.at(d, i);
-                    z = make_float2(r.x / D, r.y / D);
-                } else {
-                    z = down_black<M>(d, F, R, cx, cy);
-                }
-            }
-            if (r_out && d.mgd[i] > 0.0f) {
-                // cg_update.comp: x += alpha p, r -= alpha q (unknowns of active tiles)
-                float2 pp = p[i];
-                float2 x = d.pres[i];
-                x.x += R.ax * pp.x;
-                x.y += R.ay * pp.y;
-                d.pres[i] = x;
-                r_out[i] = R.at(d, i);
-            }
-            M::setX(d, i, z);
-        }
-        sz[threadIdx.x] = z;
-        __syncthreads();
-        if (((lx | ly) & 1) == 0) {
-            const int Cx = cx >> 1, Cy = cy >> 1;
-            if (Cx < C.w && Cy < C.h) {
-                float sx = 0.0f, sy = 0.0f;
-                for (int k = 0; k < 2; k++) {
-                    int qx = cx + k, qy = cy + k;
-                    if (!unknown<M>(d, F, qx, qy)) continue;
-                    float4 w = M::A(d, l_at(F, qx, qy));
-                    int lqx = lx + k, lqy = ly + k;
-                    for (int q = 0; q < 4; q++) {
-                        int nx = qx + NBX[q], ny = qy + NBY[q];
-                        if (!unknown<M>(d, F, nx, ny)) continue;
-                        int lnx = lqx + NBX[q], lny = lqy + NBY[q];
-                        bool here = lnx >= 0 && lny >= 0 && lnx < 16 && lny < 16;
-                        float2 zb = here ? sz[lny * 16 + lnx] : down_black<M>(d, F, R, nx, ny);
-                        float wd = wcomp(w, q);
-                        sx += wd * zb.x;
-                        sy += wd * zb.y;
-                    }
-                }
-                M::setR(d, l_at(C, Cx, Cy), make_float2(sx, sy));
+    if (d.ptile[F.toff + t] == 0u) return;
+    const int cx = (t % tx_n) * 16 + lx, cy = (t / tx_n) * 16 + ly;
+    const bool red = ((cx + cy) & 1) == 0;
+    float2 z = make_float2(0.0f, 0.0f);
+    if (l_inside(F, cx, cy)) {
+        const int i = l_at(F, cx, cy);
+        const float D = M::Dg(d, i);
+        if (D > 0.0f) {
+            if (red) {
+                float2 r = R.at(d, i);
+                z = make_float2(r.x / D, r.y / D);
+            } else {
+                z = down_black<M>(d, F, R, cx, cy);
             }
         }
-        __syncthreads();
+        if (r_out && d.mgd[i] > 0.0f) {
+            // cg_update.comp: x += alpha p, r -= alpha q (unknowns of active tiles)
+            float2 pp = p[i];
+            float2 x = d.pres[i];
+            x.x += R.ax * pp.x;
+            x.y += R.ay * pp.y;
+            d.pres[i] = x;
+            r_out[i] = R.at(d, i);
+        }
+        M::setX(d, i, z);
     }
+    sz[threadIdx.x] = z;
+    __syncthreads();
+    if (((lx | ly) & 1) == 0) {
+        const int Cx = cx >> 1, Cy = cy >> 1;
+        if (Cx < C.w && Cy < C.h) {
+            float sx = 0.0f, sy = 0.0f;
+            for (int k = 0; k < 2; k++) {
+                int qx = cx + k, qy = cy + k;
+                if (!unknown<M>(d, F, qx, qy)) continue;
+                float4 w = M::A(d, l_at(F, qx, qy));
+                int lqx = lx + k, lqy = ly + k;
+                for (int q = 0; q < 4; q++) {
+                    int nx = qx + NBX[q], ny = qy + NBY[q];
+                    if (!unknown<M>(d, F, nx, ny)) continue;
+                    int lnx = lqx + NBX[q], lny = lqy + NBY[q];
+                    bool here = lnx >= 0 && lny >= 0 && lnx < 16 && lny < 16;
+                    float2 zb = here ? sz[lny * 16 + lnx] : down_black<M>(d, F, R, nx, ny);
+                    float wd = wcomp(w, q);
+                    sx += wd * zb.x;
+                    sy += wd * zb.y;
+                }
+            }
+            M::setR(d, l_at(C, Cx, Cy), make_float2(sx, sy));
+        }
+    }
+    __syncthreads();
 }
 
 // The tail levels' state in each block's shared memory (dynamic, FP32 in both precisions):
@@ -377,11 +372,25 @@ struct Tail {
 
 DEV bool t_unknown(const Tail& tl, const Lv& L, int x, int y) { return l_inside(L, x, y) && tl.dg[L.off - tl.base + y * L.w + x] > 0.0f; }
 
+// The tail of scene d laid out in the dynamic shared memory at smem.
+DEV Tail make_tail(const DevScene& d, unsigned char* smem) {
+    Tail tl;
+    const Lv F = lev(d.lv, d.lv.tail), E = lev(d.lv, d.lv.n - 1);
+    tl.base = F.off;
+    tl.T = E.off + E.w * E.h - F.off;
+    tl.nf = F.w * F.h;
+    tl.a = reinterpret_cast<float4*>(smem);
+    tl.x = reinterpret_cast<float2*>(tl.a + tl.T);
+    tl.r = tl.x + tl.T;
+    tl.dg = reinterpret_cast<float*>(tl.r + tl.T);
+    return tl;
+}
+
 // mg_tail.comp mode 1 in every block's shared memory, once per solve: the first tail
 // level's matrix from global memory, then the Galerkin matrices of the coarser tail levels
 // (the arithmetic of mg_build.comp). Block 0 also stores them for inspection.
 template <class M>
-DEV void tail_setup(const DevScene& d, const Tail& tl) {
+DEV void tail_setup(const DevScene& d, const Tail& tl, bool writer) {
     for (int s = threadIdx.x; s < tl.nf; s += NT) {
         tl.a[s] = M::A(d, tl.base + s);
         tl.dg[s] = M::Dg(d, tl.base + s);
@@ -413,7 +422,7 @@ DEV void tail_setup(const DevScene& d, const Tail& tl) {
             }
             tl.dg[oc + t] = D > 1e-7f ? D : 0.0f;
             tl.a[oc + t] = D > 1e-7f ? A : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-            if (blockIdx.x == 0) M::setA(d, C.off + t, tl.a[oc + t], tl.dg[oc + t]);
+            if (writer) M::setA(d, C.off + t, tl.a[oc + t], tl.dg[oc + t]);
         }
         __syncthreads();
     }
@@ -451,59 +460,58 @@ DEV float2 up_black(const DevScene& d, const Lv& L, const Zc& zc, const Rsrc<M>&
     return make_float2(sum.x / di, sum.y / di);
 }
 
-// mg_up.comp on level l; on level 0 (flag) the partial sums r.z, r.r into part[tile].
+// mg_up.comp on tile t of level l; on level 0 (flag) the tile's sums of r.z, r.r into
+// part[t].
 template <class M>
-DEV void phase_up(const DevScene& d, int l, bool flag, const Rsrc<M>& rhs, const Zc& zc, float2* sz, typename M::acc4* buf) {
+DEV void up_tile(const DevScene& d, int l, int t, bool flag, const Rsrc<M>& rhs, const Zc& zc, float2* sz,
+                 typename M::acc4* buf) {
     using acc = typename M::acc;
-    Lv F = lev(d.lv, l);
+    const Lv F = lev(d.lv, l);
     const int tx_n = tiles_x(F);
-    const int T = tx_n * tiles_y(F);
     const int lx = threadIdx.x & 15, ly = threadIdx.x >> 4;
     typename M::acc4* part = M::part(d);
-    for (int t = blockIdx.x; t < T; t += gridDim.x) {
-        if (d.ptile[F.toff + t] == 0u) {
-            if (flag && threadIdx.x == 0) part[t] = M::a4(0, 0, 0, 0);
-            continue;
-        }
-        const int cx = (t % tx_n) * 16 + lx, cy = (t / tx_n) * 16 + ly;
-        const bool red = ((cx + cy) & 1) == 0;
-        const bool unk = unknown<M>(d, F, cx, cy);
-        float2 z = make_float2(0.0f, 0.0f);
-        if (unk && !red) z = up_black<M>(d, F, zc, rhs, cx, cy);
-        sz[threadIdx.x] = z;
-        __syncthreads();
-        typename M::acc4 a4 = M::a4(0, 0, 0, 0);
-        if (l_inside(F, cx, cy)) {
-            const int i = l_at(F, cx, cy);
-            if (unk) {
-                float2 r = rhs.at(d, i);
-                if (red) {
-                    float4 w = M::A(d, i);
-                    float sx = r.x, sy = r.y;
-                    for (int q = 0; q < 4; q++) {
-                        int nx = cx + NBX[q], ny = cy + NBY[q];
-                        if (!unknown<M>(d, F, nx, ny)) continue;
-                        int lnx = lx + NBX[q], lny = ly + NBY[q];
-                        bool here = lnx >= 0 && lny >= 0 && lnx < 16 && lny < 16;
-                        float2 zb = here ? sz[lny * 16 + lnx] : up_black<M>(d, F, zc, rhs, nx, ny);
-                        float wd = wcomp(w, q);
-                        sx += wd * zb.x;
-                        sy += wd * zb.y;
-                    }
-                    float di = M::Dg(d, i);
-                    z = make_float2(sx / di, sy / di);
-                }
-                a4 = M::a4((acc)r.x * (acc)z.x, (acc)r.y * (acc)z.y, (acc)r.x * (acc)r.x, (acc)r.y * (acc)r.y);
-            }
-            M::setZ(d, i, z);
-        }
-        if (flag) {
-            buf[threadIdx.x] = a4;
-            block_tree(buf);
-            if (threadIdx.x == 0) part[t] = buf[0];
-        }
-        __syncthreads();
+    if (d.ptile[F.toff + t] == 0u) {
+        if (flag && threadIdx.x == 0) part[t] = M::a4(0, 0, 0, 0);
+        return;
     }
+    const int cx = (t % tx_n) * 16 + lx, cy = (t / tx_n) * 16 + ly;
+    const bool red = ((cx + cy) & 1) == 0;
+    const bool unk = unknown<M>(d, F, cx, cy);
+    float2 z = make_float2(0.0f, 0.0f);
+    if (unk && !red) z = up_black<M>(d, F, zc, rhs, cx, cy);
+    sz[threadIdx.x] = z;
+    __syncthreads();
+    typename M::acc4 a4 = M::a4(0, 0, 0, 0);
+    if (l_inside(F, cx, cy)) {
+        const int i = l_at(F, cx, cy);
+        if (unk) {
+            float2 r = rhs.at(d, i);
+            if (red) {
+                float4 w = M::A(d, i);
+                float sx = r.x, sy = r.y;
+                for (int q = 0; q < 4; q++) {
+                    int nx = cx + NBX[q], ny = cy + NBY[q];
+                    if (!unknown<M>(d, F, nx, ny)) continue;
+                    int lnx = lx + NBX[q], lny = ly + NBY[q];
+                    bool here = lnx >= 0 && lny >= 0 && lnx < 16 && lny < 16;
+                    float2 zb = here ? sz[lny * 16 + lnx] : up_black<M>(d, F, zc, rhs, nx, ny);
+                    float wd = wcomp(w, q);
+                    sx += wd * zb.x;
+                    sy += wd * zb.y;
+                }
+                float di = M::Dg(d, i);
+                z = make_float2(sx / di, sy / di);
+            }
+            a4 = M::a4((acc)r.x * (acc)z.x, (acc)r.y * (acc)z.y, (acc)r.x * (acc)r.x, (acc)r.y * (acc)r.y);
+        }
+        M::setZ(d, i, z);
+    }
+    if (flag) {
+        buf[threadIdx.x] = a4;
+        block_tree(buf);
+        if (threadIdx.x == 0) part[t] = buf[0];
+    }
+    __syncthreads();
 }
 
 // mg_tail.comp mode 0, computed by EVERY block in its own shared memory: the V-cycle on the
@@ -511,7 +519,7 @@ DEV void phase_up(const DevScene& d, int l, bool flag, const Rsrc<M>& rhs, const
 // tail level's slots). Every block gets the same values; the way up of the level above
 // reads them from its own copy, so no grid barrier follows the tail.
 template <class M>
-DEV void phase_tail(const DevScene& d, const Tail& tl) {
+DEV void phase_tail(const DevScene& d, const Tail& tl, bool writer) {
     const int first = d.lv.tail, last = d.lv.n - 1;
     for (int s = threadIdx.x; s < tl.nf; s += NT) tl.r[s] = M::R(d, tl.base + s);
     __syncthreads();
@@ -605,12 +613,13 @@ DEV void phase_tail(const DevScene& d, const Tail& tl) {
         __syncthreads();
         sweep(F, 0, false);
     }
-    if (blockIdx.x == 0)   // the first tail level's result, for inspection
+    if (writer)   // the first tail level's result (for inspection; a batch's way up reads it)
         for (int s = threadIdx.x; s < tl.nf; s += NT) M::setZ(d, tl.base + s, tl.x[s]);
 }
 
-// One V-cycle: level 0's right-hand side through R (fused with the CG update when R.q is
-// set), result in mgz of level 0, partials of r.z and r.r. Returns false on a barrier timeout.
+// One V-cycle of one scene: level 0's right-hand side through R (fused with the CG update
+// when R.q is set), result in mgz of level 0, partials of r.z and r.r. Returns false on a
+// barrier timeout.
 template <class M>
 DEV bool vcycle(const DevScene& d, const Tail& tl, const Rsrc<M>& R, float2* r_out, const float2* p, const float2* r_new,
                 float2* sz, typename M::acc4* buf) {
@@ -618,63 +627,62 @@ DEV bool vcycle(const DevScene& d, const Tail& tl, const Rsrc<M>& R, float2* r_o
     for (int l = 0; l < tail; l++) {
         Rsrc<M> Rl = R;
         if (l > 0) Rl = Rsrc<M>{nullptr, nullptr, 0.0f, 0.0f};
-        phase_down<M>(d, l, Rl, l == 0 ? r_out : nullptr, p, sz);
+        const int T = level_tiles(d, l);
+        for (int t = blockIdx.x; t < T; t += gridDim.x) down_tile<M>(d, l, t, Rl, l == 0 ? r_out : nullptr, p, sz);
         if (!grid_sync(d.K)) return false;
     }
-    phase_tail<M>(d, tl);
+    phase_tail<M>(d, tl, blockIdx.x == 0);
     for (int l = tail - 1; l >= 0; l--) {
         const Lv C = lev(d.lv, l + 1);
         const Zc zc{(l == tail - 1) ? tl.x : nullptr, C.off, C.w};
         const Rsrc<M> rhs = l == 0 ? Rsrc<M>{r_new, nullptr, 0.0f, 0.0f} : Rsrc<M>{nullptr, nullptr, 0.0f, 0.0f};
-        phase_up<M>(d, l, l == 0, rhs, zc, sz, buf);
+        const int T = level_tiles(d, l);
+        for (int t = blockIdx.x; t < T; t += gridDim.x) up_tile<M>(d, l, t, l == 0, rhs, zc, sz, buf);
         if (!grid_sync(d.K)) return false;
     }
     return true;
 }
 
-// The mixed solve's closing check: the true residual b - A x of the final iterate with FP64
-// arithmetic (the products and sums of the FP32 values in double), per tile the sums of
-// |b - A x|^2 and |b|^2 of the pressure potential into part[tile].
-DEV void phase_true_residual(const DevScene& d, Dbl4* part, Dbl4* buf) {
-    Lv F = lev(d.lv, 0);
+// The mixed solve's closing check on level-0 tile t: the true residual b - A x of the final
+// iterate with FP64 arithmetic (the products and sums of the FP32 values in double), the
+// tile's sums of |b - A x|^2 and |b|^2 of the pressure potential into part[t].
+DEV void true_residual_tile(const DevScene& d, int t, Dbl4* part, Dbl4* buf) {
+    const Lv F = lev(d.lv, 0);
     const int tx_n = tiles_x(F);
-    const int T = tx_n * tiles_y(F);
-    for (int t = blockIdx.x; t < T; t += gridDim.x) {
-        if (d.ptile[F.toff + t] == 0u) {
-            if (threadIdx.x == 0) part[t] = Dbl4{0.0, 0.0, 0.0, 0.0};
-            continue;
-        }
-        const int cx = (t % tx_n) * 16 + (threadIdx.x & 15), cy = (t / tx_n) * 16 + (threadIdx.x >> 4);
-        Dbl4 a4{0.0, 0.0, 0.0, 0.0};
-        if (l_inside(F, cx, cy)) {
-            const int i = l_at(F, cx, cy);
-            const float D = d.mgd[i];
-            if (D > 0.0f) {
-                const float4 w = d.mga[i];
-                double r = (double)d.prhs[i].x - (double)D * (double)d.pres[i].x;
-                for (int q = 0; q < 4; q++) {
-                    int nx = cx + NBX[q], ny = cy + NBY[q];
-                    if (unknown_op(d, F, nx, ny)) r += (double)wcomp(w, q) * (double)d.pres[l_at(F, nx, ny)].x;
-                }
-                const double b = (double)d.prhs[i].x;
-                a4 = Dbl4{r * r, b * b, 0.0, 0.0};
-            }
-        }
-        buf[threadIdx.x] = a4;
-        block_tree(buf);
-        if (threadIdx.x == 0) part[t] = buf[0];
-        __syncthreads();
+    if (d.ptile[F.toff + t] == 0u) {
+        if (threadIdx.x == 0) part[t] = Dbl4{0.0, 0.0, 0.0, 0.0};
+        return;
     }
+    const int cx = (t % tx_n) * 16 + (threadIdx.x & 15), cy = (t / tx_n) * 16 + (threadIdx.x >> 4);
+    Dbl4 a4{0.0, 0.0, 0.0, 0.0};
+    if (l_inside(F, cx, cy)) {
+        const int i = l_at(F, cx, cy);
+        const float D = d.mgd[i];
+        if (D > 0.0f) {
+            const float4 w = d.mga[i];
+            double r = (double)d.prhs[i].x - (double)D * (double)d.pres[i].x;
+            for (int q = 0; q < 4; q++) {
+                int nx = cx + NBX[q], ny = cy + NBY[q];
+                if (unknown_op(d, F, nx, ny)) r += (double)wcomp(w, q) * (double)d.pres[l_at(F, nx, ny)].x;
+            }
+            const double b = (double)d.prhs[i].x;
+            a4 = Dbl4{r * r, b * b, 0.0, 0.0};
+        }
+    }
+    buf[threadIdx.x] = a4;
+    block_tree(buf);
+    if (threadIdx.x == 0) part[t] = buf[0];
+    __syncthreads();
 }
 
-// cg_apply.comp: p = z + beta p_old, q = A p (the FP32 operator), partial sums of p.q into
-// part[n + tile].
+// cg_apply.comp on level-0 tile t: p = z + beta p_old, q = A p (the FP32 operator), the
+// tile's sum of p.q into part[n + t].
 template <class M>
-DEV void phase_apply(const DevScene& d, float b0, float b1, const float2* p_old, float2* p_new, typename M::acc4* buf) {
+DEV void apply_tile(const DevScene& d, int t, float b0, float b1, const float2* p_old, float2* p_new,
+                    typename M::acc4* buf) {
     using acc = typename M::acc;
-    Lv F = lev(d.lv, 0);
+    const Lv F = lev(d.lv, 0);
     const int tx_n = tiles_x(F);
-    const int T = tx_n * tiles_y(F);
     const int n = d.nwg;
     typename M::acc4* part = M::part(d) + n;
     const bool nob = b0 == 0.0f && b1 == 0.0f;
@@ -684,47 +692,125 @@ DEV void phase_apply(const DevScene& d, float b0, float b1, const float2* p_old,
         float2 po = p_old[i];
         return make_float2(b0 != 0.0f ? z.x + b0 * po.x : z.x, b1 != 0.0f ? z.y + b1 * po.y : z.y);
     };
-    for (int t = blockIdx.x; t < T; t += gridDim.x) {
-        if (d.ptile[F.toff + t] == 0u) {
-            if (threadIdx.x == 0) part[t] = M::a4(0, 0, 0, 0);
-            continue;
-        }
-        const int cx = (t % tx_n) * 16 + (threadIdx.x & 15), cy = (t / tx_n) * 16 + (threadIdx.x >> 4);
-        typename M::acc4 a4 = M::a4(0, 0, 0, 0);
-        if (l_inside(F, cx, cy)) {
-            const int i = l_at(F, cx, cy);
-            const float D = d.mgd[i];
-            if (D > 0.0f) {
-                float2 pp = direction(i);
-                float4 w = d.mga[i];
-                float qx = D * pp.x, qy = D * pp.y;
-                for (int q = 0; q < 4; q++) {
-                    int nx = cx + NBX[q], ny = cy + NBY[q];
-                    if (unknown_op(d, F, nx, ny)) {
-                        float2 pn = direction(l_at(F, nx, ny));
-                        float wd = wcomp(w, q);
-                        qx -= wd * pn.x;
-                        qy -= wd * pn.y;
-                    }
-                }
-                p_new[i] = pp;
-                d.cgq[i] = make_float2(qx, qy);
-                a4 = M::a4(0, 0, (acc)pp.x * (acc)qx, (acc)pp.y * (acc)qy);
-            } else {
-                p_new[i] = make_float2(0.0f, 0.0f);
-            }
-        }
-        buf[threadIdx.x] = a4;
-        block_tree(buf);
-        if (threadIdx.x == 0) part[t] = buf[0];
-        __syncthreads();
+    if (d.ptile[F.toff + t] == 0u) {
+        if (threadIdx.x == 0) part[t] = M::a4(0, 0, 0, 0);
+        return;
     }
+    const int cx = (t % tx_n) * 16 + (threadIdx.x & 15), cy = (t / tx_n) * 16 + (threadIdx.x >> 4);
+    typename M::acc4 a4 = M::a4(0, 0, 0, 0);
+    if (l_inside(F, cx, cy)) {
+        const int i = l_at(F, cx, cy);
+        const float D = d.mgd[i];
+        if (D > 0.0f) {
+            float2 pp = direction(i);
+            float4 w = d.mga[i];
+            float qx = D * pp.x, qy = D * pp.y;
+            for (int q = 0; q < 4; q++) {
+                int nx = cx + NBX[q], ny = cy + NBY[q];
+                if (unknown_op(d, F, nx, ny)) {
+                    float2 pn = direction(l_at(F, nx, ny));
+                    float wd = wcomp(w, q);
+                    qx -= wd * pn.x;
+                    qy -= wd * pn.y;
+                }
+            }
+            p_new[i] = pp;
+            d.cgq[i] = make_float2(qx, qy);
+            a4 = M::a4(0, 0, (acc)pp.x * (acc)qx, (acc)pp.y * (acc)qy);
+        } else {
+            p_new[i] = make_float2(0.0f, 0.0f);
+        }
+    }
+    buf[threadIdx.x] = a4;
+    block_tree(buf);
+    if (threadIdx.x == 0) part[t] = buf[0];
+    __syncthreads();
 }
 
 template <class T>
 DEV T mix_was(T a, T keep, uint32_t was) { return mixf(a, keep, (float)was); }
 template <>
 DEV double mix_was<double>(double a, double keep, uint32_t was) { return was ? keep : a; }
+
+// The solve's scalar steps (reduce_tail.glsl:61-116), shared by the single-scene and batched
+// kernels so that a scene's numbers do not depend on which one solved it.
+// mode 0 / 8: the start, from the totals a = (r.z, r.r) and b = (b.b).
+template <class T, class A4>
+DEV void scal_start(Solve<T>& K, const A4& a, const A4& b, T tx, T ty, int second) {
+    K.bb[0] = b.x;
+    K.bb[1] = b.y;
+    K.rz[0] = a.x;
+    K.rz[1] = a.y;
+    K.rr[0] = a.z;
+    K.rr[1] = a.w;
+    K.beta[0] = K.beta[1] = 0;
+    K.alpha[0] = K.alpha[1] = 0;
+    K.iters[0] = K.iters[1] = 0u;
+    K.done[0] = a.z <= tx * tx * b.x ? 1u : 0u;
+    K.done[1] = a.w <= ty * ty * b.y ? 1u : 0u;
+    if (second) K.done[1] = 1u;
+}
+
+// mode 1: the step lengths from p.q.
+template <class T, class A4>
+DEV void scal_alpha(Solve<T>& K, const A4& b) {
+    T ax = 0, ay = 0;
+    if (K.done[0] == 0u && b.z > 0) ax = K.rz[0] / b.z;
+    if (K.done[1] == 0u && b.w > 0) ay = K.rz[1] / b.w;
+    K.alpha[0] = ax;
+    K.alpha[1] = ay;
+}
+
+// mode 2: convergence and the next direction's beta from the new (r.z, r.r).
+template <class T, class A4>
+DEV void scal_beta(Solve<T>& K, const A4& a, T tx, T ty) {
+    uint32_t was0 = K.done[0], was1 = K.done[1];
+    K.iters[0] += 1u - was0;
+    K.iters[1] += 1u - was1;
+    uint32_t now0 = a.z <= tx * tx * K.bb[0] ? 1u : 0u, now1 = a.w <= ty * ty * K.bb[1] ? 1u : 0u;
+    uint32_t d0 = was0 > now0 ? was0 : now0, d1 = was1 > now1 ? was1 : now1;
+    T bx = 0, by = 0;
+    if (d0 == 0u && K.rz[0] > 0) bx = a.x / K.rz[0];
+    if (d1 == 0u && K.rz[1] > 0) by = a.y / K.rz[1];
+    K.beta[0] = bx;
+    K.beta[1] = by;
+    K.rz[0] = a.x;
+    K.rz[1] = a.y;
+    K.rr[0] = mix_was<T>(a.z, K.rr[0], was0);
+    K.rr[1] = mix_was<T>(a.w, K.rr[1], was1);
+    K.done[0] = d0;
+    K.done[1] = d1;
+}
+
+// mode 3 / 9: the statistics of the finished solve into the scene's SolveState.
+template <class M, class T>
+DEV void scal_stats(SolveState* G, const Solve<T>& K, int second, double true_rel) {
+    if (true_rel >= 0.0) {
+        G->p_true_res = (float)true_rel;
+        G->p_true_res_max = maxf(G->p_true_res_max, (float)true_rel);
+    }
+    for (int c = 0; c < 2; c++) {
+        G->p_rz[c] = (float)K.rz[c];
+        G->p_alpha[c] = (float)K.alpha[c];
+        G->p_beta[c] = (float)K.beta[c];
+        G->p_bb[c] = (float)K.bb[c];
+        G->p_rr[c] = (float)K.rr[c];
+        G->p_done[c] = K.done[c];
+        if (!second) G->p_iters[c] = K.iters[c];
+    }
+    if (second) G->p2_iters = K.iters[0];
+    G->solves += 1u;
+    if (!second) {
+        uint32_t m = K.iters[0] > K.iters[1] ? K.iters[0] : K.iters[1];
+        if (m > G->p_it_max) G->p_it_max = m;
+        if (K.done[0] == 0u) G->p_unconv += 1u;
+    } else {
+        if (K.iters[0] > G->p2_it_max) G->p2_it_max = K.iters[0];
+        if (K.done[0] == 0u) G->p2_unconv += 1u;
+    }
+    const float rel = K.bb[0] > 0 ? (float)sqrt((double)K.rr[0] / (double)K.bb[0]) : 0.0f;
+    G->p_res_max = maxf(G->p_res_max, M::kMixed ? rel : (K.bb[0] > 0 ? sqrtf((float)K.rr[0] / (float)K.bb[0]) : 0.0f));
+}
 
 }  // namespace
 
@@ -741,29 +827,20 @@ __global__ void __launch_bounds__(NT) k_mgpcg(DevScene d, int second, int scale_
     const DevParams* P = d.P;
     const int n = d.nwg;
     acc4* part = M::part(d);
-    Tail tl;
-    {
-        const Lv F = lev(d.lv, d.lv.tail), E = lev(d.lv, d.lv.n - 1);
-        tl.base = F.off;
-        tl.T = E.off + E.w * E.h - F.off;
-        tl.nf = F.w * F.h;
-        tl.a = reinterpret_cast<float4*>(tail_smem);
-        tl.x = reinterpret_cast<float2*>(tl.a + tl.T);
-        tl.r = tl.x + tl.T;
-        tl.dg = reinterpret_cast<float*>(tl.r + tl.T);
-    }
+    const Tail tl = make_tail(d, tail_smem);
     if (!second) {
-        phase_cg_scale<M>(d, scale_mode);
+        for (int t = blockIdx.x; t < n; t += gridDim.x) cg_scale_tile<M>(d, t, scale_mode);
         for (int l = 1; l <= d.lv.tail; l++) {
             if (!grid_sync(d.K)) return;
-            phase_mg_build<M>(d, l - 1);
+            const int T = level_tiles(d, l);
+            for (int t = blockIdx.x; t < T; t += gridDim.x) mg_build_tile<M>(d, l - 1, t);
         }
         if (!grid_sync(d.K)) return;
     }
-    tail_setup<M>(d, tl);
+    tail_setup<M>(d, tl, blockIdx.x == 0);
     float2* r_cur = d.mgr;    // level 0 of mgr: the residual, double-buffered with mgr2
     float2* r_nxt = d.mgr2;
-    phase_residual<M>(d, r_cur, buf, false);
+    for (int t = blockIdx.x; t < n; t += gridDim.x) residual_tile<M>(d, t, r_cur, buf, false);
     if (!grid_sync(d.K)) return;
     // b.b now, while nothing writes the second half of the partials: the first apply phase
     // after the V-cycle does, and a block can reach it before a slower one has summed them
@@ -772,61 +849,26 @@ __global__ void __launch_bounds__(NT) k_mgpcg(DevScene d, int second, int scale_
     const acc tx = (acc)P->tol[0], ty = (acc)P->tol[1];
     {
         acc4 a = total(part, n, buf);
-        if (threadIdx.x == 0) {
-            K.bb[0] = b.x;
-            K.bb[1] = b.y;
-            K.rz[0] = a.x;
-            K.rz[1] = a.y;
-            K.rr[0] = a.z;
-            K.rr[1] = a.w;
-            K.beta[0] = K.beta[1] = 0;
-            K.alpha[0] = K.alpha[1] = 0;
-            K.iters[0] = K.iters[1] = 0u;
-            K.done[0] = a.z <= tx * tx * b.x ? 1u : 0u;
-            K.done[1] = a.w <= ty * ty * b.y ? 1u : 0u;
-            if (second) K.done[1] = 1u;
-        }
+        if (threadIdx.x == 0) scal_start<acc>(K, a, b, tx, ty, second);
         __syncthreads();
     }
     float2* p_old = d.cgp;
     float2* p_new = d.cgp2;
     for (uint32_t it = 0; it < P->pressure_max_iters; it++) {
         if (K.done[0] && K.done[1]) break;
-        phase_apply<M>(d, (float)K.beta[0], (float)K.beta[1], p_old, p_new, buf);
+        for (int t = blockIdx.x; t < n; t += gridDim.x)
+            apply_tile<M>(d, t, (float)K.beta[0], (float)K.beta[1], p_old, p_new, buf);
         if (!grid_sync(d.K)) return;
         {
             acc4 b = total(part + n, n, buf);
-            if (threadIdx.x == 0) {
-                acc ax = 0, ay = 0;
-                if (K.done[0] == 0u && b.z > 0) ax = K.rz[0] / b.z;
-                if (K.done[1] == 0u && b.w > 0) ay = K.rz[1] / b.w;
-                K.alpha[0] = ax;
-                K.alpha[1] = ay;
-            }
+            if (threadIdx.x == 0) scal_alpha<acc>(K, b);
             __syncthreads();
         }
         Rsrc<M> R{r_cur, d.cgq, (float)K.alpha[0], (float)K.alpha[1]};
         if (!vcycle<M>(d, tl, R, r_nxt, p_new, r_nxt, sz, buf)) return;
         {
             acc4 a = total(part, n, buf);
-            if (threadIdx.x == 0) {
-                uint32_t was0 = K.done[0], was1 = K.done[1];
-                K.iters[0] += 1u - was0;
-                K.iters[1] += 1u - was1;
-                uint32_t now0 = a.z <= tx * tx * K.bb[0] ? 1u : 0u, now1 = a.w <= ty * ty * K.bb[1] ? 1u : 0u;
-                uint32_t d0 = was0 > now0 ? was0 : now0, d1 = was1 > now1 ? was1 : now1;
-                acc bx = 0, by = 0;
-                if (d0 == 0u && K.rz[0] > 0) bx = a.x / K.rz[0];
-                if (d1 == 0u && K.rz[1] > 0) by = a.y / K.rz[1];
-                K.beta[0] = bx;
-                K.beta[1] = by;
-                K.rz[0] = a.x;
-                K.rz[1] = a.y;
-                K.rr[0] = mix_was<acc>(a.z, K.rr[0], was0);
-                K.rr[1] = mix_was<acc>(a.w, K.rr[1], was1);
-                K.done[0] = d0;
-                K.done[1] = d1;
-            }
+            if (threadIdx.x == 0) scal_beta<acc>(K, a, tx, ty);
             __syncthreads();
         }
         float2* t = p_old;
@@ -838,38 +880,190 @@ __global__ void __launch_bounds__(NT) k_mgpcg(DevScene d, int second, int scale_
     }
     double true_rel = -1.0;
     if constexpr (M::kMixed) {
-        phase_true_residual(d, d.partials64, reinterpret_cast<Dbl4*>(buf));
+        for (int t = blockIdx.x; t < n; t += gridDim.x) true_residual_tile(d, t, d.partials64, reinterpret_cast<Dbl4*>(buf));
         if (!grid_sync(d.K)) return;
         const Dbl4 t4 = total(d.partials64, n, reinterpret_cast<Dbl4*>(buf));
         true_rel = t4.y > 0.0 ? sqrt(t4.x / t4.y) : 0.0;
     }
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        SolveState* G = d.K;
-        if (true_rel >= 0.0) {
-            G->p_true_res = (float)true_rel;
-            G->p_true_res_max = maxf(G->p_true_res_max, (float)true_rel);
+    if (blockIdx.x == 0 && threadIdx.x == 0) scal_stats<M, acc>(d.K, K, second, true_rel);
+}
+
+// ---- many scenes in one persistent solve --------------------------------------------------
+//
+// The same solve for a batch of scenes of any sizes in one cooperative launch: every phase
+// runs over a flattened list of (scene, tile) work items of its level, so the small levels
+// of many scenes fill one pass instead of leaving most blocks idle, and one set of grid
+// barriers serves them all. Each scene's tiles go through the same tile bodies as above and
+// its scalars through the same steps, summed by one block over its own partials in the
+// same order; so a scene's result is the same alone and in any batch, to the bit. The
+// differences: a scene's tail is computed by one block into global memory (one more
+// barrier per V-cycle), each reduction is a phase of its own followed by a barrier (the
+// scalars then live in global memory), and a converged scene (or one at its iteration
+// limit) simply drops out of the work lists.
+
+namespace {
+
+// The scene, tile and level of work item g of level l: o holds the ns + 1 prefix sums of
+// the scenes' tile counts of level l.
+DEV int scene_of(const int* o, int ns, int g) {
+    int lo = 0, hi = ns;
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (o[mid] <= g) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+template <class F>
+DEV void for_tiles(const BatchView& B, int l, F&& f) {
+    const int* o = B.off + l * (B.ns + 1);
+    const int N = o[B.ns];
+    for (int g = blockIdx.x; g < N; g += gridDim.x) {
+        const int s = scene_of(o, B.ns, g);
+        f(s, B.scenes[s], g - o[s]);
+    }
+}
+
+DEV float2* parity_r(const DevScene& d, int it) { return (it & 1) ? d.mgr2 : d.mgr; }
+DEV float2* parity_p(const DevScene& d, int it) { return (it & 1) ? d.cgp2 : d.cgp; }
+
+}  // namespace
+
+template <class M>
+__global__ void __launch_bounds__(NT) k_mgpcg_batch(BatchView B, int second) {
+    using acc = typename M::acc;
+    using acc4 = typename M::acc4;
+    __shared__ float2 sz[NT];
+    __shared__ acc4 buf[NT];
+    __shared__ int s_run;
+    extern __shared__ __align__(16) unsigned char tail_smem[];
+    Solve<acc>* KS = reinterpret_cast<Solve<acc>*>(B.scal);
+    SolveState* BK = B.K;
+    auto tol = [&](const DevScene& d, int c) { return (acc)d.P->tol[c]; };
+    // a scene takes part in iteration it while neither converged nor at its limit
+    auto running = [&](int s, int it) {
+        const Solve<acc>& K = KS[s];
+        return !(K.done[0] && K.done[1]) && (uint32_t)it < B.scenes[s].P->pressure_max_iters;
+    };
+    if (!second) {
+        for_tiles(B, 0, [&](int s, const DevScene& d, int t) { cg_scale_tile<M>(d, t, B.scale[s]); });
+        for (int l = 1; l <= B.max_tail; l++) {
+            if (!grid_sync(BK)) return;
+            for_tiles(B, l, [&](int s, const DevScene& d, int t) { mg_build_tile<M>(d, l - 1, t); });
         }
-        for (int c = 0; c < 2; c++) {
-            G->p_rz[c] = (float)K.rz[c];
-            G->p_alpha[c] = (float)K.alpha[c];
-            G->p_beta[c] = (float)K.beta[c];
-            G->p_bb[c] = (float)K.bb[c];
-            G->p_rr[c] = (float)K.rr[c];
-            G->p_done[c] = K.done[c];
-            if (!second) G->p_iters[c] = K.iters[c];
+        if (!grid_sync(BK)) return;
+    }
+    for_tiles(B, 0, [&](int s, const DevScene& d, int t) { residual_tile<M>(d, t, d.mgr, buf, false); });
+    if (!grid_sync(BK)) return;
+    // b.b of each scene (before the first apply phase reuses those partials)
+    for (int s = blockIdx.x; s < B.ns; s += gridDim.x) {
+        const DevScene& d = B.scenes[s];
+        const acc4 b = total(M::part(d) + d.nwg, d.nwg, buf);
+        if (threadIdx.x == 0) {
+            KS[s].bb[0] = b.x;
+            KS[s].bb[1] = b.y;
+            KS[s].done[0] = KS[s].done[1] = 0u;
         }
-        if (second) G->p2_iters = K.iters[0];
-        G->solves += 1u;
-        if (!second) {
-            uint32_t m = K.iters[0] > K.iters[1] ? K.iters[0] : K.iters[1];
-            if (m > G->p_it_max) G->p_it_max = m;
-            if (K.done[0] == 0u) G->p_unconv += 1u;
-        } else {
-            if (K.iters[0] > G->p2_it_max) G->p2_it_max = K.iters[0];
-            if (K.done[0] == 0u) G->p2_unconv += 1u;
+        __syncthreads();
+    }
+    // One V-cycle on every running scene; it < 0: the start (right-hand side the residual
+    // of x0, no update); else the iteration's, fused with its update.
+    auto vcycle_all = [&](int it) -> bool {
+        const bool fused = it >= 0;
+        const int ir = fused ? it : 0;
+        for (int l = 0; l < B.max_tail; l++) {
+            for_tiles(B, l, [&](int s, const DevScene& d, int t) {
+                if (l >= d.lv.tail || (fused && !running(s, it))) return;
+                const Solve<acc>& K = KS[s];
+                Rsrc<M> R{nullptr, nullptr, 0.0f, 0.0f};
+                if (l == 0) R = fused ? Rsrc<M>{parity_r(d, ir), d.cgq, (float)K.alpha[0], (float)K.alpha[1]}
+                                      : Rsrc<M>{parity_r(d, ir), nullptr, 0.0f, 0.0f};
+                down_tile<M>(d, l, t, R, (l == 0 && fused) ? parity_r(d, ir + 1) : nullptr, parity_p(d, ir + 1), sz);
+            });
+            if (!grid_sync(BK)) return false;
         }
-        const float rel = K.bb[0] > 0 ? (float)sqrt((double)K.rr[0] / (double)K.bb[0]) : 0.0f;
-        G->p_res_max = maxf(G->p_res_max, M::kMixed ? rel : (K.bb[0] > 0 ? sqrtf((float)K.rr[0] / (float)K.bb[0]) : 0.0f));
+        for (int s = blockIdx.x; s < B.ns; s += gridDim.x) {
+            if (fused && !running(s, it)) continue;
+            const DevScene& d = B.scenes[s];
+            const Tail tl = make_tail(d, tail_smem);
+            tail_setup<M>(d, tl, false);
+            phase_tail<M>(d, tl, true);
+        }
+        if (!grid_sync(BK)) return false;
+        for (int l = B.max_tail - 1; l >= 0; l--) {
+            for_tiles(B, l, [&](int s, const DevScene& d, int t) {
+                if (l >= d.lv.tail || (fused && !running(s, it))) return;
+                const Lv C = lev(d.lv, l + 1);
+                const Zc zc{nullptr, C.off, C.w};
+                const Rsrc<M> rhs = l == 0 ? Rsrc<M>{parity_r(d, fused ? ir + 1 : 0), nullptr, 0.0f, 0.0f}
+                                           : Rsrc<M>{nullptr, nullptr, 0.0f, 0.0f};
+                up_tile<M>(d, l, t, l == 0, rhs, zc, sz, buf);
+            });
+            if (!grid_sync(BK)) return false;
+        }
+        return true;
+    };
+    if (!vcycle_all(-1)) return;
+    for (int s = blockIdx.x; s < B.ns; s += gridDim.x) {
+        const DevScene& d = B.scenes[s];
+        const acc4 a = total(M::part(d), d.nwg, buf);
+        if (threadIdx.x == 0) {
+            acc4 b = a;
+            b.x = KS[s].bb[0];
+            b.y = KS[s].bb[1];
+            scal_start<acc>(KS[s], a, b, tol(d, 0), tol(d, 1), second);
+        }
+        __syncthreads();
+    }
+    if (!grid_sync(BK)) return;
+    for (int it = 0;; it++) {
+        if (threadIdx.x == 0) {
+            int run = 0;
+            for (int s = 0; s < B.ns && !run; s++) run = running(s, it) ? 1 : 0;
+            s_run = run;
+        }
+        __syncthreads();
+        if (!s_run) break;
+        for_tiles(B, 0, [&](int s, const DevScene& d, int t) {
+            if (!running(s, it)) return;
+            const Solve<acc>& K = KS[s];
+            apply_tile<M>(d, t, (float)K.beta[0], (float)K.beta[1], parity_p(d, it), parity_p(d, it + 1), buf);
+        });
+        if (!grid_sync(BK)) return;
+        for (int s = blockIdx.x; s < B.ns; s += gridDim.x) {
+            if (!running(s, it)) continue;
+            const DevScene& d = B.scenes[s];
+            const acc4 b = total(M::part(d) + d.nwg, d.nwg, buf);
+            if (threadIdx.x == 0) scal_alpha<acc>(KS[s], b);
+            __syncthreads();
+        }
+        if (!grid_sync(BK)) return;
+        if (!vcycle_all(it)) return;
+        for (int s = blockIdx.x; s < B.ns; s += gridDim.x) {
+            if (!running(s, it)) continue;
+            const DevScene& d = B.scenes[s];
+            const acc4 a = total(M::part(d), d.nwg, buf);
+            if (threadIdx.x == 0) scal_beta<acc>(KS[s], a, tol(d, 0), tol(d, 1));
+            __syncthreads();
+        }
+        if (!grid_sync(BK)) return;
+    }
+    if constexpr (M::kMixed) {
+        for_tiles(B, 0, [&](int s, const DevScene& d, int t) {
+            true_residual_tile(d, t, d.partials64, reinterpret_cast<Dbl4*>(buf));
+        });
+        if (!grid_sync(BK)) return;
+    }
+    for (int s = blockIdx.x; s < B.ns; s += gridDim.x) {
+        const DevScene& d = B.scenes[s];
+        double true_rel = -1.0;
+        if constexpr (M::kMixed) {
+            const Dbl4 t4 = total(d.partials64, d.nwg, reinterpret_cast<Dbl4*>(buf));
+            true_rel = t4.y > 0.0 ? sqrt(t4.x / t4.y) : 0.0;
+        }
+        if (threadIdx.x == 0) scal_stats<M, acc>(d.K, KS[s], second, true_rel);
+        __syncthreads();
     }
 }
 
@@ -897,6 +1091,34 @@ int blocks_max(int device, size_t smem) {
 
 int pressure_blocks_max(int device, size_t smem, bool mixed) {
     return mixed ? blocks_max<Mixed>(device, smem) : blocks_max<Plain>(device, smem);
+}
+
+namespace {
+template <class M>
+int batch_blocks_max(int device, size_t smem) {
+    int sms = 0, per = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    static size_t opted = 0;
+    if (smem > opted) {
+        cudaFuncSetAttribute(k_mgpcg_batch<M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        opted = smem;
+    }
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_mgpcg_batch<M>, NT, smem);
+    return sms * per;
+}
+}  // namespace
+
+int pressure_batch_blocks_max(int device, size_t smem, bool mixed) {
+    return mixed ? batch_blocks_max<Mixed>(device, smem) : batch_blocks_max<Plain>(device, smem);
+}
+
+size_t pressure_batch_scalar_bytes() { return sizeof(Solve<double>); }
+
+cudaError_t launch_pressure_batch(const BatchView& B, bool mixed, int blocks, size_t smem, cudaStream_t st, int second) {
+    cudaMemsetAsync(&B.K->bar_count, 0, sizeof(uint32_t), st);
+    void* args[] = {(void*)&B, &second};
+    const void* fn = mixed ? (const void*)k_mgpcg_batch<Mixed> : (const void*)k_mgpcg_batch<Plain>;
+    return cudaLaunchCooperativeKernel(fn, dim3(blocks), dim3(NT), args, smem, st);
 }
 
 cudaError_t launch_pressure(const DevScene& d, const LaunchCfg& cfg, cudaStream_t st, int second) {

@@ -429,7 +429,9 @@ struct SproutSim {
         for (int k = 0; k < kStages; k++) record_stage(k, st);
     }
 
-    int ensure_graph() {
+    // The launch configuration for the tank as it is now; true when it changed (a captured
+    // substep is then stale).
+    bool refresh_cfg() {
         LaunchCfg want = cfg;
         want.n_slots = n_slots;
         want.thermal = thermal;
@@ -441,13 +443,18 @@ struct SproutSim {
         want.visc_sweeps = (int)std::min(std::max(params.viscosity_mg_sweeps, 1u), 2u);
         want.visc_blocks = std::max(1, std::min(d.nwg, visc_max[want.visc_sweeps - 1]));
         want.mixed = mixed;
-        bool same = graph_ok && want.n_slots == cfg.n_slots && want.thermal == cfg.thermal && want.heat == cfg.heat &&
+        bool same = want.n_slots == cfg.n_slots && want.thermal == cfg.thermal && want.heat == cfg.heat &&
                     want.visc_mode == cfg.visc_mode && want.twice == cfg.twice && want.viscous_warm == cfg.viscous_warm &&
                     want.visc_levels == cfg.visc_levels && want.visc_sweeps == cfg.visc_sweeps &&
-                    want.visc_blocks == cfg.visc_blocks && want.mixed == cfg.mixed && d.stride == tank.stride;
+                    want.visc_blocks == cfg.visc_blocks && want.mixed == cfg.mixed && d.stride == std::max(tank.stride, 8);
         cfg = want;
         d.stride = std::max(tank.stride, 8);
-        if (same || !use_graph) return SPROUT_OK;
+        return !same;
+    }
+
+    int ensure_graph() {
+        const bool changed = refresh_cfg();
+        if ((graph_ok && !changed) || !use_graph) return SPROUT_OK;
         if (exec) { cudaGraphExecDestroy(exec); exec = nullptr; }
         if (graph) { cudaGraphDestroy(graph); graph = nullptr; }
         graph_ok = false;
@@ -550,18 +557,30 @@ struct SproutSim {
         return upload_tables(nullptr);
     }
 
-    int step(uint32_t substeps, float target, const ToolState* tool) {
+    // What a step call does before its substeps run, on the sim's stream: the parameters and
+    // material table (when they changed), the batch words of StepBuf.
+    int prepare_step(uint32_t substeps, float target, const ToolState* tool) {
         if (n_slots == 0 || tank.rows.empty()) return fail(SPROUT_E_ARG, "step before reset (no particles)");
         int rc = derive_viscosity();
         if (rc != SPROUT_OK) return rc;
         rc = upload_tables(tool);
         if (rc != SPROUT_OK) return rc;
         if (substeps == 0) return SPROUT_OK;
-        float fl = std::max(target, 0.0f);
-        uint32_t batch[2] = {substeps, 0u};
-        CUDA_TRY(cudaMemcpyAsync(&d.S->frame_left, &fl, 4, cudaMemcpyHostToDevice, stream));
-        CUDA_TRY(cudaMemcpyAsync(&d.S->batch_steps, batch, 8, cudaMemcpyHostToDevice, stream));
+        batch_words[0] = __builtin_bit_cast(uint32_t, std::max(target, 0.0f));
+        batch_words[1] = substeps;
+        batch_words[2] = 0u;
+        CUDA_TRY(cudaMemcpyAsync(&d.S->frame_left, &batch_words[0], 4, cudaMemcpyHostToDevice, stream));
+        CUDA_TRY(cudaMemcpyAsync(&d.S->batch_steps, &batch_words[1], 8, cudaMemcpyHostToDevice, stream));
         h2d_bytes += 12;
+        return SPROUT_OK;
+    }
+    uint32_t batch_words[3] = {0u, 0u, 0u};
+    struct SproutBatch* batch = nullptr;   // the batch this sim steps in, if any
+
+    int step(uint32_t substeps, float target, const ToolState* tool) {
+        if (batch) return fail(SPROUT_E_ARG, "the sim belongs to a batch: step the batch (or remove it first)");
+        int rc = prepare_step(substeps, target, tool);
+        if (rc != SPROUT_OK || substeps == 0) return rc;
         if ((rc = ensure_graph()) != SPROUT_OK) return rc;
         for (uint32_t k = 0; k < substeps; k++) {
             if (use_graph && graph_ok) CUDA_TRY(cudaGraphLaunch(exec, stream));
@@ -645,6 +664,298 @@ struct SproutSim {
 };
 
 // ---- C ABI --------------------------------------------------------------------------------
+
+// ---- batches: many tanks advanced by one captured graph per substep ------------------------
+//
+// The particle and grid stages of the batch's tanks run as concurrent branches of the graph
+// (a few worker streams, tanks dealt round-robin), the pressure solves of all of them as one
+// persistent kernel over their flattened tile lists (launch_pressure_batch), the viscosity
+// solves one after another. A tank's results are the same as when it steps alone.
+struct SproutBatch {
+    static constexpr int kWorkers = 8;
+    std::vector<SproutSim*> sims;
+    int device = 0;
+    bool mixed = false;
+    cudaStream_t main = nullptr;
+    cudaStream_t workers[kWorkers] = {};
+    std::vector<cudaEvent_t> events;     // fork / join points of the capture
+    cudaEvent_t ev_done = nullptr;
+    std::vector<cudaEvent_t> ev_in;      // per tank: its uploads are on the device
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    bool graph_ok = false;
+    // the two solves' views (all tanks; the tanks with a second solve) and their arrays
+    struct View {
+        BatchView v{};
+        std::vector<void*> allocs;
+        int blocks = 0;
+        size_t smem = 0;
+        std::vector<SproutSim*> members;
+        std::vector<DevScene> scenes;   // the members' scenes as captured
+        void release() {
+            for (void* p : allocs) cudaFree(p);
+            allocs.clear();
+            members.clear();
+            scenes.clear();
+            v = BatchView{};
+        }
+    } first, second;
+    size_t h2d = 0;
+
+    ~SproutBatch() {
+        for (SproutSim* sim : sims) sim->batch = nullptr;
+        drop_graph();
+        first.release();
+        second.release();
+        for (cudaEvent_t e : events) cudaEventDestroy(e);
+        for (cudaEvent_t e : ev_in) cudaEventDestroy(e);
+        if (ev_done) cudaEventDestroy(ev_done);
+        for (cudaStream_t w : workers)
+            if (w) cudaStreamDestroy(w);
+        if (main) cudaStreamDestroy(main);
+    }
+
+    int init() {
+        CUDA_TRY(cudaGetDevice(&device));
+        CUDA_TRY(cudaStreamCreateWithFlags(&main, cudaStreamNonBlocking));
+        for (cudaStream_t& w : workers) CUDA_TRY(cudaStreamCreateWithFlags(&w, cudaStreamNonBlocking));
+        CUDA_TRY(cudaEventCreateWithFlags(&ev_done, cudaEventDisableTiming));
+        return SPROUT_OK;
+    }
+
+    void drop_graph() {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        exec = nullptr;
+        graph = nullptr;
+        graph_ok = false;
+    }
+
+    int add(SproutSim* sim) {
+        if (sim->batch == this) return SPROUT_OK;
+        if (sim->batch) return fail(SPROUT_E_ARG, "the sim already belongs to another batch");
+        if (sim->device != device) return fail(SPROUT_E_ARG, "the sim lives on another device than the batch");
+        CUDA_TRY(cudaStreamSynchronize(sim->stream));
+        sims.push_back(sim);
+        sim->batch = this;
+        cudaEvent_t e;
+        CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        ev_in.push_back(e);
+        drop_graph();
+        return mixed ? sim->set_precision(1) : SPROUT_OK;
+    }
+
+    int remove(SproutSim* sim) {
+        auto it = std::find(sims.begin(), sims.end(), sim);
+        if (it == sims.end()) return fail(SPROUT_E_ARG, "the sim is not in this batch");
+        CUDA_TRY(cudaStreamSynchronize(main));
+        const size_t k = (size_t)(it - sims.begin());
+        sims.erase(it);
+        cudaEventDestroy(ev_in[k]);
+        ev_in.erase(ev_in.begin() + (long)k);
+        sim->batch = nullptr;
+        drop_graph();
+        return SPROUT_OK;
+    }
+
+    int set_precision(int mode) {
+        if (mode != 0 && mode != 1) return fail(SPROUT_E_ARG, "precision mode is 0 (plain FP32) or 1 (mixed)");
+        for (SproutSim* sim : sims) {
+            int rc = sim->set_precision(mode);
+            if (rc != SPROUT_OK) return rc;
+        }
+        if (mixed != (mode == 1)) drop_graph();
+        mixed = mode == 1;
+        return SPROUT_OK;
+    }
+
+    template <class T>
+    int upload(View& V, T** out, const std::vector<T>& host) {
+        void* p = nullptr;
+        size_t b = std::max<size_t>(host.size(), 1) * sizeof(T);
+        if (cudaMalloc(&p, b) != cudaSuccess) return fail(SPROUT_E_NOMEM, "batch arrays");
+        V.allocs.push_back(p);
+        if (!host.empty()) CUDA_TRY(cudaMemcpy(p, host.data(), host.size() * sizeof(T), cudaMemcpyHostToDevice));
+        h2d += b;
+        *out = static_cast<T*>(p);
+        return SPROUT_OK;
+    }
+
+    // The device arrays of a batch view over `members`.
+    int build_view(View& V, const std::vector<SproutSim*>& members) {
+        V.release();
+        V.members = members;
+        const int ns = (int)members.size();
+        if (ns == 0) return SPROUT_OK;
+        std::vector<DevScene> scenes(ns);
+        std::vector<int> scale(ns), off((size_t)kMaxLevels * (ns + 1), 0);
+        int max_tail = 0;
+        size_t smem = 0;
+        for (int k = 0; k < ns; k++) {
+            const SproutSim* sim = members[k];
+            scenes[k] = sim->d;
+            const LaunchCfg& c = sim->cfg;
+            scale[k] = (c.visc_mode == 2 && c.twice && c.viscous_warm) ? 1 : 0;
+            max_tail = std::max(max_tail, sim->d.lv.tail);
+            smem = std::max(smem, pressure_smem(sim->d.lv));
+        }
+        for (int l = 0; l < kMaxLevels; l++) {
+            int* o = &off[(size_t)l * (ns + 1)];
+            o[0] = 0;
+            for (int k = 0; k < ns; k++) {
+                const Levels& L = members[k]->d.lv;
+                const int t = l <= L.tail ? ((L.w[l] + 15) / 16) * ((L.h[l] + 15) / 16) : 0;
+                o[k + 1] = o[k] + t;
+            }
+        }
+        int rc;
+        DevScene* ds;
+        int *doff, *dscale;
+        if ((rc = upload(V, &ds, scenes)) != SPROUT_OK) return rc;
+        if ((rc = upload(V, &doff, off)) != SPROUT_OK) return rc;
+        if ((rc = upload(V, &dscale, scale)) != SPROUT_OK) return rc;
+        std::vector<unsigned char> scal((size_t)ns * pressure_batch_scalar_bytes(), 0);
+        unsigned char* dscal;
+        if ((rc = upload(V, &dscal, scal)) != SPROUT_OK) return rc;
+        std::vector<SolveState> k0(1);
+        std::memset(k0.data(), 0, sizeof(SolveState));
+        SolveState* dk;
+        if ((rc = upload(V, &dk, k0)) != SPROUT_OK) return rc;
+        V.v = BatchView{ds, ns, doff, dscal, dscale, dk, max_tail};
+        V.scenes = scenes;
+        V.smem = smem;
+        const int mx = pressure_batch_blocks_max(device, smem, mixed);
+        int total_tiles = 0;
+        for (const SproutSim* sim : members) total_tiles += sim->d.nwg;
+        V.blocks = std::max(1, std::min(mx, std::max(total_tiles, ns)));
+        return SPROUT_OK;
+    }
+
+    cudaEvent_t event(size_t& k) {
+        while (events.size() <= k) {
+            cudaEvent_t e;
+            cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+            events.push_back(e);
+        }
+        return events[k++];
+    }
+    // main -> workers
+    void fork(size_t& k) {
+        cudaEvent_t e = event(k);
+        cudaEventRecord(e, main);
+        for (cudaStream_t w : workers) cudaStreamWaitEvent(w, e, 0);
+    }
+    // workers -> main
+    void join(size_t& k) {
+        for (cudaStream_t w : workers) {
+            cudaEvent_t e = event(k);
+            cudaEventRecord(e, w);
+            cudaStreamWaitEvent(main, e, 0);
+        }
+    }
+
+    // One substep of every tank, recorded on `main` (and the workers).
+    void record_substep() {
+        size_t k = 0;
+        fork(k);
+        for (size_t s = 0; s < sims.size(); s++)
+            for (int st = 0; st < 4; st++) sims[s]->record_stage(st, workers[s % kWorkers]);
+        join(k);
+        if (first.v.ns > 0) launch_pressure_batch(first.v, mixed, first.blocks, first.smem, main, 0);
+        fork(k);
+        for (size_t s = 0; s < sims.size(); s++) sims[s]->record_stage(5, workers[s % kWorkers]);
+        join(k);
+        if (second.v.ns > 0) {
+            for (SproutSim* sim : second.members) launch_viscosity(sim->d, sim->cfg, main, 1);
+            fork(k);
+            for (size_t s = 0; s < second.members.size(); s++) launch_second_projection_rhs(second.members[s]->d, workers[s % kWorkers]);
+            join(k);
+            launch_pressure_batch(second.v, mixed, second.blocks, second.smem, main, 1);
+            fork(k);
+            for (size_t s = 0; s < second.members.size(); s++) launch_second_projection(second.members[s]->d, workers[s % kWorkers]);
+            join(k);
+        }
+    }
+
+    int ensure_graph() {
+        bool changed = false;
+        for (SproutSim* sim : sims) changed |= sim->refresh_cfg();
+        // a tank's device arrays may have changed since the capture (its precision buffers)
+        for (size_t k = 0; k < first.scenes.size() && k < sims.size(); k++)
+            changed |= std::memcmp(&first.scenes[k], &sims[k]->d, sizeof(DevScene)) != 0;
+        if (graph_ok && !changed) return SPROUT_OK;
+        drop_graph();
+        std::vector<SproutSim*> twice;
+        for (SproutSim* sim : sims) {
+            if (sim->cfg.visc_mode == 2 && !sim->cfg.twice)
+                return fail(SPROUT_E_UNSUPPORTED, "a batch carries the implicit viscosity only between two pressure solves (viscous_projection 1)");
+            if (sim->cfg.mixed != mixed) return fail(SPROUT_E_ARG, "a batch's tanks share its precision");
+            if (sim->cfg.visc_mode == 2) twice.push_back(sim);
+        }
+        int rc;
+        if ((rc = build_view(first, sims)) != SPROUT_OK) return rc;
+        if ((rc = build_view(second, twice)) != SPROUT_OK) return rc;
+        CUDA_TRY(cudaStreamSynchronize(main));
+        CUDA_TRY(cudaStreamBeginCapture(main, cudaStreamCaptureModeThreadLocal));
+        record_substep();
+        cudaError_t e = cudaStreamEndCapture(main, &graph);
+        if (e != cudaSuccess) {
+            graph = nullptr;
+            return fail(SPROUT_E_CUDA, std::string("capturing the batch's substep: ") + cudaGetErrorString(e));
+        }
+        CUDA_TRY(cudaGraphInstantiate(&exec, graph, 0));
+        graph_ok = true;
+        return SPROUT_OK;
+    }
+
+    int step(uint32_t substeps) {
+        if (sims.empty() || substeps == 0) return SPROUT_OK;
+        for (size_t s = 0; s < sims.size(); s++) {
+            SproutSim* sim = sims[s];
+            int rc = sim->prepare_step(substeps, (float)(substeps * (double)sim->dt_estimate()), nullptr);
+            if (rc != SPROUT_OK) return rc;
+            CUDA_TRY(cudaEventRecord(ev_in[s], sim->stream));
+            CUDA_TRY(cudaStreamWaitEvent(main, ev_in[s], 0));
+        }
+        int rc = ensure_graph();
+        if (rc != SPROUT_OK) return rc;
+        for (uint32_t k = 0; k < substeps; k++) CUDA_TRY(cudaGraphLaunch(exec, main));
+        CUDA_TRY(cudaEventRecord(ev_done, main));
+        for (SproutSim* sim : sims) CUDA_TRY(cudaStreamWaitEvent(sim->stream, ev_done, 0));
+        return SPROUT_OK;
+    }
+
+    int check_error() {
+        for (View* V : {&first, &second}) {
+            if (V->v.ns == 0) continue;
+            uint32_t err = 0;
+            CUDA_TRY(cudaMemcpy(&err, &V->v.K->error, 4, cudaMemcpyDeviceToHost));
+            if (err) return fail(SPROUT_E_TIMEOUT, "a bounded device-side wait ran out (grid barrier of the batched pressure solve)");
+        }
+        for (SproutSim* sim : sims) {
+            int rc = sim->check_device_error();
+            if (rc != SPROUT_OK) return rc;
+        }
+        return SPROUT_OK;
+    }
+
+    int profile(uint32_t substeps, float* ms) {
+        cudaEvent_t a, b;
+        CUDA_TRY(cudaEventCreate(&a));
+        CUDA_TRY(cudaEventCreate(&b));
+        int rc = step(0);
+        if (rc != SPROUT_OK) return rc;
+        if ((rc = ensure_graph()) != SPROUT_OK) return rc;
+        CUDA_TRY(cudaEventRecord(a, main));
+        for (uint32_t k = 0; k < substeps; k++) CUDA_TRY(cudaGraphLaunch(exec, main));
+        CUDA_TRY(cudaEventRecord(b, main));
+        CUDA_TRY(cudaEventSynchronize(b));
+        CUDA_TRY(cudaEventElapsedTime(ms, a, b));
+        cudaEventDestroy(a);
+        cudaEventDestroy(b);
+        return check_error();
+    }
+};
 
 extern "C" {
 
@@ -742,9 +1053,57 @@ int sprout_sim_create(uint32_t w, uint32_t h, uint32_t capacity, const SproutPar
     return SPROUT_OK;
 }
 int sprout_sim_destroy(SproutSim* sim) {
+    if (sim && sim->batch) sim->batch->remove(sim);
     if (sim) cudaStreamSynchronize(sim->stream);
     delete sim;
     return SPROUT_OK;
+}
+
+int sprout_batch_create(SproutBatch** out) {
+    if (!out) return fail(SPROUT_E_ARG, "null argument");
+    SproutBatch* b = new SproutBatch();
+    int rc = b->init();
+    if (rc != SPROUT_OK) {
+        delete b;
+        return rc;
+    }
+    *out = b;
+    return SPROUT_OK;
+}
+int sprout_batch_destroy(SproutBatch* b) {
+    if (b) cudaStreamSynchronize(b->main);
+    delete b;
+    return SPROUT_OK;
+}
+int sprout_batch_add(SproutBatch* b, SproutSim* sim) {
+    if (!b || !sim) return fail(SPROUT_E_ARG, "null argument");
+    return b->add(sim);
+}
+int sprout_batch_remove(SproutBatch* b, SproutSim* sim) {
+    if (!b || !sim) return fail(SPROUT_E_ARG, "null argument");
+    return b->remove(sim);
+}
+int sprout_batch_size(SproutBatch* b, uint32_t* n) {
+    if (!b || !n) return fail(SPROUT_E_ARG, "null argument");
+    *n = (uint32_t)b->sims.size();
+    return SPROUT_OK;
+}
+int sprout_batch_set_precision(SproutBatch* b, int mode) {
+    if (!b) return fail(SPROUT_E_ARG, "null argument");
+    return b->set_precision(mode);
+}
+int sprout_batch_step(SproutBatch* b, uint32_t substeps) {
+    if (!b) return fail(SPROUT_E_ARG, "null argument");
+    return b->step(substeps);
+}
+int sprout_batch_sync(SproutBatch* b) {
+    if (!b) return fail(SPROUT_E_ARG, "null argument");
+    CUDA_TRY(cudaStreamSynchronize(b->main));
+    return b->check_error();
+}
+int sprout_batch_profile(SproutBatch* b, uint32_t substeps, float* ms) {
+    if (!b || !ms) return fail(SPROUT_E_ARG, "null argument");
+    return b->profile(substeps, ms);
 }
 int sprout_sim_set_precision(SproutSim* sim, int mode) {
     if (!sim) return fail(SPROUT_E_ARG, "null argument");
