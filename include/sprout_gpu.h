@@ -191,6 +191,8 @@ int sprout_sim_set_precision(SproutSim* sim, int mode);
  * downloads and parameters work as usual. The implicit viscosity is carried with
  * viscous_projection 1 (the default). Blocking: sync, profile. */
 typedef struct SproutBatch SproutBatch;
+/* Free and total memory of the current device (cudaMemGetInfo): a serving loop's admission. */
+int sprout_device_memory(size_t* free_bytes, size_t* total_bytes);
 int sprout_batch_create(SproutBatch** out);
 int sprout_batch_destroy(SproutBatch* b);
 int sprout_batch_add(SproutBatch* b, SproutSim* sim);
@@ -200,6 +202,13 @@ int sprout_batch_size(SproutBatch* b, uint32_t* n);
 int sprout_batch_set_precision(SproutBatch* b, int mode);
 /* `substeps` substeps of every tank (each at its own dt), asynchronous. */
 int sprout_batch_step(SproutBatch* b, uint32_t substeps);
+/* One substep of the members at indices members[0 .. n) only (in the order they were added),
+ * launched directly without a graph: for continuous batching, where the set of tanks with
+ * work changes from launch to launch. Asynchronous. */
+int sprout_batch_step_subset(SproutBatch* b, const uint32_t* members, uint32_t n);
+/* Every sprout_batch_step / _step_subset call is one ticket, numbered from 1 in issue order.
+ * Reports how many were issued and how many have finished on the device (non-blocking). */
+int sprout_batch_tickets(SproutBatch* b, uint64_t* issued, uint64_t* completed);
 int sprout_batch_sync(SproutBatch* b);
 /* Device ms of `substeps` more substeps of the batch, from CUDA events (blocking). */
 int sprout_batch_profile(SproutBatch* b, uint32_t substeps, float* ms);

@@ -42,6 +42,7 @@ EXPORTS = [
     "sprout_sim_profile_passes", "sprout_pressure_solve_static", "sprout_sim_set_precision",
     "sprout_batch_create", "sprout_batch_destroy", "sprout_batch_add", "sprout_batch_remove", "sprout_batch_size",
     "sprout_batch_set_precision", "sprout_batch_step", "sprout_batch_sync", "sprout_batch_profile",
+    "sprout_batch_step_subset", "sprout_batch_tickets", "sprout_device_memory",
 ]
 
 STAGES = ["advance", "sort", "p2g", "grid", "pressure", "project", "viscosity", "project2"]
@@ -134,6 +135,9 @@ def lib() -> C.CDLL:
         "sprout_batch_step": ([V, C.c_uint32], C.c_int),
         "sprout_batch_sync": ([V], C.c_int),
         "sprout_batch_profile": ([V, C.c_uint32, P(C.c_float)], C.c_int),
+        "sprout_batch_step_subset": ([V, P(C.c_uint32), C.c_uint32], C.c_int),
+        "sprout_batch_tickets": ([V, P(C.c_uint64), P(C.c_uint64)], C.c_int),
+        "sprout_device_memory": ([P(C.c_size_t), P(C.c_size_t)], C.c_int),
         "sprout_pressure_solve_static": ([C.c_uint32, C.c_uint32, V, V, V, V, C.c_float, C.c_float, C.c_uint32, V,
                                           P(C.c_uint32), P(C.c_float)], C.c_int),
     }
@@ -363,6 +367,17 @@ class Batch:
     def step(self, substeps: int = 1):
         _check(lib().sprout_batch_step(self._h, substeps))
 
+    def step_subset(self, members):
+        """One substep of the members at these indices only (continuous batching)."""
+        idx = (C.c_uint32 * len(members))(*members)
+        _check(lib().sprout_batch_step_subset(self._h, idx, len(members)))
+
+    def tickets(self):
+        """(issued, completed): step calls so far and how many have finished on the device."""
+        a, b = C.c_uint64(), C.c_uint64()
+        _check(lib().sprout_batch_tickets(self._h, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
     def sync(self):
         _check(lib().sprout_batch_sync(self._h))
 
@@ -370,3 +385,10 @@ class Batch:
         ms = C.c_float()
         _check(lib().sprout_batch_profile(self._h, substeps, C.byref(ms)))
         return ms.value
+
+
+def device_memory():
+    """(free, total) bytes of the current device."""
+    a, b = C.c_size_t(), C.c_size_t()
+    _check(lib().sprout_device_memory(C.byref(a), C.byref(b)))
+    return a.value, b.value

@@ -278,87 +278,6 @@ struct Rsrc {
     }
 };
 
-// mg_down black(): value of black cell n after the half-sweep from zero.
-template <class M>
-DEV float2 down_black(const DevScene& d, const Lv& L, const Rsrc<M>& R, int nx, int ny) {
-    int i = l_at(L, nx, ny);
-    float4 w = M::A(d, i);
-    float2 sum = R.at(d, i);
-    for (int q = 0; q < 4; q++) {
-        int mx = nx + NBX[q], my = ny + NBY[q];
-        if (!unknown<M>(d, L, mx, my)) continue;
-        int j = l_at(L, mx, my);
-        float wd = wcomp(w, q);
-        float2 rj = R.at(d, j);
-        float dj = M::Dg(d, j);
-        sum.x += wd * rj.x / dj;
-        sum.y += wd * rj.y / dj;
-    }
-    float di = M::Dg(d, i);
-    return make_float2(sum.x / di, sum.y / di);
-}
-
-// mg_down.comp on tile t of level l. On level 0 with `r_out` it also applies
-// cg_update.comp: x += alpha p and the residual update into r_out.
-template <class M>
-DEV void down_tile(const DevScene& d, int l, int t, const Rsrc<M>& R, float2* r_out, const float2* p, float2* sz) {
-    const Lv F = lev(d.lv, l), C = lev(d.lv, l + 1);
-    const int tx_n = tiles_x(F);
-    const int lx = threadIdx.x & 15, ly = threadIdx.x >> 4;
-    if (d.ptile[F.toff + t] == 0u) return;
-    const int cx = (t % tx_n) * 16 + lx, cy = (t / tx_n) * 16 + ly;
-    const bool red = ((cx + cy) & 1) == 0;
-    float2 z = make_float2(0.0f, 0.0f);
-    if (l_inside(F, cx, cy)) {
-        const int i = l_at(F, cx, cy);
-        const float D = M::Dg(d, i);
-        if (D > 0.0f) {
-            if (red) {
-                float2 r = R.at(d, i);
-                z = make_float2(r.x / D, r.y / D);
-            } else {
-                z = down_black<M>(d, F, R, cx, cy);
-            }
-        }
-        if (r_out && d.mgd[i] > 0.0f) {
-            // cg_update.comp: x += alpha p, r -= alpha q (unknowns of active tiles)
-            float2 pp = p[i];
-            float2 x = d.pres[i];
-            x.x += R.ax * pp.x;
-            x.y += R.ay * pp.y;
-            d.pres[i] = x;
-            r_out[i] = R.at(d, i);
-        }
-        M::setX(d, i, z);
-    }
-    sz[threadIdx.x] = z;
-    __syncthreads();
-    if (((lx | ly) & 1) == 0) {
-        const int Cx = cx >> 1, Cy = cy >> 1;
-        if (Cx < C.w && Cy < C.h) {
-            float sx = 0.0f, sy = 0.0f;
-            for (int k = 0; k < 2; k++) {
-                int qx = cx + k, qy = cy + k;
-                if (!unknown<M>(d, F, qx, qy)) continue;
-                float4 w = M::A(d, l_at(F, qx, qy));
-                int lqx = lx + k, lqy = ly + k;
-                for (int q = 0; q < 4; q++) {
-                    int nx = qx + NBX[q], ny = qy + NBY[q];
-                    if (!unknown<M>(d, F, nx, ny)) continue;
-                    int lnx = lqx + NBX[q], lny = lqy + NBY[q];
-                    bool here = lnx >= 0 && lny >= 0 && lnx < 16 && lny < 16;
-                    float2 zb = here ? sz[lny * 16 + lnx] : down_black<M>(d, F, R, nx, ny);
-                    float wd = wcomp(w, q);
-                    sx += wd * zb.x;
-                    sy += wd * zb.y;
-                }
-            }
-            M::setR(d, l_at(C, Cx, Cy), make_float2(sx, sy));
-        }
-    }
-    __syncthreads();
-}
-
 // The tail levels' state in each block's shared memory (dynamic, FP32 in both precisions):
 // per tail cell the matrix row (couplings, diagonal), the iterate and the right-hand side,
 // at its offset from the first tail level (the slots of mg_tail.comp).
@@ -435,36 +354,135 @@ struct Zc {
     int off, w;
 };
 
-// mg_up black(): new value of black cell n after the coarse correction.
+// A level's tile and RH cells around it staged in shared memory, RW x RW slots: the
+// diagonal (zero outside the level and where no unknown), the couplings, and up to three
+// vector fields. The V-cycle's and the apply's tile bodies load their region in one
+// parallel pass and then read only these slots: what they compute is the same, value for
+// value, as reading the fields from global memory one dependent load after another.
+constexpr int RH = 2;
+constexpr int RW = 16 + 2 * RH;
+constexpr int RN = RW * RW;
+struct Region {
+    float dg[RN];
+    float4 a[RN];
+    float2 u[RN], v[RN], w[RN];
+};
+DEV int rslot(int lx, int ly) { return (ly + RH) * RW + lx + RH; }
+__constant__ int RSTEP[4] = {-1, 1, -RW, RW};
+
 template <class M>
 DEV float2 coarse_z(const DevScene& d, const Zc& zc, int mx, int my) {
     const int k = (my >> 1) * zc.w + (mx >> 1);
     return zc.s ? zc.s[k] : M::Z(d, zc.off + k);
 }
 
+
+// mg_down.comp on tile t of level l. On level 0 with `r_out` it also applies
+// cg_update.comp: x += alpha p and the residual update into r_out. Region: dg, a, and the
+// right-hand side (through R) in u.
 template <class M>
-DEV float2 up_black(const DevScene& d, const Lv& L, const Zc& zc, const Rsrc<M>& rhs, int nx, int ny) {
-    int i = l_at(L, nx, ny);
-    float4 w = M::A(d, i);
-    float2 sum = rhs.at(d, i);
-    for (int q = 0; q < 4; q++) {
-        int mx = nx + NBX[q], my = ny + NBY[q];
-        if (!unknown<M>(d, L, mx, my)) continue;
-        float2 xm = M::X(d, l_at(L, mx, my));
-        float2 zcv = coarse_z<M>(d, zc, mx, my);
-        float wd = wcomp(w, q);
-        sum.x += wd * (xm.x + MG_OMEGA * zcv.x);
-        sum.y += wd * (xm.y + MG_OMEGA * zcv.y);
+DEV void down_tile(const DevScene& d, int l, int t, const Rsrc<M>& R, float2* r_out, const float2* p, float2* sz, Region& rg) {
+    const Lv F = lev(d.lv, l), C = lev(d.lv, l + 1);
+    const int tx_n = tiles_x(F);
+    const int lx = threadIdx.x & 15, ly = threadIdx.x >> 4;
+    if (d.ptile[F.toff + t] == 0u) return;
+    const int ox = (t % tx_n) * 16, oy = (t / tx_n) * 16;
+    for (int k = threadIdx.x; k < RN; k += NT) {
+        const int x = ox - RH + k % RW, y = oy - RH + k / RW;
+        float dd = 0.0f;
+        float4 aa = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        float2 rr = make_float2(0.0f, 0.0f);
+        if (l_inside(F, x, y)) {
+            const int i = l_at(F, x, y);
+            dd = M::Dg(d, i);
+            if (dd > 0.0f) {
+                aa = M::A(d, i);
+                rr = R.at(d, i);
+            } else {
+                dd = 0.0f;
+            }
+        }
+        rg.dg[k] = dd;
+        rg.a[k] = aa;
+        rg.u[k] = rr;
     }
-    float di = M::Dg(d, i);
-    return make_float2(sum.x / di, sum.y / di);
+    __syncthreads();
+    // the value of black slot k after the half-sweep from zero (mg_down black())
+    auto black = [&](int k) {
+        const float4 w = rg.a[k];
+        float2 sum = rg.u[k];
+        for (int q = 0; q < 4; q++) {
+            const int j = k + RSTEP[q];
+            const float dj = rg.dg[j];
+            if (dj <= 0.0f) continue;
+            const float wd = wcomp(w, q);
+            const float2 rj = rg.u[j];
+            sum.x += wd * rj.x / dj;
+            sum.y += wd * rj.y / dj;
+        }
+        const float di = rg.dg[k];
+        return make_float2(sum.x / di, sum.y / di);
+    };
+    const int cx = ox + lx, cy = oy + ly;
+    const int k0 = rslot(lx, ly);
+    const bool red = ((cx + cy) & 1) == 0;
+    float2 z = make_float2(0.0f, 0.0f);
+    if (l_inside(F, cx, cy)) {
+        const int i = l_at(F, cx, cy);
+        const float D = rg.dg[k0];
+        if (D > 0.0f) {
+            if (red) {
+                const float2 r = rg.u[k0];
+                z = make_float2(r.x / D, r.y / D);
+            } else {
+                z = black(k0);
+            }
+        }
+        if (r_out && d.mgd[i] > 0.0f) {
+            // cg_update.comp: x += alpha p, r -= alpha q (unknowns of active tiles)
+            float2 pp = p[i];
+            float2 x = d.pres[i];
+            x.x += R.ax * pp.x;
+            x.y += R.ay * pp.y;
+            d.pres[i] = x;
+            r_out[i] = R.at(d, i);
+        }
+        M::setX(d, i, z);
+    }
+    sz[threadIdx.x] = z;
+    __syncthreads();
+    if (((lx | ly) & 1) == 0) {
+        const int Cx = cx >> 1, Cy = cy >> 1;
+        if (Cx < C.w && Cy < C.h) {
+            float sx = 0.0f, sy = 0.0f;
+            for (int k = 0; k < 2; k++) {
+                const int kq = rslot(lx + k, ly + k);
+                if (rg.dg[kq] <= 0.0f) continue;
+                const float4 w = rg.a[kq];
+                const int lqx = lx + k, lqy = ly + k;
+                for (int q = 0; q < 4; q++) {
+                    const int kn = kq + RSTEP[q];
+                    if (rg.dg[kn] <= 0.0f) continue;
+                    const int lnx = lqx + NBX[q], lny = lqy + NBY[q];
+                    const bool here = lnx >= 0 && lny >= 0 && lnx < 16 && lny < 16;
+                    const float2 zb = here ? sz[lny * 16 + lnx] : black(kn);
+                    const float wd = wcomp(w, q);
+                    sx += wd * zb.x;
+                    sy += wd * zb.y;
+                }
+            }
+            M::setR(d, l_at(C, Cx, Cy), make_float2(sx, sy));
+        }
+    }
+    __syncthreads();
 }
 
 // mg_up.comp on tile t of level l; on level 0 (flag) the tile's sums of r.z, r.r into
-// part[t].
+// part[t]. Region: dg, a, the right-hand side in u, the pre-smoothed values (mgx) in v and
+// each slot's coarse-grid value in w.
 template <class M>
 DEV void up_tile(const DevScene& d, int l, int t, bool flag, const Rsrc<M>& rhs, const Zc& zc, float2* sz,
-                 typename M::acc4* buf) {
+                 typename M::acc4* buf, Region& rg) {
     using acc = typename M::acc;
     const Lv F = lev(d.lv, l);
     const int tx_n = tiles_x(F);
@@ -474,32 +492,74 @@ DEV void up_tile(const DevScene& d, int l, int t, bool flag, const Rsrc<M>& rhs,
         if (flag && threadIdx.x == 0) part[t] = M::a4(0, 0, 0, 0);
         return;
     }
-    const int cx = (t % tx_n) * 16 + lx, cy = (t / tx_n) * 16 + ly;
+    const int ox = (t % tx_n) * 16, oy = (t / tx_n) * 16;
+    for (int k = threadIdx.x; k < RN; k += NT) {
+        const int x = ox - RH + k % RW, y = oy - RH + k / RW;
+        float dd = 0.0f;
+        float4 aa = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        float2 r = make_float2(0.0f, 0.0f), xm = r, zcv = r;
+        if (l_inside(F, x, y)) {
+            const int i = l_at(F, x, y);
+            dd = M::Dg(d, i);
+            if (dd > 0.0f) {
+                aa = M::A(d, i);
+                r = rhs.at(d, i);
+                xm = M::X(d, i);
+                zcv = coarse_z<M>(d, zc, x, y);
+            } else {
+                dd = 0.0f;
+            }
+        }
+        rg.dg[k] = dd;
+        rg.a[k] = aa;
+        rg.u[k] = r;
+        rg.v[k] = xm;
+        rg.w[k] = zcv;
+    }
+    __syncthreads();
+    // the new value of black slot k after the coarse correction (mg_up black())
+    auto black = [&](int k) {
+        const float4 w = rg.a[k];
+        float2 sum = rg.u[k];
+        for (int q = 0; q < 4; q++) {
+            const int j = k + RSTEP[q];
+            if (rg.dg[j] <= 0.0f) continue;
+            const float2 xm = rg.v[j];
+            const float2 zcv = rg.w[j];
+            const float wd = wcomp(w, q);
+            sum.x += wd * (xm.x + MG_OMEGA * zcv.x);
+            sum.y += wd * (xm.y + MG_OMEGA * zcv.y);
+        }
+        const float di = rg.dg[k];
+        return make_float2(sum.x / di, sum.y / di);
+    };
+    const int cx = ox + lx, cy = oy + ly;
+    const int k0 = rslot(lx, ly);
     const bool red = ((cx + cy) & 1) == 0;
-    const bool unk = unknown<M>(d, F, cx, cy);
+    const bool unk = rg.dg[k0] > 0.0f;
     float2 z = make_float2(0.0f, 0.0f);
-    if (unk && !red) z = up_black<M>(d, F, zc, rhs, cx, cy);
+    if (unk && !red) z = black(k0);
     sz[threadIdx.x] = z;
     __syncthreads();
     typename M::acc4 a4 = M::a4(0, 0, 0, 0);
     if (l_inside(F, cx, cy)) {
         const int i = l_at(F, cx, cy);
         if (unk) {
-            float2 r = rhs.at(d, i);
+            const float2 r = rg.u[k0];
             if (red) {
-                float4 w = M::A(d, i);
+                const float4 w = rg.a[k0];
                 float sx = r.x, sy = r.y;
                 for (int q = 0; q < 4; q++) {
-                    int nx = cx + NBX[q], ny = cy + NBY[q];
-                    if (!unknown<M>(d, F, nx, ny)) continue;
-                    int lnx = lx + NBX[q], lny = ly + NBY[q];
-                    bool here = lnx >= 0 && lny >= 0 && lnx < 16 && lny < 16;
-                    float2 zb = here ? sz[lny * 16 + lnx] : up_black<M>(d, F, zc, rhs, nx, ny);
-                    float wd = wcomp(w, q);
+                    const int kn = k0 + RSTEP[q];
+                    if (rg.dg[kn] <= 0.0f) continue;
+                    const int lnx = lx + NBX[q], lny = ly + NBY[q];
+                    const bool here = lnx >= 0 && lny >= 0 && lnx < 16 && lny < 16;
+                    const float2 zb = here ? sz[lny * 16 + lnx] : black(kn);
+                    const float wd = wcomp(w, q);
                     sx += wd * zb.x;
                     sy += wd * zb.y;
                 }
-                float di = M::Dg(d, i);
+                const float di = rg.dg[k0];
                 z = make_float2(sx / di, sy / di);
             }
             a4 = M::a4((acc)r.x * (acc)z.x, (acc)r.y * (acc)z.y, (acc)r.x * (acc)r.x, (acc)r.y * (acc)r.y);
@@ -622,13 +682,13 @@ DEV void phase_tail(const DevScene& d, const Tail& tl, bool writer) {
 // barrier timeout.
 template <class M>
 DEV bool vcycle(const DevScene& d, const Tail& tl, const Rsrc<M>& R, float2* r_out, const float2* p, const float2* r_new,
-                float2* sz, typename M::acc4* buf) {
+                float2* sz, typename M::acc4* buf, Region& rg) {
     const int tail = d.lv.tail;
     for (int l = 0; l < tail; l++) {
         Rsrc<M> Rl = R;
         if (l > 0) Rl = Rsrc<M>{nullptr, nullptr, 0.0f, 0.0f};
         const int T = level_tiles(d, l);
-        for (int t = blockIdx.x; t < T; t += gridDim.x) down_tile<M>(d, l, t, Rl, l == 0 ? r_out : nullptr, p, sz);
+        for (int t = blockIdx.x; t < T; t += gridDim.x) down_tile<M>(d, l, t, Rl, l == 0 ? r_out : nullptr, p, sz, rg);
         if (!grid_sync(d.K)) return false;
     }
     phase_tail<M>(d, tl, blockIdx.x == 0);
@@ -637,7 +697,7 @@ DEV bool vcycle(const DevScene& d, const Tail& tl, const Rsrc<M>& R, float2* r_o
         const Zc zc{(l == tail - 1) ? tl.x : nullptr, C.off, C.w};
         const Rsrc<M> rhs = l == 0 ? Rsrc<M>{r_new, nullptr, 0.0f, 0.0f} : Rsrc<M>{nullptr, nullptr, 0.0f, 0.0f};
         const int T = level_tiles(d, l);
-        for (int t = blockIdx.x; t < T; t += gridDim.x) up_tile<M>(d, l, t, l == 0, rhs, zc, sz, buf);
+        for (int t = blockIdx.x; t < T; t += gridDim.x) up_tile<M>(d, l, t, l == 0, rhs, zc, sz, buf, rg);
         if (!grid_sync(d.K)) return false;
     }
     return true;
@@ -676,10 +736,11 @@ DEV void true_residual_tile(const DevScene& d, int t, Dbl4* part, Dbl4* buf) {
 }
 
 // cg_apply.comp on level-0 tile t: p = z + beta p_old, q = A p (the FP32 operator), the
-// tile's sum of p.q into part[n + t].
+// tile's sum of p.q into part[n + t]. Region (one ring used): the operator's diagonal and
+// couplings, and the new direction p of every slot in u.
 template <class M>
 DEV void apply_tile(const DevScene& d, int t, float b0, float b1, const float2* p_old, float2* p_new,
-                    typename M::acc4* buf) {
+                    typename M::acc4* buf, Region& rg) {
     using acc = typename M::acc;
     const Lv F = lev(d.lv, 0);
     const int tx_n = tiles_x(F);
@@ -696,20 +757,38 @@ DEV void apply_tile(const DevScene& d, int t, float b0, float b1, const float2* 
         if (threadIdx.x == 0) part[t] = M::a4(0, 0, 0, 0);
         return;
     }
-    const int cx = (t % tx_n) * 16 + (threadIdx.x & 15), cy = (t / tx_n) * 16 + (threadIdx.x >> 4);
+    const int ox = (t % tx_n) * 16, oy = (t / tx_n) * 16;
+    for (int k = threadIdx.x; k < RN; k += NT) {
+        const int x = ox - RH + k % RW, y = oy - RH + k / RW;
+        const int kx = k % RW, ky = k / RW;
+        if (kx == 0 || ky == 0 || kx == RW - 1 || ky == RW - 1) continue;   // one ring is enough
+        float dd = 0.0f;
+        float2 pp = make_float2(0.0f, 0.0f);
+        if (l_inside(F, x, y)) {
+            const int i = l_at(F, x, y);
+            dd = d.mgd[i];
+            if (dd > 0.0f) pp = direction(i);
+            else dd = 0.0f;
+        }
+        rg.dg[k] = dd;
+        rg.u[k] = pp;
+    }
+    __syncthreads();
+    const int cx = ox + (threadIdx.x & 15), cy = oy + (threadIdx.x >> 4);
+    const int k0 = rslot(threadIdx.x & 15, threadIdx.x >> 4);
     typename M::acc4 a4 = M::a4(0, 0, 0, 0);
     if (l_inside(F, cx, cy)) {
         const int i = l_at(F, cx, cy);
-        const float D = d.mgd[i];
+        const float D = rg.dg[k0];
         if (D > 0.0f) {
-            float2 pp = direction(i);
-            float4 w = d.mga[i];
+            const float2 pp = rg.u[k0];
+            const float4 w = d.mga[i];
             float qx = D * pp.x, qy = D * pp.y;
             for (int q = 0; q < 4; q++) {
-                int nx = cx + NBX[q], ny = cy + NBY[q];
-                if (unknown_op(d, F, nx, ny)) {
-                    float2 pn = direction(l_at(F, nx, ny));
-                    float wd = wcomp(w, q);
+                const int kn = k0 + RSTEP[q];
+                if (rg.dg[kn] > 0.0f) {
+                    const float2 pn = rg.u[kn];
+                    const float wd = wcomp(w, q);
                     qx -= wd * pn.x;
                     qy -= wd * pn.y;
                 }
@@ -820,6 +899,7 @@ template <class M>
 __global__ void __launch_bounds__(NT) k_mgpcg(DevScene d, int second, int scale_mode) {
     using acc = typename M::acc;
     using acc4 = typename M::acc4;
+    __shared__ Region rg;
     __shared__ float2 sz[NT];
     __shared__ acc4 buf[NT];
     __shared__ Solve<acc> K;
@@ -845,7 +925,7 @@ __global__ void __launch_bounds__(NT) k_mgpcg(DevScene d, int second, int scale_
     // b.b now, while nothing writes the second half of the partials: the first apply phase
     // after the V-cycle does, and a block can reach it before a slower one has summed them
     const acc4 b = total(part + n, n, buf);
-    if (!vcycle<M>(d, tl, Rsrc<M>{r_cur, nullptr, 0.0f, 0.0f}, nullptr, nullptr, r_cur, sz, buf)) return;
+    if (!vcycle<M>(d, tl, Rsrc<M>{r_cur, nullptr, 0.0f, 0.0f}, nullptr, nullptr, r_cur, sz, buf, rg)) return;
     const acc tx = (acc)P->tol[0], ty = (acc)P->tol[1];
     {
         acc4 a = total(part, n, buf);
@@ -857,7 +937,7 @@ __global__ void __launch_bounds__(NT) k_mgpcg(DevScene d, int second, int scale_
     for (uint32_t it = 0; it < P->pressure_max_iters; it++) {
         if (K.done[0] && K.done[1]) break;
         for (int t = blockIdx.x; t < n; t += gridDim.x)
-            apply_tile<M>(d, t, (float)K.beta[0], (float)K.beta[1], p_old, p_new, buf);
+            apply_tile<M>(d, t, (float)K.beta[0], (float)K.beta[1], p_old, p_new, buf, rg);
         if (!grid_sync(d.K)) return;
         {
             acc4 b = total(part + n, n, buf);
@@ -865,7 +945,7 @@ __global__ void __launch_bounds__(NT) k_mgpcg(DevScene d, int second, int scale_
             __syncthreads();
         }
         Rsrc<M> R{r_cur, d.cgq, (float)K.alpha[0], (float)K.alpha[1]};
-        if (!vcycle<M>(d, tl, R, r_nxt, p_new, r_nxt, sz, buf)) return;
+        if (!vcycle<M>(d, tl, R, r_nxt, p_new, r_nxt, sz, buf, rg)) return;
         {
             acc4 a = total(part, n, buf);
             if (threadIdx.x == 0) scal_beta<acc>(K, a, tx, ty);
@@ -934,6 +1014,7 @@ template <class M>
 __global__ void __launch_bounds__(NT) k_mgpcg_batch(BatchView B, int second) {
     using acc = typename M::acc;
     using acc4 = typename M::acc4;
+    __shared__ Region rg;
     __shared__ float2 sz[NT];
     __shared__ acc4 buf[NT];
     __shared__ int s_run;
@@ -979,7 +1060,7 @@ __global__ void __launch_bounds__(NT) k_mgpcg_batch(BatchView B, int second) {
                 Rsrc<M> R{nullptr, nullptr, 0.0f, 0.0f};
                 if (l == 0) R = fused ? Rsrc<M>{parity_r(d, ir), d.cgq, (float)K.alpha[0], (float)K.alpha[1]}
                                       : Rsrc<M>{parity_r(d, ir), nullptr, 0.0f, 0.0f};
-                down_tile<M>(d, l, t, R, (l == 0 && fused) ? parity_r(d, ir + 1) : nullptr, parity_p(d, ir + 1), sz);
+                down_tile<M>(d, l, t, R, (l == 0 && fused) ? parity_r(d, ir + 1) : nullptr, parity_p(d, ir + 1), sz, rg);
             });
             if (!grid_sync(BK)) return false;
         }
@@ -998,7 +1079,7 @@ __global__ void __launch_bounds__(NT) k_mgpcg_batch(BatchView B, int second) {
                 const Zc zc{nullptr, C.off, C.w};
                 const Rsrc<M> rhs = l == 0 ? Rsrc<M>{parity_r(d, fused ? ir + 1 : 0), nullptr, 0.0f, 0.0f}
                                            : Rsrc<M>{nullptr, nullptr, 0.0f, 0.0f};
-                up_tile<M>(d, l, t, l == 0, rhs, zc, sz, buf);
+                up_tile<M>(d, l, t, l == 0, rhs, zc, sz, buf, rg);
             });
             if (!grid_sync(BK)) return false;
         }
@@ -1028,7 +1109,7 @@ __global__ void __launch_bounds__(NT) k_mgpcg_batch(BatchView B, int second) {
         for_tiles(B, 0, [&](int s, const DevScene& d, int t) {
             if (!running(s, it)) return;
             const Solve<acc>& K = KS[s];
-            apply_tile<M>(d, t, (float)K.beta[0], (float)K.beta[1], parity_p(d, it), parity_p(d, it + 1), buf);
+            apply_tile<M>(d, t, (float)K.beta[0], (float)K.beta[1], parity_p(d, it), parity_p(d, it + 1), buf, rg);
         });
         if (!grid_sync(BK)) return;
         for (int s = blockIdx.x; s < B.ns; s += gridDim.x) {

@@ -110,6 +110,8 @@ struct SproutSim {
     std::vector<float> solid_host;   // kept for nothing but the device copy's lifetime
 
     ~SproutSim() {
+        drop_part_graphs();
+        if (cap_stream) cudaStreamDestroy(cap_stream);
         if (stage_params) cudaFreeHost(stage_params);
         if (stage_mats) cudaFreeHost(stage_mats);
         if (stage_done) cudaEventDestroy(stage_done);
@@ -347,6 +349,7 @@ struct SproutSim {
         bool pchg = std::memcmp(&P, &last_params, sizeof P) != 0 || last_mats.empty();
         bool mchg = last_mats.empty() || std::memcmp(mats.data(), last_mats.data(), sizeof(DevMat) * kMaxMaterials) != 0;
         if (!pchg && !mchg) return SPROUT_OK;
+        enqueued = true;
         CUDA_TRY(cudaEventSynchronize(stage_done));
         if (pchg) {
             *stage_params = P;
@@ -428,6 +431,45 @@ struct SproutSim {
     void record_substep(cudaStream_t st) {
         for (int k = 0; k < kStages; k++) record_stage(k, st);
     }
+
+    // A batch's subset stepping replays the tank's own stages from two small graphs: the
+    // particle and grid stages (0-3) and the projection (5), captured on a private stream.
+    cudaGraphExec_t part_exec[2] = {nullptr, nullptr};
+    LaunchCfg part_cfg{};
+    bool part_ok = false;
+    cudaStream_t cap_stream = nullptr;
+    void drop_part_graphs() {
+        for (cudaGraphExec_t& e : part_exec)
+            if (e) {
+                cudaGraphExecDestroy(e);
+                e = nullptr;
+            }
+        part_ok = false;
+    }
+    int ensure_part_graphs() {
+        if (part_ok && std::memcmp(&part_cfg, &cfg, sizeof(LaunchCfg)) == 0 &&
+            std::memcmp(&part_scene, &d, sizeof(DevScene)) == 0)
+            return SPROUT_OK;
+        drop_part_graphs();
+        if (!cap_stream) CUDA_TRY(cudaStreamCreateWithFlags(&cap_stream, cudaStreamNonBlocking));
+        for (int g = 0; g < 2; g++) {
+            cudaGraph_t graph_ = nullptr;
+            CUDA_TRY(cudaStreamBeginCapture(cap_stream, cudaStreamCaptureModeThreadLocal));
+            if (g == 0)
+                for (int st = 0; st < 4; st++) record_stage(st, cap_stream);
+            else
+                record_stage(5, cap_stream);
+            CUDA_TRY(cudaStreamEndCapture(cap_stream, &graph_));
+            cudaError_t e = cudaGraphInstantiate(&part_exec[g], graph_, 0);
+            cudaGraphDestroy(graph_);
+            CUDA_TRY(e);
+        }
+        part_cfg = cfg;
+        part_scene = d;
+        part_ok = true;
+        return SPROUT_OK;
+    }
+    DevScene part_scene{};
 
     // The launch configuration for the tank as it is now; true when it changed (a captured
     // substep is then stale).
@@ -560,20 +602,32 @@ struct SproutSim {
     // What a step call does before its substeps run, on the sim's stream: the parameters and
     // material table (when they changed), the batch words of StepBuf.
     int prepare_step(uint32_t substeps, float target, const ToolState* tool) {
+        enqueued = false;
         if (n_slots == 0 || tank.rows.empty()) return fail(SPROUT_E_ARG, "step before reset (no particles)");
         int rc = derive_viscosity();
         if (rc != SPROUT_OK) return rc;
         rc = upload_tables(tool);
         if (rc != SPROUT_OK) return rc;
         if (substeps == 0) return SPROUT_OK;
-        batch_words[0] = __builtin_bit_cast(uint32_t, std::max(target, 0.0f));
-        batch_words[1] = substeps;
-        batch_words[2] = 0u;
-        CUDA_TRY(cudaMemcpyAsync(&d.S->frame_left, &batch_words[0], 4, cudaMemcpyHostToDevice, stream));
-        CUDA_TRY(cudaMemcpyAsync(&d.S->batch_steps, &batch_words[1], 8, cudaMemcpyHostToDevice, stream));
-        h2d_bytes += 12;
+        const uint32_t fl = __builtin_bit_cast(uint32_t, std::max(target, 0.0f));
+        if (!words_cached || batch_words[0] != fl || batch_words[1] != substeps) {
+            batch_words[0] = fl;
+            batch_words[1] = substeps;
+            batch_words[2] = 0u;
+            CUDA_TRY(cudaMemcpyAsync(&d.S->frame_left, &batch_words[0], 4, cudaMemcpyHostToDevice, stream));
+            CUDA_TRY(cudaMemcpyAsync(&d.S->batch_steps, &batch_words[1], 8, cudaMemcpyHostToDevice, stream));
+            h2d_bytes += 12;
+            words_cached = cache_words;
+            enqueued = true;
+        }
         return SPROUT_OK;
     }
+    // With cache_words, repeated step calls with the same substeps and target do not upload
+    // the words again: only for a fixed dt, where k_step reads neither frame_left nor the
+    // batch counters (a batch's continuous stepping of fixed-rate tanks). Off for single-sim
+    // stepping, which keeps the reference's per-call upload.
+    bool cache_words = false, words_cached = false;
+    bool enqueued = false;   // the last prepare_step put work on the sim's stream
     uint32_t batch_words[3] = {0u, 0u, 0u};
     struct SproutBatch* batch = nullptr;   // the batch this sim steps in, if any
 
@@ -684,17 +738,27 @@ struct SproutBatch {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     bool graph_ok = false;
-    // the two solves' views (all tanks; the tanks with a second solve) and their arrays
+    // the two solves' views (the stepped tanks; those with a second solve) and their device
+    // arrays, kept at a capacity and rewritten in stream order (no allocation per step)
     struct View {
         BatchView v{};
-        std::vector<void*> allocs;
+        std::vector<SproutSim*> members;
+        std::vector<DevScene> scenes;   // the members' scenes as last written
         int blocks = 0;
         size_t smem = 0;
-        std::vector<SproutSim*> members;
-        std::vector<DevScene> scenes;   // the members' scenes as captured
+        int cap = 0;
+        DevScene* ds = nullptr;
+        int *doff = nullptr, *dscale = nullptr;
+        unsigned char* dscal = nullptr;
+        SolveState* dk = nullptr;
         void release() {
-            for (void* p : allocs) cudaFree(p);
-            allocs.clear();
+            for (void* p : {(void*)ds, (void*)doff, (void*)dscale, (void*)dscal, (void*)dk})
+                if (p) cudaFree(p);
+            ds = nullptr;
+            doff = dscale = nullptr;
+            dscal = nullptr;
+            dk = nullptr;
+            cap = 0;
             members.clear();
             scenes.clear();
             v = BatchView{};
@@ -709,6 +773,8 @@ struct SproutBatch {
         second.release();
         for (cudaEvent_t e : events) cudaEventDestroy(e);
         for (cudaEvent_t e : ev_in) cudaEventDestroy(e);
+        for (cudaEvent_t e : ring)
+            if (e) cudaEventDestroy(e);
         if (ev_done) cudaEventDestroy(ev_done);
         for (cudaStream_t w : workers)
             if (w) cudaStreamDestroy(w);
@@ -769,31 +835,36 @@ struct SproutBatch {
         return SPROUT_OK;
     }
 
-    template <class T>
-    int upload(View& V, T** out, const std::vector<T>& host) {
-        void* p = nullptr;
-        size_t b = std::max<size_t>(host.size(), 1) * sizeof(T);
-        if (cudaMalloc(&p, b) != cudaSuccess) return fail(SPROUT_E_NOMEM, "batch arrays");
-        V.allocs.push_back(p);
-        if (!host.empty()) CUDA_TRY(cudaMemcpy(p, host.data(), host.size() * sizeof(T), cudaMemcpyHostToDevice));
-        h2d += b;
-        *out = static_cast<T*>(p);
-        return SPROUT_OK;
-    }
-
-    // The device arrays of a batch view over `members`.
+    // The device arrays of a batch view over `members`, written on `main`.
     int build_view(View& V, const std::vector<SproutSim*>& members) {
-        V.release();
-        V.members = members;
         const int ns = (int)members.size();
-        if (ns == 0) return SPROUT_OK;
-        std::vector<DevScene> scenes(ns);
+        V.members = members;
+        V.scenes.assign(ns, DevScene{});
+        if (ns == 0) {
+            V.v = BatchView{};
+            return SPROUT_OK;
+        }
+        if (ns > V.cap) {
+            CUDA_TRY(cudaStreamSynchronize(main));
+            const int cap = std::max(ns, 2 * V.cap);
+            for (void* p : {(void*)V.ds, (void*)V.doff, (void*)V.dscale, (void*)V.dscal, (void*)V.dk})
+                if (p) cudaFree(p);
+            bool ok = cudaMalloc(&V.ds, cap * sizeof(DevScene)) == cudaSuccess &&
+                      cudaMalloc(&V.doff, (size_t)kMaxLevels * (cap + 1) * sizeof(int)) == cudaSuccess &&
+                      cudaMalloc(&V.dscale, cap * sizeof(int)) == cudaSuccess &&
+                      cudaMalloc(&V.dscal, cap * pressure_batch_scalar_bytes()) == cudaSuccess &&
+                      cudaMalloc(&V.dk, sizeof(SolveState)) == cudaSuccess;
+            if (!ok) return fail(SPROUT_E_NOMEM, "batch arrays");
+            CUDA_TRY(cudaMemset(V.dk, 0, sizeof(SolveState)));
+            CUDA_TRY(cudaMemset(V.dscal, 0, cap * pressure_batch_scalar_bytes()));
+            V.cap = cap;
+        }
         std::vector<int> scale(ns), off((size_t)kMaxLevels * (ns + 1), 0);
         int max_tail = 0;
         size_t smem = 0;
         for (int k = 0; k < ns; k++) {
             const SproutSim* sim = members[k];
-            scenes[k] = sim->d;
+            V.scenes[k] = sim->d;
             const LaunchCfg& c = sim->cfg;
             scale[k] = (c.visc_mode == 2 && c.twice && c.viscous_warm) ? 1 : 0;
             max_tail = std::max(max_tail, sim->d.lv.tail);
@@ -808,21 +879,12 @@ struct SproutBatch {
                 o[k + 1] = o[k] + t;
             }
         }
-        int rc;
-        DevScene* ds;
-        int *doff, *dscale;
-        if ((rc = upload(V, &ds, scenes)) != SPROUT_OK) return rc;
-        if ((rc = upload(V, &doff, off)) != SPROUT_OK) return rc;
-        if ((rc = upload(V, &dscale, scale)) != SPROUT_OK) return rc;
-        std::vector<unsigned char> scal((size_t)ns * pressure_batch_scalar_bytes(), 0);
-        unsigned char* dscal;
-        if ((rc = upload(V, &dscal, scal)) != SPROUT_OK) return rc;
-        std::vector<SolveState> k0(1);
-        std::memset(k0.data(), 0, sizeof(SolveState));
-        SolveState* dk;
-        if ((rc = upload(V, &dk, k0)) != SPROUT_OK) return rc;
-        V.v = BatchView{ds, ns, doff, dscal, dscale, dk, max_tail};
-        V.scenes = scenes;
+        // pageable sources: each copy is staged before the call returns, so the vectors may go
+        CUDA_TRY(cudaMemcpyAsync(V.ds, V.scenes.data(), ns * sizeof(DevScene), cudaMemcpyHostToDevice, main));
+        CUDA_TRY(cudaMemcpyAsync(V.doff, off.data(), off.size() * sizeof(int), cudaMemcpyHostToDevice, main));
+        CUDA_TRY(cudaMemcpyAsync(V.dscale, scale.data(), ns * sizeof(int), cudaMemcpyHostToDevice, main));
+        h2d += ns * sizeof(DevScene) + off.size() * sizeof(int) + ns * sizeof(int);
+        V.v = BatchView{V.ds, ns, V.doff, V.dscal, V.dscale, V.dk, max_tail};
         V.smem = smem;
         const int mx = pressure_batch_blocks_max(device, smem, mixed);
         int total_tiles = 0;
@@ -855,15 +917,24 @@ struct SproutBatch {
     }
 
     // One substep of every tank, recorded on `main` (and the workers).
-    void record_substep() {
+    // One substep of the view's tanks. `replay`: their own stages from their small graphs
+    // (the subset stepping, launched directly); else recorded kernel by kernel (into the
+    // batch's graph).
+    void record_substep(bool replay = false) {
+        const std::vector<SproutSim*>& ms = first.members;
         size_t k = 0;
         fork(k);
-        for (size_t s = 0; s < sims.size(); s++)
-            for (int st = 0; st < 4; st++) sims[s]->record_stage(st, workers[s % kWorkers]);
+        for (size_t s = 0; s < ms.size(); s++) {
+            if (replay) cudaGraphLaunch(ms[s]->part_exec[0], workers[s % kWorkers]);
+            else for (int st = 0; st < 4; st++) ms[s]->record_stage(st, workers[s % kWorkers]);
+        }
         join(k);
         if (first.v.ns > 0) launch_pressure_batch(first.v, mixed, first.blocks, first.smem, main, 0);
         fork(k);
-        for (size_t s = 0; s < sims.size(); s++) sims[s]->record_stage(5, workers[s % kWorkers]);
+        for (size_t s = 0; s < ms.size(); s++) {
+            if (replay) cudaGraphLaunch(ms[s]->part_exec[1], workers[s % kWorkers]);
+            else ms[s]->record_stage(5, workers[s % kWorkers]);
+        }
         join(k);
         if (second.v.ns > 0) {
             for (SproutSim* sim : second.members) launch_viscosity(sim->d, sim->cfg, main, 1);
@@ -877,25 +948,56 @@ struct SproutBatch {
         }
     }
 
-    int ensure_graph() {
-        bool changed = false;
-        for (SproutSim* sim : sims) changed |= sim->refresh_cfg();
-        // a tank's device arrays may have changed since the capture (its precision buffers)
-        for (size_t k = 0; k < first.scenes.size() && k < sims.size(); k++)
-            changed |= std::memcmp(&first.scenes[k], &sims[k]->d, sizeof(DevScene)) != 0;
-        if (graph_ok && !changed) return SPROUT_OK;
-        drop_graph();
-        std::vector<SproutSim*> twice;
-        for (SproutSim* sim : sims) {
+    std::vector<SproutSim*> graph_members;   // the tanks the captured graph steps
+
+    // Launch tickets: every step call is one ticket; an event ring tells which have finished.
+    static constexpr uint64_t kRing = 256;
+    cudaEvent_t ring[kRing] = {};
+    uint64_t issued = 0, completed = 0;
+    int ticket() {
+        cudaEvent_t& e = ring[issued % kRing];
+        if (!e) CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        if (issued - completed >= kRing) {   // the slot's previous ticket must be done first
+            CUDA_TRY(cudaEventSynchronize(e));
+            completed = issued - kRing + 1;
+        }
+        CUDA_TRY(cudaEventRecord(e, main));
+        issued++;
+        return SPROUT_OK;
+    }
+    uint64_t poll_completed() {
+        while (completed < issued && cudaEventQuery(ring[completed % kRing]) == cudaSuccess) completed++;
+        cudaGetLastError();   // (a not-ready query is no error)
+        return completed;
+    }
+
+    // The checks a batch makes of its stepped tanks.
+    int check_members(const std::vector<SproutSim*>& ms, std::vector<SproutSim*>& twice) {
+        twice.clear();
+        for (SproutSim* sim : ms) {
             if (sim->cfg.visc_mode == 2 && !sim->cfg.twice)
                 return fail(SPROUT_E_UNSUPPORTED, "a batch carries the implicit viscosity only between two pressure solves (viscous_projection 1)");
             if (sim->cfg.mixed != mixed) return fail(SPROUT_E_ARG, "a batch's tanks share its precision");
             if (sim->cfg.visc_mode == 2) twice.push_back(sim);
         }
-        int rc;
+        return SPROUT_OK;
+    }
+
+    int ensure_graph() {
+        bool changed = graph_members != sims;
+        for (SproutSim* sim : sims) changed |= sim->refresh_cfg();
+        // a tank's device arrays may have changed since the capture (its precision buffers)
+        for (size_t k = 0; k < first.scenes.size() && k < sims.size() && !changed; k++)
+            changed |= std::memcmp(&first.scenes[k], &sims[k]->d, sizeof(DevScene)) != 0;
+        if (graph_ok && !changed) return SPROUT_OK;
+        drop_graph();
+        std::vector<SproutSim*> twice;
+        int rc = check_members(sims, twice);
+        if (rc != SPROUT_OK) return rc;
         if ((rc = build_view(first, sims)) != SPROUT_OK) return rc;
         if ((rc = build_view(second, twice)) != SPROUT_OK) return rc;
         CUDA_TRY(cudaStreamSynchronize(main));
+        graph_members = sims;
         CUDA_TRY(cudaStreamBeginCapture(main, cudaStreamCaptureModeThreadLocal));
         record_substep();
         cudaError_t e = cudaStreamEndCapture(main, &graph);
@@ -922,7 +1024,42 @@ struct SproutBatch {
         for (uint32_t k = 0; k < substeps; k++) CUDA_TRY(cudaGraphLaunch(exec, main));
         CUDA_TRY(cudaEventRecord(ev_done, main));
         for (SproutSim* sim : sims) CUDA_TRY(cudaStreamWaitEvent(sim->stream, ev_done, 0));
-        return SPROUT_OK;
+        return ticket();
+    }
+
+    // One substep of the members at `idx` only, launched directly (no graph): the serving
+    // loop's continuous batching, where the stepped set changes from launch to launch.
+    int step_subset(const uint32_t* idx, uint32_t n) {
+        if (n == 0) return SPROUT_OK;
+        std::vector<SproutSim*> ms;
+        ms.reserve(n);
+        for (uint32_t k = 0; k < n; k++) {
+            if (idx[k] >= sims.size()) return fail(SPROUT_E_ARG, "batch member index out of range");
+            SproutSim* sim = sims[idx[k]];
+            if (std::find(ms.begin(), ms.end(), sim) != ms.end()) return fail(SPROUT_E_ARG, "a member listed twice");
+            // with a fixed dt the batch words are not read (k_step), so unchanged ones stay
+            sim->cache_words = sim->params.fixed_hz > 0.0f;
+            int rc = sim->prepare_step(1, sim->dt_estimate(), nullptr);
+            if (rc != SPROUT_OK) return rc;
+            sim->refresh_cfg();
+            if ((rc = sim->ensure_part_graphs()) != SPROUT_OK) return rc;
+            if (sim->enqueued) {
+                CUDA_TRY(cudaEventRecord(ev_in[idx[k]], sim->stream));
+                CUDA_TRY(cudaStreamWaitEvent(main, ev_in[idx[k]], 0));
+            }
+            ms.push_back(sim);
+        }
+        std::vector<SproutSim*> twice;
+        int rc = check_members(ms, twice);
+        if (rc != SPROUT_OK) return rc;
+        if ((rc = build_view(first, ms)) != SPROUT_OK) return rc;
+        if ((rc = build_view(second, twice)) != SPROUT_OK) return rc;
+        graph_ok = false;   // the views no longer hold the graph's tanks
+        record_substep(true);
+        CUDA_TRY(cudaGetLastError());
+        CUDA_TRY(cudaEventRecord(ev_done, main));
+        for (SproutSim* sim : ms) CUDA_TRY(cudaStreamWaitEvent(sim->stream, ev_done, 0));
+        return ticket();
     }
 
     int check_error() {
@@ -1059,6 +1196,11 @@ int sprout_sim_destroy(SproutSim* sim) {
     return SPROUT_OK;
 }
 
+int sprout_device_memory(size_t* free_bytes, size_t* total_bytes) {
+    if (!free_bytes || !total_bytes) return fail(SPROUT_E_ARG, "null argument");
+    CUDA_TRY(cudaMemGetInfo(free_bytes, total_bytes));
+    return SPROUT_OK;
+}
 int sprout_batch_create(SproutBatch** out) {
     if (!out) return fail(SPROUT_E_ARG, "null argument");
     SproutBatch* b = new SproutBatch();
@@ -1095,6 +1237,16 @@ int sprout_batch_set_precision(SproutBatch* b, int mode) {
 int sprout_batch_step(SproutBatch* b, uint32_t substeps) {
     if (!b) return fail(SPROUT_E_ARG, "null argument");
     return b->step(substeps);
+}
+int sprout_batch_step_subset(SproutBatch* b, const uint32_t* members, uint32_t n) {
+    if (!b || (!members && n > 0)) return fail(SPROUT_E_ARG, "null argument");
+    return b->step_subset(members, n);
+}
+int sprout_batch_tickets(SproutBatch* b, uint64_t* issued, uint64_t* completed) {
+    if (!b || !issued || !completed) return fail(SPROUT_E_ARG, "null argument");
+    *completed = b->poll_completed();
+    *issued = b->issued;
+    return SPROUT_OK;
 }
 int sprout_batch_sync(SproutBatch* b) {
     if (!b) return fail(SPROUT_E_ARG, "null argument");
