@@ -169,6 +169,15 @@ int sprout_sim_profile(SproutSim* sim, uint32_t substeps, float* ms);
  * n < 8 the stages past n - 1 are added to ms[5]. Blocking. */
 int sprout_sim_profile_passes(SproutSim* sim, float* ms, uint32_t n);
 
+/* ---- tracing of the persistent solvers' phases ---------------------------------------
+ * No counterpart in the reference (its profile_passes times whole dispatches). enable with
+ * rows > 0 keeps the last `rows` grid-barrier generations of the sim's pressure and viscosity
+ * kernels (rows == 0: off). read copies up to cap words (blocking): rows of *cols words, per
+ * block the device time (ns, %globaltimer) it reached that barrier, in the last column the
+ * time block 0 left it; *words = rows x cols. */
+int sprout_sim_trace_enable(SproutSim* sim, uint32_t rows);
+int sprout_sim_trace_read(SproutSim* sim, unsigned long long* out, size_t cap, size_t* words, uint32_t* cols);
+
 /* ---- precision of the pressure solve -------------------------------------------------
  * No counterpart in the reference (it solves in FP32 only). mode 0: the reference's
  * arithmetic, FP32 throughout (the default). mode 1: mixed precision: the multigrid

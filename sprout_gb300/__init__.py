@@ -42,7 +42,8 @@ EXPORTS = [
     "sprout_sim_profile_passes", "sprout_pressure_solve_static", "sprout_sim_set_precision",
     "sprout_batch_create", "sprout_batch_destroy", "sprout_batch_add", "sprout_batch_remove", "sprout_batch_size",
     "sprout_batch_set_precision", "sprout_batch_step", "sprout_batch_sync", "sprout_batch_profile",
-    "sprout_batch_step_subset", "sprout_batch_tickets", "sprout_device_memory",
+    "sprout_batch_step_subset", "sprout_batch_tickets", "sprout_device_memory", "sprout_sim_trace_enable",
+    "sprout_sim_trace_read",
 ]
 
 STAGES = ["advance", "sort", "p2g", "grid", "pressure", "project", "viscosity", "project2"]
@@ -138,6 +139,8 @@ def lib() -> C.CDLL:
         "sprout_batch_step_subset": ([V, P(C.c_uint32), C.c_uint32], C.c_int),
         "sprout_batch_tickets": ([V, P(C.c_uint64), P(C.c_uint64)], C.c_int),
         "sprout_device_memory": ([P(C.c_size_t), P(C.c_size_t)], C.c_int),
+        "sprout_sim_trace_enable": ([V, C.c_uint32], C.c_int),
+        "sprout_sim_trace_read": ([V, V, C.c_size_t, P(C.c_size_t), P(C.c_uint32)], C.c_int),
         "sprout_pressure_solve_static": ([C.c_uint32, C.c_uint32, V, V, V, V, C.c_float, C.c_float, C.c_uint32, V,
                                           P(C.c_uint32), P(C.c_float)], C.c_int),
     }
@@ -309,6 +312,19 @@ class FluidSim:
         BF16 matrices, FP64 dot products and convergence test, FP64 true residual at the end)."""
         m = {"plain": 0, "mixed": 1}.get(mode, mode)
         _check(lib().sprout_sim_set_precision(self._h, int(m)))
+
+    def trace_on(self, rows: int = 4096):
+        """Turns the solvers' phase trace on (rows: barrier generations kept; 0: off)."""
+        _check(lib().sprout_sim_trace_enable(self._h, rows))
+
+    def trace(self) -> np.ndarray:
+        """The phase trace so far: (rows, blocks + 1) device ns, 0 where never written."""
+        w, c = C.c_size_t(), C.c_uint32()
+        _check(lib().sprout_sim_trace_read(self._h, None, 0, C.byref(w), C.byref(c)))
+        out = np.zeros(w.value, np.uint64)
+        if w.value:
+            _check(lib().sprout_sim_trace_read(self._h, out.ctypes.data, w.value, C.byref(w), C.byref(c)))
+        return out.reshape(-1, max(c.value, 1))
 
     def profile_passes(self) -> dict:
         """One substep stage by stage: device ms per stage (STAGES)."""

@@ -71,6 +71,8 @@ struct DevScene {
     float* mgd;
     float2 *mgx, *mgz, *mgr, *mgr2, *cgp, *cgp2, *cgq;
     uint32_t* ptile;
+    uint32_t* plist;    // per level (at lv.toff), the tiles with pressure unknowns in order
+    uint32_t* pcount;   // per level, how many (kMaxLevels)
     float4* partials;   // 2 x nwg
     int nwg;
     Levels lv;

@@ -99,6 +99,11 @@ struct SolveState {
     uint32_t err_arrived;          // on a barrier timeout: blocks that had arrived, of
     uint32_t err_blocks;           // the grid's blocks (diagnostics)
     float p_true_res, p_true_res_max;   // mixed precision: |b - A x| / |b| in FP64, last / max
+    // phase trace (off when null): row g % trace_rows of trace_cols words holds, per block,
+    // the %globaltimer ns at which it reached the barrier of generation g; the last column
+    // the time block 0 left it
+    unsigned long long* trace;
+    uint32_t trace_rows, trace_cols;
 };
 
 // The multigrid hierarchy (Levels, src/sim/mod.rs:714-753).

@@ -52,6 +52,7 @@ struct BatchView {
     const int* scale;         // per scene, the warm-start mode of cg_scale (0 or 1)
     SolveState* K;            // the batch's grid barrier and error word
     int max_tail;             // the deepest tail level over the scenes
+    int* aoff;                // the same prefix sums over the scenes' active tiles (the kernel fills it)
 };
 // The batched pressure solve: `second` for the solve after the implicit viscosity.
 cudaError_t launch_pressure_batch(const BatchView& B, bool mixed, int blocks, size_t smem, cudaStream_t st, int second);

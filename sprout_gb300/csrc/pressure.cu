@@ -286,6 +286,7 @@ struct Tail {
     float* dg;
     float2* x;
     float2* r;
+    uint8_t* m;   // per cell: bit q set when neighbour q is an unknown, bit 4 when the cell is
     int base, T, nf;
 };
 
@@ -302,6 +303,7 @@ DEV Tail make_tail(const DevScene& d, unsigned char* smem) {
     tl.x = reinterpret_cast<float2*>(tl.a + tl.T);
     tl.r = tl.x + tl.T;
     tl.dg = reinterpret_cast<float*>(tl.r + tl.T);
+    tl.m = reinterpret_cast<uint8_t*>(tl.dg + tl.T);
     return tl;
 }
 
@@ -345,6 +347,18 @@ DEV void tail_setup(const DevScene& d, const Tail& tl, bool writer) {
         }
         __syncthreads();
     }
+    // the unknowns around every tail cell, for the sweeps
+    for (int l = d.lv.tail; l < d.lv.n; l++) {
+        const Lv L = lev(d.lv, l);
+        const int o = L.off - tl.base;
+        for (int t = threadIdx.x; t < L.w * L.h; t += NT) {
+            const int x = t % L.w, y = t / L.w;
+            uint32_t m = tl.dg[o + t] > 0.0f ? 16u : 0u;
+            for (int q = 0; q < 4; q++) m |= t_unknown(tl, L, x + NBX[q], y + NBY[q]) ? (1u << q) : 0u;
+            tl.m[o + t] = (uint8_t)m;
+        }
+    }
+    __syncthreads();
 }
 
 // Where a way up reads the coarse level's finished values: this block's shared copy of the
@@ -385,9 +399,12 @@ DEV void down_tile(const DevScene& d, int l, int t, const Rsrc<M>& R, float2* r_
     const Lv F = lev(d.lv, l), C = lev(d.lv, l + 1);
     const int tx_n = tiles_x(F);
     const int lx = threadIdx.x & 15, ly = threadIdx.x >> 4;
-    if (d.ptile[F.toff + t] == 0u) return;
     const int ox = (t % tx_n) * 16, oy = (t / tx_n) * 16;
-    for (int k = threadIdx.x; k < RN; k += NT) {
+    // every load of the region issued at once (none waits on another), then masked
+#pragma unroll
+    for (int j = 0; j < (RN + NT - 1) / NT; j++) {
+        const int k = threadIdx.x + j * NT;
+        if (k >= RN) break;
         const int x = ox - RH + k % RW, y = oy - RH + k / RW;
         float dd = 0.0f;
         float4 aa = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
@@ -395,11 +412,12 @@ DEV void down_tile(const DevScene& d, int l, int t, const Rsrc<M>& R, float2* r_
         if (l_inside(F, x, y)) {
             const int i = l_at(F, x, y);
             dd = M::Dg(d, i);
-            if (dd > 0.0f) {
-                aa = M::A(d, i);
-                rr = R.at(d, i);
-            } else {
+            aa = M::A(d, i);
+            rr = R.at(d, i);
+            if (!(dd > 0.0f)) {
                 dd = 0.0f;
+                aa = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                rr = make_float2(0.0f, 0.0f);
             }
         }
         rg.dg[k] = dd;
@@ -488,12 +506,11 @@ DEV void up_tile(const DevScene& d, int l, int t, bool flag, const Rsrc<M>& rhs,
     const int tx_n = tiles_x(F);
     const int lx = threadIdx.x & 15, ly = threadIdx.x >> 4;
     typename M::acc4* part = M::part(d);
-    if (d.ptile[F.toff + t] == 0u) {
-        if (flag && threadIdx.x == 0) part[t] = M::a4(0, 0, 0, 0);
-        return;
-    }
     const int ox = (t % tx_n) * 16, oy = (t / tx_n) * 16;
-    for (int k = threadIdx.x; k < RN; k += NT) {
+#pragma unroll
+    for (int j = 0; j < (RN + NT - 1) / NT; j++) {
+        const int k = threadIdx.x + j * NT;
+        if (k >= RN) break;
         const int x = ox - RH + k % RW, y = oy - RH + k / RW;
         float dd = 0.0f;
         float4 aa = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
@@ -501,13 +518,14 @@ DEV void up_tile(const DevScene& d, int l, int t, bool flag, const Rsrc<M>& rhs,
         if (l_inside(F, x, y)) {
             const int i = l_at(F, x, y);
             dd = M::Dg(d, i);
-            if (dd > 0.0f) {
-                aa = M::A(d, i);
-                r = rhs.at(d, i);
-                xm = M::X(d, i);
-                zcv = coarse_z<M>(d, zc, x, y);
-            } else {
+            aa = M::A(d, i);
+            r = rhs.at(d, i);
+            xm = M::X(d, i);
+            zcv = coarse_z<M>(d, zc, x, y);
+            if (!(dd > 0.0f)) {
                 dd = 0.0f;
+                aa = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                r = xm = zcv = make_float2(0.0f, 0.0f);
             }
         }
         rg.dg[k] = dd;
@@ -595,12 +613,13 @@ DEV void phase_tail(const DevScene& d, const Tail& tl, bool writer) {
             }
             float2 sum = tl.r[s];
             if (!zero) {
-                float4 w = tl.a[s];
+                const float4 w = tl.a[s];
+                const uint32_t m = tl.m[s];
+                const int step[4] = {-1, 1, -L.w, L.w};
                 for (int q = 0; q < 4; q++) {
-                    int nx = x + NBX[q], ny = y + NBY[q];
-                    if (t_unknown(tl, L, nx, ny)) {
+                    if (m & (1u << q)) {
                         float wd = wcomp(w, q);
-                        float2 xn = tl.x[o + ny * L.w + nx];
+                        float2 xn = tl.x[s + step[q]];
                         sum.x += wd * xn.x;
                         sum.y += wd * xn.y;
                     }
@@ -618,19 +637,21 @@ DEV void phase_tail(const DevScene& d, const Tail& tl, bool writer) {
         for (int t = threadIdx.x; t < C.w * C.h; t += NT) {
             int ccx = t % C.w, ccy = t / C.w;
             float sumx = 0.0f, sumy = 0.0f;
+            const int step[4] = {-1, 1, -L.w, L.w};
             for (int k = 0; k < 4; k++) {
                 int cx = 2 * ccx + (k & 1), cy = 2 * ccy + (k >> 1);
-                if (!t_unknown(tl, L, cx, cy)) continue;
+                if (!l_inside(L, cx, cy)) continue;
                 int s = o + cy * L.w + cx;
+                const uint32_t m = tl.m[s];
+                if (!(m & 16u)) continue;
                 float4 w = tl.a[s];
                 float Ds = tl.dg[s];
                 float2 xs = tl.x[s];
                 float azx = Ds * xs.x, azy = Ds * xs.y;
                 for (int q = 0; q < 4; q++) {
-                    int nx = cx + NBX[q], ny = cy + NBY[q];
-                    if (t_unknown(tl, L, nx, ny)) {
+                    if (m & (1u << q)) {
                         float wd = wcomp(w, q);
-                        float2 xn = tl.x[o + ny * L.w + nx];
+                        float2 xn = tl.x[s + step[q]];
                         azx -= wd * xn.x;
                         azy -= wd * xn.y;
                     }
@@ -659,9 +680,10 @@ DEV void phase_tail(const DevScene& d, const Tail& tl, bool writer) {
             if (D <= 0.0f) continue;
             float4 w = tl.a[s];
             float2 sum = tl.r[s];
+            const uint32_t m = tl.m[s];
             for (int q = 0; q < 4; q++) {
                 int nx = x + NBX[q], ny = y + NBY[q];
-                if (!t_unknown(tl, F, nx, ny)) continue;
+                if (!(m & (1u << q))) continue;
                 float wd = wcomp(w, q);
                 float2 xn = tl.x[o + ny * F.w + nx];
                 float2 xc = tl.x[oc + (ny >> 1) * C.w + (nx >> 1)];
@@ -677,18 +699,70 @@ DEV void phase_tail(const DevScene& d, const Tail& tl, bool writer) {
         for (int s = threadIdx.x; s < tl.nf; s += NT) M::setZ(d, tl.base + s, tl.x[s]);
 }
 
+// The active-tile lists of levels 0 .. tail - 1 of scene d (one block), from ptile.
+DEV void build_plists(const DevScene& d) {
+    for (int l = 0; l < d.lv.tail; l++) {
+        const Lv L = lev(d.lv, l);
+        compact_flags(d.ptile + L.toff, tiles_x(L) * tiles_y(L), d.plist + L.toff, d.pcount + l);
+    }
+}
+
+// Level-0 tiles without unknowns keep zero partial sums through the solve (their tile
+// bodies are never run): set them once at its start, every half and precision.
+template <class M>
+DEV void zero_inactive_tile(const DevScene& d, int t) {
+    if (threadIdx.x != 0 || d.ptile[t] != 0u) return;
+    const int n = d.nwg;
+    M::part(d)[t] = M::a4(0, 0, 0, 0);
+    M::part(d)[n + t] = M::a4(0, 0, 0, 0);
+    if (M::kMixed) d.partials64[t] = Dbl4{0.0, 0.0, 0.0, 0.0};
+}
+
+// This block's share of the active-tile lists, read once per solve into shared memory:
+// entry k of level l is work item blockIdx.x + k x gridDim.x (a tile index; in a batch the
+// scene in the high 16 bits), so a phase starts on its tiles without first waiting for
+// global memory. Items past kCachePer, or on levels past kCacheLevels, are read as before.
+constexpr int kCacheLevels = 8, kCachePer = 32;
+struct TileCache {
+    uint32_t cnt[kCacheLevels];
+    uint32_t item[kCacheLevels][kCachePer];
+};
+
+DEV void fill_cache(const DevScene& d, TileCache& tc) {
+    for (int l = 0; l < kCacheLevels && l < d.lv.tail; l++) {
+        const uint32_t cnt = *(volatile uint32_t*)&d.pcount[l];
+        const uint32_t* list = d.plist + d.lv.toff[l];
+        if (threadIdx.x == 0) tc.cnt[l] = cnt;
+        for (int k = threadIdx.x; k < kCachePer; k += NT) {
+            const uint32_t j = blockIdx.x + (uint32_t)k * gridDim.x;
+            if (j < cnt) tc.item[l][k] = list[j];
+        }
+    }
+    __syncthreads();
+}
+
+// For every active tile of level l of scene d, in this block's share of the list.
+template <class F>
+DEV void for_active(const DevScene& d, int l, const TileCache& tc, F&& f) {
+    const bool cached = l < kCacheLevels;
+    const uint32_t cnt = cached ? tc.cnt[l] : *(volatile uint32_t*)&d.pcount[l];
+    const uint32_t* list = d.plist + d.lv.toff[l];
+    int k = 0;
+    for (uint32_t j = blockIdx.x; j < cnt; j += gridDim.x, k++)
+        f((int)((cached && k < kCachePer) ? tc.item[l][k] : list[j]));
+}
+
 // One V-cycle of one scene: level 0's right-hand side through R (fused with the CG update
 // when R.q is set), result in mgz of level 0, partials of r.z and r.r. Returns false on a
 // barrier timeout.
 template <class M>
 DEV bool vcycle(const DevScene& d, const Tail& tl, const Rsrc<M>& R, float2* r_out, const float2* p, const float2* r_new,
-                float2* sz, typename M::acc4* buf, Region& rg) {
+                float2* sz, typename M::acc4* buf, Region& rg, const TileCache& tc) {
     const int tail = d.lv.tail;
     for (int l = 0; l < tail; l++) {
         Rsrc<M> Rl = R;
         if (l > 0) Rl = Rsrc<M>{nullptr, nullptr, 0.0f, 0.0f};
-        const int T = level_tiles(d, l);
-        for (int t = blockIdx.x; t < T; t += gridDim.x) down_tile<M>(d, l, t, Rl, l == 0 ? r_out : nullptr, p, sz, rg);
+        for_active(d, l, tc, [&](int t) { down_tile<M>(d, l, t, Rl, l == 0 ? r_out : nullptr, p, sz, rg); });
         if (!grid_sync(d.K)) return false;
     }
     phase_tail<M>(d, tl, blockIdx.x == 0);
@@ -696,8 +770,7 @@ DEV bool vcycle(const DevScene& d, const Tail& tl, const Rsrc<M>& R, float2* r_o
         const Lv C = lev(d.lv, l + 1);
         const Zc zc{(l == tail - 1) ? tl.x : nullptr, C.off, C.w};
         const Rsrc<M> rhs = l == 0 ? Rsrc<M>{r_new, nullptr, 0.0f, 0.0f} : Rsrc<M>{nullptr, nullptr, 0.0f, 0.0f};
-        const int T = level_tiles(d, l);
-        for (int t = blockIdx.x; t < T; t += gridDim.x) up_tile<M>(d, l, t, l == 0, rhs, zc, sz, buf, rg);
+        for_active(d, l, tc, [&](int t) { up_tile<M>(d, l, t, l == 0, rhs, zc, sz, buf, rg); });
         if (!grid_sync(d.K)) return false;
     }
     return true;
@@ -753,12 +826,11 @@ DEV void apply_tile(const DevScene& d, int t, float b0, float b1, const float2* 
         float2 po = p_old[i];
         return make_float2(b0 != 0.0f ? z.x + b0 * po.x : z.x, b1 != 0.0f ? z.y + b1 * po.y : z.y);
     };
-    if (d.ptile[F.toff + t] == 0u) {
-        if (threadIdx.x == 0) part[t] = M::a4(0, 0, 0, 0);
-        return;
-    }
     const int ox = (t % tx_n) * 16, oy = (t / tx_n) * 16;
-    for (int k = threadIdx.x; k < RN; k += NT) {
+#pragma unroll
+    for (int j = 0; j < (RN + NT - 1) / NT; j++) {
+        const int k = threadIdx.x + j * NT;
+        if (k >= RN) break;
         const int x = ox - RH + k % RW, y = oy - RH + k / RW;
         const int kx = k % RW, ky = k / RW;
         if (kx == 0 || ky == 0 || kx == RW - 1 || ky == RW - 1) continue;   // one ring is enough
@@ -767,8 +839,11 @@ DEV void apply_tile(const DevScene& d, int t, float b0, float b1, const float2* 
         if (l_inside(F, x, y)) {
             const int i = l_at(F, x, y);
             dd = d.mgd[i];
-            if (dd > 0.0f) pp = direction(i);
-            else dd = 0.0f;
+            pp = direction(i);
+            if (!(dd > 0.0f)) {
+                dd = 0.0f;
+                pp = make_float2(0.0f, 0.0f);
+            }
         }
         rg.dg[k] = dd;
         rg.u[k] = pp;
@@ -900,6 +975,7 @@ __global__ void __launch_bounds__(NT) k_mgpcg(DevScene d, int second, int scale_
     using acc = typename M::acc;
     using acc4 = typename M::acc4;
     __shared__ Region rg;
+    __shared__ TileCache tc;
     __shared__ float2 sz[NT];
     __shared__ acc4 buf[NT];
     __shared__ Solve<acc> K;
@@ -917,15 +993,20 @@ __global__ void __launch_bounds__(NT) k_mgpcg(DevScene d, int second, int scale_
         }
         if (!grid_sync(d.K)) return;
     }
+    // the active-tile lists (ptile is final now) and the inactive tiles' zero partial sums
+    if (blockIdx.x == 0) build_plists(d);
+    for (int t = blockIdx.x; t < n; t += gridDim.x) zero_inactive_tile<M>(d, t);
+    if (!grid_sync(d.K)) return;
+    fill_cache(d, tc);
     tail_setup<M>(d, tl, blockIdx.x == 0);
     float2* r_cur = d.mgr;    // level 0 of mgr: the residual, double-buffered with mgr2
     float2* r_nxt = d.mgr2;
-    for (int t = blockIdx.x; t < n; t += gridDim.x) residual_tile<M>(d, t, r_cur, buf, false);
+    for_active(d, 0, tc, [&](int t) { residual_tile<M>(d, t, r_cur, buf, false); });
     if (!grid_sync(d.K)) return;
     // b.b now, while nothing writes the second half of the partials: the first apply phase
     // after the V-cycle does, and a block can reach it before a slower one has summed them
     const acc4 b = total(part + n, n, buf);
-    if (!vcycle<M>(d, tl, Rsrc<M>{r_cur, nullptr, 0.0f, 0.0f}, nullptr, nullptr, r_cur, sz, buf, rg)) return;
+    if (!vcycle<M>(d, tl, Rsrc<M>{r_cur, nullptr, 0.0f, 0.0f}, nullptr, nullptr, r_cur, sz, buf, rg, tc)) return;
     const acc tx = (acc)P->tol[0], ty = (acc)P->tol[1];
     {
         acc4 a = total(part, n, buf);
@@ -936,8 +1017,7 @@ __global__ void __launch_bounds__(NT) k_mgpcg(DevScene d, int second, int scale_
     float2* p_new = d.cgp2;
     for (uint32_t it = 0; it < P->pressure_max_iters; it++) {
         if (K.done[0] && K.done[1]) break;
-        for (int t = blockIdx.x; t < n; t += gridDim.x)
-            apply_tile<M>(d, t, (float)K.beta[0], (float)K.beta[1], p_old, p_new, buf, rg);
+        for_active(d, 0, tc, [&](int t) { apply_tile<M>(d, t, (float)K.beta[0], (float)K.beta[1], p_old, p_new, buf, rg); });
         if (!grid_sync(d.K)) return;
         {
             acc4 b = total(part + n, n, buf);
@@ -945,7 +1025,7 @@ __global__ void __launch_bounds__(NT) k_mgpcg(DevScene d, int second, int scale_
             __syncthreads();
         }
         Rsrc<M> R{r_cur, d.cgq, (float)K.alpha[0], (float)K.alpha[1]};
-        if (!vcycle<M>(d, tl, R, r_nxt, p_new, r_nxt, sz, buf, rg)) return;
+        if (!vcycle<M>(d, tl, R, r_nxt, p_new, r_nxt, sz, buf, rg, tc)) return;
         {
             acc4 a = total(part, n, buf);
             if (threadIdx.x == 0) scal_beta<acc>(K, a, tx, ty);
@@ -960,7 +1040,7 @@ __global__ void __launch_bounds__(NT) k_mgpcg(DevScene d, int second, int scale_
     }
     double true_rel = -1.0;
     if constexpr (M::kMixed) {
-        for (int t = blockIdx.x; t < n; t += gridDim.x) true_residual_tile(d, t, d.partials64, reinterpret_cast<Dbl4*>(buf));
+        for_active(d, 0, tc, [&](int t) { true_residual_tile(d, t, d.partials64, reinterpret_cast<Dbl4*>(buf)); });
         if (!grid_sync(d.K)) return;
         const Dbl4 t4 = total(d.partials64, n, reinterpret_cast<Dbl4*>(buf));
         true_rel = t4.y > 0.0 ? sqrt(t4.x / t4.y) : 0.0;
@@ -1005,6 +1085,39 @@ DEV void for_tiles(const BatchView& B, int l, F&& f) {
     }
 }
 
+// For every active tile of level l over the batch's scenes (B.aoff: the prefix sums of the
+// scenes' active-tile counts, built at the solve's start).
+DEV uint32_t batch_item(const BatchView& B, int l, int g) {
+    const int* o = B.aoff + l * (B.ns + 1);
+    const int s = scene_of(o, B.ns, g);
+    const DevScene& d = B.scenes[s];
+    return ((uint32_t)s << 16) | d.plist[d.lv.toff[l] + (g - o[s])];
+}
+
+DEV void fill_cache_b(const BatchView& B, TileCache& tc) {
+    for (int l = 0; l < kCacheLevels && l < B.max_tail; l++) {
+        const int N = *(volatile const int*)&B.aoff[l * (B.ns + 1) + B.ns];
+        if (threadIdx.x == 0) tc.cnt[l] = (uint32_t)N;
+        for (int k = threadIdx.x; k < kCachePer; k += NT) {
+            const int g = blockIdx.x + k * gridDim.x;
+            if (g < N) tc.item[l][k] = batch_item(B, l, g);
+        }
+    }
+    __syncthreads();
+}
+
+template <class F>
+DEV void for_active_b(const BatchView& B, int l, const TileCache& tc, F&& f) {
+    const bool cached = l < kCacheLevels;
+    const int N = cached ? (int)tc.cnt[l] : *(volatile const int*)&B.aoff[l * (B.ns + 1) + B.ns];
+    int k = 0;
+    for (int g = blockIdx.x; g < N; g += gridDim.x, k++) {
+        const uint32_t it = (cached && k < kCachePer) ? tc.item[l][k] : batch_item(B, l, g);
+        const int s = (int)(it >> 16);
+        f(s, B.scenes[s], (int)(it & 0xffffu));
+    }
+}
+
 DEV float2* parity_r(const DevScene& d, int it) { return (it & 1) ? d.mgr2 : d.mgr; }
 DEV float2* parity_p(const DevScene& d, int it) { return (it & 1) ? d.cgp2 : d.cgp; }
 
@@ -1015,6 +1128,7 @@ __global__ void __launch_bounds__(NT) k_mgpcg_batch(BatchView B, int second) {
     using acc = typename M::acc;
     using acc4 = typename M::acc4;
     __shared__ Region rg;
+    __shared__ TileCache tc;
     __shared__ float2 sz[NT];
     __shared__ acc4 buf[NT];
     __shared__ int s_run;
@@ -1035,7 +1149,26 @@ __global__ void __launch_bounds__(NT) k_mgpcg_batch(BatchView B, int second) {
         }
         if (!grid_sync(BK)) return;
     }
-    for_tiles(B, 0, [&](int s, const DevScene& d, int t) { residual_tile<M>(d, t, d.mgr, buf, false); });
+    // every scene's active-tile lists (one block each) and the inactive tiles' zero partials
+    for (int s = blockIdx.x; s < B.ns; s += gridDim.x) build_plists(B.scenes[s]);
+    for_tiles(B, 0, [&](int s, const DevScene& d, int t) { zero_inactive_tile<M>(d, t); });
+    if (!grid_sync(BK)) return;
+    // ... and their prefix sums per level over the scenes
+    if (blockIdx.x == 0) {
+        for (int l = threadIdx.x; l < B.max_tail; l += NT) {
+            int* o = B.aoff + l * (B.ns + 1);
+            int acc_ = 0;
+            o[0] = 0;
+            for (int k = 0; k < B.ns; k++) {
+                const DevScene& d = B.scenes[k];
+                acc_ += l < d.lv.tail ? (int)d.pcount[l] : 0;
+                o[k + 1] = acc_;
+            }
+        }
+    }
+    if (!grid_sync(BK)) return;
+    fill_cache_b(B, tc);
+    for_active_b(B, 0, tc, [&](int s, const DevScene& d, int t) { residual_tile<M>(d, t, d.mgr, buf, false); });
     if (!grid_sync(BK)) return;
     // b.b of each scene (before the first apply phase reuses those partials)
     for (int s = blockIdx.x; s < B.ns; s += gridDim.x) {
@@ -1054,7 +1187,7 @@ __global__ void __launch_bounds__(NT) k_mgpcg_batch(BatchView B, int second) {
         const bool fused = it >= 0;
         const int ir = fused ? it : 0;
         for (int l = 0; l < B.max_tail; l++) {
-            for_tiles(B, l, [&](int s, const DevScene& d, int t) {
+            for_active_b(B, l, tc, [&](int s, const DevScene& d, int t) {
                 if (l >= d.lv.tail || (fused && !running(s, it))) return;
                 const Solve<acc>& K = KS[s];
                 Rsrc<M> R{nullptr, nullptr, 0.0f, 0.0f};
@@ -1073,7 +1206,7 @@ __global__ void __launch_bounds__(NT) k_mgpcg_batch(BatchView B, int second) {
         }
         if (!grid_sync(BK)) return false;
         for (int l = B.max_tail - 1; l >= 0; l--) {
-            for_tiles(B, l, [&](int s, const DevScene& d, int t) {
+            for_active_b(B, l, tc, [&](int s, const DevScene& d, int t) {
                 if (l >= d.lv.tail || (fused && !running(s, it))) return;
                 const Lv C = lev(d.lv, l + 1);
                 const Zc zc{nullptr, C.off, C.w};
@@ -1106,7 +1239,7 @@ __global__ void __launch_bounds__(NT) k_mgpcg_batch(BatchView B, int second) {
         }
         __syncthreads();
         if (!s_run) break;
-        for_tiles(B, 0, [&](int s, const DevScene& d, int t) {
+        for_active_b(B, 0, tc, [&](int s, const DevScene& d, int t) {
             if (!running(s, it)) return;
             const Solve<acc>& K = KS[s];
             apply_tile<M>(d, t, (float)K.beta[0], (float)K.beta[1], parity_p(d, it), parity_p(d, it + 1), buf, rg);
@@ -1131,7 +1264,7 @@ __global__ void __launch_bounds__(NT) k_mgpcg_batch(BatchView B, int second) {
         if (!grid_sync(BK)) return;
     }
     if constexpr (M::kMixed) {
-        for_tiles(B, 0, [&](int s, const DevScene& d, int t) {
+        for_active_b(B, 0, tc, [&](int s, const DevScene& d, int t) {
             true_residual_tile(d, t, d.partials64, reinterpret_cast<Dbl4*>(buf));
         });
         if (!grid_sync(BK)) return;
@@ -1150,7 +1283,7 @@ __global__ void __launch_bounds__(NT) k_mgpcg_batch(BatchView B, int second) {
 
 size_t pressure_smem(const Levels& lv) {
     int T = lv.off[lv.n - 1] + lv.w[lv.n - 1] * lv.h[lv.n - 1] - lv.off[lv.tail];
-    return (size_t)T * (sizeof(float4) + 2 * sizeof(float2) + sizeof(float));
+    return ((size_t)T * (sizeof(float4) + 2 * sizeof(float2) + sizeof(float) + 1) + 15) / 16 * 16;
 }
 
 namespace {
@@ -1240,6 +1373,7 @@ constexpr size_t kStaticBytes =
     align256((size_t)kStaticMaxCells * sizeof(float4)) +          // rhs as the engine lays it out
     align256((size_t)kStaticMaxCells * sizeof(float)) +           // viscous part of the warm start
     align256(kStaticTiles * sizeof(uint32_t)) +                   // tile flags of every level
+    align256(kStaticTiles * sizeof(uint32_t)) + align256(kMaxLevels * sizeof(uint32_t)) +   // active-tile lists
     align256(2 * ((size_t)kStaticMaxCells / 256 + 64) * sizeof(float4)) +   // per-tile partial sums
     align256(kStaticTotal * sizeof(float4)) + align256(kStaticTotal * sizeof(float)) +
     3 * align256(kStaticTotal * sizeof(float2)) + 4 * align256((size_t)kStaticMaxCells * sizeof(float2));
@@ -1379,6 +1513,8 @@ extern "C" int sprout_pressure_solve_static(uint32_t w, uint32_t h, const float*
     d.prhs = reinterpret_cast<float4*>(take((size_t)kStaticMaxCells * sizeof(float4)));
     d.p2keep = reinterpret_cast<float*>(take((size_t)kStaticMaxCells * sizeof(float)));
     d.ptile = reinterpret_cast<uint32_t*>(take(kStaticTiles * sizeof(uint32_t)));
+    d.plist = reinterpret_cast<uint32_t*>(take(kStaticTiles * sizeof(uint32_t)));
+    d.pcount = reinterpret_cast<uint32_t*>(take(kMaxLevels * sizeof(uint32_t)));
     d.partials = reinterpret_cast<float4*>(take(2 * ((size_t)kStaticMaxCells / 256 + 64) * sizeof(float4)));
     d.mga = reinterpret_cast<float4*>(take(kStaticTotal * sizeof(float4)));
     d.mgd = reinterpret_cast<float*>(take(kStaticTotal * sizeof(float)));

@@ -110,6 +110,7 @@ struct SproutSim {
     std::vector<float> solid_host;   // kept for nothing but the device copy's lifetime
 
     ~SproutSim() {
+        if (trace_buf) cudaFree(trace_buf);
         drop_part_graphs();
         if (cap_stream) cudaStreamDestroy(cap_stream);
         if (stage_params) cudaFreeHost(stage_params);
@@ -183,6 +184,32 @@ struct SproutSim {
             graph_ok = false;   // new device pointers: the captured substep is stale
         }
         mixed = mode == 1;
+        return SPROUT_OK;
+    }
+
+    // The solvers' phase trace: rows > 0 turns it on (rows barrier generations kept, one
+    // column per block of the widest persistent kernel plus block 0's leaving time), 0 off.
+    unsigned long long* trace_buf = nullptr;
+    uint32_t trace_rows = 0, trace_cols = 0;
+    int trace_enable(uint32_t rows) {
+        CUDA_TRY(cudaStreamSynchronize(stream));
+        if (trace_buf) {
+            cudaFree(trace_buf);
+            trace_buf = nullptr;
+        }
+        trace_rows = rows;
+        trace_cols = rows ? (uint32_t)std::max({cfg.mg_blocks, cfg.mg_blocks_mixed, cfg.visc_blocks, 1}) + 1 : 0;
+        if (rows) {
+            size_t b = (size_t)trace_rows * trace_cols * 8;
+            if (cudaMalloc(&trace_buf, b) != cudaSuccess) return fail(SPROUT_E_NOMEM, "trace buffer");
+            CUDA_TRY(cudaMemset(trace_buf, 0, b));
+        }
+        SolveState K0;
+        CUDA_TRY(cudaMemcpy(&K0, d.K, sizeof K0, cudaMemcpyDeviceToHost));
+        K0.trace = trace_buf;
+        K0.trace_rows = trace_rows;
+        K0.trace_cols = trace_cols;
+        CUDA_TRY(cudaMemcpy(d.K, &K0, sizeof K0, cudaMemcpyHostToDevice));
         return SPROUT_OK;
     }
 
@@ -262,6 +289,8 @@ struct SproutSim {
         A(d.cgp2, nc);
         A(d.cgq, nc);
         A(d.ptile, (size_t)d.lv.tiles);
+        A(d.plist, (size_t)d.lv.tiles);
+        A(d.pcount, (size_t)kMaxLevels);
         A(d.partials, 2 * (size_t)d.nwg);
 #undef A
         std::vector<float> nt(nc, NO_TEMP);
@@ -591,7 +620,14 @@ struct SproutSim {
         CUDA_TRY(cudaMemset(d.pres, 0, nc * sizeof(float2)));
         CUDA_TRY(cudaMemset(d.p2keep, 0, nc * sizeof(float)));
         CUDA_TRY(cudaMemset(d.S, 0, sizeof(StepState)));
-        CUDA_TRY(cudaMemset(d.K, 0, sizeof(SolveState)));
+        {
+            SolveState K0;
+            std::memset(&K0, 0, sizeof K0);
+            K0.trace = trace_buf;
+            K0.trace_rows = trace_rows;
+            K0.trace_cols = trace_cols;
+            CUDA_TRY(cudaMemcpy(d.K, &K0, sizeof K0, cudaMemcpyHostToDevice));
+        }
         CUDA_TRY(cudaMemset(d.dheat, 0, nc * sizeof(float4)));
         CUDA_TRY(cudaMemset(d.ledger, 0, 8 * sizeof(unsigned long long)));
         sim_time = 0.0;
@@ -748,14 +784,14 @@ struct SproutBatch {
         size_t smem = 0;
         int cap = 0;
         DevScene* ds = nullptr;
-        int *doff = nullptr, *dscale = nullptr;
+        int *doff = nullptr, *dscale = nullptr, *daoff = nullptr;
         unsigned char* dscal = nullptr;
         SolveState* dk = nullptr;
         void release() {
-            for (void* p : {(void*)ds, (void*)doff, (void*)dscale, (void*)dscal, (void*)dk})
+            for (void* p : {(void*)ds, (void*)doff, (void*)dscale, (void*)dscal, (void*)dk, (void*)daoff})
                 if (p) cudaFree(p);
             ds = nullptr;
-            doff = dscale = nullptr;
+            doff = dscale = daoff = nullptr;
             dscal = nullptr;
             dk = nullptr;
             cap = 0;
@@ -847,10 +883,11 @@ struct SproutBatch {
         if (ns > V.cap) {
             CUDA_TRY(cudaStreamSynchronize(main));
             const int cap = std::max(ns, 2 * V.cap);
-            for (void* p : {(void*)V.ds, (void*)V.doff, (void*)V.dscale, (void*)V.dscal, (void*)V.dk})
+            for (void* p : {(void*)V.ds, (void*)V.doff, (void*)V.dscale, (void*)V.dscal, (void*)V.dk, (void*)V.daoff})
                 if (p) cudaFree(p);
             bool ok = cudaMalloc(&V.ds, cap * sizeof(DevScene)) == cudaSuccess &&
                       cudaMalloc(&V.doff, (size_t)kMaxLevels * (cap + 1) * sizeof(int)) == cudaSuccess &&
+                      cudaMalloc(&V.daoff, (size_t)kMaxLevels * (cap + 1) * sizeof(int)) == cudaSuccess &&
                       cudaMalloc(&V.dscale, cap * sizeof(int)) == cudaSuccess &&
                       cudaMalloc(&V.dscal, cap * pressure_batch_scalar_bytes()) == cudaSuccess &&
                       cudaMalloc(&V.dk, sizeof(SolveState)) == cudaSuccess;
@@ -884,7 +921,7 @@ struct SproutBatch {
         CUDA_TRY(cudaMemcpyAsync(V.doff, off.data(), off.size() * sizeof(int), cudaMemcpyHostToDevice, main));
         CUDA_TRY(cudaMemcpyAsync(V.dscale, scale.data(), ns * sizeof(int), cudaMemcpyHostToDevice, main));
         h2d += ns * sizeof(DevScene) + off.size() * sizeof(int) + ns * sizeof(int);
-        V.v = BatchView{V.ds, ns, V.doff, V.dscal, V.dscale, V.dk, max_tail};
+        V.v = BatchView{V.ds, ns, V.doff, V.dscal, V.dscale, V.dk, max_tail, V.daoff};
         V.smem = smem;
         const int mx = pressure_batch_blocks_max(device, smem, mixed);
         int total_tiles = 0;
@@ -1256,6 +1293,18 @@ int sprout_batch_sync(SproutBatch* b) {
 int sprout_batch_profile(SproutBatch* b, uint32_t substeps, float* ms) {
     if (!b || !ms) return fail(SPROUT_E_ARG, "null argument");
     return b->profile(substeps, ms);
+}
+int sprout_sim_trace_enable(SproutSim* sim, uint32_t rows) {
+    if (!sim) return fail(SPROUT_E_ARG, "null argument");
+    return sim->trace_enable(rows);
+}
+int sprout_sim_trace_read(SproutSim* sim, unsigned long long* out, size_t cap, size_t* words, uint32_t* cols) {
+    if (!sim || !words || !cols) return fail(SPROUT_E_ARG, "null argument");
+    CUDA_TRY(cudaStreamSynchronize(sim->stream));
+    *words = (size_t)sim->trace_rows * sim->trace_cols;
+    *cols = sim->trace_cols;
+    if (out && sim->trace_buf) CUDA_TRY(cudaMemcpy(out, sim->trace_buf, std::min(*words, cap) * 8, cudaMemcpyDeviceToHost));
+    return SPROUT_OK;
 }
 int sprout_sim_set_precision(SproutSim* sim, int mode) {
     if (!sim) return fail(SPROUT_E_ARG, "null argument");

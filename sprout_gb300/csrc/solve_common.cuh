@@ -25,43 +25,54 @@ DEV int tiles_x(const Lv& L) { return (L.w + 15) >> 4; }
 DEV int tiles_y(const Lv& L) { return (L.h + 15) >> 4; }
 DEV float wcomp(float4 w, int k) { return k == 0 ? w.x : k == 1 ? w.y : k == 2 ? w.z : w.w; }
 
-// Grid-wide barrier over the co-resident blocks of a cooperative launch. Thread 0 of each
-// block arrives on a counter and waits on a generation word with a bounded spin; the last
-// to arrive resets the counter and advances the generation. Returns false (and every block
-// leaves) once any wait has run out.
+DEV unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Grid-wide barrier over the co-resident blocks of a cooperative launch: one arrival counter
+// that only grows (zeroed before each launch). Thread 0 of each block adds one; the value it
+// got tells which barrier this is, e = old / blocks, and it waits (bounded spin) until the
+// counter reaches (e + 1) x blocks, which the last block to arrive makes true with its own
+// add: releasing costs no store beyond the arrivals. Returns false (and every block leaves)
+// once any wait has run out.
 DEV bool grid_sync(SolveState* K) {
     __shared__ int s_ok;
     __syncthreads();
     if (threadIdx.x == 0) {
         int ok = 1;
-        volatile uint32_t* vgen = &K->bar_gen;
+        volatile uint32_t* vcnt = &K->bar_count;
         volatile uint32_t* verr = &K->error;
+        unsigned long long* trace = K->trace;
         if (*verr != 0u) {
             ok = 0;
         } else {
-            uint32_t g = *vgen;
+            const unsigned long long t_in = trace ? global_ns() : 0ull;
             __threadfence();
-            uint32_t arrived = atomicAdd(&K->bar_count, 1u) + 1u;
-            if (arrived == gridDim.x) {
-                atomicExch(&K->bar_count, 0u);
-                __threadfence();
-                atomicAdd(&K->bar_gen, 1u);
-            } else {
-                uint32_t spins = 0;
-                while (*vgen == g) {
-                    if (*verr != 0u) { ok = 0; break; }
-                    __nanosleep(32);
-                    if (++spins > SPIN_LIMIT) {
-                        if (atomicExch(&K->error, 1u) == 0u) {
-                            K->err_arrived = *(volatile uint32_t*)&K->bar_count;
-                            K->err_blocks = gridDim.x;
-                        }
-                        ok = 0;
-                        break;
+            const uint32_t old = atomicAdd(&K->bar_count, 1u);
+            const uint32_t epoch = old / gridDim.x;
+            const uint32_t target = (epoch + 1u) * gridDim.x;
+            unsigned long long* row = nullptr;
+            if (trace && blockIdx.x + 1 < K->trace_cols) {
+                row = trace + (size_t)(epoch % K->trace_rows) * K->trace_cols;
+                row[blockIdx.x] = t_in;
+            }
+            uint32_t spins = 0;
+            while (*vcnt < target) {
+                if (*verr != 0u) { ok = 0; break; }
+                __nanosleep(32);
+                if (++spins > SPIN_LIMIT) {
+                    if (atomicExch(&K->error, 1u) == 0u) {
+                        K->err_arrived = *vcnt - epoch * gridDim.x;
+                        K->err_blocks = gridDim.x;
                     }
+                    ok = 0;
+                    break;
                 }
             }
             __threadfence();
+            if (row && blockIdx.x == 0) row[K->trace_cols - 1] = global_ns();
         }
         s_ok = ok;
     }
@@ -95,6 +106,36 @@ DEV T total(const T* part, int n, T* buf) {
     T r = buf[0];
     __syncthreads();
     return r;
+}
+
+// One block compacts the nonzero flags[0 .. T) into out (their indices, in order) and
+// stores how many into *count.
+DEV void compact_flags(const uint32_t* flags, int T, uint32_t* out, uint32_t* count) {
+    __shared__ uint32_t wsum[NT / 32];
+    __shared__ uint32_t s_base;
+    if (threadIdx.x == 0) s_base = 0u;
+    __syncthreads();
+    for (int b0 = 0; b0 < T; b0 += NT) {
+        const int k = b0 + threadIdx.x;
+        const bool on = k < T && flags[k] != 0u;
+        const uint32_t bal = __ballot_sync(0xffffffffu, on);
+        const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+        if (lane == 0) wsum[w] = __popc(bal);
+        __syncthreads();
+        uint32_t before = s_base;
+        for (int j = 0; j < w; j++) before += wsum[j];
+        before += __popc(bal & ((1u << lane) - 1u));
+        if (on) out[before] = (uint32_t)k;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            uint32_t tot = 0;
+            for (int j = 0; j < NT / 32; j++) tot += wsum[j];
+            s_base += tot;
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *count = s_base;
+    __syncthreads();
 }
 
 }  // namespace solve
