@@ -104,6 +104,8 @@ struct SolveState {
     // the time block 0 left it
     unsigned long long* trace;
     uint32_t trace_rows, trace_cols;
+    uint32_t trace_base;   // barriers of the earlier launches (rows of later ones follow on)
+    uint32_t pad2;
 };
 
 // The multigrid hierarchy (Levels, src/sim/mod.rs:714-753).

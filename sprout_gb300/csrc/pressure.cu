@@ -1046,6 +1046,7 @@ __global__ void __launch_bounds__(NT) k_mgpcg(DevScene d, int second, int scale_
         true_rel = t4.y > 0.0 ? sqrt(t4.x / t4.y) : 0.0;
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) scal_stats<M, acc>(d.K, K, second, true_rel);
+    trace_launch_done(d.K);
 }
 
 // ---- many scenes in one persistent solve --------------------------------------------------
@@ -1279,6 +1280,7 @@ __global__ void __launch_bounds__(NT) k_mgpcg_batch(BatchView B, int second) {
         if (threadIdx.x == 0) scal_stats<M, acc>(d.K, KS[s], second, true_rel);
         __syncthreads();
     }
+    trace_launch_done(BK);
 }
 
 size_t pressure_smem(const Levels& lv) {

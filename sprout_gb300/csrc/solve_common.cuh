@@ -49,13 +49,14 @@ DEV bool grid_sync(SolveState* K) {
             ok = 0;
         } else {
             const unsigned long long t_in = trace ? global_ns() : 0ull;
+            const uint32_t base = trace ? *(volatile uint32_t*)&K->trace_base : 0u;
             __threadfence();
             const uint32_t old = atomicAdd(&K->bar_count, 1u);
             const uint32_t epoch = old / gridDim.x;
             const uint32_t target = (epoch + 1u) * gridDim.x;
             unsigned long long* row = nullptr;
             if (trace && blockIdx.x + 1 < K->trace_cols) {
-                row = trace + (size_t)(epoch % K->trace_rows) * K->trace_cols;
+                row = trace + (size_t)((base + epoch) % K->trace_rows) * K->trace_cols;
                 row[blockIdx.x] = t_in;
             }
             uint32_t spins = 0;
@@ -82,6 +83,12 @@ DEV bool grid_sync(SolveState* K) {
 
 DEV float4 add4(float4 a, float4 b) { return make_float4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w); }
 DEV Dbl4 add4(Dbl4 a, Dbl4 b) { return Dbl4{a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w}; }
+
+// At the end of a persistent kernel (block 0, after its last barrier, which every block has
+// reached): the trace rows of the next launch follow this one's.
+DEV void trace_launch_done(SolveState* K) {
+    if (blockIdx.x == 0 && threadIdx.x == 0 && K->trace) K->trace_base += K->bar_count / gridDim.x;
+}
 
 // Work-group tree of reduce.glsl:5-14 over the 256 values in buf; result in buf[0].
 template <class T>

@@ -317,7 +317,11 @@ struct Region {
     // load_region (vmg.glsl:90-111) with the right-hand side from rhs(i)
     template <class F>
     DEV void load(const DevScene& d, const Lv& L, F rhs) const {
-        for (int k = threadIdx.x; k < N; k += NT) {
+        // a fixed trip count, so that every round's loads are issued before any store
+#pragma unroll
+        for (int j = 0; j < PER; j++) {
+            const int k = threadIdx.x + j * NT;
+            if (k >= N) break;
             const int x = cell_x(k), y = cell_y(k);
             float4 a = make_float4(0.0f, 0.0f, 0.0f, 0.0f), b = a;
             float2 dd = f2(0.0f, 0.0f), r = dd;
@@ -388,7 +392,10 @@ struct Region {
     // coarse values (LC, if any), zero where a face is no unknown; then HALO half-sweeps,
     // black first.
     DEV void way_up(const DevScene& d, const Lv& L, const Lv* LC) const {
-        for (int k = threadIdx.x; k < N; k += NT) {
+#pragma unroll
+        for (int j = 0; j < PER; j++) {
+            const int k = threadIdx.x + j * NT;
+            if (k >= N) break;
             const int x = cell_x(k), y = cell_y(k);
             float2 v = f2(0.0f, 0.0f);
             if (l_inside(L, x, y)) {
@@ -406,14 +413,45 @@ struct Region {
     }
 };
 
+// This block's share of the active-tile lists in shared memory (entry k of level l: list
+// item blockIdx.x + k x gridDim.x), filled once per solve; items past kVCachePer are read from
+// global memory.
+constexpr int kVCacheLevels = 4, kVCachePer = 32;
+struct VTileCache {
+    uint32_t cnt[kVCacheLevels];
+    uint32_t item[kVCacheLevels][kVCachePer];
+};
+
 template <int NU>
 struct VSolve {
     const DevScene& d;
     VSmem<NU>& s;
     VScal& K;
     int n;   // level-0 tiles (partial slots per half)
+    VTileCache& tc;
 
     DEV const uint32_t* list(int l) const { return d.vlist + d.lv.toff[l]; }
+
+    DEV void fill_cache(int nlev) const {
+        for (int l = 0; l < kVCacheLevels && l <= nlev; l++) {
+            const uint32_t cnt = *(volatile uint32_t*)&d.vcount[l];
+            if (threadIdx.x == 0) tc.cnt[l] = cnt;
+            for (int k = threadIdx.x; k < kVCachePer; k += NT) {
+                const uint32_t j = blockIdx.x + (uint32_t)k * gridDim.x;
+                if (j < cnt) tc.item[l][k] = list(l)[j];
+            }
+        }
+        __syncthreads();
+    }
+    // For every active tile of level l in this block's share.
+    template <class F>
+    DEV void each(int l, F&& f) const {
+        const bool cached = l < kVCacheLevels;
+        const uint32_t cnt = cached ? tc.cnt[l] : *(volatile uint32_t*)&d.vcount[l];
+        int k = 0;
+        for (uint32_t j = blockIdx.x; j < cnt; j += gridDim.x, k++)
+            f((cached && k < kVCachePer) ? tc.item[l][k] : list(l)[j]);
+    }
 
     // Every block sums one half of the partials in the shader's order (reduce_tail.glsl).
     DEV float4 sum(int half) const { return total(d.partials + half * n, n, s.buf); }
@@ -555,10 +593,8 @@ struct VSolve {
     DEV void warm(int half) const {
         const Lv L0 = lev(d.lv, 0);
         const int tw = tiles_x(L0);
-        const uint32_t cnt = d.vcount[0];
         const int W = d.W;
-        for (uint32_t j = blockIdx.x; j < cnt; j += gridDim.x) {
-            const uint32_t tt = list(0)[j];
+        each(0, [&](uint32_t tt) {
             const int cx = (int)(tt % tw) * 16 + (threadIdx.x & 15), cy = (int)(tt / tw) * 16 + (threadIdx.x >> 4);
             float4 acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
             if (in_grid(d, cx, cy) && interior(d, cx, cy)) {
@@ -589,7 +625,7 @@ struct VSolve {
                 acc = make_float4(dot2(r, z), dot2(r, r), 0.0f, 0.0f);
             }
             tile_sum(acc, half, tt);
-        }
+        });
     }
 
     // vmg_down.comp on level l (l = 0 at the start of a solve, right-hand side vr)
@@ -597,15 +633,13 @@ struct VSolve {
         const Lv L = lev(d.lv, l);
         const Lv LC = lev(d.lv, l + 1);
         const int tw = tiles_x(L);
-        const uint32_t cnt = d.vcount[l];
-        for (uint32_t j = blockIdx.x; j < cnt; j += gridDim.x) {
-            const uint32_t tt = list(l)[j];
+        each(l, [&](uint32_t tt) {
             Region<NU, VCfg<NU>::HALO> R{s, (int)(tt % tw) * 16, (int)(tt / tw) * 16};
             if (l == 0) R.load(d, L, [&](int i) { return rhs0[i]; });
             else R.load(d, L, [&](int i) { return d.vmr[i]; });
             __syncthreads();
             R.way_down(d, L, l == nlev ? nullptr : &LC);
-        }
+        });
     }
 
     // vmg_up.comp on a coarse level l: the finished values to vmz
@@ -613,9 +647,7 @@ struct VSolve {
         const Lv L = lev(d.lv, l);
         const Lv LC = lev(d.lv, l + 1);
         const int tw = tiles_x(L);
-        const uint32_t cnt = d.vcount[l];
-        for (uint32_t j = blockIdx.x; j < cnt; j += gridDim.x) {
-            const uint32_t tt = list(l)[j];
+        each(l, [&](uint32_t tt) {
             Region<NU, VCfg<NU>::HALO> R{s, (int)(tt % tw) * 16, (int)(tt / tw) * 16};
             R.load(d, L, [&](int i) { return d.vmr[i]; });
             __syncthreads();
@@ -624,7 +656,7 @@ struct VSolve {
             const int cx = R.ox + (t & 15), cy = R.oy + (t >> 4);
             if (l_inside(L, cx, cy)) d.vmz[l_at(L, cx, cy)] = s.sx[R.tile_slot(t)];
             __syncthreads();
-        }
+        });
     }
 
     // visc_mgz.comp: the way up on level 0 with A z and the partial sums of r.z, z.A z, z.q
@@ -632,9 +664,7 @@ struct VSolve {
         const Lv L = lev(d.lv, 0);
         const Lv LC = lev(d.lv, 1);
         const int tw = tiles_x(L);
-        const uint32_t cnt = d.vcount[0];
-        for (uint32_t j = blockIdx.x; j < cnt; j += gridDim.x) {
-            const uint32_t tt = list(0)[j];
+        each(0, [&](uint32_t tt) {
             Region<NU, VCfg<NU>::HALO + 1> R{s, (int)(tt % tw) * 16, (int)(tt / tw) * 16};
             R.load(d, L, [&](int i) { return rn[i]; });
             __syncthreads();
@@ -653,7 +683,7 @@ struct VSolve {
                 acc = make_float4(dot2(s.sr[k], z), dot2(z, az), dot2(z, qn[i]), 0.0f);
             }
             tile_sum(acc, half, tt);
-        }
+        });
     }
 
     // visc_mgu.comp: p, q, x, r of the iteration and the way down on level 0 from the new r
@@ -661,7 +691,6 @@ struct VSolve {
         const Lv L = lev(d.lv, 0);
         const Lv LC = lev(d.lv, 1);
         const int tw = tiles_x(L);
-        const uint32_t cnt = d.vcount[0];
         const float a = K.alpha, b = K.beta;
         auto new_q = [&](int i) {
             const float2 sq = d.vaz[i];
@@ -669,8 +698,7 @@ struct VSolve {
             const float2 q = qo[i];
             return f2(sq.x + b * q.x, sq.y + b * q.y);
         };
-        for (uint32_t j = blockIdx.x; j < cnt; j += gridDim.x) {
-            const uint32_t tt = list(0)[j];
+        each(0, [&](uint32_t tt) {
             Region<NU, VCfg<NU>::HALO> R{s, (int)(tt % tw) * 16, (int)(tt / tw) * 16};
             const int t = threadIdx.x;
             const int cx = R.ox + (t & 15), cy = R.oy + (t >> 4);
@@ -707,7 +735,7 @@ struct VSolve {
             __syncthreads();
             R.way_down(d, L, &LC);
             tile_sum(acc, half, tt);
-        }
+        });
     }
 
     // record_visc_coarse (mod.rs:2838-2853): the coarse levels down, then up
@@ -733,13 +761,15 @@ template <int NU>
 __global__ void __launch_bounds__(NT) k_visc_solve(DevScene d, int restrain) {
     __shared__ VSmem<NU> sm;
     __shared__ VScal K;
+    __shared__ VTileCache tc;
     const DevParams* P = d.P;
     const int nlev = P->visc_levels;
-    VSolve<NU> V{d, sm, K, d.nwg};
+    VSolve<NU> V{d, sm, K, d.nwg, tc};
     const float tz = P->tol[2];
     if (blockIdx.x == 0) V.build_lists(nlev);
     if (restrain) V.strain();
     if (!grid_sync(d.K)) return;
+    V.fill_cache(nlev);
     V.start();
     if (!grid_sync(d.K)) return;
     {   // cg_reduce mode 4
@@ -840,6 +870,7 @@ __global__ void __launch_bounds__(NT) k_visc_solve(DevScene d, int restrain) {
         G->v_rr = K.rr;
         G->v_r0 = K.r0;
     }
+    trace_launch_done(d.K);
 }
 
 namespace {
