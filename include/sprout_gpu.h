@@ -133,6 +133,21 @@ int sprout_sim_set_solids(SproutSim* sim, const float* sdf, const float* solid4,
 /* FluidSim::reset (mod.rs:1981-2002): replaces every particle (ids = index, spawn fields
  * settled). SPROUT_E_UNSUPPORTED if the tank needs a capability the engine lacks. */
 int sprout_sim_reset(SproutSim* sim, const SproutParticle* p, uint32_t n);
+/* FluidSim::spawn (mod.rs:2024-2046): queues particles for the next step call (new ids
+ * follow the last given, spawn fields settled, marked fresh). *accepted = how many were
+ * queued: at most SPROUT_SPAWN_MAX wait at once, particles without a material are skipped,
+ * and 0 are taken (SPROUT_OK) when their materials do not fit the tank's channels. At the
+ * next step they fill free slots, then recycle dead ones (claim.comp); entries beyond the
+ * dead slots are dropped, as the reference drops them. SPROUT_E_ARG before a reset. */
+#define SPROUT_SPAWN_MAX 32768u
+int sprout_sim_spawn(SproutSim* sim, const SproutParticle* p, uint32_t n, uint32_t* accepted);
+/* FluidSim::cell_counts (mod.rs:3350-3387) with count.comp: live particles per cell of the
+ * window of cells [lo, hi) (inside the grid), row by row, after the work queued so far, the
+ * particles queued by spawn included. *cells = the window's cell count; out may be NULL to
+ * ask for it. Blocking; reads back only the window. SPROUT_E_ARG for a window outside the
+ * grid (the reference asserts) or cap < *cells. */
+int sprout_sim_cell_counts(SproutSim* sim, const int32_t lo[2], const int32_t hi[2], uint32_t* out,
+                           size_t cap, size_t* cells);
 /* FluidSim::record + submit (mod.rs:2400-2562): `substeps` substeps meant to cover
  * `target` seconds (ignored with a fixed step rate). Asynchronous on the sim's stream.
  * tool may be NULL. */

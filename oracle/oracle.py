@@ -129,6 +129,10 @@ def lib() -> C.CDLL:
         L.osim_set_solids.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
         L.osim_reset.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32]
         L.osim_reset.restype = C.c_int
+        L.osim_spawn.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32]
+        L.osim_spawn.restype = C.c_int
+        L.osim_cell_counts.argtypes = [C.c_void_p, P(C.c_int), P(C.c_int), C.c_void_p, C.c_size_t]
+        L.osim_cell_counts.restype = C.c_long
         L.osim_step.argtypes = [C.c_void_p, C.c_uint32, C.c_float, P(OTool)]
         L.osim_step.restype = C.c_int
         L.osim_sort.argtypes = [C.c_void_p]
@@ -219,6 +223,21 @@ class OracleSim:
     def reset(self, particles: np.ndarray) -> int:
         p = np.ascontiguousarray(particles, PARTICLE_DTYPE)
         return lib().osim_reset(self.h_, p.ctypes.data, len(p))
+
+    def spawn(self, particles: np.ndarray) -> int:
+        """FluidSim::spawn: how many were queued (0 when their materials do not fit)."""
+        p = np.ascontiguousarray(particles, PARTICLE_DTYPE)
+        return lib().osim_spawn(self.h_, p.ctypes.data, len(p))
+
+    def cell_counts(self, lo, hi) -> np.ndarray:
+        """FluidSim::cell_counts: live particles per cell of [lo, hi), shape (rows, columns)."""
+        a, b = (C.c_int * 2)(*lo), (C.c_int * 2)(*hi)
+        n = lib().osim_cell_counts(self.h_, a, b, None, 0)
+        if n < 0:
+            raise ValueError("oracle: window outside the grid")
+        out = np.zeros(n, np.uint32)
+        lib().osim_cell_counts(self.h_, a, b, out.ctypes.data, n)
+        return out.reshape(max(hi[1] - lo[1], 0), max(hi[0] - lo[0], 0))
 
     def step(self, substeps: int, target: float = 0.0, tool: OTool | None = None):
         return lib().osim_step(self.h_, substeps, target, None if tool is None else C.byref(tool))

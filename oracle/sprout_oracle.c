@@ -104,6 +104,7 @@ float o_expf(float x) {
 #define SPAWN_TEMP (-1.0e4f)
 #define SPAWN_S (-1.0f)
 #define MAX_PRESENT 12
+#define SPAWN_MAX 32768u     /* mod.rs:63 */
 #define GROUPS 4
 #define MASS_SCALE 1048576.0f
 #define MOM_SCALE 4194304.0f
@@ -666,6 +667,10 @@ struct OSim {
     uint32_t *tiles, *vtile;
     /* scratch for the particle pass */
     struct Scat* scat;
+    /* spawn queue (mod.rs:1026, 2024-2046): taken into the buffer by the next step */
+    OParticle* pending;
+    uint32_t n_pending, next_id;
+    float spawn_speed;
 };
 
 static int g_threads = 1;
@@ -942,7 +947,7 @@ static void build_params(OSim* s, const OTool* tool) {
     P->density_k = p->correction_max;
     P->dt_max = dt_limit(s);
     P->crowd_jitter = p->crowd_jitter;
-    P->ext_speed = tool ? tool_speed(tool) : 0.0f;
+    P->ext_speed = maxf(tool ? tool_speed(tool) : 0.0f, s->spawn_speed);   /* mod.rs:2300 */
     P->wall_margin = 0.1f;
     if (tool) {
         P->tool_pos[0] = tool->pos[0];
@@ -3628,6 +3633,7 @@ OSim* osim_create(int w, int h, uint32_t capacity, const OSimParams* p) {
     ALLOC(s->tiles, s->nwg); ALLOC(s->vtile, s->lv.tiles);
     ALLOC(s->ptile, s->lv.tiles);
     ALLOC(s->part, 2 * s->nwg);
+    ALLOC(s->pending, SPAWN_MAX);
     for (size_t k = 0; k < nc; k++) s->solid_t[k] = NO_TEMP;
     return s;
 }
@@ -3639,7 +3645,7 @@ void osim_destroy(OSim* s) {
                     s->vel0, s->pjump, s->pres, s->p2keep, s->hcell, s->solid, s->sdf, s->region,
                     s->solid_t, s->mga, s->mgd, s->mgx, s->mgz, s->mgr, s->cgp, s->cgp2, s->cgq,
                     s->ptile, s->part, s->vr, s->vr2, s->vp, s->vq, s->vq2, s->vd, s->vaz, s->vma,
-                    s->vmb, s->vmd, s->vmr, s->vmx, s->vmz, s->tiles, s->vtile};
+                    s->vmb, s->vmd, s->vmr, s->vmx, s->vmz, s->tiles, s->vtile, s->pending};
     for (size_t k = 0; k < sizeof ptrs / sizeof ptrs[0]; k++) free(ptrs[k]);
     free(s);
 }
@@ -3684,42 +3690,48 @@ static float enthalpy_temp(const OSimParams* p, int row, float sc, float t) {
     return (lo - l) + fr * (hi - lo + l);
 }
 
-int osim_reset(OSim* s, const OParticle* in, uint32_t n) {
-    if (n > s->capacity) n = s->capacity;
+/* Particle::settle_spawn (params.rs:70-85) and the position range every substep leaves a
+ * particle in (particles.comp:912), so that the first gather's 3 x 3 stencils stay on the
+ * grid. Returns 0, or -1 for a non-finite position. */
+static int settle(const OSim* s, OParticle* q) {
     const OSimParams* p = &s->prm;
-    /* reset: ids, settle_spawn (params.rs:71-88) */
-    for (uint32_t k = 0; k < n; k++) {
-        OParticle q = in[k];
-        q.id = k;
-        if (!isfinite(q.pos[0]) || !isfinite(q.pos[1])) return -1;
-        q.pos[0] = minf(maxf(q.pos[0], 2.01f), (float)s->W - 2.01f);
-        q.pos[1] = minf(maxf(q.pos[1], 2.01f), (float)s->H - 2.01f);
-        uint32_t mat = (q.kind & 255u);
-        if (mat != 0u && q.kind != KIND_DEAD) {
-            const OMat* def = &p->mat[mat - 1u];
-            if (q.t == SPAWN_TEMP) {
-                q.t = def->spawn_temp;
-                q.kind |= KIND_REAL_T;
-            }
-            if (q.s == SPAWN_S) q.s = def->diluent >= 0 ? clampf(def->load, 0.0f, 1.0f) : 1.0f;
-            if (q.kind & KIND_REAL_T) {
-                q.kind &= ~KIND_REAL_T;
-                q.t = enthalpy_temp(p, (int)mat - 1, q.s, q.t);
-            }
+    if (!isfinite(q->pos[0]) || !isfinite(q->pos[1])) return -1;
+    q->pos[0] = minf(maxf(q->pos[0], 2.01f), (float)s->W - 2.01f);
+    q->pos[1] = minf(maxf(q->pos[1], 2.01f), (float)s->H - 2.01f);
+    uint32_t mat = (q->kind & 255u);
+    if (mat != 0u && q->kind != KIND_DEAD) {
+        const OMat* def = &p->mat[mat - 1u];
+        if (q->t == SPAWN_TEMP) {
+            q->t = def->spawn_temp;
+            q->kind |= KIND_REAL_T;
         }
-        s->particles[k] = q;
+        if (q->s == SPAWN_S) q->s = def->diluent >= 0 ? clampf(def->load, 0.0f, 1.0f) : 1.0f;
+        if (q->kind & KIND_REAL_T) {
+            q->kind &= ~KIND_REAL_T;
+            q->t = enthalpy_temp(p, (int)mat - 1, q->s, q->t);
+        }
     }
-    s->n_slots = n;
-    /* the tank: rows present (note_materials), thermal from heated solids or temperatures */
-    int present[O_MAX_MATERIALS] = {0};
-    int thermal = s->solids_heated;
+    return 0;
+}
+
+/* Marks the materials of particles in present[] and widens *thermal by their temperatures
+ * (note_materials, mod.rs:2050-2060). */
+static void mark_materials(const OSim* s, const OParticle* q, uint32_t n, int* present, int* thermal) {
+    const OSimParams* p = &s->prm;
     for (uint32_t k = 0; k < n; k++) {
-        uint32_t m = s->particles[k].kind & 255u;
-        if (m == 0u || s->particles[k].kind == KIND_DEAD) continue;
+        uint32_t m = q[k].kind & 255u;
+        if (m == 0u || q[k].kind == KIND_DEAD) continue;
         present[m - 1u] = 1;
-        thermal |= fabsf(s->particles[k].t - p->ambient_temp) > 0.05f || p->mat[m - 1u].self_heat > 0.0f;
+        *thermal |= fabsf(q[k].t - p->ambient_temp) > 0.05f || p->mat[m - 1u].self_heat > 0.0f;
     }
-    if (fabsf(p->ambient_temp - T_REF) > 0.05f) thermal = 1;
+}
+
+/* The tank for the rows marked in present[] (ascending) and the thermal flag: Tank::layout
+ * (mod.rs:271-329), the capabilities and viscosity mode that follow. Changes s only when
+ * every check passes; returns -2 (the rows do not fit), -3 (a concentrate without its
+ * diluent) or -4 (a capability the oracle does not carry) otherwise. */
+static int set_tank(OSim* s, const int* present, int thermal) {
+    const OSimParams* p = &s->prm;
     int rows[MAX_PRESENT], nrows = 0;
     for (int r = 0; r < O_MAX_MATERIALS; r++)
         if (present[r]) {
@@ -3727,21 +3739,59 @@ int osim_reset(OSim* s, const OParticle* in, uint32_t n) {
             rows[nrows++] = r;
             if (p->mat[r].diluent >= 0 && !present[p->mat[r].diluent]) return -3;
         }
-    if (!tank_layout(&s->tank, rows, nrows, p, thermal)) return -2;
+    Tank t;
+    if (!tank_layout(&t, rows, nrows, p, thermal)) return -2;
+    const Tank old_tank = s->tank;
+    const int old_thermal = s->thermal, old_visc = s->visc_mode;
+    const uint32_t old_caps = s->caps;
+    s->tank = t;
     s->thermal = thermal;
     s->caps = compute_caps(s);
-    /* capabilities the oracle does not carry */
-    if (s->tank.families > 0) return -4;
-    if (s->caps & (CAP_RIGID | CAP_RHEO | CAP_MAGNET | CAP_ELASTIC | CAP_SETTLE | CAP_STEAM | CAP_REACT)) return -4;
-    if (__builtin_popcount(s->tank.group_mask) > 1) return -4;
+    int rc = 0;
+    if (t.families > 0) rc = -4;
+    if (s->caps & (CAP_RIGID | CAP_RHEO | CAP_MAGNET | CAP_ELASTIC | CAP_SETTLE | CAP_STEAM | CAP_REACT)) rc = -4;
+    if (__builtin_popcount(t.group_mask) > 1) rc = -4;
     for (int k = 0; k < nrows; k++) {
         const OMat* m = &p->mat[rows[k]];
-        if (m->volatility > 0.0f || (thermal && m->boil < 1e8f)) return -4;
+        if (m->volatility > 0.0f || (thermal && m->boil < 1e8f)) rc = -4;
     }
-    s->visc_mode = viscosity_mode(s);
-    /* the implicit solve with its multigrid preconditioner on at least one coarse level */
-    if (s->visc_mode == 2 && (s->prm.viscosity_precond == 0 || s->lv.tail < 1)) return -4;
+    if (rc == 0) {
+        s->visc_mode = viscosity_mode(s);
+        /* the implicit solve with its multigrid preconditioner on at least one coarse level */
+        if (s->visc_mode == 2 && (s->prm.viscosity_precond == 0 || s->lv.tail < 1)) rc = -4;
+    }
+    if (rc != 0) {
+        s->tank = old_tank;
+        s->thermal = old_thermal;
+        s->caps = old_caps;
+        s->visc_mode = old_visc;
+        return rc;
+    }
     build_mats(s);
+    return 0;
+}
+
+int osim_reset(OSim* s, const OParticle* in, uint32_t n) {
+    if (n > s->capacity) n = s->capacity;
+    const OSimParams* p = &s->prm;
+    /* reset: ids, settle_spawn (mod.rs:1981-2002) */
+    for (uint32_t k = 0; k < n; k++) {
+        OParticle q = in[k];
+        q.id = k;
+        if (settle(s, &q) != 0) return -1;
+        s->particles[k] = q;
+    }
+    s->n_slots = n;
+    s->next_id = n;
+    s->n_pending = 0;
+    s->spawn_speed = 0.0f;
+    /* the tank: rows present (note_materials), thermal from heated solids or temperatures */
+    int present[O_MAX_MATERIALS] = {0};
+    int thermal = s->solids_heated;
+    mark_materials(s, s->particles, n, present, &thermal);
+    if (fabsf(p->ambient_temp - T_REF) > 0.05f) thermal = 1;
+    int rc = set_tank(s, present, thermal);
+    if (rc != 0) return rc;
     /* buffers a reset clears (mod.rs:2451-2460) */
     size_t nc = (size_t)s->W * s->H;
     memset(s->pres, 0, nc * sizeof(V2));
@@ -3755,8 +3805,83 @@ int osim_reset(OSim* s, const OParticle* in, uint32_t n) {
     return 0;
 }
 
+int osim_spawn(OSim* s, const OParticle* in, uint32_t n) {
+    const OSimParams* p = &s->prm;
+    uint32_t room = SPAWN_MAX - s->n_pending;
+    OParticle* q = s->pending + s->n_pending;
+    uint32_t m = 0;
+    for (uint32_t k = 0; k < n && m < room; k++) {
+        /* particles without a material are not queued (reset drops them too, mod.rs:1994) */
+        uint32_t mat = in[k].kind & 255u;
+        if (in[k].kind == KIND_DEAD || mat == 0u || mat > O_MAX_MATERIALS) continue;
+        q[m] = in[k];
+        q[m].id = s->next_id + m;
+        if (settle(s, &q[m]) != 0) return -1;
+        m++;
+    }
+    int present[O_MAX_MATERIALS] = {0};
+    for (int k = 0; k < s->tank.nrows; k++) present[s->tank.rows[k]] = 1;
+    int thermal = s->thermal;
+    int before = 0;
+    for (int r = 0; r < O_MAX_MATERIALS; r++) before += present[r];
+    mark_materials(s, q, m, present, &thermal);
+    int after = 0;
+    for (int r = 0; r < O_MAX_MATERIALS; r++) after += present[r];
+    if (after != before || thermal != s->thermal) {
+        int rc = set_tank(s, present, thermal);
+        if (rc == -2 || rc == -3) return 0;   /* they do not fit: none is accepted */
+        if (rc != 0) return rc;
+    }
+    for (uint32_t k = 0; k < m; k++) {
+        s->spawn_speed = maxf(s->spawn_speed, hypotf(q[k].vel[0], q[k].vel[1]));
+        q[k].kind |= KIND_FRESH;
+    }
+    s->next_id += m;
+    s->n_pending += m;
+    return (int)m;
+}
+
+/* record (mod.rs:2486-2503) and claim.comp: queued particles fill fresh slots while there are
+ * any, then dead slots, the k-th dead slot (in slot order) taking the k-th remaining entry;
+ * entries beyond the dead slots are dropped. */
+static void take_spawns(OSim* s) {
+    uint32_t n = s->n_pending;
+    if (n == 0) return;
+    uint32_t fresh = n < s->capacity - s->n_slots ? n : s->capacity - s->n_slots;
+    memcpy(s->particles + s->n_slots, s->pending, (size_t)fresh * sizeof(OParticle));
+    s->n_slots += fresh;
+    uint32_t k = fresh;
+    for (uint32_t id = 0; id < s->n_slots && k < n; id++)
+        if (s->particles[id].kind == KIND_DEAD) s->particles[id] = s->pending[k++];
+    s->n_pending = 0;
+}
+
+long osim_cell_counts(const OSim* s, const int lo[2], const int hi[2], uint32_t* out, size_t cap) {
+    if (lo[0] < 0 || lo[1] < 0 || hi[0] > s->W || hi[1] > s->H) return -1;
+    int sw = hi[0] - lo[0] > 0 ? hi[0] - lo[0] : 0, sh = hi[1] - lo[1] > 0 ? hi[1] - lo[1] : 0;
+    size_t n = (size_t)sw * sh;
+    if (!out) return (long)n;
+    if (cap < n) return -1;
+    memset(out, 0, n * sizeof(uint32_t));
+    /* count.comp:17-23 over the slots, then the queue (mod.rs:3380-3385) */
+    for (uint32_t id = 0; id < s->n_slots; id++) {
+        const OParticle* q = &s->particles[id];
+        if ((q->kind & 255u) == 0u) continue;
+        int cx = (int)floorf(q->pos[0]) - lo[0], cy = (int)floorf(q->pos[1]) - lo[1];
+        if (cx >= 0 && cy >= 0 && cx < sw && cy < sh) out[(size_t)cy * sw + cx]++;
+    }
+    for (uint32_t k = 0; k < s->n_pending; k++) {
+        const OParticle* q = &s->pending[k];
+        int cx = (int)floorf(q->pos[0]) - lo[0], cy = (int)floorf(q->pos[1]) - lo[1];
+        if (cx >= 0 && cy >= 0 && cx < sw && cy < sh) out[(size_t)cy * sw + cx]++;
+    }
+    return (long)n;
+}
+
 int osim_step(OSim* s, uint32_t substeps, float target, const OTool* tool) {
+    take_spawns(s);
     build_params(s, tool);
+    s->spawn_speed = 0.0f;
     if (substeps > 0) {
         s->S.frame_left = maxf(target, 0.0f);
         s->S.batch_steps = substeps;

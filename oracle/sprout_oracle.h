@@ -131,6 +131,14 @@ int osim_set_solids(OSim* s, const float* sdf, const float* solid4, const uint32
 /* FluidSim::reset (src/sim/mod.rs:1981-2002): ids, settle_spawn, the tank's rows.
  * Returns 0, or a negative code if the tank needs a capability the oracle lacks. */
 int osim_reset(OSim* s, const OParticle* p, uint32_t n);
+/* FluidSim::spawn (src/sim/mod.rs:2024-2046): queues particles for the next osim_step (ids
+ * follow the last given, settle_spawn, KIND_FRESH; at most 32768 queued). Returns how many
+ * were queued: 0 when their materials do not fit the tank; a negative code as osim_reset. */
+int osim_spawn(OSim* s, const OParticle* p, uint32_t n);
+/* FluidSim::cell_counts (src/sim/mod.rs:3350-3387) with count.comp: live particles per cell
+ * of the window [lo, hi) row by row, queued ones included. out NULL: returns the cell count
+ * only. Returns -1 for a window outside the grid or cap too small. */
+long osim_cell_counts(const OSim* s, const int lo[2], const int hi[2], uint32_t* out, size_t cap);
 /* FluidSim::record (src/sim/mod.rs:2400-2562): `substeps` substeps covering `target`. */
 int osim_step(OSim* s, uint32_t substeps, float target, const OTool* tool);
 /* Reorders particles now by the stable counting sort (sort.comp, stable by slot). */

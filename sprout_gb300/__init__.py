@@ -43,7 +43,7 @@ EXPORTS = [
     "sprout_batch_create", "sprout_batch_destroy", "sprout_batch_add", "sprout_batch_remove", "sprout_batch_size",
     "sprout_batch_set_precision", "sprout_batch_step", "sprout_batch_sync", "sprout_batch_profile",
     "sprout_batch_step_subset", "sprout_batch_tickets", "sprout_device_memory", "sprout_sim_trace_enable",
-    "sprout_sim_trace_read",
+    "sprout_sim_trace_read", "sprout_sim_spawn", "sprout_sim_cell_counts",
 ]
 
 STAGES = ["advance", "sort", "p2g", "grid", "pressure", "project", "viscosity", "project2"]
@@ -119,6 +119,8 @@ def lib() -> C.CDLL:
         "sprout_sim_step_blocking": ([V, C.c_uint32, P(Tool)], C.c_int),
         "sprout_sim_advance_blocking": ([V, C.c_double, P(Tool)], C.c_int),
         "sprout_sim_sync": ([V], C.c_int),
+        "sprout_sim_spawn": ([V, V, C.c_uint32, P(C.c_uint32)], C.c_int),
+        "sprout_sim_cell_counts": ([V, P(C.c_int32), P(C.c_int32), V, C.c_size_t, P(C.c_size_t)], C.c_int),
         "sprout_sim_download_particles": ([V, V, C.c_uint32, P(C.c_uint32)], C.c_int),
         "sprout_sim_download_pressure": ([V, V], C.c_int),
         "sprout_sim_download_field": ([V, C.c_char_p, V, C.c_size_t, P(C.c_size_t)], C.c_int),
@@ -264,6 +266,25 @@ class FluidSim:
     def reset(self, particles: np.ndarray):
         p = np.ascontiguousarray(particles, PARTICLE_DTYPE)
         _check(lib().sprout_sim_reset(self._h, p.ctypes.data, len(p)))
+
+    def spawn(self, particles: np.ndarray) -> int:
+        """FluidSim::spawn: queues particles for the next step; returns how many were taken
+        (0 when their materials do not fit the tank)."""
+        p = np.ascontiguousarray(particles, PARTICLE_DTYPE)
+        n = C.c_uint32()
+        _check(lib().sprout_sim_spawn(self._h, p.ctypes.data if len(p) else None, len(p), C.byref(n)))
+        return n.value
+
+    def cell_counts(self, lo, hi) -> np.ndarray:
+        """FluidSim::cell_counts: live particles per cell of the window [lo, hi), queued ones
+        included, as an array of (rows, columns)."""
+        a, b = (C.c_int32 * 2)(*lo), (C.c_int32 * 2)(*hi)
+        n = C.c_size_t()
+        _check(lib().sprout_sim_cell_counts(self._h, a, b, None, 0, C.byref(n)))
+        out = np.zeros(n.value, np.uint32)
+        if n.value:
+            _check(lib().sprout_sim_cell_counts(self._h, a, b, out.ctypes.data, n.value, C.byref(n)))
+        return out.reshape(max(hi[1] - lo[1], 0), max(hi[0] - lo[0], 0))
 
     def step(self, substeps: int, target: float = 0.0, tool: Tool | None = None):
         _check(lib().sprout_sim_step(self._h, substeps, target, None if tool is None else C.byref(tool)))

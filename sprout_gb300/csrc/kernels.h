@@ -28,6 +28,14 @@ struct LaunchCfg {
 void launch_advance(const DevScene& d, const LaunchCfg& cfg, cudaStream_t st);
 void launch_sort(const DevScene& d, const LaunchCfg& cfg, cudaStream_t st);
 void launch_p2g(const DevScene& d, const LaunchCfg& cfg, cudaStream_t st);
+// Admission (admission.cu): queued spawns into dead slots, the k-th dead slot in slot order
+// taking entry k < claim (scratch: claim_scratch_words(n_slots) words); live particles per
+// cell of a window of sw x sh cells at (ox, oy) into out (zeroed first).
+uint32_t claim_scratch_words(uint32_t n_slots);
+void launch_claim(float4* part, uint32_t n_slots, const float4* spawn, uint32_t claim, uint32_t* scratch,
+                  cudaStream_t st);
+void launch_cell_counts(const float4* part, uint32_t n_slots, int ox, int oy, int sw, int sh, uint32_t* out,
+                        cudaStream_t st);
 void launch_grid(const DevScene& d, const LaunchCfg& cfg, cudaStream_t st);
 // `second`: the pressure solve after the implicit viscosity (same matrix and hierarchy).
 cudaError_t launch_pressure(const DevScene& d, const LaunchCfg& cfg, cudaStream_t st, int second);

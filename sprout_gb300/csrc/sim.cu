@@ -111,6 +111,8 @@ struct SproutSim {
 
     ~SproutSim() {
         if (trace_buf) cudaFree(trace_buf);
+        if (d_window) cudaFree(d_window);
+        if (h_window) cudaFreeHost(h_window);
         drop_part_graphs();
         if (cap_stream) cudaStreamDestroy(cap_stream);
         if (stage_params) cudaFreeHost(stage_params);
@@ -371,6 +373,7 @@ struct SproutSim {
         }
         DevParams P;
         build_params(params, tank, thermal, caps, W, H, n_slots, dt_limit(), tool, &P);
+        P.ext_speed = std::max(P.ext_speed, spawn_speed);   // mod.rs:2300
         P.visc_mode = visc_mode;
         P.visc_levels = std::min(P.visc_levels, d.lv.tail);
         std::vector<DevMat> mats(kMaxMaterials);
@@ -553,41 +556,46 @@ struct SproutSim {
         return SPROUT_OK;
     }
 
-    int reset(const SproutParticle* in, uint32_t n) {
-        if (n > capacity) n = capacity;
-        std::vector<SproutParticle> ps(in, in + n);
-        for (uint32_t k = 0; k < n; k++) {
-            SproutParticle& q = ps[k];
-            q.id = k;
-            // Positions stay inside [2.01, size - 2.01], the range every substep leaves them in
-            // (particles.comp:912), so that the first gather's 3 x 3 stencils stay on the grid.
-            if (!std::isfinite(q.pos[0]) || !std::isfinite(q.pos[1]))
-                return fail(SPROUT_E_ARG, "particle " + std::to_string(k) + " has a non-finite position");
-            q.pos[0] = std::min(std::max(q.pos[0], 2.01f), (float)W - 2.01f);
-            q.pos[1] = std::min(std::max(q.pos[1], 2.01f), (float)H - 2.01f);
-            uint32_t mat = q.kind & 255u;
-            if (q.kind != 0u && mat != 0u) {
-                const MatProps& def = params.mat[mat - 1u];
-                if (q.t == -1.0e4f) {
-                    q.t = def.spawn_temp;
-                    q.kind |= 0x20000u;
-                }
-                if (q.s == -1.0f) q.s = def.diluent >= 0 ? std::min(std::max(def.load, 0.0f), 1.0f) : 1.0f;
-                if (q.kind & 0x20000u) {
-                    q.kind &= ~0x20000u;
-                    q.t = params.enthalpy_temp((int)mat - 1, q.s, q.t);
-                }
+    // Particle::settle_spawn (params.rs:70-85) and the position range every substep leaves a
+    // particle in, [2.01, size - 2.01] (particles.comp:912), so that the first gather's 3 x 3
+    // stencils stay on the grid.
+    int settle(SproutParticle& q, uint32_t k) const {
+        if (!std::isfinite(q.pos[0]) || !std::isfinite(q.pos[1]))
+            return fail(SPROUT_E_ARG, "particle " + std::to_string(k) + " has a non-finite position");
+        q.pos[0] = std::min(std::max(q.pos[0], 2.01f), (float)W - 2.01f);
+        q.pos[1] = std::min(std::max(q.pos[1], 2.01f), (float)H - 2.01f);
+        uint32_t mat = q.kind & 255u;
+        if (q.kind != 0u && mat != 0u) {
+            const MatProps& def = params.mat[mat - 1u];
+            if (q.t == -1.0e4f) {
+                q.t = def.spawn_temp;
+                q.kind |= 0x20000u;
+            }
+            if (q.s == -1.0f) q.s = def.diluent >= 0 ? std::min(std::max(def.load, 0.0f), 1.0f) : 1.0f;
+            if (q.kind & 0x20000u) {
+                q.kind &= ~0x20000u;
+                q.t = params.enthalpy_temp((int)mat - 1, q.s, q.t);
             }
         }
-        bool present[kMaxMaterials] = {};
-        bool th = solids_heated;
+        return SPROUT_OK;
+    }
+
+    // The materials of particles marked in present[], *th widened by their temperatures
+    // (note_materials, mod.rs:2050-2060).
+    void mark_materials(const SproutParticle* ps, uint32_t n, bool* present, bool* th) const {
         for (uint32_t k = 0; k < n; k++) {
             uint32_t m = ps[k].kind & 255u;
             if (m == 0u || ps[k].kind == 0u) continue;
             present[m - 1u] = true;
-            th |= std::fabs(ps[k].t - params.ambient_temp) > 0.05f || params.mat[m - 1u].self_heat > 0.0f;
+            *th |= std::fabs(ps[k].t - params.ambient_temp) > 0.05f || params.mat[m - 1u].self_heat > 0.0f;
         }
-        if (std::fabs(params.ambient_temp - kTRef) > 0.05f) th = true;
+    }
+
+    // The tank for the rows marked in present[] and the thermal flag (Tank::layout,
+    // mod.rs:271-329) with the capabilities and viscosity treatment that follow. Changes
+    // nothing unless every check passes: SPROUT_E_CAPACITY when the rows do not fit the
+    // accumulator channels, SPROUT_E_UNSUPPORTED for what this engine does not carry.
+    int set_tank(const bool* present, bool th) {
         std::vector<int> rows;
         for (int r = 0; r < kMaxMaterials; r++)
             if (present[r]) {
@@ -598,21 +606,55 @@ struct SproutSim {
         rows.erase(std::unique(rows.begin(), rows.end()), rows.end());
         Tank t;
         if (!t.layout(rows, params, th)) return fail(SPROUT_E_CAPACITY, "the tank's materials do not fit the accumulator channels");
+        const Tank old_tank = tank;
+        const bool old_thermal = thermal;
+        const uint32_t old_caps = caps;
+        const int old_visc = visc_mode;
         tank = t;
         thermal = th;
         caps = compute_caps();
-        if (tank.families > 0) return fail(SPROUT_E_UNSUPPORTED, "concentration families (a material with a diluent) are not carried by this engine yet");
-        if (caps & (CAP_RIGID | CAP_RHEO | CAP_MAGNET | CAP_ELASTIC | CAP_SETTLE | CAP_STEAM | CAP_REACT))
-            return fail(SPROUT_E_UNSUPPORTED, "the tank needs rigid / rheology / magnet / elastic / settling / steam / reaction passes, which this engine does not carry");
-        if (__builtin_popcount(tank.group_mask) > 1) return fail(SPROUT_E_UNSUPPORTED, "several phase groups in one tank (drift, pair tension) are not carried by this engine yet");
+        int rc = SPROUT_OK;
+        if (tank.families > 0)
+            rc = fail(SPROUT_E_UNSUPPORTED, "concentration families (a material with a diluent) are not carried by this engine yet");
+        else if (caps & (CAP_RIGID | CAP_RHEO | CAP_MAGNET | CAP_ELASTIC | CAP_SETTLE | CAP_STEAM | CAP_REACT))
+            rc = fail(SPROUT_E_UNSUPPORTED, "the tank needs rigid / rheology / magnet / elastic / settling / steam / reaction passes, which this engine does not carry");
+        else if (__builtin_popcount(tank.group_mask) > 1)
+            rc = fail(SPROUT_E_UNSUPPORTED, "several phase groups in one tank (drift, pair tension) are not carried by this engine yet");
         for (int r : tank.rows) {
             const MatProps& m = params.mat[r];
-            if (m.volatility > 0.0f || (thermal && m.boil < 1e8f))
-                return fail(SPROUT_E_UNSUPPORTED, "evaporation and boiling are not carried by this engine");
+            if (rc == SPROUT_OK && (m.volatility > 0.0f || (thermal && m.boil < 1e8f)))
+                rc = fail(SPROUT_E_UNSUPPORTED, "evaporation and boiling are not carried by this engine");
         }
-        int rc = derive_viscosity();
+        if (rc == SPROUT_OK) rc = derive_viscosity();
+        if (rc != SPROUT_OK) {
+            tank = old_tank;
+            thermal = old_thermal;
+            caps = old_caps;
+            visc_mode = old_visc;
+            return rc;
+        }
+        return SPROUT_OK;
+    }
+
+    int reset(const SproutParticle* in, uint32_t n) {
+        if (n > capacity) n = capacity;
+        std::vector<SproutParticle> ps(in, in + n);
+        for (uint32_t k = 0; k < n; k++) {
+            ps[k].id = k;
+            int rc = settle(ps[k], k);
+            if (rc != SPROUT_OK) return rc;
+        }
+        bool present[kMaxMaterials] = {};
+        bool th = solids_heated;
+        mark_materials(ps.data(), n, present, &th);
+        if (std::fabs(params.ambient_temp - kTRef) > 0.05f) th = true;
+        int rc = set_tank(present, th);
         if (rc != SPROUT_OK) return rc;
         n_slots = n;
+        next_id = n;
+        pending.clear();
+        spawn_speed = 0.0f;
+        was_reset = true;
         d.stride = std::max(tank.stride, 8);
         CUDA_TRY(cudaStreamSynchronize(stream));
         size_t nc = (size_t)W * H;
@@ -635,14 +677,135 @@ struct SproutSim {
         return upload_tables(nullptr);
     }
 
+    // FluidSim::spawn (mod.rs:2024-2046): particles queued for the next step call, at most
+    // kSpawnMax queued; ids follow the last given; settle_spawn; KIND_FRESH. *accepted = 0
+    // when their materials do not fit the tank (nothing changes then). Particles without a
+    // material are not queued (reset drops them too, mod.rs:1994).
+    static constexpr uint32_t kSpawnMax = 32768;   // mod.rs:63
+    std::vector<SproutParticle> pending;
+    uint32_t next_id = 0;
+    float spawn_speed = 0.0f;
+    bool was_reset = false;
+    float4* d_spawn = nullptr;        // kSpawnMax particles: the entries that claim dead slots
+    uint32_t* d_claim = nullptr;      // claim_scratch_words(capacity)
+    uint32_t* d_window = nullptr;     // cell_counts' window
+    size_t window_cap = 0;
+    uint32_t* h_window = nullptr;     // pinned copy of the window
+
+    int spawn(const SproutParticle* in, uint32_t n, uint32_t* accepted) {
+        *accepted = 0;
+        if (!was_reset) return fail(SPROUT_E_ARG, "spawn before reset");
+        const uint32_t room = kSpawnMax - (uint32_t)pending.size();
+        std::vector<SproutParticle> q;
+        q.reserve(std::min(n, room));
+        for (uint32_t k = 0; k < n && q.size() < room; k++) {
+            const uint32_t mat = in[k].kind & 255u;
+            if (in[k].kind == 0u || mat == 0u || mat > (uint32_t)kMaxMaterials) continue;
+            SproutParticle p = in[k];
+            p.id = next_id + (uint32_t)q.size();
+            int rc = settle(p, k);
+            if (rc != SPROUT_OK) return rc;
+            q.push_back(p);
+        }
+        bool present[kMaxMaterials] = {};
+        for (int r : tank.rows) present[r] = true;
+        const size_t before = tank.rows.size();
+        bool th = thermal;
+        mark_materials(q.data(), (uint32_t)q.size(), present, &th);
+        size_t after = 0;
+        for (int r = 0; r < kMaxMaterials; r++) after += present[r] ? 1 : 0;
+        if (after != before || th != thermal) {
+            int rc = set_tank(present, th);
+            if (rc == SPROUT_E_CAPACITY) return SPROUT_OK;   // they do not fit: none is accepted
+            if (rc != SPROUT_OK) return rc;
+        }
+        for (SproutParticle& p : q) {
+            spawn_speed = std::max(spawn_speed, std::hypot(p.vel[0], p.vel[1]));
+            p.kind |= KIND_FRESH;
+            pending.push_back(p);
+        }
+        next_id += (uint32_t)q.size();
+        *accepted = (uint32_t)q.size();
+        return SPROUT_OK;
+    }
+
+    // record (mod.rs:2486-2503, 2530-2534): the queue fills fresh slots while there are any,
+    // then dead slots (admission.cu), on the sim's stream.
+    int take_spawns() {
+        if (pending.empty()) return SPROUT_OK;
+        const uint32_t n = (uint32_t)pending.size();
+        const uint32_t fresh = std::min(n, capacity - n_slots);
+        if (fresh > 0) {
+            CUDA_TRY(cudaMemcpyAsync(d.part + 3 * (size_t)n_slots, pending.data(), (size_t)fresh * sizeof(SproutParticle),
+                                     cudaMemcpyHostToDevice, stream));
+            h2d_bytes += (size_t)fresh * sizeof(SproutParticle);
+            n_slots += fresh;
+        }
+        if (n > fresh) {
+            const uint32_t claim = n - fresh;
+            if (!d_spawn) {
+                int rc = alloc(&d_spawn, 3 * (size_t)kSpawnMax);
+                if (rc == SPROUT_OK) rc = alloc(&d_claim, claim_scratch_words(capacity));
+                if (rc != SPROUT_OK) return rc;
+            }
+            CUDA_TRY(cudaMemcpyAsync(d_spawn, pending.data() + fresh, (size_t)claim * sizeof(SproutParticle),
+                                     cudaMemcpyHostToDevice, stream));
+            h2d_bytes += (size_t)claim * sizeof(SproutParticle);
+            launch_claim(d.part, n_slots, d_spawn, claim, d_claim, stream);
+            CUDA_TRY(cudaGetLastError());
+        }
+        // the copies read the queue from pageable memory, which they have finished with on return
+        pending.clear();
+        return SPROUT_OK;
+    }
+
+    // FluidSim::cell_counts (mod.rs:3350-3387): live particles per cell of [lo, hi) row by
+    // row after the work queued so far, the particles queued by spawn included. Blocking.
+    int cell_counts(const int32_t lo[2], const int32_t hi[2], uint32_t* out, size_t cap, size_t* cells) {
+        if (lo[0] < 0 || lo[1] < 0 || hi[0] > W || hi[1] > H)
+            return fail(SPROUT_E_ARG, "the window of cell_counts leaves the grid");
+        const int sw = std::max(hi[0] - lo[0], 0), sh = std::max(hi[1] - lo[1], 0);
+        const size_t n = (size_t)sw * sh;
+        if (cells) *cells = n;
+        if (!out || n == 0) return SPROUT_OK;
+        if (cap < n) return fail(SPROUT_E_ARG, "cell_counts: the output holds fewer cells than the window");
+        if (n > window_cap) {
+            if (d_window) cudaFree(d_window);
+            if (h_window) cudaFreeHost(h_window);
+            d_window = nullptr;
+            h_window = nullptr;
+            window_cap = 0;
+            CUDA_TRY(cudaMalloc(&d_window, n * sizeof(uint32_t)));
+            CUDA_TRY(cudaMallocHost(&h_window, n * sizeof(uint32_t)));
+            window_cap = n;
+        }
+        launch_cell_counts(d.part, n_slots, lo[0], lo[1], sw, sh, d_window, stream);
+        CUDA_TRY(cudaGetLastError());
+        CUDA_TRY(cudaMemcpyAsync(h_window, d_window, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
+        CUDA_TRY(cudaStreamSynchronize(stream));
+        d2h_bytes += n * sizeof(uint32_t);
+        std::memcpy(out, h_window, n * sizeof(uint32_t));
+        for (const SproutParticle& p : pending) {
+            const int cx = (int)std::floor(p.pos[0]) - lo[0], cy = (int)std::floor(p.pos[1]) - lo[1];
+            if (cx >= 0 && cy >= 0 && cx < sw && cy < sh) out[(size_t)cy * sw + cx]++;
+        }
+        return SPROUT_OK;
+    }
+
     // What a step call does before its substeps run, on the sim's stream: the parameters and
     // material table (when they changed), the batch words of StepBuf.
     int prepare_step(uint32_t substeps, float target, const ToolState* tool) {
         enqueued = false;
+        if (!pending.empty()) {
+            int rc = take_spawns();
+            if (rc != SPROUT_OK) return rc;
+            enqueued = true;
+        }
         if (n_slots == 0 || tank.rows.empty()) return fail(SPROUT_E_ARG, "step before reset (no particles)");
         int rc = derive_viscosity();
         if (rc != SPROUT_OK) return rc;
         rc = upload_tables(tool);
+        spawn_speed = 0.0f;
         if (rc != SPROUT_OK) return rc;
         if (substeps == 0) return SPROUT_OK;
         const uint32_t fl = __builtin_bit_cast(uint32_t, std::max(target, 0.0f));
@@ -703,7 +866,9 @@ struct SproutSim {
     // FluidSim::step_blocking (mod.rs:3315-3338).
     int step_blocking(uint32_t substeps, const ToolState* tool) {
         if (substeps == 0) {
-            int rc = upload_tables(tool);
+            int rc = take_spawns();
+            if (rc == SPROUT_OK) rc = upload_tables(tool);
+            spawn_speed = 0.0f;
             if (rc != SPROUT_OK) return rc;
             CUDA_TRY(cudaStreamSynchronize(stream));
             return SPROUT_OK;
@@ -1334,6 +1499,15 @@ int sprout_sim_set_solids(SproutSim* sim, const float* sdf, const float* solid4,
 int sprout_sim_reset(SproutSim* sim, const SproutParticle* p, uint32_t n) {
     if (!sim || (!p && n > 0)) return fail(SPROUT_E_ARG, "null argument");
     return sim->reset(p, n);
+}
+int sprout_sim_spawn(SproutSim* sim, const SproutParticle* p, uint32_t n, uint32_t* accepted) {
+    if (!sim || !accepted || (!p && n > 0)) return fail(SPROUT_E_ARG, "null argument");
+    return sim->spawn(p, n, accepted);
+}
+int sprout_sim_cell_counts(SproutSim* sim, const int32_t lo[2], const int32_t hi[2], uint32_t* out, size_t cap,
+                           size_t* cells) {
+    if (!sim || !lo || !hi) return fail(SPROUT_E_ARG, "null argument");
+    return sim->cell_counts(lo, hi, out, cap, cells);
 }
 int sprout_sim_step(SproutSim* sim, uint32_t substeps, float target, const SproutTool* tool) {
     if (!sim) return fail(SPROUT_E_ARG, "null sim");
