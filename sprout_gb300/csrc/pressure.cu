@@ -64,6 +64,12 @@ struct Plain {
     DEV static void setR(const DevScene& d, int i, float2 v) { d.mgr[i] = v; }
     DEV static acc4* part(const DevScene& d) { return d.partials; }
     DEV static acc4 a4(float x, float y, float z, float w) { return make_float4(x, y, z, w); }
+    // the stored matrix as a tile region stages it: bytes per row of couplings, their address,
+    // the diagonal's array, and the row widened to FP32 in its staged slot
+    static constexpr int kABytes = 16;
+    DEV static const void* Araw(const DevScene& d, int i) { return d.mga + i; }
+    DEV static const float* Dptr(const DevScene& d) { return d.mgd; }
+    DEV static void widen(float4&) {}
 };
 
 // a pair of BF16 values in 32 bits (x in the low half), rounded to nearest even
@@ -113,6 +119,15 @@ struct Mixed {
     DEV static void setR(const DevScene& d, int i, float2 v) { d.mgr[i] = v; }
     DEV static acc4* part(const DevScene& d) { return d.partials64; }
     DEV static acc4 a4(double x, double y, double z, double w) { return Dbl4{x, y, z, w}; }
+    static constexpr int kABytes = 8;
+    DEV static const void* Araw(const DevScene& d, int i) { return d.hga + i; }
+    DEV static const float* Dptr(const DevScene& d) { return d.hgd; }
+    // the BF16 row copied into the first 8 bytes of the slot, widened in place
+    DEV static void widen(float4& slot) {
+        const uint2 u = *reinterpret_cast<const uint2*>(&slot);
+        const float2 a = unpack(u.x), b = unpack(u.y);
+        slot = make_float4(a.x, a.y, b.x, b.y);
+    }
 };
 
 template <class T>
@@ -369,10 +384,15 @@ struct Zc {
 };
 
 // A level's tile and RH cells around it staged in shared memory, RW x RW slots: the
-// diagonal (zero outside the level and where no unknown), the couplings, and up to three
-// vector fields. The V-cycle's and the apply's tile bodies load their region in one
-// parallel pass and then read only these slots: what they compute is the same, value for
-// value, as reading the fields from global memory one dependent load after another.
+// diagonal (zero outside the level and where no unknown), the couplings, up to three vector
+// fields, and for the tile's own cells (one per thread) two more vectors and the operator's
+// diagonal. A tile body comes in two halves: stage_* issues every load of the tile as an
+// asynchronous copy into a Region (zero-filled outside the level), and finish_* runs once
+// they have landed: each thread makes the slots it copied final (the diagonal's sign test,
+// the BF16 couplings widened, the fused residual update), then the tile's arithmetic reads
+// only the slots. Its values are the same, value for value, as reading the fields from global
+// memory one after another. Every block holds two Regions: while one tile computes, the
+// copies of its next tile are in flight (pipe_active).
 constexpr int RH = 2;
 constexpr int RW = 16 + 2 * RH;
 constexpr int RN = RW * RW;
@@ -380,9 +400,68 @@ struct Region {
     float dg[RN];
     float4 a[RN];
     float2 u[RN], v[RN], w[RN];
+    float2 o1[NT], o2[NT];
+    float od[NT];
+    float2 ring[32];   // the black cells just outside the tile, once computed (ring_cell)
 };
 DEV int rslot(int lx, int ly) { return (ly + RH) * RW + lx + RH; }
 __constant__ int RSTEP[4] = {-1, 1, -RW, RW};
+
+// The cells of a tile by colour for the smoothing passes: threads 0 .. 127 take the red
+// cells ((x + y) even; tiles start at even coordinates), 128 .. 255 the black ones, eight to
+// a row, so that no warp holds both the short red formula and the long black one.
+DEV int2 colour_cell() {
+    const int c = threadIdx.x & 127, ly = c >> 3;
+    return make_int2(2 * (c & 7) + ((ly & 1) ^ (threadIdx.x < 128 ? 0 : 1)), ly);
+}
+// The 32 black cells just outside a tile that its red border cells touch: slot j of side
+// s = r / 8: (-1, 2j), (16, 2j + 1), (2j, -1), (2j + 1, 16); and the slot of such a cell.
+DEV int2 ring_cell(int r) {
+    const int j = r & 7;
+    switch (r >> 3) {
+        case 0: return make_int2(-1, 2 * j);
+        case 1: return make_int2(16, 2 * j + 1);
+        case 2: return make_int2(2 * j, -1);
+        default: return make_int2(2 * j + 1, 16);
+    }
+}
+DEV int ring_of(int lnx, int lny) {
+    if (lnx < 0) return lny >> 1;
+    if (lnx > 15) return 8 + (lny >> 1);
+    if (lny < 0) return 16 + (lnx >> 1);
+    return 24 + (lnx >> 1);
+}
+
+// The slots of a region that thread threadIdx.x copies and makes final: k = threadIdx.x +
+// j NT (j < RJ), at cell (ox - RH + k % RW, oy - RH + k / RW) of the level.
+constexpr int RJ = (RN + NT - 1) / NT;
+
+// This block's work items k = 0, 1, ... (item(k): the one at blockIdx.x + k gridDim.x of
+// cnt) through the pipeline: stage(it, rg) issues item it's copies into a region; finish(it,
+// rg) computes it and ends with __syncthreads (so that the region can take the copies of a
+// later item). Item k + 1's copies are issued before item k computes.
+template <class I, class S, class F>
+DEV void pipe_tiles(uint32_t cnt, I&& item, Region* rg, S&& stage, F&& finish) {
+    if (blockIdx.x >= cnt) return;
+    uint32_t cur = item(0);
+    stage(cur, rg[0]);
+    cp_commit();
+    for (int k = 0;; k++) {
+        const bool more = blockIdx.x + (uint32_t)(k + 1) * gridDim.x < cnt;
+        uint32_t nxt = 0;
+        if (more) {
+            nxt = item(k + 1);
+            stage(nxt, rg[(k + 1) & 1]);
+            cp_commit();
+            cp_wait<1>();
+        } else {
+            cp_wait<0>();
+        }
+        finish(cur, rg[k & 1]);
+        if (!more) break;
+        cur = nxt;
+    }
+}
 
 template <class M>
 DEV float2 coarse_z(const DevScene& d, const Zc& zc, int mx, int my) {
@@ -390,39 +469,57 @@ DEV float2 coarse_z(const DevScene& d, const Zc& zc, int mx, int my) {
     return zc.s ? zc.s[k] : M::Z(d, zc.off + k);
 }
 
-
-// mg_down.comp on tile t of level l. On level 0 with `r_out` it also applies
-// cg_update.comp: x += alpha p and the residual update into r_out. Region: dg, a, and the
-// right-hand side (through R) in u.
+// mg_down.comp on tile t of level l, copies: the diagonal, the couplings, the right-hand
+// side (level 0: the residual before the update, and q when R.q) over the region; with
+// `update` (level 0 fused with cg_update.comp) the tile's own p, x and operator diagonal.
 template <class M>
-DEV void down_tile(const DevScene& d, int l, int t, const Rsrc<M>& R, float2* r_out, const float2* p, float2* sz, Region& rg) {
-    const Lv F = lev(d.lv, l), C = lev(d.lv, l + 1);
+DEV void stage_down(const DevScene& d, int l, int t, const Rsrc<M>& R, bool update, const float2* p, Region& rg) {
+    const Lv F = lev(d.lv, l);
     const int tx_n = tiles_x(F);
-    const int lx = threadIdx.x & 15, ly = threadIdx.x >> 4;
     const int ox = (t % tx_n) * 16, oy = (t / tx_n) * 16;
-    // every load of the region issued at once (none waits on another), then masked
+    const float2* r = R.r ? R.r : d.mgr;
 #pragma unroll
-    for (int j = 0; j < (RN + NT - 1) / NT; j++) {
+    for (int j = 0; j < RJ; j++) {
         const int k = threadIdx.x + j * NT;
         if (k >= RN) break;
         const int x = ox - RH + k % RW, y = oy - RH + k / RW;
-        float dd = 0.0f;
-        float4 aa = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-        float2 rr = make_float2(0.0f, 0.0f);
-        if (l_inside(F, x, y)) {
-            const int i = l_at(F, x, y);
-            dd = M::Dg(d, i);
-            aa = M::A(d, i);
-            rr = R.at(d, i);
-            if (!(dd > 0.0f)) {
-                dd = 0.0f;
-                aa = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-                rr = make_float2(0.0f, 0.0f);
-            }
+        const bool in = l_inside(F, x, y);
+        const int i = in ? l_at(F, x, y) : 0;
+        cp_async<4>(&rg.dg[k], M::Dptr(d) + i, in);
+        cp_async<M::kABytes>(&rg.a[k], M::Araw(d, i), in);
+        cp_async<8>(&rg.u[k], r + i, in);
+        if (R.q) cp_async<8>(&rg.v[k], R.q + i, in);
+    }
+    if (update) {
+        const int cx = ox + (threadIdx.x & 15), cy = oy + (threadIdx.x >> 4);
+        const bool in = l_inside(F, cx, cy);
+        const int i = in ? l_at(F, cx, cy) : 0;
+        cp_async<4>(&rg.od[threadIdx.x], d.mgd + i, in);
+        cp_async<8>(&rg.o1[threadIdx.x], p + i, in);
+        cp_async<8>(&rg.o2[threadIdx.x], d.pres + i, in);
+    }
+}
+
+// ... and its arithmetic. On level 0 with `r_out` it also applies cg_update.comp: x +=
+// alpha p and the residual update into r_out.
+template <class M>
+DEV void finish_down(const DevScene& d, int l, int t, const Rsrc<M>& R, float2* r_out, float2* sz, Region& rg) {
+    const Lv F = lev(d.lv, l), C = lev(d.lv, l + 1);
+    const int tx_n = tiles_x(F);
+    const int ox = (t % tx_n) * 16, oy = (t / tx_n) * 16;
+#pragma unroll
+    for (int j = 0; j < RJ; j++) {
+        const int k = threadIdx.x + j * NT;
+        if (k >= RN) break;
+        if (!(rg.dg[k] > 0.0f)) rg.dg[k] = 0.0f;
+        M::widen(rg.a[k]);
+        if (R.q) {   // R.at: r - alpha q
+            float2 v = rg.u[k];
+            const float2 qq = rg.v[k];
+            v.x = v.x - R.ax * qq.x;
+            v.y = v.y - R.ay * qq.y;
+            rg.u[k] = v;
         }
-        rg.dg[k] = dd;
-        rg.a[k] = aa;
-        rg.u[k] = rr;
     }
     __syncthreads();
     // the value of black slot k after the half-sweep from zero (mg_down black())
@@ -441,9 +538,11 @@ DEV void down_tile(const DevScene& d, int l, int t, const Rsrc<M>& R, float2* r_
         const float di = rg.dg[k];
         return make_float2(sum.x / di, sum.y / di);
     };
+    const int2 lc = colour_cell();
+    const int lx = lc.x, ly = lc.y, cell = ly * 16 + lx;
     const int cx = ox + lx, cy = oy + ly;
     const int k0 = rslot(lx, ly);
-    const bool red = ((cx + cy) & 1) == 0;
+    const bool red = threadIdx.x < 128;
     float2 z = make_float2(0.0f, 0.0f);
     if (l_inside(F, cx, cy)) {
         const int i = l_at(F, cx, cy);
@@ -456,34 +555,40 @@ DEV void down_tile(const DevScene& d, int l, int t, const Rsrc<M>& R, float2* r_
                 z = black(k0);
             }
         }
-        if (r_out && d.mgd[i] > 0.0f) {
+        if (r_out && rg.od[cell] > 0.0f) {
             // cg_update.comp: x += alpha p, r -= alpha q (unknowns of active tiles)
-            float2 pp = p[i];
-            float2 x = d.pres[i];
+            const float2 pp = rg.o1[cell];
+            float2 x = rg.o2[cell];
             x.x += R.ax * pp.x;
             x.y += R.ay * pp.y;
             d.pres[i] = x;
-            r_out[i] = R.at(d, i);
+            r_out[i] = rg.u[k0];
         }
         M::setX(d, i, z);
     }
-    sz[threadIdx.x] = z;
+    sz[cell] = z;
+    if (threadIdx.x < 32) {   // (a red warp) the black cells around the tile
+        const int2 rc = ring_cell(threadIdx.x);
+        const int kr = rslot(rc.x, rc.y);
+        rg.ring[threadIdx.x] = rg.dg[kr] > 0.0f ? black(kr) : make_float2(0.0f, 0.0f);
+    }
     __syncthreads();
-    if (((lx | ly) & 1) == 0) {
-        const int Cx = cx >> 1, Cy = cy >> 1;
+    if (threadIdx.x < 64) {   // the restriction: aggregate (ax, ay), its red cells (0, 0) and (1, 1)
+        const int ax = threadIdx.x & 7, ay = threadIdx.x >> 3;
+        const int Cx = (ox >> 1) + ax, Cy = (oy >> 1) + ay;
         if (Cx < C.w && Cy < C.h) {
             float sx = 0.0f, sy = 0.0f;
             for (int k = 0; k < 2; k++) {
-                const int kq = rslot(lx + k, ly + k);
+                const int lqx = 2 * ax + k, lqy = 2 * ay + k;
+                const int kq = rslot(lqx, lqy);
                 if (rg.dg[kq] <= 0.0f) continue;
                 const float4 w = rg.a[kq];
-                const int lqx = lx + k, lqy = ly + k;
                 for (int q = 0; q < 4; q++) {
                     const int kn = kq + RSTEP[q];
                     if (rg.dg[kn] <= 0.0f) continue;
                     const int lnx = lqx + NBX[q], lny = lqy + NBY[q];
                     const bool here = lnx >= 0 && lny >= 0 && lnx < 16 && lny < 16;
-                    const float2 zb = here ? sz[lny * 16 + lnx] : black(kn);
+                    const float2 zb = here ? sz[lny * 16 + lnx] : rg.ring[ring_of(lnx, lny)];
                     const float wd = wcomp(w, q);
                     sx += wd * zb.x;
                     sy += wd * zb.y;
@@ -495,44 +600,49 @@ DEV void down_tile(const DevScene& d, int l, int t, const Rsrc<M>& R, float2* r_
     __syncthreads();
 }
 
-// mg_up.comp on tile t of level l; on level 0 (flag) the tile's sums of r.z, r.r into
-// part[t]. Region: dg, a, the right-hand side in u, the pre-smoothed values (mgx) in v and
-// each slot's coarse-grid value in w.
+// mg_up.comp on tile t of level l, copies: the diagonal, the couplings, the right-hand side
+// (u), the pre-smoothed values mgx (v) and each slot's coarse-grid value (w; from zc.s, this
+// block's shared copy of the tail, in finish_up).
 template <class M>
-DEV void up_tile(const DevScene& d, int l, int t, bool flag, const Rsrc<M>& rhs, const Zc& zc, float2* sz,
-                 typename M::acc4* buf, Region& rg) {
-    using acc = typename M::acc;
+DEV void stage_up(const DevScene& d, int l, int t, const Rsrc<M>& rhs, const Zc& zc, Region& rg) {
     const Lv F = lev(d.lv, l);
     const int tx_n = tiles_x(F);
-    const int lx = threadIdx.x & 15, ly = threadIdx.x >> 4;
-    typename M::acc4* part = M::part(d);
     const int ox = (t % tx_n) * 16, oy = (t / tx_n) * 16;
+    const float2* r = rhs.r ? rhs.r : d.mgr;
 #pragma unroll
-    for (int j = 0; j < (RN + NT - 1) / NT; j++) {
+    for (int j = 0; j < RJ; j++) {
         const int k = threadIdx.x + j * NT;
         if (k >= RN) break;
         const int x = ox - RH + k % RW, y = oy - RH + k / RW;
-        float dd = 0.0f;
-        float4 aa = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-        float2 r = make_float2(0.0f, 0.0f), xm = r, zcv = r;
-        if (l_inside(F, x, y)) {
-            const int i = l_at(F, x, y);
-            dd = M::Dg(d, i);
-            aa = M::A(d, i);
-            r = rhs.at(d, i);
-            xm = M::X(d, i);
-            zcv = coarse_z<M>(d, zc, x, y);
-            if (!(dd > 0.0f)) {
-                dd = 0.0f;
-                aa = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-                r = xm = zcv = make_float2(0.0f, 0.0f);
-            }
+        const bool in = l_inside(F, x, y);
+        const int i = in ? l_at(F, x, y) : 0;
+        cp_async<4>(&rg.dg[k], M::Dptr(d) + i, in);
+        cp_async<M::kABytes>(&rg.a[k], M::Araw(d, i), in);
+        cp_async<8>(&rg.u[k], r + i, in);
+        cp_async<8>(&rg.v[k], d.mgx + i, in);
+        if (!zc.s) cp_async<8>(&rg.w[k], d.mgz + (in ? zc.off + (y >> 1) * zc.w + (x >> 1) : 0), in);
+    }
+}
+
+// ... and its arithmetic; on level 0 (flag) the tile's sums of r.z, r.r into part[t].
+template <class M>
+DEV void finish_up(const DevScene& d, int l, int t, bool flag, const Zc& zc, float2* sz, typename M::acc4* buf,
+                   Region& rg) {
+    using acc = typename M::acc;
+    const Lv F = lev(d.lv, l);
+    const int tx_n = tiles_x(F);
+    typename M::acc4* part = M::part(d);
+    const int ox = (t % tx_n) * 16, oy = (t / tx_n) * 16;
+#pragma unroll
+    for (int j = 0; j < RJ; j++) {
+        const int k = threadIdx.x + j * NT;
+        if (k >= RN) break;
+        if (!(rg.dg[k] > 0.0f)) rg.dg[k] = 0.0f;
+        M::widen(rg.a[k]);
+        if (zc.s) {
+            const int x = ox - RH + k % RW, y = oy - RH + k / RW;
+            rg.w[k] = l_inside(F, x, y) ? coarse_z<M>(d, zc, x, y) : make_float2(0.0f, 0.0f);
         }
-        rg.dg[k] = dd;
-        rg.a[k] = aa;
-        rg.u[k] = r;
-        rg.v[k] = xm;
-        rg.w[k] = zcv;
     }
     __syncthreads();
     // the new value of black slot k after the coarse correction (mg_up black())
@@ -551,13 +661,20 @@ DEV void up_tile(const DevScene& d, int l, int t, bool flag, const Rsrc<M>& rhs,
         const float di = rg.dg[k];
         return make_float2(sum.x / di, sum.y / di);
     };
+    const int2 lc = colour_cell();
+    const int lx = lc.x, ly = lc.y, cell = ly * 16 + lx;
     const int cx = ox + lx, cy = oy + ly;
     const int k0 = rslot(lx, ly);
-    const bool red = ((cx + cy) & 1) == 0;
+    const bool red = threadIdx.x < 128;
     const bool unk = rg.dg[k0] > 0.0f;
     float2 z = make_float2(0.0f, 0.0f);
     if (unk && !red) z = black(k0);
-    sz[threadIdx.x] = z;
+    sz[cell] = z;
+    if (threadIdx.x < 32) {   // (a red warp, idle here) the black cells around the tile
+        const int2 rc = ring_cell(threadIdx.x);
+        const int kr = rslot(rc.x, rc.y);
+        rg.ring[threadIdx.x] = rg.dg[kr] > 0.0f ? black(kr) : make_float2(0.0f, 0.0f);
+    }
     __syncthreads();
     typename M::acc4 a4 = M::a4(0, 0, 0, 0);
     if (l_inside(F, cx, cy)) {
@@ -572,7 +689,7 @@ DEV void up_tile(const DevScene& d, int l, int t, bool flag, const Rsrc<M>& rhs,
                     if (rg.dg[kn] <= 0.0f) continue;
                     const int lnx = lx + NBX[q], lny = ly + NBY[q];
                     const bool here = lnx >= 0 && lny >= 0 && lnx < 16 && lny < 16;
-                    const float2 zb = here ? sz[lny * 16 + lnx] : black(kn);
+                    const float2 zb = here ? sz[lny * 16 + lnx] : rg.ring[ring_of(lnx, lny)];
                     const float wd = wcomp(w, q);
                     sx += wd * zb.x;
                     sy += wd * zb.y;
@@ -585,7 +702,7 @@ DEV void up_tile(const DevScene& d, int l, int t, bool flag, const Rsrc<M>& rhs,
         M::setZ(d, i, z);
     }
     if (flag) {
-        buf[threadIdx.x] = a4;
+        buf[cell] = a4;
         block_tree(buf);
         if (threadIdx.x == 0) part[t] = buf[0];
     }
@@ -752,17 +869,30 @@ DEV void for_active(const DevScene& d, int l, const TileCache& tc, F&& f) {
         f((int)((cached && k < kCachePer) ? tc.item[l][k] : list[j]));
 }
 
+// The same share through the two-region pipeline (stage / finish halves of a tile body).
+template <class S, class F>
+DEV void pipe_active(const DevScene& d, int l, const TileCache& tc, Region* rg, S&& stage, F&& finish) {
+    const bool cached = l < kCacheLevels;
+    const uint32_t cnt = cached ? tc.cnt[l] : *(volatile uint32_t*)&d.pcount[l];
+    const uint32_t* list = d.plist + d.lv.toff[l];
+    pipe_tiles(
+        cnt, [&](int k) { return (cached && k < kCachePer) ? tc.item[l][k] : list[blockIdx.x + (uint32_t)k * gridDim.x]; },
+        rg, [&](uint32_t t, Region& r) { stage((int)t, r); }, [&](uint32_t t, Region& r) { finish((int)t, r); });
+}
+
 // One V-cycle of one scene: level 0's right-hand side through R (fused with the CG update
 // when R.q is set), result in mgz of level 0, partials of r.z and r.r. Returns false on a
 // barrier timeout.
 template <class M>
 DEV bool vcycle(const DevScene& d, const Tail& tl, const Rsrc<M>& R, float2* r_out, const float2* p, const float2* r_new,
-                float2* sz, typename M::acc4* buf, Region& rg, const TileCache& tc) {
+                float2* sz, typename M::acc4* buf, Region* rg, const TileCache& tc) {
     const int tail = d.lv.tail;
     for (int l = 0; l < tail; l++) {
         Rsrc<M> Rl = R;
         if (l > 0) Rl = Rsrc<M>{nullptr, nullptr, 0.0f, 0.0f};
-        for_active(d, l, tc, [&](int t) { down_tile<M>(d, l, t, Rl, l == 0 ? r_out : nullptr, p, sz, rg); });
+        float2* ro = l == 0 ? r_out : nullptr;
+        pipe_active(d, l, tc, rg, [&](int t, Region& r) { stage_down<M>(d, l, t, Rl, ro != nullptr, p, r); },
+                    [&](int t, Region& r) { finish_down<M>(d, l, t, Rl, ro, sz, r); });
         if (!grid_sync(d.K)) return false;
     }
     phase_tail<M>(d, tl, blockIdx.x == 0);
@@ -770,7 +900,8 @@ DEV bool vcycle(const DevScene& d, const Tail& tl, const Rsrc<M>& R, float2* r_o
         const Lv C = lev(d.lv, l + 1);
         const Zc zc{(l == tail - 1) ? tl.x : nullptr, C.off, C.w};
         const Rsrc<M> rhs = l == 0 ? Rsrc<M>{r_new, nullptr, 0.0f, 0.0f} : Rsrc<M>{nullptr, nullptr, 0.0f, 0.0f};
-        for_active(d, l, tc, [&](int t) { up_tile<M>(d, l, t, l == 0, rhs, zc, sz, buf, rg); });
+        pipe_active(d, l, tc, rg, [&](int t, Region& r) { stage_up<M>(d, l, t, rhs, zc, r); },
+                    [&](int t, Region& r) { finish_up<M>(d, l, t, l == 0, zc, sz, buf, r); });
         if (!grid_sync(d.K)) return false;
     }
     return true;
@@ -809,44 +940,51 @@ DEV void true_residual_tile(const DevScene& d, int t, Dbl4* part, Dbl4* buf) {
 }
 
 // cg_apply.comp on level-0 tile t: p = z + beta p_old, q = A p (the FP32 operator), the
-// tile's sum of p.q into part[n + t]. Region (one ring used): the operator's diagonal and
-// couplings, and the new direction p of every slot in u.
+// tile's sum of p.q into part[n + t]. Copies (one ring around the tile is enough): the
+// operator's diagonal, z (u) and p_old (v, unless both betas are zero); the couplings of the
+// tile's own cells.
+DEV void stage_apply(const DevScene& d, int t, bool nob, const float2* p_old, Region& rg) {
+    const Lv F = lev(d.lv, 0);
+    const int tx_n = tiles_x(F);
+    const int ox = (t % tx_n) * 16, oy = (t / tx_n) * 16;
+#pragma unroll
+    for (int j = 0; j < RJ; j++) {
+        const int k = threadIdx.x + j * NT;
+        if (k >= RN) break;
+        const int kx = k % RW, ky = k / RW;
+        if (kx == 0 || ky == 0 || kx == RW - 1 || ky == RW - 1) continue;
+        const int x = ox - RH + kx, y = oy - RH + ky;
+        const bool in = l_inside(F, x, y);
+        const int i = in ? l_at(F, x, y) : 0;
+        cp_async<4>(&rg.dg[k], d.mgd + i, in);
+        cp_async<8>(&rg.u[k], d.mgz + i, in);
+        if (!nob) cp_async<8>(&rg.v[k], p_old + i, in);
+    }
+    const int cx = ox + (threadIdx.x & 15), cy = oy + (threadIdx.x >> 4);
+    const bool in = l_inside(F, cx, cy);
+    cp_async<16>(&rg.a[rslot(threadIdx.x & 15, threadIdx.x >> 4)], d.mga + (in ? l_at(F, cx, cy) : 0), in);
+}
+
 template <class M>
-DEV void apply_tile(const DevScene& d, int t, float b0, float b1, const float2* p_old, float2* p_new,
-                    typename M::acc4* buf, Region& rg) {
+DEV void finish_apply(const DevScene& d, int t, float b0, float b1, float2* p_new, typename M::acc4* buf, Region& rg) {
     using acc = typename M::acc;
     const Lv F = lev(d.lv, 0);
     const int tx_n = tiles_x(F);
     const int n = d.nwg;
     typename M::acc4* part = M::part(d) + n;
     const bool nob = b0 == 0.0f && b1 == 0.0f;
-    auto direction = [&](int i) {
-        float2 z = d.mgz[i];
-        if (nob) return z;
-        float2 po = p_old[i];
-        return make_float2(b0 != 0.0f ? z.x + b0 * po.x : z.x, b1 != 0.0f ? z.y + b1 * po.y : z.y);
-    };
     const int ox = (t % tx_n) * 16, oy = (t / tx_n) * 16;
 #pragma unroll
-    for (int j = 0; j < (RN + NT - 1) / NT; j++) {
+    for (int j = 0; j < RJ; j++) {
         const int k = threadIdx.x + j * NT;
         if (k >= RN) break;
-        const int x = ox - RH + k % RW, y = oy - RH + k / RW;
         const int kx = k % RW, ky = k / RW;
-        if (kx == 0 || ky == 0 || kx == RW - 1 || ky == RW - 1) continue;   // one ring is enough
-        float dd = 0.0f;
-        float2 pp = make_float2(0.0f, 0.0f);
-        if (l_inside(F, x, y)) {
-            const int i = l_at(F, x, y);
-            dd = d.mgd[i];
-            pp = direction(i);
-            if (!(dd > 0.0f)) {
-                dd = 0.0f;
-                pp = make_float2(0.0f, 0.0f);
-            }
+        if (kx == 0 || ky == 0 || kx == RW - 1 || ky == RW - 1) continue;
+        if (!(rg.dg[k] > 0.0f)) rg.dg[k] = 0.0f;
+        if (!nob) {   // the direction p = z + beta p_old
+            const float2 z = rg.u[k], po = rg.v[k];
+            rg.u[k] = make_float2(b0 != 0.0f ? z.x + b0 * po.x : z.x, b1 != 0.0f ? z.y + b1 * po.y : z.y);
         }
-        rg.dg[k] = dd;
-        rg.u[k] = pp;
     }
     __syncthreads();
     const int cx = ox + (threadIdx.x & 15), cy = oy + (threadIdx.x >> 4);
@@ -857,7 +995,7 @@ DEV void apply_tile(const DevScene& d, int t, float b0, float b1, const float2* 
         const float D = rg.dg[k0];
         if (D > 0.0f) {
             const float2 pp = rg.u[k0];
-            const float4 w = d.mga[i];
+            const float4 w = rg.a[k0];
             float qx = D * pp.x, qy = D * pp.y;
             for (int q = 0; q < 4; q++) {
                 const int kn = k0 + RSTEP[q];
@@ -971,10 +1109,10 @@ DEV void scal_stats(SolveState* G, const Solve<T>& K, int second, double true_re
 // The whole pressure solve. `second`: the solve after the implicit viscosity (cg_reduce
 // mode 8/9: same matrix and hierarchy, density correction counted as solved).
 template <class M>
-__global__ void __launch_bounds__(NT) k_mgpcg(DevScene d, int second, int scale_mode) {
+__global__ void __launch_bounds__(NT, 2) k_mgpcg(DevScene d, int second, int scale_mode) {
     using acc = typename M::acc;
     using acc4 = typename M::acc4;
-    __shared__ Region rg;
+    __shared__ Region rg[2];
     __shared__ TileCache tc;
     __shared__ float2 sz[NT];
     __shared__ acc4 buf[NT];
@@ -1017,7 +1155,10 @@ __global__ void __launch_bounds__(NT) k_mgpcg(DevScene d, int second, int scale_
     float2* p_new = d.cgp2;
     for (uint32_t it = 0; it < P->pressure_max_iters; it++) {
         if (K.done[0] && K.done[1]) break;
-        for_active(d, 0, tc, [&](int t) { apply_tile<M>(d, t, (float)K.beta[0], (float)K.beta[1], p_old, p_new, buf, rg); });
+        const float b0 = (float)K.beta[0], b1 = (float)K.beta[1];
+        const bool nob = b0 == 0.0f && b1 == 0.0f;
+        pipe_active(d, 0, tc, rg, [&](int t, Region& r) { stage_apply(d, t, nob, p_old, r); },
+                    [&](int t, Region& r) { finish_apply<M>(d, t, b0, b1, p_new, buf, r); });
         if (!grid_sync(d.K)) return;
         {
             acc4 b = total(part + n, n, buf);
@@ -1119,16 +1260,37 @@ DEV void for_active_b(const BatchView& B, int l, const TileCache& tc, F&& f) {
     }
 }
 
+// The same through the two-region pipeline: stage(s, d, t, rg) / finish(s, d, t, rg).
+template <class S, class F>
+DEV void pipe_active_b(const BatchView& B, int l, const TileCache& tc, Region* rg, S&& stage, F&& finish) {
+    const bool cached = l < kCacheLevels;
+    const int N = cached ? (int)tc.cnt[l] : *(volatile const int*)&B.aoff[l * (B.ns + 1) + B.ns];
+    pipe_tiles(
+        (uint32_t)N,
+        [&](int k) {
+            return (cached && k < kCachePer) ? tc.item[l][k] : batch_item(B, l, (int)(blockIdx.x + (uint32_t)k * gridDim.x));
+        },
+        rg,
+        [&](uint32_t it, Region& r) {
+            const int s = (int)(it >> 16);
+            stage(s, B.scenes[s], (int)(it & 0xffffu), r);
+        },
+        [&](uint32_t it, Region& r) {
+            const int s = (int)(it >> 16);
+            finish(s, B.scenes[s], (int)(it & 0xffffu), r);
+        });
+}
+
 DEV float2* parity_r(const DevScene& d, int it) { return (it & 1) ? d.mgr2 : d.mgr; }
 DEV float2* parity_p(const DevScene& d, int it) { return (it & 1) ? d.cgp2 : d.cgp; }
 
 }  // namespace
 
 template <class M>
-__global__ void __launch_bounds__(NT) k_mgpcg_batch(BatchView B, int second) {
+__global__ void __launch_bounds__(NT, 2) k_mgpcg_batch(BatchView B, int second) {
     using acc = typename M::acc;
     using acc4 = typename M::acc4;
-    __shared__ Region rg;
+    __shared__ Region rg[2];
     __shared__ TileCache tc;
     __shared__ float2 sz[NT];
     __shared__ acc4 buf[NT];
@@ -1188,14 +1350,23 @@ __global__ void __launch_bounds__(NT) k_mgpcg_batch(BatchView B, int second) {
         const bool fused = it >= 0;
         const int ir = fused ? it : 0;
         for (int l = 0; l < B.max_tail; l++) {
-            for_active_b(B, l, tc, [&](int s, const DevScene& d, int t) {
-                if (l >= d.lv.tail || (fused && !running(s, it))) return;
+            auto rsrc = [&](int s, const DevScene& d) {
                 const Solve<acc>& K = KS[s];
                 Rsrc<M> R{nullptr, nullptr, 0.0f, 0.0f};
                 if (l == 0) R = fused ? Rsrc<M>{parity_r(d, ir), d.cgq, (float)K.alpha[0], (float)K.alpha[1]}
                                       : Rsrc<M>{parity_r(d, ir), nullptr, 0.0f, 0.0f};
-                down_tile<M>(d, l, t, R, (l == 0 && fused) ? parity_r(d, ir + 1) : nullptr, parity_p(d, ir + 1), sz, rg);
-            });
+                return R;
+            };
+            pipe_active_b(
+                B, l, tc, rg,
+                [&](int s, const DevScene& d, int t, Region& r) {
+                    if (l >= d.lv.tail || (fused && !running(s, it))) return;
+                    stage_down<M>(d, l, t, rsrc(s, d), l == 0 && fused, parity_p(d, ir + 1), r);
+                },
+                [&](int s, const DevScene& d, int t, Region& r) {
+                    if (l >= d.lv.tail || (fused && !running(s, it))) return;
+                    finish_down<M>(d, l, t, rsrc(s, d), (l == 0 && fused) ? parity_r(d, ir + 1) : nullptr, sz, r);
+                });
             if (!grid_sync(BK)) return false;
         }
         for (int s = blockIdx.x; s < B.ns; s += gridDim.x) {
@@ -1207,14 +1378,24 @@ __global__ void __launch_bounds__(NT) k_mgpcg_batch(BatchView B, int second) {
         }
         if (!grid_sync(BK)) return false;
         for (int l = B.max_tail - 1; l >= 0; l--) {
-            for_active_b(B, l, tc, [&](int s, const DevScene& d, int t) {
-                if (l >= d.lv.tail || (fused && !running(s, it))) return;
+            auto zc_of = [&](const DevScene& d) {
                 const Lv C = lev(d.lv, l + 1);
-                const Zc zc{nullptr, C.off, C.w};
-                const Rsrc<M> rhs = l == 0 ? Rsrc<M>{parity_r(d, fused ? ir + 1 : 0), nullptr, 0.0f, 0.0f}
-                                           : Rsrc<M>{nullptr, nullptr, 0.0f, 0.0f};
-                up_tile<M>(d, l, t, l == 0, rhs, zc, sz, buf, rg);
-            });
+                return Zc{nullptr, C.off, C.w};
+            };
+            auto rhs_of = [&](const DevScene& d) {
+                return l == 0 ? Rsrc<M>{parity_r(d, fused ? ir + 1 : 0), nullptr, 0.0f, 0.0f}
+                              : Rsrc<M>{nullptr, nullptr, 0.0f, 0.0f};
+            };
+            pipe_active_b(
+                B, l, tc, rg,
+                [&](int s, const DevScene& d, int t, Region& r) {
+                    if (l >= d.lv.tail || (fused && !running(s, it))) return;
+                    stage_up<M>(d, l, t, rhs_of(d), zc_of(d), r);
+                },
+                [&](int s, const DevScene& d, int t, Region& r) {
+                    if (l >= d.lv.tail || (fused && !running(s, it))) return;
+                    finish_up<M>(d, l, t, l == 0, zc_of(d), sz, buf, r);
+                });
             if (!grid_sync(BK)) return false;
         }
         return true;
@@ -1240,11 +1421,17 @@ __global__ void __launch_bounds__(NT) k_mgpcg_batch(BatchView B, int second) {
         }
         __syncthreads();
         if (!s_run) break;
-        for_active_b(B, 0, tc, [&](int s, const DevScene& d, int t) {
-            if (!running(s, it)) return;
-            const Solve<acc>& K = KS[s];
-            apply_tile<M>(d, t, (float)K.beta[0], (float)K.beta[1], parity_p(d, it), parity_p(d, it + 1), buf, rg);
-        });
+        pipe_active_b(
+            B, 0, tc, rg,
+            [&](int s, const DevScene& d, int t, Region& r) {
+                if (!running(s, it)) return;
+                const float b0 = (float)KS[s].beta[0], b1 = (float)KS[s].beta[1];
+                stage_apply(d, t, b0 == 0.0f && b1 == 0.0f, parity_p(d, it), r);
+            },
+            [&](int s, const DevScene& d, int t, Region& r) {
+                if (!running(s, it)) return;
+                finish_apply<M>(d, t, (float)KS[s].beta[0], (float)KS[s].beta[1], parity_p(d, it + 1), buf, r);
+            });
         if (!grid_sync(BK)) return;
         for (int s = blockIdx.x; s < B.ns; s += gridDim.x) {
             if (!running(s, it)) continue;

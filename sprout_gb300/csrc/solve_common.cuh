@@ -81,6 +81,24 @@ DEV bool grid_sync(SolveState* K) {
     return s_ok != 0;
 }
 
+// Asynchronous copies global -> shared (cp.async, N = 4, 8 or 16 bytes, both addresses
+// N-aligned): when `ok` is false nothing is read and the N bytes are zero-filled (g must
+// still be a valid address). A thread sees its own copies after cp_wait; other threads'
+// after a __syncthreads that follows their cp_wait.
+template <int N>
+DEV void cp_async(void* s, const void* g, bool ok) {
+    const uint32_t sa = (uint32_t)__cvta_generic_to_shared(s);
+    const int src = ok ? N : 0;
+    if constexpr (N == 16)
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(sa), "l"(g), "r"(src) : "memory");
+    else
+        asm volatile("cp.async.ca.shared.global [%0], [%1], %2, %3;\n" ::"r"(sa), "l"(g), "n"(N), "r"(src) : "memory");
+}
+DEV void cp_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+// waits until at most N of this thread's committed groups are still in flight
+template <int N>
+DEV void cp_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
 DEV float4 add4(float4 a, float4 b) { return make_float4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w); }
 DEV Dbl4 add4(Dbl4 a, Dbl4 b) { return Dbl4{a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w}; }
 
@@ -90,15 +108,35 @@ DEV void trace_launch_done(SolveState* K) {
     if (blockIdx.x == 0 && threadIdx.x == 0 && K->trace) K->trace_base += K->bar_count / gridDim.x;
 }
 
-// Work-group tree of reduce.glsl:5-14 over the 256 values in buf; result in buf[0].
+DEV float4 shfl_down4(float4 v, int s) {
+    return make_float4(__shfl_down_sync(0xffffffffu, v.x, s), __shfl_down_sync(0xffffffffu, v.y, s),
+                       __shfl_down_sync(0xffffffffu, v.z, s), __shfl_down_sync(0xffffffffu, v.w, s));
+}
+DEV Dbl4 shfl_down4(Dbl4 v, int s) {
+    return Dbl4{__shfl_down_sync(0xffffffffu, v.x, s), __shfl_down_sync(0xffffffffu, v.y, s),
+                __shfl_down_sync(0xffffffffu, v.z, s), __shfl_down_sync(0xffffffffu, v.w, s)};
+}
+
+// Work-group tree of reduce.glsl:5-14 over the 256 values in buf; result in buf[0]. The
+// pairs are those of the tree (t with t + s, s = 128 .. 1): the three wide steps through
+// shared memory, the last five inside the first warp by shuffles.
 template <class T>
 DEV void block_tree(T* buf) {
     const int t = threadIdx.x;
     __syncthreads();
-    for (int s = 128; s > 0; s >>= 1) {
+    for (int s = 128; s >= 32; s >>= 1) {
         if (t < s) buf[t] = add4(buf[t], buf[t + s]);
         __syncthreads();
     }
+    if (t < 32) {
+        T v = buf[t];
+        for (int s = 16; s > 0; s >>= 1) {
+            const T o = shfl_down4(v, s);
+            if (t < s) v = add4(v, o);
+        }
+        if (t == 0) buf[0] = v;
+    }
+    __syncthreads();
 }
 
 // total() of reduce_tail.glsl:28-41: thread t sums partials t, t + 256, ... in order,
