@@ -436,31 +436,12 @@ DEV int ring_of(int lnx, int lny) {
 // j NT (j < RJ), at cell (ox - RH + k % RW, oy - RH + k / RW) of the level.
 constexpr int RJ = (RN + NT - 1) / NT;
 
-// This block's work items k = 0, 1, ... (item(k): the one at blockIdx.x + k gridDim.x of
-// cnt) through the pipeline: stage(it, rg) issues item it's copies into a region; finish(it,
-// rg) computes it and ends with __syncthreads (so that the region can take the copies of a
-// later item). Item k + 1's copies are issued before item k computes.
+// This block's work items through the pipeline of solve_common.cuh with kDepth regions:
+// stage(it, rg) issues item it's copies into a region, finish(it, rg) computes it.
+constexpr int kDepth = 2;
 template <class I, class S, class F>
 DEV void pipe_tiles(uint32_t cnt, I&& item, Region* rg, S&& stage, F&& finish) {
-    if (blockIdx.x >= cnt) return;
-    uint32_t cur = item(0);
-    stage(cur, rg[0]);
-    cp_commit();
-    for (int k = 0;; k++) {
-        const bool more = blockIdx.x + (uint32_t)(k + 1) * gridDim.x < cnt;
-        uint32_t nxt = 0;
-        if (more) {
-            nxt = item(k + 1);
-            stage(nxt, rg[(k + 1) & 1]);
-            cp_commit();
-            cp_wait<1>();
-        } else {
-            cp_wait<0>();
-        }
-        finish(cur, rg[k & 1]);
-        if (!more) break;
-        cur = nxt;
-    }
+    pipeline<kDepth>(cnt, item, [&](uint32_t it, int b) { stage(it, rg[b]); }, [&](uint32_t it, int b) { finish(it, rg[b]); });
 }
 
 template <class M>
@@ -1112,7 +1093,7 @@ template <class M>
 __global__ void __launch_bounds__(NT, 2) k_mgpcg(DevScene d, int second, int scale_mode) {
     using acc = typename M::acc;
     using acc4 = typename M::acc4;
-    __shared__ Region rg[2];
+    __shared__ Region rg[kDepth];
     __shared__ TileCache tc;
     __shared__ float2 sz[NT];
     __shared__ acc4 buf[NT];
@@ -1290,7 +1271,7 @@ template <class M>
 __global__ void __launch_bounds__(NT, 2) k_mgpcg_batch(BatchView B, int second) {
     using acc = typename M::acc;
     using acc4 = typename M::acc4;
-    __shared__ Region rg[2];
+    __shared__ Region rg[kDepth];
     __shared__ TileCache tc;
     __shared__ float2 sz[NT];
     __shared__ acc4 buf[NT];

@@ -99,6 +99,29 @@ DEV void cp_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 template <int N>
 DEV void cp_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
+// This block's work items k = 0, 1, ... (item(k): the one at blockIdx.x + k gridDim.x of
+// cnt) through a pipeline of D staging buffers: stage(it, b) issues item it's asynchronous
+// copies into buffer b; finish(it, b) computes the item from them and ends with
+// __syncthreads (so that the buffer can take a later item's copies). While item k computes,
+// the copies of items k + 1 .. k + D - 1 are in flight (one commit group per item, empty
+// past the last).
+template <int D, class I, class S, class F>
+DEV void pipeline(uint32_t cnt, I&& item, S&& stage, F&& finish) {
+    if (blockIdx.x >= cnt) return;
+    const uint32_t mine = (cnt - blockIdx.x + gridDim.x - 1) / gridDim.x;
+    for (int k = 0; k < D - 1; k++) {
+        if ((uint32_t)k < mine) stage(item(k), k);
+        cp_commit();
+    }
+    for (uint32_t k = 0; k < mine; k++) {
+        const uint32_t ahead = k + D - 1;
+        if (ahead < mine) stage(item((int)ahead), (int)(ahead % D));
+        cp_commit();
+        cp_wait<D - 1>();
+        finish(item((int)k), (int)(k % D));
+    }
+}
+
 DEV float4 add4(float4 a, float4 b) { return make_float4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w); }
 DEV Dbl4 add4(Dbl4 a, Dbl4 b) { return Dbl4{a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w}; }
 

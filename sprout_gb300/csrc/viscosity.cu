@@ -261,13 +261,21 @@ struct VCfg {
     static constexpr int NMAX = RWMAX * RWMAX;
 };
 
+// One tile's copies, staged asynchronously (vmg.glsl:90-111 load_region and what the pass
+// reads besides): the level's matrix (vma, vmb, vmd), the right-hand side (sr) and two more
+// per-cell fields e1, e2 (the way up: the pre-smoothed values and the coarse values; the
+// update: A z and the old q), zero-filled outside the level.
+template <int NU>
+struct VStage {
+    static constexpr int N = VCfg<NU>::NMAX;
+    float4 sa[N], sb[N];
+    float2 sd[N], sr[N], e1[N], e2[N];
+};
+
 template <int NU>
 struct VSmem {
-    float4 sa[VCfg<NU>::NMAX];
-    float4 sb[VCfg<NU>::NMAX];
-    float2 sd[VCfg<NU>::NMAX];
-    float2 sx[VCfg<NU>::NMAX];
-    float2 sr[VCfg<NU>::NMAX];
+    VStage<NU> st[2];
+    float2 sx[VCfg<NU>::NMAX];   // the iterate of the tile being computed
     float2 sres[NT];
     float4 buf[NT];
 };
@@ -278,100 +286,110 @@ struct VScal {
     uint32_t done, iters;
 };
 
-// One region of RH cells around a 16 x 16 tile: the matrix, right-hand side and iterate.
+// One region of RH cells around a 16 x 16 tile: the matrix, right-hand side and extra fields
+// in a staging buffer g, the iterate in sx.
 template <int NU, int RH>
 struct Region {
     static constexpr int RW = 16 + 2 * RH;
     static constexpr int N = RW * RW;
     static constexpr int PER = (N + NT - 1) / NT;
+    VStage<NU>& g;
+    float2* sx;
     VSmem<NU>& s;
     int ox, oy;   // first cell of the tile
 
     DEV int cell_x(int k) const { return ox - RH + k % RW; }
     DEV int cell_y(int k) const { return oy - RH + k / RW; }
     DEV static bool red(int k) { return (((k % RW) + (k / RW)) & 1) == 0; }   // ox, oy, 2 RH even
-    DEV static bool in_ring(int k, int lo) {
-        int lx = k % RW, ly = k / RW;
-        return lx >= lo && ly >= lo && lx < RW - lo && ly < RW - lo;
-    }
     DEV static int tile_slot(int t) { return ((t >> 4) + RH) * RW + (t & 15) + RH; }
 
     // offd of vmg.glsl:70-78 at slot k (x in sx)
     DEV float2 offd(int k) const {
-        const float4 a = s.sa[k], b = s.sb[k];
-        const float2 xl = s.sx[k - 1], xr = s.sx[k + 1], xd = s.sx[k - RW], xu = s.sx[k + RW];
-        float u = a.x * xl.x + s.sa[k + 1].x * xr.x + a.y * xd.x + s.sa[k + RW].y * xu.x
-                + b.x * s.sx[k].y + b.y * xl.y + b.z * xu.y + b.w * s.sx[k + RW - 1].y;
-        float v = a.z * xl.y + s.sa[k + 1].z * xr.y + a.w * xd.y + s.sa[k + RW].w * xu.y
-                + b.x * s.sx[k].x + s.sb[k + 1].y * xr.x + s.sb[k - RW].z * xd.x + s.sb[k + 1 - RW].w * s.sx[k + 1 - RW].x;
+        const float4 a = g.sa[k], b = g.sb[k];
+        const float2 xl = sx[k - 1], xr = sx[k + 1], xd = sx[k - RW], xu = sx[k + RW];
+        float u = a.x * xl.x + g.sa[k + 1].x * xr.x + a.y * xd.x + g.sa[k + RW].y * xu.x
+                + b.x * sx[k].y + b.y * xl.y + b.z * xu.y + b.w * sx[k + RW - 1].y;
+        float v = a.z * xl.y + g.sa[k + 1].z * xr.y + a.w * xd.y + g.sa[k + RW].w * xu.y
+                + b.x * sx[k].x + g.sb[k + 1].y * xr.x + g.sb[k - RW].z * xd.x + g.sb[k + 1 - RW].w * sx[k + 1 - RW].x;
         return f2(u, v);
     }
     DEV float2 relax(int k) const {
-        const float2 dd = s.sd[k];
+        const float2 dd = g.sd[k];
         const float2 o = offd(k);
-        const float2 rr = s.sr[k];
+        const float2 rr = g.sr[k];
         const float sx_ = rr.x - o.x, sy_ = rr.y - o.y;
         return f2(dd.x > 0.0f ? sx_ / dd.x : 0.0f, dd.y > 0.0f ? sy_ / dd.y : 0.0f);
     }
 
-    // load_region (vmg.glsl:90-111) with the right-hand side from rhs(i)
-    template <class F>
-    DEV void load(const DevScene& d, const Lv& L, F rhs) const {
-        // a fixed trip count, so that every round's loads are issued before any store
+    // The copies of the region: matrix, right-hand side rhs (an array of the level, offset
+    // included), and e1 / e2 from arrays f1 / f2 (null: not copied); f2 may be read at the
+    // coarse cell (x / 2, y / 2) of level LC.
+    DEV void stage(const DevScene& d, const Lv& L, const float2* rhs, const float2* f1, const float2* f2_,
+                   const Lv* LC) const {
 #pragma unroll
         for (int j = 0; j < PER; j++) {
             const int k = threadIdx.x + j * NT;
             if (k >= N) break;
             const int x = cell_x(k), y = cell_y(k);
-            float4 a = make_float4(0.0f, 0.0f, 0.0f, 0.0f), b = a;
-            float2 dd = f2(0.0f, 0.0f), r = dd;
-            if (l_inside(L, x, y)) {
-                const int i = l_at(L, x, y);
-                a = d.vma[i];
-                b = d.vmb[i];
-                dd = d.vmd[i];
-                r = rhs(i);
-            }
-            s.sa[k] = a;
-            s.sb[k] = b;
-            s.sd[k] = dd;
-            s.sr[k] = r;
+            const bool in = l_inside(L, x, y);
+            const int i = in ? l_at(L, x, y) : 0;
+            cp_async<16>(&g.sa[k], d.vma + i, in);
+            cp_async<16>(&g.sb[k], d.vmb + i, in);
+            cp_async<8>(&g.sd[k], d.vmd + i, in);
+            cp_async<8>(&g.sr[k], rhs + i, in);
+            if (f1) cp_async<8>(&g.e1[k], f1 + i, in);
+            if (f2_) cp_async<8>(&g.e2[k], f2_ + (in ? (LC ? l_at(*LC, x >> 1, y >> 1) : i) : 0), in);
         }
     }
 
-    // half_sweep (vmg.glsl:121-134)
+    // half_sweep (vmg.glsl:121-134) over the slots of one colour in ring lo (w = RW - 2 lo
+    // columns from lo, w / 2 of each colour per row): every new value from the old ones, then
+    // stored.
     DEV void half_sweep(bool is_red, int lo) const {
-        float2 nv[PER];
+        const int w = RW - 2 * lo, hw = w >> 1, cnt = w * hw;
+        constexpr int PH = (N / 2 + NT - 1) / NT;
+        float2 nv[PH];
+        int kk[PH];
 #pragma unroll
-        for (int j = 0; j < PER; j++) {
-            const int k = threadIdx.x + NT * j;
-            nv[j] = f2(0.0f, 0.0f);
-            if (k < N && in_ring(k, lo) && red(k) == is_red) nv[j] = relax(k);
+        for (int j = 0; j < PH; j++) {
+            const int m = threadIdx.x + NT * j;
+            kk[j] = -1;
+            if (m < cnt) {
+                const int ly = lo + m / hw;
+                const int lx = lo + 2 * (m % hw) + ((ly + lo + (is_red ? 0 : 1)) & 1);
+                kk[j] = ly * RW + lx;
+                nv[j] = relax(kk[j]);
+            }
         }
         __syncthreads();
 #pragma unroll
-        for (int j = 0; j < PER; j++) {
-            const int k = threadIdx.x + NT * j;
-            if (k < N && in_ring(k, lo) && red(k) == is_red) s.sx[k] = nv[j];
-        }
+        for (int j = 0; j < PH; j++)
+            if (kk[j] >= 0) sx[kk[j]] = nv[j];
         __syncthreads();
     }
 
-    // way_down (vmg.glsl:145-168) on the loaded region: pre-smoothing from zero, the tile's
+    // way_down (vmg.glsl:145-168) on the staged region: pre-smoothing from zero, the tile's
     // values to vmx and, unless coarsest, its residual summed over 2 x 2 aggregates into
-    // vmr of the next level.
-    DEV void way_down(const DevScene& d, const Lv& L, const Lv* LC) const {
-        for (int k = threadIdx.x; k < N; k += NT) {
-            const float2 dd = s.sd[k], r = s.sr[k];
+    // vmr of the next level. fix(k) first makes this thread's slot k of the right-hand side
+    // final (its own copies have landed).
+    template <class Fix>
+    DEV void way_down(const DevScene& d, const Lv& L, const Lv* LC, Fix&& fix) const {
+#pragma unroll
+        for (int j = 0; j < PER; j++) {
+            const int k = threadIdx.x + j * NT;
+            if (k >= N) break;
+            fix(k);
+            const float2 dd = g.sd[k], r = g.sr[k];
             const float2 x = f2(dd.x > 0.0f ? r.x / dd.x : 0.0f, dd.y > 0.0f ? r.y / dd.y : 0.0f);
-            s.sx[k] = red(k) ? x : f2(0.0f, 0.0f);
+            sx[k] = red(k) ? x : f2(0.0f, 0.0f);
         }
         __syncthreads();
+#pragma unroll
         for (int h = 1; h < VCfg<NU>::HALO; h++) half_sweep((h & 1) == 0, h);
         const int t = threadIdx.x;
         const int k = tile_slot(t);
         const int cx = ox + (t & 15), cy = oy + (t >> 4);
-        const float2 x = s.sx[k], dd = s.sd[k], r = s.sr[k];
+        const float2 x = sx[k], dd = g.sd[k], r = g.sr[k];
         const float2 o = offd(k);
         const float2 m = mask_of(dd);
         const float2 res = f2((r.x - dd.x * x.x - o.x) * m.x, (r.y - dd.y * x.y - o.y) * m.y);
@@ -388,27 +406,24 @@ struct Region {
         __syncthreads();
     }
 
-    // the start of a way up (vmg_up.comp:37-46, visc_mgz.comp:33-38): x = vmx plus the
-    // coarse values (LC, if any), zero where a face is no unknown; then HALO half-sweeps,
+    // the start of a way up (vmg_up.comp:37-46, visc_mgz.comp:33-38): x = vmx (e1) plus the
+    // coarse values (e2, with LC), zero where a face is no unknown; then HALO half-sweeps,
     // black first.
-    DEV void way_up(const DevScene& d, const Lv& L, const Lv* LC) const {
+    DEV void way_up(bool coarse) const {
 #pragma unroll
         for (int j = 0; j < PER; j++) {
             const int k = threadIdx.x + j * NT;
             if (k >= N) break;
-            const int x = cell_x(k), y = cell_y(k);
-            float2 v = f2(0.0f, 0.0f);
-            if (l_inside(L, x, y)) {
-                v = d.vmx[l_at(L, x, y)];
-                if (LC) {
-                    const float2 zc = d.vmz[l_at(*LC, x >> 1, y >> 1)];
-                    v = f2(v.x + zc.x, v.y + zc.y);
-                }
+            float2 v = g.e1[k];
+            if (coarse) {
+                const float2 zc = g.e2[k];
+                v = f2(v.x + zc.x, v.y + zc.y);
             }
-            const float2 m = mask_of(s.sd[k]);
-            s.sx[k] = f2(v.x * m.x, v.y * m.y);
+            const float2 m = mask_of(g.sd[k]);
+            sx[k] = f2(v.x * m.x, v.y * m.y);
         }
         __syncthreads();
+#pragma unroll
         for (int h = 1; h <= VCfg<NU>::HALO; h++) half_sweep((h & 1) == 0, h);
     }
 };
@@ -628,114 +643,139 @@ struct VSolve {
         });
     }
 
+    // For every active tile of level l in this block's share, through the pipeline of two
+    // staging buffers: stage(tt, g) issues the tile's copies, finish(tt, g) computes it.
+    template <class S, class F>
+    DEV void pipe(int l, S&& stage, F&& finish) const {
+        const bool cached = l < kVCacheLevels;
+        const uint32_t cnt = cached ? tc.cnt[l] : *(volatile uint32_t*)&d.vcount[l];
+        pipeline<2>(
+            cnt,
+            [&](int k) {
+                return (cached && k < kVCachePer) ? tc.item[l][k] : list(l)[blockIdx.x + (uint32_t)k * gridDim.x];
+            },
+            [&](uint32_t tt, int b) { stage(tt, s.st[b]); }, [&](uint32_t tt, int b) { finish(tt, s.st[b]); });
+    }
+    template <int RH>
+    DEV Region<NU, RH> region(VStage<NU>& g, const Lv& L, uint32_t tt) const {
+        const int tw = tiles_x(L);
+        return Region<NU, RH>{g, s.sx, s, (int)(tt % tw) * 16, (int)(tt / tw) * 16};
+    }
+
     // vmg_down.comp on level l (l = 0 at the start of a solve, right-hand side vr)
     DEV void down(int l, int nlev, const float2* rhs0) const {
         const Lv L = lev(d.lv, l);
         const Lv LC = lev(d.lv, l + 1);
-        const int tw = tiles_x(L);
-        each(l, [&](uint32_t tt) {
-            Region<NU, VCfg<NU>::HALO> R{s, (int)(tt % tw) * 16, (int)(tt / tw) * 16};
-            if (l == 0) R.load(d, L, [&](int i) { return rhs0[i]; });
-            else R.load(d, L, [&](int i) { return d.vmr[i]; });
-            __syncthreads();
-            R.way_down(d, L, l == nlev ? nullptr : &LC);
-        });
+        const float2* rhs = l == 0 ? rhs0 : d.vmr;
+        pipe(
+            l, [&](uint32_t tt, VStage<NU>& g) { region<VCfg<NU>::HALO>(g, L, tt).stage(d, L, rhs, nullptr, nullptr, nullptr); },
+            [&](uint32_t tt, VStage<NU>& g) {
+                region<VCfg<NU>::HALO>(g, L, tt).way_down(d, L, l == nlev ? nullptr : &LC, [](int) {});
+            });
     }
 
     // vmg_up.comp on a coarse level l: the finished values to vmz
     DEV void up(int l, int nlev) const {
         const Lv L = lev(d.lv, l);
         const Lv LC = lev(d.lv, l + 1);
-        const int tw = tiles_x(L);
-        each(l, [&](uint32_t tt) {
-            Region<NU, VCfg<NU>::HALO> R{s, (int)(tt % tw) * 16, (int)(tt / tw) * 16};
-            R.load(d, L, [&](int i) { return d.vmr[i]; });
-            __syncthreads();
-            R.way_up(d, L, l == nlev ? nullptr : &LC);
-            const int t = threadIdx.x;
-            const int cx = R.ox + (t & 15), cy = R.oy + (t >> 4);
-            if (l_inside(L, cx, cy)) d.vmz[l_at(L, cx, cy)] = s.sx[R.tile_slot(t)];
-            __syncthreads();
-        });
+        const bool coarse = l != nlev;
+        pipe(
+            l,
+            [&](uint32_t tt, VStage<NU>& g) {
+                region<VCfg<NU>::HALO>(g, L, tt).stage(d, L, d.vmr, d.vmx, coarse ? d.vmz : nullptr, coarse ? &LC : nullptr);
+            },
+            [&](uint32_t tt, VStage<NU>& g) {
+                const Region<NU, VCfg<NU>::HALO> R = region<VCfg<NU>::HALO>(g, L, tt);
+                R.way_up(coarse);
+                const int t = threadIdx.x;
+                const int cx = R.ox + (t & 15), cy = R.oy + (t >> 4);
+                if (l_inside(L, cx, cy)) d.vmz[l_at(L, cx, cy)] = s.sx[R.tile_slot(t)];
+                __syncthreads();
+            });
     }
 
     // visc_mgz.comp: the way up on level 0 with A z and the partial sums of r.z, z.A z, z.q
     DEV void mgz(const float2* rn, const float2* qn, int half) const {
         const Lv L = lev(d.lv, 0);
         const Lv LC = lev(d.lv, 1);
-        const int tw = tiles_x(L);
-        each(0, [&](uint32_t tt) {
-            Region<NU, VCfg<NU>::HALO + 1> R{s, (int)(tt % tw) * 16, (int)(tt / tw) * 16};
-            R.load(d, L, [&](int i) { return rn[i]; });
-            __syncthreads();
-            R.way_up(d, L, &LC);
-            const int t = threadIdx.x;
-            const int cx = R.ox + (t & 15), cy = R.oy + (t >> 4);
-            const int k = R.tile_slot(t);
-            float4 acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-            if (l_inside(L, cx, cy)) {
-                const int i = l_at(L, cx, cy);
-                const float2 z = s.sx[k], dd = s.sd[k];
-                const float2 o = R.offd(k);
-                const float2 az = f2(dd.x * z.x + o.x, dd.y * z.y + o.y);
-                d.vmz[i] = z;
-                d.vaz[i] = az;
-                acc = make_float4(dot2(s.sr[k], z), dot2(z, az), dot2(z, qn[i]), 0.0f);
-            }
-            tile_sum(acc, half, tt);
-        });
+        constexpr int RH = VCfg<NU>::HALO + 1;
+        pipe(
+            0, [&](uint32_t tt, VStage<NU>& g) { region<RH>(g, L, tt).stage(d, L, rn, d.vmx, d.vmz, &LC); },
+            [&](uint32_t tt, VStage<NU>& g) {
+                const Region<NU, RH> R = region<RH>(g, L, tt);
+                const int t = threadIdx.x;
+                const int cx = R.ox + (t & 15), cy = R.oy + (t >> 4);
+                const bool in = l_inside(L, cx, cy);
+                const float2 qi = in ? qn[l_at(L, cx, cy)] : f2(0.0f, 0.0f);   // (in flight meanwhile)
+                R.way_up(true);
+                const int k = R.tile_slot(t);
+                float4 acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                if (in) {
+                    const int i = l_at(L, cx, cy);
+                    const float2 z = s.sx[k], dd = g.sd[k];
+                    const float2 o = R.offd(k);
+                    const float2 az = f2(dd.x * z.x + o.x, dd.y * z.y + o.y);
+                    d.vmz[i] = z;
+                    d.vaz[i] = az;
+                    acc = make_float4(dot2(g.sr[k], z), dot2(z, az), dot2(z, qi), 0.0f);
+                }
+                tile_sum(acc, half, tt);
+            });
     }
 
-    // visc_mgu.comp: p, q, x, r of the iteration and the way down on level 0 from the new r
+    // visc_mgu.comp: p, q, x, r of the iteration and the way down on level 0 from the new r.
+    // Copies: A z (e1), the old q (e2, unless beta is zero) and the old r (sr) over the region;
+    // each slot's new r = r - alpha q, q = A z + beta q_old, made final in place.
     DEV void mgu(const float2* ro, const float2* qo, float2* rn, float2* qn, int half) const {
         const Lv L = lev(d.lv, 0);
         const Lv LC = lev(d.lv, 1);
-        const int tw = tiles_x(L);
         const float a = K.alpha, b = K.beta;
-        auto new_q = [&](int i) {
-            const float2 sq = d.vaz[i];
+        constexpr int RH = VCfg<NU>::HALO;
+        auto new_q = [&](const VStage<NU>& g, int k) {
+            const float2 sq = g.e1[k];
             if (b == 0.0f) return sq;
-            const float2 q = qo[i];
+            const float2 q = g.e2[k];
             return f2(sq.x + b * q.x, sq.y + b * q.y);
         };
-        each(0, [&](uint32_t tt) {
-            Region<NU, VCfg<NU>::HALO> R{s, (int)(tt % tw) * 16, (int)(tt / tw) * 16};
-            const int t = threadIdx.x;
-            const int cx = R.ox + (t & 15), cy = R.oy + (t >> 4);
-            float4 acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-            if (cx < d.W && cy < d.H) {
-                const int i = cy * d.W + cx;
-                const float2 z = d.vmz[i];
-                float2 p = z;
-                if (b != 0.0f) {
-                    const float2 po = d.vp[i];
-                    p = f2(z.x + b * po.x, z.y + b * po.y);
+        pipe(
+            0, [&](uint32_t tt, VStage<NU>& g) { region<RH>(g, L, tt).stage(d, L, ro, d.vaz, b != 0.0f ? qo : nullptr, nullptr); },
+            [&](uint32_t tt, VStage<NU>& g) {
+                const Region<NU, RH> R = region<RH>(g, L, tt);
+                const int t = threadIdx.x;
+                const int cx = R.ox + (t & 15), cy = R.oy + (t >> 4);
+                const bool own = cx < d.W && cy < d.H;
+                const int i = own ? cy * d.W + cx : 0;
+                const bool inner = own && interior(d, cx, cy);
+                // this cell's z, p_old, velocity and step, in flight while the region is made final
+                const float2 z = own ? d.vmz[i] : f2(0.0f, 0.0f);
+                const float2 po = (own && b != 0.0f) ? d.vp[i] : f2(0.0f, 0.0f);
+                float4 v = inner ? d.vel[i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                const float2 dv = inner ? d.vd[i] : f2(0.0f, 0.0f);
+                const int ks = R.tile_slot(t);
+                R.way_down(d, L, &LC, [&](int k) {
+                    const float2 q = new_q(g, k);
+                    const float2 r0 = g.sr[k];
+                    g.sr[k] = f2(r0.x - a * q.x, r0.y - a * q.y);
+                });
+                float4 acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                if (own) {
+                    float2 p = z;
+                    if (b != 0.0f) p = f2(z.x + b * po.x, z.y + b * po.y);
+                    const float2 q = new_q(g, ks);
+                    const float2 r = g.sr[ks];
+                    if (inner) {
+                        if (face_live(v.z)) v.x += a * p.x;
+                        if (face_live(v.w)) v.y += a * p.y;
+                        store_vel_xy(d, i, v.x, v.y);
+                        d.vd[i] = f2(dv.x + a * p.x, dv.y + a * p.y);
+                    }
+                    d.vp[i] = p;
+                    qn[i] = q;
+                    rn[i] = r;
+                    acc = make_float4(0.0f, dot2(r, r), dot2(p, q), 0.0f);
                 }
-                const float2 q = new_q(i);
-                const float2 r0 = ro[i];
-                const float2 r = f2(r0.x - a * q.x, r0.y - a * q.y);
-                if (interior(d, cx, cy)) {
-                    float4 v = d.vel[i];
-                    if (face_live(v.z)) v.x += a * p.x;
-                    if (face_live(v.w)) v.y += a * p.y;
-                    store_vel_xy(d, i, v.x, v.y);
-                    const float2 dv = d.vd[i];
-                    d.vd[i] = f2(dv.x + a * p.x, dv.y + a * p.y);
-                }
-                d.vp[i] = p;
-                qn[i] = q;
-                rn[i] = r;
-                acc = make_float4(0.0f, dot2(r, r), dot2(p, q), 0.0f);
-            }
-            R.load(d, L, [&](int i) {
-                const float2 q = new_q(i);
-                const float2 r0 = ro[i];
-                return f2(r0.x - a * q.x, r0.y - a * q.y);
+                tile_sum(acc, half, tt);
             });
-            __syncthreads();
-            R.way_down(d, L, &LC);
-            tile_sum(acc, half, tt);
-        });
     }
 
     // record_visc_coarse (mod.rs:2838-2853): the coarse levels down, then up
@@ -758,7 +798,7 @@ struct VSolve {
 // multigrid preconditioner). `restrain`: take the strain of u* again first (the first
 // pressure solve changed the velocity since visc_setup).
 template <int NU>
-__global__ void __launch_bounds__(NT) k_visc_solve(DevScene d, int restrain) {
+__global__ void __launch_bounds__(NT, 2) k_visc_solve(DevScene d, int restrain) {
     __shared__ VSmem<NU> sm;
     __shared__ VScal K;
     __shared__ VTileCache tc;
