@@ -115,6 +115,17 @@ struct Levels {
     int off[kMaxLevels] = {};
     int toff[kMaxLevels] = {};
     int total = 0, tail = 0, tiles = 0;
+    // ceil(2^32 / d) for d = the level's width and its width in 16 x 16 tiles: floor(t / d)
+    // is the high word of t x that, exactly, for t < 2^20 and d < 2^11 (set_magics)
+    uint32_t wm[kMaxLevels] = {}, tm[kMaxLevels] = {};
 };
+
+inline uint32_t div_magic(int d) { return (uint32_t)(((1ull << 32) + (unsigned long long)d - 1ull) / (unsigned long long)d); }
+inline void set_magics(Levels& L) {
+    for (int l = 0; l < L.n; l++) {
+        L.wm[l] = div_magic(L.w[l]);
+        L.tm[l] = div_magic((L.w[l] + 15) / 16);
+    }
+}
 
 }  // namespace sprout

@@ -56,7 +56,6 @@ struct Plain {
     DEV static float4 A(const DevScene& d, int i) { return d.mga[i]; }
     DEV static float Dg(const DevScene& d, int i) { return d.mgd[i]; }
     DEV static void setA(const DevScene& d, int i, float4 a, float dg) { d.mga[i] = a; d.mgd[i] = dg; }
-    DEV static float2 X(const DevScene& d, int i) { return d.mgx[i]; }
     DEV static void setX(const DevScene& d, int i, float2 v) { d.mgx[i] = v; }
     DEV static float2 Z(const DevScene& d, int i) { return d.mgz[i]; }
     DEV static void setZ(const DevScene& d, int i, float2 v) { d.mgz[i] = v; }
@@ -65,11 +64,11 @@ struct Plain {
     DEV static acc4* part(const DevScene& d) { return d.partials; }
     DEV static acc4 a4(float x, float y, float z, float w) { return make_float4(x, y, z, w); }
     // the stored matrix as a tile region stages it: bytes per row of couplings, their address,
-    // the diagonal's array, and the row widened to FP32 in its staged slot
+    // the diagonal's array, and the row read from its staged slot in FP32
     static constexpr int kABytes = 16;
     DEV static const void* Araw(const DevScene& d, int i) { return d.mga + i; }
     DEV static const float* Dptr(const DevScene& d) { return d.mgd; }
-    DEV static void widen(float4&) {}
+    DEV static float4 Aslot(const float4& slot) { return slot; }
 };
 
 // a pair of BF16 values in 32 bits (x in the low half), rounded to nearest even
@@ -111,7 +110,6 @@ struct Mixed {
     // nonlinear operator, which conjugate gradients does not tolerate (it stagnates near the
     // rounding level); the matrices are fixed during a solve, so the V-cycle built on their
     // BF16 copies stays a linear, symmetric positive definite preconditioner
-    DEV static float2 X(const DevScene& d, int i) { return d.mgx[i]; }
     DEV static void setX(const DevScene& d, int i, float2 v) { d.mgx[i] = v; }
     DEV static float2 Z(const DevScene& d, int i) { return d.mgz[i]; }
     DEV static void setZ(const DevScene& d, int i, float2 v) { d.mgz[i] = v; }
@@ -122,11 +120,11 @@ struct Mixed {
     static constexpr int kABytes = 8;
     DEV static const void* Araw(const DevScene& d, int i) { return d.hga + i; }
     DEV static const float* Dptr(const DevScene& d) { return d.hgd; }
-    // the BF16 row copied into the first 8 bytes of the slot, widened in place
-    DEV static void widen(float4& slot) {
+    // the BF16 row copied into the first 8 bytes of the slot, widened on reading
+    DEV static float4 Aslot(const float4& slot) {
         const uint2 u = *reinterpret_cast<const uint2*>(&slot);
         const float2 a = unpack(u.x), b = unpack(u.y);
-        slot = make_float4(a.x, a.y, b.x, b.y);
+        return make_float4(a.x, a.y, b.x, b.y);
     }
 };
 
@@ -336,7 +334,7 @@ DEV void tail_setup(const DevScene& d, const Tail& tl, bool writer) {
         Lv F = lev(d.lv, l), C = lev(d.lv, l + 1);
         const int o = F.off - tl.base, oc = C.off - tl.base;
         for (int t = threadIdx.x; t < C.w * C.h; t += NT) {
-            int ccx = t % C.w, ccy = t / C.w;
+            const int ccy = qdiv(t, C.wm), ccx = t - ccy * C.w;
             float D = 0.0f;
             float4 A = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
             for (int k = 0; k < 4; k++) {
@@ -367,7 +365,7 @@ DEV void tail_setup(const DevScene& d, const Tail& tl, bool writer) {
         const Lv L = lev(d.lv, l);
         const int o = L.off - tl.base;
         for (int t = threadIdx.x; t < L.w * L.h; t += NT) {
-            const int x = t % L.w, y = t / L.w;
+            const int y = qdiv(t, L.wm), x = t - y * L.w;
             uint32_t m = tl.dg[o + t] > 0.0f ? 16u : 0u;
             for (int q = 0; q < 4; q++) m |= t_unknown(tl, L, x + NBX[q], y + NBY[q]) ? (1u << q) : 0u;
             tl.m[o + t] = (uint8_t)m;
@@ -384,15 +382,15 @@ struct Zc {
 };
 
 // A level's tile and RH cells around it staged in shared memory, RW x RW slots: the
-// diagonal (zero outside the level and where no unknown), the couplings, up to three vector
-// fields, and for the tile's own cells (one per thread) two more vectors and the operator's
-// diagonal. A tile body comes in two halves: stage_* issues every load of the tile as an
-// asynchronous copy into a Region (zero-filled outside the level), and finish_* runs once
-// they have landed: each thread makes the slots it copied final (the diagonal's sign test,
-// the BF16 couplings widened, the fused residual update), then the tile's arithmetic reads
-// only the slots. Its values are the same, value for value, as reading the fields from global
-// memory one after another. Every block holds two Regions: while one tile computes, the
-// copies of its next tile are in flight (pipe_active).
+// diagonal (zero outside the level), the couplings, up to three vector fields, and for the
+// tile's own cells (one per thread) two more vectors and the operator's diagonal. A tile body
+// comes in two halves: stage_* issues every load of the tile as an asynchronous copy into a
+// Region (zero-filled outside the level), and finish_* runs once they have landed and reads
+// only the slots, each as the shader reads its field (a diagonal that is not positive as
+// zero, BF16 couplings widened, the fused residual update applied). Its values are the same,
+// value for value, as reading the fields from global memory one after another. Every block
+// holds two Regions: while one tile computes, the copies of its next tile are in flight
+// (pipe_active).
 constexpr int RH = 2;
 constexpr int RW = 16 + 2 * RH;
 constexpr int RN = RW * RW;
@@ -456,8 +454,8 @@ DEV float2 coarse_z(const DevScene& d, const Zc& zc, int mx, int my) {
 template <class M>
 DEV void stage_down(const DevScene& d, int l, int t, const Rsrc<M>& R, bool update, const float2* p, Region& rg) {
     const Lv F = lev(d.lv, l);
-    const int tx_n = tiles_x(F);
-    const int ox = (t % tx_n) * 16, oy = (t / tx_n) * 16;
+    const int2 og = tile_origin(F, t);
+    const int ox = og.x, oy = og.y;
     const float2* r = R.r ? R.r : d.mgr;
 #pragma unroll
     for (int j = 0; j < RJ; j++) {
@@ -482,41 +480,45 @@ DEV void stage_down(const DevScene& d, int l, int t, const Rsrc<M>& R, bool upda
 }
 
 // ... and its arithmetic. On level 0 with `r_out` it also applies cg_update.comp: x +=
-// alpha p and the residual update into r_out.
+// alpha p and the residual update into r_out. The staged slots are read as the shader reads
+// its fields: a diagonal that is not positive as zero (dg), the right-hand side with the fused
+// update (rhs). Every neighbour's values are read before the terms are summed, in the
+// shader's order, each kept or not by a select.
 template <class M>
 DEV void finish_down(const DevScene& d, int l, int t, const Rsrc<M>& R, float2* r_out, float2* sz, Region& rg) {
     const Lv F = lev(d.lv, l), C = lev(d.lv, l + 1);
-    const int tx_n = tiles_x(F);
-    const int ox = (t % tx_n) * 16, oy = (t / tx_n) * 16;
-#pragma unroll
-    for (int j = 0; j < RJ; j++) {
-        const int k = threadIdx.x + j * NT;
-        if (k >= RN) break;
-        if (!(rg.dg[k] > 0.0f)) rg.dg[k] = 0.0f;
-        M::widen(rg.a[k]);
-        if (R.q) {   // R.at: r - alpha q
-            float2 v = rg.u[k];
+    const int2 og = tile_origin(F, t);
+    const int ox = og.x, oy = og.y;
+    __syncthreads();   // (every thread's copies have landed)
+    const bool fused = R.q != nullptr;
+    auto dg = [&](int k) {
+        const float v = rg.dg[k];
+        return v > 0.0f ? v : 0.0f;
+    };
+    auto rhs = [&](int k) {   // R.at: r - alpha q
+        float2 v = rg.u[k];
+        if (fused) {
             const float2 qq = rg.v[k];
             v.x = v.x - R.ax * qq.x;
             v.y = v.y - R.ay * qq.y;
-            rg.u[k] = v;
         }
-    }
-    __syncthreads();
+        return v;
+    };
     // the value of black slot k after the half-sweep from zero (mg_down black())
     auto black = [&](int k) {
-        const float4 w = rg.a[k];
-        float2 sum = rg.u[k];
-        for (int q = 0; q < 4; q++) {
-            const int j = k + RSTEP[q];
-            const float dj = rg.dg[j];
-            if (dj <= 0.0f) continue;
-            const float wd = wcomp(w, q);
-            const float2 rj = rg.u[j];
-            sum.x += wd * rj.x / dj;
-            sum.y += wd * rj.y / dj;
-        }
-        const float di = rg.dg[k];
+        const float4 w = M::Aslot(rg.a[k]);
+        float2 sum = rhs(k);
+        const float d0 = dg(k - 1), d1 = dg(k + 1), d2 = dg(k - RW), d3 = dg(k + RW);
+        const float2 r0 = rhs(k - 1), r1 = rhs(k + 1), r2 = rhs(k - RW), r3 = rhs(k + RW);
+        const float t0x = w.x * r0.x / d0, t0y = w.x * r0.y / d0;
+        const float t1x = w.y * r1.x / d1, t1y = w.y * r1.y / d1;
+        const float t2x = w.z * r2.x / d2, t2y = w.z * r2.y / d2;
+        const float t3x = w.w * r3.x / d3, t3y = w.w * r3.y / d3;
+        if (d0 > 0.0f) { sum.x += t0x; sum.y += t0y; }
+        if (d1 > 0.0f) { sum.x += t1x; sum.y += t1y; }
+        if (d2 > 0.0f) { sum.x += t2x; sum.y += t2y; }
+        if (d3 > 0.0f) { sum.x += t3x; sum.y += t3y; }
+        const float di = dg(k);
         return make_float2(sum.x / di, sum.y / di);
     };
     const int2 lc = colour_cell();
@@ -527,10 +529,10 @@ DEV void finish_down(const DevScene& d, int l, int t, const Rsrc<M>& R, float2* 
     float2 z = make_float2(0.0f, 0.0f);
     if (l_inside(F, cx, cy)) {
         const int i = l_at(F, cx, cy);
-        const float D = rg.dg[k0];
+        const float D = dg(k0);
         if (D > 0.0f) {
             if (red) {
-                const float2 r = rg.u[k0];
+                const float2 r = rhs(k0);
                 z = make_float2(r.x / D, r.y / D);
             } else {
                 z = black(k0);
@@ -543,7 +545,7 @@ DEV void finish_down(const DevScene& d, int l, int t, const Rsrc<M>& R, float2* 
             x.x += R.ax * pp.x;
             x.y += R.ay * pp.y;
             d.pres[i] = x;
-            r_out[i] = rg.u[k0];
+            r_out[i] = rhs(k0);
         }
         M::setX(d, i, z);
     }
@@ -551,7 +553,7 @@ DEV void finish_down(const DevScene& d, int l, int t, const Rsrc<M>& R, float2* 
     if (threadIdx.x < 32) {   // (a red warp) the black cells around the tile
         const int2 rc = ring_cell(threadIdx.x);
         const int kr = rslot(rc.x, rc.y);
-        rg.ring[threadIdx.x] = rg.dg[kr] > 0.0f ? black(kr) : make_float2(0.0f, 0.0f);
+        rg.ring[threadIdx.x] = dg(kr) > 0.0f ? black(kr) : make_float2(0.0f, 0.0f);
     }
     __syncthreads();
     if (threadIdx.x < 64) {   // the restriction: aggregate (ax, ay), its red cells (0, 0) and (1, 1)
@@ -559,20 +561,29 @@ DEV void finish_down(const DevScene& d, int l, int t, const Rsrc<M>& R, float2* 
         const int Cx = (ox >> 1) + ax, Cy = (oy >> 1) + ay;
         if (Cx < C.w && Cy < C.h) {
             float sx = 0.0f, sy = 0.0f;
+#pragma unroll
             for (int k = 0; k < 2; k++) {
                 const int lqx = 2 * ax + k, lqy = 2 * ay + k;
                 const int kq = rslot(lqx, lqy);
-                if (rg.dg[kq] <= 0.0f) continue;
-                const float4 w = rg.a[kq];
+                const bool own = dg(kq) > 0.0f;
+                const float4 w = M::Aslot(rg.a[kq]);
+                float dn[4];
+                float2 zb[4];
+#pragma unroll
                 for (int q = 0; q < 4; q++) {
-                    const int kn = kq + RSTEP[q];
-                    if (rg.dg[kn] <= 0.0f) continue;
+                    dn[q] = dg(kq + RSTEP[q]);
                     const int lnx = lqx + NBX[q], lny = lqy + NBY[q];
                     const bool here = lnx >= 0 && lny >= 0 && lnx < 16 && lny < 16;
-                    const float2 zb = here ? sz[lny * 16 + lnx] : rg.ring[ring_of(lnx, lny)];
+                    zb[q] = here ? sz[lny * 16 + lnx] : rg.ring[ring_of(lnx, lny)];
+                }
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
                     const float wd = wcomp(w, q);
-                    sx += wd * zb.x;
-                    sy += wd * zb.y;
+                    const float ux = wd * zb[q].x, uy = wd * zb[q].y;
+                    if (own && dn[q] > 0.0f) {
+                        sx += ux;
+                        sy += uy;
+                    }
                 }
             }
             M::setR(d, l_at(C, Cx, Cy), make_float2(sx, sy));
@@ -587,8 +598,8 @@ DEV void finish_down(const DevScene& d, int l, int t, const Rsrc<M>& R, float2* 
 template <class M>
 DEV void stage_up(const DevScene& d, int l, int t, const Rsrc<M>& rhs, const Zc& zc, Region& rg) {
     const Lv F = lev(d.lv, l);
-    const int tx_n = tiles_x(F);
-    const int ox = (t % tx_n) * 16, oy = (t / tx_n) * 16;
+    const int2 og = tile_origin(F, t);
+    const int ox = og.x, oy = og.y;
     const float2* r = rhs.r ? rhs.r : d.mgr;
 #pragma unroll
     for (int j = 0; j < RJ; j++) {
@@ -605,41 +616,53 @@ DEV void stage_up(const DevScene& d, int l, int t, const Rsrc<M>& rhs, const Zc&
     }
 }
 
-// ... and its arithmetic; on level 0 (flag) the tile's sums of r.z, r.r into part[t].
+// ... and its arithmetic; on level 0 (flag) the tile's sums of r.z, r.r into part[t]. Read
+// as finish_down reads its slots.
 template <class M>
 DEV void finish_up(const DevScene& d, int l, int t, bool flag, const Zc& zc, float2* sz, typename M::acc4* buf,
                    Region& rg) {
     using acc = typename M::acc;
     const Lv F = lev(d.lv, l);
-    const int tx_n = tiles_x(F);
     typename M::acc4* part = M::part(d);
-    const int ox = (t % tx_n) * 16, oy = (t / tx_n) * 16;
+    const int2 og = tile_origin(F, t);
+    const int ox = og.x, oy = og.y;
+    if (zc.s) {   // the coarse values from this block's copy of the tail
 #pragma unroll
-    for (int j = 0; j < RJ; j++) {
-        const int k = threadIdx.x + j * NT;
-        if (k >= RN) break;
-        if (!(rg.dg[k] > 0.0f)) rg.dg[k] = 0.0f;
-        M::widen(rg.a[k]);
-        if (zc.s) {
+        for (int j = 0; j < RJ; j++) {
+            const int k = threadIdx.x + j * NT;
+            if (k >= RN) break;
             const int x = ox - RH + k % RW, y = oy - RH + k / RW;
             rg.w[k] = l_inside(F, x, y) ? coarse_z<M>(d, zc, x, y) : make_float2(0.0f, 0.0f);
         }
     }
     __syncthreads();
+    auto dg = [&](int k) {
+        const float v = rg.dg[k];
+        return v > 0.0f ? v : 0.0f;
+    };
     // the new value of black slot k after the coarse correction (mg_up black())
     auto black = [&](int k) {
-        const float4 w = rg.a[k];
+        const float4 w = M::Aslot(rg.a[k]);
         float2 sum = rg.u[k];
+        float dn[4];
+        float2 xm[4], zcv[4];
+#pragma unroll
         for (int q = 0; q < 4; q++) {
             const int j = k + RSTEP[q];
-            if (rg.dg[j] <= 0.0f) continue;
-            const float2 xm = rg.v[j];
-            const float2 zcv = rg.w[j];
-            const float wd = wcomp(w, q);
-            sum.x += wd * (xm.x + MG_OMEGA * zcv.x);
-            sum.y += wd * (xm.y + MG_OMEGA * zcv.y);
+            dn[q] = dg(j);
+            xm[q] = rg.v[j];
+            zcv[q] = rg.w[j];
         }
-        const float di = rg.dg[k];
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const float wd = wcomp(w, q);
+            const float ux = wd * (xm[q].x + MG_OMEGA * zcv[q].x), uy = wd * (xm[q].y + MG_OMEGA * zcv[q].y);
+            if (dn[q] > 0.0f) {
+                sum.x += ux;
+                sum.y += uy;
+            }
+        }
+        const float di = dg(k);
         return make_float2(sum.x / di, sum.y / di);
     };
     const int2 lc = colour_cell();
@@ -647,14 +670,14 @@ DEV void finish_up(const DevScene& d, int l, int t, bool flag, const Zc& zc, flo
     const int cx = ox + lx, cy = oy + ly;
     const int k0 = rslot(lx, ly);
     const bool red = threadIdx.x < 128;
-    const bool unk = rg.dg[k0] > 0.0f;
+    const bool unk = dg(k0) > 0.0f;
     float2 z = make_float2(0.0f, 0.0f);
     if (unk && !red) z = black(k0);
     sz[cell] = z;
     if (threadIdx.x < 32) {   // (a red warp, idle here) the black cells around the tile
         const int2 rc = ring_cell(threadIdx.x);
         const int kr = rslot(rc.x, rc.y);
-        rg.ring[threadIdx.x] = rg.dg[kr] > 0.0f ? black(kr) : make_float2(0.0f, 0.0f);
+        rg.ring[threadIdx.x] = dg(kr) > 0.0f ? black(kr) : make_float2(0.0f, 0.0f);
     }
     __syncthreads();
     typename M::acc4 a4 = M::a4(0, 0, 0, 0);
@@ -663,19 +686,27 @@ DEV void finish_up(const DevScene& d, int l, int t, bool flag, const Zc& zc, flo
         if (unk) {
             const float2 r = rg.u[k0];
             if (red) {
-                const float4 w = rg.a[k0];
-                float sx = r.x, sy = r.y;
+                const float4 w = M::Aslot(rg.a[k0]);
+                float dn[4];
+                float2 zb[4];
+#pragma unroll
                 for (int q = 0; q < 4; q++) {
-                    const int kn = k0 + RSTEP[q];
-                    if (rg.dg[kn] <= 0.0f) continue;
+                    dn[q] = dg(k0 + RSTEP[q]);
                     const int lnx = lx + NBX[q], lny = ly + NBY[q];
                     const bool here = lnx >= 0 && lny >= 0 && lnx < 16 && lny < 16;
-                    const float2 zb = here ? sz[lny * 16 + lnx] : rg.ring[ring_of(lnx, lny)];
-                    const float wd = wcomp(w, q);
-                    sx += wd * zb.x;
-                    sy += wd * zb.y;
+                    zb[q] = here ? sz[lny * 16 + lnx] : rg.ring[ring_of(lnx, lny)];
                 }
-                const float di = rg.dg[k0];
+                float sx = r.x, sy = r.y;
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    const float wd = wcomp(w, q);
+                    const float ux = wd * zb[q].x, uy = wd * zb[q].y;
+                    if (dn[q] > 0.0f) {
+                        sx += ux;
+                        sy += uy;
+                    }
+                }
+                const float di = dg(k0);
                 z = make_float2(sx / di, sy / di);
             }
             a4 = M::a4((acc)r.x * (acc)z.x, (acc)r.y * (acc)z.y, (acc)r.x * (acc)r.x, (acc)r.y * (acc)r.y);
@@ -702,7 +733,7 @@ DEV void phase_tail(const DevScene& d, const Tail& tl, bool writer) {
     auto sweep = [&](const Lv& L, int colour, bool zero) {
         const int o = L.off - tl.base;
         for (int t = threadIdx.x; t < L.w * L.h; t += NT) {
-            int x = t % L.w, y = t / L.w;
+            const int y = qdiv(t, L.wm), x = t - y * L.w;
             int s = o + t;
             float D = tl.dg[s];
             if (D <= 0.0f || ((x + y) & 1) != colour) {
@@ -733,7 +764,7 @@ DEV void phase_tail(const DevScene& d, const Tail& tl, bool writer) {
         sweep(L, 0, true);
         sweep(L, 1, false);
         for (int t = threadIdx.x; t < C.w * C.h; t += NT) {
-            int ccx = t % C.w, ccy = t / C.w;
+            const int ccy = qdiv(t, C.wm), ccx = t - ccy * C.w;
             float sumx = 0.0f, sumy = 0.0f;
             const int step[4] = {-1, 1, -L.w, L.w};
             for (int k = 0; k < 4; k++) {
@@ -771,7 +802,7 @@ DEV void phase_tail(const DevScene& d, const Tail& tl, bool writer) {
         Lv F = lev(d.lv, l), C = lev(d.lv, l + 1);
         const int o = F.off - tl.base, oc = C.off - tl.base;
         for (int t = threadIdx.x; t < F.w * F.h; t += NT) {
-            int x = t % F.w, y = t / F.w;
+            const int y = qdiv(t, F.wm), x = t - y * F.w;
             if (((x + y) & 1) == 0) continue;
             int s = o + t;
             float D = tl.dg[s];
@@ -893,12 +924,12 @@ DEV bool vcycle(const DevScene& d, const Tail& tl, const Rsrc<M>& R, float2* r_o
 // tile's sums of |b - A x|^2 and |b|^2 of the pressure potential into part[t].
 DEV void true_residual_tile(const DevScene& d, int t, Dbl4* part, Dbl4* buf) {
     const Lv F = lev(d.lv, 0);
-    const int tx_n = tiles_x(F);
     if (d.ptile[F.toff + t] == 0u) {
         if (threadIdx.x == 0) part[t] = Dbl4{0.0, 0.0, 0.0, 0.0};
         return;
     }
-    const int cx = (t % tx_n) * 16 + (threadIdx.x & 15), cy = (t / tx_n) * 16 + (threadIdx.x >> 4);
+    const int2 og = tile_origin(F, t);
+    const int cx = og.x + (threadIdx.x & 15), cy = og.y + (threadIdx.x >> 4);
     Dbl4 a4{0.0, 0.0, 0.0, 0.0};
     if (l_inside(F, cx, cy)) {
         const int i = l_at(F, cx, cy);
@@ -926,8 +957,8 @@ DEV void true_residual_tile(const DevScene& d, int t, Dbl4* part, Dbl4* buf) {
 // tile's own cells.
 DEV void stage_apply(const DevScene& d, int t, bool nob, const float2* p_old, Region& rg) {
     const Lv F = lev(d.lv, 0);
-    const int tx_n = tiles_x(F);
-    const int ox = (t % tx_n) * 16, oy = (t / tx_n) * 16;
+    const int2 og = tile_origin(F, t);
+    const int ox = og.x, oy = og.y;
 #pragma unroll
     for (int j = 0; j < RJ; j++) {
         const int k = threadIdx.x + j * NT;
@@ -950,41 +981,46 @@ template <class M>
 DEV void finish_apply(const DevScene& d, int t, float b0, float b1, float2* p_new, typename M::acc4* buf, Region& rg) {
     using acc = typename M::acc;
     const Lv F = lev(d.lv, 0);
-    const int tx_n = tiles_x(F);
     const int n = d.nwg;
     typename M::acc4* part = M::part(d) + n;
     const bool nob = b0 == 0.0f && b1 == 0.0f;
-    const int ox = (t % tx_n) * 16, oy = (t / tx_n) * 16;
-#pragma unroll
-    for (int j = 0; j < RJ; j++) {
-        const int k = threadIdx.x + j * NT;
-        if (k >= RN) break;
-        const int kx = k % RW, ky = k / RW;
-        if (kx == 0 || ky == 0 || kx == RW - 1 || ky == RW - 1) continue;
-        if (!(rg.dg[k] > 0.0f)) rg.dg[k] = 0.0f;
-        if (!nob) {   // the direction p = z + beta p_old
-            const float2 z = rg.u[k], po = rg.v[k];
-            rg.u[k] = make_float2(b0 != 0.0f ? z.x + b0 * po.x : z.x, b1 != 0.0f ? z.y + b1 * po.y : z.y);
-        }
-    }
-    __syncthreads();
+    const int2 og = tile_origin(F, t);
+    const int ox = og.x, oy = og.y;
+    __syncthreads();   // (every thread's copies have landed)
+    auto dg = [&](int k) {
+        const float v = rg.dg[k];
+        return v > 0.0f ? v : 0.0f;
+    };
+    auto dir = [&](int k) {   // the direction p = z + beta p_old
+        const float2 z = rg.u[k];
+        if (nob) return z;
+        const float2 po = rg.v[k];
+        return make_float2(b0 != 0.0f ? z.x + b0 * po.x : z.x, b1 != 0.0f ? z.y + b1 * po.y : z.y);
+    };
     const int cx = ox + (threadIdx.x & 15), cy = oy + (threadIdx.x >> 4);
     const int k0 = rslot(threadIdx.x & 15, threadIdx.x >> 4);
     typename M::acc4 a4 = M::a4(0, 0, 0, 0);
     if (l_inside(F, cx, cy)) {
         const int i = l_at(F, cx, cy);
-        const float D = rg.dg[k0];
+        const float D = dg(k0);
         if (D > 0.0f) {
-            const float2 pp = rg.u[k0];
+            const float2 pp = dir(k0);
             const float4 w = rg.a[k0];
-            float qx = D * pp.x, qy = D * pp.y;
+            float dn[4];
+            float2 pn[4];
+#pragma unroll
             for (int q = 0; q < 4; q++) {
-                const int kn = k0 + RSTEP[q];
-                if (rg.dg[kn] > 0.0f) {
-                    const float2 pn = rg.u[kn];
-                    const float wd = wcomp(w, q);
-                    qx -= wd * pn.x;
-                    qy -= wd * pn.y;
+                dn[q] = dg(k0 + RSTEP[q]);
+                pn[q] = dir(k0 + RSTEP[q]);
+            }
+            float qx = D * pp.x, qy = D * pp.y;
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const float wd = wcomp(w, q);
+                const float ux = wd * pn[q].x, uy = wd * pn[q].y;
+                if (dn[q] > 0.0f) {
+                    qx -= ux;
+                    qy -= uy;
                 }
             }
             p_new[i] = pp;
@@ -1578,6 +1614,7 @@ Levels static_levels(int w, int h) {
         tiles += ((L.w[l] + 15) / 16) * ((L.h[l] + 15) / 16);
     }
     L.tiles = tiles;
+    set_magics(L);
     return L;
 }
 

@@ -70,6 +70,7 @@ Levels make_levels(int w, int h) {
         tiles += ((L.w[l] + 15) / 16) * ((L.h[l] + 15) / 16);
     }
     L.tiles = tiles;
+    set_magics(L);
     return L;
 }
 

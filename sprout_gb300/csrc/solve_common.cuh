@@ -16,9 +16,17 @@ constexpr uint32_t SPIN_LIMIT = 1u << 24;
 
 struct Lv {
     int off, w, h, toff;
+    uint32_t wm, tm;   // division constants of the width and the width in tiles (Levels)
 };
 
-DEV Lv lev(const Levels& L, int l) { return Lv{L.off[l], L.w[l], L.h[l], L.toff[l]}; }
+DEV Lv lev(const Levels& L, int l) { return Lv{L.off[l], L.w[l], L.h[l], L.toff[l], L.wm[l], L.tm[l]}; }
+// floor(t / d) from d's constant m = ceil(2^32 / d) (exact for t < 2^20, d < 2^11)
+DEV int qdiv(int t, uint32_t m) { return (int)__umulhi((uint32_t)t, m); }
+// the first cell (x, y) of tile t of a level
+DEV int2 tile_origin(const Lv& L, int t) {
+    const int ty = qdiv(t, L.tm);
+    return make_int2((t - ty * ((L.w + 15) >> 4)) * 16, ty * 16);
+}
 DEV bool l_inside(const Lv& L, int x, int y) { return x >= 0 && y >= 0 && x < L.w && y < L.h; }
 DEV int l_at(const Lv& L, int x, int y) { return L.off + y * L.w + x; }
 DEV int tiles_x(const Lv& L) { return (L.w + 15) >> 4; }

@@ -517,11 +517,12 @@ struct VSolve {
     // visc_strain.comp: the weighted strain of the current velocities in the active tiles
     DEV void strain() const {
         const Lv L0 = lev(d.lv, 0);
-        const int tw = tiles_x(L0), T = n;
+        const int T = n;
         const int W = d.W;
         for (int tt = blockIdx.x; tt < T; tt += gridDim.x) {
             if (d.tiles[tt] == 0u) continue;
-            const int cx = (tt % tw) * 16 + (threadIdx.x & 15), cy = (tt / tw) * 16 + (threadIdx.x >> 4);
+            const int2 og = tile_origin(L0, tt);
+            const int cx = og.x + (threadIdx.x & 15), cy = og.y + (threadIdx.x >> 4);
             if (!in_grid(d, cx, cy)) continue;
             const int i = cy * W + cx;
             const float4 w4 = d.vw[i];
@@ -548,7 +549,6 @@ struct VSolve {
     // active ones, zero partials (both halves) in the others.
     DEV void start() const {
         const Lv L0 = lev(d.lv, 0);
-        const int tw = tiles_x(L0);
         for (int tt = blockIdx.x; tt < n; tt += gridDim.x) {
             if (d.tiles[tt] == 0u) {
                 if (threadIdx.x == 0) {
@@ -557,7 +557,8 @@ struct VSolve {
                 }
                 continue;
             }
-            const int cx = (tt % tw) * 16 + (threadIdx.x & 15), cy = (tt / tw) * 16 + (threadIdx.x >> 4);
+            const int2 og = tile_origin(L0, tt);
+            const int cx = og.x + (threadIdx.x & 15), cy = og.y + (threadIdx.x >> 4);
             float4 acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
             if (in_grid(d, cx, cy)) {
                 const int i = cy * d.W + cx;
@@ -607,10 +608,10 @@ struct VSolve {
     }
     DEV void warm(int half) const {
         const Lv L0 = lev(d.lv, 0);
-        const int tw = tiles_x(L0);
         const int W = d.W;
         each(0, [&](uint32_t tt) {
-            const int cx = (int)(tt % tw) * 16 + (threadIdx.x & 15), cy = (int)(tt / tw) * 16 + (threadIdx.x >> 4);
+            const int2 og = tile_origin(L0, (int)tt);
+            const int cx = og.x + (threadIdx.x & 15), cy = og.y + (threadIdx.x >> 4);
             float4 acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
             if (in_grid(d, cx, cy) && interior(d, cx, cy)) {
                 const int i = cy * W + cx;
@@ -658,8 +659,8 @@ struct VSolve {
     }
     template <int RH>
     DEV Region<NU, RH> region(VStage<NU>& g, const Lv& L, uint32_t tt) const {
-        const int tw = tiles_x(L);
-        return Region<NU, RH>{g, s.sx, s, (int)(tt % tw) * 16, (int)(tt / tw) * 16};
+        const int2 og = tile_origin(L, (int)tt);
+        return Region<NU, RH>{g, s.sx, s, og.x, og.y};
     }
 
     // vmg_down.comp on level l (l = 0 at the start of a solve, right-hand side vr)
