@@ -452,8 +452,7 @@ DEV float2 coarse_z(const DevScene& d, const Zc& zc, int mx, int my) {
 // side (level 0: the residual before the update, and q when R.q) over the region; with
 // `update` (level 0 fused with cg_update.comp) the tile's own p, x and operator diagonal.
 template <class M>
-DEV void stage_down(const DevScene& d, int l, int t, const Rsrc<M>& R, bool update, const float2* p, Region& rg) {
-    const Lv F = lev(d.lv, l);
+DEV void stage_down(const DevScene& d, const Lv& F, int t, const Rsrc<M>& R, bool update, const float2* p, Region& rg) {
     const int2 og = tile_origin(F, t);
     const int ox = og.x, oy = og.y;
     const float2* r = R.r ? R.r : d.mgr;
@@ -485,8 +484,8 @@ DEV void stage_down(const DevScene& d, int l, int t, const Rsrc<M>& R, bool upda
 // update (rhs). Every neighbour's values are read before the terms are summed, in the
 // shader's order, each kept or not by a select.
 template <class M>
-DEV void finish_down(const DevScene& d, int l, int t, const Rsrc<M>& R, float2* r_out, float2* sz, Region& rg) {
-    const Lv F = lev(d.lv, l), C = lev(d.lv, l + 1);
+DEV void finish_down(const DevScene& d, const Lv& F, const Lv& C, int t, const Rsrc<M>& R, float2* r_out, float2* sz,
+                     Region& rg) {
     const int2 og = tile_origin(F, t);
     const int ox = og.x, oy = og.y;
     __syncthreads();   // (every thread's copies have landed)
@@ -521,39 +520,51 @@ DEV void finish_down(const DevScene& d, int l, int t, const Rsrc<M>& R, float2* 
         const float di = dg(k);
         return make_float2(sum.x / di, sum.y / di);
     };
-    const int2 lc = colour_cell();
-    const int lx = lc.x, ly = lc.y, cell = ly * 16 + lx;
-    const int cx = ox + lx, cy = oy + ly;
-    const int k0 = rslot(lx, ly);
-    const bool red = threadIdx.x < 128;
-    float2 z = make_float2(0.0f, 0.0f);
-    if (l_inside(F, cx, cy)) {
-        const int i = l_at(F, cx, cy);
-        const float D = dg(k0);
-        if (D > 0.0f) {
-            if (red) {
-                const float2 r = rhs(k0);
-                z = make_float2(r.x / D, r.y / D);
-            } else {
-                z = black(k0);
+    // one cell's z (mg_down: red from zero, black after it), the CG update and mgx
+    auto own = [&](int lx, int ly, bool red) {
+        const int cell = ly * 16 + lx;
+        const int cx = ox + lx, cy = oy + ly;
+        const int k0 = rslot(lx, ly);
+        float2 z = make_float2(0.0f, 0.0f);
+        if (l_inside(F, cx, cy)) {
+            const int i = l_at(F, cx, cy);
+            const float D = dg(k0);
+            if (D > 0.0f) {
+                if (red) {
+                    const float2 r = rhs(k0);
+                    z = make_float2(r.x / D, r.y / D);
+                } else {
+                    z = black(k0);
+                }
             }
+            if (r_out && rg.od[cell] > 0.0f) {
+                // cg_update.comp: x += alpha p, r -= alpha q (unknowns of active tiles)
+                const float2 pp = rg.o1[cell];
+                float2 x = rg.o2[cell];
+                x.x += R.ax * pp.x;
+                x.y += R.ay * pp.y;
+                d.pres[i] = x;
+                r_out[i] = rhs(k0);
+            }
+            M::setX(d, i, z);
         }
-        if (r_out && rg.od[cell] > 0.0f) {
-            // cg_update.comp: x += alpha p, r -= alpha q (unknowns of active tiles)
-            const float2 pp = rg.o1[cell];
-            float2 x = rg.o2[cell];
-            x.x += R.ax * pp.x;
-            x.y += R.ay * pp.y;
-            d.pres[i] = x;
-            r_out[i] = rhs(k0);
-        }
-        M::setX(d, i, z);
-    }
-    sz[cell] = z;
-    if (threadIdx.x < 32) {   // (a red warp) the black cells around the tile
-        const int2 rc = ring_cell(threadIdx.x);
+        sz[cell] = z;
+    };
+    // warps 0-3: the 128 black cells; warp 4: the 32 black cells around the tile (ring_cell),
+    // which the restriction needs; warps 5-7: the 128 red cells (the shorter formula), 96 + 32
+    const int tid = threadIdx.x;
+    if (tid < 128) {
+        const int ly = tid >> 3;
+        own(2 * (tid & 7) + 1 - (ly & 1), ly, false);
+    } else if (tid < 160) {
+        const int2 rc = ring_cell(tid - 128);
         const int kr = rslot(rc.x, rc.y);
-        rg.ring[threadIdx.x] = dg(kr) > 0.0f ? black(kr) : make_float2(0.0f, 0.0f);
+        rg.ring[tid - 128] = dg(kr) > 0.0f ? black(kr) : make_float2(0.0f, 0.0f);
+    } else {
+        for (int c = tid - 160; c < 128; c += 96) {
+            const int ly = c >> 3;
+            own(2 * (c & 7) + (ly & 1), ly, true);
+        }
     }
     __syncthreads();
     if (threadIdx.x < 64) {   // the restriction: aggregate (ax, ay), its red cells (0, 0) and (1, 1)
@@ -596,8 +607,7 @@ DEV void finish_down(const DevScene& d, int l, int t, const Rsrc<M>& R, float2* 
 // (u), the pre-smoothed values mgx (v) and each slot's coarse-grid value (w; from zc.s, this
 // block's shared copy of the tail, in finish_up).
 template <class M>
-DEV void stage_up(const DevScene& d, int l, int t, const Rsrc<M>& rhs, const Zc& zc, Region& rg) {
-    const Lv F = lev(d.lv, l);
+DEV void stage_up(const DevScene& d, const Lv& F, int t, const Rsrc<M>& rhs, const Zc& zc, Region& rg) {
     const int2 og = tile_origin(F, t);
     const int ox = og.x, oy = og.y;
     const float2* r = rhs.r ? rhs.r : d.mgr;
@@ -619,10 +629,9 @@ DEV void stage_up(const DevScene& d, int l, int t, const Rsrc<M>& rhs, const Zc&
 // ... and its arithmetic; on level 0 (flag) the tile's sums of r.z, r.r into part[t]. Read
 // as finish_down reads its slots.
 template <class M>
-DEV void finish_up(const DevScene& d, int l, int t, bool flag, const Zc& zc, float2* sz, typename M::acc4* buf,
+DEV void finish_up(const DevScene& d, const Lv& F, int t, bool flag, const Zc& zc, float2* sz, typename M::acc4* buf,
                    Region& rg) {
     using acc = typename M::acc;
-    const Lv F = lev(d.lv, l);
     typename M::acc4* part = M::part(d);
     const int2 og = tile_origin(F, t);
     const int ox = og.x, oy = og.y;
@@ -903,8 +912,9 @@ DEV bool vcycle(const DevScene& d, const Tail& tl, const Rsrc<M>& R, float2* r_o
         Rsrc<M> Rl = R;
         if (l > 0) Rl = Rsrc<M>{nullptr, nullptr, 0.0f, 0.0f};
         float2* ro = l == 0 ? r_out : nullptr;
-        pipe_active(d, l, tc, rg, [&](int t, Region& r) { stage_down<M>(d, l, t, Rl, ro != nullptr, p, r); },
-                    [&](int t, Region& r) { finish_down<M>(d, l, t, Rl, ro, sz, r); });
+        const Lv F = lev(d.lv, l), C = lev(d.lv, l + 1);
+        pipe_active(d, l, tc, rg, [&](int t, Region& r) { stage_down<M>(d, F, t, Rl, ro != nullptr, p, r); },
+                    [&](int t, Region& r) { finish_down<M>(d, F, C, t, Rl, ro, sz, r); });
         if (!grid_sync(d.K)) return false;
     }
     phase_tail<M>(d, tl, blockIdx.x == 0);
@@ -912,8 +922,9 @@ DEV bool vcycle(const DevScene& d, const Tail& tl, const Rsrc<M>& R, float2* r_o
         const Lv C = lev(d.lv, l + 1);
         const Zc zc{(l == tail - 1) ? tl.x : nullptr, C.off, C.w};
         const Rsrc<M> rhs = l == 0 ? Rsrc<M>{r_new, nullptr, 0.0f, 0.0f} : Rsrc<M>{nullptr, nullptr, 0.0f, 0.0f};
-        pipe_active(d, l, tc, rg, [&](int t, Region& r) { stage_up<M>(d, l, t, rhs, zc, r); },
-                    [&](int t, Region& r) { finish_up<M>(d, l, t, l == 0, zc, sz, buf, r); });
+        const Lv F = lev(d.lv, l);
+        pipe_active(d, l, tc, rg, [&](int t, Region& r) { stage_up<M>(d, F, t, rhs, zc, r); },
+                    [&](int t, Region& r) { finish_up<M>(d, F, t, l == 0, zc, sz, buf, r); });
         if (!grid_sync(d.K)) return false;
     }
     return true;
@@ -955,8 +966,7 @@ DEV void true_residual_tile(const DevScene& d, int t, Dbl4* part, Dbl4* buf) {
 // tile's sum of p.q into part[n + t]. Copies (one ring around the tile is enough): the
 // operator's diagonal, z (u) and p_old (v, unless both betas are zero); the couplings of the
 // tile's own cells.
-DEV void stage_apply(const DevScene& d, int t, bool nob, const float2* p_old, Region& rg) {
-    const Lv F = lev(d.lv, 0);
+DEV void stage_apply(const DevScene& d, const Lv& F, int t, bool nob, const float2* p_old, Region& rg) {
     const int2 og = tile_origin(F, t);
     const int ox = og.x, oy = og.y;
 #pragma unroll
@@ -978,9 +988,9 @@ DEV void stage_apply(const DevScene& d, int t, bool nob, const float2* p_old, Re
 }
 
 template <class M>
-DEV void finish_apply(const DevScene& d, int t, float b0, float b1, float2* p_new, typename M::acc4* buf, Region& rg) {
+DEV void finish_apply(const DevScene& d, const Lv& F, int t, float b0, float b1, float2* p_new, typename M::acc4* buf,
+                      Region& rg) {
     using acc = typename M::acc;
-    const Lv F = lev(d.lv, 0);
     const int n = d.nwg;
     typename M::acc4* part = M::part(d) + n;
     const bool nob = b0 == 0.0f && b1 == 0.0f;
@@ -1170,12 +1180,13 @@ __global__ void __launch_bounds__(NT, 2) k_mgpcg(DevScene d, int second, int sca
     }
     float2* p_old = d.cgp;
     float2* p_new = d.cgp2;
+    const Lv L0 = lev(d.lv, 0);
     for (uint32_t it = 0; it < P->pressure_max_iters; it++) {
         if (K.done[0] && K.done[1]) break;
         const float b0 = (float)K.beta[0], b1 = (float)K.beta[1];
         const bool nob = b0 == 0.0f && b1 == 0.0f;
-        pipe_active(d, 0, tc, rg, [&](int t, Region& r) { stage_apply(d, t, nob, p_old, r); },
-                    [&](int t, Region& r) { finish_apply<M>(d, t, b0, b1, p_new, buf, r); });
+        pipe_active(d, 0, tc, rg, [&](int t, Region& r) { stage_apply(d, L0, t, nob, p_old, r); },
+                    [&](int t, Region& r) { finish_apply<M>(d, L0, t, b0, b1, p_new, buf, r); });
         if (!grid_sync(d.K)) return;
         {
             acc4 b = total(part + n, n, buf);
@@ -1378,11 +1389,12 @@ __global__ void __launch_bounds__(NT, 2) k_mgpcg_batch(BatchView B, int second) 
                 B, l, tc, rg,
                 [&](int s, const DevScene& d, int t, Region& r) {
                     if (l >= d.lv.tail || (fused && !running(s, it))) return;
-                    stage_down<M>(d, l, t, rsrc(s, d), l == 0 && fused, parity_p(d, ir + 1), r);
+                    stage_down<M>(d, lev(d.lv, l), t, rsrc(s, d), l == 0 && fused, parity_p(d, ir + 1), r);
                 },
                 [&](int s, const DevScene& d, int t, Region& r) {
                     if (l >= d.lv.tail || (fused && !running(s, it))) return;
-                    finish_down<M>(d, l, t, rsrc(s, d), (l == 0 && fused) ? parity_r(d, ir + 1) : nullptr, sz, r);
+                    finish_down<M>(d, lev(d.lv, l), lev(d.lv, l + 1), t, rsrc(s, d), (l == 0 && fused) ? parity_r(d, ir + 1) : nullptr,
+                                   sz, r);
                 });
             if (!grid_sync(BK)) return false;
         }
@@ -1407,11 +1419,11 @@ __global__ void __launch_bounds__(NT, 2) k_mgpcg_batch(BatchView B, int second) 
                 B, l, tc, rg,
                 [&](int s, const DevScene& d, int t, Region& r) {
                     if (l >= d.lv.tail || (fused && !running(s, it))) return;
-                    stage_up<M>(d, l, t, rhs_of(d), zc_of(d), r);
+                    stage_up<M>(d, lev(d.lv, l), t, rhs_of(d), zc_of(d), r);
                 },
                 [&](int s, const DevScene& d, int t, Region& r) {
                     if (l >= d.lv.tail || (fused && !running(s, it))) return;
-                    finish_up<M>(d, l, t, l == 0, zc_of(d), sz, buf, r);
+                    finish_up<M>(d, lev(d.lv, l), t, l == 0, zc_of(d), sz, buf, r);
                 });
             if (!grid_sync(BK)) return false;
         }
@@ -1443,11 +1455,11 @@ __global__ void __launch_bounds__(NT, 2) k_mgpcg_batch(BatchView B, int second) 
             [&](int s, const DevScene& d, int t, Region& r) {
                 if (!running(s, it)) return;
                 const float b0 = (float)KS[s].beta[0], b1 = (float)KS[s].beta[1];
-                stage_apply(d, t, b0 == 0.0f && b1 == 0.0f, parity_p(d, it), r);
+                stage_apply(d, lev(d.lv, 0), t, b0 == 0.0f && b1 == 0.0f, parity_p(d, it), r);
             },
             [&](int s, const DevScene& d, int t, Region& r) {
                 if (!running(s, it)) return;
-                finish_apply<M>(d, t, (float)KS[s].beta[0], (float)KS[s].beta[1], parity_p(d, it + 1), buf, r);
+                finish_apply<M>(d, lev(d.lv, 0), t, (float)KS[s].beta[0], (float)KS[s].beta[1], parity_p(d, it + 1), buf, r);
             });
         if (!grid_sync(BK)) return;
         for (int s = blockIdx.x; s < B.ns; s += gridDim.x) {
