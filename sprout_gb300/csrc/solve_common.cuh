@@ -58,8 +58,11 @@ DEV bool grid_sync(SolveState* K) {
         } else {
             const unsigned long long t_in = trace ? global_ns() : 0ull;
             const uint32_t base = trace ? *(volatile uint32_t*)&K->trace_base : 0u;
-            __threadfence();
-            const uint32_t old = atomicAdd(&K->bar_count, 1u);
+            // the arrival releases the block's writes (ordered before it by the block barrier
+            // above; release is cumulative), the acquiring reads of the wait make the other
+            // blocks' writes visible to this block after the block barrier below
+            uint32_t old;
+            asm volatile("atom.add.release.gpu.u32 %0, [%1], 1;" : "=r"(old) : "l"(&K->bar_count) : "memory");
             const uint32_t epoch = old / gridDim.x;
             const uint32_t target = (epoch + 1u) * gridDim.x;
             unsigned long long* row = nullptr;
@@ -68,7 +71,10 @@ DEV bool grid_sync(SolveState* K) {
                 row[blockIdx.x] = t_in;
             }
             uint32_t spins = 0;
-            while (*vcnt < target) {
+            for (;;) {
+                uint32_t now;
+                asm volatile("ld.acquire.gpu.u32 %0, [%1];" : "=r"(now) : "l"(&K->bar_count) : "memory");
+                if (now >= target) break;
                 if (*verr != 0u) { ok = 0; break; }
                 __nanosleep(32);
                 if (++spins > SPIN_LIMIT) {
@@ -80,7 +86,6 @@ DEV bool grid_sync(SolveState* K) {
                     break;
                 }
             }
-            __threadfence();
             if (row && blockIdx.x == 0) row[K->trace_cols - 1] = global_ns();
         }
         s_ok = ok;
