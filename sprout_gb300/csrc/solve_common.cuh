@@ -76,7 +76,6 @@ DEV bool grid_sync(SolveState* K) {
                 asm volatile("ld.acquire.gpu.u32 %0, [%1];" : "=r"(now) : "l"(&K->bar_count) : "memory");
                 if (now >= target) break;
                 if (*verr != 0u) { ok = 0; break; }
-                __nanosleep(32);
                 if (++spins > SPIN_LIMIT) {
                     if (atomicExch(&K->error, 1u) == 0u) {
                         K->err_arrived = *vcnt - epoch * gridDim.x;
