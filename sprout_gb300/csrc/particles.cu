@@ -542,8 +542,8 @@ __global__ void __launch_bounds__(256) k_cell_gather(DevScene d) {
 constexpr int P2G_T = 16;                 // nodes per tile edge
 constexpr int P2G_HALO_ROWS = P2G_T + 3;  // particle cells [n0 - 2, n0 + 16]
 
-DEV void sadd(int* sacc, int stride, int lx, int ly, int ch, int v) {
-    if (lx >= 0 && ly >= 0 && lx < P2G_T && ly < P2G_T) atomicAdd(&sacc[(ly * P2G_T + lx) * stride + ch], v);
+DEV void sadd(int* sacc, int ps, int lx, int ly, int ch, int v) {
+    if (lx >= 0 && ly >= 0 && lx < P2G_T && ly < P2G_T) atomicAdd(&sacc[(ly * P2G_T + lx) * ps + ch], v);
 }
 
 __global__ void __launch_bounds__(256) k_p2g(DevScene d) {
@@ -552,8 +552,9 @@ __global__ void __launch_bounds__(256) k_p2g(DevScene d) {
     const DevParams* P = d.P;
     const DevMat* mats = d.mats;
     const int stride = d.stride;
+    const int pst = stride + 1;   // a node's channels padded by one word: nodes on distinct banks
     const int n0x = blockIdx.x * P2G_T, n0y = blockIdx.y * P2G_T;
-    for (int k = threadIdx.x; k < P2G_T * P2G_T * stride; k += blockDim.x) sacc[k] = 0;
+    for (int k = threadIdx.x; k < P2G_T * P2G_T * pst; k += blockDim.x) sacc[k] = 0;
     if (threadIdx.x < P2G_HALO_ROWS) {
         int cy = n0y - 2 + threadIdx.x;
         uint32_t b = 0, e = 0;
@@ -617,8 +618,8 @@ __global__ void __launch_bounds__(256) k_p2g(DevScene d) {
                     if (lx < 0 || ly < 0 || lx >= P2G_T || ly >= P2G_T) continue;
                     float m = wx[a] * wy[b] * rho;
                     float ddx = (float)a - fx, ddy = (float)b - fy;
-                    sadd(sacc, stride, lx, ly, 0, (int)floorf(m * MASS_SCALE + 0.5f));
-                    sadd(sacc, stride, lx, ly, 1, (int)floorf(m * (vsx + (csx * ddx + csy * ddy)) * MOM_SCALE + 0.5f));
+                    sadd(sacc, pst, lx, ly, 0, (int)floorf(m * MASS_SCALE + 0.5f));
+                    sadd(sacc, pst, lx, ly, 1, (int)floorf(m * (vsx + (csx * ddx + csy * ddy)) * MOM_SCALE + 0.5f));
                 }
         }
         {   // v faces at (i + 0.5, j)
@@ -634,8 +635,8 @@ __global__ void __launch_bounds__(256) k_p2g(DevScene d) {
                     if (lx < 0 || ly < 0 || lx >= P2G_T || ly >= P2G_T) continue;
                     float m = wx[a] * wy[b] * rho;
                     float ddx = (float)a - fx, ddy = (float)b - fy;
-                    sadd(sacc, stride, lx, ly, 2, (int)floorf(m * MASS_SCALE + 0.5f));
-                    sadd(sacc, stride, lx, ly, 3, (int)floorf(m * (vsy + (csz * ddx + csw * ddy)) * MOM_SCALE + 0.5f));
+                    sadd(sacc, pst, lx, ly, 2, (int)floorf(m * MASS_SCALE + 0.5f));
+                    sadd(sacc, pst, lx, ly, 3, (int)floorf(m * (vsy + (csz * ddx + csw * ddy)) * MOM_SCALE + 0.5f));
                 }
         }
         {   // cell centres
@@ -650,13 +651,13 @@ __global__ void __launch_bounds__(256) k_p2g(DevScene d) {
                     int lx = bx + a - n0x, ly = by + b - n0y;
                     if (lx < 0 || ly < 0 || lx >= P2G_T || ly >= P2G_T) continue;
                     int wi = (int)floorf(wx[a] * wy[b] * MASS_SCALE + 0.5f);
-                    sadd(sacc, stride, lx, ly, 4, wi);
-                    if (cw >= 0) sadd(sacc, stride, lx, ly, cw, wi);
-                    if (cs >= 0 && ps > 0.0f) sadd(sacc, stride, lx, ly, cs, (int)floorf(wx[a] * wy[b] * ps * MASS_SCALE + 0.5f));
+                    sadd(sacc, pst, lx, ly, 4, wi);
+                    if (cw >= 0) sadd(sacc, pst, lx, ly, cw, wi);
+                    if (cs >= 0 && ps > 0.0f) sadd(sacc, pst, lx, ly, cs, (int)floorf(wx[a] * wy[b] * ps * MASS_SCALE + 0.5f));
                     if (ct >= 0) {
                         int hq = (int)floorf(wx[a] * wy[b] * CT * MASS_SCALE + 0.5f);
-                        sadd(sacc, stride, lx, ly, ct, hq);
-                        if (cg >= 0) sadd(sacc, stride, lx, ly, cg, hq);
+                        sadd(sacc, pst, lx, ly, ct, hq);
+                        if (cg >= 0) sadd(sacc, pst, lx, ly, cg, hq);
                     }
                 }
         }
@@ -666,7 +667,7 @@ __global__ void __launch_bounds__(256) k_p2g(DevScene d) {
     for (int k = threadIdx.x; k < P2G_T * P2G_T * stride; k += blockDim.x) {
         int node = k / stride, ch = k - node * stride;
         int nx = n0x + (node % P2G_T), ny = n0y + node / P2G_T;
-        if (nx < d.W && ny < d.H) d.acc[(ny * d.W + nx) * stride + ch] = sacc[k];
+        if (nx < d.W && ny < d.H) d.acc[(ny * d.W + nx) * stride + ch] = sacc[node * pst + ch];
     }
 }
 
@@ -697,7 +698,7 @@ void launch_sort(const DevScene& d, const LaunchCfg& cfg, cudaStream_t st) {
 void launch_p2g(const DevScene& d, const LaunchCfg& cfg, cudaStream_t st) {
     (void)cfg;
     dim3 tiles((d.W + P2G_T - 1) / P2G_T, (d.H + P2G_T - 1) / P2G_T);
-    size_t smem = (size_t)P2G_T * P2G_T * d.stride * sizeof(int);
+    size_t smem = (size_t)P2G_T * P2G_T * (d.stride + 1) * sizeof(int);
     k_p2g<<<tiles, 256, smem, st>>>(d);
 }
 
