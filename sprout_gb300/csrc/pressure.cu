@@ -901,6 +901,14 @@ DEV void pipe_active(const DevScene& d, int l, const TileCache& tc, Region* rg, 
         rg, [&](uint32_t t, Region& r) { stage((int)t, r); }, [&](uint32_t t, Region& r) { finish((int)t, r); });
 }
 
+// Whether this block computes the tail of scene d: it owns a tile of the level above the tail
+// (whose way up reads the tail's result from the block's own copy), or it is block 0.
+DEV bool tail_reader(const DevScene& d, const TileCache& tc) {
+    const int l = d.lv.tail - 1;
+    const uint32_t cnt = l < kCacheLevels ? tc.cnt[l] : *(volatile uint32_t*)&d.pcount[l];
+    return blockIdx.x == 0 || blockIdx.x < cnt;
+}
+
 // One V-cycle of one scene: level 0's right-hand side through R (fused with the CG update
 // when R.q is set), result in mgz of level 0, partials of r.z and r.r. Returns false on a
 // barrier timeout.
@@ -917,7 +925,9 @@ DEV bool vcycle(const DevScene& d, const Tail& tl, const Rsrc<M>& R, float2* r_o
                     [&](int t, Region& r) { finish_down<M>(d, F, C, t, Rl, ro, sz, r); });
         if (!grid_sync(d.K)) return false;
     }
-    phase_tail<M>(d, tl, blockIdx.x == 0);
+    // only the blocks with a tile of the level above the tail read the tail's result (from
+    // their own copy); block 0 also stores it
+    if (tail_reader(d, tc)) phase_tail<M>(d, tl, blockIdx.x == 0);
     for (int l = tail - 1; l >= 0; l--) {
         const Lv C = lev(d.lv, l + 1);
         const Zc zc{(l == tail - 1) ? tl.x : nullptr, C.off, C.w};
@@ -1163,7 +1173,7 @@ __global__ void __launch_bounds__(NT, 2) k_mgpcg(DevScene d, int second, int sca
     for (int t = blockIdx.x; t < n; t += gridDim.x) zero_inactive_tile<M>(d, t);
     if (!grid_sync(d.K)) return;
     fill_cache(d, tc);
-    tail_setup<M>(d, tl, blockIdx.x == 0);
+    if (tail_reader(d, tc)) tail_setup<M>(d, tl, blockIdx.x == 0);
     float2* r_cur = d.mgr;    // level 0 of mgr: the residual, double-buffered with mgr2
     float2* r_nxt = d.mgr2;
     for_active(d, 0, tc, [&](int t) { residual_tile<M>(d, t, r_cur, buf, false); });
