@@ -62,7 +62,12 @@ struct Plain {
     DEV static float2 R(const DevScene& d, int i) { return d.mgr[i]; }   // a coarse level's rhs
     DEV static void setR(const DevScene& d, int i, float2 v) { d.mgr[i] = v; }
     DEV static acc4* part(const DevScene& d) { return d.partials; }
-    DEV static acc4 a4(float x, float y, float z, float w) { return make_float4(x, y, z, w); }
+    DEV static acc4 zero4() { return make_float4(0.0f, 0.0f, 0.0f, 0.0f); }
+    // the four products a_k b_k of a cell's partial sums, and a total as the scalars use it
+    DEV static acc4 prod4(float a0, float b0, float a1, float b1, float a2, float b2, float a3, float b3) {
+        return make_float4(a0 * b0, a1 * b1, a2 * b2, a3 * b3);
+    }
+    DEV static float4 fin(acc4 a) { return a; }
     // the stored matrix as a tile region stages it: bytes per row of couplings, their address,
     // the diagonal's array, and the row read from its staged slot in FP32
     static constexpr int kABytes = 16;
@@ -81,7 +86,7 @@ DEV float2 unpack(uint32_t u) { return __bfloat1622float2(*reinterpret_cast<cons
 struct Mixed {
     static constexpr bool kMixed = true;
     using acc = double;
-    using acc4 = Dbl4;
+    using acc4 = FF4;   // the partial sums as float pairs, their totals to FP64 (fin)
     // the hierarchy in BF16: a row's four couplings as two bfloat162 in a uint2
     DEV static float4 A(const DevScene& d, int i) {
         const uint2 u = d.hga[i];
@@ -115,8 +120,12 @@ struct Mixed {
     DEV static void setZ(const DevScene& d, int i, float2 v) { d.mgz[i] = v; }
     DEV static float2 R(const DevScene& d, int i) { return d.mgr[i]; }
     DEV static void setR(const DevScene& d, int i, float2 v) { d.mgr[i] = v; }
-    DEV static acc4* part(const DevScene& d) { return d.partials64; }
-    DEV static acc4 a4(double x, double y, double z, double w) { return Dbl4{x, y, z, w}; }
+    DEV static acc4* part(const DevScene& d) { return reinterpret_cast<FF4*>(d.partials64); }
+    DEV static acc4 zero4() { return FF4{make_float4(0.0f, 0.0f, 0.0f, 0.0f), make_float4(0.0f, 0.0f, 0.0f, 0.0f)}; }
+    DEV static acc4 prod4(float a0, float b0, float a1, float b1, float a2, float b2, float a3, float b3) {
+        return ff_prod4(a0, b0, a1, b1, a2, b2, a3, b3);
+    }
+    DEV static Dbl4 fin(acc4 a) { return to_dbl(a); }
     static constexpr int kABytes = 8;
     DEV static const void* Araw(const DevScene& d, int i) { return d.hga + i; }
     DEV static const float* Dptr(const DevScene& d) { return d.hgd; }
@@ -228,11 +237,11 @@ DEV void residual_tile(const DevScene& d, int t, float2* r0, typename M::acc4* b
     const int n = d.nwg;
     typename M::acc4* part = M::part(d) + (rr ? 0 : n);
     if (d.ptile[F.toff + t] == 0u) {
-        if (threadIdx.x == 0) part[t] = M::a4(0, 0, 0, 0);
+        if (threadIdx.x == 0) part[t] = M::zero4();
         return;
     }
     const int cx = (t % tiles_x(F)) * 16 + (threadIdx.x & 15), cy = (t / tiles_x(F)) * 16 + (threadIdx.x >> 4);
-    typename M::acc4 a4 = M::a4(0, 0, 0, 0);
+    typename M::acc4 a4 = M::zero4();
     if (l_inside(F, cx, cy)) {
         const int i = l_at(F, cx, cy);
         const float D = d.mgd[i];
@@ -252,8 +261,8 @@ DEV void residual_tile(const DevScene& d, int t, float2* r0, typename M::acc4* b
             float4 b = d.prhs[i];
             const float2 r = make_float2(b.x - axx, b.y - axy);
             r0[i] = r;
-            if (rr) a4 = M::a4(0, 0, (acc)r.x * (acc)r.x, (acc)r.y * (acc)r.y);
-            else a4 = M::a4((acc)b.x * (acc)b.x, (acc)b.y * (acc)b.y, 0, 0);
+            if (rr) a4 = M::prod4(0.0f, 0.0f, 0.0f, 0.0f, r.x, r.x, r.y, r.y);
+            else a4 = M::prod4(b.x, b.x, b.y, b.y, 0.0f, 0.0f, 0.0f, 0.0f);
         } else {
             r0[i] = make_float2(0.0f, 0.0f);
         }
@@ -689,7 +698,7 @@ DEV void finish_up(const DevScene& d, const Lv& F, int t, bool flag, const Zc& z
         rg.ring[threadIdx.x] = dg(kr) > 0.0f ? black(kr) : make_float2(0.0f, 0.0f);
     }
     __syncthreads();
-    typename M::acc4 a4 = M::a4(0, 0, 0, 0);
+    typename M::acc4 a4 = M::zero4();
     if (l_inside(F, cx, cy)) {
         const int i = l_at(F, cx, cy);
         if (unk) {
@@ -718,7 +727,7 @@ DEV void finish_up(const DevScene& d, const Lv& F, int t, bool flag, const Zc& z
                 const float di = dg(k0);
                 z = make_float2(sx / di, sy / di);
             }
-            a4 = M::a4((acc)r.x * (acc)z.x, (acc)r.y * (acc)z.y, (acc)r.x * (acc)r.x, (acc)r.y * (acc)r.y);
+            a4 = M::prod4(r.x, z.x, r.y, z.y, r.x, r.x, r.y, r.y);
         }
         M::setZ(d, i, z);
     }
@@ -851,8 +860,8 @@ template <class M>
 DEV void zero_inactive_tile(const DevScene& d, int t) {
     if (threadIdx.x != 0 || d.ptile[t] != 0u) return;
     const int n = d.nwg;
-    M::part(d)[t] = M::a4(0, 0, 0, 0);
-    M::part(d)[n + t] = M::a4(0, 0, 0, 0);
+    M::part(d)[t] = M::zero4();
+    M::part(d)[n + t] = M::zero4();
     if (M::kMixed) d.partials64[t] = Dbl4{0.0, 0.0, 0.0, 0.0};
 }
 
@@ -1019,7 +1028,7 @@ DEV void finish_apply(const DevScene& d, const Lv& F, int t, float b0, float b1,
     };
     const int cx = ox + (threadIdx.x & 15), cy = oy + (threadIdx.x >> 4);
     const int k0 = rslot(threadIdx.x & 15, threadIdx.x >> 4);
-    typename M::acc4 a4 = M::a4(0, 0, 0, 0);
+    typename M::acc4 a4 = M::zero4();
     if (l_inside(F, cx, cy)) {
         const int i = l_at(F, cx, cy);
         const float D = dg(k0);
@@ -1045,7 +1054,7 @@ DEV void finish_apply(const DevScene& d, const Lv& F, int t, float b0, float b1,
             }
             p_new[i] = pp;
             d.cgq[i] = make_float2(qx, qy);
-            a4 = M::a4(0, 0, (acc)pp.x * (acc)qx, (acc)pp.y * (acc)qy);
+            a4 = M::prod4(0.0f, 0.0f, 0.0f, 0.0f, pp.x, qx, pp.y, qy);
         } else {
             p_new[i] = make_float2(0.0f, 0.0f);
         }
@@ -1180,11 +1189,11 @@ __global__ void __launch_bounds__(NT, 2) k_mgpcg(DevScene d, int second, int sca
     if (!grid_sync(d.K)) return;
     // b.b now, while nothing writes the second half of the partials: the first apply phase
     // after the V-cycle does, and a block can reach it before a slower one has summed them
-    const acc4 b = total(part + n, n, buf);
+    const auto b = M::fin(total(part + n, n, buf));
     if (!vcycle<M>(d, tl, Rsrc<M>{r_cur, nullptr, 0.0f, 0.0f}, nullptr, nullptr, r_cur, sz, buf, rg, tc)) return;
     const acc tx = (acc)P->tol[0], ty = (acc)P->tol[1];
     {
-        acc4 a = total(part, n, buf);
+        const auto a = M::fin(total(part, n, buf));
         if (threadIdx.x == 0) scal_start<acc>(K, a, b, tx, ty, second);
         __syncthreads();
     }
@@ -1199,14 +1208,14 @@ __global__ void __launch_bounds__(NT, 2) k_mgpcg(DevScene d, int second, int sca
                     [&](int t, Region& r) { finish_apply<M>(d, L0, t, b0, b1, p_new, buf, r); });
         if (!grid_sync(d.K)) return;
         {
-            acc4 b = total(part + n, n, buf);
+            const auto b = M::fin(total(part + n, n, buf));
             if (threadIdx.x == 0) scal_alpha<acc>(K, b);
             __syncthreads();
         }
         Rsrc<M> R{r_cur, d.cgq, (float)K.alpha[0], (float)K.alpha[1]};
         if (!vcycle<M>(d, tl, R, r_nxt, p_new, r_nxt, sz, buf, rg, tc)) return;
         {
-            acc4 a = total(part, n, buf);
+            const auto a = M::fin(total(part, n, buf));
             if (threadIdx.x == 0) scal_beta<acc>(K, a, tx, ty);
             __syncthreads();
         }
@@ -1374,7 +1383,7 @@ __global__ void __launch_bounds__(NT, 2) k_mgpcg_batch(BatchView B, int second) 
     // b.b of each scene (before the first apply phase reuses those partials)
     for (int s = blockIdx.x; s < B.ns; s += gridDim.x) {
         const DevScene& d = B.scenes[s];
-        const acc4 b = total(M::part(d) + d.nwg, d.nwg, buf);
+        const auto b = M::fin(total(M::part(d) + d.nwg, d.nwg, buf));
         if (threadIdx.x == 0) {
             KS[s].bb[0] = b.x;
             KS[s].bb[1] = b.y;
@@ -1442,9 +1451,9 @@ __global__ void __launch_bounds__(NT, 2) k_mgpcg_batch(BatchView B, int second) 
     if (!vcycle_all(-1)) return;
     for (int s = blockIdx.x; s < B.ns; s += gridDim.x) {
         const DevScene& d = B.scenes[s];
-        const acc4 a = total(M::part(d), d.nwg, buf);
+        const auto a = M::fin(total(M::part(d), d.nwg, buf));
         if (threadIdx.x == 0) {
-            acc4 b = a;
+            auto b = a;
             b.x = KS[s].bb[0];
             b.y = KS[s].bb[1];
             scal_start<acc>(KS[s], a, b, tol(d, 0), tol(d, 1), second);
@@ -1475,7 +1484,7 @@ __global__ void __launch_bounds__(NT, 2) k_mgpcg_batch(BatchView B, int second) 
         for (int s = blockIdx.x; s < B.ns; s += gridDim.x) {
             if (!running(s, it)) continue;
             const DevScene& d = B.scenes[s];
-            const acc4 b = total(M::part(d) + d.nwg, d.nwg, buf);
+            const auto b = M::fin(total(M::part(d) + d.nwg, d.nwg, buf));
             if (threadIdx.x == 0) scal_alpha<acc>(KS[s], b);
             __syncthreads();
         }
@@ -1484,7 +1493,7 @@ __global__ void __launch_bounds__(NT, 2) k_mgpcg_batch(BatchView B, int second) 
         for (int s = blockIdx.x; s < B.ns; s += gridDim.x) {
             if (!running(s, it)) continue;
             const DevScene& d = B.scenes[s];
-            const acc4 a = total(M::part(d), d.nwg, buf);
+            const auto a = M::fin(total(M::part(d), d.nwg, buf));
             if (threadIdx.x == 0) scal_beta<acc>(KS[s], a, tol(d, 0), tol(d, 1));
             __syncthreads();
         }

@@ -517,6 +517,11 @@ struct SproutSim {
         want.visc_levels = std::min((int)std::max(params.viscosity_mg_levels, 1u), d.lv.tail);
         want.visc_sweeps = (int)std::min(std::max(params.viscosity_mg_sweeps, 1u), 2u);
         want.visc_blocks = std::max(1, std::min(d.nwg, visc_max[want.visc_sweeps - 1]));
+        // SPROUT_VISC_BLOCKS: a tuning override of the persistent viscosity kernel's block count
+        if (const char* e = std::getenv("SPROUT_VISC_BLOCKS")) {
+            const int v = std::atoi(e);
+            if (v > 0) want.visc_blocks = std::max(1, std::min(v, visc_max[want.visc_sweeps - 1]));
+        }
         want.mixed = mixed;
         bool same = want.n_slots == cfg.n_slots && want.thermal == cfg.thermal && want.heat == cfg.heat &&
                     want.visc_mode == cfg.visc_mode && want.twice == cfg.twice && want.viscous_warm == cfg.viscous_warm &&

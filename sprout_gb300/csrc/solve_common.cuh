@@ -137,6 +137,37 @@ DEV void pipeline(uint32_t cnt, I&& item, S&& stage, F&& finish) {
 DEV float4 add4(float4 a, float4 b) { return make_float4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w); }
 DEV Dbl4 add4(Dbl4 a, Dbl4 b) { return Dbl4{a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w}; }
 
+// Four sums each carried as an unevaluated pair of floats, hi + lo (about 48 significant
+// bits): FP32 error-free transformations instead of FP64 arithmetic, which runs at a small
+// fraction of the FP32 rate on this GPU. A product of two floats is exact as a pair (the FMA
+// gives its rounding error); a sum of pairs keeps the rounding error of the high parts.
+struct FF4 {
+    float4 hi, lo;
+};
+DEV float2 ff_add(float ahi, float alo, float bhi, float blo) {
+    const float s = ahi + bhi;
+    const float bv = s - ahi;
+    float e = (ahi - (s - bv)) + (bhi - bv);
+    e += alo + blo;
+    const float hi = s + e;
+    return make_float2(hi, e - (hi - s));
+}
+DEV FF4 add4(FF4 a, FF4 b) {
+    const float2 x = ff_add(a.hi.x, a.lo.x, b.hi.x, b.lo.x), y = ff_add(a.hi.y, a.lo.y, b.hi.y, b.lo.y);
+    const float2 z = ff_add(a.hi.z, a.lo.z, b.hi.z, b.lo.z), w = ff_add(a.hi.w, a.lo.w, b.hi.w, b.lo.w);
+    return FF4{make_float4(x.x, y.x, z.x, w.x), make_float4(x.y, y.y, z.y, w.y)};
+}
+// the exact products a0 b0 .. a3 b3 as pairs
+DEV FF4 ff_prod4(float a0, float b0, float a1, float b1, float a2, float b2, float a3, float b3) {
+    const float p0 = a0 * b0, p1 = a1 * b1, p2 = a2 * b2, p3 = a3 * b3;
+    return FF4{make_float4(p0, p1, p2, p3),
+               make_float4(fmaf(a0, b0, -p0), fmaf(a1, b1, -p1), fmaf(a2, b2, -p2), fmaf(a3, b3, -p3))};
+}
+DEV Dbl4 to_dbl(FF4 a) {
+    return Dbl4{(double)a.hi.x + (double)a.lo.x, (double)a.hi.y + (double)a.lo.y, (double)a.hi.z + (double)a.lo.z,
+                (double)a.hi.w + (double)a.lo.w};
+}
+
 // At the end of a persistent kernel (block 0, after its last barrier, which every block has
 // reached): the trace rows of the next launch follow this one's.
 DEV void trace_launch_done(SolveState* K) {
@@ -151,6 +182,7 @@ DEV Dbl4 shfl_down4(Dbl4 v, int s) {
     return Dbl4{__shfl_down_sync(0xffffffffu, v.x, s), __shfl_down_sync(0xffffffffu, v.y, s),
                 __shfl_down_sync(0xffffffffu, v.z, s), __shfl_down_sync(0xffffffffu, v.w, s)};
 }
+DEV FF4 shfl_down4(FF4 v, int s) { return FF4{shfl_down4(v.hi, s), shfl_down4(v.lo, s)}; }
 
 // Work-group tree of reduce.glsl:5-14 over the 256 values in buf; result in buf[0]. The
 // pairs are those of the tree (t with t + s, s = 128 .. 1): the three wide steps through
