@@ -45,6 +45,19 @@ void launch_project(const DevScene& d, const LaunchCfg& cfg, cudaStream_t st);
 // and projection of the second pressure solve.
 void launch_viscosity_setup(const DevScene& d, const LaunchCfg& cfg, cudaStream_t st);
 cudaError_t launch_viscosity(const DevScene& d, const LaunchCfg& cfg, cudaStream_t st, int restrain);
+// The viscosity solves of a batch of tanks (all with the same sweep count) in one persistent
+// kernel over their flattened active-tile lists.
+struct VBatchView {
+    const DevScene* scenes;   // ns tanks
+    int ns;
+    const int* off0;          // the ns + 1 prefix sums of the tanks' level-0 tile counts
+    void* scal;               // per tank, the solve's scalars (viscosity_batch_scalar_bytes each)
+    SolveState* K;            // the batch's grid barrier and error word
+    int* aoff;                // per level 0 .. max_lev, the ns + 1 prefix sums of active tiles (filled)
+    int max_lev;              // the most coarse levels over the tanks
+};
+size_t viscosity_batch_scalar_bytes();
+cudaError_t launch_viscosity_batch(const VBatchView& B, int sweeps, int blocks, cudaStream_t st);
 void launch_second_projection_rhs(const DevScene& d, cudaStream_t st);
 void launch_second_projection(const DevScene& d, cudaStream_t st);
 // Blocks of the persistent viscosity kernel that fit on the device at once.

@@ -973,11 +973,56 @@ struct SproutBatch {
     } first, second;
     size_t h2d = 0;
 
+    // The viscosity solves of the tanks with a second solve, batched in one persistent kernel
+    // when they share a sweep count (vis_ok): the second view's scenes, level-0 prefix sums,
+    // barrier word and active-tile array, with scalars of its own.
+    VBatchView vis{};
+    bool vis_ok = false;
+    int vis_sweeps = 0, vis_blocks = 0, vis_cap = 0;
+    unsigned char* dvscal = nullptr;
+    int build_visc_view() {
+        vis_ok = false;
+        const int ns = second.v.ns;
+        if (ns < 2) return SPROUT_OK;
+        // SPROUT_BATCH_VISCOSITY=0: one viscosity solve per tank (for comparison)
+        if (const char* e = std::getenv("SPROUT_BATCH_VISCOSITY"))
+            if (std::atoi(e) == 0) return SPROUT_OK;
+        const int sw = second.members[0]->cfg.visc_sweeps;
+        int max_lev = 0, tiles = 0;
+        for (const SproutSim* sim : second.members) {
+            if (sim->cfg.visc_sweeps != sw) return SPROUT_OK;   // mixed sweep counts: one solve per tank
+            max_lev = std::max(max_lev, sim->cfg.visc_levels);
+            tiles += sim->d.nwg;
+        }
+        // large tanks fill the device one at a time: the batched solve only adds its separate
+        // reduction phases (measured: +13 to +44 % for 8-16 tanks of 128 x 72 to 256 x 144,
+        // -2.5 % for 4 tanks of 1024 x 576)
+        if (tiles > 1500 * ns) return SPROUT_OK;
+        if (ns > vis_cap) {
+            CUDA_TRY(cudaStreamSynchronize(main));
+            if (dvscal) cudaFree(dvscal);
+            dvscal = nullptr;
+            vis_cap = 0;
+            const int cap = std::max(ns, 2 * second.cap);
+            if (cudaMalloc(&dvscal, (size_t)cap * viscosity_batch_scalar_bytes()) != cudaSuccess) {
+                dvscal = nullptr;
+                return fail(SPROUT_E_NOMEM, "batch viscosity scalars");
+            }
+            vis_cap = cap;
+        }
+        vis = VBatchView{second.ds, ns, second.doff, dvscal, second.dk, second.daoff, max_lev};
+        vis_sweeps = sw;
+        vis_blocks = std::max(1, std::min(viscosity_blocks_max(device, sw), tiles));
+        vis_ok = true;
+        return SPROUT_OK;
+    }
+
     ~SproutBatch() {
         for (SproutSim* sim : sims) sim->batch = nullptr;
         drop_graph();
         first.release();
         second.release();
+        if (dvscal) cudaFree(dvscal);
         for (cudaEvent_t e : events) cudaEventDestroy(e);
         for (cudaEvent_t e : ev_in) cudaEventDestroy(e);
         for (cudaEvent_t e : ring)
@@ -1145,7 +1190,8 @@ struct SproutBatch {
         }
         join(k);
         if (second.v.ns > 0) {
-            for (SproutSim* sim : second.members) launch_viscosity(sim->d, sim->cfg, main, 1);
+            if (vis_ok) launch_viscosity_batch(vis, vis_sweeps, vis_blocks, main);
+            else for (SproutSim* sim : second.members) launch_viscosity(sim->d, sim->cfg, main, 1);
             fork(k);
             for (size_t s = 0; s < second.members.size(); s++) launch_second_projection_rhs(second.members[s]->d, workers[s % kWorkers]);
             join(k);
@@ -1204,6 +1250,7 @@ struct SproutBatch {
         if (rc != SPROUT_OK) return rc;
         if ((rc = build_view(first, sims)) != SPROUT_OK) return rc;
         if ((rc = build_view(second, twice)) != SPROUT_OK) return rc;
+        if ((rc = build_visc_view()) != SPROUT_OK) return rc;
         CUDA_TRY(cudaStreamSynchronize(main));
         graph_members = sims;
         CUDA_TRY(cudaStreamBeginCapture(main, cudaStreamCaptureModeThreadLocal));
@@ -1262,6 +1309,7 @@ struct SproutBatch {
         if (rc != SPROUT_OK) return rc;
         if ((rc = build_view(first, ms)) != SPROUT_OK) return rc;
         if ((rc = build_view(second, twice)) != SPROUT_OK) return rc;
+        if ((rc = build_visc_view()) != SPROUT_OK) return rc;
         graph_ok = false;   // the views no longer hold the graph's tanks
         record_substep(true);
         CUDA_TRY(cudaGetLastError());

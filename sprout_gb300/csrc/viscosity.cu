@@ -514,70 +514,72 @@ struct VSolve {
         }
     }
 
-    // visc_strain.comp: the weighted strain of the current velocities in the active tiles
-    DEV void strain() const {
+    // visc_strain.comp on level-0 tile tt (if active): the weighted strain of the current
+    // velocities
+    DEV void strain_tile(int tt) const {
+        if (d.tiles[tt] == 0u) return;
         const Lv L0 = lev(d.lv, 0);
-        const int T = n;
         const int W = d.W;
-        for (int tt = blockIdx.x; tt < T; tt += gridDim.x) {
-            if (d.tiles[tt] == 0u) continue;
-            const int2 og = tile_origin(L0, tt);
-            const int cx = og.x + (threadIdx.x & 15), cy = og.y + (threadIdx.x >> 4);
-            if (!in_grid(d, cx, cy)) continue;
-            const int i = cy * W + cx;
-            const float4 w4 = d.vw[i];
-            float4 o = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-            auto vu = [&](int j) { float4 v = d.vel[j]; return face_live(v.z) ? v.x : 0.0f; };
-            auto vv = [&](int j) { float4 v = d.vel[j]; return face_live(v.w) ? v.y : 0.0f; };
-            if (w4.x > 0.0f) {
-                o.x = w4.x * (vu(i + 1) - vu(i));
-                o.y = w4.x * (vv(i + W) - vv(i));
-            }
-            if (w4.y > 0.0f) {
-                float ua = vu(i), ub = vu(i - W), va = vv(i), vb = vv(i - 1);
-                if (v_closed_u(d, i) && v_live_u(d, i - W)) ua = -ub;
-                if (v_closed_u(d, i - W) && v_live_u(d, i)) ub = -ua;
-                if (v_closed_v(d, i) && v_live_v(d, i - 1)) va = -vb;
-                if (v_closed_v(d, i - 1) && v_live_v(d, i)) vb = -va;
-                o.z = w4.y * 0.5f * ((ua - ub) + (va - vb));
-            }
-            d.vs[i] = o;
+        const int2 og = tile_origin(L0, tt);
+        const int cx = og.x + (threadIdx.x & 15), cy = og.y + (threadIdx.x >> 4);
+        if (!in_grid(d, cx, cy)) return;
+        const int i = cy * W + cx;
+        const float4 w4 = d.vw[i];
+        float4 o = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        auto vu = [&](int j) { float4 v = d.vel[j]; return face_live(v.z) ? v.x : 0.0f; };
+        auto vv = [&](int j) { float4 v = d.vel[j]; return face_live(v.w) ? v.y : 0.0f; };
+        if (w4.x > 0.0f) {
+            o.x = w4.x * (vu(i + 1) - vu(i));
+            o.y = w4.x * (vv(i + W) - vv(i));
         }
+        if (w4.y > 0.0f) {
+            float ua = vu(i), ub = vu(i - W), va = vv(i), vb = vv(i - 1);
+            if (v_closed_u(d, i) && v_live_u(d, i - W)) ua = -ub;
+            if (v_closed_u(d, i - W) && v_live_u(d, i)) ub = -ua;
+            if (v_closed_v(d, i) && v_live_v(d, i - 1)) va = -vb;
+            if (v_closed_v(d, i - 1) && v_live_v(d, i)) vb = -va;
+            o.z = w4.y * 0.5f * ((ua - ub) + (va - vb));
+        }
+        d.vs[i] = o;
+    }
+    DEV void strain() const {
+        for (int tt = blockIdx.x; tt < n; tt += gridDim.x) strain_tile(tt);
     }
 
-    // visc_apply.comp mode 0 over every level-0 tile: r = -G^T W G u*, z = r / diag in the
-    // active ones, zero partials (both halves) in the others.
-    DEV void start() const {
-        const Lv L0 = lev(d.lv, 0);
-        for (int tt = blockIdx.x; tt < n; tt += gridDim.x) {
-            if (d.tiles[tt] == 0u) {
-                if (threadIdx.x == 0) {
-                    d.partials[tt] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-                    d.partials[n + tt] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-                }
-                continue;
+    // visc_apply.comp mode 0 on level-0 tile tt: r = -G^T W G u*, z = r / diag in an active
+    // tile, zero partials (both halves) in the others.
+    DEV void start_tile(int tt) const {
+        if (d.tiles[tt] == 0u) {
+            if (threadIdx.x == 0) {
+                d.partials[tt] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                d.partials[n + tt] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
             }
-            const int2 og = tile_origin(L0, tt);
-            const int cx = og.x + (threadIdx.x & 15), cy = og.y + (threadIdx.x >> 4);
-            float4 acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-            if (in_grid(d, cx, cy)) {
-                const int i = cy * d.W + cx;
-                if (interior(d, cx, cy)) {
-                    const float2 g = gts_vs(d, i);
-                    const float lu = v_live_u(d, i) ? 1.0f : 0.0f, lv = v_live_v(d, i) ? 1.0f : 0.0f;
-                    const float4 w4 = d.vw[i];
-                    const float2 r = f2(-g.x * lu, -g.y * lv);
-                    const float2 z = f2(r.x / w4.z, r.y / w4.w);
-                    d.vr[i] = r;
-                    d.vp[i] = z;
-                    acc = make_float4(dot2(r, z), dot2(r, r), 0.0f, 0.0f);
-                } else {
-                    d.vr[i] = f2(0.0f, 0.0f);
-                    d.vp[i] = f2(0.0f, 0.0f);
-                }
-            }
-            tile_sum(acc, 0, (uint32_t)tt);
+            return;
         }
+        const Lv L0 = lev(d.lv, 0);
+        const int2 og = tile_origin(L0, tt);
+        const int cx = og.x + (threadIdx.x & 15), cy = og.y + (threadIdx.x >> 4);
+        float4 acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if (in_grid(d, cx, cy)) {
+            const int i = cy * d.W + cx;
+            if (interior(d, cx, cy)) {
+                const float2 g = gts_vs(d, i);
+                const float lu = v_live_u(d, i) ? 1.0f : 0.0f, lv = v_live_v(d, i) ? 1.0f : 0.0f;
+                const float4 w4 = d.vw[i];
+                const float2 r = f2(-g.x * lu, -g.y * lv);
+                const float2 z = f2(r.x / w4.z, r.y / w4.w);
+                d.vr[i] = r;
+                d.vp[i] = z;
+                acc = make_float4(dot2(r, z), dot2(r, r), 0.0f, 0.0f);
+            } else {
+                d.vr[i] = f2(0.0f, 0.0f);
+                d.vp[i] = f2(0.0f, 0.0f);
+            }
+        }
+        tile_sum(acc, 0, (uint32_t)tt);
+    }
+    DEV void start() const {
+        for (int tt = blockIdx.x; tt < n; tt += gridDim.x) start_tile(tt);
     }
 
     // visc_iter.comp WARM at one interior cell: the step d of the warm start
@@ -606,10 +608,11 @@ struct VSolve {
         }
         return o;
     }
-    DEV void warm(int half) const {
+    // visc_iter.comp WARM on active level-0 tile tt
+    DEV void warm_tile(uint32_t tt, int half) const {
         const Lv L0 = lev(d.lv, 0);
         const int W = d.W;
-        each(0, [&](uint32_t tt) {
+        {
             const int2 og = tile_origin(L0, (int)tt);
             const int cx = og.x + (threadIdx.x & 15), cy = og.y + (threadIdx.x >> 4);
             float4 acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
@@ -641,7 +644,10 @@ struct VSolve {
                 acc = make_float4(dot2(r, z), dot2(r, r), 0.0f, 0.0f);
             }
             tile_sum(acc, half, tt);
-        });
+        }
+    }
+    DEV void warm(int half) const {
+        each(0, [&](uint32_t tt) { warm_tile(tt, half); });
     }
 
     // For every active tile of level l in this block's share, through the pipeline of two
@@ -663,120 +669,131 @@ struct VSolve {
         return Region<NU, RH>{g, s.sx, s, og.x, og.y};
     }
 
-    // vmg_down.comp on level l (l = 0 at the start of a solve, right-hand side vr)
+    // vmg_down.comp on tile tt of level l (l = 0 at the start of a solve, right-hand side rhs0)
+    DEV void down_stage(uint32_t tt, VStage<NU>& g, int l, const float2* rhs0) const {
+        const Lv L = lev(d.lv, l);
+        region<VCfg<NU>::HALO>(g, L, tt).stage(d, L, l == 0 ? rhs0 : d.vmr, nullptr, nullptr, nullptr);
+    }
+    DEV void down_finish(uint32_t tt, VStage<NU>& g, int l, int nlev) const {
+        const Lv L = lev(d.lv, l), LC = lev(d.lv, l + 1);
+        region<VCfg<NU>::HALO>(g, L, tt).way_down(d, L, l == nlev ? nullptr : &LC, [](int) {});
+    }
     DEV void down(int l, int nlev, const float2* rhs0) const {
-        const Lv L = lev(d.lv, l);
-        const Lv LC = lev(d.lv, l + 1);
-        const float2* rhs = l == 0 ? rhs0 : d.vmr;
         pipe(
-            l, [&](uint32_t tt, VStage<NU>& g) { region<VCfg<NU>::HALO>(g, L, tt).stage(d, L, rhs, nullptr, nullptr, nullptr); },
-            [&](uint32_t tt, VStage<NU>& g) {
-                region<VCfg<NU>::HALO>(g, L, tt).way_down(d, L, l == nlev ? nullptr : &LC, [](int) {});
-            });
+            l, [&](uint32_t tt, VStage<NU>& g) { down_stage(tt, g, l, rhs0); },
+            [&](uint32_t tt, VStage<NU>& g) { down_finish(tt, g, l, nlev); });
     }
 
-    // vmg_up.comp on a coarse level l: the finished values to vmz
-    DEV void up(int l, int nlev) const {
-        const Lv L = lev(d.lv, l);
-        const Lv LC = lev(d.lv, l + 1);
+    // vmg_up.comp on tile tt of a coarse level l: the finished values to vmz
+    DEV void up_stage(uint32_t tt, VStage<NU>& g, int l, int nlev) const {
+        const Lv L = lev(d.lv, l), LC = lev(d.lv, l + 1);
         const bool coarse = l != nlev;
+        region<VCfg<NU>::HALO>(g, L, tt).stage(d, L, d.vmr, d.vmx, coarse ? d.vmz : nullptr, coarse ? &LC : nullptr);
+    }
+    DEV void up_finish(uint32_t tt, VStage<NU>& g, int l, int nlev) const {
+        const Lv L = lev(d.lv, l);
+        const Region<NU, VCfg<NU>::HALO> R = region<VCfg<NU>::HALO>(g, L, tt);
+        R.way_up(l != nlev);
+        const int t = threadIdx.x;
+        const int cx = R.ox + (t & 15), cy = R.oy + (t >> 4);
+        if (l_inside(L, cx, cy)) d.vmz[l_at(L, cx, cy)] = s.sx[R.tile_slot(t)];
+        __syncthreads();
+    }
+    DEV void up(int l, int nlev) const {
         pipe(
-            l,
-            [&](uint32_t tt, VStage<NU>& g) {
-                region<VCfg<NU>::HALO>(g, L, tt).stage(d, L, d.vmr, d.vmx, coarse ? d.vmz : nullptr, coarse ? &LC : nullptr);
-            },
-            [&](uint32_t tt, VStage<NU>& g) {
-                const Region<NU, VCfg<NU>::HALO> R = region<VCfg<NU>::HALO>(g, L, tt);
-                R.way_up(coarse);
-                const int t = threadIdx.x;
-                const int cx = R.ox + (t & 15), cy = R.oy + (t >> 4);
-                if (l_inside(L, cx, cy)) d.vmz[l_at(L, cx, cy)] = s.sx[R.tile_slot(t)];
-                __syncthreads();
-            });
+            l, [&](uint32_t tt, VStage<NU>& g) { up_stage(tt, g, l, nlev); },
+            [&](uint32_t tt, VStage<NU>& g) { up_finish(tt, g, l, nlev); });
     }
 
-    // visc_mgz.comp: the way up on level 0 with A z and the partial sums of r.z, z.A z, z.q
+    // visc_mgz.comp on level-0 tile tt: the way up with A z and the partial sums of r.z, z.A z,
+    // z.q
+    DEV void mgz_stage(uint32_t tt, VStage<NU>& g, const float2* rn) const {
+        const Lv L = lev(d.lv, 0), LC = lev(d.lv, 1);
+        region<VCfg<NU>::HALO + 1>(g, L, tt).stage(d, L, rn, d.vmx, d.vmz, &LC);
+    }
+    DEV void mgz_finish(uint32_t tt, VStage<NU>& g, const float2* qn, int half) const {
+        const Lv L = lev(d.lv, 0);
+        const Region<NU, VCfg<NU>::HALO + 1> R = region<VCfg<NU>::HALO + 1>(g, L, tt);
+        const int t = threadIdx.x;
+        const int cx = R.ox + (t & 15), cy = R.oy + (t >> 4);
+        const bool in = l_inside(L, cx, cy);
+        const float2 qi = in ? qn[l_at(L, cx, cy)] : f2(0.0f, 0.0f);   // (in flight meanwhile)
+        R.way_up(true);
+        const int k = R.tile_slot(t);
+        float4 acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if (in) {
+            const int i = l_at(L, cx, cy);
+            const float2 z = s.sx[k], dd = g.sd[k];
+            const float2 o = R.offd(k);
+            const float2 az = f2(dd.x * z.x + o.x, dd.y * z.y + o.y);
+            d.vmz[i] = z;
+            d.vaz[i] = az;
+            acc = make_float4(dot2(g.sr[k], z), dot2(z, az), dot2(z, qi), 0.0f);
+        }
+        tile_sum(acc, half, tt);
+    }
     DEV void mgz(const float2* rn, const float2* qn, int half) const {
-        const Lv L = lev(d.lv, 0);
-        const Lv LC = lev(d.lv, 1);
-        constexpr int RH = VCfg<NU>::HALO + 1;
         pipe(
-            0, [&](uint32_t tt, VStage<NU>& g) { region<RH>(g, L, tt).stage(d, L, rn, d.vmx, d.vmz, &LC); },
-            [&](uint32_t tt, VStage<NU>& g) {
-                const Region<NU, RH> R = region<RH>(g, L, tt);
-                const int t = threadIdx.x;
-                const int cx = R.ox + (t & 15), cy = R.oy + (t >> 4);
-                const bool in = l_inside(L, cx, cy);
-                const float2 qi = in ? qn[l_at(L, cx, cy)] : f2(0.0f, 0.0f);   // (in flight meanwhile)
-                R.way_up(true);
-                const int k = R.tile_slot(t);
-                float4 acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-                if (in) {
-                    const int i = l_at(L, cx, cy);
-                    const float2 z = s.sx[k], dd = g.sd[k];
-                    const float2 o = R.offd(k);
-                    const float2 az = f2(dd.x * z.x + o.x, dd.y * z.y + o.y);
-                    d.vmz[i] = z;
-                    d.vaz[i] = az;
-                    acc = make_float4(dot2(g.sr[k], z), dot2(z, az), dot2(z, qi), 0.0f);
-                }
-                tile_sum(acc, half, tt);
-            });
+            0, [&](uint32_t tt, VStage<NU>& g) { mgz_stage(tt, g, rn); },
+            [&](uint32_t tt, VStage<NU>& g) { mgz_finish(tt, g, qn, half); });
     }
 
-    // visc_mgu.comp: p, q, x, r of the iteration and the way down on level 0 from the new r.
-    // Copies: A z (e1), the old q (e2, unless beta is zero) and the old r (sr) over the region;
-    // each slot's new r = r - alpha q, q = A z + beta q_old, made final in place.
-    DEV void mgu(const float2* ro, const float2* qo, float2* rn, float2* qn, int half) const {
+    // visc_mgu.comp on level-0 tile tt: p, q, x, r of the iteration and the way down from the
+    // new r. Copies: A z (e1), the old q (e2, unless beta is zero) and the old r (sr) over the
+    // region; each slot's new r = r - alpha q, q = A z + beta q_old, made final in place.
+    DEV void mgu_stage(uint32_t tt, VStage<NU>& g, const float2* ro, const float2* qo) const {
         const Lv L = lev(d.lv, 0);
-        const Lv LC = lev(d.lv, 1);
+        region<VCfg<NU>::HALO>(g, L, tt).stage(d, L, ro, d.vaz, K.beta != 0.0f ? qo : nullptr, nullptr);
+    }
+    DEV void mgu_finish(uint32_t tt, VStage<NU>& g, float2* rn, float2* qn, int half) const {
+        const Lv L = lev(d.lv, 0), LC = lev(d.lv, 1);
         const float a = K.alpha, b = K.beta;
-        constexpr int RH = VCfg<NU>::HALO;
-        auto new_q = [&](const VStage<NU>& g, int k) {
+        auto new_q = [&](int k) {
             const float2 sq = g.e1[k];
             if (b == 0.0f) return sq;
             const float2 q = g.e2[k];
             return f2(sq.x + b * q.x, sq.y + b * q.y);
         };
+        const Region<NU, VCfg<NU>::HALO> R = region<VCfg<NU>::HALO>(g, L, tt);
+        const int t = threadIdx.x;
+        const int cx = R.ox + (t & 15), cy = R.oy + (t >> 4);
+        const bool own = cx < d.W && cy < d.H;
+        const int i = own ? cy * d.W + cx : 0;
+        const bool inner = own && interior(d, cx, cy);
+        // this cell's z, p_old, velocity and step, in flight while the region is made final
+        const float2 z = own ? d.vmz[i] : f2(0.0f, 0.0f);
+        const float2 po = (own && b != 0.0f) ? d.vp[i] : f2(0.0f, 0.0f);
+        float4 v = inner ? d.vel[i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        const float2 dv = inner ? d.vd[i] : f2(0.0f, 0.0f);
+        const int ks = R.tile_slot(t);
+        R.way_down(d, L, &LC, [&](int k) {
+            const float2 q = new_q(k);
+            const float2 r0 = g.sr[k];
+            g.sr[k] = f2(r0.x - a * q.x, r0.y - a * q.y);
+        });
+        float4 acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if (own) {
+            float2 p = z;
+            if (b != 0.0f) p = f2(z.x + b * po.x, z.y + b * po.y);
+            const float2 q = new_q(ks);
+            const float2 r = g.sr[ks];
+            if (inner) {
+                if (face_live(v.z)) v.x += a * p.x;
+                if (face_live(v.w)) v.y += a * p.y;
+                store_vel_xy(d, i, v.x, v.y);
+                d.vd[i] = f2(dv.x + a * p.x, dv.y + a * p.y);
+            }
+            d.vp[i] = p;
+            qn[i] = q;
+            rn[i] = r;
+            acc = make_float4(0.0f, dot2(r, r), dot2(p, q), 0.0f);
+        }
+        tile_sum(acc, half, tt);
+    }
+    DEV void mgu(const float2* ro, const float2* qo, float2* rn, float2* qn, int half) const {
         pipe(
-            0, [&](uint32_t tt, VStage<NU>& g) { region<RH>(g, L, tt).stage(d, L, ro, d.vaz, b != 0.0f ? qo : nullptr, nullptr); },
-            [&](uint32_t tt, VStage<NU>& g) {
-                const Region<NU, RH> R = region<RH>(g, L, tt);
-                const int t = threadIdx.x;
-                const int cx = R.ox + (t & 15), cy = R.oy + (t >> 4);
-                const bool own = cx < d.W && cy < d.H;
-                const int i = own ? cy * d.W + cx : 0;
-                const bool inner = own && interior(d, cx, cy);
-                // this cell's z, p_old, velocity and step, in flight while the region is made final
-                const float2 z = own ? d.vmz[i] : f2(0.0f, 0.0f);
-                const float2 po = (own && b != 0.0f) ? d.vp[i] : f2(0.0f, 0.0f);
-                float4 v = inner ? d.vel[i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-                const float2 dv = inner ? d.vd[i] : f2(0.0f, 0.0f);
-                const int ks = R.tile_slot(t);
-                R.way_down(d, L, &LC, [&](int k) {
-                    const float2 q = new_q(g, k);
-                    const float2 r0 = g.sr[k];
-                    g.sr[k] = f2(r0.x - a * q.x, r0.y - a * q.y);
-                });
-                float4 acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-                if (own) {
-                    float2 p = z;
-                    if (b != 0.0f) p = f2(z.x + b * po.x, z.y + b * po.y);
-                    const float2 q = new_q(g, ks);
-                    const float2 r = g.sr[ks];
-                    if (inner) {
-                        if (face_live(v.z)) v.x += a * p.x;
-                        if (face_live(v.w)) v.y += a * p.y;
-                        store_vel_xy(d, i, v.x, v.y);
-                        d.vd[i] = f2(dv.x + a * p.x, dv.y + a * p.y);
-                    }
-                    d.vp[i] = p;
-                    qn[i] = q;
-                    rn[i] = r;
-                    acc = make_float4(0.0f, dot2(r, r), dot2(p, q), 0.0f);
-                }
-                tile_sum(acc, half, tt);
-            });
+            0, [&](uint32_t tt, VStage<NU>& g) { mgu_stage(tt, g, ro, qo); },
+            [&](uint32_t tt, VStage<NU>& g) { mgu_finish(tt, g, rn, qn, half); });
     }
 
     // record_visc_coarse (mod.rs:2838-2853): the coarse levels down, then up
@@ -914,6 +931,278 @@ __global__ void __launch_bounds__(NT, 2) k_visc_solve(DevScene d, int restrain) 
     trace_launch_done(d.K);
 }
 
+// ---- many tanks' viscosity solves in one persistent solve -----------------------------------
+//
+// The same solve for a batch of tanks in one cooperative launch, over flattened (tank, tile)
+// work lists per level, as k_mgpcg_batch does for the pressure: every tile goes through the
+// same tile bodies as above and every tank's scalars through the same steps (reduce_tail
+// modes 4, 10-13, 7), summed by one block over the tank's own partials in the same order; so a
+// tank's result is the same alone and in any batch, to the bit. The differences: each
+// reduction is a phase of its own followed by a barrier (the scalars live in global memory),
+// and a tank whose solve has converged (or reached its iteration limit) drops out of the
+// work lists.
+
+namespace {
+
+// per tank: its scalars, which half of the partials the next reduction reads, whether it
+// takes part in the rest of the current iteration
+struct VBatchScene {
+    VScal K;
+    int half, run2, pad0, pad1;
+};
+
+DEV int vscene_of(const int* o, int ns, int g) {
+    int lo = 0, hi = ns;
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (o[mid] <= g) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// work item g of level l's active tiles over the tanks: the tank in the high 16 bits
+DEV uint32_t vbatch_item(const VBatchView& B, int l, int g) {
+    const int* o = B.aoff + l * (B.ns + 1);
+    const int s = vscene_of(o, B.ns, g);
+    const DevScene& d = B.scenes[s];
+    return ((uint32_t)s << 16) | d.vlist[d.lv.toff[l] + (g - o[s])];
+}
+
+DEV void vbatch_fill_cache(const VBatchView& B, VTileCache& tc) {
+    for (int l = 0; l < kVCacheLevels && l <= B.max_lev; l++) {
+        const int N = *(volatile const int*)&B.aoff[l * (B.ns + 1) + B.ns];
+        if (threadIdx.x == 0) tc.cnt[l] = (uint32_t)N;
+        for (int k = threadIdx.x; k < kVCachePer; k += NT) {
+            const int g = blockIdx.x + k * gridDim.x;
+            if (g < N) tc.item[l][k] = vbatch_item(B, l, g);
+        }
+    }
+    __syncthreads();
+}
+
+}  // namespace
+
+template <int NU>
+__global__ void __launch_bounds__(NT, 2) k_visc_batch(VBatchView B) {
+    __shared__ VSmem<NU> sm;
+    __shared__ VTileCache tc;
+    __shared__ int s_run;
+    VBatchScene* S = reinterpret_cast<VBatchScene*>(B.scal);
+    SolveState* BK = B.K;
+    const int ns = B.ns;
+    auto V = [&](int s) { return VSolve<NU>{B.scenes[s], sm, S[s].K, B.scenes[s].nwg, tc}; };
+    auto nlev = [&](int s) { return B.scenes[s].P->visc_levels; };
+    // every level-0 tile of every tank
+    auto for_all0 = [&](auto&& f) {
+        const int N = B.off0[ns];
+        for (int g = blockIdx.x; g < N; g += gridDim.x) {
+            const int s = vscene_of(B.off0, ns, g);
+            f(s, g - B.off0[s]);
+        }
+    };
+    // this block's share of level l's active tiles over the tanks, plain or through the pipeline
+    auto count = [&](int l) {
+        return l < kVCacheLevels ? tc.cnt[l] : (uint32_t)*(volatile const int*)&B.aoff[l * (ns + 1) + ns];
+    };
+    auto item = [&](int l, int k) {
+        return (l < kVCacheLevels && k < kVCachePer) ? tc.item[l][k]
+                                                      : vbatch_item(B, l, (int)(blockIdx.x + (uint32_t)k * gridDim.x));
+    };
+    auto for_active = [&](int l, auto&& f) {
+        const uint32_t N = count(l);
+        int k = 0;
+        for (uint32_t g = blockIdx.x; g < N; g += gridDim.x, k++) {
+            const uint32_t it = item(l, k);
+            f((int)(it >> 16), it & 0xffffu);
+        }
+    };
+    auto pipe = [&](int l, auto&& stage, auto&& finish) {
+        pipeline<2>(
+            count(l), [&](int k) { return item(l, k); },
+            [&](uint32_t it, int b) { stage((int)(it >> 16), it & 0xffffu, sm.st[b]); },
+            [&](uint32_t it, int b) { finish((int)(it >> 16), it & 0xffffu, sm.st[b]); });
+    };
+    // one V-cycle's coarse levels for the tanks run(s) says
+    auto coarse = [&](auto&& run) -> bool {
+        for (int l = 1; l <= B.max_lev; l++) {
+            pipe(
+                l, [&](int s, uint32_t tt, VStage<NU>& g) { if (l <= nlev(s) && run(s)) V(s).down_stage(tt, g, l, nullptr); },
+                [&](int s, uint32_t tt, VStage<NU>& g) { if (l <= nlev(s) && run(s)) V(s).down_finish(tt, g, l, nlev(s)); });
+            if (!grid_sync(BK)) return false;
+        }
+        for (int l = B.max_lev; l >= 1; l--) {
+            pipe(
+                l, [&](int s, uint32_t tt, VStage<NU>& g) { if (l <= nlev(s) && run(s)) V(s).up_stage(tt, g, l, nlev(s)); },
+                [&](int s, uint32_t tt, VStage<NU>& g) { if (l <= nlev(s) && run(s)) V(s).up_finish(tt, g, l, nlev(s)); });
+            if (!grid_sync(BK)) return false;
+        }
+        return true;
+    };
+    auto mgz = [&](auto&& run, int par) {
+        pipe(
+            0, [&](int s, uint32_t tt, VStage<NU>& g) {
+                if (run(s)) V(s).mgz_stage(tt, g, (par & 1) ? B.scenes[s].vr2 : B.scenes[s].vr); },
+            [&](int s, uint32_t tt, VStage<NU>& g) {
+                if (run(s)) V(s).mgz_finish(tt, g, (par & 1) ? B.scenes[s].vq2 : B.scenes[s].vq, S[s].half); });
+    };
+
+    // the lists (one block per tank) and the strain of u* (every tank takes it again)
+    for (int s = blockIdx.x; s < ns; s += gridDim.x) V(s).build_lists(nlev(s));
+    for_all0([&](int s, int tt) { V(s).strain_tile(tt); });
+    if (!grid_sync(BK)) return;
+    // the prefix sums of the active tiles per level over the tanks, and the start
+    if (blockIdx.x == 0) {
+        for (int l = threadIdx.x; l <= B.max_lev; l += NT) {
+            int* o = B.aoff + l * (ns + 1);
+            int a = 0;
+            o[0] = 0;
+            for (int k = 0; k < ns; k++) {
+                a += l <= nlev(k) ? (int)B.scenes[k].vcount[l] : 0;
+                o[k + 1] = a;
+            }
+        }
+    }
+    for_all0([&](int s, int tt) { V(s).start_tile(tt); });
+    if (!grid_sync(BK)) return;
+    vbatch_fill_cache(B, tc);
+    for (int s = blockIdx.x; s < ns; s += gridDim.x) {   // cg_reduce mode 4
+        const float4 a = V(s).sum(0);
+        if (threadIdx.x == 0) {
+            VScal& K = S[s].K;
+            K.rz = a.x;
+            K.r0 = a.y;
+            K.rr = a.y;
+            K.beta = 0.0f;
+            K.alpha = 0.0f;
+            K.pq = 0.0f;
+            K.iters = 0u;
+            K.done = (a.y <= 1e-30f || a.x <= 0.0f) ? 1u : 0u;
+            S[s].half = 1;
+        }
+        __syncthreads();
+    }
+    if (!grid_sync(BK)) return;
+    // the warm start, for the tanks that take it and have not converged
+    auto warm_on = [&](int s) { return B.scenes[s].P->viscosity_warm != 0 && S[s].K.done == 0u; };
+    for_active(0, [&](int s, uint32_t tt) { if (warm_on(s)) V(s).warm_tile(tt, S[s].half); });
+    if (!grid_sync(BK)) return;
+    for (int s = blockIdx.x; s < ns; s += gridDim.x) {   // mode 10
+        if (!warm_on(s)) continue;
+        const float4 a = V(s).sum(S[s].half);
+        if (threadIdx.x == 0) {
+            VScal& K = S[s].K;
+            const float tz = B.scenes[s].P->tol[2];
+            K.rz = a.x;
+            K.rr = a.y;
+            K.beta = 0.0f;
+            K.done = (a.y <= tz * tz * K.r0 || a.x <= 0.0f) ? 1u : 0u;
+            S[s].half ^= 1;
+        }
+        __syncthreads();
+    }
+    if (!grid_sync(BK)) return;
+    // the first V-cycle of the tanks not converged
+    {
+        auto run = [&](int s) { return S[s].K.done == 0u; };
+        pipe(
+            0, [&](int s, uint32_t tt, VStage<NU>& g) { if (run(s)) V(s).down_stage(tt, g, 0, B.scenes[s].vr); },
+            [&](int s, uint32_t tt, VStage<NU>& g) { if (run(s)) V(s).down_finish(tt, g, 0, nlev(s)); });
+        if (!grid_sync(BK)) return;
+        if (!coarse(run)) return;
+        mgz(run, 0);
+        if (!grid_sync(BK)) return;
+        for (int s = blockIdx.x; s < ns; s += gridDim.x) {   // mode 11
+            if (!run(s)) continue;
+            const float4 a = V(s).sum(S[s].half);
+            if (threadIdx.x == 0) {
+                VScal& K = S[s].K;
+                K.rz = a.x;
+                K.beta = 0.0f;
+                K.pq = a.y;
+                K.alpha = a.y > 0.0f ? a.x / a.y : 0.0f;
+                if (a.x <= 0.0f || a.y <= 0.0f) K.done = 1u;
+                S[s].half ^= 1;
+            }
+            __syncthreads();
+        }
+        if (!grid_sync(BK)) return;
+    }
+    for (uint32_t k = 0;; k++) {
+        auto running = [&](int s) { return S[s].K.done == 0u && k < B.scenes[s].P->viscosity_max_iters; };
+        if (threadIdx.x == 0) {
+            int r = 0;
+            for (int s = 0; s < ns && !r; s++) r = running(s) ? 1 : 0;
+            s_run = r;
+        }
+        __syncthreads();
+        if (!s_run) break;
+        const int par = (int)(k & 1u);
+        pipe(
+            0, [&](int s, uint32_t tt, VStage<NU>& g) {
+                const DevScene& d = B.scenes[s];
+                if (running(s)) V(s).mgu_stage(tt, g, par ? d.vr2 : d.vr, par ? d.vq2 : d.vq); },
+            [&](int s, uint32_t tt, VStage<NU>& g) {
+                const DevScene& d = B.scenes[s];
+                if (running(s)) V(s).mgu_finish(tt, g, par ? d.vr : d.vr2, par ? d.vq : d.vq2, S[s].half); });
+        if (!grid_sync(BK)) return;
+        for (int s = blockIdx.x; s < ns; s += gridDim.x) {   // mode 12
+            const bool was_running = running(s);
+            if (was_running) {
+                const float4 a = V(s).sum(S[s].half);
+                if (threadIdx.x == 0) {
+                    VScal& K = S[s].K;
+                    const float tz = B.scenes[s].P->tol[2];
+                    const uint32_t was = K.done;
+                    K.iters += 1u - was;
+                    const uint32_t now = a.y <= tz * tz * K.r0 ? 1u : 0u;
+                    if (was == 0u) K.rr = a.y;
+                    K.pq = a.z;
+                    K.done = was > now ? was : now;
+                    S[s].half ^= 1;
+                }
+            }
+            if (threadIdx.x == 0) S[s].run2 = (was_running && S[s].K.done == 0u) ? 1 : 0;
+            __syncthreads();
+        }
+        if (!grid_sync(BK)) return;
+        auto run2 = [&](int s) { return S[s].run2 != 0; };
+        if (!coarse(run2)) return;
+        mgz(run2, par ^ 1);
+        if (!grid_sync(BK)) return;
+        for (int s = blockIdx.x; s < ns; s += gridDim.x) {   // mode 13
+            if (!run2(s)) continue;
+            const float4 a = V(s).sum(S[s].half);
+            if (threadIdx.x == 0) {
+                VScal& K = S[s].K;
+                const float beta = (K.done == 0u && K.rz > 0.0f) ? a.x / K.rz : 0.0f;
+                const float pq = a.y + 2.0f * beta * a.z + beta * beta * K.pq;
+                K.beta = beta;
+                K.alpha = (K.done == 0u && pq > 0.0f) ? a.x / pq : 0.0f;
+                K.rz = a.x;
+                S[s].half ^= 1;
+            }
+            __syncthreads();
+        }
+        if (!grid_sync(BK)) return;
+    }
+    for (int s = blockIdx.x; s < ns; s += gridDim.x) {   // mode 7
+        if (threadIdx.x == 0) {
+            const VScal& K = S[s].K;
+            SolveState* G = B.scenes[s].K;
+            if (K.iters > G->v_it_max) G->v_it_max = K.iters;
+            if (K.done == 0u) G->v_unconv += 1u;
+            const float rel = K.r0 > 0.0f ? sqrtf(K.rr / K.r0) : 0.0f;
+            G->v_res_max = maxf(G->v_res_max, rel);
+            G->v_iters = K.iters;
+            G->v_done = K.done;
+            G->v_rr = K.rr;
+            G->v_r0 = K.r0;
+        }
+    }
+    trace_launch_done(BK);
+}
+
 namespace {
 
 // rhs_visc.comp
@@ -975,6 +1264,15 @@ int visc_blocks_max_nu(int device) {
 }
 
 }  // namespace
+
+size_t viscosity_batch_scalar_bytes() { return sizeof(VBatchScene); }
+
+cudaError_t launch_viscosity_batch(const VBatchView& B, int sweeps, int blocks, cudaStream_t st) {
+    cudaMemsetAsync(&B.K->bar_count, 0, sizeof(uint32_t), st);
+    void* args[] = {(void*)&B};
+    const void* fn = sweeps >= 2 ? (const void*)k_visc_batch<2> : (const void*)k_visc_batch<1>;
+    return cudaLaunchCooperativeKernel(fn, dim3(blocks), dim3(NT), args, 0, st);
+}
 
 int viscosity_blocks_max(int device, int sweeps) {
     return sweeps >= 2 ? visc_blocks_max_nu<2>(device) : visc_blocks_max_nu<1>(device);
