@@ -3407,6 +3407,133 @@ static void mgu_new_r(OSim* s, const V2* Rold, const V2* Qold, V2* out) {
     }
 }
 
+/* visc_iter.comp (not WARM), the Jacobi-preconditioned iteration (viscosity_precond 0): the
+ * direction p = z + beta p_old (z = r / diag) at every interior cell, its weighted strain, and
+ * per cell of an active tile q = M p + G^T s into vq, p into Pnew; partial sums of p.q */
+typedef struct JacCtx {
+    const V2* P;   /* the new direction at every cell */
+    const V4* S;   /* its weighted strain at every cell */
+    V2* Pnew;
+} JacCtx;
+static inline float jU(const JacCtx* c, const OSim* s, int x, int y, int i) {
+    return live_u(s, i) ? c->P[cidx(s, x, y)].x : 0.0f;
+}
+static inline float jV(const JacCtx* c, const OSim* s, int x, int y, int i) {
+    return live_v(s, i) ? c->P[cidx(s, x, y)].y : 0.0f;
+}
+static V4 jac_strain(const JacCtx* c, const OSim* s, int cx, int cy) {
+    if (!in_grid_c(s, cx, cy)) return v4(0, 0, 0, 0);
+    int i = cidx(s, cx, cy), W = s->W;
+    V4 o = v4(0, 0, 0, 0);
+    V4 w = s->vw[i];
+    if (w.x > 0.0f) {
+        o.x = w.x * (jU(c, s, cx + 1, cy, i + 1) - jU(c, s, cx, cy, i));
+        o.y = w.x * (jV(c, s, cx, cy + 1, i + W) - jV(c, s, cx, cy, i));
+    }
+    if (w.y > 0.0f) {
+        float ua = jU(c, s, cx, cy, i), ub = jU(c, s, cx, cy - 1, i - W), va = jV(c, s, cx, cy, i), vb = jV(c, s, cx - 1, cy, i - 1);
+        if (closed_u(s, i) && live_u(s, i - W)) ua = -ub;
+        if (closed_u(s, i - W) && live_u(s, i)) ub = -ua;
+        if (closed_v(s, i) && live_v(s, i - 1)) va = -vb;
+        if (closed_v(s, i - 1) && live_v(s, i)) vb = -va;
+        o.z = w.y * 0.5f * ((ua - ub) + (va - vb));
+    }
+    return o;
+}
+static V4 cell_jac_iter(OSim* s, int cx, int cy, void* ctx) {
+    JacCtx* c = (JacCtx*)ctx;
+    if (!in_grid_c(s, cx, cy)) return v4(0, 0, 0, 0);
+    int i = cidx(s, cx, cy), W = s->W;
+    V2 pn = c->P[i];
+    c->Pnew[i] = pn;
+    if (!interior_c(s, cx, cy)) {
+        s->vq[i] = v2(0, 0);
+        return v4(0, 0, 0, 0);
+    }
+    V2 g = v2(0, 0);
+    if (live_u(s, i)) {
+        float c1 = closed_u(s, i - W) ? 1.0f : 0.5f, c2 = closed_u(s, i + W) ? -1.0f : -0.5f;
+        V4 sl = c->S[i - 1], sc = c->S[i], su = c->S[i + W];
+        g.x = sl.x - sc.x + sc.z * c1 + su.z * c2;
+    }
+    if (live_v(s, i)) {
+        float d1 = closed_v(s, i - 1) ? 1.0f : 0.5f, d2 = closed_v(s, i + 1) ? -1.0f : -0.5f;
+        V4 sd = c->S[i - W], sc = c->S[i], sr = c->S[i + 1];
+        g.y = sd.y - sc.y + sc.z * d1 + sr.z * d2;
+    }
+    V2 live = v2(live_u(s, i) ? 1.0f : 0.0f, live_v(s, i) ? 1.0f : 0.0f);
+    V4 cf = s->coef[i];
+    V2 p = v2(pn.x * live.x, pn.y * live.y);
+    V2 q = v2((cf.z * p.x + g.x) * live.x, (cf.w * p.y + g.y) * live.y);
+    s->vq[i] = q;
+    return v4(0.0f, 0.0f, dot2(p, q), 0.0f);
+}
+/* visc_update.comp: u += alpha p, the warm-start step, r -= alpha q; partial sums of r.z, r.r */
+static V4 cell_jac_update(OSim* s, int cx, int cy, void* ctx) {
+    const V2* Pcur = (const V2*)ctx;
+    if (!in_grid_c(s, cx, cy) || !interior_c(s, cx, cy)) return v4(0, 0, 0, 0);
+    int i = cidx(s, cx, cy);
+    float a = s->K.v_alpha;
+    V2 p = Pcur[i];
+    if (live_u(s, i)) s->vel[i].x += a * p.x;
+    if (live_v(s, i)) s->vel[i].y += a * p.y;
+    s->vd[i].x += a * (live_u(s, i) ? p.x : 0.0f);
+    s->vd[i].y += a * (live_v(s, i) ? p.y : 0.0f);
+    V2 r = v2(s->vr[i].x - a * s->vq[i].x, s->vr[i].y - a * s->vq[i].y);
+    s->vr[i] = r;
+    V2 z = v2(r.x / s->vw[i].z, r.y / s->vw[i].w);
+    return v4(dot2(r, z), dot2(r, r), 0.0f, 0.0f);
+}
+/* the Jacobi-preconditioned conjugate gradients (record_viscosity_solve, mod.rs:2909-2921):
+ * per iteration visc_iter + cg_reduce mode 5, visc_update + mode 6. The directions alternate
+ * between vp and vr2 (free without the multigrid) as vp / vp2 swap in the reference. */
+static void viscosity_jacobi(OSim* s) {
+    SolveBuf* K = &s->K;
+    const float tz = P_.tol[2];
+    int n = s->W * s->H;
+    V2* P = (V2*)malloc((size_t)n * sizeof(V2));
+    V4* S = (V4*)malloc((size_t)n * sizeof(V4));
+    V2 *pa = s->vp, *pb = s->vr2;
+    for (uint32_t k = 0; k < s->prm.viscosity_max_iters && !K->v_done; k++) {
+        float b = K->v_beta;
+#pragma omp parallel for schedule(static) num_threads(g_threads)
+        for (int i = 0; i < n; i++) {
+            int cx = i % s->W, cy = i / s->W;
+            V2 p = v2(0, 0);
+            if (interior_c(s, cx, cy)) {
+                V2 z = v2(s->vr[i].x / s->vw[i].z, s->vr[i].y / s->vw[i].w);
+                p = b == 0.0f ? z : v2(z.x + b * pa[i].x, z.y + b * pa[i].y);
+            }
+            P[i] = p;
+        }
+        JacCtx c = {P, S, pb};
+#pragma omp parallel for schedule(static) num_threads(g_threads)
+        for (int i = 0; i < n; i++) S[i] = jac_strain(&c, s, i % s->W, i / s->W);
+        tile_partials(s, s->part, cell_jac_iter, &c);
+        {   /* mode 5 */
+            V4 t = total(s, 0, s->nwg);
+            K->v_alpha = (K->v_done == 0u && t.z > 0.0f) ? K->v_rz / t.z : 0.0f;
+        }
+        tile_partials(s, s->part, cell_jac_update, pb);
+        {   /* mode 6 */
+            V4 t = total(s, 0, s->nwg);
+            uint32_t was = K->v_done;
+            K->v_iters += 1u - was;
+            uint32_t now = t.y <= tz * tz * K->v_r0;
+            uint32_t done = was > now ? was : now;
+            K->v_beta = (done == 0u && K->v_rz > 0.0f) ? t.x / K->v_rz : 0.0f;
+            K->v_rz = t.x;
+            if (was == 0u) K->v_rr = t.y;
+            K->v_done = done;
+        }
+        V2* tmp = pa;
+        pa = pb;
+        pb = tmp;
+    }
+    free(P);
+    free(S);
+}
+
 /* record_viscosity_solve (mod.rs:2867-2923) with the device-decided loop */
 static void viscosity_solve(OSim* s, int restrain) {
     const int nlev = (int)mini(maxi((int)s->prm.viscosity_mg_levels, 1), s->lv.tail);
@@ -3438,6 +3565,10 @@ static void viscosity_solve(OSim* s, int restrain) {
         K->v_rr = a.y;
         K->v_beta = 0.0f;
         K->v_done = (a.y <= tz * tz * K->v_r0 || a.x <= 0.0f) ? 1u : 0u;
+    }
+    if (s->prm.viscosity_precond == 0) {
+        viscosity_jacobi(s);
+        goto stats;
     }
     /* the buffers of the two parities: the current residual alternates between vr and vr2 */
     V2 *RA = s->vr, *RB = s->vr2, *QA = s->vq, *QB = s->vq2;
@@ -3482,6 +3613,7 @@ static void viscosity_solve(OSim* s, int restrain) {
         }
     }
     free(newr);
+stats:
     /* mode 7 */
     if (K->v_iters > K->v_it_max) K->v_it_max = K->v_iters;
     if (K->v_done == 0u) K->v_unconv += 1u;
@@ -3757,8 +3889,8 @@ static int set_tank(OSim* s, const int* present, int thermal) {
     }
     if (rc == 0) {
         s->visc_mode = viscosity_mode(s);
-        /* the implicit solve with its multigrid preconditioner on at least one coarse level */
-        if (s->visc_mode == 2 && (s->prm.viscosity_precond == 0 || s->lv.tail < 1)) rc = -4;
+        /* the multigrid-preconditioned implicit solve needs at least one coarse level */
+        if (s->visc_mode == 2 && s->prm.viscosity_precond != 0 && s->lv.tail < 1) rc = -4;
     }
     if (rc != 0) {
         s->tank = old_tank;

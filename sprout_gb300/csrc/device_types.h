@@ -65,6 +65,7 @@ struct DevParams {
     int visc_levels;   // levels below the grid in its V-cycle: min(viscosity_mg_levels, tail)
     int visc_sweeps;   // Gauss-Seidel sweeps per visit of a level (1 or 2)
     int viscosity_warm, viscous_warm, viscous_projection;
+    int viscosity_precond;   // 0: the Jacobi-preconditioned iteration, 1: the multigrid one
 };
 
 // StepBuf (common.glsl:122-135) plus the engine's own step flags.

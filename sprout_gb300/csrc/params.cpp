@@ -612,6 +612,7 @@ void build_params(const SimParams& p, const Tank& t, bool thermal, uint32_t caps
     P->viscosity_warm = p.viscosity_warm != 0 ? 1 : 0;
     P->viscous_warm = p.viscous_warm != 0 ? 1 : 0;
     P->viscous_projection = p.viscous_projection != 0 ? 1 : 0;
+    P->viscosity_precond = p.viscosity_precond != 0 ? 1 : 0;
 }
 
 }  // namespace sprout

@@ -221,9 +221,8 @@ struct SproutSim {
     int derive_viscosity() {
         visc_mode = viscosity_mode();
         if (visc_mode != 2) return SPROUT_OK;
-        if (params.viscosity_precond == 0)
-            return fail(SPROUT_E_UNSUPPORTED, "the Jacobi-preconditioned viscosity solve (viscosity_precond 0) is not carried by this engine; use the multigrid one (1, the default)");
-        if (d.lv.tail < 1) return fail(SPROUT_E_UNSUPPORTED, "the implicit viscosity solve needs a grid with at least one multigrid level below it");
+        if (params.viscosity_precond != 0 && d.lv.tail < 1)
+            return fail(SPROUT_E_UNSUPPORTED, "the multigrid-preconditioned viscosity solve needs a grid with at least one multigrid level below it");
         return ensure_visc_buffers();
     }
 
@@ -991,6 +990,7 @@ struct SproutBatch {
         int max_lev = 0, tiles = 0;
         for (const SproutSim* sim : second.members) {
             if (sim->cfg.visc_sweeps != sw) return SPROUT_OK;   // mixed sweep counts: one solve per tank
+            if (sim->params.viscosity_precond == 0) return SPROUT_OK;   // the Jacobi iteration: one solve per tank
             max_lev = std::max(max_lev, sim->cfg.visc_levels);
             tiles += sim->d.nwg;
         }

@@ -650,6 +650,118 @@ struct VSolve {
         each(0, [&](uint32_t tt) { warm_tile(tt, half); });
     }
 
+    // visc_iter.comp (not WARM), the Jacobi-preconditioned iteration on active level-0 tile
+    // tt: the direction p = z + beta p_old (z = r / diag) on the tile and two cells around, its
+    // weighted strain on the tile and one cell around (both in the shared staging area, which
+    // this path does not otherwise use), then q = M p + G^T s on the tile into vq and p into
+    // p_new; partial sums of p.q
+    DEV void jac_iter_tile(uint32_t tt, const float2* p_old, float2* p_new, int half) const {
+        constexpr int PW = 20, SW = 18;
+        float2* sp = reinterpret_cast<float2*>(&s.st[0]);
+        float4* ss = reinterpret_cast<float4*>(sp + PW * PW);
+        const Lv L0 = lev(d.lv, 0);
+        const int2 O = tile_origin(L0, (int)tt);
+        const float b = K.beta;
+        for (int k = threadIdx.x; k < PW * PW; k += NT) {
+            const int x = O.x - 2 + k % PW, y = O.y - 2 + k / PW;
+            float2 p = f2(0.0f, 0.0f);
+            if (in_grid(d, x, y) && interior(d, x, y)) {
+                const int i = y * d.W + x;
+                const float4 w = d.vw[i];
+                const float2 r = d.vr[i];
+                const float2 z = f2(r.x / w.z, r.y / w.w);
+                if (b == 0.0f) p = z;
+                else {
+                    const float2 po = p_old[i];
+                    p = f2(z.x + b * po.x, z.y + b * po.y);
+                }
+            }
+            sp[k] = p;
+        }
+        __syncthreads();
+        auto pd = [&](int x, int y) { return sp[(y - O.y + 2) * PW + (x - O.x + 2)]; };
+        auto U = [&](int x, int y, int j) { return v_live_u(d, j) ? pd(x, y).x : 0.0f; };
+        auto Vv = [&](int x, int y, int j) { return v_live_v(d, j) ? pd(x, y).y : 0.0f; };
+        const int W = d.W;
+        for (int k = threadIdx.x; k < SW * SW; k += NT) {
+            const int cx = O.x - 1 + k % SW, cy = O.y - 1 + k / SW;
+            float4 o = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            if (in_grid(d, cx, cy)) {
+                const int i = cy * W + cx;
+                const float4 w = d.vw[i];
+                if (w.x > 0.0f) {
+                    o.x = w.x * (U(cx + 1, cy, i + 1) - U(cx, cy, i));
+                    o.y = w.x * (Vv(cx, cy + 1, i + W) - Vv(cx, cy, i));
+                }
+                if (w.y > 0.0f) {
+                    float ua = U(cx, cy, i), ub = U(cx, cy - 1, i - W), va = Vv(cx, cy, i), vb = Vv(cx - 1, cy, i - 1);
+                    if (v_closed_u(d, i) && v_live_u(d, i - W)) ua = -ub;
+                    if (v_closed_u(d, i - W) && v_live_u(d, i)) ub = -ua;
+                    if (v_closed_v(d, i) && v_live_v(d, i - 1)) va = -vb;
+                    if (v_closed_v(d, i - 1) && v_live_v(d, i)) vb = -va;
+                    o.z = w.y * 0.5f * ((ua - ub) + (va - vb));
+                }
+            }
+            ss[k] = o;
+        }
+        __syncthreads();
+        auto sat = [&](int x, int y) { return ss[(y - O.y + 1) * SW + (x - O.x + 1)]; };
+        const int cx = O.x + (threadIdx.x & 15), cy = O.y + (threadIdx.x >> 4);
+        float4 acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if (in_grid(d, cx, cy)) {
+            const int i = cy * W + cx;
+            const float2 pn = pd(cx, cy);
+            p_new[i] = pn;
+            if (interior(d, cx, cy)) {
+                float2 g = f2(0.0f, 0.0f);
+                if (v_live_u(d, i)) {
+                    const float c1 = v_closed_u(d, i - W) ? 1.0f : 0.5f, c2 = v_closed_u(d, i + W) ? -1.0f : -0.5f;
+                    g.x = sat(cx - 1, cy).x - sat(cx, cy).x + sat(cx, cy).z * c1 + sat(cx, cy + 1).z * c2;
+                }
+                if (v_live_v(d, i)) {
+                    const float d1 = v_closed_v(d, i - 1) ? 1.0f : 0.5f, d2 = v_closed_v(d, i + 1) ? -1.0f : -0.5f;
+                    g.y = sat(cx, cy - 1).y - sat(cx, cy).y + sat(cx, cy).z * d1 + sat(cx + 1, cy).z * d2;
+                }
+                const float lu = v_live_u(d, i) ? 1.0f : 0.0f, lv = v_live_v(d, i) ? 1.0f : 0.0f;
+                const float4 cf = d.coef[i];
+                const float2 p = f2(pn.x * lu, pn.y * lv);
+                const float2 q = f2((cf.z * p.x + g.x) * lu, (cf.w * p.y + g.y) * lv);
+                d.vq[i] = q;
+                acc = make_float4(0.0f, 0.0f, dot2(p, q), 0.0f);
+            } else {
+                d.vq[i] = f2(0.0f, 0.0f);
+            }
+        }
+        tile_sum(acc, half, tt);
+    }
+    // visc_update.comp on active level-0 tile tt: u += alpha p, the warm-start step, r -= alpha
+    // q; partial sums of r.z and r.r
+    DEV void jac_update_tile(uint32_t tt, const float2* p_cur, int half) const {
+        const Lv L0 = lev(d.lv, 0);
+        const int2 O = tile_origin(L0, (int)tt);
+        const int cx = O.x + (threadIdx.x & 15), cy = O.y + (threadIdx.x >> 4);
+        float4 acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if (in_grid(d, cx, cy) && interior(d, cx, cy)) {
+            const int i = cy * d.W + cx;
+            const float a = K.alpha;
+            float4 v = d.vel[i];
+            const float2 p = p_cur[i];
+            const bool lu = face_live(v.z), lv = face_live(v.w);
+            if (lu) v.x += a * p.x;
+            if (lv) v.y += a * p.y;
+            store_vel_xy(d, i, v.x, v.y);
+            const float2 dv = d.vd[i];
+            d.vd[i] = f2(dv.x + a * (lu ? p.x : 0.0f), dv.y + a * (lv ? p.y : 0.0f));
+            const float2 r0 = d.vr[i], q = d.vq[i];
+            const float2 r = f2(r0.x - a * q.x, r0.y - a * q.y);
+            d.vr[i] = r;
+            const float4 w = d.vw[i];
+            const float2 z = f2(r.x / w.z, r.y / w.w);
+            acc = make_float4(dot2(r, z), dot2(r, r), 0.0f, 0.0f);
+        }
+        tile_sum(acc, half, tt);
+    }
+
     // For every active tile of level l in this block's share, through the pipeline of two
     // staging buffers: stage(tt, g) issues the tile's copies, finish(tt, g) computes it.
     template <class S, class F>
@@ -858,10 +970,46 @@ __global__ void __launch_bounds__(NT, 2) k_visc_solve(DevScene d, int restrain) 
         __syncthreads();
         half ^= 1;
     }
+    if (P->viscosity_precond == 0) {
+        // the Jacobi-preconditioned iteration (mod.rs:2909-2921): visc_iter with cg_reduce mode
+        // 5, visc_update with mode 6; the directions alternate between vp and vr2 (free without
+        // the multigrid) as vp / vp2 swap in the reference
+        float2 *pa = d.vp, *pb = d.vr2;
+        for (uint32_t k = 0; k < P->viscosity_max_iters && K.done == 0u; k++) {
+            V.each(0, [&](uint32_t tt) { V.jac_iter_tile(tt, pa, pb, half); });
+            if (!grid_sync(d.K)) return;
+            {
+                const float4 a = V.sum(half);   // mode 5
+                if (threadIdx.x == 0) K.alpha = (K.done == 0u && a.z > 0.0f) ? K.rz / a.z : 0.0f;
+                __syncthreads();
+                half ^= 1;
+            }
+            V.each(0, [&](uint32_t tt) { V.jac_update_tile(tt, pb, half); });
+            if (!grid_sync(d.K)) return;
+            {
+                const float4 a = V.sum(half);   // mode 6
+                if (threadIdx.x == 0) {
+                    const uint32_t was = K.done;
+                    K.iters += 1u - was;
+                    const uint32_t now = a.y <= tz * tz * K.r0 ? 1u : 0u;
+                    const uint32_t done = was > now ? was : now;
+                    K.beta = (done == 0u && K.rz > 0.0f) ? a.x / K.rz : 0.0f;
+                    K.rz = a.x;
+                    if (was == 0u) K.rr = a.y;
+                    K.done = done;
+                }
+                __syncthreads();
+                half ^= 1;
+            }
+            float2* t = pa;
+            pa = pb;
+            pb = t;
+        }
+    }
     // the two parities of the residual and of q: the current residual alternates between
     // vr and vr2 (visc_mgu.comp writes the other one)
     float2 *ra = d.vr, *rb = d.vr2, *qa = d.vq, *qb = d.vq2;
-    if (K.done == 0u) {
+    if (K.done == 0u && P->viscosity_precond != 0) {
         V.down(0, nlev, ra);
         if (!grid_sync(d.K)) return;
         if (!V.coarse(nlev)) return;
@@ -878,7 +1026,7 @@ __global__ void __launch_bounds__(NT, 2) k_visc_solve(DevScene d, int restrain) 
         __syncthreads();
         half ^= 1;
     }
-    for (uint32_t k = 0; k < P->viscosity_max_iters && K.done == 0u; k++) {
+    for (uint32_t k = 0; k < P->viscosity_max_iters && K.done == 0u && P->viscosity_precond != 0; k++) {
         V.mgu(ra, qa, rb, qb, half);
         if (!grid_sync(d.K)) return;
         {

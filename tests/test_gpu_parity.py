@@ -167,6 +167,18 @@ def test_implicit_viscosity_variants_bit_exact():
     assert not problems, "\n".join(problems)
 
 
+def test_jacobi_preconditioned_viscosity_bit_exact():
+    """viscosity_precond 0: the reference's Jacobi-preconditioned iteration (visc_iter.comp,
+    visc_update.comp) in place of the multigrid one, warm starts on."""
+    t = tanks.stratified(160, 96, extra={"viscosity_precond": 0})
+    sim, ora, problems = run_pair(t, 6, check_every=3)
+    assert not problems, "\n".join(problems)
+    st = sim.stats()
+    assert st.viscosity_mode == 2 and st.viscosity_iters_max > 0
+    problems = compare_viscosity(sim, ora)
+    assert not problems, "\n".join(problems)
+
+
 def test_full_physics_pour_bit_exact():
     """The full-physics pour at 160 x 96 (same physical tank, 6.4 mm cells): eight liquids,
     heater strip, surface tension, heat and the implicit viscosity together."""

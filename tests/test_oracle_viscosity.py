@@ -70,3 +70,19 @@ def test_solves_reach_their_tolerance(viscous_sim):
     assert 0 < st.v_it_max < 50
     assert st.v_res_max <= 1e-5
     assert st.p2_it_max > 0                     # the second projection ran
+
+
+def test_jacobi_preconditioned_solve_reaches_the_same_velocities():
+    """viscosity_precond 0 (visc_iter.comp / visc_update.comp, cg_reduce modes 5 and 6): the
+    Jacobi-preconditioned iteration solves the same system to the same tolerance as the
+    multigrid one, in more iterations."""
+    mg = O.build_tank(stratified(W, H, extra={"viscosity_warm": 0}), 4)[0]
+    jac = O.build_tank(stratified(W, H, extra={"viscosity_warm": 0, "viscosity_precond": 0}), 4)[0]
+    mg.step(1)
+    jac.step(1)
+    a, b = mg.stats(), jac.stats()
+    assert a.viscosity_mode == b.viscosity_mode == 2
+    assert b.v_unconv == 0 and b.v_res_max <= 1e-5 and b.v_it_max > a.v_it_max > 0
+    va, vb = mg.field("vel").reshape(-1, 4), jac.field("vel").reshape(-1, 4)
+    scale = np.abs(va[:, :2]).max()
+    assert np.abs(va[:, :2] - vb[:, :2]).max() <= 1e-4 * scale
