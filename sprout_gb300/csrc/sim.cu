@@ -1176,8 +1176,18 @@ struct SproutBatch {
     void record_substep(bool replay = false) {
         const std::vector<SproutSim*>& ms = first.members;
         size_t k = 0;
+        // a tank whose implicit viscosity runs before its only pressure solve (viscous_projection
+        // 0) has its cooperative viscosity kernel inside the grid stage: its stages run on the
+        // main stream, never beside another tank's kernels
+        auto serial = [](const SproutSim* sim) { return sim->cfg.visc_mode == 2 && !sim->cfg.twice; };
+        for (SproutSim* sim : ms)
+            if (serial(sim)) {
+                if (replay) cudaGraphLaunch(sim->part_exec[0], main);
+                else for (int st = 0; st < 4; st++) sim->record_stage(st, main);
+            }
         fork(k);
         for (size_t s = 0; s < ms.size(); s++) {
+            if (serial(ms[s])) continue;
             if (replay) cudaGraphLaunch(ms[s]->part_exec[0], workers[s % kWorkers]);
             else for (int st = 0; st < 4; st++) ms[s]->record_stage(st, workers[s % kWorkers]);
         }
@@ -1229,10 +1239,8 @@ struct SproutBatch {
     int check_members(const std::vector<SproutSim*>& ms, std::vector<SproutSim*>& twice) {
         twice.clear();
         for (SproutSim* sim : ms) {
-            if (sim->cfg.visc_mode == 2 && !sim->cfg.twice)
-                return fail(SPROUT_E_UNSUPPORTED, "a batch carries the implicit viscosity only between two pressure solves (viscous_projection 1)");
             if (sim->cfg.mixed != mixed) return fail(SPROUT_E_ARG, "a batch's tanks share its precision");
-            if (sim->cfg.visc_mode == 2) twice.push_back(sim);
+            if (sim->cfg.visc_mode == 2 && sim->cfg.twice) twice.push_back(sim);
         }
         return SPROUT_OK;
     }

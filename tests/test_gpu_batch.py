@@ -54,6 +54,33 @@ def test_batch_equals_alone(precision):
     assert st.viscosity_mode == 2 and st.pressure2_iters_max > 0
 
 
+def test_batch_viscosity_variants_equal_alone():
+    """The implicit viscosity before a single pressure solve (viscous_projection 0: its solve
+    runs inside the grid stage, on the batch's main stream), the Jacobi-preconditioned solve
+    (one solve per tank), and multigrid-preconditioned tanks solved together in one batched
+    viscosity kernel: each tank as it steps alone."""
+    def variants():
+        return [tanks.stratified(128, 72, extra={"viscous_projection": 0}),
+                tanks.stratified(96, 64, extra={"viscosity_precond": 0}),
+                tanks.stratified(128, 72), tanks.full_physics(160, 96, cell=0.0064),
+                tanks.dam_break(96, 64)]
+    alone = [t.engine()[0] for t in variants()]
+    batched = [t.engine()[0] for t in variants()]
+    batch = S.Batch(batched, "plain")
+    n = 6
+    for s in alone:
+        s.step(n, n / 240.0)
+    batch.step(n)
+    batch.sync()
+    problems = []
+    for k, (a, b) in enumerate(zip(alone, batched)):
+        problems += compare(a, b, f"tank {k}")
+    assert not problems, "\n".join(problems)
+    st = [s.stats() for s in batched]
+    assert st[0].viscosity_mode == 2 and st[0].pressure2_iters_max == 0
+    assert st[1].viscosity_iters_max > st[2].viscosity_iters_max > 0
+
+
 def test_batch_membership_changes():
     """Adding and removing tanks between steps re-records the batch; a removed tank steps
     alone again."""
