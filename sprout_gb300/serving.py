@@ -37,9 +37,12 @@ class Request:
 
 
 class Server:
-    def __init__(self, precision: str = "plain", max_batch: int = 64, reserve_bytes: float = 4e9):
+    def __init__(self, precision: str = "plain", max_batch: int = 64, reserve_bytes: float = 4e9,
+                 max_inflight: int = 2):
         self.batch = Batch([], precision)
         self.max_batch = max_batch
+        self.max_inflight = max_inflight       # launches queued on the device at most
+        self.completed = 0
         self.reserve = reserve_bytes
         self.sims = []                          # in batch order
         self.live = []                          # live particles per tank
@@ -76,11 +79,16 @@ class Server:
         return r
 
     def pump(self) -> int:
-        """One launch: the oldest tanks with work (at most max_batch) advance one substep.
-        Returns how many tanks were stepped."""
+        """One launch: the oldest tanks with work (at most max_batch) advance one substep,
+        unless max_inflight launches are still on the device (requests that arrive meanwhile
+        then join a larger launch). Returns how many tanks were stepped."""
         n = min(len(self.order), self.max_batch)
         if n == 0:
             return 0
+        if self.launches - self.completed >= self.max_inflight:
+            self.completed = self.batch.tickets()[1]
+            if self.launches - self.completed >= self.max_inflight:
+                return 0
         chosen = [self.order.popleft() for _ in range(n)]
         self.batch.step_subset(chosen)
         self.launches += 1
@@ -101,6 +109,7 @@ class Server:
     def poll(self, now: float):
         """Requests whose last launch has finished on the device."""
         _, completed = self.batch.tickets()
+        self.completed = completed
         while self.inflight and self.inflight[0].ticket <= completed:
             r = self.inflight.popleft()
             r.done_at = now
@@ -124,9 +133,9 @@ def serving_tanks(n: int, seed: int = 0):
 
 
 def run(scenes: int = 512, rate: float = 2000.0, seconds: float = 60.0, precision: str = "plain",
-        max_batch: int = 64, seed: int = 0) -> dict:
+        max_batch: int = 64, seed: int = 0, max_inflight: int = 2) -> dict:
     """A seeded Poisson stream of scene-step requests (1-8 substeps) over resident tanks."""
-    srv = Server(precision, max_batch)
+    srv = Server(precision, max_batch, max_inflight=max_inflight)
     t0 = time.perf_counter()
     admitted = 0
     for t in serving_tanks(scenes, seed):
@@ -148,12 +157,15 @@ def run(scenes: int = 512, rate: float = 2000.0, seconds: float = 60.0, precisio
         while k < len(arrivals) and arrivals[k] <= now:
             srv.submit(int(targets[k]), int(steps[k]), float(arrivals[k]))
             k += 1
-        stepped = srv.pump()
         srv.poll(time.perf_counter() - start)
+        stepped = srv.pump()
         if k >= len(arrivals) and not srv.order:
             break
-        if not stepped and k < len(arrivals):
-            time.sleep(max(0.0, min(arrivals[k] - (time.perf_counter() - start), 0.001)))
+        if not stepped:
+            if srv.order:   # the device is busy: check again shortly
+                time.sleep(2e-5)
+            elif k < len(arrivals):
+                time.sleep(max(0.0, min(arrivals[k] - (time.perf_counter() - start), 0.001)))
     srv.batch.sync()
     end = time.perf_counter() - start
     srv.poll(end)
@@ -164,7 +176,7 @@ def run(scenes: int = 512, rate: float = 2000.0, seconds: float = 60.0, precisio
             "particle_steps_per_s": srv.particle_steps / end,
             "p50_ms": float(np.percentile(lat, 50)) if len(lat) else None,
             "p99_ms": float(np.percentile(lat, 99)) if len(lat) else None,
-            "precision": precision, "max_batch": max_batch}
+            "precision": precision, "max_batch": max_batch, "max_inflight": max_inflight}
 
 
 def main():
@@ -175,8 +187,9 @@ def main():
     ap.add_argument("--precision", default="plain", choices=["plain", "mixed"])
     ap.add_argument("--max-batch", type=int, default=64)
     ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--max-inflight", type=int, default=2)
     a = ap.parse_args()
-    print(json.dumps(run(a.scenes, a.rate, a.seconds, a.precision, a.max_batch, a.seed)), flush=True)
+    print(json.dumps(run(a.scenes, a.rate, a.seconds, a.precision, a.max_batch, a.seed, a.max_inflight)), flush=True)
 
 
 if __name__ == "__main__":
