@@ -4,10 +4,12 @@
 //               collisions, crowd jitter (particles.comp:98-949); float4 particle loads;
 //               emits the particle's new cell and its arrival rank there
 //   scan        exclusive scan of the per-cell counts
-//   k_place / k_cell_gather
+//   k_place / k_cell_sort / k_cell_gather
 //               a stable counting sort by cell (ties by slot), the permutation the
-//               reference's sort.comp:83-119 defines up to its within-cell atomic order;
-//               dead slots go to the end and are cleared
+//               reference's sort.comp:83-119 defines up to its within-cell atomic order:
+//               ranks by arrival, each cell's few entries put in slot order, then one thread
+//               per slot copies its particle (coalesced); dead slots go to the end and are
+//               cleared
 //   k_p2g       P2G as a per-tile gather over the sorted particles: each 16 x 16 tile of
 //               nodes accumulates the fixed-point mass / momentum / channel sums of the
 //               particles of its 19 x 19 cell neighbourhood in shared memory (integer
@@ -477,63 +479,62 @@ __global__ void k_place(DevScene d) {
 // One thread per cell: orders the cell's arrivals by slot (insertion sort in registers for
 // up to 16, in place otherwise), then copies the particles into their sorted slots.
 // Threads past the last cell clear the slots after the live particles.
-__global__ void __launch_bounds__(256) k_cell_gather(DevScene d) {
-    int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c < d.ncell) {
-        uint32_t n = d.count[c];
-        if (n == 0u) return;
-        uint32_t s0 = d.start[c];
-        uint32_t* seg = d.perm + s0;
-        if (n <= 16u) {
-            uint32_t v[16];
+// Each cell's arrivals in slot order: the stable order of the counting sort (sort.comp keeps
+// a cell's particles in arrival order, which atomics make arbitrary; slot order makes it
+// deterministic). One thread per cell sorts the cell's few entries of perm in place.
+__global__ void __launch_bounds__(256) k_cell_sort(DevScene d) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= d.ncell) return;
+    const uint32_t n = d.count[c];
+    if (n < 2u) return;
+    uint32_t* seg = d.perm + d.start[c];
+    if (n <= 16u) {
+        uint32_t v[16];
 #pragma unroll
-            for (int k = 0; k < 16; k++)
-                if ((uint32_t)k < n) v[k] = seg[k];
-            for (uint32_t k = 1; k < n; k++) {
-                uint32_t x = v[k];
-                int j = (int)k - 1;
-                while (j >= 0 && v[j] > x) {
-                    v[j + 1] = v[j];
-                    j--;
-                }
-                v[j + 1] = x;
+        for (int k = 0; k < 16; k++)
+            if ((uint32_t)k < n) v[k] = seg[k];
+        for (uint32_t k = 1; k < n; k++) {
+            const uint32_t x = v[k];
+            int j = (int)k - 1;
+            while (j >= 0 && v[j] > x) {
+                v[j + 1] = v[j];
+                j--;
             }
-#pragma unroll
-            for (int k = 0; k < 16; k++)
-                if ((uint32_t)k < n) {
-                    uint32_t src = v[k];
-                    seg[k] = src;
-                    d.part[3 * (s0 + k) + 0] = d.part2[3 * src + 0];
-                    d.part[3 * (s0 + k) + 1] = d.part2[3 * src + 1];
-                    d.part[3 * (s0 + k) + 2] = d.part2[3 * src + 2];
-                }
-        } else {
-            for (uint32_t k = 1; k < n; k++) {
-                uint32_t x = seg[k];
-                int j = (int)k - 1;
-                while (j >= 0 && seg[j] > x) {
-                    seg[j + 1] = seg[j];
-                    j--;
-                }
-                seg[j + 1] = x;
-            }
-            for (uint32_t k = 0; k < n; k++) {
-                uint32_t src = seg[k];
-                d.part[3 * (s0 + k) + 0] = d.part2[3 * src + 0];
-                d.part[3 * (s0 + k) + 1] = d.part2[3 * src + 1];
-                d.part[3 * (s0 + k) + 2] = d.part2[3 * src + 2];
-            }
+            v[j + 1] = x;
         }
+#pragma unroll
+        for (int k = 0; k < 16; k++)
+            if ((uint32_t)k < n) seg[k] = v[k];
     } else {
-        // slots [n_live, n_slots) become dead (zero) slots
-        uint32_t k0 = d.S->n_live + (uint32_t)(c - d.ncell);
-        uint32_t stride = gridDim.x * blockDim.x - (uint32_t)d.ncell;
-        for (uint32_t k = k0; k < d.P->n_slots; k += stride) {
-            float4 z = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-            d.part[3 * k + 0] = z;
-            d.part[3 * k + 1] = z;
-            d.part[3 * k + 2] = z;
+        for (uint32_t k = 1; k < n; k++) {
+            const uint32_t x = seg[k];
+            int j = (int)k - 1;
+            while (j >= 0 && seg[j] > x) {
+                seg[j + 1] = seg[j];
+                j--;
+            }
+            seg[j + 1] = x;
         }
+    }
+}
+
+// The particles in sorted order, one thread per slot: slot j < n_live takes the advanced
+// particle perm[j] (consecutive slots write consecutive records), slots [n_live, n_slots)
+// become dead (zero) slots.
+__global__ void __launch_bounds__(256) k_cell_gather(DevScene d) {
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= d.P->n_slots) return;
+    if (j < d.S->n_live) {
+        const uint32_t src = d.perm[j];
+        const float4 a = d.part2[3 * src + 0], b = d.part2[3 * src + 1], c = d.part2[3 * src + 2];
+        d.part[3 * j + 0] = a;
+        d.part[3 * j + 1] = b;
+        d.part[3 * j + 2] = c;
+    } else {
+        const float4 z = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        d.part[3 * j + 0] = z;
+        d.part[3 * j + 1] = z;
+        d.part[3 * j + 2] = z;
     }
 }
 
@@ -691,8 +692,8 @@ void launch_sort(const DevScene& d, const LaunchCfg& cfg, cudaStream_t st) {
     k_scan_top<<<1, SCAN_BLOCK, 0, st>>>(d.scan_tmp, sb, d.S);
     k_scan_add<<<sb, SCAN_BLOCK, 0, st>>>(d.start, d.scan_tmp, n);
     k_place<<<nb, 256, 0, st>>>(d);
-    int cg = (d.ncell + 255) / 256 + 64;
-    k_cell_gather<<<cg, 256, 0, st>>>(d);
+    k_cell_sort<<<(d.ncell + 255) / 256, 256, 0, st>>>(d);
+    k_cell_gather<<<nb, 256, 0, st>>>(d);
 }
 
 void launch_p2g(const DevScene& d, const LaunchCfg& cfg, cudaStream_t st) {
