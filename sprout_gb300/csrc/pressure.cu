@@ -518,16 +518,15 @@ DEV void finish_down(const DevScene& d, const Lv& F, const Lv& C, int t, const R
         float2 sum = rhs(k);
         const float d0 = dg(k - 1), d1 = dg(k + 1), d2 = dg(k - RW), d3 = dg(k + RW);
         const float2 r0 = rhs(k - 1), r1 = rhs(k + 1), r2 = rhs(k - RW), r3 = rhs(k + RW);
-        const float t0x = w.x * r0.x / d0, t0y = w.x * r0.y / d0;
-        const float t1x = w.y * r1.x / d1, t1y = w.y * r1.y / d1;
-        const float t2x = w.z * r2.x / d2, t2y = w.z * r2.y / d2;
-        const float t3x = w.w * r3.x / d3, t3y = w.w * r3.y / d3;
+        const float t0x = divp(w.x * r0.x, d0), t0y = divp(w.x * r0.y, d0);
+        const float t1x = divp(w.y * r1.x, d1), t1y = divp(w.y * r1.y, d1);
+        const float t2x = divp(w.z * r2.x, d2), t2y = divp(w.z * r2.y, d2);
+        const float t3x = divp(w.w * r3.x, d3), t3y = divp(w.w * r3.y, d3);
         if (d0 > 0.0f) { sum.x += t0x; sum.y += t0y; }
         if (d1 > 0.0f) { sum.x += t1x; sum.y += t1y; }
         if (d2 > 0.0f) { sum.x += t2x; sum.y += t2y; }
         if (d3 > 0.0f) { sum.x += t3x; sum.y += t3y; }
-        const float di = dg(k);
-        return make_float2(sum.x / di, sum.y / di);
+        return divz(sum, dg(k));
     };
     // one cell's z (mg_down: red from zero, black after it), the CG update and mgx
     auto own = [&](int lx, int ly, bool red) {
@@ -540,8 +539,7 @@ DEV void finish_down(const DevScene& d, const Lv& F, const Lv& C, int t, const R
             const float D = dg(k0);
             if (D > 0.0f) {
                 if (red) {
-                    const float2 r = rhs(k0);
-                    z = make_float2(r.x / D, r.y / D);
+                    z = divz(rhs(k0), D);
                 } else {
                     z = black(k0);
                 }
@@ -680,8 +678,7 @@ DEV void finish_up(const DevScene& d, const Lv& F, int t, bool flag, const Zc& z
                 sum.y += uy;
             }
         }
-        const float di = dg(k);
-        return make_float2(sum.x / di, sum.y / di);
+        return divz(sum, dg(k));
     };
     const int2 lc = colour_cell();
     const int lx = lc.x, ly = lc.y, cell = ly * 16 + lx;
@@ -724,8 +721,7 @@ DEV void finish_up(const DevScene& d, const Lv& F, int t, bool flag, const Zc& z
                         sy += uy;
                     }
                 }
-                const float di = dg(k0);
-                z = make_float2(sx / di, sy / di);
+                z = divz(make_float2(sx, sy), dg(k0));
             }
             a4 = M::prod4(r.x, z.x, r.y, z.y, r.x, r.x, r.y, r.y);
         }
@@ -748,31 +744,32 @@ DEV void phase_tail(const DevScene& d, const Tail& tl, bool writer) {
     const int first = d.lv.tail, last = d.lv.n - 1;
     for (int s = threadIdx.x; s < tl.nf; s += NT) tl.r[s] = M::R(d, tl.base + s);
     __syncthreads();
+    // a half-sweep: every slot's reads are issued before its terms are summed (neighbour
+    // slots clamped into the level and kept or not by the mask), in the shader's order
     auto sweep = [&](const Lv& L, int colour, bool zero) {
-        const int o = L.off - tl.base;
-        for (int t = threadIdx.x; t < L.w * L.h; t += NT) {
+        const int o = L.off - tl.base, n = L.w * L.h;
+        const int lo = o, hi = o + n - 1;
+        for (int t = threadIdx.x; t < n; t += NT) {
             const int y = qdiv(t, L.wm), x = t - y * L.w;
-            int s = o + t;
-            float D = tl.dg[s];
-            if (D <= 0.0f || ((x + y) & 1) != colour) {
-                if (zero) tl.x[s] = make_float2(0.0f, 0.0f);
+            const int s = o + t;
+            const float D = tl.dg[s];
+            const float2 r = tl.r[s];
+            const bool mine = !(D <= 0.0f) && ((x + y) & 1) == colour;
+            if (zero) {
+                if (mine) tl.x[s] = divz(r, D);
+                else tl.x[s] = make_float2(0.0f, 0.0f);
                 continue;
             }
-            float2 sum = tl.r[s];
-            if (!zero) {
-                const float4 w = tl.a[s];
-                const uint32_t m = tl.m[s];
-                const int step[4] = {-1, 1, -L.w, L.w};
-                for (int q = 0; q < 4; q++) {
-                    if (m & (1u << q)) {
-                        float wd = wcomp(w, q);
-                        float2 xn = tl.x[s + step[q]];
-                        sum.x += wd * xn.x;
-                        sum.y += wd * xn.y;
-                    }
-                }
-            }
-            tl.x[s] = make_float2(sum.x / D, sum.y / D);
+            const float4 w = tl.a[s];
+            const uint32_t m = tl.m[s];
+            const float2 x0 = tl.x[max(s - 1, lo)], x1 = tl.x[min(s + 1, hi)];
+            const float2 x2 = tl.x[max(s - L.w, lo)], x3 = tl.x[min(s + L.w, hi)];
+            float2 sum = r;
+            if (m & 1u) { sum.x += w.x * x0.x; sum.y += w.x * x0.y; }
+            if (m & 2u) { sum.x += w.y * x1.x; sum.y += w.y * x1.y; }
+            if (m & 4u) { sum.x += w.z * x2.x; sum.y += w.z * x2.y; }
+            if (m & 8u) { sum.x += w.w * x3.x; sum.y += w.w * x3.y; }
+            if (mine) tl.x[s] = divz(sum, D);
         }
         __syncthreads();
     };
@@ -837,7 +834,7 @@ DEV void phase_tail(const DevScene& d, const Tail& tl, bool writer) {
                 sum.x += wd * (xn.x + MG_OMEGA * xc.x);
                 sum.y += wd * (xn.y + MG_OMEGA * xc.y);
             }
-            tl.x[s] = make_float2(sum.x / D, sum.y / D);
+            tl.x[s] = divz(sum, D);
         }
         __syncthreads();
         sweep(F, 0, false);

@@ -318,7 +318,7 @@ struct Region {
         const float2 o = offd(k);
         const float2 rr = g.sr[k];
         const float sx_ = rr.x - o.x, sy_ = rr.y - o.y;
-        return f2(dd.x > 0.0f ? sx_ / dd.x : 0.0f, dd.y > 0.0f ? sy_ / dd.y : 0.0f);
+        return f2(divp(sx_, dd.x), divp(sy_, dd.y));
     }
 
     // The copies of the region: matrix, right-hand side rhs (an array of the level, offset
@@ -380,7 +380,7 @@ struct Region {
             if (k >= N) break;
             fix(k);
             const float2 dd = g.sd[k], r = g.sr[k];
-            const float2 x = f2(dd.x > 0.0f ? r.x / dd.x : 0.0f, dd.y > 0.0f ? r.y / dd.y : 0.0f);
+            const float2 x = f2(divp(r.x, dd.x), divp(r.y, dd.y));
             sx[k] = red(k) ? x : f2(0.0f, 0.0f);
         }
         __syncthreads();
@@ -567,7 +567,7 @@ struct VSolve {
                 const float lu = v_live_u(d, i) ? 1.0f : 0.0f, lv = v_live_v(d, i) ? 1.0f : 0.0f;
                 const float4 w4 = d.vw[i];
                 const float2 r = f2(-g.x * lu, -g.y * lv);
-                const float2 z = f2(r.x / w4.z, r.y / w4.w);
+                const float2 z = f2(divz(r.x, w4.z), divz(r.y, w4.w));
                 d.vr[i] = r;
                 d.vp[i] = z;
                 acc = make_float4(dot2(r, z), dot2(r, r), 0.0f, 0.0f);
@@ -640,7 +640,7 @@ struct VSolve {
                 const float2 r = f2(r0.x - q.x, r0.y - q.y);
                 d.vr[i] = r;
                 const float4 w4 = d.vw[i];
-                const float2 z = f2(r.x / w4.z, r.y / w4.w);
+                const float2 z = f2(divz(r.x, w4.z), divz(r.y, w4.w));
                 acc = make_float4(dot2(r, z), dot2(r, r), 0.0f, 0.0f);
             }
             tile_sum(acc, half, tt);
@@ -669,7 +669,7 @@ struct VSolve {
                 const int i = y * d.W + x;
                 const float4 w = d.vw[i];
                 const float2 r = d.vr[i];
-                const float2 z = f2(r.x / w.z, r.y / w.w);
+                const float2 z = f2(divz(r.x, w.z), divz(r.y, w.w));
                 if (b == 0.0f) p = z;
                 else {
                     const float2 po = p_old[i];
@@ -756,7 +756,7 @@ struct VSolve {
             const float2 r = f2(r0.x - a * q.x, r0.y - a * q.y);
             d.vr[i] = r;
             const float4 w = d.vw[i];
-            const float2 z = f2(r.x / w.z, r.y / w.w);
+            const float2 z = f2(divz(r.x, w.z), divz(r.y, w.w));
             acc = make_float4(dot2(r, z), dot2(r, r), 0.0f, 0.0f);
         }
         tile_sum(acc, half, tt);
