@@ -50,9 +50,11 @@ def workload(name: str, rank: int):
                 "pressure_tol": 1e-5, "viscosity_tol": 1e-5, "solver": "plain fp32 MGPCG + implicit viscosity MG-PCG",
                 "heater": "600 K, bottom 8 rows", "surface_tension": "0.02-0.5 N/m", "seed": 0}
     elif name == "stratified_512":
-        t = WL.stratified(512, 288, cell=0.002, tol=1e-5)
+        # built-in honey (a water concentrate, mix rate 1.5 / s) and water exchange concentration
+        t = WL.stratified(512, 288, cell=0.002, tol=1e-5, honey_family=True)
         desc = {"workload": "stratified_honey_water_oil_512x288", "grid": [512, 288], "cell_size_m": 0.002,
                 "fill": "honey / water / olive oil layers, 20% of the height each", "ppc": 4, "substep_s": 1 / 240,
+                "family": "honey in water, mix rate 1.5/s",
                 "pressure_tol": 1e-5, "viscosity_tol": 1e-5, "solver": "plain fp32 MGPCG + implicit viscosity MG-PCG"}
     elif name == "dam_break_1024":
         # 1024 x 576 MAC grid, 1 mm cells, water over the left 40 % and bottom 60 %, 4 particles

@@ -96,6 +96,12 @@ int sprout_params_copy(const SproutParams* src, SproutParams** out);
 int sprout_params_set(SproutParams* p, const char* key, float v, int* ok);
 /* Reads a parameter by the same names; *ok = 0 for an unknown name. */
 int sprout_params_get(const SproutParams* p, const char* key, float* v, int* ok);
+/* The diluent of custom liquid `row` (59..95), as the library's loader resolves a liquid's
+ * "diluent" reference into `MatProps::diluent` (src/library.rs:318-330): -1 for none, else
+ * another row that is a built-in without a diluent of its own, or a custom liquid. The
+ * liquid is then `s` parts itself and 1 - s parts the diluent (a concentration family).
+ * *ok = 0 and nothing changes for a built-in row or a diluent the loader would drop. */
+int sprout_params_set_diluent(SproutParams* p, uint32_t row, int32_t diluent, int* ok);
 
 /* ---- scene: Scene (src/scene.rs) ---------------------------------------------------- */
 int sprout_scene_new(uint32_t w, uint32_t h, SproutScene** out);

@@ -334,6 +334,8 @@ def build_tank(tank, threads: int | None = None):
     p = default_params()
     for k, v in tank.settings.items():
         apply_setting(p, k, v)
+    for row, dil in getattr(tank, "diluents", {}).items():
+        p.mat[row].diluent = dil
     sdf, solid, region, temp = rasterize(tank.w, tank.h, tank.shapes)
     parts = None
     for rect, mat, t in tank.fills:

@@ -573,6 +573,7 @@ typedef struct GParams {   /* common.glsl:37-86 (subset) */
     int primary;
     uint32_t group_heat;
     int present[MAX_PRESENT];
+    int fams[MAX_PRESENT][2];   /* per family: its row, its diluent's row (mod.rs:2250-2255) */
     float heat[4], heat2[4];
     float sep_tau, cfl, tool_crowd_max, density_k, dt_max, crowd_jitter, ext_speed, wall_margin;
     float tool_pos[2], tool_vel[2], tool_radius;
@@ -647,6 +648,7 @@ struct OSim {
     V4 *vel, *cell, *comp, *coef, *sprop, *surf, *surf2, *aux, *grho, *therm, *dheat, *vw, *vs, *prhs;
     V2 *vel0, *pjump, *pres;
     float* p2keep;
+    float* mixb;   /* per cell, families 1 .. n_fam - 1: the concentration (-1: not here) */
     I2* hcell;
     V4* solid;
     float* sdf;
@@ -933,6 +935,12 @@ static void build_params(OSim* s, const OTool* tool) {
     for (int g = 0; g < GROUPS; g++) gh += ((uint32_t)(s->tank.chan_g[g] + 1) & 255u) << (8 * g);
     P->group_heat = gh;
     for (int k = 0; k < s->tank.nrows; k++) P->present[k] = s->tank.rows[k];
+    for (int j = 0; j < MAX_PRESENT; j++) P->fams[j][0] = P->fams[j][1] = -1;
+    for (int k = 0; k < s->tank.nrows; k++)
+        if (s->tank.chan[k][2] >= 0) {
+            P->fams[s->tank.chan[k][2]][0] = s->tank.rows[k];
+            P->fams[s->tank.chan[k][2]][1] = p->mat[s->tank.rows[k]].diluent;
+        }
     P->heat[0] = p->ambient_temp;
     P->heat[1] = p->heat_rate;
     P->heat[2] = p->air_cooling / (WATER_HEAT * dx);
@@ -1047,6 +1055,10 @@ static V4 thermal_of(const OSim* s, uint32_t row, float sc) {   /* common.glsl:5
     float C = mixf(dth[0], m->th[0], sc);
     return v4(dth[2] + shift, dth[3] + shift, mixf(dth[0] * s->mats[d].th2[0], m->th[0] * ld, sc) / C, C);
 }
+
+/* particles.comp:78-80: the enthalpy temperature that keeps the heat when the heat capacity
+ * changes from c0 to c1 */
+static float keep_heat(float t, float c0, float c1) { return c0 == c1 ? t : (t + 273.15f) * c0 / c1 - 273.15f; }
 
 static V2 phase_of(float te, V4 m) {   /* common.glsl:515-521 */
     if (te >= m.y) return v2(te, 0.0f);
@@ -1241,6 +1253,7 @@ static void advance(OSim* s, uint32_t id, int gather, Scat* g) {
     float dt = s->S.dt;
     uint32_t row = (p.kind & 255u) - 1u;
     const int* Mia = s->mats[row].ia;
+    const int fam = s->mats[row].ib[0];   /* particles.comp:143 */
     int thermal = has_cap(s, CAP_THERMAL);
     V2 pos = v2(p.pos[0], p.pos[1]);
     if (gather) {
@@ -1331,14 +1344,24 @@ static void advance(OSim* s, uint32_t id, int gather, Scat* g) {
             int bx = (int)floorf(gp.x - 0.5f), by = (int)floorf(gp.y - 0.5f);
             float fx = gp.x - (float)bx, fy = gp.y - (float)by;
             bspline(fx, fy, w);
-            float sw = 0.0f;
+            /* sw: weight of the cells holding liquid; sfw, sfs: weight and concentration of
+             * those holding the particle's own family (a diluent's: family 0) */
+            float sw = 0.0f, sfw = 0.0f, sfs = 0.0f;
+            const int nmix = P_.n_fam - 1;
             for (int b = 0; b < 3; b++)
                 for (int a = 0; a < 3; a++) {
                     int ci = cidx(s, bx + a, by + b);
                     V4 q = s->comp[ci];
                     float wt = w[a].x * w[b].y;
                     crowd += wt * q.w;
-                    if (q.x > 0.0f) sw += wt;
+                    if (q.x > 0.0f) {
+                        sw += wt;
+                        float sb = fam > 0 ? s->mixb[(size_t)ci * nmix + fam - 1] : q.z;
+                        if (sb >= 0.0f) {
+                            sfw += wt;
+                            sfs += wt * sb;
+                        }
+                    }
                 }
             if (thermal && (p.kind & KIND_FRESH) == 0u) {
                 float dT = 0.0f;
@@ -1354,7 +1377,49 @@ static void advance(OSim* s, uint32_t id, int gather, Scat* g) {
                 }
                 p.t += dT;
             }
-            (void)sw;
+            if (sw > 1e-4f) {
+                /* miscible exchange within a family (particles.comp:519-543) */
+                int diluent0 = fam < 0 && P_.primary >= 0 && P_.fams[0][1] == (int)row;
+                if (fam >= 0 || diluent0) {
+                    if (sfw > 1e-4f) {
+                        float s0 = diluent0 ? 0.0f : p.s;
+                        float rate = s->mats[diluent0 ? (uint32_t)P_.primary : row].a[3];
+                        float s1 = clampf(s0 + (sfs / sfw - s0) * (1.0f - o_expf(-rate * dt)), 0.0f, 1.0f);
+                        float c0 = thermal ? thermal_of(s, row, p.s).w : 0.0f;
+                        if (!diluent0) {
+                            p.s = s1;
+                        } else if (s1 > 0.0f) {
+                            row = (uint32_t)P_.primary;
+                            Mia = s->mats[row].ia;
+                            p.kind = (p.kind & ~255u) | (row + 1u);
+                            p.s = s1;
+                        }
+                        if (thermal) p.t = keep_heat(p.t, c0, thermal_of(s, row, p.s).w);
+                    }
+                }
+                /* a pure diluent next to another of its concentrates joins that family
+                 * (particles.comp:544-569) */
+                if (fam < 0 && has_cap(s, CAP_FAMILIES) && (p.kind & 255u) - 1u == row && s->mats[row].ib[0] < 0) {
+                    for (int j = P_.primary >= 0 ? 1 : 0; j < P_.n_fam; j++) {
+                        if (P_.fams[j][1] != (int)row) continue;
+                        float found = 0.0f;
+                        if (j == 0) {
+                            found = sfw;
+                        } else {
+                            for (int b = 0; b < 3; b++)
+                                for (int a = 0; a < 3; a++)
+                                    if (s->mixb[(size_t)cidx(s, bx + a, by + b) * nmix + j - 1] >= 0.0f) found += w[a].x * w[b].y;
+                        }
+                        if (found > 1e-4f) {
+                            row = (uint32_t)P_.fams[j][0];
+                            Mia = s->mats[row].ia;
+                            p.kind = (p.kind & ~255u) | (row + 1u);
+                            p.s = 0.0f;
+                            break;
+                        }
+                    }
+                }
+            }
         }
         /* mouse tool (particles.comp:596-631) */
         int pushed = 0;
@@ -1650,6 +1715,8 @@ static void k_grid_prep(OSim* s) {
             float fam0 = -1.0f;
             float rho = 0.0f, mu = 0.0f, rho_c = 0.0f, nu_c = 0.0f;
             int thermal = has_cap(s, CAP_THERMAL);
+            const int nmix = P_.n_fam - 1;   /* grid_prep.comp:67-68 */
+            for (int q = 0; q < nmix; q++) s->mixb[(size_t)i * nmix + q] = -1.0f;
             float T = P_.heat[0], kappa = 0.0f, emis = 0.0f, frozen = 0.0f, Craw = 0.0f;
             int major = 0, top_row = -1;
             float top_share = 0.0f;
@@ -1699,10 +1766,14 @@ static void k_grid_prep(OSim* s) {
                     if (ia[1] >= 0) {
                         const float* da = s->mats[ia[1]].a;
                         rho_m = mixf(da[0], rho_m, sc);
+                        /* blend_share(s, e) = s: every concentrate here blends with exponent 1 */
                         lnu = mixf(thermal ? da[1] + temp_law(s, ia[1], Tm) : da[1], lnu, sc);
                         sig = mixf(da[2], sig, sc);
                         csv = v2(mixf(s->mats[ia[1]].b[0], csv.x, sc), mixf(s->mats[ia[1]].b[1], csv.y, sc));
-                        if (s->mats[r].ib[0] == 0) fam0 = sc;
+                        /* grid_prep.comp:144-146 */
+                        const int fam = s->mats[r].ib[0];
+                        if (fam == 0) fam0 = sc;
+                        else if (fam > 0) s->mixb[(size_t)i * nmix + fam - 1] = sc;
                     }
                     rho_m *= xp;
                     if (thermal) {
@@ -3753,6 +3824,7 @@ OSim* osim_create(int w, int h, uint32_t capacity, const OSimParams* p) {
     ALLOC(s->sprop, nc); ALLOC(s->surf, nc); ALLOC(s->surf2, nc); ALLOC(s->aux, nc);
     ALLOC(s->grho, nc); ALLOC(s->therm, nc); ALLOC(s->dheat, nc); ALLOC(s->vw, nc);
     ALLOC(s->vs, nc); ALLOC(s->prhs, nc); ALLOC(s->vel0, nc); ALLOC(s->pjump, nc);
+    ALLOC(s->mixb, nc * (MAX_PRESENT - 1));
     ALLOC(s->pres, nc); ALLOC(s->p2keep, nc); ALLOC(s->hcell, nc); ALLOC(s->solid, nc);
     ALLOC(s->sdf, (size_t)(w + 1) * (h + 1)); ALLOC(s->region, nc); ALLOC(s->solid_t, nc);
     ALLOC(s->mga, s->lv.total); ALLOC(s->mgd, s->lv.total); ALLOC(s->mgx, s->lv.total);
@@ -3777,7 +3849,7 @@ void osim_destroy(OSim* s) {
                     s->vel0, s->pjump, s->pres, s->p2keep, s->hcell, s->solid, s->sdf, s->region,
                     s->solid_t, s->mga, s->mgd, s->mgx, s->mgz, s->mgr, s->cgp, s->cgp2, s->cgq,
                     s->ptile, s->part, s->vr, s->vr2, s->vp, s->vq, s->vq2, s->vd, s->vaz, s->vma,
-                    s->vmb, s->vmd, s->vmr, s->vmx, s->vmz, s->tiles, s->vtile, s->pending};
+                    s->vmb, s->vmd, s->vmr, s->vmx, s->vmz, s->tiles, s->vtile, s->pending, s->mixb};
     for (size_t k = 0; k < sizeof ptrs / sizeof ptrs[0]; k++) free(ptrs[k]);
     free(s);
 }
@@ -3880,7 +3952,6 @@ static int set_tank(OSim* s, const int* present, int thermal) {
     s->thermal = thermal;
     s->caps = compute_caps(s);
     int rc = 0;
-    if (t.families > 0) rc = -4;
     if (s->caps & (CAP_RIGID | CAP_RHEO | CAP_MAGNET | CAP_ELASTIC | CAP_SETTLE | CAP_STEAM | CAP_REACT)) rc = -4;
     if (__builtin_popcount(t.group_mask) > 1) rc = -4;
     for (int k = 0; k < nrows; k++) {
@@ -4066,6 +4137,7 @@ long osim_field(const OSim* s, const char* name, void* out, size_t cap) {
     F("mgz", s->mgz, (size_t)s->lv.total * 8)
     F("ptile", s->ptile, (size_t)s->lv.tiles * 4)
     F("p2keep", s->p2keep, nc * 4)
+    F("mixb", s->mixb, nc * 4 * (size_t)(s->P.n_fam > 1 ? s->P.n_fam - 1 : 0))
     F("tiles", s->tiles, (size_t)s->nwg * 4)
     F("vtile", s->vtile, (size_t)s->lv.tiles * 4)
     F("vd", s->vd, nc * 8)

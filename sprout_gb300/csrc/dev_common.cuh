@@ -60,6 +60,7 @@ struct DevScene {
     float4 *vel, *cell, *comp, *coef, *sprop, *surf, *surf2, *aux, *grho, *therm, *dheat, *vw, *vs, *prhs;
     float2 *vel0, *pjump, *pres;
     float* p2keep;
+    float* mixb;      // per cell, families 1 .. n_fam - 1: the family's concentration (-1: not here)
     int2* hcell;
     const float4* solid;
     const float* sdf;
@@ -183,6 +184,10 @@ DEV float4 thermal_of(const DevMat* mats, uint32_t row, float s) {
     float C = mixf(dm.th[0], m.th[0], s);
     return make_float4(dm.th[2] + shift, dm.th[3] + shift, mixf(dm.th[0] * dm.th2[0], m.th[0] * ld, s) / C, C);
 }
+
+// The enthalpy temperature that keeps a particle's heat when its heat capacity changes from
+// c0 to c1 (particles.comp:78-80).
+DEV float keep_heat(float t, float c0, float c1) { return c0 == c1 ? t : (t + 273.15f) * c0 / c1 - 273.15f; }
 
 // Temperature and frozen share from the enthalpy temperature.
 DEV float2 phase_of(float te, float4 m) {

@@ -51,6 +51,7 @@ struct DevParams {
     int primary;
     uint32_t group_heat;
     int present[kMaxPresent];
+    int fams[kMaxPresent][2];   // per concentration family: its row, its diluent's row (-1 none)
     float heat[4], heat2[4], heat3[4];
     float sep_tau, cfl, tool_crowd_max, density_k, dt_max, crowd_jitter, ext_speed, wall_margin;
     float tool_pos[2], tool_vel[2], tool_radius;

@@ -62,6 +62,8 @@ __global__ void __launch_bounds__(256) k_grid_prep(DevScene d) {
         float T = P->heat[0], kappa = 0.0f, emis = 0.0f, frozen = 0.0f, Craw = 0.0f;
         int major = 0, top_row = -1;
         float top_share = 0.0f;
+        const int nmix = P->n_fam - 1;
+        for (int q = 0; q < nmix; q++) d.mixb[(size_t)i * nmix + q] = -1.0f;
         if (cw > 0) {
             int others = 0;
             for (int j = 0; j < P->n_present; j++) {
@@ -125,11 +127,14 @@ __global__ void __launch_bounds__(256) k_grid_prep(DevScene d) {
                 if (ia[1] >= 0) {
                     const float* da = mats[ia[1]].a;
                     rho_m = mixf(da[0], rho_m, sc);
+                    // blend_share(s, e) = s: every concentrate here blends with exponent 1
                     lnu = mixf(thermal ? da[1] + temp_law(mats, ia[1], Tm) : da[1], lnu, sc);
                     sig = mixf(da[2], sig, sc);
                     csx = mixf(mats[ia[1]].b[0], csx, sc);
                     csy = mixf(mats[ia[1]].b[1], csy, sc);
-                    if (mats[r].ib[0] == 0) fam0 = sc;
+                    const int fam = mats[r].ib[0];
+                    if (fam == 0) fam0 = sc;
+                    else if (fam > 0) d.mixb[(size_t)i * nmix + fam - 1] = sc;
                 }
                 rho_m *= xp;
                 if (thermal) {

@@ -313,6 +313,18 @@ SimParams::SimParams() {
     o.opacity = 0.25f; o.gloss = 1.0f; o.ior = 1.47f;
 }
 
+bool SimParams::set_diluent(int row, int diluent) {
+    if (row < kBuiltinCount || row >= kMaxMaterials) return false;
+    if (diluent == -1) {
+        mat[row].diluent = -1;
+        return true;
+    }
+    if (diluent < 0 || diluent >= kMaxMaterials || diluent == row) return false;
+    if (diluent < kBuiltinCount && mat[diluent].diluent >= 0) return false;
+    mat[row].diluent = diluent;
+    return true;
+}
+
 bool SimParams::set(const std::string& key, float v) {
     Found f = find(key);
     if (!f.g && !f.m) return false;
@@ -559,6 +571,12 @@ void build_params(const SimParams& p, const Tank& t, bool thermal, uint32_t caps
     P->group_mask = t.group_mask;
     P->caps = caps;
     P->primary = t.rows.empty() ? -1 : t.primary;
+    for (int j = 0; j < kMaxPresent; j++) P->fams[j][0] = P->fams[j][1] = -1;
+    for (size_t k = 0; k < t.rows.size(); k++)
+        if (t.chan[k][2] >= 0) {
+            P->fams[t.chan[k][2]][0] = t.rows[k];
+            P->fams[t.chan[k][2]][1] = p.mat[t.rows[k]].diluent;
+        }
     uint32_t gh = 0;
     for (int g = 0; g < 4; g++) gh += ((uint32_t)(t.chan_g[g] + 1) & 255u) << (8 * g);
     P->group_heat = gh;

@@ -95,6 +95,10 @@ struct SimParams {
     float dt_capillary(const std::vector<int>& rows) const;
     float dt_thermal(const std::vector<int>& rows) const;
     float enthalpy_temp(int row, float s, float t) const;
+    // A custom liquid's diluent as the library resolves it (library.rs:318-330): -1 (none),
+    // or another row that is a built-in without a diluent of its own or a custom liquid.
+    // False (nothing changed) for a built-in row or a diluent the library would not take.
+    bool set_diluent(int row, int diluent);
 };
 
 // Tank (mod.rs:222-245).

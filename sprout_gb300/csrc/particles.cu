@@ -247,10 +247,30 @@ __global__ void __launch_bounds__(256) k_advance(DevScene d) {
                     float fx = gx - (float)bx, fy = gy - (float)by;
                     float wx[3], wy[3];
                     bspline(fx, fy, wx, wy);
+                    // with concentration families: sw, the weight of the cells holding liquid;
+                    // sfw, sfs, the weight and concentration of those that hold the particle's
+                    // own family (a diluent's: family 0)
+                    const int fam = mats[row].ib[0];
+                    const int nmix = P->n_fam - 1;
+                    const bool fams = P->n_fam > 0;
+                    float sw = 0.0f, sfw = 0.0f, sfs = 0.0f;
 #pragma unroll
                     for (int b = 0; b < 3; b++)
 #pragma unroll
-                        for (int a = 0; a < 3; a++) crowd += wx[a] * wy[b] * __ldg(&d.comp[(by + b) * d.W + bx + a]).w;
+                        for (int a = 0; a < 3; a++) {
+                            const int ci = (by + b) * d.W + bx + a;
+                            const float4 q = __ldg(&d.comp[ci]);
+                            const float wt = wx[a] * wy[b];
+                            crowd += wt * q.w;
+                            if (fams && q.x > 0.0f) {
+                                sw += wt;
+                                const float sb = fam > 0 ? d.mixb[(size_t)ci * nmix + fam - 1] : q.z;
+                                if (sb >= 0.0f) {
+                                    sfw += wt;
+                                    sfs += wt * sb;
+                                }
+                            }
+                        }
                     if (thermal && (kind & KIND_FRESH) == 0u) {
                         float dT = 0.0f;
 #pragma unroll
@@ -266,6 +286,52 @@ __global__ void __launch_bounds__(256) k_advance(DevScene d) {
                             dT += own.y * (own.z - (float)hq.y / (float)hq.x) * T_SCALE;
                         }
                         pt += dT;
+                    }
+                    if (fams && sw > 1e-4f) {
+                        // Miscible exchange: the concentration relaxes towards its family's
+                        // local mean; the first row, the diluent of the primary family, takes
+                        // part as concentration 0 and becomes a particle of the family when it
+                        // gains any (particles.comp:519-543).
+                        const bool dil0 = fam < 0 && P->primary >= 0 && P->fams[0][1] == (int)row;
+                        if ((fam >= 0 || dil0) && sfw > 1e-4f) {
+                            const float s0 = dil0 ? 0.0f : ps;
+                            const float rate = mats[dil0 ? (uint32_t)P->primary : row].a[3];
+                            const float s1 = clampf(s0 + (sfs / sfw - s0) * (1.0f - sp_expf(-rate * dt)), 0.0f, 1.0f);
+                            const float c0 = thermal ? thermal_of(mats, row, ps).w : 0.0f;
+                            if (!dil0) {
+                                ps = s1;
+                            } else if (s1 > 0.0f) {
+                                row = (uint32_t)P->primary;
+                                ia1 = mats[row].ia[1];
+                                kind = (kind & ~255u) | (row + 1u);
+                                ps = s1;
+                            }
+                            if (thermal) pt = keep_heat(pt, c0, thermal_of(mats, row, ps).w);
+                        }
+                        // A pure diluent next to another of its concentrates joins that family
+                        // at concentration 0 (the same liquid): the primary family if it gained
+                        // some above, else the first family in table order found around it
+                        // (particles.comp:544-569).
+                        if (fam < 0 && (kind & 255u) - 1u == row && mats[row].ib[0] < 0) {
+                            for (int j = P->primary >= 0 ? 1 : 0; j < P->n_fam; j++) {
+                                if (P->fams[j][1] != (int)row) continue;
+                                float found = 0.0f;
+                                if (j == 0) {
+                                    found = sfw;
+                                } else {
+                                    for (int b = 0; b < 3; b++)
+                                        for (int a = 0; a < 3; a++)
+                                            if (d.mixb[(size_t)((by + b) * d.W + bx + a) * nmix + j - 1] >= 0.0f) found += wx[a] * wy[b];
+                                }
+                                if (found > 1e-4f) {
+                                    row = (uint32_t)P->fams[j][0];
+                                    ia1 = mats[row].ia[1];
+                                    kind = (kind & ~255u) | (row + 1u);
+                                    ps = 0.0f;
+                                    break;
+                                }
+                            }
+                        }
                     }
                 }
                 bool pushed = false;

@@ -619,9 +619,7 @@ struct SproutSim {
         thermal = th;
         caps = compute_caps();
         int rc = SPROUT_OK;
-        if (tank.families > 0)
-            rc = fail(SPROUT_E_UNSUPPORTED, "concentration families (a material with a diluent) are not carried by this engine yet");
-        else if (caps & (CAP_RIGID | CAP_RHEO | CAP_MAGNET | CAP_ELASTIC | CAP_SETTLE | CAP_STEAM | CAP_REACT))
+        if (caps & (CAP_RIGID | CAP_RHEO | CAP_MAGNET | CAP_ELASTIC | CAP_SETTLE | CAP_STEAM | CAP_REACT))
             rc = fail(SPROUT_E_UNSUPPORTED, "the tank needs rigid / rheology / magnet / elastic / settling / steam / reaction passes, which this engine does not carry");
         else if (__builtin_popcount(tank.group_mask) > 1)
             rc = fail(SPROUT_E_UNSUPPORTED, "several phase groups in one tank (drift, pair tension) are not carried by this engine yet");
@@ -629,6 +627,11 @@ struct SproutSim {
             const MatProps& m = params.mat[r];
             if (rc == SPROUT_OK && (m.volatility > 0.0f || (thermal && m.boil < 1e8f)))
                 rc = fail(SPROUT_E_UNSUPPORTED, "evaporation and boiling are not carried by this engine");
+        }
+        if (rc == SPROUT_OK && tank.families > 1 && d.mixb == nullptr) {
+            // the concentrations of families 1.. per cell, from the first tank that has them
+            rc = alloc(&d.mixb, (size_t)W * H * (kMaxPresent - 1));
+            graph_ok = false;   // new device pointers: the captured substep is stale
         }
         if (rc == SPROUT_OK) rc = derive_viscosity();
         if (rc != SPROUT_OK) {
@@ -1382,6 +1385,11 @@ int sprout_params_set(SproutParams* p, const char* key, float v, int* ok) {
     *ok = p->p.set(key, v) ? 1 : 0;
     return SPROUT_OK;
 }
+int sprout_params_set_diluent(SproutParams* p, uint32_t row, int32_t diluent, int* ok) {
+    if (!p || !ok) return fail(SPROUT_E_ARG, "null argument");
+    *ok = p->p.set_diluent((int)row, (int)diluent) ? 1 : 0;
+    return SPROUT_OK;
+}
 int sprout_params_get(const SproutParams* p, const char* key, float* v, int* ok) {
     if (!p || !key || !v || !ok) return fail(SPROUT_E_ARG, "null argument");
     *ok = p->p.get(key, v) ? 1 : 0;
@@ -1631,6 +1639,7 @@ int sprout_sim_download_field(SproutSim* sim, const char* name, void* out, size_
     else if (n == "mgz") { src = d.mgz; b = (size_t)d.lv.total * 8; }
     else if (n == "ptile") { src = d.ptile; b = (size_t)d.lv.tiles * 4; }
     else if (n == "p2keep") { src = d.p2keep; b = nc * 4; }
+    else if (d.mixb && n == "mixb") { src = d.mixb; b = nc * 4 * (size_t)std::max(sim->tank.families - 1, 0); }
     else if (sim->visc_alloc && n == "tiles") { src = d.tiles; b = (size_t)d.nwg * 4; }
     else if (sim->visc_alloc && n == "vtile") { src = d.vtile; b = (size_t)d.lv.tiles * 4; }
     else if (sim->visc_alloc && n == "vd") { src = d.vd; b = nc * 8; }

@@ -19,11 +19,15 @@ class Tank:
     shapes: list = field(default_factory=list)      # dicts: kind box/circle, c, half/r, angle, temp
     fills: list = field(default_factory=list)       # (rect, material row, temperature or None)
     capacity_extra: int = 64
+    diluents: dict = field(default_factory=dict)    # custom row -> its diluent's row (a family)
 
     # ---- the engine -----------------------------------------------------------------------
     def engine(self):
         import sprout_gb300 as S
         p = S.SimParams(self.settings)
+        for row, dil in self.diluents.items():
+            if not p.set_diluent(row, dil):
+                raise ValueError(f"row {row} cannot take diluent {dil}")
         sc = S.Scene(self.w, self.h)
         for s in self.shapes:
             if s["kind"] == "box":
@@ -101,15 +105,27 @@ STRATIFIED_LAYERS = [
 
 
 def stratified(w: int = 512, h: int = 288, cell: float = 0.002, tol: float = 1e-5,
-               extra: dict | None = None) -> Tank:
+               extra: dict | None = None, honey_family: bool = False) -> Tank:
     """Honey, water and olive oil stacked bottom to top, each 20% of the height (the second
-    configuration at 512 x 288); the honey layer takes the implicit viscosity solve."""
+    configuration at 512 x 288); the honey layer takes the implicit viscosity solve.
+
+    Three custom liquids with the layers' properties by default. With `honey_family` the
+    bottom two layers are the built-in honey and water rows instead: honey is a water
+    concentrate (presets.rs:61-90), so the two exchange concentration at its mix rate
+    (1.5 / s) and water that gains some becomes honey at that concentration."""
     s = {"cell_size": cell, "fixed_hz": 240.0, "pressure_tol": tol, "viscosity_tol": tol}
+    rows = [59, 60, 61]
     for k, props in enumerate(STRATIFIED_LAYERS):
         for name, val in props.items():
             s[f"mat{59 + k}.{name}"] = val
+    if honey_family:
+        rows = [1, 0, 61]
+        for name, val in STRATIFIED_LAYERS[0].items():
+            s[f"{name}_honey"] = val
+        for name, val in STRATIFIED_LAYERS[1].items():
+            s[f"{name}_water"] = val
     s.update(extra or {})
-    fills = [([0.0, k * 0.2 * h, float(w), (k + 1) * 0.2 * h], 59 + k, None) for k in range(3)]
+    fills = [([0.0, k * 0.2 * h, float(w), (k + 1) * 0.2 * h], rows[k], None) for k in range(3)]
     return Tank(w, h, s, [], fills)
 
 

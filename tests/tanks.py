@@ -7,3 +7,32 @@ from sprout_gb300.workloads import Tank
 def oracle_of(tank: Tank):
     from oracle import oracle as O
     return O.build_tank(tank)
+
+
+def honey_dam(w: int = 96, h: int = 64, cell: float = 0.002, mix_rate: float | None = None) -> Tank:
+    """A water column falling onto a layer of the built-in honey (a water concentrate): the
+    two meet, exchange concentration, and water that gains some becomes honey."""
+    s = {"cell_size": cell, "fixed_hz": 240.0, "pressure_tol": 1e-5, "viscosity_tol": 1e-5,
+         "tension_water": 0.0, "tension_honey": 0.0, "viscosity_honey": 2e-4}
+    if mix_rate is not None:
+        s["mix_rate_honey"] = mix_rate
+    fills = [([0.0, 0.0, float(w), 0.3 * h], 1, None), ([0.0, 0.3 * h, 0.4 * w, 0.8 * h], 0, None)]
+    return Tank(w, h, s, [], fills)
+
+
+def families_tank(w: int = 96, h: int = 64, cell: float = 0.002) -> Tank:
+    """Three concentration families in one tank: honey in water (the primary family, 0), a
+    custom water concentrate (mat59, family 1) and a concentrate (mat61, family 2) of another
+    custom liquid (mat60), each block beside its diluent."""
+    s = {"cell_size": cell, "fixed_hz": 240.0, "pressure_tol": 1e-5, "viscosity_tol": 1e-5,
+         "tension_water": 0.0, "tension_honey": 0.0, "viscosity_honey": 2e-4}
+    for row, props in {59: {"density": 1200.0, "viscosity": 1e-4, "mix_rate": 2.0},
+                       60: {"density": 900.0, "viscosity": 1e-5},
+                       61: {"density": 1100.0, "viscosity": 5e-4, "mix_rate": 3.0}}.items():
+        for name, val in dict(props, tension=0.0).items():
+            s[f"mat{row}.{name}"] = val
+    sx, sy = w / 96.0, h / 64.0
+    box = lambda x0, y0, x1, y1: [x0 * sx, y0 * sy, x1 * sx, y1 * sy]
+    fills = [(box(48, 0, 96, 16), 1, None), (box(0, 0, 48, 16), 59, None), (box(0, 16, 30, 50), 0, None),
+             (box(60, 30, 90, 50), 60, None), (box(60, 16, 90, 30), 61, None)]
+    return Tank(w, h, s, [], fills, diluents={59: 0, 61: 60})
