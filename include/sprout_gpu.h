@@ -102,6 +102,11 @@ int sprout_params_get(const SproutParams* p, const char* key, float* v, int* ok)
  * liquid is then `s` parts itself and 1 - s parts the diluent (a concentration family).
  * *ok = 0 and nothing changes for a built-in row or a diluent the loader would drop. */
 int sprout_params_set_diluent(SproutParams* p, uint32_t row, int32_t diluent, int* ok);
+/* The phase group of custom liquid `row` (59..95), as the library's loader reads a liquid's
+ * "group" (src/library.rs:283-286): 0 aqueous, 1 oil-like, 2 metal, 3 silicate. Liquids of
+ * different groups are immiscible: they drift apart and meet at interfaces with the pair
+ * tension of their groups. *ok = 0 and nothing changes for a built-in row or another group. */
+int sprout_params_set_group(SproutParams* p, uint32_t row, uint32_t group, int* ok);
 
 /* ---- scene: Scene (src/scene.rs) ---------------------------------------------------- */
 int sprout_scene_new(uint32_t w, uint32_t h, SproutScene** out);

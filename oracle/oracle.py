@@ -336,6 +336,8 @@ def build_tank(tank, threads: int | None = None):
         apply_setting(p, k, v)
     for row, dil in getattr(tank, "diluents", {}).items():
         p.mat[row].diluent = dil
+    for row, grp in getattr(tank, "groups", {}).items():
+        p.mat[row].group = grp
     sdf, solid, region, temp = rasterize(tank.w, tank.h, tank.shapes)
     parts = None
     for rect, mat, t in tank.fills:

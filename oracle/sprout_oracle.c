@@ -646,6 +646,7 @@ struct OSim {
     /* grid */
     int32_t* acc;
     V4 *vel, *cell, *comp, *coef, *sprop, *surf, *surf2, *aux, *grho, *therm, *dheat, *vw, *vs, *prhs;
+    V4* gbase;   /* per cell: share x base density of phase groups 1 - 3 (grid_prep.comp:53, 172, 247) */
     V2 *vel0, *pjump, *pres;
     float* p2keep;
     float* mixb;   /* per cell, families 1 .. n_fam - 1: the concentration (-1: not here) */
@@ -1033,6 +1034,30 @@ static float row_density(const OSim* s, uint32_t row, float sc) {   /* common.gl
     return d >= 0 ? mixf(s->mats[d].a[0], rho, sc) : rho;
 }
 
+/* common.glsl:590-602: whether phase group g drifts within itself (two or more plain liquids
+ * of the group in the tank, and no concentrate in or of it) */
+static int group_sorts(const OSim* s, int g) {
+    if (g <= 0) return 0;
+    int n = 0;
+    for (int j = 0; j < P_.n_present; j++) {
+        const int* ia = s->mats[P_.present[j]].ia;
+        if (ia[1] >= 0 && s->mats[ia[1]].ia[0] == g) return 0;
+        if (ia[0] != g) continue;
+        if (ia[1] >= 0) return 0;
+        n++;
+    }
+    return n >= 2;
+}
+
+/* common.glsl:370-374: terminal velocity of a droplet, drag 24 / Re + 0.44 */
+static float terminal(const OSim* s, float drho, float rho_c, float nu_c, float d) {
+    float qa = 0.44f * rho_c, qb = 24.0f * nu_c * rho_c / d, qc = 4.0f / 3.0f * fabsf(drho) * P_.gravity * d;
+    return qc > 0.0f ? 2.0f * qc / (qb + sqrtf(qb * qb + 4.0f * qa * qc)) : 0.0f;
+}
+
+static float v4c(V4 v, int k) { return k == 0 ? v.x : k == 1 ? v.y : k == 2 ? v.z : v.w; }
+static int lead4(V4 f) { return f.x >= maxf(f.y, maxf(f.z, f.w)) ? 0 : f.y >= maxf(f.z, f.w) ? 1 : f.z >= f.w ? 2 : 3; }
+
 static float expansion_of(const OSim* s, uint32_t row, float sc, float T) {   /* common.glsl:485-494 */
     const GMat* m = &s->mats[row];
     int d = m->ia[1];
@@ -1348,6 +1373,11 @@ static void advance(OSim* s, uint32_t id, int gather, Scat* g) {
              * those holding the particle's own family (a diluent's: family 0) */
             float sw = 0.0f, sfw = 0.0f, sfs = 0.0f;
             const int nmix = P_.n_fam - 1;
+            /* sg: shares of groups 1 - 3; sbg: share x base density of the particle's group */
+            float sg[3] = {0.0f, 0.0f, 0.0f}, sbg = 0.0f;
+            const int more = (P_.group_mask & 12u) != 0u;
+            const int groups = (P_.group_mask & (P_.group_mask - 1u)) != 0u;
+            const int sorts = group_sorts(s, Mia[0]);
             for (int b = 0; b < 3; b++)
                 for (int a = 0; a < 3; a++) {
                     int ci = cidx(s, bx + a, by + b);
@@ -1356,6 +1386,12 @@ static void advance(OSim* s, uint32_t id, int gather, Scat* g) {
                     crowd += wt * q.w;
                     if (q.x > 0.0f) {
                         sw += wt;
+                        sg[0] += wt * q.y;
+                        if (more) {
+                            sg[1] += wt * s->aux[ci].z;
+                            sg[2] += wt * s->aux[ci].w;
+                        }
+                        if (sorts) sbg += wt * v4c(s->gbase[ci], Mia[0] - 1);
                         float sb = fam > 0 ? s->mixb[(size_t)ci * nmix + fam - 1] : q.z;
                         if (sb >= 0.0f) {
                             sfw += wt;
@@ -1378,6 +1414,80 @@ static void advance(OSim* s, uint32_t id, int gather, Scat* g) {
                 p.t += dT;
             }
             if (sw > 1e-4f) {
+                /* drift between immiscible phase groups (particles.comp:374-476) */
+                for (int q = 0; q < 3; q++) sg[q] /= sw;
+                int g = Mia[0];
+                float fg = g == 0 ? 1.0f - sg[0] - sg[1] - sg[2] : sg[g - 1];
+                float others = 1.0f - fg;
+                if (others > 1e-4f && groups) {
+                    V4 sgr = v4(0.0f, 0.0f, 0.0f, 0.0f), snu = sgr, snw = sgr;
+                    for (int b = 0; b < 3; b++)
+                        for (int a = 0; a < 3; a++) {
+                            int ci = cidx(s, bx + a, by + b);
+                            V4 q = s->comp[ci];
+                            if (q.x <= 0.0f) continue;
+                            float wt = w[a].x * w[b].y;
+                            V4 gr = s->grho[ci];
+                            sgr.x += wt * gr.x; sgr.y += wt * gr.y; sgr.z += wt * gr.z; sgr.w += wt * gr.w;
+                            V4 ax = s->aux[ci];
+                            V4 fc = v4(1.0f - q.y - ax.z - ax.w, q.y, ax.z, ax.w);
+                            float top = maxf(maxf(fc.x, fc.y), maxf(fc.z, fc.w));
+                            V4 oh = v4(fc.x == top ? 1.0f : 0.0f, fc.y == top ? 1.0f : 0.0f, fc.z == top ? 1.0f : 0.0f, fc.w == top ? 1.0f : 0.0f);
+                            float on = maxf(oh.x + oh.y + oh.z + oh.w, 1.0f);
+                            oh = v4(oh.x / on, oh.y / on, oh.z / on, oh.w / on);
+                            float wn = wt * ax.x;
+                            snu.x += wn * oh.x; snu.y += wn * oh.y; snu.z += wn * oh.z; snu.w += wn * oh.w;
+                            snw.x += wt * oh.x; snw.y += wt * oh.y; snw.z += wt * oh.z; snw.w += wt * oh.w;
+                        }
+                    sgr = v4(sgr.x / sw, sgr.y / sw, sgr.z / sw, sgr.w / sw);
+                    float rho_g = fg > 1e-4f ? v4c(sgr, g) / fg : row_density(s, row, p.s);
+                    float rho_o = (sgr.x + sgr.y + sgr.z + sgr.w - v4c(sgr, g)) / others;
+                    float drho = rho_g - rho_o;
+                    int W = s->W;
+                    int k = clampi((int)pos.y, 1, s->H - 2) * W + clampi((int)pos.x, 1, W - 2);
+                    V4 fsv = v4(1.0f - sg[0] - sg[1] - sg[2], sg[0], sg[1], sg[2]);
+                    int G = lead4(fsv);
+                    float rho_c = v4c(sgr, G) / maxf(v4c(fsv, G), 1e-4f);
+                    float nu_c = v4c(snw, G) > 1e-6f ? v4c(snu, G) / v4c(snw, G) : s->aux[k].x;
+                    float vt = terminal(s, drho, rho_c, nu_c, P_.sep_tau);
+                    float sep_max = P_.corr[2] > 0.0f ? P_.cfl / dt : 1e30f;
+                    slip = -minf(vt, sep_max) * signf(drho) * others;
+                    V4 fs = fsv;
+                    if (g == 0) fs.x = -1.0f; else if (g == 1) fs.y = -1.0f; else if (g == 2) fs.z = -1.0f; else fs.w = -1.0f;
+                    int h = lead4(fs);
+                    float bond = fabsf(drho) * P_.gravity / maxf(P_.pair[g][h], 1e-9f);
+                    float hold = clampf(1.0f - bond, 0.0f, 1.0f);
+                    if (slip != 0.0f && hold > 0.0f) {
+                        int hi = g > h ? g : h;
+                        float gx, gy;
+                        if (hi == 1) {
+                            gx = 0.5f * (s->surf[k + 1].y - s->surf[k - 1].y);
+                            gy = 0.5f * (s->surf[k + W].y - s->surf[k - W].y);
+                        } else if (hi == 2) {
+                            gx = 0.5f * (s->surf2[k + 1].x - s->surf2[k - 1].x);
+                            gy = 0.5f * (s->surf2[k + W].x - s->surf2[k - W].x);
+                        } else {
+                            gx = 0.5f * (s->surf2[k + 1].y - s->surf2[k - 1].y);
+                            gy = 0.5f * (s->surf2[k + W].y - s->surf2[k - W].y);
+                        }
+                        float resolved = 1.0f - clampf((0.12f - len2(v2(gx, gy))) / (0.12f - 0.04f), 0.0f, 1.0f);
+                        slip *= 1.0f - hold * resolved;
+                    }
+                }
+                /* drift within a phase group (particles.comp:478-502) */
+                if (sorts) {
+                    float fgi = groups ? sg[Mia[0] - 1] : 1.0f;
+                    if (fgi > 1e-4f) {
+                        float rmean = sbg / sw / fgi;
+                        float drho = s->mats[row].a[0] - rmean;
+                        int pcx = clampi((int)pos.x, 0, s->W - 1), pcy = clampi((int)pos.y, 0, s->H - 1);
+                        V4 cq = s->cell[cidx(s, pcx, pcy)];
+                        float nu_c = cq.y > 0.0f ? cq.z / cq.y : s->aux[cidx(s, pcx, pcy)].x;
+                        float vt = terminal(s, drho, rmean, nu_c, P_.sep_tau);
+                        float sep_max = P_.corr[2] > 0.0f ? P_.cfl / dt : 1e30f;
+                        slip -= minf(vt, sep_max) * signf(drho);
+                    }
+                }
                 /* miscible exchange within a family (particles.comp:519-543) */
                 int diluent0 = fam < 0 && P_.primary >= 0 && P_.fams[0][1] == (int)row;
                 if (fam >= 0 || diluent0) {
@@ -1717,6 +1827,7 @@ static void k_grid_prep(OSim* s) {
             int thermal = has_cap(s, CAP_THERMAL);
             const int nmix = P_.n_fam - 1;   /* grid_prep.comp:67-68 */
             for (int q = 0; q < nmix; q++) s->mixb[(size_t)i * nmix + q] = -1.0f;
+            float bg[3] = {0.0f, 0.0f, 0.0f};   /* share x base density of groups 1 - 3 */
             float T = P_.heat[0], kappa = 0.0f, emis = 0.0f, frozen = 0.0f, Craw = 0.0f;
             int major = 0, top_row = -1;
             float top_share = 0.0f;
@@ -1791,6 +1902,7 @@ static void k_grid_prep(OSim* s) {
                         top_row = r;
                     }
                     int g = ia[0];
+                    if (g > 0) bg[g - 1] += share * ma[0];   /* grid_prep.comp:172 */
                     f[g] += share;
                     rg[g] += share * rho_m;
                     lg[g] += share * lnu;
@@ -1820,6 +1932,7 @@ static void k_grid_prep(OSim* s) {
             if (sol.w > 0.0f && level <= 0.0f) region_air |= 1u << (s->region[i] & REGION_MASK);
             s->cell[i] = v4(phi_f, rho, mu, level);
             s->comp[i] = v4(rho, f[1], fam0, phi_t);
+            if (group_sorts(s, 1) || group_sorts(s, 2) || group_sorts(s, 3)) s->gbase[i] = v4(bg[0], bg[1], bg[2], 0.0f);
             if ((P_.group_mask & (P_.group_mask - 1u)) != 0u) {
                 s->aux[i] = v4(nu_c, rho_c, f[2], f[3]);
                 s->grho[i] = v4(rg[0], rg[1], rg[2], rg[3]);
@@ -3825,6 +3938,7 @@ OSim* osim_create(int w, int h, uint32_t capacity, const OSimParams* p) {
     ALLOC(s->grho, nc); ALLOC(s->therm, nc); ALLOC(s->dheat, nc); ALLOC(s->vw, nc);
     ALLOC(s->vs, nc); ALLOC(s->prhs, nc); ALLOC(s->vel0, nc); ALLOC(s->pjump, nc);
     ALLOC(s->mixb, nc * (MAX_PRESENT - 1));
+    ALLOC(s->gbase, nc);
     ALLOC(s->pres, nc); ALLOC(s->p2keep, nc); ALLOC(s->hcell, nc); ALLOC(s->solid, nc);
     ALLOC(s->sdf, (size_t)(w + 1) * (h + 1)); ALLOC(s->region, nc); ALLOC(s->solid_t, nc);
     ALLOC(s->mga, s->lv.total); ALLOC(s->mgd, s->lv.total); ALLOC(s->mgx, s->lv.total);
@@ -3849,7 +3963,7 @@ void osim_destroy(OSim* s) {
                     s->vel0, s->pjump, s->pres, s->p2keep, s->hcell, s->solid, s->sdf, s->region,
                     s->solid_t, s->mga, s->mgd, s->mgx, s->mgz, s->mgr, s->cgp, s->cgp2, s->cgq,
                     s->ptile, s->part, s->vr, s->vr2, s->vp, s->vq, s->vq2, s->vd, s->vaz, s->vma,
-                    s->vmb, s->vmd, s->vmr, s->vmx, s->vmz, s->tiles, s->vtile, s->pending, s->mixb};
+                    s->vmb, s->vmd, s->vmr, s->vmx, s->vmz, s->tiles, s->vtile, s->pending, s->mixb, s->gbase};
     for (size_t k = 0; k < sizeof ptrs / sizeof ptrs[0]; k++) free(ptrs[k]);
     free(s);
 }
@@ -3953,7 +4067,6 @@ static int set_tank(OSim* s, const int* present, int thermal) {
     s->caps = compute_caps(s);
     int rc = 0;
     if (s->caps & (CAP_RIGID | CAP_RHEO | CAP_MAGNET | CAP_ELASTIC | CAP_SETTLE | CAP_STEAM | CAP_REACT)) rc = -4;
-    if (__builtin_popcount(t.group_mask) > 1) rc = -4;
     for (int k = 0; k < nrows; k++) {
         const OMat* m = &p->mat[rows[k]];
         if (m->volatility > 0.0f || (thermal && m->boil < 1e8f)) rc = -4;
@@ -4138,6 +4251,10 @@ long osim_field(const OSim* s, const char* name, void* out, size_t cap) {
     F("ptile", s->ptile, (size_t)s->lv.tiles * 4)
     F("p2keep", s->p2keep, nc * 4)
     F("mixb", s->mixb, nc * 4 * (size_t)(s->P.n_fam > 1 ? s->P.n_fam - 1 : 0))
+    F("aux", s->aux, nc * 16)
+    F("grho", s->grho, nc * 16)
+    F("gbase", s->gbase, nc * 16)
+    F("surf2", s->surf2, nc * 16)
     F("tiles", s->tiles, (size_t)s->nwg * 4)
     F("vtile", s->vtile, (size_t)s->lv.tiles * 4)
     F("vd", s->vd, nc * 8)

@@ -33,7 +33,7 @@ ERRORS = {
 # Every entry point include/sprout_gpu.h declares.
 EXPORTS = [
     "sprout_last_error", "sprout_version", "sprout_params_new", "sprout_params_free", "sprout_params_copy",
-    "sprout_params_set", "sprout_params_get", "sprout_params_set_diluent", "sprout_scene_new", "sprout_scene_free", "sprout_scene_add_box",
+    "sprout_params_set", "sprout_params_get", "sprout_params_set_diluent", "sprout_params_set_group", "sprout_scene_new", "sprout_scene_free", "sprout_scene_add_box",
     "sprout_scene_add_circle", "sprout_scene_sdf", "sprout_scene_rasterize", "sprout_fill_rect",
     "sprout_sim_create", "sprout_sim_destroy", "sprout_sim_set_params", "sprout_sim_set_solids",
     "sprout_sim_reset", "sprout_sim_step", "sprout_sim_step_blocking", "sprout_sim_advance_blocking",
@@ -106,6 +106,7 @@ def lib() -> C.CDLL:
         "sprout_params_set": ([V, C.c_char_p, C.c_float, P(C.c_int)], C.c_int),
         "sprout_params_get": ([V, C.c_char_p, P(C.c_float), P(C.c_int)], C.c_int),
         "sprout_params_set_diluent": ([V, C.c_uint32, C.c_int32, P(C.c_int)], C.c_int),
+        "sprout_params_set_group": ([V, C.c_uint32, C.c_uint32, P(C.c_int)], C.c_int),
         "sprout_scene_new": ([C.c_uint32, C.c_uint32, P(V)], C.c_int), "sprout_scene_free": ([V], C.c_int),
         "sprout_scene_add_box": ([V] + [C.c_float] * 6, C.c_int),
         "sprout_scene_add_circle": ([V] + [C.c_float] * 4, C.c_int),
@@ -186,6 +187,13 @@ class SimParams:
         False for a built-in row or a diluent the loader would drop."""
         ok = C.c_int()
         _check(lib().sprout_params_set_diluent(self._h, int(row), int(diluent), C.byref(ok)))
+        return bool(ok.value)
+
+    def set_group(self, row: int, group: int) -> bool:
+        """A custom liquid's phase group as the library's loader reads it (library.rs:283-286):
+        0 aqueous, 1 oil-like, 2 metal, 3 silicate; False for a built-in row."""
+        ok = C.c_int()
+        _check(lib().sprout_params_set_group(self._h, int(row), int(group), C.byref(ok)))
         return bool(ok.value)
 
     def get(self, key: str) -> float:

@@ -61,6 +61,7 @@ struct DevScene {
     float2 *vel0, *pjump, *pres;
     float* p2keep;
     float* mixb;      // per cell, families 1 .. n_fam - 1: the family's concentration (-1: not here)
+    float4* gbase;    // per cell: share x base density of phase groups 1 - 3 (w unused)
     int2* hcell;
     const float4* solid;
     const float* sdf;
@@ -101,6 +102,15 @@ DEV float clampf(float x, float lo, float hi) { return minf(maxf(x, lo), hi); }
 DEV int clampi(int x, int lo, int hi) { return min(max(x, lo), hi); }
 DEV float mixf(float x, float y, float a) { return x * (1.0f - a) + y * a; }
 DEV float len2(float x, float y) { return sqrtf(x * x + y * y); }
+// GLSL sign(x): -1, 0 or 1.
+DEV float signf(float x) { return x > 0.0f ? 1.0f : (x < 0.0f ? -1.0f : 0.0f); }
+// The terminal velocity (cells / s) of a droplet of diameter d (cells) and density difference
+// drho in a liquid of density rho_c and kinematic viscosity nu_c, drag C_d = 24 / Re + 0.44:
+// the positive root of 0.44 rho_c v^2 + 24 nu_c rho_c v / d = 4/3 |drho| g d (common.glsl:370-374).
+DEV float terminal(float drho, float rho_c, float nu_c, float d, float gravity) {
+    const float qa = 0.44f * rho_c, qb = 24.0f * nu_c * rho_c / d, qc = 4.0f / 3.0f * fabsf(drho) * gravity * d;
+    return qc > 0.0f ? 2.0f * qc / (qb + sqrtf(qb * qb + 4.0f * qa * qc)) : 0.0f;
+}
 DEV float smoothstepf(float e0, float e1, float x) {
     float t = clampf((x - e0) / (e1 - e0), 0.0f, 1.0f);
     return t * t * (3.0f - 2.0f * t);

@@ -52,6 +52,7 @@ struct DevParams {
     uint32_t group_heat;
     int present[kMaxPresent];
     int fams[kMaxPresent][2];   // per concentration family: its row, its diluent's row (-1 none)
+    uint32_t sorts;   // bit g: phase group g drifts within itself (group_sorts, common.glsl:590-602)
     float heat[4], heat2[4], heat3[4];
     float sep_tau, cfl, tool_crowd_max, density_k, dt_max, crowd_jitter, ext_speed, wall_margin;
     float tool_pos[2], tool_vel[2], tool_radius;

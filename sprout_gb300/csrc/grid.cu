@@ -64,6 +64,7 @@ __global__ void __launch_bounds__(256) k_grid_prep(DevScene d) {
         float top_share = 0.0f;
         const int nmix = P->n_fam - 1;
         for (int q = 0; q < nmix; q++) d.mixb[(size_t)i * nmix + q] = -1.0f;
+        float bg[3] = {0.0f, 0.0f, 0.0f};   // share x base density of groups 1 - 3
         if (cw > 0) {
             int others = 0;
             for (int j = 0; j < P->n_present; j++) {
@@ -152,6 +153,7 @@ __global__ void __launch_bounds__(256) k_grid_prep(DevScene d) {
                     top_row = r;
                 }
                 const int g = ia[0];
+                if (g > 0) bg[g - 1] += share * ma[0];
                 f[g] += share;
                 rg[g] += share * rho_m;
                 lg[g] += share * lnu;
@@ -181,6 +183,7 @@ __global__ void __launch_bounds__(256) k_grid_prep(DevScene d) {
         if (sol.w > 0.0f && level <= 0.0f) air_bits = 1u << (__ldg(&d.region[i]) & REGION_MASK);
         d.cell[i] = make_float4(phi_f, rho, mu, level);
         d.comp[i] = make_float4(rho, f[1], fam0, phi_t);
+        if (P->sorts != 0u) d.gbase[i] = make_float4(bg[0], bg[1], bg[2], 0.0f);
         if ((P->group_mask & (P->group_mask - 1u)) != 0u) {
             d.aux[i] = make_float4(nu_c, rho_c, f[2], f[3]);
             d.grho[i] = make_float4(rg[0], rg[1], rg[2], rg[3]);

@@ -325,6 +325,12 @@ bool SimParams::set_diluent(int row, int diluent) {
     return true;
 }
 
+bool SimParams::set_group(int row, int group) {
+    if (row < kBuiltinCount || row >= kMaxMaterials || group < 0 || group > 3) return false;
+    mat[row].group = (uint32_t)group;
+    return true;
+}
+
 bool SimParams::set(const std::string& key, float v) {
     Found f = find(key);
     if (!f.g && !f.m) return false;
@@ -571,6 +577,22 @@ void build_params(const SimParams& p, const Tank& t, bool thermal, uint32_t caps
     P->group_mask = t.group_mask;
     P->caps = caps;
     P->primary = t.rows.empty() ? -1 : t.primary;
+    // group_sorts (common.glsl:590-602): a group past the first with two or more plain liquids
+    // and no concentrate, nor any concentrate whose diluent is in it, sorts its materials
+    P->sorts = 0u;
+    for (int g = 1; g < 4; g++) {
+        int n = 0;
+        bool no = false;
+        for (int r : t.rows) {
+            const MatProps& m = p.mat[r];
+            const int mg = (int)std::min<uint32_t>(m.group, 3u);
+            if (m.diluent >= 0 && (int)std::min<uint32_t>(p.mat[m.diluent].group, 3u) == g) { no = true; break; }
+            if (mg != g) continue;
+            if (m.diluent >= 0) { no = true; break; }
+            n++;
+        }
+        if (!no && n >= 2) P->sorts |= 1u << g;
+    }
     for (int j = 0; j < kMaxPresent; j++) P->fams[j][0] = P->fams[j][1] = -1;
     for (size_t k = 0; k < t.rows.size(); k++)
         if (t.chan[k][2] >= 0) {

@@ -99,6 +99,9 @@ struct SimParams {
     // or another row that is a built-in without a diluent of its own or a custom liquid.
     // False (nothing changed) for a built-in row or a diluent the library would not take.
     bool set_diluent(int row, int diluent);
+    // A custom liquid's phase group as the library reads it (library.rs:283-286): 0 aqueous,
+    // 1 oil-like, 2 metal, 3 silicate. False (nothing changed) for a built-in row or another value.
+    bool set_group(int row, int group);
 };
 
 // Tank (mod.rs:222-245).

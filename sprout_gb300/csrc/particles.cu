@@ -198,6 +198,90 @@ DEV bool gather_face(const Grid& g, float px, float py, float& vel_out, float& c
     return false;
 }
 
+DEV float f4c(float4 v, int k) { return k == 0 ? v.x : k == 1 ? v.y : k == 2 ? v.z : v.w; }
+// The group that leads among shares f (the first of equals).
+DEV int lead4(float4 f) { return f.x >= maxf(f.y, maxf(f.z, f.w)) ? 0 : f.y >= maxf(f.z, f.w) ? 1 : f.z >= f.w ? 2 : 3; }
+
+// Drift between immiscible phase groups (particles.comp:374-476): the terminal velocity of a
+// droplet of the unresolved size (sep_tau cells) of the particle's group, against the others'
+// local mean density, in the continuous phase that leads around it, times the others' share;
+// held back where a resolved interface (a clear gradient of the smoothed share of the pair's
+// later group) has interfacial tension enough to keep droplets from shedding (cell Bond
+// number below 1). Returns the vertical slip (cells / s).
+DEV float group_drift(const DevScene& d, const DevMat* mats, uint32_t row, float ps, int grp, float px, float py,
+                      int bx, int by, const float wx[3], const float wy[3], float sw, float fg, float others,
+                      float sgx, float sgy, float sgz, float dt) {
+    const DevParams* P = d.P;
+    float4 sgr = make_float4(0.0f, 0.0f, 0.0f, 0.0f), snu = sgr, snw = sgr;   // share x density; viscosity of the majority group and its weight
+#pragma unroll
+    for (int b = 0; b < 3; b++)
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+            const int ci = (by + b) * d.W + bx + a;
+            const float4 q = __ldg(&d.comp[ci]);
+            if (q.x <= 0.0f) continue;
+            const float wt = wx[a] * wy[b];
+            const float4 gr = __ldg(&d.grho[ci]);
+            sgr.x += wt * gr.x;
+            sgr.y += wt * gr.y;
+            sgr.z += wt * gr.z;
+            sgr.w += wt * gr.w;
+            const float4 ax = __ldg(&d.aux[ci]);
+            const float4 fc = make_float4(1.0f - q.y - ax.z - ax.w, q.y, ax.z, ax.w);
+            const float top = maxf(maxf(fc.x, fc.y), maxf(fc.z, fc.w));
+            float4 oh = make_float4(fc.x == top ? 1.0f : 0.0f, fc.y == top ? 1.0f : 0.0f, fc.z == top ? 1.0f : 0.0f, fc.w == top ? 1.0f : 0.0f);
+            const float on = maxf(oh.x + oh.y + oh.z + oh.w, 1.0f);
+            oh = make_float4(oh.x / on, oh.y / on, oh.z / on, oh.w / on);
+            const float wn = wt * ax.x;
+            snu.x += wn * oh.x;
+            snu.y += wn * oh.y;
+            snu.z += wn * oh.z;
+            snu.w += wn * oh.w;
+            snw.x += wt * oh.x;
+            snw.y += wt * oh.y;
+            snw.z += wt * oh.z;
+            snw.w += wt * oh.w;
+        }
+    sgr = make_float4(sgr.x / sw, sgr.y / sw, sgr.z / sw, sgr.w / sw);
+    const float rho_g = fg > 1e-4f ? f4c(sgr, grp) / fg : row_density(mats, row, ps);
+    const float rho_o = (sgr.x + sgr.y + sgr.z + sgr.w - f4c(sgr, grp)) / others;
+    const float drho = rho_g - rho_o;
+    const int W = d.W;
+    const int k = clampi((int)py, 1, d.H - 2) * W + clampi((int)px, 1, W - 2);
+    const float4 fsv = make_float4(1.0f - sgx - sgy - sgz, sgx, sgy, sgz);
+    const int G = lead4(fsv);
+    const float rho_c = f4c(sgr, G) / maxf(f4c(fsv, G), 1e-4f);
+    const float nu_c = f4c(snw, G) > 1e-6f ? f4c(snu, G) / f4c(snw, G) : __ldg(&d.aux[k]).x;
+    const float vt = terminal(drho, rho_c, nu_c, P->sep_tau, P->gravity);
+    const float sep_max = P->corr[2] > 0.0f ? P->cfl / dt : 1e30f;
+    float slip = -minf(vt, sep_max) * signf(drho) * others;
+    float4 fs = fsv;
+    if (grp == 0) fs.x = -1.0f;
+    else if (grp == 1) fs.y = -1.0f;
+    else if (grp == 2) fs.z = -1.0f;
+    else fs.w = -1.0f;
+    const int h = lead4(fs);
+    const float bond = fabsf(drho) * P->gravity / maxf(P->pair[grp][h], 1e-9f);
+    const float hold = clampf(1.0f - bond, 0.0f, 1.0f);
+    if (slip != 0.0f && hold > 0.0f) {
+        const int hi = max(grp, h);
+        float gx, gy;
+        if (hi == 1) {
+            gx = 0.5f * (__ldg(&d.surf[k + 1]).y - __ldg(&d.surf[k - 1]).y);
+            gy = 0.5f * (__ldg(&d.surf[k + W]).y - __ldg(&d.surf[k - W]).y);
+        } else if (hi == 2) {
+            gx = 0.5f * (__ldg(&d.surf2[k + 1]).x - __ldg(&d.surf2[k - 1]).x);
+            gy = 0.5f * (__ldg(&d.surf2[k + W]).x - __ldg(&d.surf2[k - W]).x);
+        } else {
+            gx = 0.5f * (__ldg(&d.surf2[k + 1]).y - __ldg(&d.surf2[k - 1]).y);
+            gy = 0.5f * (__ldg(&d.surf2[k + W]).y - __ldg(&d.surf2[k - W]).y);
+        }
+        const float resolved = 1.0f - clampf((0.12f - len2(gx, gy)) / (0.12f - 0.04f), 0.0f, 1.0f);
+        slip *= 1.0f - hold * resolved;
+    }
+    return slip;
+}
+
 __global__ void __launch_bounds__(256) k_advance(DevScene d) {
     const DevParams* P = d.P;
     const StepState* S = d.S;
@@ -222,7 +306,7 @@ __global__ void __launch_bounds__(256) k_advance(DevScene d) {
             if (S->gather) {
                 Grid g{d.vel, d.sdf, d.W, d.H};
                 float vx = pvx, vy = pvy, corrx = 0.0f, corry = 0.0f;
-                const float slip = 0.0f;
+                float slip = 0.0f;   // vertical drift relative to the mixture (cells / s)
                 float crowd = 0.0f;
                 gather_face<0>(g, px, py, vx, corrx, C.x, C.y);
                 gather_face<1>(g, px, py, vy, corry, C.z, C.w);
@@ -253,7 +337,15 @@ __global__ void __launch_bounds__(256) k_advance(DevScene d) {
                     const int fam = mats[row].ib[0];
                     const int nmix = P->n_fam - 1;
                     const bool fams = P->n_fam > 0;
-                    float sw = 0.0f, sfw = 0.0f, sfs = 0.0f;
+                    // with several phase groups: sg, the shares of groups 1 - 3 around the
+                    // particle; with a group that sorts its materials, sbg, share x base density
+                    // of the particle's group
+                    const int grp = mats[row].ia[0];
+                    const uint32_t gm = P->group_mask;
+                    const bool groups = (gm & (gm - 1u)) != 0u, more = (gm & 12u) != 0u;
+                    const bool sorts = grp > 0 && ((P->sorts >> grp) & 1u) != 0u;
+                    const bool gather = fams || groups || sorts;
+                    float sw = 0.0f, sfw = 0.0f, sfs = 0.0f, sg0 = 0.0f, sg1 = 0.0f, sg2 = 0.0f, sbg = 0.0f;
 #pragma unroll
                     for (int b = 0; b < 3; b++)
 #pragma unroll
@@ -262,8 +354,17 @@ __global__ void __launch_bounds__(256) k_advance(DevScene d) {
                             const float4 q = __ldg(&d.comp[ci]);
                             const float wt = wx[a] * wy[b];
                             crowd += wt * q.w;
-                            if (fams && q.x > 0.0f) {
+                            if (gather && q.x > 0.0f) {
                                 sw += wt;
+                                sg0 += wt * q.y;
+                                if (more) {
+                                    const float4 ax = __ldg(&d.aux[ci]);
+                                    sg1 += wt * ax.z;
+                                    sg2 += wt * ax.w;
+                                }
+                                if (sorts) sbg += wt * f4c(__ldg(&d.gbase[ci]), grp - 1);
+                            }
+                            if (fams && q.x > 0.0f) {
                                 const float sb = fam > 0 ? d.mixb[(size_t)ci * nmix + fam - 1] : q.z;
                                 if (sb >= 0.0f) {
                                     sfw += wt;
@@ -286,6 +387,28 @@ __global__ void __launch_bounds__(256) k_advance(DevScene d) {
                             dT += own.y * (own.z - (float)hq.y / (float)hq.x) * T_SCALE;
                         }
                         pt += dT;
+                    }
+                    if (gather && sw > 1e-4f) {
+                        const float sgx = sg0 / sw, sgy = sg1 / sw, sgz = sg2 / sw;
+                        const float fg = grp == 0 ? 1.0f - sgx - sgy - sgz : (grp == 1 ? sgx : grp == 2 ? sgy : sgz);
+                        const float others = 1.0f - fg;
+                        if (others > 1e-4f && groups)
+                            slip = group_drift(d, mats, row, ps, grp, px, py, bx, by, wx, wy, sw, fg, others, sgx, sgy, sgz, dt);
+                        if (sorts) {
+                            // drift within the particle's own group against its local mean base
+                            // density (particles.comp:478-502)
+                            const float fgi = groups ? (grp == 1 ? sgx : grp == 2 ? sgy : sgz) : 1.0f;
+                            if (fgi > 1e-4f) {
+                                const float rmean = sbg / sw / fgi;
+                                const float drho = mats[row].a[0] - rmean;
+                                const int pcx = clampi((int)px, 0, d.W - 1), pcy = clampi((int)py, 0, d.H - 1);
+                                const float4 cq = __ldg(&d.cell[pcy * d.W + pcx]);
+                                const float nu_c = cq.y > 0.0f ? cq.z / cq.y : __ldg(&d.aux[pcy * d.W + pcx]).x;
+                                const float vt = terminal(drho, rmean, nu_c, P->sep_tau, P->gravity);
+                                const float sep_max = P->corr[2] > 0.0f ? P->cfl / dt : 1e30f;
+                                slip -= minf(vt, sep_max) * signf(drho);
+                            }
+                        }
                     }
                     if (fams && sw > 1e-4f) {
                         // Miscible exchange: the concentration relaxes towards its family's

@@ -265,7 +265,7 @@ struct SproutSim {
         A(d.scan_tmp, (nc + 1 + 1023) / 1024 + 1);
         A(d.acc, nc * 32);
         A(d.vel, nc); A(d.cell, nc); A(d.comp, nc); A(d.coef, nc); A(d.sprop, nc); A(d.surf, nc);
-        A(d.surf2, nc); A(d.aux, nc); A(d.grho, nc); A(d.therm, nc); A(d.dheat, nc); A(d.vw, nc);
+        A(d.surf2, nc); A(d.aux, nc); A(d.grho, nc); A(d.gbase, nc); A(d.therm, nc); A(d.dheat, nc); A(d.vw, nc);
         A(d.vs, nc); A(d.prhs, nc); A(d.vel0, nc); A(d.pjump, nc); A(d.pres, nc); A(d.p2keep, nc);
         A(d.hcell, nc);
         float4* solid;
@@ -621,8 +621,6 @@ struct SproutSim {
         int rc = SPROUT_OK;
         if (caps & (CAP_RIGID | CAP_RHEO | CAP_MAGNET | CAP_ELASTIC | CAP_SETTLE | CAP_STEAM | CAP_REACT))
             rc = fail(SPROUT_E_UNSUPPORTED, "the tank needs rigid / rheology / magnet / elastic / settling / steam / reaction passes, which this engine does not carry");
-        else if (__builtin_popcount(tank.group_mask) > 1)
-            rc = fail(SPROUT_E_UNSUPPORTED, "several phase groups in one tank (drift, pair tension) are not carried by this engine yet");
         for (int r : tank.rows) {
             const MatProps& m = params.mat[r];
             if (rc == SPROUT_OK && (m.volatility > 0.0f || (thermal && m.boil < 1e8f)))
@@ -1390,6 +1388,11 @@ int sprout_params_set_diluent(SproutParams* p, uint32_t row, int32_t diluent, in
     *ok = p->p.set_diluent((int)row, (int)diluent) ? 1 : 0;
     return SPROUT_OK;
 }
+int sprout_params_set_group(SproutParams* p, uint32_t row, uint32_t group, int* ok) {
+    if (!p || !ok) return fail(SPROUT_E_ARG, "null argument");
+    *ok = p->p.set_group((int)row, (int)group) ? 1 : 0;
+    return SPROUT_OK;
+}
 int sprout_params_get(const SproutParams* p, const char* key, float* v, int* ok) {
     if (!p || !key || !v || !ok) return fail(SPROUT_E_ARG, "null argument");
     *ok = p->p.get(key, v) ? 1 : 0;
@@ -1639,6 +1642,10 @@ int sprout_sim_download_field(SproutSim* sim, const char* name, void* out, size_
     else if (n == "mgz") { src = d.mgz; b = (size_t)d.lv.total * 8; }
     else if (n == "ptile") { src = d.ptile; b = (size_t)d.lv.tiles * 4; }
     else if (n == "p2keep") { src = d.p2keep; b = nc * 4; }
+    else if (n == "aux") { src = d.aux; b = nc * 16; }
+    else if (n == "grho") { src = d.grho; b = nc * 16; }
+    else if (n == "gbase") { src = d.gbase; b = nc * 16; }
+    else if (n == "surf2") { src = d.surf2; b = nc * 16; }
     else if (d.mixb && n == "mixb") { src = d.mixb; b = nc * 4 * (size_t)std::max(sim->tank.families - 1, 0); }
     else if (sim->visc_alloc && n == "tiles") { src = d.tiles; b = (size_t)d.nwg * 4; }
     else if (sim->visc_alloc && n == "vtile") { src = d.vtile; b = (size_t)d.lv.tiles * 4; }

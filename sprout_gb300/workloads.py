@@ -20,6 +20,7 @@ class Tank:
     fills: list = field(default_factory=list)       # (rect, material row, temperature or None)
     capacity_extra: int = 64
     diluents: dict = field(default_factory=dict)    # custom row -> its diluent's row (a family)
+    groups: dict = field(default_factory=dict)      # custom row -> its phase group (0-3)
 
     # ---- the engine -----------------------------------------------------------------------
     def engine(self):
@@ -28,6 +29,9 @@ class Tank:
         for row, dil in self.diluents.items():
             if not p.set_diluent(row, dil):
                 raise ValueError(f"row {row} cannot take diluent {dil}")
+        for row, grp in self.groups.items():
+            if not p.set_group(row, grp):
+                raise ValueError(f"row {row} cannot take phase group {grp}")
         sc = S.Scene(self.w, self.h)
         for s in self.shapes:
             if s["kind"] == "box":

@@ -36,3 +36,50 @@ def families_tank(w: int = 96, h: int = 64, cell: float = 0.002) -> Tank:
     fills = [(box(48, 0, 96, 16), 1, None), (box(0, 0, 48, 16), 59, None), (box(0, 16, 30, 50), 0, None),
              (box(60, 30, 90, 50), 60, None), (box(60, 16, 90, 30), 61, None)]
     return Tank(w, h, s, [], fills, diluents={59: 0, 61: 60})
+
+
+
+def around(rect, holes):
+    """Rectangles covering `rect` less the `holes` (x0, y0, x1, y1 in whole cells), so that
+    liquid filled around blocks of other liquids does not land on them (fill_rect does not
+    look at what is already there)."""
+    x0, y0, x1, y1 = rect
+    ys = sorted({y0, y1, *[v for hh in holes for v in (hh[1], hh[3]) if y0 < v < y1]})
+    out = []
+    for ya, yb in zip(ys, ys[1:]):
+        cuts = sorted((max(hh[0], x0), min(hh[2], x1)) for hh in holes if hh[1] <= ya and hh[3] >= yb and hh[0] < x1 and hh[2] > x0)
+        x = x0
+        for ca, cb in cuts:
+            if ca > x:
+                out.append([float(x), float(ya), float(ca), float(yb)])
+            x = max(x, cb)
+        if x < x1:
+            out.append([float(x), float(ya), float(x1), float(yb)])
+    return out
+
+
+def water_oil(w: int = 96, h: int = 64, cell: float = 0.002) -> Tank:
+    """A block of the built-in olive oil (phase group 1) under water: immiscible, it drifts
+    up through the water and meets it with the groups' pair tension."""
+    s = {"cell_size": cell, "fixed_hz": 240.0, "pressure_tol": 1e-5, "tension_water": 0.0, "tension_oil": 0.0}
+    oil = [int(0.3 * w), int(0.1 * h), int(0.6 * w), int(0.35 * h)]
+    fills = [([float(v) for v in oil], 2, None)]
+    fills += [(r, 0, None) for r in around([0, 0, w, int(0.6 * h)], [oil])]
+    return Tank(w, h, s, [], fills)
+
+
+def three_groups(w: int = 96, h: int = 64, cell: float = 0.002) -> Tank:
+    """Water with two oil-like custom liquids stacked in one block, the lighter below (group 1
+    sorts them by density), and a dense metal-like custom liquid (group 2) above: three
+    phase groups."""
+    s = {"cell_size": cell, "fixed_hz": 240.0, "pressure_tol": 1e-5, "viscosity_tol": 1e-5, "tension_water": 0.0}
+    for row, props in {59: {"density": 850.0, "viscosity": 5e-5}, 60: {"density": 960.0, "viscosity": 2e-5},
+                       61: {"density": 3000.0, "viscosity": 1e-6}}.items():
+        for name, val in dict(props, tension=0.0).items():
+            s[f"mat{row}.{name}"] = val
+    sx, sy = w / 96.0, h / 64.0
+    box = lambda x0, y0, x1, y1: [int(x0 * sx), int(y0 * sy), int(x1 * sx), int(y1 * sy)]
+    a, b, c = box(10, 4, 40, 14), box(10, 14, 40, 24), box(60, 26, 80, 36)
+    fills = [([float(v) for v in a], 59, None), ([float(v) for v in b], 60, None), ([float(v) for v in c], 61, None)]
+    fills += [(r, 0, None) for r in around([0, 0, w, int(36 * sy)], [a, b, c])]
+    return Tank(w, h, s, [], fills, groups={59: 1, 60: 1, 61: 2})
