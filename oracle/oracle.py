@@ -304,8 +304,16 @@ def _row(name: str) -> int:
     raise KeyError(name)
 
 
+PAIR_TENSIONS = {"tension_oil_water": (0, 1), "tension_metal_water": (0, 2), "tension_metal_oil": (1, 2),
+                 "tension_melt_water": (0, 3), "tension_melt_oil": (1, 3), "tension_melt_metal": (2, 3)}
+
+
 def apply_setting(p: OSimParams, key: str, v: float):
     """The oracle-side counterpart of SimParams::set for the names the workloads use."""
+    if key in PAIR_TENSIONS:
+        a, b = PAIR_TENSIONS[key]
+        p.pair_tension[a][b] = p.pair_tension[b][a] = float(v)
+        return
     prop = row = None
     if "." in key:
         mat, prop = key.split(".", 1)

@@ -109,25 +109,27 @@ STRATIFIED_LAYERS = [
 
 
 def stratified(w: int = 512, h: int = 288, cell: float = 0.002, tol: float = 1e-5,
-               extra: dict | None = None, honey_family: bool = False) -> Tank:
+               extra: dict | None = None, builtins: bool = False) -> Tank:
     """Honey, water and olive oil stacked bottom to top, each 20% of the height (the second
     configuration at 512 x 288); the honey layer takes the implicit viscosity solve.
 
-    Three custom liquids with the layers' properties by default. With `honey_family` the
-    bottom two layers are the built-in honey and water rows instead: honey is a water
-    concentrate (presets.rs:61-90), so the two exchange concentration at its mix rate
-    (1.5 / s) and water that gains some becomes honey at that concentration."""
+    Three custom liquids (one phase group, no exchange) with the layers' properties by
+    default. With `builtins` the layers are the built-in honey, water and olive oil rows with
+    those properties: honey is a water concentrate (presets.rs:61-90), so the two exchange
+    concentration at its mix rate (1.5 / s) and water that gains some becomes honey; olive oil
+    is phase group 1, immiscible, drifting against the water with no interfacial tension
+    (tension_oil_water 0: at 2 mm cells a tension would want substeps below the fixed 1/240 s)."""
     s = {"cell_size": cell, "fixed_hz": 240.0, "pressure_tol": tol, "viscosity_tol": tol}
     rows = [59, 60, 61]
     for k, props in enumerate(STRATIFIED_LAYERS):
         for name, val in props.items():
             s[f"mat{59 + k}.{name}"] = val
-    if honey_family:
-        rows = [1, 0, 61]
-        for name, val in STRATIFIED_LAYERS[0].items():
-            s[f"{name}_honey"] = val
-        for name, val in STRATIFIED_LAYERS[1].items():
-            s[f"{name}_water"] = val
+    if builtins:
+        rows = [1, 0, 2]
+        for k, mat in enumerate(["honey", "water", "oil"]):
+            for name, val in STRATIFIED_LAYERS[k].items():
+                s[f"{name}_{mat}"] = val
+        s["tension_oil_water"] = 0.0
     s.update(extra or {})
     fills = [([0.0, k * 0.2 * h, float(w), (k + 1) * 0.2 * h], rows[k], None) for k in range(3)]
     return Tank(w, h, s, [], fills)

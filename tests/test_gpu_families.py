@@ -31,7 +31,7 @@ def test_several_families_bit_exact():
 
 
 def test_stratified_honey_family_bit_exact():
-    sim, ora, problems = run_pair(tanks.stratified(128, 72, honey_family=True), 8)
+    sim, ora, problems = run_pair(tanks.stratified(128, 72, builtins=True), 8)
     assert not problems, "\n".join(problems[:10])
 
 
