@@ -292,7 +292,14 @@ def threads_available() -> int:
 
 # ---- building the oracle's tank from a workload description -----------------------------
 
-BUILTIN_ROWS = {"water": 0, "honey": 1, "oil": 2}
+def _builtin_rows() -> dict:
+    """Built-in row keys (presets.rs BUILTINS order), from the table's header."""
+    import re
+    inc = Path(__file__).resolve().parents[1] / "sprout_gb300" / "csrc" / "builtin_rows.inc"
+    return {k: int(r) for r, k in re.findall(r"(\d+):([a-z_]+)", inc.read_text().split("*/", 2)[1])}
+
+
+BUILTIN_ROWS = _builtin_rows()
 MAT_FIELDS = {f for f, _ in OMat._fields_} - {"group", "diluent", "rheology", "react_with"}
 
 

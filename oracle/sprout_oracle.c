@@ -236,22 +236,12 @@ void oparams_default(OSimParams* p) {
     p->slip_cap = 1;
     p->sealed_vent = 1;
     for (int r = 0; r < O_MAX_MATERIALS; r++) mat_default(&p->mat[r]);
-    /* water (presets.rs:37-60) */
-    OMat* w = &p->mat[0];
-    w->temp_model = 2; w->temp_b = 578.9f; w->temp_c = 137.5f;
-    w->melt_lo = -0.5f; w->melt_hi = 0.0f; w->latent = 334.0e3f; w->density_solid = 917.0f;
-    w->boil = 100.0f; w->latent_vap = 2257.0e3f; w->emissivity = 0.96f;
-    /* honey (presets.rs:61-90) */
-    OMat* h = &p->mat[1];
-    h->diluent = 0; h->density = 1.4f * 998.0f; h->viscosity = 0.06f; h->temp_model = 1;
-    h->temp_b = 10500.0f; h->tension = 0.076f; h->mix_rate = 1.5f; h->heat_capacity = 2300.0f;
-    h->conductivity = 0.35f; h->expansion = 5.0e-4f; h->boil = 110.0f; h->latent_vap = 2257.0e3f;
-    /* olive oil (presets.rs:92-117) */
-    OMat* o = &p->mat[2];
-    o->group = 1; o->density = 0.9f * 998.0f; o->viscosity = 6.0e-5f; o->temp_model = 1;
-    o->temp_b = 3900.0f; o->tension = 0.032f; o->heat_capacity = 1970.0f; o->conductivity = 0.17f;
-    o->expansion = 7.0e-4f; o->melt_lo = -8.0f; o->melt_hi = -4.0f; o->latent = 150.0e3f;
-    o->density_solid = 925.0f;
+    /* the built-in liquids (presets.rs: BUILTINS): the fields the oracle carries */
+#define BUILTIN_P(row, field, v) p->mat[row].field = v;
+#define BUILTIN_O(row, field, v)
+#include "../sprout_gb300/csrc/builtin_rows.inc"
+#undef BUILTIN_P
+#undef BUILTIN_O
 }
 
 /* ------------------------------------------------------------------------------------ */

@@ -294,23 +294,12 @@ SimParams::SimParams() {
     set_pair(0, 3, 0.2f);
     set_pair(1, 3, 0.2f);
     set_pair(2, 3, 0.4f);
-    // Water (presets.rs:37-60).
-    MatProps& w = mat[0];
-    w.temp_model = 2; w.temp_b = 578.9f; w.temp_c = 137.5f; w.melt_lo = -0.5f; w.melt_hi = 0.0f;
-    w.latent = 334.0e3f; w.density_solid = 917.0f; w.boil = 100.0f; w.latent_vap = 2257.0e3f;
-    w.emissivity = 0.96f; w.gloss = 0.35f; w.foam = 1.0f; w.froth = 0.6f;
-    // Honey (presets.rs:61-90).
-    MatProps& h = mat[1];
-    h.diluent = 0; h.density = 1.4f * 998.0f; h.viscosity = 0.06f; h.temp_model = 1; h.temp_b = 10500.0f;
-    h.tension = 0.076f; h.mix_rate = 1.5f; h.heat_capacity = 2300.0f; h.conductivity = 0.35f;
-    h.expansion = 5.0e-4f; h.boil = 110.0f; h.latent_vap = 2257.0e3f; h.opacity = 0.55f; h.gloss = 0.9f;
-    h.ior = 1.49f; h.cloud = 2.0e-4f; h.cloud_size = 5.0e-6f; h.cloud_ior = 1.55f; h.solids = 0.8f;
-    // Olive oil (presets.rs:92-117).
-    MatProps& o = mat[2];
-    o.group = 1; o.density = 0.9f * 998.0f; o.viscosity = 6.0e-5f; o.temp_model = 1; o.temp_b = 3900.0f;
-    o.tension = 0.032f; o.heat_capacity = 1970.0f; o.conductivity = 0.17f; o.expansion = 7.0e-4f;
-    o.melt_lo = -8.0f; o.melt_hi = -4.0f; o.latent = 150.0e3f; o.density_solid = 925.0f;
-    o.opacity = 0.25f; o.gloss = 1.0f; o.ior = 1.47f;
+    // The built-in liquids (presets.rs: BUILTINS): what differs from MatProps::default().
+#define BUILTIN_P(row, field, v) mat[row].field = v;
+#define BUILTIN_O(row, field, v) mat[row].field = v;
+#include "builtin_rows.inc"
+#undef BUILTIN_P
+#undef BUILTIN_O
 }
 
 bool SimParams::set_diluent(int row, int diluent) {

@@ -83,3 +83,20 @@ def three_groups(w: int = 96, h: int = 64, cell: float = 0.002) -> Tank:
     fills = [([float(v) for v in a], 59, None), ([float(v) for v in b], 60, None), ([float(v) for v in c], 61, None)]
     fills += [(r, 0, None) for r in around([0, 0, w, int(36 * sy)], [a, b, c])]
     return Tank(w, h, s, [], fills, groups={59: 1, 60: 1, 61: 2})
+
+
+def builtin_mix(w: int = 96, h: int = 64, cell: float = 0.002) -> Tank:
+    """Built-in liquids side by side: water, ink and milk (water concentrates: two families),
+    olive oil (phase group 1) and mercury (phase group 2), no surface tension."""
+    s = {"cell_size": cell, "fixed_hz": 240.0, "pressure_tol": 1e-5, "viscosity_tol": 1e-5}
+    for k in ["water", "ink", "milk", "oil", "mercury"]:
+        s[f"tension_{k}"] = 0.0
+    for k in ["tension_oil_water", "tension_metal_water", "tension_metal_oil"]:
+        s[k] = 0.0
+    sx, sy = w / 96.0, h / 64.0
+    box = lambda x0, y0, x1, y1: [int(x0 * sx), int(y0 * sy), int(x1 * sx), int(y1 * sy)]
+    ink, milk, oil, hg = box(8, 4, 28, 16), box(40, 4, 60, 16), box(66, 4, 86, 14), box(40, 30, 52, 40)
+    fills = [([float(v) for v in ink], 4, None), ([float(v) for v in milk], 11, None),
+             ([float(v) for v in oil], 2, None), ([float(v) for v in hg], 8, None)]
+    fills += [(r, 0, None) for r in around([0, 0, w, int(36 * sy)], [ink, milk, oil, hg])]
+    return Tank(w, h, s, [], fills)

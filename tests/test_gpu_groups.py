@@ -49,3 +49,11 @@ def test_group_tanks_in_a_batch_equal_alone():
     for k, (a, b) in enumerate(zip(alone, batched)):
         problems += compare(a, b, f"tank {k}")
     assert not problems, "\n".join(problems)
+
+
+def test_builtin_liquids_bit_exact():
+    """Water, ink and milk (two families), olive oil and mercury (three groups): the built-in
+    rows as the reference's table has them."""
+    sim, ora, problems = run_pair(tanks.builtin_mix(), 12)
+    assert not problems, "\n".join(problems[:10])
+    assert not fields_agree(sim, ora, ["aux", "grho", "mixb"])

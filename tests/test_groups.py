@@ -53,3 +53,30 @@ def test_three_groups_separate():
     assert gbase[:, 0].max() > 0.0 and np.all(gbase[:, 2:] == 0.0)
     aux = ora.field("aux").reshape(-1, 4)
     assert aux[:, 2].max() > 0.5, "group 2's share in the cells it fills"
+
+
+def test_builtin_rows_carry_the_reference_table():
+    """Known answers of presets.rs for rows past the first three (every row comes from one
+    table shared with the oracle)."""
+    import sprout_gb300 as S
+    p = S.SimParams()
+    for key, want in [("density_mercury", 13534.0), ("viscosity_mercury", 1.13e-7), ("tension_mercury", 0.485),
+                      ("density_ink", 1050.0), ("mix_rate_ink", 0.25), ("density_brine", 1200.0),
+                      ("mix_rate_brine", 1.0), ("density_milk", 1030.0), ("mix_rate_milk", 0.8)]:
+        assert abs(p.get(key) - want) <= 1e-6 * abs(want), key
+    from oracle import oracle as O
+    q = O.default_params()
+    assert q.mat[8].group == 2 and q.mat[4].diluent == 0 and q.mat[11].diluent == 0 and q.mat[14].diluent == 0
+
+
+def test_builtin_liquids_mix_and_separate():
+    ora, parts, _ = tanks.oracle_of(tanks.builtin_mix())
+    before, _ = mean_heights(parts)
+    for _ in range(24):
+        ora.step(1, DT)
+    after, live = mean_heights(ora.particles())
+    assert np.isfinite(live["pos"]).all()
+    assert after[8] < before[8] - 2.0, "mercury sank"
+    assert after[2] > before[2], "oil rose"
+    row = (live["kind"] & 255).astype(np.int64) - 1
+    assert np.any((row == 4) & (live["s"] < 1.0)) and np.any((row == 11) & (live["s"] < 1.0)), "ink and milk diluted"
