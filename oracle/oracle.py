@@ -39,6 +39,7 @@ class OMat(C.Structure):
         ("shear_modulus", C.c_float), ("susceptibility", C.c_float), ("skin", C.c_float),
         ("friction", C.c_float), ("self_heat", C.c_float), ("volatility", C.c_float),
         ("react_with", C.c_int32), ("react_rate", C.c_float), ("fume", C.c_float),
+        ("yield_stress", C.c_float), ("flow_index", C.c_float), ("shear_time", C.c_float), ("visc_ratio", C.c_float),
     ]
 
 

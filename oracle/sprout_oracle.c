@@ -94,6 +94,43 @@ float o_expf(float x) {
     return (p * s1) * s2;
 }
 
+/* ln(x), x > 0: x = m 2^e, m in [sqrt(1/2), sqrt(2)) (subnormals scaled by 2^24 first);
+ * ln m = 2 atanh(s), s = (m - 1) / (m + 1), by the atanh series to s^13 (Horner in s^2);
+ * e ln 2 added in two parts. */
+float o_logf(float x) {
+    if (x != x || x < 0.0f) return bitsf(0x7fc00000u);
+    if (x == 0.0f) return bitsf(0xff800000u);
+    if (x == bitsf(0x7f800000u)) return x;
+    int e = 0;
+    if (x < 1.17549435e-38f) {
+        x *= 16777216.0f;
+        e = -24;
+    }
+    uint32_t u;
+    memcpy(&u, &x, 4);
+    e += (int)((u >> 23) & 255u) - 127;
+    float m = bitsf((u & 0x7fffffu) | 0x3f800000u);
+    if (m > 1.41421356f) {
+        m *= 0.5f;
+        e += 1;
+    }
+    float sv = (m - 1.0f) / (m + 1.0f);
+    float z = sv * sv;
+    float q = 7.69230769e-02f;   /* 1/13 */
+    q = q * z + 9.09090909e-02f;
+    q = q * z + 1.11111111e-01f;
+    q = q * z + 1.42857143e-01f;
+    q = q * z + 2.00000000e-01f;
+    q = q * z + 3.33333333e-01f;
+    q = q * z + 1.0f;
+    float lm = 2.0f * sv * q;
+    float fe = (float)e;
+    return fe * 0.693145752f + (fe * 1.42860677e-06f + lm);
+}
+
+/* x^y = exp(y ln x) with the two functions above (x > 0; 1 for x = 1) */
+float o_powf(float x, float y) { return x == 1.0f ? 1.0f : o_expf(y * o_logf(x)); }
+
 /* ------------------------------------------------------------------------------------ */
 /* Constants (shaders/common.glsl, src/sim/ sources)                                       */
 /* ------------------------------------------------------------------------------------ */
@@ -180,6 +217,10 @@ static void mat_default(OMat* m) {
     m->freeze_shift = 0.0f;
     m->spawn_temp = T_REF;
     m->react_with = -1;
+    m->yield_stress = 0.0f;
+    m->flow_index = 1.0f;
+    m->shear_time = 1.0f;
+    m->visc_ratio = 1.0f;
 }
 
 void oparams_default(OSimParams* p) {
@@ -550,6 +591,8 @@ uint32_t ofill_rect(int w, int h, int nshapes, const OShape* shapes, const float
 typedef struct GMat {   /* common.glsl:224-238 (the fields the restated passes read) */
     int ia[4], ib[4];
     float a[4], b[4], temp[4], th[4], th2[4], el[4], misc[4], rx[4];
+    float rheo[4];   /* yield stress / water's density (cells^2/s^2); flow index; shear time; ratio */
+    float gr[4];     /* friction; fume; fizz; unused */
 } GMat;
 
 typedef struct GParams {   /* common.glsl:37-86 (subset) */
@@ -637,6 +680,7 @@ struct OSim {
     int32_t* acc;
     V4 *vel, *cell, *comp, *coef, *sprop, *surf, *surf2, *aux, *grho, *therm, *dheat, *vw, *vs, *prhs;
     V4* gbase;   /* per cell: share x base density of phase groups 1 - 3 (grid_prep.comp:53, 172, 247) */
+    V4* rh;      /* per cell: its non-Newtonian liquid: share, row, concentration, stiff */
     V2 *vel0, *pjump, *pres;
     float* p2keep;
     float* mixb;   /* per cell, families 1 .. n_fam - 1: the concentration (-1: not here) */
@@ -878,6 +922,12 @@ static void build_mats(OSim* s) {
         g->misc[3] = m->expansion;
         g->rx[2] = m->self_heat / m->heat_capacity;
         g->rx[3] = m->volatility;
+        g->rheo[0] = m->yield_stress / (WATER_DENSITY * dx * dx);   /* mod.rs:2184 stress() */
+        g->rheo[1] = m->flow_index;
+        g->rheo[2] = m->shear_time;
+        g->rheo[3] = m->visc_ratio;
+        g->gr[0] = m->friction;
+        g->gr[1] = m->fume;
     }
 }
 
@@ -1813,6 +1863,7 @@ static void k_grid_prep(OSim* s) {
             float sigma = 0.0f;
             V2 contact = v2(0.0f, 0.0f);
             float fam0 = -1.0f;
+            V4 nn = v4(0.0f, -1.0f, 1.0f, 0.0f);   /* grid_prep.comp:62: the cell's non-Newtonian liquid */
             float rho = 0.0f, mu = 0.0f, rho_c = 0.0f, nu_c = 0.0f;
             int thermal = has_cap(s, CAP_THERMAL);
             const int nmix = P_.n_fam - 1;   /* grid_prep.comp:67-68 */
@@ -1887,6 +1938,8 @@ static void k_grid_prep(OSim* s) {
                             frozen += share * fs;
                         }
                     }
+                    if ((s->mats[r].ib[1] != 0 || s->mats[r].temp[3] > 0.0f || s->mats[r].gr[0] > 0.0f) && share > nn.x)
+                        nn = v4(share, (float)r, sc, 0.0f);   /* grid_prep.comp:162 */
                     if (r != 57 && share > top_share) {
                         top_share = share;
                         top_row = r;
@@ -1917,9 +1970,15 @@ static void k_grid_prep(OSim* s) {
             float level = has ? phi_t - LIQUID_THR : -LIQUID_THR;
             if (has && level <= 0.0f && cx > 0 && cy > 0 && cx < W - 1 && cy < H - 1) {
                 if ((packed(s, i - 1) && packed(s, i + 1)) || (packed(s, i - W) && packed(s, i + W))) level = 0.05f;
-                else if (P_.gravity > 0.0f && phi_t > 0.25f && packed(s, i - W)) level = 0.05f;
+                else if (P_.gravity > 0.0f && nn.x <= 0.0f && phi_t > 0.25f && packed(s, i - W)) level = 0.05f;
             }
             if (sol.w > 0.0f && level <= 0.0f) region_air |= 1u << (s->region[i] & REGION_MASK);
+            if (s->caps & (CAP_RIGID | CAP_RHEO)) {   /* grid_prep.comp:232-237 */
+                float cap = rho * o_expf(P_.heat2[0]);
+                if (mu >= cap && level > 0.0f) nn.w = 1.0f;
+                mu = minf(mu, cap);
+                s->rh[i] = nn;
+            }
             s->cell[i] = v4(phi_f, rho, mu, level);
             s->comp[i] = v4(rho, f[1], fam0, phi_t);
             if (group_sorts(s, 1) || group_sorts(s, 2) || group_sorts(s, 3)) s->gbase[i] = v4(bg[0], bg[1], bg[2], 0.0f);
@@ -1940,6 +1999,73 @@ static void k_grid_prep(OSim* s) {
 /* ------------------------------------------------------------------------------------ */
 /* grid_coef.comp, surf_smooth.comp, surf_curv.comp, surf_apply.comp                      */
 /* ------------------------------------------------------------------------------------ */
+
+/* common.glsl:527-540: the shear rate of cell i from its faces (gravity's last increment taken
+ * back out when pre) */
+static float shear_rate(const OSim* s, int i, int pre) {
+    int W = s->W;
+    float gv = pre ? P_.gravity * s->S.dt : 0.0f;
+#define UF(k) (face_live(s->vel[k].z) ? s->vel[k].x : 0.0f)
+#define VF(k) (face_live(s->vel[k].w) ? s->vel[k].y + gv : 0.0f)
+    float dxx = UF(i + 1) - UF(i);
+    float dyy = VF(i + W) - VF(i);
+    float duy = 0.25f * (UF(i + W) + UF(i + 1 + W) - UF(i - W) - UF(i + 1 - W));
+    float dvx = 0.25f * (VF(i + 1) + VF(i + 1 + W) - VF(i - 1) - VF(i - 1 + W));
+#undef UF
+#undef VF
+    float dxy = 0.5f * (duy + dvx);
+    return sqrtf(2.0f * (dxx * dxx + dyy * dyy + 2.0f * dxy * dxy));
+}
+
+/* common.glsl:546-571: the non-Newtonian factor F and yield stress tau of the cell's liquid */
+static void nn_eval(const OSim* s, int i, V4 q, float g, float* Fo, float* tauo) {
+    const GMat* m = &s->mats[(int)q.y];
+    const float* rp = m->rheo;
+    int model = m->ib[1];
+    float F = 1.0f, tau = 0.0f;
+    if (model == 1) {
+        F = rp[3] + (1.0f - rp[3]) * o_powf(1.0f + (rp[2] * g) * (rp[2] * g), 0.5f * (rp[1] - 1.0f));
+    } else if (model == 2) {
+        F = o_powf(maxf(g, 1e-6f), rp[1] - 1.0f);
+        tau = rp[0] * q.z;
+    } else if (model == 3) {
+        F = minf(o_powf(1.0f + (rp[2] * g) * (rp[2] * g), 0.5f * (rp[1] - 1.0f)), rp[3]);
+    }
+    float fr = m->gr[0];
+    if (fr > 0.0f) tau += fr * q.z * q.z * q.z * maxf(s->pres[i].x, 0.0f) / maxf(s->S.dt, 1e-6f);
+    int W = s->W;
+    float skin = m->temp[3];
+    if (skin > 0.0f && (s->cell[i - 1].w <= 0.0f || s->cell[i + 1].w <= 0.0f || s->cell[i - W].w <= 0.0f || s->cell[i + W].w <= 0.0f))
+        tau += skin;
+    *Fo = 1.0f + q.x * (F - 1.0f);
+    *tauo = tau * q.x;
+}
+
+/* rheo.comp: a non-Newtonian cell's viscosity at its shear rate, capped at rigid_viscosity */
+static void k_rheo(OSim* s) {
+    int W = s->W, H = s->H;
+#pragma omp parallel for schedule(static)
+    for (int cy = 1; cy < H - 1; cy++)
+        for (int cx = 1; cx < W - 1; cx++) {
+            int i = cy * W + cx;
+            V4 me = s->cell[i];
+            V4 q = s->rh[i];
+            if (me.w <= 0.0f || q.x <= 0.0f) continue;
+            float g = shear_rate(s, i, 1);
+            float F, tau;
+            nn_eval(s, i, q, g, &F, &tau);
+            float eff = me.z * F + tau / maxf(g, 1e-6f);
+            float cap = me.y * o_expf(P_.heat2[0]);
+            float skin = q.x * s->mats[(int)q.y].temp[3];
+            if (skin > 0.0f && me.y * g * g < skin &&
+                (s->cell[i - 1].w <= 0.0f || s->cell[i + 1].w <= 0.0f || s->cell[i - W].w <= 0.0f || s->cell[i + W].w <= 0.0f)) {
+                q.w = 1.0f;
+                s->rh[i] = q;
+            }
+            me.z = minf(eff, cap);
+            s->cell[i] = me;
+        }
+}
 
 static void coef_face(V4 a, V4 b, float open, float* g, float* rho) {
     float wsum = a.x + b.x;
@@ -3871,6 +3997,7 @@ static void substep(OSim* s, int gather) {
     if (s->thermal) memset(s->hcell, 0, (size_t)s->W * s->H * sizeof(I2));
     k_particles(s, gather);
     k_grid_prep(s);
+    if (s->caps & CAP_RHEO) k_rheo(s);
     k_grid_coef(s);
     k_surf_smooth(s);
     k_surf_curv(s);
@@ -3929,6 +4056,7 @@ OSim* osim_create(int w, int h, uint32_t capacity, const OSimParams* p) {
     ALLOC(s->vs, nc); ALLOC(s->prhs, nc); ALLOC(s->vel0, nc); ALLOC(s->pjump, nc);
     ALLOC(s->mixb, nc * (MAX_PRESENT - 1));
     ALLOC(s->gbase, nc);
+    ALLOC(s->rh, nc);
     ALLOC(s->pres, nc); ALLOC(s->p2keep, nc); ALLOC(s->hcell, nc); ALLOC(s->solid, nc);
     ALLOC(s->sdf, (size_t)(w + 1) * (h + 1)); ALLOC(s->region, nc); ALLOC(s->solid_t, nc);
     ALLOC(s->mga, s->lv.total); ALLOC(s->mgd, s->lv.total); ALLOC(s->mgx, s->lv.total);
@@ -3953,7 +4081,7 @@ void osim_destroy(OSim* s) {
                     s->vel0, s->pjump, s->pres, s->p2keep, s->hcell, s->solid, s->sdf, s->region,
                     s->solid_t, s->mga, s->mgd, s->mgx, s->mgz, s->mgr, s->cgp, s->cgp2, s->cgq,
                     s->ptile, s->part, s->vr, s->vr2, s->vp, s->vq, s->vq2, s->vd, s->vaz, s->vma,
-                    s->vmb, s->vmd, s->vmr, s->vmx, s->vmz, s->tiles, s->vtile, s->pending, s->mixb, s->gbase};
+                    s->vmb, s->vmd, s->vmr, s->vmx, s->vmz, s->tiles, s->vtile, s->pending, s->mixb, s->gbase, s->rh};
     for (size_t k = 0; k < sizeof ptrs / sizeof ptrs[0]; k++) free(ptrs[k]);
     free(s);
 }
@@ -4056,7 +4184,7 @@ static int set_tank(OSim* s, const int* present, int thermal) {
     s->thermal = thermal;
     s->caps = compute_caps(s);
     int rc = 0;
-    if (s->caps & (CAP_RIGID | CAP_RHEO | CAP_MAGNET | CAP_ELASTIC | CAP_SETTLE | CAP_STEAM | CAP_REACT)) rc = -4;
+    if (s->caps & (CAP_RIGID | CAP_MAGNET | CAP_ELASTIC | CAP_SETTLE | CAP_STEAM | CAP_REACT)) rc = -4;
     for (int k = 0; k < nrows; k++) {
         const OMat* m = &p->mat[rows[k]];
         if (m->volatility > 0.0f || (thermal && m->boil < 1e8f)) rc = -4;
@@ -4244,6 +4372,7 @@ long osim_field(const OSim* s, const char* name, void* out, size_t cap) {
     F("aux", s->aux, nc * 16)
     F("grho", s->grho, nc * 16)
     F("gbase", s->gbase, nc * 16)
+    F("rh", s->rh, nc * 16)
     F("surf2", s->surf2, nc * 16)
     F("tiles", s->tiles, (size_t)s->nwg * 4)
     F("vtile", s->vtile, (size_t)s->lv.tiles * 4)

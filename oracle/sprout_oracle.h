@@ -51,6 +51,7 @@ typedef struct OMat {
     int32_t react_with;
     float react_rate;
     float fume;
+    float yield_stress, flow_index, shear_time, visc_ratio;
 } OMat;
 
 #define O_MAX_MATERIALS 96
@@ -158,6 +159,8 @@ void osim_set_threads(int n);
 /* exp restated from the mathematics (Cody-Waite reduction, degree-7 Taylor), the same
  * arithmetic the device code uses, so both sides round identically. */
 float o_expf(float x);
+float o_logf(float x);
+float o_powf(float x, float y);
 
 #ifdef __cplusplus
 }

@@ -62,6 +62,7 @@ struct DevScene {
     float* p2keep;
     float* mixb;      // per cell, families 1 .. n_fam - 1: the family's concentration (-1: not here)
     float4* gbase;    // per cell: share x base density of phase groups 1 - 3 (w unused)
+    float4* rh;       // per cell: its non-Newtonian liquid (share, row, concentration, stiff)
     int2* hcell;
     const float4* solid;
     const float* sdf;
@@ -154,6 +155,42 @@ DEV float sp_expf(float x) {
     float s2 = __int_as_float((k2 + 127) << 23);
     return (p * s1) * s2;
 }
+
+// ln(x) for x > 0: x = m 2^e with m in [sqrt(1/2), sqrt(2)) (subnormals scaled by 2^24
+// first), ln m = 2 atanh(s) with s = (m - 1) / (m + 1), |s| <= 0.172, by the atanh series
+// to s^13 in Horner form in s^2, and e ln 2 added in two parts. The same operations in the
+// same order as the CPU evaluation used by the tests.
+DEV float sp_logf(float x) {
+    if (x != x || x < 0.0f) return __int_as_float(0x7fc00000);
+    if (x == 0.0f) return __int_as_float(0xff800000);
+    if (x == __int_as_float(0x7f800000)) return x;
+    int e = 0;
+    if (x < 1.17549435e-38f) {
+        x *= 16777216.0f;
+        e = -24;
+    }
+    const uint32_t u = __float_as_uint(x);
+    e += (int)((u >> 23) & 255u) - 127;
+    float m = __uint_as_float((u & 0x7fffffu) | 0x3f800000u);
+    if (m > 1.41421356f) {
+        m *= 0.5f;
+        e += 1;
+    }
+    const float s = (m - 1.0f) / (m + 1.0f);
+    const float z = s * s;
+    float p = 7.69230769e-02f;   // 1/13
+    p = p * z + 9.09090909e-02f;  // 1/11
+    p = p * z + 1.11111111e-01f;  // 1/9
+    p = p * z + 1.42857143e-01f;  // 1/7
+    p = p * z + 2.00000000e-01f;  // 1/5
+    p = p * z + 3.33333333e-01f;  // 1/3
+    p = p * z + 1.0f;
+    const float lm = 2.0f * s * p;
+    const float fe = (float)e;
+    return fe * 0.693145752f + (fe * 1.42860677e-06f + lm);
+}
+// x^y as exp(y ln x) with the two functions above (x > 0; 1 for x = 1).
+DEV float sp_powf(float x, float y) { return x == 1.0f ? 1.0f : sp_expf(y * sp_logf(x)); }
 
 // Quadratic B-spline weights (common.glsl:639-643) of a point at offset f from its base node.
 DEV void bspline(float fx, float fy, float wx[3], float wy[3]) {

@@ -38,6 +38,8 @@ struct DevMat {
     float th2[4];   // latent heat (degrees); emissivity; boiling point; latent heat of vaporisation
     float misc[4];  // freeze shift; load; viscosity blend exponent; thermal expansion (1/K)
     float rx[4];    // reaction rate; reaction heat; self-heating (K/s); volatility
+    float rheo[4];  // yield stress / water's density (cells^2/s^2); flow index; shear time (s); viscosity ratio
+    float gr[4];    // friction coefficient; fume; fizz; unused
 };
 
 struct DevParams {

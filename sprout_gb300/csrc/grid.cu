@@ -57,6 +57,7 @@ __global__ void __launch_bounds__(256) k_grid_prep(DevScene d) {
         const float phi_f = (float)cw / MASS_SCALE * P->inv_ppc;
         float f[kGroups] = {0.0f, 0.0f, 0.0f, 0.0f}, rg[kGroups] = {0.0f, 0.0f, 0.0f, 0.0f}, lg[kGroups] = {0.0f, 0.0f, 0.0f, 0.0f};
         float sigma = 0.0f, contx = 0.0f, conty = 0.0f, fam0 = -1.0f;
+        float4 nn = make_float4(0.0f, -1.0f, 1.0f, 0.0f);   // the cell's non-Newtonian liquid: share, row, concentration, stiff
         float rho = 0.0f, mu = 0.0f, rho_c = 0.0f, nu_c = 0.0f;
         const bool thermal = P->thermal != 0;
         float T = P->heat[0], kappa = 0.0f, emis = 0.0f, frozen = 0.0f, Craw = 0.0f;
@@ -148,6 +149,8 @@ __global__ void __launch_bounds__(256) k_grid_prep(DevScene d) {
                         frozen += share * fs;
                     }
                 }
+                if ((mats[r].ib[1] != 0 || mats[r].temp[3] > 0.0f || mats[r].gr[0] > 0.0f) && share > nn.x)
+                    nn = make_float4(share, (float)r, sc, 0.0f);
                 if (r != 57 && share > top_share) {
                     top_share = share;
                     top_row = r;
@@ -178,9 +181,16 @@ __global__ void __launch_bounds__(256) k_grid_prep(DevScene d) {
         float level = has ? phi_t - LIQUID_THR : -LIQUID_THR;
         if (has && level <= 0.0f && cx > 0 && cy > 0 && cx < W - 1 && cy < H - 1) {
             if ((packed(d, i - 1) && packed(d, i + 1)) || (packed(d, i - W) && packed(d, i + W))) level = 0.05f;
-            else if (P->gravity > 0.0f && phi_t > 0.25f && packed(d, i - W)) level = 0.05f;
+            else if (P->gravity > 0.0f && nn.x <= 0.0f && phi_t > 0.25f && packed(d, i - W)) level = 0.05f;
         }
         if (sol.w > 0.0f && level <= 0.0f) air_bits = 1u << (__ldg(&d.region[i]) & REGION_MASK);
+        if ((P->caps & (CAP_RIGID | CAP_RHEO)) != 0u) {
+            // the viscosity solve stops at rigid_viscosity; a cell that would need more is stiff
+            const float cap = rho * sp_expf(P->heat2[0]);
+            if (mu >= cap && level > 0.0f) nn.w = 1.0f;
+            mu = minf(mu, cap);
+            d.rh[i] = nn;
+        }
         d.cell[i] = make_float4(phi_f, rho, mu, level);
         d.comp[i] = make_float4(rho, f[1], fam0, phi_t);
         if (P->sorts != 0u) d.gbase[i] = make_float4(bg[0], bg[1], bg[2], 0.0f);
@@ -702,10 +712,77 @@ __global__ void __launch_bounds__(256) k_project(DevScene d) {
     if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0 && threadIdx.y == 0) d.S->gather = 1u;
 }
 
+// The shear rate |D| sqrt(2) of cell i from its faces' velocities, gravity's last increment
+// taken back out when `pre` (common.glsl:527-540).
+DEV float shear_rate(const DevScene& d, int i, bool pre) {
+    const int W = d.W;
+    const float gv = pre ? d.P->gravity * d.S->dt : 0.0f;
+    auto U = [&](int k) { const float4 v = d.vel[k]; return face_live(v.z) ? v.x : 0.0f; };
+    auto V = [&](int k) { const float4 v = d.vel[k]; return face_live(v.w) ? v.y + gv : 0.0f; };
+    const float dxx = U(i + 1) - U(i);
+    const float dyy = V(i + W) - V(i);
+    const float duy = 0.25f * (U(i + W) + U(i + 1 + W) - U(i - W) - U(i + 1 - W));
+    const float dvx = 0.25f * (V(i + 1) + V(i + 1 + W) - V(i - 1) - V(i - 1 + W));
+    const float dxy = 0.5f * (duy + dvx);
+    return sqrtf(2.0f * (dxx * dxx + dyy * dyy + 2.0f * dxy * dxy));
+}
+
+// The non-Newtonian factor F on the viscosity and the yield stress tau of the cell's liquid q
+// (rh: share, row, concentration) at shear rate g: Carreau, Herschel-Bulkley, thickening;
+// friction and skin add to tau; both scale with the liquid's share (common.glsl:546-571).
+DEV void nn_eval(const DevScene& d, int i, float4 q, float g, float& F, float& tau) {
+    const DevMat& m = d.mats[(int)q.y];
+    const float* rp = m.rheo;
+    const int model = m.ib[1];
+    F = 1.0f;
+    tau = 0.0f;
+    if (model == 1) {
+        F = rp[3] + (1.0f - rp[3]) * sp_powf(1.0f + (rp[2] * g) * (rp[2] * g), 0.5f * (rp[1] - 1.0f));
+    } else if (model == 2) {
+        F = sp_powf(maxf(g, 1e-6f), rp[1] - 1.0f);
+        tau = rp[0] * q.z;
+    } else if (model == 3) {
+        F = minf(sp_powf(1.0f + (rp[2] * g) * (rp[2] * g), 0.5f * (rp[1] - 1.0f)), rp[3]);
+    }
+    const float fr = m.gr[0];
+    if (fr > 0.0f) tau += fr * q.z * q.z * q.z * maxf(d.pres[i].x, 0.0f) / maxf(d.S->dt, 1e-6f);
+    const int W = d.W;
+    const float skin = m.temp[3];
+    if (skin > 0.0f && (d.cell[i - 1].w <= 0.0f || d.cell[i + 1].w <= 0.0f || d.cell[i - W].w <= 0.0f || d.cell[i + W].w <= 0.0f))
+        tau += skin;
+    F = 1.0f + q.x * (F - 1.0f);
+    tau *= q.x;
+}
+
+// rheo.comp: the viscosity of a cell holding a non-Newtonian liquid at its shear rate, capped
+// at rigid_viscosity; a skinned surface cell too slow to yield turns stiff.
+__global__ void __launch_bounds__(256) k_rheo(DevScene d) {
+    CELL_XY;
+    if (cx < 1 || cy < 1 || cx >= W - 1 || cy >= H - 1) return;
+    const int i = cy * W + cx;
+    float4 me = d.cell[i];
+    float4 q = d.rh[i];
+    if (me.w <= 0.0f || q.x <= 0.0f) return;
+    const float g = shear_rate(d, i, true);
+    float F, tau;
+    nn_eval(d, i, q, g, F, tau);
+    const float eff = me.z * F + tau / maxf(g, 1e-6f);
+    const float cap = me.y * sp_expf(d.P->heat2[0]);
+    const float skin = q.x * d.mats[(int)q.y].temp[3];
+    if (skin > 0.0f && me.y * g * g < skin &&
+        (d.cell[i - 1].w <= 0.0f || d.cell[i + 1].w <= 0.0f || d.cell[i - W].w <= 0.0f || d.cell[i + W].w <= 0.0f)) {
+        q.w = 1.0f;
+        d.rh[i] = q;
+    }
+    me.z = minf(eff, cap);
+    d.cell[i] = me;
+}
+
 void launch_grid(const DevScene& d, const LaunchCfg& cfg, cudaStream_t st) {
     dim3 blk(16, 16);
     dim3 grd((d.W + 15) / 16, (d.H + 15) / 16);
     k_grid_prep<<<grd, blk, 0, st>>>(d);
+    if (cfg.rheo) k_rheo<<<grd, blk, 0, st>>>(d);
     k_coef_smooth<<<grd, blk, 0, st>>>(d);
     k_curv<<<grd, blk, 0, st>>>(d);
     k_apply<<<grd, blk, 0, st>>>(d);

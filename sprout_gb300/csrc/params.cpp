@@ -529,6 +529,14 @@ void build_materials(const SimParams& p, const Tank& t, bool thermal, DevMat* ou
         g.rx[1] = m.react_heat / m.heat_capacity;
         g.rx[2] = m.self_heat / m.heat_capacity;
         g.rx[3] = m.volatility;
+        g.rheo[0] = m.yield_stress / (kWaterDensity * dx * dx);   // Pa over water's density, cells^2/s^2
+        g.rheo[1] = m.flow_index;
+        g.rheo[2] = m.shear_time;
+        g.rheo[3] = m.visc_ratio;
+        g.gr[0] = m.friction;
+        g.gr[1] = m.fume;
+        g.gr[2] = m.fizz;
+        g.gr[3] = 0.0f;
     }
 }
 

@@ -265,7 +265,7 @@ struct SproutSim {
         A(d.scan_tmp, (nc + 1 + 1023) / 1024 + 1);
         A(d.acc, nc * 32);
         A(d.vel, nc); A(d.cell, nc); A(d.comp, nc); A(d.coef, nc); A(d.sprop, nc); A(d.surf, nc);
-        A(d.surf2, nc); A(d.aux, nc); A(d.grho, nc); A(d.gbase, nc); A(d.therm, nc); A(d.dheat, nc); A(d.vw, nc);
+        A(d.surf2, nc); A(d.aux, nc); A(d.grho, nc); A(d.gbase, nc); A(d.rh, nc); A(d.therm, nc); A(d.dheat, nc); A(d.vw, nc);
         A(d.vs, nc); A(d.prhs, nc); A(d.vel0, nc); A(d.pjump, nc); A(d.pres, nc); A(d.p2keep, nc);
         A(d.hcell, nc);
         float4* solid;
@@ -510,6 +510,7 @@ struct SproutSim {
         want.n_slots = n_slots;
         want.thermal = thermal;
         want.heat = thermal && params.heat_rate > 0.0f;
+        want.rheo = (caps & CAP_RHEO) != 0u;
         want.visc_mode = visc_mode;
         want.twice = visc_mode == 2 && params.viscous_projection != 0;
         want.viscous_warm = params.viscous_warm != 0;
@@ -522,7 +523,7 @@ struct SproutSim {
             if (v > 0) want.visc_blocks = std::max(1, std::min(v, visc_max[want.visc_sweeps - 1]));
         }
         want.mixed = mixed;
-        bool same = want.n_slots == cfg.n_slots && want.thermal == cfg.thermal && want.heat == cfg.heat &&
+        bool same = want.n_slots == cfg.n_slots && want.thermal == cfg.thermal && want.heat == cfg.heat && want.rheo == cfg.rheo &&
                     want.visc_mode == cfg.visc_mode && want.twice == cfg.twice && want.viscous_warm == cfg.viscous_warm &&
                     want.visc_levels == cfg.visc_levels && want.visc_sweeps == cfg.visc_sweeps &&
                     want.visc_blocks == cfg.visc_blocks && want.mixed == cfg.mixed && d.stride == std::max(tank.stride, 8);
@@ -619,8 +620,8 @@ struct SproutSim {
         thermal = th;
         caps = compute_caps();
         int rc = SPROUT_OK;
-        if (caps & (CAP_RIGID | CAP_RHEO | CAP_MAGNET | CAP_ELASTIC | CAP_SETTLE | CAP_STEAM | CAP_REACT))
-            rc = fail(SPROUT_E_UNSUPPORTED, "the tank needs rigid / rheology / magnet / elastic / settling / steam / reaction passes, which this engine does not carry");
+        if (caps & (CAP_RIGID | CAP_MAGNET | CAP_ELASTIC | CAP_SETTLE | CAP_STEAM | CAP_REACT))
+            rc = fail(SPROUT_E_UNSUPPORTED, "the tank needs rigid / magnet / elastic / settling / steam / reaction passes, which this engine does not carry");
         for (int r : tank.rows) {
             const MatProps& m = params.mat[r];
             if (rc == SPROUT_OK && (m.volatility > 0.0f || (thermal && m.boil < 1e8f)))
@@ -1645,6 +1646,7 @@ int sprout_sim_download_field(SproutSim* sim, const char* name, void* out, size_
     else if (n == "aux") { src = d.aux; b = nc * 16; }
     else if (n == "grho") { src = d.grho; b = nc * 16; }
     else if (n == "gbase") { src = d.gbase; b = nc * 16; }
+    else if (n == "rh") { src = d.rh; b = nc * 16; }
     else if (n == "surf2") { src = d.surf2; b = nc * 16; }
     else if (d.mixb && n == "mixb") { src = d.mixb; b = nc * 4 * (size_t)std::max(sim->tank.families - 1, 0); }
     else if (sim->visc_alloc && n == "tiles") { src = d.tiles; b = (size_t)d.nwg * 4; }

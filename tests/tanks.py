@@ -100,3 +100,14 @@ def builtin_mix(w: int = 96, h: int = 64, cell: float = 0.002) -> Tank:
              ([float(v) for v in oil], 2, None), ([float(v) for v in hg], 8, None)]
     fills += [(r, 0, None) for r in around([0, 0, w, int(36 * sy)], [ink, milk, oil, hg])]
     return Tank(w, h, s, [], fills)
+
+
+def shear_thinning(w: int = 96, h: int = 64, cell: float = 0.002, mat: int = 7) -> Tank:
+    """A dam break of a Carreau (shear-thinning) built-in, blood by default (soap: 19), beside
+    water: rheo.comp sets each cell's viscosity from its shear rate."""
+    s = {"cell_size": cell, "fixed_hz": 240.0, "pressure_tol": 1e-5, "viscosity_tol": 1e-5, "tension_water": 0.0,
+         "tension_" + {7: "blood", 19: "soap"}[mat]: 0.0}
+    sx, sy = w / 96.0, h / 64.0
+    box = lambda x0, y0, x1, y1: [float(int(x0 * sx)), float(int(y0 * sy)), float(int(x1 * sx)), float(int(y1 * sy))]
+    fills = [(box(4, 4, 40, 44), mat, None), (box(60, 4, 92, 20), 0, None)]
+    return Tank(w, h, s, [], fills)
