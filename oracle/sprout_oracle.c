@@ -681,6 +681,9 @@ struct OSim {
     V4 *vel, *cell, *comp, *coef, *sprop, *surf, *surf2, *aux, *grho, *therm, *dheat, *vw, *vs, *prhs;
     V4* gbase;   /* per cell: share x base density of phase groups 1 - 3 (grid_prep.comp:53, 172, 247) */
     V4* rh;      /* per cell: its non-Newtonian liquid: share, row, concentration, stiff */
+    float* famocc;   /* per cell and family: its occupancy (settling) */
+    V2* dsettle;     /* per cell and family: the concentration gain / loss rates of settling */
+    int settle_fams; /* families the settling buffers hold */
     V2 *vel0, *pjump, *pres;
     float* p2keep;
     float* mixb;   /* per cell, families 1 .. n_fam - 1: the concentration (-1: not here) */
@@ -837,10 +840,36 @@ static int viscosity_mode(const OSim* s) {   /* mod.rs:2768-2792 */
     return 2;
 }
 
+/* mod.rs:2139-2143: a family in the tank settles (a concentrate with grains, under gravity) */
+static int settles(const OSim* s) {
+    if (!(s->prm.gravity > 0.0f)) return 0;
+    for (int k = 0; k < s->tank.nrows; k++) {
+        const OMat* m = &s->prm.mat[s->tank.rows[k]];
+        if (m->diluent >= 0 && m->grain > 0.0f) return 1;
+    }
+    return 0;
+}
+
+/* mod.rs:2114-2136: the settling buffers for fams families; new zeroed ones when the count
+ * grows or drops to none, the present ones otherwise */
+static int set_settling(OSim* s, int fams) {
+    if (fams == s->settle_fams || (fams > 0 && fams < s->settle_fams)) return 0;
+    size_t n = (size_t)s->W * s->H * (size_t)fams;
+    if (n < 1) n = 1;
+    free(s->famocc);
+    free(s->dsettle);
+    s->famocc = calloc(n, sizeof(float));
+    s->dsettle = calloc(n, sizeof(V2));
+    if (!s->famocc || !s->dsettle) return -2;
+    s->settle_fams = fams;
+    return 0;
+}
+
 static uint32_t compute_caps(const OSim* s) {   /* mod.rs:2717-2761 (the bits that apply) */
     const OSimParams* p = &s->prm;
     uint32_t caps = 0;
     if (s->tank.families > 0) caps |= CAP_FAMILIES;
+    if (s->settle_fams >= s->tank.families && s->tank.families > 0 && settles(s)) caps |= CAP_SETTLE;
     if (s->thermal) caps |= CAP_THERMAL;
     int rigid = 0;
     for (int k = 0; k < s->tank.nrows; k++) {
@@ -1318,7 +1347,7 @@ static void advance(OSim* s, uint32_t id, int gather, Scat* g) {
     float dt = s->S.dt;
     uint32_t row = (p.kind & 255u) - 1u;
     const int* Mia = s->mats[row].ia;
-    const int fam = s->mats[row].ib[0];   /* particles.comp:143 */
+    int fam = s->mats[row].ib[0];   /* particles.comp:143 */
     int thermal = has_cap(s, CAP_THERMAL);
     V2 pos = v2(p.pos[0], p.pos[1]);
     if (gather) {
@@ -1439,6 +1468,32 @@ static void advance(OSim* s, uint32_t id, int gather, Scat* g) {
                         }
                     }
                 }
+            /* settling: each cell's change of its family's concentration (particles.comp:331-352) */
+            {
+                int dil0 = fam < 0 && P_.primary >= 0 && P_.fams[0][1] == (int)row;
+                int sf = dil0 ? 0 : fam;
+                if ((s->caps & CAP_SETTLE) && sf >= 0 && (p.kind & KIND_FRESH) == 0u && s->mats[dil0 ? (uint32_t)P_.primary : row].b[2] > 0.0f) {
+                    V2 ds = v2(0.0f, 0.0f);
+                    for (int b = 0; b < 3; b++)
+                        for (int a = 0; a < 3; a++) {
+                            V2 v = s->dsettle[(size_t)cidx(s, bx + a, by + b) * P_.n_fam + sf];
+                            float wt = w[a].x * w[b].y;
+                            ds.x += wt * v.x;
+                            ds.y += wt * v.y;
+                        }
+                    float s0 = dil0 ? 0.0f : p.s;
+                    float s1 = clampf(s0 + (1.0f - s0) * ds.x - s0 * ds.y, 0.0f, 1.0f);
+                    float c0 = thermal ? thermal_of(s, row, p.s).w : 0.0f;
+                    if (dil0 && s1 > 0.0f) {
+                        row = (uint32_t)P_.primary;
+                        Mia = s->mats[row].ia;
+                        fam = 0;
+                        p.kind = (p.kind & ~255u) | (row + 1u);
+                    }
+                    if (!dil0 || s1 > 0.0f) p.s = s1;
+                    if (thermal) p.t = keep_heat(p.t, c0, thermal_of(s, row, p.s).w);
+                }
+            }
             if (thermal && (p.kind & KIND_FRESH) == 0u) {
                 float dT = 0.0f;
                 for (int b = 0; b < 3; b++)
@@ -1869,6 +1924,9 @@ static void k_grid_prep(OSim* s) {
             const int nmix = P_.n_fam - 1;   /* grid_prep.comp:67-68 */
             for (int q = 0; q < nmix; q++) s->mixb[(size_t)i * nmix + q] = -1.0f;
             float bg[3] = {0.0f, 0.0f, 0.0f};   /* share x base density of groups 1 - 3 */
+            const int settle = (s->caps & CAP_SETTLE) != 0u;   /* grid_prep.comp:69-70, 147 */
+            if (settle)
+                for (int q = 0; q < P_.n_fam; q++) s->famocc[(size_t)i * P_.n_fam + q] = 0.0f;
             float T = P_.heat[0], kappa = 0.0f, emis = 0.0f, frozen = 0.0f, Craw = 0.0f;
             int major = 0, top_row = -1;
             float top_share = 0.0f;
@@ -1926,6 +1984,7 @@ static void k_grid_prep(OSim* s) {
                         const int fam = s->mats[r].ib[0];
                         if (fam == 0) fam0 = sc;
                         else if (fam > 0) s->mixb[(size_t)i * nmix + fam - 1] = sc;
+                        if (settle && fam >= 0) s->famocc[(size_t)i * P_.n_fam + fam] = share * phi_f;
                     }
                     rho_m *= xp;
                     if (thermal) {
@@ -2039,6 +2098,47 @@ static void nn_eval(const OSim* s, int i, V4 q, float g, float* Fo, float* tauo)
         tau += skin;
     *Fo = 1.0f + q.x * (F - 1.0f);
     *tauo = tau * q.x;
+}
+
+/* settle.comp:8-16: family f's settling flux from an upper cell into a lower one */
+static float settle_flux(const OSim* s, int up, int dn, int f, float vt) {
+    int nf = P_.n_fam;
+    float ou = s->famocc[(size_t)up * nf + f], od = s->famocc[(size_t)dn * nf + f];
+    if (ou <= 1e-3f || od <= 1e-3f) return 0.0f;
+    float su = f == 0 ? s->comp[up].z : s->mixb[(size_t)up * (nf - 1) + f - 1];
+    float sd = f == 0 ? s->comp[dn].z : s->mixb[(size_t)dn * (nf - 1) + f - 1];
+    if (su <= 0.0f || sd < 0.0f) return 0.0f;
+    float F = vt * su * (1.0f - sd) * minf(ou, od);
+    return minf(F, minf(su * ou, (1.0f - sd) * od) / s->S.dt);
+}
+
+/* settle.comp:18-52: per cell and family with grains, the concentration gain / loss rates */
+static void k_settle(OSim* s) {
+    int W = s->W, H = s->H, nf = P_.n_fam;
+    int thermal = has_cap(s, CAP_THERMAL);
+#pragma omp parallel for schedule(static)
+    for (int cy = 0; cy < H; cy++)
+        for (int cx = 0; cx < W; cx++) {
+            int i = cy * W + cx;
+            for (int f = 0; f < nf; f++) {
+                int row = P_.fams[f][0], dl = P_.fams[f][1];
+                float gd = s->mats[row].b[2];
+                float occ = s->famocc[(size_t)i * nf + f];
+                V2 ds = v2(0.0f, 0.0f);
+                if (gd > 0.0f && occ > 1e-3f && cy > 0 && cy < H - 1) {
+                    float drho = s->mats[row].a[0] - s->mats[dl].a[0];
+                    float T = thermal ? s->therm[i].x : P_.heat[0];
+                    float lnu = s->mats[dl].a[1] + (thermal ? temp_law(s, dl, T) : 0.0f);   /* row_lnu(dl, 1) */
+                    float vt = terminal(s, drho, s->mats[dl].a[0], o_expf(lnu), gd);
+                    float gain = drho > 0.0f ? settle_flux(s, i + W, i, f, vt) : settle_flux(s, i - W, i, f, vt);
+                    float loss = drho > 0.0f ? settle_flux(s, i, i - W, f, vt) : settle_flux(s, i, i + W, f, vt);
+                    float sv = f == 0 ? s->comp[i].z : s->mixb[(size_t)i * (nf - 1) + f - 1];
+                    float dt = s->S.dt;
+                    ds = v2(dt * (gain / maxf(occ * (1.0f - sv), 1e-6f)), dt * (loss / maxf(occ * sv, 1e-6f)));
+                }
+                s->dsettle[(size_t)i * nf + f] = ds;
+            }
+        }
 }
 
 /* rheo.comp: a non-Newtonian cell's viscosity at its shear rate, capped at rigid_viscosity */
@@ -3998,6 +4098,7 @@ static void substep(OSim* s, int gather) {
     k_particles(s, gather);
     k_grid_prep(s);
     if (s->caps & CAP_RHEO) k_rheo(s);
+    if (s->caps & CAP_SETTLE) k_settle(s);
     k_grid_coef(s);
     k_surf_smooth(s);
     k_surf_curv(s);
@@ -4081,7 +4182,7 @@ void osim_destroy(OSim* s) {
                     s->vel0, s->pjump, s->pres, s->p2keep, s->hcell, s->solid, s->sdf, s->region,
                     s->solid_t, s->mga, s->mgd, s->mgx, s->mgz, s->mgr, s->cgp, s->cgp2, s->cgq,
                     s->ptile, s->part, s->vr, s->vr2, s->vp, s->vq, s->vq2, s->vd, s->vaz, s->vma,
-                    s->vmb, s->vmd, s->vmr, s->vmx, s->vmz, s->tiles, s->vtile, s->pending, s->mixb, s->gbase, s->rh};
+                    s->vmb, s->vmd, s->vmr, s->vmx, s->vmz, s->tiles, s->vtile, s->pending, s->mixb, s->gbase, s->rh, s->famocc, s->dsettle};
     for (size_t k = 0; k < sizeof ptrs / sizeof ptrs[0]; k++) free(ptrs[k]);
     free(s);
 }
@@ -4184,11 +4285,13 @@ static int set_tank(OSim* s, const int* present, int thermal) {
     s->thermal = thermal;
     s->caps = compute_caps(s);
     int rc = 0;
-    if (s->caps & (CAP_RIGID | CAP_MAGNET | CAP_ELASTIC | CAP_SETTLE | CAP_STEAM | CAP_REACT)) rc = -4;
+    if (s->caps & (CAP_RIGID | CAP_MAGNET | CAP_ELASTIC | CAP_STEAM | CAP_REACT)) rc = -4;
     for (int k = 0; k < nrows; k++) {
         const OMat* m = &p->mat[rows[k]];
         if (m->volatility > 0.0f || (thermal && m->boil < 1e8f)) rc = -4;
     }
+    if (rc == 0) rc = set_settling(s, settles(s) ? s->tank.families : 0);
+    if (rc == 0) s->caps = compute_caps(s);   /* with the settling buffers in place */
     if (rc == 0) {
         s->visc_mode = viscosity_mode(s);
         /* the multigrid-preconditioned implicit solve needs at least one coarse level */
@@ -4373,6 +4476,8 @@ long osim_field(const OSim* s, const char* name, void* out, size_t cap) {
     F("grho", s->grho, nc * 16)
     F("gbase", s->gbase, nc * 16)
     F("rh", s->rh, nc * 16)
+    F("famocc", s->famocc, nc * 4 * (size_t)s->settle_fams)
+    F("dsettle", s->dsettle, nc * 8 * (size_t)s->settle_fams)
     F("surf2", s->surf2, nc * 16)
     F("tiles", s->tiles, (size_t)s->nwg * 4)
     F("vtile", s->vtile, (size_t)s->lv.tiles * 4)

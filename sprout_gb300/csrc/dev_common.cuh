@@ -63,6 +63,8 @@ struct DevScene {
     float* mixb;      // per cell, families 1 .. n_fam - 1: the family's concentration (-1: not here)
     float4* gbase;    // per cell: share x base density of phase groups 1 - 3 (w unused)
     float4* rh;       // per cell: its non-Newtonian liquid (share, row, concentration, stiff)
+    float* famocc;    // per cell and family: the family's occupancy (settling)
+    float2* dsettle;  // per cell and family: the concentration gain / loss rates settling hands the particles
     int2* hcell;
     const float4* solid;
     const float* sdf;

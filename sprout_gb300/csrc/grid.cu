@@ -66,6 +66,9 @@ __global__ void __launch_bounds__(256) k_grid_prep(DevScene d) {
         const int nmix = P->n_fam - 1;
         for (int q = 0; q < nmix; q++) d.mixb[(size_t)i * nmix + q] = -1.0f;
         float bg[3] = {0.0f, 0.0f, 0.0f};   // share x base density of groups 1 - 3
+        const bool settle = (P->caps & CAP_SETTLE) != 0u;
+        if (settle)
+            for (int q = 0; q < P->n_fam; q++) d.famocc[(size_t)i * P->n_fam + q] = 0.0f;
         if (cw > 0) {
             int others = 0;
             for (int j = 0; j < P->n_present; j++) {
@@ -137,6 +140,7 @@ __global__ void __launch_bounds__(256) k_grid_prep(DevScene d) {
                     const int fam = mats[r].ib[0];
                     if (fam == 0) fam0 = sc;
                     else if (fam > 0) d.mixb[(size_t)i * nmix + fam - 1] = sc;
+                    if (settle && fam >= 0) d.famocc[(size_t)i * P->n_fam + fam] = share * phi_f;
                 }
                 rho_m *= xp;
                 if (thermal) {
@@ -778,11 +782,57 @@ __global__ void __launch_bounds__(256) k_rheo(DevScene d) {
     d.cell[i] = me;
 }
 
+// The settling flux of family f between an upper cell and a lower one at terminal velocity vt:
+// concentrate leaving the upper cell into the diluent of the lower one, bounded by what either
+// holds (settle.comp:8-16).
+DEV float settle_flux(const DevScene& d, int up, int dn, int f, float vt) {
+    const int nf = d.P->n_fam;
+    const float ou = d.famocc[(size_t)up * nf + f], od = d.famocc[(size_t)dn * nf + f];
+    if (ou <= 1e-3f || od <= 1e-3f) return 0.0f;
+    const float su = f == 0 ? d.comp[up].z : d.mixb[(size_t)up * (nf - 1) + f - 1];
+    const float sd = f == 0 ? d.comp[dn].z : d.mixb[(size_t)dn * (nf - 1) + f - 1];
+    if (su <= 0.0f || sd < 0.0f) return 0.0f;
+    const float F = vt * su * (1.0f - sd) * minf(ou, od);
+    return minf(F, minf(su * ou, (1.0f - sd) * od) / d.S->dt);
+}
+
+// settle.comp: per cell and family with grains, the rates at which its particles gain
+// concentrate from the cell above (or below, for grains lighter than the diluent) and lose it
+// to the next, as fractions of what they can take or give this substep.
+__global__ void __launch_bounds__(256) k_settle(DevScene d) {
+    CELL_XY;
+    if (cx >= W || cy >= H) return;
+    const int i = cy * W + cx;
+    const DevParams* P = d.P;
+    const int nf = P->n_fam;
+    const bool thermal = (P->caps & CAP_THERMAL) != 0u;
+    for (int f = 0; f < nf; f++) {
+        const int row = P->fams[f][0], dl = P->fams[f][1];
+        const float gd = d.mats[row].b[2];
+        const float occ = d.famocc[(size_t)i * nf + f];
+        float2 ds = make_float2(0.0f, 0.0f);
+        if (gd > 0.0f && occ > 1e-3f && cy > 0 && cy < H - 1) {
+            const float drho = d.mats[row].a[0] - d.mats[dl].a[0];
+            const float T = thermal ? d.therm[i].x : P->heat[0];
+            // row_lnu of the (plain) diluent at concentration 1
+            const float lnu = d.mats[dl].a[1] + (thermal ? temp_law(d.mats, dl, T) : 0.0f);
+            const float vt = terminal(drho, d.mats[dl].a[0], sp_expf(lnu), gd, P->gravity);
+            const float gain = drho > 0.0f ? settle_flux(d, i + W, i, f, vt) : settle_flux(d, i - W, i, f, vt);
+            const float loss = drho > 0.0f ? settle_flux(d, i, i - W, f, vt) : settle_flux(d, i, i + W, f, vt);
+            const float sv = f == 0 ? d.comp[i].z : d.mixb[(size_t)i * (nf - 1) + f - 1];
+            const float dt = d.S->dt;
+            ds = make_float2(dt * (gain / maxf(occ * (1.0f - sv), 1e-6f)), dt * (loss / maxf(occ * sv, 1e-6f)));
+        }
+        d.dsettle[(size_t)i * nf + f] = ds;
+    }
+}
+
 void launch_grid(const DevScene& d, const LaunchCfg& cfg, cudaStream_t st) {
     dim3 blk(16, 16);
     dim3 grd((d.W + 15) / 16, (d.H + 15) / 16);
     k_grid_prep<<<grd, blk, 0, st>>>(d);
     if (cfg.rheo) k_rheo<<<grd, blk, 0, st>>>(d);
+    if (cfg.settle) k_settle<<<grd, blk, 0, st>>>(d);
     k_coef_smooth<<<grd, blk, 0, st>>>(d);
     k_curv<<<grd, blk, 0, st>>>(d);
     k_apply<<<grd, blk, 0, st>>>(d);

@@ -334,7 +334,7 @@ __global__ void __launch_bounds__(256) k_advance(DevScene d) {
                     // with concentration families: sw, the weight of the cells holding liquid;
                     // sfw, sfs, the weight and concentration of those that hold the particle's
                     // own family (a diluent's: family 0)
-                    const int fam = mats[row].ib[0];
+                    int fam = mats[row].ib[0];
                     const int nmix = P->n_fam - 1;
                     const bool fams = P->n_fam > 0;
                     // with several phase groups: sg, the shares of groups 1 - 3 around the
@@ -372,6 +372,36 @@ __global__ void __launch_bounds__(256) k_advance(DevScene d) {
                                 }
                             }
                         }
+                    if ((P->caps & CAP_SETTLE) != 0u) {
+                        // Settling hands each cell a change of its family's concentration, taken
+                        // with the scatter's weights; the first row, as the primary family's
+                        // diluent, takes part at concentration 0 (particles.comp:331-352).
+                        const bool dil0 = fam < 0 && P->primary >= 0 && P->fams[0][1] == (int)row;
+                        const int sf = dil0 ? 0 : fam;
+                        if (sf >= 0 && (kind & KIND_FRESH) == 0u && mats[dil0 ? (uint32_t)P->primary : row].b[2] > 0.0f) {
+                            float dsx = 0.0f, dsy = 0.0f;
+#pragma unroll
+                            for (int b = 0; b < 3; b++)
+#pragma unroll
+                                for (int a = 0; a < 3; a++) {
+                                    const float2 v = d.dsettle[(size_t)((by + b) * d.W + bx + a) * P->n_fam + sf];
+                                    const float wt = wx[a] * wy[b];
+                                    dsx += wt * v.x;
+                                    dsy += wt * v.y;
+                                }
+                            const float s0 = dil0 ? 0.0f : ps;
+                            const float s1 = clampf(s0 + (1.0f - s0) * dsx - s0 * dsy, 0.0f, 1.0f);
+                            const float c0 = thermal ? thermal_of(mats, row, ps).w : 0.0f;
+                            if (dil0 && s1 > 0.0f) {
+                                row = (uint32_t)P->primary;
+                                ia1 = mats[row].ia[1];
+                                fam = 0;
+                                kind = (kind & ~255u) | (row + 1u);
+                            }
+                            if (!dil0 || s1 > 0.0f) ps = s1;
+                            if (thermal) pt = keep_heat(pt, c0, thermal_of(mats, row, ps).w);
+                        }
+                    }
                     if (thermal && (kind & KIND_FRESH) == 0u) {
                         float dT = 0.0f;
 #pragma unroll
@@ -390,14 +420,15 @@ __global__ void __launch_bounds__(256) k_advance(DevScene d) {
                     }
                     if (gather && sw > 1e-4f) {
                         const float sgx = sg0 / sw, sgy = sg1 / sw, sgz = sg2 / sw;
-                        const float fg = grp == 0 ? 1.0f - sgx - sgy - sgz : (grp == 1 ? sgx : grp == 2 ? sgy : sgz);
+                        const int gnow = mats[row].ia[0];   // the group of the row as settling left it
+                        const float fg = gnow == 0 ? 1.0f - sgx - sgy - sgz : (gnow == 1 ? sgx : gnow == 2 ? sgy : sgz);
                         const float others = 1.0f - fg;
                         if (others > 1e-4f && groups)
-                            slip = group_drift(d, mats, row, ps, grp, px, py, bx, by, wx, wy, sw, fg, others, sgx, sgy, sgz, dt);
+                            slip = group_drift(d, mats, row, ps, gnow, px, py, bx, by, wx, wy, sw, fg, others, sgx, sgy, sgz, dt);
                         if (sorts) {
                             // drift within the particle's own group against its local mean base
                             // density (particles.comp:478-502)
-                            const float fgi = groups ? (grp == 1 ? sgx : grp == 2 ? sgy : sgz) : 1.0f;
+                            const float fgi = groups ? (gnow == 1 ? sgx : gnow == 2 ? sgy : sgz) : 1.0f;
                             if (fgi > 1e-4f) {
                                 const float rmean = sbg / sw / fgi;
                                 const float drho = mats[row].a[0] - rmean;

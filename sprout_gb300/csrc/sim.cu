@@ -332,9 +332,32 @@ struct SproutSim {
         return 2;
     }
 
+    // Whether a family in the tank settles: a concentrate with grains under gravity (mod.rs:2139-2143).
+    bool settles() const {
+        if (!(params.gravity > 0.0f)) return false;
+        for (int r : tank.rows)
+            if (params.mat[r].diluent >= 0 && params.mat[r].grain > 0.0f) return true;
+        return false;
+    }
+
+    // The settling buffers for `fams` families (mod.rs:2114-2136): new zero-filled ones when the
+    // count grows or drops to none, the present ones otherwise.
+    int settle_fams = 0;
+    int set_settling(int fams) {
+        if (fams == settle_fams || (fams > 0 && fams < settle_fams)) return SPROUT_OK;
+        const size_t n = std::max<size_t>((size_t)W * H * (size_t)fams, 1);
+        int rc = alloc(&d.famocc, n);
+        if (rc == SPROUT_OK) rc = alloc(&d.dsettle, n);
+        if (rc != SPROUT_OK) return rc;
+        settle_fams = fams;
+        graph_ok = false;   // new device pointers: the captured substep is stale
+        return SPROUT_OK;
+    }
+
     uint32_t compute_caps() const {
         uint32_t c = 0;
         if (tank.families > 0) c |= CAP_FAMILIES;
+        if (settle_fams >= tank.families && tank.families > 0 && settles()) c |= CAP_SETTLE;
         if (thermal) c |= CAP_THERMAL;
         bool rigid = false;
         for (int r : tank.rows) {
@@ -511,6 +534,7 @@ struct SproutSim {
         want.thermal = thermal;
         want.heat = thermal && params.heat_rate > 0.0f;
         want.rheo = (caps & CAP_RHEO) != 0u;
+        want.settle = (caps & CAP_SETTLE) != 0u;
         want.visc_mode = visc_mode;
         want.twice = visc_mode == 2 && params.viscous_projection != 0;
         want.viscous_warm = params.viscous_warm != 0;
@@ -523,7 +547,7 @@ struct SproutSim {
             if (v > 0) want.visc_blocks = std::max(1, std::min(v, visc_max[want.visc_sweeps - 1]));
         }
         want.mixed = mixed;
-        bool same = want.n_slots == cfg.n_slots && want.thermal == cfg.thermal && want.heat == cfg.heat && want.rheo == cfg.rheo &&
+        bool same = want.n_slots == cfg.n_slots && want.thermal == cfg.thermal && want.heat == cfg.heat && want.rheo == cfg.rheo && want.settle == cfg.settle &&
                     want.visc_mode == cfg.visc_mode && want.twice == cfg.twice && want.viscous_warm == cfg.viscous_warm &&
                     want.visc_levels == cfg.visc_levels && want.visc_sweeps == cfg.visc_sweeps &&
                     want.visc_blocks == cfg.visc_blocks && want.mixed == cfg.mixed && d.stride == std::max(tank.stride, 8);
@@ -620,13 +644,15 @@ struct SproutSim {
         thermal = th;
         caps = compute_caps();
         int rc = SPROUT_OK;
-        if (caps & (CAP_RIGID | CAP_MAGNET | CAP_ELASTIC | CAP_SETTLE | CAP_STEAM | CAP_REACT))
-            rc = fail(SPROUT_E_UNSUPPORTED, "the tank needs rigid / magnet / elastic / settling / steam / reaction passes, which this engine does not carry");
+        if (caps & (CAP_RIGID | CAP_MAGNET | CAP_ELASTIC | CAP_STEAM | CAP_REACT))
+            rc = fail(SPROUT_E_UNSUPPORTED, "the tank needs rigid / magnet / elastic / steam / reaction passes, which this engine does not carry");
         for (int r : tank.rows) {
             const MatProps& m = params.mat[r];
             if (rc == SPROUT_OK && (m.volatility > 0.0f || (thermal && m.boil < 1e8f)))
                 rc = fail(SPROUT_E_UNSUPPORTED, "evaporation and boiling are not carried by this engine");
         }
+        if (rc == SPROUT_OK) rc = set_settling(settles() ? tank.families : 0);
+        if (rc == SPROUT_OK) caps = compute_caps();   // with the settling buffers in place
         if (rc == SPROUT_OK && tank.families > 1 && d.mixb == nullptr) {
             // the concentrations of families 1.. per cell, from the first tank that has them
             rc = alloc(&d.mixb, (size_t)W * H * (kMaxPresent - 1));
@@ -1647,6 +1673,8 @@ int sprout_sim_download_field(SproutSim* sim, const char* name, void* out, size_
     else if (n == "grho") { src = d.grho; b = nc * 16; }
     else if (n == "gbase") { src = d.gbase; b = nc * 16; }
     else if (n == "rh") { src = d.rh; b = nc * 16; }
+    else if (d.famocc && n == "famocc") { src = d.famocc; b = nc * 4 * (size_t)sim->settle_fams; }
+    else if (d.dsettle && n == "dsettle") { src = d.dsettle; b = nc * 8 * (size_t)sim->settle_fams; }
     else if (n == "surf2") { src = d.surf2; b = nc * 16; }
     else if (d.mixb && n == "mixb") { src = d.mixb; b = nc * 4 * (size_t)std::max(sim->tank.families - 1, 0); }
     else if (sim->visc_alloc && n == "tiles") { src = d.tiles; b = (size_t)d.nwg * 4; }

@@ -111,3 +111,14 @@ def shear_thinning(w: int = 96, h: int = 64, cell: float = 0.002, mat: int = 7) 
     box = lambda x0, y0, x1, y1: [float(int(x0 * sx)), float(int(y0 * sy)), float(int(x1 * sx)), float(int(y1 * sy))]
     fills = [(box(4, 4, 40, 44), mat, None), (box(60, 4, 92, 20), 0, None)]
     return Tank(w, h, s, [], fills)
+
+
+def settling(w: int = 96, h: int = 64, cell: float = 0.002, mat: int = 51) -> Tank:
+    """A suspension over clear water: silt (51, grains of 0.1 mm, a water concentrate) by
+    default, or mud (3: also shear-thinning). Its grains settle through the water below."""
+    key = {51: "silt", 3: "mud"}[mat]
+    s = {"cell_size": cell, "fixed_hz": 240.0, "pressure_tol": 1e-5, "viscosity_tol": 1e-5,
+         "tension_water": 0.0, f"tension_{key}": 0.0}
+    fills = [([0.0, 0.0, float(w), float(int(0.3 * h))], 0, None),
+             ([0.0, float(int(0.3 * h)), float(w), float(int(0.55 * h))], mat, None)]
+    return Tank(w, h, s, [], fills)
