@@ -50,6 +50,13 @@ typedef struct SproutTool {
     float strength;
 } SproutTool;
 
+/* Current (src/sim/params.rs:1113-1121): a zone (pos, radius, cells) that drives the liquid
+ * in it towards vel (cells / s) at `rate` (1 / s), or drains it at -rate when rate < 0. */
+typedef struct SproutCurrent {
+    float pos[2], radius, vel[2], rate;
+} SproutCurrent;
+#define SPROUT_MAX_CURRENTS 16
+
 /* SolverStats (src/sim/mod.rs:334-363) plus the step scalars of StepBuf (common.glsl:122-135). */
 typedef struct SproutSolverStats {
     uint64_t substeps;                 /* substeps run since the last reset */
@@ -144,6 +151,9 @@ int sprout_sim_set_solids(SproutSim* sim, const float* sdf, const float* solid4,
 /* FluidSim::reset (mod.rs:1981-2002): replaces every particle (ids = index, spawn fields
  * settled). SPROUT_E_UNSUPPORTED if the tank needs a capability the engine lacks. */
 int sprout_sim_reset(SproutSim* sim, const SproutParticle* p, uint32_t n);
+/* FluidSim::set_currents (mod.rs:2008-2012): replaces the currents, keeping the first
+ * SPROUT_MAX_CURRENTS; they act from the next step on and survive a reset. */
+int sprout_sim_set_currents(SproutSim* sim, const SproutCurrent* c, uint32_t n);
 /* FluidSim::spawn (mod.rs:2024-2046): queues particles for the next step call (new ids
  * follow the last given, spawn fields settled, marked fresh). *accepted = how many were
  * queued: at most SPROUT_SPAWN_MAX wait at once, particles without a material are skipped,

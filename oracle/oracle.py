@@ -129,6 +129,8 @@ def lib() -> C.CDLL:
         L.osim_set_params.argtypes = [C.c_void_p, P(OSimParams)]
         L.osim_set_solids.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
         L.osim_reset.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32]
+        L.osim_set_currents.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32]
+        L.osim_set_currents.restype = C.c_int
         L.osim_reset.restype = C.c_int
         L.osim_spawn.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32]
         L.osim_spawn.restype = C.c_int
@@ -224,6 +226,11 @@ class OracleSim:
     def reset(self, particles: np.ndarray) -> int:
         p = np.ascontiguousarray(particles, PARTICLE_DTYPE)
         return lib().osim_reset(self.h_, p.ctypes.data, len(p))
+
+    def set_currents(self, currents):
+        from sprout_gb300 import current_array
+        arr = current_array(currents)
+        return lib().osim_set_currents(self.h_, arr.ctypes.data if len(arr) else None, len(arr))
 
     def spawn(self, particles: np.ndarray) -> int:
         """FluidSim::spawn: how many were queued (0 when their materials do not fit)."""
@@ -363,6 +370,8 @@ def build_tank(tank, threads: int | None = None):
             parts["t"][before:] = t
             parts["kind"][before:] |= 0x20000
     sim = OracleSim(tank.w, tank.h, len(parts) + tank.capacity_extra, p)
+    if getattr(tank, "currents", None):
+        sim.set_currents(tank.currents)
     sim.set_solids(sdf, solid, region, temp)
     rc = sim.reset(parts)
     if rc != 0:

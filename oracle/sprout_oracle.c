@@ -613,6 +613,8 @@ typedef struct GParams {   /* common.glsl:37-86 (subset) */
     int tool_mode;
     float tool_strength;
     float tol[4], ext[4], corr[4], heat3[4];
+    float current_zone[O_MAX_CURRENTS][4];   /* common.glsl:76-77 */
+    float current_vel[O_MAX_CURRENTS][4];
     float corr_gain;   /* min(1 - exp(-dt / tol.w), density_k) is per substep: see rhs */
 } GParams;
 
@@ -684,6 +686,8 @@ struct OSim {
     float* famocc;   /* per cell and family: its occupancy (settling) */
     V2* dsettle;     /* per cell and family: the concentration gain / loss rates of settling */
     int settle_fams; /* families the settling buffers hold */
+    OCurrent currents[O_MAX_CURRENTS];   /* set_currents, kept across resets */
+    int n_currents;
     V2 *vel0, *pjump, *pres;
     float* p2keep;
     float* mixb;   /* per cell, families 1 .. n_fam - 1: the concentration (-1: not here) */
@@ -1045,7 +1049,16 @@ static void build_params(OSim* s, const OTool* tool) {
     P->ext[0] = speed_cap_cells(p, s->H);
     P->ext[1] = (float)p->advection_order;
     P->ext[2] = p->spray_cfl;
-    P->ext[3] = 0.0f;
+    P->ext[3] = (float)s->n_currents;
+    for (int i = 0; i < s->n_currents; i++) {   /* mod.rs:2265-2270 */
+        const OCurrent* c = &s->currents[i];
+        P->current_zone[i][0] = c->pos[0];
+        P->current_zone[i][1] = c->pos[1];
+        P->current_zone[i][2] = maxf(c->radius, 0.01f);
+        P->current_zone[i][3] = c->rate;
+        P->current_vel[i][0] = c->vel[0];
+        P->current_vel[i][1] = c->vel[1];
+    }
     P->corr[0] = p->correction_step_max;
     P->corr[1] = p->correction_deadband;
     P->corr[2] = (float)p->slip_cap;
@@ -1626,6 +1639,20 @@ static void advance(OSim* s, uint32_t id, int gather, Scat* g) {
                 }
             }
         }
+        /* drains (particles.comp:577-594) */
+        for (int c = 0; c < (int)P_.ext[3]; c++) {
+            const float* z = P_.current_zone[c];
+            if (z[3] >= 0.0f) continue;
+            V2 dz = v2(pos.x - z[0], pos.y - z[1]);
+            float r2 = (dz.x * dz.x + dz.y * dz.y) / (z[2] * z[2]);
+            if (r2 < 1.0f) {
+                float u = (float)(hash32(p.id * 2246822519u + s->S.substeps * 3266489917u + (uint32_t)c) >> 8) / 16777216.0f;
+                if (u < -z[3] * (1.0f - 0.75f * r2) * dt) {
+                    s->particles[id].kind = KIND_DEAD;
+                    return;
+                }
+            }
+        }
         /* mouse tool (particles.comp:596-631) */
         int pushed = 0;
         if (P_.tool_mode != 0) {
@@ -1660,6 +1687,26 @@ static void advance(OSim* s, uint32_t id, int gather, Scat* g) {
             float e = s->mats[row].rx[2] * s->mats[row].th[0] * (Mia[1] >= 0 ? p.s : 1.0f) * dt * P_.heat[1];
             p.t += e / thermal_of(s, row, p.s).w;
             ledger_add(s, 7, e * P_.inv_ppc);
+        }
+        /* currents (particles.comp:809-835) */
+        {
+            float drive = P_.tool_crowd_max > 0.0f ? clampf((P_.tool_crowd_max - crowd) / (0.25f * P_.tool_crowd_max), 0.0f, 1.0f) : 1.0f;
+            for (int c = 0; c < (int)P_.ext[3] && drive > 0.0f; c++) {
+                const float* z = P_.current_zone[c];
+                if (z[3] <= 0.0f) continue;
+                V2 dz = v2(pos.x - z[0], pos.y - z[1]);
+                float r2 = (dz.x * dz.x + dz.y * dz.y) / (z[2] * z[2]);
+                if (r2 < 1.0f) {
+                    V2 target = v2(P_.current_vel[c][0], P_.current_vel[c][1]);
+                    float speed = len2(target);
+                    V2 dir = v2(target.x / maxf(speed, 1e-6f), target.y / maxf(speed, 1e-6f));
+                    float fall = (1.0f - r2) * (1.0f - r2);
+                    float gap = maxf(speed - (v.x * dir.x + v.y * dir.y), 0.0f);
+                    float e = 1.0f - o_expf(-z[3] * fall * dt);
+                    v.x += dir.x * gap * e * drive;
+                    v.y += dir.y * gap * e * drive;
+                }
+            }
         }
         /* speed cap */
         float vcap = P_.ext[0];
@@ -4185,6 +4232,12 @@ void osim_destroy(OSim* s) {
                     s->vmb, s->vmd, s->vmr, s->vmx, s->vmz, s->tiles, s->vtile, s->pending, s->mixb, s->gbase, s->rh, s->famocc, s->dsettle};
     for (size_t k = 0; k < sizeof ptrs / sizeof ptrs[0]; k++) free(ptrs[k]);
     free(s);
+}
+
+int osim_set_currents(OSim* s, const OCurrent* c, uint32_t n) {   /* mod.rs:2008-2012 */
+    s->n_currents = 0;
+    for (uint32_t i = 0; i < n && i < O_MAX_CURRENTS; i++) s->currents[s->n_currents++] = c[i];
+    return 0;
 }
 
 int osim_set_params(OSim* s, const OSimParams* p) {

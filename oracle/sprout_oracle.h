@@ -55,6 +55,12 @@ typedef struct OMat {
 } OMat;
 
 #define O_MAX_MATERIALS 96
+#define O_MAX_CURRENTS 16
+
+/* Current (src/sim/params.rs:1113-1121) */
+typedef struct OCurrent {
+    float pos[2], radius, vel[2], rate;
+} OCurrent;
 #define O_GROUPS 4
 
 /* The SimParams fields the substep reads (src/sim/params.rs:149-375). */
@@ -127,6 +133,7 @@ uint32_t ofill_rect(int w, int h, int nshapes, const OShape* shapes, const float
 OSim* osim_create(int w, int h, uint32_t capacity, const OSimParams* p);
 void osim_destroy(OSim* s);
 int osim_set_params(OSim* s, const OSimParams* p);
+int osim_set_currents(OSim* s, const OCurrent* c, uint32_t n);
 int osim_set_solids(OSim* s, const float* sdf, const float* solid4, const uint32_t* region,
                     const float* temp);
 /* FluidSim::reset (src/sim/mod.rs:1981-2002): ids, settle_spawn, the tank's rows.

@@ -36,7 +36,7 @@ EXPORTS = [
     "sprout_params_set", "sprout_params_get", "sprout_params_set_diluent", "sprout_params_set_group", "sprout_scene_new", "sprout_scene_free", "sprout_scene_add_box",
     "sprout_scene_add_circle", "sprout_scene_sdf", "sprout_scene_rasterize", "sprout_fill_rect",
     "sprout_sim_create", "sprout_sim_destroy", "sprout_sim_set_params", "sprout_sim_set_solids",
-    "sprout_sim_reset", "sprout_sim_step", "sprout_sim_step_blocking", "sprout_sim_advance_blocking",
+    "sprout_sim_reset", "sprout_sim_set_currents", "sprout_sim_step", "sprout_sim_step_blocking", "sprout_sim_advance_blocking",
     "sprout_sim_sync", "sprout_sim_download_particles", "sprout_sim_download_pressure",
     "sprout_sim_download_field", "sprout_sim_stats", "sprout_sim_device_bytes", "sprout_sim_profile",
     "sprout_sim_profile_passes", "sprout_pressure_solve_static", "sprout_sim_set_precision",
@@ -117,6 +117,7 @@ def lib() -> C.CDLL:
         "sprout_sim_destroy": ([V], C.c_int), "sprout_sim_set_params": ([V, V], C.c_int),
         "sprout_sim_set_solids": ([V, V, V, V, V], C.c_int),
         "sprout_sim_reset": ([V, V, C.c_uint32], C.c_int),
+        "sprout_sim_set_currents": ([V, V, C.c_uint32], C.c_int),
         "sprout_sim_step": ([V, C.c_uint32, C.c_float, P(Tool)], C.c_int),
         "sprout_sim_step_blocking": ([V, C.c_uint32, P(Tool)], C.c_int),
         "sprout_sim_advance_blocking": ([V, C.c_double, P(Tool)], C.c_int),
@@ -159,6 +160,20 @@ def lib() -> C.CDLL:
 def _check(rc: int):
     if rc != SPROUT_OK:
         raise SproutError(rc, lib().sprout_last_error().decode())
+
+
+CURRENT_DTYPE = np.dtype([("pos", "<f4", 2), ("radius", "<f4"), ("vel", "<f4", 2), ("rate", "<f4")])
+
+
+def current_array(currents) -> np.ndarray:
+    """Current records (src/sim/params.rs:1113-1121) from dicts with pos, radius, vel, rate."""
+    arr = np.zeros(len(currents), CURRENT_DTYPE)
+    for k, c in enumerate(currents):
+        arr[k]["pos"] = c["pos"]
+        arr[k]["radius"] = c["radius"]
+        arr[k]["vel"] = c.get("vel", (0.0, 0.0))
+        arr[k]["rate"] = c["rate"]
+    return arr
 
 
 class SimParams:
@@ -282,6 +297,12 @@ class FluidSim:
     def reset(self, particles: np.ndarray):
         p = np.ascontiguousarray(particles, PARTICLE_DTYPE)
         _check(lib().sprout_sim_reset(self._h, p.ctypes.data, len(p)))
+
+    def set_currents(self, currents):
+        """FluidSim::set_currents: zones {pos, radius, vel, rate} (cells, cells / s, 1 / s; a
+        negative rate drains); the first 16 are kept, across resets."""
+        arr = current_array(currents)
+        _check(lib().sprout_sim_set_currents(self._h, arr.ctypes.data if len(arr) else None, len(arr)))
 
     def spawn(self, particles: np.ndarray) -> int:
         """FluidSim::spawn: queues particles for the next step; returns how many were taken

@@ -15,6 +15,7 @@ using array3i = std::array<int, 3>;
 namespace sprout {
 
 constexpr int kMaxPresent = 12;
+constexpr int kMaxCurrents = 16;   // params.rs: MAX_CURRENTS
 constexpr int kGroups = 4;
 constexpr int kMaxLevels = 24;
 
@@ -70,6 +71,10 @@ struct DevParams {
     int visc_sweeps;   // Gauss-Seidel sweeps per visit of a level (1 or 2)
     int viscosity_warm, viscous_warm, viscous_projection;
     int viscosity_precond;   // 0: the Jacobi-preconditioned iteration, 1: the multigrid one
+    // currents (params.rs:1113-1121): position (cells), radius, rate (1/s; negative: a drain);
+    // the velocity the liquid is driven towards (cells/s). ext[3] holds how many.
+    float current_zone[kMaxCurrents][4];
+    float current_vel[kMaxCurrents][4];
 };
 
 // StepBuf (common.glsl:122-135) plus the engine's own step flags.

@@ -552,7 +552,7 @@ static float tool_speed(const ToolState* t) {
 }
 
 void build_params(const SimParams& p, const Tank& t, bool thermal, uint32_t caps, int W, int H, uint32_t n_slots,
-                  float dt_limit, const ToolState* tool, DevParams* P) {
+                  float dt_limit, const ToolState* tool, DevParams* P, const std::vector<Current>& currents) {
     std::memset(P, 0, sizeof *P);
     float dx = p.cell_size;
     P->grid[0] = W;
@@ -636,7 +636,16 @@ void build_params(const SimParams& p, const Tank& t, bool thermal, uint32_t caps
     P->ext[0] = p.speed_cap_cells((uint32_t)H);
     P->ext[1] = (float)p.advection_order;
     P->ext[2] = p.spray_cfl;
-    P->ext[3] = 0.0f;
+    P->ext[3] = (float)currents.size();
+    for (size_t i = 0; i < currents.size() && i < (size_t)kMaxCurrents; i++) {   // mod.rs:2265-2270
+        const Current& c = currents[i];
+        P->current_zone[i][0] = c.pos[0];
+        P->current_zone[i][1] = c.pos[1];
+        P->current_zone[i][2] = std::max(c.radius, 0.01f);
+        P->current_zone[i][3] = c.rate;
+        P->current_vel[i][0] = c.vel[0];
+        P->current_vel[i][1] = c.vel[1];
+    }
     P->corr[0] = p.correction_step_max;
     P->corr[1] = p.correction_deadband;
     P->corr[2] = (float)p.slip_cap;

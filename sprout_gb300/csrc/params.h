@@ -104,6 +104,12 @@ struct SimParams {
     bool set_group(int row, int group);
 };
 
+// Current (params.rs:1113-1121): a zone that drives the liquid in it towards `vel` at `rate`
+// (1/s), or removes it at -rate when negative (a drain).
+struct Current {
+    float pos[2], radius, vel[2], rate;
+};
+
 // Tank (mod.rs:222-245).
 struct Tank {
     std::vector<int> rows;
@@ -118,7 +124,8 @@ struct Tank {
 // The material table and parameters in grid units for the device.
 void build_materials(const SimParams& p, const Tank& t, bool thermal, DevMat* out);
 void build_params(const SimParams& p, const Tank& t, bool thermal, uint32_t caps, int W, int H,
-                  uint32_t n_slots, float dt_limit, const ToolState* tool, DevParams* out);
+                  uint32_t n_slots, float dt_limit, const ToolState* tool, DevParams* out,
+                  const std::vector<Current>& currents = {});
 
 // The name of built-in row r (presets.rs BUILTINS keys), or "" past them.
 const char* builtin_key(int r);

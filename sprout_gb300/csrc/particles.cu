@@ -488,8 +488,21 @@ __global__ void __launch_bounds__(256) k_advance(DevScene d) {
                         }
                     }
                 }
+                // drains: a zone with a negative rate removes each particle in it with probability
+                // -rate (1 - 0.75 r^2) dt per substep (particles.comp:577-594)
+                const int ncur = (int)P->ext[3];
+                for (int c = 0; c < ncur && alive; c++) {
+                    const float* z = P->current_zone[c];
+                    if (z[3] >= 0.0f) continue;
+                    const float dzx = px - z[0], dzy = py - z[1];
+                    const float r2 = (dzx * dzx + dzy * dzy) / (z[2] * z[2]);
+                    if (r2 < 1.0f) {
+                        const float u = (float)(hash32(pid * 2246822519u + S->substeps * 3266489917u + (uint32_t)c) >> 8) / 16777216.0f;
+                        if (u < -z[3] * (1.0f - 0.75f * r2) * dt) alive = false;
+                    }
+                }
                 bool pushed = false;
-                if (P->tool_mode != 0) {
+                if (alive && P->tool_mode != 0) {
                     float dx = P->tool_pos[0] - px, dy = P->tool_pos[1] - py;
                     float r2 = (dx * dx + dy * dy) / (P->tool_radius * P->tool_radius);
                     if (r2 < 1.0f) {
@@ -520,6 +533,25 @@ __global__ void __launch_bounds__(256) k_advance(DevScene d) {
                         float e = mats[row].rx[2] * mats[row].th[0] * (ia1 >= 0 ? ps : 1.0f) * dt * P->heat[1];
                         pt += e / thermal_of(mats, row, ps).w;
                         ledger_add(d.ledger, 7, e * P->inv_ppc);
+                    }
+                    // currents: raise the velocity along each towards its speed, never brake, and
+                    // not in a crowd (particles.comp:809-835)
+                    const float drive = P->tool_crowd_max > 0.0f ? clampf((P->tool_crowd_max - crowd) / (0.25f * P->tool_crowd_max), 0.0f, 1.0f) : 1.0f;
+                    for (int c = 0; c < ncur && drive > 0.0f; c++) {
+                        const float* z = P->current_zone[c];
+                        if (z[3] <= 0.0f) continue;
+                        const float dzx = px - z[0], dzy = py - z[1];
+                        const float r2 = (dzx * dzx + dzy * dzy) / (z[2] * z[2]);
+                        if (r2 < 1.0f) {
+                            const float tx = P->current_vel[c][0], ty = P->current_vel[c][1];
+                            const float speed = len2(tx, ty);
+                            const float dx = tx / maxf(speed, 1e-6f), dy = ty / maxf(speed, 1e-6f);
+                            const float fall = (1.0f - r2) * (1.0f - r2);
+                            const float gap = maxf(speed - (vx * dx + vy * dy), 0.0f);
+                            const float e = 1.0f - sp_expf(-z[3] * fall * dt);
+                            vx += dx * gap * e * drive;
+                            vy += dy * gap * e * drive;
+                        }
                     }
                     float vcap = P->ext[0];
                     {

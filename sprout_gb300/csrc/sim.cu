@@ -343,6 +343,7 @@ struct SproutSim {
     // The settling buffers for `fams` families (mod.rs:2114-2136): new zero-filled ones when the
     // count grows or drops to none, the present ones otherwise.
     int settle_fams = 0;
+    std::vector<Current> currents;   // set_currents: kept across resets, like the reference's
     int set_settling(int fams) {
         if (fams == settle_fams || (fams > 0 && fams < settle_fams)) return SPROUT_OK;
         const size_t n = std::max<size_t>((size_t)W * H * (size_t)fams, 1);
@@ -395,7 +396,7 @@ struct SproutSim {
             CUDA_TRY(cudaEventCreateWithFlags(&stage_done, cudaEventDisableTiming));
         }
         DevParams P;
-        build_params(params, tank, thermal, caps, W, H, n_slots, dt_limit(), tool, &P);
+        build_params(params, tank, thermal, caps, W, H, n_slots, dt_limit(), tool, &P, currents);
         P.ext_speed = std::max(P.ext_speed, spawn_speed);   // mod.rs:2300
         P.visc_mode = visc_mode;
         P.visc_levels = std::min(P.visc_levels, d.lv.tail);
@@ -1574,6 +1575,16 @@ int sprout_sim_trace_read(SproutSim* sim, unsigned long long* out, size_t cap, s
 int sprout_sim_set_precision(SproutSim* sim, int mode) {
     if (!sim) return fail(SPROUT_E_ARG, "null argument");
     return sim->set_precision(mode);
+}
+int sprout_sim_set_currents(SproutSim* sim, const SproutCurrent* c, uint32_t n) {
+    if (!sim || (n > 0 && !c)) return fail(SPROUT_E_ARG, "null argument");
+    sim->currents.clear();
+    for (uint32_t i = 0; i < n && i < (uint32_t)kMaxCurrents; i++) {
+        Current q;
+        std::memcpy(&q, &c[i], sizeof q);
+        sim->currents.push_back(q);
+    }
+    return SPROUT_OK;
 }
 int sprout_sim_set_params(SproutSim* sim, const SproutParams* p) {
     if (!sim || !p) return fail(SPROUT_E_ARG, "null argument");

@@ -21,6 +21,7 @@ class Tank:
     capacity_extra: int = 64
     diluents: dict = field(default_factory=dict)    # custom row -> its diluent's row (a family)
     groups: dict = field(default_factory=dict)      # custom row -> its phase group (0-3)
+    currents: list = field(default_factory=list)    # dicts: pos, radius, vel, rate (negative: a drain)
 
     # ---- the engine -----------------------------------------------------------------------
     def engine(self):
@@ -47,6 +48,8 @@ class Tank:
                 parts["t"][before:] = t
                 parts["kind"][before:] |= 0x20000   # KIND_REAL_T: a temperature to settle
         sim = S.FluidSim(self.w, self.h, len(parts) + self.capacity_extra, p)
+        if self.currents:
+            sim.set_currents(self.currents)
         sim.set_solids(sdf, solid, region, temp)
         sim.reset(parts)
         return sim, parts, (sdf, solid, region, temp)

@@ -122,3 +122,12 @@ def settling(w: int = 96, h: int = 64, cell: float = 0.002, mat: int = 51) -> Ta
     fills = [([0.0, 0.0, float(w), float(int(0.3 * h))], 0, None),
              ([0.0, float(int(0.3 * h)), float(w), float(int(0.55 * h))], mat, None)]
     return Tank(w, h, s, [], fills)
+
+
+def currents(w: int = 96, h: int = 64, cell: float = 0.002) -> Tank:
+    """A resting pool with a current driving its left half to the right and a drain near the
+    right wall's floor."""
+    t = dam_break(w, h, width=1.0, height=0.5)
+    t.currents = [{"pos": (0.25 * w, 0.2 * h), "radius": 0.15 * h, "vel": (60.0, 5.0), "rate": 20.0},
+                  {"pos": (0.85 * w, 0.08 * h), "radius": 0.1 * h, "vel": (0.0, 0.0), "rate": -30.0}]
+    return t

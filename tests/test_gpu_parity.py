@@ -199,3 +199,10 @@ def test_full_physics_pour_bit_exact():
         problems.append(f"pressure iterations differ: {list(a.pressure_iters)}/{a.pressure2_iters} vs "
                         f"{list(b.p_iters)}/{b.p2_iters}")
     assert not problems, "\n".join(problems)
+
+
+def test_currents_and_drains_bit_exact():
+    """A current driving the liquid and a drain removing it (particles.comp:577-594, 809-835)."""
+    sim, ora, problems = run_pair(tanks.currents(), 16)
+    assert not problems, "\n".join(problems[:10])
+    assert sim.stats().n_live < len(tanks.currents().engine()[1])
