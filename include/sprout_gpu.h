@@ -173,6 +173,13 @@ int sprout_sim_cell_counts(SproutSim* sim, const int32_t lo[2], const int32_t hi
  * `target` seconds (ignored with a fixed step rate). Asynchronous on the sim's stream.
  * tool may be NULL. */
 int sprout_sim_step(SproutSim* sim, uint32_t substeps, float target, const SproutTool* tool);
+/* FluidSim::frame_blocking (mod.rs:3342-3349): sprout_sim_step, then waits for it; *advanced =
+ * the simulated seconds it covered. */
+int sprout_sim_frame_blocking(SproutSim* sim, uint32_t substeps, float target, const SproutTool* tool,
+                              double* advanced);
+/* FluidSim::dt_estimate (mod.rs:1960-1963): the substep length the next step will most likely
+ * take, s (1 / fixed_hz with a fixed rate, else the last CFL estimate read back). */
+int sprout_sim_dt_estimate(SproutSim* sim, float* dt);
 /* FluidSim::step_blocking (mod.rs:3315-3338): `substeps` ticks of 1/240 s, blocking. */
 int sprout_sim_step_blocking(SproutSim* sim, uint32_t substeps, const SproutTool* tool);
 /* FluidSim::advance_blocking (mod.rs:3284-3312): exactly `seconds`, blocking. */

@@ -36,7 +36,7 @@ EXPORTS = [
     "sprout_params_set", "sprout_params_get", "sprout_params_set_diluent", "sprout_params_set_group", "sprout_scene_new", "sprout_scene_free", "sprout_scene_add_box",
     "sprout_scene_add_circle", "sprout_scene_sdf", "sprout_scene_rasterize", "sprout_fill_rect",
     "sprout_sim_create", "sprout_sim_destroy", "sprout_sim_set_params", "sprout_sim_set_solids",
-    "sprout_sim_reset", "sprout_sim_set_currents", "sprout_sim_step", "sprout_sim_step_blocking", "sprout_sim_advance_blocking",
+    "sprout_sim_reset", "sprout_sim_set_currents", "sprout_sim_frame_blocking", "sprout_sim_dt_estimate", "sprout_sim_step", "sprout_sim_step_blocking", "sprout_sim_advance_blocking",
     "sprout_sim_sync", "sprout_sim_download_particles", "sprout_sim_download_pressure",
     "sprout_sim_download_field", "sprout_sim_stats", "sprout_sim_device_bytes", "sprout_sim_profile",
     "sprout_sim_profile_passes", "sprout_pressure_solve_static", "sprout_sim_set_precision",
@@ -118,6 +118,8 @@ def lib() -> C.CDLL:
         "sprout_sim_set_solids": ([V, V, V, V, V], C.c_int),
         "sprout_sim_reset": ([V, V, C.c_uint32], C.c_int),
         "sprout_sim_set_currents": ([V, V, C.c_uint32], C.c_int),
+        "sprout_sim_frame_blocking": ([V, C.c_uint32, C.c_float, V, P(C.c_double)], C.c_int),
+        "sprout_sim_dt_estimate": ([V, P(C.c_float)], C.c_int),
         "sprout_sim_step": ([V, C.c_uint32, C.c_float, P(Tool)], C.c_int),
         "sprout_sim_step_blocking": ([V, C.c_uint32, P(Tool)], C.c_int),
         "sprout_sim_advance_blocking": ([V, C.c_double, P(Tool)], C.c_int),
@@ -297,6 +299,18 @@ class FluidSim:
     def reset(self, particles: np.ndarray):
         p = np.ascontiguousarray(particles, PARTICLE_DTYPE)
         _check(lib().sprout_sim_reset(self._h, p.ctypes.data, len(p)))
+
+    def frame_blocking(self, substeps: int, target: float, tool: "Tool | None" = None) -> float:
+        """FluidSim::frame_blocking: steps and waits; the simulated seconds covered."""
+        adv = C.c_double()
+        _check(lib().sprout_sim_frame_blocking(self._h, substeps, float(target), None if tool is None else C.byref(tool), C.byref(adv)))
+        return adv.value
+
+    def dt_estimate(self) -> float:
+        """FluidSim::dt_estimate: the substep length the next step will most likely take, s."""
+        dt = C.c_float()
+        _check(lib().sprout_sim_dt_estimate(self._h, C.byref(dt)))
+        return dt.value
 
     def set_currents(self, currents):
         """FluidSim::set_currents: zones {pos, radius, vel, rate} (cells, cells / s, 1 / s; a

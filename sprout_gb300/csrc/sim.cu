@@ -1624,6 +1624,20 @@ int sprout_sim_step(SproutSim* sim, uint32_t substeps, float target, const Sprou
     if (!sim) return fail(SPROUT_E_ARG, "null sim");
     return sim->step(substeps, target, reinterpret_cast<const ToolState*>(tool));
 }
+int sprout_sim_frame_blocking(SproutSim* sim, uint32_t substeps, float target, const SproutTool* tool, double* advanced) {
+    if (!sim || !advanced) return fail(SPROUT_E_ARG, "null argument");
+    const double start = sim->sim_time;
+    int rc = sim->step(substeps, target, reinterpret_cast<const ToolState*>(tool));
+    if (rc == SPROUT_OK) rc = sim->poll();
+    if (rc == SPROUT_OK) rc = sim->check_device_error();
+    *advanced = sim->sim_time - start;
+    return rc;
+}
+int sprout_sim_dt_estimate(SproutSim* sim, float* dt) {
+    if (!sim || !dt) return fail(SPROUT_E_ARG, "null argument");
+    *dt = sim->dt_estimate();
+    return SPROUT_OK;
+}
 int sprout_sim_step_blocking(SproutSim* sim, uint32_t substeps, const SproutTool* tool) {
     if (!sim) return fail(SPROUT_E_ARG, "null sim");
     return sim->step_blocking(substeps, reinterpret_cast<const ToolState*>(tool));

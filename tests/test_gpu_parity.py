@@ -206,3 +206,10 @@ def test_currents_and_drains_bit_exact():
     sim, ora, problems = run_pair(tanks.currents(), 16)
     assert not problems, "\n".join(problems[:10])
     assert sim.stats().n_live < len(tanks.currents().engine()[1])
+
+
+def test_frame_blocking_reports_the_time_covered():
+    sim, _, _ = tanks.dam_break(96, 64).engine()
+    adv = sim.frame_blocking(4, 4 / 240.0)
+    assert abs(adv - 4 / 240.0) < 1e-6
+    assert abs(sim.dt_estimate() - 1 / 240.0) < 1e-9
