@@ -57,6 +57,13 @@ typedef struct SproutCurrent {
 } SproutCurrent;
 #define SPROUT_MAX_CURRENTS 16
 
+/* Magnet (src/sim/params.rs:1082-1087): a point dipole at pos (cells), radius (cells), field
+ * strength on its axis at the rim (T), north pole along dir. */
+typedef struct SproutMagnet {
+    float pos[2], radius, strength, dir[2];
+} SproutMagnet;
+#define SPROUT_MAX_MAGNETS 8
+
 /* SolverStats (src/sim/mod.rs:334-363) plus the step scalars of StepBuf (common.glsl:122-135). */
 typedef struct SproutSolverStats {
     uint64_t substeps;                 /* substeps run since the last reset */
@@ -154,6 +161,10 @@ int sprout_sim_reset(SproutSim* sim, const SproutParticle* p, uint32_t n);
 /* FluidSim::set_currents (mod.rs:2008-2012): replaces the currents, keeping the first
  * SPROUT_MAX_CURRENTS; they act from the next step on and survive a reset. */
 int sprout_sim_set_currents(SproutSim* sim, const SproutCurrent* c, uint32_t n);
+/* FluidSim::set_magnets (mod.rs:2018-2022): replaces the magnets, keeping the first
+ * SPROUT_MAX_MAGNETS; they survive a reset. With a susceptible liquid in the tank (its
+ * `susceptibility`) the field's energy pulls on it (magnet.comp). */
+int sprout_sim_set_magnets(SproutSim* sim, const SproutMagnet* m, uint32_t n);
 /* FluidSim::spawn (mod.rs:2024-2046): queues particles for the next step call (new ids
  * follow the last given, spawn fields settled, marked fresh). *accepted = how many were
  * queued: at most SPROUT_SPAWN_MAX wait at once, particles without a material are skipped,

@@ -40,6 +40,7 @@ class OMat(C.Structure):
         ("friction", C.c_float), ("self_heat", C.c_float), ("volatility", C.c_float),
         ("react_with", C.c_int32), ("react_rate", C.c_float), ("fume", C.c_float),
         ("yield_stress", C.c_float), ("flow_index", C.c_float), ("shear_time", C.c_float), ("visc_ratio", C.c_float),
+        ("saturation", C.c_float),
     ]
 
 
@@ -64,6 +65,7 @@ class OSimParams(C.Structure):
         ("tool_crowd_max", C.c_float), ("apic_clamp", C.c_float), ("curvature_max", C.c_float),
         ("slip_cap", C.c_uint32), ("sealed_vent", C.c_uint32),
         ("mat", OMat * 96),
+        ("magnet_demag", C.c_float),
     ]
 
 
@@ -130,6 +132,8 @@ def lib() -> C.CDLL:
         L.osim_set_solids.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
         L.osim_reset.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32]
         L.osim_set_currents.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32]
+        L.osim_set_magnets.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32]
+        L.osim_set_magnets.restype = C.c_int
         L.osim_set_currents.restype = C.c_int
         L.osim_reset.restype = C.c_int
         L.osim_spawn.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32]
@@ -226,6 +230,11 @@ class OracleSim:
     def reset(self, particles: np.ndarray) -> int:
         p = np.ascontiguousarray(particles, PARTICLE_DTYPE)
         return lib().osim_reset(self.h_, p.ctypes.data, len(p))
+
+    def set_magnets(self, magnets):
+        from sprout_gb300 import magnet_array
+        arr = magnet_array(magnets)
+        return lib().osim_set_magnets(self.h_, arr.ctypes.data if len(arr) else None, len(arr))
 
     def set_currents(self, currents):
         from sprout_gb300 import current_array
@@ -372,6 +381,8 @@ def build_tank(tank, threads: int | None = None):
     sim = OracleSim(tank.w, tank.h, len(parts) + tank.capacity_extra, p)
     if getattr(tank, "currents", None):
         sim.set_currents(tank.currents)
+    if getattr(tank, "magnets", None):
+        sim.set_magnets(tank.magnets)
     sim.set_solids(sdf, solid, region, temp)
     rc = sim.reset(parts)
     if rc != 0:

@@ -221,6 +221,7 @@ static void mat_default(OMat* m) {
     m->flow_index = 1.0f;
     m->shear_time = 1.0f;
     m->visc_ratio = 1.0f;
+    m->saturation = 0.05f;
 }
 
 void oparams_default(OSimParams* p) {
@@ -613,6 +614,8 @@ typedef struct GParams {   /* common.glsl:37-86 (subset) */
     int tool_mode;
     float tool_strength;
     float tol[4], ext[4], corr[4], heat3[4];
+    float mag[4];   /* magnets, strongest susceptibility, its saturation, 1 / (rho_w dx^2) */
+    float magnet[O_MAX_MAGNETS][4], magnet_dir[O_MAX_MAGNETS][4];
     float current_zone[O_MAX_CURRENTS][4];   /* common.glsl:76-77 */
     float current_vel[O_MAX_CURRENTS][4];
     float corr_gain;   /* min(1 - exp(-dt / tol.w), density_k) is per substep: see rhs */
@@ -687,6 +690,9 @@ struct OSim {
     V2* dsettle;     /* per cell and family: the concentration gain / loss rates of settling */
     int settle_fams; /* families the settling buffers hold */
     OCurrent currents[O_MAX_CURRENTS];   /* set_currents, kept across resets */
+    OMagnet magnets[O_MAX_MAGNETS];      /* set_magnets, likewise */
+    int n_magnets;
+    V2* magc;   /* per cell: susceptibility; magnetic energy density (magnet.comp) */
     int n_currents;
     V2 *vel0, *pjump, *pres;
     float* p2keep;
@@ -890,6 +896,8 @@ static uint32_t compute_caps(const OSim* s) {   /* mod.rs:2717-2761 (the bits th
     if (rigid) caps |= CAP_RIGID;
     for (int k = 0; k < s->tank.nrows; k++)
         if (s->tank.rows[k] == 57 && s->thermal) caps |= CAP_STEAM;
+    for (int k = 0; k < s->tank.nrows; k++)   /* mod.rs:2749-2751 */
+        if (s->n_magnets > 0 && p->mat[s->tank.rows[k]].susceptibility > 0.0f) caps |= CAP_MAGNET;
     return caps;
 }
 
@@ -1066,6 +1074,28 @@ static void build_params(OSim* s, const OTool* tool) {
     P->heat3[0] = maxf(p->eddy_heat, 0.0f);
     P->heat3[1] = p->evaporation ? 2.257e6f / 1005.0f : 0.0f;
     P->heat3[2] = 0.0f;
+    P->heat3[3] = clampf(p->magnet_demag, 0.0f, 1.0f);
+    float chi_max = 0.0f, sat = 0.05f;   /* mod.rs:2264 */
+    for (int k = 0; k < s->tank.nrows; k++) {
+        const OMat* m = &p->mat[s->tank.rows[k]];
+        if (m->susceptibility > chi_max) {
+            chi_max = m->susceptibility;
+            sat = m->saturation;
+        }
+    }
+    P->mag[0] = (float)s->n_magnets;
+    P->mag[1] = maxf(chi_max, 1e-6f);
+    P->mag[2] = sat;
+    P->mag[3] = 1.0f / (WATER_DENSITY * p->cell_size * p->cell_size);
+    for (int i = 0; i < s->n_magnets; i++) {   /* mod.rs:2258-2263 */
+        const OMagnet* m = &s->magnets[i];
+        P->magnet[i][0] = m->pos[0];
+        P->magnet[i][1] = m->pos[1];
+        P->magnet[i][2] = maxf(m->radius, 0.5f);
+        P->magnet[i][3] = m->strength;
+        P->magnet_dir[i][0] = m->dir[0];
+        P->magnet_dir[i][1] = m->dir[1];
+    }
 }
 
 /* Levels::new (mod.rs:734-753) */
@@ -1966,6 +1996,7 @@ static void k_grid_prep(OSim* s) {
             V2 contact = v2(0.0f, 0.0f);
             float fam0 = -1.0f;
             V4 nn = v4(0.0f, -1.0f, 1.0f, 0.0f);   /* grid_prep.comp:62: the cell's non-Newtonian liquid */
+            float chi = 0.0f;   /* grid_prep.comp:63 */
             float rho = 0.0f, mu = 0.0f, rho_c = 0.0f, nu_c = 0.0f;
             int thermal = has_cap(s, CAP_THERMAL);
             const int nmix = P_.n_fam - 1;   /* grid_prep.comp:67-68 */
@@ -2050,6 +2081,7 @@ static void k_grid_prep(OSim* s) {
                         top_share = share;
                         top_row = r;
                     }
+                    chi += share * s->mats[r].el[2];   /* grid_prep.comp:168 */
                     int g = ia[0];
                     if (g > 0) bg[g - 1] += share * ma[0];   /* grid_prep.comp:172 */
                     f[g] += share;
@@ -2077,8 +2109,16 @@ static void k_grid_prep(OSim* s) {
             if (has && level <= 0.0f && cx > 0 && cy > 0 && cx < W - 1 && cy < H - 1) {
                 if ((packed(s, i - 1) && packed(s, i + 1)) || (packed(s, i - W) && packed(s, i + W))) level = 0.05f;
                 else if (P_.gravity > 0.0f && nn.x <= 0.0f && phi_t > 0.25f && packed(s, i - W)) level = 0.05f;
+                else if ((s->caps & CAP_MAGNET) && nn.x <= 0.0f && phi_t > 0.25f && chi > 0.0f) {   /* grid_prep.comp:216-220 */
+                    float km = chi / P_.mag[1] / maxf(rho, 0.05f);
+                    float pk = -km * 0.5f;
+                    V2 pull = v2(pk * (s->magc[i + 1].y - s->magc[i - 1].y) - 0.0f, pk * (s->magc[i + W].y - s->magc[i - W].y) - P_.gravity);
+                    int toward = fabsf(pull.x) > fabsf(pull.y) ? (pull.x > 0.0f ? i + 1 : i - 1) : (pull.y > 0.0f ? i + W : i - W);
+                    if (packed(s, toward)) level = 0.05f;
+                }
             }
             if (sol.w > 0.0f && level <= 0.0f) region_air |= 1u << (s->region[i] & REGION_MASK);
+            if (s->caps & CAP_MAGNET) s->magc[i].x = chi;   /* grid_prep.comp:240 */
             if (s->caps & (CAP_RIGID | CAP_RHEO)) {   /* grid_prep.comp:232-237 */
                 float cap = rho * o_expf(P_.heat2[0]);
                 if (mu >= cap && level > 0.0f) nn.w = 1.0f;
@@ -2145,6 +2185,78 @@ static void nn_eval(const OSim* s, int i, V4 q, float g, float* Fo, float* tauo)
         tau += skin;
     *Fo = 1.0f + q.x * (F - 1.0f);
     *tauo = tau * q.x;
+}
+
+/* common.glsl:388-402: the magnets' field at (x, y), T */
+static V2 magnet_field(const OSim* s, float x, float y) {
+    V2 B = v2(0.0f, 0.0f);
+    for (int k = 0; k < (int)P_.mag[0]; k++) {
+        const float* mg = P_.magnet[k];
+        V2 m = v2(P_.magnet_dir[k][0], P_.magnet_dir[k][1]);
+        V2 d = v2(x - mg[0], y - mg[1]);
+        float len = len2(d);
+        float r = maxf(len, mg[2]);
+        V2 e = len > 1e-4f ? v2(d.x / len, d.y / len) : m;
+        float a = mg[3] * o_powf(mg[2] / r, 3.0f) * 0.5f;
+        float me3 = 3.0f * (m.x * e.x + m.y * e.y);
+        B.x += a * (me3 * e.x - m.x);
+        B.y += a * (me3 * e.y - m.y);
+    }
+    return B;
+}
+
+/* magnet.comp mode 0: the magnetic energy density of pure magnetic liquid per cell */
+static void k_magnet_energy(OSim* s) {
+    int W = s->W, H = s->H;
+    const float MU0 = 1.25663706e-6f;
+#pragma omp parallel for schedule(static)
+    for (int cy = 0; cy < H; cy++)
+        for (int cx = 0; cx < W; cx++) {
+            int i = cy * W + cx;
+            V2 B = magnet_field(s, (float)cx + 0.5f, (float)cy + 0.5f);
+            float Bl = len2(B);
+            float Hf = Bl / MU0;
+            float psi = 0.0f;
+            float chi = P_.mag[1];
+            if (Hf > 0.0f && chi > 0.0f) {
+                float N = 1.0f / 3.0f;
+                if (P_.heat3[3] > 0.0f) {
+                    V2 g = v2(0.0f, 0.0f);
+                    if (cx > 0 && cy > 0 && cx < W - 1 && cy < H - 1)
+                        g = v2(0.5f * (s->surf[i + 1].x - s->surf[i - 1].x), 0.5f * (s->surf[i + W].x - s->surf[i - W].x));
+                    float gl = len2(g);
+                    float nh = gl > 1e-6f ? (g.x / gl) * (B.x / Bl) + (g.y / gl) * (B.y / Bl) : 0.0f;
+                    N = mixf(1.0f / 3.0f, nh * nh, clampf(gl / 0.25f, 0.0f, 1.0f) * P_.heat3[3]);
+                }
+                float ce = chi / (1.0f + N * chi);
+                float Ms = P_.mag[2] / MU0;
+                float xs = ce * Hf / Ms;
+                float f = xs < 0.02f ? xs * xs * (0.5f - xs * (1.0f / 3.0f - 0.25f * xs)) : xs - o_logf(1.0f + xs);
+                psi = -MU0 * Ms * Ms / ce * f * P_.mag[3];
+            }
+            s->magc[i].y = psi;
+        }
+}
+
+/* magnet.comp mode 1: the energy gradient's force on the liquid's faces */
+static float magnet_face_force(const OSim* s, int i, int n, float rho) {
+    int li = s->cell[i].w > 0.0f, ln = s->cell[n].w > 0.0f;
+    float sc = (li == ln ? 0.5f * (s->magc[i].x + s->magc[n].x) : li ? s->magc[i].x : s->magc[n].x) / P_.mag[1];
+    return -s->S.dt * sc * (s->magc[i].y - s->magc[n].y) / maxf(rho, 0.05f);
+}
+
+static void k_magnet_force(OSim* s) {
+    int W = s->W, H = s->H;
+#pragma omp parallel for schedule(static)
+    for (int cy = 1; cy < H; cy++)
+        for (int cx = 1; cx < W; cx++) {
+            int i = cy * W + cx;
+            V4 me = s->vel[i];
+            V4 cf = s->coef[i];
+            if (face_live(me.z) && cf.x != 0.0f) me.x += magnet_face_force(s, i, i - 1, cf.z);
+            if (face_live(me.w) && cf.y != 0.0f) me.y += magnet_face_force(s, i, i - W, cf.w);
+            s->vel[i] = me;
+        }
 }
 
 /* settle.comp:8-16: family f's settling flux from an upper cell into a lower one */
@@ -4150,6 +4262,10 @@ static void substep(OSim* s, int gather) {
     k_surf_smooth(s);
     k_surf_curv(s);
     k_surf_apply(s);
+    if (s->caps & CAP_MAGNET) {
+        k_magnet_energy(s);
+        k_magnet_force(s);
+    }
     if (s->thermal && s->prm.heat_rate > 0.0f) k_heat(s);
     if (s->visc_mode == 1) {
         k_visc_setup(s);
@@ -4205,6 +4321,7 @@ OSim* osim_create(int w, int h, uint32_t capacity, const OSimParams* p) {
     ALLOC(s->mixb, nc * (MAX_PRESENT - 1));
     ALLOC(s->gbase, nc);
     ALLOC(s->rh, nc);
+    ALLOC(s->magc, nc);
     ALLOC(s->pres, nc); ALLOC(s->p2keep, nc); ALLOC(s->hcell, nc); ALLOC(s->solid, nc);
     ALLOC(s->sdf, (size_t)(w + 1) * (h + 1)); ALLOC(s->region, nc); ALLOC(s->solid_t, nc);
     ALLOC(s->mga, s->lv.total); ALLOC(s->mgd, s->lv.total); ALLOC(s->mgx, s->lv.total);
@@ -4229,9 +4346,16 @@ void osim_destroy(OSim* s) {
                     s->vel0, s->pjump, s->pres, s->p2keep, s->hcell, s->solid, s->sdf, s->region,
                     s->solid_t, s->mga, s->mgd, s->mgx, s->mgz, s->mgr, s->cgp, s->cgp2, s->cgq,
                     s->ptile, s->part, s->vr, s->vr2, s->vp, s->vq, s->vq2, s->vd, s->vaz, s->vma,
-                    s->vmb, s->vmd, s->vmr, s->vmx, s->vmz, s->tiles, s->vtile, s->pending, s->mixb, s->gbase, s->rh, s->famocc, s->dsettle};
+                    s->vmb, s->vmd, s->vmr, s->vmx, s->vmz, s->tiles, s->vtile, s->pending, s->mixb, s->gbase, s->rh, s->famocc, s->dsettle, s->magc};
     for (size_t k = 0; k < sizeof ptrs / sizeof ptrs[0]; k++) free(ptrs[k]);
     free(s);
+}
+
+int osim_set_magnets(OSim* s, const OMagnet* m, uint32_t n) {   /* mod.rs:2018-2022 */
+    s->n_magnets = 0;
+    for (uint32_t i = 0; i < n && i < O_MAX_MAGNETS; i++) s->magnets[s->n_magnets++] = m[i];
+    if (s->tank.nrows > 0) s->caps = compute_caps(s);
+    return 0;
 }
 
 int osim_set_currents(OSim* s, const OCurrent* c, uint32_t n) {   /* mod.rs:2008-2012 */
@@ -4338,7 +4462,7 @@ static int set_tank(OSim* s, const int* present, int thermal) {
     s->thermal = thermal;
     s->caps = compute_caps(s);
     int rc = 0;
-    if (s->caps & (CAP_RIGID | CAP_MAGNET | CAP_ELASTIC | CAP_STEAM | CAP_REACT)) rc = -4;
+    if (s->caps & (CAP_RIGID | CAP_ELASTIC | CAP_STEAM | CAP_REACT)) rc = -4;
     for (int k = 0; k < nrows; k++) {
         const OMat* m = &p->mat[rows[k]];
         if (m->volatility > 0.0f || (thermal && m->boil < 1e8f)) rc = -4;
@@ -4529,6 +4653,7 @@ long osim_field(const OSim* s, const char* name, void* out, size_t cap) {
     F("grho", s->grho, nc * 16)
     F("gbase", s->gbase, nc * 16)
     F("rh", s->rh, nc * 16)
+    F("magc", s->magc, nc * 8)
     F("famocc", s->famocc, nc * 4 * (size_t)s->settle_fams)
     F("dsettle", s->dsettle, nc * 8 * (size_t)s->settle_fams)
     F("surf2", s->surf2, nc * 16)

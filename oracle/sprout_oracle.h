@@ -52,10 +52,18 @@ typedef struct OMat {
     float react_rate;
     float fume;
     float yield_stress, flow_index, shear_time, visc_ratio;
+    float saturation;
 } OMat;
 
 #define O_MAX_MATERIALS 96
 #define O_MAX_CURRENTS 16
+
+#define O_MAX_MAGNETS 8
+
+/* Magnet (src/sim/params.rs:1082-1087) */
+typedef struct OMagnet {
+    float pos[2], radius, strength, dir[2];
+} OMagnet;
 
 /* Current (src/sim/params.rs:1113-1121) */
 typedef struct OCurrent {
@@ -84,6 +92,7 @@ typedef struct OSimParams {
     float correction_step_max, crowd_jitter, tool_crowd_max, apic_clamp, curvature_max;
     uint32_t slip_cap, sealed_vent;
     OMat mat[O_MAX_MATERIALS];
+    float magnet_demag;
 } OSimParams;
 
 /* ToolState (src/sim/params.rs:1141-1213). */
@@ -134,6 +143,7 @@ OSim* osim_create(int w, int h, uint32_t capacity, const OSimParams* p);
 void osim_destroy(OSim* s);
 int osim_set_params(OSim* s, const OSimParams* p);
 int osim_set_currents(OSim* s, const OCurrent* c, uint32_t n);
+int osim_set_magnets(OSim* s, const OMagnet* m, uint32_t n);
 int osim_set_solids(OSim* s, const float* sdf, const float* solid4, const uint32_t* region,
                     const float* temp);
 /* FluidSim::reset (src/sim/mod.rs:1981-2002): ids, settle_spawn, the tank's rows.

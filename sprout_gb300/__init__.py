@@ -36,7 +36,7 @@ EXPORTS = [
     "sprout_params_set", "sprout_params_get", "sprout_params_set_diluent", "sprout_params_set_group", "sprout_scene_new", "sprout_scene_free", "sprout_scene_add_box",
     "sprout_scene_add_circle", "sprout_scene_sdf", "sprout_scene_rasterize", "sprout_fill_rect",
     "sprout_sim_create", "sprout_sim_destroy", "sprout_sim_set_params", "sprout_sim_set_solids",
-    "sprout_sim_reset", "sprout_sim_set_currents", "sprout_sim_frame_blocking", "sprout_sim_dt_estimate", "sprout_sim_step", "sprout_sim_step_blocking", "sprout_sim_advance_blocking",
+    "sprout_sim_reset", "sprout_sim_set_currents", "sprout_sim_set_magnets", "sprout_sim_frame_blocking", "sprout_sim_dt_estimate", "sprout_sim_step", "sprout_sim_step_blocking", "sprout_sim_advance_blocking",
     "sprout_sim_sync", "sprout_sim_download_particles", "sprout_sim_download_pressure",
     "sprout_sim_download_field", "sprout_sim_stats", "sprout_sim_device_bytes", "sprout_sim_profile",
     "sprout_sim_profile_passes", "sprout_pressure_solve_static", "sprout_sim_set_precision",
@@ -118,6 +118,7 @@ def lib() -> C.CDLL:
         "sprout_sim_set_solids": ([V, V, V, V, V], C.c_int),
         "sprout_sim_reset": ([V, V, C.c_uint32], C.c_int),
         "sprout_sim_set_currents": ([V, V, C.c_uint32], C.c_int),
+        "sprout_sim_set_magnets": ([V, V, C.c_uint32], C.c_int),
         "sprout_sim_frame_blocking": ([V, C.c_uint32, C.c_float, V, P(C.c_double)], C.c_int),
         "sprout_sim_dt_estimate": ([V, P(C.c_float)], C.c_int),
         "sprout_sim_step": ([V, C.c_uint32, C.c_float, P(Tool)], C.c_int),
@@ -175,6 +176,20 @@ def current_array(currents) -> np.ndarray:
         arr[k]["radius"] = c["radius"]
         arr[k]["vel"] = c.get("vel", (0.0, 0.0))
         arr[k]["rate"] = c["rate"]
+    return arr
+
+
+MAGNET_DTYPE = np.dtype([("pos", "<f4", 2), ("radius", "<f4"), ("strength", "<f4"), ("dir", "<f4", 2)])
+
+
+def magnet_array(magnets) -> np.ndarray:
+    """Magnet records (src/sim/params.rs:1082-1087) from dicts with pos, radius, strength, dir."""
+    arr = np.zeros(len(magnets), MAGNET_DTYPE)
+    for k, m in enumerate(magnets):
+        arr[k]["pos"] = m["pos"]
+        arr[k]["radius"] = m["radius"]
+        arr[k]["strength"] = m["strength"]
+        arr[k]["dir"] = m.get("dir", (0.0, 1.0))
     return arr
 
 
@@ -311,6 +326,12 @@ class FluidSim:
         dt = C.c_float()
         _check(lib().sprout_sim_dt_estimate(self._h, C.byref(dt)))
         return dt.value
+
+    def set_magnets(self, magnets):
+        """FluidSim::set_magnets: dipoles {pos, radius, strength, dir} (cells, T); the first 8
+        are kept, across resets."""
+        arr = magnet_array(magnets)
+        _check(lib().sprout_sim_set_magnets(self._h, arr.ctypes.data if len(arr) else None, len(arr)))
 
     def set_currents(self, currents):
         """FluidSim::set_currents: zones {pos, radius, vel, rate} (cells, cells / s, 1 / s; a

@@ -65,6 +65,7 @@ struct DevScene {
     float4* rh;       // per cell: its non-Newtonian liquid (share, row, concentration, stiff)
     float* famocc;    // per cell and family: the family's occupancy (settling)
     float2* dsettle;  // per cell and family: the concentration gain / loss rates settling hands the particles
+    float2* magc;     // per cell: its liquid's susceptibility; the magnetic energy density of magnetic liquid there
     int2* hcell;
     const float4* solid;
     const float* sdf;

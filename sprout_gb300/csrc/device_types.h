@@ -16,6 +16,7 @@ namespace sprout {
 
 constexpr int kMaxPresent = 12;
 constexpr int kMaxCurrents = 16;   // params.rs: MAX_CURRENTS
+constexpr int kMaxMagnets = 8;     // params.rs: MAX_MAGNETS
 constexpr int kGroups = 4;
 constexpr int kMaxLevels = 24;
 
@@ -41,6 +42,7 @@ struct DevMat {
     float rx[4];    // reaction rate; reaction heat; self-heating (K/s); volatility
     float rheo[4];  // yield stress / water's density (cells^2/s^2); flow index; shear time (s); viscosity ratio
     float gr[4];    // friction coefficient; fume; fizz; unused
+    float el[4];    // shear modulus / water's density; relaxation time; susceptibility; residue share
 };
 
 struct DevParams {
@@ -75,6 +77,12 @@ struct DevParams {
     // the velocity the liquid is driven towards (cells/s). ext[3] holds how many.
     float current_zone[kMaxCurrents][4];
     float current_vel[kMaxCurrents][4];
+    // magnets (params.rs:1082-1087): how many, the strongest susceptibility in the tank, its
+    // saturation (T), 1 / (water density dx^2); each magnet's position (cells), radius, strength
+    // (T) and the direction of its north pole
+    float mag[4];
+    float magnet[kMaxMagnets][4];
+    float magnet_dir[kMaxMagnets][4];
 };
 
 // StepBuf (common.glsl:122-135) plus the engine's own step flags.

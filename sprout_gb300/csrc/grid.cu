@@ -58,6 +58,7 @@ __global__ void __launch_bounds__(256) k_grid_prep(DevScene d) {
         float f[kGroups] = {0.0f, 0.0f, 0.0f, 0.0f}, rg[kGroups] = {0.0f, 0.0f, 0.0f, 0.0f}, lg[kGroups] = {0.0f, 0.0f, 0.0f, 0.0f};
         float sigma = 0.0f, contx = 0.0f, conty = 0.0f, fam0 = -1.0f;
         float4 nn = make_float4(0.0f, -1.0f, 1.0f, 0.0f);   // the cell's non-Newtonian liquid: share, row, concentration, stiff
+        float chi = 0.0f;   // the cell's liquid's susceptibility (share-weighted)
         float rho = 0.0f, mu = 0.0f, rho_c = 0.0f, nu_c = 0.0f;
         const bool thermal = P->thermal != 0;
         float T = P->heat[0], kappa = 0.0f, emis = 0.0f, frozen = 0.0f, Craw = 0.0f;
@@ -159,6 +160,7 @@ __global__ void __launch_bounds__(256) k_grid_prep(DevScene d) {
                     top_share = share;
                     top_row = r;
                 }
+                chi += share * mats[r].el[2];
                 const int g = ia[0];
                 if (g > 0) bg[g - 1] += share * ma[0];
                 f[g] += share;
@@ -186,6 +188,16 @@ __global__ void __launch_bounds__(256) k_grid_prep(DevScene d) {
         if (has && level <= 0.0f && cx > 0 && cy > 0 && cx < W - 1 && cy < H - 1) {
             if ((packed(d, i - 1) && packed(d, i + 1)) || (packed(d, i - W) && packed(d, i + W))) level = 0.05f;
             else if (P->gravity > 0.0f && nn.x <= 0.0f && phi_t > 0.25f && packed(d, i - W)) level = 0.05f;
+            else if ((P->caps & CAP_MAGNET) != 0u && nn.x <= 0.0f && phi_t > 0.25f && chi > 0.0f) {
+                // with a magnet, lying on is towards gravity and the field's pull together
+                // (grid_prep.comp:216-220, from the last substep's energy)
+                const float km = chi / P->mag[1] / maxf(rho, 0.05f);
+                const float pk = -km * 0.5f;
+                const float pxl = pk * (d.magc[i + 1].y - d.magc[i - 1].y) - 0.0f;
+                const float pyl = pk * (d.magc[i + W].y - d.magc[i - W].y) - P->gravity;
+                const int toward = fabsf(pxl) > fabsf(pyl) ? (pxl > 0.0f ? i + 1 : i - 1) : (pyl > 0.0f ? i + W : i - W);
+                if (packed(d, toward)) level = 0.05f;
+            }
         }
         if (sol.w > 0.0f && level <= 0.0f) air_bits = 1u << (__ldg(&d.region[i]) & REGION_MASK);
         if ((P->caps & (CAP_RIGID | CAP_RHEO)) != 0u) {
@@ -195,6 +207,7 @@ __global__ void __launch_bounds__(256) k_grid_prep(DevScene d) {
             mu = minf(mu, cap);
             d.rh[i] = nn;
         }
+        if ((P->caps & CAP_MAGNET) != 0u) d.magc[i].x = chi;
         d.cell[i] = make_float4(phi_f, rho, mu, level);
         d.comp[i] = make_float4(rho, f[1], fam0, phi_t);
         if (P->sorts != 0u) d.gbase[i] = make_float4(bg[0], bg[1], bg[2], 0.0f);
@@ -827,6 +840,77 @@ __global__ void __launch_bounds__(256) k_settle(DevScene d) {
     }
 }
 
+// The field of the magnets at x (cells), T: each a point dipole in the plane,
+// B0 (R / r)^3 (3 (m.e) e - m) / 2, constant inside the rim (common.glsl:388-402).
+DEV float2 magnet_field(const DevParams* P, float x, float y) {
+    float bx = 0.0f, by = 0.0f;
+    for (int k = 0; k < (int)P->mag[0]; k++) {
+        const float* mg = P->magnet[k];
+        const float mx = P->magnet_dir[k][0], my = P->magnet_dir[k][1];
+        const float dx = x - mg[0], dy = y - mg[1];
+        const float len = len2(dx, dy);
+        const float r = maxf(len, mg[2]);
+        const float ex = len > 1e-4f ? dx / len : mx, ey = len > 1e-4f ? dy / len : my;
+        const float a = mg[3] * sp_powf(mg[2] / r, 3.0f) * 0.5f;
+        const float me3 = 3.0f * (mx * ex + my * ey);
+        bx += a * (me3 * ex - mx);
+        by += a * (me3 * ey - my);
+    }
+    return make_float2(bx, by);
+}
+
+// magnet.comp mode 0: the magnetic energy density of pure magnetic liquid in each cell
+// (Langevin-like saturation, a demagnetising factor from the liquid's surface).
+__global__ void __launch_bounds__(256) k_magnet_energy(DevScene d) {
+    CELL_XY;
+    if (cx >= W || cy >= H) return;
+    const int i = cy * W + cx;
+    const DevParams* P = d.P;
+    const float MU0 = 1.25663706e-6f;
+    const float2 B = magnet_field(P, (float)cx + 0.5f, (float)cy + 0.5f);
+    const float Bl = len2(B.x, B.y);
+    const float Hf = Bl / MU0;
+    float psi = 0.0f;
+    const float chi = P->mag[1];
+    if (Hf > 0.0f && chi > 0.0f) {
+        float N = 1.0f / 3.0f;
+        if (P->heat3[3] > 0.0f) {
+            float gx = 0.0f, gy = 0.0f;
+            if (cx > 0 && cy > 0 && cx < W - 1 && cy < H - 1) {
+                gx = 0.5f * (d.surf[i + 1].x - d.surf[i - 1].x);
+                gy = 0.5f * (d.surf[i + W].x - d.surf[i - W].x);
+            }
+            const float gl = len2(gx, gy);
+            const float nh = gl > 1e-6f ? (gx / gl) * (B.x / Bl) + (gy / gl) * (B.y / Bl) : 0.0f;
+            N = mixf(1.0f / 3.0f, nh * nh, clampf(gl / 0.25f, 0.0f, 1.0f) * P->heat3[3]);
+        }
+        const float ce = chi / (1.0f + N * chi);
+        const float Ms = P->mag[2] / MU0;
+        const float xs = ce * Hf / Ms;
+        const float f = xs < 0.02f ? xs * xs * (0.5f - xs * (1.0f / 3.0f - 0.25f * xs)) : xs - sp_logf(1.0f + xs);
+        psi = -MU0 * Ms * Ms / ce * f * P->mag[3];
+    }
+    d.magc[i].y = psi;
+}
+
+DEV float magnet_face_force(const DevScene& d, int i, int n, float rho) {
+    const bool li = d.cell[i].w > 0.0f, ln = d.cell[n].w > 0.0f;
+    const float sc = (li == ln ? 0.5f * (d.magc[i].x + d.magc[n].x) : li ? d.magc[i].x : d.magc[n].x) / d.P->mag[1];
+    return -d.S->dt * sc * (d.magc[i].y - d.magc[n].y) / maxf(rho, 0.05f);
+}
+
+// magnet.comp mode 1: the force of the energy's gradient on the liquid's faces.
+__global__ void __launch_bounds__(256) k_magnet_force(DevScene d) {
+    CELL_XY;
+    if (cx >= W || cy >= H || cx < 1 || cy < 1) return;
+    const int i = cy * W + cx;
+    float4 me = d.vel[i];
+    const float4 cf = d.coef[i];
+    if (face_live(me.z) && cf.x != 0.0f) me.x += magnet_face_force(d, i, i - 1, cf.z);
+    if (face_live(me.w) && cf.y != 0.0f) me.y += magnet_face_force(d, i, i - W, cf.w);
+    d.vel[i] = me;
+}
+
 void launch_grid(const DevScene& d, const LaunchCfg& cfg, cudaStream_t st) {
     dim3 blk(16, 16);
     dim3 grd((d.W + 15) / 16, (d.H + 15) / 16);
@@ -836,6 +920,10 @@ void launch_grid(const DevScene& d, const LaunchCfg& cfg, cudaStream_t st) {
     k_coef_smooth<<<grd, blk, 0, st>>>(d);
     k_curv<<<grd, blk, 0, st>>>(d);
     k_apply<<<grd, blk, 0, st>>>(d);
+    if (cfg.magnet) {
+        k_magnet_energy<<<grd, blk, 0, st>>>(d);
+        k_magnet_force<<<grd, blk, 0, st>>>(d);
+    }
     if (cfg.heat) k_heat<<<grd, blk, 0, st>>>(d);
     if (cfg.visc_mode == 1) {
         k_visc_setup<<<grd, blk, 0, st>>>(d);

@@ -537,6 +537,10 @@ void build_materials(const SimParams& p, const Tank& t, bool thermal, DevMat* ou
         g.gr[1] = m.fume;
         g.gr[2] = m.fizz;
         g.gr[3] = 0.0f;
+        g.el[0] = m.shear_modulus / (kWaterDensity * dx * dx);
+        g.el[1] = m.relax_time;
+        g.el[2] = m.susceptibility;
+        g.el[3] = m.residue_share;
     }
 }
 
@@ -552,7 +556,8 @@ static float tool_speed(const ToolState* t) {
 }
 
 void build_params(const SimParams& p, const Tank& t, bool thermal, uint32_t caps, int W, int H, uint32_t n_slots,
-                  float dt_limit, const ToolState* tool, DevParams* P, const std::vector<Current>& currents) {
+                  float dt_limit, const ToolState* tool, DevParams* P, const std::vector<Current>& currents,
+                  const std::vector<Magnet>& magnets) {
     std::memset(P, 0, sizeof *P);
     float dx = p.cell_size;
     P->grid[0] = W;
@@ -610,6 +615,27 @@ void build_params(const SimParams& p, const Tank& t, bool thermal, uint32_t caps
     P->heat2[3] = p.contact_heat / (kWaterHeat * dx);
     P->heat3[0] = std::max(p.eddy_heat, 0.0f);
     P->heat3[1] = p.evaporation ? 2.257e6f / 1005.0f : 0.0f;
+    P->heat3[3] = std::min(std::max(p.magnet_demag, 0.0f), 1.0f);
+    // the strongest susceptibility in the tank and its saturation (mod.rs:2264)
+    float chi_max = 0.0f, sat = 0.05f;
+    for (int r : t.rows)
+        if (p.mat[r].susceptibility > chi_max) {
+            chi_max = p.mat[r].susceptibility;
+            sat = p.mat[r].saturation;
+        }
+    P->mag[0] = (float)magnets.size();
+    P->mag[1] = std::max(chi_max, 1e-6f);
+    P->mag[2] = sat;
+    P->mag[3] = 1.0f / (kWaterDensity * dx * dx);
+    for (size_t i = 0; i < magnets.size() && i < (size_t)kMaxMagnets; i++) {   // mod.rs:2258-2263
+        const Magnet& m = magnets[i];
+        P->magnet[i][0] = m.pos[0];
+        P->magnet[i][1] = m.pos[1];
+        P->magnet[i][2] = std::max(m.radius, 0.5f);
+        P->magnet[i][3] = m.strength;
+        P->magnet_dir[i][0] = m.dir[0];
+        P->magnet_dir[i][1] = m.dir[1];
+    }
     P->sep_tau = p.droplet_cells;
     P->cfl = p.cfl;
     P->tool_crowd_max = p.tool_crowd_max;

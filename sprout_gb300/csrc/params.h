@@ -110,6 +110,12 @@ struct Current {
     float pos[2], radius, vel[2], rate;
 };
 
+// Magnet (params.rs:1082-1087): a point dipole at pos (cells) of radius `radius`, field
+// `strength` (T) on its axis at the rim, north pole along `dir`.
+struct Magnet {
+    float pos[2], radius, strength, dir[2];
+};
+
 // Tank (mod.rs:222-245).
 struct Tank {
     std::vector<int> rows;
@@ -125,7 +131,7 @@ struct Tank {
 void build_materials(const SimParams& p, const Tank& t, bool thermal, DevMat* out);
 void build_params(const SimParams& p, const Tank& t, bool thermal, uint32_t caps, int W, int H,
                   uint32_t n_slots, float dt_limit, const ToolState* tool, DevParams* out,
-                  const std::vector<Current>& currents = {});
+                  const std::vector<Current>& currents = {}, const std::vector<Magnet>& magnets = {});
 
 // The name of built-in row r (presets.rs BUILTINS keys), or "" past them.
 const char* builtin_key(int r);

@@ -265,7 +265,7 @@ struct SproutSim {
         A(d.scan_tmp, (nc + 1 + 1023) / 1024 + 1);
         A(d.acc, nc * 32);
         A(d.vel, nc); A(d.cell, nc); A(d.comp, nc); A(d.coef, nc); A(d.sprop, nc); A(d.surf, nc);
-        A(d.surf2, nc); A(d.aux, nc); A(d.grho, nc); A(d.gbase, nc); A(d.rh, nc); A(d.therm, nc); A(d.dheat, nc); A(d.vw, nc);
+        A(d.surf2, nc); A(d.aux, nc); A(d.grho, nc); A(d.gbase, nc); A(d.rh, nc); A(d.magc, nc); A(d.therm, nc); A(d.dheat, nc); A(d.vw, nc);
         A(d.vs, nc); A(d.prhs, nc); A(d.vel0, nc); A(d.pjump, nc); A(d.pres, nc); A(d.p2keep, nc);
         A(d.hcell, nc);
         float4* solid;
@@ -344,6 +344,7 @@ struct SproutSim {
     // count grows or drops to none, the present ones otherwise.
     int settle_fams = 0;
     std::vector<Current> currents;   // set_currents: kept across resets, like the reference's
+    std::vector<Magnet> magnets;     // set_magnets: likewise
     int set_settling(int fams) {
         if (fams == settle_fams || (fams > 0 && fams < settle_fams)) return SPROUT_OK;
         const size_t n = std::max<size_t>((size_t)W * H * (size_t)fams, 1);
@@ -371,6 +372,7 @@ struct SproutSim {
             if (thermal) rigid |= m.freezes() || (dil && dil->freezes()) || m.temp_model != 0 || (dil && dil->temp_model != 0);
             rigid |= m.viscosity_at(params.ambient_temp) >= params.rigid_viscosity || (!thermal && m.freezes() && params.ambient_temp < m.melt_hi);
             if (m.shear_modulus > 0.0f) c |= CAP_ELASTIC;
+            if (!magnets.empty() && m.susceptibility > 0.0f) c |= CAP_MAGNET;
             if (m.react_with >= 0 && m.react_rate > 0.0f && std::find(tank.rows.begin(), tank.rows.end(), m.react_with) != tank.rows.end()) c |= CAP_REACT;
             if (r == 57 && thermal) c |= CAP_STEAM;
         }
@@ -396,7 +398,7 @@ struct SproutSim {
             CUDA_TRY(cudaEventCreateWithFlags(&stage_done, cudaEventDisableTiming));
         }
         DevParams P;
-        build_params(params, tank, thermal, caps, W, H, n_slots, dt_limit(), tool, &P, currents);
+        build_params(params, tank, thermal, caps, W, H, n_slots, dt_limit(), tool, &P, currents, magnets);
         P.ext_speed = std::max(P.ext_speed, spawn_speed);   // mod.rs:2300
         P.visc_mode = visc_mode;
         P.visc_levels = std::min(P.visc_levels, d.lv.tail);
@@ -536,6 +538,7 @@ struct SproutSim {
         want.heat = thermal && params.heat_rate > 0.0f;
         want.rheo = (caps & CAP_RHEO) != 0u;
         want.settle = (caps & CAP_SETTLE) != 0u;
+        want.magnet = (caps & CAP_MAGNET) != 0u;
         want.visc_mode = visc_mode;
         want.twice = visc_mode == 2 && params.viscous_projection != 0;
         want.viscous_warm = params.viscous_warm != 0;
@@ -548,7 +551,7 @@ struct SproutSim {
             if (v > 0) want.visc_blocks = std::max(1, std::min(v, visc_max[want.visc_sweeps - 1]));
         }
         want.mixed = mixed;
-        bool same = want.n_slots == cfg.n_slots && want.thermal == cfg.thermal && want.heat == cfg.heat && want.rheo == cfg.rheo && want.settle == cfg.settle &&
+        bool same = want.n_slots == cfg.n_slots && want.thermal == cfg.thermal && want.heat == cfg.heat && want.rheo == cfg.rheo && want.settle == cfg.settle && want.magnet == cfg.magnet &&
                     want.visc_mode == cfg.visc_mode && want.twice == cfg.twice && want.viscous_warm == cfg.viscous_warm &&
                     want.visc_levels == cfg.visc_levels && want.visc_sweeps == cfg.visc_sweeps &&
                     want.visc_blocks == cfg.visc_blocks && want.mixed == cfg.mixed && d.stride == std::max(tank.stride, 8);
@@ -645,8 +648,8 @@ struct SproutSim {
         thermal = th;
         caps = compute_caps();
         int rc = SPROUT_OK;
-        if (caps & (CAP_RIGID | CAP_MAGNET | CAP_ELASTIC | CAP_STEAM | CAP_REACT))
-            rc = fail(SPROUT_E_UNSUPPORTED, "the tank needs rigid / magnet / elastic / steam / reaction passes, which this engine does not carry");
+        if (caps & (CAP_RIGID | CAP_ELASTIC | CAP_STEAM | CAP_REACT))
+            rc = fail(SPROUT_E_UNSUPPORTED, "the tank needs rigid / elastic / steam / reaction passes, which this engine does not carry");
         for (int r : tank.rows) {
             const MatProps& m = params.mat[r];
             if (rc == SPROUT_OK && (m.volatility > 0.0f || (thermal && m.boil < 1e8f)))
@@ -1586,6 +1589,18 @@ int sprout_sim_set_currents(SproutSim* sim, const SproutCurrent* c, uint32_t n) 
     }
     return SPROUT_OK;
 }
+int sprout_sim_set_magnets(SproutSim* sim, const SproutMagnet* m, uint32_t n) {
+    if (!sim || (n > 0 && !m)) return fail(SPROUT_E_ARG, "null argument");
+    sim->magnets.clear();
+    for (uint32_t i = 0; i < n && i < (uint32_t)kMaxMagnets; i++) {
+        Magnet q;
+        std::memcpy(&q, &m[i], sizeof q);
+        sim->magnets.push_back(q);
+    }
+    // whether the tank needs magnet.comp changes with the magnets (mod.rs:2749-2751)
+    if (!sim->tank.rows.empty()) sim->caps = sim->compute_caps();
+    return SPROUT_OK;
+}
 int sprout_sim_set_params(SproutSim* sim, const SproutParams* p) {
     if (!sim || !p) return fail(SPROUT_E_ARG, "null argument");
     sim->params = p->p;
@@ -1698,6 +1713,7 @@ int sprout_sim_download_field(SproutSim* sim, const char* name, void* out, size_
     else if (n == "grho") { src = d.grho; b = nc * 16; }
     else if (n == "gbase") { src = d.gbase; b = nc * 16; }
     else if (n == "rh") { src = d.rh; b = nc * 16; }
+    else if (n == "magc") { src = d.magc; b = nc * 8; }
     else if (d.famocc && n == "famocc") { src = d.famocc; b = nc * 4 * (size_t)sim->settle_fams; }
     else if (d.dsettle && n == "dsettle") { src = d.dsettle; b = nc * 8 * (size_t)sim->settle_fams; }
     else if (n == "surf2") { src = d.surf2; b = nc * 16; }

@@ -22,6 +22,7 @@ class Tank:
     diluents: dict = field(default_factory=dict)    # custom row -> its diluent's row (a family)
     groups: dict = field(default_factory=dict)      # custom row -> its phase group (0-3)
     currents: list = field(default_factory=list)    # dicts: pos, radius, vel, rate (negative: a drain)
+    magnets: list = field(default_factory=list)     # dicts: pos, radius, strength (T), dir
 
     # ---- the engine -----------------------------------------------------------------------
     def engine(self):
@@ -50,6 +51,8 @@ class Tank:
         sim = S.FluidSim(self.w, self.h, len(parts) + self.capacity_extra, p)
         if self.currents:
             sim.set_currents(self.currents)
+        if self.magnets:
+            sim.set_magnets(self.magnets)
         sim.set_solids(sdf, solid, region, temp)
         sim.reset(parts)
         return sim, parts, (sdf, solid, region, temp)

@@ -131,3 +131,16 @@ def currents(w: int = 96, h: int = 64, cell: float = 0.002) -> Tank:
     t.currents = [{"pos": (0.25 * w, 0.2 * h), "radius": 0.15 * h, "vel": (60.0, 5.0), "rate": 20.0},
                   {"pos": (0.85 * w, 0.08 * h), "radius": 0.1 * h, "vel": (0.0, 0.0), "rate": -30.0}]
     return t
+
+
+def magnetic(w: int = 96, h: int = 64, cell: float = 0.002, mat: int = 37, demag: float = 0.0) -> Tank:
+    """A pool of a magnetic built-in ("magnetic", 37, or ferrofluid, 13) over water with a
+    magnet above it, north pole up: the field's energy pulls the liquid towards the magnet."""
+    key = {37: "magnetic", 13: "ferrofluid"}[mat]
+    s = {"cell_size": cell, "fixed_hz": 240.0, "pressure_tol": 1e-5, "viscosity_tol": 1e-5,
+         "tension_water": 0.0, f"tension_{key}": 0.0, "magnet_demag": demag}
+    fills = [([0.0, 0.0, float(w), float(int(0.2 * h))], 0, None),
+             ([float(int(0.3 * w)), float(int(0.2 * h)), float(int(0.7 * w)), float(int(0.35 * h))], mat, None)]
+    t = Tank(w, h, s, [], fills)
+    t.magnets = [{"pos": (0.5 * w, 0.45 * h), "radius": 4.0, "strength": 1.0, "dir": (0.0, 1.0)}]
+    return t
