@@ -16,6 +16,7 @@ struct LaunchCfg {
     bool rheo = false;        // a non-Newtonian liquid is in the tank: rheo.comp runs
     bool settle = false;      // a family with grains settles: settle.comp runs
     bool magnet = false;      // a magnet and a susceptible liquid: magnet.comp runs
+    bool xtra = false;        // families, several phase groups, settling or currents: the particle pass's full form
     int visc_mode = 0;        // 0 none, 1 explicit, 2 implicit
     bool twice = false;       // implicit viscosity between two pressure solves
     bool viscous_warm = false;   // the first solve starts from last substep's P1 (cg_scale mode 1)

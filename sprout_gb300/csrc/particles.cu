@@ -282,6 +282,10 @@ DEV float group_drift(const DevScene& d, const DevMat* mats, uint32_t row, float
     return slip;
 }
 
+// XTRA: the tank has concentration families, several phase groups, settling or currents.
+// Without them the pass is compiled without that code (64 registers against ~90, so twice
+// the resident warps for its latency-bound gathers); the launcher picks the instantiation.
+template <bool XTRA>
 __global__ void __launch_bounds__(256) k_advance(DevScene d) {
     const DevParams* P = d.P;
     const StepState* S = d.S;
@@ -336,14 +340,14 @@ __global__ void __launch_bounds__(256) k_advance(DevScene d) {
                     // own family (a diluent's: family 0)
                     int fam = mats[row].ib[0];
                     const int nmix = P->n_fam - 1;
-                    const bool fams = P->n_fam > 0;
+                    const bool fams = XTRA && P->n_fam > 0;
                     // with several phase groups: sg, the shares of groups 1 - 3 around the
                     // particle; with a group that sorts its materials, sbg, share x base density
                     // of the particle's group
                     const int grp = mats[row].ia[0];
                     const uint32_t gm = P->group_mask;
-                    const bool groups = (gm & (gm - 1u)) != 0u, more = (gm & 12u) != 0u;
-                    const bool sorts = grp > 0 && ((P->sorts >> grp) & 1u) != 0u;
+                    const bool groups = XTRA && (gm & (gm - 1u)) != 0u, more = XTRA && (gm & 12u) != 0u;
+                    const bool sorts = XTRA && grp > 0 && ((P->sorts >> grp) & 1u) != 0u;
                     const bool gather = fams || groups || sorts;
                     float sw = 0.0f, sfw = 0.0f, sfs = 0.0f, sg0 = 0.0f, sg1 = 0.0f, sg2 = 0.0f, sbg = 0.0f;
 #pragma unroll
@@ -372,7 +376,7 @@ __global__ void __launch_bounds__(256) k_advance(DevScene d) {
                                 }
                             }
                         }
-                    if ((P->caps & CAP_SETTLE) != 0u) {
+                    if (XTRA && (P->caps & CAP_SETTLE) != 0u) {
                         // Settling hands each cell a change of its family's concentration, taken
                         // with the scatter's weights; the first row, as the primary family's
                         // diluent, takes part at concentration 0 (particles.comp:331-352).
@@ -490,7 +494,7 @@ __global__ void __launch_bounds__(256) k_advance(DevScene d) {
                 }
                 // drains: a zone with a negative rate removes each particle in it with probability
                 // -rate (1 - 0.75 r^2) dt per substep (particles.comp:577-594)
-                const int ncur = (int)P->ext[3];
+                const int ncur = XTRA ? (int)P->ext[3] : 0;
                 for (int c = 0; c < ncur && alive; c++) {
                     const float* z = P->current_zone[c];
                     if (z[3] >= 0.0f) continue;
@@ -932,7 +936,8 @@ void launch_advance(const DevScene& d, const LaunchCfg& cfg, cudaStream_t st) {
     if (cfg.thermal) cudaMemsetAsync(d.hcell, 0, (size_t)d.ncell * sizeof(int2), st);
     uint32_t nb = (cfg.n_slots + 255) / 256;
     if (nb == 0) nb = 1;
-    k_advance<<<nb, 256, 0, st>>>(d);
+    if (cfg.xtra) k_advance<true><<<nb, 256, 0, st>>>(d);
+    else k_advance<false><<<nb, 256, 0, st>>>(d);
 }
 
 void launch_sort(const DevScene& d, const LaunchCfg& cfg, cudaStream_t st) {

@@ -742,11 +742,28 @@ DEV void finish_up(const DevScene& d, const Lv& F, int t, bool flag, const Zc& z
 template <class M>
 DEV void phase_tail(const DevScene& d, const Tail& tl, bool writer) {
     const int first = d.lv.tail, last = d.lv.n - 1;
-    for (int s = threadIdx.x; s < tl.nf; s += NT) tl.r[s] = M::R(d, tl.base + s);
+    // Each level's first half-sweep starts from zero: its black cells are r / D, the rest 0.
+    // It is taken where the level's right-hand side is made (here for the first tail level,
+    // in the restriction for the others), which saves a pass and a barrier per level.
+    auto from_zero = [&](const Lv& L, int t, float2 r) {
+        const int y = qdiv(t, L.wm), x = t - y * L.w;
+        const int s = L.off - tl.base + t;
+        const float D = tl.dg[s];
+        if (!(D <= 0.0f) && ((x + y) & 1) == 0) tl.x[s] = divz(r, D);
+        else tl.x[s] = make_float2(0.0f, 0.0f);
+    };
+    {
+        const Lv F = lev(d.lv, first);
+        for (int s = threadIdx.x; s < tl.nf; s += NT) {
+            const float2 r = M::R(d, tl.base + s);
+            tl.r[s] = r;
+            from_zero(F, s, r);
+        }
+    }
     __syncthreads();
     // a half-sweep: every slot's reads are issued before its terms are summed (neighbour
     // slots clamped into the level and kept or not by the mask), in the shader's order
-    auto sweep = [&](const Lv& L, int colour, bool zero) {
+    auto sweep = [&](const Lv& L, int colour) {
         const int o = L.off - tl.base, n = L.w * L.h;
         const int lo = o, hi = o + n - 1;
         for (int t = threadIdx.x; t < n; t += NT) {
@@ -755,11 +772,6 @@ DEV void phase_tail(const DevScene& d, const Tail& tl, bool writer) {
             const float D = tl.dg[s];
             const float2 r = tl.r[s];
             const bool mine = !(D <= 0.0f) && ((x + y) & 1) == colour;
-            if (zero) {
-                if (mine) tl.x[s] = divz(r, D);
-                else tl.x[s] = make_float2(0.0f, 0.0f);
-                continue;
-            }
             const float4 w = tl.a[s];
             const uint32_t m = tl.m[s];
             const float2 x0 = tl.x[max(s - 1, lo)], x1 = tl.x[min(s + 1, hi)];
@@ -776,8 +788,7 @@ DEV void phase_tail(const DevScene& d, const Tail& tl, bool writer) {
     for (int l = first; l < last; l++) {
         Lv L = lev(d.lv, l), C = lev(d.lv, l + 1);
         const int o = L.off - tl.base, oc = C.off - tl.base;
-        sweep(L, 0, true);
-        sweep(L, 1, false);
+        sweep(L, 1);
         for (int t = threadIdx.x; t < C.w * C.h; t += NT) {
             const int ccy = qdiv(t, C.wm), ccx = t - ccy * C.w;
             float sumx = 0.0f, sumy = 0.0f;
@@ -805,13 +816,13 @@ DEV void phase_tail(const DevScene& d, const Tail& tl, bool writer) {
                 sumy += rh.y - azy;
             }
             tl.r[oc + t] = make_float2(sumx, sumy);
+            from_zero(C, t, make_float2(sumx, sumy));
         }
         __syncthreads();
     }
     {
         Lv L = lev(d.lv, last);
-        sweep(L, 0, true);
-        for (int s = 1; s < 9; s++) sweep(L, s & 1, false);
+        for (int s = 1; s < 9; s++) sweep(L, s & 1);
     }
     for (int l = last - 1; l >= first; l--) {
         Lv F = lev(d.lv, l), C = lev(d.lv, l + 1);
@@ -837,7 +848,7 @@ DEV void phase_tail(const DevScene& d, const Tail& tl, bool writer) {
             tl.x[s] = divz(sum, D);
         }
         __syncthreads();
-        sweep(F, 0, false);
+        sweep(F, 0);
     }
     if (writer)   // the first tail level's result (for inspection; a batch's way up reads it)
         for (int s = threadIdx.x; s < tl.nf; s += NT) M::setZ(d, tl.base + s, tl.x[s]);

@@ -539,6 +539,7 @@ struct SproutSim {
         want.rheo = (caps & CAP_RHEO) != 0u;
         want.settle = (caps & CAP_SETTLE) != 0u;
         want.magnet = (caps & CAP_MAGNET) != 0u;
+        want.xtra = tank.families > 0 || (tank.group_mask & ~1u) != 0u || !currents.empty();
         want.visc_mode = visc_mode;
         want.twice = visc_mode == 2 && params.viscous_projection != 0;
         want.viscous_warm = params.viscous_warm != 0;
@@ -551,7 +552,7 @@ struct SproutSim {
             if (v > 0) want.visc_blocks = std::max(1, std::min(v, visc_max[want.visc_sweeps - 1]));
         }
         want.mixed = mixed;
-        bool same = want.n_slots == cfg.n_slots && want.thermal == cfg.thermal && want.heat == cfg.heat && want.rheo == cfg.rheo && want.settle == cfg.settle && want.magnet == cfg.magnet &&
+        bool same = want.n_slots == cfg.n_slots && want.thermal == cfg.thermal && want.heat == cfg.heat && want.rheo == cfg.rheo && want.settle == cfg.settle && want.magnet == cfg.magnet && want.xtra == cfg.xtra &&
                     want.visc_mode == cfg.visc_mode && want.twice == cfg.twice && want.viscous_warm == cfg.viscous_warm &&
                     want.visc_levels == cfg.visc_levels && want.visc_sweeps == cfg.visc_sweeps &&
                     want.visc_blocks == cfg.visc_blocks && want.mixed == cfg.mixed && d.stride == std::max(tank.stride, 8);
