@@ -223,8 +223,12 @@ def run_reference(args, rank, world, pg, budget_s: float = 90.0):
 
 
 def kernels_per_substep(stats, settings: dict) -> int:
-    n = 2 + 5 + 1                 # step + advance; scan x3 + place + cell gather; p2g
+    n = 2 + 6 + 1                 # step + advance; scan x3 + place + cell sort + cell gather; p2g
     n += 4 + 1                    # grid_prep, coef/smooth, curvature, jumps; rhs
+    caps = int(stats.caps)
+    n += 1 if caps & 8 else 0     # rheo.comp
+    n += 1 if caps & 64 else 0    # settle.comp
+    n += 2 if caps & 16 else 0    # magnet.comp, both modes
     n += 1 if stats.thermal else 0
     n += 2 if stats.viscosity_mode == 1 else 0
     n += 1 + 1                    # pressure (persistent), project
