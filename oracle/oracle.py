@@ -41,6 +41,7 @@ class OMat(C.Structure):
         ("react_with", C.c_int32), ("react_rate", C.c_float), ("fume", C.c_float),
         ("yield_stress", C.c_float), ("flow_index", C.c_float), ("shear_time", C.c_float), ("visc_ratio", C.c_float),
         ("saturation", C.c_float),
+        ("relax_time", C.c_float),
     ]
 
 
@@ -66,6 +67,7 @@ class OSimParams(C.Structure):
         ("slip_cap", C.c_uint32), ("sealed_vent", C.c_uint32),
         ("mat", OMat * 96),
         ("magnet_demag", C.c_float),
+        ("elastic_stress_max", C.c_float), ("elastic_step_max", C.c_float),
     ]
 
 

@@ -277,6 +277,8 @@ void oparams_default(OSimParams* p) {
     p->curvature_max = 0.5f;
     p->slip_cap = 1;
     p->sealed_vent = 1;
+    p->elastic_stress_max = 10.0f;   /* params.rs:447-448 */
+    p->elastic_step_max = 0.25f;
     for (int r = 0; r < O_MAX_MATERIALS; r++) mat_default(&p->mat[r]);
     /* the built-in liquids (presets.rs: BUILTINS): the fields the oracle carries */
 #define BUILTIN_P(row, field, v) p->mat[row].field = v;
@@ -614,6 +616,7 @@ typedef struct GParams {   /* common.glsl:37-86 (subset) */
     int tool_mode;
     float tool_strength;
     float tol[4], ext[4], corr[4], heat3[4];
+    float elastic[4];   /* stress channel, largest modulus / rho_w (cells^2/s^2), stress cap, step cap */
     float mag[4];   /* magnets, strongest susceptibility, its saturation, 1 / (rho_w dx^2) */
     float magnet[O_MAX_MAGNETS][4], magnet_dir[O_MAX_MAGNETS][4];
     float current_zone[O_MAX_CURRENTS][4];   /* common.glsl:76-77 */
@@ -625,7 +628,7 @@ typedef struct Tank {   /* mod.rs:222-245 */
     int nrows;
     int rows[MAX_PRESENT];
     int chan[MAX_PRESENT][3];
-    int stride, families, primary, chan_t;
+    int stride, families, primary, chan_t, chan_e;
     uint32_t group_mask;
     int chan_g[GROUPS];
 } Tank;
@@ -693,6 +696,9 @@ struct OSim {
     OMagnet magnets[O_MAX_MAGNETS];      /* set_magnets, likewise */
     int n_magnets;
     V2* magc;   /* per cell: susceptibility; magnetic energy density (magnet.comp) */
+    V4* pstress;   /* per particle slot: viscoelastic stress (xx, yy, xy), in place */
+    V4* estr;      /* per cell: the deposited stress (elastic.comp) */
+    int elastic_on;
     int n_currents;
     V2 *vel0, *pjump, *pres;
     float* p2keep;
@@ -779,6 +785,10 @@ static int tank_layout(Tank* t, const int* rows, int nrows, const OSimParams* p,
                 first = 0;
             }
     }
+    int elastic = 0;   /* three stress channels when an elastic material is in (mod.rs:316-317) */
+    for (int k = 0; k < nrows; k++) elastic |= p->mat[rows[k]].shear_modulus > 0.0f;
+    t->chan_e = elastic ? next : -1;
+    next += elastic ? 3 : 0;
     if (next > ACC_MAX) return 0;
     int stride = next > ACC_MIN ? next : ACC_MIN;
     stride = (stride + 3) / 4 * 4;
@@ -825,11 +835,22 @@ static float dt_thermal(const OSimParams* p, const Tank* t) {   /* params.rs:907
     return m;
 }
 
+/* params.rs:947-960: the longest substep that keeps elastic waves within half a cell */
+static float dt_elastic(const OSimParams* p, const Tank* t) {
+    float stiff = 1.0f + (p->elastic_stress_max > 0.0f ? p->elastic_stress_max : 50.0f);
+    float m = INFINITY;
+    for (int k = 0; k < t->nrows; k++) {
+        const OMat* q = &p->mat[t->rows[k]];
+        if (q->shear_modulus > 0.0f) m = minf(m, 0.5f * p->cell_size / sqrtf(stiff * q->shear_modulus / q->density));
+    }
+    return m;
+}
+
 static float dt_limit(const OSim* s) {   /* mod.rs:2332-2339 */
     const OSimParams* p = &s->prm;
     float dt = minf(p->dt_max, dt_capillary(p, &s->tank));
     if (s->thermal) dt = minf(dt, dt_thermal(p, &s->tank));
-    return dt;
+    return minf(dt, dt_elastic(p, &s->tank));
 }
 
 static int viscosity_mode(const OSim* s) {   /* mod.rs:2768-2792 */
@@ -875,11 +896,27 @@ static int set_settling(OSim* s, int fams) {
     return 0;
 }
 
+/* mod.rs:2084-2110: the particles' stress buffer while an elastic material is in the tank,
+ * zero-filled each time it is taken up again */
+static int set_elastic(OSim* s, int on) {
+    if (on == s->elastic_on) return 0;
+    if (on) {
+        free(s->pstress);
+        free(s->estr);
+        s->pstress = calloc((size_t)s->capacity, sizeof(V4));
+        s->estr = calloc((size_t)s->W * s->H, sizeof(V4));
+        if (!s->pstress || !s->estr) return -2;
+    }
+    s->elastic_on = on;
+    return 0;
+}
+
 static uint32_t compute_caps(const OSim* s) {   /* mod.rs:2717-2761 (the bits that apply) */
     const OSimParams* p = &s->prm;
     uint32_t caps = 0;
     if (s->tank.families > 0) caps |= CAP_FAMILIES;
     if (s->settle_fams >= s->tank.families && s->tank.families > 0 && settles(s)) caps |= CAP_SETTLE;
+    if (s->tank.chan_e >= 0 && s->elastic_on) caps |= CAP_ELASTIC;   /* mod.rs:2746-2748 */
     if (s->thermal) caps |= CAP_THERMAL;
     int rigid = 0;
     for (int k = 0; k < s->tank.nrows; k++) {
@@ -956,6 +993,8 @@ static void build_mats(OSim* s) {
         g->th2[1] = m->emissivity;
         g->th2[2] = m->boil;
         g->th2[3] = m->latent_vap / m->heat_capacity;
+        g->el[0] = m->shear_modulus / (WATER_DENSITY * dx * dx);   /* mod.rs:2184 stress() */
+        g->el[1] = m->relax_time;
         g->el[2] = m->susceptibility;
         g->misc[0] = m->freeze_shift;
         g->misc[1] = m->load;
@@ -1075,6 +1114,12 @@ static void build_params(OSim* s, const OTool* tool) {
     P->heat3[1] = p->evaporation ? 2.257e6f / 1005.0f : 0.0f;
     P->heat3[2] = 0.0f;
     P->heat3[3] = clampf(p->magnet_demag, 0.0f, 1.0f);
+    float gmax = 0.0f;   /* mod.rs:2316-2321 */
+    for (int k = 0; k < s->tank.nrows; k++) gmax = maxf(gmax, p->mat[s->tank.rows[k]].shear_modulus);
+    P->elastic[0] = (float)s->tank.chan_e;
+    P->elastic[1] = maxf(gmax, 1e-3f) / (WATER_DENSITY * p->cell_size * p->cell_size);
+    P->elastic[2] = p->elastic_stress_max;
+    P->elastic[3] = p->elastic_step_max;
     float chi_max = 0.0f, sat = 0.05f;   /* mod.rs:2264 */
     for (int k = 0; k < s->tank.nrows; k++) {
         const OMat* m = &p->mat[s->tank.rows[k]];
@@ -1368,6 +1413,8 @@ typedef struct Scat {
     V4 Cs;
     float rho, sc, CT;
     int cw, cs, ct, cg;
+    int ce;     /* stress channel, -1: nothing to deposit */
+    V4 te;      /* stress / the largest modulus x STRESS_FIX */
 } Scat;
 
 static void report_umax(uint32_t* slot, float m) {
@@ -1393,6 +1440,10 @@ static void advance(OSim* s, uint32_t id, int gather, Scat* g) {
     int fam = s->mats[row].ib[0];   /* particles.comp:143 */
     int thermal = has_cap(s, CAP_THERMAL);
     V2 pos = v2(p.pos[0], p.pos[1]);
+    /* viscoelastic stress (particles.comp:152-156) */
+    int elastic = has_cap(s, CAP_ELASTIC);
+    V4 tau = v4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (elastic && (p.kind & KIND_FRESH) == 0u && s->mats[row].el[0] > 0.0f) tau = s->pstress[id];
     if (gather) {
         V2 v = v2(p.vel[0], p.vel[1]);
         V4 C = v4(p.c[0], p.c[1], p.c[2], p.c[3]);
@@ -1460,6 +1511,40 @@ static void advance(OSim* s, uint32_t id, int gather, Scat* g) {
                 C.z = 4.0f * (sud.x - u * sd.x) / sw;
                 C.w = 4.0f * (sud.y - u * sd.y) / sw;
             }
+        }
+        /* the upper-convected Maxwell update (particles.comp:250-279) */
+        if (elastic) {
+            float G = s->mats[row].el[0];
+            if (G > 0.0f) {
+                float l00 = C.x, l01 = C.y, l10 = C.z, l11 = C.w;   /* L = [[du/dx, du/dy], [dv/dx, dv/dy]] */
+                float lnorm = sqrtf(C.x * C.x + C.y * C.y + C.z * C.z + C.w * C.w) * dt;
+                if (P_.elastic[3] > 0.0f && lnorm > P_.elastic[3]) {
+                    float k = P_.elastic[3] / lnorm;
+                    l00 *= k; l01 *= k; l10 *= k; l11 *= k;
+                }
+                float t00 = tau.x, t01 = tau.z, t10 = tau.z, t11 = tau.y;
+                /* D = L T + T L^T + G (L + L^T) */
+                float d00 = ((l00 * t00 + l01 * t10) + (t00 * l00 + t01 * l01)) + G * (l00 + l00);
+                float d01 = ((l00 * t01 + l01 * t11) + (t00 * l10 + t01 * l11)) + G * (l01 + l10);
+                float d10 = ((l10 * t00 + l11 * t10) + (t10 * l00 + t11 * l01)) + G * (l10 + l01);
+                float d11 = ((l10 * t01 + l11 * t11) + (t10 * l10 + t11 * l11)) + G * (l11 + l11);
+                float lam = maxf(s->mats[row].el[1], 1e-4f);
+                float den = 1.0f + dt / lam;
+                float n00 = (t00 + dt * d00) / den, n01 = (t01 + dt * d01) / den;
+                float n10 = (t10 + dt * d10) / den, n11 = (t11 + dt * d11) / den;
+                tau = v4(n00, n11, 0.5f * (n01 + n10), 0.0f);
+                float tn = sqrtf(tau.x * tau.x + tau.y * tau.y + tau.z * tau.z);
+                if (P_.elastic[2] > 0.0f && tn > P_.elastic[2] * G) {
+                    float k = P_.elastic[2] * G / tn;
+                    tau = v4(tau.x * k, tau.y * k, tau.z * k, tau.w * k);
+                }
+                int c1x = clampi((int)pos.x, 1, s->W - 2), c1y = clampi((int)pos.y, 1, s->H - 2);
+                float around = 0.0f;
+                for (int b = -1; b <= 1; b++)
+                    for (int a = -1; a <= 1; a++) around += minf(s->cell[cidx(s, c1x + a, c1y + b)].x, 1.0f);
+                if (around < 1.0f) tau = v4(0.0f, 0.0f, 0.0f, 0.0f);
+            }
+            s->pstress[id] = tau;
         }
         if (P_.apic_clamp > 0.0f) {
             float lim = P_.apic_clamp / dt;
@@ -1836,6 +1921,9 @@ static void advance(OSim* s, uint32_t id, int gather, Scat* g) {
     g->cs = Mia[3];
     g->ct = thermal ? (int)P_.heat2[2] : -1;
     g->cg = thermal ? group_heat_chan(s, Mia[0]) : -1;
+    /* particles.comp:983-984 */
+    g->ce = elastic && (tau.x != 0.0f || tau.y != 0.0f || tau.z != 0.0f || tau.w != 0.0f) ? (int)P_.elastic[0] : -1;
+    g->te = v4(tau.x / P_.elastic[1] * 65536.0f, tau.y / P_.elastic[1] * 65536.0f, tau.z / P_.elastic[1] * 65536.0f, 0.0f);
 }
 
 static inline void acc_add(OSim* s, int x, int y, int ch, int v) {
@@ -1884,6 +1972,12 @@ static void deposit(OSim* s, const Scat* g) {
                 acc_add(s, nx, ny, 4, wi);
                 if (g->cw >= 0) acc_add(s, nx, ny, g->cw, wi);
                 if (g->cs >= 0 && g->sc > 0.0f) acc_add(s, nx, ny, g->cs, (int)floorf(w[a].x * w[b].y * g->sc * MASS_SCALE + 0.5f));
+                if (g->ce >= 0) {   /* particles.comp:1053-1058 */
+                    float wab = w[a].x * w[b].y;
+                    acc_add(s, nx, ny, g->ce, (int)floorf(wab * g->te.x + 0.5f));
+                    acc_add(s, nx, ny, g->ce + 1, (int)floorf(wab * g->te.y + 0.5f));
+                    acc_add(s, nx, ny, g->ce + 2, (int)floorf(wab * g->te.z + 0.5f));
+                }
                 if (g->ct >= 0) {
                     int hq = (int)floorf(w[a].x * w[b].y * g->CT * MASS_SCALE + 0.5f);
                     acc_add(s, nx, ny, g->ct, hq);
@@ -2119,6 +2213,11 @@ static void k_grid_prep(OSim* s) {
             }
             if (sol.w > 0.0f && level <= 0.0f) region_air |= 1u << (s->region[i] & REGION_MASK);
             if (s->caps & CAP_MAGNET) s->magc[i].x = chi;   /* grid_prep.comp:240 */
+            if (s->caps & CAP_ELASTIC) {   /* grid_prep.comp:241-244 */
+                int ce = (int)P_.elastic[0];
+                float sc = P_.elastic[1] * P_.inv_ppc / 65536.0f;
+                s->estr[i] = v4((float)s->acc[k + ce] * sc, (float)s->acc[k + ce + 1] * sc, (float)s->acc[k + ce + 2] * sc, 0.0f * sc);
+            }
             if (s->caps & (CAP_RIGID | CAP_RHEO)) {   /* grid_prep.comp:232-237 */
                 float cap = rho * o_expf(P_.heat2[0]);
                 if (mu >= cap && level > 0.0f) nn.w = 1.0f;
@@ -2185,6 +2284,35 @@ static void nn_eval(const OSim* s, int i, V4 q, float g, float* Fo, float* tauo)
         tau += skin;
     *Fo = 1.0f + q.x * (F - 1.0f);
     *tauo = tau * q.x;
+}
+
+/* elastic.comp: the divergence of the deposited stress accelerates the faces */
+static float txy_node(const OSim* s, int i) {
+    int W = s->W;
+    return 0.25f * (s->estr[i].z + s->estr[i - 1].z + s->estr[i - W].z + s->estr[i - W - 1].z);
+}
+
+static void k_elastic(OSim* s) {
+    int W = s->W, H = s->H;
+    float dt = s->S.dt;
+#pragma omp parallel for schedule(static)
+    for (int cy = 2; cy < H - 1; cy++)
+        for (int cx = 2; cx < W - 1; cx++) {
+            int i = cy * W + cx;
+            V4 q = s->vel[i];
+            V4 a = s->cell[i], l = s->cell[i - 1], b = s->cell[i - W];
+            if (face_live(q.z)) {
+                float rho = (a.x * a.y + l.x * l.y) / maxf(a.x + l.x, 1e-6f);
+                float f = (s->estr[i].x - s->estr[i - 1].x) + (txy_node(s, i + W) - txy_node(s, i));
+                q.x += dt * f / maxf(rho, 0.05f);
+            }
+            if (face_live(q.w)) {
+                float rho = (a.x * a.y + b.x * b.y) / maxf(a.x + b.x, 1e-6f);
+                float f = (s->estr[i].y - s->estr[i - W].y) + (txy_node(s, i + 1) - txy_node(s, i));
+                q.y += dt * f / maxf(rho, 0.05f);
+            }
+            s->vel[i] = q;
+        }
 }
 
 /* common.glsl:388-402: the magnets' field at (x, y), T */
@@ -4257,6 +4385,7 @@ static void substep(OSim* s, int gather) {
     k_particles(s, gather);
     k_grid_prep(s);
     if (s->caps & CAP_RHEO) k_rheo(s);
+    if (s->caps & CAP_ELASTIC) k_elastic(s);
     if (s->caps & CAP_SETTLE) k_settle(s);
     k_grid_coef(s);
     k_surf_smooth(s);
@@ -4346,7 +4475,7 @@ void osim_destroy(OSim* s) {
                     s->vel0, s->pjump, s->pres, s->p2keep, s->hcell, s->solid, s->sdf, s->region,
                     s->solid_t, s->mga, s->mgd, s->mgx, s->mgz, s->mgr, s->cgp, s->cgp2, s->cgq,
                     s->ptile, s->part, s->vr, s->vr2, s->vp, s->vq, s->vq2, s->vd, s->vaz, s->vma,
-                    s->vmb, s->vmd, s->vmr, s->vmx, s->vmz, s->tiles, s->vtile, s->pending, s->mixb, s->gbase, s->rh, s->famocc, s->dsettle, s->magc};
+                    s->vmb, s->vmd, s->vmr, s->vmx, s->vmz, s->tiles, s->vtile, s->pending, s->mixb, s->gbase, s->rh, s->famocc, s->dsettle, s->magc, s->pstress, s->estr};
     for (size_t k = 0; k < sizeof ptrs / sizeof ptrs[0]; k++) free(ptrs[k]);
     free(s);
 }
@@ -4462,12 +4591,13 @@ static int set_tank(OSim* s, const int* present, int thermal) {
     s->thermal = thermal;
     s->caps = compute_caps(s);
     int rc = 0;
-    if (s->caps & (CAP_RIGID | CAP_ELASTIC | CAP_STEAM | CAP_REACT)) rc = -4;
+    if (s->caps & (CAP_RIGID | CAP_STEAM | CAP_REACT)) rc = -4;
     for (int k = 0; k < nrows; k++) {
         const OMat* m = &p->mat[rows[k]];
         if (m->volatility > 0.0f || (thermal && m->boil < 1e8f)) rc = -4;
     }
     if (rc == 0) rc = set_settling(s, settles(s) ? s->tank.families : 0);
+    if (rc == 0) rc = set_elastic(s, s->tank.chan_e >= 0);
     if (rc == 0) s->caps = compute_caps(s);   /* with the settling buffers in place */
     if (rc == 0) {
         s->visc_mode = viscosity_mode(s);
@@ -4654,6 +4784,7 @@ long osim_field(const OSim* s, const char* name, void* out, size_t cap) {
     F("gbase", s->gbase, nc * 16)
     F("rh", s->rh, nc * 16)
     F("magc", s->magc, nc * 8)
+    F("estr", s->estr, nc * 16)
     F("famocc", s->famocc, nc * 4 * (size_t)s->settle_fams)
     F("dsettle", s->dsettle, nc * 8 * (size_t)s->settle_fams)
     F("surf2", s->surf2, nc * 16)

@@ -53,6 +53,7 @@ typedef struct OMat {
     float fume;
     float yield_stress, flow_index, shear_time, visc_ratio;
     float saturation;
+    float relax_time;
 } OMat;
 
 #define O_MAX_MATERIALS 96
@@ -93,6 +94,7 @@ typedef struct OSimParams {
     uint32_t slip_cap, sealed_vent;
     OMat mat[O_MAX_MATERIALS];
     float magnet_demag;
+    float elastic_stress_max, elastic_step_max;
 } OSimParams;
 
 /* ToolState (src/sim/params.rs:1141-1213). */

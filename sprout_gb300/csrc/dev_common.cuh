@@ -66,6 +66,10 @@ struct DevScene {
     float* famocc;    // per cell and family: the family's occupancy (settling)
     float2* dsettle;  // per cell and family: the concentration gain / loss rates settling hands the particles
     float2* magc;     // per cell: its liquid's susceptibility; the magnetic energy density of magnetic liquid there
+    float4* pstress;  // per particle slot (sorted order): its viscoelastic stress (xx, yy, xy)
+    float4* pstress2; // the same after the particle pass, in the pass's order
+    float4* pdep;     // the stress each particle deposits this substep, in the pass's order
+    float4* estr;     // per cell: the deposited stress (elastic.comp)
     int2* hcell;
     const float4* solid;
     const float* sdf;

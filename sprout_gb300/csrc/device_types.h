@@ -80,6 +80,7 @@ struct DevParams {
     // magnets (params.rs:1082-1087): how many, the strongest susceptibility in the tank, its
     // saturation (T), 1 / (water density dx^2); each magnet's position (cells), radius, strength
     // (T) and the direction of its north pole
+    float elastic[4];   // stress channel; the largest shear modulus / water's density (cells^2/s^2); stress cap (x G); step cap
     float mag[4];
     float magnet[kMaxMagnets][4];
     float magnet_dir[kMaxMagnets][4];

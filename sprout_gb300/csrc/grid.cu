@@ -208,6 +208,11 @@ __global__ void __launch_bounds__(256) k_grid_prep(DevScene d) {
             d.rh[i] = nn;
         }
         if ((P->caps & CAP_MAGNET) != 0u) d.magc[i].x = chi;
+        if ((P->caps & CAP_ELASTIC) != 0u) {   // the deposited stress (grid_prep.comp:241-244)
+            const int ce = (int)P->elastic[0];
+            const float sc = P->elastic[1] * P->inv_ppc / 65536.0f;
+            d.estr[i] = make_float4((float)d.acc[k + ce] * sc, (float)d.acc[k + ce + 1] * sc, (float)d.acc[k + ce + 2] * sc, 0.0f * sc);
+        }
         d.cell[i] = make_float4(phi_f, rho, mu, level);
         d.comp[i] = make_float4(rho, f[1], fam0, phi_t);
         if (P->sorts != 0u) d.gbase[i] = make_float4(bg[0], bg[1], bg[2], 0.0f);
@@ -795,6 +800,33 @@ __global__ void __launch_bounds__(256) k_rheo(DevScene d) {
     d.cell[i] = me;
 }
 
+// The shear stress at node i (the cell corner at its lower left): the four cells' mean.
+DEV float txy_node(const DevScene& d, int i) {
+    const int W = d.W;
+    return 0.25f * (d.estr[i].z + d.estr[i - 1].z + d.estr[i - W].z + d.estr[i - W - 1].z);
+}
+
+// elastic.comp: the divergence of the particles' deposited stress accelerates the faces.
+__global__ void __launch_bounds__(256) k_elastic(DevScene d) {
+    CELL_XY;
+    if (cx >= W - 1 || cy >= H - 1 || cx < 2 || cy < 2) return;
+    const int i = cy * W + cx;
+    float4 q = d.vel[i];
+    const float4 a = d.cell[i], l = d.cell[i - 1], b = d.cell[i - W];
+    const float dt = d.S->dt;
+    if (face_live(q.z)) {
+        const float rho = (a.x * a.y + l.x * l.y) / maxf(a.x + l.x, 1e-6f);
+        const float f = (d.estr[i].x - d.estr[i - 1].x) + (txy_node(d, i + W) - txy_node(d, i));
+        q.x += dt * f / maxf(rho, 0.05f);
+    }
+    if (face_live(q.w)) {
+        const float rho = (a.x * a.y + b.x * b.y) / maxf(a.x + b.x, 1e-6f);
+        const float f = (d.estr[i].y - d.estr[i - W].y) + (txy_node(d, i + 1) - txy_node(d, i));
+        q.y += dt * f / maxf(rho, 0.05f);
+    }
+    d.vel[i] = q;
+}
+
 // The settling flux of family f between an upper cell and a lower one at terminal velocity vt:
 // concentrate leaving the upper cell into the diluent of the lower one, bounded by what either
 // holds (settle.comp:8-16).
@@ -916,6 +948,7 @@ void launch_grid(const DevScene& d, const LaunchCfg& cfg, cudaStream_t st) {
     dim3 grd((d.W + 15) / 16, (d.H + 15) / 16);
     k_grid_prep<<<grd, blk, 0, st>>>(d);
     if (cfg.rheo) k_rheo<<<grd, blk, 0, st>>>(d);
+    if (cfg.elastic) k_elastic<<<grd, blk, 0, st>>>(d);
     if (cfg.settle) k_settle<<<grd, blk, 0, st>>>(d);
     k_coef_smooth<<<grd, blk, 0, st>>>(d);
     k_curv<<<grd, blk, 0, st>>>(d);

@@ -15,6 +15,7 @@ struct LaunchCfg {
     bool heat = false;        // thermal and heat_rate > 0: heat.comp runs
     bool rheo = false;        // a non-Newtonian liquid is in the tank: rheo.comp runs
     bool settle = false;      // a family with grains settles: settle.comp runs
+    bool elastic = false;     // a viscoelastic liquid: particles carry a stress, elastic.comp runs
     bool magnet = false;      // a magnet and a susceptible liquid: magnet.comp runs
     bool xtra = false;        // families, several phase groups, settling or currents: the particle pass's full form
     int visc_mode = 0;        // 0 none, 1 explicit, 2 implicit

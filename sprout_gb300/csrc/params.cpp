@@ -393,6 +393,15 @@ float SimParams::dt_capillary(const std::vector<int>& rows) const {
     return 0.5f * std::sqrt(1.0f / (2.0f * 3.14159274f * worst));
 }
 
+float SimParams::dt_elastic(const std::vector<int>& rows) const {
+    const float stiff = 1.0f + (elastic_stress_max > 0.0f ? elastic_stress_max : 50.0f);
+    float m = INFINITY;
+    for (int i : rows)
+        if (mat[i].shear_modulus > 0.0f)
+            m = std::min(m, 0.5f * cell_size / std::sqrt(stiff * mat[i].shear_modulus / mat[i].density));
+    return m;
+}
+
 float SimParams::dt_thermal(const std::vector<int>& rows) const {
     if (heat_rate <= 0.0f) return INFINITY;
     float dx2 = cell_size * cell_size;
@@ -456,6 +465,11 @@ bool Tank::layout(const std::vector<int>& rows_in, const SimParams& p, bool ther
                 first = false;
             }
     }
+    // three stress channels after the temperature ones when an elastic material is in (mod.rs:316-317)
+    bool elastic = false;
+    for (int r : rows_in) elastic |= p.mat[r].shear_modulus > 0.0f;
+    const int ce = elastic ? next : -1;
+    next += elastic ? 3 : 0;
     if (next > 32) return false;
     rows = rows_in;
     chan = ch;
@@ -464,6 +478,7 @@ bool Tank::layout(const std::vector<int>& rows_in, const SimParams& p, bool ther
     group_mask = gm;
     primary = prim >= 0 ? rows_in[prim] : -1;
     chan_t = ct;
+    chan_e = ce;
     for (int g = 0; g < 4; g++) chan_g[g] = cg[g];
     return true;
 }
@@ -616,6 +631,12 @@ void build_params(const SimParams& p, const Tank& t, bool thermal, uint32_t caps
     P->heat3[0] = std::max(p.eddy_heat, 0.0f);
     P->heat3[1] = p.evaporation ? 2.257e6f / 1005.0f : 0.0f;
     P->heat3[3] = std::min(std::max(p.magnet_demag, 0.0f), 1.0f);
+    float gmax = 0.0f;   // mod.rs:2316-2321
+    for (int r : t.rows) gmax = std::max(gmax, p.mat[r].shear_modulus);
+    P->elastic[0] = (float)t.chan_e;
+    P->elastic[1] = std::max(gmax, 1e-3f) / (kWaterDensity * dx * dx);
+    P->elastic[2] = p.elastic_stress_max;
+    P->elastic[3] = p.elastic_step_max;
     // the strongest susceptibility in the tank and its saturation (mod.rs:2264)
     float chi_max = 0.0f, sat = 0.05f;
     for (int r : t.rows)

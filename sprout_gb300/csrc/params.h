@@ -94,6 +94,8 @@ struct SimParams {
     float particle_heat_vol(int row) const;
     float dt_capillary(const std::vector<int>& rows) const;
     float dt_thermal(const std::vector<int>& rows) const;
+    // Longest substep that keeps elastic waves within half a cell (params.rs:947-960).
+    float dt_elastic(const std::vector<int>& rows) const;
     float enthalpy_temp(int row, float s, float t) const;
     // A custom liquid's diluent as the library resolves it (library.rs:318-330): -1 (none),
     // or another row that is a built-in without a diluent of its own or a custom liquid.
@@ -120,7 +122,7 @@ struct Magnet {
 struct Tank {
     std::vector<int> rows;
     std::vector<std::array3i> chan;
-    int stride = 8, families = 0, primary = -1, chan_t = -1;
+    int stride = 8, families = 0, primary = -1, chan_t = -1, chan_e = -1;
     uint32_t group_mask = 0;
     int chan_g[4] = {-1, -1, -1, -1};
     // Tank::layout (mod.rs:271-329). False if the rows do not fit.

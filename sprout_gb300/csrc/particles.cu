@@ -306,6 +306,14 @@ __global__ void __launch_bounds__(256) k_advance(DevScene d) {
             float4 C = q1;
             float ps = q2.x, pt = q2.w;
             uint32_t pid = __float_as_uint(q2.z);
+            // viscoelastic stress (upper-convected Maxwell): a particle that has not run a substep
+            // yet starts unstressed; the slot keeps what it held unless the pass updates it
+            // (particles.comp:152-156, 250-279)
+            const bool elastic = XTRA && (P->caps & CAP_ELASTIC) != 0u;
+            const float4 held_tau = elastic ? d.pstress[id] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            float4 tau = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            if (elastic && (kind & KIND_FRESH) == 0u && mats[row].el[0] > 0.0f) tau = held_tau;
+            float4 tau_store = held_tau;
             bool alive = true;
             if (S->gather) {
                 Grid g{d.vel, d.sdf, d.W, d.H};
@@ -314,6 +322,45 @@ __global__ void __launch_bounds__(256) k_advance(DevScene d) {
                 float crowd = 0.0f;
                 gather_face<0>(g, px, py, vx, corrx, C.x, C.y);
                 gather_face<1>(g, px, py, vy, corry, C.z, C.w);
+                if (elastic) {
+                    const float G = mats[row].el[0];
+                    if (G > 0.0f) {
+                        // L = [[du/dx, du/dy], [dv/dx, dv/dy]] (the APIC matrix); at most
+                        // elastic_step_max of deformation per substep enters the stress
+                        float l00 = C.x, l01 = C.y, l10 = C.z, l11 = C.w;
+                        const float lnorm = sqrtf(C.x * C.x + C.y * C.y + C.z * C.z + C.w * C.w) * dt;
+                        if (P->elastic[3] > 0.0f && lnorm > P->elastic[3]) {
+                            const float k = P->elastic[3] / lnorm;
+                            l00 *= k;
+                            l01 *= k;
+                            l10 *= k;
+                            l11 *= k;
+                        }
+                        const float t00 = tau.x, t01 = tau.z, t10 = tau.z, t11 = tau.y;
+                        // D = L T + T L^T + G (L + L^T), each entry summed in that order
+                        const float d00 = ((l00 * t00 + l01 * t10) + (t00 * l00 + t01 * l01)) + G * (l00 + l00);
+                        const float d01 = ((l00 * t01 + l01 * t11) + (t00 * l10 + t01 * l11)) + G * (l01 + l10);
+                        const float d10 = ((l10 * t00 + l11 * t10) + (t10 * l00 + t11 * l01)) + G * (l10 + l01);
+                        const float d11 = ((l10 * t01 + l11 * t11) + (t10 * l10 + t11 * l11)) + G * (l11 + l11);
+                        const float lam = maxf(mats[row].el[1], 1e-4f);
+                        const float den = 1.0f + dt / lam;
+                        const float n00 = (t00 + dt * d00) / den, n01 = (t01 + dt * d01) / den;
+                        const float n10 = (t10 + dt * d10) / den, n11 = (t11 + dt * d11) / den;
+                        tau = make_float4(n00, n11, 0.5f * (n01 + n10), 0.0f);
+                        const float tn = sqrtf(tau.x * tau.x + tau.y * tau.y + tau.z * tau.z);
+                        if (P->elastic[2] > 0.0f && tn > P->elastic[2] * G) {
+                            const float k = P->elastic[2] * G / tn;
+                            tau = make_float4(tau.x * k, tau.y * k, tau.z * k, tau.w * k);
+                        }
+                        // no liquid around (spray, a torn-off droplet): no stress the grid can carry
+                        const int c1x = clampi((int)px, 1, d.W - 2), c1y = clampi((int)py, 1, d.H - 2);
+                        float around = 0.0f;
+                        for (int b = -1; b <= 1; b++)
+                            for (int a = -1; a <= 1; a++) around += minf(d.cell[(c1y + b) * d.W + c1x + a].x, 1.0f);
+                        if (around < 1.0f) tau = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                    }
+                    tau_store = tau;
+                }
                 if (P->apic_clamp > 0.0f) {
                     float lim = P->apic_clamp / dt;
                     C.x = clampf(C.x, -lim, lim);
@@ -638,6 +685,10 @@ __global__ void __launch_bounds__(256) k_advance(DevScene d) {
                 d.part2[3 * id + 0] = make_float4(px, py, pvx, pvy);
                 d.part2[3 * id + 1] = C;
                 d.part2[3 * id + 2] = make_float4(ps, __uint_as_float(kind), __uint_as_float(pid), pt);
+                if (elastic) {
+                    d.pstress2[id] = tau_store;
+                    d.pdep[id] = tau;
+                }
             }
         }
     }
@@ -786,11 +837,13 @@ __global__ void __launch_bounds__(256) k_cell_gather(DevScene d) {
         d.part[3 * j + 0] = a;
         d.part[3 * j + 1] = b;
         d.part[3 * j + 2] = c;
+        if (d.pstress) d.pstress[j] = d.pstress2[src];   // the stress moves with its particle (sort.comp:66)
     } else {
         const float4 z = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         d.part[3 * j + 0] = z;
         d.part[3 * j + 1] = z;
         d.part[3 * j + 2] = z;
+        if (d.pstress) d.pstress[j] = z;
     }
 }
 
@@ -861,6 +914,18 @@ __global__ void __launch_bounds__(256) k_p2g(DevScene d) {
         const float vsx = q0.z * dt, vsy = q0.w * dt;
         const float csx = q1.x * dt, csy = q1.y * dt, csz = q1.z * dt, csw = q1.w * dt;
         const int cw = ia[2], cs = ia[3];
+        // the stress it deposits (particles.comp:983-984, 1050-1055): only a stressed particle
+        int ce = -1;
+        float tex = 0.0f, tey = 0.0f, tez = 0.0f;
+        if (d.pdep && (P->caps & CAP_ELASTIC) != 0u) {
+            const float4 tau = d.pdep[d.perm[pi]];
+            if (tau.x != 0.0f || tau.y != 0.0f || tau.z != 0.0f || tau.w != 0.0f) {
+                ce = (int)P->elastic[0];
+                tex = tau.x / P->elastic[1] * 65536.0f;
+                tey = tau.y / P->elastic[1] * 65536.0f;
+                tez = tau.z / P->elastic[1] * 65536.0f;
+            }
+        }
         float wx[3], wy[3];
         {   // u faces at (i, j + 0.5)
             float gx = px - 0.0f, gy = py - 0.5f;
@@ -911,6 +976,12 @@ __global__ void __launch_bounds__(256) k_p2g(DevScene d) {
                     sadd(sacc, pst, lx, ly, 4, wi);
                     if (cw >= 0) sadd(sacc, pst, lx, ly, cw, wi);
                     if (cs >= 0 && ps > 0.0f) sadd(sacc, pst, lx, ly, cs, (int)floorf(wx[a] * wy[b] * ps * MASS_SCALE + 0.5f));
+                    if (ce >= 0) {
+                        const float wab = wx[a] * wy[b];
+                        sadd(sacc, pst, lx, ly, ce, (int)floorf(wab * tex + 0.5f));
+                        sadd(sacc, pst, lx, ly, ce + 1, (int)floorf(wab * tey + 0.5f));
+                        sadd(sacc, pst, lx, ly, ce + 2, (int)floorf(wab * tez + 0.5f));
+                    }
                     if (ct >= 0) {
                         int hq = (int)floorf(wx[a] * wy[b] * CT * MASS_SCALE + 0.5f);
                         sadd(sacc, pst, lx, ly, ct, hq);

@@ -312,7 +312,7 @@ struct SproutSim {
     float dt_limit() const {
         float dt = std::min(params.dt_max, params.dt_capillary(tank.rows));
         if (thermal) dt = std::min(dt, params.dt_thermal(tank.rows));
-        return dt;
+        return std::min(dt, params.dt_elastic(tank.rows));
     }
 
     int viscosity_mode() const {
@@ -330,6 +330,27 @@ struct SproutSim {
         if (dmax <= 0.0f) return 0;
         if (dmax <= 0.05f) return 1;
         return 2;
+    }
+
+    // The particles' stress buffers while the tank holds an elastic material (set_elastic,
+    // mod.rs:2084-2110): zero-filled each time they are taken up again.
+    bool elastic_on = false;
+    int set_elastic(bool on) {
+        if (on == elastic_on) return SPROUT_OK;
+        if (on) {
+            if (!d.pstress) {
+                int rc = alloc(&d.pstress, (size_t)capacity);
+                if (rc == SPROUT_OK) rc = alloc(&d.pstress2, (size_t)capacity);
+                if (rc == SPROUT_OK) rc = alloc(&d.pdep, (size_t)capacity);
+                if (rc == SPROUT_OK) rc = alloc(&d.estr, (size_t)W * H);
+                if (rc != SPROUT_OK) return rc;
+            } else {
+                CUDA_TRY(cudaMemsetAsync(d.pstress, 0, (size_t)capacity * sizeof(float4), stream));
+            }
+            graph_ok = false;   // new device pointers: the captured substep is stale
+        }
+        elastic_on = on;
+        return SPROUT_OK;
     }
 
     // Whether a family in the tank settles: a concentrate with grains under gravity (mod.rs:2139-2143).
@@ -360,6 +381,7 @@ struct SproutSim {
         uint32_t c = 0;
         if (tank.families > 0) c |= CAP_FAMILIES;
         if (settle_fams >= tank.families && tank.families > 0 && settles()) c |= CAP_SETTLE;
+        if (tank.chan_e >= 0 && elastic_on) c |= CAP_ELASTIC;   // mod.rs:2746-2748
         if (thermal) c |= CAP_THERMAL;
         bool rigid = false;
         for (int r : tank.rows) {
@@ -371,7 +393,6 @@ struct SproutSim {
             }
             if (thermal) rigid |= m.freezes() || (dil && dil->freezes()) || m.temp_model != 0 || (dil && dil->temp_model != 0);
             rigid |= m.viscosity_at(params.ambient_temp) >= params.rigid_viscosity || (!thermal && m.freezes() && params.ambient_temp < m.melt_hi);
-            if (m.shear_modulus > 0.0f) c |= CAP_ELASTIC;
             if (!magnets.empty() && m.susceptibility > 0.0f) c |= CAP_MAGNET;
             if (m.react_with >= 0 && m.react_rate > 0.0f && std::find(tank.rows.begin(), tank.rows.end(), m.react_with) != tank.rows.end()) c |= CAP_REACT;
             if (r == 57 && thermal) c |= CAP_STEAM;
@@ -539,7 +560,8 @@ struct SproutSim {
         want.rheo = (caps & CAP_RHEO) != 0u;
         want.settle = (caps & CAP_SETTLE) != 0u;
         want.magnet = (caps & CAP_MAGNET) != 0u;
-        want.xtra = tank.families > 0 || (tank.group_mask & ~1u) != 0u || !currents.empty();
+        want.elastic = (caps & CAP_ELASTIC) != 0u;
+        want.xtra = tank.families > 0 || (tank.group_mask & ~1u) != 0u || !currents.empty() || tank.chan_e >= 0;
         want.visc_mode = visc_mode;
         want.twice = visc_mode == 2 && params.viscous_projection != 0;
         want.viscous_warm = params.viscous_warm != 0;
@@ -552,7 +574,7 @@ struct SproutSim {
             if (v > 0) want.visc_blocks = std::max(1, std::min(v, visc_max[want.visc_sweeps - 1]));
         }
         want.mixed = mixed;
-        bool same = want.n_slots == cfg.n_slots && want.thermal == cfg.thermal && want.heat == cfg.heat && want.rheo == cfg.rheo && want.settle == cfg.settle && want.magnet == cfg.magnet && want.xtra == cfg.xtra &&
+        bool same = want.n_slots == cfg.n_slots && want.thermal == cfg.thermal && want.heat == cfg.heat && want.rheo == cfg.rheo && want.settle == cfg.settle && want.magnet == cfg.magnet && want.elastic == cfg.elastic && want.xtra == cfg.xtra &&
                     want.visc_mode == cfg.visc_mode && want.twice == cfg.twice && want.viscous_warm == cfg.viscous_warm &&
                     want.visc_levels == cfg.visc_levels && want.visc_sweeps == cfg.visc_sweeps &&
                     want.visc_blocks == cfg.visc_blocks && want.mixed == cfg.mixed && d.stride == std::max(tank.stride, 8);
@@ -649,14 +671,15 @@ struct SproutSim {
         thermal = th;
         caps = compute_caps();
         int rc = SPROUT_OK;
-        if (caps & (CAP_RIGID | CAP_ELASTIC | CAP_STEAM | CAP_REACT))
-            rc = fail(SPROUT_E_UNSUPPORTED, "the tank needs rigid / elastic / steam / reaction passes, which this engine does not carry");
+        if (caps & (CAP_RIGID | CAP_STEAM | CAP_REACT))
+            rc = fail(SPROUT_E_UNSUPPORTED, "the tank needs rigid / steam / reaction passes, which this engine does not carry");
         for (int r : tank.rows) {
             const MatProps& m = params.mat[r];
             if (rc == SPROUT_OK && (m.volatility > 0.0f || (thermal && m.boil < 1e8f)))
                 rc = fail(SPROUT_E_UNSUPPORTED, "evaporation and boiling are not carried by this engine");
         }
         if (rc == SPROUT_OK) rc = set_settling(settles() ? tank.families : 0);
+        if (rc == SPROUT_OK) rc = set_elastic(tank.chan_e >= 0);
         if (rc == SPROUT_OK) caps = compute_caps();   // with the settling buffers in place
         if (rc == SPROUT_OK && tank.families > 1 && d.mixb == nullptr) {
             // the concentrations of families 1.. per cell, from the first tank that has them
@@ -1715,6 +1738,7 @@ int sprout_sim_download_field(SproutSim* sim, const char* name, void* out, size_
     else if (n == "gbase") { src = d.gbase; b = nc * 16; }
     else if (n == "rh") { src = d.rh; b = nc * 16; }
     else if (n == "magc") { src = d.magc; b = nc * 8; }
+    else if (d.estr && n == "estr") { src = d.estr; b = nc * 16; }
     else if (d.famocc && n == "famocc") { src = d.famocc; b = nc * 4 * (size_t)sim->settle_fams; }
     else if (d.dsettle && n == "dsettle") { src = d.dsettle; b = nc * 8 * (size_t)sim->settle_fams; }
     else if (n == "surf2") { src = d.surf2; b = nc * 16; }

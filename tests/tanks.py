@@ -144,3 +144,14 @@ def magnetic(w: int = 96, h: int = 64, cell: float = 0.002, mat: int = 37, demag
     t = Tank(w, h, s, [], fills)
     t.magnets = [{"pos": (0.5 * w, 0.45 * h), "radius": 4.0, "strength": 1.0, "dir": (0.0, 1.0)}]
     return t
+
+
+def elastic_drop(w: int = 96, h: int = 64, cell: float = 0.002, mat: int = 12) -> Tank:
+    """A block of a viscoelastic built-in (slime, 12, or putty, 33) falling into water: its
+    particles carry an upper-convected Maxwell stress that elastic.comp turns into force."""
+    key = {12: "slime", 33: "putty"}[mat]
+    s = {"cell_size": cell, "fixed_hz": 240.0, "pressure_tol": 1e-5, "viscosity_tol": 1e-5,
+         "tension_water": 0.0, f"tension_{key}": 0.0}
+    fills = [([0.0, 0.0, float(w), float(int(0.25 * h))], 0, None),
+             ([float(int(0.35 * w)), float(int(0.45 * h)), float(int(0.65 * w)), float(int(0.7 * h))], mat, None)]
+    return Tank(w, h, s, [], fills)
