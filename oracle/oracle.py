@@ -68,6 +68,7 @@ class OSimParams(C.Structure):
         ("mat", OMat * 96),
         ("magnet_demag", C.c_float),
         ("elastic_stress_max", C.c_float), ("elastic_step_max", C.c_float),
+        ("rigid_contact", C.c_uint32), ("rigid_friction", C.c_float),
     ]
 
 

@@ -279,6 +279,8 @@ void oparams_default(OSimParams* p) {
     p->sealed_vent = 1;
     p->elastic_stress_max = 10.0f;   /* params.rs:447-448 */
     p->elastic_step_max = 0.25f;
+    p->rigid_contact = 1;   /* params.rs: rigid_contact, rigid_friction */
+    p->rigid_friction = 0.6f;
     for (int r = 0; r < O_MAX_MATERIALS; r++) mat_default(&p->mat[r]);
     /* the built-in liquids (presets.rs: BUILTINS): the fields the oracle carries */
 #define BUILTIN_P(row, field, v) p->mat[row].field = v;
@@ -698,6 +700,9 @@ struct OSim {
     V2* magc;   /* per cell: susceptibility; magnetic energy density (magnet.comp) */
     V4* pstress;   /* per particle slot: viscoelastic stress (xx, yy, xy), in place */
     V4* estr;      /* per cell: the deposited stress (elastic.comp) */
+    I2* rl;        /* per cell: rigid label (root cell, -1 not rigid); its body at the root */
+    int64_t* rbody;   /* per body: 15 fixed-point sums (rigid.comp) */
+    uint32_t nbodies;
     int elastic_on;
     int n_currents;
     V2 *vel0, *pjump, *pres;
@@ -935,6 +940,12 @@ static uint32_t compute_caps(const OSim* s) {   /* mod.rs:2717-2761 (the bits th
         if (s->tank.rows[k] == 57 && s->thermal) caps |= CAP_STEAM;
     for (int k = 0; k < s->tank.nrows; k++)   /* mod.rs:2749-2751 */
         if (s->n_magnets > 0 && p->mat[s->tank.rows[k]].susceptibility > 0.0f) caps |= CAP_MAGNET;
+    for (int k = 0; k < s->tank.nrows; k++) {   /* mod.rs:2755-2757 */
+        const OMat* m = &p->mat[s->tank.rows[k]];
+        if (m->react_with >= 0 && m->react_rate > 0.0f)
+            for (int j = 0; j < s->tank.nrows; j++)
+                if (s->tank.rows[j] == m->react_with) caps |= CAP_REACT;
+    }
     return caps;
 }
 
@@ -1045,7 +1056,7 @@ static void build_params(OSim* s, const OTool* tool) {
     P->misc[0] = p->curvature_max;
     P->misc[1] = (float)p->sealed_vent;
     P->misc[2] = p->cell_size;
-    P->misc[3] = -1.0f;
+    P->misc[3] = p->rigid_contact != 0 ? p->rigid_friction : -1.0f;   /* mod.rs:2280 */
     P->n_present = s->tank.nrows;
     P->acc_stride = s->tank.stride > ACC_MIN ? s->tank.stride : ACC_MIN;
     P->n_fam = s->tank.families;
@@ -1428,6 +1439,11 @@ static void report_umax(uint32_t* slot, float m) {
 /* advance() (particles.comp:98-985) restricted to the capabilities the oracle carries:
  * single phase group or several without drift, no families, no rigid bodies, elasticity,
  * settling, steam, reactions or evaporation; thermal conduction and exchange supported. */
+#define O_MAX_BODIES 4096   /* common.glsl: MAX_BODIES */
+typedef struct { float x, y, z; } V3f;
+static float row_lnu(const OSim* s, uint32_t row, float sc, float T, int thermal);
+static int body_motion(const OSim* s, int b, int r, V2 x, V3f* u);
+
 static void advance(OSim* s, uint32_t id, int gather, Scat* g) {
     g->live = 0;
     if (id >= P_.n_slots) return;
@@ -1440,6 +1456,14 @@ static void advance(OSim* s, uint32_t id, int gather, Scat* g) {
     int fam = s->mats[row].ib[0];   /* particles.comp:143 */
     int thermal = has_cap(s, CAP_THERMAL);
     V2 pos = v2(p.pos[0], p.pos[1]);
+    /* particles.comp:144-151: frozen, or too viscous to flow: part of a rigid body */
+    int rigid_cap = has_cap(s, CAP_RIGID);
+    int frozen = 0;
+    if (rigid_cap) {
+        V2 ph = thermal ? phase_of(p.t, thermal_of(s, row, p.s)) : v2(P_.heat[0], 0.0f);
+        frozen = ph.y > 0.5f || row_lnu(s, row, p.s, ph.x, thermal) >= P_.heat2[0];
+    }
+    int held = 0;
     /* viscoelastic stress (particles.comp:152-156) */
     int elastic = has_cap(s, CAP_ELASTIC);
     V4 tau = v4(0.0f, 0.0f, 0.0f, 0.0f);
@@ -1510,6 +1534,27 @@ static void advance(OSim* s, uint32_t id, int gather, Scat* g) {
                 corr.y = sc / sw;
                 C.z = 4.0f * (sud.x - u * sd.x) / sw;
                 C.w = 4.0f * (sud.y - u * sd.y) / sw;
+            }
+        }
+        /* particles.comp:222-248: a frozen particle, a yield-stress plug's particle in a sparse
+         * cell, or any particle in a rigid cell moves exactly with the body around it */
+        if (rigid_cap) {
+            int pcx = clampi((int)pos.x, 0, s->W - 1), pcy = clampi((int)pos.y, 0, s->H - 1);
+            int plug = (s->mats[row].rheo[0] > 0.0f || s->mats[row].temp[3] > 0.0f) && s->cell[cidx(s, pcx, pcy)].w <= 0.0f;
+            int c0x = clampi((int)pos.x, 1, s->W - 2), c0y = clampi((int)pos.y, 1, s->H - 2);
+            int in_body = row != 57u && s->rl[cidx(s, c0x, c0y)].x >= 0;
+            if (frozen || plug || in_body) {
+                static const int ox[9] = {0, -1, 1, 0, 0, -1, 1, -1, 1}, oy[9] = {0, 0, 0, -1, 1, -1, -1, 1, 1};
+                for (int k = 0; k < 9 && !held; k++) {
+                    int root = s->rl[cidx(s, c0x + ox[k], c0y + oy[k])].x;
+                    if (root < 0 || s->rl[root].y < 0) continue;
+                    V3f u;
+                    if (body_motion(s, s->rl[root].y, root, pos, &u)) {
+                        v = v2(u.x, u.y);
+                        C = v4(0.0f, -u.z, u.z, 0.0f);
+                        held = 1;
+                    }
+                }
             }
         }
         /* the upper-convected Maxwell update (particles.comp:250-279) */
@@ -1642,7 +1687,7 @@ static void advance(OSim* s, uint32_t id, int gather, Scat* g) {
                 int g = Mia[0];
                 float fg = g == 0 ? 1.0f - sg[0] - sg[1] - sg[2] : sg[g - 1];
                 float others = 1.0f - fg;
-                if (others > 1e-4f && groups) {
+                if (others > 1e-4f && groups && !held) {
                     V4 sgr = v4(0.0f, 0.0f, 0.0f, 0.0f), snu = sgr, snw = sgr;
                     for (int b = 0; b < 3; b++)
                         for (int a = 0; a < 3; a++) {
@@ -1698,7 +1743,7 @@ static void advance(OSim* s, uint32_t id, int gather, Scat* g) {
                     }
                 }
                 /* drift within a phase group (particles.comp:478-502) */
-                if (sorts) {
+                if (sorts && !held) {
                     float fgi = groups ? sg[Mia[0] - 1] : 1.0f;
                     if (fgi > 1e-4f) {
                         float rmean = sbg / sw / fgi;
@@ -1754,6 +1799,7 @@ static void advance(OSim* s, uint32_t id, int gather, Scat* g) {
                 }
             }
         }
+        if (held && crowd <= REST_PHI + maxf(P_.corr[1], 0.05f)) corr = v2(0.0f, 0.0f);   /* particles.comp:576 */
         /* drains (particles.comp:577-594) */
         for (int c = 0; c < (int)P_.ext[3]; c++) {
             const float* z = P_.current_zone[c];
@@ -1834,7 +1880,7 @@ static void advance(OSim* s, uint32_t id, int gather, Scat* g) {
         }
         /* advect (particles.comp:847-865) */
         V2 va = v;
-        if (P_.ext[1] >= 2.0f && !pushed) {
+        if (P_.ext[1] >= 2.0f && !pushed && !held) {
             V2 xm = v2(clampf(pos.x + 0.5f * dt * (v.x + corr.x + 0.0f), 2.01f, (float)s->W - 2.01f),
                        clampf(pos.y + 0.5f * dt * (v.y + corr.y + slip), 2.01f, (float)s->H - 2.01f));
             V2 here = sample_vel(s, pos, v);
@@ -2312,6 +2358,207 @@ static void k_elastic(OSim* s) {
                 q.y += dt * f / maxf(rho, 0.05f);
             }
             s->vel[i] = q;
+        }
+}
+
+/* ---- rigid bodies (rigid.comp; common.glsl:265-340) ------------------------------- */
+#define O_FIX 65536.0f
+
+/* common.glsl:275-277: a body sum, as the shader reads its two words */
+static float get64(int64_t v) {
+    uint64_t u = (uint64_t)v;
+    return ((float)(int32_t)(uint32_t)(u >> 32) * 4294967296.0f + (float)(uint32_t)u) / O_FIX;
+}
+
+/* rigid.comp add64: x rounded to an integer, added in 64 bits */
+static void add64(int64_t* w, float x) {
+    x = floorf(x + 0.5f);
+    *w += (int64_t)x;
+}
+
+/* common.glsl:631-636 */
+static float row_lnu(const OSim* s, uint32_t row, float sc, float T, int thermal) {
+    float l = s->mats[row].a[1] + (thermal ? temp_law(s, (int)row, T) : 0.0f);
+    int d = s->mats[row].ia[1];
+    if (d >= 0) l = mixf(s->mats[d].a[1] + (thermal ? temp_law(s, d, T) : 0.0f), l, sc);
+    return l;
+}
+
+/* common.glsl:289-325: contact of a body with the solids it touches */
+static void body_contact(const int64_t* o, float mu, V2 cm, V2* U, float* w) {
+    float nc = get64(o[7]);
+    if (mu < 0.0f || nc < 0.5f) return;
+    V2 ns = v2(get64(o[8]), get64(o[9]));
+    if (len2(ns) < 0.25f * nc) return;
+    float ln = len2(ns);
+    V2 n = v2(ns.x / ln, ns.y / ln);
+    V2 t = v2(n.y, -n.x);
+    V2 cc = v2(get64(o[10]) / nc, get64(o[11]) / nc);
+    float sqx = get64(o[12]) / nc - cc.x * cc.x, sqy = get64(o[13]) / nc - cc.y * cc.y, sqz = get64(o[14]) / nc - cc.x * cc.y;
+    float ext = sqrtf(3.0f * maxf(t.x * t.x * sqx + t.y * t.y * sqy + 2.0f * t.x * t.y * sqz, 0.0f)) + 0.5f;
+    V2 rc = v2(cc.x - cm.x, cc.y - cm.y);
+    V2 uc = v2(U->x + *w * -rc.y, U->y + *w * rc.x);
+    float vn = uc.x * n.x + uc.y * n.y;
+    float sp = (cm.x - cc.x) * t.x + (cm.y - cc.y) * t.y;
+    float vn1 = vn, w1 = *w;
+    if (fabsf(sp) <= ext) {
+        vn1 = maxf(vn, 0.0f);
+        w1 = clampf(*w, -vn1 / ext, vn1 / ext);
+    } else {
+        float edge = signf(sp) * ext;
+        vn1 = maxf(vn + *w * edge, 0.0f) - *w * edge;
+    }
+    if (vn1 == vn && w1 == *w) return;
+    float vt = uc.x * t.x + uc.y * t.y;
+    float vt1 = signf(vt) * maxf(fabsf(vt) - mu * (vn1 - vn), 0.0f);
+    uc = v2(uc.x + ((vn1 - vn) * n.x + (vt1 - vt) * t.x), uc.y + ((vn1 - vn) * n.y + (vt1 - vt) * t.y));
+    *w = w1;
+    *U = v2(uc.x - w1 * -rc.y, uc.y - w1 * rc.x);
+}
+
+/* common.glsl:327-340: the rigid motion of body b (root cell r) at x: velocity, spin */
+static int body_motion(const OSim* s, int b, int r, V2 x, V3f* u) {
+    const int64_t* o = s->rbody + (size_t)b * 16;
+    float M = get64(o[0]);
+    if (M <= 1e-3f) return 0;
+    V2 cm = v2(get64(o[1]) / M, get64(o[2]) / M);
+    V2 U = v2(get64(o[3]) / M, get64(o[4]) / M);
+    float L = get64(o[5]) - M * (cm.x * U.y - cm.y * U.x);
+    float I = get64(o[6]) - M * (cm.x * cm.x + cm.y * cm.y);
+    float w = I > 1e-3f ? L / I : 0.0f;
+    body_contact(o, P_.misc[3], cm, &U, &w);
+    V2 d = v2(x.x - ((float)(r % s->W) + 0.5f) - cm.x, x.y - ((float)(r / s->W) + 0.5f) - cm.y);
+    u->x = U.x + w * -d.y;
+    u->y = U.y + w * d.x;
+    u->z = w;
+    return 1;
+}
+
+/* rigid.comp:10-25: whether liquid cell i moves rigidly */
+static int cell_rigid(const OSim* s, int cx, int cy, int i) {
+    V4 me = s->cell[i];
+    if (me.w <= 0.0f) return 0;
+    if ((s->caps & CAP_THERMAL) && s->therm[i].w > 0.5f) return 1;
+    V4 q = s->rh[i];
+    if (q.w > 0.5f) return 1;
+    if (!(s->caps & CAP_RHEO) || q.x <= 0.0f || cx < 1 || cy < 1 || cx >= s->W - 1 || cy >= s->H - 1) return 0;
+    float g = shear_rate(s, i, 0);
+    float F, tau;
+    nn_eval(s, i, q, g, &F, &tau);
+    if (tau > 0.0f && me.z * g < tau) return 1;
+    return s->mats[(int)q.y].ib[1] == 3 && me.z * F >= me.y * o_expf(P_.heat2[0]);
+}
+
+/* rigid.comp:27-36: the node SDF bilinearly, and its gradient */
+static float rigid_sdf(const OSim* s, float x, float y, V2* grad) {
+    float gx = clampf(x, 0.0f, (float)s->W - 0.001f), gy = clampf(y, 0.0f, (float)s->H - 0.001f);
+    int ix = (int)gx, iy = (int)gy;
+    float fx = gx - (float)ix, fy = gy - (float)iy;
+    int w1 = s->W + 1, k = iy * w1 + ix;
+    float d00 = s->sdf[k], d10 = s->sdf[k + 1], d01 = s->sdf[k + w1], d11 = s->sdf[k + w1 + 1];
+    *grad = v2(mixf(d10 - d00, d11 - d01, fy), mixf(d01 - d00, d11 - d10, fx));
+    return mixf(mixf(d00, d10, fx), mixf(d01, d11, fx), fy);
+}
+
+static int rl_find(const OSim* s, int i) {
+    while (s->rl[i].x != i) i = s->rl[i].x;
+    return i;
+}
+
+/* rigid.comp modes 0-4: label the rigid cells, join them into bodies (each body's root is
+ * its smallest cell), sum each body's mass, moments and contacts, and move the faces inside
+ * a body with it */
+static void k_rigid(OSim* s) {
+    int W = s->W, H = s->H;
+    size_t nc = (size_t)W * H;
+    for (int cy = 0; cy < H; cy++)
+        for (int cx = 0; cx < W; cx++) {
+            int i = cy * W + cx;
+            s->rl[i] = (I2){cell_rigid(s, cx, cy, i) ? i : -1, -1};
+        }
+    s->nbodies = 0;
+    for (int cy = 0; cy < H; cy++)
+        for (int cx = 0; cx < W; cx++) {
+            int i = cy * W + cx;
+            if (s->rl[i].x < 0) continue;
+            int nb[4] = {cx > 0 ? i - 1 : -1, cy > 0 ? i - W : -1, (cy > 0 && cx > 0) ? i - W - 1 : -1,
+                         (cy > 0 && cx < W - 1) ? i - W + 1 : -1};
+            for (int q = 0; q < 4; q++) {
+                if (nb[q] < 0 || s->rl[nb[q]].x < 0) continue;
+                int a = rl_find(s, i), b = rl_find(s, nb[q]);
+                if (a < b) s->rl[b].x = a;
+                else if (b < a) s->rl[a].x = b;
+            }
+        }
+    for (size_t i = 0; i < nc; i++) {
+        if (s->rl[i].x < 0) continue;
+        int r = rl_find(s, (int)i);
+        s->rl[i].x = r;
+        if (r == (int)i && s->nbodies < O_MAX_BODIES) {
+            uint32_t b = s->nbodies++;
+            memset(s->rbody + (size_t)b * 16, 0, 16 * sizeof(int64_t));
+            s->rl[i].y = (int)b;
+        }
+    }
+    for (int cy = 0; cy < H; cy++)
+        for (int cx = 0; cx < W; cx++) {
+            int i = cy * W + cx;
+            int l = s->rl[i].x;
+            if (l < 0) continue;
+            int b = s->rl[l].y;
+            if (b < 0) continue;
+            int64_t* o = s->rbody + (size_t)b * 16;
+            float m = s->cell[i].y * minf(s->cell[i].x, 1.0f) * O_FIX;
+            V2 d = v2((float)(cx - l % W), (float)(cy - l / W));
+            V4 q = s->vel[i];
+            float ur = cx < W - 1 ? s->vel[i + 1].x : 0.0f, ut = cy < H - 1 ? s->vel[i + W].y : 0.0f;
+            V2 u = v2(0.5f * (q.x + ur), 0.5f * (q.y + ut));
+            add64(&o[0], m);
+            add64(&o[1], m * d.x);
+            add64(&o[2], m * d.y);
+            add64(&o[3], m * u.x);
+            add64(&o[4], m * u.y);
+            add64(&o[5], m * (d.x * u.y - d.y * u.x));
+            add64(&o[6], m * ((d.x * d.x + d.y * d.y) + 1.0f / 6.0f));
+            if (P_.misc[3] >= 0.0f) {
+                V2 g;
+                float dist = rigid_sdf(s, (float)cx + 0.5f, (float)cy + 0.5f, &g);
+                if (dist < 1.0f && g.x * g.x + g.y * g.y > 1e-8f) {
+                    float gl = len2(g);
+                    V2 nrm = v2(g.x / gl, g.y / gl);
+                    add64(&o[7], O_FIX);
+                    add64(&o[8], O_FIX * nrm.x);
+                    add64(&o[9], O_FIX * nrm.y);
+                    add64(&o[10], O_FIX * d.x);
+                    add64(&o[11], O_FIX * d.y);
+                    add64(&o[12], O_FIX * d.x * d.x);
+                    add64(&o[13], O_FIX * d.y * d.y);
+                    add64(&o[14], O_FIX * d.x * d.y);
+                }
+            }
+        }
+    float clump = REST_PHI + maxf(P_.corr[1], 0.05f);
+#pragma omp parallel for schedule(static)
+    for (int cy = 0; cy < H; cy++)
+        for (int cx = 0; cx < W; cx++) {
+            int i = cy * W + cx;
+            int l = s->rl[i].x;
+            V4 q = s->vel[i];
+            int changed = 0, cl = s->cell[i].x > clump;
+            V3f u;
+            if (l >= 0 && cx > 0 && s->rl[i - 1].x == l && face_live(q.z) && s->rl[l].y >= 0 &&
+                body_motion(s, s->rl[l].y, l, v2((float)cx, (float)cy + 0.5f), &u)) {
+                q.x = u.x;
+                if (!cl && s->cell[i - 1].x <= clump) q.z = 0.0f;
+                changed = 1;
+            }
+            if (l >= 0 && cy > 0 && s->rl[i - W].x == l && face_live(q.w) && s->rl[l].y >= 0 &&
+                body_motion(s, s->rl[l].y, l, v2((float)cx + 0.5f, (float)cy), &u)) {
+                q.y = u.y;
+                if (!cl && s->cell[i - W].x <= clump) q.w = 0.0f;
+                changed = 1;
+            }
+            if (changed) s->vel[i] = q;
         }
 }
 
@@ -4422,6 +4669,7 @@ static void substep(OSim* s, int gather) {
         pressure_solve(s, 1);
         k_project_visc(s);
     }
+    if (s->caps & CAP_RIGID) k_rigid(s);   /* mod.rs:2701-2707 */
 }
 
 /* ------------------------------------------------------------------------------------ */
@@ -4451,6 +4699,9 @@ OSim* osim_create(int w, int h, uint32_t capacity, const OSimParams* p) {
     ALLOC(s->gbase, nc);
     ALLOC(s->rh, nc);
     ALLOC(s->magc, nc);
+    ALLOC(s->rl, nc);
+    ALLOC(s->rbody, (size_t)O_MAX_BODIES * 16);
+    for (size_t k = 0; k < nc; k++) s->rl[k] = (I2){-1, -1};
     ALLOC(s->pres, nc); ALLOC(s->p2keep, nc); ALLOC(s->hcell, nc); ALLOC(s->solid, nc);
     ALLOC(s->sdf, (size_t)(w + 1) * (h + 1)); ALLOC(s->region, nc); ALLOC(s->solid_t, nc);
     ALLOC(s->mga, s->lv.total); ALLOC(s->mgd, s->lv.total); ALLOC(s->mgx, s->lv.total);
@@ -4475,7 +4726,7 @@ void osim_destroy(OSim* s) {
                     s->vel0, s->pjump, s->pres, s->p2keep, s->hcell, s->solid, s->sdf, s->region,
                     s->solid_t, s->mga, s->mgd, s->mgx, s->mgz, s->mgr, s->cgp, s->cgp2, s->cgq,
                     s->ptile, s->part, s->vr, s->vr2, s->vp, s->vq, s->vq2, s->vd, s->vaz, s->vma,
-                    s->vmb, s->vmd, s->vmr, s->vmx, s->vmz, s->tiles, s->vtile, s->pending, s->mixb, s->gbase, s->rh, s->famocc, s->dsettle, s->magc, s->pstress, s->estr};
+                    s->vmb, s->vmd, s->vmr, s->vmx, s->vmz, s->tiles, s->vtile, s->pending, s->mixb, s->gbase, s->rh, s->famocc, s->dsettle, s->magc, s->pstress, s->estr, s->rl, s->rbody};
     for (size_t k = 0; k < sizeof ptrs / sizeof ptrs[0]; k++) free(ptrs[k]);
     free(s);
 }
@@ -4591,7 +4842,7 @@ static int set_tank(OSim* s, const int* present, int thermal) {
     s->thermal = thermal;
     s->caps = compute_caps(s);
     int rc = 0;
-    if (s->caps & (CAP_RIGID | CAP_STEAM | CAP_REACT)) rc = -4;
+    if (s->caps & (CAP_STEAM | CAP_REACT)) rc = -4;
     for (int k = 0; k < nrows; k++) {
         const OMat* m = &p->mat[rows[k]];
         if (m->volatility > 0.0f || (thermal && m->boil < 1e8f)) rc = -4;
@@ -4785,6 +5036,7 @@ long osim_field(const OSim* s, const char* name, void* out, size_t cap) {
     F("rh", s->rh, nc * 16)
     F("magc", s->magc, nc * 8)
     F("estr", s->estr, nc * 16)
+    F("rl", s->rl, nc * 8)
     F("famocc", s->famocc, nc * 4 * (size_t)s->settle_fams)
     F("dsettle", s->dsettle, nc * 8 * (size_t)s->settle_fams)
     F("surf2", s->surf2, nc * 16)

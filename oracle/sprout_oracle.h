@@ -95,6 +95,8 @@ typedef struct OSimParams {
     OMat mat[O_MAX_MATERIALS];
     float magnet_demag;
     float elastic_stress_max, elastic_step_max;
+    uint32_t rigid_contact;
+    float rigid_friction;
 } OSimParams;
 
 /* ToolState (src/sim/params.rs:1141-1213). */

@@ -70,6 +70,9 @@ struct DevScene {
     float4* pstress2; // the same after the particle pass, in the pass's order
     float4* pdep;     // the stress each particle deposits this substep, in the pass's order
     float4* estr;     // per cell: the deposited stress (elastic.comp)
+    int2* rl;         // per cell: rigid label (its body's root cell, -1 not rigid); at a root, its body
+    unsigned long long* rbody;   // per body: 15 fixed-point sums (mass, moments, contacts), 16 apart
+    uint32_t* nbodies;           // bodies labelled in the last rigid pass
     int2* hcell;
     const float4* solid;
     const float* sdf;
@@ -199,6 +202,65 @@ DEV float sp_logf(float x) {
 // x^y as exp(y ln x) with the two functions above (x > 0; 1 for x = 1).
 DEV float sp_powf(float x, float y) { return x == 1.0f ? 1.0f : sp_expf(y * sp_logf(x)); }
 
+constexpr int kMaxBodies = 4096;   // common.glsl: MAX_BODIES
+constexpr float RIGID_FIX = 65536.0f;
+
+// A body sum as the shader reads its two words: (hi as int) 2^32 + lo, over the fixed-point scale.
+DEV float get64(unsigned long long v) {
+    return ((float)(int)(uint32_t)(v >> 32) * 4294967296.0f + (float)(uint32_t)v) / RIGID_FIX;
+}
+
+// Contact of a body with the solids it touches: it neither sinks into its support nor
+// spins through it, and slides on it against friction mu (common.glsl:289-325).
+DEV void body_contact(const unsigned long long* o, float mu, float cmx, float cmy, float& Ux, float& Uy, float& w) {
+    const float nc = get64(o[7]);
+    if (mu < 0.0f || nc < 0.5f) return;
+    const float nsx = get64(o[8]), nsy = get64(o[9]);
+    const float ln = len2(nsx, nsy);
+    if (ln < 0.25f * nc) return;
+    const float nx = nsx / ln, ny = nsy / ln;
+    const float tx = ny, ty = -nx;
+    const float ccx = get64(o[10]) / nc, ccy = get64(o[11]) / nc;
+    const float sqx = get64(o[12]) / nc - ccx * ccx, sqy = get64(o[13]) / nc - ccy * ccy, sqz = get64(o[14]) / nc - ccx * ccy;
+    const float ext = sqrtf(3.0f * maxf(tx * tx * sqx + ty * ty * sqy + 2.0f * tx * ty * sqz, 0.0f)) + 0.5f;
+    const float rcx = ccx - cmx, rcy = ccy - cmy;
+    float ucx = Ux + w * -rcy, ucy = Uy + w * rcx;
+    const float vn = ucx * nx + ucy * ny;
+    const float sp = (cmx - ccx) * tx + (cmy - ccy) * ty;
+    float vn1 = vn, w1 = w;
+    if (fabsf(sp) <= ext) {
+        vn1 = maxf(vn, 0.0f);
+        w1 = clampf(w, -vn1 / ext, vn1 / ext);
+    } else {
+        const float edge = signf(sp) * ext;
+        vn1 = maxf(vn + w * edge, 0.0f) - w * edge;
+    }
+    if (vn1 == vn && w1 == w) return;
+    const float vt = ucx * tx + ucy * ty;
+    const float vt1 = signf(vt) * maxf(fabsf(vt) - mu * (vn1 - vn), 0.0f);
+    ucx = ucx + ((vn1 - vn) * nx + (vt1 - vt) * tx);
+    ucy = ucy + ((vn1 - vn) * ny + (vt1 - vt) * ty);
+    w = w1;
+    Ux = ucx - w1 * -rcy;
+    Uy = ucy - w1 * rcx;
+}
+
+// The rigid motion of body b (root cell r) at x: velocity and spin (common.glsl:327-340).
+DEV bool body_motion(const DevScene& d, int b, int r, float x, float y, float3& u) {
+    const unsigned long long* o = d.rbody + (size_t)b * 16;
+    const float M = get64(o[0]);
+    if (M <= 1e-3f) return false;
+    const float cmx = get64(o[1]) / M, cmy = get64(o[2]) / M;
+    float Ux = get64(o[3]) / M, Uy = get64(o[4]) / M;
+    const float L = get64(o[5]) - M * (cmx * Uy - cmy * Ux);
+    const float I = get64(o[6]) - M * (cmx * cmx + cmy * cmy);
+    float w = I > 1e-3f ? L / I : 0.0f;
+    body_contact(o, d.P->misc[3], cmx, cmy, Ux, Uy, w);
+    const float dx = x - ((float)(r % d.W) + 0.5f) - cmx, dy = y - ((float)(r / d.W) + 0.5f) - cmy;
+    u = make_float3(Ux + w * -dy, Uy + w * dx, w);
+    return true;
+}
+
 // Quadratic B-spline weights (common.glsl:639-643) of a point at offset f from its base node.
 DEV void bspline(float fx, float fy, float wx[3], float wy[3]) {
     wx[0] = 0.5f * (1.5f - fx) * (1.5f - fx);
@@ -262,6 +324,15 @@ DEV float temp_law(const DevMat* mats, int r, float T) {
 }
 
 DEV int group_heat_chan(const DevParams* P, int g) { return (int)((P->group_heat >> (8u * (uint32_t)g)) & 255u) - 1; }
+
+// ln nu of `row` at concentration s and temperature T (common.glsl:631-636; every concentrate
+// here blends with exponent 1).
+DEV float row_lnu(const DevMat* mats, uint32_t row, float s, float T, bool thermal) {
+    float l = mats[row].a[1] + (thermal ? temp_law(mats, (int)row, T) : 0.0f);
+    const int dl = mats[row].ia[1];
+    if (dl >= 0) l = mixf(mats[dl].a[1] + (thermal ? temp_law(mats, dl, T) : 0.0f), l, s);
+    return l;
+}
 
 DEV int2 heat_quanta(float C, float T) {
     int ci = (int)floorf(C * MASS_SCALE + 0.5f);

@@ -943,6 +943,182 @@ __global__ void __launch_bounds__(256) k_magnet_force(DevScene d) {
     d.vel[i] = me;
 }
 
+// ---- rigid bodies (rigid.comp) ---------------------------------------------------------
+// Whether liquid cell i moves rigidly: frozen, stiff, or a non-Newtonian liquid that has not
+// yielded or has jammed (rigid.comp:10-25).
+DEV bool cell_rigid(const DevScene& d, int cx, int cy, int i) {
+    const float4 me = d.cell[i];
+    if (me.w <= 0.0f) return false;
+    const DevParams* P = d.P;
+    if ((P->caps & CAP_THERMAL) != 0u && d.therm[i].w > 0.5f) return true;
+    const float4 q = d.rh[i];
+    if (q.w > 0.5f) return true;
+    if ((P->caps & CAP_RHEO) == 0u || q.x <= 0.0f || cx < 1 || cy < 1 || cx >= d.W - 1 || cy >= d.H - 1) return false;
+    const float g = shear_rate(d, i, false);
+    float F, tau;
+    nn_eval(d, i, q, g, F, tau);
+    if (tau > 0.0f && me.z * g < tau) return true;
+    return d.mats[(int)q.y].ib[1] == 3 && me.z * F >= me.y * sp_expf(P->heat2[0]);
+}
+
+DEV float rigid_sdf(const DevScene& d, float x, float y, float& gx_out, float& gy_out) {
+    const float gx = clampf(x, 0.0f, (float)d.W - 0.001f), gy = clampf(y, 0.0f, (float)d.H - 0.001f);
+    const int ix = (int)gx, iy = (int)gy;
+    const float fx = gx - (float)ix, fy = gy - (float)iy;
+    const int w1 = d.W + 1, k = iy * w1 + ix;
+    const float d00 = d.sdf[k], d10 = d.sdf[k + 1], d01 = d.sdf[k + w1], d11 = d.sdf[k + w1 + 1];
+    gx_out = mixf(d10 - d00, d11 - d01, fy);
+    gy_out = mixf(d01 - d00, d11 - d10, fx);
+    return mixf(mixf(d00, d10, fx), mixf(d01, d11, fx), fy);
+}
+
+DEV int rl_root(const DevScene& d, int i) {
+    int l = d.rl[i].x;
+    for (int guard = 0; guard < (1 << 20) && l != i; guard++) {
+        i = l;
+        l = d.rl[i].x;
+    }
+    return i;
+}
+
+// mode 0: label each rigid cell with itself
+__global__ void __launch_bounds__(256) k_rigid_label(DevScene d) {
+    CELL_XY;
+    if (cx >= W || cy >= H) return;
+    const int i = cy * W + cx;
+    d.rl[i] = make_int2(cell_rigid(d, cx, cy, i) ? i : -1, -1);
+    if (i == 0) *d.nbodies = 0u;
+}
+
+// mode 1: join rigid neighbours (left, below, and the two below diagonals); each link takes
+// the smaller root, so every body ends with its smallest cell as root whatever the order
+__global__ void __launch_bounds__(256) k_rigid_unite(DevScene d) {
+    CELL_XY;
+    if (cx >= W || cy >= H) return;
+    const int i = cy * W + cx;
+    if (d.rl[i].x < 0) return;
+    const int nb[4] = {cx > 0 ? i - 1 : -1, cy > 0 ? i - W : -1, (cy > 0 && cx > 0) ? i - W - 1 : -1,
+                       (cy > 0 && cx < W - 1) ? i - W + 1 : -1};
+    for (int q = 0; q < 4; q++) {
+        if (nb[q] < 0 || d.rl[nb[q]].x < 0) continue;
+        int a = i, b = nb[q];
+        bool done = false;
+        for (int guard = 0; guard < 4096 && !done; guard++) {
+            a = rl_root(d, a);
+            b = rl_root(d, b);
+            if (a < b) {
+                const int old = atomicMin(&d.rl[b].x, a);
+                done = old == b;
+                b = old;
+            } else if (b < a) {
+                const int old = atomicMin(&d.rl[a].x, b);
+                done = old == a;
+                a = old;
+            } else {
+                done = true;
+            }
+        }
+    }
+}
+
+// mode 2: every cell points at its root; each root takes a body
+__global__ void __launch_bounds__(256) k_rigid_bodies(DevScene d) {
+    CELL_XY;
+    if (cx >= W || cy >= H) return;
+    const int i = cy * W + cx;
+    if (d.rl[i].x < 0) return;
+    const int r = rl_root(d, i);
+    d.rl[i].x = r;
+    if (r == i) {
+        const uint32_t b = atomicAdd(d.nbodies, 1u);
+        if (b < (uint32_t)kMaxBodies) {
+            for (int k = 0; k < 16; k++) d.rbody[(size_t)b * 16 + k] = 0ull;
+            d.rl[i].y = (int)b;
+        }
+    }
+}
+
+DEV void add64(unsigned long long* w, float x) {
+    x = floorf(x + 0.5f);
+    atomicAdd(w, (unsigned long long)(long long)x);
+}
+
+// mode 3: each body's mass, moments and contacts with the solids, in 64-bit fixed point
+__global__ void __launch_bounds__(256) k_rigid_sums(DevScene d) {
+    CELL_XY;
+    if (cx >= W || cy >= H) return;
+    const int i = cy * W + cx;
+    const int l = d.rl[i].x;
+    if (l < 0) return;
+    const int b = d.rl[l].y;
+    if (b < 0) return;
+    unsigned long long* o = d.rbody + (size_t)b * 16;
+    const float m = d.cell[i].y * minf(d.cell[i].x, 1.0f) * RIGID_FIX;
+    const float dx = (float)(cx - l % W), dy = (float)(cy - l / W);
+    const float4 q = d.vel[i];
+    const float ur = cx < W - 1 ? d.vel[i + 1].x : 0.0f, ut = cy < H - 1 ? d.vel[i + W].y : 0.0f;
+    const float ux = 0.5f * (q.x + ur), uy = 0.5f * (q.y + ut);
+    add64(&o[0], m);
+    add64(&o[1], m * dx);
+    add64(&o[2], m * dy);
+    add64(&o[3], m * ux);
+    add64(&o[4], m * uy);
+    add64(&o[5], m * (dx * uy - dy * ux));
+    add64(&o[6], m * ((dx * dx + dy * dy) + 1.0f / 6.0f));
+    if (d.P->misc[3] >= 0.0f) {
+        float gx, gy;
+        const float dist = rigid_sdf(d, (float)cx + 0.5f, (float)cy + 0.5f, gx, gy);
+        if (dist < 1.0f && gx * gx + gy * gy > 1e-8f) {
+            const float gl = len2(gx, gy);
+            const float nx = gx / gl, ny = gy / gl;
+            add64(&o[7], RIGID_FIX);
+            add64(&o[8], RIGID_FIX * nx);
+            add64(&o[9], RIGID_FIX * ny);
+            add64(&o[10], RIGID_FIX * dx);
+            add64(&o[11], RIGID_FIX * dy);
+            add64(&o[12], RIGID_FIX * dx * dx);
+            add64(&o[13], RIGID_FIX * dy * dy);
+            add64(&o[14], RIGID_FIX * dx * dy);
+        }
+    }
+}
+
+// mode 4: the faces inside a body move with it
+__global__ void __launch_bounds__(256) k_rigid_faces(DevScene d) {
+    CELL_XY;
+    if (cx >= W || cy >= H) return;
+    const int i = cy * W + cx;
+    const int l = d.rl[i].x;
+    float4 q = d.vel[i];
+    bool changed = false;
+    const float clump = REST_PHI + maxf(d.P->corr[1], 0.05f);
+    const bool cl = d.cell[i].x > clump;
+    float3 u;
+    if (l >= 0 && cx > 0 && d.rl[i - 1].x == l && face_live(q.z) && d.rl[l].y >= 0 &&
+        body_motion(d, d.rl[l].y, l, (float)cx, (float)cy + 0.5f, u)) {
+        q.x = u.x;
+        if (!cl && d.cell[i - 1].x <= clump) q.z = 0.0f;
+        changed = true;
+    }
+    if (l >= 0 && cy > 0 && d.rl[i - W].x == l && face_live(q.w) && d.rl[l].y >= 0 &&
+        body_motion(d, d.rl[l].y, l, (float)cx + 0.5f, (float)cy, u)) {
+        q.y = u.y;
+        if (!cl && d.cell[i - W].x <= clump) q.w = 0.0f;
+        changed = true;
+    }
+    if (changed) d.vel[i] = q;
+}
+
+void launch_rigid(const DevScene& d, cudaStream_t st) {
+    dim3 blk(16, 16);
+    dim3 grd((d.W + 15) / 16, (d.H + 15) / 16);
+    k_rigid_label<<<grd, blk, 0, st>>>(d);
+    k_rigid_unite<<<grd, blk, 0, st>>>(d);
+    k_rigid_bodies<<<grd, blk, 0, st>>>(d);
+    k_rigid_sums<<<grd, blk, 0, st>>>(d);
+    k_rigid_faces<<<grd, blk, 0, st>>>(d);
+}
+
 void launch_grid(const DevScene& d, const LaunchCfg& cfg, cudaStream_t st) {
     dim3 blk(16, 16);
     dim3 grd((d.W + 15) / 16, (d.H + 15) / 16);

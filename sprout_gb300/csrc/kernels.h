@@ -16,6 +16,7 @@ struct LaunchCfg {
     bool rheo = false;        // a non-Newtonian liquid is in the tank: rheo.comp runs
     bool settle = false;      // a family with grains settles: settle.comp runs
     bool elastic = false;     // a viscoelastic liquid: particles carry a stress, elastic.comp runs
+    bool rigid = false;       // liquid can turn rigid: rigid.comp runs
     bool magnet = false;      // a magnet and a susceptible liquid: magnet.comp runs
     bool xtra = false;        // families, several phase groups, settling or currents: the particle pass's full form
     int visc_mode = 0;        // 0 none, 1 explicit, 2 implicit
@@ -42,6 +43,8 @@ void launch_claim(float4* part, uint32_t n_slots, const float4* spawn, uint32_t 
 void launch_cell_counts(const float4* part, uint32_t n_slots, int ox, int oy, int sw, int sh, uint32_t* out,
                         cudaStream_t st);
 void launch_grid(const DevScene& d, const LaunchCfg& cfg, cudaStream_t st);
+// rigid.comp's five modes at the end of a substep (tanks with CAP_RIGID)
+void launch_rigid(const DevScene& d, cudaStream_t st);
 // `second`: the pressure solve after the implicit viscosity (same matrix and hierarchy).
 cudaError_t launch_pressure(const DevScene& d, const LaunchCfg& cfg, cudaStream_t st, int second);
 void launch_project(const DevScene& d, const LaunchCfg& cfg, cudaStream_t st);

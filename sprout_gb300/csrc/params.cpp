@@ -587,7 +587,7 @@ void build_params(const SimParams& p, const Tank& t, bool thermal, uint32_t caps
     P->misc[0] = p.curvature_max;
     P->misc[1] = (float)p.sealed_vent;
     P->misc[2] = p.cell_size;
-    P->misc[3] = -1.0f;
+    P->misc[3] = p.rigid_contact != 0 ? p.rigid_friction : -1.0f;   // mod.rs:2280
     P->n_present = (int)t.rows.size();
     P->acc_stride = std::max(t.stride, 8);
     P->n_fam = t.families;

@@ -309,6 +309,14 @@ __global__ void __launch_bounds__(256) k_advance(DevScene d) {
             // viscoelastic stress (upper-convected Maxwell): a particle that has not run a substep
             // yet starts unstressed; the slot keeps what it held unless the pass updates it
             // (particles.comp:152-156, 250-279)
+            // frozen, or too viscous to flow: part of a rigid body (particles.comp:144-151)
+            const bool rigid_cap = XTRA && (P->caps & CAP_RIGID) != 0u;
+            bool frozen = false;
+            if (rigid_cap) {
+                const float2 ph = thermal ? phase_of(pt, thermal_of(mats, row, ps)) : make_float2(P->heat[0], 0.0f);
+                frozen = ph.y > 0.5f || row_lnu(mats, row, ps, ph.x, thermal) >= P->heat2[0];
+            }
+            bool held = false;
             const bool elastic = XTRA && (P->caps & CAP_ELASTIC) != 0u;
             const float4 held_tau = elastic ? d.pstress[id] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
             float4 tau = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
@@ -322,6 +330,29 @@ __global__ void __launch_bounds__(256) k_advance(DevScene d) {
                 float crowd = 0.0f;
                 gather_face<0>(g, px, py, vx, corrx, C.x, C.y);
                 gather_face<1>(g, px, py, vy, corry, C.z, C.w);
+                if (rigid_cap) {
+                    // a frozen particle, a yield-stress plug's particle in a sparse cell, or any
+                    // particle in a rigid cell moves exactly with the body around it
+                    // (particles.comp:222-248)
+                    const int pcx = clampi((int)px, 0, d.W - 1), pcy = clampi((int)py, 0, d.H - 1);
+                    const bool plug = (mats[row].rheo[0] > 0.0f || mats[row].temp[3] > 0.0f) && d.cell[pcy * d.W + pcx].w <= 0.0f;
+                    const int c0x = clampi((int)px, 1, d.W - 2), c0y = clampi((int)py, 1, d.H - 2);
+                    const bool in_body = row != 57u && d.rl[c0y * d.W + c0x].x >= 0;
+                    if (frozen || plug || in_body) {
+                        const int ox[9] = {0, -1, 1, 0, 0, -1, 1, -1, 1}, oy[9] = {0, 0, 0, -1, 1, -1, -1, 1, 1};
+                        for (int k = 0; k < 9 && !held; k++) {
+                            const int root = d.rl[(c0y + oy[k]) * d.W + c0x + ox[k]].x;
+                            if (root < 0 || d.rl[root].y < 0) continue;
+                            float3 u;
+                            if (body_motion(d, d.rl[root].y, root, px, py, u)) {
+                                vx = u.x;
+                                vy = u.y;
+                                C = make_float4(0.0f, -u.z, u.z, 0.0f);
+                                held = true;
+                            }
+                        }
+                    }
+                }
                 if (elastic) {
                     const float G = mats[row].el[0];
                     if (G > 0.0f) {
@@ -474,9 +505,9 @@ __global__ void __launch_bounds__(256) k_advance(DevScene d) {
                         const int gnow = mats[row].ia[0];   // the group of the row as settling left it
                         const float fg = gnow == 0 ? 1.0f - sgx - sgy - sgz : (gnow == 1 ? sgx : gnow == 2 ? sgy : sgz);
                         const float others = 1.0f - fg;
-                        if (others > 1e-4f && groups)
+                        if (others > 1e-4f && groups && !held)
                             slip = group_drift(d, mats, row, ps, gnow, px, py, bx, by, wx, wy, sw, fg, others, sgx, sgy, sgz, dt);
-                        if (sorts) {
+                        if (sorts && !held) {
                             // drift within the particle's own group against its local mean base
                             // density (particles.comp:478-502)
                             const float fgi = groups ? (gnow == 1 ? sgx : gnow == 2 ? sgy : sgz) : 1.0f;
@@ -538,6 +569,10 @@ __global__ void __launch_bounds__(256) k_advance(DevScene d) {
                             }
                         }
                     }
+                }
+                if (held && crowd <= REST_PHI + maxf(P->corr[1], 0.05f)) {   // particles.comp:576
+                    corrx = 0.0f;
+                    corry = 0.0f;
                 }
                 // drains: a zone with a negative rate removes each particle in it with probability
                 // -rate (1 - 0.75 r^2) dt per substep (particles.comp:577-594)
@@ -613,7 +648,7 @@ __global__ void __launch_bounds__(256) k_advance(DevScene d) {
                         }
                     }
                     float vax = vx, vay = vy;
-                    if (P->ext[1] >= 2.0f && !pushed) {
+                    if (P->ext[1] >= 2.0f && !pushed && !held) {
                         float xmx = clampf(px + 0.5f * dt * (vx + corrx + 0.0f), 2.01f, (float)d.W - 2.01f);
                         float xmy = clampf(py + 0.5f * dt * (vy + corry + slip), 2.01f, (float)d.H - 2.01f);
                         float2 here = sample_vel(g, px, py, make_float2(vx, vy));

@@ -265,7 +265,7 @@ struct SproutSim {
         A(d.scan_tmp, (nc + 1 + 1023) / 1024 + 1);
         A(d.acc, nc * 32);
         A(d.vel, nc); A(d.cell, nc); A(d.comp, nc); A(d.coef, nc); A(d.sprop, nc); A(d.surf, nc);
-        A(d.surf2, nc); A(d.aux, nc); A(d.grho, nc); A(d.gbase, nc); A(d.rh, nc); A(d.magc, nc); A(d.therm, nc); A(d.dheat, nc); A(d.vw, nc);
+        A(d.surf2, nc); A(d.aux, nc); A(d.grho, nc); A(d.gbase, nc); A(d.rh, nc); A(d.magc, nc); A(d.rl, nc); A(d.rbody, (size_t)kMaxBodies * 16); A(d.nbodies, 1); A(d.therm, nc); A(d.dheat, nc); A(d.vw, nc);
         A(d.vs, nc); A(d.prhs, nc); A(d.vel0, nc); A(d.pjump, nc); A(d.pres, nc); A(d.p2keep, nc);
         A(d.hcell, nc);
         float4* solid;
@@ -295,6 +295,7 @@ struct SproutSim {
         A(d.pcount, (size_t)kMaxLevels);
         A(d.partials, 2 * (size_t)d.nwg);
 #undef A
+        CUDA_TRY(cudaMemset(d.rl, 0xff, nc * sizeof(int2)));   // no cell rigid before the first rigid pass
         std::vector<float> nt(nc, NO_TEMP);
         CUDA_TRY(cudaMemcpy(solid_t, nt.data(), nc * sizeof(float), cudaMemcpyHostToDevice));
         int mx = pressure_blocks_max(device, pressure_smem(d.lv), false);
@@ -503,6 +504,7 @@ struct SproutSim {
                 launch_pressure(d, cfg, st, 1);
                 launch_second_projection(d, st);
             }
+            if (cfg.rigid) launch_rigid(d, st);   // mod.rs:2701-2707
             break;
         }
     }
@@ -561,7 +563,8 @@ struct SproutSim {
         want.settle = (caps & CAP_SETTLE) != 0u;
         want.magnet = (caps & CAP_MAGNET) != 0u;
         want.elastic = (caps & CAP_ELASTIC) != 0u;
-        want.xtra = tank.families > 0 || (tank.group_mask & ~1u) != 0u || !currents.empty() || tank.chan_e >= 0;
+        want.rigid = (caps & CAP_RIGID) != 0u;
+        want.xtra = tank.families > 0 || (tank.group_mask & ~1u) != 0u || !currents.empty() || tank.chan_e >= 0 || (caps & CAP_RIGID) != 0u;
         want.visc_mode = visc_mode;
         want.twice = visc_mode == 2 && params.viscous_projection != 0;
         want.viscous_warm = params.viscous_warm != 0;
@@ -574,7 +577,7 @@ struct SproutSim {
             if (v > 0) want.visc_blocks = std::max(1, std::min(v, visc_max[want.visc_sweeps - 1]));
         }
         want.mixed = mixed;
-        bool same = want.n_slots == cfg.n_slots && want.thermal == cfg.thermal && want.heat == cfg.heat && want.rheo == cfg.rheo && want.settle == cfg.settle && want.magnet == cfg.magnet && want.elastic == cfg.elastic && want.xtra == cfg.xtra &&
+        bool same = want.n_slots == cfg.n_slots && want.thermal == cfg.thermal && want.heat == cfg.heat && want.rheo == cfg.rheo && want.settle == cfg.settle && want.magnet == cfg.magnet && want.elastic == cfg.elastic && want.rigid == cfg.rigid && want.xtra == cfg.xtra &&
                     want.visc_mode == cfg.visc_mode && want.twice == cfg.twice && want.viscous_warm == cfg.viscous_warm &&
                     want.visc_levels == cfg.visc_levels && want.visc_sweeps == cfg.visc_sweeps &&
                     want.visc_blocks == cfg.visc_blocks && want.mixed == cfg.mixed && d.stride == std::max(tank.stride, 8);
@@ -671,8 +674,8 @@ struct SproutSim {
         thermal = th;
         caps = compute_caps();
         int rc = SPROUT_OK;
-        if (caps & (CAP_RIGID | CAP_STEAM | CAP_REACT))
-            rc = fail(SPROUT_E_UNSUPPORTED, "the tank needs rigid / steam / reaction passes, which this engine does not carry");
+        if (caps & (CAP_STEAM | CAP_REACT))
+            rc = fail(SPROUT_E_UNSUPPORTED, "the tank needs steam / reaction passes, which this engine does not carry");
         for (int r : tank.rows) {
             const MatProps& m = params.mat[r];
             if (rc == SPROUT_OK && (m.volatility > 0.0f || (thermal && m.boil < 1e8f)))
@@ -1266,6 +1269,8 @@ struct SproutBatch {
             for (size_t s = 0; s < second.members.size(); s++) launch_second_projection(second.members[s]->d, workers[s % kWorkers]);
             join(k);
         }
+        for (SproutSim* sim : ms)
+            if (sim->cfg.rigid) launch_rigid(sim->d, main);
     }
 
     std::vector<SproutSim*> graph_members;   // the tanks the captured graph steps
@@ -1739,6 +1744,7 @@ int sprout_sim_download_field(SproutSim* sim, const char* name, void* out, size_
     else if (n == "rh") { src = d.rh; b = nc * 16; }
     else if (n == "magc") { src = d.magc; b = nc * 8; }
     else if (d.estr && n == "estr") { src = d.estr; b = nc * 16; }
+    else if (n == "rl") { src = d.rl; b = nc * 8; }
     else if (d.famocc && n == "famocc") { src = d.famocc; b = nc * 4 * (size_t)sim->settle_fams; }
     else if (d.dsettle && n == "dsettle") { src = d.dsettle; b = nc * 8 * (size_t)sim->settle_fams; }
     else if (n == "surf2") { src = d.surf2; b = nc * 16; }

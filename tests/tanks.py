@@ -155,3 +155,12 @@ def elastic_drop(w: int = 96, h: int = 64, cell: float = 0.002, mat: int = 12) -
     fills = [([0.0, 0.0, float(w), float(int(0.25 * h))], 0, None),
              ([float(int(0.35 * w)), float(int(0.45 * h)), float(int(0.65 * w)), float(int(0.7 * h))], mat, None)]
     return Tank(w, h, s, [], fills)
+
+
+def yield_stress(w: int = 96, h: int = 64, cell: float = 0.002, mat: int = 5) -> Tank:
+    """A dam break of a yield-stress built-in (molten chocolate, 5, or clay slip, 6): where
+    its stress stays below the yield stress it moves as rigid bodies (rigid.comp)."""
+    key = {5: "chocolate", 6: "clay"}[mat]
+    s = {"cell_size": cell, "fixed_hz": 240.0, "pressure_tol": 1e-5, "viscosity_tol": 1e-5, f"tension_{key}": 0.0}
+    fills = [([0.0, 0.0, float(int(0.4 * w)), float(int(0.6 * h))], mat, None)]
+    return Tank(w, h, s, [], fills)

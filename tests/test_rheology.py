@@ -54,10 +54,11 @@ def test_shear_thinning_viscosity(mat):
     assert np.all(rh[mine, 1] == mat)
 
 
-def test_yield_stress_liquids_stay_refused():
-    """Herschel-Bulkley (chocolate) needs the rigid-body pass: the oracle refuses the tank."""
+def test_reacting_liquids_stay_refused():
+    """Part A and Part B react (the reactions pass is not carried): the oracle refuses the tank,
+    as the engine does."""
     t = tanks.shear_thinning(mat=7)
-    t.fills = [(t.fills[0][0], 5, None)]
-    t.settings.pop("tension_blood", None)
+    t.fills = [(t.fills[0][0], 52, None), (t.fills[1][0], 53, None)]
+    t.settings = {k: v for k, v in t.settings.items() if not k.startswith("tension_")}
     with pytest.raises(RuntimeError):
         tanks.oracle_of(t)
