@@ -164,3 +164,11 @@ def yield_stress(w: int = 96, h: int = 64, cell: float = 0.002, mat: int = 5) ->
     s = {"cell_size": cell, "fixed_hz": 240.0, "pressure_tol": 1e-5, "viscosity_tol": 1e-5, f"tension_{key}": 0.0}
     fills = [([0.0, 0.0, float(int(0.4 * w)), float(int(0.6 * h))], mat, None)]
     return Tank(w, h, s, [], fills)
+
+
+def cooling_lava(w: int = 96, h: int = 64, cell: float = 0.002) -> Tank:
+    """A blob of lava (9) at 760 C, near its solidus, falling through 20 C air onto the floor: it loses heat to
+    the air and the walls and its crust freezes into rigid bodies."""
+    s = {"cell_size": cell, "fixed_hz": 240.0, "pressure_tol": 1e-5, "viscosity_tol": 1e-5, "tension_lava": 0.0}
+    fills = [([float(int(0.3 * w)), float(int(0.2 * h)), float(int(0.6 * w)), float(int(0.5 * h))], 9, 760.0)]
+    return Tank(w, h, s, [], fills)

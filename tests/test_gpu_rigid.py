@@ -35,3 +35,12 @@ def test_rigid_tank_in_a_batch_equals_alone():
     for k, (a, b) in enumerate(zip(alone, batched)):
         problems += compare(a, b, f"tank {k}")
     assert not problems, "\n".join(problems)
+
+
+def test_freezing_lava_bit_exact():
+    """Heat and freezing: the frozen share of the cells (therm.w) makes them rigid, and the
+    frozen particles move with the body."""
+    sim, ora, problems = run_pair(tanks.cooling_lava(), 24)
+    assert not problems, "\n".join(problems[:10])
+    a, b = sim.field("rl", np.int32).reshape(-1, 2), ora.field("rl", np.int32).reshape(-1, 2)
+    assert np.array_equal(a[:, 0], b[:, 0]) and (a[:, 0] >= 0).sum() > 100

@@ -22,3 +22,13 @@ def test_yield_stress_liquid_forms_bodies():
     assert np.all(rl[roots, 0] == roots), "roots point at themselves"
     p = ora.particles()
     assert np.isfinite(p["pos"]).all() and np.isfinite(p["vel"]).all()
+
+
+def test_freezing_lava_becomes_one_body():
+    ora, parts, _ = tanks.oracle_of(tanks.cooling_lava())
+    assert ora.stats().caps & 6 == 6, "heat and rigid bodies"
+    for _ in range(24):
+        ora.step(1, DT)
+    rl = ora.field("rl", np.int32).reshape(-1, 2)
+    rigid = rl[:, 0] >= 0
+    assert rigid.sum() > 100 and len(set(rl[rigid, 0].tolist())) >= 1
