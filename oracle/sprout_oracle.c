@@ -4821,17 +4821,21 @@ static void mark_materials(const OSim* s, const OParticle* q, uint32_t n, int* p
 }
 
 /* The tank for the rows marked in present[] (ascending) and the thermal flag: Tank::layout
- * (mod.rs:271-329), the capabilities and viscosity mode that follow. Changes s only when
- * every check passes; returns -2 (the rows do not fit), -3 (a concentrate without its
- * diluent) or -4 (a capability the oracle does not carry) otherwise. */
-static int set_tank(OSim* s, const int* present, int thermal) {
+ * (mod.rs:271-329), the capabilities and viscosity mode that follow. A concentrate brings
+ * its diluent into the tank's rows (mod.rs:223: the materials "with their diluents"). Changes
+ * s only when every check passes; returns -2 (the rows do not fit) or -4 (a capability the
+ * oracle does not carry) otherwise. */
+static int set_tank(OSim* s, const int* present_in, int thermal) {
     const OSimParams* p = &s->prm;
+    int present[O_MAX_MATERIALS];
+    for (int r = 0; r < O_MAX_MATERIALS; r++) present[r] = present_in[r];
+    for (int r = 0; r < O_MAX_MATERIALS; r++)
+        if (present_in[r] && p->mat[r].diluent >= 0) present[p->mat[r].diluent] = 1;
     int rows[MAX_PRESENT], nrows = 0;
     for (int r = 0; r < O_MAX_MATERIALS; r++)
         if (present[r]) {
             if (nrows == MAX_PRESENT) return -2;
             rows[nrows++] = r;
-            if (p->mat[r].diluent >= 0 && !present[p->mat[r].diluent]) return -3;
         }
     Tank t;
     if (!tank_layout(&t, rows, nrows, p, thermal)) return -2;

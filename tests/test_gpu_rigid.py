@@ -44,3 +44,15 @@ def test_freezing_lava_bit_exact():
     assert not problems, "\n".join(problems[:10])
     a, b = sim.field("rl", np.int32).reshape(-1, 2), ora.field("rl", np.int32).reshape(-1, 2)
     assert np.array_equal(a[:, 0], b[:, 0]) and (a[:, 0] >= 0).sum() > 100
+
+
+def test_clay_combined_capabilities_bit_exact():
+    """Clay slip: a water concentrate (family) with grains (settling), a yield stress
+    (rheology) and unyielded plugs (rigid bodies), all in one tank; its diluent, water, joins
+    the tank's rows though no water particle was placed."""
+    sim, ora, problems = run_pair(tanks.yield_stress(mat=6), 16)
+    assert not problems, "\n".join(problems[:10])
+    st = sim.stats()
+    assert st.caps & (1 | 4 | 8 | 64) == (1 | 4 | 8 | 64)
+    a, b = sim.field("rl", np.int32).reshape(-1, 2), ora.field("rl", np.int32).reshape(-1, 2)
+    assert np.array_equal(a[:, 0], b[:, 0])
