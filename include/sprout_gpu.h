@@ -244,6 +244,40 @@ int sprout_sim_trace_read(SproutSim* sim, unsigned long long* out, size_t cap, s
  * matrices. */
 int sprout_sim_set_precision(SproutSim* sim, int mode);
 
+/* ---- launch shape of the persistent solvers --------------------------------------------
+ * No counterpart in the reference (its dispatch sizes follow from the shaders' 16 x 16 work
+ * groups). The pressure and viscosity solves each run as one persistent kernel; these are
+ * their block counts. 0 = the default: one block per 16 x 16 tile of the grid (a batch: of
+ * its tanks), at most as many as the device holds at once; a larger count is lowered to the
+ * smaller of the two. Results do not
+ * depend on the counts (every block runs the same tile bodies and sums the same partials in
+ * the same order; fewer blocks only take more tiles each). batch_viscosity (batches only):
+ * 0 = the default (the implicit viscosity solves of a batch's tanks in one persistent kernel
+ * when the tanks average at most 1,500 tiles), 1 = always in one kernel, 2 = one solve per
+ * tank. The autotuner (sprout_gb300.tune) picks these per grid size from timed candidates.
+ * Takes effect from the next step. */
+typedef struct SproutLaunch {
+    uint32_t pressure_blocks;        /* the plain FP32 pressure solve */
+    uint32_t pressure_blocks_mixed;  /* the mixed-precision pressure solve */
+    uint32_t viscosity_blocks;       /* the implicit viscosity solve */
+    uint32_t batch_viscosity;        /* batches: 1 batched viscosity solve for small tanks, 0 one per tank */
+    uint32_t reserved[4];            /* zero */
+} SproutLaunch;
+int sprout_sim_set_launch(SproutSim* sim, const SproutLaunch* launch);
+/* The counts in effect for the tank as it is now (after the lowering to what fits). */
+int sprout_sim_get_launch(SproutSim* sim, SproutLaunch* out);
+
+/* ---- failure injection for tests ---------------------------------------------------------
+ * No counterpart in the reference. Makes the persistent solvers' bounded grid-barrier wait
+ * run out on purpose, to test that it ends: block `block` of every later persistent solve of
+ * this sim arrives `stall_ns` nanoseconds late (its wait measured on the device's clock and
+ * capped at one second), and every block gives up waiting after `spin_limit` polls instead of
+ * the default (about a second). The solve then stops with every block returned, the step's
+ * blocking calls report SPROUT_E_TIMEOUT, and later solves of the sim do nothing until a
+ * reset, which clears the error and this setting. stall_ns = 0 and spin_limit = 0 switch it
+ * off. */
+int sprout_sim_debug_stall(SproutSim* sim, uint32_t block, uint32_t stall_ns, uint32_t spin_limit);
+
 /* ---- batches: many tanks, one captured graph per substep -------------------------------
  * The batched and serving layer the reference does not have (it steps one FluidSim). A
  * batch advances its tanks (sims created, filled and reset as usual) together: their
@@ -275,6 +309,10 @@ int sprout_batch_tickets(SproutBatch* b, uint64_t* issued, uint64_t* completed);
 int sprout_batch_sync(SproutBatch* b);
 /* Device ms of `substeps` more substeps of the batch, from CUDA events (blocking). */
 int sprout_batch_profile(SproutBatch* b, uint32_t substeps, float* ms);
+/* The block counts of the batch's persistent solves (SproutLaunch; viscosity_blocks for the
+ * batched viscosity solve, pressure_blocks / pressure_blocks_mixed for the batched pressure
+ * solves), 0 = the default; as for a sim, results do not depend on them. */
+int sprout_batch_set_launch(SproutBatch* b, const SproutLaunch* launch);
 
 /* ---- a pressure solve that allocates nothing ------------------------------------------
  * No counterpart in the reference: an addition for callers that cannot allocate device

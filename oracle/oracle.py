@@ -232,7 +232,43 @@ class OracleSim:
 
     def reset(self, particles: np.ndarray) -> int:
         p = np.ascontiguousarray(particles, PARTICLE_DTYPE)
+        self.sim_time, self.dt_est = 0.0, float(np.float32(1.0) / np.float32(240.0))
         return lib().osim_reset(self.h_, p.ctypes.data, len(p))
+
+    # The host loop of FluidSim::advance_blocking (src/sim/mod.rs:3284-3312) over the oracle,
+    # with the engine's host arithmetic: the substep count and target of each step call, the
+    # simulated time and the CFL estimate read back after it (poll_readbacks).
+    fixed_hz = 0.0
+    sliver = float(np.float32(0.02))   # min_substep_share as a float
+
+    def dt_estimate(self) -> float:
+        if self.fixed_hz > 0.0:
+            return float(np.float32(1.0) / np.float32(self.fixed_hz))
+        return self.dt_est
+
+    def _poll(self):
+        st = self.field("step")
+        advanced, dt_cfl, comp = float(st[1]), float(st[8]), float(st[11:12].view(np.float32)[0])
+        t = advanced - comp
+        if t > self.sim_time:
+            self.sim_time = t
+        if dt_cfl > 0.0:
+            self.dt_est = dt_cfl
+
+    def advance_blocking(self, seconds: float):
+        goal = self.sim_time + seconds
+        for _ in range(1000000):
+            left = goal - self.sim_time
+            dt = self.dt_estimate()
+            if left <= self.sliver * dt:
+                break
+            nn = max(round(left / dt), 1.0) if self.fixed_hz > 0.0 else float(np.ceil(left / dt))
+            n = int(min(max(nn, 1.0), 16.0))
+            target = n * dt if self.fixed_hz > 0.0 else left
+            self.step(n, float(np.float32(target)))
+            self._poll()
+            if self.fixed_hz > 0.0 and (goal - self.sim_time) < 0.5 * dt:
+                break
 
     def set_magnets(self, magnets):
         from sprout_gb300 import magnet_array
@@ -381,7 +417,11 @@ def build_tank(tank, threads: int | None = None):
         if t is not None:
             parts["t"][before:] = t
             parts["kind"][before:] |= 0x20000
+    if getattr(tank, "prepare", None) is not None:
+        parts = tank.prepare(parts)
     sim = OracleSim(tank.w, tank.h, len(parts) + tank.capacity_extra, p)
+    sim.fixed_hz = float(p.fixed_hz)
+    sim.sliver = float(max(np.float32(tank.settings.get("min_substep_share", 0.02)), np.float32(1e-6)))
     if getattr(tank, "currents", None):
         sim.set_currents(tank.currents)
     if getattr(tank, "magnets", None):

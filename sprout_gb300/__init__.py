@@ -43,7 +43,8 @@ EXPORTS = [
     "sprout_batch_create", "sprout_batch_destroy", "sprout_batch_add", "sprout_batch_remove", "sprout_batch_size",
     "sprout_batch_set_precision", "sprout_batch_step", "sprout_batch_sync", "sprout_batch_profile",
     "sprout_batch_step_subset", "sprout_batch_tickets", "sprout_device_memory", "sprout_sim_trace_enable",
-    "sprout_sim_trace_read", "sprout_sim_spawn", "sprout_sim_cell_counts",
+    "sprout_sim_trace_read", "sprout_sim_spawn", "sprout_sim_cell_counts", "sprout_sim_set_launch",
+    "sprout_sim_get_launch", "sprout_sim_debug_stall", "sprout_batch_set_launch",
 ]
 
 STAGES = ["advance", "sort", "p2g", "grid", "pressure", "project", "viscosity", "project2"]
@@ -85,6 +86,16 @@ class SolverStats(C.Structure):
         ("viscosity_iters", C.c_uint32), ("viscosity_residual", C.c_float), ("pressure2_iters", C.c_uint32),
         ("pressure_true_residual", C.c_float), ("pressure_true_residual_max", C.c_float),
     ]
+
+
+class Launch(C.Structure):
+    """SproutLaunch: block counts of the persistent solvers (0: the default)."""
+    _fields_ = [("pressure_blocks", C.c_uint32), ("pressure_blocks_mixed", C.c_uint32),
+                ("viscosity_blocks", C.c_uint32), ("batch_viscosity", C.c_uint32), ("reserved", C.c_uint32 * 4)]
+
+    def as_dict(self) -> dict:
+        return {k: int(getattr(self, k)) for k in ("pressure_blocks", "pressure_blocks_mixed", "viscosity_blocks",
+                                                   "batch_viscosity")}
 
 
 _lib = None
@@ -149,6 +160,10 @@ def lib() -> C.CDLL:
         "sprout_device_memory": ([P(C.c_size_t), P(C.c_size_t)], C.c_int),
         "sprout_sim_trace_enable": ([V, C.c_uint32], C.c_int),
         "sprout_sim_trace_read": ([V, V, C.c_size_t, P(C.c_size_t), P(C.c_uint32)], C.c_int),
+        "sprout_sim_set_launch": ([V, P(Launch)], C.c_int),
+        "sprout_sim_get_launch": ([V, P(Launch)], C.c_int),
+        "sprout_sim_debug_stall": ([V, C.c_uint32, C.c_uint32, C.c_uint32], C.c_int),
+        "sprout_batch_set_launch": ([V, P(Launch)], C.c_int),
         "sprout_pressure_solve_static": ([C.c_uint32, C.c_uint32, V, V, V, V, C.c_float, C.c_float, C.c_uint32, V,
                                           P(C.c_uint32), P(C.c_float)], C.c_int),
     }
@@ -430,6 +445,23 @@ class FluidSim:
         _check(lib().sprout_sim_device_bytes(self._h, C.byref(b)))
         return b.value
 
+    def set_launch(self, pressure_blocks: int = 0, pressure_blocks_mixed: int = 0, viscosity_blocks: int = 0):
+        """Block counts of the persistent pressure and viscosity solves (0: the default, one
+        block per tile up to what the device holds). Results do not depend on them."""
+        lc = Launch(pressure_blocks, pressure_blocks_mixed, viscosity_blocks, 0)
+        _check(lib().sprout_sim_set_launch(self._h, C.byref(lc)))
+
+    def launch(self) -> dict:
+        """The block counts in effect."""
+        lc = Launch()
+        _check(lib().sprout_sim_get_launch(self._h, C.byref(lc)))
+        return lc.as_dict()
+
+    def debug_stall(self, block: int, stall_ns: int, spin_limit: int):
+        """Failure injection for tests: block `block` of later persistent solves arrives
+        stall_ns late at each grid barrier and waits give up after spin_limit polls."""
+        _check(lib().sprout_sim_debug_stall(self._h, block, stall_ns, spin_limit))
+
 
 def pressure_solve_static(w: int, h: int, mga_ptr: int, mgd_ptr: int, rhs_ptr: int, x_ptr: int, tol_p: float,
                           tol_psi: float, max_iters: int = 60, stream: int | None = None):
@@ -494,6 +526,13 @@ class Batch:
         ms = C.c_float()
         _check(lib().sprout_batch_profile(self._h, substeps, C.byref(ms)))
         return ms.value
+
+    def set_launch(self, pressure_blocks: int = 0, pressure_blocks_mixed: int = 0, viscosity_blocks: int = 0,
+                   batch_viscosity: int = 0):
+        """Block counts of the batch's persistent solves (0: defaults); batch_viscosity 0 the
+        default, 1 always one batched viscosity solve, 2 one solve per tank."""
+        lc = Launch(pressure_blocks, pressure_blocks_mixed, viscosity_blocks, batch_viscosity)
+        _check(lib().sprout_batch_set_launch(self._h, C.byref(lc)))
 
 
 def device_memory():

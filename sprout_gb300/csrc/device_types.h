@@ -19,6 +19,7 @@ constexpr int kMaxCurrents = 16;   // params.rs: MAX_CURRENTS
 constexpr int kMaxMagnets = 8;     // params.rs: MAX_MAGNETS
 constexpr int kGroups = 4;
 constexpr int kMaxLevels = 24;
+constexpr int kMaxDevices = 64;   // devices per process the library keeps per-device state for
 
 constexpr uint32_t CAP_FAMILIES = 1u, CAP_THERMAL = 2u, CAP_RIGID = 4u, CAP_RHEO = 8u, CAP_MAGNET = 16u,
                    CAP_ELASTIC = 32u, CAP_SETTLE = 64u, CAP_STEAM = 128u, CAP_REACT = 256u;
@@ -125,7 +126,13 @@ struct SolveState {
     uint32_t trace_rows, trace_cols;
     uint32_t trace_base;   // barriers of the earlier launches (rows of later ones follow on)
     uint32_t pad2;
+    // failure injection for tests (0: off): block dbg_block arrives dbg_stall_ns late at every
+    // grid barrier, and a wait gives up after dbg_spin_limit polls instead of SPIN_LIMIT
+    uint32_t dbg_block, dbg_stall_ns, dbg_spin_limit, pad3;
 };
+// SolveState::error bits: a bounded wait ran out; a solve's residual or right-hand side was
+// not finite (the solve stopped)
+constexpr uint32_t ERR_TIMEOUT = 1u, ERR_DIVERGED = 2u;
 
 // The multigrid hierarchy (Levels, src/sim/mod.rs:714-753).
 struct Levels {
@@ -139,12 +146,51 @@ struct Levels {
     uint32_t wm[kMaxLevels] = {}, tm[kMaxLevels] = {};
 };
 
-inline uint32_t div_magic(int d) { return (uint32_t)(((1ull << 32) + (unsigned long long)d - 1ull) / (unsigned long long)d); }
-inline void set_magics(Levels& L) {
+constexpr uint32_t div_magic(int d) { return (uint32_t)(((1ull << 32) + (unsigned long long)d - 1ull) / (unsigned long long)d); }
+constexpr void set_magics(Levels& L) {
     for (int l = 0; l < L.n; l++) {
         L.wm[l] = div_magic(L.w[l]);
         L.tm[l] = div_magic((L.w[l] + 15) / 16);
     }
+}
+
+// The hierarchy of a w x h grid (Levels, src/sim/mod.rs:714-753): each level halves the one
+// above, rounding up, until a level has at most 4 cells; the tail (solved by one work group)
+// starts at the first level below the grid with at most 1500 cells. Level l's 16 x 16 tiles
+// are numbered from toff[l], for the levels down to the tail. constexpr, so that a fixed-size
+// array can be sized for the worst grid it accepts.
+constexpr Levels make_levels(int w, int h) {
+    Levels L;
+    L.w[0] = w;
+    L.h[0] = h;
+    L.n = 1;
+    while (L.w[L.n - 1] * L.h[L.n - 1] > 4 && L.n < kMaxLevels) {
+        L.w[L.n] = (L.w[L.n - 1] + 1) / 2;
+        L.h[L.n] = (L.h[L.n - 1] + 1) / 2;
+        L.n++;
+    }
+    int total = 0;
+    for (int l = 0; l < L.n; l++) {
+        L.off[l] = total;
+        total += L.w[l] * L.h[l];
+    }
+    L.total = total;
+    int tail = L.n - 1;
+    for (int l = 1; l < L.n; l++)
+        if (L.w[l] * L.h[l] <= 1500) {
+            tail = l;
+            break;
+        }
+    L.tail = tail < 1 ? 1 : tail;
+    if (L.tail > L.n - 1) L.tail = L.n - 1;
+    int tiles = 0;
+    for (int l = 0; l <= L.tail; l++) {
+        L.toff[l] = tiles;
+        tiles += ((L.w[l] + 15) / 16) * ((L.h[l] + 15) / 16);
+    }
+    L.tiles = tiles;
+    set_magics(L);
+    return L;
 }
 
 }  // namespace sprout

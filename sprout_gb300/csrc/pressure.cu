@@ -141,7 +141,11 @@ template <class T>
 struct Solve {
     T rz[2], alpha[2], beta[2], bb[2], rr[2];
     uint32_t done[2], iters[2];
+    uint32_t bad;   // a total was not finite: the solve stopped (SolveState ERR_DIVERGED)
 };
+
+template <class A4>
+DEV bool finite4(const A4& a) { return isfinite(a.x) && isfinite(a.y) && isfinite(a.z) && isfinite(a.w); }
 
 // ---- setup phases ---------------------------------------------------------------------
 
@@ -1095,6 +1099,9 @@ DEV void scal_start(Solve<T>& K, const A4& a, const A4& b, T tx, T ty, int secon
     K.done[0] = a.z <= tx * tx * b.x ? 1u : 0u;
     K.done[1] = a.w <= ty * ty * b.y ? 1u : 0u;
     if (second) K.done[1] = 1u;
+    // a non-finite right-hand side or residual: no iteration can converge, stop here
+    K.bad = finite4(a) && finite4(b) ? 0u : 1u;
+    if (K.bad) K.done[0] = K.done[1] = 1u;
 }
 
 // mode 1: the step lengths from p.q.
@@ -1126,6 +1133,10 @@ DEV void scal_beta(Solve<T>& K, const A4& a, T tx, T ty) {
     K.rr[1] = mix_was<T>(a.w, K.rr[1], was1);
     K.done[0] = d0;
     K.done[1] = d1;
+    if (!finite4(a)) {
+        K.bad = 1u;
+        K.done[0] = K.done[1] = 1u;
+    }
 }
 
 // mode 3 / 9: the statistics of the finished solve into the scene's SolveState.
@@ -1154,6 +1165,7 @@ DEV void scal_stats(SolveState* G, const Solve<T>& K, int second, double true_re
         if (K.iters[0] > G->p2_it_max) G->p2_it_max = K.iters[0];
         if (K.done[0] == 0u) G->p2_unconv += 1u;
     }
+    if (K.bad) atomicOr(&G->error, ERR_DIVERGED);
     const float rel = K.bb[0] > 0 ? (float)sqrt((double)K.rr[0] / (double)K.bb[0]) : 0.0f;
     G->p_res_max = maxf(G->p_res_max, M::kMixed ? rel : (K.bb[0] > 0 ? sqrtf((float)K.rr[0] / (float)K.bb[0]) : 0.0f));
 }
@@ -1537,11 +1549,12 @@ int blocks_max(int device, size_t smem) {
     int sms = 0, per = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     // Opt in to the dynamic shared memory the largest tank so far needs (static + dynamic
-    // above 48 KB needs it; the attribute belongs to the kernel, shared by every sim).
-    static size_t opted = 0;
-    if (smem > opted) {
+    // above 48 KB needs it). The attribute belongs to the kernel on the current device, so
+    // it is tracked per device.
+    static size_t opted[kMaxDevices] = {};
+    if (device < 0 || device >= kMaxDevices || smem > opted[device]) {
         cudaFuncSetAttribute(k_mgpcg<M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        opted = smem;
+        if (device >= 0 && device < kMaxDevices) opted[device] = smem;
     }
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_mgpcg<M>, NT, smem);
     return sms * per;
@@ -1557,10 +1570,10 @@ template <class M>
 int batch_blocks_max(int device, size_t smem) {
     int sms = 0, per = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-    static size_t opted = 0;
-    if (smem > opted) {
+    static size_t opted[kMaxDevices] = {};
+    if (device < 0 || device >= kMaxDevices || smem > opted[device]) {
         cudaFuncSetAttribute(k_mgpcg_batch<M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        opted = smem;
+        if (device >= 0 && device < kMaxDevices) opted[device] = smem;
     }
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_mgpcg_batch<M>, NT, smem);
     return sms * per;
@@ -1606,12 +1619,33 @@ namespace sprout {
 // holds until the process exits.
 
 constexpr int kStaticMaxCells = 512 * 288;   // the largest grid the array holds (147,456 cells)
-constexpr int kStaticMaxLevels = kMaxLevels;
+constexpr int kStaticMinSide = 16;           // and its narrowest side
 
-// Byte layout of the array for kStaticMaxCells (every level of the hierarchy adds at most a
-// third again: 4/3 n + one cell per level).
-constexpr size_t kStaticTotal = (size_t)kStaticMaxCells * 4 / 3 + 64;
-constexpr size_t kStaticTiles = (size_t)kStaticMaxCells / 256 * 2 + 256;
+// The most any accepted grid (both sides >= 16, at most kStaticMaxCells cells) needs of each
+// part of the array: hierarchy cells, tiles of the levels down to the tail, level-0 tiles.
+// For a given width every count grows with the height, so the tallest grid of each width is
+// the one to check. Long thin grids need the most hierarchy: once a level is one cell high,
+// each further level halves only the width.
+struct StaticNeed {
+    int total, tiles, nwg;
+};
+constexpr StaticNeed static_need() {
+    StaticNeed m{0, 0, 0};
+    for (int w = kStaticMinSide; w <= kStaticMaxCells / kStaticMinSide; w++) {
+        const int h = kStaticMaxCells / w;
+        const Levels L = make_levels(w, h);
+        const int nwg = ((w + 15) / 16) * ((h + 15) / 16);
+        if (L.total > m.total) m.total = L.total;
+        if (L.tiles > m.tiles) m.tiles = L.tiles;
+        if (nwg > m.nwg) m.nwg = nwg;
+    }
+    return m;
+}
+constexpr StaticNeed kStaticNeed = static_need();
+constexpr size_t kStaticTotal = (size_t)kStaticNeed.total;
+constexpr size_t kStaticTiles = (size_t)kStaticNeed.tiles;
+constexpr size_t kStaticNwg = (size_t)kStaticNeed.nwg;
+static_assert(kStaticTotal >= (size_t)kStaticMaxCells * 4 / 3, "the hierarchy holds at least 4/3 of the grid");
 constexpr size_t align256(size_t b) { return (b + 255) / 256 * 256; }
 constexpr size_t kStaticBytes =
     align256(sizeof(DevParams)) + align256(sizeof(StepState)) + align256(sizeof(SolveState)) +
@@ -1619,43 +1653,13 @@ constexpr size_t kStaticBytes =
     align256((size_t)kStaticMaxCells * sizeof(float)) +           // viscous part of the warm start
     align256(kStaticTiles * sizeof(uint32_t)) +                   // tile flags of every level
     align256(kStaticTiles * sizeof(uint32_t)) + align256(kMaxLevels * sizeof(uint32_t)) +   // active-tile lists
-    align256(2 * ((size_t)kStaticMaxCells / 256 + 64) * sizeof(float4)) +   // per-tile partial sums
+    align256(2 * kStaticNwg * sizeof(float4)) +                   // per-tile partial sums
     align256(kStaticTotal * sizeof(float4)) + align256(kStaticTotal * sizeof(float)) +
     3 * align256(kStaticTotal * sizeof(float2)) + 4 * align256((size_t)kStaticMaxCells * sizeof(float2));
 
 static __device__ __align__(256) unsigned char g_solve_scratch[kStaticBytes];
 
 namespace {
-
-Levels static_levels(int w, int h) {
-    Levels L;
-    L.w[0] = w;
-    L.h[0] = h;
-    L.n = 1;
-    while (L.w[L.n - 1] * L.h[L.n - 1] > 4 && L.n < kStaticMaxLevels) {
-        L.w[L.n] = (L.w[L.n - 1] + 1) / 2;
-        L.h[L.n] = (L.h[L.n - 1] + 1) / 2;
-        L.n++;
-    }
-    int total = 0;
-    for (int l = 0; l < L.n; l++) {
-        L.off[l] = total;
-        total += L.w[l] * L.h[l];
-    }
-    L.total = total;
-    int tail = L.n - 1;
-    for (int l = 1; l < L.n; l++)
-        if (L.w[l] * L.h[l] <= 1500) { tail = l; break; }
-    L.tail = tail < 1 ? 1 : (tail > L.n - 1 ? L.n - 1 : tail);
-    int tiles = 0;
-    for (int l = 0; l <= L.tail; l++) {
-        L.toff[l] = tiles;
-        tiles += ((L.w[l] + 15) / 16) * ((L.h[l] + 15) / 16);
-    }
-    L.tiles = tiles;
-    set_magics(L);
-    return L;
-}
 
 // Prepares a solve in the array: the level-0 matrix and right-hand side copied in, every
 // coarse matrix and tile flag cleared (a call starts as the first solve of a fresh tank),
@@ -1668,10 +1672,14 @@ __global__ void k_static_prep(DevScene d, const float4* mga, const float* mgd, c
     for (int i = t0; i < d.lv.total; i += stride) {
         if (i < n0) {
             d.mga[i] = mga[i];
-            d.mgd[i] = mgd[i];
+            const float D = mgd[i];
+            d.mgd[i] = D;
             float2 b = rhs[i];
             d.prhs[i] = make_float4(b.x, b.y, 0.0f, 0.0f);
             d.p2keep[i] = 0.0f;
+            // a cell that is no unknown leaves with zero potentials, also in tiles without
+            // unknowns, which the solve itself never visits
+            if (!(D > 0.0f)) d.pres[i] = make_float2(0.0f, 0.0f);
         } else {
             d.mga[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
             d.mgd[i] = 0.0f;
@@ -1705,7 +1713,7 @@ struct StaticSlot {
     int ready;
     unsigned char* base;
 };
-StaticSlot g_slots[64];
+StaticSlot g_slots[kMaxDevices];
 
 }  // namespace
 
@@ -1721,12 +1729,12 @@ extern "C" int sprout_pressure_solve_static(uint32_t w, uint32_t h, const float*
         sprout_internal_set_error("null argument");
         return -1;
     }
-    if (w < 16 || h < 16 || (size_t)w * h > (size_t)kStaticMaxCells) {
+    if (w < (uint32_t)kStaticMinSide || h < (uint32_t)kStaticMinSide || (size_t)w * h > (size_t)kStaticMaxCells) {
         sprout_internal_set_error("grid outside 16 x 16 .. 147,456 cells, the most the fixed solve array holds");
         return -3;
     }
     int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
         sprout_internal_set_error("no current CUDA device");
         return -6;
     }
@@ -1743,7 +1751,7 @@ extern "C" int sprout_pressure_solve_static(uint32_t w, uint32_t h, const float*
         slot.base = static_cast<unsigned char*>(ptr);
         slot.ready = 1;
     }
-    const Levels L = static_levels((int)w, (int)h);
+    const Levels L = make_levels((int)w, (int)h);
     DevScene d{};
     d.W = (int)w;
     d.H = (int)h;
@@ -1761,7 +1769,7 @@ extern "C" int sprout_pressure_solve_static(uint32_t w, uint32_t h, const float*
     d.ptile = reinterpret_cast<uint32_t*>(take(kStaticTiles * sizeof(uint32_t)));
     d.plist = reinterpret_cast<uint32_t*>(take(kStaticTiles * sizeof(uint32_t)));
     d.pcount = reinterpret_cast<uint32_t*>(take(kMaxLevels * sizeof(uint32_t)));
-    d.partials = reinterpret_cast<float4*>(take(2 * ((size_t)kStaticMaxCells / 256 + 64) * sizeof(float4)));
+    d.partials = reinterpret_cast<float4*>(take(2 * kStaticNwg * sizeof(float4)));
     d.mga = reinterpret_cast<float4*>(take(kStaticTotal * sizeof(float4)));
     d.mgd = reinterpret_cast<float*>(take(kStaticTotal * sizeof(float)));
     d.mgx = reinterpret_cast<float2*>(take(kStaticTotal * sizeof(float2)));
@@ -1772,20 +1780,27 @@ extern "C" int sprout_pressure_solve_static(uint32_t w, uint32_t h, const float*
     d.cgp2 = reinterpret_cast<float2*>(take((size_t)kStaticMaxCells * sizeof(float2)));
     d.cgq = reinterpret_cast<float2*>(take((size_t)kStaticMaxCells * sizeof(float2)));
     d.pres = reinterpret_cast<float2*>(x);
-    if ((size_t)(p - slot.base) > kStaticBytes || (size_t)L.total > kStaticTotal || (size_t)L.tiles > kStaticTiles) {
+    // (every accepted grid fits by construction of kStaticNeed; checked all the same)
+    if ((size_t)(p - slot.base) > kStaticBytes || (size_t)L.total > kStaticTotal || (size_t)L.tiles > kStaticTiles ||
+        (size_t)d.nwg > kStaticNwg) {
         sprout_internal_set_error("fixed solve array layout overflow");
         return -3;
     }
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     k_static_prep<<<128, 256, 0, st>>>(d, reinterpret_cast<const float4*>(mga), mgd, reinterpret_cast<const float2*>(rhs),
                                        tol_p, tol_psi, max_iters);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        sprout_internal_set_error(cudaGetErrorString(e));
+        return -6;
+    }
     const size_t smem = pressure_smem(L);
     int blocks = pressure_blocks_max(dev, smem, false);
     if (blocks > d.nwg) blocks = d.nwg;
     if (blocks < 1) blocks = 1;
     int second = 0, scale_mode = 0;
     void* args[] = {(void*)&d, &second, &scale_mode};
-    cudaError_t e = cudaLaunchCooperativeKernel((const void*)k_mgpcg<Plain>, dim3(blocks), dim3(NT), args, smem, st);
+    e = cudaLaunchCooperativeKernel((const void*)k_mgpcg<Plain>, dim3(blocks), dim3(NT), args, smem, st);
     if (e != cudaSuccess) {
         sprout_internal_set_error(cudaGetErrorString(e));
         return -6;
@@ -1797,6 +1812,10 @@ extern "C" int sprout_pressure_solve_static(uint32_t w, uint32_t h, const float*
         if (e != cudaSuccess) {
             sprout_internal_set_error(cudaGetErrorString(e));
             return -6;
+        }
+        if (K.error & ERR_DIVERGED) {
+            sprout_internal_set_error("the solve met a non-finite right-hand side or residual and stopped");
+            return -4;
         }
         if (K.error) {
             sprout_internal_set_error("a bounded device-side wait ran out (grid barrier of the pressure solve)");

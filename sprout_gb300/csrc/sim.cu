@@ -44,36 +44,6 @@ int fail(int code, const std::string& msg) {
 
 constexpr float kNominalDt = 1.0f / 240.0f;
 
-Levels make_levels(int w, int h) {
-    Levels L;
-    L.w[0] = w;
-    L.h[0] = h;
-    L.n = 1;
-    while (L.w[L.n - 1] * L.h[L.n - 1] > 4) {
-        L.w[L.n] = (L.w[L.n - 1] + 1) / 2;
-        L.h[L.n] = (L.h[L.n - 1] + 1) / 2;
-        L.n++;
-    }
-    int total = 0;
-    for (int l = 0; l < L.n; l++) {
-        L.off[l] = total;
-        total += L.w[l] * L.h[l];
-    }
-    L.total = total;
-    int tail = L.n - 1;
-    for (int l = 1; l < L.n; l++)
-        if (L.w[l] * L.h[l] <= 1500) { tail = l; break; }
-    L.tail = std::min(std::max(tail, 1), L.n - 1);
-    int tiles = 0;
-    for (int l = 0; l <= L.tail; l++) {
-        L.toff[l] = tiles;
-        tiles += ((L.w[l] + 15) / 16) * ((L.h[l] + 15) / 16);
-    }
-    L.tiles = tiles;
-    set_magics(L);
-    return L;
-}
-
 }  // namespace
 
 namespace sprout {
@@ -176,12 +146,8 @@ struct SproutSim {
             A(d.hga, tot); A(d.hgd, tot);
             A(d.partials64, 2 * (size_t)d.nwg);
 #undef A
-            int mx = pressure_blocks_max(device, pressure_smem(d.lv), true);
-            cfg.mg_blocks_mixed = std::max(1, std::min(d.nwg, mx));
-            if (const char* e = std::getenv("SPROUT_MG_BLOCKS")) {
-                int want = std::atoi(e);
-                if (want > 0) cfg.mg_blocks_mixed = std::max(1, std::min(want, mx));
-            }
+            mg_max_mixed = pressure_blocks_max(device, pressure_smem(d.lv), true);
+            cfg.mg_blocks_mixed = pick_blocks(launch_req.pressure_blocks_mixed, mg_max_mixed);
             CUDA_TRY(cudaDeviceSynchronize());
             mixed_alloc = true;
             graph_ok = false;   // new device pointers: the captured substep is stale
@@ -298,15 +264,46 @@ struct SproutSim {
         CUDA_TRY(cudaMemset(d.rl, 0xff, nc * sizeof(int2)));   // no cell rigid before the first rigid pass
         std::vector<float> nt(nc, NO_TEMP);
         CUDA_TRY(cudaMemcpy(solid_t, nt.data(), nc * sizeof(float), cudaMemcpyHostToDevice));
-        int mx = pressure_blocks_max(device, pressure_smem(d.lv), false);
-        cfg.mg_blocks = std::max(1, std::min(d.nwg, mx));
-        // SPROUT_MG_BLOCKS: a tuning override of the persistent kernel's block count
-        // (at most what fits on the device at once).
-        if (const char* e = std::getenv("SPROUT_MG_BLOCKS")) {
-            int want = std::atoi(e);
-            if (want > 0) cfg.mg_blocks = std::max(1, std::min(want, mx));
-        }
+        mg_max = pressure_blocks_max(device, pressure_smem(d.lv), false);
+        cfg.mg_blocks = pick_blocks(launch_req.pressure_blocks, mg_max);
         CUDA_TRY(cudaDeviceSynchronize());
+        return SPROUT_OK;
+    }
+
+    // The persistent solvers' block counts: the caller's request (0: one block per level-0
+    // tile), at most what the device holds at once (mx).
+    SproutLaunch launch_req{};
+    int mg_max = 1, mg_max_mixed = 1;
+    int pick_blocks(uint32_t want, int mx) const {
+        const int b = want != 0u ? (int)std::min<uint32_t>(want, (uint32_t)d.nwg) : d.nwg;
+        return std::max(1, std::min(b, std::max(mx, 1)));
+    }
+    int set_launch(const SproutLaunch& l) {
+        CUDA_TRY(cudaStreamSynchronize(stream));
+        launch_req = l;
+        cfg.mg_blocks = pick_blocks(l.pressure_blocks, mg_max);
+        if (mixed_alloc) cfg.mg_blocks_mixed = pick_blocks(l.pressure_blocks_mixed, mg_max_mixed);
+        graph_ok = false;   // the captured substep launches the old counts
+        return SPROUT_OK;
+    }
+    void get_launch(SproutLaunch* out) const {
+        *out = SproutLaunch{};
+        out->pressure_blocks = (uint32_t)cfg.mg_blocks;
+        out->pressure_blocks_mixed = mixed_alloc ? (uint32_t)cfg.mg_blocks_mixed : 0u;
+        const int sw = (int)std::min(std::max(params.viscosity_mg_sweeps, 1u), 2u);
+        out->viscosity_blocks = visc_alloc ? (uint32_t)pick_blocks(launch_req.viscosity_blocks, visc_max[sw - 1]) : 0u;
+        out->batch_viscosity = launch_req.batch_viscosity;
+    }
+
+    // Failure injection for tests: the fields of SolveState the grid barrier reads.
+    int debug_stall(uint32_t block, uint32_t stall_ns, uint32_t spin_limit) {
+        CUDA_TRY(cudaStreamSynchronize(stream));
+        SolveState K0;
+        CUDA_TRY(cudaMemcpy(&K0, d.K, sizeof K0, cudaMemcpyDeviceToHost));
+        K0.dbg_block = block;
+        K0.dbg_stall_ns = stall_ns;
+        K0.dbg_spin_limit = spin_limit;
+        CUDA_TRY(cudaMemcpy(d.K, &K0, sizeof K0, cudaMemcpyHostToDevice));
         return SPROUT_OK;
     }
 
@@ -570,12 +567,7 @@ struct SproutSim {
         want.viscous_warm = params.viscous_warm != 0;
         want.visc_levels = std::min((int)std::max(params.viscosity_mg_levels, 1u), d.lv.tail);
         want.visc_sweeps = (int)std::min(std::max(params.viscosity_mg_sweeps, 1u), 2u);
-        want.visc_blocks = std::max(1, std::min(d.nwg, visc_max[want.visc_sweeps - 1]));
-        // SPROUT_VISC_BLOCKS: a tuning override of the persistent viscosity kernel's block count
-        if (const char* e = std::getenv("SPROUT_VISC_BLOCKS")) {
-            const int v = std::atoi(e);
-            if (v > 0) want.visc_blocks = std::max(1, std::min(v, visc_max[want.visc_sweeps - 1]));
-        }
+        want.visc_blocks = pick_blocks(launch_req.viscosity_blocks, visc_max[want.visc_sweeps - 1]);
         want.mixed = mixed;
         bool same = want.n_slots == cfg.n_slots && want.thermal == cfg.thermal && want.heat == cfg.heat && want.rheo == cfg.rheo && want.settle == cfg.settle && want.magnet == cfg.magnet && want.elastic == cfg.elastic && want.rigid == cfg.rigid && want.xtra == cfg.xtra &&
                     want.visc_mode == cfg.visc_mode && want.twice == cfg.twice && want.viscous_warm == cfg.viscous_warm &&
@@ -923,7 +915,8 @@ struct SproutSim {
     int check_device_error() {
         uint32_t err = 0;
         CUDA_TRY(cudaMemcpy(&err, &d.K->error, 4, cudaMemcpyDeviceToHost));
-        if (err) return fail(SPROUT_E_TIMEOUT, "a bounded device-side wait ran out (grid barrier of the pressure solve)");
+        if (err & ERR_DIVERGED) return fail(SPROUT_E_DIVERGED, "a solve met a non-finite right-hand side or residual and stopped");
+        if (err) return fail(SPROUT_E_TIMEOUT, "a bounded device-side wait ran out (grid barrier of a persistent solve)");
         return SPROUT_OK;
     }
 
@@ -1042,9 +1035,7 @@ struct SproutBatch {
         vis_ok = false;
         const int ns = second.v.ns;
         if (ns < 2) return SPROUT_OK;
-        // SPROUT_BATCH_VISCOSITY=0: one viscosity solve per tank (for comparison)
-        if (const char* e = std::getenv("SPROUT_BATCH_VISCOSITY"))
-            if (std::atoi(e) == 0) return SPROUT_OK;
+        if (launch_req.batch_viscosity == 2u) return SPROUT_OK;   // asked for one solve per tank
         const int sw = second.members[0]->cfg.visc_sweeps;
         int max_lev = 0, tiles = 0;
         for (const SproutSim* sim : second.members) {
@@ -1056,7 +1047,7 @@ struct SproutBatch {
         // large tanks fill the device one at a time: the batched solve only adds its separate
         // reduction phases (measured: +13 to +44 % for 8-16 tanks of 128 x 72 to 256 x 144,
         // -2.5 % for 4 tanks of 1024 x 576)
-        if (tiles > 1500 * ns) return SPROUT_OK;
+        if (tiles > 1500 * ns && launch_req.batch_viscosity != 1u) return SPROUT_OK;
         if (ns > vis_cap) {
             CUDA_TRY(cudaStreamSynchronize(main));
             if (dvscal) cudaFree(dvscal);
@@ -1071,7 +1062,8 @@ struct SproutBatch {
         }
         vis = VBatchView{second.ds, ns, second.doff, dvscal, second.dk, second.daoff, max_lev};
         vis_sweeps = sw;
-        vis_blocks = std::max(1, std::min(viscosity_blocks_max(device, sw), tiles));
+        const int vmx = viscosity_blocks_max(device, sw);
+        vis_blocks = std::max(1, std::min(vmx, launch_req.viscosity_blocks ? (int)std::min<uint32_t>(launch_req.viscosity_blocks, (uint32_t)tiles) : tiles));
         vis_ok = true;
         return SPROUT_OK;
     }
@@ -1201,7 +1193,19 @@ struct SproutBatch {
         const int mx = pressure_batch_blocks_max(device, smem, mixed);
         int total_tiles = 0;
         for (const SproutSim* sim : members) total_tiles += sim->d.nwg;
-        V.blocks = std::max(1, std::min(mx, std::max(total_tiles, ns)));
+        const uint32_t req = mixed ? launch_req.pressure_blocks_mixed : launch_req.pressure_blocks;
+        const int most = std::max(total_tiles, ns);
+        V.blocks = std::max(1, std::min(mx, req ? (int)std::min<uint32_t>(req, (uint32_t)most) : most));
+        return SPROUT_OK;
+    }
+
+    // The block counts of the batch's persistent solves (0: the defaults above).
+    SproutLaunch launch_req{};
+    int set_launch(const SproutLaunch& l) {
+        CUDA_TRY(cudaStreamSynchronize(main));
+        if (l.batch_viscosity > 2u) return fail(SPROUT_E_ARG, "batch_viscosity is 0 (default), 1 (batched) or 2 (one solve per tank)");
+        launch_req = l;
+        drop_graph();
         return SPROUT_OK;
     }
 
@@ -1604,6 +1608,27 @@ int sprout_sim_trace_read(SproutSim* sim, unsigned long long* out, size_t cap, s
     if (out && sim->trace_buf) CUDA_TRY(cudaMemcpy(out, sim->trace_buf, std::min(*words, cap) * 8, cudaMemcpyDeviceToHost));
     return SPROUT_OK;
 }
+int sprout_sim_set_launch(SproutSim* sim, const SproutLaunch* l) {
+    if (!sim || !l) return fail(SPROUT_E_ARG, "null argument");
+    return sim->set_launch(*l);
+}
+
+int sprout_sim_get_launch(SproutSim* sim, SproutLaunch* out) {
+    if (!sim || !out) return fail(SPROUT_E_ARG, "null argument");
+    sim->get_launch(out);
+    return SPROUT_OK;
+}
+
+int sprout_sim_debug_stall(SproutSim* sim, uint32_t block, uint32_t stall_ns, uint32_t spin_limit) {
+    if (!sim) return fail(SPROUT_E_ARG, "null argument");
+    return sim->debug_stall(block, stall_ns, spin_limit);
+}
+
+int sprout_batch_set_launch(SproutBatch* b, const SproutLaunch* l) {
+    if (!b || !l) return fail(SPROUT_E_ARG, "null argument");
+    return b->set_launch(*l);
+}
+
 int sprout_sim_set_precision(SproutSim* sim, int mode) {
     if (!sim) return fail(SPROUT_E_ARG, "null argument");
     return sim->set_precision(mode);

@@ -71,6 +71,15 @@ DEV bool grid_sync(SolveState* K) {
         if (*verr != 0u) {
             ok = 0;
         } else {
+            // failure injection (tests only, off unless set): this block arrives late, by a
+            // wait bounded by the device clock (at most a second) and by a poll count
+            const uint32_t stall = K->dbg_stall_ns;
+            if (stall != 0u && blockIdx.x == K->dbg_block) {
+                const unsigned long long t0 = global_ns();
+                const unsigned long long lim = stall < 1000000000u ? stall : 1000000000u;
+                for (uint32_t k = 0; k < (1u << 21) && global_ns() - t0 < lim; k++) __nanosleep(500);
+            }
+            const uint32_t spin_limit = K->dbg_spin_limit != 0u ? K->dbg_spin_limit : SPIN_LIMIT;
             const unsigned long long t_in = trace ? global_ns() : 0ull;
             const uint32_t base = trace ? *(volatile uint32_t*)&K->trace_base : 0u;
             // the arrival releases the block's writes (ordered before it by the block barrier
@@ -91,8 +100,8 @@ DEV bool grid_sync(SolveState* K) {
                 asm volatile("ld.acquire.gpu.u32 %0, [%1];" : "=r"(now) : "l"(&K->bar_count) : "memory");
                 if (now >= target) break;
                 if (*verr != 0u) { ok = 0; break; }
-                if (++spins > SPIN_LIMIT) {
-                    if (atomicExch(&K->error, 1u) == 0u) {
+                if (++spins > spin_limit) {
+                    if (atomicOr(&K->error, ERR_TIMEOUT) == 0u) {
                         K->err_arrived = *vcnt - epoch * gridDim.x;
                         K->err_blocks = gridDim.x;
                     }

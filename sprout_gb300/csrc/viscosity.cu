@@ -1075,6 +1075,7 @@ __global__ void __launch_bounds__(NT, 2) k_visc_solve(DevScene d, int restrain) 
         G->v_done = K.done;
         G->v_rr = K.rr;
         G->v_r0 = K.r0;
+        if (!isfinite(K.rr) || !isfinite(K.r0)) atomicOr(&G->error, ERR_DIVERGED);
     }
     trace_launch_done(d.K);
 }
@@ -1346,6 +1347,7 @@ __global__ void __launch_bounds__(NT, 2) k_visc_batch(VBatchView B) {
             G->v_done = K.done;
             G->v_rr = K.rr;
             G->v_r0 = K.r0;
+            if (!isfinite(K.rr) || !isfinite(K.r0)) atomicOr(&G->error, ERR_DIVERGED);
         }
     }
     trace_launch_done(BK);

@@ -23,6 +23,9 @@ class Tank:
     groups: dict = field(default_factory=dict)      # custom row -> its phase group (0-3)
     currents: list = field(default_factory=list)    # dicts: pos, radius, vel, rate (negative: a drain)
     magnets: list = field(default_factory=list)     # dicts: pos, radius, strength (T), dir
+    # applied to the filled particles before the reset (both implementations): a function of
+    # the particle array returning the array to start from (a velocity field, a selection)
+    prepare: object = None
 
     # ---- the engine -----------------------------------------------------------------------
     def engine(self):
@@ -48,6 +51,8 @@ class Tank:
             if t is not None:
                 parts["t"][before:] = t
                 parts["kind"][before:] |= 0x20000   # KIND_REAL_T: a temperature to settle
+        if self.prepare is not None:
+            parts = self.prepare(parts)
         sim = S.FluidSim(self.w, self.h, len(parts) + self.capacity_extra, p)
         if self.currents:
             sim.set_currents(self.currents)
