@@ -72,6 +72,7 @@ def workload(name: str, rank: int):
                 "solver": "plain fp32 MGPCG"}
     else:
         raise SystemExit(f"unknown workload {name}")
+    desc["l2"] = l2_note(t)[1]
     return t, desc
 
 
@@ -251,6 +252,135 @@ def active_viscosity_cells(sim, w: int, h: int) -> int:
     return int(n)
 
 
+def l2_note(tank) -> tuple[bool, str]:
+    """Whether a tank's substep fits in L2 (then each timed substep runs behind a 512 MB write),
+    from the bytes it touches at least: every particle slot read and written (48 B each, 4 per
+    cell at most) and ~400 B of per-cell grid records. The same in both arms' config."""
+    touched = (96 * 4 + 400) * tank.w * tank.h
+    flush = touched <= L2_BYTES
+    return flush, (f"~{touched / 1e6:.0f} MB touched per substep <= L2 (129 MB): a 512 MB write before each "
+                   "timed substep, substeps alone timed" if flush else
+                   f"~{touched / 1e6:.0f} MB touched per substep > L2 (129 MB): no flush")
+
+
+def device_resident(sim, tank, args, pg, local):
+    """ms of `steps` substeps after `warmup`, CUDA events on the sim's stream (max over ranks)."""
+    dt = 1.0 / 240.0
+    for _ in range(args.warmup):
+        sim.step(1, dt)
+    sim.sync()
+    flush, _ = l2_note(tank)
+    barrier(pg)
+    sim.sync()
+    if flush:
+        import torch
+        scratch = torch.empty(512 << 20, dtype=torch.uint8, device=f"cuda:{local}")
+        ms = 0.0
+        for _ in range(args.steps):
+            scratch.fill_(1)
+            torch.cuda.synchronize()
+            ms += sim.profile(1)
+        del scratch
+    else:
+        ms = sim.profile(args.steps)
+    sim.sync()
+    barrier(pg)
+    return allreduce_max(pg, ms)
+
+
+def end_to_end(tank, args, pg):
+    """The same metric through the public API on a fresh copy of the tank, over the same
+    substep indices as the device-resident timing (warmup, then steps): each step call
+    uploads its inputs (the step's batch words, parameters when they change) and reads the
+    step's result back (the solver statistics), all inside the timed region."""
+    sim, _, _ = tank.engine()
+    dt = 1.0 / 240.0
+    for _ in range(args.warmup):
+        sim.step(1, dt)
+    sim.sync()
+    live = sim.stats().n_live
+    h0 = sim.stats()
+    lat = []
+    barrier(pg)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        a = time.perf_counter()
+        sim.step(1, dt)
+        sim.stats()               # the step's result read back to the host (blocking)
+        lat.append(time.perf_counter() - a)
+    el = time.perf_counter() - t0
+    el = allreduce_max(pg, el)
+    h1 = sim.stats()
+    value = allreduce_sum(pg, float(live)) * args.steps / el
+    return {"value": value, "unit": UNIT,
+            "h2d_bytes_per_step": (h1.h2d_bytes - h0.h2d_bytes) / args.steps,
+            # h1's own read is counted in h1 - h0 with the loop's reads, all the same size
+            "d2h_bytes_per_step": (h1.d2h_bytes - h0.d2h_bytes) / (args.steps + 1),
+            "p50_ms": float(np.percentile(lat, 50) * 1e3), "p99_ms": float(np.percentile(lat, 99) * 1e3),
+            "substeps": f"{args.warmup + 1}..{args.warmup + args.steps} of a fresh copy of the tank (as value)"}
+
+
+def run_batched(args, pg, rank: int = 0, world: int = 1) -> dict:
+    """The batched configuration: 64 seeded dam breaks of uneven sizes (128 x 72 .. 1024 x
+    576), one or two liquids each from the full-physics ranges, mixed precision, stepped as
+    one batch (one captured graph per substep, the solves as persistent kernels over the
+    flattened tile lists); then the same tanks in plain FP32. Under torchrun each rank steps
+    its share of the tanks (sprout_gb300.placement), with no exchange on the data path."""
+    import sprout_gb300 as S
+    from sprout_gb300 import placement
+    from sprout_gb300 import workloads as WL
+    t0 = time.perf_counter()
+    tanks = WL.uneven_dam_breaks(args.batch_tanks, seed=0)
+    mine = placement.my_tanks(tanks, rank, world)
+    sims = [tanks[i].engine()[0] for i in mine]
+    b = S.Batch(sims, "mixed")
+    setup = time.perf_counter() - t0
+    out = {"workload": f"{len(tanks)} uneven dam breaks (128x72..1024x576, 1-2 config-3 liquids), seed 0",
+           "setup_s": setup, "placement": f"{len(mine)} of {len(tanks)} tanks on this rank (greedy by cells + particles/4)"}
+    for prec in ("mixed", "plain"):
+        b.set_precision(prec)
+        b.step(args.warmup)
+        b.sync()
+        live = sum(s.stats().n_live for s in sims)
+        barrier(pg)
+        ms = allreduce_max(pg, b.profile(args.steps))
+        sts = [s.stats() for s in sims]
+        out[prec] = {"value": allreduce_sum(pg, float(live)) * args.steps / (ms / 1e3), "unit": UNIT,
+                     "ms_per_step": ms / args.steps, "particles": int(live),
+                     "pressure_unconverged": int(sum(x.pressure_unconverged for x in sts)),
+                     "device_errors": int(sum(1 for x in sts if x.device_error))}
+        if prec == "mixed":
+            out[prec]["pressure_true_residual_max_fp64"] = float(max(x.pressure_true_residual_max for x in sts))
+    out["launch"] = {"batch_blocks": "one per tile of the tanks, at most what fits (2 per SM)"}
+    b.close()
+    # the same tanks on the single-scene path, one after another, plain FP32: each tank's own
+    # captured substep, `steps` substeps each after 2 more warm-up substeps
+    seq_ms = 0.0
+    for s_ in sims:
+        s_.set_precision("plain")
+        s_.step(2, 2 / 240.0)
+        seq_ms += s_.profile(args.steps)
+    live = sum(s_.stats().n_live for s_ in sims)
+    seq_ms = allreduce_max(pg, seq_ms)
+    out["plain_single_scene"] = {"value": allreduce_sum(pg, float(live)) * args.steps / (seq_ms / 1e3), "unit": UNIT,
+                                 "ms_per_step": seq_ms / args.steps,
+                                 "how": "the same tanks stepped one at a time through their own captured substeps, plain FP32"}
+    out["ratio_mixed_batched_vs_plain_single_scene"] = out["mixed"]["value"] / out["plain_single_scene"]["value"]
+    for s_ in sims:
+        s_.close()
+    return out
+
+
+def run_serving(args) -> dict:
+    """The serving mix: a seeded Poisson stream of scene-step requests (1-8 substeps each) at
+    `serve_rate` per second over resident tanks whose sizes follow the mix's weights, mixed
+    precision, continuous batching (sprout_gb300.serving)."""
+    from sprout_gb300 import serving
+    r = serving.run(scenes=args.serve_tanks, rate=args.serve_rate, seconds=args.serve_seconds, precision="mixed")
+    r["target_p99_ms"] = 16.0
+    return r
+
+
 def run_engine(args, rank, world, local, pg):
     import sprout_gb300 as S
     from sprout_gb300 import bytes_model as BM
@@ -261,41 +391,18 @@ def run_engine(args, rank, world, local, pg):
         pass
     tank, desc = workload(args.workload, rank)
     sim, parts, _ = tank.engine()
-    dt = 1.0 / 240.0
-    for _ in range(max(args.warmup, 3)):
-        sim.step(1, dt)
-    sim.sync()
-    st0 = sim.stats()
-    live = st0.n_live
-    # ---- device-resident throughput ------------------------------------------------------
-    # Bytes one substep touches at least: every particle slot read and written (48 B each)
-    # and ~400 B of per-cell grid records. Above the L2 nothing is flushed; below it every
-    # timed substep runs after a 512 MB write and only the substeps are timed.
-    touched = 96 * st0.n_slots + 400 * tank.w * tank.h
-    flush = touched <= L2_BYTES
-    barrier(pg)
-    sim.sync()
+    live = None
     with Clocks(local) as clk:
-        if flush:
-            import torch
-            scratch = torch.empty(512 << 20, dtype=torch.uint8, device=f"cuda:{local}")
-            ms = 0.0
-            for _ in range(args.steps):
-                scratch.fill_(1)
-                torch.cuda.synchronize()
-                ms += sim.profile(1)
-            del scratch
-        else:
-            ms = sim.profile(args.steps)
-    sim.sync()
-    barrier(pg)
-    l2_note = (f"~{touched / 1e6:.0f} MB touched per substep <= L2 (129 MB): a 512 MB write before each "
-               "timed substep, substeps alone timed" if flush else
-               f"~{touched / 1e6:.0f} MB touched per substep > L2 (129 MB): no flush")
-    ms = allreduce_max(pg, ms)
-    live_all = allreduce_sum(pg, float(live))
+        ms = device_resident(sim, tank, args, pg, local)
     st1 = sim.stats()
+    live = st1.n_live
+    live_all = allreduce_sum(pg, float(live))
     value = live_all * args.steps / (ms / 1e3)
+    run = {"particles": int(live), "pressure_iters_last": list(st1.pressure_iters),
+           "pressure_residual": st1.pressure_residual, "pressure_unconverged": st1.pressure_unconverged,
+           "viscosity_iters_last": st1.viscosity_iters, "viscosity_residual": st1.viscosity_residual,
+           "viscosity_unconverged": st1.viscosity_unconverged, "pressure2_iters_last": st1.pressure2_iters,
+           "launch": sim.launch()}
     # ---- per-stage times (CUDA events) and the roofline of the dominant stage ---------------
     stages = sim.profile_passes()
     st2 = sim.stats()
@@ -304,6 +411,7 @@ def run_engine(args, rank, world, local, pg):
     iters = max(st2.pressure_iters[0], st2.pressure_iters[1])
     top = max(stages, key=stages.get)
     active = active_viscosity_cells(sim, tank.w, tank.h) if st2.viscosity_mode == 2 else 0
+    run["viscosity_active_cells"] = active
     algo = BM.stage_bytes(top, st2.n_live, tank.w * tank.h, unknowns, iters, st2.acc_stride, bool(st2.thermal),
                           st2.viscosity_mode, active_cells=active, visc_iterations=st2.viscosity_iters,
                           iterations2=st2.pressure2_iters)
@@ -313,21 +421,21 @@ def run_engine(args, rank, world, local, pg):
             "algorithmic_bytes": algo, "stage_ms": stages[top]}
     traffic_file = ROOT / "profiles" / "traffic.json"
     if traffic_file.exists():
-        tr = json.loads(traffic_file.read_text()).get(args.workload, {}).get(top)
-        if tr:
-            roof["traffic"] = tr
+        tr = json.loads(traffic_file.read_text())
+        v = tr.get(args.workload, {}).get(top)
+        if v:
+            roof["traffic"] = v
+            roof["traffic_source"] = (f"profiles/traffic.json: dram__bytes_read.sum + dram__bytes_write.sum of one "
+                                      f"launch of this stage's kernel on this workload ({tr.get('command', 'ncu')}), "
+                                      "not measured in this run")
     # ---- the mixed-precision solve on the same tank (BF16 matrices, FP64 dot products) ------
     mixed = None
     if args.precision in ("both", "mixed"):
         msim, _, _ = tank.engine()
         msim.set_precision("mixed")
-        for _ in range(max(args.warmup, 3)):
-            msim.step(1, dt)
-        msim.sync()
-        mlive = msim.stats().n_live
-        barrier(pg)
-        mms = allreduce_max(pg, msim.profile(args.steps))
+        mms = device_resident(msim, tank, args, pg, local)
         mst = msim.stats()
+        mlive = mst.n_live
         mstages = msim.profile_passes()
         mixed = {"value": allreduce_sum(pg, float(mlive)) * args.steps / (mms / 1e3), "unit": UNIT,
                  "ms_per_step": mms / args.steps, "stages_ms": mstages,
@@ -336,41 +444,27 @@ def run_engine(args, rank, world, local, pg):
                  "pressure_true_residual_max_fp64": mst.pressure_true_residual_max,
                  "storage": "BF16 couplings + FP32 row-sum-keeping diagonal on every level; FP32 vectors",
                  "dots": "FP64", "speedup_vs_plain": (ms / args.steps) / (mms / args.steps)}
-    # ---- end to end through the public API: a host round trip every step -------------------
-    h0 = sim.stats()
-    lat = []
-    barrier(pg)
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        a = time.perf_counter()
-        sim.step(1, dt)
-        s = sim.stats()           # the step's result read back to the host (blocking)
-        lat.append(time.perf_counter() - a)
-    el = time.perf_counter() - t0
-    el = allreduce_max(pg, el)
-    h1 = sim.stats()
-    e2e_value = live_all * args.steps / el
-    e2e = {"value": e2e_value, "unit": UNIT,
-           "h2d_bytes_per_step": (h1.h2d_bytes - h0.h2d_bytes) / args.steps,
-           # h1's own read is counted in h1 - h0 with the K reads of the loop, all the same size
-           "d2h_bytes_per_step": (h1.d2h_bytes - h0.d2h_bytes) / (args.steps + 1),
-           "p50_ms": float(np.percentile(lat, 50) * 1e3), "p99_ms": float(np.percentile(lat, 99) * 1e3)}
+    # ---- end to end through the public API, on a fresh copy over the same substeps ----------
+    e2e = end_to_end(tank, args, pg)
+    batched = run_batched(args, pg, rank, world) if args.batch_tanks > 0 else None
+    serving_r = run_serving(args) if (args.serve_seconds > 0 and world == 1) else None
     if rank != 0:
         return
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f32", "data": "synthetic (seeded tank, no dataset)",
-            "config": dict(desc, particles=int(live), parallelism=f"replicas x{world}",
-                           l2=l2_note,
-                           pressure_iters_last=list(st2.pressure_iters), pressure_residual=st2.pressure_residual,
-                           pressure_unconverged=st2.pressure_unconverged,
-                           viscosity_iters_last=st2.viscosity_iters, viscosity_residual=st2.viscosity_residual,
-                           viscosity_unconverged=st2.viscosity_unconverged, pressure2_iters_last=st2.pressure2_iters,
-                           viscosity_active_cells=active),
+            "dtype": "f32", "data": "synthetic (seeded tank, no dataset)", "config": desc,
+            "parallelism": f"replicas x{world}", "run": run,
             "clocks": clk.summary(), "e2e": e2e, "gpu_launches": kernels_per_substep(st2, tank.settings) * args.steps,
             "roofline": roof, "stages_ms": stages, "latency_ms": {"p50": e2e["p50_ms"], "p99": e2e["p99_ms"]}}
     if mixed is not None:
         line["mixed"] = mixed
+    if batched is not None:
+        batched["ratio_mixed_batched_vs_plain_single"] = batched["mixed"]["value"] / value
+        batched["ratio_plain_batched_vs_plain_single"] = batched["plain"]["value"] / value
+        batched["target_ratio"] = 3.0
+        line["batched"] = batched
+    if serving_r is not None:
+        line["serving"] = serving_r
     if not args.no_cpu_baseline:
         # the checkers, on the host: the oracle's rate, and the FP64 reference solution of each
         # arm's last pressure system
@@ -398,6 +492,12 @@ def main():
     ap.add_argument("--precision", default="both", choices=["plain", "mixed", "both"],
                     help="plain: the reference's FP32 arithmetic (the headline value); mixed: also time "
                          "the mixed-precision pressure solve on the same tank (reported under 'mixed')")
+    ap.add_argument("--batch-tanks", type=int, default=64,
+                    help="tanks of the batched configuration's leg (0: skip it)")
+    ap.add_argument("--serve-seconds", type=float, default=10.0,
+                    help="seconds of the serving mix's arrival stream (the configuration runs 60; 0: skip it)")
+    ap.add_argument("--serve-rate", type=float, default=2000.0)
+    ap.add_argument("--serve-tanks", type=int, default=512)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, world, local, pg = dist_setup(args.gpus)

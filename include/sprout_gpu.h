@@ -144,6 +144,14 @@ int sprout_scene_rasterize(const SproutScene* s, float* sdf, float* solid4, uint
 int sprout_fill_rect(const SproutScene* s, const float rect[4], uint32_t material,
                      uint32_t n_before, SproutParticle* out, uint32_t cap, uint32_t* n);
 
+/* ---- devices ----------------------------------------------------------------------------
+ * No counterpart in the reference (it opens one Vulkan device). Sims and batches are created
+ * on the calling thread's current CUDA device and keep using it; these select it. One process
+ * may drive several devices, one sim or batch per device at a time per thread. */
+int sprout_device_count(int* n);
+int sprout_set_device(int device);
+int sprout_get_device(int* device);
+
 /* ---- the simulation: FluidSim (src/sim/mod.rs:862-3474) ----------------------------- */
 /* FluidSim::new (mod.rs:1034): a w x h grid for at most `capacity` particles, on the
  * current CUDA device. */
@@ -180,6 +188,21 @@ int sprout_sim_spawn(SproutSim* sim, const SproutParticle* p, uint32_t n, uint32
  * grid (the reference asserts) or cap < *cells. */
 int sprout_sim_cell_counts(SproutSim* sim, const int32_t lo[2], const int32_t hi[2], uint32_t* out,
                            size_t cap, size_t* cells);
+/* Stats (src/sim/mod.rs:130-136): live particles and, per material row, its particles and the
+ * sum of their concentrations (in particles, a multiple of 1/256). */
+#define SPROUT_MATERIAL_ROWS 96
+typedef struct SproutStats {
+    uint32_t live;
+    uint32_t count[SPROUT_MATERIAL_ROWS];
+    float conc[SPROUT_MATERIAL_ROWS];
+} SproutStats;
+/* FluidSim::request_stats (mod.rs:3246-3255, stats.comp): records the census of the particle
+ * slots on the sim's stream, after the work queued so far; nothing while one is in flight.
+ * Asynchronous. */
+int sprout_sim_request_stats(SproutSim* sim);
+/* FluidSim::poll_stats (mod.rs:3258-3273): *ready = 1 and *out filled when the last requested
+ * census has finished on the device, else *ready = 0 (and *out untouched). Non-blocking. */
+int sprout_sim_poll_stats(SproutSim* sim, SproutStats* out, int* ready);
 /* FluidSim::record + submit (mod.rs:2400-2562): `substeps` substeps meant to cover
  * `target` seconds (ignored with a fixed step rate). Asynchronous on the sim's stream.
  * tool may be NULL. */
@@ -314,6 +337,29 @@ int sprout_batch_profile(SproutBatch* b, uint32_t substeps, float* ms);
  * solves), 0 = the default; as for a sim, results do not depend on them. */
 int sprout_batch_set_launch(SproutBatch* b, const SproutLaunch* launch);
 
+/* ---- frame pacing: Pacer (src/pacing.rs) -------------------------------------------------
+ * Host-side planner of how many substeps each rendered frame records and what simulated
+ * time they should cover, from the frame's length, the expected substep length, the
+ * slow-motion factor, the measured device cost of a substep (sprout_sim_profile; 0 while
+ * unknown) and the device time a frame may spend simulating. */
+#define SPROUT_MAX_SUBSTEPS_PER_FRAME 24
+typedef struct SproutPacer SproutPacer;
+/* Plan (pacing.rs:43-50): substeps to record and the simulated seconds they should cover
+ * (target) and are expected to cover (expected). */
+typedef struct SproutPlan {
+    uint32_t substeps;
+    float target, expected;
+} SproutPlan;
+int sprout_pacer_new(SproutPacer** out);
+int sprout_pacer_free(SproutPacer* p);
+/* Pacer::reset (pacing.rs:58-61): forgets owed time. */
+int sprout_pacer_reset(SproutPacer* p);
+/* Pacer::speed (pacing.rs:63-66): simulated time delivered over asked (1: real time). */
+int sprout_pacer_speed(const SproutPacer* p, float* speed);
+/* Pacer::plan (pacing.rs:67-112). fixed != 0: a fixed step rate (dt exact). */
+int sprout_pacer_plan(SproutPacer* p, float frame_dt, float dt, int fixed, float time_scale, float cost, float budget,
+                      SproutPlan* out);
+
 /* ---- a pressure solve that allocates nothing ------------------------------------------
  * No counterpart in the reference: an addition for callers that cannot allocate device
  * memory (a host whose allocator owns the whole device, a path that must not allocate
@@ -325,15 +371,20 @@ int sprout_batch_set_launch(SproutBatch* b, const SproutLaunch* launch);
  * density-correction right-hand sides; x 2 floats per cell, the starting guess on entry
  * and the solution on return, zeroed where the cell is no unknown).
  * All scratch (multigrid hierarchy, Krylov vectors, the solve's scalars) lives in one
- * fixed device array of about 16 MB inside the library, which every GPU that loads it
- * holds until the process exits; grids above 147,456 cells (512 x 288) are refused with
- * SPROUT_E_CAPACITY. No cudaMalloc, cudaFree or allocating routine is called.
+ * fixed device array of about 17 MB inside the library, which every GPU that loads it
+ * holds until the process exits. It is sized for the worst grid shape it accepts: both
+ * sides at least 16 cells and at most 147,456 cells (512 x 288) in all, long thin grids
+ * included; other grids are refused with SPROUT_E_CAPACITY. No cudaMalloc, cudaFree or
+ * allocating routine is called.
  * The first call on each device looks up the array's device address (with that device
  * current); make that first call before any stream capture. Every call shares the array
  * and starts from cleared scratch, so calls whose work overlaps on the GPU (different
  * streams, several host threads) race: serialise them. `stream` is a cudaStream_t (NULL:
  * the default stream). iters_out (2 values) and residual_out may be NULL; if either is
- * given the call waits for the solve and reports its iterations and |r|/|b|. */
+ * given the call waits for the solve and reports its iterations and |r|/|b|, and returns
+ * SPROUT_E_TIMEOUT if a bounded wait ran out or SPROUT_E_DIVERGED if the system was not
+ * finite. With both NULL the call returns once the work is queued and reports neither:
+ * pass one of them to learn how the solve ended. */
 int sprout_pressure_solve_static(uint32_t w, uint32_t h, const float* mga, const float* mgd,
                                  const float* rhs, float* x, float tol_p, float tol_psi,
                                  uint32_t max_iters, void* stream, uint32_t* iters_out,

@@ -44,7 +44,9 @@ EXPORTS = [
     "sprout_batch_set_precision", "sprout_batch_step", "sprout_batch_sync", "sprout_batch_profile",
     "sprout_batch_step_subset", "sprout_batch_tickets", "sprout_device_memory", "sprout_sim_trace_enable",
     "sprout_sim_trace_read", "sprout_sim_spawn", "sprout_sim_cell_counts", "sprout_sim_set_launch",
-    "sprout_sim_get_launch", "sprout_sim_debug_stall", "sprout_batch_set_launch",
+    "sprout_sim_get_launch", "sprout_sim_debug_stall", "sprout_batch_set_launch", "sprout_sim_request_stats",
+    "sprout_sim_poll_stats", "sprout_pacer_new", "sprout_pacer_free", "sprout_pacer_reset", "sprout_pacer_speed",
+    "sprout_pacer_plan", "sprout_device_count", "sprout_set_device", "sprout_get_device",
 ]
 
 STAGES = ["advance", "sort", "p2g", "grid", "pressure", "project", "viscosity", "project2"]
@@ -96,6 +98,17 @@ class Launch(C.Structure):
     def as_dict(self) -> dict:
         return {k: int(getattr(self, k)) for k in ("pressure_blocks", "pressure_blocks_mixed", "viscosity_blocks",
                                                    "batch_viscosity")}
+
+
+class Census(C.Structure):
+    """SproutStats (Stats, src/sim/mod.rs:130-136): live particles, per material row its
+    particles and the sum of their concentrations."""
+    _fields_ = [("live", C.c_uint32), ("count", C.c_uint32 * 96), ("conc", C.c_float * 96)]
+
+
+class Plan(C.Structure):
+    """SproutPlan (pacing.rs Plan): substeps, target and expected simulated seconds."""
+    _fields_ = [("substeps", C.c_uint32), ("target", C.c_float), ("expected", C.c_float)]
 
 
 _lib = None
@@ -160,6 +173,13 @@ def lib() -> C.CDLL:
         "sprout_device_memory": ([P(C.c_size_t), P(C.c_size_t)], C.c_int),
         "sprout_sim_trace_enable": ([V, C.c_uint32], C.c_int),
         "sprout_sim_trace_read": ([V, V, C.c_size_t, P(C.c_size_t), P(C.c_uint32)], C.c_int),
+        "sprout_device_count": ([P(C.c_int)], C.c_int), "sprout_set_device": ([C.c_int], C.c_int),
+        "sprout_get_device": ([P(C.c_int)], C.c_int),
+        "sprout_pacer_new": ([P(V)], C.c_int), "sprout_pacer_free": ([V], C.c_int),
+        "sprout_pacer_reset": ([V], C.c_int), "sprout_pacer_speed": ([V, P(C.c_float)], C.c_int),
+        "sprout_pacer_plan": ([V, C.c_float, C.c_float, C.c_int, C.c_float, C.c_float, C.c_float, P(Plan)], C.c_int),
+        "sprout_sim_request_stats": ([V], C.c_int),
+        "sprout_sim_poll_stats": ([V, P(Census), P(C.c_int)], C.c_int),
         "sprout_sim_set_launch": ([V, P(Launch)], C.c_int),
         "sprout_sim_get_launch": ([V, P(Launch)], C.c_int),
         "sprout_sim_debug_stall": ([V, C.c_uint32, C.c_uint32, C.c_uint32], C.c_int),
@@ -445,6 +465,16 @@ class FluidSim:
         _check(lib().sprout_sim_device_bytes(self._h, C.byref(b)))
         return b.value
 
+    def request_stats(self):
+        """FluidSim::request_stats: records the census of the particles (asynchronous)."""
+        _check(lib().sprout_sim_request_stats(self._h))
+
+    def poll_stats(self) -> "Census | None":
+        """FluidSim::poll_stats: the census once the device has finished it, else None."""
+        out, ready = Census(), C.c_int()
+        _check(lib().sprout_sim_poll_stats(self._h, C.byref(out), C.byref(ready)))
+        return out if ready.value else None
+
     def set_launch(self, pressure_blocks: int = 0, pressure_blocks_mixed: int = 0, viscosity_blocks: int = 0):
         """Block counts of the persistent pressure and viscosity solves (0: the default, one
         block per tile up to what the device holds). Results do not depend on them."""
@@ -461,6 +491,35 @@ class FluidSim:
         """Failure injection for tests: block `block` of later persistent solves arrives
         stall_ns late at each grid barrier and waits give up after spin_limit polls."""
         _check(lib().sprout_sim_debug_stall(self._h, block, stall_ns, spin_limit))
+
+
+class Pacer:
+    """Pacer (src/pacing.rs): plans each frame's substeps from the frame length, the step
+    length and the measured device cost of a substep."""
+
+    def __init__(self):
+        self._h = C.c_void_p()
+        _check(lib().sprout_pacer_new(C.byref(self._h)))
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().sprout_pacer_free(self._h)
+            self._h = None
+
+    __del__ = close
+
+    def plan(self, frame_dt: float, dt: float, fixed: bool, time_scale: float, cost: float, budget: float) -> Plan:
+        out = Plan()
+        _check(lib().sprout_pacer_plan(self._h, frame_dt, dt, int(fixed), time_scale, cost, budget, C.byref(out)))
+        return out
+
+    def reset(self):
+        _check(lib().sprout_pacer_reset(self._h))
+
+    def speed(self) -> float:
+        v = C.c_float()
+        _check(lib().sprout_pacer_speed(self._h, C.byref(v)))
+        return v.value
 
 
 def pressure_solve_static(w: int, h: int, mga_ptr: int, mgd_ptr: int, rhs_ptr: int, x_ptr: int, tol_p: float,
@@ -533,6 +592,17 @@ class Batch:
         default, 1 always one batched viscosity solve, 2 one solve per tank."""
         lc = Launch(pressure_blocks, pressure_blocks_mixed, viscosity_blocks, batch_viscosity)
         _check(lib().sprout_batch_set_launch(self._h, C.byref(lc)))
+
+
+def set_device(device: int):
+    """Sims and batches created on this thread from now on live on `device`."""
+    _check(lib().sprout_set_device(device))
+
+
+def device_count() -> int:
+    n = C.c_int()
+    _check(lib().sprout_device_count(C.byref(n)))
+    return n.value
 
 
 def device_memory():

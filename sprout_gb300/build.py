@@ -17,7 +17,8 @@ PKG = Path(__file__).resolve().parent
 CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = PKG / "libsprout_gpu.so"
-SOURCES = ["particles.cu", "admission.cu", "grid.cu", "pressure.cu", "viscosity.cu", "sim.cu", "params.cpp", "scene.cpp"]
+SOURCES = ["particles.cu", "admission.cu", "grid.cu", "pressure.cu", "viscosity.cu", "sim.cu", "params.cpp", "scene.cpp",
+           "pacer.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -38,7 +39,7 @@ def _flags(src: str) -> list[str]:
 def _compile(src: str, verbose: bool) -> Path:
     obj = BUILD / (src.replace(".", "_") + ".o")
     s = CSRC / src
-    deps = [s] + list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh")) + [PKG.parent / "include" / "sprout_gpu.h"]
+    deps = [s] + list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh")) + list(CSRC.glob("*.inc")) + [PKG.parent / "include" / "sprout_gpu.h"]
     if obj.exists() and obj.stat().st_mtime >= max(p.stat().st_mtime for p in deps):
         return obj
     cmd = [nvcc(), "-c", str(s), "-o", str(obj)] + _flags(src)

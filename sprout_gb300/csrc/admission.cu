@@ -9,6 +9,8 @@
 // depend on scheduling (one of the outcomes claim.comp allows).
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "dev_common.cuh"
 #include "kernels.h"
 
@@ -104,7 +106,50 @@ __global__ void k_cell_counts(const float4* part, uint32_t n_slots, int ox, int 
     atomicAdd(&out[cy * sw + cx], 1u);
 }
 
+// stats.comp:14-42: the census of the particle slots: live particles, and per material row
+// its particles and the sum of their concentrations in 1/256 of a particle, each particle's
+// quantised as uint(clamp(s, 0, 1) * 256 + 0.5). The reference folds runs of 64 slots before
+// its atomics; here every block first sums its slots per row in shared memory (integer adds,
+// so the totals do not depend on the order), then adds each non-zero row once to the global
+// counters: out[0] live, out[1 + m] count of row m, out[1 + kStatsRows + m] concentration.
+constexpr int STATS_BLOCK = 256;
+__global__ void __launch_bounds__(STATS_BLOCK) k_stats(const float4* part, uint32_t n_slots, uint32_t* out) {
+    __shared__ uint32_t cnt[kStatsRows], conc[kStatsRows];
+    __shared__ uint32_t live;
+    for (int m = threadIdx.x; m < kStatsRows; m += STATS_BLOCK) cnt[m] = conc[m] = 0u;
+    if (threadIdx.x == 0) live = 0u;
+    __syncthreads();
+    uint32_t mine = 0u;
+    for (uint32_t id = blockIdx.x * STATS_BLOCK + threadIdx.x; id < n_slots; id += gridDim.x * STATS_BLOCK) {
+        const float4 q2 = part[3 * id + 2];
+        const uint32_t kind = __float_as_uint(q2.y) & 255u;
+        if (kind == 0u || kind > (uint32_t)kStatsRows) continue;
+        mine++;
+        const float sc = fminf(fmaxf(q2.x, 0.0f), 1.0f);
+        atomicAdd(&cnt[kind - 1u], 1u);
+        atomicAdd(&conc[kind - 1u], (uint32_t)(sc * 256.0f + 0.5f));
+    }
+    // live particles of the block: a warp sum, then one shared add per warp
+    for (int o = 16; o > 0; o >>= 1) mine += __shfl_down_sync(0xffffffffu, mine, o);
+    if ((threadIdx.x & 31) == 0 && mine) atomicAdd(&live, mine);
+    __syncthreads();
+    for (int m = threadIdx.x; m < kStatsRows; m += STATS_BLOCK) {
+        if (cnt[m]) atomicAdd(&out[1 + m], cnt[m]);
+        if (conc[m]) atomicAdd(&out[1 + kStatsRows + m], conc[m]);
+    }
+    if (threadIdx.x == 0 && live) atomicAdd(&out[0], live);
+}
+
 }  // namespace
+
+void launch_stats(const float4* part, uint32_t n_slots, uint32_t* out, cudaStream_t st) {
+    cudaMemsetAsync(out, 0, stats_words() * sizeof(uint32_t), st);
+    if (n_slots == 0) return;
+    int sms = 152;
+    const uint32_t want = (n_slots + STATS_BLOCK - 1) / STATS_BLOCK;
+    const int blocks = (int)std::min<uint32_t>(want, (uint32_t)(4 * sms));
+    k_stats<<<blocks, STATS_BLOCK, 0, st>>>(part, n_slots, out);
+}
 
 uint32_t claim_scratch_words(uint32_t n_slots) { return (n_slots + CLAIM_BLOCK - 1) / CLAIM_BLOCK + 1; }
 

@@ -94,6 +94,7 @@ struct DevScene {
     uint2* hga;         // four BF16 couplings per cell
     float* hgd;         // FP32 diagonal, rebuilt so that each row keeps its exact excess over
                         // the BF16 couplings (the part of D that is no coupling: air, vent)
+    float* hgi;         // 1 / hgd (0 where no unknown): the smoothers multiply by it
     Dbl4* partials64;
     // implicit viscosity (visc*.comp, vmg*.comp): Krylov vectors on the grid, the multigrid
     // hierarchy over the levels of lv, tile flags and the compact lists of active tiles

@@ -42,6 +42,11 @@ void launch_claim(float4* part, uint32_t n_slots, const float4* spawn, uint32_t 
                   cudaStream_t st);
 void launch_cell_counts(const float4* part, uint32_t n_slots, int ox, int oy, int sw, int sh, uint32_t* out,
                         cudaStream_t st);
+// stats.comp: the census of the particle slots into out (stats_words() words, zeroed first):
+// live particles, per material row its particles and their concentration in 1/256.
+constexpr int kStatsRows = 96;   // the material table's rows (MAX_MATERIALS)
+constexpr uint32_t stats_words() { return 1u + 2u * (uint32_t)kStatsRows; }
+void launch_stats(const float4* part, uint32_t n_slots, uint32_t* out, cudaStream_t st);
 void launch_grid(const DevScene& d, const LaunchCfg& cfg, cudaStream_t st);
 // rigid.comp's five modes at the end of a substep (tanks with CAP_RIGID)
 void launch_rigid(const DevScene& d, cudaStream_t st);
@@ -92,5 +97,7 @@ size_t pressure_batch_scalar_bytes();
 int pressure_blocks_max(int device, size_t smem, bool mixed);
 // Dynamic shared memory of the persistent pressure kernel: the tail levels of each block.
 size_t pressure_smem(const Levels& lv);
+// ... and of the batched one, whose staging regions share it with the tail.
+size_t pressure_batch_smem(const Levels& lv);
 
 }  // namespace sprout

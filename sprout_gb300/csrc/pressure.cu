@@ -74,6 +74,11 @@ struct Plain {
     DEV static const void* Araw(const DevScene& d, int i) { return d.mga + i; }
     DEV static const float* Dptr(const DevScene& d) { return d.mgd; }
     DEV static float4 Aslot(const float4& slot) { return slot; }
+    // a / D with D's staged slot (the diagonal): the shader's IEEE division; quotp is zero
+    // unless the slot is positive
+    DEV static float quot(float a, float slot) { return divz(a, slot); }
+    DEV static float2 quot(float2 a, float slot) { return divz(a, slot); }
+    DEV static float quotp(float a, float slot) { return divp(a, slot); }
 };
 
 // a pair of BF16 values in 32 bits (x in the low half), rounded to nearest even
@@ -104,12 +109,15 @@ struct Mixed {
         d.hga[i] = u;
         if (dg <= 0.0f) {
             d.hgd[i] = 0.0f;
+            d.hgi[i] = 0.0f;
             return;
         }
         const float2 lo = unpack(u.x), hi = unpack(u.y);
         const float c32 = ((m & 1) ? a.x : 0.0f) + ((m & 2) ? a.y : 0.0f) + ((m & 4) ? a.z : 0.0f) + ((m & 8) ? a.w : 0.0f);
         const float c16 = ((m & 1) ? lo.x : 0.0f) + ((m & 2) ? lo.y : 0.0f) + ((m & 4) ? hi.x : 0.0f) + ((m & 8) ? hi.y : 0.0f);
-        d.hgd[i] = (dg - c32) + c16;
+        const float D = (dg - c32) + c16;
+        d.hgd[i] = D;
+        d.hgi[i] = D > 0.0f ? 1.0f / D : 0.0f;
     }
     // the vectors stay FP32 on every level: rounding them would make the V-cycle a
     // nonlinear operator, which conjugate gradients does not tolerate (it stagnates near the
@@ -128,7 +136,14 @@ struct Mixed {
     DEV static Dbl4 fin(acc4 a) { return to_dbl(a); }
     static constexpr int kABytes = 8;
     DEV static const void* Araw(const DevScene& d, int i) { return d.hga + i; }
-    DEV static const float* Dptr(const DevScene& d) { return d.hgd; }
+    // the level passes stage the inverse diagonal in the diagonal's slot (positive exactly
+    // where the diagonal is) and multiply by it instead of dividing: a V-cycle is a
+    // preconditioner here, not the reference's arithmetic, and ten IEEE divisions per black
+    // cell were most of a way down's instructions
+    DEV static const float* Dptr(const DevScene& d) { return d.hgi; }
+    DEV static float quot(float a, float slot) { return a * slot; }
+    DEV static float2 quot(float2 a, float slot) { return make_float2(a.x * slot, a.y * slot); }
+    DEV static float quotp(float a, float slot) { return slot > 0.0f ? a * slot : 0.0f; }
     // the BF16 row copied into the first 8 bytes of the slot, widened on reading
     DEV static float4 Aslot(const float4& slot) {
         const uint2 u = *reinterpret_cast<const uint2*>(&slot);
@@ -318,8 +333,10 @@ struct Tail {
 
 DEV bool t_unknown(const Tail& tl, const Lv& L, int x, int y) { return l_inside(L, x, y) && tl.dg[L.off - tl.base + y * L.w + x] > 0.0f; }
 
-// The tail of scene d laid out in the dynamic shared memory at smem.
-DEV Tail make_tail(const DevScene& d, unsigned char* smem) {
+// The tail of scene d laid out in the dynamic shared memory at smem; its right-hand sides at
+// r_store if given (they are live only inside the tail phase, so a caller may keep them in
+// bytes that other phases use), else after the iterates.
+DEV Tail make_tail(const DevScene& d, unsigned char* smem, float2* r_store = nullptr) {
     Tail tl;
     const Lv F = lev(d.lv, d.lv.tail), E = lev(d.lv, d.lv.n - 1);
     tl.base = F.off;
@@ -327,10 +344,22 @@ DEV Tail make_tail(const DevScene& d, unsigned char* smem) {
     tl.nf = F.w * F.h;
     tl.a = reinterpret_cast<float4*>(smem);
     tl.x = reinterpret_cast<float2*>(tl.a + tl.T);
-    tl.r = tl.x + tl.T;
-    tl.dg = reinterpret_cast<float*>(tl.r + tl.T);
+    if (r_store) {
+        tl.r = r_store;
+        tl.dg = reinterpret_cast<float*>(tl.x + tl.T);
+    } else {
+        tl.r = tl.x + tl.T;
+        tl.dg = reinterpret_cast<float*>(tl.r + tl.T);
+    }
     tl.m = reinterpret_cast<uint8_t*>(tl.dg + tl.T);
     return tl;
+}
+
+// Cells of the tail levels, and the tail's bytes with and without its right-hand sides.
+__host__ __device__ inline int tail_cells(const Levels& lv) { return lv.off[lv.n - 1] + lv.w[lv.n - 1] * lv.h[lv.n - 1] - lv.off[lv.tail]; }
+__host__ __device__ inline size_t tail_bytes(int T, bool with_r) {
+    const size_t per = sizeof(float4) + sizeof(float2) + (with_r ? sizeof(float2) : 0) + sizeof(float) + 1;
+    return ((size_t)T * per + 15) / 16 * 16;
 }
 
 // mg_tail.comp mode 1 in every block's shared memory, once per solve: the first tail
@@ -522,15 +551,15 @@ DEV void finish_down(const DevScene& d, const Lv& F, const Lv& C, int t, const R
         float2 sum = rhs(k);
         const float d0 = dg(k - 1), d1 = dg(k + 1), d2 = dg(k - RW), d3 = dg(k + RW);
         const float2 r0 = rhs(k - 1), r1 = rhs(k + 1), r2 = rhs(k - RW), r3 = rhs(k + RW);
-        const float t0x = divp(w.x * r0.x, d0), t0y = divp(w.x * r0.y, d0);
-        const float t1x = divp(w.y * r1.x, d1), t1y = divp(w.y * r1.y, d1);
-        const float t2x = divp(w.z * r2.x, d2), t2y = divp(w.z * r2.y, d2);
-        const float t3x = divp(w.w * r3.x, d3), t3y = divp(w.w * r3.y, d3);
+        const float t0x = M::quotp(w.x * r0.x, d0), t0y = M::quotp(w.x * r0.y, d0);
+        const float t1x = M::quotp(w.y * r1.x, d1), t1y = M::quotp(w.y * r1.y, d1);
+        const float t2x = M::quotp(w.z * r2.x, d2), t2y = M::quotp(w.z * r2.y, d2);
+        const float t3x = M::quotp(w.w * r3.x, d3), t3y = M::quotp(w.w * r3.y, d3);
         if (d0 > 0.0f) { sum.x += t0x; sum.y += t0y; }
         if (d1 > 0.0f) { sum.x += t1x; sum.y += t1y; }
         if (d2 > 0.0f) { sum.x += t2x; sum.y += t2y; }
         if (d3 > 0.0f) { sum.x += t3x; sum.y += t3y; }
-        return divz(sum, dg(k));
+        return M::quot(sum, dg(k));
     };
     // one cell's z (mg_down: red from zero, black after it), the CG update and mgx
     auto own = [&](int lx, int ly, bool red) {
@@ -543,7 +572,7 @@ DEV void finish_down(const DevScene& d, const Lv& F, const Lv& C, int t, const R
             const float D = dg(k0);
             if (D > 0.0f) {
                 if (red) {
-                    z = divz(rhs(k0), D);
+                    z = M::quot(rhs(k0), D);
                 } else {
                     z = black(k0);
                 }
@@ -682,7 +711,7 @@ DEV void finish_up(const DevScene& d, const Lv& F, int t, bool flag, const Zc& z
                 sum.y += uy;
             }
         }
-        return divz(sum, dg(k));
+        return M::quot(sum, dg(k));
     };
     const int2 lc = colour_cell();
     const int lx = lc.x, ly = lc.y, cell = ly * 16 + lx;
@@ -725,7 +754,7 @@ DEV void finish_up(const DevScene& d, const Lv& F, int t, bool flag, const Zc& z
                         sy += uy;
                     }
                 }
-                z = divz(make_float2(sx, sy), dg(k0));
+                z = M::quot(make_float2(sx, sy), dg(k0));
             }
             a4 = M::prod4(r.x, z.x, r.y, z.y, r.x, r.x, r.y, r.y);
         }
@@ -1178,16 +1207,19 @@ template <class M>
 __global__ void __launch_bounds__(NT, 2) k_mgpcg(DevScene d, int second, int scale_mode) {
     using acc = typename M::acc;
     using acc4 = typename M::acc4;
-    __shared__ Region rg[kDepth];
     __shared__ TileCache tc;
     __shared__ float2 sz[NT];
     __shared__ acc4 buf[NT];
     __shared__ Solve<acc> K;
-    extern __shared__ __align__(16) unsigned char tail_smem[];
+    // dynamic: the staging regions, then the tail levels (matrices, iterates, masks: kept for
+    // the whole solve); the tail's right-hand sides, live only in the tail phase, when no
+    // tile is being staged, in the regions' bytes
+    extern __shared__ __align__(16) unsigned char dyn_smem[];
+    Region* rg = reinterpret_cast<Region*>(dyn_smem);
     const DevParams* P = d.P;
     const int n = d.nwg;
     acc4* part = M::part(d);
-    const Tail tl = make_tail(d, tail_smem);
+    const Tail tl = make_tail(d, dyn_smem + kDepth * sizeof(Region), reinterpret_cast<float2*>(dyn_smem));
     if (!second) {
         for (int t = blockIdx.x; t < n; t += gridDim.x) cg_scale_tile<M>(d, t, scale_mode);
         for (int l = 1; l <= d.lv.tail; l++) {
@@ -1353,16 +1385,26 @@ DEV float2* parity_p(const DevScene& d, int it) { return (it & 1) ? d.cgp2 : d.c
 
 }  // namespace
 
+static_assert(sizeof(Region) % 16 == 0, "regions laid end to end in dynamic shared memory");
+
+// The batched solve's dynamic shared memory: the staging regions and, during the tail phase
+// only, one scene's tail (a scene's tail is rebuilt and solved within that phase and its
+// result stored to global memory, while no tile is being staged), in the same bytes.
+size_t pressure_batch_smem(const Levels& lv) {
+    return std::max(tail_bytes(tail_cells(lv), true), (size_t)kDepth * sizeof(Region));
+}
+
 template <class M>
 __global__ void __launch_bounds__(NT, 2) k_mgpcg_batch(BatchView B, int second) {
     using acc = typename M::acc;
     using acc4 = typename M::acc4;
-    __shared__ Region rg[kDepth];
     __shared__ TileCache tc;
     __shared__ float2 sz[NT];
     __shared__ acc4 buf[NT];
     __shared__ int s_run;
-    extern __shared__ __align__(16) unsigned char tail_smem[];
+    extern __shared__ __align__(16) unsigned char dyn_smem[];
+    Region* rg = reinterpret_cast<Region*>(dyn_smem);
+    unsigned char* tail_smem = dyn_smem;
     Solve<acc>* KS = reinterpret_cast<Solve<acc>*>(B.scal);
     SolveState* BK = B.K;
     auto tol = [&](const DevScene& d, int c) { return (acc)d.P->tol[c]; };
@@ -1539,8 +1581,10 @@ __global__ void __launch_bounds__(NT, 2) k_mgpcg_batch(BatchView B, int second) 
 }
 
 size_t pressure_smem(const Levels& lv) {
-    int T = lv.off[lv.n - 1] + lv.w[lv.n - 1] * lv.h[lv.n - 1] - lv.off[lv.tail];
-    return ((size_t)T * (sizeof(float4) + 2 * sizeof(float2) + sizeof(float) + 1) + 15) / 16 * 16;
+    // the tail's first level has at most 1500 cells and each coarser level at most half the
+    // one above, so a tail holds fewer than 3000 cells
+    static_assert(kDepth * sizeof(Region) >= 4096 * sizeof(float2), "the tail's right-hand sides fit in the regions");
+    return kDepth * sizeof(Region) + tail_bytes(tail_cells(lv), false);
 }
 
 namespace {

@@ -43,6 +43,27 @@ int fail(int code, const std::string& msg) {
     } while (0)
 
 constexpr float kNominalDt = 1.0f / 240.0f;
+static_assert(SPROUT_MATERIAL_ROWS == kStatsRows && kStatsRows == kMaxMaterials, "the census has a row per material");
+
+// The autotuner's table (sprout_gb300/tune.py): per grid size, the block counts of the
+// persistent solves that timed fastest; a sim of that size starts from them.
+struct TunedLaunch {
+    int w, h, pressure, pressure_mixed, viscosity;
+};
+constexpr TunedLaunch kTuned[] = {
+#include "tuned_launch.inc"
+    {0, 0, 0, 0, 0}};
+
+SproutLaunch tuned_launch(int w, int h) {
+    SproutLaunch l{};
+    for (const TunedLaunch& t : kTuned)
+        if (t.w == w && t.h == h) {
+            l.pressure_blocks = (uint32_t)t.pressure;
+            l.pressure_blocks_mixed = (uint32_t)t.pressure_mixed;
+            l.viscosity_blocks = (uint32_t)t.viscosity;
+        }
+    return l;
+}
 
 }  // namespace
 
@@ -81,6 +102,8 @@ struct SproutSim {
     std::vector<float> solid_host;   // kept for nothing but the device copy's lifetime
 
     ~SproutSim() {
+        if (stats_ev) cudaEventDestroy(stats_ev);
+        if (h_stats) cudaFreeHost(h_stats);
         if (trace_buf) cudaFree(trace_buf);
         if (d_window) cudaFree(d_window);
         if (h_window) cudaFreeHost(h_window);
@@ -143,11 +166,11 @@ struct SproutSim {
             size_t tot = (size_t)d.lv.total;
             int rc = SPROUT_OK;
 #define A(ptr, n) do { if ((rc = alloc(&(ptr), (n))) != SPROUT_OK) return rc; } while (0)
-            A(d.hga, tot); A(d.hgd, tot);
+            A(d.hga, tot); A(d.hgd, tot); A(d.hgi, tot);
             A(d.partials64, 2 * (size_t)d.nwg);
 #undef A
             mg_max_mixed = pressure_blocks_max(device, pressure_smem(d.lv), true);
-            cfg.mg_blocks_mixed = pick_blocks(launch_req.pressure_blocks_mixed, mg_max_mixed);
+            cfg.mg_blocks_mixed = pick_blocks(launch_req.pressure_blocks_mixed, mg_max_mixed, tuned.pressure_blocks_mixed);
             CUDA_TRY(cudaDeviceSynchronize());
             mixed_alloc = true;
             graph_ok = false;   // new device pointers: the captured substep is stale
@@ -264,25 +287,28 @@ struct SproutSim {
         CUDA_TRY(cudaMemset(d.rl, 0xff, nc * sizeof(int2)));   // no cell rigid before the first rigid pass
         std::vector<float> nt(nc, NO_TEMP);
         CUDA_TRY(cudaMemcpy(solid_t, nt.data(), nc * sizeof(float), cudaMemcpyHostToDevice));
+        tuned = tuned_launch(W, H);
         mg_max = pressure_blocks_max(device, pressure_smem(d.lv), false);
-        cfg.mg_blocks = pick_blocks(launch_req.pressure_blocks, mg_max);
+        cfg.mg_blocks = pick_blocks(launch_req.pressure_blocks, mg_max, tuned.pressure_blocks);
         CUDA_TRY(cudaDeviceSynchronize());
         return SPROUT_OK;
     }
 
     // The persistent solvers' block counts: the caller's request (0: one block per level-0
     // tile), at most what the device holds at once (mx).
-    SproutLaunch launch_req{};
+    // tuned: the autotuner's counts for this grid size (0 where it has none).
+    SproutLaunch launch_req{}, tuned{};
     int mg_max = 1, mg_max_mixed = 1;
-    int pick_blocks(uint32_t want, int mx) const {
+    int pick_blocks(uint32_t want, int mx, uint32_t tuned_count) const {
+        if (want == 0u) want = tuned_count;
         const int b = want != 0u ? (int)std::min<uint32_t>(want, (uint32_t)d.nwg) : d.nwg;
         return std::max(1, std::min(b, std::max(mx, 1)));
     }
     int set_launch(const SproutLaunch& l) {
         CUDA_TRY(cudaStreamSynchronize(stream));
         launch_req = l;
-        cfg.mg_blocks = pick_blocks(l.pressure_blocks, mg_max);
-        if (mixed_alloc) cfg.mg_blocks_mixed = pick_blocks(l.pressure_blocks_mixed, mg_max_mixed);
+        cfg.mg_blocks = pick_blocks(l.pressure_blocks, mg_max, tuned.pressure_blocks);
+        if (mixed_alloc) cfg.mg_blocks_mixed = pick_blocks(l.pressure_blocks_mixed, mg_max_mixed, tuned.pressure_blocks_mixed);
         graph_ok = false;   // the captured substep launches the old counts
         return SPROUT_OK;
     }
@@ -291,7 +317,8 @@ struct SproutSim {
         out->pressure_blocks = (uint32_t)cfg.mg_blocks;
         out->pressure_blocks_mixed = mixed_alloc ? (uint32_t)cfg.mg_blocks_mixed : 0u;
         const int sw = (int)std::min(std::max(params.viscosity_mg_sweeps, 1u), 2u);
-        out->viscosity_blocks = visc_alloc ? (uint32_t)pick_blocks(launch_req.viscosity_blocks, visc_max[sw - 1]) : 0u;
+        out->viscosity_blocks =
+            visc_alloc ? (uint32_t)pick_blocks(launch_req.viscosity_blocks, visc_max[sw - 1], tuned.viscosity_blocks) : 0u;
         out->batch_viscosity = launch_req.batch_viscosity;
     }
 
@@ -567,7 +594,7 @@ struct SproutSim {
         want.viscous_warm = params.viscous_warm != 0;
         want.visc_levels = std::min((int)std::max(params.viscosity_mg_levels, 1u), d.lv.tail);
         want.visc_sweeps = (int)std::min(std::max(params.viscosity_mg_sweeps, 1u), 2u);
-        want.visc_blocks = pick_blocks(launch_req.viscosity_blocks, visc_max[want.visc_sweeps - 1]);
+        want.visc_blocks = pick_blocks(launch_req.viscosity_blocks, visc_max[want.visc_sweeps - 1], tuned.viscosity_blocks);
         want.mixed = mixed;
         bool same = want.n_slots == cfg.n_slots && want.thermal == cfg.thermal && want.heat == cfg.heat && want.rheo == cfg.rheo && want.settle == cfg.settle && want.magnet == cfg.magnet && want.elastic == cfg.elastic && want.rigid == cfg.rigid && want.xtra == cfg.xtra &&
                     want.visc_mode == cfg.visc_mode && want.twice == cfg.twice && want.viscous_warm == cfg.viscous_warm &&
@@ -812,6 +839,47 @@ struct SproutSim {
         }
         // the copies read the queue from pageable memory, which they have finished with on return
         pending.clear();
+        return SPROUT_OK;
+    }
+
+    // FluidSim::request_stats / poll_stats (mod.rs:3246-3273): the census of the slots
+    // (stats.comp) into a device buffer, copied to pinned host memory behind an event.
+    uint32_t* d_stats = nullptr;
+    uint32_t* h_stats = nullptr;
+    cudaEvent_t stats_ev = nullptr;
+    bool stats_in_flight = false;
+    int request_stats() {
+        if (stats_in_flight) return SPROUT_OK;
+        if (!d_stats) {
+            int rc = alloc(&d_stats, stats_words());
+            if (rc != SPROUT_OK) return rc;
+            CUDA_TRY(cudaMallocHost(&h_stats, stats_words() * sizeof(uint32_t)));
+            CUDA_TRY(cudaEventCreateWithFlags(&stats_ev, cudaEventDisableTiming));
+        }
+        launch_stats(d.part, n_slots, d_stats, stream);
+        CUDA_TRY(cudaGetLastError());
+        CUDA_TRY(cudaMemcpyAsync(h_stats, d_stats, stats_words() * sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
+        CUDA_TRY(cudaEventRecord(stats_ev, stream));
+        d2h_bytes += stats_words() * sizeof(uint32_t);
+        stats_in_flight = true;
+        return SPROUT_OK;
+    }
+    int poll_stats(SproutStats* out, int* ready) {
+        *ready = 0;
+        if (!stats_in_flight) return SPROUT_OK;
+        const cudaError_t e = cudaEventQuery(stats_ev);
+        if (e == cudaErrorNotReady) {
+            cudaGetLastError();
+            return SPROUT_OK;
+        }
+        CUDA_TRY(e);
+        out->live = h_stats[0];
+        for (int m = 0; m < SPROUT_MATERIAL_ROWS; m++) {
+            out->count[m] = h_stats[1 + m];
+            out->conc[m] = (float)h_stats[1 + kStatsRows + m] / 256.0f;
+        }
+        stats_in_flight = false;
+        *ready = 1;
         return SPROUT_OK;
     }
 
@@ -1172,7 +1240,7 @@ struct SproutBatch {
             const LaunchCfg& c = sim->cfg;
             scale[k] = (c.visc_mode == 2 && c.twice && c.viscous_warm) ? 1 : 0;
             max_tail = std::max(max_tail, sim->d.lv.tail);
-            smem = std::max(smem, pressure_smem(sim->d.lv));
+            smem = std::max(smem, pressure_batch_smem(sim->d.lv));
         }
         for (int l = 0; l < kMaxLevels; l++) {
             int* o = &off[(size_t)l * (ns + 1)];
@@ -1535,6 +1603,26 @@ int sprout_sim_destroy(SproutSim* sim) {
     return SPROUT_OK;
 }
 
+int sprout_device_count(int* n) {
+    if (!n) return fail(SPROUT_E_ARG, "null argument");
+    CUDA_TRY(cudaGetDeviceCount(n));
+    return SPROUT_OK;
+}
+
+int sprout_set_device(int device) {
+    int n = 0;
+    CUDA_TRY(cudaGetDeviceCount(&n));
+    if (device < 0 || device >= n) return fail(SPROUT_E_ARG, "no such device");
+    CUDA_TRY(cudaSetDevice(device));
+    return SPROUT_OK;
+}
+
+int sprout_get_device(int* device) {
+    if (!device) return fail(SPROUT_E_ARG, "null argument");
+    CUDA_TRY(cudaGetDevice(device));
+    return SPROUT_OK;
+}
+
 int sprout_device_memory(size_t* free_bytes, size_t* total_bytes) {
     if (!free_bytes || !total_bytes) return fail(SPROUT_E_ARG, "null argument");
     CUDA_TRY(cudaMemGetInfo(free_bytes, total_bytes));
@@ -1608,6 +1696,16 @@ int sprout_sim_trace_read(SproutSim* sim, unsigned long long* out, size_t cap, s
     if (out && sim->trace_buf) CUDA_TRY(cudaMemcpy(out, sim->trace_buf, std::min(*words, cap) * 8, cudaMemcpyDeviceToHost));
     return SPROUT_OK;
 }
+int sprout_sim_request_stats(SproutSim* sim) {
+    if (!sim) return fail(SPROUT_E_ARG, "null argument");
+    return sim->request_stats();
+}
+
+int sprout_sim_poll_stats(SproutSim* sim, SproutStats* out, int* ready) {
+    if (!sim || !out || !ready) return fail(SPROUT_E_ARG, "null argument");
+    return sim->poll_stats(out, ready);
+}
+
 int sprout_sim_set_launch(SproutSim* sim, const SproutLaunch* l) {
     if (!sim || !l) return fail(SPROUT_E_ARG, "null argument");
     return sim->set_launch(*l);

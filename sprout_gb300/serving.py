@@ -20,11 +20,7 @@ import time
 import numpy as np
 
 from . import Batch, device_memory
-from .workloads import dam_break
-
-# the batched configurations' grid sizes and the serving mix's weights of them
-SIZES = [(128, 72), (256, 144), (384, 216), (512, 288), (768, 432), (1024, 576)]
-WEIGHTS = [0.30, 0.25, 0.20, 0.12, 0.08, 0.05]
+from .workloads import SERVING_WEIGHTS, uneven_dam_breaks
 
 
 class Request:
@@ -121,15 +117,10 @@ class Server:
 
 
 def serving_tanks(n: int, seed: int = 0):
-    """The serving mix's resident tanks: grid sizes by the mix's weights, seeded dam breaks of
-    one liquid row (water), fill fractions as the batched configuration draws them."""
-    rng = np.random.default_rng(seed)
-    tanks = []
-    for _ in range(n):
-        w, h = SIZES[rng.choice(len(SIZES), p=WEIGHTS)]
-        tanks.append(dam_break(w, h, cell=0.001 * 1024 / w, width=float(rng.uniform(0.2, 0.6)),
-                               height=float(rng.uniform(0.3, 0.8))))
-    return tanks
+    """The serving mix's resident tanks: grid sizes by the mix's weights (30/25/20/12/8/5 % of
+    128 x 72 .. 1024 x 576), seeded dam breaks of one or two liquids from the full-physics
+    ranges, as the batched configuration draws them."""
+    return uneven_dam_breaks(n, seed, weights=SERVING_WEIGHTS)
 
 
 def run(scenes: int = 512, rate: float = 2000.0, seconds: float = 60.0, precision: str = "plain",

@@ -163,3 +163,48 @@ def full_physics(w: int = 1024, h: int = 576, cell: float = 0.001, n_liquids: in
     ex.update(extra or {})
     return layered_custom(w, h, rows, cell=cell, heater_rows=heater_rows, heater_temp=326.85,
                           ambient=19.85, tol=tol, columns=True, seed=seed + 1, extra=ex)
+
+
+# ---- many tanks: the batched and serving configurations ---------------------------------------
+
+# the grid sizes both draw from, and the serving mix's weights of them
+UNEVEN_SIZES = [(128, 72), (256, 144), (384, 216), (512, 288), (768, 432), (1024, 576)]
+SERVING_WEIGHTS = [0.30, 0.25, 0.20, 0.12, 0.08, 0.05]
+
+
+def config3_liquid(rng) -> dict:
+    """One liquid from the full-physics pour's ranges: rho uniform in 800-13500 kg/m^3, dynamic
+    viscosity log-uniform in 1e-3-50 Pa s, surface tension uniform in 0.02-0.5 N/m."""
+    rho = float(rng.uniform(800.0, 13500.0))
+    mu = float(np.exp(rng.uniform(np.log(1e-3), np.log(50.0))))
+    return {"density": rho, "viscosity": min(mu / rho, 0.5), "tension": float(rng.uniform(0.02, 0.5))}
+
+
+def uneven_dam_breaks(n: int = 64, seed: int = 0, weights: list | None = None, tol: float = 1e-5,
+                      extra: dict | None = None) -> list:
+    """Seeded dam breaks of uneven sizes (the batched configuration: 64 tanks, sizes uniform
+    over UNEVEN_SIZES; the serving mix: sizes by SERVING_WEIGHTS). Each tank is the same
+    physical box, 1.024 m wide (cell size 1.024 m / width), fixed 1/240 s substeps; its liquid
+    block covers a seeded 0.2-0.6 of the width and 0.3-0.8 of the height and holds one or two
+    liquids (side by side) drawn from the full-physics pour's ranges; pressure and viscosity
+    to `tol`."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n):
+        k = int(rng.choice(len(UNEVEN_SIZES), p=weights)) if weights is not None else int(rng.integers(len(UNEVEN_SIZES)))
+        w, h = UNEVEN_SIZES[k]
+        fw, fh = float(rng.uniform(0.2, 0.6)), float(rng.uniform(0.3, 0.8))
+        nliq = int(rng.integers(1, 3))
+        s = {"cell_size": 1.024 / w, "fixed_hz": 240.0, "pressure_tol": tol, "viscosity_tol": tol}
+        for j in range(nliq):
+            for name, val in config3_liquid(rng).items():
+                s[f"mat{59 + j}.{name}"] = val
+        s.update(extra or {})
+        x1, y1 = fw * w, fh * h
+        if nliq == 1:
+            fills = [([0.0, 0.0, x1, y1], 59, None)]
+        else:
+            xm = float(int(x1 * rng.uniform(0.3, 0.7)))
+            fills = [([0.0, 0.0, xm, y1], 59, None), ([xm, 0.0, x1, y1], 60, None)]
+        out.append(Tank(w, h, s, [], fills))
+    return out

@@ -1,17 +1,28 @@
 """The mixed-precision pressure solve (BF16 hierarchy, FP32 iterate and residual, FP64 dot
-products and convergence test, true-residual refinement) against the plain FP32 solve and the
-FP64 reference solution, on the same tanks.
+products and convergence test) against the plain FP32 solve and the FP64 reference solution,
+on the same tanks.
 
 Mixed precision changes the preconditioner's rounding, so its results are not bit-exact with
-the reference's arithmetic; what must hold is the reference's own stopping rule — the same
-relative residual (pressure_tol = 1e-5) — and an error against the FP64 solution of the same
-order as the plain solve's (both stated here with the tolerance the test uses).
+the reference's arithmetic; what must hold is the reference's own stopping rule (the same
+relative residual of the carried residual, pressure_tol = 1e-5) and a true residual, evaluated
+in FP64, of the same order as the plain solve's. Neither can go below the FP32 floor: the
+FP64 solution itself, rounded to FP32, leaves a relative residual of ~5e-5 on a dam break and
+~1e-3 on the sealed full-physics pour, so the bounds here are stated against that floor and
+against the plain arm on the same system, with the factors written in the tests.
 """
 import numpy as np
 import pytest
 
 import tanks
-from oracle.fp64_mgpcg import accuracy
+from oracle.fp64_mgpcg import FP64MGPCG, accuracy
+
+
+def fp32_floor(sim, tank) -> float:
+    """|b - A fl32(x*)| / |b| of the FP64 solution x* of the last pressure system, rounded to FP32."""
+    s = FP64MGPCG(sim.field("mga"), sim.field("mgd"), tank.w, tank.h)
+    b = np.asarray(sim.field("prhs"), np.float64).reshape(tank.h, tank.w, 4)[..., :2]
+    x, _ = s.solve(b)
+    return float(s.residual(x.astype(np.float32).astype(np.float64), b)[0])
 
 pytestmark = pytest.mark.gpu
 
@@ -46,9 +57,11 @@ def test_mixed_first_solve_matches_plain():
     assert np.linalg.norm(pm - pp) <= 1e-4 * np.linalg.norm(pp)
     ap = last_system_accuracy(plain, t, (0,))
     am = last_system_accuracy(mixed, t, (0,))
-    # stopping rule 1e-5 on the residual; against the FP64 solution both stay below 1e-4
-    assert ap[0]["error_vs_fp64"] < 1e-4 and am[0]["error_vs_fp64"] < 1e-4, (ap, am)
-    assert am[0]["residual_fp64"] < 1e-4, am
+    # stopping rule 1e-5 on the carried residual; against the FP64 solution both within 5e-5,
+    # and the FP64 true residual within 4x of the larger of the plain arm's and the FP32 floor
+    assert ap[0]["error_vs_fp64"] < 5e-5 and am[0]["error_vs_fp64"] < 5e-5, (ap, am)
+    floor = fp32_floor(plain, t)
+    assert am[0]["residual_fp64"] <= 4.0 * max(ap[0]["residual_fp64"], floor), (am, ap, floor)
     assert mixed.stats().pressure_residual <= 1e-5 * 1.0001
     # the FP64 true residual the mixed solve reports agrees with the one computed here
     assert abs(mixed.stats().pressure_true_residual - am[0]["residual_fp64"]) <= 1e-3 * am[0]["residual_fp64"] + 1e-9
@@ -75,12 +88,17 @@ def test_mixed_runs_the_full_physics_pour():
     assert sm.device_error == 0
     assert sm.pressure_unconverged == 0 and sm.pressure2_unconverged == 0
     assert sm.pressure_residual_max <= 1e-5 * 1.0001
-    assert 0.0 < sm.pressure_true_residual_max < 1e-3
     # the tanks evolve alike: particle positions within a small fraction of a cell
     g = np.sort(plain.download_particles(), order="id")
     m = np.sort(mixed.download_particles(), order="id")
     assert np.array_equal(g["id"], m["id"])
     d = np.abs(g["pos"] - m["pos"]).max()
     assert d < 0.05, d
+    # the last system of each arm: true residual (FP64) within 4x of the larger of the plain
+    # arm's and the FP32 floor, error against the FP64 solution within 4x of the plain arm's
     am = last_system_accuracy(mixed, t, (0,))
-    assert am[0]["error_vs_fp64"] < 1e-2, am
+    ap = last_system_accuracy(plain, t, (0,))
+    floor = max(fp32_floor(mixed, t), fp32_floor(plain, t))
+    assert am[0]["residual_fp64"] <= 4.0 * max(ap[0]["residual_fp64"], floor), (am, ap, floor)
+    assert am[0]["error_vs_fp64"] <= 4.0 * max(ap[0]["error_vs_fp64"], 1e-5), (am, ap)
+    assert abs(sm.pressure_true_residual - am[0]["residual_fp64"]) <= 1e-3 * am[0]["residual_fp64"] + 1e-9

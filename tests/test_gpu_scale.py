@@ -136,3 +136,20 @@ def test_full_physics_1024_config_bit_exact():
     assert not problems, "\n".join(problems[:12])
     st = sim.stats()
     assert st.levels == 10 and st.thermal == 1 and st.viscosity_mode == 2 and st.device_error == 0
+
+
+def test_tuned_launch_is_applied_and_bit_exact():
+    """A grid size the autotuner has an entry for starts from the tuned block counts, and the
+    results stay those of the oracle."""
+    import json
+    from pathlib import Path
+    table = json.loads((Path(__file__).resolve().parents[1] / "sprout_gb300" / "tuned_launch.json").read_text())
+    entry = next(s["best"] for s in table["sizes"] if s["grid"] == [256, 144])
+    t = tanks.full_physics(256, 144, cell=0.004)
+    sim, _, _ = t.engine()
+    ora, _, _ = tanks.oracle_of(t)
+    oracle_threads()
+    problems = step_and_compare(sim, ora, 4, 2, viscosity=True)
+    assert not problems, "\n".join(problems[:12])
+    got = sim.launch()
+    assert got["pressure_blocks"] == entry["pressure_blocks"] and got["viscosity_blocks"] == entry["viscosity_blocks"], (got, entry)
