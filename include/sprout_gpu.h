@@ -137,6 +137,12 @@ int sprout_scene_sdf(const SproutScene* s, float x, float y, float* d);
  * temp[w h] (may be NULL; *heated = 1 if any shape is held at a temperature). */
 int sprout_scene_rasterize(const SproutScene* s, float* sdf, float* solid4, uint32_t* region,
                            float* temp, int* heated);
+/* Scene::rasterize computed on the current CUDA device, into the same host arrays as
+ * sprout_scene_rasterize and bit-identical to it: the node distances and chamfer union depth,
+ * open volumes, pocket sealing, face fractions, occupancy, regions and held temperatures as
+ * device passes. Blocking. */
+int sprout_scene_rasterize_device(const SproutScene* s, float* sdf, float* solid4, uint32_t* region, float* temp,
+                                  int* heated);
 /* maps::fill_rect (maps.rs:466-492): rest-density particles of `material` in rect
  * (x0, y0, x1, y1, cells), skipping solids. `n_before` is the number of particles already
  * placed (it seeds the jitter, as out.len() does in the reference). Writes at most `cap`
@@ -163,6 +169,10 @@ int sprout_sim_set_params(SproutSim* sim, const SproutParams* p);
 /* FluidSim::set_solids (mod.rs:1976): arrays as sprout_scene_rasterize fills them. */
 int sprout_sim_set_solids(SproutSim* sim, const float* sdf, const float* solid4,
                           const uint32_t* region, const float* temp);
+/* FluidSim::set_solids with the scene rasterised on the device straight into the sim's
+ * buffers (no host arrays, no copies): what World::new does with Scene::rasterize and
+ * set_solids (world.rs), for a scene of the sim's grid size. Blocking. */
+int sprout_sim_set_scene(SproutSim* sim, const SproutScene* s);
 /* FluidSim::reset (mod.rs:1981-2002): replaces every particle (ids = index, spawn fields
  * settled). SPROUT_E_UNSUPPORTED if the tank needs a capability the engine lacks. */
 int sprout_sim_reset(SproutSim* sim, const SproutParticle* p, uint32_t n);

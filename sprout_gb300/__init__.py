@@ -47,6 +47,7 @@ EXPORTS = [
     "sprout_sim_get_launch", "sprout_sim_debug_stall", "sprout_batch_set_launch", "sprout_sim_request_stats",
     "sprout_sim_poll_stats", "sprout_pacer_new", "sprout_pacer_free", "sprout_pacer_reset", "sprout_pacer_speed",
     "sprout_pacer_plan", "sprout_device_count", "sprout_set_device", "sprout_get_device",
+    "sprout_scene_rasterize_device", "sprout_sim_set_scene",
 ]
 
 STAGES = ["advance", "sort", "p2g", "grid", "pressure", "project", "viscosity", "project2"]
@@ -136,6 +137,8 @@ def lib() -> C.CDLL:
         "sprout_scene_add_circle": ([V] + [C.c_float] * 4, C.c_int),
         "sprout_scene_sdf": ([V, C.c_float, C.c_float, P(C.c_float)], C.c_int),
         "sprout_scene_rasterize": ([V, V, V, V, V, P(C.c_int)], C.c_int),
+        "sprout_scene_rasterize_device": ([V, V, V, V, V, P(C.c_int)], C.c_int),
+        "sprout_sim_set_scene": ([V, V], C.c_int),
         "sprout_fill_rect": ([V, P(C.c_float), C.c_uint32, C.c_uint32, V, C.c_uint32, P(C.c_uint32)], C.c_int),
         "sprout_sim_create": ([C.c_uint32, C.c_uint32, C.c_uint32, V, P(V)], C.c_int),
         "sprout_sim_destroy": ([V], C.c_int), "sprout_sim_set_params": ([V, V], C.c_int),
@@ -295,16 +298,17 @@ class Scene:
         _check(lib().sprout_scene_sdf(self._h, x, y, C.byref(d)))
         return d.value
 
-    def rasterize(self):
-        """(sdf, solid[n,4], region, temp or None), as Scene::rasterize fills SolidField."""
+    def rasterize(self, device: bool = False):
+        """(sdf, solid[n,4], region, temp or None), as Scene::rasterize fills SolidField;
+        with `device` computed on the current CUDA device (the same fields, bit for bit)."""
         w, h = self.w, self.h
         sdf = np.zeros((h + 1) * (w + 1), np.float32)
         solid = np.zeros((h * w, 4), np.float32)
         region = np.zeros(h * w, np.uint32)
         temp = np.zeros(h * w, np.float32)
         heated = C.c_int()
-        _check(lib().sprout_scene_rasterize(self._h, sdf.ctypes.data, solid.ctypes.data, region.ctypes.data,
-                                            temp.ctypes.data, C.byref(heated)))
+        fn = lib().sprout_scene_rasterize_device if device else lib().sprout_scene_rasterize
+        _check(fn(self._h, sdf.ctypes.data, solid.ctypes.data, region.ctypes.data, temp.ctypes.data, C.byref(heated)))
         return sdf, solid, region, (temp if heated.value else None)
 
     def fill_rect(self, rect, material: int, existing: np.ndarray | None = None) -> np.ndarray:
@@ -345,6 +349,10 @@ class FluidSim:
         d = None if temp is None else np.ascontiguousarray(temp, np.float32)
         _check(lib().sprout_sim_set_solids(self._h, a.ctypes.data, b.ctypes.data, c.ctypes.data,
                                            None if d is None else d.ctypes.data))
+
+    def set_scene(self, scene: "Scene"):
+        """set_solids with the scene rasterised on the device, straight into the sim's buffers."""
+        _check(lib().sprout_sim_set_scene(self._h, scene._h))
 
     def reset(self, particles: np.ndarray):
         p = np.ascontiguousarray(particles, PARTICLE_DTYPE)

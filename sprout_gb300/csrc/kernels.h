@@ -92,6 +92,11 @@ struct BatchView {
 cudaError_t launch_pressure_batch(const BatchView& B, bool mixed, int blocks, size_t smem, cudaStream_t st, int second);
 int pressure_batch_blocks_max(int device, size_t smem, bool mixed);
 size_t pressure_batch_scalar_bytes();
+// Scene::rasterize on the device (raster.cu): the tank's solid fields straight into device
+// buffers, bit-identical to the host's Scene::rasterize (scene.cpp).
+struct Scene;
+cudaError_t rasterize_device(const Scene& sc, float* sdf, float4* solid, uint32_t* region, float* temp, bool* heated,
+                             cudaStream_t st);
 // Blocks of the persistent pressure kernel (plain or mixed precision) that fit on the
 // device at once.
 int pressure_blocks_max(int device, size_t smem, bool mixed);

@@ -1574,6 +1574,47 @@ int sprout_scene_rasterize(const SproutScene* s, float* sdf, float* solid4, uint
     if (heated) *heated = h ? 1 : 0;
     return SPROUT_OK;
 }
+
+int sprout_scene_rasterize_device(const SproutScene* s, float* sdf, float* solid4, uint32_t* region, float* temp, int* heated) {
+    if (!s || !sdf || !solid4 || !region) return fail(SPROUT_E_ARG, "null argument");
+    const int w = s->s.w, h = s->s.h;
+    const size_t nn = (size_t)(w + 1) * (h + 1), nc = (size_t)w * h;
+    float *dsdf = nullptr, *dtemp = nullptr;
+    float4* dsolid = nullptr;
+    uint32_t* dregion = nullptr;
+    cudaError_t e = cudaMalloc(&dsdf, nn * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc(&dsolid, nc * sizeof(float4));
+    if (e == cudaSuccess) e = cudaMalloc(&dregion, nc * sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMalloc(&dtemp, nc * sizeof(float));
+    bool hot = false;
+    if (e == cudaSuccess) e = rasterize_device(s->s, dsdf, dsolid, dregion, dtemp, &hot, nullptr);
+    if (e == cudaSuccess) e = cudaMemcpy(sdf, dsdf, nn * sizeof(float), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(solid4, dsolid, nc * sizeof(float4), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(region, dregion, nc * sizeof(uint32_t), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && hot && temp) e = cudaMemcpy(temp, dtemp, nc * sizeof(float), cudaMemcpyDeviceToHost);
+    for (void* p : {(void*)dsdf, (void*)dsolid, (void*)dregion, (void*)dtemp})
+        if (p) cudaFree(p);
+    if (e != cudaSuccess) return fail(SPROUT_E_CUDA, std::string("rasterising on the device: ") + cudaGetErrorString(e));
+    if (heated) *heated = hot ? 1 : 0;
+    return SPROUT_OK;
+}
+
+int sprout_sim_set_scene(SproutSim* sim, const SproutScene* s) {
+    if (!sim || !s) return fail(SPROUT_E_ARG, "null argument");
+    if (s->s.w != sim->W || s->s.h != sim->H) return fail(SPROUT_E_ARG, "the scene's grid is not the sim's");
+    CUDA_TRY(cudaStreamSynchronize(sim->stream));
+    bool hot = false;
+    cudaError_t e = rasterize_device(s->s, const_cast<float*>(sim->d.sdf), const_cast<float4*>(sim->d.solid),
+                                     const_cast<uint32_t*>(sim->d.region), const_cast<float*>(sim->d.solid_t), &hot,
+                                     sim->stream);
+    if (e != cudaSuccess) return fail(SPROUT_E_CUDA, std::string("rasterising on the device: ") + cudaGetErrorString(e));
+    if (!hot) {
+        std::vector<float> nt((size_t)sim->W * sim->H, NO_TEMP);
+        CUDA_TRY(cudaMemcpy((void*)sim->d.solid_t, nt.data(), nt.size() * sizeof(float), cudaMemcpyHostToDevice));
+    }
+    sim->solids_heated = hot;
+    return SPROUT_OK;
+}
 int sprout_fill_rect(const SproutScene* s, const float rect[4], uint32_t material, uint32_t n_before,
                      SproutParticle* out, uint32_t cap, uint32_t* n) {
     if (!s || !rect || !n) return fail(SPROUT_E_ARG, "null argument");
