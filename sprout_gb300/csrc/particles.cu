@@ -921,8 +921,10 @@ __global__ void __launch_bounds__(256) k_p2g(DevScene d) {
     const float dt = d.S->dt;
     const bool thermal = P->thermal != 0;
     const int ct = thermal ? (int)P->heat2[2] : -1;
+    // particle f of the tile's neighbourhood lies in row r: f only grows, so each thread's row
+    // search continues from where its previous particle was found
+    int r = 0;
     for (uint32_t f = threadIdx.x; f < total; f += blockDim.x) {
-        int r = 0;
         while (row_pre[r + 1] <= f) r++;
         uint32_t pi = row_beg[r] + (f - row_pre[r]);
         float4 q0 = d.part[3 * pi + 0], q1 = d.part[3 * pi + 1], q2 = d.part[3 * pi + 2];

@@ -439,9 +439,14 @@ constexpr int RN = RW * RW;
 struct Region {
     float dg[RN];
     float4 a[RN];
-    float2 u[RN], v[RN], w[RN];
-    float2 o1[NT], o2[NT];
-    float od[NT];
+    float2 u[RN], v[RN];
+    union {
+        float2 w[RN];   // a way up: each slot's coarse-grid value
+        struct {        // a way down fused with the CG update: the tile's own p, x and diagonal
+            float2 o1[NT], o2[NT];
+            float od[NT];
+        } o;
+    };
     float2 ring[32];   // the black cells just outside the tile, once computed (ring_cell)
 };
 DEV int rslot(int lx, int ly) { return (ly + RH) * RW + lx + RH; }
@@ -514,9 +519,9 @@ DEV void stage_down(const DevScene& d, const Lv& F, int t, const Rsrc<M>& R, boo
         const int cx = ox + (threadIdx.x & 15), cy = oy + (threadIdx.x >> 4);
         const bool in = l_inside(F, cx, cy);
         const int i = in ? l_at(F, cx, cy) : 0;
-        cp_async<4>(&rg.od[threadIdx.x], d.mgd + i, in);
-        cp_async<8>(&rg.o1[threadIdx.x], p + i, in);
-        cp_async<8>(&rg.o2[threadIdx.x], d.pres + i, in);
+        cp_async<4>(&rg.o.od[threadIdx.x], d.mgd + i, in);
+        cp_async<8>(&rg.o.o1[threadIdx.x], p + i, in);
+        cp_async<8>(&rg.o.o2[threadIdx.x], d.pres + i, in);
     }
 }
 
@@ -577,10 +582,10 @@ DEV void finish_down(const DevScene& d, const Lv& F, const Lv& C, int t, const R
                     z = black(k0);
                 }
             }
-            if (r_out && rg.od[cell] > 0.0f) {
+            if (r_out && rg.o.od[cell] > 0.0f) {
                 // cg_update.comp: x += alpha p, r -= alpha q (unknowns of active tiles)
-                const float2 pp = rg.o1[cell];
-                float2 x = rg.o2[cell];
+                const float2 pp = rg.o.o1[cell];
+                float2 x = rg.o.o2[cell];
                 x.x += R.ax * pp.x;
                 x.y += R.ay * pp.y;
                 d.pres[i] = x;
@@ -1205,6 +1210,7 @@ DEV void scal_stats(SolveState* G, const Solve<T>& K, int second, double true_re
 // mode 8/9: same matrix and hierarchy, density correction counted as solved).
 template <class M>
 __global__ void __launch_bounds__(NT, 2) k_mgpcg(DevScene d, int second, int scale_mode) {
+    grid_begin();
     using acc = typename M::acc;
     using acc4 = typename M::acc4;
     __shared__ TileCache tc;
@@ -1396,6 +1402,7 @@ size_t pressure_batch_smem(const Levels& lv) {
 
 template <class M>
 __global__ void __launch_bounds__(NT, 2) k_mgpcg_batch(BatchView B, int second) {
+    grid_begin();
     using acc = typename M::acc;
     using acc4 = typename M::acc4;
     __shared__ TileCache tc;

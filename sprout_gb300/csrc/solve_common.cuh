@@ -54,12 +54,24 @@ DEV unsigned long long global_ns() {
     return t;
 }
 
+// The number of grid barriers this block has passed in the current launch (one per block, in
+// shared memory; grid_begin sets it to zero at the start of every persistent kernel).
+DEV uint32_t& grid_epoch() {
+    __shared__ uint32_t epoch;
+    return epoch;
+}
+DEV void grid_begin() {
+    if (threadIdx.x == 0) grid_epoch() = 0u;
+    __syncthreads();
+}
+
 // Grid-wide barrier over the co-resident blocks of a cooperative launch: one arrival counter
-// that only grows (zeroed before each launch). Thread 0 of each block adds one; the value it
-// got tells which barrier this is, e = old / blocks, and it waits (bounded spin) until the
-// counter reaches (e + 1) x blocks, which the last block to arrive makes true with its own
-// add: releasing costs no store beyond the arrivals. Returns false (and every block leaves)
-// once any wait has run out.
+// that only grows (zeroed before each launch). At its e-th barrier (e counted by the block
+// itself) thread 0 of each block adds one without waiting for the old value and waits
+// (bounded spin) until the counter reaches (e + 1) x blocks, which the last block to arrive
+// makes true with its own add: releasing costs no store beyond the arrivals, and no block
+// waits for its arrival's round trip before it starts to poll. Returns false (and every
+// block leaves) once any wait has run out.
 DEV bool grid_sync(SolveState* K) {
     __shared__ int s_ok;
     __syncthreads();
@@ -68,6 +80,8 @@ DEV bool grid_sync(SolveState* K) {
         volatile uint32_t* vcnt = &K->bar_count;
         volatile uint32_t* verr = &K->error;
         unsigned long long* trace = K->trace;
+        const uint32_t epoch = grid_epoch();
+        grid_epoch() = epoch + 1u;
         if (*verr != 0u) {
             ok = 0;
         } else {
@@ -84,10 +98,9 @@ DEV bool grid_sync(SolveState* K) {
             const uint32_t base = trace ? *(volatile uint32_t*)&K->trace_base : 0u;
             // the arrival releases the block's writes (ordered before it by the block barrier
             // above; release is cumulative), the acquiring reads of the wait make the other
-            // blocks' writes visible to this block after the block barrier below
-            uint32_t old;
-            asm volatile("atom.add.release.gpu.u32 %0, [%1], 1;" : "=r"(old) : "l"(&K->bar_count) : "memory");
-            const uint32_t epoch = old / gridDim.x;
+            // blocks' writes visible to this block after the block barrier below; this
+            // thread's own add is ordered before its later loads of the same word
+            asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(&K->bar_count) : "memory");
             const uint32_t target = (epoch + 1u) * gridDim.x;
             unsigned long long* row = nullptr;
             if (trace && blockIdx.x + 1 < K->trace_cols) {

@@ -929,6 +929,7 @@ struct VSolve {
 // pressure solve changed the velocity since visc_setup).
 template <int NU>
 __global__ void __launch_bounds__(NT, 2) k_visc_solve(DevScene d, int restrain) {
+    grid_begin();
     __shared__ VSmem<NU> sm;
     __shared__ VScal K;
     __shared__ VTileCache tc;
@@ -1134,6 +1135,7 @@ DEV void vbatch_fill_cache(const VBatchView& B, VTileCache& tc) {
 
 template <int NU>
 __global__ void __launch_bounds__(NT, 2) k_visc_batch(VBatchView B) {
+    grid_begin();
     __shared__ VSmem<NU> sm;
     __shared__ VTileCache tc;
     __shared__ int s_run;
