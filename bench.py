@@ -442,6 +442,10 @@ def run_engine(args, rank, world, local, pg):
                  "pressure_iters_last": list(mst.pressure_iters), "pressure2_iters_last": mst.pressure2_iters,
                  "pressure_residual_max": mst.pressure_residual_max, "pressure_unconverged": mst.pressure_unconverged,
                  "pressure_true_residual_max_fp64": mst.pressure_true_residual_max,
+                 "refinement": {"residual_replacements": mst.pressure_replacements,
+                                "rule": "true residual b - A x (FP64 sums of the FP32 values) checked each time the "
+                                        "carried |r| falls 100x; adopted where it exceeds twice the carried one and "
+                                        "ten times the FP32 rounding floor eps |A| |x|"},
                  "storage": "BF16 couplings + FP32 row-sum-keeping diagonal on every level; FP32 vectors",
                  "dots": "FP64", "speedup_vs_plain": (ms / args.steps) / (mms / args.steps)}
     # ---- end to end through the public API, on a fresh copy over the same substeps ----------
@@ -470,12 +474,19 @@ def run_engine(args, rank, world, local, pg):
         # arm's last pressure system
         cb, _, _ = cpu_oracle_rate(tank)
         line["cpu_baseline"] = cb
-        from oracle.fp64_mgpcg import accuracy
+        from oracle.fp64_mgpcg import FP64MGPCG, accuracy
         acc = {}
         for name, s_ in [("plain", sim)] + ([("mixed", msim)] if mixed is not None else []):
             a = accuracy(s_.field("mga"), s_.field("mgd"), s_.field("prhs"), s_.field("pres"), tank.w, tank.h, columns=(0,))
-            acc[name] = {"pressure_error_vs_fp64": a[0]["error_vs_fp64"], "pressure_residual_fp64": a[0]["residual_fp64"]}
+            f = FP64MGPCG(s_.field("mga"), s_.field("mgd"), tank.w, tank.h)
+            b = np.asarray(s_.field("prhs"), np.float64).reshape(tank.h, tank.w, 4)[..., :2]
+            x64, _ = f.solve(b)
+            floor = float(f.residual(x64.astype(np.float32).astype(np.float64), b)[0])
+            acc[name] = {"pressure_error_vs_fp64": a[0]["error_vs_fp64"], "pressure_residual_fp64": a[0]["residual_fp64"],
+                         "fp32_floor": floor}
         acc["system"] = "the last pressure solve of each arm's tank, solved again by an FP64 MGPCG to 1e-12"
+        acc["fp32_floor"] = ("|b - A fl32(x*)| / |b|: the true residual that rounding the FP64 solution x* to FP32 "
+                             "leaves, the scale below which no FP32 iterate's true residual goes")
         line["accuracy"] = acc
     print(json.dumps(line), flush=True)
 

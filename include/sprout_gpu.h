@@ -89,6 +89,8 @@ typedef struct SproutSolverStats {
     float pressure_true_residual;      /* mixed precision: |b - A x| / |b| of the last solve's
                                           pressure evaluated in FP64 (0 in plain mode) */
     float pressure_true_residual_max;
+    uint32_t pressure_replacements;    /* mixed precision: times the carried residual was replaced
+                                          by b - A x evaluated in FP64 (cumulative) */
 } SproutSolverStats;
 
 typedef struct SproutParams SproutParams;   /* SimParams */
@@ -270,8 +272,11 @@ int sprout_sim_trace_read(SproutSim* sim, unsigned long long* out, size_t cap, s
  * arithmetic, FP32 throughout (the default). mode 1: mixed precision: the multigrid
  * hierarchy's matrices stored in BF16 (with an FP32 diagonal that keeps every row sum) and
  * computed in FP32; every vector, the CG iterate, residual and operator in FP32; the dot
- * products, step lengths and convergence test in FP64; at the end of each solve the true
- * residual b - A x evaluated in FP64 (stats: pressure_true_residual). Both stop at the same
+ * products, step lengths and convergence test in FP64; as refinement, each time the carried
+ * residual has fallen 100x the true residual b - A x is evaluated in FP64 and replaces the
+ * carried one where it exceeds it twice over and lies well above the FP32 rounding floor
+ * (stats: pressure_replacements); at the end of each solve the true residual is evaluated in
+ * FP64 (stats: pressure_true_residual). Both stop at the same
  * relative residual (pressure_tol) of the residual the iteration carries, as the reference
  * does. Takes effect from the next step; the first switch to mode 1 allocates the BF16
  * matrices. */

@@ -88,6 +88,7 @@ class SolverStats(C.Structure):
         ("device_error", C.c_uint32), ("h2d_bytes", C.c_uint64), ("d2h_bytes", C.c_uint64),
         ("viscosity_iters", C.c_uint32), ("viscosity_residual", C.c_float), ("pressure2_iters", C.c_uint32),
         ("pressure_true_residual", C.c_float), ("pressure_true_residual_max", C.c_float),
+        ("pressure_replacements", C.c_uint32),
     ]
 
 

@@ -125,7 +125,7 @@ struct SolveState {
     unsigned long long* trace;
     uint32_t trace_rows, trace_cols;
     uint32_t trace_base;   // barriers of the earlier launches (rows of later ones follow on)
-    uint32_t pad2;
+    uint32_t p_repl;       // mixed precision: residual replacements, all solves since the reset
     // failure injection for tests (0: off): block dbg_block arrives dbg_stall_ns late at every
     // grid barrier, and a wait gives up after dbg_spin_limit polls instead of SPIN_LIMIT
     uint32_t dbg_block, dbg_stall_ns, dbg_spin_limit, pad3;

@@ -155,8 +155,12 @@ struct Mixed {
 template <class T>
 struct Solve {
     T rz[2], alpha[2], beta[2], bb[2], rr[2];
+    T rmark;   // mixed precision: the pressure column's r.r at the last residual check
     uint32_t done[2], iters[2];
     uint32_t bad;   // a total was not finite: the solve stopped (SolveState ERR_DIVERGED)
+    uint32_t replaced;   // residual replacements in this solve
+    uint32_t floor_hit;  // a check found the carried residual near the FP32 rounding floor
+    uint32_t adopt;      // a batch: this iteration's check adopts the true residual
 };
 
 template <class A4>
@@ -1027,6 +1031,91 @@ DEV void true_residual_tile(const DevScene& d, int t, Dbl4* part, Dbl4* buf) {
     __syncthreads();
 }
 
+// The mixed solve's refinement (residual replacement: van der Vorst and Ye, "Residual
+// replacement strategies for Krylov subspace iterative methods", SIAM J. Sci. Comput. 22,
+// 2000). The recurrence r -= alpha q drifts from b - A x by rounding; at a few points of the
+// convergence the true residual of the current iterate is evaluated (the products and sums of
+// the FP32 values in FP64, rounded once to FP32) and, where the drift is worth removing, it
+// replaces the carried one; the iteration continues with its directions unchanged.
+//
+// check_tile: on level-0 tile t, the true residual b - A x of both columns into rt, and the
+// tile's sums of |b - A x|^2 and of (eps |A| |x|)^2 of the pressure column into part[t]: the
+// second is the size of the residual that rounding x to FP32 alone leaves (eps = 2^-24), below
+// which a replacement would feed that rounding back into the recurrence instead of removing
+// drift.
+DEV void check_tile(const DevScene& d, int t, float2* rt, Dbl4* part, Dbl4* buf) {
+    const Lv F = lev(d.lv, 0);
+    if (d.ptile[F.toff + t] == 0u) {
+        if (threadIdx.x == 0) part[t] = Dbl4{0.0, 0.0, 0.0, 0.0};
+        return;
+    }
+    const int2 og = tile_origin(F, t);
+    const int cx = og.x + (threadIdx.x & 15), cy = og.y + (threadIdx.x >> 4);
+    Dbl4 a4{0.0, 0.0, 0.0, 0.0};
+    if (l_inside(F, cx, cy)) {
+        const int i = l_at(F, cx, cy);
+        const float D = d.mgd[i];
+        if (D > 0.0f) {
+            const float4 w = d.mga[i];
+            const float2 x = d.pres[i];
+            const float4 b = d.prhs[i];
+            double rx = (double)b.x - (double)D * (double)x.x, ry = (double)b.y - (double)D * (double)x.y;
+            double ax = fabs((double)D * (double)x.x);
+            for (int q = 0; q < 4; q++) {
+                const int nx = cx + NBX[q], ny = cy + NBY[q];
+                if (unknown_op(d, F, nx, ny)) {
+                    const float2 xn = d.pres[l_at(F, nx, ny)];
+                    const double wq = (double)wcomp(w, q);
+                    rx += wq * (double)xn.x;
+                    ry += wq * (double)xn.y;
+                    ax += fabs(wq * (double)xn.x);
+                }
+            }
+            rt[i] = make_float2((float)rx, (float)ry);
+            const double fl = ax * 0x1p-24;
+            a4 = Dbl4{rx * rx, fl * fl, 0.0, 0.0};
+        } else {
+            rt[i] = make_float2(0.0f, 0.0f);
+        }
+    }
+    buf[threadIdx.x] = a4;
+    block_tree(buf);
+    if (threadIdx.x == 0) part[t] = buf[0];
+    __syncthreads();
+}
+
+// ... and, where it is adopted, the carried residual r of tile t replaced by it.
+DEV void adopt_tile(const DevScene& d, int t, const float2* rt, float2* r) {
+    const Lv F = lev(d.lv, 0);
+    if (d.ptile[F.toff + t] == 0u) return;
+    const int2 og = tile_origin(F, t);
+    const int cx = og.x + (threadIdx.x & 15), cy = og.y + (threadIdx.x >> 4);
+    if (!l_inside(F, cx, cy)) return;
+    const int i = l_at(F, cx, cy);
+    if (d.mgd[i] > 0.0f) r[i] = rt[i];
+}
+
+// When to check: each time the pressure column's carried r.r has fallen by kCheckDrop (its
+// norm by 100) since the start or the last check, before the solve has converged, unless a
+// check found the carried residual already near the rounding floor.
+// Whether to adopt: the true residual is more than twice the carried one (drift worth
+// removing) and more than ten times the rounding floor.
+constexpr double kCheckDrop = 1e-4;
+template <class T>
+DEV bool want_check(const Solve<T>& K) {
+    return K.done[0] == 0u && K.floor_hit == 0u && K.rr[0] > 0 && K.rr[0] <= (T)kCheckDrop * K.rmark;
+}
+// Decides from the check's totals (|b - A x|^2, floor^2); updates the marks. Returns adopt.
+template <class T>
+DEV bool decide_check(Solve<T>& K, const Dbl4& tot) {
+    K.rmark = K.rr[0];
+    const double carried = (double)K.rr[0];
+    if (carried <= 100.0 * tot.y) K.floor_hit = 1u;
+    const bool adopt = tot.x > 4.0 * carried && tot.x > 100.0 * tot.y;
+    if (adopt) K.replaced += 1u;
+    return adopt;
+}
+
 // cg_apply.comp on level-0 tile t: p = z + beta p_old, q = A p (the FP32 operator), the
 // tile's sum of p.q into part[n + t]. Copies (one ring around the tile is enough): the
 // operator's diagonal, z (u) and p_old (v, unless both betas are zero); the couplings of the
@@ -1127,6 +1216,10 @@ DEV void scal_start(Solve<T>& K, const A4& a, const A4& b, T tx, T ty, int secon
     K.rz[1] = a.y;
     K.rr[0] = a.z;
     K.rr[1] = a.w;
+    K.rmark = a.z;
+    K.replaced = 0u;
+    K.floor_hit = 0u;
+    K.adopt = 0u;
     K.beta[0] = K.beta[1] = 0;
     K.alpha[0] = K.alpha[1] = 0;
     K.iters[0] = K.iters[1] = 0u;
@@ -1180,6 +1273,7 @@ DEV void scal_stats(SolveState* G, const Solve<T>& K, int second, double true_re
         G->p_true_res = (float)true_rel;
         G->p_true_res_max = maxf(G->p_true_res_max, (float)true_rel);
     }
+    G->p_repl += K.replaced;
     for (int c = 0; c < 2; c++) {
         G->p_rz[c] = (float)K.rz[c];
         G->p_alpha[c] = (float)K.alpha[c];
@@ -1260,6 +1354,23 @@ __global__ void __launch_bounds__(NT, 2) k_mgpcg(DevScene d, int second, int sca
     const Lv L0 = lev(d.lv, 0);
     for (uint32_t it = 0; it < P->pressure_max_iters; it++) {
         if (K.done[0] && K.done[1]) break;
+        if constexpr (M::kMixed) {
+            // the refinement (the same decisions in every block: the same K); q is free until
+            // the apply phase rewrites it, and the partials' second half until it sums p.q
+            if (it > 0 && want_check(K)) {
+                Dbl4* pc = d.partials64 + n;
+                for_active(d, 0, tc, [&](int t) { check_tile(d, t, d.cgq, pc, reinterpret_cast<Dbl4*>(buf)); });
+                if (!grid_sync(d.K)) return;
+                const Dbl4 tot = total(pc, n, reinterpret_cast<Dbl4*>(buf));
+                __shared__ int s_adopt;
+                if (threadIdx.x == 0) s_adopt = decide_check(K, tot) ? 1 : 0;
+                __syncthreads();
+                if (s_adopt) {
+                    for_active(d, 0, tc, [&](int t) { adopt_tile(d, t, d.cgq, r_cur); });
+                    if (!grid_sync(d.K)) return;
+                }
+            }
+        }
         const float b0 = (float)K.beta[0], b1 = (float)K.beta[1];
         const bool nob = b0 == 0.0f && b1 == 0.0f;
         pipe_active(d, 0, tc, rg, [&](int t, Region& r) { stage_apply(d, L0, t, nob, p_old, r); },
@@ -1538,6 +1649,38 @@ __global__ void __launch_bounds__(NT, 2) k_mgpcg_batch(BatchView B, int second) 
         }
         __syncthreads();
         if (!s_run) break;
+        if constexpr (M::kMixed) {   // the refinement, as the single-scene solve takes it
+            // a scene checks at iteration it when want_check holds at the top of the iteration;
+            // one block decides (after the check's barrier) and leaves the outcome in KS[s].adopt
+            auto chk = [&](int s) { return it > 0 && running(s, it) && want_check(KS[s]); };
+            if (threadIdx.x == 0) {
+                int any = 0;
+                for (int s = 0; s < B.ns && !any; s++) any = chk(s) ? 1 : 0;
+                s_run = any;
+            }
+            __syncthreads();
+            if (s_run) {
+                for_active_b(B, 0, tc, [&](int s, const DevScene& d, int t) {
+                    if (chk(s)) check_tile(d, t, d.cgq, d.partials64 + d.nwg, reinterpret_cast<Dbl4*>(buf));
+                });
+                if (!grid_sync(BK)) return;
+                // each scene's decision by one block (it alone writes KS[s] until the next barrier)
+                for (int s = blockIdx.x; s < B.ns; s += gridDim.x) {
+                    if (!chk(s)) continue;
+                    const DevScene& d = B.scenes[s];
+                    const Dbl4 tot = total(d.partials64 + d.nwg, d.nwg, reinterpret_cast<Dbl4*>(buf));
+                    if (threadIdx.x == 0) KS[s].adopt = decide_check(KS[s], tot) ? 1u : 0u;
+                    __syncthreads();
+                }
+                if (!grid_sync(BK)) return;
+                for_active_b(B, 0, tc, [&](int s, const DevScene& d, int t) {
+                    if (KS[s].adopt) adopt_tile(d, t, d.cgq, parity_r(d, it));
+                });
+                if (!grid_sync(BK)) return;
+                for (int s = blockIdx.x; s < B.ns; s += gridDim.x)
+                    if (threadIdx.x == 0) KS[s].adopt = 0u;
+            }
+        }
         pipe_active_b(
             B, 0, tc, rg,
             [&](int s, const DevScene& d, int t, Region& r) {

@@ -1973,6 +1973,7 @@ int sprout_sim_stats(SproutSim* sim, SproutSolverStats* o) {
     o->pressure2_iters = K.p2_iters;
     o->pressure_true_residual = K.p_true_res;
     o->pressure_true_residual_max = K.p_true_res_max;
+    o->pressure_replacements = K.p_repl;
     o->viscosity_residual = K.v_r0 > 0.0f ? std::sqrt(K.v_rr / K.v_r0) : 0.0f;
     o->h2d_bytes = sim->h2d_bytes;
     o->d2h_bytes = sim->d2h_bytes;

@@ -102,3 +102,22 @@ def test_mixed_runs_the_full_physics_pour():
     assert am[0]["residual_fp64"] <= 4.0 * max(ap[0]["residual_fp64"], floor), (am, ap, floor)
     assert am[0]["error_vs_fp64"] <= 4.0 * max(ap[0]["error_vs_fp64"], 1e-5), (am, ap)
     assert abs(sm.pressure_true_residual - am[0]["residual_fp64"]) <= 1e-3 * am[0]["residual_fp64"] + 1e-9
+
+
+def test_refinement_keeps_the_plain_arms_true_residual():
+    """The refinement (residual replacement, checked against the FP32 rounding floor) leaves
+    the mixed solve converged to the reference's tolerance, with a true residual within 2x of
+    the plain solve's, or of the floor where that is larger: a replacement is adopted only
+    well above the floor, so none can have pushed the residual there."""
+    t = tanks.dam_break(256, 144)
+    plain, mixed = pair(t)
+    for s in (plain, mixed):
+        s.step(16, 16 / 240.0)
+    sm = mixed.stats()
+    assert sm.device_error == 0 and sm.pressure_unconverged == 0 and sm.pressure2_unconverged == 0
+    assert sm.pressure_residual_max <= 1e-5 * 1.0001
+    am = last_system_accuracy(mixed, t, (0,))
+    ap = last_system_accuracy(plain, t, (0,))
+    floor = fp32_floor(mixed, t)
+    assert am[0]["residual_fp64"] <= 2.0 * max(ap[0]["residual_fp64"], floor), (am, ap, floor)
+    assert plain.stats().pressure_replacements == 0   # the plain arm is the reference's arithmetic
