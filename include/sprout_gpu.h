@@ -200,6 +200,48 @@ int sprout_sim_spawn(SproutSim* sim, const SproutParticle* p, uint32_t n, uint32
  * grid (the reference asserts) or cap < *cells. */
 int sprout_sim_cell_counts(SproutSim* sim, const int32_t lo[2], const int32_t hi[2], uint32_t* out,
                            size_t cap, size_t* cells);
+
+/* ---- the brush's emitters on the device ------------------------------------------------
+ * World::emit's sources (world.rs:609-727) with brush.rs's geometry, replacing the host's
+ * candidates + FluidSim::cell_counts (a blocking read-back) + Admission + FluidSim::spawn:
+ * the candidates are laid out, tested against the solids (World::solid_distance, from the
+ * sim's own node distances) and admitted against the live particles of each cell on the
+ * device, in the order World::emit takes them, and queued into particle slots with the ids
+ * and the per-step cap FluidSim::spawn gives. Nothing is read back: the calls return once
+ * the work is queued on the sim's stream. The material row joins the tank as a spawn of it
+ * would (also when no candidate is admitted). World::rand's generator (seeded 0x12345678 as
+ * World::new does) and the next particle id live on the device from the first emission on.
+ * Particles queued by sprout_sim_spawn before an emission take their ids first. A sim in a
+ * batch takes no emission (SPROUT_E_ARG). */
+typedef struct SproutSpout {   /* brush::Spout (brush.rs:18-23) */
+    float direction[2];
+    float speed;               /* cells / s */
+    float width;               /* cells */
+} SproutSpout;
+/* Spout::pour (kind 0), Spout::jet (1), Spout::faucet (2) (brush.rs:28-47); `degrees`
+ * clockwise from straight down (jet and faucet), `rate` particles / s, `radius` cells. */
+int sprout_spout(int kind, float degrees, float rate, float radius, SproutSpout* out);
+/* World::stream (world.rs:714-727) with Stream::advance (brush.rs:86-115): the particles of
+ * the spout's lattice that appear during `seconds` while the brush moves from `from` to
+ * `to`, launched at the spout's velocity where no solid or full cell (1.5 x rest density)
+ * holds them back. *stream_time is brush::Stream's state (simulated seconds the stream has
+ * run; 0 for a new stroke), advanced by `seconds`. */
+int sprout_sim_emit_stream(SproutSim* sim, const SproutSpout* spout, double* stream_time, const float from[2],
+                           const float to[2], float seconds, uint32_t material);
+/* World::paint (world.rs:644-685): up to `count` particles on the rest-density lattice (or,
+ * with `spray`, the sparse spray lattice, jittered, launched outwards from the stroke,
+ * brush::spray_velocity) inside the stroke of `radius` from `from` to `to`, in empty cells
+ * only, in World::rand's shuffled order. World::stamp is from == to with count 32768. */
+int sprout_sim_emit_paint(SproutSim* sim, const float from[2], const float to[2], float radius, uint32_t count,
+                          int spray, uint32_t material);
+/* World::rain (world.rs:689-710): `count` drops drawn in the cloud 3 radii either side of
+ * `at`, falling at brush::RAIN_SPEED, where they find an empty cell. */
+int sprout_sim_emit_rain(SproutSim* sim, const float at[2], float radius, uint32_t count, uint32_t material);
+/* Sets World::rand's state on the device (blocking). */
+int sprout_sim_emitter_seed(SproutSim* sim, uint32_t rng);
+/* The particles the emitters have queued since the sim was made (and the last emission's),
+ * read back (blocking): what World::emit returns, for a caller that wants it. */
+int sprout_sim_emitted(SproutSim* sim, uint64_t* total, uint32_t* last);
 /* Stats (src/sim/mod.rs:130-136): live particles and, per material row, its particles and the
  * sum of their concentrations (in particles, a multiple of 1/256). */
 #define SPROUT_MATERIAL_ROWS 96

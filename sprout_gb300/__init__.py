@@ -47,7 +47,8 @@ EXPORTS = [
     "sprout_sim_get_launch", "sprout_sim_debug_stall", "sprout_batch_set_launch", "sprout_sim_request_stats",
     "sprout_sim_poll_stats", "sprout_pacer_new", "sprout_pacer_free", "sprout_pacer_reset", "sprout_pacer_speed",
     "sprout_pacer_plan", "sprout_device_count", "sprout_set_device", "sprout_get_device",
-    "sprout_scene_rasterize_device", "sprout_sim_set_scene",
+    "sprout_scene_rasterize_device", "sprout_sim_set_scene", "sprout_spout", "sprout_sim_emit_stream",
+    "sprout_sim_emit_paint", "sprout_sim_emit_rain", "sprout_sim_emitter_seed", "sprout_sim_emitted",
 ]
 
 STAGES = ["advance", "sort", "p2g", "grid", "pressure", "project", "viscosity", "project2"]
@@ -90,6 +91,25 @@ class SolverStats(C.Structure):
         ("pressure_true_residual", C.c_float), ("pressure_true_residual_max", C.c_float),
         ("pressure_replacements", C.c_uint32),
     ]
+
+
+class Spout(C.Structure):
+    """SproutSpout: brush::Spout (direction, speed cells/s, width cells)."""
+    _fields_ = [("direction", C.c_float * 2), ("speed", C.c_float), ("width", C.c_float)]
+
+    @staticmethod
+    def make(kind: str, rate: float, radius: float, degrees: float = 0.0) -> "Spout":
+        """Spout::pour / jet / faucet."""
+        s = Spout()
+        _check(lib().sprout_spout({"pour": 0, "jet": 1, "faucet": 2}[kind], degrees, rate, radius, C.byref(s)))
+        return s
+
+
+class StreamState:
+    """brush::Stream: simulated seconds the stream has run (0 for a new stroke)."""
+
+    def __init__(self, time: float = 0.0):
+        self.time = time
 
 
 class Launch(C.Structure):
@@ -155,6 +175,12 @@ def lib() -> C.CDLL:
         "sprout_sim_sync": ([V], C.c_int),
         "sprout_sim_spawn": ([V, V, C.c_uint32, P(C.c_uint32)], C.c_int),
         "sprout_sim_cell_counts": ([V, P(C.c_int32), P(C.c_int32), V, C.c_size_t, P(C.c_size_t)], C.c_int),
+        "sprout_spout": ([C.c_int, C.c_float, C.c_float, C.c_float, V], C.c_int),
+        "sprout_sim_emit_stream": ([V, V, P(C.c_double), P(C.c_float), P(C.c_float), C.c_float, C.c_uint32], C.c_int),
+        "sprout_sim_emit_paint": ([V, P(C.c_float), P(C.c_float), C.c_float, C.c_uint32, C.c_int, C.c_uint32], C.c_int),
+        "sprout_sim_emit_rain": ([V, P(C.c_float), C.c_float, C.c_uint32, C.c_uint32], C.c_int),
+        "sprout_sim_emitter_seed": ([V, C.c_uint32], C.c_int),
+        "sprout_sim_emitted": ([V, P(C.c_uint64), P(C.c_uint32)], C.c_int),
         "sprout_sim_download_particles": ([V, V, C.c_uint32, P(C.c_uint32)], C.c_int),
         "sprout_sim_download_pressure": ([V, V], C.c_int),
         "sprout_sim_download_field": ([V, C.c_char_p, V, C.c_size_t, P(C.c_size_t)], C.c_int),
@@ -401,6 +427,32 @@ class FluidSim:
         if n.value:
             _check(lib().sprout_sim_cell_counts(self._h, a, b, out.ctypes.data, n.value, C.byref(n)))
         return out.reshape(max(hi[1] - lo[1], 0), max(hi[0] - lo[0], 0))
+
+    # ---- the brush's emitters on the device (World::emit without a read-back) -------------
+    def emit_stream(self, spout: "Spout", stream: "StreamState", frm, to, seconds: float, material: int):
+        """World::stream: the frame's particles of the spout's stream, admitted on the device."""
+        t = C.c_double(stream.time)
+        _check(lib().sprout_sim_emit_stream(self._h, C.byref(spout), C.byref(t), (C.c_float * 2)(*frm),
+                                            (C.c_float * 2)(*to), seconds, material))
+        stream.time = t.value
+
+    def emit_paint(self, frm, to, radius: float, count: int, spray: bool, material: int):
+        """World::paint (stamp: frm == to, count 32768; spray: the sparse launched lattice)."""
+        _check(lib().sprout_sim_emit_paint(self._h, (C.c_float * 2)(*frm), (C.c_float * 2)(*to), radius, count,
+                                           1 if spray else 0, material))
+
+    def emit_rain(self, at, radius: float, count: int, material: int):
+        """World::rain: `count` drops from the cloud around `at`."""
+        _check(lib().sprout_sim_emit_rain(self._h, (C.c_float * 2)(*at), radius, count, material))
+
+    def emitter_seed(self, rng: int):
+        _check(lib().sprout_sim_emitter_seed(self._h, rng & 0xFFFFFFFF))
+
+    def emitted(self) -> tuple[int, int]:
+        """(particles the emitters have queued in all, in the last emission); blocking."""
+        t, last = C.c_uint64(), C.c_uint32()
+        _check(lib().sprout_sim_emitted(self._h, C.byref(t), C.byref(last)))
+        return t.value, last.value
 
     def step(self, substeps: int, target: float = 0.0, tool: Tool | None = None):
         _check(lib().sprout_sim_step(self._h, substeps, target, None if tool is None else C.byref(tool)))

@@ -93,6 +93,28 @@ __global__ void __launch_bounds__(CLAIM_BLOCK) k_claim_place(float4* part, uint3
     part[3 * id + 2] = spawn[3 * r + 2];
 }
 
+// k_claim_place with its entries counted on the device: entries skip .. st->count of spawn.
+__global__ void __launch_bounds__(CLAIM_BLOCK) k_claim_place_dev(float4* part, uint32_t n_slots, const uint32_t* blk,
+                                                                 const float4* spawn, const EmitState* st,
+                                                                 uint32_t skip) {
+    __shared__ uint32_t warp_n[CLAIM_BLOCK / 32];
+    const uint32_t claim = st->count > skip ? st->count - skip : 0u;
+    const uint32_t id = blockIdx.x * CLAIM_BLOCK + threadIdx.x;
+    const bool dead = id < n_slots && kind_of(part, id) == KIND_DEAD;
+    const uint32_t bal = __ballot_sync(0xffffffffu, dead);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) warp_n[wid] = __popc(bal);
+    __syncthreads();
+    if (!dead) return;
+    uint32_t r = blk[blockIdx.x] + __popc(bal & ((1u << lane) - 1u));
+    for (int w = 0; w < wid; w++) r += warp_n[w];
+    if (r >= claim) return;
+    const float4* e = spawn + 3 * (size_t)(skip + r);
+    part[3 * id + 0] = e[0];
+    part[3 * id + 1] = e[1];
+    part[3 * id + 2] = e[2];
+}
+
 // count.comp:17-23: live particles (a material in the low byte of kind) per cell of the window
 // at origin (ox, oy) of sw x sh cells, row by row. Integer atomics: the counts do not depend on
 // the order of the adds.
@@ -160,6 +182,15 @@ void launch_claim(float4* part, uint32_t n_slots, const float4* spawn, uint32_t 
     k_claim_count<<<nb, CLAIM_BLOCK, 0, st>>>(part, n_slots, scratch);
     k_claim_scan<<<1, CLAIM_SCAN, 0, st>>>(scratch, nb);
     k_claim_place<<<nb, CLAIM_BLOCK, 0, st>>>(part, n_slots, scratch, spawn, claim);
+}
+
+void launch_claim_dev(float4* part, uint32_t n_slots, const float4* spawn, const EmitState* est, uint32_t skip,
+                      uint32_t* scratch, cudaStream_t st) {
+    if (n_slots == 0) return;
+    const int nb = (int)((n_slots + CLAIM_BLOCK - 1) / CLAIM_BLOCK);
+    k_claim_count<<<nb, CLAIM_BLOCK, 0, st>>>(part, n_slots, scratch);
+    k_claim_scan<<<1, CLAIM_SCAN, 0, st>>>(scratch, nb);
+    k_claim_place_dev<<<nb, CLAIM_BLOCK, 0, st>>>(part, n_slots, scratch, spawn, est, skip);
 }
 
 void launch_cell_counts(const float4* part, uint32_t n_slots, int ox, int oy, int sw, int sh, uint32_t* out,

@@ -101,6 +101,7 @@ struct StepState {
     uint32_t region_air;  // bit per region holding a cell without liquid (grid_prep.comp)
     uint32_t n_live;      // live particles after the last sort
     float corr_gain;      // min(1 - exp(-dt / tau), density_k): rhs.comp:79
+    float emit_speed;     // fastest particle the device emitters queued for the next step call
 };
 
 // SolveBuf (common.glsl:138-149): pressure scalars and statistics.

@@ -42,6 +42,43 @@ void launch_claim(float4* part, uint32_t n_slots, const float4* spawn, uint32_t 
                   cudaStream_t st);
 void launch_cell_counts(const float4* part, uint32_t n_slots, int ox, int oy, int sw, int sh, uint32_t* out,
                         cudaStream_t st);
+// The same claim with the entry count on the device: entries spawn[skip ..] of *count.
+struct EmitState;
+void launch_claim_dev(float4* part, uint32_t n_slots, const float4* spawn, const EmitState* st, uint32_t skip,
+                      uint32_t* scratch, cudaStream_t s);
+// The brush's emitters on the device (emit.cu). EmitArgs: one emission as World::emit issues it
+// (host-computed bounds and constants); EmitState: the emitters' device state (World::rand's
+// generator, the next particle id, particles queued since the last step call, this
+// emission's count and the running total).
+constexpr int EMIT_STREAM = 0, EMIT_PAINT = 1, EMIT_RAIN = 2;
+struct EmitArgs {
+    int mode, W, H, ppc;
+    float from[2], to[2];
+    // stream: the spout and the frame's range of lattice indices [k0, k0 + ncand)
+    float dir[2], speed, width, vel[2];
+    double start, end, rate;
+    uint64_t k0;
+    uint32_t ncand, keep;
+    // paint: the stroke's lattice bounds; rain: the cloud
+    float radius, spacing, at[2], half;
+    int lat_lo[2], lat_hi[2];
+    uint32_t count, spray, limit;
+    // the admission window [win_lo, win_lo + win_size)
+    int win_lo[2], win_size[2];
+    // the settled template particle
+    float s, t;
+    uint32_t kind;
+};
+struct EmitState {
+    uint32_t rng, next_id, queued, count;
+    unsigned long long total;
+};
+void launch_emit(const EmitArgs& a, float2* cand, uint8_t* flag, uint32_t* room, const float* sdf, float4* q,
+                 EmitState* st, StepState* S, cudaStream_t s);
+void launch_emit_fresh(float4* part, uint32_t base, uint32_t fresh, const float4* q, const EmitState* st,
+                       cudaStream_t s);
+void launch_spawn_ids(float4* part, uint32_t base, uint32_t fresh, float4* q, uint32_t n, EmitState* st,
+                      cudaStream_t s);
 // stats.comp: the census of the particle slots into out (stats_words() words, zeroed first):
 // live particles, per material row its particles and their concentration in 1/256.
 constexpr int kStatsRows = 96;   // the material table's rows (MAX_MATERIALS)

@@ -28,7 +28,7 @@ __global__ void k_step(DevScene d) {
     const DevParams* P = d.P;
     StepState* S = d.S;
     float u = maxf(minf(__uint_as_float(S->umax_grid), P->ext[0]), __uint_as_float(S->umax_part));
-    u = maxf(u, P->ext_speed);
+    u = maxf(maxf(u, P->ext_speed), S->emit_speed);
     float dt_cfl = P->cfl / (u + sqrtf(5.0f * maxf(P->gravity, 0.0f)) + 1e-6f);
     float dt;
     if (P->dt_fixed > 0.0f) {

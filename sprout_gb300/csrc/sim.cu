@@ -107,6 +107,7 @@ struct SproutSim {
         if (trace_buf) cudaFree(trace_buf);
         if (d_window) cudaFree(d_window);
         if (h_window) cudaFreeHost(h_window);
+        for (void* p : emit_bufs) cudaFree(p);
         drop_part_graphs();
         if (cap_stream) cudaStreamDestroy(cap_stream);
         if (stage_params) cudaFreeHost(stage_params);
@@ -488,6 +489,7 @@ struct SproutSim {
         CUDA_TRY(cudaEventElapsedTime(ms, a, b));
         cudaEventDestroy(a);
         cudaEventDestroy(b);
+        if ((rc = end_emit_call()) != SPROUT_OK) return rc;
         return check_device_error();
     }
 
@@ -505,6 +507,7 @@ struct SproutSim {
         CUDA_TRY(cudaEventSynchronize(ev[kStages]));
         for (int k = 0; k < kStages; k++) CUDA_TRY(cudaEventElapsedTime(&ms[k], ev[k], ev[k + 1]));
         for (auto& e : ev) cudaEventDestroy(e);
+        if ((rc = end_emit_call()) != SPROUT_OK) return rc;
         return check_device_error();
     }
 
@@ -736,6 +739,11 @@ struct SproutSim {
         n_slots = n;
         next_id = n;
         pending.clear();
+        if (d_emit) {
+            const uint32_t w2[2] = {n, 0u};   // next_id, queued
+            CUDA_TRY(cudaMemcpyAsync(&d_emit->next_id, w2, sizeof w2, cudaMemcpyHostToDevice, stream));
+            CUDA_TRY(cudaStreamSynchronize(stream));
+        }
         spawn_speed = 0.0f;
         was_reset = true;
         d.stride = std::max(tank.stride, 8);
@@ -818,6 +826,7 @@ struct SproutSim {
         if (pending.empty()) return SPROUT_OK;
         const uint32_t n = (uint32_t)pending.size();
         const uint32_t fresh = std::min(n, capacity - n_slots);
+        const uint32_t base = n_slots;
         if (fresh > 0) {
             CUDA_TRY(cudaMemcpyAsync(d.part + 3 * (size_t)n_slots, pending.data(), (size_t)fresh * sizeof(SproutParticle),
                                      cudaMemcpyHostToDevice, stream));
@@ -834,11 +843,132 @@ struct SproutSim {
             CUDA_TRY(cudaMemcpyAsync(d_spawn, pending.data() + fresh, (size_t)claim * sizeof(SproutParticle),
                                      cudaMemcpyHostToDevice, stream));
             h2d_bytes += (size_t)claim * sizeof(SproutParticle);
-            launch_claim(d.part, n_slots, d_spawn, claim, d_claim, stream);
+        }
+        // once the device emitters have run, the device holds the next id: the queue takes
+        // its ids there, in call order after what the emitters queued
+        if (ids_on_device) launch_spawn_ids(d.part, base, fresh, d_spawn, n, d_emit, stream);
+        if (n > fresh) {
+            launch_claim(d.part, n_slots, d_spawn, n - fresh, d_claim, stream);
             CUDA_TRY(cudaGetLastError());
         }
         // the copies read the queue from pageable memory, which they have finished with on return
         pending.clear();
+        return SPROUT_OK;
+    }
+
+    // ---- the brush's emitters on the device (emit.cu) ----
+    static constexpr int kPPC = 4;   // sim::PPC
+    EmitState* d_emit = nullptr;     // allocated by the first emission
+    bool ids_on_device = false;
+    float2* d_cand = nullptr;
+    uint8_t* d_cflag = nullptr;
+    size_t cand_cap = 0;
+    uint32_t* d_room = nullptr;
+    size_t room_cap = 0;
+    std::vector<void*> emit_bufs;    // the grown buffers above, freed with the sim
+
+    template <class T>
+    int grow(T** p, size_t* cap, size_t n) {
+        if (n <= *cap && *p) return SPROUT_OK;
+        if (*p) {
+            CUDA_TRY(cudaStreamSynchronize(stream));
+            cudaFree(*p);
+            emit_bufs.erase(std::remove(emit_bufs.begin(), emit_bufs.end(), (void*)*p), emit_bufs.end());
+            *p = nullptr;
+        }
+        const size_t m = std::max<size_t>(n, 1024);
+        if (cudaMalloc((void**)p, m * sizeof(T)) != cudaSuccess) return fail(SPROUT_E_NOMEM, "emitter buffers");
+        emit_bufs.push_back((void*)*p);
+        *cap = m;
+        return SPROUT_OK;
+    }
+
+    // World::admission's window (world.rs:729-736): Admission::window (brush.rs:219-224)
+    // clamped to the grid
+    void window_of(const float from[2], const float to[2], float margin, EmitArgs& a) const {
+        int lo[2], hi[2];
+        for (int c = 0; c < 2; c++) {
+            lo[c] = (int)std::floor(std::min(from[c], to[c]) - margin);
+            hi[c] = (int)std::ceil(std::max(from[c], to[c]) + margin) + 1;
+        }
+        const int g[2] = {W, H};
+        for (int c = 0; c < 2; c++) {
+            lo[c] = std::min(std::max(lo[c], 0), g[c]);
+            hi[c] = std::min(std::max(hi[c], lo[c]), g[c]);
+            a.win_lo[c] = lo[c];
+            a.win_size[c] = hi[c] - lo[c];
+        }
+    }
+
+    // One emission: the template of the material (Particle::new + settle_spawn), the tank
+    // taking the material's row as spawn does, the window's counts, the kernels, the
+    // placement into `upper` fresh slots reserved for it (or dead ones). Nothing is read back.
+    int emit(EmitArgs& a, uint32_t material, uint32_t upper, uint32_t* reserved) {
+        if (reserved) *reserved = 0;
+        if (!was_reset) return fail(SPROUT_E_ARG, "emit before reset");
+        if (batch) return fail(SPROUT_E_ARG, "the sim belongs to a batch: emit into sims outside a batch");
+        if (material >= (uint32_t)kMaxMaterials) return fail(SPROUT_E_ARG, "no such material row");
+        SproutParticle p{};
+        p.pos[0] = 0.5f * (float)W;
+        p.pos[1] = 0.5f * (float)H;
+        p.s = -1.0f;           // SPAWN_S
+        p.t = -1.0e4f;         // SPAWN_TEMP
+        p.kind = material + 1u;
+        int rc = settle(p, 0);
+        if (rc != SPROUT_OK) return rc;
+        bool present[kMaxMaterials] = {};
+        for (int r : tank.rows) present[r] = true;
+        const size_t before = tank.rows.size();
+        bool th = thermal;
+        mark_materials(&p, 1, present, &th);
+        size_t after = 0;
+        for (int r = 0; r < kMaxMaterials; r++) after += present[r] ? 1 : 0;
+        if (after != before || th != thermal) {
+            rc = set_tank(present, th);
+            if (rc == SPROUT_E_CAPACITY) return SPROUT_OK;   // the material does not fit: nothing is emitted
+            if (rc != SPROUT_OK) return rc;
+        }
+        // what the host queued so far goes first (ids in call order)
+        if ((rc = take_spawns()) != SPROUT_OK) return rc;
+        if (!d_emit) {
+            if ((rc = alloc(&d_emit, 1)) != SPROUT_OK) return rc;
+            EmitState e{};
+            e.rng = 0x12345678u;   // World::new (world.rs:181)
+            CUDA_TRY(cudaMemcpyAsync(d_emit, &e, sizeof e, cudaMemcpyHostToDevice, stream));
+            CUDA_TRY(cudaStreamSynchronize(stream));
+        }
+        if (!ids_on_device) {
+            CUDA_TRY(cudaMemcpyAsync(&d_emit->next_id, &next_id, sizeof(uint32_t), cudaMemcpyHostToDevice, stream));
+            CUDA_TRY(cudaStreamSynchronize(stream));
+            ids_on_device = true;
+        }
+        if (!d_spawn) {
+            if ((rc = alloc(&d_spawn, 3 * (size_t)kSpawnMax)) != SPROUT_OK) return rc;
+            if ((rc = alloc(&d_claim, claim_scratch_words(capacity))) != SPROUT_OK) return rc;
+        }
+        a.W = W;
+        a.H = H;
+        a.ppc = kPPC;
+        a.s = p.s;
+        a.t = p.t;
+        a.kind = p.kind;
+        a.limit = kSpawnMax;
+        const size_t nwin = (size_t)a.win_size[0] * a.win_size[1];
+        if ((rc = grow(&d_cand, &cand_cap, a.ncand)) != SPROUT_OK) return rc;
+        size_t fcap = cand_cap;
+        if ((rc = grow(&d_cflag, &fcap, a.ncand)) != SPROUT_OK) return rc;
+        if ((rc = grow(&d_room, &room_cap, nwin + (a.mode == EMIT_PAINT ? a.ncand : 0))) != SPROUT_OK) return rc;
+        launch_cell_counts(d.part, n_slots, a.win_lo[0], a.win_lo[1], a.win_size[0], a.win_size[1], d_room, stream);
+        launch_emit(a, d_cand, d_cflag, d_room, d.sdf, d_spawn, d_emit, const_cast<StepState*>(d.S), stream);
+        upper = std::min(upper, kSpawnMax);
+        const uint32_t fresh = std::min(upper, capacity - n_slots);
+        const uint32_t base = n_slots;
+        launch_emit_fresh(d.part, base, fresh, d_spawn, d_emit, stream);
+        n_slots += fresh;
+        if (upper > fresh) launch_claim_dev(d.part, n_slots, d_spawn, d_emit, fresh, d_claim, stream);
+        CUDA_TRY(cudaGetLastError());
+        emitted = true;
+        if (reserved) *reserved = fresh;
         return SPROUT_OK;
     }
 
@@ -925,6 +1055,10 @@ struct SproutSim {
             if (rc != SPROUT_OK) return rc;
             enqueued = true;
         }
+        if (d_emit) {   // the queue's per-step count (record clears pending_spawn)
+            CUDA_TRY(cudaMemsetAsync(&d_emit->queued, 0, sizeof(uint32_t), stream));
+            enqueued = true;
+        }
         if (n_slots == 0 || tank.rows.empty()) return fail(SPROUT_E_ARG, "step before reset (no particles)");
         int rc = derive_viscosity();
         if (rc != SPROUT_OK) return rc;
@@ -964,6 +1098,15 @@ struct SproutSim {
             else record_substep(stream);
         }
         CUDA_TRY(cudaGetLastError());
+        return end_emit_call();
+    }
+    // The fastest particle the device emitters queued raises the CFL limit of one step call,
+    // as spawn_speed does (mod.rs:2300): cleared after the call's substeps.
+    bool emitted = false;
+    int end_emit_call() {
+        if (!emitted) return SPROUT_OK;
+        CUDA_TRY(cudaMemsetAsync(&d.S->emit_speed, 0, sizeof(float), stream));
+        emitted = false;
         return SPROUT_OK;
     }
 
@@ -1823,6 +1966,144 @@ int sprout_sim_spawn(SproutSim* sim, const SproutParticle* p, uint32_t n, uint32
     if (!sim || !accepted || (!p && n > 0)) return fail(SPROUT_E_ARG, "null argument");
     return sim->spawn(p, n, accepted);
 }
+// ---- the brush's emitters on the device ----
+
+namespace {
+constexpr float kPPCf = 4.0f;                                  // sim::PPC
+constexpr float kPourSpeed[2] = {60.0f, 400.0f};               // brush.rs:5
+constexpr float kJetSpeed = 320.0f;                            // brush.rs:7
+constexpr float kRadsPerDeg = 3.14159265358979323846f / 180.0f;   // f32::to_radians
+constexpr float kRainSpan = 3.0f;                              // brush.rs:133
+constexpr uint32_t kSpawnLimit = 32768;                        // mod.rs:63
+}  // namespace
+
+int sprout_spout(int kind, float degrees, float rate, float radius, SproutSpout* out) {
+    if (!out || kind < 0 || kind > 2) return fail(SPROUT_E_ARG, "sprout_spout: kind 0 (pour), 1 (jet) or 2 (faucet)");
+    float dir[2] = {0.0f, -1.0f};
+    if (kind != 0) {   // jet_direction (brush.rs:166-169)
+        const float r = degrees * kRadsPerDeg;
+        dir[0] = std::sin(r);
+        dir[1] = -std::cos(r);
+    }
+    // Spout::pour / jet / faucet and Spout::new (brush.rs:28-47)
+    const float speed = kind == 1 ? kJetSpeed : std::min(std::max(rate / (kPPCf * 2.0f * radius), kPourSpeed[0]), kPourSpeed[1]);
+    out->direction[0] = dir[0];
+    out->direction[1] = dir[1];
+    out->speed = speed;
+    out->width = std::min(rate / (kPPCf * speed), 2.0f * radius);
+    return SPROUT_OK;
+}
+
+int sprout_sim_emit_stream(SproutSim* sim, const SproutSpout* spout, double* stream_time, const float from[2],
+                           const float to[2], float seconds, uint32_t material) {
+    if (!sim || !spout || !stream_time || !from || !to) return fail(SPROUT_E_ARG, "null argument");
+    if (!(seconds > 0.0f)) return SPROUT_OK;   // World::emit: a paused brush only moves
+    if (!(spout->speed > 0.0f) || !(spout->width >= 0.0f)) return fail(SPROUT_E_ARG, "a spout needs a positive speed");
+    EmitArgs a{};
+    a.mode = EMIT_STREAM;
+    for (int c = 0; c < 2; c++) {
+        a.from[c] = from[c];
+        a.to[c] = to[c];
+        a.dir[c] = spout->direction[c];
+        a.vel[c] = spout->direction[c] * spout->speed;   // Spout::velocity
+    }
+    a.speed = spout->speed;
+    a.width = spout->width;
+    // Stream::advance (brush.rs:86-115): the frame's range of lattice indices
+    a.rate = (double)(kPPCf * spout->speed * spout->width);
+    a.start = *stream_time;
+    a.end = a.start + (double)seconds;
+    const float half = 0.5f * spout->width;
+    auto index = [&](double t) { return (uint64_t)std::max(std::floor(a.rate * t - 0.5) + 1.0, 0.0); };
+    uint64_t k0 = index(a.start - (double)(half / spout->speed)), k1 = index(a.end);
+    if (k1 < k0) k1 = k0;
+    // Only the last kSpawnLimit that appear are kept (World::stream's limit): they lie among the
+    // last kSpawnLimit indices plus those that may still be crossing the arc at the frame's end.
+    const uint64_t span = (uint64_t)kSpawnLimit + (uint64_t)std::ceil(a.rate * (double)(half / spout->speed)) + 2u;
+    if (k1 - k0 > span) k0 = k1 - span;
+    a.k0 = k0;
+    a.ncand = (uint32_t)(k1 - k0);
+    a.keep = kSpawnLimit;
+    *stream_time = a.end;
+    // World::stream (world.rs:714-727): the window reaches as far as the frame's stream
+    sim->window_of(from, to, spout->speed * seconds + spout->width + 1.0f, a);
+    return sim->emit(a, material, std::min<uint32_t>(a.ncand, kSpawnLimit), nullptr);
+}
+
+int sprout_sim_emit_paint(SproutSim* sim, const float from[2], const float to[2], float radius, uint32_t count,
+                          int spray, uint32_t material) {
+    if (!sim || !from || !to) return fail(SPROUT_E_ARG, "null argument");
+    count = std::min(count, kSpawnLimit);   // World::paint (world.rs:644-648)
+    if (count == 0) return SPROUT_OK;
+    EmitArgs a{};
+    a.mode = EMIT_PAINT;
+    a.spray = spray ? 1u : 0u;
+    a.count = count;
+    a.radius = radius;
+    a.spacing = spray ? 1.5f : 1.0f / std::sqrt(kPPCf);   // SPRAY_SPACING, brush.rs:126
+    for (int c = 0; c < 2; c++) {
+        a.from[c] = from[c];
+        a.to[c] = to[c];
+    }
+    // brush::stroke's lattice bounds (brush.rs:134-141)
+    const int g[2] = {sim->W, sim->H};
+    for (int c = 0; c < 2; c++) {
+        const float lo = std::min(std::max(std::min(from[c], to[c]) - radius, 0.0f), (float)g[c]);
+        const float hi = std::min(std::max(std::max(from[c], to[c]) + radius, 0.0f), (float)g[c]);
+        a.lat_lo[c] = (int)std::floor(lo / a.spacing);
+        a.lat_hi[c] = (int)std::ceil(hi / a.spacing);
+    }
+    const int nx = std::max(a.lat_hi[0] - a.lat_lo[0], 0), ny = std::max(a.lat_hi[1] - a.lat_lo[1], 0);
+    if ((uint64_t)nx * (uint64_t)ny > (1ull << 28)) return fail(SPROUT_E_ARG, "the stroke covers too many lattice points");
+    a.ncand = (uint32_t)(nx * ny);
+    sim->window_of(from, to, radius + 1.0f, a);
+    return sim->emit(a, material, std::min(count, a.ncand), nullptr);
+}
+
+int sprout_sim_emit_rain(SproutSim* sim, const float at[2], float radius, uint32_t count, uint32_t material) {
+    if (!sim || !at) return fail(SPROUT_E_ARG, "null argument");
+    count = std::min(count, kSpawnLimit);
+    if (count == 0) return SPROUT_OK;
+    EmitArgs a{};
+    a.mode = EMIT_RAIN;
+    a.count = count;
+    a.at[0] = at[0];
+    a.at[1] = at[1];
+    a.half = radius * kRainSpan;   // World::rain (world.rs:689-710)
+    const float from[2] = {at[0] - a.half, at[1]}, to[2] = {at[0] + a.half, at[1]};
+    for (int c = 0; c < 2; c++) {
+        a.from[c] = from[c];
+        a.to[c] = to[c];
+    }
+    sim->window_of(from, to, 3.0f, a);
+    return sim->emit(a, material, count, nullptr);
+}
+
+int sprout_sim_emitter_seed(SproutSim* sim, uint32_t rng) {
+    if (!sim) return fail(SPROUT_E_ARG, "null argument");
+    if (!sim->d_emit) {
+        int rc = sim->alloc(&sim->d_emit, 1);
+        if (rc != SPROUT_OK) return rc;
+    }
+    CUDA_TRY(cudaMemcpyAsync(&sim->d_emit->rng, &rng, sizeof rng, cudaMemcpyHostToDevice, sim->stream));
+    CUDA_TRY(cudaStreamSynchronize(sim->stream));
+    return SPROUT_OK;
+}
+
+int sprout_sim_emitted(SproutSim* sim, uint64_t* total, uint32_t* last) {
+    if (!sim || !total) return fail(SPROUT_E_ARG, "null argument");
+    *total = 0;
+    if (last) *last = 0;
+    if (!sim->d_emit) return SPROUT_OK;
+    EmitState e;
+    CUDA_TRY(cudaMemcpyAsync(&e, sim->d_emit, sizeof e, cudaMemcpyDeviceToHost, sim->stream));
+    CUDA_TRY(cudaStreamSynchronize(sim->stream));
+    sim->d2h_bytes += sizeof e;
+    *total = e.total;
+    if (last) *last = e.count;
+    return SPROUT_OK;
+}
+
 int sprout_sim_cell_counts(SproutSim* sim, const int32_t lo[2], const int32_t hi[2], uint32_t* out, size_t cap,
                            size_t* cells) {
     if (!sim || !lo || !hi) return fail(SPROUT_E_ARG, "null argument");
