@@ -337,6 +337,8 @@ def run_batched(args, pg, rank: int = 0, world: int = 1) -> dict:
     setup = time.perf_counter() - t0
     out = {"workload": f"{len(tanks)} uneven dam breaks (128x72..1024x576, 1-2 config-3 liquids), seed 0",
            "setup_s": setup, "placement": f"{len(mine)} of {len(tanks)} tanks on this rank (greedy by cells + particles/4)"}
+    from sprout_gb300 import bytes_model as BM
+    unknowns = None
     for prec in ("mixed", "plain"):
         b.set_precision(prec)
         b.step(args.warmup)
@@ -345,10 +347,18 @@ def run_batched(args, pg, rank: int = 0, world: int = 1) -> dict:
         barrier(pg)
         ms = allreduce_max(pg, b.profile(args.steps))
         sts = [s.stats() for s in sims]
+        if unknowns is None:   # level-0 unknowns of each tank's pressure system
+            unknowns = [int(np.count_nonzero(s_.field("mgd")[: s_.w * s_.h] > 0.0)) for s_ in sims]
+        # the algorithmic bytes of the last substep's batched pressure launches (both solves),
+        # from each tank's iterations: the numerator of the batched solver's roofline
+        pbytes = sum(BM.pressure_bytes(u, max(x.pressure_iters)) for u, x in zip(unknowns, sts))
+        pbytes2 = sum(u * (44 + (x.pressure2_iters + 1) * BM.PRESSURE_ITER) for u, x in zip(unknowns, sts)
+                      if x.pressure2_iters > 0)
         out[prec] = {"value": allreduce_sum(pg, float(live)) * args.steps / (ms / 1e3), "unit": UNIT,
                      "ms_per_step": ms / args.steps, "particles": int(live),
                      "pressure_unconverged": int(sum(x.pressure_unconverged for x in sts)),
-                     "device_errors": int(sum(1 for x in sts if x.device_error))}
+                     "device_errors": int(sum(1 for x in sts if x.device_error)),
+                     "pressure_algorithmic_bytes_last_substep": {"first_solve": pbytes, "second_solve": pbytes2}}
         if prec == "mixed":
             out[prec]["pressure_true_residual_max_fp64"] = float(max(x.pressure_true_residual_max for x in sts))
     out["launch"] = {"batch_blocks": "one per tile of the tanks, at most what fits (2 per SM)"}
@@ -509,6 +519,9 @@ def main():
                     help="seconds of the serving mix's arrival stream (the configuration runs 60; 0: skip it)")
     ap.add_argument("--serve-rate", type=float, default=2000.0)
     ap.add_argument("--serve-tanks", type=int, default=512)
+    ap.add_argument("--batch-only", action="store_true",
+                    help="run only the batched configuration's leg and print it (a profiler's capture of the "
+                         "batched solves)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, world, local, pg = dist_setup(args.gpus)
@@ -518,7 +531,10 @@ def main():
         else:
             from sprout_gb300 import build
             build.build()
-            run_engine(args, rank, world, local, pg)
+            if args.batch_only:
+                print(json.dumps({"batched": run_batched(args, pg, rank, world)}), flush=True)
+            else:
+                run_engine(args, rank, world, local, pg)
     finally:
         if pg is not None:
             pg.destroy_process_group()

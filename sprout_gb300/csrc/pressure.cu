@@ -327,27 +327,37 @@ struct Rsrc {
 // per tail cell the matrix row (couplings, diagonal), the iterate and the right-hand side,
 // at its offset from the first tail level (the slots of mg_tail.comp).
 struct Tail {
-    float4* a;
+    float4* a;    // couplings of tail cells aoff .. T - 1 (at a[s - aoff])
     float* dg;
     float2* x;
     float2* r;
     uint8_t* m;   // per cell: bit q set when neighbour q is an unknown, bit 4 when the cell is
     int base, T, nf;
+    int aoff;     // 0: every level's couplings in shared memory; nf: the first tail level's read
+                  // from the level's stored matrix (a batch, whose blocks then fit four per SM)
 };
+
+// The couplings of tail cell s, from shared memory or (the first level of a batch's tail)
+// from the level's stored matrix: the same values tail_setup would have copied.
+template <class M>
+DEV float4 tail_a(const DevScene& d, const Tail& tl, int s) {
+    return s < tl.aoff ? M::A(d, tl.base + s) : tl.a[s - tl.aoff];
+}
 
 DEV bool t_unknown(const Tail& tl, const Lv& L, int x, int y) { return l_inside(L, x, y) && tl.dg[L.off - tl.base + y * L.w + x] > 0.0f; }
 
 // The tail of scene d laid out in the dynamic shared memory at smem; its right-hand sides at
 // r_store if given (they are live only inside the tail phase, so a caller may keep them in
 // bytes that other phases use), else after the iterates.
-DEV Tail make_tail(const DevScene& d, unsigned char* smem, float2* r_store = nullptr) {
+DEV Tail make_tail(const DevScene& d, unsigned char* smem, float2* r_store = nullptr, bool first_global = false) {
     Tail tl;
     const Lv F = lev(d.lv, d.lv.tail), E = lev(d.lv, d.lv.n - 1);
     tl.base = F.off;
     tl.T = E.off + E.w * E.h - F.off;
     tl.nf = F.w * F.h;
+    tl.aoff = first_global ? tl.nf : 0;
     tl.a = reinterpret_cast<float4*>(smem);
-    tl.x = reinterpret_cast<float2*>(tl.a + tl.T);
+    tl.x = reinterpret_cast<float2*>(tl.a + (tl.T - tl.aoff));
     if (r_store) {
         tl.r = r_store;
         tl.dg = reinterpret_cast<float*>(tl.x + tl.T);
@@ -361,10 +371,12 @@ DEV Tail make_tail(const DevScene& d, unsigned char* smem, float2* r_store = nul
 
 // Cells of the tail levels, and the tail's bytes with and without its right-hand sides.
 __host__ __device__ inline int tail_cells(const Levels& lv) { return lv.off[lv.n - 1] + lv.w[lv.n - 1] * lv.h[lv.n - 1] - lv.off[lv.tail]; }
-__host__ __device__ inline size_t tail_bytes(int T, bool with_r) {
-    const size_t per = sizeof(float4) + sizeof(float2) + (with_r ? sizeof(float2) : 0) + sizeof(float) + 1;
-    return ((size_t)T * per + 15) / 16 * 16;
+__host__ __device__ inline size_t tail_bytes(int T, bool with_r, int aoff = 0) {
+    const size_t per = sizeof(float2) + (with_r ? sizeof(float2) : 0) + sizeof(float) + 1;
+    return ((size_t)T * per + (size_t)(T - aoff) * sizeof(float4) + 15) / 16 * 16;
 }
+// The first tail level's cells (a batch keeps their couplings out of shared memory).
+__host__ __device__ inline int tail_first_cells(const Levels& lv) { return lv.w[lv.tail] * lv.h[lv.tail]; }
 
 // mg_tail.comp mode 1 in every block's shared memory, once per solve: the first tail
 // level's matrix from global memory, then the Galerkin matrices of the coarser tail levels
@@ -372,7 +384,7 @@ __host__ __device__ inline size_t tail_bytes(int T, bool with_r) {
 template <class M>
 DEV void tail_setup(const DevScene& d, const Tail& tl, bool writer) {
     for (int s = threadIdx.x; s < tl.nf; s += NT) {
-        tl.a[s] = M::A(d, tl.base + s);
+        if (s >= tl.aoff) tl.a[s - tl.aoff] = M::A(d, tl.base + s);
         tl.dg[s] = M::Dg(d, tl.base + s);
     }
     __syncthreads();
@@ -388,7 +400,7 @@ DEV void tail_setup(const DevScene& d, const Tail& tl, bool writer) {
                 if (!t_unknown(tl, F, cx, cy)) continue;
                 int i = o + cy * F.w + cx;
                 D += tl.dg[i];
-                float4 w = tl.a[i];
+                float4 w = tail_a<M>(d, tl, i);
                 for (int q = 0; q < 4; q++) {
                     int nx = cx + NBX[q], ny = cy + NBY[q];
                     if (!t_unknown(tl, F, nx, ny)) continue;
@@ -401,8 +413,8 @@ DEV void tail_setup(const DevScene& d, const Tail& tl, bool writer) {
                 }
             }
             tl.dg[oc + t] = D > 1e-7f ? D : 0.0f;
-            tl.a[oc + t] = D > 1e-7f ? A : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-            if (writer) M::setA(d, C.off + t, tl.a[oc + t], tl.dg[oc + t]);
+            tl.a[oc + t - tl.aoff] = D > 1e-7f ? A : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            if (writer) M::setA(d, C.off + t, tl.a[oc + t - tl.aoff], tl.dg[oc + t]);
         }
         __syncthreads();
     }
@@ -814,7 +826,7 @@ DEV void phase_tail(const DevScene& d, const Tail& tl, bool writer) {
             const float D = tl.dg[s];
             const float2 r = tl.r[s];
             const bool mine = !(D <= 0.0f) && ((x + y) & 1) == colour;
-            const float4 w = tl.a[s];
+            const float4 w = tail_a<M>(d, tl, s);
             const uint32_t m = tl.m[s];
             const float2 x0 = tl.x[max(s - 1, lo)], x1 = tl.x[min(s + 1, hi)];
             const float2 x2 = tl.x[max(s - L.w, lo)], x3 = tl.x[min(s + L.w, hi)];
@@ -841,7 +853,7 @@ DEV void phase_tail(const DevScene& d, const Tail& tl, bool writer) {
                 int s = o + cy * L.w + cx;
                 const uint32_t m = tl.m[s];
                 if (!(m & 16u)) continue;
-                float4 w = tl.a[s];
+                float4 w = tail_a<M>(d, tl, s);
                 float Ds = tl.dg[s];
                 float2 xs = tl.x[s];
                 float azx = Ds * xs.x, azy = Ds * xs.y;
@@ -875,7 +887,7 @@ DEV void phase_tail(const DevScene& d, const Tail& tl, bool writer) {
             int s = o + t;
             float D = tl.dg[s];
             if (D <= 0.0f) continue;
-            float4 w = tl.a[s];
+            float4 w = tail_a<M>(d, tl, s);
             float2 sum = tl.r[s];
             const uint32_t m = tl.m[s];
             for (int q = 0; q < 4; q++) {
@@ -1508,11 +1520,11 @@ static_assert(sizeof(Region) % 16 == 0, "regions laid end to end in dynamic shar
 // only, one scene's tail (a scene's tail is rebuilt and solved within that phase and its
 // result stored to global memory, while no tile is being staged), in the same bytes.
 size_t pressure_batch_smem(const Levels& lv) {
-    return std::max(tail_bytes(tail_cells(lv), true), (size_t)kDepth * sizeof(Region));
+    return std::max(tail_bytes(tail_cells(lv), true, tail_first_cells(lv)), (size_t)kDepth * sizeof(Region));
 }
 
 template <class M>
-__global__ void __launch_bounds__(NT, 2) k_mgpcg_batch(BatchView B, int second) {
+__global__ void __launch_bounds__(NT, 4) k_mgpcg_batch(BatchView B, int second) {
     grid_begin();
     using acc = typename M::acc;
     using acc4 = typename M::acc4;
@@ -1600,7 +1612,7 @@ __global__ void __launch_bounds__(NT, 2) k_mgpcg_batch(BatchView B, int second) 
         for (int s = blockIdx.x; s < B.ns; s += gridDim.x) {
             if (fused && !running(s, it)) continue;
             const DevScene& d = B.scenes[s];
-            const Tail tl = make_tail(d, tail_smem);
+            const Tail tl = make_tail(d, tail_smem, nullptr, true);
             tail_setup<M>(d, tl, false);
             phase_tail<M>(d, tl, true);
         }
