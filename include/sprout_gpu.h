@@ -242,6 +242,33 @@ int sprout_sim_emitter_seed(SproutSim* sim, uint32_t rng);
 /* The particles the emitters have queued since the sim was made (and the last emission's),
  * read back (blocking): what World::emit returns, for a caller that wants it. */
 int sprout_sim_emitted(SproutSim* sim, uint64_t* total, uint32_t* last);
+
+/* ---- the render side's cell passes ----------------------------------------------------
+ * FluidSim::record_cell_optics (mod.rs:1626-1660) without a window: the per-cell optics of
+ * cell_optics.comp (20 layers: absorption and scattering of the aqueous and other liquids,
+ * opacity / gloss, emission and speed, frozen colour and share, effects, the key light, the
+ * coat, the look key, ...), the key light from above through the liquid (light.comp) and the
+ * 3 x 3 smoothing with the light's sideways spread (optics_blur.comp), into device buffers of
+ * RGBA16F texels as the reference's image array holds them. Not computed: the ferrofluid
+ * spikes' field and phase (layers 13 xy and 14 xy stay zero), the specks' dust field (layer 18
+ * zero), the film map, smoke, subsurface light and glow images.
+ * material.rs optics_table: rows 0 .. rows - 1 of the optics table of a parameter set, each
+ * 240 bytes laid out as GpuOptics (material.rs:551-597). */
+int sprout_params_optics(const SproutParams* p, void* out, uint32_t rows);
+/* A colour of a material row, as a custom liquid's library entry gives it (library.rs):
+ * field one of color, color_solid, color_hot, cloud_color, dust_color, glow_color; sRGB in
+ * 0 .. 1 (clamped). *ok = 0 for an unknown field or row. */
+int sprout_params_set_color(SproutParams* p, uint32_t row, const char* field, const float rgb[3], int* ok);
+int sprout_params_get_color(const SproutParams* p, uint32_t row, const char* field, float rgb[3], int* ok);
+/* A material row's phase group and diluent row (-1 none). */
+int sprout_params_get_row(const SproutParams* p, uint32_t row, int32_t* group, int32_t* diluent);
+/* Computes the cell passes from what the last substep left on the grid, on the sim's stream
+ * (no wait); `inv_speed` = 1 / the speed that counts as fast, cells / s. */
+int sprout_sim_render(SproutSim* sim, float inv_speed);
+/* The layers (blocking): smoothed (optics_blur.comp's output, layer 10 left zero) or raw
+ * (cell_optics.comp's with light.comp's layer 10), layer-major, W x H texels of four IEEE
+ * half words each. *words = the layers' word count; out may be NULL to ask for it. */
+int sprout_sim_download_render(SproutSim* sim, int smoothed, uint16_t* out, size_t cap, size_t* words);
 /* Stats (src/sim/mod.rs:130-136): live particles and, per material row, its particles and the
  * sum of their concentrations (in particles, a multiple of 1/256). */
 #define SPROUT_MATERIAL_ROWS 96

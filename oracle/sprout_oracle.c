@@ -5006,6 +5006,420 @@ uint32_t osim_particles(const OSim* s, OParticle* out, uint32_t cap) {
     return s->n_slots;
 }
 
+/* ------------------------------------------------------------------------------------ */
+/* The render side's cell passes: cell_optics.comp, light.comp, optics_blur.comp            */
+/* (mod.rs:1626-1660), into layers of RGBA16F texels as the reference's image array holds   */
+/* them. exp / log / pow are the oracle's own (o_expf, o_logf, o_powf). The ferrofluid      */
+/* spikes (layers 13 xy, 14 xy), the dust field (layer 18) and the film tiles are left out, */
+/* as in the engine.                                                                         */
+/* ------------------------------------------------------------------------------------ */
+
+typedef struct OOptics {   /* material.rs GpuOptics: 240 bytes */
+    float absorb[4], solid[4], opt[4], sty[4];
+    int idx[4];
+    float fx[4], fx2[4], lum[4], hot[4], thermo[4], scat[4], opt2[4], dust[4], dust2[4], dcol[4];
+} OOptics;
+
+/* IEEE binary16 from binary32, rounded to nearest even; and back */
+static uint16_t o_half(float f) {
+    uint32_t x;
+    memcpy(&x, &f, 4);
+    uint32_t sign = (x >> 16) & 0x8000u;
+    uint32_t mant = x & 0x7fffffu;
+    int e = (int)((x >> 23) & 255u);
+    if (e == 255) return (uint16_t)(sign | 0x7c00u | (mant ? 0x200u : 0u));
+    int he = e - 127 + 15;
+    if (he >= 31) return (uint16_t)(sign | 0x7c00u);
+    if (he <= 0) {   /* subnormal half (or zero) */
+        if (he < -10) return (uint16_t)sign;
+        uint32_t m = mant | 0x800000u;
+        int shift = 14 - he;   /* 24 bits down to (10 + he) bits */
+        uint32_t hm = m >> shift, rem = m & ((1u << shift) - 1u), half = 1u << (shift - 1);
+        if (rem > half || (rem == half && (hm & 1u))) hm++;
+        return (uint16_t)(sign | hm);
+    }
+    uint32_t hm = mant >> 13, rem = mant & 0x1fffu;
+    uint32_t out = sign | ((uint32_t)he << 10) | hm;
+    if (rem > 0x1000u || (rem == 0x1000u && (hm & 1u))) out++;   /* may carry into the exponent: right */
+    return (uint16_t)out;
+}
+static float o_unhalf(uint16_t h) {
+    uint32_t sign = (uint32_t)(h & 0x8000u) << 16;
+    int e = (h >> 10) & 31;
+    uint32_t m = h & 0x3ffu, x;
+    if (e == 0) {
+        if (m == 0) x = sign;
+        else {
+            e = 1;
+            while (!(m & 0x400u)) { m <<= 1; e--; }
+            m &= 0x3ffu;
+            x = sign | ((uint32_t)(e - 15 + 127) << 23) | (m << 13);
+        }
+    } else if (e == 31) {
+        x = sign | 0x7f800000u | (m << 13);
+    } else {
+        x = sign | ((uint32_t)(e - 15 + 127) << 23) | (m << 13);
+    }
+    float f;
+    memcpy(&f, &x, 4);
+    return f;
+}
+static void put_texel(uint16_t* out, size_t i, V4 v) {
+    out[4 * i + 0] = o_half(v.x);
+    out[4 * i + 1] = o_half(v.y);
+    out[4 * i + 2] = o_half(v.z);
+    out[4 * i + 3] = o_half(v.w);
+}
+static V4 get_texel(const uint16_t* in, size_t i) {
+    return v4(o_unhalf(in[4 * i + 0]), o_unhalf(in[4 * i + 1]), o_unhalf(in[4 * i + 2]), o_unhalf(in[4 * i + 3]));
+}
+static V4 v4add(V4 a, V4 b) { return v4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w); }
+static V4 v4mul(float s, V4 a) { return v4(s * a.x, s * a.y, s * a.z, s * a.w); }
+static V4 v4muls(V4 a, float s) { return v4(a.x * s, a.y * s, a.z * s, a.w * s); }
+static V4 v4mix(V4 a, V4 b, float t) { return v4(mixf(a.x, b.x, t), mixf(a.y, b.y, t), mixf(a.z, b.z, t), mixf(a.w, b.w, t)); }
+static V4 v4ld(const float* f) { return v4(f[0], f[1], f[2], f[3]); }
+
+/* optics.glsl: to_srgb, deep_reflectance, film_colour, look_key */
+static float o_srgb1(float v) {
+    v = clampf(v, 0.0f, 1.0f);
+    return mixf(v * 12.92f, 1.055f * o_powf(v, 1.0f / 2.4f) - 0.055f, v < 0.0031308f ? 0.0f : 1.0f);
+}
+static V4 o_look_key(V4 k) {
+    const float film = 0.35f;
+    float kk[3] = {k.x, k.y, k.z}, out[3];
+    for (int c = 0; c < 3; c++) {
+        float ext = kk[c] + k.w;
+        float tv = o_expf(-2.0f * ext * film);
+        float w = k.w / maxf(kk[c] + k.w, 1e-6f);
+        float q = sqrtf(maxf(1.0f - w, 0.0f));
+        float refl = (1.0f - q) / (1.0f + q) * (1.0f - tv);
+        out[c] = o_srgb1(refl + 0.75f * tv * o_expf(-2.0f * kk[c] * film));
+    }
+    return v4(out[0], out[1], out[2], 1.0f);
+}
+/* cell_optics.comp glow: the colour and brightness of a grey body at T (deg C) */
+static void o_glow(float T, float out[3]) {
+    float K = T + 273.15f;
+    if (K < 760.0f) { out[0] = out[1] = out[2] = 0.0f; return; }
+    float rel = o_expf(23587.0f / 1300.0f - 23587.0f / K);
+    float level = minf(o_logf(1.0f + 200.0f * rel) / o_logf(201.0f), 1.6f);
+    float cr = 1.0f, cg = 1.677f * o_expf(-2573.0f / K), cb = 3.89f * o_expf(-7355.0f / K);
+    float m = maxf(cr, maxf(cg, cb));
+    out[0] = cr / m * level;
+    out[1] = cg / m * level;
+    out[2] = cb / m * level;
+}
+static float o_occ_of(const OSim* s, int x, int y) {
+    if (x < 0 || y < 0 || x >= s->W || y >= s->H) return 0.0f;
+    return minf((float)s->acc[(y * s->W + x) * s->tank.stride + 4] / MASS_SCALE * P_.inv_ppc, 1.0f);
+}
+static float o_sdf_cell(const OSim* s, int x, int y) {
+    x = mini(maxi(x, 0), s->W - 1);
+    y = mini(maxi(y, 0), s->H - 1);
+    int w1 = s->W + 1, k = y * w1 + x;
+    return 0.25f * (s->sdf[k] + s->sdf[k + 1] + s->sdf[k + w1] + s->sdf[k + w1 + 1]);
+}
+static float o_aq_share(const OSim* s, int x, int y) {
+    if (x < 0 || y < 0 || x >= s->W || y >= s->H) return 0.0f;
+    int kq = (y * s->W + x) * s->tank.stride;
+    int cwq = s->acc[kq + 4];
+    if (cwq <= 0) return 0.0f;
+    int others = 0, aqw = 0;
+    for (int j = 0; j < P_.n_present; j++) {
+        const int* ia = s->mats[P_.present[j]].ia;
+        if (ia[2] < 0) continue;
+        int w = s->acc[kq + ia[2]];
+        others += w;
+        if (ia[0] == 0) aqw += w;
+    }
+    int rest = maxi(cwq - others, 0);
+    if (s->mats[P_.present[0]].ia[0] == 0) aqw += rest;
+    return clampf((float)aqw / (float)cwq, 0.0f, 1.0f);
+}
+
+static void o_cell_optics(const OSim* s, const OOptics* opt, float inv_speed, int cx, int cy, uint16_t* raw) {
+    const int i = cy * s->W + cx, k = i * s->tank.stride;
+    const size_t nc = (size_t)s->W * s->H;
+    const int cw = s->acc[k + 4];
+    V4 o[20];
+    for (int l = 0; l < 20; l++) o[l] = v4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (cw > 0) {
+        int thermal = has_cap(s, CAP_THERMAL);
+        float T = thermal ? s->therm[i].x : P_.heat[0];
+        int others = 0;
+        for (int j = 0; j < P_.n_present; j++) {
+            int ch = s->mats[P_.present[j]].ia[2];
+            if (ch >= 0) others += s->acc[k + ch];
+        }
+        int cl = maxi(cw, 1);
+        float occ = minf((float)cw / MASS_SCALE * P_.inv_ppc, 1.0f);
+        float Tg[GROUPS];
+        {
+            float Csh = 0.0f, Cg[GROUPS] = {0};
+            if (thermal) {
+                for (int j = 0; j < P_.n_present; j++) {
+                    int r = P_.present[j];
+                    const int* ia = s->mats[r].ia;
+                    if (ia[2] < 0 && P_.primary >= 0 && r != P_.primary) continue;
+                    int w = ia[2] >= 0 ? s->acc[k + ia[2]] : maxi(cw - others, 0);
+                    if (w <= 0) continue;
+                    float sh = w >= cw ? 1.0f : clampf((float)w / (float)cw, 0.0f, 1.0f);
+                    float sc = (ia[1] >= 0 && ia[3] >= 0) ? clampf((float)s->acc[k + ia[3]] / (float)w, 0.0f, 1.0f) : 1.0f;
+                    float cr = sh * thermal_of(s, (uint32_t)r, sc).w;
+                    Csh += cr;
+                    Cg[ia[0]] += cr;
+                }
+            }
+            group_temperatures(s, k, cw, Csh, Cg, &T, Tg);
+        }
+        V4 aq = v4(0, 0, 0, 0), ot = aq, op_sum = aq, sty = aq, aq_plain = aq, aq_conc = aq, iaq = aq, iot = aq, fx = aq, fx2 = aq;
+        V4 dense = aq;
+        float c_aq = 0.0f, lum[3] = {0, 0, 0}, em[3] = {0, 0, 0}, ior_sum = 0.0f;
+        V4 vi = s->vel[i];
+        float vsx = face_live(vi.z) ? vi.x : 0.0f, vsy = face_live(vi.w) ? vi.y : 0.0f;
+        float stirred = smoothstepf(1.5f, 12.0f, sqrtf(vsx * vsx + vsy * vsy));
+        float best_sh = 0.0f, wden = 0.0f, fden = 0.0f, mag = 0.0f, fzx = 0.0f, fzy = 0.0f, waq = 0.0f, wot = 0.0f, skin = 0.0f;
+        int best_row = -1;
+        float waq_here = o_aq_share(s, cx, cy);
+        for (int j = 0; j < P_.n_present; j++) {
+            int r = P_.present[j];
+            const int* ia = s->mats[r].ia;
+            if (ia[2] < 0 && P_.primary >= 0 && r != P_.primary) continue;
+            int w = ia[2] >= 0 ? s->acc[k + ia[2]] : maxi(cw - others, 0);
+            if (w <= 0) continue;
+            float sh = clampf((float)w / (float)cl, 0.0f, 1.0f);
+            float sc = (ia[1] >= 0 && ia[3] >= 0) ? clampf((float)s->acc[k + ia[3]] / (float)w, 0.0f, 1.0f) : 1.0f;
+            const OOptics* oo = &opt[r];
+            V4 absorb = v4ld(oo->absorb);
+            if (oo->thermo[1] > oo->thermo[0]) absorb = v4mix(absorb, v4ld(oo->hot), smoothstepf(oo->thermo[0], oo->thermo[1], Tg[ia[0]]));
+            V4 lab = absorb, op = v4ld(oo->opt), st = v4ld(oo->sty), ef = v4ld(oo->fx), lm = v4ld(oo->lum);
+            V4 e2 = v4(oo->fx2[0], oo->fx2[1], absorb.w * oo->scat[0], absorb.w * oo->scat[2]);
+            float labs[3] = {oo->solid[0], oo->solid[1], oo->solid[2]};
+            if (ia[1] >= 0) {
+                const OOptics* dd = &opt[ia[1]];
+                lab = v4mix(v4ld(dd->absorb), absorb, sc);
+                for (int c = 0; c < 3; c++) labs[c] = mixf(dd->solid[c], labs[c], sc);
+                op = v4mix(v4ld(dd->opt), op, sc);
+                st = v4mix(v4ld(dd->sty), st, sc);
+                ef = v4mix(v4ld(dd->fx), ef, sc);
+                e2 = v4mix(v4(dd->fx2[0], dd->fx2[1], dd->absorb[3] * dd->scat[0], dd->absorb[3] * dd->scat[2]), e2, sc);
+                lm = v4mix(v4ld(dd->lum), lm, sc);
+            }
+            V4 kl = absorb;
+            if (absorb.w <= 1e-3f && oo->opt[0] < 0.2f) {
+                float grey = kl.x * 0.3f + kl.y * 0.45f + kl.z * 0.25f;
+                kl = v4(grey, grey, grey, kl.w);
+            }
+            if (ia[1] >= 0) {
+                const OOptics* dd = &opt[ia[1]];
+                V4 kd = v4ld(dd->absorb);
+                if (dd->absorb[3] <= 1e-3f && dd->opt[0] < 0.2f) {
+                    float grey = kd.x * 0.3f + kd.y * 0.45f + kd.z * 0.25f;
+                    kd = v4(grey, grey, grey, kd.w);
+                }
+                kl = v4mix(kd, absorb, sc);
+            }
+            o[19] = v4add(o[19], v4mul(sh, kl));
+            ior_sum += sh * (ia[1] >= 0 ? mixf(opt[ia[1]].opt2[0], oo->opt2[0], sc) : oo->opt2[0]);
+            fx2 = v4add(fx2, v4mul(sh, e2));
+            float sl = mixf(1.0f, stirred, lm.w);
+            lum[0] += sh * lm.x * sl;
+            lum[1] += sh * lm.y * sl;
+            lum[2] += sh * lm.z * sl;
+            mag += sh * s->mats[r].el[2];
+            float Tm = Tg[ia[0]], fs = 0.0f;
+            if (thermal) {
+                V4 th = thermal_of(s, (uint32_t)r, sc);
+                fs = th.y > -1e8f ? clampf((th.y - Tm) / maxf(th.y - th.x, 1e-3f), 0.0f, 1.0f) : 0.0f;
+                op.w *= 1.0f - 0.6f * fs;
+                op.x = mixf(op.x, maxf(op.x, 0.6f), fs);
+            }
+            if (oo->idx[1] == 0) {
+                aq = v4add(aq, v4mul(sh, lab));
+                if (ia[1] >= 0) {
+                    aq_plain = v4add(aq_plain, v4mul(sh * (1.0f - sc), v4ld(opt[ia[1]].absorb)));
+                    aq_conc = v4add(aq_conc, v4mul(sh * sc, absorb));
+                    c_aq += sh * sc;
+                } else {
+                    aq_plain = v4add(aq_plain, v4mul(sh, absorb));
+                }
+                waq += sh;
+                iaq = v4add(iaq, v4mul(sh * fs, v4(labs[0], labs[1], labs[2], 0.0f)));
+                fzx += sh * fs;
+            } else {
+                if (oo->idx[1] == 1) ot = v4add(ot, v4mul(sh, lab));
+                else {
+                    dense = v4add(dense, v4mul(sh, lab));
+                    wden += sh;
+                    fden += sh * fs;
+                }
+                wot += sh;
+                iot = v4add(iot, v4mul(sh * fs, v4(labs[0], labs[1], labs[2], 0.0f)));
+                fzy += sh * fs;
+            }
+            if (thermal && ia[0] == 3 && ef.w > 0.01f && Tm > 0.0f) {
+                V4 th = thermal_of(s, (uint32_t)r, sc);
+                if (th.y > -1e8f) {
+                    float g = 2.0f * s->mats[r].th[1];
+                    float hc = P_.heat2[3], Tw = minf(Tg[0], 100.0f), Ta = P_.heat[0] + 273.15f;
+                    float ts_w = (g * Tm + hc * Tw) / maxf(g + hc, 1e-12f), ts_a = Tm;
+                    for (int it = 0; it < 4; it++) {
+                        float Kk = ts_a + 273.15f;
+                        float h = P_.heat[2] + st.w * P_.heat[3] * (Kk * Kk + Ta * Ta) * (Kk + Ta);
+                        ts_a = (g * Tm + h * P_.heat[0]) / maxf(g + h, 1e-12f);
+                    }
+                    float range = maxf(th.y - th.x, 1e-3f);
+                    float sk_w = clampf((th.y - ts_w) / range, 0.0f, 1.0f), sk_a = clampf((th.y - ts_a) / range, 0.0f, 1.0f);
+                    float to_air = 0.0f, to_water = waq_here;
+                    for (int q = 0; q < 4; q++) {
+                        int nx = cx + (q == 0 ? -1 : q == 1 ? 1 : 0), ny = cy + (q == 2 ? -1 : q == 3 ? 1 : 0);
+                        if (o_sdf_cell(s, nx, ny) < 0.0f) continue;
+                        float on = o_occ_of(s, nx, ny);
+                        to_air += 1.0f - on;
+                        to_water += on * o_aq_share(s, nx, ny);
+                    }
+                    skin = maxf(skin, sh * maxf(sk_w * clampf(to_water, 0.0f, 1.0f), sk_a * clampf(to_air, 0.0f, 1.0f)));
+                }
+            }
+            op_sum = v4add(op_sum, v4mul(sh, op));
+            fx = v4add(fx, v4mul(sh, ef));
+            if (sh > best_sh) { best_sh = sh; best_row = r; }
+            sty = v4add(sty, v4mul(sh, st));
+            float gl[3];
+            o_glow(Tm, gl);
+            for (int c = 0; c < 3; c++) em[c] += sh * gl[c] * st.w;
+        }
+        float speed = minf(sqrtf(vsx * vsx + vsy * vsy) * inv_speed, 1.5f);
+        o[15] = v4muls(v4(aq_plain.x, aq_plain.y, aq_plain.z, maxf(waq - c_aq, 0.0f)), occ);
+        if (waq > 0.0f) aq = v4add(v4muls(aq_plain, o_expf(-24.0f * c_aq / waq)), aq_conc);
+        o[0] = v4muls(aq, occ);
+        o[1] = v4muls(ot, occ);
+        o[2] = v4muls(op_sum, occ);
+        float sk = 1.0f - 0.6f * clampf(skin, 0.0f, 1.0f);
+        for (int c = 0; c < 3; c++) em[c] *= sk;
+        o[3] = v4muls(v4(em[0] + lum[0], em[1] + lum[1], em[2] + lum[2], speed), occ);
+        float s_mean = aq.w + ot.w + dense.w;
+        o[16] = v4(fx2.x * occ, fx2.y * occ, s_mean > 1e-5f ? fx2.z / s_mean : 1.0f, s_mean > 1e-5f ? fx2.w / s_mean : 1.0f);
+        o[19] = v4add(v4muls(o[19], occ), o[18]);
+        o[17] = v4muls(v4(lum[0], lum[1], lum[2], ior_sum), occ);
+        o[4] = v4muls(v4(sty.x, sty.y, waq, waq + wot), occ);
+        o[5] = v4muls(v4(iaq.x, iaq.y, iaq.z, wden), occ);
+        o[6] = v4muls(v4(iot.x, iot.y, iot.z, fden), occ);
+        o[11] = v4muls(dense, occ);
+        int last = s->W * s->H - 1;
+        V4 vr = s->vel[mini(i + 1, last)], vt = s->vel[mini(i + s->W, last)];
+        float ucx = 0.5f * (vsx + (face_live(vr.z) ? vr.x : 0.0f)), ucy = 0.5f * (vsy + (face_live(vt.w) ? vt.y : 0.0f));
+        o[7] = v4muls(v4(fzx, fzy, ucx, ucy), occ);
+        o[8] = v4muls(fx, occ);
+        o[9] = v4muls(v4(0.0f, 0.0f, 0.0f, skin), occ);
+        o[10] = v4(fx.y * occ, 0.0f, 0.0f, 0.0f);
+        o[13].z = fx.x * occ;
+        o[14].w = (float)(best_row + 1);
+        float wl = waq + wot;
+        if (wl > 0.0f) {
+            V4 sum = v4add(v4add(aq, ot), dense);
+            o[12] = v4muls(o_look_key(v4(sum.x / wl, sum.y / wl, sum.z / wl, sum.w / wl)), occ);
+        }
+        o[14].z = P_.mag[1] > 0.0f ? mag / P_.mag[1] * occ : 0.0f;
+    }
+    for (int l = 0; l < 20; l++) put_texel(raw, (size_t)l * nc + i, o[l]);
+}
+
+static void o_light(const OSim* s, uint16_t* raw) {
+    const int H = s->H, W = s->W;
+    const size_t nc = (size_t)W * H;
+    const int stretch = mini((H + 63) / 64, 32);
+    for (int x = 0; x < W; x++) {
+        float sums[64][3];
+        for (int t = 0; t < 64; t++) {
+            int top = H - 1 - t * stretch;
+            float sm[3] = {0, 0, 0};
+            for (int k = 0; k < stretch; k++) {
+                int y = top - k;
+                if (y < 0) break;
+                V4 kv = get_texel(raw, (size_t)19 * nc + (size_t)y * W + x);
+                float kk[3] = {kv.x, kv.y, kv.z};
+                for (int c = 0; c < 3; c++) sm[c] += minf(sqrtf(maxf(kk[c] * (kk[c] + 3.0f * kv.w), 0.0f)), 0.25f);
+            }
+            for (int c = 0; c < 3; c++) sums[t][c] = sm[c];
+        }
+        for (int t = 0; t < 64; t++) {
+            int top = H - 1 - t * stretch;
+            float tau[3] = {0, 0, 0};
+            for (int j = 0; j < t; j++)
+                for (int c = 0; c < 3; c++) tau[c] += sums[j][c];
+            for (int k = 0; k < stretch; k++) {
+                int y = top - k;
+                if (y < 0) break;
+                V4 kv = get_texel(raw, (size_t)19 * nc + (size_t)y * W + x);
+                float kk[3] = {kv.x, kv.y, kv.z}, a[3];
+                for (int c = 0; c < 3; c++) a[c] = minf(sqrtf(maxf(kk[c] * (kk[c] + 3.0f * kv.w), 0.0f)), 0.25f);
+                size_t at = (size_t)10 * nc + (size_t)y * W + x;
+                V4 l10 = get_texel(raw, at);
+                V4 il = v4(l10.x, o_expf(-0.35f * (tau[0] + 0.5f * a[0])), o_expf(-0.35f * (tau[1] + 0.5f * a[1])),
+                           o_expf(-0.35f * (tau[2] + 0.5f * a[2])));
+                put_texel(raw, at, il);
+                for (int c = 0; c < 3; c++) tau[c] += a[c];
+            }
+        }
+    }
+}
+
+static void o_optics_blur(const OSim* s, const uint16_t* raw, uint16_t* sm, int cx, int cy) {
+    const int W = s->W, H = s->H;
+    const size_t nc = (size_t)W * H;
+    const float K[3] = {1.0f, 2.0f, 1.0f};
+    V4 acc[20];
+    for (int l = 0; l < 20; l++) acc[l] = v4(0, 0, 0, 0);
+    float wsum = 0.0f, hx = (float)cx + 0.5f, hy = (float)cy + 0.5f;
+    for (int b = -1; b <= 1; b++)
+        for (int a = -1; a <= 1; a++) {
+            int qx = cx + a, qy = cy + b;
+            if (qx < 0 || qy < 0 || qx >= W || qy >= H) continue;
+            if (a != 0 || b != 0) {
+                int nx = mini(maxi((int)rintf(hx + 0.5f * (float)a), 0), W);
+                int ny = mini(maxi((int)rintf(hy + 0.5f * (float)b), 0), H);
+                if (s->sdf[ny * (W + 1) + nx] < 0.0f) continue;
+            }
+            float w = K[a + 1] * K[b + 1];
+            wsum += w;
+            size_t q = (size_t)qy * W + qx;
+            for (int l = 0; l < 20; l++)
+                if (l != 10) acc[l] = v4add(acc[l], v4mul(w, get_texel(raw, (size_t)l * nc + q)));
+        }
+    for (int l = 0; l < 20; l++) acc[l] = v4(acc[l].x / wsum, acc[l].y / wsum, acc[l].z / wsum, acc[l].w / wsum);
+    {
+        float il[3] = {0, 0, 0}, iw = 0.0f;
+        for (int a = -14; a <= 14; a++) {
+            int qx = cx + a;
+            if (qx < 0 || qx >= W) continue;
+            float w = o_expf(-0.5f * (float)(a * a) / (6.0f * 6.0f));
+            V4 l10 = get_texel(raw, (size_t)10 * nc + (size_t)cy * W + qx);
+            il[0] += w * l10.y;
+            il[1] += w * l10.z;
+            il[2] += w * l10.w;
+            iw += w;
+        }
+        float iv = maxf(iw, 1e-6f);
+        acc[9] = v4(il[0] / iv * acc[4].w, il[1] / iv * acc[4].w, il[2] / iv * acc[4].w, acc[9].w);
+    }
+    size_t i = (size_t)cy * W + cx;
+    for (int l = 0; l < 20; l++)
+        if (l != 10) put_texel(sm, (size_t)l * nc + i, acc[l]);
+}
+
+/* The three passes over the oracle's current grid; raw and smooth hold 20 x W x H texels of
+ * four half words (layer-major; smooth's layer 10 is left as it was). */
+long osim_render(const OSim* s, const void* optics, float inv_speed, uint16_t* raw, uint16_t* smooth) {
+    const OOptics* opt = (const OOptics*)optics;
+    for (int y = 0; y < s->H; y++)
+        for (int x = 0; x < s->W; x++) o_cell_optics(s, opt, inv_speed, x, y, raw);
+    o_light(s, raw);
+    for (int y = 0; y < s->H; y++)
+        for (int x = 0; x < s->W; x++) o_optics_blur(s, raw, smooth, x, y);
+    return 0;
+}
+
 long osim_field(const OSim* s, const char* name, void* out, size_t cap) {
     size_t nc = (size_t)s->W * s->H;
     const void* src = NULL;

@@ -168,6 +168,10 @@ void osim_sort(OSim* s);
 uint32_t osim_particles(const OSim* s, OParticle* out, uint32_t cap);
 /* Copies a named field (see sprout_oracle.c: field table). Returns bytes, or -1. */
 long osim_field(const OSim* s, const char* name, void* out, size_t cap);
+/* cell_optics.comp, light.comp, optics_blur.comp on the current grid (mod.rs:1626-1660):
+ * optics = 96 rows of material.rs GpuOptics (240 bytes each); raw and smooth: 20 x W x H
+ * RGBA16F texels (four IEEE half words), layer-major. */
+long osim_render(const OSim* s, const void* optics, float inv_speed, uint16_t* raw, uint16_t* smooth);
 void osim_stats(const OSim* s, OStats* out);
 /* Test hook: the implicit viscosity's assembled level-0 matrix and its matrix-free operator
  * applied to x (2 floats per cell) on the unknown faces; returns the number of unknowns. */

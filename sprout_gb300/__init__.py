@@ -49,7 +49,16 @@ EXPORTS = [
     "sprout_pacer_plan", "sprout_device_count", "sprout_set_device", "sprout_get_device",
     "sprout_scene_rasterize_device", "sprout_sim_set_scene", "sprout_spout", "sprout_sim_emit_stream",
     "sprout_sim_emit_paint", "sprout_sim_emit_rain", "sprout_sim_emitter_seed", "sprout_sim_emitted",
+    "sprout_params_optics", "sprout_params_set_color", "sprout_sim_render", "sprout_sim_download_render",
+    "sprout_params_get_color", "sprout_params_get_row",
 ]
+
+# One row of the optics table (material.rs GpuOptics): 15 four-word fields, 240 bytes.
+OPTICS_FIELDS = ["absorb", "solid", "opt", "sty", "idx", "fx", "fx2", "lum", "hot", "thermo", "scat", "opt2", "dust",
+                 "dust2", "dcol"]
+OPTICS_DTYPE = np.dtype([(f, "<i4" if f == "idx" else "<f4", 4) for f in OPTICS_FIELDS])
+assert OPTICS_DTYPE.itemsize == 240
+RENDER_LAYERS = 20
 
 STAGES = ["advance", "sort", "p2g", "grid", "pressure", "project", "viscosity", "project2"]
 
@@ -181,6 +190,12 @@ def lib() -> C.CDLL:
         "sprout_sim_emit_rain": ([V, P(C.c_float), C.c_float, C.c_uint32, C.c_uint32], C.c_int),
         "sprout_sim_emitter_seed": ([V, C.c_uint32], C.c_int),
         "sprout_sim_emitted": ([V, P(C.c_uint64), P(C.c_uint32)], C.c_int),
+        "sprout_params_optics": ([V, V, C.c_uint32], C.c_int),
+        "sprout_params_set_color": ([V, C.c_uint32, C.c_char_p, P(C.c_float), P(C.c_int)], C.c_int),
+        "sprout_sim_render": ([V, C.c_float], C.c_int),
+        "sprout_params_get_color": ([V, C.c_uint32, C.c_char_p, P(C.c_float), P(C.c_int)], C.c_int),
+        "sprout_params_get_row": ([V, C.c_uint32, P(C.c_int32), P(C.c_int32)], C.c_int),
+        "sprout_sim_download_render": ([V, C.c_int, V, C.c_size_t, P(C.c_size_t)], C.c_int),
         "sprout_sim_download_particles": ([V, V, C.c_uint32, P(C.c_uint32)], C.c_int),
         "sprout_sim_download_pressure": ([V, V], C.c_int),
         "sprout_sim_download_field": ([V, C.c_char_p, V, C.c_size_t, P(C.c_size_t)], C.c_int),
@@ -285,6 +300,32 @@ class SimParams:
         ok = C.c_int()
         _check(lib().sprout_params_set_diluent(self._h, int(row), int(diluent), C.byref(ok)))
         return bool(ok.value)
+
+    def set_color(self, row: int, field: str, rgb) -> bool:
+        """A colour of a material row (color, color_solid, color_hot, cloud_color, dust_color,
+        glow_color; sRGB 0..1), as a custom liquid's library entry gives it."""
+        ok = C.c_int()
+        _check(lib().sprout_params_set_color(self._h, int(row), field.encode(), (C.c_float * 3)(*rgb), C.byref(ok)))
+        return bool(ok.value)
+
+    def get_color(self, row: int, field: str) -> tuple:
+        rgb, ok = (C.c_float * 3)(), C.c_int()
+        _check(lib().sprout_params_get_color(self._h, int(row), field.encode(), rgb, C.byref(ok)))
+        if not ok.value:
+            raise KeyError(field)
+        return tuple(rgb)
+
+    def row_kind(self, row: int) -> tuple[int, int]:
+        """(phase group, diluent row or -1) of a material row."""
+        g, dil = C.c_int32(), C.c_int32()
+        _check(lib().sprout_params_get_row(self._h, int(row), C.byref(g), C.byref(dil)))
+        return g.value, dil.value
+
+    def optics_table(self, rows: int = 96) -> np.ndarray:
+        """material.rs optics_table: one OPTICS_DTYPE row per material row."""
+        out = np.zeros(rows, OPTICS_DTYPE)
+        _check(lib().sprout_params_optics(self._h, out.ctypes.data, rows))
+        return out
 
     def set_group(self, row: int, group: int) -> bool:
         """A custom liquid's phase group as the library's loader reads it (library.rs:283-286):
@@ -427,6 +468,19 @@ class FluidSim:
         if n.value:
             _check(lib().sprout_sim_cell_counts(self._h, a, b, out.ctypes.data, n.value, C.byref(n)))
         return out.reshape(max(hi[1] - lo[1], 0), max(hi[0] - lo[0], 0))
+
+    # ---- the render side's cell passes (record_cell_optics without a window) --------------
+    def render(self, inv_speed: float = 1.0 / 60.0):
+        """cell_optics.comp, light.comp and optics_blur.comp on the device (no wait)."""
+        _check(lib().sprout_sim_render(self._h, inv_speed))
+
+    def download_render(self, smoothed: bool = True) -> np.ndarray:
+        """The layers as float16, shape (RENDER_LAYERS, h, w, 4)."""
+        n = C.c_size_t()
+        _check(lib().sprout_sim_download_render(self._h, 1 if smoothed else 0, None, 0, C.byref(n)))
+        out = np.zeros(n.value, np.uint16)
+        _check(lib().sprout_sim_download_render(self._h, 1 if smoothed else 0, out.ctypes.data, n.value, C.byref(n)))
+        return out.view(np.float16).reshape(RENDER_LAYERS, self.h, self.w, 4)
 
     # ---- the brush's emitters on the device (World::emit without a read-back) -------------
     def emit_stream(self, spout: "Spout", stream: "StreamState", frm, to, seconds: float, material: int):

@@ -46,6 +46,26 @@ struct DevMat {
     float el[4];    // shear modulus / water's density; relaxation time; susceptibility; residue share
 };
 
+// One row of the optics table (material.rs GpuOptics, optics.glsl struct Optics): 240 bytes.
+struct DevOptics {
+    float absorb[4];   // absorption (linear RGB) and mean reduced scattering, 1 / cell
+    float solid[4];    // frozen colour (linear RGB); tint depth (cells)
+    float opt[4];      // opacity, platelet sheen, metal, gloss
+    float sty[4];      // fullness, foam, drying time of its coat (s), emissivity
+    int idx[4];        // diluent row (-1 none), phase group, dried film's scatter x 1000
+    float fx[4];       // volatile share, coat (FILM_UNITs), iridescence, crust
+    float fx2[4];      // froth (s), fizz, specks drawn per cell, drainage time of its foam (s)
+    float lum[4];      // its own light (linear RGB), the share of it that needs stirring
+    float hot[4];      // absorption and scattering at thermo_hi
+    float thermo[4];   // thermochromic range lo, hi; wetting; soapy aqueous
+    float scat[4];     // reduced scattering red, green, blue over its mean; asymmetry g
+    float opt2[4];     // refractive index; platelets' rotational diffusion; Bretherton constant; evaporation
+    float dust[4];     // what one drawn speck stands for: absorption (RGB), scattering
+    float dust2[4];    // speck radius (m), density, thickness over diameter, mirror reflectance
+    float dcol[4];     // speck colour (linear RGB); drawn specks per cell where packed
+};
+static_assert(sizeof(DevOptics) == 240, "GpuOptics is 240 bytes");
+
 struct DevParams {
     int grid[2];
     uint32_t n_slots;

@@ -129,6 +129,11 @@ struct BatchView {
 cudaError_t launch_pressure_batch(const BatchView& B, bool mixed, int blocks, size_t smem, cudaStream_t st, int second);
 int pressure_batch_blocks_max(int device, size_t smem, bool mixed);
 size_t pressure_batch_scalar_bytes();
+// The render side's cell passes (optics.cu): cell_optics.comp into raw (20 layers of RGBA16F
+// texels, layer-major), light.comp into raw's layer 10, optics_blur.comp into smooth.
+struct DevOptics;
+void launch_cell_optics(const DevScene& d, const DevOptics* opt, float inv_speed, ushort4* raw, ushort4* smooth,
+                        cudaStream_t st);
 // Scene::rasterize on the device (raster.cu): the tank's solid fields straight into device
 // buffers, bit-identical to the host's Scene::rasterize (scene.cpp).
 struct Scene;

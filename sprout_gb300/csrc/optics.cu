@@ -1,0 +1,432 @@
+// The render side's per-cell passes on the device, into a headless buffer of layers
+// (FluidSim::record_cell_optics, mod.rs:1626-1660): cell_optics.comp (what the liquid in each
+// cell looks like, 20 layers), light.comp (the key light from above through the liquid) and
+// optics_blur.comp (the 3 x 3 binomial smoothing and the light's sideways spread). Layers are
+// RGBA16F as the reference's image array holds them: IEEE half, rounded to nearest even, and
+// read back as such by the later passes. exp / log / pow are the engine's own (sp_expf,
+// sp_logf, sp_powf), the same arithmetic as the oracle's, where GLSL leaves their precision to
+// the implementation.
+//
+// Not computed here: the ferrofluid spikes' field and phase (layers 13 xy, 14 xy, zero), the
+// dust field of spray.comp (layer 18, zero: the specks are not carried) and the film map's
+// tile flags (no film map).
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include "dev_common.cuh"
+#include "kernels.h"
+#include "optics.h"
+
+namespace sprout {
+
+namespace {
+
+constexpr int kLayers = 20;
+constexpr float kDiluentFade = 24.0f;   // optics.glsl: DILUENT_FADE
+constexpr float kGlowRef = 1300.0f;     // cell_optics.comp: GLOW_REF
+constexpr float kLightPath = 0.35f;     // light.comp: LIGHT_PATH
+constexpr float kCellTau = 0.25f;       // light.comp: CELL_TAU
+constexpr int kMaxStretch = 32;
+constexpr int kLightSpread = 14;        // optics_blur.comp: LIGHT_SPREAD
+constexpr float kLightSigma = 6.0f;
+
+DEV float4 f4(float x, float y, float z, float w) { return make_float4(x, y, z, w); }
+DEV float4 add(float4 a, float4 b) { return f4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w); }
+DEV float4 mul(float s, float4 a) { return f4(s * a.x, s * a.y, s * a.z, s * a.w); }
+DEV float4 mul(float4 a, float s) { return f4(a.x * s, a.y * s, a.z * s, a.w * s); }
+DEV float4 mix4(float4 a, float4 b, float t) { return f4(mixf(a.x, b.x, t), mixf(a.y, b.y, t), mixf(a.z, b.z, t), mixf(a.w, b.w, t)); }
+DEV float4 ld4(const float v[4]) { return f4(v[0], v[1], v[2], v[3]); }
+
+// an RGBA16F texel: IEEE half, round to nearest even
+DEV ushort4 to_half4(float4 v) {
+    return make_ushort4(__half_as_ushort(__float2half_rn(v.x)), __half_as_ushort(__float2half_rn(v.y)),
+                        __half_as_ushort(__float2half_rn(v.z)), __half_as_ushort(__float2half_rn(v.w)));
+}
+DEV float4 from_half4(ushort4 h) {
+    return f4(__half2float(__ushort_as_half(h.x)), __half2float(__ushort_as_half(h.y)), __half2float(__ushort_as_half(h.z)),
+              __half2float(__ushort_as_half(h.w)));
+}
+
+// optics.glsl: to_srgb, deep_reflectance, film_colour, look_key
+DEV float srgb1(float v) {
+    v = clampf(v, 0.0f, 1.0f);
+    return mixf(v * 12.92f, 1.055f * sp_powf(v, 1.0f / 2.4f) - 0.055f, v < 0.0031308f ? 0.0f : 1.0f);
+}
+DEV float4 look_key(float4 k) {
+    const float film = 0.35f;
+    float out[3];
+    const float kk[3] = {k.x, k.y, k.z};
+    for (int c = 0; c < 3; c++) {
+        const float ext = kk[c] + k.w;
+        const float tv = sp_expf(-2.0f * ext * film);
+        const float w = k.w / maxf(kk[c] + k.w, 1e-6f);
+        const float q = sqrtf(maxf(1.0f - w, 0.0f));
+        const float refl = (1.0f - q) / (1.0f + q) * (1.0f - tv);
+        out[c] = srgb1(refl + 0.75f * tv * sp_expf(-2.0f * kk[c] * film));
+    }
+    return f4(out[0], out[1], out[2], 1.0f);
+}
+
+// cell_optics.comp: glow (black-body colour and brightness of a grey body at T, deg C)
+DEV float3 glow_of(float T) {
+    const float K = T + 273.15f;
+    if (K < 760.0f) return make_float3(0.0f, 0.0f, 0.0f);
+    const float rel = sp_expf(23587.0f / kGlowRef - 23587.0f / K);
+    const float level = minf(sp_logf(1.0f + 200.0f * rel) / sp_logf(201.0f), 1.6f);
+    const float cr = 1.0f, cg = 1.677f * sp_expf(-2573.0f / K), cb = 3.89f * sp_expf(-7355.0f / K);
+    const float m = maxf(cr, maxf(cg, cb));
+    return make_float3(cr / m * level, cg / m * level, cb / m * level);
+}
+
+DEV bool in_grid2(const DevScene& d, int x, int y) { return x >= 0 && y >= 0 && x < d.W && y < d.H; }
+DEV float occ_of(const DevScene& d, int x, int y) {
+    if (!in_grid2(d, x, y)) return 0.0f;
+    return minf((float)d.acc[(y * d.W + x) * d.stride + 4] / MASS_SCALE * d.P->inv_ppc, 1.0f);
+}
+DEV float sdf_cell(const DevScene& d, int x, int y) {
+    x = min(max(x, 0), d.W - 1);
+    y = min(max(y, 0), d.H - 1);
+    const int w1 = d.W + 1, k = y * w1 + x;
+    return 0.25f * (d.sdf[k] + d.sdf[k + 1] + d.sdf[k + w1] + d.sdf[k + w1 + 1]);
+}
+// the share of a cell's liquid that is aqueous (cell_optics.comp aq_share)
+DEV float aq_share(const DevScene& d, int x, int y) {
+    if (!in_grid2(d, x, y)) return 0.0f;
+    const DevParams* P = d.P;
+    const int kq = (y * d.W + x) * d.stride;
+    const int cwq = d.acc[kq + 4];
+    if (cwq <= 0) return 0.0f;
+    int others = 0, aqw = 0;
+    for (int j = 0; j < P->n_present; j++) {
+        const int r = P->present[j];
+        const int* ia = d.mats[r].ia;
+        if (ia[2] < 0) continue;
+        const int w = d.acc[kq + ia[2]];
+        others += w;
+        if (ia[0] == 0) aqw += w;
+    }
+    const int rest = max(cwq - others, 0);
+    if (d.mats[P->present[0]].ia[0] == 0) aqw += rest;
+    return clampf((float)aqw / (float)cwq, 0.0f, 1.0f);
+}
+
+__global__ void __launch_bounds__(256) k_cell_optics(DevScene d, const DevOptics* opt, float inv_speed, ushort4* raw) {
+    const int cx = blockIdx.x * 16 + threadIdx.x, cy = blockIdx.y * 16 + threadIdx.y;
+    if (cx >= d.W || cy >= d.H) return;
+    const DevParams* P = d.P;
+    const DevMat* mats = d.mats;
+    const int i = cy * d.W + cx, k = i * d.stride;
+    const int cw = d.acc[k + 4];
+    const size_t nc = (size_t)d.W * d.H;
+    float4 o[kLayers];
+    for (int l = 0; l < kLayers; l++) o[l] = f4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (cw > 0) {
+        const bool thermal = P->thermal != 0;
+        float T = thermal ? d.therm[i].x : P->heat[0];
+        int others = 0;
+        for (int j = 0; j < P->n_present; j++) {
+            const int ch = mats[P->present[j]].ia[2];
+            if (ch >= 0) others += d.acc[k + ch];
+        }
+        const int cl = max(cw, 1);   // (no steam in this engine's tanks: its weight is zero)
+        const float occ = minf((float)cw / MASS_SCALE * P->inv_ppc, 1.0f);
+        float Tg[kGroups];
+        {
+            float Csh = 0.0f;
+            float Cg[kGroups] = {0.0f, 0.0f, 0.0f, 0.0f};
+            if (thermal) {
+                for (int j = 0; j < P->n_present; j++) {
+                    const int r = P->present[j];
+                    const int* ia = mats[r].ia;
+                    if (ia[2] < 0 && P->primary >= 0 && r != P->primary) continue;
+                    const int w = ia[2] >= 0 ? d.acc[k + ia[2]] : max(cw - others, 0);
+                    if (w <= 0) continue;
+                    const float sh = w >= cw ? 1.0f : clampf((float)w / (float)cw, 0.0f, 1.0f);
+                    const float s = (ia[1] >= 0 && ia[3] >= 0) ? clampf((float)d.acc[k + ia[3]] / (float)w, 0.0f, 1.0f) : 1.0f;
+                    const float cr = sh * thermal_of(mats, (uint32_t)r, s).w;
+                    Csh += cr;
+                    Cg[ia[0]] += cr;
+                }
+            }
+            // group_temperatures (common.glsl:610-629)
+            for (int g = 0; g < kGroups; g++) Tg[g] = T;
+            if (Csh > 0.0f) {
+                const int Htot = d.acc[k + (int)P->heat2[2]];
+                T = (float)Htot * T_SCALE / (Csh * (float)cw) - 273.15f;
+                for (int g = 0; g < kGroups; g++) Tg[g] = T;
+                int rest = Htot, first = -1;
+                for (int g = 0; g < kGroups; g++) {
+                    const int ch = group_heat_chan(P, g);
+                    if (ch >= 0) {
+                        const int h = d.acc[k + ch];
+                        rest -= h;
+                        if (Cg[g] > 0.0f) Tg[g] = (float)h * T_SCALE / (Cg[g] * (float)cw) - 273.15f;
+                    } else if (first < 0 && (P->group_mask & (1u << (uint32_t)g)) != 0u) {
+                        first = g;
+                    }
+                }
+                if (first >= 0 && Cg[first] > 0.0f) Tg[first] = (float)rest * T_SCALE / (Cg[first] * (float)cw) - 273.15f;
+            }
+        }
+        float4 aq = f4(0, 0, 0, 0), ot = f4(0, 0, 0, 0), op_sum = f4(0, 0, 0, 0), sty = f4(0, 0, 0, 0);
+        float4 aq_plain = f4(0, 0, 0, 0), aq_conc = f4(0, 0, 0, 0);
+        float c_aq = 0.0f;
+        float4 iaq = f4(0, 0, 0, 0), iot = f4(0, 0, 0, 0), fx = f4(0, 0, 0, 0), fx2 = f4(0, 0, 0, 0);
+        float3 lum = make_float3(0.0f, 0.0f, 0.0f);
+        float ior_sum = 0.0f;
+        const float4 vi = d.vel[i];
+        const float vsx = face_live(vi.z) ? vi.x : 0.0f, vsy = face_live(vi.w) ? vi.y : 0.0f;
+        const float stirred = smoothstepf(1.5f, 12.0f, sqrtf(vsx * vsx + vsy * vsy));
+        float4 dense = f4(0, 0, 0, 0);
+        float best_sh = 0.0f;
+        int best_row = -1;
+        float wden = 0.0f, fden = 0.0f, mag = 0.0f, fzx = 0.0f, fzy = 0.0f, waq = 0.0f, wot = 0.0f, skin = 0.0f;
+        float3 em = make_float3(0.0f, 0.0f, 0.0f);
+        const float waq_here = aq_share(d, cx, cy);
+        for (int j = 0; j < P->n_present; j++) {
+            const int r = P->present[j];
+            const int* ia = mats[r].ia;
+            if (ia[2] < 0 && P->primary >= 0 && r != P->primary) continue;
+            const int w = ia[2] >= 0 ? d.acc[k + ia[2]] : max(cw - others, 0);
+            if (w <= 0) continue;
+            const float sh = clampf((float)w / (float)cl, 0.0f, 1.0f);
+            const float s = (ia[1] >= 0 && ia[3] >= 0) ? clampf((float)d.acc[k + ia[3]] / (float)w, 0.0f, 1.0f) : 1.0f;
+            const DevOptics& oo = opt[r];
+            float4 absorb = ld4(oo.absorb);
+            if (oo.thermo[1] > oo.thermo[0]) absorb = mix4(absorb, ld4(oo.hot), smoothstepf(oo.thermo[0], oo.thermo[1], Tg[ia[0]]));
+            float4 lab = absorb, op = ld4(oo.opt), st = ld4(oo.sty), ef = ld4(oo.fx);
+            float4 e2 = f4(oo.fx2[0], oo.fx2[1], absorb.w * oo.scat[0], absorb.w * oo.scat[2]);
+            float4 lm = ld4(oo.lum);
+            float3 labs = make_float3(oo.solid[0], oo.solid[1], oo.solid[2]);
+            if (ia[1] >= 0) {
+                const DevOptics& dd = opt[ia[1]];
+                lab = mix4(ld4(dd.absorb), absorb, s);
+                labs = make_float3(mixf(dd.solid[0], labs.x, s), mixf(dd.solid[1], labs.y, s), mixf(dd.solid[2], labs.z, s));
+                op = mix4(ld4(dd.opt), op, s);
+                st = mix4(ld4(dd.sty), st, s);
+                ef = mix4(ld4(dd.fx), ef, s);
+                e2 = mix4(f4(dd.fx2[0], dd.fx2[1], dd.absorb[3] * dd.scat[0], dd.absorb[3] * dd.scat[2]), e2, s);
+                lm = mix4(ld4(dd.lum), lm, s);
+            }
+            // for light: a clear plain liquid's tint attenuates it without colour
+            float4 kl = absorb;
+            if (absorb.w <= 1e-3f && oo.opt[0] < 0.2f) {
+                const float grey = kl.x * 0.3f + kl.y * 0.45f + kl.z * 0.25f;
+                kl = f4(grey, grey, grey, kl.w);
+            }
+            if (ia[1] >= 0) {
+                const DevOptics& dd = opt[ia[1]];
+                float4 kd = ld4(dd.absorb);
+                if (dd.absorb[3] <= 1e-3f && dd.opt[0] < 0.2f) {
+                    const float grey = kd.x * 0.3f + kd.y * 0.45f + kd.z * 0.25f;
+                    kd = f4(grey, grey, grey, kd.w);
+                }
+                kl = mix4(kd, absorb, s);
+            }
+            o[19] = add(o[19], mul(sh, kl));
+            ior_sum += sh * (ia[1] >= 0 ? mixf(opt[ia[1]].opt2[0], oo.opt2[0], s) : oo.opt2[0]);
+            fx2 = add(fx2, mul(sh, e2));
+            const float sl = mixf(1.0f, stirred, lm.w);
+            lum = make_float3(lum.x + sh * lm.x * sl, lum.y + sh * lm.y * sl, lum.z + sh * lm.z * sl);
+            mag += sh * mats[r].el[2];
+            const float Tm = Tg[ia[0]];
+            float fs = 0.0f;
+            if (thermal) {
+                const float4 th = thermal_of(mats, (uint32_t)r, s);
+                fs = th.y > -1e8f ? clampf((th.y - Tm) / maxf(th.y - th.x, 1e-3f), 0.0f, 1.0f) : 0.0f;
+                op.w *= 1.0f - 0.6f * fs;
+                op.x = mixf(op.x, maxf(op.x, 0.6f), fs);
+            }
+            if (oo.idx[1] == 0) {
+                aq = add(aq, mul(sh, lab));
+                if (ia[1] >= 0) {
+                    aq_plain = add(aq_plain, mul(sh * (1.0f - s), ld4(opt[ia[1]].absorb)));
+                    aq_conc = add(aq_conc, mul(sh * s, absorb));
+                    c_aq += sh * s;
+                } else {
+                    aq_plain = add(aq_plain, mul(sh, absorb));
+                }
+                waq += sh;
+                iaq = add(iaq, mul(sh * fs, f4(labs.x, labs.y, labs.z, 0.0f)));
+                fzx += sh * fs;
+            } else {
+                if (oo.idx[1] == 1) {
+                    ot = add(ot, mul(sh, lab));
+                } else {
+                    dense = add(dense, mul(sh, lab));
+                    wden += sh;
+                    fden += sh * fs;
+                }
+                wot += sh;
+                iot = add(iot, mul(sh * fs, f4(labs.x, labs.y, labs.z, 0.0f)));
+                fzy += sh * fs;
+            }
+            // the quenched skin of a melt that crusts, against the liquid and air beside it
+            if (thermal && ia[0] == 3 && ef.w > 0.01f && Tm > 0.0f) {
+                const float4 th = thermal_of(mats, (uint32_t)r, s);
+                if (th.y > -1e8f) {
+                    const float g = 2.0f * mats[r].th[1];
+                    const float hc = P->heat2[3], Tw = minf(Tg[0], 100.0f);
+                    const float Ta = P->heat[0] + 273.15f;
+                    const float ts_w = (g * Tm + hc * Tw) / maxf(g + hc, 1e-12f);
+                    float ts_a = Tm;
+                    for (int it = 0; it < 4; it++) {
+                        const float Kk = ts_a + 273.15f;
+                        const float h = P->heat[2] + st.w * P->heat[3] * (Kk * Kk + Ta * Ta) * (Kk + Ta);
+                        ts_a = (g * Tm + h * P->heat[0]) / maxf(g + h, 1e-12f);
+                    }
+                    const float range = maxf(th.y - th.x, 1e-3f);
+                    const float sk_w = clampf((th.y - ts_w) / range, 0.0f, 1.0f);
+                    const float sk_a = clampf((th.y - ts_a) / range, 0.0f, 1.0f);
+                    float to_air = 0.0f, to_water = waq_here;
+                    for (int q = 0; q < 4; q++) {
+                        const int nx = cx + (q == 0 ? -1 : q == 1 ? 1 : 0), ny = cy + (q == 2 ? -1 : q == 3 ? 1 : 0);
+                        if (sdf_cell(d, nx, ny) < 0.0f) continue;
+                        const float on = occ_of(d, nx, ny);
+                        to_air += 1.0f - on;
+                        to_water += on * aq_share(d, nx, ny);
+                    }
+                    skin = maxf(skin, sh * maxf(sk_w * clampf(to_water, 0.0f, 1.0f), sk_a * clampf(to_air, 0.0f, 1.0f)));
+                }
+            }
+            op_sum = add(op_sum, mul(sh, op));
+            fx = add(fx, mul(sh, ef));
+            if (sh > best_sh) {
+                best_sh = sh;
+                best_row = r;
+            }
+            sty = add(sty, mul(sh, st));
+            const float3 gl = glow_of(Tm);
+            em = make_float3(em.x + sh * gl.x * st.w, em.y + sh * gl.y * st.w, em.z + sh * gl.z * st.w);
+        }
+        const float speed = minf(sqrtf(vsx * vsx + vsy * vsy) * inv_speed, 1.5f);
+        o[15] = mul(f4(aq_plain.x, aq_plain.y, aq_plain.z, maxf(waq - c_aq, 0.0f)), occ);
+        if (waq > 0.0f) aq = add(mul(aq_plain, sp_expf(-kDiluentFade * c_aq / waq)), aq_conc);
+        o[0] = mul(aq, occ);
+        o[1] = mul(ot, occ);
+        o[2] = mul(op_sum, occ);
+        const float sk = 1.0f - 0.6f * clampf(skin, 0.0f, 1.0f);
+        em = make_float3(em.x * sk, em.y * sk, em.z * sk);
+        o[3] = mul(f4(em.x + lum.x, em.y + lum.y, em.z + lum.z, speed), occ);
+        const float s_mean = aq.w + ot.w + dense.w;
+        o[16] = f4(fx2.x * occ, fx2.y * occ, s_mean > 1e-5f ? fx2.z / s_mean : 1.0f, s_mean > 1e-5f ? fx2.w / s_mean : 1.0f);
+        o[19] = add(mul(o[19], occ), o[18]);
+        o[17] = mul(f4(lum.x, lum.y, lum.z, ior_sum), occ);
+        o[4] = mul(f4(sty.x, sty.y, waq, waq + wot), occ);
+        o[5] = mul(f4(iaq.x, iaq.y, iaq.z, wden), occ);
+        o[6] = mul(f4(iot.x, iot.y, iot.z, fden), occ);
+        o[11] = mul(dense, occ);
+        const int last = d.W * d.H - 1;
+        const float4 vr = d.vel[min(i + 1, last)], vt = d.vel[min(i + d.W, last)];
+        const float ucx = 0.5f * (vsx + (face_live(vr.z) ? vr.x : 0.0f)), ucy = 0.5f * (vsy + (face_live(vt.w) ? vt.y : 0.0f));
+        o[7] = mul(f4(fzx, fzy, ucx, ucy), occ);
+        o[8] = mul(fx, occ);
+        o[9] = mul(f4(0.0f, 0.0f, 0.0f, skin), occ);
+        o[10] = f4(fx.y * occ, 0.0f, 0.0f, 0.0f);
+        o[13].z = fx.x * occ;
+        o[14].w = (float)(best_row + 1);
+        const float wl = waq + wot;
+        if (wl > 0.0f) {
+            const float4 sum = add(add(aq, ot), dense);
+            o[12] = mul(look_key(f4(sum.x / wl, sum.y / wl, sum.z / wl, sum.w / wl)), occ);
+        }
+        o[14].z = P->mag[1] > 0.0f ? mag / P->mag[1] * occ : 0.0f;
+    }
+    for (int l = 0; l < kLayers; l++) raw[(size_t)l * nc + i] = to_half4(o[l]);
+}
+
+// light.comp: one block per column, a thread per stretch of it from the top
+__global__ void __launch_bounds__(64) k_light(DevScene d, ushort4* raw) {
+    __shared__ float3 s_sum[64];
+    const int x = blockIdx.x, t = threadIdx.x, H = d.H;
+    const size_t nc = (size_t)d.W * d.H;
+    const int stretch = min((H + 63) / 64, kMaxStretch);
+    const int top = H - 1 - t * stretch;
+    auto alpha_at = [&](int y) {
+        const float4 k = from_half4(raw[(size_t)19 * nc + (size_t)y * d.W + x]);
+        return make_float3(minf(sqrtf(maxf(k.x * (k.x + 3.0f * k.w), 0.0f)), kCellTau),
+                           minf(sqrtf(maxf(k.y * (k.y + 3.0f * k.w), 0.0f)), kCellTau),
+                           minf(sqrtf(maxf(k.z * (k.z + 3.0f * k.w), 0.0f)), kCellTau));
+    };
+    float3 sum = make_float3(0.0f, 0.0f, 0.0f);
+    for (int k = 0; k < stretch; k++) {
+        const int y = top - k;
+        if (y < 0) break;
+        const float3 a = alpha_at(y);
+        sum = make_float3(sum.x + a.x, sum.y + a.y, sum.z + a.z);
+    }
+    s_sum[t] = sum;
+    __syncthreads();
+    float3 tau = make_float3(0.0f, 0.0f, 0.0f);
+    for (int j = 0; j < t; j++) tau = make_float3(tau.x + s_sum[j].x, tau.y + s_sum[j].y, tau.z + s_sum[j].z);
+    for (int k = 0; k < stretch; k++) {
+        const int y = top - k;
+        if (y < 0) break;
+        const float3 a = alpha_at(y);
+        ushort4* p = &raw[(size_t)10 * nc + (size_t)y * d.W + x];
+        const float4 l10 = from_half4(*p);
+        const float4 il = f4(l10.x, sp_expf(-kLightPath * (tau.x + 0.5f * a.x)), sp_expf(-kLightPath * (tau.y + 0.5f * a.y)),
+                             sp_expf(-kLightPath * (tau.z + 0.5f * a.z)));
+        *p = to_half4(il);
+        tau = make_float3(tau.x + a.x, tau.y + a.y, tau.z + a.z);
+    }
+}
+
+// optics_blur.comp: 3 x 3 binomial smoothing that leaves out neighbours behind a solid, and the
+// light from above spread sideways by a Gaussian, into the smoothed layers
+__global__ void __launch_bounds__(256) k_optics_blur(DevScene d, const ushort4* raw, ushort4* sm) {
+    const int cx = blockIdx.x * 16 + threadIdx.x, cy = blockIdx.y * 16 + threadIdx.y;
+    if (cx >= d.W || cy >= d.H) return;
+    const size_t nc = (size_t)d.W * d.H;
+    const float K[3] = {1.0f, 2.0f, 1.0f};
+    float4 s[kLayers];
+    for (int l = 0; l < kLayers; l++) s[l] = f4(0.0f, 0.0f, 0.0f, 0.0f);
+    float wsum = 0.0f;
+    const float hx = (float)cx + 0.5f, hy = (float)cy + 0.5f;
+    for (int b = -1; b <= 1; b++) {
+        for (int a = -1; a <= 1; a++) {
+            const int qx = cx + a, qy = cy + b;
+            if (qx < 0 || qy < 0 || qx >= d.W || qy >= d.H) continue;
+            if (a != 0 || b != 0) {   // sdf_at(here + 0.5 (a, b)): the nearest node
+                const int nx = min(max((int)rintf(hx + 0.5f * (float)a), 0), d.W);
+                const int ny = min(max((int)rintf(hy + 0.5f * (float)b), 0), d.H);
+                if (d.sdf[ny * (d.W + 1) + nx] < 0.0f) continue;
+            }
+            const float w = K[a + 1] * K[b + 1];
+            wsum += w;
+            const size_t q = (size_t)qy * d.W + qx;
+            for (int l = 0; l < kLayers; l++)
+                if (l != 10) s[l] = add(s[l], mul(w, from_half4(raw[(size_t)l * nc + q])));
+        }
+    }
+    for (int l = 0; l < kLayers; l++) s[l] = f4(s[l].x / wsum, s[l].y / wsum, s[l].z / wsum, s[l].w / wsum);
+    {
+        float3 il = make_float3(0.0f, 0.0f, 0.0f);
+        float iw = 0.0f;
+        for (int a = -kLightSpread; a <= kLightSpread; a++) {
+            const int qx = cx + a;
+            if (qx < 0 || qx >= d.W) continue;
+            const float w = sp_expf(-0.5f * (float)(a * a) / (kLightSigma * kLightSigma));
+            const float4 l10 = from_half4(raw[(size_t)10 * nc + (size_t)cy * d.W + qx]);
+            il = make_float3(il.x + w * l10.y, il.y + w * l10.z, il.z + w * l10.w);
+            iw += w;
+        }
+        const float iv = maxf(iw, 1e-6f);
+        s[9] = f4(il.x / iv * s[4].w, il.y / iv * s[4].w, il.z / iv * s[4].w, s[9].w);
+    }
+    const size_t i = (size_t)cy * d.W + cx;
+    for (int l = 0; l < kLayers; l++)
+        if (l != 10) sm[(size_t)l * nc + i] = to_half4(s[l]);
+}
+
+}  // namespace
+
+void launch_cell_optics(const DevScene& d, const DevOptics* opt, float inv_speed, ushort4* raw, ushort4* smooth,
+                        cudaStream_t st) {
+    const dim3 tiles((d.W + 15) / 16, (d.H + 15) / 16), block(16, 16);
+    k_cell_optics<<<tiles, block, 0, st>>>(d, opt, inv_speed, raw);
+    k_light<<<d.W, 64, 0, st>>>(d, raw);
+    k_optics_blur<<<tiles, block, 0, st>>>(d, raw, smooth);
+}
+
+}  // namespace sprout

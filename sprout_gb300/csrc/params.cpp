@@ -300,6 +300,9 @@ SimParams::SimParams() {
 #include "builtin_rows.inc"
 #undef BUILTIN_P
 #undef BUILTIN_O
+#define BUILTIN_C(row, field, r, g, b) do { mat[row].field[0] = r; mat[row].field[1] = g; mat[row].field[2] = b; } while (0);
+#include "builtin_colors.inc"
+#undef BUILTIN_C
 }
 
 bool SimParams::set_diluent(int row, int diluent) {

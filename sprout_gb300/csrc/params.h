@@ -44,6 +44,11 @@ struct MatProps {
     int32_t react_with = -1, react_into = -1;
     float react_rate = 0.0f, react_heat = 0.0f, froth = 0.0f, fizz = 0.0f, fume = 0.0f;
     float luminous = 0.0f, glow_shear = 0.0f, thermo_lo = 0.0f, thermo_hi = 0.0f, ior = 1.33f;
+    // colours (sRGB, as material.rs holds them): dissolved, frozen, at thermo_hi, of the fine
+    // particles, of the specks, of its own light (material.rs:385-416)
+    float color[3] = {0.17f, 0.52f, 0.94f}, color_solid[3] = {0.8f, 0.9f, 1.0f};
+    float color_hot[3] = {0.95f, 0.35f, 0.45f}, cloud_color[3] = {0.95f, 0.95f, 0.95f};
+    float dust_color[3] = {0.80f, 0.75f, 0.65f}, glow_color[3] = {0.4f, 1.0f, 0.5f};
 
     bool freezes() const { return melt_hi > -273.0f; }
     float temp_factor_ln(float t) const;

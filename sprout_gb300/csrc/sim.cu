@@ -22,6 +22,7 @@
 #include "../../include/sprout_gpu.h"
 #include "dev_common.cuh"
 #include "kernels.h"
+#include "optics.h"
 #include "params.h"
 #include "scene.h"
 
@@ -969,6 +970,30 @@ struct SproutSim {
         CUDA_TRY(cudaGetLastError());
         emitted = true;
         if (reserved) *reserved = fresh;
+        return SPROUT_OK;
+    }
+
+    // ---- the render side's cell passes (optics.cu; FluidSim::record_cell_optics) ----
+    static constexpr int kRenderLayers = 20;
+    DevOptics* d_optics = nullptr;
+    ushort4* d_raw = nullptr;      // cell_optics.comp + light.comp
+    ushort4* d_smooth = nullptr;   // optics_blur.comp
+    std::vector<DevOptics> h_optics;
+    int render(float inv_speed) {
+        if (!was_reset) return fail(SPROUT_E_ARG, "render before reset");
+        int rc = upload_tables(nullptr);
+        if (rc != SPROUT_OK) return rc;
+        const size_t nc = (size_t)W * H;
+        if (!d_raw) {
+            if ((rc = alloc(&d_raw, kRenderLayers * nc)) != SPROUT_OK) return rc;
+            if ((rc = alloc(&d_smooth, kRenderLayers * nc)) != SPROUT_OK) return rc;
+            if ((rc = alloc(&d_optics, kMaxMaterials)) != SPROUT_OK) return rc;
+        }
+        h_optics.resize(kMaxMaterials);
+        optics_table(params, h_optics.data());
+        CUDA_TRY(cudaMemcpyAsync(d_optics, h_optics.data(), sizeof(DevOptics) * kMaxMaterials, cudaMemcpyHostToDevice, stream));
+        launch_cell_optics(d, d_optics, inv_speed, d_raw, d_smooth, stream);
+        CUDA_TRY(cudaGetLastError());
         return SPROUT_OK;
     }
 
@@ -2101,6 +2126,72 @@ int sprout_sim_emitted(SproutSim* sim, uint64_t* total, uint32_t* last) {
     sim->d2h_bytes += sizeof e;
     *total = e.total;
     if (last) *last = e.count;
+    return SPROUT_OK;
+}
+
+// ---- the render side's cell passes ----
+
+int sprout_params_optics(const SproutParams* p, void* out, uint32_t rows) {
+    if (!p || (!out && rows > 0)) return fail(SPROUT_E_ARG, "null argument");
+    DevOptics* o = static_cast<DevOptics*>(out);
+    for (uint32_t r = 0; r < rows && r < (uint32_t)kMaxMaterials; r++) optics_row(p->p, (int)r, o[r]);
+    return SPROUT_OK;
+}
+
+int sprout_params_set_color(SproutParams* p, uint32_t row, const char* field, const float rgb[3], int* ok) {
+    if (!p || !field || !rgb || !ok) return fail(SPROUT_E_ARG, "null argument");
+    *ok = 0;
+    if (row >= (uint32_t)kMaxMaterials) return SPROUT_OK;
+    MatProps& m = p->p.mat[row];
+    const std::string f(field);
+    float* dst = f == "color" ? m.color : f == "color_solid" ? m.color_solid : f == "color_hot" ? m.color_hot
+               : f == "cloud_color" ? m.cloud_color : f == "dust_color" ? m.dust_color : f == "glow_color" ? m.glow_color
+               : nullptr;
+    if (!dst) return SPROUT_OK;
+    for (int c = 0; c < 3; c++) dst[c] = std::min(std::max(rgb[c], 0.0f), 1.0f);
+    if (row >= p->p.mat_count) p->p.mat_count = row + 1;
+    *ok = 1;
+    return SPROUT_OK;
+}
+
+int sprout_params_get_color(const SproutParams* p, uint32_t row, const char* field, float rgb[3], int* ok) {
+    if (!p || !field || !rgb || !ok) return fail(SPROUT_E_ARG, "null argument");
+    *ok = 0;
+    if (row >= (uint32_t)kMaxMaterials) return SPROUT_OK;
+    const MatProps& m = p->p.mat[row];
+    const std::string f(field);
+    const float* src = f == "color" ? m.color : f == "color_solid" ? m.color_solid : f == "color_hot" ? m.color_hot
+                     : f == "cloud_color" ? m.cloud_color : f == "dust_color" ? m.dust_color : f == "glow_color" ? m.glow_color
+                     : nullptr;
+    if (!src) return SPROUT_OK;
+    for (int c = 0; c < 3; c++) rgb[c] = src[c];
+    *ok = 1;
+    return SPROUT_OK;
+}
+
+int sprout_params_get_row(const SproutParams* p, uint32_t row, int32_t* group, int32_t* diluent) {
+    if (!p || !group || !diluent) return fail(SPROUT_E_ARG, "null argument");
+    if (row >= (uint32_t)kMaxMaterials) return fail(SPROUT_E_ARG, "no such material row");
+    *group = (int32_t)p->p.mat[row].group;
+    *diluent = p->p.mat[row].diluent;
+    return SPROUT_OK;
+}
+
+int sprout_sim_render(SproutSim* sim, float inv_speed) {
+    if (!sim) return fail(SPROUT_E_ARG, "null argument");
+    return sim->render(inv_speed);
+}
+
+int sprout_sim_download_render(SproutSim* sim, int smoothed, uint16_t* out, size_t cap, size_t* words) {
+    if (!sim || !words) return fail(SPROUT_E_ARG, "null argument");
+    const size_t n = (size_t)SproutSim::kRenderLayers * sim->W * sim->H * 4;
+    *words = n;
+    if (!out) return SPROUT_OK;
+    if (cap < n) return fail(SPROUT_E_ARG, "download_render: the output holds fewer words than the layers");
+    if (!sim->d_raw) return fail(SPROUT_E_ARG, "download_render before render");
+    CUDA_TRY(cudaStreamSynchronize(sim->stream));
+    CUDA_TRY(cudaMemcpy(out, smoothed ? sim->d_smooth : sim->d_raw, n * sizeof(uint16_t), cudaMemcpyDeviceToHost));
+    sim->d2h_bytes += n * sizeof(uint16_t);
     return SPROUT_OK;
 }
 
