@@ -248,10 +248,11 @@ int sprout_sim_emitted(SproutSim* sim, uint64_t* total, uint32_t* last);
  * cell_optics.comp (20 layers: absorption and scattering of the aqueous and other liquids,
  * opacity / gloss, emission and speed, frozen colour and share, effects, the key light, the
  * coat, the look key, ...), the key light from above through the liquid (light.comp) and the
- * 3 x 3 smoothing with the light's sideways spread (optics_blur.comp), into device buffers of
+ * 3 x 3 smoothing with the light's sideways spread (optics_blur.comp), the light under the
+ * surface (sss.comp) and the glow field (glow.comp), into device buffers of
  * RGBA16F texels as the reference's image array holds them. Not computed: the ferrofluid
  * spikes' field and phase (layers 13 xy and 14 xy stay zero), the specks' dust field (layer 18
- * zero), the film map, smoke, subsurface light and glow images.
+ * zero), the film map and the smoke field.
  * material.rs optics_table: rows 0 .. rows - 1 of the optics table of a parameter set, each
  * 240 bytes laid out as GpuOptics (material.rs:551-597). */
 int sprout_params_optics(const SproutParams* p, void* out, uint32_t rows);
@@ -265,10 +266,13 @@ int sprout_params_get_row(const SproutParams* p, uint32_t row, int32_t* group, i
 /* Computes the cell passes from what the last substep left on the grid, on the sim's stream
  * (no wait); `inv_speed` = 1 / the speed that counts as fast, cells / s. */
 int sprout_sim_render(SproutSim* sim, float inv_speed);
-/* The layers (blocking): smoothed (optics_blur.comp's output, layer 10 left zero) or raw
- * (cell_optics.comp's with light.comp's layer 10), layer-major, W x H texels of four IEEE
- * half words each. *words = the layers' word count; out may be NULL to ask for it. */
-int sprout_sim_download_render(SproutSim* sim, int smoothed, uint16_t* out, size_t cap, size_t* words);
+/* The layers (blocking), texels of four IEEE half words: which 0, raw (cell_optics.comp's 20
+ * layers with light.comp's layer 10); 1, the smoothed image the composite samples
+ * (optics_blur.comp's layers 0-19 with 10 left zero, and sss.comp's 20-23: the light under the
+ * surface in 20, warm-started from the last call); layer-major, W x H texels each; 2, the glow
+ * field (glow.comp), ceil(W / 2) x ceil(H / 2) texels. *words = the word count; out may be
+ * NULL to ask for it. */
+int sprout_sim_download_render(SproutSim* sim, int which, uint16_t* out, size_t cap, size_t* words);
 /* Stats (src/sim/mod.rs:130-136): live particles and, per material row, its particles and the
  * sum of their concentrations (in particles, a multiple of 1/256). */
 #define SPROUT_MATERIAL_ROWS 96

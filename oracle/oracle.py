@@ -156,7 +156,8 @@ def lib() -> C.CDLL:
         L.osim_vmg_apply.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
         L.osim_vmg_apply.restype = C.c_long
         L.osim_set_threads.argtypes = [C.c_int]
-        L.osim_render.argtypes = [C.c_void_p, C.c_void_p, C.c_float, C.c_void_p, C.c_void_p]
+        L.osim_render.argtypes = [C.c_void_p, C.c_void_p, C.c_float, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                                  C.c_void_p]
         L.osim_render.restype = C.c_long
         L.o_expf.argtypes = [C.c_float]
         L.o_expf.restype = C.c_float
@@ -309,18 +310,23 @@ class OracleSim:
         lib().osim_particles(self.h_, out.ctypes.data, n)
         return out
 
-    def render(self, optics: np.ndarray, inv_speed: float = 1.0 / 60.0):
-        """cell_optics.comp, light.comp, optics_blur.comp on the current grid, from the optics
-        table `optics` (96 rows of 240 bytes): (raw, smooth) as float16 arrays of shape
-        (20, h, w, 4)."""
+    def render(self, optics: np.ndarray, inv_speed: float = 1.0 / 60.0, sss_iters: int = 4):
+        """cell_optics.comp, light.comp, optics_blur.comp, sss.comp, glow.comp on the current
+        grid, from the optics table `optics` (96 rows of 240 bytes): (raw (20, h, w, 4), smooth
+        (24, h, w, 4), glow (ceil(h / 2), ceil(w / 2), 4)) as float16 arrays. The smoothed
+        layers persist between calls (sss.comp's warm start), as the engine's do."""
         tab = np.ascontiguousarray(optics)
         assert tab.nbytes == 96 * 240
-        n = 20 * self.w * self.h * 4
-        raw = np.zeros(n, np.uint16)
-        smooth = np.zeros(n, np.uint16)
-        lib().osim_render(self.h_, tab.ctypes.data, inv_speed, raw.ctypes.data, smooth.ctypes.data)
-        shape = (20, self.h, self.w, 4)
-        return raw.view(np.float16).reshape(shape), smooth.view(np.float16).reshape(shape)
+        if getattr(self, "_smooth", None) is None:
+            self._smooth = np.zeros(24 * self.w * self.h * 4, np.uint16)
+        raw = np.zeros(20 * self.w * self.h * 4, np.uint16)
+        hw, hh = (self.w + 1) // 2, (self.h + 1) // 2
+        ga, gb = np.zeros(hw * hh * 4, np.uint16), np.zeros(hw * hh * 4, np.uint16)
+        lib().osim_render(self.h_, tab.ctypes.data, inv_speed, sss_iters, raw.ctypes.data, self._smooth.ctypes.data,
+                          ga.ctypes.data, gb.ctypes.data)
+        return (raw.view(np.float16).reshape(20, self.h, self.w, 4),
+                self._smooth.copy().view(np.float16).reshape(24, self.h, self.w, 4),
+                gb.view(np.float16).reshape(hh, hw, 4))
 
     def field(self, name: str, dtype=np.float32) -> np.ndarray:
         n = lib().osim_field(self.h_, name.encode(), None, 0)

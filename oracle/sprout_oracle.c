@@ -5408,15 +5408,120 @@ static void o_optics_blur(const OSim* s, const uint16_t* raw, uint16_t* sm, int 
         if (l != 10) put_texel(sm, (size_t)l * nc + i, acc[l]);
 }
 
-/* The three passes over the oracle's current grid; raw and smooth hold 20 x W x H texels of
- * four half words (layer-major; smooth's layer 10 is left as it was). */
-long osim_render(const OSim* s, const void* optics, float inv_speed, uint16_t* raw, uint16_t* smooth) {
+/* sss.comp: stage 0 prepares layers 22 (E, D) and 23 (s, kind) of co (and 20 in air), stage 1
+ * a Jacobi iteration from layer src into the other of 20, 21 (whole grid, read before written) */
+static void o_sss(const OSim* s, const uint16_t* raw, uint16_t* co, int stage, int src) {
+    const int W = s->W, H = s->H;
+    const size_t nc = (size_t)W * H;
+    const float KA = -1.0f, KS = -2.0f;
+    if (stage == 0) {
+        for (int y = 0; y < H; y++)
+            for (int x = 0; x < W; x++) {
+                size_t i = (size_t)y * W + x;
+                float occ = get_texel(co, (size_t)4 * nc + i).w;
+                int w1 = W + 1, k = y * w1 + x;
+                float sdc = 0.25f * (s->sdf[k] + s->sdf[k + 1] + s->sdf[k + w1] + s->sdf[k + w1 + 1]);
+                if (sdc < -0.3f) {
+                    put_texel(co, (size_t)22 * nc + i, v4(0, 0, 0, 0));
+                    put_texel(co, (size_t)23 * nc + i, v4(0, 0, 0, KS));
+                    continue;
+                }
+                if (occ < 0.05f) {
+                    V4 r10 = get_texel(raw, (size_t)10 * nc + i);
+                    put_texel(co, (size_t)22 * nc + i, v4(r10.y, r10.z, r10.w, 0.0f));
+                    put_texel(co, (size_t)23 * nc + i, v4(0, 0, 0, KA));
+                    put_texel(co, (size_t)20 * nc + i, v4(r10.y, r10.z, r10.w, 0.0f));
+                    continue;
+                }
+                V4 k19 = get_texel(co, (size_t)19 * nc + i), l9 = get_texel(co, (size_t)9 * nc + i);
+                V4 kk = v4(k19.x / occ, k19.y / occ, k19.z / occ, k19.w / occ);
+                float lum_a = kk.x * 0.3f + kk.y * 0.45f + kk.z * 0.25f;
+                float D = clampf(1.0f / (3.0f * (lum_a + kk.w) + 1e-4f), 0.04f, 1.6f);
+                put_texel(co, (size_t)22 * nc + i, v4(l9.x / occ, l9.y / occ, l9.z / occ, D));
+                put_texel(co, (size_t)23 * nc + i, v4(kk.x + 0.04f, kk.y + 0.04f, kk.z + 0.04f, occ));
+            }
+        return;
+    }
+    int dst = src == 20 ? 21 : 20;
+    for (int y = 0; y < H; y++)
+        for (int x = 0; x < W; x++) {
+            size_t i = (size_t)y * W + x;
+            V4 kc = get_texel(co, (size_t)23 * nc + i), ec = get_texel(co, (size_t)22 * nc + i);
+            if (kc.w < 0.0f) {
+                put_texel(co, (size_t)dst * nc + i, kc.w == KA ? v4(ec.x, ec.y, ec.z, 0.0f) : v4(0, 0, 0, 0));
+                continue;
+            }
+            float num[3] = {kc.x * ec.x, kc.y * ec.y, kc.z * ec.z}, den[3] = {kc.x, kc.y, kc.z};
+            for (int q = 0; q < 4; q++) {
+                int qx = x + (q == 0 ? -1 : q == 1 ? 1 : 0), qy = y + (q == 2 ? -1 : q == 3 ? 1 : 0);
+                if (qx < 0 || qy < 0 || qx >= W || qy >= H) continue;
+                size_t n = (size_t)qy * W + qx;
+                float kind = get_texel(co, (size_t)23 * nc + n).w;
+                if (kind == KS) continue;
+                float Dn = kind == KA ? ec.w : get_texel(co, (size_t)22 * nc + n).w;
+                float Df = 2.0f * ec.w * Dn / maxf(ec.w + Dn, 1e-6f);
+                V4 pn = get_texel(co, (size_t)src * nc + n);
+                num[0] += Df * pn.x;
+                num[1] += Df * pn.y;
+                num[2] += Df * pn.z;
+                for (int c = 0; c < 3; c++) den[c] += Df;
+            }
+            put_texel(co, (size_t)dst * nc + i, v4(num[0] / den[0], num[1] / den[1], num[2] / den[2], 0.0f));
+        }
+}
+
+/* glow.comp: the 2 x 2 means of raw layer 3's emission blurred across into ga, then down into gb */
+static void o_glow_pass(const OSim* s, const uint16_t* raw, uint16_t* ga, uint16_t* gb, int dir) {
+    const int W = s->W, H = s->H, hw = (W + 1) / 2, hh = (H + 1) / 2;
+    const size_t nc = (size_t)W * H;
+    for (int hy = 0; hy < hh; hy++)
+        for (int hx = 0; hx < hw; hx++) {
+            V4 sum = v4(0, 0, 0, 0);
+            float norm = 0.0f;
+            for (int t = -9; t <= 9; t++) {
+                float w = o_expf(-0.5f * (float)(t * t) / (3.0f * 3.0f));
+                norm += w;
+                int qx = hx + (dir == 0 ? t : 0), qy = hy + (dir == 0 ? 0 : t);
+                if (qx < 0 || qy < 0 || qx >= hw || qy >= hh) continue;
+                V4 v;
+                if (dir == 0) {
+                    V4 sm = v4(0, 0, 0, 0);
+                    for (int j = 0; j < 2; j++)
+                        for (int i = 0; i < 2; i++) {
+                            int cx = 2 * qx + i, cy = 2 * qy + j;
+                            if (cx >= W || cy >= H) continue;
+                            V4 e = get_texel(raw, (size_t)3 * nc + (size_t)cy * W + cx);
+                            sm = v4add(sm, v4(e.x, e.y, e.z, 0.0f));
+                        }
+                    v = v4mul(0.25f, sm);
+                } else {
+                    v = get_texel(ga, (size_t)qy * hw + qx);
+                }
+                sum = v4add(sum, v4mul(w, v));
+            }
+            sum = v4(sum.x / norm, sum.y / norm, sum.z / norm, sum.w / norm);
+            put_texel(dir == 0 ? ga : gb, (size_t)hy * hw + hx, sum);
+        }
+}
+
+/* The passes over the oracle's current grid: raw holds 20 x W x H texels of four half words,
+ * smooth 24 (layer-major; its layer 10 is left as it was, its layer 20 is the warm start of
+ * sss.comp), ga and gb ceil(W / 2) x ceil(H / 2). */
+long osim_render(const OSim* s, const void* optics, float inv_speed, int sss_iters, uint16_t* raw, uint16_t* smooth,
+                 uint16_t* ga, uint16_t* gb) {
     const OOptics* opt = (const OOptics*)optics;
     for (int y = 0; y < s->H; y++)
         for (int x = 0; x < s->W; x++) o_cell_optics(s, opt, inv_speed, x, y, raw);
     o_light(s, raw);
     for (int y = 0; y < s->H; y++)
         for (int x = 0; x < s->W; x++) o_optics_blur(s, raw, smooth, x, y);
+    int iters = (sss_iters + 1) / 2 * 2;
+    if (iters > 0) {
+        o_sss(s, raw, smooth, 0, 20);
+        for (int k = 0; k < iters; k++) o_sss(s, raw, smooth, 1, k % 2 == 0 ? 20 : 21);
+    }
+    o_glow_pass(s, raw, ga, gb, 0);
+    o_glow_pass(s, raw, ga, gb, 1);
     return 0;
 }
 

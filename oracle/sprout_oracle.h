@@ -169,9 +169,11 @@ uint32_t osim_particles(const OSim* s, OParticle* out, uint32_t cap);
 /* Copies a named field (see sprout_oracle.c: field table). Returns bytes, or -1. */
 long osim_field(const OSim* s, const char* name, void* out, size_t cap);
 /* cell_optics.comp, light.comp, optics_blur.comp on the current grid (mod.rs:1626-1660):
- * optics = 96 rows of material.rs GpuOptics (240 bytes each); raw and smooth: 20 x W x H
- * RGBA16F texels (four IEEE half words), layer-major. */
-long osim_render(const OSim* s, const void* optics, float inv_speed, uint16_t* raw, uint16_t* smooth);
+ * then sss.comp and glow.comp: optics = 96 rows of material.rs GpuOptics (240 bytes each);
+ * raw 20 and smooth 24 layers of W x H RGBA16F texels (four IEEE half words), layer-major;
+ * ga, gb the glow field's two half-resolution images. */
+long osim_render(const OSim* s, const void* optics, float inv_speed, int sss_iters, uint16_t* raw, uint16_t* smooth,
+                 uint16_t* ga, uint16_t* gb);
 void osim_stats(const OSim* s, OStats* out);
 /* Test hook: the implicit viscosity's assembled level-0 matrix and its matrix-free operator
  * applied to x (2 floats per cell) on the unknown faces; returns the number of unknowns. */

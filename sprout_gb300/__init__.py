@@ -474,13 +474,17 @@ class FluidSim:
         """cell_optics.comp, light.comp and optics_blur.comp on the device (no wait)."""
         _check(lib().sprout_sim_render(self._h, inv_speed))
 
-    def download_render(self, smoothed: bool = True) -> np.ndarray:
-        """The layers as float16, shape (RENDER_LAYERS, h, w, 4)."""
+    def download_render(self, which: str = "smoothed") -> np.ndarray:
+        """The layers as float16: "raw" (20, h, w, 4), "smoothed" (24, h, w, 4) or "glow"
+        (ceil(h / 2), ceil(w / 2), 4)."""
+        k = {"raw": 0, "smoothed": 1, "glow": 2}[which]
         n = C.c_size_t()
-        _check(lib().sprout_sim_download_render(self._h, 1 if smoothed else 0, None, 0, C.byref(n)))
+        _check(lib().sprout_sim_download_render(self._h, k, None, 0, C.byref(n)))
         out = np.zeros(n.value, np.uint16)
-        _check(lib().sprout_sim_download_render(self._h, 1 if smoothed else 0, out.ctypes.data, n.value, C.byref(n)))
-        return out.view(np.float16).reshape(RENDER_LAYERS, self.h, self.w, 4)
+        _check(lib().sprout_sim_download_render(self._h, k, out.ctypes.data, n.value, C.byref(n)))
+        shape = {0: (RENDER_LAYERS, self.h, self.w, 4), 1: (24, self.h, self.w, 4),
+                 2: ((self.h + 1) // 2, (self.w + 1) // 2, 4)}[k]
+        return out.view(np.float16).reshape(shape)
 
     # ---- the brush's emitters on the device (World::emit without a read-back) -------------
     def emit_stream(self, spout: "Spout", stream: "StreamState", frm, to, seconds: float, material: int):

@@ -130,10 +130,12 @@ cudaError_t launch_pressure_batch(const BatchView& B, bool mixed, int blocks, si
 int pressure_batch_blocks_max(int device, size_t smem, bool mixed);
 size_t pressure_batch_scalar_bytes();
 // The render side's cell passes (optics.cu): cell_optics.comp into raw (20 layers of RGBA16F
-// texels, layer-major), light.comp into raw's layer 10, optics_blur.comp into smooth.
+// texels, layer-major), light.comp into raw's layer 10, optics_blur.comp into smooth's layers
+// 0-19, sss.comp into its layers 20-23 (sss_iters Jacobi iterations, rounded up to even),
+// glow.comp into glow_a then glow_b (half resolution).
 struct DevOptics;
-void launch_cell_optics(const DevScene& d, const DevOptics* opt, float inv_speed, ushort4* raw, ushort4* smooth,
-                        cudaStream_t st);
+void launch_cell_optics(const DevScene& d, const DevOptics* opt, float inv_speed, int sss_iters, ushort4* raw,
+                        ushort4* smooth, ushort4* glow_a, ushort4* glow_b, cudaStream_t st);
 // Scene::rasterize on the device (raster.cu): the tank's solid fields straight into device
 // buffers, bit-identical to the host's Scene::rasterize (scene.cpp).
 struct Scene;

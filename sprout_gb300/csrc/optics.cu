@@ -7,6 +7,9 @@
 // sp_logf, sp_powf), the same arithmetic as the oracle's, where GLSL leaves their precision to
 // the implementation.
 //
+// Then sss.comp (the light under the surface, layers 20-23 of the smoothed buffer, warm-started
+// from the last call) and glow.comp (the emission blurred at half resolution).
+//
 // Not computed here: the ferrofluid spikes' field and phase (layers 13 xy, 14 xy, zero), the
 // dust field of spray.comp (layer 18, zero: the specks are not carried) and the film map's
 // tile flags (no film map).
@@ -419,14 +422,120 @@ __global__ void __launch_bounds__(256) k_optics_blur(DevScene d, const ushort4* 
         if (l != 10) sm[(size_t)l * nc + i] = to_half4(s[l]);
 }
 
+// sss.comp: the light under the surface by the diffusion approximation, per channel
+// -div(D grad phi) + s phi = s E, Jacobi iterations warm-started from the last call's
+// solution (layer 20). stage 0 prepares each cell (layer 22: E, D; 23: s, kind), stage 1
+// iterates from layer src into the other of 20, 21.
+constexpr float kEscape = 0.04f, kDMax = 1.6f, kDMin = 0.04f, kKindAir = -1.0f, kKindSolid = -2.0f;
+__global__ void __launch_bounds__(256) k_sss(DevScene d, const ushort4* raw, ushort4* co, int stage, int src) {
+    const int cx = blockIdx.x * 16 + threadIdx.x, cy = blockIdx.y * 16 + threadIdx.y;
+    if (cx >= d.W || cy >= d.H) return;
+    const size_t nc = (size_t)d.W * d.H, i = (size_t)cy * d.W + cx;
+    auto L = [&](int l, size_t c) { return from_half4(co[(size_t)l * nc + c]); };
+    if (stage == 0) {
+        const float occ = L(4, i).w;
+        const int w1 = d.W + 1, k = cy * w1 + cx;
+        const float sdc = 0.25f * (d.sdf[k] + d.sdf[k + 1] + d.sdf[k + w1] + d.sdf[k + w1 + 1]);
+        if (sdc < -0.3f) {
+            co[(size_t)22 * nc + i] = to_half4(f4(0.0f, 0.0f, 0.0f, 0.0f));
+            co[(size_t)23 * nc + i] = to_half4(f4(0.0f, 0.0f, 0.0f, kKindSolid));
+            return;
+        }
+        if (occ < 0.05f) {
+            const float4 r10 = from_half4(raw[(size_t)10 * nc + i]);
+            co[(size_t)22 * nc + i] = to_half4(f4(r10.y, r10.z, r10.w, 0.0f));
+            co[(size_t)23 * nc + i] = to_half4(f4(0.0f, 0.0f, 0.0f, kKindAir));
+            co[(size_t)20 * nc + i] = to_half4(f4(r10.y, r10.z, r10.w, 0.0f));
+            return;
+        }
+        const float4 k19 = L(19, i), l9 = L(9, i);
+        const float4 kk = f4(k19.x / occ, k19.y / occ, k19.z / occ, k19.w / occ);
+        const float ex = l9.x / occ, ey = l9.y / occ, ez = l9.z / occ;
+        const float lum_a = kk.x * 0.3f + kk.y * 0.45f + kk.z * 0.25f;
+        const float D = clampf(1.0f / (3.0f * (lum_a + kk.w) + 1e-4f), kDMin, kDMax);
+        co[(size_t)22 * nc + i] = to_half4(f4(ex, ey, ez, D));
+        co[(size_t)23 * nc + i] = to_half4(f4(kk.x + kEscape, kk.y + kEscape, kk.z + kEscape, occ));
+        return;
+    }
+    const int dst = src == 20 ? 21 : 20;
+    const float4 kc = L(23, i), ec = L(22, i);
+    if (kc.w < 0.0f) {
+        co[(size_t)dst * nc + i] = to_half4(kc.w == kKindAir ? f4(ec.x, ec.y, ec.z, 0.0f) : f4(0.0f, 0.0f, 0.0f, 0.0f));
+        return;
+    }
+    float nx = kc.x * ec.x, ny = kc.y * ec.y, nz = kc.z * ec.z;
+    float dx = kc.x, dy = kc.y, dz = kc.z;
+    for (int q = 0; q < 4; q++) {
+        const int qx = cx + (q == 0 ? -1 : q == 1 ? 1 : 0), qy = cy + (q == 2 ? -1 : q == 3 ? 1 : 0);
+        if (qx < 0 || qy < 0 || qx >= d.W || qy >= d.H) continue;
+        const size_t n = (size_t)qy * d.W + qx;
+        const float kind = L(23, n).w;
+        if (kind == kKindSolid) continue;
+        const float Dn = kind == kKindAir ? ec.w : L(22, n).w;
+        const float Df = 2.0f * ec.w * Dn / maxf(ec.w + Dn, 1e-6f);
+        const float4 pn = L(src, n);
+        nx += Df * pn.x;
+        ny += Df * pn.y;
+        nz += Df * pn.z;
+        dx += Df;
+        dy += Df;
+        dz += Df;
+    }
+    co[(size_t)dst * nc + i] = to_half4(f4(nx / dx, ny / dy, nz / dz, 0.0f));
+}
+
+// glow.comp: the emission at half the grid's resolution (the mean of 2 x 2 cells of raw layer
+// 3) blurred by one separable Gaussian, across (dir 0, into ga) then down (dir 1, into gb)
+constexpr int kGlowR = 9;
+constexpr float kGlowSigma = 3.0f;
+__global__ void __launch_bounds__(256) k_glow(DevScene d, const ushort4* raw, ushort4* ga, ushort4* gb, int dir) {
+    const int hx = blockIdx.x * 16 + threadIdx.x, hy = blockIdx.y * 16 + threadIdx.y;
+    const int hw = (d.W + 1) / 2, hh = (d.H + 1) / 2;
+    if (hx >= hw || hy >= hh) return;
+    const size_t nc = (size_t)d.W * d.H;
+    float4 sum = f4(0.0f, 0.0f, 0.0f, 0.0f);
+    float norm = 0.0f;
+    for (int t = -kGlowR; t <= kGlowR; t++) {
+        const float w = sp_expf(-0.5f * (float)(t * t) / (kGlowSigma * kGlowSigma));
+        norm += w;
+        const int qx = hx + (dir == 0 ? t : 0), qy = hy + (dir == 0 ? 0 : t);
+        if (qx < 0 || qy < 0 || qx >= hw || qy >= hh) continue;
+        float4 v;
+        if (dir == 0) {
+            float4 s = f4(0.0f, 0.0f, 0.0f, 0.0f);
+            for (int j = 0; j < 2; j++)
+                for (int i = 0; i < 2; i++) {
+                    const int cx = 2 * qx + i, cy = 2 * qy + j;
+                    if (cx >= d.W || cy >= d.H) continue;
+                    const float4 e = from_half4(raw[(size_t)3 * nc + (size_t)cy * d.W + cx]);
+                    s = add(s, f4(e.x, e.y, e.z, 0.0f));
+                }
+            v = mul(0.25f, s);
+        } else {
+            v = from_half4(ga[(size_t)qy * hw + qx]);
+        }
+        sum = add(sum, mul(w, v));
+    }
+    sum = f4(sum.x / norm, sum.y / norm, sum.z / norm, sum.w / norm);
+    (dir == 0 ? ga : gb)[(size_t)hy * hw + hx] = to_half4(sum);
+}
+
 }  // namespace
 
-void launch_cell_optics(const DevScene& d, const DevOptics* opt, float inv_speed, ushort4* raw, ushort4* smooth,
-                        cudaStream_t st) {
+void launch_cell_optics(const DevScene& d, const DevOptics* opt, float inv_speed, int sss_iters, ushort4* raw,
+                        ushort4* smooth, ushort4* glow_a, ushort4* glow_b, cudaStream_t st) {
     const dim3 tiles((d.W + 15) / 16, (d.H + 15) / 16), block(16, 16);
     k_cell_optics<<<tiles, block, 0, st>>>(d, opt, inv_speed, raw);
     k_light<<<d.W, 64, 0, st>>>(d, raw);
     k_optics_blur<<<tiles, block, 0, st>>>(d, raw, smooth);
+    // sss.comp (mod.rs:1666-1675): prepared, then an even number of iterations, ending in layer 20
+    const int iters = (sss_iters + 1) / 2 * 2;
+    if (iters > 0) {
+        k_sss<<<tiles, block, 0, st>>>(d, raw, smooth, 0, 20);
+        for (int k = 0; k < iters; k++) k_sss<<<tiles, block, 0, st>>>(d, raw, smooth, 1, k % 2 == 0 ? 20 : 21);
+    }
+    const dim3 half(((d.W + 1) / 2 + 15) / 16, ((d.H + 1) / 2 + 15) / 16);
+    for (int dir = 0; dir < 2; dir++) k_glow<<<half, block, 0, st>>>(d, raw, glow_a, glow_b, dir);
 }
 
 }  // namespace sprout

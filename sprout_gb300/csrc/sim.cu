@@ -974,10 +974,12 @@ struct SproutSim {
     }
 
     // ---- the render side's cell passes (optics.cu; FluidSim::record_cell_optics) ----
-    static constexpr int kRenderLayers = 20;
+    static constexpr int kRenderLayers = 20, kSmoothLayers = 24;
     DevOptics* d_optics = nullptr;
     ushort4* d_raw = nullptr;      // cell_optics.comp + light.comp
-    ushort4* d_smooth = nullptr;   // optics_blur.comp
+    ushort4* d_smooth = nullptr;   // optics_blur.comp (0-19), sss.comp (20-23)
+    ushort4* d_glow = nullptr;     // glow.comp: two half-resolution images
+    size_t glow_texels() const { return (size_t)((W + 1) / 2) * ((H + 1) / 2); }
     std::vector<DevOptics> h_optics;
     int render(float inv_speed) {
         if (!was_reset) return fail(SPROUT_E_ARG, "render before reset");
@@ -986,13 +988,15 @@ struct SproutSim {
         const size_t nc = (size_t)W * H;
         if (!d_raw) {
             if ((rc = alloc(&d_raw, kRenderLayers * nc)) != SPROUT_OK) return rc;
-            if ((rc = alloc(&d_smooth, kRenderLayers * nc)) != SPROUT_OK) return rc;
+            if ((rc = alloc(&d_smooth, kSmoothLayers * nc)) != SPROUT_OK) return rc;
+            if ((rc = alloc(&d_glow, 2 * glow_texels())) != SPROUT_OK) return rc;
             if ((rc = alloc(&d_optics, kMaxMaterials)) != SPROUT_OK) return rc;
         }
         h_optics.resize(kMaxMaterials);
         optics_table(params, h_optics.data());
         CUDA_TRY(cudaMemcpyAsync(d_optics, h_optics.data(), sizeof(DevOptics) * kMaxMaterials, cudaMemcpyHostToDevice, stream));
-        launch_cell_optics(d, d_optics, inv_speed, d_raw, d_smooth, stream);
+        launch_cell_optics(d, d_optics, inv_speed, (int)params.sss_iters, d_raw, d_smooth, d_glow, d_glow + glow_texels(),
+                           stream);
         CUDA_TRY(cudaGetLastError());
         return SPROUT_OK;
     }
@@ -2182,15 +2186,19 @@ int sprout_sim_render(SproutSim* sim, float inv_speed) {
     return sim->render(inv_speed);
 }
 
-int sprout_sim_download_render(SproutSim* sim, int smoothed, uint16_t* out, size_t cap, size_t* words) {
+int sprout_sim_download_render(SproutSim* sim, int which, uint16_t* out, size_t cap, size_t* words) {
     if (!sim || !words) return fail(SPROUT_E_ARG, "null argument");
-    const size_t n = (size_t)SproutSim::kRenderLayers * sim->W * sim->H * 4;
+    if (which < 0 || which > 2) return fail(SPROUT_E_ARG, "download_render: which is 0 (raw), 1 (smoothed) or 2 (glow)");
+    const size_t nc = (size_t)sim->W * sim->H;
+    const size_t n = 4 * (which == 0 ? SproutSim::kRenderLayers * nc : which == 1 ? SproutSim::kSmoothLayers * nc : sim->glow_texels());
     *words = n;
     if (!out) return SPROUT_OK;
     if (cap < n) return fail(SPROUT_E_ARG, "download_render: the output holds fewer words than the layers");
     if (!sim->d_raw) return fail(SPROUT_E_ARG, "download_render before render");
     CUDA_TRY(cudaStreamSynchronize(sim->stream));
-    CUDA_TRY(cudaMemcpy(out, smoothed ? sim->d_smooth : sim->d_raw, n * sizeof(uint16_t), cudaMemcpyDeviceToHost));
+    const void* src = which == 0 ? (const void*)sim->d_raw : which == 1 ? (const void*)sim->d_smooth
+                                                                        : (const void*)(sim->d_glow + sim->glow_texels());
+    CUDA_TRY(cudaMemcpy(out, src, n * sizeof(uint16_t), cudaMemcpyDeviceToHost));
     sim->d2h_bytes += n * sizeof(uint16_t);
     return SPROUT_OK;
 }

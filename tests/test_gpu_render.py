@@ -20,14 +20,15 @@ def render_pair(tank, substeps, inv_speed=1.0 / 80.0):
     sim, ora, problems = run_pair(tank, substeps)
     assert not problems, "\n".join(problems[:10])
     sim.render(inv_speed)
-    e_raw, e_sm = sim.download_render(False), sim.download_render(True)
+    e = (sim.download_render("raw"), sim.download_render("smoothed"), sim.download_render("glow"))
     table = S.SimParams(tank.settings)
     for row, dil in tank.diluents.items():
         table.set_diluent(row, dil)
     for row, grp in tank.groups.items():
         table.set_group(row, grp)
-    o_raw, o_sm = ora.render(table.optics_table(), inv_speed)
-    return sim, (e_raw, e_sm), (o_raw, o_sm)
+    o = ora.render(table.optics_table(), inv_speed, int(table.get("sss_iters")))
+    render_pair.ora, render_pair.table = ora, table
+    return sim, e, o
 
 
 def diff(a, b, what):
@@ -44,16 +45,28 @@ def test_cell_passes_bit_exact(name):
     tank = {"full_physics": lambda: tanks.full_physics(96, 64, cell=0.0106),
             "honey_dam": lambda: tanks.honey_dam(), "water_oil": lambda: tanks.water_oil(),
             "cooling_lava": lambda: tanks.cooling_lava(), "magnetic": lambda: tanks.magnetic()}[name]()
-    sim, (er, es), (orw, osm) = render_pair(tank, 6)
+    sim, (er, es, eg), (orw, osm, og) = render_pair(tank, 6)
     for a, b, what in ((er, orw, "raw"), (es, osm, "smoothed")):
         m = diff(a, b, what)
         assert m is None, m
+    assert np.array_equal(eg.view(np.uint16), og.view(np.uint16)), "glow"
+    # a second frame: sss.comp starts from the last call's light under the surface
+    from oracle import oracle as O
+    for _ in range(2):
+        sim.step(1, 1 / 240.0)
+        render_pair.ora.step(1, 1 / 240.0)
+    sim.render(1 / 80.0)
+    o2 = render_pair.ora.render(render_pair.table.optics_table(), 1 / 80.0, int(render_pair.table.get("sss_iters")))
+    m = diff(sim.download_render("smoothed"), o2[1], "smoothed, second frame")
+    assert m is None, m
+    assert float(es[20, ..., :3].astype(np.float32).max()) > 0.0
     # the layers hold something: occupancy (4.w), a look key (12), the light from above (raw 10 yzw)
     assert float(er[4, ..., 3].astype(np.float32).max()) > 0.5
     assert float(er[12, ..., :3].astype(np.float32).max()) > 0.0
     assert 0.0 < float(er[10, ..., 1].astype(np.float32).min()) <= 1.0
     if name == "cooling_lava":   # lava near 760 C glows (a heater at 327 C is below the Draper point)
         assert float(er[3, ..., :3].astype(np.float32).max()) > 0.0
+        assert float(eg[..., :3].astype(np.float32).max()) > 0.0
 
 
 def test_render_is_what_the_reference_draws():
@@ -63,7 +76,7 @@ def test_render_is_what_the_reference_draws():
     sim, _, _ = tank.engine()
     sim.step(2, 2 / 240.0)
     sim.render(1 / 80.0)
-    raw = sim.download_render(False).astype(np.float32)
+    raw = sim.download_render("raw").astype(np.float32)
     occ = raw[4, ..., 3]
     light = raw[10, ..., 1]
     assert np.all(light[-1] == 1.0) or np.all(light[-1] >= light[0])
