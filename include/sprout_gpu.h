@@ -263,15 +263,24 @@ int sprout_params_set_color(SproutParams* p, uint32_t row, const char* field, co
 int sprout_params_get_color(const SproutParams* p, uint32_t row, const char* field, float rgb[3], int* ok);
 /* A material row's phase group and diluent row (-1 none). */
 int sprout_params_get_row(const SproutParams* p, uint32_t row, int32_t* group, int32_t* diluent);
-/* Computes the cell passes from what the last substep left on the grid, on the sim's stream
- * (no wait); `inv_speed` = 1 / the speed that counts as fast, cells / s. */
+/* FluidSim::record_cell_optics (src/sim/mod.rs:1626-1712): computes the cell passes from what
+ * the last substep left on the grid, on the sim's stream (no wait); `inv_speed` = 1 / the
+ * speed that counts as fast, cells / s. As the reference, a call records nothing when no
+ * substep, reset, table change or other inv_speed came since the last one; the flow map
+ * (flow_map.comp) advances by the simulated time since the last call (at most 0.25 s, read on
+ * the device) and is cleared by the first call on a new tank. */
 int sprout_sim_render(SproutSim* sim, float inv_speed);
+/* FluidSim::flow_view's parity (mod.rs:1850-1853): the copy of the flow map that holds it now
+ * (blocking). */
+int sprout_sim_flow_parity(SproutSim* sim, uint32_t* parity);
 /* The layers (blocking), texels of four IEEE half words: which 0, raw (cell_optics.comp's 20
  * layers with light.comp's layer 10); 1, the smoothed image the composite samples
  * (optics_blur.comp's layers 0-19 with 10 left zero, and sss.comp's 20-23: the light under the
  * surface in 20, warm-started from the last call); layer-major, W x H texels each; 2, the glow
- * field (glow.comp), ceil(W / 2) x ceil(H / 2) texels. *words = the word count; out may be
- * NULL to ask for it. */
+ * field (glow.comp), ceil(W / 2) x ceil(H / 2) texels; 3, the flow map (flow_map.comp), four
+ * layers: copy 0 (short, long period), copy 1 (short, long), each texel the displacement of
+ * two restarts half a period apart (xy, zw), cells. *words = the word count; out may be NULL
+ * to ask for it. */
 int sprout_sim_download_render(SproutSim* sim, int which, uint16_t* out, size_t cap, size_t* words);
 /* Stats (src/sim/mod.rs:130-136): live particles and, per material row, its particles and the
  * sum of their concentrations (in particles, a multiple of 1/256). */

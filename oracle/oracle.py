@@ -159,6 +159,8 @@ def lib() -> C.CDLL:
         L.osim_render.argtypes = [C.c_void_p, C.c_void_p, C.c_float, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
                                   C.c_void_p]
         L.osim_render.restype = C.c_long
+        L.osim_flow_map.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_float, C.c_float, C.c_uint32]
+        L.osim_flow_map.restype = C.c_long
         L.o_expf.argtypes = [C.c_float]
         L.o_expf.restype = C.c_float
         _lib = L
@@ -236,6 +238,8 @@ class OracleSim:
     def reset(self, particles: np.ndarray) -> int:
         p = np.ascontiguousarray(particles, PARTICLE_DTYPE)
         self.sim_time, self.dt_est = 0.0, float(np.float32(1.0) / np.float32(240.0))
+        self._resets = getattr(self, "_resets", 0) + 1
+        self._stain_valid = False
         return lib().osim_reset(self.h_, p.ctypes.data, len(p))
 
     # The host loop of FluidSim::advance_blocking (src/sim/mod.rs:3284-3312) over the oracle,
@@ -299,6 +303,8 @@ class OracleSim:
         return out.reshape(max(hi[1] - lo[1], 0), max(hi[0] - lo[0], 0))
 
     def step(self, substeps: int, target: float = 0.0, tool: OTool | None = None):
+        if substeps > 0:
+            self._substeps = getattr(self, "_substeps", 0) + substeps
         return lib().osim_step(self.h_, substeps, target, None if tool is None else C.byref(tool))
 
     def sort(self):
@@ -311,22 +317,47 @@ class OracleSim:
         return out
 
     def render(self, optics: np.ndarray, inv_speed: float = 1.0 / 60.0, sss_iters: int = 4):
-        """cell_optics.comp, light.comp, optics_blur.comp, sss.comp, glow.comp on the current
-        grid, from the optics table `optics` (96 rows of 240 bytes): (raw (20, h, w, 4), smooth
-        (24, h, w, 4), glow (ceil(h / 2), ceil(w / 2), 4)) as float16 arrays. The smoothed
-        layers persist between calls (sss.comp's warm start), as the engine's do."""
+        """FluidSim::record_cell_optics (mod.rs:1626-1712) on the current grid, from the optics
+        table `optics` (96 rows of 240 bytes): cell_optics.comp, light.comp, optics_blur.comp,
+        sss.comp, flow_map.comp and glow.comp. Returns (raw (20, h, w, 4), smooth (24, h, w, 4),
+        glow (ceil(h / 2), ceil(w / 2), 4), flow (4, h, w, 4), flow parity) as float16 arrays.
+        Every buffer persists between calls (sss.comp's warm start, the flow map), and a call
+        records nothing when no substep, reset, other table or other inv_speed came since the
+        last one (the reference's optics_key; parameter changes between two calls with no
+        substep are not tracked here). The clock (stain_at): the simulated time after the last
+        substep, the compensated sum step.comp keeps, minus the last call's, clamped to
+        0 .. 0.25 s and zero on the first call on a new tank, which also clears the flow map."""
         tab = np.ascontiguousarray(optics)
         assert tab.nbytes == 96 * 240
-        if getattr(self, "_smooth", None) is None:
-            self._smooth = np.zeros(24 * self.w * self.h * 4, np.uint16)
-        raw = np.zeros(20 * self.w * self.h * 4, np.uint16)
+        nc = self.w * self.h
         hw, hh = (self.w + 1) // 2, (self.h + 1) // 2
-        ga, gb = np.zeros(hw * hh * 4, np.uint16), np.zeros(hw * hh * 4, np.uint16)
-        lib().osim_render(self.h_, tab.ctypes.data, inv_speed, sss_iters, raw.ctypes.data, self._smooth.ctypes.data,
-                          ga.ctypes.data, gb.ctypes.data)
-        return (raw.view(np.float16).reshape(20, self.h, self.w, 4),
+        if getattr(self, "_smooth", None) is None:
+            self._smooth = np.zeros(24 * nc * 4, np.uint16)
+            self._raw = np.zeros(20 * nc * 4, np.uint16)
+            self._flow = np.zeros(4 * nc * 4, np.uint16)
+            self._ga, self._gb = np.zeros(hw * hh * 4, np.uint16), np.zeros(hw * hh * 4, np.uint16)
+            self._parity, self._stain, self._key = 0, 0.0, None
+        valid = getattr(self, "_stain_valid", False)
+        if not valid:
+            self._flow[:] = 0
+        st = self.field("step")
+        now = float(st[1]) - float(st[11:12].view(np.float32)[0])
+        dt = np.float32(min(max(now - self._stain, 0.0), 0.25)) if valid else np.float32(0.0)
+        self._stain, self._stain_valid = now, True
+        key = (getattr(self, "_substeps", 0), getattr(self, "_resets", 0), tab.tobytes(),
+               int(np.float32(inv_speed).view(np.uint32)))
+        if key != self._key:
+            self._key = key
+            lib().osim_render(self.h_, tab.ctypes.data, inv_speed, sss_iters, self._raw.ctypes.data,
+                              self._smooth.ctypes.data, self._ga.ctypes.data, self._gb.ctypes.data)
+            if dt > 0.0:
+                lib().osim_flow_map(self.h_, self._smooth.ctypes.data, self._flow.ctypes.data, float(dt),
+                                    float(np.float32(now)), self._parity)
+                self._parity = 1 - self._parity
+        return (self._raw.copy().view(np.float16).reshape(20, self.h, self.w, 4),
                 self._smooth.copy().view(np.float16).reshape(24, self.h, self.w, 4),
-                gb.view(np.float16).reshape(hh, hw, 4))
+                self._gb.copy().view(np.float16).reshape(hh, hw, 4),
+                self._flow.copy().view(np.float16).reshape(4, self.h, self.w, 4), self._parity)
 
     def field(self, name: str, dtype=np.float32) -> np.ndarray:
         n = lib().osim_field(self.h_, name.encode(), None, 0)

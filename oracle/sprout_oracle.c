@@ -5525,6 +5525,49 @@ long osim_render(const OSim* s, const void* optics, float inv_speed, int sss_ite
     return 0;
 }
 
+/* flow_map.comp:54-72 on every cell of the grid: the displacement carried by the smoothed
+ * velocity (layer 7 zw over the occupancy of layer 4 w, capped at SPEED_MAX = 30 cells/s) from
+ * copy `src` of the map into the other, grown by u dt; each pair restarted (zero) when
+ * floor(now / period + o) changed over the step (o = 0 for xy, 0.5 for zw). Periods
+ * FLOW_PERIOD_SHORT = 4 s and FLOW_PERIOD_LONG = 12 s (mod.rs:431-432). sample_at
+ * (flow_map.comp:41-50): bilinear at a cell-centred position, clamped to the grid. */
+long osim_flow_map(const OSim* s, const uint16_t* smooth, uint16_t* flow, float dt, float now, uint32_t src) {
+    const size_t nc = (size_t)s->W * s->H;
+    const int sl = 2 * (int)src, dl = 2 * (1 - (int)src);
+    for (int cy = 0; cy < s->H; cy++)
+        for (int cx = 0; cx < s->W; cx++) {
+            const size_t i = (size_t)cy * s->W + cx;
+            float occ = get_texel(smooth, 4 * nc + i).w;
+            V2 u = v2(0.0f, 0.0f);
+            if (occ > 0.02f) {
+                V4 v = get_texel(smooth, 7 * nc + i);
+                u = v2(v.z / occ, v.w / occ);
+            }
+            float sp = len2(u);
+            if (sp > 30.0f) {
+                float k = 30.0f / sp;
+                u = v2(u.x * k, u.y * k);
+            }
+            V2 from = v2(((float)cx + 0.5f) - u.x * dt, ((float)cy + 0.5f) - u.y * dt);
+            V2 q = v2(clampf(from.x - 0.5f, 0.0f, (float)(s->W - 1)), clampf(from.y - 0.5f, 0.0f, (float)(s->H - 1)));
+            int i0x = q.x == q.x ? (int)floorf(q.x) : 0, i0y = q.y == q.y ? (int)floorf(q.y) : 0;
+            int i1x = mini(i0x + 1, s->W - 1), i1y = mini(i0y + 1, s->H - 1);
+            V2 f = v2(q.x - (float)i0x, q.y - (float)i0y);
+            for (int k = 0; k < 2; k++) {
+                float period = k == 0 ? 4.0f : 12.0f;
+                const uint16_t* L = flow + 4 * (size_t)(sl + k) * nc;
+                V4 a = v4mix(get_texel(L, (size_t)i0y * s->W + i0x), get_texel(L, (size_t)i0y * s->W + i1x), f.x);
+                V4 b = v4mix(get_texel(L, (size_t)i1y * s->W + i0x), get_texel(L, (size_t)i1y * s->W + i1x), f.x);
+                V4 sa = v4mix(a, b, f.y);
+                V4 d = v4(sa.x + u.x * dt, sa.y + u.y * dt, sa.z + u.x * dt, sa.w + u.y * dt);
+                if (floorf(now / period + 0.0f) != floorf((now - dt) / period + 0.0f)) d.x = d.y = 0.0f;
+                if (floorf(now / period + 0.5f) != floorf((now - dt) / period + 0.5f)) d.z = d.w = 0.0f;
+                put_texel(flow + 4 * (size_t)(dl + k) * nc, i, d);
+            }
+        }
+    return 0;
+}
+
 long osim_field(const OSim* s, const char* name, void* out, size_t cap) {
     size_t nc = (size_t)s->W * s->H;
     const void* src = NULL;

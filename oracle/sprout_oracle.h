@@ -174,6 +174,8 @@ long osim_field(const OSim* s, const char* name, void* out, size_t cap);
  * ga, gb the glow field's two half-resolution images. */
 long osim_render(const OSim* s, const void* optics, float inv_speed, int sss_iters, uint16_t* raw, uint16_t* smooth,
                  uint16_t* ga, uint16_t* gb);
+/* flow_map.comp over the grid from copy `src` of `flow` (4 layers) into the other copy. */
+long osim_flow_map(const OSim* s, const uint16_t* smooth, uint16_t* flow, float dt, float now, uint32_t src);
 void osim_stats(const OSim* s, OStats* out);
 /* Test hook: the implicit viscosity's assembled level-0 matrix and its matrix-free operator
  * applied to x (2 floats per cell) on the unknown faces; returns the number of unknowns. */

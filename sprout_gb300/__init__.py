@@ -50,7 +50,7 @@ EXPORTS = [
     "sprout_scene_rasterize_device", "sprout_sim_set_scene", "sprout_spout", "sprout_sim_emit_stream",
     "sprout_sim_emit_paint", "sprout_sim_emit_rain", "sprout_sim_emitter_seed", "sprout_sim_emitted",
     "sprout_params_optics", "sprout_params_set_color", "sprout_sim_render", "sprout_sim_download_render",
-    "sprout_params_get_color", "sprout_params_get_row",
+    "sprout_params_get_color", "sprout_params_get_row", "sprout_sim_flow_parity",
 ]
 
 # One row of the optics table (material.rs GpuOptics): 15 four-word fields, 240 bytes.
@@ -193,6 +193,7 @@ def lib() -> C.CDLL:
         "sprout_params_optics": ([V, V, C.c_uint32], C.c_int),
         "sprout_params_set_color": ([V, C.c_uint32, C.c_char_p, P(C.c_float), P(C.c_int)], C.c_int),
         "sprout_sim_render": ([V, C.c_float], C.c_int),
+        "sprout_sim_flow_parity": ([V, P(C.c_uint32)], C.c_int),
         "sprout_params_get_color": ([V, C.c_uint32, C.c_char_p, P(C.c_float), P(C.c_int)], C.c_int),
         "sprout_params_get_row": ([V, C.c_uint32, P(C.c_int32), P(C.c_int32)], C.c_int),
         "sprout_sim_download_render": ([V, C.c_int, V, C.c_size_t, P(C.c_size_t)], C.c_int),
@@ -471,19 +472,27 @@ class FluidSim:
 
     # ---- the render side's cell passes (record_cell_optics without a window) --------------
     def render(self, inv_speed: float = 1.0 / 60.0):
-        """cell_optics.comp, light.comp and optics_blur.comp on the device (no wait)."""
+        """record_cell_optics on the device (no wait): cell_optics.comp, light.comp,
+        optics_blur.comp, sss.comp, flow_map.comp and glow.comp; nothing when nothing changed
+        since the last call."""
         _check(lib().sprout_sim_render(self._h, inv_speed))
 
+    def flow_parity(self) -> int:
+        """The copy of the flow map that holds it now (blocking)."""
+        v = C.c_uint32()
+        _check(lib().sprout_sim_flow_parity(self._h, C.byref(v)))
+        return int(v.value)
+
     def download_render(self, which: str = "smoothed") -> np.ndarray:
-        """The layers as float16: "raw" (20, h, w, 4), "smoothed" (24, h, w, 4) or "glow"
-        (ceil(h / 2), ceil(w / 2), 4)."""
-        k = {"raw": 0, "smoothed": 1, "glow": 2}[which]
+        """The layers as float16: "raw" (20, h, w, 4), "smoothed" (24, h, w, 4), "glow"
+        (ceil(h / 2), ceil(w / 2), 4) or "flow" (4, h, w, 4)."""
+        k = {"raw": 0, "smoothed": 1, "glow": 2, "flow": 3}[which]
         n = C.c_size_t()
         _check(lib().sprout_sim_download_render(self._h, k, None, 0, C.byref(n)))
         out = np.zeros(n.value, np.uint16)
         _check(lib().sprout_sim_download_render(self._h, k, out.ctypes.data, n.value, C.byref(n)))
         shape = {0: (RENDER_LAYERS, self.h, self.w, 4), 1: (24, self.h, self.w, 4),
-                 2: ((self.h + 1) // 2, (self.w + 1) // 2, 4)}[k]
+                 2: ((self.h + 1) // 2, (self.w + 1) // 2, 4), 3: (4, self.h, self.w, 4)}[k]
         return out.view(np.float16).reshape(shape)
 
     # ---- the brush's emitters on the device (World::emit without a read-back) -------------

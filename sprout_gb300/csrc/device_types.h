@@ -66,6 +66,20 @@ struct DevOptics {
 };
 static_assert(sizeof(DevOptics) == 240, "GpuOptics is 240 bytes");
 
+// The render side's clock (FluidSim::record_cell_optics: stain_at, flow_parity), kept on the
+// device so that a render call needs no read-back: the simulated time of the last call, and
+// what this call's flow map uses (its step, the time after it, the copy it reads, whether it
+// runs).
+struct RenderClock {
+    double stain;      // simulated time of the last render call, s
+    float dt, now;     // this call: time since the last one (0 .. 0.25 s), and now, as f32
+    uint32_t src;      // the copy (0 or 1) the flow map reads: the one that holds it now
+    uint32_t parity;   // the copy that holds it after this call
+    uint32_t run;      // 1: the flow map runs in this call
+    uint32_t pad;
+};
+static_assert(sizeof(RenderClock) == 32, "RenderClock is 32 bytes");
+
 struct DevParams {
     int grid[2];
     uint32_t n_slots;

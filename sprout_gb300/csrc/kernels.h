@@ -132,10 +132,18 @@ size_t pressure_batch_scalar_bytes();
 // The render side's cell passes (optics.cu): cell_optics.comp into raw (20 layers of RGBA16F
 // texels, layer-major), light.comp into raw's layer 10, optics_blur.comp into smooth's layers
 // 0-19, sss.comp into its layers 20-23 (sss_iters Jacobi iterations, rounded up to even),
-// glow.comp into glow_a then glow_b (half resolution).
+// flow_map.comp into flow (four layers: copy 0 short and long period, copy 1 short and long)
+// when the clock says it runs, glow.comp into glow_a then glow_b (half resolution).
 struct DevOptics;
+struct RenderClock;
 void launch_cell_optics(const DevScene& d, const DevOptics* opt, float inv_speed, int sss_iters, ushort4* raw,
-                        ushort4* smooth, ushort4* glow_a, ushort4* glow_b, cudaStream_t st);
+                        ushort4* smooth, ushort4* flow, const RenderClock* clock, ushort4* glow_a, ushort4* glow_b,
+                        cudaStream_t st);
+// The clock of a render call (record_cell_optics, mod.rs:1628-1641, 1674-1680): `valid` 0 for
+// the first call on a new tank (no step: the flow map does not run), `changed` 0 when the call
+// records nothing (its key is the last call's); the time since the last call from the
+// device's own simulated time.
+void launch_render_clock(const DevScene& d, RenderClock* clock, int valid, int changed, cudaStream_t st);
 // Scene::rasterize on the device (raster.cu): the tank's solid fields straight into device
 // buffers, bit-identical to the host's Scene::rasterize (scene.cpp).
 struct Scene;

@@ -8,7 +8,8 @@
 // the implementation.
 //
 // Then sss.comp (the light under the surface, layers 20-23 of the smoothed buffer, warm-started
-// from the last call) and glow.comp (the emission blurred at half resolution).
+// from the last call), flow_map.comp (how far the liquid has moved since its patterns
+// restarted, four layers) and glow.comp (the emission blurred at half resolution).
 //
 // Not computed here: the ferrofluid spikes' field and phase (layers 13 xy, 14 xy, zero), the
 // dust field of spray.comp (layer 18, zero: the specks are not carried) and the film map's
@@ -520,10 +521,81 @@ __global__ void __launch_bounds__(256) k_glow(DevScene d, const ushort4* raw, us
     (dir == 0 ? ga : gb)[(size_t)hy * hw + hx] = to_half4(sum);
 }
 
+// record_cell_optics' clock (mod.rs:1628-1641, 1674-1680): the time since the last call from
+// the simulated time after the last substep (the compensated sum of the substeps' lengths,
+// step.comp), clamped to 0 .. 0.25 s in double precision and then rounded to f32; zero on the
+// first call on a new tank. The flow map runs when the call records (`changed`) and dt > 0,
+// reading the copy that holds the map and leaving it in the other.
+__global__ void k_render_clock(const StepState* S, RenderClock* c, int valid, int changed) {
+    const double now = (double)S->advanced - (double)__uint_as_float(S->pad0);
+    double dt = 0.0;
+    if (valid) dt = fmin(fmax(now - c->stain, 0.0), 0.25);
+    c->stain = now;
+    c->dt = (float)dt;
+    c->now = (float)now;
+    c->src = c->parity;
+    c->run = (changed && c->dt > 0.0f) ? 1u : 0u;
+    if (c->run) c->parity = 1u - c->parity;
+}
+
+// flow_map.comp: how far the liquid at each cell has moved since its pattern last restarted,
+// carried semi-Lagrangian by the smoothed velocity (layer 7 zw over the occupancy, layer 4 w)
+// and grown by u dt; two copies per period half a period apart, each restarted (zero) as its
+// weight in the composite reaches zero. Layers 2 copy + period (0 short, 1 long).
+constexpr float kFlowSpeedMax = 30.0f;   // flow_map.comp: SPEED_MAX, cells/s
+constexpr float kFlowPeriodShort = 4.0f;  // mod.rs FLOW_PERIOD_SHORT, s
+constexpr float kFlowPeriodLong = 12.0f;  // mod.rs FLOW_PERIOD_LONG, s
+__global__ void __launch_bounds__(256) k_flow_map(DevScene d, const ushort4* sm, ushort4* flow, const RenderClock* c) {
+    if (!c->run) return;
+    const int cx = blockIdx.x * 16 + threadIdx.x, cy = blockIdx.y * 16 + threadIdx.y;
+    if (cx >= d.W || cy >= d.H) return;
+    const size_t nc = (size_t)d.W * d.H, i = (size_t)cy * d.W + cx;
+    const float dt = c->dt, now = c->now;
+    const float occ = from_half4(sm[(size_t)4 * nc + i]).w;
+    float ux = 0.0f, uy = 0.0f;
+    if (occ > 0.02f) {
+        const float4 v = from_half4(sm[(size_t)7 * nc + i]);
+        ux = v.z / occ;
+        uy = v.w / occ;
+    }
+    const float s = len2(ux, uy);
+    if (s > kFlowSpeedMax) {
+        const float k = kFlowSpeedMax / s;
+        ux *= k;
+        uy *= k;
+    }
+    const float fx = ((float)cx + 0.5f) - ux * dt, fy = ((float)cy + 0.5f) - uy * dt;
+    // sample_at: bilinear at a cell-centred position, clamped to the grid
+    const float qx = clampf(fx - 0.5f, 0.0f, (float)(d.W - 1)), qy = clampf(fy - 0.5f, 0.0f, (float)(d.H - 1));
+    // a position that is not a number (a texel that overflowed half) samples cell 0
+    const int i0x = qx == qx ? (int)floorf(qx) : 0, i0y = qy == qy ? (int)floorf(qy) : 0;
+    const int i1x = min(i0x + 1, d.W - 1), i1y = min(i0y + 1, d.H - 1);
+    const float tx = qx - (float)i0x, ty = qy - (float)i0y;
+    const int src = 2 * (int)c->src, dst = 2 * (1 - (int)c->src);
+    for (int k = 0; k < 2; k++) {
+        const float period = k == 0 ? kFlowPeriodShort : kFlowPeriodLong;
+        const ushort4* L = flow + (size_t)(src + k) * nc;
+        const float4 a = mix4(from_half4(L[(size_t)i0y * d.W + i0x]), from_half4(L[(size_t)i0y * d.W + i1x]), tx);
+        const float4 b = mix4(from_half4(L[(size_t)i1y * d.W + i0x]), from_half4(L[(size_t)i1y * d.W + i1x]), tx);
+        const float4 sa = mix4(a, b, ty);
+        float4 o = f4(sa.x + ux * dt, sa.y + uy * dt, sa.z + ux * dt, sa.w + uy * dt);
+        // restarted(period, o): floor(now / period + o) != floor((now - dt) / period + o)
+        const float before = now - dt;
+        if (floorf(now / period + 0.0f) != floorf(before / period + 0.0f)) o.x = o.y = 0.0f;
+        if (floorf(now / period + 0.5f) != floorf(before / period + 0.5f)) o.z = o.w = 0.0f;
+        flow[(size_t)(dst + k) * nc + i] = to_half4(o);
+    }
+}
+
 }  // namespace
 
+void launch_render_clock(const DevScene& d, RenderClock* clock, int valid, int changed, cudaStream_t st) {
+    k_render_clock<<<1, 1, 0, st>>>(d.S, clock, valid, changed);
+}
+
 void launch_cell_optics(const DevScene& d, const DevOptics* opt, float inv_speed, int sss_iters, ushort4* raw,
-                        ushort4* smooth, ushort4* glow_a, ushort4* glow_b, cudaStream_t st) {
+                        ushort4* smooth, ushort4* flow, const RenderClock* clock, ushort4* glow_a, ushort4* glow_b,
+                        cudaStream_t st) {
     const dim3 tiles((d.W + 15) / 16, (d.H + 15) / 16), block(16, 16);
     k_cell_optics<<<tiles, block, 0, st>>>(d, opt, inv_speed, raw);
     k_light<<<d.W, 64, 0, st>>>(d, raw);
@@ -534,6 +606,7 @@ void launch_cell_optics(const DevScene& d, const DevOptics* opt, float inv_speed
         k_sss<<<tiles, block, 0, st>>>(d, raw, smooth, 0, 20);
         for (int k = 0; k < iters; k++) k_sss<<<tiles, block, 0, st>>>(d, raw, smooth, 1, k % 2 == 0 ? 20 : 21);
     }
+    k_flow_map<<<tiles, block, 0, st>>>(d, smooth, flow, clock);   // mod.rs:1673-1680
     const dim3 half(((d.W + 1) / 2 + 15) / 16, ((d.H + 1) / 2 + 15) / 16);
     for (int dir = 0; dir < 2; dir++) k_glow<<<half, block, 0, st>>>(d, raw, glow_a, glow_b, dir);
 }

@@ -456,6 +456,7 @@ struct SproutSim {
         bool mchg = last_mats.empty() || std::memcmp(mats.data(), last_mats.data(), sizeof(DevMat) * kMaxMaterials) != 0;
         if (!pchg && !mchg) return SPROUT_OK;
         enqueued = true;
+        tables_gen++;
         CUDA_TRY(cudaEventSynchronize(stage_done));
         if (pchg) {
             *stage_params = P;
@@ -481,6 +482,7 @@ struct SproutSim {
         int rc = ensure_graph();
         if (rc != SPROUT_OK) return rc;
         CUDA_TRY(cudaEventRecord(a, stream));
+        substeps_issued += substeps;
         for (uint32_t k = 0; k < substeps; k++) {
             if (use_graph && graph_ok) CUDA_TRY(cudaGraphLaunch(exec, stream));
             else record_substep(stream);
@@ -501,6 +503,7 @@ struct SproutSim {
         cudaEvent_t ev[kStages + 1];
         for (auto& e : ev) CUDA_TRY(cudaEventCreate(&e));
         CUDA_TRY(cudaEventRecord(ev[0], stream));
+        substeps_issued++;
         for (int k = 0; k < kStages; k++) {
             record_stage(k, stream);
             CUDA_TRY(cudaEventRecord(ev[k + 1], stream));
@@ -766,6 +769,8 @@ struct SproutSim {
         CUDA_TRY(cudaMemset(d.ledger, 0, 8 * sizeof(unsigned long long)));
         sim_time = 0.0;
         dt_est = kNominalDt;
+        resets++;
+        stain_valid = false;
         return upload_tables(nullptr);
     }
 
@@ -974,13 +979,21 @@ struct SproutSim {
     }
 
     // ---- the render side's cell passes (optics.cu; FluidSim::record_cell_optics) ----
-    static constexpr int kRenderLayers = 20, kSmoothLayers = 24;
+    static constexpr int kRenderLayers = 20, kSmoothLayers = 24, kFlowLayers = 4;
     DevOptics* d_optics = nullptr;
     ushort4* d_raw = nullptr;      // cell_optics.comp + light.comp
     ushort4* d_smooth = nullptr;   // optics_blur.comp (0-19), sss.comp (20-23)
+    ushort4* d_flow = nullptr;     // flow_map.comp: two copies of (short, long period)
     ushort4* d_glow = nullptr;     // glow.comp: two half-resolution images
+    RenderClock* d_clock = nullptr;
     size_t glow_texels() const { return (size_t)((W + 1) / 2) * ((H + 1) / 2); }
-    std::vector<DevOptics> h_optics;
+    std::vector<DevOptics> h_optics, last_optics;
+    // The reference records nothing when nothing changed since its last call (optics_key:
+    // substeps done, resets, table uploads, inv_speed), and keeps the time of the last call
+    // for the tank it was made on (stain_at).
+    uint64_t substeps_issued = 0, resets = 0, tables_gen = 0;
+    uint64_t render_key[4] = {0, 0, 0, 0};
+    bool render_key_set = false, stain_valid = false;
     int render(float inv_speed) {
         if (!was_reset) return fail(SPROUT_E_ARG, "render before reset");
         int rc = upload_tables(nullptr);
@@ -989,15 +1002,42 @@ struct SproutSim {
         if (!d_raw) {
             if ((rc = alloc(&d_raw, kRenderLayers * nc)) != SPROUT_OK) return rc;
             if ((rc = alloc(&d_smooth, kSmoothLayers * nc)) != SPROUT_OK) return rc;
+            if ((rc = alloc(&d_flow, kFlowLayers * nc)) != SPROUT_OK) return rc;
             if ((rc = alloc(&d_glow, 2 * glow_texels())) != SPROUT_OK) return rc;
             if ((rc = alloc(&d_optics, kMaxMaterials)) != SPROUT_OK) return rc;
+            if ((rc = alloc(&d_clock, 1)) != SPROUT_OK) return rc;
+            CUDA_TRY(cudaMemsetAsync(d_clock, 0, sizeof(RenderClock), stream));
         }
         h_optics.resize(kMaxMaterials);
         optics_table(params, h_optics.data());
-        CUDA_TRY(cudaMemcpyAsync(d_optics, h_optics.data(), sizeof(DevOptics) * kMaxMaterials, cudaMemcpyHostToDevice, stream));
-        launch_cell_optics(d, d_optics, inv_speed, (int)params.sss_iters, d_raw, d_smooth, d_glow, d_glow + glow_texels(),
-                           stream);
+        if (last_optics.size() != h_optics.size() ||
+            std::memcmp(last_optics.data(), h_optics.data(), sizeof(DevOptics) * kMaxMaterials) != 0) {
+            CUDA_TRY(cudaMemcpyAsync(d_optics, h_optics.data(), sizeof(DevOptics) * kMaxMaterials, cudaMemcpyHostToDevice,
+                                     stream));
+            last_optics = h_optics;
+            tables_gen++;
+        }
+        // a new tank: nothing carried (mod.rs:1631-1638)
+        if (!stain_valid) CUDA_TRY(cudaMemsetAsync(d_flow, 0, sizeof(ushort4) * kFlowLayers * nc, stream));
+        const uint64_t key[4] = {substeps_issued, resets, tables_gen, (uint64_t)__builtin_bit_cast(uint32_t, inv_speed)};
+        const bool changed = !render_key_set || std::memcmp(key, render_key, sizeof key) != 0;
+        launch_render_clock(d, d_clock, stain_valid ? 1 : 0, changed ? 1 : 0, stream);
+        stain_valid = true;
+        if (changed) {
+            std::memcpy(render_key, key, sizeof key);
+            render_key_set = true;
+            launch_cell_optics(d, d_optics, inv_speed, (int)params.sss_iters, d_raw, d_smooth, d_flow, d_clock, d_glow,
+                               d_glow + glow_texels(), stream);
+        }
         CUDA_TRY(cudaGetLastError());
+        return SPROUT_OK;
+    }
+    int flow_parity(uint32_t* parity) {
+        if (!d_clock) return fail(SPROUT_E_ARG, "flow_parity before render");
+        RenderClock c;
+        CUDA_TRY(cudaMemcpyAsync(&c, d_clock, sizeof c, cudaMemcpyDeviceToHost, stream));
+        CUDA_TRY(cudaStreamSynchronize(stream));
+        *parity = c.parity;
         return SPROUT_OK;
     }
 
@@ -1095,6 +1135,7 @@ struct SproutSim {
         spawn_speed = 0.0f;
         if (rc != SPROUT_OK) return rc;
         if (substeps == 0) return SPROUT_OK;
+        substeps_issued += substeps;
         const uint32_t fl = __builtin_bit_cast(uint32_t, std::max(target, 0.0f));
         if (!words_cached || batch_words[0] != fl || batch_words[1] != substeps) {
             batch_words[0] = fl;
@@ -2188,19 +2229,30 @@ int sprout_sim_render(SproutSim* sim, float inv_speed) {
 
 int sprout_sim_download_render(SproutSim* sim, int which, uint16_t* out, size_t cap, size_t* words) {
     if (!sim || !words) return fail(SPROUT_E_ARG, "null argument");
-    if (which < 0 || which > 2) return fail(SPROUT_E_ARG, "download_render: which is 0 (raw), 1 (smoothed) or 2 (glow)");
+    if (which < 0 || which > 3)
+        return fail(SPROUT_E_ARG, "download_render: which is 0 (raw), 1 (smoothed), 2 (glow) or 3 (flow map)");
     const size_t nc = (size_t)sim->W * sim->H;
-    const size_t n = 4 * (which == 0 ? SproutSim::kRenderLayers * nc : which == 1 ? SproutSim::kSmoothLayers * nc : sim->glow_texels());
+    const size_t n = 4 * (which == 0   ? SproutSim::kRenderLayers * nc
+                          : which == 1 ? SproutSim::kSmoothLayers * nc
+                          : which == 2 ? sim->glow_texels()
+                                       : SproutSim::kFlowLayers * nc);
     *words = n;
     if (!out) return SPROUT_OK;
     if (cap < n) return fail(SPROUT_E_ARG, "download_render: the output holds fewer words than the layers");
     if (!sim->d_raw) return fail(SPROUT_E_ARG, "download_render before render");
     CUDA_TRY(cudaStreamSynchronize(sim->stream));
-    const void* src = which == 0 ? (const void*)sim->d_raw : which == 1 ? (const void*)sim->d_smooth
-                                                                        : (const void*)(sim->d_glow + sim->glow_texels());
+    const void* src = which == 0   ? (const void*)sim->d_raw
+                      : which == 1 ? (const void*)sim->d_smooth
+                      : which == 2 ? (const void*)(sim->d_glow + sim->glow_texels())
+                                   : (const void*)sim->d_flow;
     CUDA_TRY(cudaMemcpy(out, src, n * sizeof(uint16_t), cudaMemcpyDeviceToHost));
     sim->d2h_bytes += n * sizeof(uint16_t);
     return SPROUT_OK;
+}
+
+int sprout_sim_flow_parity(SproutSim* sim, uint32_t* parity) {
+    if (!sim || !parity) return fail(SPROUT_E_ARG, "null argument");
+    return sim->flow_parity(parity);
 }
 
 int sprout_sim_cell_counts(SproutSim* sim, const int32_t lo[2], const int32_t hi[2], uint32_t* out, size_t cap,

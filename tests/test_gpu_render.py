@@ -1,5 +1,5 @@
 """The render side's cell passes on the device (sprout_sim_render: cell_optics.comp, light.comp,
-optics_blur.comp) against the oracle's restatement (osim_render) on the same grid, bit for bit
+optics_blur.comp, sss.comp, flow_map.comp, glow.comp) against the oracle's restatement (osim_render) on the same grid, bit for bit
 in their RGBA16F texels: the state after a few substeps is itself bit-exact between engine and
 oracle (run_pair), and both passes take the engine's optics table, which test_optics.py pins to
 its own restatement. Tanks that reach the branches: eight custom liquids over a heater (glow,
@@ -45,7 +45,7 @@ def test_cell_passes_bit_exact(name):
     tank = {"full_physics": lambda: tanks.full_physics(96, 64, cell=0.0106),
             "honey_dam": lambda: tanks.honey_dam(), "water_oil": lambda: tanks.water_oil(),
             "cooling_lava": lambda: tanks.cooling_lava(), "magnetic": lambda: tanks.magnetic()}[name]()
-    sim, (er, es, eg), (orw, osm, og) = render_pair(tank, 6)
+    sim, (er, es, eg), (orw, osm, og, _, _) = render_pair(tank, 6)
     for a, b, what in ((er, orw, "raw"), (es, osm, "smoothed")):
         m = diff(a, b, what)
         assert m is None, m
@@ -83,3 +83,59 @@ def test_render_is_what_the_reference_draws():
     col = light[:, 10]
     assert np.all(np.diff(col[::-1]) <= 0.0)   # from the top down, never brighter
     assert np.all(raw[0][occ == 0.0] == 0.0)
+
+
+def test_flow_map_bit_exact():
+    """flow_map.comp over frames of a dam break against the oracle, with record_cell_optics'
+    clock and key: the first call on a new tank carries nothing; a call after substeps advances
+    the map by the simulated time since the last call and swaps its copies; a call with no
+    substep since the last records nothing (the map, its copy and sss.comp's warm start stay as
+    they were); crossing t = 2 s restarts the short period's second pair (zw: floor(t / 4 +
+    0.5) changes); a reset clears the map."""
+    tank = tanks.dam_break(96, 64)
+    sim, _, _ = render_pair(tank, 6)
+    ora, table = render_pair.ora, render_pair.table
+    inv = 1.0 / 80.0
+
+    def frame(substeps):
+        for _ in range(substeps):
+            sim.step(1, 1 / 240.0)
+            ora.step(1, 1 / 240.0)
+        sim.render(inv)
+        o = ora.render(table.optics_table(), inv, int(table.get("sss_iters")))
+        e_flow, e_par = sim.download_render("flow"), sim.flow_parity()
+        assert e_par == o[4], f"flow parity {e_par} vs {o[4]}"
+        m = diff(e_flow, o[3], "flow map")
+        assert m is None, m
+        m = diff(sim.download_render("smoothed"), o[1], "smoothed")
+        assert m is None, m
+        return e_flow, e_par
+
+    f0 = sim.download_render("flow")
+    assert not np.any(f0.view(np.uint16)), "the first call on a new tank carries nothing"
+    p0 = sim.flow_parity()
+    f1, p1 = frame(4)
+    assert p1 == 1 - p0
+    moved = f1[2 * p1].astype(np.float32)
+    assert np.abs(moved).max() > 0.0, "the liquid moved the map"
+    sm1 = sim.download_render("smoothed")
+    f2, p2 = frame(0)   # nothing new: nothing recorded
+    assert p2 == p1 and np.array_equal(f2.view(np.uint16), f1.view(np.uint16))
+    assert np.array_equal(sim.download_render("smoothed").view(np.uint16), sm1.view(np.uint16))
+    for n in (4, 3, 5):
+        frame(n)
+    # up to just before t = 2 s, then across it
+    done = 6 + 4 + 3 + 4 + 5
+    frame(476 - done)
+    f3, p3 = frame(8)
+    short_zw = f3[2 * p3, ..., 2:].astype(np.float32)
+    short_xy = f3[2 * p3, ..., :2].astype(np.float32)
+    assert not np.any(short_zw), "the short period's second pair restarted at t = 2 s"
+    assert np.abs(short_xy).max() > 0.0
+    # a reset of the same sim: the next call clears the map and keeps the copy that holds it
+    _, parts, _ = tank.engine()
+    sim.reset(parts)
+    sim.step(2, 2 / 240.0)
+    sim.render(inv)
+    assert not np.any(sim.download_render("flow").view(np.uint16))
+    assert sim.flow_parity() == p3
