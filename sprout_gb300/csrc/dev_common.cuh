@@ -52,6 +52,7 @@ struct DevScene {
     uint32_t* pkey;   // new cell of each advanced particle (0xffffffff: dead)
     uint32_t* prank;  // its arrival rank in that cell
     uint32_t* perm;   // sorted slot -> slot in part2
+    uint32_t* crowd;  // the sort's cells of more than 16 particles: [0] how many, then the cells
     uint32_t* count;  // particles per cell (ncell + 1)
     uint32_t* start;  // first sorted slot of each cell (ncell + 1)
     uint32_t* scan_tmp;

@@ -4,7 +4,7 @@
 //               collisions, crowd jitter (particles.comp:98-949); float4 particle loads;
 //               emits the particle's new cell and its arrival rank there
 //   scan        exclusive scan of the per-cell counts
-//   k_place / k_cell_sort / k_cell_gather
+//   k_place / k_cell_sort / k_crowd_sort / k_cell_gather
 //               a stable counting sort by cell (ties by slot), the permutation the
 //               reference's sort.comp:83-119 defines up to its within-cell atomic order:
 //               ranks by arrival, each cell's few entries put in slot order, then one thread
@@ -818,12 +818,13 @@ __global__ void k_place(DevScene d) {
     d.perm[d.start[key] + d.prank[i]] = i;
 }
 
-// One thread per cell: orders the cell's arrivals by slot (insertion sort in registers for
-// up to 16, in place otherwise), then copies the particles into their sorted slots.
-// Threads past the last cell clear the slots after the live particles.
 // Each cell's arrivals in slot order: the stable order of the counting sort (sort.comp keeps
 // a cell's particles in arrival order, which atomics make arbitrary; slot order makes it
-// deterministic). One thread per cell sorts the cell's few entries of perm in place.
+// deterministic). One thread per cell sorts up to 16 entries of perm in registers; a cell with
+// more goes on the crowd list for k_crowd_sort (a thread's sort in place in global memory
+// costs two dependent global accesses per step, and one cell of 60 took 0.25 ms).
+constexpr int kCrowdMax = 4096;    // entries a block sorts in shared memory
+constexpr int kCrowdBlocks = 152;  // k_crowd_sort's grid: one block per SM over the list
 __global__ void __launch_bounds__(256) k_cell_sort(DevScene d) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= d.ncell) return;
@@ -847,7 +848,10 @@ __global__ void __launch_bounds__(256) k_cell_sort(DevScene d) {
 #pragma unroll
         for (int k = 0; k < 16; k++)
             if ((uint32_t)k < n) seg[k] = v[k];
-    } else {
+    } else if (n <= (uint32_t)kCrowdMax) {
+        const uint32_t at = atomicAdd(&d.crowd[0], 1u);   // at most ncell cells: the list holds them
+        d.crowd[1 + at] = (uint32_t)c;
+    } else {   // (more particles in one cell than a block sorts in shared memory)
         for (uint32_t k = 1; k < n; k++) {
             const uint32_t x = seg[k];
             int j = (int)k - 1;
@@ -857,6 +861,29 @@ __global__ void __launch_bounds__(256) k_cell_sort(DevScene d) {
             }
             seg[j + 1] = x;
         }
+    }
+}
+
+// The crowded cells, a block each: the entries (distinct slots) into shared memory, each
+// entry's place = how many entries are smaller, written back in that order.
+__global__ void __launch_bounds__(256) k_crowd_sort(DevScene d) {
+    __shared__ uint32_t in[kCrowdMax], out[kCrowdMax];
+    const uint32_t cells = d.crowd[0];
+    for (uint32_t b = blockIdx.x; b < cells; b += gridDim.x) {
+        const uint32_t c = d.crowd[1 + b];
+        const uint32_t n = d.count[c];
+        uint32_t* seg = d.perm + d.start[c];
+        for (uint32_t k = threadIdx.x; k < n; k += blockDim.x) in[k] = seg[k];
+        __syncthreads();
+        for (uint32_t k = threadIdx.x; k < n; k += blockDim.x) {
+            const uint32_t x = in[k];
+            uint32_t r = 0;
+            for (uint32_t j = 0; j < n; j++) r += in[j] < x ? 1u : 0u;
+            out[r] = x;
+        }
+        __syncthreads();
+        for (uint32_t k = threadIdx.x; k < n; k += blockDim.x) seg[k] = out[k];
+        __syncthreads();
     }
 }
 
@@ -1057,7 +1084,9 @@ void launch_sort(const DevScene& d, const LaunchCfg& cfg, cudaStream_t st) {
     k_scan_top<<<1, SCAN_BLOCK, 0, st>>>(d.scan_tmp, sb, d.S);
     k_scan_add<<<sb, SCAN_BLOCK, 0, st>>>(d.start, d.scan_tmp, n);
     k_place<<<nb, 256, 0, st>>>(d);
+    cudaMemsetAsync(d.crowd, 0, sizeof(uint32_t), st);
     k_cell_sort<<<(d.ncell + 255) / 256, 256, 0, st>>>(d);
+    k_crowd_sort<<<kCrowdBlocks, 256, 0, st>>>(d);
     k_cell_gather<<<nb, 256, 0, st>>>(d);
 }
 

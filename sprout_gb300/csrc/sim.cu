@@ -251,6 +251,7 @@ struct SproutSim {
         A(d.pkey, cap);
         A(d.prank, cap);
         A(d.perm, cap);
+        A(d.crowd, nc + 1);
         A(d.count, nc + 1);
         A(d.start, nc + 1);
         A(d.scan_tmp, (nc + 1 + 1023) / 1024 + 1);
