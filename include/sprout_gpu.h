@@ -270,6 +270,13 @@ int sprout_params_get_row(const SproutParams* p, uint32_t row, int32_t* group, i
  * (flow_map.comp) advances by the simulated time since the last call (at most 0.25 s, read on
  * the device) and is cleared by the first call on a new tank. */
 int sprout_sim_render(SproutSim* sim, float inv_speed);
+/* FluidSim::recorded_iters (mod.rs:1965-1968): the iterations the next substeps record for
+ * the first pressure solve, the second and the viscosity solve (blocking). A solve that has
+ * not converged stops there (rounded up to even; the Jacobi viscosity solve to a multiple of
+ * 4). As in the reference, a new scene records pressure_max_iters / viscosity_max_iters, and
+ * every step call (a frame; each substep of sprout_sim_profile) adapts them from its own
+ * solves when it ends (mod.rs:3093-3114), where the reference adapts on the frame's read-back. */
+int sprout_sim_recorded_iters(SproutSim* sim, uint32_t out[3]);
 /* FluidSim::flow_view's parity (mod.rs:1850-1853): the copy of the flow map that holds it now
  * (blocking). */
 int sprout_sim_flow_parity(SproutSim* sim, uint32_t* parity);

@@ -69,6 +69,7 @@ class OSimParams(C.Structure):
         ("magnet_demag", C.c_float),
         ("elastic_stress_max", C.c_float), ("elastic_step_max", C.c_float),
         ("rigid_contact", C.c_uint32), ("rigid_friction", C.c_float),
+        ("iters_margin", C.c_float),
     ]
 
 
@@ -161,6 +162,8 @@ def lib() -> C.CDLL:
         L.osim_render.restype = C.c_long
         L.osim_flow_map.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_float, C.c_float, C.c_uint32]
         L.osim_flow_map.restype = C.c_long
+        L.osim_recorded_iters.argtypes = [C.c_void_p, C.c_void_p]
+        L.osim_recorded_iters.restype = None
         L.o_expf.argtypes = [C.c_float]
         L.o_expf.restype = C.c_float
         _lib = L
@@ -301,6 +304,12 @@ class OracleSim:
         out = np.zeros(n, np.uint32)
         lib().osim_cell_counts(self.h_, a, b, out.ctypes.data, n)
         return out.reshape(max(hi[1] - lo[1], 0), max(hi[0] - lo[0], 0))
+
+    def recorded_iters(self) -> list:
+        """FluidSim::recorded_iters: [first pressure solve, second, viscosity]."""
+        v = (C.c_uint32 * 3)()
+        lib().osim_recorded_iters(self.h_, v)
+        return [int(x) for x in v]
 
     def step(self, substeps: int, target: float = 0.0, tool: OTool | None = None):
         if substeps > 0:

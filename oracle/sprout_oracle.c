@@ -255,6 +255,7 @@ void oparams_default(OSimParams* p) {
     p->fixed_hz = 0.0f;
     p->pressure_tol = 1e-4f;
     p->pressure_max_iters = 60;
+    p->iters_margin = 0.25f;
     p->correction_tol = 1e-2f;
     p->viscosity_tol = 1e-3f;
     p->viscosity_max_iters = 200;
@@ -655,6 +656,9 @@ typedef struct SolveBuf {   /* common.glsl:138-149 */
     uint32_t v_done, v_iters, v_it_max, v_unconv;
     float v_res_max;
     uint32_t p1_iters[2], p2_last;   /* bookkeeping: the last first and second solves' iterations */
+    /* the recorded iteration counts (pressure_rec, pressure2_rec, viscosity_rec), the limits a
+     * frame's solves stop at, and the frame's most iterations and unconverged solves */
+    uint32_t rec[3], cap[3], f_it[3], f_un[3];
 } SolveBuf;
 
 typedef struct Levels {   /* mod.rs:714-753 */
@@ -3764,16 +3768,20 @@ static void reduce_end(OSim* s, int mode) {
         uint32_t m = K->p_iters[0] > K->p_iters[1] ? K->p_iters[0] : K->p_iters[1];
         if (m > K->p_it_max) K->p_it_max = m;
         if (K->p_done[0] == 0u) K->p_unconv += 1u;
+        if (m > K->f_it[0]) K->f_it[0] = m;
+        if (K->p_done[0] == 0u) K->f_un[0] += 1u;
     } else {
         if (K->p_iters[0] > K->p2_it_max) K->p2_it_max = K->p_iters[0];
         if (K->p_done[0] == 0u) K->p2_unconv += 1u;
+        if (K->p_iters[0] > K->f_it[1]) K->f_it[1] = K->p_iters[0];
+        if (K->p_done[0] == 0u) K->f_un[1] += 1u;
     }
     float rel = K->p_bb[0] > 0.0f ? sqrtf(K->p_rr[0] / K->p_bb[0]) : 0.0f;
     K->p_res_max = maxf(K->p_res_max, rel);
 }
 
-/* record_pressure + record_cg (mod.rs:2956-3010) with the device-decided loop: the
- * iterations run until both potentials are done or pressure_max_iters have run. */
+/* record_pressure + record_cg (mod.rs:2956-3010): the iterations run until both potentials
+ * are done or the frame's recorded iterations (K.cap) have run. */
 static void pressure_solve(OSim* s, int second) {
     if (!second) {
         for (int l = 1; l <= s->lv.tail; l++) k_mg_build(s, l - 1);
@@ -3786,7 +3794,8 @@ static void pressure_solve(OSim* s, int second) {
     reduce_start(s, second ? 8 : 0);
     V2* pa = s->cgp;
     V2* pb = s->cgp2;
-    for (uint32_t k = 0; k < s->prm.pressure_max_iters; k++) {
+    const uint32_t cap = s->K.cap[second ? 1 : 0];
+    for (uint32_t k = 0; k < cap; k++) {
         if (s->K.p_done[0] && s->K.p_done[1]) break;
         k_cg_apply(s, pa, pb);
         reduce_alpha(s);
@@ -4428,7 +4437,7 @@ static void viscosity_jacobi(OSim* s) {
     V2* P = (V2*)malloc((size_t)n * sizeof(V2));
     V4* S = (V4*)malloc((size_t)n * sizeof(V4));
     V2 *pa = s->vp, *pb = s->vr2;
-    for (uint32_t k = 0; k < s->prm.viscosity_max_iters && !K->v_done; k++) {
+    for (uint32_t k = 0; k < K->cap[2] && !K->v_done; k++) {
         float b = K->v_beta;
 #pragma omp parallel for schedule(static) num_threads(g_threads)
         for (int i = 0; i < n; i++) {
@@ -4518,7 +4527,7 @@ static void viscosity_solve(OSim* s, int restrain) {
         if (a.x <= 0.0f || a.y <= 0.0f) K->v_done = 1u;
     }
     V2* newr = (V2*)malloc((size_t)n * sizeof(V2));
-    for (uint32_t k = 0; k < s->prm.viscosity_max_iters && !K->v_done; k++) {
+    for (uint32_t k = 0; k < K->cap[2] && !K->v_done; k++) {
         V2 *Rold = (k % 2 == 0) ? RA : RB, *Qold = (k % 2 == 0) ? QA : QB;
         V2 *Rnew = (k % 2 == 0) ? RB : RA, *Qnew = (k % 2 == 0) ? QB : QA;
         mgu_new_r(s, Rold, Qold, newr);
@@ -4551,6 +4560,8 @@ stats:
     /* mode 7 */
     if (K->v_iters > K->v_it_max) K->v_it_max = K->v_iters;
     if (K->v_done == 0u) K->v_unconv += 1u;
+    if (K->v_iters > K->f_it[2]) K->f_it[2] = K->v_iters;
+    if (K->v_done == 0u) K->f_un[2] += 1u;
     float rel = K->v_r0 > 0.0f ? sqrtf(K->v_rr / K->v_r0) : 0.0f;
     K->v_res_max = maxf(K->v_res_max, rel);
 }
@@ -4870,6 +4881,8 @@ static int set_tank(OSim* s, const int* present_in, int thermal) {
     return 0;
 }
 
+static uint32_t recorded_limit(uint32_t rec, int viscosity, int mg_precond);
+
 int osim_reset(OSim* s, const OParticle* in, uint32_t n) {
     if (n > s->capacity) n = s->capacity;
     const OSimParams* p = &s->prm;
@@ -4896,6 +4909,13 @@ int osim_reset(OSim* s, const OParticle* in, uint32_t n) {
     memset(s->pres, 0, nc * sizeof(V2));
     memset(s->p2keep, 0, nc * sizeof(float));
     memset(&s->S, 0, sizeof s->S);
+    /* a new scene records the most until its frames say otherwise (mod.rs:2478-2483) */
+    s->K.rec[0] = s->K.rec[1] = p->pressure_max_iters;
+    s->K.rec[2] = p->viscosity_max_iters;
+    for (int k = 0; k < 3; k++) {
+        s->K.cap[k] = recorded_limit(s->K.rec[k], k == 2, p->viscosity_precond != 0);
+        s->K.f_it[k] = s->K.f_un[k] = 0u;
+    }
     memset(s->dheat, 0, nc * sizeof(V4));
     memset(s->ledger, 0, sizeof s->ledger);
     s->grid_valid = 0;
@@ -4977,6 +4997,47 @@ long osim_cell_counts(const OSim* s, const int lo[2], const int hi[2], uint32_t*
     return (long)n;
 }
 
+/* The iterations a frame records for a solve (mod.rs:2569, 2603-2606): its count rounded up
+ * to even, the viscosity solve's to a multiple of 4 with the Jacobi preconditioner. */
+static uint32_t recorded_limit(uint32_t rec, int viscosity, int mg_precond) {
+    uint32_t q = (viscosity && !mg_precond) ? 4u : 2u;
+    return (rec + q - 1u) / q * q;
+}
+
+/* poll_readbacks' adaptation (mod.rs:3100-3106). */
+static uint32_t adapt_rec(uint32_t rec, uint32_t used, uint32_t unconverged, uint32_t max, float margin) {
+    if (unconverged > 0u) {
+        uint32_t v = rec + rec / 2u + 2u;
+        return v < max ? v : max;
+    }
+    uint32_t v = used + (uint32_t)((float)used * margin) + 2u;
+    return v < 2u ? 2u : (v > max ? max : v);
+}
+
+/* The end of a frame (a step call): the recorded counts adapted from the frame's solves as the
+ * reference adapts them when the frame's read-back arrives (mod.rs:3093-3114), the limits of
+ * the next frame, the frame's statistics cleared. */
+static void frame_end(OSim* s) {
+    SolveBuf* K = &s->K;
+    float margin = maxf(s->prm.iters_margin, 0.0f);
+    uint32_t pmax = s->prm.pressure_max_iters, vmax = s->prm.viscosity_max_iters;
+    K->rec[0] = adapt_rec(K->rec[0], K->f_it[0], K->f_un[0], pmax, margin);
+    if (s->visc_mode == 2 && s->prm.viscous_projection != 0)
+        K->rec[1] = adapt_rec(K->rec[1], K->f_it[1], K->f_un[1], pmax, margin);
+    else
+        K->rec[1] = K->rec[0];
+    K->rec[2] = adapt_rec(K->rec[2], K->f_it[2], K->f_un[2], vmax, 0.5f);
+    for (int k = 0; k < 3; k++) {
+        K->cap[k] = recorded_limit(K->rec[k], k == 2, s->prm.viscosity_precond != 0);
+        K->f_it[k] = 0u;
+        K->f_un[k] = 0u;
+    }
+}
+
+void osim_recorded_iters(const OSim* s, uint32_t out[3]) {
+    for (int k = 0; k < 3; k++) out[k] = s->K.rec[k];
+}
+
 int osim_step(OSim* s, uint32_t substeps, float target, const OTool* tool) {
     take_spawns(s);
     build_params(s, tool);
@@ -4996,6 +5057,7 @@ int osim_step(OSim* s, uint32_t substeps, float target, const OTool* tool) {
         s->grid_valid = 1;
         s->substeps_done++;
     }
+    if (substeps > 0) frame_end(s);
     s->sim_time = s->S.advanced;
     return 0;
 }

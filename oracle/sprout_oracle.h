@@ -97,6 +97,7 @@ typedef struct OSimParams {
     float elastic_stress_max, elastic_step_max;
     uint32_t rigid_contact;
     float rigid_friction;
+    float iters_margin;   /* params.rs:284: the recorded iterations' margin */
 } OSimParams;
 
 /* ToolState (src/sim/params.rs:1141-1213). */
@@ -175,6 +176,8 @@ long osim_field(const OSim* s, const char* name, void* out, size_t cap);
 long osim_render(const OSim* s, const void* optics, float inv_speed, int sss_iters, uint16_t* raw, uint16_t* smooth,
                  uint16_t* ga, uint16_t* gb);
 /* flow_map.comp over the grid from copy `src` of `flow` (4 layers) into the other copy. */
+/* FluidSim::recorded_iters: the recorded iteration counts (first solve, second, viscosity). */
+void osim_recorded_iters(const OSim* s, uint32_t out[3]);
 long osim_flow_map(const OSim* s, const uint16_t* smooth, uint16_t* flow, float dt, float now, uint32_t src);
 void osim_stats(const OSim* s, OStats* out);
 /* Test hook: the implicit viscosity's assembled level-0 matrix and its matrix-free operator

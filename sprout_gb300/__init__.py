@@ -50,7 +50,7 @@ EXPORTS = [
     "sprout_scene_rasterize_device", "sprout_sim_set_scene", "sprout_spout", "sprout_sim_emit_stream",
     "sprout_sim_emit_paint", "sprout_sim_emit_rain", "sprout_sim_emitter_seed", "sprout_sim_emitted",
     "sprout_params_optics", "sprout_params_set_color", "sprout_sim_render", "sprout_sim_download_render",
-    "sprout_params_get_color", "sprout_params_get_row", "sprout_sim_flow_parity",
+    "sprout_params_get_color", "sprout_params_get_row", "sprout_sim_flow_parity", "sprout_sim_recorded_iters",
 ]
 
 # One row of the optics table (material.rs GpuOptics): 15 four-word fields, 240 bytes.
@@ -194,6 +194,7 @@ def lib() -> C.CDLL:
         "sprout_params_set_color": ([V, C.c_uint32, C.c_char_p, P(C.c_float), P(C.c_int)], C.c_int),
         "sprout_sim_render": ([V, C.c_float], C.c_int),
         "sprout_sim_flow_parity": ([V, P(C.c_uint32)], C.c_int),
+        "sprout_sim_recorded_iters": ([V, P(C.c_uint32)], C.c_int),
         "sprout_params_get_color": ([V, C.c_uint32, C.c_char_p, P(C.c_float), P(C.c_int)], C.c_int),
         "sprout_params_get_row": ([V, C.c_uint32, P(C.c_int32), P(C.c_int32)], C.c_int),
         "sprout_sim_download_render": ([V, C.c_int, V, C.c_size_t, P(C.c_size_t)], C.c_int),
@@ -476,6 +477,12 @@ class FluidSim:
         optics_blur.comp, sss.comp, flow_map.comp and glow.comp; nothing when nothing changed
         since the last call."""
         _check(lib().sprout_sim_render(self._h, inv_speed))
+
+    def recorded_iters(self) -> list:
+        """FluidSim::recorded_iters: [first pressure solve, second, viscosity] (blocking)."""
+        v = (C.c_uint32 * 3)()
+        _check(lib().sprout_sim_recorded_iters(self._h, v))
+        return [int(x) for x in v]
 
     def flow_parity(self) -> int:
         """The copy of the flow map that holds it now (blocking)."""

@@ -119,6 +119,7 @@ struct DevParams {
     float mag[4];
     float magnet[kMaxMagnets][4];
     float magnet_dir[kMaxMagnets][4];
+    float iters_margin;   // recorded iterations' margin over the last frame's (params.rs:284)
 };
 
 // StepBuf (common.glsl:122-135) plus the engine's own step flags.
@@ -161,10 +162,29 @@ struct SolveState {
     uint32_t trace_rows, trace_cols;
     uint32_t trace_base;   // barriers of the earlier launches (rows of later ones follow on)
     uint32_t p_repl;       // mixed precision: residual replacements, all solves since the reset
+    // The reference's recorded iteration counts (FluidSim pressure_rec, pressure2_rec,
+    // viscosity_rec; mod.rs:3093-3114) for the first pressure solve, the second and the
+    // implicit viscosity solve: a solve that has not converged stops at cap, rec rounded up as
+    // the reference records it (mod.rs:2569, 2603-2606). A step call is a frame: its solves'
+    // most iterations (f_it) and unconverged solves (f_un) adapt rec when it ends (k_frame_end).
+    uint32_t rec[3], cap[3], f_it[3], f_un[3];
     // failure injection for tests (0: off): block dbg_block arrives dbg_stall_ns late at every
     // grid barrier, and a wait gives up after dbg_spin_limit polls instead of SPIN_LIMIT
     uint32_t dbg_block, dbg_stall_ns, dbg_spin_limit, pad3;
 };
+// The iterations a frame records for a solve from its recorded count (mod.rs:2569, 2603-2606):
+// rounded up to even, and the viscosity solve's to a multiple of 4 with the Jacobi
+// preconditioner (whose iterations cost less).
+#ifdef __CUDACC__
+#define SP_HOST_DEVICE __host__ __device__
+#else
+#define SP_HOST_DEVICE
+#endif
+SP_HOST_DEVICE inline uint32_t recorded_limit(uint32_t rec, bool viscosity, bool mg_precond) {
+    const uint32_t q = (viscosity && !mg_precond) ? 4u : 2u;
+    return (rec + q - 1u) / q * q;
+}
+
 // SolveState::error bits: a bounded wait ran out; a solve's residual or right-hand side was
 // not finite (the solve stopped)
 constexpr uint32_t ERR_TIMEOUT = 1u, ERR_DIVERGED = 2u;

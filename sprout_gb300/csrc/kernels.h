@@ -143,6 +143,10 @@ void launch_cell_optics(const DevScene& d, const DevOptics* opt, float inv_speed
 // the first call on a new tank (no step: the flow map does not run), `changed` 0 when the call
 // records nothing (its key is the last call's); the time since the last call from the
 // device's own simulated time.
+// The end of a frame (a step call, or each substep of a profile): FluidSim's adaptation of the
+// recorded iteration counts from the frame's solves (mod.rs:3093-3114) and the next limits.
+void launch_frame_end(const DevScene& d, cudaStream_t st);
+void launch_frame_end_many(const DevScene* scenes, int n, cudaStream_t st);   // a batch's members
 void launch_render_clock(const DevScene& d, RenderClock* clock, int valid, int changed, cudaStream_t st);
 // Scene::rasterize on the device (raster.cu): the tank's solid fields straight into device
 // buffers, bit-identical to the host's Scene::rasterize (scene.cpp).

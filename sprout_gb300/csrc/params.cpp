@@ -709,6 +709,7 @@ void build_params(const SimParams& p, const Tank& t, bool thermal, uint32_t caps
     P->viscous_warm = p.viscous_warm != 0 ? 1 : 0;
     P->viscous_projection = p.viscous_projection != 0 ? 1 : 0;
     P->viscosity_precond = p.viscosity_precond != 0 ? 1 : 0;
+    P->iters_margin = std::max(p.iters_margin, 0.0f);
 }
 
 }  // namespace sprout

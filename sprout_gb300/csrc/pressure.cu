@@ -1301,9 +1301,13 @@ DEV void scal_stats(SolveState* G, const Solve<T>& K, int second, double true_re
         uint32_t m = K.iters[0] > K.iters[1] ? K.iters[0] : K.iters[1];
         if (m > G->p_it_max) G->p_it_max = m;
         if (K.done[0] == 0u) G->p_unconv += 1u;
+        if (m > G->f_it[0]) G->f_it[0] = m;
+        if (K.done[0] == 0u) G->f_un[0] += 1u;
     } else {
         if (K.iters[0] > G->p2_it_max) G->p2_it_max = K.iters[0];
         if (K.done[0] == 0u) G->p2_unconv += 1u;
+        if (K.iters[0] > G->f_it[1]) G->f_it[1] = K.iters[0];
+        if (K.done[0] == 0u) G->f_un[1] += 1u;
     }
     if (K.bad) atomicOr(&G->error, ERR_DIVERGED);
     const float rel = K.bb[0] > 0 ? (float)sqrt((double)K.rr[0] / (double)K.bb[0]) : 0.0f;
@@ -1364,7 +1368,8 @@ __global__ void __launch_bounds__(NT, 2) k_mgpcg(DevScene d, int second, int sca
     float2* p_old = d.cgp;
     float2* p_new = d.cgp2;
     const Lv L0 = lev(d.lv, 0);
-    for (uint32_t it = 0; it < P->pressure_max_iters; it++) {
+    const uint32_t cap = d.K->cap[second ? 1 : 0];   // this frame's recorded iterations
+    for (uint32_t it = 0; it < cap; it++) {
         if (K.done[0] && K.done[1]) break;
         if constexpr (M::kMixed) {
             // the refinement (the same decisions in every block: the same K); q is free until
@@ -1541,7 +1546,7 @@ __global__ void __launch_bounds__(NT, 4) k_mgpcg_batch(BatchView B, int second) 
     // a scene takes part in iteration it while neither converged nor at its limit
     auto running = [&](int s, int it) {
         const Solve<acc>& K = KS[s];
-        return !(K.done[0] && K.done[1]) && (uint32_t)it < B.scenes[s].P->pressure_max_iters;
+        return !(K.done[0] && K.done[1]) && (uint32_t)it < B.scenes[s].K->cap[second ? 1 : 0];
     };
     if (!second) {
         for_tiles(B, 0, [&](int s, const DevScene& d, int t) { cg_scale_tile<M>(d, t, B.scale[s]); });
@@ -1799,6 +1804,46 @@ cudaError_t launch_pressure_batch(const BatchView& B, bool mixed, int blocks, si
     return cudaLaunchCooperativeKernel(fn, dim3(blocks), dim3(NT), args, smem, st);
 }
 
+// FluidSim::poll_readbacks' adaptation of a recorded iteration count (mod.rs:3100-3106):
+// after a frame in which the solve ran out, half again plus two; otherwise the frame's most
+// iterations plus the margin's share (truncated, as `as u32`) plus two, within [2, max].
+DEV uint32_t adapt_rec(uint32_t rec, uint32_t used, uint32_t unconverged, uint32_t max, float margin) {
+    if (unconverged > 0u) return min(rec + rec / 2u + 2u, max);
+    const uint32_t v = used + (uint32_t)((float)used * margin) + 2u;
+    return v < 2u ? 2u : (v > max ? max : v);
+}
+
+// The end of a frame (a step call): the recorded counts adapted from the frame's solves as
+// the reference adapts them when the frame's read-back arrives (mod.rs:3093-3114: the second
+// solve's follows the first's when it does not run; the viscosity solve's with margin 0.5),
+// the next frame's limits, and the frame's statistics cleared.
+DEV void frame_end(const DevScene& d) {
+    const DevParams* P = d.P;
+    SolveState* K = d.K;
+    K->rec[0] = adapt_rec(K->rec[0], K->f_it[0], K->f_un[0], P->pressure_max_iters, P->iters_margin);
+    if (P->visc_mode == 2 && P->viscous_projection != 0)
+        K->rec[1] = adapt_rec(K->rec[1], K->f_it[1], K->f_un[1], P->pressure_max_iters, P->iters_margin);
+    else
+        K->rec[1] = K->rec[0];
+    K->rec[2] = adapt_rec(K->rec[2], K->f_it[2], K->f_un[2], P->viscosity_max_iters, 0.5f);
+    for (int k = 0; k < 3; k++) {
+        K->cap[k] = recorded_limit(K->rec[k], k == 2, P->viscosity_precond != 0);
+        K->f_it[k] = 0u;
+        K->f_un[k] = 0u;
+    }
+}
+
+__global__ void k_frame_end(DevScene d) { frame_end(d); }
+__global__ void k_frame_end_many(const DevScene* scenes, int n) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < n) frame_end(scenes[s]);
+}
+
+void launch_frame_end(const DevScene& d, cudaStream_t st) { k_frame_end<<<1, 1, 0, st>>>(d); }
+void launch_frame_end_many(const DevScene* scenes, int n, cudaStream_t st) {
+    if (n > 0) k_frame_end_many<<<(n + 127) / 128, 128, 0, st>>>(scenes, n);
+}
+
 cudaError_t launch_pressure(const DevScene& d, const LaunchCfg& cfg, cudaStream_t st, int second) {
     // barrier counter back to zero (a solve left by a timeout may have stopped mid-barrier)
     cudaMemsetAsync(&d.K->bar_count, 0, sizeof(uint32_t), st);
@@ -1912,6 +1957,7 @@ __global__ void k_static_prep(DevScene d, const float4* mga, const float* mgd, c
         SolveState* K = d.K;
         unsigned char* k = reinterpret_cast<unsigned char*>(K);
         for (size_t b = 0; b < sizeof(SolveState); b++) k[b] = 0;
+        K->cap[0] = K->cap[1] = max_iters;   // the caller's limit, not a recorded count
     }
 }
 

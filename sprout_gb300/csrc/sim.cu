@@ -484,9 +484,10 @@ struct SproutSim {
         if (rc != SPROUT_OK) return rc;
         CUDA_TRY(cudaEventRecord(a, stream));
         substeps_issued += substeps;
-        for (uint32_t k = 0; k < substeps; k++) {
+        for (uint32_t k = 0; k < substeps; k++) {   // each substep a frame of its own
             if (use_graph && graph_ok) CUDA_TRY(cudaGraphLaunch(exec, stream));
             else record_substep(stream);
+            launch_frame_end(d, stream);
         }
         CUDA_TRY(cudaEventRecord(b, stream));
         CUDA_TRY(cudaEventSynchronize(b));
@@ -509,6 +510,7 @@ struct SproutSim {
             record_stage(k, stream);
             CUDA_TRY(cudaEventRecord(ev[k + 1], stream));
         }
+        launch_frame_end(d, stream);
         CUDA_TRY(cudaEventSynchronize(ev[kStages]));
         for (int k = 0; k < kStages; k++) CUDA_TRY(cudaEventElapsedTime(&ms[k], ev[k], ev[k + 1]));
         for (auto& e : ev) cudaEventDestroy(e);
@@ -761,6 +763,10 @@ struct SproutSim {
         {
             SolveState K0;
             std::memset(&K0, 0, sizeof K0);
+            // a new scene records the most until its frames say otherwise (mod.rs:2478-2483)
+            K0.rec[0] = K0.rec[1] = params.pressure_max_iters;
+            K0.rec[2] = params.viscosity_max_iters;
+            for (int k = 0; k < 3; k++) K0.cap[k] = recorded_limit(K0.rec[k], k == 2, params.viscosity_precond != 0);
             K0.trace = trace_buf;
             K0.trace_rows = trace_rows;
             K0.trace_cols = trace_cols;
@@ -1168,6 +1174,7 @@ struct SproutSim {
             if (use_graph && graph_ok) CUDA_TRY(cudaGraphLaunch(exec, stream));
             else record_substep(stream);
         }
+        launch_frame_end(d, stream);   // the call is a frame: its solves adapt the recorded counts
         CUDA_TRY(cudaGetLastError());
         return end_emit_call();
     }
@@ -1632,6 +1639,7 @@ struct SproutBatch {
         int rc = ensure_graph();
         if (rc != SPROUT_OK) return rc;
         for (uint32_t k = 0; k < substeps; k++) CUDA_TRY(cudaGraphLaunch(exec, main));
+        launch_frame_end_many(first.v.scenes, first.v.ns, main);   // the call is every member's frame
         CUDA_TRY(cudaEventRecord(ev_done, main));
         for (SproutSim* sim : sims) CUDA_TRY(cudaStreamWaitEvent(sim->stream, ev_done, 0));
         return ticket();
@@ -1667,6 +1675,7 @@ struct SproutBatch {
         if ((rc = build_visc_view()) != SPROUT_OK) return rc;
         graph_ok = false;   // the views no longer hold the graph's tanks
         record_substep(true);
+        launch_frame_end_many(first.v.scenes, first.v.ns, main);
         CUDA_TRY(cudaGetLastError());
         CUDA_TRY(cudaEventRecord(ev_done, main));
         for (SproutSim* sim : ms) CUDA_TRY(cudaStreamWaitEvent(sim->stream, ev_done, 0));
@@ -1695,7 +1704,10 @@ struct SproutBatch {
         if (rc != SPROUT_OK) return rc;
         if ((rc = ensure_graph()) != SPROUT_OK) return rc;
         CUDA_TRY(cudaEventRecord(a, main));
-        for (uint32_t k = 0; k < substeps; k++) CUDA_TRY(cudaGraphLaunch(exec, main));
+        for (uint32_t k = 0; k < substeps; k++) {   // each substep a frame of its own
+            CUDA_TRY(cudaGraphLaunch(exec, main));
+            launch_frame_end_many(first.v.scenes, first.v.ns, main);
+        }
         CUDA_TRY(cudaEventRecord(b, main));
         CUDA_TRY(cudaEventSynchronize(b));
         CUDA_TRY(cudaEventElapsedTime(ms, a, b));
@@ -2248,6 +2260,15 @@ int sprout_sim_download_render(SproutSim* sim, int which, uint16_t* out, size_t 
                                    : (const void*)sim->d_flow;
     CUDA_TRY(cudaMemcpy(out, src, n * sizeof(uint16_t), cudaMemcpyDeviceToHost));
     sim->d2h_bytes += n * sizeof(uint16_t);
+    return SPROUT_OK;
+}
+
+int sprout_sim_recorded_iters(SproutSim* sim, uint32_t out[3]) {
+    if (!sim || !out) return fail(SPROUT_E_ARG, "null argument");
+    SolveState K;
+    CUDA_TRY(cudaMemcpyAsync(&K, sim->d.K, sizeof K, cudaMemcpyDeviceToHost, sim->stream));
+    CUDA_TRY(cudaStreamSynchronize(sim->stream));
+    for (int k = 0; k < 3; k++) out[k] = K.rec[k];
     return SPROUT_OK;
 }
 

@@ -976,7 +976,7 @@ __global__ void __launch_bounds__(NT, 2) k_visc_solve(DevScene d, int restrain) 
         // 5, visc_update with mode 6; the directions alternate between vp and vr2 (free without
         // the multigrid) as vp / vp2 swap in the reference
         float2 *pa = d.vp, *pb = d.vr2;
-        for (uint32_t k = 0; k < P->viscosity_max_iters && K.done == 0u; k++) {
+        for (uint32_t k = 0; k < d.K->cap[2] && K.done == 0u; k++) {
             V.each(0, [&](uint32_t tt) { V.jac_iter_tile(tt, pa, pb, half); });
             if (!grid_sync(d.K)) return;
             {
@@ -1027,7 +1027,7 @@ __global__ void __launch_bounds__(NT, 2) k_visc_solve(DevScene d, int restrain) 
         __syncthreads();
         half ^= 1;
     }
-    for (uint32_t k = 0; k < P->viscosity_max_iters && K.done == 0u && P->viscosity_precond != 0; k++) {
+    for (uint32_t k = 0; k < d.K->cap[2] && K.done == 0u && P->viscosity_precond != 0; k++) {
         V.mgu(ra, qa, rb, qb, half);
         if (!grid_sync(d.K)) return;
         {
@@ -1070,6 +1070,8 @@ __global__ void __launch_bounds__(NT, 2) k_visc_solve(DevScene d, int restrain) 
         SolveState* G = d.K;
         if (K.iters > G->v_it_max) G->v_it_max = K.iters;
         if (K.done == 0u) G->v_unconv += 1u;
+        if (K.iters > G->f_it[2]) G->f_it[2] = K.iters;
+        if (K.done == 0u) G->f_un[2] += 1u;
         const float rel = K.r0 > 0.0f ? sqrtf(K.rr / K.r0) : 0.0f;
         G->v_res_max = maxf(G->v_res_max, rel);
         G->v_iters = K.iters;
@@ -1280,7 +1282,7 @@ __global__ void __launch_bounds__(NT, 2) k_visc_batch(VBatchView B) {
         if (!grid_sync(BK)) return;
     }
     for (uint32_t k = 0;; k++) {
-        auto running = [&](int s) { return S[s].K.done == 0u && k < B.scenes[s].P->viscosity_max_iters; };
+        auto running = [&](int s) { return S[s].K.done == 0u && k < B.scenes[s].K->cap[2]; };
         if (threadIdx.x == 0) {
             int r = 0;
             for (int s = 0; s < ns && !r; s++) r = running(s) ? 1 : 0;
@@ -1343,6 +1345,8 @@ __global__ void __launch_bounds__(NT, 2) k_visc_batch(VBatchView B) {
             SolveState* G = B.scenes[s].K;
             if (K.iters > G->v_it_max) G->v_it_max = K.iters;
             if (K.done == 0u) G->v_unconv += 1u;
+            if (K.iters > G->f_it[2]) G->f_it[2] = K.iters;
+            if (K.done == 0u) G->f_un[2] += 1u;
             const float rel = K.r0 > 0.0f ? sqrtf(K.rr / K.r0) : 0.0f;
             G->v_res_max = maxf(G->v_res_max, rel);
             G->v_iters = K.iters;
