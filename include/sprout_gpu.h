@@ -277,6 +277,14 @@ int sprout_sim_render(SproutSim* sim, float inv_speed);
  * every step call (a frame; each substep of sprout_sim_profile) adapts them from its own
  * solves when it ends (mod.rs:3093-3114), where the reference adapts on the frame's read-back. */
 int sprout_sim_recorded_iters(SproutSim* sim, uint32_t out[3]);
+/* What the particles of a liquid with a look keep (look.comp; FluidSim's plook, mod.rs:926-929),
+ * after the last sprout_sim_render that recorded (blocking): per particle slot, in the order of
+ * sprout_sim_download_particles, four words (its id, 0, A_xx A_yy A_xy of its platelets at 10
+ * bits each with A_xy offset by 0.5, 0), and the slots listed for the look splat (their order
+ * is the device atomics'). *slots = 0 until a render found such a liquid in the tank. The
+ * specks a new particle would bring into spray.comp's pool are not made (no pool). */
+int sprout_sim_download_look(SproutSim* sim, uint32_t* state, size_t state_cap, uint32_t* list, size_t list_cap,
+                             uint32_t* slots, uint32_t* listed);
 /* FluidSim::flow_view's parity (mod.rs:1850-1853): the copy of the flow map that holds it now
  * (blocking). */
 int sprout_sim_flow_parity(SproutSim* sim, uint32_t* parity);

@@ -164,6 +164,10 @@ def lib() -> C.CDLL:
         L.osim_flow_map.restype = C.c_long
         L.osim_recorded_iters.argtypes = [C.c_void_p, C.c_void_p]
         L.osim_recorded_iters.restype = None
+        L.osim_look.argtypes = [C.c_void_p, C.c_void_p, C.c_float, C.c_void_p, C.c_uint32]
+        L.osim_look.restype = C.c_long
+        L.osim_look_state.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t]
+        L.osim_look_state.restype = C.c_long
         L.o_expf.argtypes = [C.c_float]
         L.o_expf.restype = C.c_float
         _lib = L
@@ -305,6 +309,17 @@ class OracleSim:
         lib().osim_cell_counts(self.h_, a, b, out.ctypes.data, n)
         return out.reshape(max(hi[1] - lo[1], 0), max(hi[0] - lo[0], 0))
 
+    def n_slots_(self) -> int:
+        return int(lib().osim_particles(self.h_, None, 0))
+
+    def look(self):
+        """look.comp's state per slot (n, 4) uint32 and the slots the last render listed."""
+        n = lib().osim_look_state(self.h_, None, 0)
+        st = np.zeros((max(n, 0), 4), np.uint32)
+        if n > 0:
+            lib().osim_look_state(self.h_, st.ctypes.data, st.size)
+        return st, getattr(self, "_look_list", np.zeros(0, np.uint32))
+
     def recorded_iters(self) -> list:
         """FluidSim::recorded_iters: [first pressure solve, second, viscosity]."""
         v = (C.c_uint32 * 3)()
@@ -363,6 +378,11 @@ class OracleSim:
                 lib().osim_flow_map(self.h_, self._smooth.ctypes.data, self._flow.ctypes.data, float(dt),
                                     float(np.float32(now)), self._parity)
                 self._parity = 1 - self._parity
+            # record_look: particles of a liquid without a look are left as they are, so the
+            # pass runs whether or not the tank holds such a liquid
+            lst = np.zeros(max(self.n_slots_(), 1), np.uint32)
+            n = lib().osim_look(self.h_, tab.ctypes.data, float(dt), lst.ctypes.data, len(lst))
+            self._look_list = lst[: min(max(n, 0), len(lst))].copy()
         return (self._raw.copy().view(np.float16).reshape(20, self.h, self.w, 4),
                 self._smooth.copy().view(np.float16).reshape(24, self.h, self.w, 4),
                 self._gb.copy().view(np.float16).reshape(hh, hw, 4),
@@ -428,6 +448,10 @@ def _row(name: str) -> int:
     raise KeyError(name)
 
 
+# material fields only the render side reads (the optics table the tests take from the engine)
+RENDER_ONLY = {"cloud", "cloud_size", "cloud_ior", "cloud_shape", "dust", "dust_size", "dust_density",
+               "dust_shape", "dust_reflect"}
+
 PAIR_TENSIONS = {"tension_oil_water": (0, 1), "tension_metal_water": (0, 2), "tension_metal_oil": (1, 2),
                  "tension_melt_water": (0, 3), "tension_melt_oil": (1, 3), "tension_melt_metal": (2, 3)}
 
@@ -452,6 +476,8 @@ def apply_setting(p: OSimParams, key: str, v: float):
                     pass
     if prop is not None:
         m = p.mat[row]
+        if prop in RENDER_ONLY and prop not in dict(m._fields_):
+            return   # read by the optics table (the engine's SimParams), not by a substep
         typ = dict(m._fields_)[prop]
         setattr(m, prop, int(v) if typ in (C.c_uint32, C.c_int32) else float(v))
         return

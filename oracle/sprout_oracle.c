@@ -703,6 +703,8 @@ struct OSim {
     int n_magnets;
     V2* magc;   /* per cell: susceptibility; magnetic energy density (magnet.comp) */
     V4* pstress;   /* per particle slot: viscoelastic stress (xx, yy, xy), in place */
+    uint32_t* plook;   /* per particle slot: look.comp's four words (null until a look pass runs) */
+    uint32_t frame;    /* FluidSim::frame: step calls so far (mod.rs:2402) */
     V4* estr;      /* per cell: the deposited stress (elastic.comp) */
     I2* rl;        /* per cell: rigid label (root cell, -1 not rigid); its body at the root */
     int64_t* rbody;   /* per body: 15 fixed-point sums (rigid.comp) */
@@ -2068,13 +2070,21 @@ void osim_sort(OSim* s) {
         run += k;
     }
     memset(s->sorted, 0, (size_t)n * sizeof(OParticle));
+    /* the look's state moves with its particle (sort.comp's plook) */
+    uint32_t* look2 = s->plook ? (uint32_t*)calloc((size_t)n * 4 + 4, sizeof(uint32_t)) : NULL;
     for (uint32_t i = 0; i < n; i++) {
         const OParticle* p = &s->particles[i];
         if (p->kind == KIND_DEAD) continue;
         int cx = clampi((int)p->pos[0], 0, s->W - 1), cy = clampi((int)p->pos[1], 0, s->H - 1);
-        s->sorted[count[cidx(s, cx, cy)]++] = *p;
+        uint32_t dst = count[cidx(s, cx, cy)]++;
+        s->sorted[dst] = *p;
+        if (look2) memcpy(look2 + 4 * (size_t)dst, s->plook + 4 * (size_t)i, 4 * sizeof(uint32_t));
     }
     memcpy(s->particles, s->sorted, (size_t)n * sizeof(OParticle));
+    if (look2) {
+        memcpy(s->plook, look2, (size_t)n * 4 * sizeof(uint32_t));
+        free(look2);
+    }
     free(count);
 }
 
@@ -4732,6 +4742,7 @@ OSim* osim_create(int w, int h, uint32_t capacity, const OSimParams* p) {
 
 void osim_destroy(OSim* s) {
     if (!s) return;
+    free(s->plook);
     void* ptrs[] = {s->particles, s->sorted, s->acc, s->vel, s->cell, s->comp, s->coef, s->sprop,
                     s->surf, s->surf2, s->aux, s->grho, s->therm, s->dheat, s->vw, s->vs, s->prhs,
                     s->vel0, s->pjump, s->pres, s->p2keep, s->hcell, s->solid, s->sdf, s->region,
@@ -5039,6 +5050,7 @@ void osim_recorded_iters(const OSim* s, uint32_t out[3]) {
 }
 
 int osim_step(OSim* s, uint32_t substeps, float target, const OTool* tool) {
+    s->frame += 1u;
     take_spawns(s);
     build_params(s, tool);
     s->spawn_speed = 0.0f;
@@ -5628,6 +5640,104 @@ long osim_flow_map(const OSim* s, const uint16_t* smooth, uint16_t* flow, float 
             }
         }
     return 0;
+}
+
+/* look.comp (main, 93-171) over the particle slots in order, from the optics table `optics`,
+ * FluidSim's frame counter and `dt`, the simulated time since the last optics call: the
+ * second moment A of the platelets' normals of each particle of a liquid with platelets,
+ * Jeffery's equation with the quadratic closure on the shear part of its APIC gradient, in
+ * sub = clamp(ceil(rate dt / 0.15), 1, 8) steps, then rotational diffusion (mix towards I / 3
+ * by 1 - exp(-6 Dr dt)), kept at 10 bits each rounded stochastically (quant, pack_a); a slot
+ * whose stored id differs holds a new particle, which starts at I / 3. The listed slots (in
+ * slot order) go to `list` (at most `cap`); returns how many were listed. The specks' part
+ * (a new particle's specks into spray.comp's pool) is not restated: no pool (dust_cap 0). */
+static float o_rnd24(uint32_t h) { return (float)(h >> 8) / 16777216.0f; }
+static uint32_t o_quant10(float v, uint32_t h) {
+    const float m = 1023.0f;
+    return (uint32_t)clampf(floorf(clampf(v, 0.0f, 1.0f) * m + o_rnd24(h)), 0.0f, m);
+}
+static uint32_t o_pack_a(float ax, float ay, float az, uint32_t h) {
+    return o_quant10(ax, hash32(h ^ 0x1b873593u)) | (o_quant10(ay, hash32(h ^ 0xcc9e2d51u)) << 10) |
+           (o_quant10(az + 0.5f, hash32(h ^ 0xe6546b64u)) << 20);
+}
+long osim_look(OSim* s, const void* optics, float dt, uint32_t* list, uint32_t cap) {
+    const OOptics* opt = (const OOptics*)optics;
+    if (!s->plook) {
+        s->plook = (uint32_t*)calloc((size_t)s->capacity * 4, sizeof(uint32_t));
+        if (!s->plook) return -2;
+    }
+    long listed = 0;
+    const float third = 1.0f / 3.0f;
+    for (uint32_t i = 0; i < s->n_slots; i++) {
+        const OParticle* p = &s->particles[i];
+        uint32_t low = p->kind & 255u;
+        if (p->kind == KIND_DEAD || low == 0u || low > 96u) continue;   /* rows of the table */
+        uint32_t row = low - 1u;
+        const OOptics* o = &opt[row];
+        float lx = o->opt[1], ly = o->fx2[2];   /* look_of */
+        if (o->idx[0] >= 0) {
+            const OOptics* dl = &opt[o->idx[0]];
+            float t = clampf(p->s, 0.0f, 1.0f);
+            lx = mixf(dl->opt[1], lx, t);
+            ly = mixf(dl->fx2[2], ly, t);
+        }
+        if (maxf(lx, ly) <= 0.0f) continue;
+        uint32_t* st = s->plook + 4 * (size_t)i;
+        int fresh = st[0] != p->id;
+        uint32_t h = hash32(p->id * 0x9e3779b1u ^ hash32(s->frame * 0x85ebca6bu + 0x165667b1u));
+        if (lx <= 0.0f) {
+            if (fresh) {
+                st[0] = p->id; st[1] = 0u; st[2] = o_pack_a(third, third, 0.0f, h); st[3] = 0u;
+            }
+            continue;
+        }
+        float ax = third, ay = third, az = 0.0f;
+        if (!fresh) {
+            ax = (float)(st[2] & 1023u) / 1023.0f;
+            ay = (float)((st[2] >> 10) & 1023u) / 1023.0f;
+            az = (float)((st[2] >> 20) & 1023u) / 1023.0f - 0.5f;
+            if (dt > 0.0f) {
+                float Bc = o->opt2[2];
+                float w = 0.5f * (p->c[2] - p->c[1]);
+                float dv = 0.5f * (p->c[0] + p->c[3]);
+                float exx = p->c[0] - dv, eyy = p->c[3] - dv, exy = 0.5f * (p->c[1] + p->c[2]);
+                float rate = fabsf(w) + fabsf(exx) + fabsf(eyy) + fabsf(exy);
+                float sf = ceilf(rate * dt / 0.15f);
+                int sub = sf >= 8.0f ? 8 : (sf >= 1.0f ? (int)sf : 1);
+                float h1 = dt / (float)sub;
+                float ezz = 0.0f;
+                for (int k = 0; k < sub; k++) {
+                    float a = ax, b = ay, c = az, z = 1.0f - a - b;
+                    float AE = exx * a + eyy * b + 2.0f * exy * c + ezz * z;
+                    float rx = -2.0f * w * c, ry = 2.0f * w * c, rz = w * (a - b);
+                    float e2 = 2.0f * AE;
+                    float sx = 2.0f * (exx * a + exy * c) - e2 * a;
+                    float sy = 2.0f * (exy * c + eyy * b) - e2 * b;
+                    float sz = c * (exx + eyy) + exy * (a + b) - e2 * c;
+                    ax = ax + h1 * (rx + Bc * sx);
+                    ay = ay + h1 * (ry + Bc * sy);
+                    az = az + h1 * (rz + Bc * sz);
+                }
+                float t = 1.0f - o_expf(-6.0f * o->opt2[1] * dt);
+                ax = mixf(ax, third, t);
+                ay = mixf(ay, third, t);
+                az = mixf(az, 0.0f, t);
+                ax = clampf(ax, 0.0f, 1.0f);
+                ay = clampf(ay, 0.0f, 1.0f);
+                az = clampf(az, -0.5f, 0.5f);
+            }
+        }
+        st[0] = p->id; st[1] = 0u; st[2] = o_pack_a(ax, ay, az, h); st[3] = 0u;
+        if ((uint32_t)listed < cap) list[listed] = i;
+        listed++;
+    }
+    return listed;
+}
+/* look.comp's state per slot (4 words each, n_slots slots); returns the slots. */
+long osim_look_state(const OSim* s, uint32_t* out, size_t cap) {
+    if (!s->plook) return 0;
+    if (out && cap >= 4 * (size_t)s->n_slots) memcpy(out, s->plook, (size_t)s->n_slots * 4 * sizeof(uint32_t));
+    return (long)s->n_slots;
 }
 
 long osim_field(const OSim* s, const char* name, void* out, size_t cap) {

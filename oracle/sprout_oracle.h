@@ -176,6 +176,9 @@ long osim_field(const OSim* s, const char* name, void* out, size_t cap);
 long osim_render(const OSim* s, const void* optics, float inv_speed, int sss_iters, uint16_t* raw, uint16_t* smooth,
                  uint16_t* ga, uint16_t* gb);
 /* flow_map.comp over the grid from copy `src` of `flow` (4 layers) into the other copy. */
+/* look.comp over the slots (the oracle keeps the state; its sort moves it), and its state. */
+long osim_look(OSim* s, const void* optics, float dt, uint32_t* list, uint32_t cap);
+long osim_look_state(const OSim* s, uint32_t* out, size_t cap);
 /* FluidSim::recorded_iters: the recorded iteration counts (first solve, second, viscosity). */
 void osim_recorded_iters(const OSim* s, uint32_t out[3]);
 long osim_flow_map(const OSim* s, const uint16_t* smooth, uint16_t* flow, float dt, float now, uint32_t src);

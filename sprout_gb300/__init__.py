@@ -51,6 +51,7 @@ EXPORTS = [
     "sprout_sim_emit_paint", "sprout_sim_emit_rain", "sprout_sim_emitter_seed", "sprout_sim_emitted",
     "sprout_params_optics", "sprout_params_set_color", "sprout_sim_render", "sprout_sim_download_render",
     "sprout_params_get_color", "sprout_params_get_row", "sprout_sim_flow_parity", "sprout_sim_recorded_iters",
+    "sprout_sim_download_look",
 ]
 
 # One row of the optics table (material.rs GpuOptics): 15 four-word fields, 240 bytes.
@@ -195,6 +196,7 @@ def lib() -> C.CDLL:
         "sprout_sim_render": ([V, C.c_float], C.c_int),
         "sprout_sim_flow_parity": ([V, P(C.c_uint32)], C.c_int),
         "sprout_sim_recorded_iters": ([V, P(C.c_uint32)], C.c_int),
+        "sprout_sim_download_look": ([V, V, C.c_size_t, V, C.c_size_t, P(C.c_uint32), P(C.c_uint32)], C.c_int),
         "sprout_params_get_color": ([V, C.c_uint32, C.c_char_p, P(C.c_float), P(C.c_int)], C.c_int),
         "sprout_params_get_row": ([V, C.c_uint32, P(C.c_int32), P(C.c_int32)], C.c_int),
         "sprout_sim_download_render": ([V, C.c_int, V, C.c_size_t, P(C.c_size_t)], C.c_int),
@@ -483,6 +485,16 @@ class FluidSim:
         v = (C.c_uint32 * 3)()
         _check(lib().sprout_sim_recorded_iters(self._h, v))
         return [int(x) for x in v]
+
+    def download_look(self):
+        """look.comp's state: (per slot (id, 0, packed A, 0) as uint32 (n, 4), the listed slots)."""
+        n, m = C.c_uint32(), C.c_uint32()
+        _check(lib().sprout_sim_download_look(self._h, None, 0, None, 0, C.byref(n), C.byref(m)))
+        st = np.zeros((n.value, 4), np.uint32)
+        ls = np.zeros(max(m.value, 1), np.uint32)
+        _check(lib().sprout_sim_download_look(self._h, st.ctypes.data, st.size, ls.ctypes.data, ls.size,
+                                              C.byref(n), C.byref(m)))
+        return st, ls[: m.value]
 
     def flow_parity(self) -> int:
         """The copy of the flow map that holds it now (blocking)."""

@@ -69,6 +69,9 @@ struct DevScene {
     float2* magc;     // per cell: its liquid's susceptibility; the magnetic energy density of magnetic liquid there
     float4* pstress;  // per particle slot (sorted order): its viscoelastic stress (xx, yy, xy)
     float4* pstress2; // the same after the particle pass, in the pass's order
+    uint4* plook;     // per particle slot: look.comp's state (its id, -, A_xx A_yy A_xy, -); null
+                      // until a render finds a liquid with a look (moves with its particle)
+    uint4* plook2;    // the sort's target for it
     float4* pdep;     // the stress each particle deposits this substep, in the pass's order
     float4* estr;     // per cell: the deposited stress (elastic.comp)
     int2* rl;         // per cell: rigid label (its body's root cell, -1 not rigid); at a root, its body

@@ -148,6 +148,11 @@ void launch_cell_optics(const DevScene& d, const DevOptics* opt, float inv_speed
 void launch_frame_end(const DevScene& d, cudaStream_t st);
 void launch_frame_end_many(const DevScene* scenes, int n, cudaStream_t st);   // a batch's members
 void launch_render_clock(const DevScene& d, RenderClock* clock, int valid, int changed, cudaStream_t st);
+// look.comp over the particle slots (d.plook must be allocated): the platelets' orientation of
+// each particle of a liquid with a look, evolved by the clock's dt, and the slots listed for
+// the look splat (*count of them, at most cap in list). `frame`: FluidSim's frame counter.
+void launch_look(const DevScene& d, const DevOptics* opt, const RenderClock* clock, uint32_t frame, uint32_t* count,
+                 uint32_t* list, uint32_t cap, uint32_t n_slots, cudaStream_t st);
 // Scene::rasterize on the device (raster.cu): the tank's solid fields straight into device
 // buffers, bit-identical to the host's Scene::rasterize (scene.cpp).
 struct Scene;

@@ -587,7 +587,99 @@ __global__ void __launch_bounds__(256) k_flow_map(DevScene d, const ushort4* sm,
     }
 }
 
+// look.comp: the orientation of the platelets each particle of a liquid with platelets stands
+// for, the second moment A of their normals (A_xx, A_yy, A_xy), evolved by Jeffery's equation
+// averaged over them with the quadratic closure (the shear part of the particle's velocity
+// gradient only), relaxed towards isotropy by rotational diffusion, and kept at 10 bits each,
+// rounded stochastically (pack_a). A slot whose stored id is not its particle's holds a new
+// particle, which starts isotropic. The particles with platelets are listed for the look
+// splat (the order of that list is the atomics'). The specks a new particle brings into
+// spray.comp's pool are not made: there is no pool here (the reference's dust_cap = 0 case).
+DEV float rnd24(uint32_t h) { return (float)(h >> 8) / 16777216.0f; }
+DEV uint32_t quant10(float v, uint32_t h) {
+    const float m = 1023.0f;
+    return (uint32_t)clampf(floorf(clampf(v, 0.0f, 1.0f) * m + rnd24(h)), 0.0f, m);
+}
+DEV uint32_t pack_a(float ax, float ay, float az, uint32_t h) {
+    return quant10(ax, hash32(h ^ 0x1b873593u)) | (quant10(ay, hash32(h ^ 0xcc9e2d51u)) << 10) |
+           (quant10(az + 0.5f, hash32(h ^ 0xe6546b64u)) << 20);
+}
+__global__ void __launch_bounds__(128) k_look(DevScene d, const DevOptics* opt, const RenderClock* clk, uint32_t frame,
+                                             uint32_t* count, uint32_t* list, uint32_t cap) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.P->n_slots) return;
+    const float4 q0 = d.part[3 * i + 1], q1 = d.part[3 * i + 2];   // c; s, kind, id, t
+    const uint32_t kind = __float_as_uint(q1.y), id = __float_as_uint(q1.z), low = kind & 255u;
+    if (kind == KIND_DEAD || low == 0u || low > 96u) return;   // rows of the optics table
+    const uint32_t row = low - 1u;
+    const DevOptics& o = opt[row];
+    // look_of: the platelets' sheen weight and the drawn specks, a concentrate's blended with
+    // its diluent's by its concentration
+    float lx = o.opt[1], ly = o.fx2[2];
+    if (o.idx[0] >= 0) {
+        const DevOptics& dl = opt[o.idx[0]];
+        const float t = clampf(q1.x, 0.0f, 1.0f);
+        lx = mixf(dl.opt[1], lx, t);
+        ly = mixf(dl.fx2[2], ly, t);
+    }
+    if (maxf(lx, ly) <= 0.0f) return;
+    const uint4 st = d.plook[i];
+    const bool fresh = st.x != id;
+    const uint32_t h = hash32(id * 0x9e3779b1u ^ hash32(frame * 0x85ebca6bu + 0x165667b1u));
+    const float third = 1.0f / 3.0f;
+    if (lx <= 0.0f) {
+        if (fresh) d.plook[i] = make_uint4(id, 0u, pack_a(third, third, 0.0f, h), 0u);
+        return;
+    }
+    float ax = third, ay = third, az = 0.0f;
+    if (!fresh) {
+        ax = (float)(st.z & 1023u) / 1023.0f;
+        ay = (float)((st.z >> 10) & 1023u) / 1023.0f;
+        az = (float)((st.z >> 20) & 1023u) / 1023.0f - 0.5f;
+        const float dt = clk->dt;
+        if (dt > 0.0f) {
+            const float Bc = o.opt2[2];
+            const float w = 0.5f * (q0.z - q0.y);   // rotation rate, 1 / s
+            const float dv = 0.5f * (q0.x + q0.w);
+            const float exx = q0.x - dv, eyy = q0.w - dv, exy = 0.5f * (q0.y + q0.z);
+            const float rate = fabsf(w) + fabsf(exx) + fabsf(eyy) + fabsf(exy);
+            const float sf = ceilf(rate * dt / 0.15f);
+            const int sub = sf >= 8.0f ? 8 : (sf >= 1.0f ? (int)sf : 1);
+            const float h1 = dt / (float)sub;
+            const float ezz = 0.0f;
+            for (int k = 0; k < sub; k++) {
+                const float a = ax, b = ay, c = az, z = 1.0f - a - b;
+                const float AE = exx * a + eyy * b + 2.0f * exy * c + ezz * z;
+                const float rx = -2.0f * w * c, ry = 2.0f * w * c, rz = w * (a - b);
+                const float e2 = 2.0f * AE;
+                const float sx = 2.0f * (exx * a + exy * c) - e2 * a;
+                const float sy = 2.0f * (exy * c + eyy * b) - e2 * b;
+                const float sz = c * (exx + eyy) + exy * (a + b) - e2 * c;
+                ax = ax + h1 * (rx + Bc * sx);
+                ay = ay + h1 * (ry + Bc * sy);
+                az = az + h1 * (rz + Bc * sz);
+            }
+            const float t = 1.0f - sp_expf(-6.0f * o.opt2[1] * dt);   // rotational diffusion
+            ax = mixf(ax, third, t);
+            ay = mixf(ay, third, t);
+            az = mixf(az, 0.0f, t);
+            ax = clampf(ax, 0.0f, 1.0f);
+            ay = clampf(ay, 0.0f, 1.0f);
+            az = clampf(az, -0.5f, 0.5f);
+        }
+    }
+    d.plook[i] = make_uint4(id, 0u, pack_a(ax, ay, az, h), 0u);
+    const uint32_t k = atomicAdd(count, 1u);   // listed for the look splat
+    if (k < cap) list[k] = i;
+}
+
 }  // namespace
+
+void launch_look(const DevScene& d, const DevOptics* opt, const RenderClock* clock, uint32_t frame, uint32_t* count,
+                 uint32_t* list, uint32_t cap, uint32_t n_slots, cudaStream_t st) {
+    cudaMemsetAsync(count, 0, sizeof(uint32_t), st);
+    if (n_slots > 0) k_look<<<(n_slots + 127) / 128, 128, 0, st>>>(d, opt, clock, frame, count, list, cap);
+}
 
 void launch_render_clock(const DevScene& d, RenderClock* clock, int valid, int changed, cudaStream_t st) {
     k_render_clock<<<1, 1, 0, st>>>(d.S, clock, valid, changed);

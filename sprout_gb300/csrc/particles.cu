@@ -900,13 +900,21 @@ __global__ void __launch_bounds__(256) k_cell_gather(DevScene d) {
         d.part[3 * j + 1] = b;
         d.part[3 * j + 2] = c;
         if (d.pstress) d.pstress[j] = d.pstress2[src];   // the stress moves with its particle (sort.comp:66)
+        if (d.plook) d.plook2[j] = d.plook[src];          // and the look's state (sort.comp's plook)
     } else {
         const float4 z = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         d.part[3 * j + 0] = z;
         d.part[3 * j + 1] = z;
         d.part[3 * j + 2] = z;
         if (d.pstress) d.pstress[j] = z;
+        if (d.plook) d.plook2[j] = make_uint4(0u, 0u, 0u, 0u);
     }
+}
+
+// The look's state back from the sort's target, slot for slot.
+__global__ void __launch_bounds__(256) k_look_back(DevScene d) {
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < d.P->n_slots) d.plook[j] = d.plook2[j];
 }
 
 // ---- P2G gather ------------------------------------------------------------------------
@@ -1088,6 +1096,7 @@ void launch_sort(const DevScene& d, const LaunchCfg& cfg, cudaStream_t st) {
     k_cell_sort<<<(d.ncell + 255) / 256, 256, 0, st>>>(d);
     k_crowd_sort<<<kCrowdBlocks, 256, 0, st>>>(d);
     k_cell_gather<<<nb, 256, 0, st>>>(d);
+    if (d.plook) k_look_back<<<nb, 256, 0, st>>>(d);
 }
 
 void launch_p2g(const DevScene& d, const LaunchCfg& cfg, cudaStream_t st) {

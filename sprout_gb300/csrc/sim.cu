@@ -1035,8 +1035,47 @@ struct SproutSim {
             render_key_set = true;
             launch_cell_optics(d, d_optics, inv_speed, (int)params.sss_iters, d_raw, d_smooth, d_flow, d_clock, d_glow,
                                d_glow + glow_texels(), stream);
+            if (look_live() && n_slots > 0) {   // record_look (mod.rs:1717-1729)
+                if (!d.plook) {
+                    if ((rc = alloc(&d.plook, (size_t)capacity)) != SPROUT_OK) return rc;
+                    if ((rc = alloc(&d.plook2, (size_t)capacity)) != SPROUT_OK) return rc;
+                    if ((rc = alloc(&d_look_list, (size_t)capacity + 1)) != SPROUT_OK) return rc;
+                    CUDA_TRY(cudaMemsetAsync(d.plook, 0, (size_t)capacity * sizeof(uint4), stream));
+                    graph_ok = false;   // the sort now carries the look's state: recapture
+                }
+                launch_look(d, d_optics, d_clock, frames, d_look_list, d_look_list + 1, capacity, n_slots, stream);
+            }
         }
         CUDA_TRY(cudaGetLastError());
+        return SPROUT_OK;
+    }
+    // A liquid with platelets (cloud_shape below 2/3) or specks is in the tank (mod.rs:1718-1721).
+    uint32_t* d_look_list = nullptr;   // [0] how many listed, then their slots
+    bool look_live() const {
+        for (int r : tank.rows) {
+            const MatProps& m = params.mat[r];
+            if ((m.cloud > 0.0f && m.cloud_shape < 2.0f / 3.0f) || m.dust > 0.0f) return true;
+        }
+        return false;
+    }
+    int download_look(uint32_t* state, size_t cap, uint32_t* list, size_t list_cap, uint32_t* slots, uint32_t* listed) {
+        *slots = 0;
+        *listed = 0;
+        if (!d.plook) return SPROUT_OK;
+        CUDA_TRY(cudaStreamSynchronize(stream));
+        uint32_t count = 0;
+        CUDA_TRY(cudaMemcpy(&count, d_look_list, sizeof count, cudaMemcpyDeviceToHost));
+        *slots = n_slots;
+        *listed = std::min(count, capacity);
+        if (state) {
+            if (cap < 4 * (size_t)n_slots) return fail(SPROUT_E_ARG, "download_look: the state holds fewer than 4 words per slot");
+            CUDA_TRY(cudaMemcpy(state, d.plook, (size_t)n_slots * sizeof(uint4), cudaMemcpyDeviceToHost));
+        }
+        if (list) {
+            if (list_cap < *listed) return fail(SPROUT_E_ARG, "download_look: the list holds fewer entries than listed");
+            CUDA_TRY(cudaMemcpy(list, d_look_list + 1, (size_t)*listed * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+        }
+        d2h_bytes += (size_t)n_slots * sizeof(uint4) + (size_t)*listed * 4;
         return SPROUT_OK;
     }
     int flow_parity(uint32_t* parity) {
@@ -1124,7 +1163,9 @@ struct SproutSim {
 
     // What a step call does before its substeps run, on the sim's stream: the parameters and
     // material table (when they changed), the batch words of StepBuf.
+    uint32_t frames = 0;   // FluidSim::frame: step calls so far (mod.rs:2402), wrapping
     int prepare_step(uint32_t substeps, float target, const ToolState* tool) {
+        frames += 1u;
         enqueued = false;
         if (!pending.empty()) {
             int rc = take_spawns();
@@ -2261,6 +2302,12 @@ int sprout_sim_download_render(SproutSim* sim, int which, uint16_t* out, size_t 
     CUDA_TRY(cudaMemcpy(out, src, n * sizeof(uint16_t), cudaMemcpyDeviceToHost));
     sim->d2h_bytes += n * sizeof(uint16_t);
     return SPROUT_OK;
+}
+
+int sprout_sim_download_look(SproutSim* sim, uint32_t* state, size_t state_cap, uint32_t* list, size_t list_cap,
+                             uint32_t* slots, uint32_t* listed) {
+    if (!sim || !slots || !listed) return fail(SPROUT_E_ARG, "null argument");
+    return sim->download_look(state, state_cap, list, list_cap, slots, listed);
 }
 
 int sprout_sim_recorded_iters(SproutSim* sim, uint32_t out[3]) {
