@@ -170,6 +170,11 @@ def lib() -> C.CDLL:
         L.osim_look_state.restype = C.c_long
         L.o_expf.argtypes = [C.c_float]
         L.o_expf.restype = C.c_float
+        for fn in ("o_sinf", "o_cosf"):
+            getattr(L, fn).argtypes = [C.c_float]
+            getattr(L, fn).restype = C.c_float
+        L.o_atan2.argtypes = [C.c_float, C.c_float]
+        L.o_atan2.restype = C.c_float
         _lib = L
     return _lib
 

@@ -5083,9 +5083,9 @@ uint32_t osim_particles(const OSim* s, OParticle* out, uint32_t cap) {
 /* ------------------------------------------------------------------------------------ */
 /* The render side's cell passes: cell_optics.comp, light.comp, optics_blur.comp            */
 /* (mod.rs:1626-1660), into layers of RGBA16F texels as the reference's image array holds   */
-/* them. exp / log / pow are the oracle's own (o_expf, o_logf, o_powf). The ferrofluid      */
-/* spikes (layers 13 xy, 14 xy), the dust field (layer 18) and the film tiles are left out, */
-/* as in the engine.                                                                         */
+/* them. exp / log / pow, sin / cos and atan are the oracle's own (o_expf, o_logf, o_powf,   */
+/* o_sincos, o_atan2). The dust field (layer 18) and the film tiles are left out, as in the  */
+/* engine.                                                                                   */
 /* ------------------------------------------------------------------------------------ */
 
 typedef struct OOptics {   /* material.rs GpuOptics: 240 bytes */
@@ -5211,12 +5211,121 @@ static float o_aq_share(const OSim* s, int x, int y) {
     return clampf((float)aqw / (float)cwq, 0.0f, 1.0f);
 }
 
-static void o_cell_optics(const OSim* s, const OOptics* opt, float inv_speed, int cx, int cy, uint16_t* raw) {
+/* sin and cos rounded once from FP64: reduction by the nearest multiple q of pi/2 (Cody and
+ * Waite, pi/2 in 33 + 53 bits), Taylor series to r^15 / r^16 on [-pi/4, pi/4], the quadrant's
+ * swap and signs. The same operations as the engine's, so the same bits. */
+static void o_sincos(float af, float* s, float* c) {
+    const double a = (double)af;
+    if (!(fabs(a) < 1e9)) {
+        *s = *c = af - af;
+        return;
+    }
+    const double q = rint(a * 0.63661977236758134308);
+    const double r = (a - q * 1.57079632673412561417) - q * 6.07710050650619224932e-11;
+    const double x2 = r * r;
+    double sn = 1.0 / 1307674368000.0;
+    sn = 1.0 / 6227020800.0 - x2 * sn;
+    sn = 1.0 / 39916800.0 - x2 * sn;
+    sn = 1.0 / 362880.0 - x2 * sn;
+    sn = 1.0 / 5040.0 - x2 * sn;
+    sn = 1.0 / 120.0 - x2 * sn;
+    sn = 1.0 / 6.0 - x2 * sn;
+    sn = r - r * x2 * sn;
+    double cs = 1.0 / 20922789888000.0;
+    cs = 1.0 / 87178291200.0 - x2 * cs;
+    cs = 1.0 / 479001600.0 - x2 * cs;
+    cs = 1.0 / 3628800.0 - x2 * cs;
+    cs = 1.0 / 40320.0 - x2 * cs;
+    cs = 1.0 / 720.0 - x2 * cs;
+    cs = 1.0 / 24.0 - x2 * cs;
+    cs = 0.5 - x2 * cs;
+    cs = 1.0 - x2 * cs;
+    const int n = ((int)q) & 3;
+    *s = (float)(n == 0 ? sn : n == 1 ? cs : n == 2 ? -sn : -cs);
+    *c = (float)(n == 0 ? cs : n == 1 ? -sn : n == 2 ? -cs : sn);
+}
+/* atan(y, x) rounded once from FP64: two angle halvings, the series to u^25, the octant;
+ * 0 at x = y = 0 (GLSL leaves it undefined). */
+float o_atan2(float yf, float xf) {
+    const double y = (double)yf, x = (double)xf, ay = fabs(y), ax = fabs(x);
+    if (ax == 0.0 && ay == 0.0) return 0.0f;
+    const int swap = ay > ax;
+    const double t = swap ? ax / ay : ay / ax;
+    double u = t / (1.0 + sqrt(1.0 + t * t));
+    u = u / (1.0 + sqrt(1.0 + u * u));
+    const double u2 = u * u;
+    double p = 1.0 / 25.0;
+    for (int k = 11; k >= 0; k--) p = 1.0 / (double)(2 * k + 1) - u2 * p;
+    double at = 4.0 * u * p;
+    if (swap) at = 1.5707963267948966 - at;
+    if (x < 0.0) at = 3.141592653589793 - at;
+    if (y < 0.0) at = -at;
+    return (float)at;
+}
+float o_sinf(float a) { float s, c; o_sincos(a, &s, &c); return s; }
+float o_cosf(float a) { float s, c; o_sincos(a, &s, &c); return c; }
+
+/* FluidSim::spike_params (mod.rs:1885-1899). */
+static void o_spike_params(const OSim* s, float* gap, float* mc) {
+    *gap = *mc = 0.0f;
+    const OMat* best = NULL;
+    for (int k = 0; k < s->tank.nrows; k++) {
+        const OMat* m = &s->prm.mat[s->tank.rows[k]];
+        if (m->susceptibility > 0.0f && (!best || m->susceptibility >= best->susceptibility)) best = m;
+    }
+    if (!best || s->n_magnets == 0) return;
+    float g = maxf(s->prm.gravity, 1.0f);
+    float rho = maxf(best->density, 1.0f), sigma = maxf(best->tension, 1e-4f);
+    float gp = 2.0f * 3.14159265f * sqrtf(sigma / (rho * g)) / s->prm.cell_size;
+    *gap = gp > 3.0f ? gp : 3.0f;
+    const float mu0 = 1.2566371e-6f;
+    *mc = sqrtf(2.0f * mu0 * (1.0f + 1.0f / (1.0f + best->susceptibility)) * sqrtf(rho * g * sigma));
+}
+/* cell_optics.comp:86-117: the spikes' height and where they stand */
+static float o_spike_height(const OSim* s, float gap, float mc, float B) {
+    if (gap <= 0.0f || P_.mag[1] <= 0.0f) return 0.0f;
+    float chi = P_.mag[1], ce = chi / (1.0f + chi);
+    float m = ce * B / (1.0f + ce * B / maxf(P_.mag[2], 1e-6f));
+    float over = m * m / maxf(mc * mc, 1e-12f) - 1.0f;
+    return over > 0.0f ? 0.85f * gap * (1.0f - o_expf(-over)) : 0.0f;
+}
+static V2 o_spike_phase(const OSim* s, float gap, float x, float y) {
+    int best = 0;
+    float bb = -1.0f;
+    for (int k = 0; k < (int)P_.mag[0]; k++) {
+        const float* mg = P_.magnet[k];
+        float r = maxf(len2(v2(x - mg[0], y - mg[1])), mg[2]);
+        float b = mg[3] * o_powf(mg[2] / r, 3.0f);
+        if (b > bb) {
+            bb = b;
+            best = k;
+        }
+    }
+    float dx = x - P_.magnet[best][0], dy = y - P_.magnet[best][1];
+    float mx = P_.magnet_dir[best][0], my = P_.magnet_dir[best][1];
+    float ang = o_atan2(mx * dy - my * dx, mx * dx + my * dy);
+    float ph = 6.2831853f * len2(v2(dx, dy)) * ang / (maxf(gap, 1e-3f) * 4.0f);
+    float sn, cs;
+    o_sincos(ph, &sn, &cs);
+    return v2(cs, sn);
+}
+
+static void o_cell_optics(const OSim* s, const OOptics* opt, float inv_speed, float spike_gap, float spike_mc, int cx,
+                          int cy, uint16_t* raw) {
     const int i = cy * s->W + cx, k = i * s->tank.stride;
     const size_t nc = (size_t)s->W * s->H;
     const int cw = s->acc[k + 4];
     V4 o[20];
     for (int l = 0; l < 20; l++) o[l] = v4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (spike_gap > 0.0f) {   /* every cell: the spikes stand in the air */
+        float px = (float)cx + 0.5f, py = (float)cy + 0.5f;
+        V2 B = magnet_field(s, px, py);
+        float b = len2(B), hgt = o_spike_height(s, spike_gap, spike_mc, b);
+        o[13] = v4(b > 1e-9f ? B.x / b * hgt : 0.0f, b > 1e-9f ? B.y / b * hgt : 0.0f, 0.0f, spike_gap);
+        V2 ph = o_spike_phase(s, spike_gap, px, py);
+        o[14].x = ph.x;
+        o[14].y = ph.y;
+    }
     if (cw > 0) {
         int thermal = has_cap(s, CAP_THERMAL);
         float T = thermal ? s->therm[i].x : P_.heat[0];
@@ -5584,8 +5693,10 @@ static void o_glow_pass(const OSim* s, const uint16_t* raw, uint16_t* ga, uint16
 long osim_render(const OSim* s, const void* optics, float inv_speed, int sss_iters, uint16_t* raw, uint16_t* smooth,
                  uint16_t* ga, uint16_t* gb) {
     const OOptics* opt = (const OOptics*)optics;
+    float gap, mc;
+    o_spike_params(s, &gap, &mc);
     for (int y = 0; y < s->H; y++)
-        for (int x = 0; x < s->W; x++) o_cell_optics(s, opt, inv_speed, x, y, raw);
+        for (int x = 0; x < s->W; x++) o_cell_optics(s, opt, inv_speed, gap, mc, x, y, raw);
     o_light(s, raw);
     for (int y = 0; y < s->H; y++)
         for (int x = 0; x < s->W; x++) o_optics_blur(s, raw, smooth, x, y);

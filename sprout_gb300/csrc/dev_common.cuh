@@ -207,6 +207,81 @@ DEV float sp_logf(float x) {
 // x^y as exp(y ln x) with the two functions above (x > 0; 1 for x = 1).
 DEV float sp_powf(float x, float y) { return x == 1.0f ? 1.0f : sp_expf(y * sp_logf(x)); }
 
+// The field of the magnets at x (cells), T: each a point dipole in the plane,
+// B0 (R / r)^3 (3 (m.e) e - m) / 2, constant inside the rim (common.glsl:388-402).
+DEV float2 magnet_field(const DevParams* P, float x, float y) {
+    float bx = 0.0f, by = 0.0f;
+    for (int k = 0; k < (int)P->mag[0]; k++) {
+        const float* mg = P->magnet[k];
+        const float mx = P->magnet_dir[k][0], my = P->magnet_dir[k][1];
+        const float dx = x - mg[0], dy = y - mg[1];
+        const float len = len2(dx, dy);
+        const float r = maxf(len, mg[2]);
+        const float ex = len > 1e-4f ? dx / len : mx, ey = len > 1e-4f ? dy / len : my;
+        const float a = mg[3] * sp_powf(mg[2] / r, 3.0f) * 0.5f;
+        const float me3 = 3.0f * (mx * ex + my * ey);
+        bx += a * (me3 * ex - mx);
+        by += a * (me3 * ey - my);
+    }
+    return make_float2(bx, by);
+}
+
+// sin and cos of a float angle, each rounded once from FP64 (GLSL leaves their precision to the
+// implementation): the angle reduced by the nearest multiple q of pi/2 (Cody and Waite, pi/2
+// in two parts of 33 and 53 bits), the Taylor series to r^15 and r^16 on [-pi/4, pi/4], then
+// the quadrant q mod 4's swap and signs. Within an ulp of the true values for |a| < 1e9.
+DEV void sp_sincos(float af, float* s, float* c) {
+    const double a = (double)af;
+    if (!(fabs(a) < 1e9)) {
+        *s = *c = af - af;
+        return;
+    }
+    const double q = rint(a * 0.63661977236758134308);
+    const double r = (a - q * 1.57079632673412561417) - q * 6.07710050650619224932e-11;
+    const double x2 = r * r;
+    double sn = 1.0 / 1307674368000.0;
+    sn = 1.0 / 6227020800.0 - x2 * sn;
+    sn = 1.0 / 39916800.0 - x2 * sn;
+    sn = 1.0 / 362880.0 - x2 * sn;
+    sn = 1.0 / 5040.0 - x2 * sn;
+    sn = 1.0 / 120.0 - x2 * sn;
+    sn = 1.0 / 6.0 - x2 * sn;
+    sn = r - r * x2 * sn;
+    double cs = 1.0 / 20922789888000.0;
+    cs = 1.0 / 87178291200.0 - x2 * cs;
+    cs = 1.0 / 479001600.0 - x2 * cs;
+    cs = 1.0 / 3628800.0 - x2 * cs;
+    cs = 1.0 / 40320.0 - x2 * cs;
+    cs = 1.0 / 720.0 - x2 * cs;
+    cs = 1.0 / 24.0 - x2 * cs;
+    cs = 0.5 - x2 * cs;
+    cs = 1.0 - x2 * cs;
+    const int n = ((int)q) & 3;
+    *s = (float)(n == 0 ? sn : n == 1 ? cs : n == 2 ? -sn : -cs);
+    *c = (float)(n == 0 ? cs : n == 1 ? -sn : n == 2 ? -cs : sn);
+}
+
+// atan(y, x) rounded once from FP64 (GLSL leaves its precision to the implementation, and the
+// result at x = y = 0: here 0): t = min / max of |x|, |y| in [0, 1]; atan t = 4 atan u with u
+// from two halvings of the angle, u / (1 + sqrt(1 + u^2)), so |u| <= tan(pi / 16); the series
+// to u^25; then the octant.
+DEV float sp_atan2(float yf, float xf) {
+    const double y = (double)yf, x = (double)xf, ay = fabs(y), ax = fabs(x);
+    if (ax == 0.0 && ay == 0.0) return 0.0f;
+    const bool swap = ay > ax;
+    const double t = swap ? ax / ay : ay / ax;
+    double u = t / (1.0 + sqrt(1.0 + t * t));
+    u = u / (1.0 + sqrt(1.0 + u * u));
+    const double u2 = u * u;
+    double p = 1.0 / 25.0;
+    for (int k = 11; k >= 0; k--) p = 1.0 / (double)(2 * k + 1) - u2 * p;
+    double at = 4.0 * u * p;
+    if (swap) at = 1.5707963267948966 - at;
+    if (x < 0.0) at = 3.141592653589793 - at;
+    if (y < 0.0) at = -at;
+    return (float)at;
+}
+
 constexpr int kMaxBodies = 4096;   // common.glsl: MAX_BODIES
 constexpr float RIGID_FIX = 65536.0f;
 

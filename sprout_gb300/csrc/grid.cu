@@ -872,25 +872,6 @@ __global__ void __launch_bounds__(256) k_settle(DevScene d) {
     }
 }
 
-// The field of the magnets at x (cells), T: each a point dipole in the plane,
-// B0 (R / r)^3 (3 (m.e) e - m) / 2, constant inside the rim (common.glsl:388-402).
-DEV float2 magnet_field(const DevParams* P, float x, float y) {
-    float bx = 0.0f, by = 0.0f;
-    for (int k = 0; k < (int)P->mag[0]; k++) {
-        const float* mg = P->magnet[k];
-        const float mx = P->magnet_dir[k][0], my = P->magnet_dir[k][1];
-        const float dx = x - mg[0], dy = y - mg[1];
-        const float len = len2(dx, dy);
-        const float r = maxf(len, mg[2]);
-        const float ex = len > 1e-4f ? dx / len : mx, ey = len > 1e-4f ? dy / len : my;
-        const float a = mg[3] * sp_powf(mg[2] / r, 3.0f) * 0.5f;
-        const float me3 = 3.0f * (mx * ex + my * ey);
-        bx += a * (me3 * ex - mx);
-        by += a * (me3 * ey - my);
-    }
-    return make_float2(bx, by);
-}
-
 // magnet.comp mode 0: the magnetic energy density of pure magnetic liquid in each cell
 // (Langevin-like saturation, a demagnetising factor from the liquid's surface).
 __global__ void __launch_bounds__(256) k_magnet_energy(DevScene d) {

@@ -136,9 +136,11 @@ size_t pressure_batch_scalar_bytes();
 // when the clock says it runs, glow.comp into glow_a then glow_b (half resolution).
 struct DevOptics;
 struct RenderClock;
-void launch_cell_optics(const DevScene& d, const DevOptics* opt, float inv_speed, int sss_iters, ushort4* raw,
-                        ushort4* smooth, ushort4* flow, const RenderClock* clock, ushort4* glow_a, ushort4* glow_b,
-                        cudaStream_t st);
+// spike_gap, spike_mc: the ferrofluid spikes' spacing (cells; 0: none) and Rosensweig
+// threshold mu0 Mc (T), FluidSim::spike_params.
+void launch_cell_optics(const DevScene& d, const DevOptics* opt, float inv_speed, float spike_gap, float spike_mc,
+                        int sss_iters, ushort4* raw, ushort4* smooth, ushort4* flow, const RenderClock* clock,
+                        ushort4* glow_a, ushort4* glow_b, cudaStream_t st);
 // The clock of a render call (record_cell_optics, mod.rs:1628-1641, 1674-1680): `valid` 0 for
 // the first call on a new tank (no step: the flow map does not run), `changed` 0 when the call
 // records nothing (its key is the last call's); the time since the last call from the

@@ -11,9 +11,8 @@
 // from the last call), flow_map.comp (how far the liquid has moved since its patterns
 // restarted, four layers) and glow.comp (the emission blurred at half resolution).
 //
-// Not computed here: the ferrofluid spikes' field and phase (layers 13 xy, 14 xy, zero), the
-// dust field of spray.comp (layer 18, zero: the specks are not carried) and the film map's
-// tile flags (no film map).
+// Not computed here: the dust field of spray.comp (layer 18, zero: the specks are not carried)
+// and the film map's tile flags (no film map).
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
@@ -114,7 +113,41 @@ DEV float aq_share(const DevScene& d, int x, int y) {
     return clampf((float)aqw / (float)cwq, 0.0f, 1.0f);
 }
 
-__global__ void __launch_bounds__(256) k_cell_optics(DevScene d, const DevOptics* opt, float inv_speed, ushort4* raw) {
+// Ferrofluid spikes (cell_optics.comp:78-117): their height from the field where a
+// magnetisable surface faces it past the Rosensweig threshold (mu0 M of a flat surface, N = 1),
+// to kSpikeK of their spacing; and where along the surface they stand, as the cos and sin of
+// the distance round the magnet whose field is strongest, in spacings / 4 (SPIKE_PHASE_DIV).
+constexpr float kSpikeK = 0.85f;   // mod.rs SPIKE_HEIGHT
+DEV float spike_height(const DevParams* P, float gap, float mc, float B) {
+    if (gap <= 0.0f || P->mag[1] <= 0.0f) return 0.0f;
+    const float chi = P->mag[1], ce = chi / (1.0f + chi);
+    const float m = ce * B / (1.0f + ce * B / maxf(P->mag[2], 1e-6f));   // mu0 M, T
+    const float over = m * m / maxf(mc * mc, 1e-12f) - 1.0f;
+    return over > 0.0f ? kSpikeK * gap * (1.0f - sp_expf(-over)) : 0.0f;
+}
+DEV float2 spike_phase(const DevParams* P, float gap, float x, float y) {
+    int best = 0;
+    float bb = -1.0f;
+    for (int k = 0; k < (int)P->mag[0]; k++) {
+        const float* mg = P->magnet[k];
+        const float r = maxf(len2(x - mg[0], y - mg[1]), mg[2]);
+        const float b = mg[3] * sp_powf(mg[2] / r, 3.0f);
+        if (b > bb) {
+            bb = b;
+            best = k;
+        }
+    }
+    const float dx = x - P->magnet[best][0], dy = y - P->magnet[best][1];
+    const float mx = P->magnet_dir[best][0], my = P->magnet_dir[best][1];
+    const float ang = sp_atan2(mx * dy - my * dx, mx * dx + my * dy);
+    const float ph = 6.2831853f * len2(dx, dy) * ang / (maxf(gap, 1e-3f) * 4.0f);
+    float s, c;
+    sp_sincos(ph, &s, &c);
+    return make_float2(c, s);
+}
+
+__global__ void __launch_bounds__(256) k_cell_optics(DevScene d, const DevOptics* opt, float inv_speed, float spike_gap,
+                                                    float spike_mc, ushort4* raw) {
     const int cx = blockIdx.x * 16 + threadIdx.x, cy = blockIdx.y * 16 + threadIdx.y;
     if (cx >= d.W || cy >= d.H) return;
     const DevParams* P = d.P;
@@ -124,6 +157,15 @@ __global__ void __launch_bounds__(256) k_cell_optics(DevScene d, const DevOptics
     const size_t nc = (size_t)d.W * d.H;
     float4 o[kLayers];
     for (int l = 0; l < kLayers; l++) o[l] = f4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (spike_gap > 0.0f) {   // in every cell: the spikes stand in the air
+        const float px = (float)cx + 0.5f, py = (float)cy + 0.5f;
+        const float2 B = magnet_field(P, px, py);
+        const float b = len2(B.x, B.y), hgt = spike_height(P, spike_gap, spike_mc, b);
+        o[13] = f4(b > 1e-9f ? B.x / b * hgt : 0.0f, b > 1e-9f ? B.y / b * hgt : 0.0f, 0.0f, spike_gap);
+        const float2 ph = spike_phase(P, spike_gap, px, py);
+        o[14].x = ph.x;
+        o[14].y = ph.y;
+    }
     if (cw > 0) {
         const bool thermal = P->thermal != 0;
         float T = thermal ? d.therm[i].x : P->heat[0];
@@ -685,11 +727,11 @@ void launch_render_clock(const DevScene& d, RenderClock* clock, int valid, int c
     k_render_clock<<<1, 1, 0, st>>>(d.S, clock, valid, changed);
 }
 
-void launch_cell_optics(const DevScene& d, const DevOptics* opt, float inv_speed, int sss_iters, ushort4* raw,
-                        ushort4* smooth, ushort4* flow, const RenderClock* clock, ushort4* glow_a, ushort4* glow_b,
-                        cudaStream_t st) {
+void launch_cell_optics(const DevScene& d, const DevOptics* opt, float inv_speed, float spike_gap, float spike_mc,
+                        int sss_iters, ushort4* raw, ushort4* smooth, ushort4* flow, const RenderClock* clock,
+                        ushort4* glow_a, ushort4* glow_b, cudaStream_t st) {
     const dim3 tiles((d.W + 15) / 16, (d.H + 15) / 16), block(16, 16);
-    k_cell_optics<<<tiles, block, 0, st>>>(d, opt, inv_speed, raw);
+    k_cell_optics<<<tiles, block, 0, st>>>(d, opt, inv_speed, spike_gap, spike_mc, raw);
     k_light<<<d.W, 64, 0, st>>>(d, raw);
     k_optics_blur<<<tiles, block, 0, st>>>(d, raw, smooth);
     // sss.comp (mod.rs:1666-1675): prepared, then an even number of iterations, ending in layer 20

@@ -1033,8 +1033,10 @@ struct SproutSim {
         if (changed) {
             std::memcpy(render_key, key, sizeof key);
             render_key_set = true;
-            launch_cell_optics(d, d_optics, inv_speed, (int)params.sss_iters, d_raw, d_smooth, d_flow, d_clock, d_glow,
-                               d_glow + glow_texels(), stream);
+            float gap = 0.0f, mc = 0.0f;
+            spike_params(&gap, &mc);
+            launch_cell_optics(d, d_optics, inv_speed, gap, mc, (int)params.sss_iters, d_raw, d_smooth, d_flow, d_clock,
+                               d_glow, d_glow + glow_texels(), stream);
             if (look_live() && n_slots > 0) {   // record_look (mod.rs:1717-1729)
                 if (!d.plook) {
                     if ((rc = alloc(&d.plook, (size_t)capacity)) != SPROUT_OK) return rc;
@@ -1048,6 +1050,23 @@ struct SproutSim {
         }
         CUDA_TRY(cudaGetLastError());
         return SPROUT_OK;
+    }
+    // FluidSim::spike_params (mod.rs:1885-1899): the spikes' spacing, the fastest growing wave
+    // 2 pi sqrt(sigma / (rho g)) in cells (at least SPIKE_MIN_GAP = 3), and mu0 Mc of the most
+    // susceptible liquid in the tank (the last of equals); none without a magnet.
+    void spike_params(float* gap, float* mc) const {
+        *gap = *mc = 0.0f;
+        const MatProps* best = nullptr;
+        for (int r : tank.rows) {
+            const MatProps& m = params.mat[r];
+            if (m.susceptibility > 0.0f && (!best || m.susceptibility >= best->susceptibility)) best = &m;
+        }
+        if (!best || magnets.empty()) return;
+        const float g = std::max(params.gravity, 1.0f);
+        const float rho = std::max(best->density, 1.0f), sigma = std::max(best->tension, 1e-4f);
+        *gap = std::max(2.0f * 3.14159265f * std::sqrt(sigma / (rho * g)) / params.cell_size, 3.0f);
+        const float mu0 = 1.2566371e-6f;
+        *mc = std::sqrt(2.0f * mu0 * (1.0f + 1.0f / (1.0f + best->susceptibility)) * std::sqrt(rho * g * sigma));
     }
     // A liquid with platelets (cloud_shape below 2/3) or specks is in the tank (mod.rs:1718-1721).
     uint32_t* d_look_list = nullptr;   // [0] how many listed, then their slots

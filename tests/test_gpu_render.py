@@ -64,6 +64,9 @@ def test_cell_passes_bit_exact(name):
     assert float(er[4, ..., 3].astype(np.float32).max()) > 0.5
     assert float(er[12, ..., :3].astype(np.float32).max()) > 0.0
     assert 0.0 < float(er[10, ..., 1].astype(np.float32).min()) <= 1.0
+    if name == "magnetic":   # the spikes' spacing and phase in every cell, their height where the field is strong
+        assert float(er[13, ..., 3].astype(np.float32).min()) > 0.0
+        assert float(np.abs(er[14, ..., :2].astype(np.float32)).max()) > 0.5
     if name == "cooling_lava":   # lava near 760 C glows (a heater at 327 C is below the Draper point)
         assert float(er[3, ..., :3].astype(np.float32).max()) > 0.0
         assert float(eg[..., :3].astype(np.float32).max()) > 0.0

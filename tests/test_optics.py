@@ -68,3 +68,25 @@ def test_table_is_what_the_reference_describes():
     assert t[60]["absorb"][3] > 1.0 and t[60]["opt"][2] == pytest.approx(0.9)
     assert t[63]["fx"][3] > 0.0 and t[63]["idx"][1] == 3
     assert not np.array_equal(t[62]["hot"], t[62]["absorb"])
+
+
+def test_own_sin_cos_and_atan_within_an_ulp():
+    """The ferrofluid spikes' phase takes the engine's own sin, cos and atan (GLSL leaves their
+    precision to the implementation; the oracle runs the same FP64 operations, rounded once):
+    within an ulp of float64's over the phases and directions the spikes meet."""
+    import math
+    from oracle import oracle as O
+    L = O.lib()
+    rng = np.random.default_rng(11)
+    for a in np.float32(np.concatenate([rng.uniform(-3000.0, 3000.0, 3000), rng.uniform(-4.0, 4.0, 2000),
+                                        [0.0, 1e-30, math.pi, -math.pi / 2, 1e6]])):
+        for fn, ref in ((L.o_sinf, math.sin), (L.o_cosf, math.cos)):
+            want = ref(float(a))
+            got = fn(float(a))
+            assert abs(got - want) <= abs(np.spacing(np.float32(want))) + 1e-38, (fn.__name__, a, got, want)
+    for y, x in np.float32(rng.uniform(-50.0, 50.0, (4000, 2))).tolist() + [[0.0, 1.0], [1.0, 0.0], [-1.0, -1e-20],
+                                                                         [1e-20, -1.0], [3.0, 3.0]]:
+        want = math.atan2(float(np.float32(y)), float(np.float32(x)))
+        got = L.o_atan2(float(y), float(x))
+        assert abs(got - want) <= abs(np.spacing(np.float32(want))) + 1e-38, (y, x, got, want)
+    assert L.o_atan2(0.0, 0.0) == 0.0
