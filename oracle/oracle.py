@@ -168,6 +168,10 @@ def lib() -> C.CDLL:
         L.osim_look.restype = C.c_long
         L.osim_look_state.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t]
         L.osim_look_state.restype = C.c_long
+        L.osim_spray.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_float, C.c_float]
+        L.osim_spray.restype = C.c_long
+        L.osim_spray_state.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        L.osim_spray_state.restype = C.c_long
         L.o_expf.argtypes = [C.c_float]
         L.o_expf.restype = C.c_float
         for fn in ("o_sinf", "o_cosf"):
@@ -317,6 +321,18 @@ class OracleSim:
     def n_slots_(self) -> int:
         return int(lib().osim_particles(self.h_, None, 0))
 
+    def spray(self):
+        """spray.comp's pool: (entries, free stack, listed entries, foam (2, h, w), counters)."""
+        from sprout_gb300 import DIFFUSE_DTYPE, DIFFUSE_MAX
+        st = (C.c_uint32 * 4)()
+        pool = np.zeros(DIFFUSE_MAX, DIFFUSE_DTYPE)
+        stack = np.zeros(DIFFUSE_MAX, np.uint32)
+        lst = np.zeros(DIFFUSE_MAX, np.uint32)
+        foam = np.zeros(2 * self.w * self.h, np.uint32)
+        lib().osim_spray_state(self.h_, pool.ctypes.data, stack.ctypes.data, lst.ctypes.data, foam.ctypes.data, st)
+        s = [int(x) for x in st]
+        return pool, stack[: s[1]], lst[: s[2]], foam.reshape(2, self.h, self.w), s
+
     def look(self):
         """look.comp's state per slot (n, 4) uint32 and the slots the last render listed."""
         n = lib().osim_look_state(self.h_, None, 0)
@@ -345,7 +361,7 @@ class OracleSim:
         lib().osim_particles(self.h_, out.ctypes.data, n)
         return out
 
-    def render(self, optics: np.ndarray, inv_speed: float = 1.0 / 60.0, sss_iters: int = 4):
+    def render(self, optics: np.ndarray, inv_speed: float = 1.0 / 60.0, sss_iters: int = 4, bubbles: float = 1.0):
         """FluidSim::record_cell_optics (mod.rs:1626-1712) on the current grid, from the optics
         table `optics` (96 rows of 240 bytes): cell_optics.comp, light.comp, optics_blur.comp,
         sss.comp, flow_map.comp and glow.comp. Returns (raw (20, h, w, 4), smooth (24, h, w, 4),
@@ -388,6 +404,7 @@ class OracleSim:
             lst = np.zeros(max(self.n_slots_(), 1), np.uint32)
             n = lib().osim_look(self.h_, tab.ctypes.data, float(dt), lst.ctypes.data, len(lst))
             self._look_list = lst[: min(max(n, 0), len(lst))].copy()
+            lib().osim_spray(self.h_, self._smooth.ctypes.data, tab.ctypes.data, float(dt), float(bubbles))
         return (self._raw.copy().view(np.float16).reshape(20, self.h, self.w, 4),
                 self._smooth.copy().view(np.float16).reshape(24, self.h, self.w, 4),
                 self._gb.copy().view(np.float16).reshape(hh, hw, 4),
@@ -455,7 +472,7 @@ def _row(name: str) -> int:
 
 # material fields only the render side reads (the optics table the tests take from the engine)
 RENDER_ONLY = {"cloud", "cloud_size", "cloud_ior", "cloud_shape", "dust", "dust_size", "dust_density",
-               "dust_shape", "dust_reflect"}
+               "dust_shape", "dust_reflect", "foam", "froth", "fizz"}
 
 PAIR_TENSIONS = {"tension_oil_water": (0, 1), "tension_metal_water": (0, 2), "tension_metal_oil": (1, 2),
                  "tension_melt_water": (0, 3), "tension_melt_oil": (1, 3), "tension_melt_metal": (2, 3)}

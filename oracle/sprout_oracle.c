@@ -705,6 +705,12 @@ struct OSim {
     V4* pstress;   /* per particle slot: viscoelastic stress (xx, yy, xy), in place */
     uint32_t* plook;   /* per particle slot: look.comp's four words (null until a look pass runs) */
     uint32_t frame;    /* FluidSim::frame: step calls so far (mod.rs:2402) */
+    /* spray.comp's pool: entries, free stack, listed entries, foam per cell (two copies),
+     * the counters (never handed out, stack height, listed), the copy counted next */
+    struct ODiffuse* dpool;
+    uint32_t *dstack, *dlist, *dcount;
+    uint32_t d_hw, d_top, d_listed, d_parity;
+    int d_seen;   /* a liquid that foams or fizzes has been in the tank */
     V4* estr;      /* per cell: the deposited stress (elastic.comp) */
     I2* rl;        /* per cell: rigid label (root cell, -1 not rigid); its body at the root */
     int64_t* rbody;   /* per body: 15 fixed-point sums (rigid.comp) */
@@ -4743,6 +4749,10 @@ OSim* osim_create(int w, int h, uint32_t capacity, const OSimParams* p) {
 void osim_destroy(OSim* s) {
     if (!s) return;
     free(s->plook);
+    free(s->dpool);
+    free(s->dstack);
+    free(s->dlist);
+    free(s->dcount);
     void* ptrs[] = {s->particles, s->sorted, s->acc, s->vel, s->cell, s->comp, s->coef, s->sprop,
                     s->surf, s->surf2, s->aux, s->grho, s->therm, s->dheat, s->vw, s->vs, s->prhs,
                     s->vel0, s->pjump, s->pres, s->p2keep, s->hcell, s->solid, s->sdf, s->region,
@@ -5844,6 +5854,337 @@ long osim_look(OSim* s, const void* optics, float dt, uint32_t* list, uint32_t c
     }
     return listed;
 }
+/* spray.comp (main 171-494; mod.rs:1739-1773): bubbles, foam and spray in a pool of 65536.
+ * Stage 0 (make, per cell) where liquid traps air, folds in, crests, or fizzes; stage 1 (move,
+ * per entry) as bubble, foam or spray, the foam counted per cell, the live entries listed.
+ * The pool is handed out in one deterministic order the reference's atomics allow: the
+ * frame's emissions ranked by cell and by their order in it take the free stack's top first,
+ * then unused entries; freed entries go onto the stack, and live ones into the list, in entry
+ * order. Not restated: the specks (not carried) and a droplet's splat into the film map's
+ * intake (film_lay.glsl; no film map): the droplet is removed as the reference removes it. */
+typedef struct ODiffuse { float px, py, vx, vy, life, r; uint32_t info; float z; } ODiffuse;
+#define D_MAX 65536u
+enum { D_FREE = 0, D_BUBBLE = 1, D_FOAM = 2, D_SPRAY = 3 };
+static float d_rnd(uint32_t h) { return (float)(h >> 8) / 16777216.0f; }
+static float d_ramp(float x, float lo, float hi) { return clampf((x - lo) / (hi - lo), 0.0f, 1.0f); }
+static float d_occ_cell(const OSim* s, int x, int y) {
+    if (x < 0 || y < 0 || x >= s->W || y >= s->H) return 0.0f;
+    return clampf(s->cell[y * s->W + x].x, 0.0f, 1.5f);
+}
+static float d_occ_at(const OSim* s, float px, float py) {
+    float gx = px - 0.5f, gy = py - 0.5f;
+    int bx = (int)floorf(gx), by = (int)floorf(gy);
+    float fx = gx - (float)bx, fy = gy - (float)by;
+    return mixf(mixf(d_occ_cell(s, bx, by), d_occ_cell(s, bx + 1, by), fx),
+                mixf(d_occ_cell(s, bx, by + 1), d_occ_cell(s, bx + 1, by + 1), fx), fy);
+}
+static V2 d_centre_vel(const OSim* s, int i) {
+    int n = s->W * s->H;
+    V4 v = s->vel[i];
+    float ux = face_live(v.z) ? v.x : 0.0f, uy = face_live(v.w) ? v.y : 0.0f;
+    V4 vr = s->vel[mini(i + 1, n - 1)], vt = s->vel[mini(i + s->W, n - 1)];
+    return v2(0.5f * (ux + (face_live(vr.z) ? vr.x : 0.0f)), 0.5f * (uy + (face_live(vt.w) ? vt.y : 0.0f)));
+}
+/* air.glsl sample_vel at an entry: a face's cell by its linear index, zeros off the buffer */
+static V4 d_vel_lin(const OSim* s, int x, int y) {
+    long long k = (long long)y * s->W + x;
+    return (k >= 0 && k < (long long)s->W * s->H) ? s->vel[k] : v4(0.0f, 0.0f, 0.0f, 0.0f);
+}
+static V2 d_sample_vel(const OSim* s, float x, float y) {
+    float o[2] = {0.0f, 0.0f};
+    for (int comp = 0; comp < 2; comp++) {
+        float gx = comp == 0 ? x : x - 0.5f, gy = comp == 0 ? y - 0.5f : y;
+        int bx = (int)floorf(gx), by = (int)floorf(gy);
+        float fx = gx - (float)bx, fy = gy - (float)by;
+        float sw = 0.0f, su = 0.0f;
+        for (int b = 0; b < 2; b++)
+            for (int a = 0; a < 2; a++) {
+                V4 q = d_vel_lin(s, bx + a, by + b);
+                if (face_live(comp == 0 ? q.z : q.w)) {
+                    float wt = (a == 0 ? 1.0f - fx : fx) * (b == 0 ? 1.0f - fy : fy);
+                    sw += wt;
+                    su += wt * (comp == 0 ? q.x : q.y);
+                }
+            }
+        if (sw > 1e-3f) o[comp] = su / sw;
+    }
+    return v2(o[0], o[1]);
+}
+static float d_crowd(const OSim* s, int x, int y, uint32_t copy) {
+    x = clampi(x, 0, s->W - 1);
+    y = clampi(y, 0, s->H - 1);
+    return (float)s->dcount[(size_t)copy * s->W * s->H + (size_t)y * s->W + x];
+}
+static int d_dominant_row(const OSim* s, int i) {
+    int k = i * s->tank.stride, cw = s->acc[k + 4];
+    if (cw <= 0) return -1;
+    int others = 0;
+    for (int j = 0; j < P_.n_present; j++) {
+        int ch = s->mats[P_.present[j]].ia[2];
+        if (ch >= 0) others += s->acc[k + ch];
+    }
+    int best = -1, bw = 0;
+    for (int j = 0; j < P_.n_present; j++) {
+        int r = P_.present[j];
+        const int* ia = s->mats[r].ia;
+        if (ia[2] < 0 && P_.primary >= 0 && r != P_.primary) continue;
+        int w = ia[2] >= 0 ? s->acc[k + ia[2]] : maxi(cw - others, 0);
+        if (w > bw) {
+            bw = w;
+            best = r;
+        }
+    }
+    return best;
+}
+static ODiffuse d_bubble(int cx, int cy, uint32_t h, int k, float r0, uint32_t grows, float ux, float uy, float spread,
+                         int row) {
+    uint32_t hk = hash32(h + (uint32_t)k * 0x9e3779b9u);
+    ODiffuse e;
+    e.px = (float)cx + d_rnd(hk);
+    e.py = (float)cy + d_rnd(hash32(hk ^ 0x51ed270bu));
+    float a = 6.2831853f * d_rnd(hash32(hk ^ 0x2545f491u));
+    float sn, cs;
+    o_sincos(a, &sn, &cs);
+    float j = d_rnd(hash32(hk ^ 0x27d4eb2fu));
+    e.vx = ux + spread * cs * j;
+    e.vy = uy + spread * sn * j;
+    float sr = d_rnd(hash32(hk ^ 0x165667b1u));
+    e.r = r0 * (0.45f + 1.1f * sr * sr);
+    e.info = (uint32_t)D_BUBBLE | grows | ((uint32_t)(row + 1) << 8) | (hash32(hk ^ 0x68e31da4u) & 0xffff8000u);
+    e.life = 40.0f;
+    e.z = d_rnd(hash32(hk ^ 0xb5297a4du));
+    return e;
+}
+static int d_take(const OSim* s, uint32_t r, uint32_t top0, uint32_t hw0) {
+    if (r < top0) return (int)s->dstack[top0 - 1u - r];
+    uint32_t hw = hw0 + (r - top0);
+    return hw < D_MAX ? (int)hw : -1;
+}
+/* make(): the cell's emissions, each into the slot of its rank (from *rank on) */
+static void d_make(OSim* s, const uint16_t* sm, int cx, int cy, float dt, float amount, uint32_t* rank, uint32_t top0,
+                   uint32_t hw0) {
+    const size_t nc = (size_t)s->W * s->H;
+    int W = s->W, H = s->H, i = cy * W + cx;
+    float occ = d_occ_cell(s, cx, cy);
+    if (occ < 0.08f) return;
+    V4 l4 = get_texel(sm, 4 * nc + i);
+    if (l4.w < 0.02f) return;
+    float foam_k = l4.y / l4.w;
+    float fizz = get_texel(sm, 16 * nc + i).y / l4.w;
+    float cs = P_.misc[2];
+    V2 u = d_centre_vel(s, i);
+    float ta = 0.0f, gx = 0.0f, gy = 0.0f;
+    for (int q = 0; q < 4; q++) {
+        int dx = q == 0 ? -1 : q == 1 ? 1 : 0, dy = q == 2 ? -1 : q == 3 ? 1 : 0;
+        int nx = cx + dx, ny = cy + dy;
+        float on = d_occ_cell(s, nx, ny);
+        gx += (float)dx * on;
+        gy += (float)dy * on;
+        if (on < 0.08f || nx < 0 || ny < 0 || nx >= W || ny >= H) continue;
+        V2 un = d_centre_vel(s, ny * W + nx);
+        float dvx = u.x - un.x, dvy = u.y - un.y;
+        float m = len2(v2(dvx, dvy));
+        if (m < 1e-4f) continue;
+        ta += m * (1.0f - (dvx / m * -(float)dx + dvy / m * -(float)dy));
+    }
+    float ul = len2(u);
+    float speed = ul * cs;
+    float energy = d_ramp(speed, 0.6f, 3.0f), trapped = d_ramp(ta * cs, 1.0f, 5.0f);
+    float g = len2(v2(gx, gy));
+    float crest = 0.0f, plunge = 0.0f;
+    if (g > 0.15f && speed > 0.05f) {
+        float nox = -gx / g, noy = -gy / g;
+        float along = u.x / ul * nox + u.y / ul * noy;
+        crest = d_ramp(along, 0.6f, 0.95f) * d_ramp(speed, 1.0f, 3.5f);
+        plunge = d_ramp(-along, 0.4f, 0.9f) * d_ramp(speed, 0.08f, 1.2f) * smoothstepf(0.15f, 0.6f, g);
+    }
+    float tension = maxf(s->sprop[i].x, 0.0f) * cs * cs * cs / 7.2e-5f;
+    float r0 = clampf(1.2e-3f * sqrtf(clampf(tension, 0.05f, 4.0f)) / cs, 0.03f, 0.4f);
+    uint32_t h = hash32((uint32_t)i * 0x85ebca6bu ^ hash32(s->frame * 0x9e3779b1u + 0x3c6ef372u));
+    float rate = amount * (40.0f * trapped * energy + 30.0f * plunge + 25.0f * crest * foam_k);
+    float fn = floorf(rate * dt + d_rnd(h));
+    int n = fn >= 6.0f ? 6 : (fn >= 1.0f ? (int)fn : 0);
+    int row = (n > 0 || fizz > 0.0f) ? d_dominant_row(s, i) : -1;
+    for (int k = 0; k < n; k++) {
+        int slot = d_take(s, (*rank)++, top0, hw0);
+        if (slot >= 0) s->dpool[slot] = d_bubble(cx, cy, h, k, r0, 0u, u.x, u.y, 0.3f * ul, row);
+    }
+    if (fizz > 0.0f) {
+        int w1 = W + 1, kk = cy * w1 + cx;
+        float sd = 0.25f * (s->sdf[kk] + s->sdf[kk + 1] + s->sdf[kk + w1] + s->sdf[kk + w1 + 1]);
+        float wall = 1.0f - d_ramp(sd, 0.5f, 2.0f);
+        float fr = amount * 1.6f * fizz * minf(occ, 1.0f) * (1.0f + 5.0f * wall);
+        uint32_t h2 = hash32(h ^ 0x7feb352du);
+        float ff = floorf(fr * dt + d_rnd(h2));
+        int nf = ff >= 2.0f ? 2 : (ff >= 1.0f ? (int)ff : 0);
+        float r0f = clampf(0.25e-3f / cs, 0.02f, 0.2f);
+        for (int k = 0; k < nf; k++) {
+            int slot = d_take(s, (*rank)++, top0, hw0);
+            if (slot >= 0) s->dpool[slot] = d_bubble(cx, cy, h2, k, r0f, 4u, u.x, u.y, 0.0f, row);
+        }
+    }
+}
+/* move(): entry i; 0 nothing, 1 freed, 2 live */
+static int d_move(OSim* s, const uint16_t* sm, uint32_t i, float dt) {
+    const size_t nc = (size_t)s->W * s->H;
+    ODiffuse e = s->dpool[i];
+    uint32_t st = e.info & 3u;
+    if (st == D_FREE || (e.info & 8u) != 0u) return 0;
+    int W = s->W, H = s->H;
+    uint32_t copy_in = 1u - s->d_parity, copy_out = s->d_parity;
+    float cs = P_.misc[2];
+    float sf = ceilf(dt * 120.0f);
+    int steps = sf >= 8.0f ? 8 : (sf >= 1.0f ? (int)sf : 1);
+    float h = dt / (float)steps;
+    for (int k = 0; k < steps && st != D_FREE; k++) {
+        int cx = clampi((int)e.px, 0, W - 1), cy = clampi((int)e.py, 0, H - 1), ci = cy * W + cx;
+        float occ = d_occ_at(s, e.px, e.py);
+        V2 uf = d_sample_vel(s, e.px, e.py);
+        float crowd = d_crowd(s, cx, cy, copy_in);
+        float gcx = d_crowd(s, cx + 1, cy, copy_in) - d_crowd(s, cx - 1, cy, copy_in);
+        float gcy = d_crowd(s, cx, cy + 1, copy_in) - d_crowd(s, cx, cy - 1, copy_in);
+        uint32_t want = occ > 0.62f ? D_BUBBLE : (occ + 0.06f * crowd > 0.10f ? D_FOAM : D_SPRAY);
+        V4 l4 = get_texel(sm, 4 * nc + ci);
+        float wl = maxf(l4.w, 1e-3f);
+        if (want != st) {
+            if (want == D_FOAM || (want == D_BUBBLE && st == D_SPRAY)) {
+                float foam_k = l4.w > 0.02f ? l4.y / wl : 0.0f;
+                float froth = l4.w > 0.02f ? get_texel(sm, 16 * nc + ci).x / wl : 0.0f;
+                if (st == D_SPRAY && foam_k < 0.05f) { st = D_FREE; break; }
+                if (want == D_FOAM && st == D_BUBBLE && (crowd > 5.0f || foam_k < 0.05f)) { st = D_FREE; break; }
+                if (want == D_FOAM) {
+                    e.life = maxf(froth, 0.05f) * (0.5f + d_rnd(hash32(e.info ^ (uint32_t)k)));
+                    e.z = e.life;
+                }
+                if (want == D_BUBBLE) e.life = 40.0f;
+            }
+            if (want == D_SPRAY) e.life = minf(e.life, 1.5f);
+            if (want == D_BUBBLE && st == D_FOAM) e.z = d_rnd(hash32(e.info ^ 0xb5297a4du));
+            st = want;
+        }
+        float tx, ty, tau;
+        if (st == D_BUBBLE) {
+            V4 cf = s->cell[ci];
+            float rho = maxf(cf.y, 0.3f), nu = maxf(cf.z / rho, 1e-6f);
+            float vt = terminal(s, rho, rho, nu, 2.0f * e.r);
+            tx = uf.x + 0.0f;
+            ty = uf.y + vt;
+            tau = 0.03f;
+            if ((e.info & 4u) != 0u) e.r = minf(e.r + 0.5e-3f / cs * h, 0.35f);
+            e.life -= h;
+        } else if (st == D_FOAM) {
+            float sub = clampf(occ * 2.0f, 0.0f, 1.0f);
+            tx = uf.x * sub;
+            ty = uf.y * sub;
+            float below = d_occ_at(s, e.px - 0.0f, e.py - 0.7f) + 0.25f * d_crowd(s, cx, cy - 1, copy_in);
+            int held = occ > 0.25f || below > 0.45f;
+            float push = d_ramp(crowd, 2.0f * 0.7f, 2.0f * 2.0f);
+            float gl = len2(v2(gcx, gcy));
+            if (gl > 1e-3f) {
+                float spx = -gcx / gl * 6.0f * push, spy = -gcy / gl * 6.0f * push;
+                if (!held) spy = minf(spy, 0.0f);
+                tx += spx;
+                ty += spy;
+            }
+            ty -= held ? 1.5f * (1.0f - d_ramp(occ, 0.1f, 0.4f)) : 8.0f;
+            if (occ > 0.45f) ty += 4.0f * (occ - 0.45f);
+            tau = 0.06f;
+            e.life -= h * (crowd < 2.0f ? 2.5f : 1.0f);
+        } else {
+            tx = e.vx + 0.0f - e.vx * 1.2f * h;
+            ty = e.vy + -P_.gravity * h - e.vy * 1.2f * h;
+            tau = 0.0f;
+            e.life -= h;
+        }
+        if (tau > 0.0f) {
+            float t = 1.0f - o_expf(-h / tau);
+            e.vx = mixf(e.vx, tx, t);
+            e.vy = mixf(e.vy, ty, t);
+        } else {
+            e.vx = tx;
+            e.vy = ty;
+        }
+        e.px += e.vx * h;
+        e.py += e.vy * h;
+        V2 gs;
+        float sd = sample_sdf(s, v2(e.px, e.py), &gs);
+        float rim = e.r + 0.1f;
+        int drow = (int)((e.info >> 8) & 127u) - 1;
+        if (st == D_SPRAY && sd < rim && drow >= 0) { st = D_FREE; break; }
+        if (sd < rim) {
+            float gl = maxf(len2(gs), 1e-6f);
+            float nx = gs.x / gl, ny = gs.y / gl;
+            e.px += nx * (rim - sd);
+            e.py += ny * (rim - sd);
+            float vn = minf(e.vx * nx + e.vy * ny, 0.0f);
+            e.vx -= nx * vn;
+            e.vy -= ny * vn;
+        }
+        if (e.life <= 0.0f || e.px < 0.0f || e.py < 0.0f || e.px >= (float)W || e.py >= (float)H) st = D_FREE;
+    }
+    e.info = (e.info & ~3u) | st;
+    s->dpool[i] = e;
+    if (st == D_FREE) return 1;
+    if (st == D_FOAM) {
+        int cx = clampi((int)e.px, 0, W - 1), cy = clampi((int)e.py, 0, H - 1);
+        s->dcount[(size_t)copy_out * nc + (size_t)cy * W + cx] += 1u;
+    }
+    return 2;
+}
+/* record_spray: once a liquid that foams or fizzes (optics sty.y, fx2.y) has been in the tank
+ * with bubbles on: the foam counts of this frame's copy cleared, stage 0 when one is and
+ * dt > 0, stage 1, the copies swapped. The smoothed layers are osim_render's. */
+long osim_spray(OSim* s, const uint16_t* smooth, const void* optics, float dt, float amount) {
+    const size_t nc = (size_t)s->W * s->H;
+    const OOptics* opt = (const OOptics*)optics;
+    int makes = 0;
+    if (amount > 0.0f)
+        for (int k = 0; k < s->tank.nrows; k++) {
+            const OOptics* o = &opt[s->tank.rows[k]];
+            if (o->sty[1] > 0.0f || o->fx2[1] > 0.0f) makes = 1;
+        }
+    if (makes) s->d_seen = 1;
+    if (!s->d_seen) return 0;
+    if (!s->dpool) {
+        s->dpool = (ODiffuse*)calloc(D_MAX, sizeof(ODiffuse));
+        s->dstack = (uint32_t*)calloc(D_MAX, sizeof(uint32_t));
+        s->dlist = (uint32_t*)calloc(D_MAX, sizeof(uint32_t));
+        s->dcount = (uint32_t*)calloc(2 * nc, sizeof(uint32_t));
+        if (!s->dpool || !s->dstack || !s->dlist || !s->dcount) return -2;
+    }
+    memset(s->dcount + (size_t)s->d_parity * nc, 0, nc * sizeof(uint32_t));
+    if (makes && dt > 0.0f) {
+        uint32_t rank = 0, top0 = s->d_top, hw0 = s->d_hw;
+        for (int cy = 0; cy < s->H; cy++)
+            for (int cx = 0; cx < s->W; cx++) d_make(s, smooth, cx, cy, dt, amount, &rank, top0, hw0);
+        s->d_top = rank < top0 ? top0 - rank : 0u;
+        s->d_hw += rank > top0 ? rank - top0 : 0u;
+    }
+    uint32_t listed = 0;
+    for (uint32_t i = 0; i < D_MAX; i++) {
+        int f = d_move(s, smooth, i, dt);
+        if (f == 1) s->dstack[s->d_top++] = i;
+        else if (f == 2) s->dlist[listed++] = i;
+    }
+    s->d_listed = listed;
+    s->d_parity ^= 1u;
+    return (long)listed;
+}
+/* The pool (65536 entries of 8 words), its free stack and list, the foam counts (2 x W x H)
+ * and the counters (never handed out, stack height, listed, the copy counted next). */
+long osim_spray_state(const OSim* s, void* pool, uint32_t* stack, uint32_t* list, uint32_t* foam, uint32_t state[4]) {
+    state[0] = s->d_hw;
+    state[1] = s->d_top;
+    state[2] = s->d_listed;
+    state[3] = s->d_parity;
+    if (!s->dpool) return 0;
+    if (pool) memcpy(pool, s->dpool, D_MAX * sizeof(ODiffuse));
+    if (stack) memcpy(stack, s->dstack, (size_t)s->d_top * 4);
+    if (list) memcpy(list, s->dlist, (size_t)s->d_listed * 4);
+    if (foam) memcpy(foam, s->dcount, 2 * (size_t)s->W * s->H * 4);
+    return 1;
+}
+
 /* look.comp's state per slot (4 words each, n_slots slots); returns the slots. */
 long osim_look_state(const OSim* s, uint32_t* out, size_t cap) {
     if (!s->plook) return 0;

@@ -179,6 +179,9 @@ long osim_render(const OSim* s, const void* optics, float inv_speed, int sss_ite
 /* look.comp over the slots (the oracle keeps the state; its sort moves it), and its state. */
 long osim_look(OSim* s, const void* optics, float dt, uint32_t* list, uint32_t cap);
 long osim_look_state(const OSim* s, uint32_t* out, size_t cap);
+/* spray.comp over the pool the oracle keeps (smooth: osim_render's smoothed layers). */
+long osim_spray(OSim* s, const uint16_t* smooth, const void* optics, float dt, float amount);
+long osim_spray_state(const OSim* s, void* pool, uint32_t* stack, uint32_t* list, uint32_t* foam, uint32_t state[4]);
 /* FluidSim::recorded_iters: the recorded iteration counts (first solve, second, viscosity). */
 void osim_recorded_iters(const OSim* s, uint32_t out[3]);
 long osim_flow_map(const OSim* s, const uint16_t* smooth, uint16_t* flow, float dt, float now, uint32_t src);

@@ -51,7 +51,7 @@ EXPORTS = [
     "sprout_sim_emit_paint", "sprout_sim_emit_rain", "sprout_sim_emitter_seed", "sprout_sim_emitted",
     "sprout_params_optics", "sprout_params_set_color", "sprout_sim_render", "sprout_sim_download_render",
     "sprout_params_get_color", "sprout_params_get_row", "sprout_sim_flow_parity", "sprout_sim_recorded_iters",
-    "sprout_sim_download_look",
+    "sprout_sim_download_look", "sprout_sim_download_spray",
 ]
 
 # One row of the optics table (material.rs GpuOptics): 15 four-word fields, 240 bytes.
@@ -60,6 +60,10 @@ OPTICS_FIELDS = ["absorb", "solid", "opt", "sty", "idx", "fx", "fx2", "lum", "ho
 OPTICS_DTYPE = np.dtype([(f, "<i4" if f == "idx" else "<f4", 4) for f in OPTICS_FIELDS])
 assert OPTICS_DTYPE.itemsize == 240
 RENDER_LAYERS = 20
+# spray.comp's pool entry (the reference's Diffuse) and the pool's size (mod.rs DIFFUSE_MAX)
+DIFFUSE_DTYPE = np.dtype([("pos", np.float32, 2), ("vel", np.float32, 2), ("life", np.float32), ("r", np.float32),
+                          ("info", np.uint32), ("z", np.float32)])
+DIFFUSE_MAX = 1 << 16
 
 STAGES = ["advance", "sort", "p2g", "grid", "pressure", "project", "viscosity", "project2"]
 
@@ -197,6 +201,7 @@ def lib() -> C.CDLL:
         "sprout_sim_flow_parity": ([V, P(C.c_uint32)], C.c_int),
         "sprout_sim_recorded_iters": ([V, P(C.c_uint32)], C.c_int),
         "sprout_sim_download_look": ([V, V, C.c_size_t, V, C.c_size_t, P(C.c_uint32), P(C.c_uint32)], C.c_int),
+        "sprout_sim_download_spray": ([V, V, C.c_size_t, V, V, C.c_size_t, V, C.c_size_t, P(C.c_uint32)], C.c_int),
         "sprout_params_get_color": ([V, C.c_uint32, C.c_char_p, P(C.c_float), P(C.c_int)], C.c_int),
         "sprout_params_get_row": ([V, C.c_uint32, P(C.c_int32), P(C.c_int32)], C.c_int),
         "sprout_sim_download_render": ([V, C.c_int, V, C.c_size_t, P(C.c_size_t)], C.c_int),
@@ -485,6 +490,20 @@ class FluidSim:
         v = (C.c_uint32 * 3)()
         _check(lib().sprout_sim_recorded_iters(self._h, v))
         return [int(x) for x in v]
+
+    def download_spray(self):
+        """spray.comp's pool: (entries (65536, DIFFUSE_DTYPE), free stack, listed entries,
+        foam per cell (2, h, w), (never handed out, stack height, listed, next parity))."""
+        st = (C.c_uint32 * 4)()
+        _check(lib().sprout_sim_download_spray(self._h, None, 0, None, None, 0, None, 0, st))
+        pool = np.zeros(DIFFUSE_MAX, DIFFUSE_DTYPE)
+        stack = np.zeros(DIFFUSE_MAX, np.uint32)
+        lst = np.zeros(DIFFUSE_MAX, np.uint32)
+        foam = np.zeros(2 * self.w * self.h, np.uint32)
+        _check(lib().sprout_sim_download_spray(self._h, pool.ctypes.data, DIFFUSE_MAX, stack.ctypes.data, lst.ctypes.data,
+                                               DIFFUSE_MAX, foam.ctypes.data, foam.size, st))
+        s = [int(x) for x in st]
+        return pool, stack[: s[1]], lst[: s[2]], foam.reshape(2, self.h, self.w), s
 
     def download_look(self):
         """look.comp's state: (per slot (id, 0, packed A, 0) as uint32 (n, 4), the listed slots)."""

@@ -155,6 +155,28 @@ void launch_render_clock(const DevScene& d, RenderClock* clock, int valid, int c
 // the look splat (*count of them, at most cap in list). `frame`: FluidSim's frame counter.
 void launch_look(const DevScene& d, const DevOptics* opt, const RenderClock* clock, uint32_t frame, uint32_t* count,
                  uint32_t* list, uint32_t cap, uint32_t n_slots, cudaStream_t st);
+// spray.comp's pool (spray.cu): an entry (the reference's Diffuse, 32 bytes), the pool's
+// counters (entries never handed out so far, the free stack's height, the live entries listed,
+// this frame's emissions), and its buffers.
+constexpr uint32_t kDiffuseMax = 1u << 16;   // mod.rs DIFFUSE_MAX
+struct DevDiffuse {
+    float px, py, vx, vy, life, r;
+    uint32_t info;
+    float z;
+};
+static_assert(sizeof(DevDiffuse) == 32, "Diffuse is 32 bytes");
+struct PoolState {
+    uint32_t hw, top, listed, total;
+};
+struct SprayBufs {
+    DevDiffuse* pool;
+    uint32_t *stack, *list, *dcount, *counts, *bsum, *flags;
+    PoolState* ps;
+};
+// record_spray: stage 0 (when `makes`, and the clock's dt > 0) and stage 1 of spray.comp, the
+// foam counted into copy `parity` of dcount. `amount`: params.bubbles.
+void launch_spray(const DevScene& d, const ushort4* smooth, const SprayBufs& b, const RenderClock* clock, uint32_t frame,
+                  uint32_t parity, float amount, bool makes, cudaStream_t st);
 // Scene::rasterize on the device (raster.cu): the tank's solid fields straight into device
 // buffers, bit-identical to the host's Scene::rasterize (scene.cpp).
 struct Scene;

@@ -19,6 +19,7 @@
 
 #include "dev_common.cuh"
 #include "kernels.h"
+#include "sample.cuh"
 
 namespace sprout {
 
@@ -58,25 +59,6 @@ __global__ void k_step(DevScene d) {
 
 // ---- G2P and advection ------------------------------------------------------------------
 
-struct Grid {
-    const float4* vel;
-    const float* sdf;
-    int W, H;
-    DEV float4 v(int x, int y) const { return __ldg(&vel[y * W + x]); }
-};
-
-DEV float sample_sdf(const Grid& g, float x, float y, float* gx_out, float* gy_out) {
-    float gx = clampf(x, 0.0f, (float)g.W - 0.001f), gy = clampf(y, 0.0f, (float)g.H - 0.001f);
-    int ix = (int)gx, iy = (int)gy;
-    float fx = gx - (float)ix, fy = gy - (float)iy;
-    int w1 = g.W + 1;
-    int k = iy * w1 + ix;
-    float d00 = __ldg(&g.sdf[k]), d10 = __ldg(&g.sdf[k + 1]), d01 = __ldg(&g.sdf[k + w1]), d11 = __ldg(&g.sdf[k + w1 + 1]);
-    *gx_out = mixf(d10 - d00, d11 - d01, fy);
-    *gy_out = mixf(d01 - d00, d11 - d10, fx);
-    return mixf(mixf(d00, d10, fx), mixf(d01, d11, fx), fy);
-}
-
 DEV bool collide(const Grid& g, float wall_margin, float& x, float& y, float& vx, float& vy, bool beyond) {
     float nx, ny;
     float d = sample_sdf(g, x, y, &nx, &ny);
@@ -99,47 +81,6 @@ DEV bool collide(const Grid& g, float wall_margin, float& x, float& y, float& vx
     return false;
 }
 
-// Bilinear grid velocity over live faces; components without a live face keep the fallback.
-DEV float2 sample_vel(const Grid& g, float x, float y, float2 fb) {
-    float2 o = fb;
-    {
-        float gx = x, gy = y - 0.5f;
-        int bx = (int)floorf(gx), by = (int)floorf(gy);
-        float fx = gx - (float)bx, fy = gy - (float)by;
-        float sw = 0.0f, su = 0.0f;
-#pragma unroll
-        for (int b = 0; b < 2; b++)
-#pragma unroll
-            for (int a = 0; a < 2; a++) {
-                float4 q = g.v(bx + a, by + b);
-                if (face_live(q.z)) {
-                    float wt = (a == 0 ? 1.0f - fx : fx) * (b == 0 ? 1.0f - fy : fy);
-                    sw += wt;
-                    su += wt * q.x;
-                }
-            }
-        if (sw > 1e-3f) o.x = su / sw;
-    }
-    {
-        float gx = x - 0.5f, gy = y;
-        int bx = (int)floorf(gx), by = (int)floorf(gy);
-        float fx = gx - (float)bx, fy = gy - (float)by;
-        float sw = 0.0f, su = 0.0f;
-#pragma unroll
-        for (int b = 0; b < 2; b++)
-#pragma unroll
-            for (int a = 0; a < 2; a++) {
-                float4 q = g.v(bx + a, by + b);
-                if (face_live(q.w)) {
-                    float wt = (a == 0 ? 1.0f - fx : fx) * (b == 0 ? 1.0f - fy : fy);
-                    sw += wt;
-                    su += wt * q.y;
-                }
-            }
-        if (sw > 1e-3f) o.y = su / sw;
-    }
-    return o;
-}
 
 DEV float2 tool_target(const DevParams* P, float dx, float dy) {
     float l = len2(dx, dy);

@@ -1047,6 +1047,30 @@ struct SproutSim {
                 }
                 launch_look(d, d_optics, d_clock, frames, d_look_list, d_look_list + 1, capacity, n_slots, stream);
             }
+            // record_spray (mod.rs:1739-1773): once a liquid that foams or fizzes has been in the
+            // tank, the pool is moved every frame; new entries are made while one is
+            bool makes = false;
+            if (params.bubbles > 0.0f)
+                for (int r : tank.rows) makes |= params.mat[r].foam > 0.0f || params.mat[r].fizz > 0.0f;
+            diffuse_seen |= makes;
+            if (diffuse_seen) {
+                if (!spray.pool) {
+                    const size_t nc = (size_t)W * H;
+                    if ((rc = alloc(&spray.pool, (size_t)kDiffuseMax)) != SPROUT_OK) return rc;
+                    if ((rc = alloc(&spray.stack, (size_t)kDiffuseMax)) != SPROUT_OK) return rc;
+                    if ((rc = alloc(&spray.list, (size_t)kDiffuseMax)) != SPROUT_OK) return rc;
+                    if ((rc = alloc(&spray.flags, (size_t)kDiffuseMax)) != SPROUT_OK) return rc;
+                    if ((rc = alloc(&spray.dcount, 2 * nc)) != SPROUT_OK) return rc;
+                    if ((rc = alloc(&spray.counts, nc)) != SPROUT_OK) return rc;
+                    if ((rc = alloc(&spray.bsum, nc / 1024 + 2)) != SPROUT_OK) return rc;
+                    if ((rc = alloc(&spray.ps, 1)) != SPROUT_OK) return rc;
+                    CUDA_TRY(cudaMemsetAsync(spray.pool, 0, (size_t)kDiffuseMax * sizeof(DevDiffuse), stream));
+                    CUDA_TRY(cudaMemsetAsync(spray.dcount, 0, 2 * nc * sizeof(uint32_t), stream));
+                    CUDA_TRY(cudaMemsetAsync(spray.ps, 0, sizeof(PoolState), stream));
+                }
+                launch_spray(d, d_smooth, spray, d_clock, frames, diffuse_parity, params.bubbles, makes, stream);
+                diffuse_parity ^= 1u;
+            }
         }
         CUDA_TRY(cudaGetLastError());
         return SPROUT_OK;
@@ -1067,6 +1091,37 @@ struct SproutSim {
         *gap = std::max(2.0f * 3.14159265f * std::sqrt(sigma / (rho * g)) / params.cell_size, 3.0f);
         const float mu0 = 1.2566371e-6f;
         *mc = std::sqrt(2.0f * mu0 * (1.0f + 1.0f / (1.0f + best->susceptibility)) * std::sqrt(rho * g * sigma));
+    }
+    // spray.comp's pool (spray.cu): made, moved and listed by render calls
+    SprayBufs spray{};
+    bool diffuse_seen = false;
+    uint32_t diffuse_parity = 0;
+    int download_spray(SproutDiffuse* pool, size_t pool_cap, uint32_t* stack, uint32_t* list, size_t cap,
+                       uint32_t* foam, size_t foam_cap, uint32_t state[4]) {
+        for (int k = 0; k < 4; k++) state[k] = 0;
+        if (!spray.pool) return SPROUT_OK;
+        CUDA_TRY(cudaStreamSynchronize(stream));
+        PoolState ps;
+        CUDA_TRY(cudaMemcpy(&ps, spray.ps, sizeof ps, cudaMemcpyDeviceToHost));
+        state[0] = ps.hw;
+        state[1] = ps.top;
+        state[2] = ps.listed;
+        state[3] = diffuse_parity;
+        const size_t nc = (size_t)W * H;
+        if (pool) {
+            if (pool_cap < kDiffuseMax) return fail(SPROUT_E_ARG, "download_spray: the pool holds 65536 entries");
+            CUDA_TRY(cudaMemcpy(pool, spray.pool, (size_t)kDiffuseMax * sizeof(DevDiffuse), cudaMemcpyDeviceToHost));
+        }
+        if (stack || list) {
+            if (cap < kDiffuseMax) return fail(SPROUT_E_ARG, "download_spray: the stack and list hold 65536 entries");
+            if (stack) CUDA_TRY(cudaMemcpy(stack, spray.stack, (size_t)ps.top * 4, cudaMemcpyDeviceToHost));
+            if (list) CUDA_TRY(cudaMemcpy(list, spray.list, (size_t)ps.listed * 4, cudaMemcpyDeviceToHost));
+        }
+        if (foam) {
+            if (foam_cap < 2 * nc) return fail(SPROUT_E_ARG, "download_spray: the foam counts hold 2 x W x H");
+            CUDA_TRY(cudaMemcpy(foam, spray.dcount, 2 * nc * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+        }
+        return SPROUT_OK;
     }
     // A liquid with platelets (cloud_shape below 2/3) or specks is in the tank (mod.rs:1718-1721).
     uint32_t* d_look_list = nullptr;   // [0] how many listed, then their slots
@@ -2321,6 +2376,12 @@ int sprout_sim_download_render(SproutSim* sim, int which, uint16_t* out, size_t 
     CUDA_TRY(cudaMemcpy(out, src, n * sizeof(uint16_t), cudaMemcpyDeviceToHost));
     sim->d2h_bytes += n * sizeof(uint16_t);
     return SPROUT_OK;
+}
+
+int sprout_sim_download_spray(SproutSim* sim, SproutDiffuse* pool, size_t pool_cap, uint32_t* stack, uint32_t* list,
+                              size_t cap, uint32_t* foam, size_t foam_cap, uint32_t state[4]) {
+    if (!sim || !state) return fail(SPROUT_E_ARG, "null argument");
+    return sim->download_spray(pool, pool_cap, stack, list, cap, foam, foam_cap, state);
 }
 
 int sprout_sim_download_look(SproutSim* sim, uint32_t* state, size_t state_cap, uint32_t* list, size_t list_cap,
