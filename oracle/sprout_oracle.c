@@ -177,8 +177,6 @@ float o_powf(float x, float y) { return x == 1.0f ? 1.0f : o_expf(y * o_logf(x))
 #define TAIL_CELLS 1500
 #define MG_OMEGA 1.8f
 #define GRID_GROUP 16
-#define SORT_INTERVAL 128u
-#define SORT_MIN_PARTICLES 16384u
 #define WALL 3.0f
 #define PPC 4
 
@@ -2076,8 +2074,10 @@ void osim_sort(OSim* s) {
         run += k;
     }
     memset(s->sorted, 0, (size_t)n * sizeof(OParticle));
-    /* the look's state moves with its particle (sort.comp's plook) */
+    /* the look's state and the viscoelastic stress move with their particle (sort.comp's
+     * plook, pstress: sort.comp:66); dead slots end zeroed */
     uint32_t* look2 = s->plook ? (uint32_t*)calloc((size_t)n * 4 + 4, sizeof(uint32_t)) : NULL;
+    V4* stress2 = s->pstress ? (V4*)calloc((size_t)n + 1, sizeof(V4)) : NULL;
     for (uint32_t i = 0; i < n; i++) {
         const OParticle* p = &s->particles[i];
         if (p->kind == KIND_DEAD) continue;
@@ -2085,11 +2085,16 @@ void osim_sort(OSim* s) {
         uint32_t dst = count[cidx(s, cx, cy)]++;
         s->sorted[dst] = *p;
         if (look2) memcpy(look2 + 4 * (size_t)dst, s->plook + 4 * (size_t)i, 4 * sizeof(uint32_t));
+        if (stress2) stress2[dst] = s->pstress[i];
     }
     memcpy(s->particles, s->sorted, (size_t)n * sizeof(OParticle));
     if (look2) {
         memcpy(s->plook, look2, (size_t)n * 4 * sizeof(uint32_t));
         free(look2);
+    }
+    if (stress2) {
+        memcpy(s->pstress, stress2, (size_t)n * sizeof(V4));
+        free(stress2);
     }
     free(count);
 }
@@ -5070,12 +5075,11 @@ int osim_step(OSim* s, uint32_t substeps, float target, const OTool* tool) {
         s->S.batch_done = 0;
     }
     for (uint32_t k = 0; k < substeps; k++) {
-        s->since_sort++;
-        if (s->since_sort >= SORT_INTERVAL && s->n_slots >= SORT_MIN_PARTICLES) {
-            s->since_sort = 0;
-            osim_sort(s);
-        }
         substep(s, s->grid_valid);
+        /* the particles sorted by cell after every substep, as the engine keeps them (the
+         * reference sorts every 128 substeps, mod.rs:100, 2546; the order changes no physics:
+         * the deposits are integer sums and every particle is updated on its own) */
+        osim_sort(s);
         s->grid_valid = 1;
         s->substeps_done++;
     }

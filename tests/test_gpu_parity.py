@@ -213,3 +213,40 @@ def test_frame_blocking_reports_the_time_covered():
     adv = sim.frame_blocking(4, 4 / 240.0)
     assert abs(adv - 4 / 240.0) < 1e-6
     assert abs(sim.dt_estimate() - 1 / 240.0) < 1e-9
+
+
+@pytest.mark.parametrize("name", ["dam_break", "stratified", "elastic", "claims"])
+def test_slot_order_is_the_oracles(name):
+    """The engine and the oracle both sort the particles by cell after every substep (a
+    stable counting sort in slot order), so they hold every particle in the same slot: the
+    particle arrays are equal slot for slot, not only by id (what the render side's passes
+    that rank by slot, look.comp's specks, rely on). "claims": particles erased, then new ones
+    queued into the freed slots."""
+    DT = 1.0 / 240.0
+    if name == "claims":
+        import sprout_gb300 as S
+        from oracle import oracle as O
+        from test_gpu_admission import pair, small_tank
+        sim, ora, _ = pair(small_tank(capacity_extra=16))
+        sim.step(1, DT)
+        ora.step(1, DT)
+        tool = S.Tool()
+        tool.pos[0], tool.pos[1], tool.radius, tool.mode = 20.0, 20.0, 4.0, 2
+        otool = O.OTool()
+        otool.pos[0], otool.pos[1], otool.radius, otool.mode = 20.0, 20.0, 4.0, 2
+        sim.step(1, DT, tool)
+        ora.step(1, DT, otool)
+        new = O.fill_rect(96, 64, [60.0, 40.0, 72.0, 50.0], 59)
+        assert sim.spawn(new) == ora.spawn(new) == len(new)
+        for _ in range(4):
+            sim.step(1, DT)
+            ora.step(1, DT)
+    else:
+        make = {"dam_break": lambda: tanks.dam_break(96, 64), "stratified": lambda: tanks.stratified(96, 64),
+                "elastic": lambda: tanks.elastic_drop()}[name]
+        sim, ora, problems = run_pair(make(), 6)
+        assert not problems, "\n".join(problems[:10])
+    g, o = sim.download_particles(), ora.particles()
+    assert len(g) == len(o)
+    bad = np.nonzero(g.view(np.uint8).reshape(len(g), -1).any(axis=1) != o.view(np.uint8).reshape(len(o), -1).any(axis=1))[0]
+    assert np.array_equal(g.view(np.uint8), o.view(np.uint8)), f"particles differ slot for slot ({len(bad)} live/dead mismatches)"
