@@ -285,22 +285,26 @@ int sprout_sim_recorded_iters(SproutSim* sim, uint32_t out[3]);
  * specks a new particle would bring into spray.comp's pool are not made (no pool). */
 int sprout_sim_download_look(SproutSim* sim, uint32_t* state, size_t state_cap, uint32_t* list, size_t list_cap,
                              uint32_t* slots, uint32_t* listed);
-/* spray.comp's pool (FluidSim::diffuse_buffers, mod.rs:1773-1777): the bubbles, foam and spray
- * of the render calls so far (blocking). An entry is the reference's Diffuse: position and
- * velocity (cells, cells / s), life left (s), radius (cells), info (bits 0-1 state: 0 free,
- * 1 bubble, 2 foam, 3 spray; bit 2 grows; bits 8-14 the liquid's row + 1; 15-31 a seed),
- * depth or the foam's given life. pool: all 65536 entries; stack: the free stack (state[1]
- * entries); list: the live entries for the sprites (state[2]), in entry order; foam: the foam
- * per cell, two copies of W x H; state: entries never handed out, the free stack's height,
- * the entries listed, the copy of the foam counts the next frame counts into. Each pointer may
- * be NULL. Entries are handed out in a deterministic order (emissions ranked by cell). */
+/* spray.comp's pool (FluidSim::diffuse_buffers, mod.rs:1773-1777): the bubbles, foam, spray
+ * and specks of the render calls so far (blocking). An entry is the reference's Diffuse:
+ * position and velocity (cells, cells / s), life left (s; a speck: its flake's packed
+ * normal), radius (cells), info (bits 0-1 state: 0 free, then bubble, foam, spray, or for a
+ * speck suspended, resting, falling; bit 2 grows; bit 3 a speck; bits 8-14 the liquid's row
+ * + 1; 15-31 a seed), depth or the foam's given life. pool: all 196608 entries (65536 for
+ * bubbles, foam and spray, then 131072 for specks); stack, stack1: the two parts' free stacks
+ * (state[1], state[5] entries); list: the live entries for the sprites (state[2]), in entry
+ * order; counts: foam per cell (copies 0, 1) and resting specks per cell (2, 3), W x H each;
+ * state: bubbles never handed out, their stack's height, entries listed, the copy the next
+ * frame counts into, specks never handed out, their stack's height, 0, 0. Each pointer may be
+ * NULL. Entries are handed out in a deterministic order: a frame's bubbles ranked by cell,
+ * its specks by particle slot. */
 typedef struct SproutDiffuse {
     float pos[2], vel[2], life, r;
     uint32_t info;
     float z;
 } SproutDiffuse;
-int sprout_sim_download_spray(SproutSim* sim, SproutDiffuse* pool, size_t pool_cap, uint32_t* stack, uint32_t* list,
-                              size_t cap, uint32_t* foam, size_t foam_cap, uint32_t state[4]);
+int sprout_sim_download_spray(SproutSim* sim, SproutDiffuse* pool, size_t pool_cap, uint32_t* stack, uint32_t* stack1,
+                              uint32_t* list, size_t cap, uint32_t* counts, size_t counts_cap, uint32_t state[8]);
 /* FluidSim::flow_view's parity (mod.rs:1850-1853): the copy of the flow map that holds it now
  * (blocking). */
 int sprout_sim_flow_parity(SproutSim* sim, uint32_t* parity);

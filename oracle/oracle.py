@@ -170,7 +170,9 @@ def lib() -> C.CDLL:
         L.osim_look_state.restype = C.c_long
         L.osim_spray.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_float, C.c_float]
         L.osim_spray.restype = C.c_long
-        L.osim_spray_state.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        L.osim_spray_state.argtypes = [C.c_void_p] + [C.c_void_p] * 6
+        L.osim_set_dust.argtypes = [C.c_void_p, C.c_int]
+        L.osim_set_dust.restype = None
         L.osim_spray_state.restype = C.c_long
         L.o_expf.argtypes = [C.c_float]
         L.o_expf.restype = C.c_float
@@ -322,16 +324,17 @@ class OracleSim:
         return int(lib().osim_particles(self.h_, None, 0))
 
     def spray(self):
-        """spray.comp's pool: (entries, free stack, listed entries, foam (2, h, w), counters)."""
-        from sprout_gb300 import DIFFUSE_DTYPE, DIFFUSE_MAX
-        st = (C.c_uint32 * 4)()
-        pool = np.zeros(DIFFUSE_MAX, DIFFUSE_DTYPE)
-        stack = np.zeros(DIFFUSE_MAX, np.uint32)
-        lst = np.zeros(DIFFUSE_MAX, np.uint32)
-        foam = np.zeros(2 * self.w * self.h, np.uint32)
-        lib().osim_spray_state(self.h_, pool.ctypes.data, stack.ctypes.data, lst.ctypes.data, foam.ctypes.data, st)
+        """spray.comp's pool: (entries, bubbles' stack, specks' stack, listed entries, counts
+        (4, h, w), state (8)) as FluidSim.download_spray gives them."""
+        from sprout_gb300 import DIFFUSE_DTYPE, POOL_MAX
+        st = (C.c_uint32 * 8)()
+        pool = np.zeros(POOL_MAX, DIFFUSE_DTYPE)
+        stack, stack1, lst = (np.zeros(POOL_MAX, np.uint32) for _ in range(3))
+        counts = np.zeros(4 * self.w * self.h, np.uint32)
+        lib().osim_spray_state(self.h_, pool.ctypes.data, stack.ctypes.data, stack1.ctypes.data, lst.ctypes.data,
+                               counts.ctypes.data, st)
         s = [int(x) for x in st]
-        return pool, stack[: s[1]], lst[: s[2]], foam.reshape(2, self.h, self.w), s
+        return pool, stack[: s[1]], stack1[: s[5]], lst[: s[2]], counts.reshape(4, self.h, self.w), s
 
     def look(self):
         """look.comp's state per slot (n, 4) uint32 and the slots the last render listed."""
@@ -361,7 +364,8 @@ class OracleSim:
         lib().osim_particles(self.h_, out.ctypes.data, n)
         return out
 
-    def render(self, optics: np.ndarray, inv_speed: float = 1.0 / 60.0, sss_iters: int = 4, bubbles: float = 1.0):
+    def render(self, optics: np.ndarray, inv_speed: float = 1.0 / 60.0, sss_iters: int = 4, bubbles: float = 1.0,
+               has_dust: bool = False):
         """FluidSim::record_cell_optics (mod.rs:1626-1712) on the current grid, from the optics
         table `optics` (96 rows of 240 bytes): cell_optics.comp, light.comp, optics_blur.comp,
         sss.comp, flow_map.comp and glow.comp. Returns (raw (20, h, w, 4), smooth (24, h, w, 4),
@@ -393,6 +397,7 @@ class OracleSim:
                int(np.float32(inv_speed).view(np.uint32)))
         if key != self._key:
             self._key = key
+            lib().osim_set_dust(self.h_, 1 if has_dust else 0)   # a liquid with specks in the tank
             lib().osim_render(self.h_, tab.ctypes.data, inv_speed, sss_iters, self._raw.ctypes.data,
                               self._smooth.ctypes.data, self._ga.ctypes.data, self._gb.ctypes.data)
             if dt > 0.0:

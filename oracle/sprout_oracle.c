@@ -705,10 +705,12 @@ struct OSim {
     uint32_t frame;    /* FluidSim::frame: step calls so far (mod.rs:2402) */
     /* spray.comp's pool: entries, free stack, listed entries, foam per cell (two copies),
      * the counters (never handed out, stack height, listed), the copy counted next */
-    struct ODiffuse* dpool;
-    uint32_t *dstack, *dlist, *dcount;
-    uint32_t d_hw, d_top, d_listed, d_parity;
-    int d_seen;   /* a liquid that foams or fizzes has been in the tank */
+    struct ODiffuse* dpool;   /* 65536 bubbles' entries, then 131072 specks' */
+    uint32_t *dstack, *dstack1, *dlist, *dcount;   /* counts: foam x 2, resting specks x 2 */
+    int32_t* dfield;          /* the dust field, 4 ints a cell */
+    uint32_t d_hw, d_top, d_listed, d_parity, d_hw1, d_top1;
+    int d_seen;       /* a liquid that foams, fizzes or carries specks has been in the tank */
+    int has_dust;     /* a liquid with specks is in the tank (set before a render) */
     V4* estr;      /* per cell: the deposited stress (elastic.comp) */
     I2* rl;        /* per cell: rigid label (root cell, -1 not rigid); its body at the root */
     int64_t* rbody;   /* per body: 15 fixed-point sums (rigid.comp) */
@@ -4755,6 +4757,8 @@ void osim_destroy(OSim* s) {
     if (!s) return;
     free(s->plook);
     free(s->dpool);
+    free(s->dstack1);
+    free(s->dfield);
     free(s->dstack);
     free(s->dlist);
     free(s->dcount);
@@ -5324,8 +5328,8 @@ static V2 o_spike_phase(const OSim* s, float gap, float x, float y) {
     return v2(cs, sn);
 }
 
-static void o_cell_optics(const OSim* s, const OOptics* opt, float inv_speed, float spike_gap, float spike_mc, int cx,
-                          int cy, uint16_t* raw) {
+static void o_cell_optics(const OSim* s, const OOptics* opt, float inv_speed, float spike_gap, float spike_mc,
+                          const int32_t* dfield, float dust, int cx, int cy, uint16_t* raw) {
     const int i = cy * s->W + cx, k = i * s->tank.stride;
     const size_t nc = (size_t)s->W * s->H;
     const int cw = s->acc[k + 4];
@@ -5497,6 +5501,13 @@ static void o_cell_optics(const OSim* s, const OOptics* opt, float inv_speed, fl
         o[3] = v4muls(v4(em[0] + lum[0], em[1] + lum[1], em[2] + lum[2], speed), occ);
         float s_mean = aq.w + ot.w + dense.w;
         o[16] = v4(fx2.x * occ, fx2.y * occ, s_mean > 1e-5f ? fx2.z / s_mean : 1.0f, s_mean > 1e-5f ? fx2.w / s_mean : 1.0f);
+        if (dust > 0.0f && occ > 0.02f) {   /* cell_optics.comp:387-390 */
+            const float f = 1.0f / 1024.0f;
+            o[18] = v4((float)dfield[4 * i] * f, (float)dfield[4 * i + 1] * f, (float)dfield[4 * i + 2] * f,
+                       (float)dfield[4 * i + 3] * f);
+            float cap = 200.0f * occ;
+            o[18] = v4(minf(o[18].x, cap), minf(o[18].y, cap), minf(o[18].z, cap), minf(o[18].w, cap));
+        }
         o[19] = v4add(v4muls(o[19], occ), o[18]);
         o[17] = v4muls(v4(lum[0], lum[1], lum[2], ior_sum), occ);
         o[4] = v4muls(v4(sty.x, sty.y, waq, waq + wot), occ);
@@ -5709,8 +5720,10 @@ long osim_render(const OSim* s, const void* optics, float inv_speed, int sss_ite
     const OOptics* opt = (const OOptics*)optics;
     float gap, mc;
     o_spike_params(s, &gap, &mc);
+    /* the last frame's dust field, once the pool has run (mod.rs:1653) */
+    float dust = (s->d_seen && s->has_dust && s->dfield) ? 1.0f : 0.0f;
     for (int y = 0; y < s->H; y++)
-        for (int x = 0; x < s->W; x++) o_cell_optics(s, opt, inv_speed, gap, mc, x, y, raw);
+        for (int x = 0; x < s->W; x++) o_cell_optics(s, opt, inv_speed, gap, mc, s->dfield, dust, x, y, raw);
     o_light(s, raw);
     for (int y = 0; y < s->H; y++)
         for (int x = 0; x < s->W; x++) o_optics_blur(s, raw, smooth, x, y);
@@ -5767,97 +5780,6 @@ long osim_flow_map(const OSim* s, const uint16_t* smooth, uint16_t* flow, float 
     return 0;
 }
 
-/* look.comp (main, 93-171) over the particle slots in order, from the optics table `optics`,
- * FluidSim's frame counter and `dt`, the simulated time since the last optics call: the
- * second moment A of the platelets' normals of each particle of a liquid with platelets,
- * Jeffery's equation with the quadratic closure on the shear part of its APIC gradient, in
- * sub = clamp(ceil(rate dt / 0.15), 1, 8) steps, then rotational diffusion (mix towards I / 3
- * by 1 - exp(-6 Dr dt)), kept at 10 bits each rounded stochastically (quant, pack_a); a slot
- * whose stored id differs holds a new particle, which starts at I / 3. The listed slots (in
- * slot order) go to `list` (at most `cap`); returns how many were listed. The specks' part
- * (a new particle's specks into spray.comp's pool) is not restated: no pool (dust_cap 0). */
-static float o_rnd24(uint32_t h) { return (float)(h >> 8) / 16777216.0f; }
-static uint32_t o_quant10(float v, uint32_t h) {
-    const float m = 1023.0f;
-    return (uint32_t)clampf(floorf(clampf(v, 0.0f, 1.0f) * m + o_rnd24(h)), 0.0f, m);
-}
-static uint32_t o_pack_a(float ax, float ay, float az, uint32_t h) {
-    return o_quant10(ax, hash32(h ^ 0x1b873593u)) | (o_quant10(ay, hash32(h ^ 0xcc9e2d51u)) << 10) |
-           (o_quant10(az + 0.5f, hash32(h ^ 0xe6546b64u)) << 20);
-}
-long osim_look(OSim* s, const void* optics, float dt, uint32_t* list, uint32_t cap) {
-    const OOptics* opt = (const OOptics*)optics;
-    if (!s->plook) {
-        s->plook = (uint32_t*)calloc((size_t)s->capacity * 4, sizeof(uint32_t));
-        if (!s->plook) return -2;
-    }
-    long listed = 0;
-    const float third = 1.0f / 3.0f;
-    for (uint32_t i = 0; i < s->n_slots; i++) {
-        const OParticle* p = &s->particles[i];
-        uint32_t low = p->kind & 255u;
-        if (p->kind == KIND_DEAD || low == 0u || low > 96u) continue;   /* rows of the table */
-        uint32_t row = low - 1u;
-        const OOptics* o = &opt[row];
-        float lx = o->opt[1], ly = o->fx2[2];   /* look_of */
-        if (o->idx[0] >= 0) {
-            const OOptics* dl = &opt[o->idx[0]];
-            float t = clampf(p->s, 0.0f, 1.0f);
-            lx = mixf(dl->opt[1], lx, t);
-            ly = mixf(dl->fx2[2], ly, t);
-        }
-        if (maxf(lx, ly) <= 0.0f) continue;
-        uint32_t* st = s->plook + 4 * (size_t)i;
-        int fresh = st[0] != p->id;
-        uint32_t h = hash32(p->id * 0x9e3779b1u ^ hash32(s->frame * 0x85ebca6bu + 0x165667b1u));
-        if (lx <= 0.0f) {
-            if (fresh) {
-                st[0] = p->id; st[1] = 0u; st[2] = o_pack_a(third, third, 0.0f, h); st[3] = 0u;
-            }
-            continue;
-        }
-        float ax = third, ay = third, az = 0.0f;
-        if (!fresh) {
-            ax = (float)(st[2] & 1023u) / 1023.0f;
-            ay = (float)((st[2] >> 10) & 1023u) / 1023.0f;
-            az = (float)((st[2] >> 20) & 1023u) / 1023.0f - 0.5f;
-            if (dt > 0.0f) {
-                float Bc = o->opt2[2];
-                float w = 0.5f * (p->c[2] - p->c[1]);
-                float dv = 0.5f * (p->c[0] + p->c[3]);
-                float exx = p->c[0] - dv, eyy = p->c[3] - dv, exy = 0.5f * (p->c[1] + p->c[2]);
-                float rate = fabsf(w) + fabsf(exx) + fabsf(eyy) + fabsf(exy);
-                float sf = ceilf(rate * dt / 0.15f);
-                int sub = sf >= 8.0f ? 8 : (sf >= 1.0f ? (int)sf : 1);
-                float h1 = dt / (float)sub;
-                float ezz = 0.0f;
-                for (int k = 0; k < sub; k++) {
-                    float a = ax, b = ay, c = az, z = 1.0f - a - b;
-                    float AE = exx * a + eyy * b + 2.0f * exy * c + ezz * z;
-                    float rx = -2.0f * w * c, ry = 2.0f * w * c, rz = w * (a - b);
-                    float e2 = 2.0f * AE;
-                    float sx = 2.0f * (exx * a + exy * c) - e2 * a;
-                    float sy = 2.0f * (exy * c + eyy * b) - e2 * b;
-                    float sz = c * (exx + eyy) + exy * (a + b) - e2 * c;
-                    ax = ax + h1 * (rx + Bc * sx);
-                    ay = ay + h1 * (ry + Bc * sy);
-                    az = az + h1 * (rz + Bc * sz);
-                }
-                float t = 1.0f - o_expf(-6.0f * o->opt2[1] * dt);
-                ax = mixf(ax, third, t);
-                ay = mixf(ay, third, t);
-                az = mixf(az, 0.0f, t);
-                ax = clampf(ax, 0.0f, 1.0f);
-                ay = clampf(ay, 0.0f, 1.0f);
-                az = clampf(az, -0.5f, 0.5f);
-            }
-        }
-        st[0] = p->id; st[1] = 0u; st[2] = o_pack_a(ax, ay, az, h); st[3] = 0u;
-        if ((uint32_t)listed < cap) list[listed] = i;
-        listed++;
-    }
-    return listed;
-}
 /* spray.comp (main 171-494; mod.rs:1739-1773): bubbles, foam and spray in a pool of 65536.
  * Stage 0 (make, per cell) where liquid traps air, folds in, crests, or fizzes; stage 1 (move,
  * per entry) as bubble, foam or spray, the foam counted per cell, the live entries listed.
@@ -5867,7 +5789,21 @@ long osim_look(OSim* s, const void* optics, float dt, uint32_t* list, uint32_t c
  * order. Not restated: the specks (not carried) and a droplet's splat into the film map's
  * intake (film_lay.glsl; no film map): the droplet is removed as the reference removes it. */
 typedef struct ODiffuse { float px, py, vx, vy, life, r; uint32_t info; float z; } ODiffuse;
-#define D_MAX 65536u
+#define D_MAX 65536u       /* DIFFUSE_MAX */
+#define D_DUST 131072u     /* DUST_MAX */
+#define D_POOL (D_MAX + D_DUST)
+static int d_alloc(OSim* s) {
+    if (s->dpool) return 0;
+    const size_t nc = (size_t)s->W * s->H;
+    s->dpool = (ODiffuse*)calloc(D_POOL, sizeof(ODiffuse));
+    s->dstack = (uint32_t*)calloc(D_MAX, sizeof(uint32_t));
+    s->dstack1 = (uint32_t*)calloc(D_DUST, sizeof(uint32_t));
+    s->dlist = (uint32_t*)calloc(D_POOL, sizeof(uint32_t));
+    s->dcount = (uint32_t*)calloc(4 * nc, sizeof(uint32_t));
+    s->dfield = (int32_t*)calloc(4 * nc, sizeof(int32_t));
+    return (s->dpool && s->dstack && s->dstack1 && s->dlist && s->dcount && s->dfield) ? 0 : -2;
+}
+void osim_set_dust(OSim* s, int has_dust) { s->has_dust = has_dust; }
 enum { D_FREE = 0, D_BUBBLE = 1, D_FOAM = 2, D_SPRAY = 3 };
 static float d_rnd(uint32_t h) { return (float)(h >> 8) / 16777216.0f; }
 static float d_ramp(float x, float lo, float hi) { return clampf((x - lo) / (hi - lo), 0.0f, 1.0f); }
@@ -5894,8 +5830,8 @@ static V4 d_vel_lin(const OSim* s, int x, int y) {
     long long k = (long long)y * s->W + x;
     return (k >= 0 && k < (long long)s->W * s->H) ? s->vel[k] : v4(0.0f, 0.0f, 0.0f, 0.0f);
 }
-static V2 d_sample_vel(const OSim* s, float x, float y) {
-    float o[2] = {0.0f, 0.0f};
+static V2 d_sample_vel_fb(const OSim* s, float x, float y, V2 fb) {
+    float o[2] = {fb.x, fb.y};
     for (int comp = 0; comp < 2; comp++) {
         float gx = comp == 0 ? x : x - 0.5f, gy = comp == 0 ? y - 0.5f : y;
         int bx = (int)floorf(gx), by = (int)floorf(gy);
@@ -6028,12 +5964,184 @@ static void d_make(OSim* s, const uint16_t* sm, int cx, int cy, float dt, float 
         }
     }
 }
-/* move(): entry i; 0 nothing, 1 freed, 2 live */
-static int d_move(OSim* s, const uint16_t* sm, uint32_t i, float dt) {
+/* hemi-octahedral flake normals (look.comp pack_n, spray.comp unpack_n) */
+static uint32_t d_quant10(float v, uint32_t h) {
+    const float m = 1023.0f;
+    return (uint32_t)clampf(floorf(clampf(v, 0.0f, 1.0f) * m + d_rnd(h)), 0.0f, m);
+}
+static uint32_t d_pack_n(float nx, float ny, float nz, uint32_t h) {
+    if (nz < 0.0f) {
+        nx = -nx;
+        ny = -ny;
+        nz = -nz;
+    }
+    float den = maxf(fabsf(nx) + fabsf(ny) + nz, 1e-6f);
+    float px = nx / den, py = ny / den;
+    float qx = (px + py) * 0.5f + 0.5f, qy = (px - py) * 0.5f + 0.5f;
+    return d_quant10(qx, hash32(h)) | (d_quant10(qy, hash32(h ^ 0x68e31da4u)) << 10);
+}
+static void d_normalize3(float* x, float* y, float* z) {
+    float l = sqrtf(*x * *x + *y * *y + *z * *z);
+    *x = *x / l;
+    *y = *y / l;
+    *z = *z / l;
+}
+static void d_unpack_n(uint32_t b, float* x, float* y, float* z) {
+    float qx = (float)(b & 1023u) / 1023.0f * 2.0f - 1.0f, qy = (float)((b >> 10) & 1023u) / 1023.0f * 2.0f - 1.0f;
+    *x = (qx + qy) * 0.5f;
+    *y = (qx - qy) * 0.5f;
+    *z = maxf(1.0f - fabsf(*x) - fabsf(*y), 0.0f);
+    d_normalize3(x, y, z);
+}
+/* spray.comp move_dust (lines 272-367): a speck suspended, resting or falling; resting ones
+ * counted per cell (copies 2, 3), its share of the colour into the dust field */
+static int d_move_dust(OSim* s, const OOptics* opt, uint32_t i, float dt) {
     const size_t nc = (size_t)s->W * s->H;
     ODiffuse e = s->dpool[i];
     uint32_t st = e.info & 3u;
-    if (st == D_FREE || (e.info & 8u) != 0u) return 0;
+    int W = s->W, H = s->H;
+    uint32_t copy_in = 1u - s->d_parity, copy_out = s->d_parity;
+    int row = (int)((e.info >> 8) & 127u) - 1;
+    if (row < 0) {
+        s->dpool[i].info = 0u;
+        return 1;
+    }
+    const OOptics* o = &opt[row];
+    float rho_p = o->dust2[1] / 998.0f;
+    float aspect = o->dust2[2];
+    float rr = e.r;
+    float d_eq = 2.0f * rr * (aspect < 0.6667f ? o_powf(1.5f * maxf(aspect, 0.005f), 1.0f / 3.0f) : 1.0f);
+    float pack = maxf(o->dcol[3], 1.0f);
+    float Bc = (aspect * aspect - 1.0f) / (aspect * aspect + 1.0f);
+    float nx, ny, nz;
+    uint32_t lb;
+    memcpy(&lb, &e.life, 4);
+    d_unpack_n(lb, &nx, &ny, &nz);
+    uint32_t h0 = hash32(e.info ^ hash32(s->frame * 0x9e3779b1u + i));
+    float sf = ceilf(dt * 120.0f);
+    int steps = sf >= 8.0f ? 8 : (sf >= 1.0f ? (int)sf : 1);
+    float h = dt / (float)steps;
+    for (int k = 0; k < steps && st != D_FREE; k++) {
+        int cx = clampi((int)e.px, 0, W - 1), cy = clampi((int)e.py, 0, H - 1), ci = cy * W + cx;
+        float occ = d_occ_at(s, e.px, e.py);
+        V4 cf = s->cell[ci];
+        float rho = maxf(cf.y, 0.3f), nu = maxf(cf.z / rho, 1e-6f);
+        float drho = rho_p - rho;
+        float down = drho >= 0.0f ? 1.0f : -1.0f;
+        float ux_ = e.px - 0.0f, uy_ = e.py - down * (rr + 0.35f);
+        V2 gu;
+        float sd_u = sample_sdf(s, v2(ux_, uy_), &gu);
+        int cux = clampi((int)ux_, 0, W - 1), cuy = clampi((int)uy_, 0, H - 1);
+        float packed = (float)s->dcount[(size_t)(2u + copy_in) * nc + (size_t)cuy * W + cux];
+        int held = sd_u < 0.0f || ((cux != cx || cuy != cy) && packed >= pack) || uy_ < 0.0f;
+        int wet = occ > 0.30f;
+        V2 uf = d_sample_vel_fb(s, e.px, e.py, v2(0.0f, 0.0f));
+        float u_crit = 8.0f * sqrtf(0.05f * fabsf(drho) * P_.gravity * d_eq / rho);
+        if (st == D_FOAM) {
+            if (!held) st = wet ? D_BUBBLE : D_SPRAY;
+            else if (wet && len2(uf) > u_crit) {
+                st = D_BUBBLE;
+                e.vx = uf.x;
+                e.vy = uf.y;
+            } else {
+                float bx = 0.0f, by = 1.0f, bz = 0.0f;
+                if (sd_u < 0.0f) {
+                    bx = gu.x + 0.0f;
+                    by = gu.y + 1e-4f;
+                    float l = sqrtf(bx * bx + by * by);
+                    bx = bx / l;
+                    by = by / l;
+                }
+                float sg = signf(nx * bx + ny * by + nz * bz + 1e-4f);
+                float t = 1.0f - o_expf(-h / 0.3f);
+                nx = mixf(nx, bx * sg, t);
+                ny = mixf(ny, by * sg, t);
+                nz = mixf(nz, bz * sg, t);
+                d_normalize3(&nx, &ny, &nz);
+                e.vx = wet ? 0.0f : e.vx + h;
+                e.vy = 0.0f;
+                if (e.vx > 30.0f) st = D_FREE;
+                continue;
+            }
+        }
+        if (st == D_SPRAY && wet) st = D_BUBBLE;
+        if (st == D_BUBBLE && !wet) st = D_SPRAY;
+        if (st == D_BUBBLE) {
+            float vt = terminal(s, drho, rho, nu, d_eq);
+            float tx = uf.x - 0.0f, ty = uf.y - down * vt;
+            float tau = clampf(rho_p * d_eq * d_eq / (18.0f * rho * nu), 0.004f, 0.5f);
+            float t = 1.0f - o_expf(-h / tau);
+            e.vx = mixf(e.vx, tx, t);
+            e.vy = mixf(e.vy, ty, t);
+            if (aspect < 0.6667f) {
+                V2 ux1 = d_sample_vel_fb(s, e.px + 0.5f, e.py + 0.0f, uf), ux0 = d_sample_vel_fb(s, e.px - 0.5f, e.py - 0.0f, uf);
+                V2 uy1 = d_sample_vel_fb(s, e.px + 0.0f, e.py + 0.5f, uf), uy0 = d_sample_vel_fb(s, e.px - 0.0f, e.py - 0.5f, uf);
+                float gxx = ux1.x - ux0.x, gxy = ux1.y - ux0.y, gyx = uy1.x - uy0.x, gyy = uy1.y - uy0.y;
+                float w = 0.5f * (gxy - gyx);
+                float dv = 0.5f * (gxx + gyy);
+                float exx = gxx - dv, eyy = gyy - dv, exy = 0.5f * (gyx + gxy);
+                float wnx = -w * ny, wny = w * nx, wnz = 0.0f;
+                float enx = exx * nx + exy * ny, eny = exy * nx + eyy * ny, enz = 0.0f;
+                float ne = nx * enx + ny * eny + nz * enz;
+                nx = nx + h * (wnx + Bc * (enx - ne * nx));
+                ny = ny + h * (wny + Bc * (eny - ne * ny));
+                nz = nz + h * (wnz + Bc * (enz - ne * nz));
+                d_normalize3(&nx, &ny, &nz);
+            }
+            if (held && (e.vx - uf.x) * 0.0f + (e.vy - uf.y) * -down >= 0.0f && len2(uf) < u_crit) {
+                st = D_FOAM;
+                e.vx = 0.0f;
+                e.vy = 0.0f;
+            }
+        } else if (st == D_SPRAY) {
+            e.vx += 0.0f - e.vx * 1.2f * h;
+            e.vy += -P_.gravity * h - e.vy * 1.2f * h;
+        }
+        e.px += e.vx * h;
+        e.py += e.vy * h;
+        V2 gs;
+        float sd = sample_sdf(s, v2(e.px, e.py), &gs);
+        float rim = rr + 0.05f;
+        if (sd < rim) {
+            float gl = maxf(len2(gs), 1e-6f);
+            float nrx = gs.x / gl, nry = gs.y / gl;
+            e.px += nrx * (rim - sd);
+            e.py += nry * (rim - sd);
+            float vn = minf(e.vx * nrx + e.vy * nry, 0.0f);
+            e.vx -= nrx * vn;
+            e.vy -= nry * vn;
+            if (st == D_SPRAY) {
+                st = D_FOAM;
+                e.vx = 0.0f;
+                e.vy = 0.0f;
+            }
+        }
+        if (e.px < 0.0f || e.py < -1.0f || e.px >= (float)W || e.py >= (float)H) st = D_FREE;
+    }
+    uint32_t nb = d_pack_n(nx, ny, nz, h0);
+    memcpy(&e.life, &nb, 4);
+    e.info = (e.info & ~3u) | st;
+    s->dpool[i] = e;
+    if (st == D_FREE) return 1;
+    int cx = clampi((int)e.px, 0, W - 1), cy = clampi((int)e.py, 0, H - 1), ci = cy * W + cx;
+    if (st == D_FOAM) s->dcount[(size_t)(2u + copy_out) * nc + ci] += 1u;
+    if (o->dust[3] > 0.0f && d_occ_cell(s, cx, cy) > 0.05f) {
+        int qx = (int)(o->dust[0] * 1024.0f + 0.5f), qy = (int)(o->dust[1] * 1024.0f + 0.5f);
+        int qz = (int)(o->dust[2] * 1024.0f + 0.5f), qw = (int)(o->dust[3] * 1024.0f + 0.5f);
+        if (qx > 0) s->dfield[4 * ci] += qx;
+        if (qy > 0) s->dfield[4 * ci + 1] += qy;
+        if (qz > 0) s->dfield[4 * ci + 2] += qz;
+        s->dfield[4 * ci + 3] += qw;
+    }
+    return 2;
+}
+/* move(): entry i; 0 nothing, 1 freed, 2 live */
+static int d_move(OSim* s, const uint16_t* sm, const OOptics* opt, uint32_t i, float dt) {
+    const size_t nc = (size_t)s->W * s->H;
+    ODiffuse e = s->dpool[i];
+    uint32_t st = e.info & 3u;
+    if (st == D_FREE) return 0;
+    if ((e.info & 8u) != 0u) return d_move_dust(s, opt, i, dt);
     int W = s->W, H = s->H;
     uint32_t copy_in = 1u - s->d_parity, copy_out = s->d_parity;
     float cs = P_.misc[2];
@@ -6043,7 +6151,7 @@ static int d_move(OSim* s, const uint16_t* sm, uint32_t i, float dt) {
     for (int k = 0; k < steps && st != D_FREE; k++) {
         int cx = clampi((int)e.px, 0, W - 1), cy = clampi((int)e.py, 0, H - 1), ci = cy * W + cx;
         float occ = d_occ_at(s, e.px, e.py);
-        V2 uf = d_sample_vel(s, e.px, e.py);
+        V2 uf = d_sample_vel_fb(s, e.px, e.py, v2(0.0f, 0.0f));
         float crowd = d_crowd(s, cx, cy, copy_in);
         float gcx = d_crowd(s, cx + 1, cy, copy_in) - d_crowd(s, cx - 1, cy, copy_in);
         float gcy = d_crowd(s, cx, cy + 1, copy_in) - d_crowd(s, cx, cy - 1, copy_in);
@@ -6147,16 +6255,12 @@ long osim_spray(OSim* s, const uint16_t* smooth, const void* optics, float dt, f
             const OOptics* o = &opt[s->tank.rows[k]];
             if (o->sty[1] > 0.0f || o->fx2[1] > 0.0f) makes = 1;
         }
-    if (makes) s->d_seen = 1;
+    if (makes || s->has_dust) s->d_seen = 1;
     if (!s->d_seen) return 0;
-    if (!s->dpool) {
-        s->dpool = (ODiffuse*)calloc(D_MAX, sizeof(ODiffuse));
-        s->dstack = (uint32_t*)calloc(D_MAX, sizeof(uint32_t));
-        s->dlist = (uint32_t*)calloc(D_MAX, sizeof(uint32_t));
-        s->dcount = (uint32_t*)calloc(2 * nc, sizeof(uint32_t));
-        if (!s->dpool || !s->dstack || !s->dlist || !s->dcount) return -2;
-    }
+    if (d_alloc(s)) return -2;
     memset(s->dcount + (size_t)s->d_parity * nc, 0, nc * sizeof(uint32_t));
+    memset(s->dcount + (size_t)(2 + s->d_parity) * nc, 0, nc * sizeof(uint32_t));
+    memset(s->dfield, 0, 4 * nc * sizeof(int32_t));
     if (makes && dt > 0.0f) {
         uint32_t rank = 0, top0 = s->d_top, hw0 = s->d_hw;
         for (int cy = 0; cy < s->H; cy++)
@@ -6165,30 +6269,171 @@ long osim_spray(OSim* s, const uint16_t* smooth, const void* optics, float dt, f
         s->d_hw += rank > top0 ? rank - top0 : 0u;
     }
     uint32_t listed = 0;
-    for (uint32_t i = 0; i < D_MAX; i++) {
-        int f = d_move(s, smooth, i, dt);
-        if (f == 1) s->dstack[s->d_top++] = i;
-        else if (f == 2) s->dlist[listed++] = i;
+    for (uint32_t i = 0; i < D_POOL; i++) {
+        int f = d_move(s, smooth, opt, i, dt);
+        if (f == 1) {
+            if (i < D_MAX) s->dstack[s->d_top++] = i;
+            else s->dstack1[s->d_top1++] = i;
+        } else if (f == 2) s->dlist[listed++] = i;
     }
     s->d_listed = listed;
     s->d_parity ^= 1u;
     return (long)listed;
 }
-/* The pool (65536 entries of 8 words), its free stack and list, the foam counts (2 x W x H)
- * and the counters (never handed out, stack height, listed, the copy counted next). */
-long osim_spray_state(const OSim* s, void* pool, uint32_t* stack, uint32_t* list, uint32_t* foam, uint32_t state[4]) {
+/* The pool (196608 entries of 8 words), its free stacks and list, the counts (foam x 2,
+ * resting specks x 2, W x H each) and the counters (bubbles never handed out, their stack's
+ * height, listed, the copy counted next, specks never handed out, their stack's height). */
+long osim_spray_state(const OSim* s, void* pool, uint32_t* stack, uint32_t* stack1, uint32_t* list, uint32_t* counts,
+                      uint32_t state[8]) {
     state[0] = s->d_hw;
     state[1] = s->d_top;
     state[2] = s->d_listed;
     state[3] = s->d_parity;
+    state[4] = s->d_hw1;
+    state[5] = s->d_top1;
+    state[6] = state[7] = 0u;
     if (!s->dpool) return 0;
-    if (pool) memcpy(pool, s->dpool, D_MAX * sizeof(ODiffuse));
+    if (pool) memcpy(pool, s->dpool, D_POOL * sizeof(ODiffuse));
     if (stack) memcpy(stack, s->dstack, (size_t)s->d_top * 4);
+    if (stack1) memcpy(stack1, s->dstack1, (size_t)s->d_top1 * 4);
     if (list) memcpy(list, s->dlist, (size_t)s->d_listed * 4);
-    if (foam) memcpy(foam, s->dcount, 2 * (size_t)s->W * s->H * 4);
+    if (counts) memcpy(counts, s->dcount, 4 * (size_t)s->W * s->H * 4);
     return 1;
 }
 
+/* look.comp (main, 93-171) over the particle slots in order, from the optics table `optics`,
+ * FluidSim's frame counter and `dt`, the simulated time since the last optics call: the
+ * second moment A of the platelets' normals of each particle of a liquid with platelets,
+ * Jeffery's equation with the quadratic closure on the shear part of its APIC gradient, in
+ * sub = clamp(ceil(rate dt / 0.15), 1, 8) steps, then rotational diffusion (mix towards I / 3
+ * by 1 - exp(-6 Dr dt)), kept at 10 bits each rounded stochastically (quant, pack_a); a slot
+ * whose stored id differs holds a new particle, which starts at I / 3. The listed slots (in
+ * slot order) go to `list` (at most `cap`); returns how many were listed. The specks' part
+ * (a new particle's specks into spray.comp's pool) is not restated: no pool (dust_cap 0). */
+static float o_rnd24(uint32_t h) { return (float)(h >> 8) / 16777216.0f; }
+static uint32_t o_quant10(float v, uint32_t h) {
+    const float m = 1023.0f;
+    return (uint32_t)clampf(floorf(clampf(v, 0.0f, 1.0f) * m + o_rnd24(h)), 0.0f, m);
+}
+static uint32_t o_pack_a(float ax, float ay, float az, uint32_t h) {
+    return o_quant10(ax, hash32(h ^ 0x1b873593u)) | (o_quant10(ay, hash32(h ^ 0xcc9e2d51u)) << 10) |
+           (o_quant10(az + 0.5f, hash32(h ^ 0xe6546b64u)) << 20);
+}
+long osim_look(OSim* s, const void* optics, float dt, uint32_t* list, uint32_t cap) {
+    const OOptics* opt = (const OOptics*)optics;
+    if (!s->plook) {
+        s->plook = (uint32_t*)calloc((size_t)s->capacity * 4, sizeof(uint32_t));
+        if (!s->plook) return -2;
+    }
+    if (s->has_dust && d_alloc(s)) return -2;
+    long listed = 0;
+    const float third = 1.0f / 3.0f;
+    uint32_t speck_rank = 0, top1 = s->d_top1, hw1 = s->d_hw1;
+    for (uint32_t i = 0; i < s->n_slots; i++) {
+        const OParticle* p = &s->particles[i];
+        uint32_t low = p->kind & 255u;
+        if (p->kind == KIND_DEAD || low == 0u || low > 96u) continue;   /* rows of the table */
+        uint32_t row = low - 1u;
+        const OOptics* o = &opt[row];
+        float lx = o->opt[1], ly = o->fx2[2];   /* look_of */
+        if (o->idx[0] >= 0) {
+            const OOptics* dl = &opt[o->idx[0]];
+            float t = clampf(p->s, 0.0f, 1.0f);
+            lx = mixf(dl->opt[1], lx, t);
+            ly = mixf(dl->fx2[2], ly, t);
+        }
+        if (maxf(lx, ly) <= 0.0f) continue;
+        uint32_t* st = s->plook + 4 * (size_t)i;
+        int fresh = st[0] != p->id;
+        uint32_t h = hash32(p->id * 0x9e3779b1u ^ hash32(s->frame * 0x85ebca6bu + 0x165667b1u));
+        /* look.comp:103-128: the specks a new particle brings into the pool's second part, in
+         * slot order, the k-th of the frame taking what the k-th take gets */
+        if (fresh && ly > 0.0f && s->dpool) {
+            int src = o->fx2[2] > 0.0f ? (int)row : o->idx[0];
+            float e = ly * P_.inv_ppc;
+            float fn = floorf(e + o_rnd24(hash32(h ^ 0x2545f491u)));
+            uint32_t n = fn >= 8.0f ? 8u : (fn >= 1.0f ? (uint32_t)fn : 0u);
+            const OOptics* ds = &opt[src > 0 ? src : 0];
+            for (uint32_t k = 0; k < n; k++) {
+                uint32_t r = speck_rank + k;
+                int slot;
+                if (r < top1) slot = (int)s->dstack1[top1 - 1u - r];
+                else {
+                    uint32_t hw = hw1 + (r - top1);
+                    slot = hw < D_DUST ? (int)(D_MAX + hw) : -1;
+                }
+                if (slot < 0) break;
+                uint32_t hk = hash32(h + k * 0x9e3779b9u);
+                float u1 = o_rnd24(hash32(hk ^ 0x2c1b3c6du)), u2 = o_rnd24(hash32(hk ^ 0x297a2d39u));
+                float z = u1, a = 6.2831853f * u2, rr = sqrtf(maxf(1.0f - z * z, 0.0f));
+                float sn, cs;
+                o_sincos(a, &sn, &cs);
+                ODiffuse d;
+                d.px = p->pos[0] + (o_rnd24(hash32(hk ^ 0x51ed270bu)) - 0.5f) * 0.9f;
+                d.py = p->pos[1] + (o_rnd24(hash32(hk ^ 0x7feb352du)) - 0.5f) * 0.9f;
+                d.vx = p->vel[0];
+                d.vy = p->vel[1];
+                uint32_t nb = d_pack_n(rr * cs, rr * sn, z, hk);
+                memcpy(&d.life, &nb, 4);
+                d.r = ds->dust2[0] / P_.misc[2];
+                d.info = 1u | 8u | ((uint32_t)((src > 0 ? src : 0) + 1) << 8) | (hash32(hk ^ 0x68e31da4u) & 0xffff8000u);
+                d.z = o_rnd24(hash32(hk ^ 0xb5297a4du));
+                s->dpool[slot] = d;
+            }
+            speck_rank += n;
+        }
+        if (lx <= 0.0f) {
+            if (fresh) {
+                st[0] = p->id; st[1] = 0u; st[2] = o_pack_a(third, third, 0.0f, h); st[3] = 0u;
+            }
+            continue;
+        }
+        float ax = third, ay = third, az = 0.0f;
+        if (!fresh) {
+            ax = (float)(st[2] & 1023u) / 1023.0f;
+            ay = (float)((st[2] >> 10) & 1023u) / 1023.0f;
+            az = (float)((st[2] >> 20) & 1023u) / 1023.0f - 0.5f;
+            if (dt > 0.0f) {
+                float Bc = o->opt2[2];
+                float w = 0.5f * (p->c[2] - p->c[1]);
+                float dv = 0.5f * (p->c[0] + p->c[3]);
+                float exx = p->c[0] - dv, eyy = p->c[3] - dv, exy = 0.5f * (p->c[1] + p->c[2]);
+                float rate = fabsf(w) + fabsf(exx) + fabsf(eyy) + fabsf(exy);
+                float sf = ceilf(rate * dt / 0.15f);
+                int sub = sf >= 8.0f ? 8 : (sf >= 1.0f ? (int)sf : 1);
+                float h1 = dt / (float)sub;
+                float ezz = 0.0f;
+                for (int k = 0; k < sub; k++) {
+                    float a = ax, b = ay, c = az, z = 1.0f - a - b;
+                    float AE = exx * a + eyy * b + 2.0f * exy * c + ezz * z;
+                    float rx = -2.0f * w * c, ry = 2.0f * w * c, rz = w * (a - b);
+                    float e2 = 2.0f * AE;
+                    float sx = 2.0f * (exx * a + exy * c) - e2 * a;
+                    float sy = 2.0f * (exy * c + eyy * b) - e2 * b;
+                    float sz = c * (exx + eyy) + exy * (a + b) - e2 * c;
+                    ax = ax + h1 * (rx + Bc * sx);
+                    ay = ay + h1 * (ry + Bc * sy);
+                    az = az + h1 * (rz + Bc * sz);
+                }
+                float t = 1.0f - o_expf(-6.0f * o->opt2[1] * dt);
+                ax = mixf(ax, third, t);
+                ay = mixf(ay, third, t);
+                az = mixf(az, 0.0f, t);
+                ax = clampf(ax, 0.0f, 1.0f);
+                ay = clampf(ay, 0.0f, 1.0f);
+                az = clampf(az, -0.5f, 0.5f);
+            }
+        }
+        st[0] = p->id; st[1] = 0u; st[2] = o_pack_a(ax, ay, az, h); st[3] = 0u;
+        if ((uint32_t)listed < cap) list[listed] = i;
+        listed++;
+    }
+    if (s->dpool) {   /* the takes' effect on the specks' counters */
+        s->d_top1 = speck_rank < top1 ? top1 - speck_rank : 0u;
+        s->d_hw1 += speck_rank > top1 ? speck_rank - top1 : 0u;
+    }
+    return listed;
+}
 /* look.comp's state per slot (4 words each, n_slots slots); returns the slots. */
 long osim_look_state(const OSim* s, uint32_t* out, size_t cap) {
     if (!s->plook) return 0;

@@ -181,7 +181,9 @@ long osim_look(OSim* s, const void* optics, float dt, uint32_t* list, uint32_t c
 long osim_look_state(const OSim* s, uint32_t* out, size_t cap);
 /* spray.comp over the pool the oracle keeps (smooth: osim_render's smoothed layers). */
 long osim_spray(OSim* s, const uint16_t* smooth, const void* optics, float dt, float amount);
-long osim_spray_state(const OSim* s, void* pool, uint32_t* stack, uint32_t* list, uint32_t* foam, uint32_t state[4]);
+long osim_spray_state(const OSim* s, void* pool, uint32_t* stack, uint32_t* stack1, uint32_t* list, uint32_t* counts,
+                      uint32_t state[8]);
+void osim_set_dust(OSim* s, int has_dust);
 /* FluidSim::recorded_iters: the recorded iteration counts (first solve, second, viscosity). */
 void osim_recorded_iters(const OSim* s, uint32_t out[3]);
 long osim_flow_map(const OSim* s, const uint16_t* smooth, uint16_t* flow, float dt, float now, uint32_t src);

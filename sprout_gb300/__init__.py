@@ -64,6 +64,7 @@ RENDER_LAYERS = 20
 DIFFUSE_DTYPE = np.dtype([("pos", np.float32, 2), ("vel", np.float32, 2), ("life", np.float32), ("r", np.float32),
                           ("info", np.uint32), ("z", np.float32)])
 DIFFUSE_MAX = 1 << 16
+POOL_MAX = DIFFUSE_MAX + (1 << 17)   # then the specks' part (mod.rs DUST_MAX)
 
 STAGES = ["advance", "sort", "p2g", "grid", "pressure", "project", "viscosity", "project2"]
 
@@ -201,7 +202,7 @@ def lib() -> C.CDLL:
         "sprout_sim_flow_parity": ([V, P(C.c_uint32)], C.c_int),
         "sprout_sim_recorded_iters": ([V, P(C.c_uint32)], C.c_int),
         "sprout_sim_download_look": ([V, V, C.c_size_t, V, C.c_size_t, P(C.c_uint32), P(C.c_uint32)], C.c_int),
-        "sprout_sim_download_spray": ([V, V, C.c_size_t, V, V, C.c_size_t, V, C.c_size_t, P(C.c_uint32)], C.c_int),
+        "sprout_sim_download_spray": ([V, V, C.c_size_t, V, V, V, C.c_size_t, V, C.c_size_t, P(C.c_uint32)], C.c_int),
         "sprout_params_get_color": ([V, C.c_uint32, C.c_char_p, P(C.c_float), P(C.c_int)], C.c_int),
         "sprout_params_get_row": ([V, C.c_uint32, P(C.c_int32), P(C.c_int32)], C.c_int),
         "sprout_sim_download_render": ([V, C.c_int, V, C.c_size_t, P(C.c_size_t)], C.c_int),
@@ -492,18 +493,16 @@ class FluidSim:
         return [int(x) for x in v]
 
     def download_spray(self):
-        """spray.comp's pool: (entries (65536, DIFFUSE_DTYPE), free stack, listed entries,
-        foam per cell (2, h, w), (never handed out, stack height, listed, next parity))."""
-        st = (C.c_uint32 * 4)()
-        _check(lib().sprout_sim_download_spray(self._h, None, 0, None, None, 0, None, 0, st))
-        pool = np.zeros(DIFFUSE_MAX, DIFFUSE_DTYPE)
-        stack = np.zeros(DIFFUSE_MAX, np.uint32)
-        lst = np.zeros(DIFFUSE_MAX, np.uint32)
-        foam = np.zeros(2 * self.w * self.h, np.uint32)
-        _check(lib().sprout_sim_download_spray(self._h, pool.ctypes.data, DIFFUSE_MAX, stack.ctypes.data, lst.ctypes.data,
-                                               DIFFUSE_MAX, foam.ctypes.data, foam.size, st))
+        """spray.comp's pool: (entries (196608, DIFFUSE_DTYPE), bubbles' free stack, specks'
+        free stack, listed entries, counts (4, h, w): foam x 2, resting specks x 2, state (8))."""
+        st = (C.c_uint32 * 8)()
+        pool = np.zeros(POOL_MAX, DIFFUSE_DTYPE)
+        stack, stack1, lst = (np.zeros(POOL_MAX, np.uint32) for _ in range(3))
+        counts = np.zeros(4 * self.w * self.h, np.uint32)
+        _check(lib().sprout_sim_download_spray(self._h, pool.ctypes.data, POOL_MAX, stack.ctypes.data, stack1.ctypes.data,
+                                               lst.ctypes.data, POOL_MAX, counts.ctypes.data, counts.size, st))
         s = [int(x) for x in st]
-        return pool, stack[: s[1]], lst[: s[2]], foam.reshape(2, self.h, self.w), s
+        return pool, stack[: s[1]], stack1[: s[5]], lst[: s[2]], counts.reshape(4, self.h, self.w), s
 
     def download_look(self):
         """look.comp's state: (per slot (id, 0, packed A, 0) as uint32 (n, 4), the listed slots)."""

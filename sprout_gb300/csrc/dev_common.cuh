@@ -226,6 +226,20 @@ DEV float2 magnet_field(const DevParams* P, float x, float y) {
     return make_float2(bx, by);
 }
 
+// look.comp look_of: the platelets' sheen weight and the specks drawn per cell of material
+// `row` at concentration s, a concentrate's blended with its diluent's
+DEV float2 look_of(const DevOptics* opt, uint32_t row, float s) {
+    const DevOptics& o = opt[row];
+    float lx = o.opt[1], ly = o.fx2[2];
+    if (o.idx[0] >= 0) {
+        const DevOptics& dl = opt[o.idx[0]];
+        const float t = clampf(s, 0.0f, 1.0f);
+        lx = mixf(dl.opt[1], lx, t);
+        ly = mixf(dl.fx2[2], ly, t);
+    }
+    return make_float2(lx, ly);
+}
+
 // sin and cos of a float angle, each rounded once from FP64 (GLSL leaves their precision to the
 // implementation): the angle reduced by the nearest multiple q of pi/2 (Cody and Waite, pi/2
 // in two parts of 33 and 53 bits), the Taylor series to r^15 and r^16 on [-pi/4, pi/4], then

@@ -138,9 +138,11 @@ struct DevOptics;
 struct RenderClock;
 // spike_gap, spike_mc: the ferrofluid spikes' spacing (cells; 0: none) and Rosensweig
 // threshold mu0 Mc (T), FluidSim::spike_params.
+// dfield, dust: spray.comp's dust field (4 ints a cell: the specks' absorption and scattering
+// x 1024) and whether it is read (a speck liquid in a tank whose pool has run).
 void launch_cell_optics(const DevScene& d, const DevOptics* opt, float inv_speed, float spike_gap, float spike_mc,
-                        int sss_iters, ushort4* raw, ushort4* smooth, ushort4* flow, const RenderClock* clock,
-                        ushort4* glow_a, ushort4* glow_b, cudaStream_t st);
+                        const int* dfield, float dust, int sss_iters, ushort4* raw, ushort4* smooth, ushort4* flow,
+                        const RenderClock* clock, ushort4* glow_a, ushort4* glow_b, cudaStream_t st);
 // The clock of a render call (record_cell_optics, mod.rs:1628-1641, 1674-1680): `valid` 0 for
 // the first call on a new tank (no step: the flow map does not run), `changed` 0 when the call
 // records nothing (its key is the last call's); the time since the last call from the
@@ -158,7 +160,9 @@ void launch_look(const DevScene& d, const DevOptics* opt, const RenderClock* clo
 // spray.comp's pool (spray.cu): an entry (the reference's Diffuse, 32 bytes), the pool's
 // counters (entries never handed out so far, the free stack's height, the live entries listed,
 // this frame's emissions), and its buffers.
-constexpr uint32_t kDiffuseMax = 1u << 16;   // mod.rs DIFFUSE_MAX
+constexpr uint32_t kDiffuseMax = 1u << 16;   // mod.rs DIFFUSE_MAX: bubbles, foam and spray
+constexpr uint32_t kDustMax = 1u << 17;      // mod.rs DUST_MAX: the specks' part, after them
+constexpr uint32_t kPoolMax = kDiffuseMax + kDustMax;
 struct DevDiffuse {
     float px, py, vx, vy, life, r;
     uint32_t info;
@@ -166,17 +170,27 @@ struct DevDiffuse {
 };
 static_assert(sizeof(DevDiffuse) == 32, "Diffuse is 32 bytes");
 struct PoolState {
-    uint32_t hw, top, listed, total;
+    uint32_t hw, top, listed, total;   // bubbles' part (listed: both parts)
+    uint32_t hw1, top1, total1, pad;   // the specks' part
 };
 struct SprayBufs {
-    DevDiffuse* pool;
-    uint32_t *stack, *list, *dcount, *counts, *bsum, *flags;
+    DevDiffuse* pool;                     // kPoolMax entries
+    uint32_t *stack, *stack1, *list;      // free stacks of the two parts, the live entries
+    uint32_t *dcount;                     // foam per cell (copies 0, 1), resting specks (2, 3)
+    uint32_t *counts, *bsum, *flags;      // stage 0's ranks, scan partials, stage 1's flags
+    uint32_t* nspeck;                     // per particle slot + 1: the specks it brings in, ranked
+    int* dfield;                          // the dust field, 4 ints a cell
     PoolState* ps;
 };
+// look.comp's specks (lines 103-128): a new particle of a liquid with specks brings its share
+// of them into the pool's second part, ranked in slot order (the engine's slot order is the
+// oracle's); runs before launch_look, which marks the particles seen.
+void launch_specks(const DevScene& d, const DevOptics* opt, const SprayBufs& b, uint32_t frame, uint32_t n_slots,
+                   cudaStream_t st);
 // record_spray: stage 0 (when `makes`, and the clock's dt > 0) and stage 1 of spray.comp, the
 // foam counted into copy `parity` of dcount. `amount`: params.bubbles.
-void launch_spray(const DevScene& d, const ushort4* smooth, const SprayBufs& b, const RenderClock* clock, uint32_t frame,
-                  uint32_t parity, float amount, bool makes, cudaStream_t st);
+void launch_spray(const DevScene& d, const ushort4* smooth, const DevOptics* opt, const SprayBufs& b,
+                  const RenderClock* clock, uint32_t frame, uint32_t parity, float amount, bool makes, cudaStream_t st);
 // Scene::rasterize on the device (raster.cu): the tank's solid fields straight into device
 // buffers, bit-identical to the host's Scene::rasterize (scene.cpp).
 struct Scene;

@@ -11,8 +11,7 @@
 // from the last call), flow_map.comp (how far the liquid has moved since its patterns
 // restarted, four layers) and glow.comp (the emission blurred at half resolution).
 //
-// Not computed here: the dust field of spray.comp (layer 18, zero: the specks are not carried)
-// and the film map's tile flags (no film map).
+// Not computed here: the film map's tile flags (no film map).
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
@@ -147,7 +146,7 @@ DEV float2 spike_phase(const DevParams* P, float gap, float x, float y) {
 }
 
 __global__ void __launch_bounds__(256) k_cell_optics(DevScene d, const DevOptics* opt, float inv_speed, float spike_gap,
-                                                    float spike_mc, ushort4* raw) {
+                                                    float spike_mc, const int* dfield, float dust, ushort4* raw) {
     const int cx = blockIdx.x * 16 + threadIdx.x, cy = blockIdx.y * 16 + threadIdx.y;
     if (cx >= d.W || cy >= d.H) return;
     const DevParams* P = d.P;
@@ -356,6 +355,15 @@ __global__ void __launch_bounds__(256) k_cell_optics(DevScene d, const DevOptics
         o[3] = mul(f4(em.x + lum.x, em.y + lum.y, em.z + lum.z, speed), occ);
         const float s_mean = aq.w + ot.w + dense.w;
         o[16] = f4(fx2.x * occ, fx2.y * occ, s_mean > 1e-5f ? fx2.z / s_mean : 1.0f, s_mean > 1e-5f ? fx2.w / s_mean : 1.0f);
+        // the specks' share of the colour (spray.comp's dust field, laid down last frame), per
+        // cell of the tank: over the occupancy per unit of liquid, premultiplied by it again
+        if (dust > 0.0f && occ > 0.02f) {
+            const float f = 1.0f / 1024.0f;   // DUST_FIX
+            o[18] = f4((float)dfield[4 * i] * f, (float)dfield[4 * i + 1] * f, (float)dfield[4 * i + 2] * f,
+                       (float)dfield[4 * i + 3] * f);
+            const float cap = 200.0f * occ;
+            o[18] = f4(minf(o[18].x, cap), minf(o[18].y, cap), minf(o[18].z, cap), minf(o[18].w, cap));
+        }
         o[19] = add(mul(o[19], occ), o[18]);
         o[17] = mul(f4(lum.x, lum.y, lum.z, ior_sum), occ);
         o[4] = mul(f4(sty.x, sty.y, waq, waq + wot), occ);
@@ -655,15 +663,8 @@ __global__ void __launch_bounds__(128) k_look(DevScene d, const DevOptics* opt, 
     if (kind == KIND_DEAD || low == 0u || low > 96u) return;   // rows of the optics table
     const uint32_t row = low - 1u;
     const DevOptics& o = opt[row];
-    // look_of: the platelets' sheen weight and the drawn specks, a concentrate's blended with
-    // its diluent's by its concentration
-    float lx = o.opt[1], ly = o.fx2[2];
-    if (o.idx[0] >= 0) {
-        const DevOptics& dl = opt[o.idx[0]];
-        const float t = clampf(q1.x, 0.0f, 1.0f);
-        lx = mixf(dl.opt[1], lx, t);
-        ly = mixf(dl.fx2[2], ly, t);
-    }
+    const float2 lk = look_of(opt, row, q1.x);
+    const float lx = lk.x, ly = lk.y;
     if (maxf(lx, ly) <= 0.0f) return;
     const uint4 st = d.plook[i];
     const bool fresh = st.x != id;
@@ -728,10 +729,10 @@ void launch_render_clock(const DevScene& d, RenderClock* clock, int valid, int c
 }
 
 void launch_cell_optics(const DevScene& d, const DevOptics* opt, float inv_speed, float spike_gap, float spike_mc,
-                        int sss_iters, ushort4* raw, ushort4* smooth, ushort4* flow, const RenderClock* clock,
-                        ushort4* glow_a, ushort4* glow_b, cudaStream_t st) {
+                        const int* dfield, float dust, int sss_iters, ushort4* raw, ushort4* smooth, ushort4* flow,
+                        const RenderClock* clock, ushort4* glow_a, ushort4* glow_b, cudaStream_t st) {
     const dim3 tiles((d.W + 15) / 16, (d.H + 15) / 16), block(16, 16);
-    k_cell_optics<<<tiles, block, 0, st>>>(d, opt, inv_speed, spike_gap, spike_mc, raw);
+    k_cell_optics<<<tiles, block, 0, st>>>(d, opt, inv_speed, spike_gap, spike_mc, dfield, dust, raw);
     k_light<<<d.W, 64, 0, st>>>(d, raw);
     k_optics_blur<<<tiles, block, 0, st>>>(d, raw, smooth);
     // sss.comp (mod.rs:1666-1675): prepared, then an even number of iterations, ending in layer 20

@@ -1035,8 +1035,16 @@ struct SproutSim {
             render_key_set = true;
             float gap = 0.0f, mc = 0.0f;
             spike_params(&gap, &mc);
-            launch_cell_optics(d, d_optics, inv_speed, gap, mc, (int)params.sss_iters, d_raw, d_smooth, d_flow, d_clock,
-                               d_glow, d_glow + glow_texels(), stream);
+            bool makes = false, has_dust = false;
+            for (int r : tank.rows) {
+                makes |= params.bubbles > 0.0f && (params.mat[r].foam > 0.0f || params.mat[r].fizz > 0.0f);
+                has_dust |= params.mat[r].dust > 0.0f;
+            }
+            // the dust field of the last frame's pool, once the pool has run (mod.rs:1653)
+            const float dust = (diffuse_seen && has_dust && spray.dfield) ? 1.0f : 0.0f;
+            launch_cell_optics(d, d_optics, inv_speed, gap, mc, spray.dfield, dust, (int)params.sss_iters, d_raw, d_smooth,
+                               d_flow, d_clock, d_glow, d_glow + glow_texels(), stream);
+            if ((makes || has_dust) && !spray.pool && (rc = alloc_spray()) != SPROUT_OK) return rc;
             if (look_live() && n_slots > 0) {   // record_look (mod.rs:1717-1729)
                 if (!d.plook) {
                     if ((rc = alloc(&d.plook, (size_t)capacity)) != SPROUT_OK) return rc;
@@ -1045,30 +1053,16 @@ struct SproutSim {
                     CUDA_TRY(cudaMemsetAsync(d.plook, 0, (size_t)capacity * sizeof(uint4), stream));
                     graph_ok = false;   // the sort now carries the look's state: recapture
                 }
+                // a new particle of a liquid with specks brings them into the pool (look.comp)
+                if (spray.pool) launch_specks(d, d_optics, spray, frames, n_slots, stream);
                 launch_look(d, d_optics, d_clock, frames, d_look_list, d_look_list + 1, capacity, n_slots, stream);
             }
-            // record_spray (mod.rs:1739-1773): once a liquid that foams or fizzes has been in the
-            // tank, the pool is moved every frame; new entries are made while one is
-            bool makes = false;
-            if (params.bubbles > 0.0f)
-                for (int r : tank.rows) makes |= params.mat[r].foam > 0.0f || params.mat[r].fizz > 0.0f;
-            diffuse_seen |= makes;
+            // record_spray (mod.rs:1739-1773): once a liquid that foams, fizzes or carries specks
+            // has been in the tank, the pool is moved every frame; new entries are made while one
+            // that foams or fizzes is
+            diffuse_seen |= makes || has_dust;
             if (diffuse_seen) {
-                if (!spray.pool) {
-                    const size_t nc = (size_t)W * H;
-                    if ((rc = alloc(&spray.pool, (size_t)kDiffuseMax)) != SPROUT_OK) return rc;
-                    if ((rc = alloc(&spray.stack, (size_t)kDiffuseMax)) != SPROUT_OK) return rc;
-                    if ((rc = alloc(&spray.list, (size_t)kDiffuseMax)) != SPROUT_OK) return rc;
-                    if ((rc = alloc(&spray.flags, (size_t)kDiffuseMax)) != SPROUT_OK) return rc;
-                    if ((rc = alloc(&spray.dcount, 2 * nc)) != SPROUT_OK) return rc;
-                    if ((rc = alloc(&spray.counts, nc)) != SPROUT_OK) return rc;
-                    if ((rc = alloc(&spray.bsum, nc / 1024 + 2)) != SPROUT_OK) return rc;
-                    if ((rc = alloc(&spray.ps, 1)) != SPROUT_OK) return rc;
-                    CUDA_TRY(cudaMemsetAsync(spray.pool, 0, (size_t)kDiffuseMax * sizeof(DevDiffuse), stream));
-                    CUDA_TRY(cudaMemsetAsync(spray.dcount, 0, 2 * nc * sizeof(uint32_t), stream));
-                    CUDA_TRY(cudaMemsetAsync(spray.ps, 0, sizeof(PoolState), stream));
-                }
-                launch_spray(d, d_smooth, spray, d_clock, frames, diffuse_parity, params.bubbles, makes, stream);
+                launch_spray(d, d_smooth, d_optics, spray, d_clock, frames, diffuse_parity, params.bubbles, makes, stream);
                 diffuse_parity ^= 1u;
             }
         }
@@ -1094,11 +1088,31 @@ struct SproutSim {
     }
     // spray.comp's pool (spray.cu): made, moved and listed by render calls
     SprayBufs spray{};
+    int alloc_spray() {
+        const size_t nc = (size_t)W * H;
+        int rc;
+        if ((rc = alloc(&spray.pool, (size_t)kPoolMax)) != SPROUT_OK) return rc;
+        if ((rc = alloc(&spray.stack, (size_t)kDiffuseMax)) != SPROUT_OK) return rc;
+        if ((rc = alloc(&spray.stack1, (size_t)kDustMax)) != SPROUT_OK) return rc;
+        if ((rc = alloc(&spray.list, (size_t)kPoolMax)) != SPROUT_OK) return rc;
+        if ((rc = alloc(&spray.flags, (size_t)kPoolMax)) != SPROUT_OK) return rc;
+        if ((rc = alloc(&spray.dcount, 4 * nc)) != SPROUT_OK) return rc;
+        if ((rc = alloc(&spray.counts, nc)) != SPROUT_OK) return rc;
+        if ((rc = alloc(&spray.nspeck, (size_t)capacity + 1)) != SPROUT_OK) return rc;
+        if ((rc = alloc(&spray.bsum, std::max(nc, (size_t)capacity + 1) / 1024 + 2)) != SPROUT_OK) return rc;
+        if ((rc = alloc(&spray.dfield, 4 * nc)) != SPROUT_OK) return rc;
+        if ((rc = alloc(&spray.ps, 1)) != SPROUT_OK) return rc;
+        CUDA_TRY(cudaMemsetAsync(spray.pool, 0, (size_t)kPoolMax * sizeof(DevDiffuse), stream));
+        CUDA_TRY(cudaMemsetAsync(spray.dcount, 0, 4 * nc * sizeof(uint32_t), stream));
+        CUDA_TRY(cudaMemsetAsync(spray.dfield, 0, 4 * nc * sizeof(int), stream));
+        CUDA_TRY(cudaMemsetAsync(spray.ps, 0, sizeof(PoolState), stream));
+        return SPROUT_OK;
+    }
     bool diffuse_seen = false;
     uint32_t diffuse_parity = 0;
-    int download_spray(SproutDiffuse* pool, size_t pool_cap, uint32_t* stack, uint32_t* list, size_t cap,
-                       uint32_t* foam, size_t foam_cap, uint32_t state[4]) {
-        for (int k = 0; k < 4; k++) state[k] = 0;
+    int download_spray(SproutDiffuse* pool, size_t pool_cap, uint32_t* stack, uint32_t* stack1, uint32_t* list, size_t cap,
+                       uint32_t* foam, size_t foam_cap, uint32_t state[8]) {
+        for (int k = 0; k < 8; k++) state[k] = 0;
         if (!spray.pool) return SPROUT_OK;
         CUDA_TRY(cudaStreamSynchronize(stream));
         PoolState ps;
@@ -1107,19 +1121,22 @@ struct SproutSim {
         state[1] = ps.top;
         state[2] = ps.listed;
         state[3] = diffuse_parity;
+        state[4] = ps.hw1;
+        state[5] = ps.top1;
         const size_t nc = (size_t)W * H;
         if (pool) {
-            if (pool_cap < kDiffuseMax) return fail(SPROUT_E_ARG, "download_spray: the pool holds 65536 entries");
-            CUDA_TRY(cudaMemcpy(pool, spray.pool, (size_t)kDiffuseMax * sizeof(DevDiffuse), cudaMemcpyDeviceToHost));
+            if (pool_cap < kPoolMax) return fail(SPROUT_E_ARG, "download_spray: the pool holds 196608 entries");
+            CUDA_TRY(cudaMemcpy(pool, spray.pool, (size_t)kPoolMax * sizeof(DevDiffuse), cudaMemcpyDeviceToHost));
         }
-        if (stack || list) {
-            if (cap < kDiffuseMax) return fail(SPROUT_E_ARG, "download_spray: the stack and list hold 65536 entries");
+        if (stack || stack1 || list) {
+            if (cap < kPoolMax) return fail(SPROUT_E_ARG, "download_spray: the stacks and list hold 196608 entries");
             if (stack) CUDA_TRY(cudaMemcpy(stack, spray.stack, (size_t)ps.top * 4, cudaMemcpyDeviceToHost));
+            if (stack1) CUDA_TRY(cudaMemcpy(stack1, spray.stack1, (size_t)ps.top1 * 4, cudaMemcpyDeviceToHost));
             if (list) CUDA_TRY(cudaMemcpy(list, spray.list, (size_t)ps.listed * 4, cudaMemcpyDeviceToHost));
         }
         if (foam) {
-            if (foam_cap < 2 * nc) return fail(SPROUT_E_ARG, "download_spray: the foam counts hold 2 x W x H");
-            CUDA_TRY(cudaMemcpy(foam, spray.dcount, 2 * nc * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+            if (foam_cap < 4 * nc) return fail(SPROUT_E_ARG, "download_spray: the counts hold 4 x W x H");
+            CUDA_TRY(cudaMemcpy(foam, spray.dcount, 4 * nc * sizeof(uint32_t), cudaMemcpyDeviceToHost));
         }
         return SPROUT_OK;
     }
@@ -2378,10 +2395,10 @@ int sprout_sim_download_render(SproutSim* sim, int which, uint16_t* out, size_t 
     return SPROUT_OK;
 }
 
-int sprout_sim_download_spray(SproutSim* sim, SproutDiffuse* pool, size_t pool_cap, uint32_t* stack, uint32_t* list,
-                              size_t cap, uint32_t* foam, size_t foam_cap, uint32_t state[4]) {
+int sprout_sim_download_spray(SproutSim* sim, SproutDiffuse* pool, size_t pool_cap, uint32_t* stack, uint32_t* stack1,
+                              uint32_t* list, size_t cap, uint32_t* counts, size_t counts_cap, uint32_t state[8]) {
     if (!sim || !state) return fail(SPROUT_E_ARG, "null argument");
-    return sim->download_spray(pool, pool_cap, stack, list, cap, foam, foam_cap, state);
+    return sim->download_spray(pool, pool_cap, stack, stack1, list, cap, counts, counts_cap, state);
 }
 
 int sprout_sim_download_look(SproutSim* sim, uint32_t* state, size_t state_cap, uint32_t* list, size_t list_cap,

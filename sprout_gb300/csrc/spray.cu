@@ -47,15 +47,52 @@ DEV float4 half4(ushort4 h) {
                        __half2float(__ushort_as_half(h.z)), __half2float(__ushort_as_half(h.w)));
 }
 
+// A speck's flake normal in hemi-octahedral form, 10 + 10 bits (look.comp pack_n, spray.comp
+// unpack_n): a disc's normal and its opposite are one orientation.
+DEV uint32_t quant10(float v, uint32_t h) {
+    const float m = 1023.0f;
+    return (uint32_t)clampf(floorf(clampf(v, 0.0f, 1.0f) * m + rnd24(h)), 0.0f, m);
+}
+DEV uint32_t pack_n(float nx, float ny, float nz, uint32_t h) {
+    if (nz < 0.0f) {
+        nx = -nx;
+        ny = -ny;
+        nz = -nz;
+    }
+    const float den = maxf(fabsf(nx) + fabsf(ny) + nz, 1e-6f);
+    const float px = nx / den, py = ny / den;
+    const float qx = (px + py) * 0.5f + 0.5f, qy = (px - py) * 0.5f + 0.5f;
+    return quant10(qx, hash32(h)) | (quant10(qy, hash32(h ^ 0x68e31da4u)) << 10);
+}
+DEV void normalize3(float& x, float& y, float& z) {
+    const float l = sqrtf(x * x + y * y + z * z);
+    x = x / l;
+    y = y / l;
+    z = z / l;
+}
+DEV void unpack_n(uint32_t b, float& x, float& y, float& z) {
+    const float qx = (float)(b & 1023u) / 1023.0f * 2.0f - 1.0f, qy = (float)((b >> 10) & 1023u) / 1023.0f * 2.0f - 1.0f;
+    x = (qx + qy) * 0.5f;
+    y = (qx - qy) * 0.5f;
+    z = maxf(1.0f - fabsf(x) - fabsf(y), 0.0f);
+    normalize3(x, y, z);
+}
+DEV float signf(float x) { return x > 0.0f ? 1.0f : (x < 0.0f ? -1.0f : 0.0f); }
+constexpr float DUST_IN = 0.30f, DUST_DRY_LIFE = 30.0f, SHIELDS = 0.05f, BED_U = 8.0f, DUST_FIX = 1024.0f;
+
 struct Spray {
     DevScene d;
     const ushort4* sm;     // the smoothed layers (optics_blur.comp)
+    const DevOptics* opt;
     DevDiffuse* pool;
     uint32_t* stack;       // the free stack
+    uint32_t* stack1;      // the specks' free stack
     uint32_t* list;        // the live entries for the sprites
     uint32_t* dcount;      // foam per cell, two copies
     uint32_t* counts;      // stage 0: emissions per cell, then their first rank
     uint32_t* flags;       // stage 1: per entry, bit 0 freed, bit 1 listed
+    int* dfield;
+    uint32_t* nspeck;      // look.comp's specks: per particle slot, ranked
     PoolState* ps;
     const RenderClock* clk;
     uint32_t frame, parity;
@@ -88,8 +125,9 @@ struct Spray {
         const long long k = (long long)y * W + x;
         return (k >= 0 && k < (long long)W * H) ? d.vel[k] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     }
-    DEV float2 sample_vel_at(float x, float y) const {
-        float2 o = make_float2(0.0f, 0.0f);
+    DEV float2 sample_vel_at(float x, float y) const { return sample_vel_fb(x, y, make_float2(0.0f, 0.0f)); }
+    DEV float2 sample_vel_fb(float x, float y, float2 fb) const {
+        float2 o = fb;
         for (int comp = 0; comp < 2; comp++) {
             const float gx = comp == 0 ? x : x - 0.5f, gy = comp == 0 ? y - 0.5f : y;
             const int bx = (int)floorf(gx), by = (int)floorf(gy);
@@ -234,11 +272,155 @@ struct Spray {
         return e;
     }
 
+    // move_dust(): a speck, suspended (BUBBLE: settling at its terminal velocity, lagging the
+    // flow by its response time, a flake turned by the flow's gradient), resting (FOAM: held by
+    // a solid or the packed specks below it, until the flow over it passes the Shields
+    // threshold; a flake lies flat; left dry, gone after DUST_DRY_LIFE s) or falling (SPRAY);
+    // resting ones counted per cell, and its share of the liquid's colour into the dust field
+    DEV uint32_t move_dust(uint32_t i, DevDiffuse e) const {
+        uint32_t st = e.info & 3u;
+        const DevParams* P = d.P;
+        const uint32_t copy_in = 1u - parity, copy_out = parity;
+        const int row = (int)((e.info >> 8) & 127u) - 1;
+        if (row < 0) {
+            pool[i].info = 0u;
+            return 1u;
+        }
+        const DevOptics& o = opt[row];
+        const float rho_p = o.dust2[1] / 998.0f;
+        const float aspect = o.dust2[2];
+        const float rr = e.r;
+        const float d_eq = 2.0f * rr * (aspect < 0.6667f ? sp_powf(1.5f * maxf(aspect, 0.005f), 1.0f / 3.0f) : 1.0f);
+        const float pack = maxf(o.dcol[3], 1.0f);
+        const float Bc = (aspect * aspect - 1.0f) / (aspect * aspect + 1.0f);
+        float nx, ny, nz;
+        unpack_n(__float_as_uint(e.life), nx, ny, nz);
+        const uint32_t h0 = hash32(e.info ^ hash32(frame * 0x9e3779b1u + i));
+        const float dt = clk->dt;
+        const float sf = ceilf(dt * 120.0f);
+        const int steps = sf >= 8.0f ? 8 : (sf >= 1.0f ? (int)sf : 1);
+        const float h = dt / (float)steps;
+        const Grid g{d.vel, d.sdf, W, H};
+        for (int k = 0; k < steps && st != FREE; k++) {
+            const int cx = min(max((int)e.px, 0), W - 1), cy = min(max((int)e.py, 0), H - 1), ci = cy * W + cx;
+            const float occ = occ_at(e.px, e.py);
+            const float4 cf = d.cell[ci];
+            const float rho = maxf(cf.y, 0.3f), nu = maxf(cf.z / rho, 1e-6f);
+            const float drho = rho_p - rho;
+            const float down = drho >= 0.0f ? 1.0f : -1.0f;
+            const float ux_ = e.px - 0.0f, uy_ = e.py - down * (rr + 0.35f);
+            float gux, guy;
+            const float sd_u = sample_sdf(g, ux_, uy_, &gux, &guy);
+            const int cux = min(max((int)ux_, 0), W - 1), cuy = min(max((int)uy_, 0), H - 1);
+            const float packed = (float)dcount[(size_t)(2u + copy_in) * nc() + (size_t)cuy * W + cux];
+            const bool held = sd_u < 0.0f || ((cux != cx || cuy != cy) && packed >= pack) || uy_ < 0.0f;
+            const bool wet = occ > DUST_IN;
+            const float2 uf = sample_vel_at(e.px, e.py);
+            const float u_crit = BED_U * sqrtf(SHIELDS * fabsf(drho) * P->gravity * d_eq / rho);
+            if (st == FOAM) {
+                if (!held) st = wet ? BUBBLE : SPRAY;
+                else if (wet && len2(uf.x, uf.y) > u_crit) {
+                    st = BUBBLE;
+                    e.vx = uf.x;
+                    e.vy = uf.y;
+                } else {   // at rest: a flake lies flat on what holds it
+                    float bx = 0.0f, by = 1.0f, bz = 0.0f;
+                    if (sd_u < 0.0f) {
+                        bx = gux + 0.0f;
+                        by = guy + 1e-4f;
+                        const float l = sqrtf(bx * bx + by * by);
+                        bx = bx / l;
+                        by = by / l;
+                    }
+                    const float sg = signf(nx * bx + ny * by + nz * bz + 1e-4f);
+                    const float t = 1.0f - sp_expf(-h / 0.3f);
+                    nx = mixf(nx, bx * sg, t);
+                    ny = mixf(ny, by * sg, t);
+                    nz = mixf(nz, bz * sg, t);
+                    normalize3(nx, ny, nz);
+                    e.vx = wet ? 0.0f : e.vx + h;
+                    e.vy = 0.0f;
+                    if (e.vx > DUST_DRY_LIFE) st = FREE;
+                    continue;
+                }
+            }
+            if (st == SPRAY && wet) st = BUBBLE;
+            if (st == BUBBLE && !wet) st = SPRAY;
+            if (st == BUBBLE) {
+                const float vt = terminal(drho, rho, nu, d_eq, P->gravity);
+                const float tx = uf.x - 0.0f, ty = uf.y - down * vt;
+                const float tau = clampf(rho_p * d_eq * d_eq / (18.0f * rho * nu), 0.004f, 0.5f);
+                const float t = 1.0f - sp_expf(-h / tau);
+                e.vx = mixf(e.vx, tx, t);
+                e.vy = mixf(e.vy, ty, t);
+                if (aspect < 0.6667f) {   // a flake turns with the flow (Jeffery)
+                    const float2 ux1 = sample_vel_fb(e.px + 0.5f, e.py + 0.0f, uf), ux0 = sample_vel_fb(e.px - 0.5f, e.py - 0.0f, uf);
+                    const float2 uy1 = sample_vel_fb(e.px + 0.0f, e.py + 0.5f, uf), uy0 = sample_vel_fb(e.px - 0.0f, e.py - 0.5f, uf);
+                    const float gxx = ux1.x - ux0.x, gxy = ux1.y - ux0.y, gyx = uy1.x - uy0.x, gyy = uy1.y - uy0.y;
+                    const float w = 0.5f * (gxy - gyx);
+                    const float dv = 0.5f * (gxx + gyy);
+                    const float exx = gxx - dv, eyy = gyy - dv, exy = 0.5f * (gyx + gxy);
+                    const float wnx = -w * ny, wny = w * nx, wnz = 0.0f;
+                    const float enx = exx * nx + exy * ny, eny = exy * nx + eyy * ny, enz = 0.0f;
+                    const float ne = nx * enx + ny * eny + nz * enz;
+                    nx = nx + h * (wnx + Bc * (enx - ne * nx));
+                    ny = ny + h * (wny + Bc * (eny - ne * ny));
+                    nz = nz + h * (wnz + Bc * (enz - ne * nz));
+                    normalize3(nx, ny, nz);
+                }
+                if (held && (e.vx - uf.x) * 0.0f + (e.vy - uf.y) * -down >= 0.0f && len2(uf.x, uf.y) < u_crit) {
+                    st = FOAM;
+                    e.vx = 0.0f;
+                    e.vy = 0.0f;
+                }
+            } else if (st == SPRAY) {
+                e.vx += 0.0f - e.vx * SPRAY_DRAG * h;
+                e.vy += -P->gravity * h - e.vy * SPRAY_DRAG * h;
+            }
+            e.px += e.vx * h;
+            e.py += e.vy * h;
+            float gsx, gsy;
+            const float sd = sample_sdf(g, e.px, e.py, &gsx, &gsy);
+            const float rim = rr + 0.05f;
+            if (sd < rim) {   // kept out of the solids; landing on one, it rests there
+                const float gl = maxf(len2(gsx, gsy), 1e-6f);
+                const float nrx = gsx / gl, nry = gsy / gl;
+                e.px += nrx * (rim - sd);
+                e.py += nry * (rim - sd);
+                const float vn = minf(e.vx * nrx + e.vy * nry, 0.0f);
+                e.vx -= nrx * vn;
+                e.vy -= nry * vn;
+                if (st == SPRAY) {
+                    st = FOAM;
+                    e.vx = 0.0f;
+                    e.vy = 0.0f;
+                }
+            }
+            if (e.px < 0.0f || e.py < -1.0f || e.px >= (float)W || e.py >= (float)H) st = FREE;
+        }
+        e.life = __uint_as_float(pack_n(nx, ny, nz, h0));
+        e.info = (e.info & ~3u) | st;
+        pool[i] = e;
+        if (st == FREE) return 1u;
+        const int cx = min(max((int)e.px, 0), W - 1), cy = min(max((int)e.py, 0), H - 1), ci = cy * W + cx;
+        if (st == FOAM) atomicAdd(&dcount[(size_t)(2u + copy_out) * nc() + ci], 1u);
+        if (o.dust[3] > 0.0f && occ_cell(cx, cy) > 0.05f) {   // its share of the liquid's colour
+            const int qx = (int)(o.dust[0] * DUST_FIX + 0.5f), qy = (int)(o.dust[1] * DUST_FIX + 0.5f);
+            const int qz = (int)(o.dust[2] * DUST_FIX + 0.5f), qw = (int)(o.dust[3] * DUST_FIX + 0.5f);
+            if (qx > 0) atomicAdd(&dfield[4 * ci], qx);
+            if (qy > 0) atomicAdd(&dfield[4 * ci + 1], qy);
+            if (qz > 0) atomicAdd(&dfield[4 * ci + 2], qz);
+            atomicAdd(&dfield[4 * ci + 3], qw);
+        }
+        return 2u;
+    }
+
     // move(): entry i for the frame's dt in up to 8 steps
     DEV uint32_t move(uint32_t i) const {
         DevDiffuse e = pool[i];
         uint32_t st = e.info & 3u;
-        if (st == FREE || (e.info & DUST) != 0u) return 0u;
+        if (st == FREE) return 0u;
+        if ((e.info & DUST) != 0u) return move_dust(i, e);
         const DevParams* P = d.P;
         const uint32_t copy_in = 1u - parity, copy_out = parity;
         const float cs = P->misc[2], dt = clk->dt;
@@ -380,7 +562,7 @@ __global__ void __launch_bounds__(kScan) k_spray_scan1(uint32_t* counts, uint32_
     if (i < n) counts[i] = t[threadIdx.x] - v;
     if (threadIdx.x == kScan - 1) bsum[blockIdx.x] = t[threadIdx.x];
 }
-__global__ void __launch_bounds__(kScan) k_spray_scan2(uint32_t* bsum, int nb, PoolState* ps) {
+__global__ void __launch_bounds__(kScan) k_spray_scan2(uint32_t* bsum, int nb, uint32_t* total) {
     __shared__ uint32_t t[kScan];
     uint32_t carry = 0u;
     for (int b0 = 0; b0 < nb; b0 += kScan) {
@@ -399,7 +581,7 @@ __global__ void __launch_bounds__(kScan) k_spray_scan2(uint32_t* bsum, int nb, P
         __syncthreads();
         carry += tot;
     }
-    if (threadIdx.x == 0) ps->total = carry;
+    if (threadIdx.x == 0) *total = carry;
 }
 __global__ void __launch_bounds__(kScan) k_spray_scan3(uint32_t* counts, const uint32_t* bsum, int n) {
     const int i = blockIdx.x * kScan + threadIdx.x;
@@ -432,66 +614,160 @@ __global__ void k_spray_taken(PoolState* ps, const RenderClock* clk) {
 
 __global__ void __launch_bounds__(256) k_spray_move(Spray s) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= kDiffuseMax) return;
+    if (i >= kPoolMax) return;
     s.flags[i] = s.move(i);
 }
 
-// freed entries onto the stack and live ones into the list, both in entry order
+// freed entries onto their part's stack and live ones into the list, all in entry order
 __global__ void __launch_bounds__(kScan) k_spray_returns(Spray s) {
-    __shared__ uint32_t tf[kScan], tl[kScan];
-    constexpr uint32_t per = kDiffuseMax / kScan;
+    __shared__ uint32_t tf[kScan], tg[kScan], tl[kScan];
+    constexpr uint32_t per = kPoolMax / kScan;
+    static_assert(kPoolMax % kScan == 0, "whole chunks");
     const uint32_t b = threadIdx.x * per;
-    uint32_t nf = 0u, nl = 0u;
+    uint32_t nf = 0u, ng = 0u, nl = 0u;
     for (uint32_t j = 0; j < per; j++) {
         const uint32_t f = s.flags[b + j];
-        nf += f == 1u;
+        if (f == 1u) {
+            if (b + j < kDiffuseMax) nf++;
+            else ng++;
+        }
         nl += f == 2u;
     }
     tf[threadIdx.x] = nf;
+    tg[threadIdx.x] = ng;
     tl[threadIdx.x] = nl;
     __syncthreads();
     for (int o = 1; o < kScan; o <<= 1) {
         const uint32_t a = threadIdx.x >= (unsigned)o ? tf[threadIdx.x - o] : 0u;
-        const uint32_t c = threadIdx.x >= (unsigned)o ? tl[threadIdx.x - o] : 0u;
+        const uint32_t c = threadIdx.x >= (unsigned)o ? tg[threadIdx.x - o] : 0u;
+        const uint32_t e = threadIdx.x >= (unsigned)o ? tl[threadIdx.x - o] : 0u;
         __syncthreads();
         tf[threadIdx.x] += a;
-        tl[threadIdx.x] += c;
+        tg[threadIdx.x] += c;
+        tl[threadIdx.x] += e;
         __syncthreads();
     }
-    const uint32_t top = s.ps->top;
-    uint32_t pf = top + tf[threadIdx.x] - nf, pl = tl[threadIdx.x] - nl;
+    const uint32_t top = s.ps->top, top1 = s.ps->top1;
+    uint32_t pf = top + tf[threadIdx.x] - nf, pg = top1 + tg[threadIdx.x] - ng, pl = tl[threadIdx.x] - nl;
     for (uint32_t j = 0; j < per; j++) {
         const uint32_t f = s.flags[b + j];
-        if (f == 1u) s.stack[pf++] = b + j;
-        else if (f == 2u) s.list[pl++] = b + j;
+        if (f == 1u) {
+            if (b + j < kDiffuseMax) s.stack[pf++] = b + j;
+            else s.stack1[pg++] = b + j;
+        } else if (f == 2u) s.list[pl++] = b + j;
     }
     __syncthreads();
     if (threadIdx.x == kScan - 1) {
         s.ps->top = top + tf[kScan - 1];
+        s.ps->top1 = top1 + tg[kScan - 1];
         s.ps->listed = tl[kScan - 1];
     }
 }
 
+// look.comp's specks: how many each slot's particle brings in (a new particle of a liquid with
+// specks: floor(drawn specks per cell / particles per cell + a draw), at most 8), before the
+// look pass marks it seen
+__global__ void __launch_bounds__(256) k_speck_count(Spray s, uint32_t n_slots) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i > n_slots) return;
+    uint32_t n = 0u;
+    if (i < n_slots) {
+        const float4 q1 = s.d.part[3 * i + 2];
+        const uint32_t kind = __float_as_uint(q1.y), id = __float_as_uint(q1.z), low = kind & 255u;
+        if (kind != KIND_DEAD && low != 0u && low <= 96u) {
+            const float2 lk = look_of(s.opt, low - 1u, q1.x);
+            if (maxf(lk.x, lk.y) > 0.0f && s.d.plook[i].x != id && lk.y > 0.0f) {
+                const uint32_t h = hash32(id * 0x9e3779b1u ^ hash32(s.frame * 0x85ebca6bu + 0x165667b1u));
+                const float e = lk.y * s.d.P->inv_ppc;
+                const float fn = floorf(e + rnd24(hash32(h ^ 0x2545f491u)));
+                n = fn >= 8.0f ? 8u : (fn >= 1.0f ? (uint32_t)fn : 0u);
+            }
+        }
+    }
+    s.nspeck[i] = n;
+}
+// ... and brings them in: speck k of the slot takes what the take of its rank gets
+__global__ void __launch_bounds__(256) k_speck_emit(Spray s, uint32_t n_slots) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_slots) return;
+    const uint32_t r0 = s.nspeck[i], n = s.nspeck[i + 1] - r0;
+    if (n == 0u) return;
+    const float4 q0 = s.d.part[3 * i], q1 = s.d.part[3 * i + 2];
+    const uint32_t id = __float_as_uint(q1.z), row = (__float_as_uint(q1.y) & 255u) - 1u;
+    const DevOptics& o = s.opt[row];
+    const int src = o.fx2[2] > 0.0f ? (int)row : o.idx[0];
+    const DevOptics& ds = s.opt[max(src, 0)];
+    const uint32_t h = hash32(id * 0x9e3779b1u ^ hash32(s.frame * 0x85ebca6bu + 0x165667b1u));
+    const uint32_t top1 = s.ps->top1, hw1 = s.ps->hw1;
+    for (uint32_t k = 0; k < n; k++) {
+        const uint32_t r = r0 + k;
+        int slot;
+        if (r < top1) slot = (int)s.stack1[top1 - 1u - r];
+        else {
+            const uint32_t hw = hw1 + (r - top1);
+            slot = hw < kDustMax ? (int)(kDiffuseMax + hw) : -1;
+        }
+        if (slot < 0) break;
+        const uint32_t hk = hash32(h + k * 0x9e3779b9u);
+        const float u1 = rnd24(hash32(hk ^ 0x2c1b3c6du)), u2 = rnd24(hash32(hk ^ 0x297a2d39u));
+        const float z = u1, a = 6.2831853f * u2, rr = sqrtf(maxf(1.0f - z * z, 0.0f));
+        float sn, cs;
+        sp_sincos(a, &sn, &cs);
+        DevDiffuse e;
+        e.px = q0.x + (rnd24(hash32(hk ^ 0x51ed270bu)) - 0.5f) * 0.9f;
+        e.py = q0.y + (rnd24(hash32(hk ^ 0x7feb352du)) - 0.5f) * 0.9f;
+        e.vx = q0.z;
+        e.vy = q0.w;
+        e.life = __uint_as_float(pack_n(rr * cs, rr * sn, z, hk));
+        e.r = ds.dust2[0] / s.d.P->misc[2];
+        e.info = BUBBLE | DUST | ((uint32_t)(max(src, 0) + 1) << 8) | (hash32(hk ^ 0x68e31da4u) & 0xffff8000u);
+        e.z = rnd24(hash32(hk ^ 0xb5297a4du));
+        s.pool[slot] = e;
+    }
+}
+__global__ void k_speck_taken(PoolState* ps) {
+    const uint32_t n = ps->total1, top = ps->top1;
+    ps->top1 = n < top ? top - n : 0u;
+    ps->hw1 += n > top ? n - top : 0u;
+}
+
 }  // namespace
 
-void launch_spray(const DevScene& d, const ushort4* smooth, const SprayBufs& b, const RenderClock* clock, uint32_t frame,
-                  uint32_t parity, float amount, bool makes, cudaStream_t st) {
-    Spray s{d, smooth, b.pool, b.stack, b.list, b.dcount, b.counts, b.flags, b.ps, clock, frame, parity, amount, d.W, d.H};
+void launch_spray(const DevScene& d, const ushort4* smooth, const DevOptics* opt, const SprayBufs& b,
+                  const RenderClock* clock, uint32_t frame, uint32_t parity, float amount, bool makes, cudaStream_t st) {
+    Spray s{d, smooth, opt, b.pool, b.stack, b.stack1, b.list, b.dcount, b.counts, b.flags, b.dfield, b.nspeck, b.ps, clock,
+            frame, parity, amount, d.W, d.H};
     const int n = d.W * d.H;
-    // this frame's foam count starts from nothing (mod.rs:1751-1752)
+    // this frame's foam and resting specks counted from nothing, the dust field laid anew
+    // (mod.rs:1751-1754)
     cudaMemsetAsync(b.dcount + (size_t)parity * n, 0, (size_t)n * sizeof(uint32_t), st);
+    cudaMemsetAsync(b.dcount + (size_t)(2 + parity) * n, 0, (size_t)n * sizeof(uint32_t), st);
+    cudaMemsetAsync(b.dfield, 0, (size_t)4 * n * sizeof(int), st);
     const dim3 tiles((d.W + 15) / 16, (d.H + 15) / 16), block(16, 16);
     if (makes) {
         const int nb = (n + kScan - 1) / kScan;
         k_spray_count<<<tiles, block, 0, st>>>(s);
         k_spray_scan1<<<nb, kScan, 0, st>>>(b.counts, b.bsum, n);
-        k_spray_scan2<<<1, kScan, 0, st>>>(b.bsum, nb, b.ps);
+        k_spray_scan2<<<1, kScan, 0, st>>>(b.bsum, nb, &b.ps->total);
         k_spray_scan3<<<nb, kScan, 0, st>>>(b.counts, b.bsum, n);
         k_spray_make<<<tiles, block, 0, st>>>(s);
         k_spray_taken<<<1, 1, 0, st>>>(b.ps, clock);
     }
-    k_spray_move<<<(kDiffuseMax + 255) / 256, 256, 0, st>>>(s);
+    k_spray_move<<<(kPoolMax + 255) / 256, 256, 0, st>>>(s);
     k_spray_returns<<<1, kScan, 0, st>>>(s);
+}
+
+void launch_specks(const DevScene& d, const DevOptics* opt, const SprayBufs& b, uint32_t frame, uint32_t n_slots,
+                   cudaStream_t st) {
+    Spray s{d, nullptr, opt, b.pool, b.stack, b.stack1, b.list, b.dcount, b.counts, b.flags, b.dfield, b.nspeck, b.ps,
+            nullptr, frame, 0u, 0.0f, d.W, d.H};
+    const int n = (int)n_slots + 1, nb = (n + kScan - 1) / kScan;
+    k_speck_count<<<(n + 255) / 256, 256, 0, st>>>(s, n_slots);
+    k_spray_scan1<<<nb, kScan, 0, st>>>(b.nspeck, b.bsum, n);
+    k_spray_scan2<<<1, kScan, 0, st>>>(b.bsum, nb, &b.ps->total1);
+    k_spray_scan3<<<nb, kScan, 0, st>>>(b.nspeck, b.bsum, n);
+    k_speck_emit<<<(n_slots + 255) / 256, 256, 0, st>>>(s, n_slots);
+    k_speck_taken<<<1, 1, 0, st>>>(b.ps);
 }
 
 }  // namespace sprout

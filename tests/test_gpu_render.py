@@ -197,13 +197,51 @@ def test_spray_bit_exact():
             ora.step(1, 1 / 240.0)
         sim.render(inv)
         ora.render(table.optics_table(), inv, int(table.get("sss_iters")), amount)
-        ep, es, el, ef, ec = sim.download_spray()
-        op, os_, ol, of, oc = ora.spray()
+        ep, es, es1, el, ef, ec = sim.download_spray()
+        op, os_, os1, ol, of, oc = ora.spray()
         assert ec == oc, f"counters {ec} vs {oc}"
-        assert np.array_equal(es, os_) and np.array_equal(el, ol), "free stack or list"
+        assert np.array_equal(es, os_) and np.array_equal(es1, os1) and np.array_equal(el, ol), "free stacks or list"
         assert np.array_equal(ef, of), "foam per cell"
         bad = np.nonzero(ep.view(np.uint32).reshape(-1, 8) != op.view(np.uint32).reshape(-1, 8))[0]
         assert len(bad) == 0, f"{len(np.unique(bad))} pool entries differ, first {bad[0]}: {ep[bad[0]]} vs {op[bad[0]]}"
         seen |= set((ep["info"][el] & 3).tolist())
     assert ec[0] > 0 and ec[2] > 0, "bubbles were made and live"
     assert {1, 2} <= seen, f"bubbles and foam seen ({seen})"
+
+
+def test_specks_bit_exact():
+    """look.comp's specks and spray.comp's move_dust on a dam break of water carrying sand
+    (dust 0.02): new particles bring their share of the specks into the pool's second part
+    (ranked by particle slot, the engine's slot order being the oracle's), the specks settle,
+    rest on the floor and are stirred up again, and lay their share of the colour into the dust
+    field that cell_optics.comp reads on the next frame. Over frames: the whole pool, both free
+    stacks, the list, the foam and resting-speck counts, the counters and the raw cell layers
+    (layer 18 the dust field) equal the oracle's bit for bit."""
+    sandy = {"mat0.dust": 0.02}
+    tank = tanks.dam_break(96, 64, extra=sandy)
+    sim, ora, problems = run_pair(tank, 4)
+    assert not problems, "\n".join(problems[:10])
+    table = S.SimParams(tank.settings)
+    inv = 1.0 / 80.0
+    states = set()
+    for n in (0, 3, 4, 2, 6, 5):
+        for _ in range(n):
+            sim.step(1, 1 / 240.0)
+            ora.step(1, 1 / 240.0)
+        sim.render(inv)
+        o = ora.render(table.optics_table(), inv, int(table.get("sss_iters")), float(table.get("bubbles")), has_dust=True)
+        m = diff(sim.download_render("raw"), o[0], "raw")
+        assert m is None, m
+        ep, es, es1, el, ef, ec = sim.download_spray()
+        op, os_, os1, ol, of, oc = ora.spray()
+        assert ec == oc, f"counters {ec} vs {oc}"
+        assert np.array_equal(es1, os1) and np.array_equal(el, ol), "specks' free stack or list"
+        assert np.array_equal(ef, of), "counts per cell"
+        bad = np.nonzero(ep.view(np.uint32).reshape(-1, 8) != op.view(np.uint32).reshape(-1, 8))[0]
+        assert len(bad) == 0, f"{len(np.unique(bad))} pool entries differ, first {bad[0]}: {ep[bad[0]]} vs {op[bad[0]]}"
+        specks = ep[el][(ep["info"][el] & 8) != 0]
+        states |= set((specks["info"] & 3).tolist())
+    assert ec[4] > 0, "specks came in"
+    assert {1, 2} <= states, f"specks suspended and resting ({states})"
+    raw = sim.download_render("raw").astype(np.float32)
+    assert float(raw[18, ..., 3].max()) > 0.0, "the dust field coloured the liquid"
