@@ -469,7 +469,7 @@ def run_engine(args, rank, world, local, pg):
                  "pressure_residual_max": mst.pressure_residual_max, "pressure_unconverged": mst.pressure_unconverged,
                  "pressure_true_residual_max_fp64": mst.pressure_true_residual_max,
                  "refinement": {"residual_replacements": mst.pressure_replacements,
-                                "rule": "true residual b - A x (FP64 sums of the FP32 values) checked each time the "
+                                "rule": "true residual b - A x (float-pair products and sums of the FP32 values) checked each time the "
                                         "carried |r| falls 100x; adopted where it exceeds twice the carried one and "
                                         "ten times the FP32 rounding floor eps |A| |x|"},
                  "storage": "BF16 couplings + FP32 row-sum-keeping diagonal on every level; FP32 vectors",

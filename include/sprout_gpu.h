@@ -87,10 +87,11 @@ typedef struct SproutSolverStats {
     float viscosity_residual;          /* |r| / |r0| of the last implicit viscosity solve */
     uint32_t pressure2_iters;          /* iterations of the last second pressure solve */
     float pressure_true_residual;      /* mixed precision: |b - A x| / |b| of the last solve's
-                                          pressure evaluated in FP64 (0 in plain mode) */
+                                          pressure with about 48 significant bits (products
+                                          and sums as float pairs; 0 in plain mode) */
     float pressure_true_residual_max;
     uint32_t pressure_replacements;    /* mixed precision: times the carried residual was replaced
-                                          by b - A x evaluated in FP64 (cumulative) */
+                                          by b - A x evaluated as float pairs (cumulative) */
 } SproutSolverStats;
 
 typedef struct SproutParams SproutParams;   /* SimParams */
@@ -390,10 +391,10 @@ int sprout_sim_trace_read(SproutSim* sim, unsigned long long* out, size_t cap, s
  * hierarchy's matrices stored in BF16 (with an FP32 diagonal that keeps every row sum) and
  * computed in FP32; every vector, the CG iterate, residual and operator in FP32; the dot
  * products, step lengths and convergence test in FP64; as refinement, each time the carried
- * residual has fallen 100x the true residual b - A x is evaluated in FP64 and replaces the
+ * residual has fallen 100x the true residual b - A x is evaluated as float pairs and replaces the
  * carried one where it exceeds it twice over and lies well above the FP32 rounding floor
- * (stats: pressure_replacements); at the end of each solve the true residual is evaluated in
- * FP64 (stats: pressure_true_residual). Both stop at the same
+ * (stats: pressure_replacements); at the end of each solve the true residual is evaluated as
+ * float pairs (stats: pressure_true_residual). Both stop at the same
  * relative residual (pressure_tol) of the residual the iteration carries, as the reference
  * does. Takes effect from the next step; the first switch to mode 1 allocates the BF16
  * matrices. */

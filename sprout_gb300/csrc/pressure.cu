@@ -1011,30 +1011,40 @@ DEV bool vcycle(const DevScene& d, const Tail& tl, const Rsrc<M>& R, float2* r_o
     return true;
 }
 
-// The mixed solve's closing check on level-0 tile t: the true residual b - A x of the final
-// iterate with FP64 arithmetic (the products and sums of the FP32 values in double), the
-// tile's sums of |b - A x|^2 and |b|^2 of the pressure potential into part[t].
-DEV void true_residual_tile(const DevScene& d, int t, Dbl4* part, Dbl4* buf) {
+// b - A x of a level-0 cell's pressure column, and of both columns, evaluated as float pairs:
+// each product exact (fma), the sum compensated (about 48 significant bits, FP64's job here
+// at a small fraction of FP64's cost on this GPU), rounded once to FP32 at the end
+DEV float2 pair_prod(float a, float b) {
+    const float p = a * b;
+    return make_float2(p, fmaf(a, b, -p));
+}
+DEV float2 pair_acc(float2 s, float2 t) { return ff_add(s.x, s.y, t.x, t.y); }
+
+// The true residual |b - A x| / |b| of the pressure column after a mixed-precision solve:
+// the tile's sums of (b - A x)^2 and b^2 as float pairs into part[t].
+DEV void true_residual_tile(const DevScene& d, int t, FF4* part, FF4* buf) {
     const Lv F = lev(d.lv, 0);
     if (d.ptile[F.toff + t] == 0u) {
-        if (threadIdx.x == 0) part[t] = Dbl4{0.0, 0.0, 0.0, 0.0};
+        if (threadIdx.x == 0) part[t] = FF4{make_float4(0.0f, 0.0f, 0.0f, 0.0f), make_float4(0.0f, 0.0f, 0.0f, 0.0f)};
         return;
     }
     const int2 og = tile_origin(F, t);
     const int cx = og.x + (threadIdx.x & 15), cy = og.y + (threadIdx.x >> 4);
-    Dbl4 a4{0.0, 0.0, 0.0, 0.0};
+    FF4 a4{make_float4(0.0f, 0.0f, 0.0f, 0.0f), make_float4(0.0f, 0.0f, 0.0f, 0.0f)};
     if (l_inside(F, cx, cy)) {
         const int i = l_at(F, cx, cy);
         const float D = d.mgd[i];
         if (D > 0.0f) {
             const float4 w = d.mga[i];
-            double r = (double)d.prhs[i].x - (double)D * (double)d.pres[i].x;
+            const float b = d.prhs[i].x;
+            const float2 dx = pair_prod(D, d.pres[i].x);
+            float2 r = pair_acc(make_float2(b, 0.0f), make_float2(-dx.x, -dx.y));
             for (int q = 0; q < 4; q++) {
-                int nx = cx + NBX[q], ny = cy + NBY[q];
-                if (unknown_op(d, F, nx, ny)) r += (double)wcomp(w, q) * (double)d.pres[l_at(F, nx, ny)].x;
+                const int nx = cx + NBX[q], ny = cy + NBY[q];
+                if (unknown_op(d, F, nx, ny)) r = pair_acc(r, pair_prod(wcomp(w, q), d.pres[l_at(F, nx, ny)].x));
             }
-            const double b = (double)d.prhs[i].x;
-            a4 = Dbl4{r * r, b * b, 0.0, 0.0};
+            const float rf = r.x + r.y;
+            a4 = ff_prod4(rf, rf, b, b, 0.0f, 0.0f, 0.0f, 0.0f);
         }
     }
     buf[threadIdx.x] = a4;
@@ -1047,7 +1057,7 @@ DEV void true_residual_tile(const DevScene& d, int t, Dbl4* part, Dbl4* buf) {
 // replacement strategies for Krylov subspace iterative methods", SIAM J. Sci. Comput. 22,
 // 2000). The recurrence r -= alpha q drifts from b - A x by rounding; at a few points of the
 // convergence the true residual of the current iterate is evaluated (the products and sums of
-// the FP32 values in FP64, rounded once to FP32) and, where the drift is worth removing, it
+// the FP32 values as float pairs, rounded once to FP32) and, where the drift is worth removing, it
 // replaces the carried one; the iteration continues with its directions unchanged.
 //
 // check_tile: on level-0 tile t, the true residual b - A x of both columns into rt, and the
@@ -1055,15 +1065,16 @@ DEV void true_residual_tile(const DevScene& d, int t, Dbl4* part, Dbl4* buf) {
 // second is the size of the residual that rounding x to FP32 alone leaves (eps = 2^-24), below
 // which a replacement would feed that rounding back into the recurrence instead of removing
 // drift.
-DEV void check_tile(const DevScene& d, int t, float2* rt, Dbl4* part, Dbl4* buf) {
+DEV void check_tile(const DevScene& d, int t, float2* rt, FF4* part, FF4* buf) {
     const Lv F = lev(d.lv, 0);
+    const FF4 zero{make_float4(0.0f, 0.0f, 0.0f, 0.0f), make_float4(0.0f, 0.0f, 0.0f, 0.0f)};
     if (d.ptile[F.toff + t] == 0u) {
-        if (threadIdx.x == 0) part[t] = Dbl4{0.0, 0.0, 0.0, 0.0};
+        if (threadIdx.x == 0) part[t] = zero;
         return;
     }
     const int2 og = tile_origin(F, t);
     const int cx = og.x + (threadIdx.x & 15), cy = og.y + (threadIdx.x >> 4);
-    Dbl4 a4{0.0, 0.0, 0.0, 0.0};
+    FF4 a4 = zero;
     if (l_inside(F, cx, cy)) {
         const int i = l_at(F, cx, cy);
         const float D = d.mgd[i];
@@ -1071,21 +1082,24 @@ DEV void check_tile(const DevScene& d, int t, float2* rt, Dbl4* part, Dbl4* buf)
             const float4 w = d.mga[i];
             const float2 x = d.pres[i];
             const float4 b = d.prhs[i];
-            double rx = (double)b.x - (double)D * (double)x.x, ry = (double)b.y - (double)D * (double)x.y;
-            double ax = fabs((double)D * (double)x.x);
+            const float2 dx = pair_prod(D, x.x), dy = pair_prod(D, x.y);
+            float2 rx = pair_acc(make_float2(b.x, 0.0f), make_float2(-dx.x, -dx.y));
+            float2 ry = pair_acc(make_float2(b.y, 0.0f), make_float2(-dy.x, -dy.y));
+            float ax = fabsf(D * x.x);
             for (int q = 0; q < 4; q++) {
                 const int nx = cx + NBX[q], ny = cy + NBY[q];
                 if (unknown_op(d, F, nx, ny)) {
                     const float2 xn = d.pres[l_at(F, nx, ny)];
-                    const double wq = (double)wcomp(w, q);
-                    rx += wq * (double)xn.x;
-                    ry += wq * (double)xn.y;
-                    ax += fabs(wq * (double)xn.x);
+                    const float wq = wcomp(w, q);
+                    rx = pair_acc(rx, pair_prod(wq, xn.x));
+                    ry = pair_acc(ry, pair_prod(wq, xn.y));
+                    ax += fabsf(wq * xn.x);
                 }
             }
-            rt[i] = make_float2((float)rx, (float)ry);
-            const double fl = ax * 0x1p-24;
-            a4 = Dbl4{rx * rx, fl * fl, 0.0, 0.0};
+            const float rfx = rx.x + rx.y, rfy = ry.x + ry.y;
+            rt[i] = make_float2(rfx, rfy);
+            const float fl = ax * 0x1p-24f;
+            a4 = ff_prod4(rfx, rfx, fl, fl, 0.0f, 0.0f, 0.0f, 0.0f);
         } else {
             rt[i] = make_float2(0.0f, 0.0f);
         }
@@ -1375,10 +1389,10 @@ __global__ void __launch_bounds__(NT, 2) k_mgpcg(DevScene d, int second, int sca
             // the refinement (the same decisions in every block: the same K); q is free until
             // the apply phase rewrites it, and the partials' second half until it sums p.q
             if (it > 0 && want_check(K)) {
-                Dbl4* pc = d.partials64 + n;
-                for_active(d, 0, tc, [&](int t) { check_tile(d, t, d.cgq, pc, reinterpret_cast<Dbl4*>(buf)); });
+                FF4* pc = reinterpret_cast<FF4*>(d.partials64) + n;
+                for_active(d, 0, tc, [&](int t) { check_tile(d, t, d.cgq, pc, reinterpret_cast<FF4*>(buf)); });
                 if (!grid_sync(d.K)) return;
-                const Dbl4 tot = total(pc, n, reinterpret_cast<Dbl4*>(buf));
+                const Dbl4 tot = to_dbl(total(pc, n, reinterpret_cast<FF4*>(buf)));
                 __shared__ int s_adopt;
                 if (threadIdx.x == 0) s_adopt = decide_check(K, tot) ? 1 : 0;
                 __syncthreads();
@@ -1414,9 +1428,10 @@ __global__ void __launch_bounds__(NT, 2) k_mgpcg(DevScene d, int second, int sca
     }
     double true_rel = -1.0;
     if constexpr (M::kMixed) {
-        for_active(d, 0, tc, [&](int t) { true_residual_tile(d, t, d.partials64, reinterpret_cast<Dbl4*>(buf)); });
+        FF4* pt = reinterpret_cast<FF4*>(d.partials64);
+        for_active(d, 0, tc, [&](int t) { true_residual_tile(d, t, pt, reinterpret_cast<FF4*>(buf)); });
         if (!grid_sync(d.K)) return;
-        const Dbl4 t4 = total(d.partials64, n, reinterpret_cast<Dbl4*>(buf));
+        const Dbl4 t4 = to_dbl(total(pt, n, reinterpret_cast<FF4*>(buf)));
         true_rel = t4.y > 0.0 ? sqrt(t4.x / t4.y) : 0.0;
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) scal_stats<M, acc>(d.K, K, second, true_rel);
@@ -1678,14 +1693,14 @@ __global__ void __launch_bounds__(NT, 4) k_mgpcg_batch(BatchView B, int second) 
             __syncthreads();
             if (s_run) {
                 for_active_b(B, 0, tc, [&](int s, const DevScene& d, int t) {
-                    if (chk(s)) check_tile(d, t, d.cgq, d.partials64 + d.nwg, reinterpret_cast<Dbl4*>(buf));
+                    if (chk(s)) check_tile(d, t, d.cgq, reinterpret_cast<FF4*>(d.partials64) + d.nwg, reinterpret_cast<FF4*>(buf));
                 });
                 if (!grid_sync(BK)) return;
                 // each scene's decision by one block (it alone writes KS[s] until the next barrier)
                 for (int s = blockIdx.x; s < B.ns; s += gridDim.x) {
                     if (!chk(s)) continue;
                     const DevScene& d = B.scenes[s];
-                    const Dbl4 tot = total(d.partials64 + d.nwg, d.nwg, reinterpret_cast<Dbl4*>(buf));
+                    const Dbl4 tot = to_dbl(total(reinterpret_cast<FF4*>(d.partials64) + d.nwg, d.nwg, reinterpret_cast<FF4*>(buf)));
                     if (threadIdx.x == 0) KS[s].adopt = decide_check(KS[s], tot) ? 1u : 0u;
                     __syncthreads();
                 }
@@ -1730,7 +1745,7 @@ __global__ void __launch_bounds__(NT, 4) k_mgpcg_batch(BatchView B, int second) 
     }
     if constexpr (M::kMixed) {
         for_active_b(B, 0, tc, [&](int s, const DevScene& d, int t) {
-            true_residual_tile(d, t, d.partials64, reinterpret_cast<Dbl4*>(buf));
+            true_residual_tile(d, t, reinterpret_cast<FF4*>(d.partials64), reinterpret_cast<FF4*>(buf));
         });
         if (!grid_sync(BK)) return;
     }
@@ -1738,7 +1753,7 @@ __global__ void __launch_bounds__(NT, 4) k_mgpcg_batch(BatchView B, int second) 
         const DevScene& d = B.scenes[s];
         double true_rel = -1.0;
         if constexpr (M::kMixed) {
-            const Dbl4 t4 = total(d.partials64, d.nwg, reinterpret_cast<Dbl4*>(buf));
+            const Dbl4 t4 = to_dbl(total(reinterpret_cast<FF4*>(d.partials64), d.nwg, reinterpret_cast<FF4*>(buf)));
             true_rel = t4.y > 0.0 ? sqrt(t4.x / t4.y) : 0.0;
         }
         if (threadIdx.x == 0) scal_stats<M, acc>(d.K, KS[s], second, true_rel);
