@@ -224,7 +224,8 @@ def run_reference(args, rank, world, pg, budget_s: float = 90.0):
 
 
 def kernels_per_substep(stats, settings: dict) -> int:
-    n = 2 + 7 + 1                 # step + advance; scan x3 + place + cell sort + crowd sort + gather; p2g
+    n = 2 + 7 + 1 + 1             # step + advance; scan x3 + place + cell sort + crowd sort + gather; p2g;
+                                  # the frame's end (the recorded iteration counts, each profiled substep)
     n += 4 + 1                    # grid_prep, coef/smooth, curvature, jumps; rhs
     caps = int(stats.caps)
     n += 1 if caps & 8 else 0     # rheo.comp
