@@ -318,6 +318,32 @@ int sprout_sim_flow_parity(SproutSim* sim, uint32_t* parity);
  * two restarts half a period apart (xy, zw), cells. *words = the word count; out may be NULL
  * to ask for it. */
 int sprout_sim_download_render(SproutSim* sim, int which, uint16_t* out, size_t cap, size_t* words);
+/* Renderer::render's particle fields for one view (src/render.rs:886-1075) and the wet map
+ * (render.rs:640-668), into headless device images on the sim's stream (no wait); replaces the
+ * splat, tint, down and blur passes (shaders/splat.vert, splat.frag, tint.frag, down.frag,
+ * blur.frag) and wet.frag. The view: (center_x, center_y) in cells, `zoom` pixels per cell
+ * (> 0), width x height pixels (1 to 16384 each). As render.rs lays them out:
+ * - the sharp field: each phase group's weight times the splat kernel, RGBA16F texels of
+ *   clamp(1.5 zoom / 2.8, 1, 2) pixels, every live particle drawn stretched back along its path
+ *   over 1/160 s;
+ * - the tint field, twice as coarse, only when two liquids of one phase group are in the tank
+ *   (else its images keep what they held): absorption (RGB) of the concentrate part and the
+ *   scattering; the concentrate share, the aqueous weight, the other weight, 0;
+ * - the wide field: the sharp field box-filtered down to texels of clamp(2 zoom / 3, 2, 64)
+ *   pixels and blurred by a 13-tap Gaussian across, then down;
+ * - the wet map (RGBA32F, a texel per cell, kept between calls): where liquid (occupancy at least
+ *   0.3) lies within 1.75 cells of a solid, its leading material row + 1, family 0's
+ *   concentration and the simulated time; written once per simulated time, cleared on a new
+ *   tank.
+ * Each texel of a splat is the sum over the particles of kernel x weight, added as 64-bit
+ * fixed point (2^-32) and rounded to half once: the same whatever order the particles land in
+ * (the reference blends in the hardware's order into half floats). */
+int sprout_sim_draw(SproutSim* sim, float center_x, float center_y, float zoom, uint32_t width, uint32_t height);
+/* An image of the last sprout_sim_draw (blocking): which 0, the sharp field; 1, the tint field's
+ * absorption image; 2, its share image; 3, the wide field (RGBA16F, 8 bytes a texel); 4, the wet
+ * map (RGBA32F, 16 bytes a texel, W x H). dims = its texels across and down (0 x 0: not drawn);
+ * out may be NULL to ask for them. */
+int sprout_sim_download_draw(SproutSim* sim, int which, void* out, size_t cap, uint32_t dims[2]);
 /* Stats (src/sim/mod.rs:130-136): live particles and, per material row, its particles and the
  * sum of their concentrations (in particles, a multiple of 1/256). */
 #define SPROUT_MATERIAL_ROWS 96
@@ -356,7 +382,8 @@ int sprout_sim_download_particles(SproutSim* sim, SproutParticle* out, uint32_t 
 /* FluidSim::download_pressure: the two potentials per cell (p dt, psi), 2 w h floats. */
 int sprout_sim_download_pressure(SproutSim* sim, float* out);
 /* A named grid field (vel, cell, comp, coef, acc, pres, prhs, mga, mgd, pjump, surf, sprop,
- * therm, dheat, hcell, vw, vs, ptile, step, region_air, ledger) into `out` (at most cap
+ * therm, dheat, hcell, vw, vs, ptile, step, region_air, ledger; sdf, the solid distance at the
+ * (W + 1) x (H + 1) nodes) into `out` (at most cap
  * bytes); *bytes = its size. Blocking. For tests and tools. */
 int sprout_sim_download_field(SproutSim* sim, const char* name, void* out, size_t cap, size_t* bytes);
 /* SolverStats and the step scalars. Blocking. */

@@ -51,7 +51,7 @@ EXPORTS = [
     "sprout_sim_emit_paint", "sprout_sim_emit_rain", "sprout_sim_emitter_seed", "sprout_sim_emitted",
     "sprout_params_optics", "sprout_params_set_color", "sprout_sim_render", "sprout_sim_download_render",
     "sprout_params_get_color", "sprout_params_get_row", "sprout_sim_flow_parity", "sprout_sim_recorded_iters",
-    "sprout_sim_download_look", "sprout_sim_download_spray",
+    "sprout_sim_download_look", "sprout_sim_download_spray", "sprout_sim_draw", "sprout_sim_download_draw",
 ]
 
 # One row of the optics table (material.rs GpuOptics): 15 four-word fields, 240 bytes.
@@ -199,6 +199,8 @@ def lib() -> C.CDLL:
         "sprout_params_optics": ([V, V, C.c_uint32], C.c_int),
         "sprout_params_set_color": ([V, C.c_uint32, C.c_char_p, P(C.c_float), P(C.c_int)], C.c_int),
         "sprout_sim_render": ([V, C.c_float], C.c_int),
+        "sprout_sim_draw": ([V, C.c_float, C.c_float, C.c_float, C.c_uint32, C.c_uint32], C.c_int),
+        "sprout_sim_download_draw": ([V, C.c_int, V, C.c_size_t, P(C.c_uint32)], C.c_int),
         "sprout_sim_flow_parity": ([V, P(C.c_uint32)], C.c_int),
         "sprout_sim_recorded_iters": ([V, P(C.c_uint32)], C.c_int),
         "sprout_sim_download_look": ([V, V, C.c_size_t, V, C.c_size_t, P(C.c_uint32), P(C.c_uint32)], C.c_int),
@@ -531,6 +533,24 @@ class FluidSim:
         shape = {0: (RENDER_LAYERS, self.h, self.w, 4), 1: (24, self.h, self.w, 4),
                  2: ((self.h + 1) // 2, (self.w + 1) // 2, 4), 3: (4, self.h, self.w, 4)}[k]
         return out.view(np.float16).reshape(shape)
+
+    def draw(self, center, zoom: float, size):
+        """Renderer::render's particle fields for a view of size = (width, height) pixels centred
+        on `center` (cells) at `zoom` pixels per cell, and the wet map (no wait)."""
+        _check(lib().sprout_sim_draw(self._h, float(center[0]), float(center[1]), float(zoom), int(size[0]), int(size[1])))
+
+    def download_draw(self, which: str = "sharp") -> np.ndarray:
+        """An image of the last draw: "sharp", "tint", "share" or "wide" as (h, w, 4) float16,
+        "wet" as (H, W, 4) float32; None when it was never drawn."""
+        k = {"sharp": 0, "tint": 1, "share": 2, "wide": 3, "wet": 4}[which]
+        dims = (C.c_uint32 * 2)()
+        _check(lib().sprout_sim_download_draw(self._h, k, None, 0, dims))
+        w, h = int(dims[0]), int(dims[1])
+        if w == 0:
+            return None
+        out = np.zeros((h, w, 4), np.float32 if k == 4 else np.float16)
+        _check(lib().sprout_sim_download_draw(self._h, k, out.ctypes.data, out.nbytes, dims))
+        return out
 
     # ---- the brush's emitters on the device (World::emit without a read-back) -------------
     def emit_stream(self, spout: "Spout", stream: "StreamState", frm, to, seconds: float, material: int):

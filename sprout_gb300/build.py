@@ -17,7 +17,7 @@ PKG = Path(__file__).resolve().parent
 CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = PKG / "libsprout_gpu.so"
-SOURCES = ["particles.cu", "admission.cu", "grid.cu", "pressure.cu", "viscosity.cu", "sim.cu", "params.cpp", "scene.cpp",
+SOURCES = ["draw.cu", "particles.cu", "admission.cu", "grid.cu", "pressure.cu", "viscosity.cu", "sim.cu", "params.cpp", "scene.cpp",
            "pacer.cpp", "raster.cu", "emit.cu", "optics.cpp", "optics.cu", "spray.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

@@ -1,0 +1,254 @@
+// The renderer's particle fields (Renderer::render, src/render.rs:886-1075) and the wet map
+// (render.rs:640-668, shaders/wet.frag) as kernels into headless device images, for one view
+// (centre, zoom in pixels per cell, extent in pixels):
+//   k_splat       splat.vert + splat.frag (the sharp field: each phase group's weight times
+//                 the kernel) and, with the tint flag, splat.vert + tint.frag (the tint field:
+//                 absorption and scattering, concentrate share, aqueous and other weight)
+//   k_fields_out  the texel sums to RGBA16F, the sums cleared for the next draw
+//   k_down        down.frag: the box filter of bilinear taps into the wide field
+//   k_blur        blur.frag: one direction of the 13-tap Gaussian of the wide field
+//   k_wet         wet.frag: the liquid that last lay against a solid, per cell
+// The reference rasterises one triangle per particle and blends additively into RGBA16F
+// targets, in an order the hardware picks. Here a thread takes a particle, finds the texels
+// whose centres lie inside its kernel from the same affine map the triangle interpolates
+// (uv = the position's coordinates along the particle's path and across it, in kernel radii),
+// and adds kernel x weight to 64-bit fixed-point texel sums (2^-32, integer atomics): the sum
+// is the same whatever order the particles land in, and is rounded to half once.
+#include <cuda_fp16.h>
+
+#include "dev_common.cuh"
+#include "kernels.h"
+
+namespace sprout {
+
+namespace {
+
+constexpr float kFix = 4294967296.0f;   // 2^32
+constexpr double kUnfix = 1.0 / 4294967296.0;
+constexpr uint32_t kRowSteam = 57u;     // common.glsl ROW_STEAM
+constexpr float kStreakMax = 1.5f;      // splat.vert STREAK_MAX, kernel radii
+constexpr float kReach = 1.75f;         // wet.frag REACH, cells
+constexpr float kWetting = 0.3f;        // wet.frag WETTING
+
+DEV int clampi_(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
+DEV float minf_(float a, float b) { return a < b ? a : b; }
+DEV float maxf_(float a, float b) { return a > b ? a : b; }
+DEV float clampf_(float v, float lo, float hi) { return minf_(maxf_(v, lo), hi); }
+DEV long long fix(float v) { return __float2ll_rn(v * kFix); }
+DEV void add_fix(long long* p, float v) {
+    const long long q = fix(v);
+    if (q != 0) atomicAdd(reinterpret_cast<unsigned long long*>(p), (unsigned long long)q);
+}
+DEV float unfix(long long s) { return (float)((double)s * kUnfix); }
+DEV ushort4 half4(float a, float b, float c, float d) {
+    return make_ushort4(__half_as_ushort(__float2half_rn(a)), __half_as_ushort(__float2half_rn(b)),
+                        __half_as_ushort(__float2half_rn(c)), __half_as_ushort(__float2half_rn(d)));
+}
+DEV float4 unhalf4(ushort4 v) {
+    return make_float4(__half2float(__ushort_as_half(v.x)), __half2float(__ushort_as_half(v.y)),
+                       __half2float(__ushort_as_half(v.z)), __half2float(__ushort_as_half(v.w)));
+}
+
+// The bilinear sample of a used region of w x h texels at (x, y) in texel units (a texel's
+// centre at i + 0.5), clamped to its edge: (1 - fy) ((1 - fx) t00 + fx t10) + fy ((1 - fx) t01
+// + fx t11), channel by channel in that order.
+DEV float4 bilinear(const ushort4* img, int w, int h, float x, float y) {
+    const float xs = x - 0.5f, ys = y - 0.5f;
+    const float xf = floorf(xs), yf = floorf(ys);
+    const float fx = xs - xf, fy = ys - yf;
+    const int x0 = clampi_((int)xf, 0, w - 1), x1 = clampi_((int)xf + 1, 0, w - 1);
+    const int y0 = clampi_((int)yf, 0, h - 1), y1 = clampi_((int)yf + 1, 0, h - 1);
+    const float4 a = unhalf4(img[(size_t)y0 * w + x0]), b = unhalf4(img[(size_t)y0 * w + x1]);
+    const float4 c = unhalf4(img[(size_t)y1 * w + x0]), e = unhalf4(img[(size_t)y1 * w + x1]);
+    const float gx = 1.0f - fx, gy = 1.0f - fy;
+    return make_float4(gy * (gx * a.x + fx * b.x) + fy * (gx * c.x + fx * e.x),
+                       gy * (gx * a.y + fx * b.y) + fy * (gx * c.y + fx * e.y),
+                       gy * (gx * a.z + fx * b.z) + fy * (gx * c.z + fx * e.z),
+                       gy * (gx * a.w + fx * b.w) + fy * (gx * c.w + fx * e.w));
+}
+
+// splat.vert + splat.frag / tint.frag for particle slot id. A texel (i, j) of the image sits at
+// (cx + ((i + 0.5) div - half_w) / zoom, cy - ((j + 0.5) div - half_h) / zoom) in cells (the
+// view's map, y up); its uv is the position relative to the kernel's centre along the path
+// over `along` and across it over the radius; inside the unit disc it takes (1 - |uv|^2)^2.
+__global__ void __launch_bounds__(256) k_splat(DevScene d, const DevOptics* opt, uint32_t n_slots, DrawPass v,
+                                               long long* acc) {
+    const uint32_t id = blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= n_slots) return;
+    const float4 q0 = d.part[3 * id + 0], q2 = d.part[3 * id + 2];
+    const uint32_t kind = __float_as_uint(q2.y), low = kind & 255u;
+    if (low == 0u || (v.tint && low - 1u == kRowSteam)) return;
+    const uint32_t row = low - 1u;
+    const float speed = sqrtf(q0.z * q0.z + q0.w * q0.w);
+    const float dx = speed > 1e-3f ? q0.z / speed : 1.0f, dy = speed > 1e-3f ? q0.w / speed : 0.0f;
+    const float streak = minf_(speed * v.exposure, kStreakMax * v.radius);
+    const float along = v.radius + 0.5f * streak;
+    const float ex = q0.x - dx * (0.5f * streak), ey = q0.y - dy * (0.5f * streak);
+    // the texels whose centres can lie within `along` of the centre (none farther is inside)
+    const float tx0 = ((ex - along - v.cx) * v.zoom + v.half_w) / v.div, tx1 = ((ex + along - v.cx) * v.zoom + v.half_w) / v.div;
+    const float ty0 = (-(ey + along - v.cy) * v.zoom + v.half_h) / v.div, ty1 = (-(ey - along - v.cy) * v.zoom + v.half_h) / v.div;
+    if (!(tx1 >= -1.0f && ty1 >= -1.0f && tx0 <= (float)v.w + 1.0f && ty0 <= (float)v.h + 1.0f)) return;
+    const int i0 = (int)maxf_(floorf(tx0) - 1.0f, 0.0f), i1 = (int)minf_(ceilf(tx1) + 1.0f, (float)(v.w - 1));
+    const int j0 = (int)maxf_(floorf(ty0) - 1.0f, 0.0f), j1 = (int)minf_(ceilf(ty1) + 1.0f, (float)(v.h - 1));
+    // what the particle lays down (per unit kernel)
+    float c[7];
+    int ch0, nch;
+    if (!v.tint) {
+        ch0 = clampi_(d.mats[row].ia[0], 0, 3);
+        nch = 1;
+        c[0] = v.weight;
+    } else {
+        const DevOptics& o = opt[row];
+        const float s = o.idx[0] >= 0 ? clampf_(q2.x, 0.0f, 1.0f) : 0.0f;
+        const float* kc = o.absorb;
+        const float* kp = o.idx[0] >= 0 ? opt[o.idx[0]].absorb : o.absorb;
+        const float w = row == kRowSteam ? 0.0f : v.weight;
+        if (o.idx[1] == 0) {
+            c[0] = (s * kc[0]) * w;
+            c[1] = (s * kc[1]) * w;
+            c[2] = (s * kc[2]) * w;
+            c[3] = (s * kc[3] + (1.0f - s) * kp[3]) * w;
+            c[4] = s * w;
+            c[5] = 1.0f * w;
+            c[6] = 0.0f * w;
+        } else {
+            c[0] = kc[0] * w;
+            c[1] = kc[1] * w;
+            c[2] = kc[2] * w;
+            c[3] = kc[3] * w;
+            c[4] = 0.0f * w;
+            c[5] = 0.0f * w;
+            c[6] = w;
+        }
+        ch0 = 0;
+        nch = 7;
+    }
+    const int stride = v.tint ? 8 : 4;
+    for (int j = j0; j <= j1; j++) {
+        const float py = v.cy - (((float)j + 0.5f) * v.div - v.half_h) / v.zoom;
+        for (int i = i0; i <= i1; i++) {
+            const float px = v.cx + (((float)i + 0.5f) * v.div - v.half_w) / v.zoom;
+            const float rx = px - ex, ry = py - ey;
+            const float u = (rx * dx + ry * dy) / along, w2 = (ry * dx - rx * dy) / v.radius;
+            const float r2 = u * u + w2 * w2;
+            if (r2 >= 1.0f) continue;
+            const float k = (1.0f - r2) * (1.0f - r2);
+            long long* t = acc + ((size_t)j * v.w + i) * stride + ch0;
+            for (int q = 0; q < nch; q++) add_fix(t + q, c[q] * k);
+        }
+    }
+}
+
+// The texel sums of a pass to RGBA16F (the tint field's to its two images), cleared after.
+__global__ void __launch_bounds__(256) k_fields_out(long long* acc, int n, int tint, ushort4* a, ushort4* b) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    long long* s = acc + (size_t)i * (tint ? 8 : 4);
+    a[i] = half4(unfix(s[0]), unfix(s[1]), unfix(s[2]), unfix(s[3]));
+    if (tint) b[i] = half4(unfix(s[4]), unfix(s[5]), unfix(s[6]), 0.0f);
+    for (int q = 0; q < (tint ? 8 : 4); q++) s[q] = 0;
+}
+
+// down.frag: wide texel (i, j) averages taps x taps bilinear samples of the sharp field around
+// (i + 0.5, j + 0.5) x factor (its texels per wide texel), each held to the last used texel.
+__global__ void __launch_bounds__(256) k_down(const ushort4* src, int sw, int sh, ushort4* dst, int dw, int dh,
+                                              float factor, int taps) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= dw * dh) return;
+    const int y = i / dw, x = i - y * dw;
+    const float cx = ((float)x + 0.5f) * factor, cy = ((float)y + 0.5f) * factor;
+    const float mx = (float)sw - 0.5f, my = (float)sh - 0.5f;
+    float4 sum = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    for (int tj = 0; tj < taps; tj++)
+        for (int ti = 0; ti < taps; ti++) {
+            const float ox = (((float)ti + 0.5f) / (float)taps - 0.5f) * factor;
+            const float oy = (((float)tj + 0.5f) / (float)taps - 0.5f) * factor;
+            const float4 s = bilinear(src, sw, sh, minf_(cx + ox, mx), minf_(cy + oy, my));
+            sum.x += s.x;
+            sum.y += s.y;
+            sum.z += s.z;
+            sum.w += s.w;
+        }
+    const float n = (float)(taps * taps);
+    dst[i] = half4(sum.x / n, sum.y / n, sum.z / n, sum.w / n);
+}
+
+// blur.frag: one direction (vertical when vert) of the 13-tap Gaussian exp(-(k / 2)^2 / 2),
+// taps `step` texels apart, each held inside the used texels (the liquid carries on past the
+// edge of the view as it is at the edge).
+__global__ void __launch_bounds__(256) k_blur(const ushort4* src, ushort4* dst, int w, int h, float step, int vert) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= w * h) return;
+    const float G[7] = {1.0f, 0.8825f, 0.6065f, 0.3247f, 0.1353f, 0.0439f, 0.0111f};
+    const int y = i / w, x = i - y * w;
+    const float px = (float)x + 0.5f, py = (float)y + 0.5f;
+    const float lo = 0.5f, hx = (float)w - 0.5f, hy = (float)h - 0.5f;
+    const float4 c = bilinear(src, w, h, px, py);
+    float4 sum = make_float4(G[0] * c.x, G[0] * c.y, G[0] * c.z, G[0] * c.w);
+    float norm = G[0];
+    for (int k = 1; k < 7; k++) {
+        const float o = (float)k * step;
+        const float4 a = vert ? bilinear(src, w, h, px, clampf_(py + o, lo, hy)) : bilinear(src, w, h, clampf_(px + o, lo, hx), py);
+        const float4 b = vert ? bilinear(src, w, h, px, clampf_(py - o, lo, hy)) : bilinear(src, w, h, clampf_(px - o, lo, hx), py);
+        sum.x += G[k] * (a.x + b.x);
+        sum.y += G[k] * (a.y + b.y);
+        sum.z += G[k] * (a.z + b.z);
+        sum.w += G[k] * (a.w + b.w);
+        norm += 2.0f * G[k];
+    }
+    dst[i] = half4(sum.x / norm, sum.y / norm, sum.z / norm, sum.w / norm);
+}
+
+// The wet map's clock: whether the simulated time moved since the map was last written (the
+// reference writes it once per (tank, simulated time), render.rs:644-651).
+__global__ void k_wet_clock(const StepState* S, WetClock* c) {
+    const double now = (double)S->advanced - (double)__uint_as_float(S->pad0);
+    c->run = (!c->valid || now != c->last) ? 1u : 0u;
+    c->now = (float)now;
+    c->last = now;
+    c->valid = 1u;
+}
+
+// wet.frag: a cell close to a solid (the mean of its four nodes' distances at most REACH) and
+// held by liquid (occupancy at least WETTING) records its leading material (table row + 1),
+// family 0's concentration and the time; every other texel keeps what it had.
+__global__ void __launch_bounds__(256) k_wet(DevScene d, const WetClock* c, float4* wet) {
+    if (!c->run) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.W * d.H) return;
+    const int y = i / d.W, x = i - y * d.W;
+    const int w1 = d.W + 1, k = y * w1 + x;
+    const float dist = 0.25f * (d.sdf[k] + d.sdf[k + 1] + d.sdf[k + w1] + d.sdf[k + w1 + 1]);
+    if (dist > kReach || d.cell[i].x < kWetting) return;
+    const float sw = d.sprop[i].w;
+    const float code = floorf((sw - floorf(sw)) * 128.0f + 0.5f);
+    if (code < 1.0f) return;
+    wet[i] = make_float4(code, d.comp[i].z, c->now, 1.0f);
+}
+
+}  // namespace
+
+void launch_draw(const DevScene& d, const DevOptics* opt, uint32_t n_slots, const DrawPass& sharp, const DrawPass* tint,
+                const DrawWide& wide, DrawBufs& b, cudaStream_t st) {
+    const uint32_t nb = (n_slots + 255u) / 256u;
+    if (n_slots > 0) k_splat<<<nb, 256, 0, st>>>(d, opt, n_slots, sharp, b.acc);
+    const int na = sharp.w * sharp.h;
+    k_fields_out<<<(na + 255) / 256, 256, 0, st>>>(b.acc, na, 0, b.sharp, nullptr);
+    if (tint) {
+        if (n_slots > 0) k_splat<<<nb, 256, 0, st>>>(d, opt, n_slots, *tint, b.tacc);
+        const int nt = tint->w * tint->h;
+        k_fields_out<<<(nt + 255) / 256, 256, 0, st>>>(b.tacc, nt, 1, b.conc, b.share);
+    }
+    const int nw = wide.w * wide.h;
+    k_down<<<(nw + 255) / 256, 256, 0, st>>>(b.sharp, sharp.w, sharp.h, b.wide0, wide.w, wide.h, wide.factor, wide.taps);
+    k_blur<<<(nw + 255) / 256, 256, 0, st>>>(b.wide0, b.wide1, wide.w, wide.h, wide.step, 0);
+    k_blur<<<(nw + 255) / 256, 256, 0, st>>>(b.wide1, b.wide0, wide.w, wide.h, wide.step, 1);
+}
+
+void launch_wet(const DevScene& d, WetClock* clock, float4* wet, cudaStream_t st) {
+    k_wet_clock<<<1, 1, 0, st>>>(d.S, clock);
+    const int n = d.W * d.H;
+    k_wet<<<(n + 255) / 256, 256, 0, st>>>(d, clock, wet);
+}
+
+}  // namespace sprout

@@ -191,6 +191,36 @@ void launch_specks(const DevScene& d, const DevOptics* opt, const SprayBufs& b, 
 // foam counted into copy `parity` of dcount. `amount`: params.bubbles.
 void launch_spray(const DevScene& d, const ushort4* smooth, const DevOptics* opt, const SprayBufs& b,
                   const RenderClock* clock, uint32_t frame, uint32_t parity, float amount, bool makes, cudaStream_t st);
+// The renderer's particle fields for one view (draw.cu; Renderer::render, render.rs:886-1075).
+// One splat pass: the view's map (centre, zoom in pixels per cell, texels of div pixels from
+// the top-left of an extent of 2 half_w x 2 half_h pixels), its kernel and the used texels.
+struct DrawPass {
+    float cx, cy, zoom, div, half_w, half_h;
+    float radius, weight, exposure;
+    int w, h, tint;
+};
+// The wide field's layout (WideLayout): used texels, bilinear taps per axis, sharp-field
+// texels per wide texel, the blur's step (half a standard deviation) in texels.
+struct DrawWide {
+    int w, h, taps;
+    float factor, step;
+};
+struct DrawBufs {
+    long long *acc, *tacc;              // fixed-point texel sums (2^-32): 4 and 8 a texel
+    ushort4 *sharp, *conc, *share;      // RGBA16F: the sharp field, the tint field's two images
+    ushort4 *wide0, *wide1;             // the wide field (finished in wide0) and the blur's other image
+};
+// splat (+ tint when given), then the wide field: down, blur across, blur down.
+void launch_draw(const DevScene& d, const DevOptics* opt, uint32_t n_slots, const DrawPass& sharp, const DrawPass* tint,
+                 const DrawWide& wide, DrawBufs& b, cudaStream_t st);
+// The wet map (wet.frag) once per simulated time: the clock reads the time after the last
+// substep on the device and lets the pass run when it moved.
+struct WetClock {
+    double last;
+    float now;
+    uint32_t run, valid, pad;
+};
+void launch_wet(const DevScene& d, WetClock* clock, float4* wet, cudaStream_t st);
 // Scene::rasterize on the device (raster.cu): the tank's solid fields straight into device
 // buffers, bit-identical to the host's Scene::rasterize (scene.cpp).
 struct Scene;

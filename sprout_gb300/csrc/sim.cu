@@ -1001,19 +1001,11 @@ struct SproutSim {
     uint64_t substeps_issued = 0, resets = 0, tables_gen = 0;
     uint64_t render_key[4] = {0, 0, 0, 0};
     bool render_key_set = false, stain_valid = false;
-    int render(float inv_speed) {
-        if (!was_reset) return fail(SPROUT_E_ARG, "render before reset");
-        int rc = upload_tables(nullptr);
-        if (rc != SPROUT_OK) return rc;
-        const size_t nc = (size_t)W * H;
-        if (!d_raw) {
-            if ((rc = alloc(&d_raw, kRenderLayers * nc)) != SPROUT_OK) return rc;
-            if ((rc = alloc(&d_smooth, kSmoothLayers * nc)) != SPROUT_OK) return rc;
-            if ((rc = alloc(&d_flow, kFlowLayers * nc)) != SPROUT_OK) return rc;
-            if ((rc = alloc(&d_glow, 2 * glow_texels())) != SPROUT_OK) return rc;
-            if ((rc = alloc(&d_optics, kMaxMaterials)) != SPROUT_OK) return rc;
-            if ((rc = alloc(&d_clock, 1)) != SPROUT_OK) return rc;
-            CUDA_TRY(cudaMemsetAsync(d_clock, 0, sizeof(RenderClock), stream));
+    // The optics table of the current parameters on the device (uploaded when it changed).
+    int upload_optics() {
+        if (!d_optics) {
+            const int rc = alloc(&d_optics, kMaxMaterials);
+            if (rc != SPROUT_OK) return rc;
         }
         h_optics.resize(kMaxMaterials);
         optics_table(params, h_optics.data());
@@ -1024,6 +1016,22 @@ struct SproutSim {
             last_optics = h_optics;
             tables_gen++;
         }
+        return SPROUT_OK;
+    }
+    int render(float inv_speed) {
+        if (!was_reset) return fail(SPROUT_E_ARG, "render before reset");
+        int rc = upload_tables(nullptr);
+        if (rc != SPROUT_OK) return rc;
+        const size_t nc = (size_t)W * H;
+        if (!d_raw) {
+            if ((rc = alloc(&d_raw, kRenderLayers * nc)) != SPROUT_OK) return rc;
+            if ((rc = alloc(&d_smooth, kSmoothLayers * nc)) != SPROUT_OK) return rc;
+            if ((rc = alloc(&d_flow, kFlowLayers * nc)) != SPROUT_OK) return rc;
+            if ((rc = alloc(&d_glow, 2 * glow_texels())) != SPROUT_OK) return rc;
+            if ((rc = alloc(&d_clock, 1)) != SPROUT_OK) return rc;
+            CUDA_TRY(cudaMemsetAsync(d_clock, 0, sizeof(RenderClock), stream));
+        }
+        if ((rc = upload_optics()) != SPROUT_OK) return rc;
         // a new tank: nothing carried (mod.rs:1631-1638)
         if (!stain_valid) CUDA_TRY(cudaMemsetAsync(d_flow, 0, sizeof(ushort4) * kFlowLayers * nc, stream));
         const uint64_t key[4] = {substeps_issued, resets, tables_gen, (uint64_t)__builtin_bit_cast(uint32_t, inv_speed)};
@@ -1086,6 +1094,122 @@ struct SproutSim {
         const float mu0 = 1.2566371e-6f;
         *mc = std::sqrt(2.0f * mu0 * (1.0f + 1.0f / (1.0f + best->susceptibility)) * std::sqrt(rho * g * sigma));
     }
+    // ---- the renderer's particle fields (draw.cu; Renderer::render, render.rs:886-1075) ----
+    // render.rs's constants: SPLAT_RADIUS, ACCUM_KERNEL_TEXELS, ACCUM_MAX_DIV, SPLAT_MIN_TEXELS,
+    // EXPOSURE, WIDE_SIGMA, WIDE_SIGMA_TEXELS, WIDE_MIN_FACTOR, WIDE_MAX_FACTOR, TINT_DIV
+    static constexpr float kSplatRadius = 1.5f, kAccumKernelTexels = 2.8f, kAccumMaxDiv = 2.0f, kSplatMinTexels = 1.5f;
+    static constexpr float kWideSigma = 2.0f, kWideSigmaTexels = 3.0f, kWideMinFactor = 2.0f, kWideMaxFactor = 64.0f;
+    static constexpr uint32_t kTintDiv = 2u, kDrawMaxExtent = 16384u;
+    DrawBufs drawb{};
+    size_t cap_acc = 0, cap_tacc = 0, cap_sharp = 0, cap_conc = 0, cap_share = 0, cap_w0 = 0, cap_w1 = 0;
+    uint32_t draw_dims[4][2] = {};   // used texels of the sharp field, the tint field (0 x 0: never drawn), the wide field
+    float4* d_wet = nullptr;
+    WetClock* d_wet_clock = nullptr;
+    size_t wet_cells = 0;
+    uint64_t wet_resets = ~0ull;
+    // FluidSim::shares_a_group (mod.rs:1872-1878): two liquids of one phase group in the tank,
+    // steam aside
+    bool shares_a_group() const {
+        uint32_t seen[8] = {};
+        for (int r : tank.rows) {
+            if (r == 57) continue;
+            const uint32_t g = std::min<uint32_t>((uint32_t)params.mat[r].group, 7u);
+            if (++seen[g] >= 2) return true;
+        }
+        return false;
+    }
+    // grow() for buffers that must start zeroed (the fixed-point texel sums)
+    template <class T>
+    int grow_zeroed(T** p, size_t* cap, size_t n) {
+        T* before = *p;
+        const int rc = grow(p, cap, n);
+        if (rc != SPROUT_OK) return rc;
+        if (*p != before) CUDA_TRY(cudaMemsetAsync(*p, 0, *cap * sizeof(T), stream));
+        return SPROUT_OK;
+    }
+    // Renderer::render's passes 1, 1a and 2-4 (render.rs:889-1075) for a view of `ew` x `eh`
+    // pixels centred on (cx, cy) cells at `zoom` pixels per cell, and the wet map
+    // (render.rs:640-668), on the sim's stream (no wait).
+    int draw(float cx, float cy, float zoom, uint32_t ew, uint32_t eh) {
+        if (!was_reset) return fail(SPROUT_E_ARG, "draw before reset");
+        if (!(zoom > 0.0f) || !std::isfinite(zoom) || !std::isfinite(cx) || !std::isfinite(cy))
+            return fail(SPROUT_E_ARG, "draw: the zoom is a positive number of pixels per cell and the centre is finite");
+        if (ew < 1u || eh < 1u || ew > kDrawMaxExtent || eh > kDrawMaxExtent)
+            return fail(SPROUT_E_ARG, "draw: the extent is 1 to 16384 pixels a side");
+        int rc = upload_tables(nullptr);
+        if (rc != SPROUT_OK) return rc;
+        if ((rc = upload_optics()) != SPROUT_OK) return rc;
+        const float half_w = (float)ew * 0.5f, half_h = (float)eh * 0.5f;
+        // pass 1: the sharp field, in texels of div pixels
+        const float div = std::clamp(kSplatRadius * zoom / kAccumKernelTexels, 1.0f, kAccumMaxDiv);
+        const uint32_t aw = std::clamp((uint32_t)std::ceil((float)ew / div), 1u, ew);
+        const uint32_t ah = std::clamp((uint32_t)std::ceil((float)eh / div), 1u, eh);
+        const float radius = std::max(kSplatRadius, kSplatMinTexels * div / zoom);
+        const float exposure = 1.0f / 160.0f;
+        DrawPass sharp{cx, cy, zoom, div, half_w, half_h, radius, (kSplatRadius / radius) * (kSplatRadius / radius), exposure,
+                       (int)aw, (int)ah, 0};
+        // pass 1a: the tint field, TINT_DIV times coarser, where it can show something
+        const bool tint_live = n_slots > 0 && shares_a_group();
+        const float dt = div * (float)kTintDiv;
+        const uint32_t tw = std::clamp((aw + kTintDiv - 1) / kTintDiv, 1u, (ew + kTintDiv - 1) / kTintDiv);
+        const uint32_t th = std::clamp((ah + kTintDiv - 1) / kTintDiv, 1u, (eh + kTintDiv - 1) / kTintDiv);
+        const float rt = std::max(kSplatRadius, kSplatMinTexels * dt / zoom);
+        DrawPass tint{cx, cy, zoom, dt, half_w, half_h, rt, (kSplatRadius / rt) * (kSplatRadius / rt), exposure, (int)tw, (int)th, 1};
+        // passes 2-4: the wide field (WideLayout::new)
+        const float factor = std::clamp(kWideSigma * zoom / kWideSigmaTexels, kWideMinFactor, kWideMaxFactor);
+        const uint32_t iw = std::max(1u, (uint32_t)std::ceil((float)ew / kWideMinFactor));
+        const uint32_t ih = std::max(1u, (uint32_t)std::ceil((float)eh / kWideMinFactor));
+        const uint32_t ww = std::clamp((uint32_t)std::ceil((float)ew / factor), 1u, iw);
+        const uint32_t wh = std::clamp((uint32_t)std::ceil((float)eh / factor), 1u, ih);
+        DrawWide wide{(int)ww, (int)wh, (int)std::ceil(factor / div * 0.5f), factor / div, 0.5f * kWideSigma * zoom / factor};
+        const size_t na = (size_t)aw * ah, nt = (size_t)tw * th, nw = (size_t)ww * wh;
+        if ((rc = grow_zeroed(&drawb.acc, &cap_acc, 4 * na)) != SPROUT_OK) return rc;
+        if ((rc = grow(&drawb.sharp, &cap_sharp, na)) != SPROUT_OK) return rc;
+        if (tint_live) {
+            if ((rc = grow_zeroed(&drawb.tacc, &cap_tacc, 8 * nt)) != SPROUT_OK) return rc;
+            if ((rc = grow(&drawb.conc, &cap_conc, nt)) != SPROUT_OK) return rc;
+            if ((rc = grow(&drawb.share, &cap_share, nt)) != SPROUT_OK) return rc;
+        }
+        if ((rc = grow(&drawb.wide0, &cap_w0, nw)) != SPROUT_OK) return rc;
+        if ((rc = grow(&drawb.wide1, &cap_w1, nw)) != SPROUT_OK) return rc;
+        launch_draw(d, d_optics, n_slots, sharp, tint_live ? &tint : nullptr, wide, drawb, stream);
+        draw_dims[0][0] = aw, draw_dims[0][1] = ah;
+        if (tint_live) draw_dims[1][0] = draw_dims[2][0] = tw, draw_dims[1][1] = draw_dims[2][1] = th;
+        draw_dims[3][0] = ww, draw_dims[3][1] = wh;
+        // the wet map: a new map, or a tank that started over, holds nothing wet
+        const size_t nc = (size_t)W * H;
+        if (!d_wet || wet_cells != nc) {
+            if ((rc = grow(&d_wet, &wet_cells, nc)) != SPROUT_OK) return rc;
+            wet_cells = nc;
+            wet_resets = ~0ull;
+        }
+        if (!d_wet_clock && (rc = alloc(&d_wet_clock, 1)) != SPROUT_OK) return rc;
+        if (wet_resets != resets) {
+            CUDA_TRY(cudaMemsetAsync(d_wet, 0, nc * sizeof(float4), stream));
+            CUDA_TRY(cudaMemsetAsync(d_wet_clock, 0, sizeof(WetClock), stream));
+            wet_resets = resets;
+        }
+        launch_wet(d, d_wet_clock, d_wet, stream);
+        CUDA_TRY(cudaGetLastError());
+        return SPROUT_OK;
+    }
+    int download_draw(int which, void* out, size_t cap, uint32_t dims[2]) {
+        if (which < 0 || which > 4)
+            return fail(SPROUT_E_ARG, "download_draw: which is 0 (sharp), 1 (tint), 2 (tint share), 3 (wide) or 4 (wet map)");
+        const uint32_t w = which == 4 ? (d_wet ? (uint32_t)W : 0u) : draw_dims[which][0];
+        const uint32_t h = which == 4 ? (d_wet ? (uint32_t)H : 0u) : draw_dims[which][1];
+        dims[0] = w, dims[1] = h;
+        const size_t n = (size_t)w * h * (which == 4 ? sizeof(float4) : sizeof(ushort4));
+        if (!out || n == 0) return SPROUT_OK;
+        if (cap < n) return fail(SPROUT_E_ARG, "download_draw: the output holds fewer bytes than the image");
+        const void* src = which == 0 ? (const void*)drawb.sharp : which == 1 ? (const void*)drawb.conc
+                          : which == 2 ? (const void*)drawb.share : which == 3 ? (const void*)drawb.wide0 : (const void*)d_wet;
+        CUDA_TRY(cudaStreamSynchronize(stream));
+        CUDA_TRY(cudaMemcpy(out, src, n, cudaMemcpyDeviceToHost));
+        d2h_bytes += n;
+        return SPROUT_OK;
+    }
+
     // spray.comp's pool (spray.cu): made, moved and listed by render calls
     SprayBufs spray{};
     int alloc_spray() {
@@ -2395,6 +2519,16 @@ int sprout_sim_download_render(SproutSim* sim, int which, uint16_t* out, size_t 
     return SPROUT_OK;
 }
 
+int sprout_sim_draw(SproutSim* sim, float center_x, float center_y, float zoom, uint32_t width, uint32_t height) {
+    if (!sim) return fail(SPROUT_E_ARG, "null argument");
+    return sim->draw(center_x, center_y, zoom, width, height);
+}
+
+int sprout_sim_download_draw(SproutSim* sim, int which, void* out, size_t cap, uint32_t dims[2]) {
+    if (!sim || !dims) return fail(SPROUT_E_ARG, "null argument");
+    return sim->download_draw(which, out, cap, dims);
+}
+
 int sprout_sim_download_spray(SproutSim* sim, SproutDiffuse* pool, size_t pool_cap, uint32_t* stack, uint32_t* stack1,
                               uint32_t* list, size_t cap, uint32_t* counts, size_t counts_cap, uint32_t state[8]) {
     if (!sim || !state) return fail(SPROUT_E_ARG, "null argument");
@@ -2486,6 +2620,7 @@ int sprout_sim_download_field(SproutSim* sim, const char* name, void* out, size_
     else if (n == "comp") { src = d.comp; b = nc * 16; }
     else if (n == "coef") { src = d.coef; b = nc * 16; }
     else if (n == "sprop") { src = d.sprop; b = nc * 16; }
+    else if (n == "sdf") { src = d.sdf; b = (size_t)(sim->W + 1) * (sim->H + 1) * 4; }
     else if (n == "surf") { src = d.surf; b = nc * 16; }
     else if (n == "pjump") { src = d.pjump; b = nc * 8; }
     else if (n == "therm") { src = d.therm; b = nc * 16; }
