@@ -403,6 +403,28 @@ def median_stages(runs) -> dict:
     return {k: float(np.median([r[0][k] for r in runs])) for k in runs[0][0]}
 
 
+def draw_timing(sim, tank) -> dict:
+    """The renderer's particle fields (sprout_sim_draw: the splat and tint fields, the wide
+    field, the wet map) for a 1920 x 1080 view of the whole tank after the timed substeps: host
+    ms per call including a sync, median of 10 after 3."""
+    import time
+    zoom = min(1920.0 / tank.w, 1080.0 / tank.h)
+    center = (tank.w * 0.5, tank.h * 0.5)
+    for _ in range(3):
+        sim.draw(center, zoom, (1920, 1080))
+    sim.sync()
+    ts = []
+    for _ in range(10):
+        t0 = time.perf_counter()
+        sim.draw(center, zoom, (1920, 1080))
+        sim.sync()
+        ts.append((time.perf_counter() - t0) * 1e3)
+    sharp, tint = sim.download_draw("sharp"), sim.download_draw("tint")
+    return {"view": "1920x1080", "zoom_px_per_cell": zoom, "ms_median": float(np.median(ts)), "ms_min": float(min(ts)),
+            "sharp_texels": list(sharp.shape[1::-1]), "tint_texels": None if tint is None else list(tint.shape[1::-1]),
+            "kernels": "k_splat x2, k_fields_out x2, k_down, k_blur x2, k_wet_clock, k_wet"}
+
+
 def run_engine(args, rank, world, local, pg):
     import sprout_gb300 as S
     from sprout_gb300 import bytes_model as BM
@@ -477,6 +499,7 @@ def run_engine(args, rank, world, local, pg):
                  "dots": "FP64", "speedup_vs_plain": (ms / args.steps) / (mms / args.steps)}
     # ---- end to end through the public API, on a fresh copy over the same substeps ----------
     e2e = end_to_end(tank, args, pg)
+    draw = draw_timing(sim, tank)
     batched = run_batched(args, pg, rank, world) if args.batch_tanks > 0 else None
     serving_r = run_serving(args) if (args.serve_seconds > 0 and world == 1) else None
     if rank != 0:
@@ -487,6 +510,7 @@ def run_engine(args, rank, world, local, pg):
             "parallelism": f"replicas x{world}", "run": run,
             "clocks": clk.summary(), "e2e": e2e, "gpu_launches": kernels_per_substep(st2, tank.settings) * args.steps,
             "roofline": roof, "stages_ms": stages, "latency_ms": {"p50": e2e["p50_ms"], "p99": e2e["p99_ms"]}}
+    line["draw"] = draw
     if mixed is not None:
         line["mixed"] = mixed
     if batched is not None:

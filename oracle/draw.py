@@ -6,7 +6,8 @@ Test infrastructure: the checker of the engine's draw (sprout_sim_draw). numpy f
 the arithmetic, each operation in the order the engine's kernels take it, so the two agree bit
 for bit. Where the reference leaves the order or the precision to the graphics hardware, the
 engine fixes them and this restatement follows the engine:
-- a texel's uv is the affine map the triangle interpolates, evaluated at the texel's centre;
+- a texel's uv is the affine map the triangle interpolates, evaluated at the texel's centre
+  (by reciprocals of the zoom, the kernel's radius and its length along the path);
 - the particles' contributions are summed as 64-bit fixed point (2^-32, round to nearest
   even) and rounded to half once (the hardware blends each one into a half-float target);
 - bilinear taps weigh the texels by the exact fraction (the hardware by a few bits of it).
@@ -55,12 +56,14 @@ def layout(center, zoom, extent, tint_live=True):
     radius = max(SPLAT_RADIUS, f32(SPLAT_MIN_TEXELS * div / zoom))
     weight = f32(f32(SPLAT_RADIUS / radius) * f32(SPLAT_RADIUS / radius))
     base = dict(cx=f32(center[0]), cy=f32(center[1]), zoom=zoom, half_w=half_w, half_h=half_h, exposure=EXPOSURE)
-    sharp = dict(base, div=div, radius=radius, weight=weight, w=aw, h=ah, tint=False)
+    sharp = dict(base, div=div, radius=radius, weight=weight, w=aw, h=ah, tint=False, izoom=f32(f32(1.0) / zoom),
+                 iradius=f32(f32(1.0) / radius))
     dt = f32(div * f32(TINT_DIV))
     tw = min(max(-(-aw // TINT_DIV), 1), -(-ew // TINT_DIV))
     th = min(max(-(-ah // TINT_DIV), 1), -(-eh // TINT_DIV))
     rt = max(SPLAT_RADIUS, f32(SPLAT_MIN_TEXELS * dt / zoom))
-    tint = dict(base, div=dt, radius=rt, weight=f32(f32(SPLAT_RADIUS / rt) * f32(SPLAT_RADIUS / rt)), w=tw, h=th, tint=True)
+    tint = dict(base, div=dt, radius=rt, weight=f32(f32(SPLAT_RADIUS / rt) * f32(SPLAT_RADIUS / rt)), w=tw, h=th, tint=True,
+                izoom=f32(f32(1.0) / zoom), iradius=f32(f32(1.0) / rt))
     factor = _clampf(WIDE_SIGMA * zoom / WIDE_SIGMA_TEXELS, WIDE_MIN_FACTOR, WIDE_MAX_FACTOR)
     image = [max(1, int(np.ceil(f32(ew) / WIDE_MIN_FACTOR))), max(1, int(np.ceil(f32(eh) / WIDE_MIN_FACTOR)))]
     ww = min(max(int(np.ceil(f32(ew) / factor)), 1), image[0])
@@ -116,6 +119,7 @@ def splat(parts, groups, optics, v):
         dx, dy = (f32(vx / speed), f32(vy / speed)) if speed > f32(1e-3) else (f32(1.0), f32(0.0))
         streak = min(f32(speed * v["exposure"]), f32(STREAK_MAX * radius))
         along = f32(radius + f32(f32(0.5) * streak))
+        ialong = f32(f32(1.0) / along)
         ex = f32(f32(p["pos"][0]) - f32(dx * f32(f32(0.5) * streak)))
         ey = f32(f32(p["pos"][1]) - f32(dy * f32(f32(0.5) * streak)))
         tx0 = f32(f32(f32(f32(f32(ex - along) - cx) * zoom) + half_w) / div)
@@ -132,12 +136,12 @@ def splat(parts, groups, optics, v):
             continue
         ii = np.arange(i0, i1 + 1).astype(f32)
         jj = np.arange(j0, j1 + 1).astype(f32)
-        px = cx + ((ii + f32(0.5)) * div - half_w) / zoom
-        py = cy - ((jj + f32(0.5)) * div - half_h) / zoom
+        px = cx + ((ii + f32(0.5)) * div - half_w) * v["izoom"]
+        py = cy - ((jj + f32(0.5)) * div - half_h) * v["izoom"]
         rx = (px[None, :] - ex).astype(f32)
         ry = (py[:, None] - ey).astype(f32)
-        u = (rx * dx + ry * dy) / along
-        w2 = (ry * dx - rx * dy) / radius
+        u = (rx * dx + ry * dy) * ialong
+        w2 = (ry * dx - rx * dy) * v["iradius"]
         r2 = u * u + w2 * w2
         inside = r2 < f32(1.0)
         k = (f32(1.0) - r2) * (f32(1.0) - r2)

@@ -16,6 +16,8 @@
 // is the same whatever order the particles land in, and is rounded to half once.
 #include <cuda_fp16.h>
 
+#include <climits>
+
 #include "dev_common.cuh"
 #include "kernels.h"
 
@@ -71,32 +73,38 @@ DEV float4 bilinear(const ushort4* img, int w, int h, float x, float y) {
 // (cx + ((i + 0.5) div - half_w) / zoom, cy - ((j + 0.5) div - half_h) / zoom) in cells (the
 // view's map, y up); its uv is the position relative to the kernel's centre along the path
 // over `along` and across it over the radius; inside the unit disc it takes (1 - |uv|^2)^2.
-__global__ void __launch_bounds__(256) k_splat(DevScene d, const DevOptics* opt, uint32_t n_slots, DrawPass v,
-                                               long long* acc) {
-    const uint32_t id = blockIdx.x * blockDim.x + threadIdx.x;
-    if (id >= n_slots) return;
+struct Splat {
+    float ex, ey, dx, dy, along, ialong;
+    int i0, i1, j0, j1;   // the texels it may reach (empty: i1 < i0)
+    int ch0, nch;
+    float c[7];           // what it lays down per unit kernel, channels ch0 ..
+};
+
+DEV Splat splat_of(const DevScene& d, const DevOptics* opt, uint32_t id, const DrawPass& v) {
+    Splat sp;
+    sp.i0 = 0, sp.i1 = -1, sp.j0 = 0, sp.j1 = -1, sp.ch0 = 0, sp.nch = 0;
     const float4 q0 = d.part[3 * id + 0], q2 = d.part[3 * id + 2];
     const uint32_t kind = __float_as_uint(q2.y), low = kind & 255u;
-    if (low == 0u || (v.tint && low - 1u == kRowSteam)) return;
+    if (low == 0u || (v.tint && low - 1u == kRowSteam)) return sp;
     const uint32_t row = low - 1u;
     const float speed = sqrtf(q0.z * q0.z + q0.w * q0.w);
-    const float dx = speed > 1e-3f ? q0.z / speed : 1.0f, dy = speed > 1e-3f ? q0.w / speed : 0.0f;
+    sp.dx = speed > 1e-3f ? q0.z / speed : 1.0f;
+    sp.dy = speed > 1e-3f ? q0.w / speed : 0.0f;
     const float streak = minf_(speed * v.exposure, kStreakMax * v.radius);
-    const float along = v.radius + 0.5f * streak;
-    const float ex = q0.x - dx * (0.5f * streak), ey = q0.y - dy * (0.5f * streak);
+    sp.along = v.radius + 0.5f * streak;
+    sp.ialong = 1.0f / sp.along;
+    sp.ex = q0.x - sp.dx * (0.5f * streak);
+    sp.ey = q0.y - sp.dy * (0.5f * streak);
     // the texels whose centres can lie within `along` of the centre (none farther is inside)
-    const float tx0 = ((ex - along - v.cx) * v.zoom + v.half_w) / v.div, tx1 = ((ex + along - v.cx) * v.zoom + v.half_w) / v.div;
-    const float ty0 = (-(ey + along - v.cy) * v.zoom + v.half_h) / v.div, ty1 = (-(ey - along - v.cy) * v.zoom + v.half_h) / v.div;
-    if (!(tx1 >= -1.0f && ty1 >= -1.0f && tx0 <= (float)v.w + 1.0f && ty0 <= (float)v.h + 1.0f)) return;
-    const int i0 = (int)maxf_(floorf(tx0) - 1.0f, 0.0f), i1 = (int)minf_(ceilf(tx1) + 1.0f, (float)(v.w - 1));
-    const int j0 = (int)maxf_(floorf(ty0) - 1.0f, 0.0f), j1 = (int)minf_(ceilf(ty1) + 1.0f, (float)(v.h - 1));
-    // what the particle lays down (per unit kernel)
-    float c[7];
-    int ch0, nch;
+    const float tx0 = ((sp.ex - sp.along - v.cx) * v.zoom + v.half_w) / v.div, tx1 = ((sp.ex + sp.along - v.cx) * v.zoom + v.half_w) / v.div;
+    const float ty0 = (-(sp.ey + sp.along - v.cy) * v.zoom + v.half_h) / v.div, ty1 = (-(sp.ey - sp.along - v.cy) * v.zoom + v.half_h) / v.div;
+    if (!(tx1 >= -1.0f && ty1 >= -1.0f && tx0 <= (float)v.w + 1.0f && ty0 <= (float)v.h + 1.0f)) return sp;
+    sp.i0 = (int)maxf_(floorf(tx0) - 1.0f, 0.0f), sp.i1 = (int)minf_(ceilf(tx1) + 1.0f, (float)(v.w - 1));
+    sp.j0 = (int)maxf_(floorf(ty0) - 1.0f, 0.0f), sp.j1 = (int)minf_(ceilf(ty1) + 1.0f, (float)(v.h - 1));
     if (!v.tint) {
-        ch0 = clampi_(d.mats[row].ia[0], 0, 3);
-        nch = 1;
-        c[0] = v.weight;
+        sp.ch0 = clampi_(d.mats[row].ia[0], 0, 3);
+        sp.nch = 1;
+        sp.c[0] = v.weight;
     } else {
         const DevOptics& o = opt[row];
         const float s = o.idx[0] >= 0 ? clampf_(q2.x, 0.0f, 1.0f) : 0.0f;
@@ -104,38 +112,108 @@ __global__ void __launch_bounds__(256) k_splat(DevScene d, const DevOptics* opt,
         const float* kp = o.idx[0] >= 0 ? opt[o.idx[0]].absorb : o.absorb;
         const float w = row == kRowSteam ? 0.0f : v.weight;
         if (o.idx[1] == 0) {
-            c[0] = (s * kc[0]) * w;
-            c[1] = (s * kc[1]) * w;
-            c[2] = (s * kc[2]) * w;
-            c[3] = (s * kc[3] + (1.0f - s) * kp[3]) * w;
-            c[4] = s * w;
-            c[5] = 1.0f * w;
-            c[6] = 0.0f * w;
+            sp.c[0] = (s * kc[0]) * w;
+            sp.c[1] = (s * kc[1]) * w;
+            sp.c[2] = (s * kc[2]) * w;
+            sp.c[3] = (s * kc[3] + (1.0f - s) * kp[3]) * w;
+            sp.c[4] = s * w;
+            sp.c[5] = 1.0f * w;
+            sp.c[6] = 0.0f * w;
         } else {
-            c[0] = kc[0] * w;
-            c[1] = kc[1] * w;
-            c[2] = kc[2] * w;
-            c[3] = kc[3] * w;
-            c[4] = 0.0f * w;
-            c[5] = 0.0f * w;
-            c[6] = w;
+            sp.c[0] = kc[0] * w;
+            sp.c[1] = kc[1] * w;
+            sp.c[2] = kc[2] * w;
+            sp.c[3] = kc[3] * w;
+            sp.c[4] = 0.0f * w;
+            sp.c[5] = 0.0f * w;
+            sp.c[6] = w;
         }
-        ch0 = 0;
-        nch = 7;
+        sp.nch = 7;
     }
-    const int stride = v.tint ? 8 : 4;
-    for (int j = j0; j <= j1; j++) {
-        const float py = v.cy - (((float)j + 0.5f) * v.div - v.half_h) / v.zoom;
-        for (int i = i0; i <= i1; i++) {
-            const float px = v.cx + (((float)i + 0.5f) * v.div - v.half_w) / v.zoom;
-            const float rx = px - ex, ry = py - ey;
-            const float u = (rx * dx + ry * dy) / along, w2 = (ry * dx - rx * dy) / v.radius;
+    return sp;
+}
+
+// A 64-bit sum in shared memory as two 32-bit words (low, high), added to with the native
+// 32-bit atomics: the low word's carry goes to the high word (mod 2^64, as a 64-bit add).
+DEV void add_fix_shared(uint32_t* w, float v) {
+    const unsigned long long u = (unsigned long long)fix(v);
+    if (u == 0ull) return;
+    const uint32_t lo = (uint32_t)u, hi = (uint32_t)(u >> 32);
+    const uint32_t old = atomicAdd(w, lo);
+    const uint32_t up = hi + ((uint32_t)(old + lo) < old ? 1u : 0u);
+    if (up != 0u) atomicAdd(w + 1, up);
+}
+DEV void add_fix(uint32_t* w, float v) { add_fix_shared(w, v); }
+
+// The particle's kernel x payload into sums laid out as `pitch` texels a row from texel
+// (oi, oj), `stride` sums a texel: 64-bit words in global memory, or word pairs in shared.
+template <class Acc, int kWords>
+DEV void splat_into(const Splat& sp, const DrawPass& v, Acc* acc, int oi, int oj, int pitch, int stride, int ch0) {
+    for (int j = sp.j0; j <= sp.j1; j++) {
+        const float py = v.cy - (((float)j + 0.5f) * v.div - v.half_h) * v.izoom;
+        for (int i = sp.i0; i <= sp.i1; i++) {
+            const float px = v.cx + (((float)i + 0.5f) * v.div - v.half_w) * v.izoom;
+            const float rx = px - sp.ex, ry = py - sp.ey;
+            const float u = (rx * sp.dx + ry * sp.dy) * sp.ialong, w2 = (ry * sp.dx - rx * sp.dy) * v.iradius;
             const float r2 = u * u + w2 * w2;
             if (r2 >= 1.0f) continue;
             const float k = (1.0f - r2) * (1.0f - r2);
-            long long* t = acc + ((size_t)j * v.w + i) * stride + ch0;
-            for (int q = 0; q < nch; q++) add_fix(t + q, c[q] * k);
+            Acc* t = acc + (((size_t)(j - oj) * pitch + (i - oi)) * stride + ch0) * kWords;
+#pragma unroll
+            for (int q = 0; q < 7; q++)
+                if (q < sp.nch) add_fix(t + q * kWords, sp.c[q] * k);
         }
+    }
+}
+
+// A block takes 256 consecutive slots. Sorted by cell, they mostly sit along a short run of
+// cells, so the block sums them over the texels their kernels reach in shared memory first
+// (one word a texel when they all lay down one channel, the sharp field of one phase group)
+// and adds each texel's non-zero sums to the image's once; where that run of texels does not
+// fit (a block across two rows of cells, a close view), each particle adds to the image
+// directly. Integer sums: the same either way.
+constexpr int kSplatSmemWords = 3072;   // 24 KB: five blocks of 256 threads still fit an SM
+__global__ void __launch_bounds__(256) k_splat(DevScene d, const DevOptics* opt, uint32_t n_slots, DrawPass v,
+                                               long long* acc) {
+    __shared__ uint32_t sacc[2 * kSplatSmemWords];
+    __shared__ int box[6];
+    const uint32_t id = blockIdx.x * blockDim.x + threadIdx.x;
+    Splat sp;
+    if (id < n_slots) sp = splat_of(d, opt, id, v);
+    else sp.i0 = 0, sp.i1 = -1, sp.j0 = 0, sp.j1 = -1, sp.ch0 = 0, sp.nch = 0;
+    if (threadIdx.x == 0) box[0] = box[1] = box[4] = INT_MAX, box[2] = box[3] = box[5] = INT_MIN;
+    __syncthreads();
+    const bool any = sp.i1 >= sp.i0 && sp.j1 >= sp.j0;
+    if (any) {
+        atomicMin(&box[0], sp.i0);
+        atomicMin(&box[1], sp.j0);
+        atomicMax(&box[2], sp.i1);
+        atomicMax(&box[3], sp.j1);
+        atomicMin(&box[4], sp.ch0);
+        atomicMax(&box[5], sp.ch0);
+    }
+    __syncthreads();
+    if (box[2] < box[0]) return;   // nothing of the block's in view
+    const int stride = v.tint ? 8 : 4;
+    const bool one = !v.tint && box[4] == box[5];
+    const int sstride = one ? 1 : stride;
+    const int bw = box[2] - box[0] + 1, bh = box[3] - box[1] + 1;
+    const long long words = (long long)bw * bh * sstride;
+    if (words > kSplatSmemWords) {
+        if (any) splat_into<long long, 1>(sp, v, acc, 0, 0, v.w, stride, sp.ch0);
+        return;
+    }
+    for (int k = threadIdx.x; k < 2 * (int)words; k += blockDim.x) sacc[k] = 0u;
+    __syncthreads();
+    if (any) splat_into<uint32_t, 2>(sp, v, sacc, box[0], box[1], bw, sstride, one ? 0 : sp.ch0);
+    __syncthreads();
+    for (int k = threadIdx.x; k < (int)words; k += blockDim.x) {
+        const unsigned long long q = ((unsigned long long)sacc[2 * k + 1] << 32) | sacc[2 * k];
+        if (q == 0ull) continue;
+        const int t = k / sstride, c = one ? box[4] : k - t * sstride;
+        const int ty = t / bw, tx = t - ty * bw;
+        atomicAdd(reinterpret_cast<unsigned long long*>(acc + ((size_t)(box[1] + ty) * v.w + box[0] + tx) * stride + c),
+                  q);
     }
 }
 

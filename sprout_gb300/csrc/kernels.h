@@ -198,6 +198,7 @@ struct DrawPass {
     float cx, cy, zoom, div, half_w, half_h;
     float radius, weight, exposure;
     int w, h, tint;
+    float izoom, iradius;   // 1 / zoom, 1 / radius
 };
 // The wide field's layout (WideLayout): used texels, bilinear taps per axis, sharp-field
 // texels per wide texel, the blur's step (half a standard deviation) in texels.

@@ -1147,14 +1147,15 @@ struct SproutSim {
         const float radius = std::max(kSplatRadius, kSplatMinTexels * div / zoom);
         const float exposure = 1.0f / 160.0f;
         DrawPass sharp{cx, cy, zoom, div, half_w, half_h, radius, (kSplatRadius / radius) * (kSplatRadius / radius), exposure,
-                       (int)aw, (int)ah, 0};
+                       (int)aw, (int)ah, 0, 1.0f / zoom, 1.0f / radius};
         // pass 1a: the tint field, TINT_DIV times coarser, where it can show something
         const bool tint_live = n_slots > 0 && shares_a_group();
         const float dt = div * (float)kTintDiv;
         const uint32_t tw = std::clamp((aw + kTintDiv - 1) / kTintDiv, 1u, (ew + kTintDiv - 1) / kTintDiv);
         const uint32_t th = std::clamp((ah + kTintDiv - 1) / kTintDiv, 1u, (eh + kTintDiv - 1) / kTintDiv);
         const float rt = std::max(kSplatRadius, kSplatMinTexels * dt / zoom);
-        DrawPass tint{cx, cy, zoom, dt, half_w, half_h, rt, (kSplatRadius / rt) * (kSplatRadius / rt), exposure, (int)tw, (int)th, 1};
+        DrawPass tint{cx, cy, zoom, dt, half_w, half_h, rt, (kSplatRadius / rt) * (kSplatRadius / rt), exposure, (int)tw, (int)th, 1,
+                      1.0f / zoom, 1.0f / rt};
         // passes 2-4: the wide field (WideLayout::new)
         const float factor = std::clamp(kWideSigma * zoom / kWideSigmaTexels, kWideMinFactor, kWideMaxFactor);
         const uint32_t iw = std::max(1u, (uint32_t)std::ceil((float)ew / kWideMinFactor));
