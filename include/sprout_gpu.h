@@ -331,6 +331,10 @@ int sprout_sim_download_render(SproutSim* sim, int which, uint16_t* out, size_t 
  *   scattering; the concentrate share, the aqueous weight, the other weight, 0;
  * - the wide field: the sharp field box-filtered down to texels of clamp(2 zoom / 3, 2, 64)
  *   pixels and blurred by a 13-tap Gaussian across, then down;
+ * - the look field (render.rs:1004-1036, look.vert, look.frag), in the sharp field's texels: the
+ *   particles the last sprout_sim_render listed (look.comp) as discs of radius 1 cell (at least
+ *   1.5 texels), each laying down its platelets' sheen, its carried scalar, which way the
+ *   platelets lie and its weight; clear without a liquid with a look;
  * - the wet map (RGBA32F, a texel per cell, kept between calls): where liquid (occupancy at least
  *   0.3) lies within 1.75 cells of a solid, its leading material row + 1, family 0's
  *   concentration and the simulated time; written once per simulated time, cleared on a new
@@ -340,8 +344,9 @@ int sprout_sim_download_render(SproutSim* sim, int which, uint16_t* out, size_t 
  * (the reference blends in the hardware's order into half floats). */
 int sprout_sim_draw(SproutSim* sim, float center_x, float center_y, float zoom, uint32_t width, uint32_t height);
 /* An image of the last sprout_sim_draw (blocking): which 0, the sharp field; 1, the tint field's
- * absorption image; 2, its share image; 3, the wide field (RGBA16F, 8 bytes a texel); 4, the wet
- * map (RGBA32F, 16 bytes a texel, W x H). dims = its texels across and down (0 x 0: not drawn);
+ * absorption image; 2, its share image; 3, the wide field; 5, the look field (RGBA16F, 8 bytes a
+ * texel); 4, the wet map (RGBA32F, 16 bytes a texel, W x H). dims = its texels across and down
+ * (0 x 0: not drawn);
  * out may be NULL to ask for them. */
 int sprout_sim_download_draw(SproutSim* sim, int which, void* out, size_t cap, uint32_t dims[2]);
 /* Stats (src/sim/mod.rs:130-136): live particles and, per material row, its particles and the

@@ -32,6 +32,7 @@ WIDE_SIGMA_TEXELS = f32(3.0)
 WIDE_MIN_FACTOR = f32(2.0)
 WIDE_MAX_FACTOR = f32(64.0)
 TINT_DIV = 2
+LOOK_RADIUS = f32(1.0)
 ROW_STEAM = 57         # common.glsl
 STREAK_MAX = f32(1.5)  # splat.vert
 REACH = f32(1.75)      # wet.frag
@@ -70,7 +71,12 @@ def layout(center, zoom, extent, tint_live=True):
     wh = min(max(int(np.ceil(f32(eh) / factor)), 1), image[1])
     wide = dict(w=ww, h=wh, taps=int(np.ceil(f32(f32(factor / div) * f32(0.5)))), factor=f32(factor / div),
                 wide_factor=factor, step=f32(f32(f32(f32(0.5) * WIDE_SIGMA) * zoom) / factor), image=image)
-    return dict(sharp=sharp, tint=tint if tint_live else None, wide=wide)
+    rl = max(LOOK_RADIUS, f32(SPLAT_MIN_TEXELS * div / zoom))
+    h0, h1, h2 = f32(-0.3375), f32(0.67), f32(f32(0.66) + f32(1.0))   # composite.frag's key light + the view
+    hn = np.sqrt(f32(f32(f32(h0 * h0) + f32(h1 * h1)) + f32(h2 * h2)))
+    look = dict(base, div=div, radius=rl, weight=f32(f32(LOOK_RADIUS / rl) * f32(LOOK_RADIUS / rl)), w=aw, h=ah, look=True,
+                tint=False, izoom=f32(f32(1.0) / zoom), iradius=f32(f32(1.0) / rl), H=(f32(h0 / hn), f32(h1 / hn), f32(h2 / hn)))
+    return dict(sharp=sharp, tint=tint if tint_live else None, wide=wide, look=look)
 
 
 def shares_a_group(rows, groups):
@@ -83,8 +89,19 @@ def shares_a_group(rows, groups):
     return any(n >= 2 for n in seen)
 
 
-def _payload(p, row, groups, optics, v):
-    """What particle p lays down per unit kernel: (first channel, values) (splat.vert)."""
+def _payload(p, row, groups, optics, v, st=None):
+    """What particle p lays down per unit kernel: (first channel, values) (splat.vert; look.vert
+    with its look.comp state st)."""
+    if v.get("look"):
+        z, w = int(st[2]), v["weight"]
+        ax, ay = f32(f32(z & 1023) / f32(1023.0)), f32(f32((z >> 10) & 1023) / f32(1023.0))
+        az = f32(f32(f32((z >> 20) & 1023) / f32(1023.0)) - f32(0.5))
+        hx, hy, hz = v["H"]
+        sheen = f32(f32(f32(f32(f32(hx * hx) * ax) + f32(f32(hy * hy) * ay)) + f32(f32(f32(f32(2.0) * hx) * hy) * az))
+                    + f32(f32(hz * hz) * f32(f32(f32(1.0) - ax) - ay)))
+        phi = f32(f32(int(st[3]) & 0xFFFF) / f32(65535.0))
+        lie = _clampf(f32(0.5) + f32(ax - ay), 0.0, 1.0)
+        return 0, [f32(sheen * w), f32(phi * w), f32(lie * w), f32(f32(1.0) * w)]
     if not v["tint"]:
         return min(max(int(groups[row]), 0), 3), [v["weight"]]
     o = optics[row]
@@ -101,20 +118,24 @@ def _payload(p, row, groups, optics, v):
     return 0, [f32(x) for x in c]
 
 
-def splat(parts, groups, optics, v):
-    """The fixed-point texel sums of one splat pass (splat.vert + splat.frag, or tint.frag with
-    v["tint"]): int64 (h, w, 4 or 8), 2^-32 units."""
+def splat(parts, groups, optics, v, look_state=None, look_list=None):
+    """The fixed-point texel sums of one splat pass (splat.vert + splat.frag, tint.frag with
+    v["tint"], or look.vert + look.frag over the listed slots with their look.comp state):
+    int64 (h, w, 4 or 8), 2^-32 units."""
     h, w = v["h"], v["w"]
     nch = 8 if v["tint"] else 4
     acc = np.zeros((h, w, nch), np.int64)
     cx, cy, zoom, div = v["cx"], v["cy"], v["zoom"], v["div"]
     half_w, half_h, radius = v["half_w"], v["half_h"], v["radius"]
-    for p in parts:
+    look = bool(v.get("look"))
+    slots = look_list if look else range(len(parts))
+    for slot in slots:
+        p = parts[int(slot)]
         low = int(p["kind"]) & 255
-        if low == 0 or (v["tint"] and low - 1 == ROW_STEAM):
+        if not look and (low == 0 or (v["tint"] and low - 1 == ROW_STEAM)):
             continue
         row = low - 1
-        vx, vy = f32(p["vel"][0]), f32(p["vel"][1])
+        vx, vy = (f32(0.0), f32(0.0)) if look else (f32(p["vel"][0]), f32(p["vel"][1]))
         speed = np.sqrt(f32(f32(vx * vx) + f32(vy * vy)))
         dx, dy = (f32(vx / speed), f32(vy / speed)) if speed > f32(1e-3) else (f32(1.0), f32(0.0))
         streak = min(f32(speed * v["exposure"]), f32(STREAK_MAX * radius))
@@ -145,7 +166,7 @@ def splat(parts, groups, optics, v):
         r2 = u * u + w2 * w2
         inside = r2 < f32(1.0)
         k = (f32(1.0) - r2) * (f32(1.0) - r2)
-        ch0, c = _payload(p, row, groups, optics, v)
+        ch0, c = _payload(p, row, groups, optics, v, look_state[int(slot)] if look else None)
         for q, cq in enumerate(c):
             val = (cq * k).astype(f32)
             fix = np.rint(val * f32(FIX)).astype(np.int64)
@@ -156,6 +177,11 @@ def splat(parts, groups, optics, v):
 def unfix(acc):
     """The fixed-point sums as half floats (through FP64 and FP32, as the engine rounds them)."""
     return (acc.astype(np.float64) * (1.0 / FIX)).astype(np.float32).astype(np.float16)
+
+
+def look_field(parts, look_state, look_list, lay):
+    """The look field (h, w, 4) float16 of the listed slots."""
+    return unfix(splat(parts, None, None, lay["look"], look_state, look_list))
 
 
 def fields(parts, groups, optics, lay):

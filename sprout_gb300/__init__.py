@@ -540,9 +540,9 @@ class FluidSim:
         _check(lib().sprout_sim_draw(self._h, float(center[0]), float(center[1]), float(zoom), int(size[0]), int(size[1])))
 
     def download_draw(self, which: str = "sharp") -> np.ndarray:
-        """An image of the last draw: "sharp", "tint", "share" or "wide" as (h, w, 4) float16,
-        "wet" as (H, W, 4) float32; None when it was never drawn."""
-        k = {"sharp": 0, "tint": 1, "share": 2, "wide": 3, "wet": 4}[which]
+        """An image of the last draw: "sharp", "tint", "share", "wide" or "look" as (h, w, 4)
+        float16, "wet" as (H, W, 4) float32; None when it was never drawn."""
+        k = {"sharp": 0, "tint": 1, "share": 2, "wide": 3, "wet": 4, "look": 5}[which]
         dims = (C.c_uint32 * 2)()
         _check(lib().sprout_sim_download_draw(self._h, k, None, 0, dims))
         w, h = int(dims[0]), int(dims[1])

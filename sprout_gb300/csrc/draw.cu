@@ -2,8 +2,10 @@
 // (render.rs:640-668, shaders/wet.frag) as kernels into headless device images, for one view
 // (centre, zoom in pixels per cell, extent in pixels):
 //   k_splat       splat.vert + splat.frag (the sharp field: each phase group's weight times
-//                 the kernel) and, with the tint flag, splat.vert + tint.frag (the tint field:
-//                 absorption and scattering, concentrate share, aqueous and other weight)
+//                 the kernel), splat.vert + tint.frag (the tint field: absorption and
+//                 scattering, concentrate share, aqueous and other weight), and look.vert +
+//                 look.frag (the look field of the particles look.comp listed: their
+//                 platelets' sheen, carried scalar, which way they lie, and weight)
 //   k_fields_out  the texel sums to RGBA16F, the sums cleared for the next draw
 //   k_down        down.frag: the box filter of bilinear taps into the wide field
 //   k_blur        blur.frag: one direction of the 13-tap Gaussian of the wide field
@@ -85,9 +87,11 @@ DEV Splat splat_of(const DevScene& d, const DevOptics* opt, uint32_t id, const D
     sp.i0 = 0, sp.i1 = -1, sp.j0 = 0, sp.j1 = -1, sp.ch0 = 0, sp.nch = 0;
     const float4 q0 = d.part[3 * id + 0], q2 = d.part[3 * id + 2];
     const uint32_t kind = __float_as_uint(q2.y), low = kind & 255u;
-    if (low == 0u || (v.tint && low - 1u == kRowSteam)) return sp;
+    // look.vert draws every listed slot as a disc about the particle (no streak)
+    const bool look = v.mode == 2;
+    if (!look && (low == 0u || (v.mode == 1 && low - 1u == kRowSteam))) return sp;
     const uint32_t row = low - 1u;
-    const float speed = sqrtf(q0.z * q0.z + q0.w * q0.w);
+    const float speed = look ? 0.0f : sqrtf(q0.z * q0.z + q0.w * q0.w);
     sp.dx = speed > 1e-3f ? q0.z / speed : 1.0f;
     sp.dy = speed > 1e-3f ? q0.w / speed : 0.0f;
     const float streak = minf_(speed * v.exposure, kStreakMax * v.radius);
@@ -101,7 +105,21 @@ DEV Splat splat_of(const DevScene& d, const DevOptics* opt, uint32_t id, const D
     if (!(tx1 >= -1.0f && ty1 >= -1.0f && tx0 <= (float)v.w + 1.0f && ty0 <= (float)v.h + 1.0f)) return sp;
     sp.i0 = (int)maxf_(floorf(tx0) - 1.0f, 0.0f), sp.i1 = (int)minf_(ceilf(tx1) + 1.0f, (float)(v.w - 1));
     sp.j0 = (int)maxf_(floorf(ty0) - 1.0f, 0.0f), sp.j1 = (int)minf_(ceilf(ty1) + 1.0f, (float)(v.h - 1));
-    if (!v.tint) {
+    if (look) {
+        // the platelets' sheen H.A.H over their packed second moment A, the carried scalar,
+        // which way they lie in the plane (A_xx - A_yy about 0.5), and the weight
+        const uint4 st = d.plook[id];
+        const float ax = (float)(st.z & 1023u) / 1023.0f, ay = (float)((st.z >> 10) & 1023u) / 1023.0f;
+        const float az = (float)((st.z >> 20) & 1023u) / 1023.0f - 0.5f;
+        const float sheen = v.hx * v.hx * ax + v.hy * v.hy * ay + 2.0f * v.hx * v.hy * az + v.hz * v.hz * (1.0f - ax - ay);
+        const float phi = (float)(st.w & 0xffffu) / 65535.0f;
+        const float lie = clampf_(0.5f + (ax - ay), 0.0f, 1.0f);
+        sp.nch = 4;
+        sp.c[0] = sheen * v.weight;
+        sp.c[1] = phi * v.weight;
+        sp.c[2] = lie * v.weight;
+        sp.c[3] = 1.0f * v.weight;
+    } else if (v.mode == 0) {
         sp.ch0 = clampi_(d.mats[row].ia[0], 0, 3);
         sp.nch = 1;
         sp.c[0] = v.weight;
@@ -174,12 +192,13 @@ DEV void splat_into(const Splat& sp, const DrawPass& v, Acc* acc, int oi, int oj
 // directly. Integer sums: the same either way.
 constexpr int kSplatSmemWords = 3072;   // 24 KB: five blocks of 256 threads still fit an SM
 __global__ void __launch_bounds__(256) k_splat(DevScene d, const DevOptics* opt, uint32_t n_slots, DrawPass v,
-                                               long long* acc) {
+                                               const uint32_t* list, long long* acc) {
     __shared__ uint32_t sacc[2 * kSplatSmemWords];
     __shared__ int box[6];
     const uint32_t id = blockIdx.x * blockDim.x + threadIdx.x;
     Splat sp;
-    if (id < n_slots) sp = splat_of(d, opt, id, v);
+    const uint32_t n = list ? list[0] : n_slots;
+    if (id < n) sp = splat_of(d, opt, list ? list[1 + id] : id, v);
     else sp.i0 = 0, sp.i1 = -1, sp.j0 = 0, sp.j1 = -1, sp.ch0 = 0, sp.nch = 0;
     if (threadIdx.x == 0) box[0] = box[1] = box[4] = INT_MAX, box[2] = box[3] = box[5] = INT_MIN;
     __syncthreads();
@@ -194,8 +213,8 @@ __global__ void __launch_bounds__(256) k_splat(DevScene d, const DevOptics* opt,
     }
     __syncthreads();
     if (box[2] < box[0]) return;   // nothing of the block's in view
-    const int stride = v.tint ? 8 : 4;
-    const bool one = !v.tint && box[4] == box[5];
+    const int stride = v.mode == 1 ? 8 : 4;
+    const bool one = v.mode == 0 && box[4] == box[5];
     const int sstride = one ? 1 : stride;
     const int bw = box[2] - box[0] + 1, bh = box[3] - box[1] + 1;
     const long long words = (long long)bw * bh * sstride;
@@ -307,13 +326,17 @@ __global__ void __launch_bounds__(256) k_wet(DevScene d, const WetClock* c, floa
 }  // namespace
 
 void launch_draw(const DevScene& d, const DevOptics* opt, uint32_t n_slots, const DrawPass& sharp, const DrawPass* tint,
-                const DrawWide& wide, DrawBufs& b, cudaStream_t st) {
+                 const DrawPass* look, const uint32_t* look_list, const DrawWide& wide, DrawBufs& b, cudaStream_t st) {
     const uint32_t nb = (n_slots + 255u) / 256u;
-    if (n_slots > 0) k_splat<<<nb, 256, 0, st>>>(d, opt, n_slots, sharp, b.acc);
+    if (n_slots > 0) k_splat<<<nb, 256, 0, st>>>(d, opt, n_slots, sharp, nullptr, b.acc);
     const int na = sharp.w * sharp.h;
     k_fields_out<<<(na + 255) / 256, 256, 0, st>>>(b.acc, na, 0, b.sharp, nullptr);
+    if (look) {   // into the same sums, which k_fields_out left cleared
+        if (n_slots > 0) k_splat<<<nb, 256, 0, st>>>(d, opt, n_slots, *look, look_list, b.acc);
+        k_fields_out<<<(na + 255) / 256, 256, 0, st>>>(b.acc, na, 0, b.look, nullptr);
+    }
     if (tint) {
-        if (n_slots > 0) k_splat<<<nb, 256, 0, st>>>(d, opt, n_slots, *tint, b.tacc);
+        if (n_slots > 0) k_splat<<<nb, 256, 0, st>>>(d, opt, n_slots, *tint, nullptr, b.tacc);
         const int nt = tint->w * tint->h;
         k_fields_out<<<(nt + 255) / 256, 256, 0, st>>>(b.tacc, nt, 1, b.conc, b.share);
     }

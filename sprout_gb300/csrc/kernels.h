@@ -197,8 +197,9 @@ void launch_spray(const DevScene& d, const ushort4* smooth, const DevOptics* opt
 struct DrawPass {
     float cx, cy, zoom, div, half_w, half_h;
     float radius, weight, exposure;
-    int w, h, tint;
+    int w, h, mode;         // 0 the sharp field, 1 the tint field, 2 the look field
     float izoom, iradius;   // 1 / zoom, 1 / radius
+    float hx, hy, hz;       // the look field: the half vector between the key light and the viewer
 };
 // The wide field's layout (WideLayout): used texels, bilinear taps per axis, sharp-field
 // texels per wide texel, the blur's step (half a standard deviation) in texels.
@@ -210,10 +211,12 @@ struct DrawBufs {
     long long *acc, *tacc;              // fixed-point texel sums (2^-32): 4 and 8 a texel
     ushort4 *sharp, *conc, *share;      // RGBA16F: the sharp field, the tint field's two images
     ushort4 *wide0, *wide1;             // the wide field (finished in wide0) and the blur's other image
+    ushort4* look;                      // the look field (the sharp field's texels)
 };
-// splat (+ tint when given), then the wide field: down, blur across, blur down.
+// splat (+ tint, + look over look_list = [count, slots ...] when given), then the wide field:
+// down, blur across, blur down.
 void launch_draw(const DevScene& d, const DevOptics* opt, uint32_t n_slots, const DrawPass& sharp, const DrawPass* tint,
-                 const DrawWide& wide, DrawBufs& b, cudaStream_t st);
+                 const DrawPass* look, const uint32_t* look_list, const DrawWide& wide, DrawBufs& b, cudaStream_t st);
 // The wet map (wet.frag) once per simulated time: the clock reads the time after the last
 // substep on the device and lets the pass run when it moved.
 struct WetClock {

@@ -1100,9 +1100,12 @@ struct SproutSim {
     static constexpr float kSplatRadius = 1.5f, kAccumKernelTexels = 2.8f, kAccumMaxDiv = 2.0f, kSplatMinTexels = 1.5f;
     static constexpr float kWideSigma = 2.0f, kWideSigmaTexels = 3.0f, kWideMinFactor = 2.0f, kWideMaxFactor = 64.0f;
     static constexpr uint32_t kTintDiv = 2u, kDrawMaxExtent = 16384u;
+    static constexpr float kLookRadius = 1.0f;   // LOOK_RADIUS
     DrawBufs drawb{};
-    size_t cap_acc = 0, cap_tacc = 0, cap_sharp = 0, cap_conc = 0, cap_share = 0, cap_w0 = 0, cap_w1 = 0;
-    uint32_t draw_dims[4][2] = {};   // used texels of the sharp field, the tint field (0 x 0: never drawn), the wide field
+    size_t cap_acc = 0, cap_tacc = 0, cap_sharp = 0, cap_conc = 0, cap_share = 0, cap_w0 = 0, cap_w1 = 0, cap_look = 0;
+    // used texels of the sharp field, the tint field's two images (0 x 0: never drawn), the
+    // wide field, the look field
+    uint32_t draw_dims[5][2] = {};
     float4* d_wet = nullptr;
     WetClock* d_wet_clock = nullptr;
     size_t wet_cells = 0;
@@ -1173,7 +1176,19 @@ struct SproutSim {
         }
         if ((rc = grow(&drawb.wide0, &cap_w0, nw)) != SPROUT_OK) return rc;
         if ((rc = grow(&drawb.wide1, &cap_w1, nw)) != SPROUT_OK) return rc;
-        launch_draw(d, d_optics, n_slots, sharp, tint_live ? &tint : nullptr, wide, drawb, stream);
+        // pass 1c: the look field (render.rs:1004-1036) of the particles the last render listed
+        // (look.comp), in the sharp field's texels; without a liquid with a look it is clear
+        const bool look_on = look_live() && d.plook && d_look_list && n_slots > 0;
+        const float rl = std::max(kLookRadius, kSplatMinTexels * div / zoom);
+        const float h0 = -0.3375f, h1 = 0.67f, h2 = 0.66f + 1.0f;   // composite.frag's key light + the view
+        const float hn = std::sqrt(h0 * h0 + h1 * h1 + h2 * h2);
+        DrawPass look{cx, cy, zoom, div, half_w, half_h, rl, (kLookRadius / rl) * (kLookRadius / rl), exposure, (int)aw, (int)ah, 2,
+                      1.0f / zoom, 1.0f / rl, h0 / hn, h1 / hn, h2 / hn};
+        if ((rc = grow(&drawb.look, &cap_look, na)) != SPROUT_OK) return rc;
+        if (!look_on) CUDA_TRY(cudaMemsetAsync(drawb.look, 0, na * sizeof(ushort4), stream));
+        launch_draw(d, d_optics, n_slots, sharp, tint_live ? &tint : nullptr, look_on ? &look : nullptr, d_look_list, wide,
+                    drawb, stream);
+        draw_dims[4][0] = aw, draw_dims[4][1] = ah;
         draw_dims[0][0] = aw, draw_dims[0][1] = ah;
         if (tint_live) draw_dims[1][0] = draw_dims[2][0] = tw, draw_dims[1][1] = draw_dims[2][1] = th;
         draw_dims[3][0] = ww, draw_dims[3][1] = wh;
@@ -1195,16 +1210,19 @@ struct SproutSim {
         return SPROUT_OK;
     }
     int download_draw(int which, void* out, size_t cap, uint32_t dims[2]) {
-        if (which < 0 || which > 4)
-            return fail(SPROUT_E_ARG, "download_draw: which is 0 (sharp), 1 (tint), 2 (tint share), 3 (wide) or 4 (wet map)");
-        const uint32_t w = which == 4 ? (d_wet ? (uint32_t)W : 0u) : draw_dims[which][0];
-        const uint32_t h = which == 4 ? (d_wet ? (uint32_t)H : 0u) : draw_dims[which][1];
+        if (which < 0 || which > 5)
+            return fail(SPROUT_E_ARG,
+                        "download_draw: which is 0 (sharp), 1 (tint), 2 (tint share), 3 (wide), 4 (wet map) or 5 (look)");
+        const int k = which == 5 ? 4 : which;
+        const uint32_t w = which == 4 ? (d_wet ? (uint32_t)W : 0u) : draw_dims[k][0];
+        const uint32_t h = which == 4 ? (d_wet ? (uint32_t)H : 0u) : draw_dims[k][1];
         dims[0] = w, dims[1] = h;
         const size_t n = (size_t)w * h * (which == 4 ? sizeof(float4) : sizeof(ushort4));
         if (!out || n == 0) return SPROUT_OK;
         if (cap < n) return fail(SPROUT_E_ARG, "download_draw: the output holds fewer bytes than the image");
         const void* src = which == 0 ? (const void*)drawb.sharp : which == 1 ? (const void*)drawb.conc
-                          : which == 2 ? (const void*)drawb.share : which == 3 ? (const void*)drawb.wide0 : (const void*)d_wet;
+                          : which == 2 ? (const void*)drawb.share : which == 3 ? (const void*)drawb.wide0
+                          : which == 4 ? (const void*)d_wet : (const void*)drawb.look;
         CUDA_TRY(cudaStreamSynchronize(stream));
         CUDA_TRY(cudaMemcpy(out, src, n, cudaMemcpyDeviceToHost));
         d2h_bytes += n;

@@ -3,7 +3,8 @@ passes of Renderer::render, render.rs:886-1075, and wet.frag's wet map) against 
 restatement (oracle/draw.py) on the engine's own particles and grid, bit for bit in every
 texel. Views near and far (the kernel widened below 1.5 texels, the sharp field at full and at
 half resolution), tanks with and without two liquids of one phase group (the tint field drawn
-or left alone), moving liquid (streaks), and the wet map kept over frames."""
+or left alone), moving liquid (streaks), the look field of a liquid carrying platelets, and the
+wet map kept over frames."""
 import numpy as np
 import pytest
 
@@ -104,3 +105,28 @@ def test_draw_rejects_bad_views():
                                ((10, 10), 2.0, (0, 64)), ((10, 10), 2.0, (64, 20000))):
         with pytest.raises(S.SproutError):
             sim.draw(center, zoom, size)
+
+
+def test_look_field_bit_exact():
+    """look.vert + look.frag over the particles look.comp listed (a dam break of water carrying
+    mica platelets): every texel of the look field equals the oracle's from the same state and
+    list; a tank without a liquid with a look leaves it clear."""
+    mica = {"mat0.cloud": 0.05, "mat0.cloud_shape": 0.05, "mat0.cloud_size": 1.5e-5}
+    tank = tanks.dam_break(96, 64, extra=mica)
+    sim, _, _ = tank.engine()
+    sim.step(6, 6 / 240.0)
+    sim.render(1.0 / 80.0)
+    for center, zoom, size in (((48.0, 30.0), 4.0, (384, 256)), ((40.5, 20.25), 0.8, (160, 100))):
+        sim.draw(center, zoom, size)
+        st, lst = sim.download_look()
+        lay = D.layout(center, zoom, size)
+        want = D.look_field(sim.download_particles(), st, lst, lay)
+        same(sim.download_draw("look"), want, f"look field at zoom {zoom}")
+        w = want.astype(np.float32)
+        assert w[..., 3].max() > 0.5 and w[..., 0].max() > 0.0
+    plain = tanks.dam_break(96, 64)
+    sim2, _, _ = plain.engine()
+    sim2.step(2, 2 / 240.0)
+    sim2.render(1.0 / 80.0)
+    sim2.draw((48.0, 30.0), 4.0, (384, 256))
+    assert not sim2.download_draw("look").astype(np.float32).any()
