@@ -563,6 +563,9 @@ def main():
     ap.add_argument("--batch-only", action="store_true",
                     help="run only the batched configuration's leg and print it (a profiler's capture of the "
                          "batched solves)")
+    ap.add_argument("--draw-only", action="store_true",
+                    help="step the workload five substeps, time only the renderer's particle fields for a "
+                         "1920 x 1080 view of it and print them (a profiler's capture of the draw)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, world, local, pg = dist_setup(args.gpus)
@@ -574,6 +577,12 @@ def main():
             build.build()
             if args.batch_only:
                 print(json.dumps({"batched": run_batched(args, pg, rank, world)}), flush=True)
+            elif args.draw_only:
+                tank, _ = workload(args.workload, rank)
+                sim, _, _ = tank.engine()
+                sim.step(5, 5 / 240.0)
+                sim.sync()
+                print(json.dumps({"draw": draw_timing(sim, tank)}), flush=True)
             else:
                 run_engine(args, rank, world, local, pg)
     finally:
