@@ -477,7 +477,7 @@ def run_engine(args, rank, world, local, pg):
             roof["traffic_source"] = (f"profiles/traffic.json: dram__bytes_read.sum + dram__bytes_write.sum of one "
                                       f"launch of this stage's kernel on this workload ({tr.get('command', 'ncu')}), "
                                       "not measured in this run")
-    # ---- the mixed-precision solve on the same tank (BF16 matrices, FP64 dot products) ------
+    # ---- the mixed-precision solve on the same tank (BF16 matrices, FP64 scalars) -----------
     mixed = None
     if args.precision in ("both", "mixed"):
         msim, _, _ = tank.engine()
@@ -496,7 +496,8 @@ def run_engine(args, rank, world, local, pg):
                                         "carried |r| falls 100x; adopted where it exceeds twice the carried one and "
                                         "ten times the FP32 rounding floor eps |A| |x|"},
                  "storage": "BF16 couplings + FP32 row-sum-keeping diagonal on every level; FP32 vectors",
-                 "dots": "FP64", "speedup_vs_plain": (ms / args.steps) / (mms / args.steps)}
+                 "dots": "FP32 sums (the plain solve's trees), FP64 totals, step lengths and convergence test",
+                 "speedup_vs_plain": (ms / args.steps) / (mms / args.steps)}
     # ---- end to end through the public API, on a fresh copy over the same substeps ----------
     e2e = end_to_end(tank, args, pg)
     draw = draw_timing(sim, tank)

@@ -422,7 +422,8 @@ int sprout_sim_trace_read(SproutSim* sim, unsigned long long* out, size_t cap, s
  * arithmetic, FP32 throughout (the default). mode 1: mixed precision: the multigrid
  * hierarchy's matrices stored in BF16 (with an FP32 diagonal that keeps every row sum) and
  * computed in FP32; every vector, the CG iterate, residual and operator in FP32; the dot
- * products, step lengths and convergence test in FP64; as refinement, each time the carried
+ * products summed in FP32 as mode 0 sums them, their totals, the step lengths and the
+ * convergence test in FP64; as refinement, each time the carried
  * residual has fallen 100x the true residual b - A x is evaluated as float pairs and replaces the
  * carried one where it exceeds it twice over and lies well above the FP32 rounding floor
  * (stats: pressure_replacements); at the end of each solve the true residual is evaluated as

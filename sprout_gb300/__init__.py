@@ -622,7 +622,8 @@ class FluidSim:
 
     def set_precision(self, mode: str | int):
         """The pressure solve's precision: "plain" (0, FP32 as the reference) or "mixed" (1:
-        BF16 matrices, FP64 dot products and convergence test, FP64 true residual at the end)."""
+        BF16 matrices, FP32 dot products with FP64 totals, step lengths and convergence test, the
+        true residual at the end as float pairs)."""
         m = {"plain": 0, "mixed": 1}.get(mode, mode)
         _check(lib().sprout_sim_set_precision(self._h, int(m)))
 

@@ -22,16 +22,15 @@
 //          the reference's order (bit-exact with the oracle).
 //   Mixed  the V-cycle's matrices (every level's couplings) stored in BF16 and computed in
 //          FP32; the CG operator (level 0's matrix), every vector, iterate, residual and
-//          direction stay FP32; the dot products, step
-//          lengths and convergence test in FP64; and at the end of each solve the true
-//          residual b - A x of the pressure evaluated in FP64 arithmetic and reported (it is
-//          not fed back: for these near-singular systems the FP32-evaluated true residual is
-//          rounding noise at 1e-3 |b| and the best FP32 iterate's FP64 one sits near
-//          5e-5 |b|, so replacing the carried residual with either stalls the iteration
-//          above the reference's 1e-5 tolerance). The BF16 couplings come with an FP32
-//          diagonal that keeps each row's exact excess over them (see Mixed::setA).
+//          direction stay FP32; the dot products summed in FP32 as the plain solve sums
+//          them, their totals widened to FP64 for the step lengths and the convergence
+//          test; the refinement's checks and the closing true residual b - A x evaluated
+//          as float pairs (products exact, sums compensated). The BF16 couplings come with
+//          an FP32 diagonal that keeps each row's exact excess over them (see Mixed::setA).
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
+
+#include <type_traits>
 
 #include "dev_common.cuh"
 #include "kernels.h"
@@ -91,7 +90,9 @@ DEV float2 unpack(uint32_t u) { return __bfloat1622float2(*reinterpret_cast<cons
 struct Mixed {
     static constexpr bool kMixed = true;
     using acc = double;
-    using acc4 = FF4;   // the partial sums as float pairs, their totals to FP64 (fin)
+    // the dot products' partial sums and totals in FP32 as the plain solve takes them (the
+    // reference's trees), widened to FP64 for the step lengths and the convergence test
+    using acc4 = float4;
     // the hierarchy in BF16: a row's four couplings as two bfloat162 in a uint2
     DEV static float4 A(const DevScene& d, int i) {
         const uint2 u = d.hga[i];
@@ -128,12 +129,12 @@ struct Mixed {
     DEV static void setZ(const DevScene& d, int i, float2 v) { d.mgz[i] = v; }
     DEV static float2 R(const DevScene& d, int i) { return d.mgr[i]; }
     DEV static void setR(const DevScene& d, int i, float2 v) { d.mgr[i] = v; }
-    DEV static acc4* part(const DevScene& d) { return reinterpret_cast<FF4*>(d.partials64); }
-    DEV static acc4 zero4() { return FF4{make_float4(0.0f, 0.0f, 0.0f, 0.0f), make_float4(0.0f, 0.0f, 0.0f, 0.0f)}; }
+    DEV static acc4* part(const DevScene& d) { return d.partials; }
+    DEV static acc4 zero4() { return make_float4(0.0f, 0.0f, 0.0f, 0.0f); }
     DEV static acc4 prod4(float a0, float b0, float a1, float b1, float a2, float b2, float a3, float b3) {
-        return ff_prod4(a0, b0, a1, b1, a2, b2, a3, b3);
+        return make_float4(a0 * b0, a1 * b1, a2 * b2, a3 * b3);
     }
-    DEV static Dbl4 fin(acc4 a) { return to_dbl(a); }
+    DEV static Dbl4 fin(acc4 a) { return Dbl4{(double)a.x, (double)a.y, (double)a.z, (double)a.w}; }
     static constexpr int kABytes = 8;
     DEV static const void* Araw(const DevScene& d, int i) { return d.hga + i; }
     // the level passes stage the inverse diagonal in the diagonal's slot (positive exactly
@@ -1339,7 +1340,10 @@ __global__ void __launch_bounds__(NT, 2) k_mgpcg(DevScene d, int second, int sca
     using acc4 = typename M::acc4;
     __shared__ TileCache tc;
     __shared__ float2 sz[NT];
-    __shared__ acc4 buf[NT];
+    // the block's tree buffer: float pairs in mixed precision (the refinement's checks), whose
+    // bytes the dot products' trees use as acc4 in other phases
+    __shared__ typename std::conditional<M::kMixed, FF4, acc4>::type buf_raw[NT];
+    acc4* buf = reinterpret_cast<acc4*>(buf_raw);
     __shared__ Solve<acc> K;
     // dynamic: the staging regions, then the tail levels (matrices, iterates, masks: kept for
     // the whole solve); the tail's right-hand sides, live only in the tail phase, when no
@@ -1390,9 +1394,9 @@ __global__ void __launch_bounds__(NT, 2) k_mgpcg(DevScene d, int second, int sca
             // the apply phase rewrites it, and the partials' second half until it sums p.q
             if (it > 0 && want_check(K)) {
                 FF4* pc = reinterpret_cast<FF4*>(d.partials64) + n;
-                for_active(d, 0, tc, [&](int t) { check_tile(d, t, d.cgq, pc, reinterpret_cast<FF4*>(buf)); });
+                for_active(d, 0, tc, [&](int t) { check_tile(d, t, d.cgq, pc, reinterpret_cast<FF4*>(buf_raw)); });
                 if (!grid_sync(d.K)) return;
-                const Dbl4 tot = to_dbl(total(pc, n, reinterpret_cast<FF4*>(buf)));
+                const Dbl4 tot = to_dbl(total(pc, n, reinterpret_cast<FF4*>(buf_raw)));
                 __shared__ int s_adopt;
                 if (threadIdx.x == 0) s_adopt = decide_check(K, tot) ? 1 : 0;
                 __syncthreads();
@@ -1429,9 +1433,9 @@ __global__ void __launch_bounds__(NT, 2) k_mgpcg(DevScene d, int second, int sca
     double true_rel = -1.0;
     if constexpr (M::kMixed) {
         FF4* pt = reinterpret_cast<FF4*>(d.partials64);
-        for_active(d, 0, tc, [&](int t) { true_residual_tile(d, t, pt, reinterpret_cast<FF4*>(buf)); });
+        for_active(d, 0, tc, [&](int t) { true_residual_tile(d, t, pt, reinterpret_cast<FF4*>(buf_raw)); });
         if (!grid_sync(d.K)) return;
-        const Dbl4 t4 = to_dbl(total(pt, n, reinterpret_cast<FF4*>(buf)));
+        const Dbl4 t4 = to_dbl(total(pt, n, reinterpret_cast<FF4*>(buf_raw)));
         true_rel = t4.y > 0.0 ? sqrt(t4.x / t4.y) : 0.0;
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) scal_stats<M, acc>(d.K, K, second, true_rel);
@@ -1550,7 +1554,10 @@ __global__ void __launch_bounds__(NT, 4) k_mgpcg_batch(BatchView B, int second) 
     using acc4 = typename M::acc4;
     __shared__ TileCache tc;
     __shared__ float2 sz[NT];
-    __shared__ acc4 buf[NT];
+    // the block's tree buffer: float pairs in mixed precision (the refinement's checks), whose
+    // bytes the dot products' trees use as acc4 in other phases
+    __shared__ typename std::conditional<M::kMixed, FF4, acc4>::type buf_raw[NT];
+    acc4* buf = reinterpret_cast<acc4*>(buf_raw);
     __shared__ int s_run;
     extern __shared__ __align__(16) unsigned char dyn_smem[];
     Region* rg = reinterpret_cast<Region*>(dyn_smem);
@@ -1693,14 +1700,14 @@ __global__ void __launch_bounds__(NT, 4) k_mgpcg_batch(BatchView B, int second) 
             __syncthreads();
             if (s_run) {
                 for_active_b(B, 0, tc, [&](int s, const DevScene& d, int t) {
-                    if (chk(s)) check_tile(d, t, d.cgq, reinterpret_cast<FF4*>(d.partials64) + d.nwg, reinterpret_cast<FF4*>(buf));
+                    if (chk(s)) check_tile(d, t, d.cgq, reinterpret_cast<FF4*>(d.partials64) + d.nwg, reinterpret_cast<FF4*>(buf_raw));
                 });
                 if (!grid_sync(BK)) return;
                 // each scene's decision by one block (it alone writes KS[s] until the next barrier)
                 for (int s = blockIdx.x; s < B.ns; s += gridDim.x) {
                     if (!chk(s)) continue;
                     const DevScene& d = B.scenes[s];
-                    const Dbl4 tot = to_dbl(total(reinterpret_cast<FF4*>(d.partials64) + d.nwg, d.nwg, reinterpret_cast<FF4*>(buf)));
+                    const Dbl4 tot = to_dbl(total(reinterpret_cast<FF4*>(d.partials64) + d.nwg, d.nwg, reinterpret_cast<FF4*>(buf_raw)));
                     if (threadIdx.x == 0) KS[s].adopt = decide_check(KS[s], tot) ? 1u : 0u;
                     __syncthreads();
                 }
@@ -1745,7 +1752,7 @@ __global__ void __launch_bounds__(NT, 4) k_mgpcg_batch(BatchView B, int second) 
     }
     if constexpr (M::kMixed) {
         for_active_b(B, 0, tc, [&](int s, const DevScene& d, int t) {
-            true_residual_tile(d, t, reinterpret_cast<FF4*>(d.partials64), reinterpret_cast<FF4*>(buf));
+            true_residual_tile(d, t, reinterpret_cast<FF4*>(d.partials64), reinterpret_cast<FF4*>(buf_raw));
         });
         if (!grid_sync(BK)) return;
     }
@@ -1753,7 +1760,7 @@ __global__ void __launch_bounds__(NT, 4) k_mgpcg_batch(BatchView B, int second) 
         const DevScene& d = B.scenes[s];
         double true_rel = -1.0;
         if constexpr (M::kMixed) {
-            const Dbl4 t4 = to_dbl(total(reinterpret_cast<FF4*>(d.partials64), d.nwg, reinterpret_cast<FF4*>(buf)));
+            const Dbl4 t4 = to_dbl(total(reinterpret_cast<FF4*>(d.partials64), d.nwg, reinterpret_cast<FF4*>(buf_raw)));
             true_rel = t4.y > 0.0 ? sqrt(t4.x / t4.y) : 0.0;
         }
         if (threadIdx.x == 0) scal_stats<M, acc>(d.K, KS[s], second, true_rel);
