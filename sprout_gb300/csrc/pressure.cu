@@ -1712,12 +1712,22 @@ __global__ void __launch_bounds__(NT, 4) k_mgpcg_batch(BatchView B, int second) 
                     __syncthreads();
                 }
                 if (!grid_sync(BK)) return;
-                for_active_b(B, 0, tc, [&](int s, const DevScene& d, int t) {
-                    if (KS[s].adopt) adopt_tile(d, t, d.cgq, parity_r(d, it));
-                });
-                if (!grid_sync(BK)) return;
-                for (int s = blockIdx.x; s < B.ns; s += gridDim.x)
-                    if (threadIdx.x == 0) KS[s].adopt = 0u;
+                // every block reads the same decisions: without an adoption, the adopt pass
+                // and its barrier are skipped by all of them
+                if (threadIdx.x == 0) {
+                    int adopt = 0;
+                    for (int s = 0; s < B.ns && !adopt; s++) adopt = KS[s].adopt ? 1 : 0;
+                    s_run = adopt;
+                }
+                __syncthreads();
+                if (s_run) {
+                    for_active_b(B, 0, tc, [&](int s, const DevScene& d, int t) {
+                        if (KS[s].adopt) adopt_tile(d, t, d.cgq, parity_r(d, it));
+                    });
+                    if (!grid_sync(BK)) return;
+                    for (int s = blockIdx.x; s < B.ns; s += gridDim.x)
+                        if (threadIdx.x == 0) KS[s].adopt = 0u;
+                }
             }
         }
         pipe_active_b(
